@@ -1,0 +1,291 @@
+"""Seeded synthetic scenes for the Box2D step (the workloads the parity tests and the benchmark run).
+
+A scene is a flat description of the calls a user makes on a ``b2World``: bodies in creation order,
+each followed by its fixtures, then joints. It is stored as numpy arrays so that any implementation
+(the GPU world, the reference, the CPU oracle) can be built from it with one bulk call:
+
+* ``body_type`` int32[N], ``body_f`` float32[N, 9] = (x, y, angle, vx, vy, w, linearDamping,
+  angularDamping, gravityScale), ``body_flags`` int32[N] (1 allowSleep, 2 awake, 4 fixedRotation,
+  8 bullet, 16 active).
+* ``fix_body`` int32[M] (non-decreasing: fixtures follow their body), ``fix_type`` int32[M]
+  (0 circle {px, py, r}; 1 edge {v1, v2, v0, v3, hasV0, hasV3}; 2 polygon from points (hull by
+  ``b2PolygonShape::Set``); 3 box {hx, hy} or {hx, hy, cx, cy, angle}), ``fix_shape`` float32[M, 16],
+  ``fix_n`` int32[M], ``fix_mat`` float32[M, 3] = (density, friction, restitution), ``fix_filt``
+  int32[M, 4] = (categoryBits, maskBits, groupIndex, isSensor).
+* ``joint_a``/``joint_b`` int32[J], ``joint_f`` float32[J, 9] = (localAnchorA, localAnchorB,
+  referenceAngle, lowerAngle, upperAngle, motorSpeed, maxMotorTorque), ``joint_flags`` int32[J]
+  (1 limit, 2 motor, 4 collideConnected) - revolute joints.
+
+Random numbers come from splitmix64 on Python integers, so a seed gives the same scene on every
+machine. No public benchmark scene set exists for Box2D; these follow the workload descriptions:
+a 20-row box pyramid on an edge ground, a drop of mixed circles/polygons into an edge container,
+vertical box stacks, and chains of revolute-jointed links.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# b2BodyType
+STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
+# shape encodings of the bulk build call
+CIRCLE, EDGE, POLYGON, BOX = 0, 1, 2, 3
+DEFAULT_FLAGS = 1 | 2 | 16  # allowSleep, awake, active
+
+
+class SplitMix64:
+    """splitmix64 generator (Steele, Lea, Flood 2014) on Python ints: portable and seedable."""
+
+    def __init__(self, seed: int):
+        self.state = seed & 0xFFFFFFFFFFFFFFFF
+
+    def next_u64(self) -> int:
+        self.state = (self.state + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+        z = self.state
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+        return z ^ (z >> 31)
+
+    def uniform(self, lo: float = 0.0, hi: float = 1.0) -> float:
+        return lo + (hi - lo) * ((self.next_u64() >> 11) * (1.0 / 9007199254740992.0))
+
+    def randint(self, lo: int, hi: int) -> int:
+        """Integer uniform in [lo, hi] inclusive."""
+        return lo + (self.next_u64() % (hi - lo + 1))
+
+
+def _q(x: float) -> float:
+    """Quantise a generated coordinate to a 2^-20 grid so that libm differences in the double
+    cos/sin used to lay out polygon vertices cannot change the float32 scene between machines."""
+    return round(x * 1048576.0) / 1048576.0
+
+
+@dataclass
+class Scene:
+    gravity: tuple = (0.0, -10.0)
+    allow_sleep: bool = True
+    warm_starting: bool = True
+    continuous: bool = True
+    sub_stepping: bool = False
+    name: str = ""
+    bodies: list = field(default_factory=list)   # (type, f9, flags)
+    fixtures: list = field(default_factory=list)  # (body, type, shape list, n, mat3, filt4)
+    joints: list = field(default_factory=list)    # (a, b, f9, flags)
+
+    # ------------------------------------------------------------------ building
+    def body(self, type_, x, y, angle=0.0, vx=0.0, vy=0.0, w=0.0, lin_damp=0.0, ang_damp=0.0,
+             gravity_scale=1.0, flags=DEFAULT_FLAGS) -> int:
+        self.bodies.append((type_, [x, y, angle, vx, vy, w, lin_damp, ang_damp, gravity_scale], flags))
+        return len(self.bodies) - 1
+
+    def fixture(self, body, type_, shape, n=0, density=0.0, friction=0.2, restitution=0.0,
+                category=1, mask=0xFFFF, group=0, sensor=False) -> int:
+        assert body == len(self.bodies) - 1, "fixtures must follow their body"
+        self.fixtures.append((body, type_, list(shape), n, [density, friction, restitution],
+                              [category, mask, group, int(sensor)]))
+        return len(self.fixtures) - 1
+
+    def revolute(self, a, b, anchor_a, anchor_b, ref_angle=0.0, lower=0.0, upper=0.0, motor_speed=0.0,
+                 max_motor_torque=0.0, flags=0) -> int:
+        self.joints.append((a, b, [anchor_a[0], anchor_a[1], anchor_b[0], anchor_b[1], ref_angle, lower,
+                                   upper, motor_speed, max_motor_torque], flags))
+        return len(self.joints) - 1
+
+    # ------------------------------------------------------------------ arrays
+    def arrays(self) -> dict:
+        nb, nf, nj = len(self.bodies), len(self.fixtures), len(self.joints)
+        a = {
+            "body_type": np.array([b[0] for b in self.bodies], dtype=np.int32).reshape(nb),
+            "body_f": np.array([b[1] for b in self.bodies], dtype=np.float32).reshape(nb, 9),
+            "body_flags": np.array([b[2] for b in self.bodies], dtype=np.int32).reshape(nb),
+            "fix_body": np.array([f[0] for f in self.fixtures], dtype=np.int32).reshape(nf),
+            "fix_type": np.array([f[1] for f in self.fixtures], dtype=np.int32).reshape(nf),
+            "fix_shape": np.zeros((nf, 16), dtype=np.float32),
+            "fix_n": np.array([f[3] for f in self.fixtures], dtype=np.int32).reshape(nf),
+            "fix_mat": np.array([f[4] for f in self.fixtures], dtype=np.float32).reshape(nf, 3),
+            "fix_filt": np.array([f[5] for f in self.fixtures], dtype=np.int32).reshape(nf, 4),
+            "joint_a": np.array([j[0] for j in self.joints], dtype=np.int32).reshape(nj),
+            "joint_b": np.array([j[1] for j in self.joints], dtype=np.int32).reshape(nj),
+            "joint_f": np.array([j[2] for j in self.joints], dtype=np.float32).reshape(nj, 9),
+            "joint_flags": np.array([j[3] for j in self.joints], dtype=np.int32).reshape(nj),
+        }
+        for i, f in enumerate(self.fixtures):
+            a["fix_shape"][i, :len(f[2])] = np.array(f[2], dtype=np.float32)
+        return a
+
+    @property
+    def dynamic_count(self) -> int:
+        return sum(1 for b in self.bodies if b[0] == DYNAMIC)
+
+
+def _settings(s: Scene, allow_sleep: bool) -> Scene:
+    s.allow_sleep = allow_sleep
+    return s
+
+
+# ---------------------------------------------------------------------- scene kinds
+def pyramid(rows: int = 20, allow_sleep: bool = True, half: float = 0.5, spacing: float = 1.125,
+            density: float = 5.0, friction: float = 0.6, ground_half: float = 40.0) -> Scene:
+    """A box pyramid on a static edge ground: row r (0 = bottom) has rows - r boxes of half-extent
+    ``half`` spaced ``spacing`` apart, offset by half a spacing per row and 2*half higher, the bottom
+    row resting on y = 0. rows = 20 gives 210 boxes."""
+    s = Scene(name=f"pyramid{rows}")
+    g = s.body(STATIC, 0.0, 0.0)
+    s.fixture(g, EDGE, [-ground_half, 0.0, ground_half, 0.0, 0, 0, 0, 0, 0, 0], friction=friction)
+    x0 = -(rows - 1) * spacing / 2.0
+    for r in range(rows):
+        for j in range(rows - r):
+            x = x0 + r * spacing / 2.0 + j * spacing
+            y = half + r * 2.0 * half
+            b = s.body(DYNAMIC, x, y)
+            s.fixture(b, BOX, [half, half], 2, density=density, friction=friction)
+    return _settings(s, allow_sleep)
+
+
+def stacks(n_bodies: int, rng: SplitMix64, allow_sleep: bool = True, half: float = 0.5,
+           density: float = 1.0, friction: float = 0.6) -> Scene:
+    """Vertical stacks of boxes of seeded height 5..40 standing 2 m apart on an edge ground."""
+    h = rng.randint(5, 40)
+    n_stacks = max(1, -(-n_bodies // h))
+    s = Scene(name=f"stacks{n_bodies}")
+    width = n_stacks * 2.0 + 10.0
+    g = s.body(STATIC, 0.0, 0.0)
+    s.fixture(g, EDGE, [-width, 0.0, width, 0.0, 0, 0, 0, 0, 0, 0], friction=friction)
+    placed = 0
+    for k in range(n_stacks):
+        x = (k - (n_stacks - 1) / 2.0) * 2.0
+        for i in range(h):
+            if placed == n_bodies:
+                break
+            b = s.body(DYNAMIC, x, half + i * 2.0 * half)
+            s.fixture(b, BOX, [half, half], 2, density=density, friction=friction)
+            placed += 1
+    return _settings(s, allow_sleep)
+
+
+def _random_polygon(rng: SplitMix64, radius: float) -> list:
+    k = rng.randint(3, 8)
+    pts = []
+    for i in range(k):
+        ang = 2.0 * math.pi * (i + rng.uniform(-0.3, 0.3)) / k
+        pts += [_q(radius * math.cos(ang)), _q(radius * math.sin(ang))]
+    return pts
+
+
+def drop(n_bodies: int, rng: SplitMix64, half_size: float | None = None, allow_sleep: bool = True,
+         upper_half_only: bool = False, friction: float = 0.4) -> Scene:
+    """Mixed circles / convex polygons (50/50, radius U[0.25, 1]) dropped into a static square
+    container of 4 edges with side 2*half_size, floor at y = 0. Polygons have 3..8 vertices on a
+    jittered circle, hulled by b2PolygonShape::Set. Positions are random sequential adsorption with
+    non-overlapping bounding circles (over the upper half when it can hold them, else the whole
+    interior), density U[0.5, 5]."""
+    if half_size is None:
+        half_size = max(8.0, math.ceil(1.1 * math.sqrt(n_bodies)) + 2.0)
+    L = float(half_size)
+    s = Scene(name=f"drop{n_bodies}")
+    g = s.body(STATIC, 0.0, 0.0)
+    for v in ([-L, 0, L, 0], [-L, 0, -L, 2 * L], [L, 0, L, 2 * L], [-L, 2 * L, L, 2 * L]):
+        s.fixture(g, EDGE, v + [0, 0, 0, 0, 0, 0], friction=friction)
+    ylo = L if upper_half_only else 0.0
+    cell = 2.1
+    grid: dict = {}
+    placed = []
+    for i in range(n_bodies):
+        is_circle = rng.uniform() < 0.5
+        r = rng.uniform(0.25, 1.0)
+        shape = None if is_circle else _random_polygon(rng, r)
+        density = rng.uniform(0.5, 5.0)
+        for _attempt in range(10000):
+            x = rng.uniform(-L + 1.05, L - 1.05)
+            y = rng.uniform(ylo + 1.05, 2 * L - 1.05)
+            cx, cy = int(math.floor(x / cell)), int(math.floor(y / cell))
+            ok = True
+            for dx in (-1, 0, 1):
+                for dy in (-1, 0, 1):
+                    for (px, py, pr) in grid.get((cx + dx, cy + dy), ()):
+                        if (px - x) ** 2 + (py - y) ** 2 < (pr + r + 0.05) ** 2:
+                            ok = False
+                            break
+                    if not ok:
+                        break
+                if not ok:
+                    break
+            if ok:
+                break
+        else:
+            raise RuntimeError("drop scene too dense for its container")
+        x, y = _q(x), _q(y)
+        grid.setdefault((cx, cy), []).append((x, y, r))
+        placed.append((x, y))
+        b = s.body(DYNAMIC, x, y)
+        if is_circle:
+            s.fixture(b, CIRCLE, [0.0, 0.0, _q(r)], density=density, friction=friction)
+        else:
+            s.fixture(b, POLYGON, shape, len(shape) // 2, density=density, friction=friction)
+    return _settings(s, allow_sleep)
+
+
+def chains(n_chains: int, links: int, rng: SplitMix64, allow_sleep: bool = True, spacing: float = 3.0,
+           limit: float = math.pi / 6.0) -> Scene:
+    """Chains of revolute-jointed 0.1 x 0.5 m box links (limits +/-30 degrees) hanging from a static
+    anchor body, with loose boxes and circles (half-extent / radius U[0.2, 0.8]) dropped beside them."""
+    s = Scene(name=f"chains{n_chains}x{links}")
+    g = s.body(STATIC, 0.0, 0.0)
+    W = n_chains * spacing + 10.0
+    s.fixture(g, EDGE, [-W, 0.0, W, 0.0, 0, 0, 0, 0, 0, 0], friction=0.6)
+    top = links * 1.0 + 4.0
+    for c in range(n_chains):
+        x = (c - (n_chains - 1) / 2.0) * spacing
+        prev = g
+        prev_anchor = (x, top)
+        for k in range(links):
+            y = top - 0.5 - k * 1.0
+            b = s.body(DYNAMIC, x, y)
+            s.fixture(b, BOX, [0.1, 0.5], 2, density=1.0, friction=0.4, group=-(c + 1))
+            anchor_world = (x, y + 0.5)
+            if prev == g:
+                la = anchor_world
+            else:
+                la = (0.0, -0.5)
+            s.revolute(prev, b, la, (0.0, 0.5), 0.0, -limit, limit, flags=1)
+            prev = b
+    return _settings(s, allow_sleep)
+
+
+# ---------------------------------------------------------------------- named workloads
+def config1(allow_sleep: bool = True) -> Scene:
+    """210-box pyramid on an edge ground (dt 1/60, 8/3 iterations, 600 steps)."""
+    return pyramid(20, allow_sleep=allow_sleep)
+
+
+def config2(n_bodies: int = 10000, seed: int = 1, allow_sleep: bool = True) -> Scene:
+    """Mixed drop into a 200 x 200 m edge box (dt 1/60, 8/3 iterations, 1000 steps)."""
+    return drop(n_bodies, SplitMix64(seed), half_size=100.0, allow_sleep=allow_sleep)
+
+
+def config3(n_worlds: int = 4096, seed: int = 1, allow_sleep: bool = True, min_bodies: int = 16,
+            max_bodies: int = 512) -> list:
+    """Independent worlds with log-uniform body counts in [min, max] and a seeded kind among
+    pyramid / stacks / drop (dt 1/60, 8/3 iterations, 600 steps)."""
+    rng = SplitMix64(seed)
+    worlds = []
+    for w in range(n_worlds):
+        n = int(round(math.exp(rng.uniform(math.log(min_bodies), math.log(max_bodies)))))
+        kind = rng.randint(0, 2)
+        sub = SplitMix64(rng.next_u64())
+        if kind == 0:
+            rows = max(1, int((math.sqrt(8 * n + 1) - 1) // 2))
+            sc = pyramid(rows, allow_sleep=allow_sleep)
+        elif kind == 1:
+            sc = stacks(n, sub, allow_sleep=allow_sleep)
+        else:
+            sc = drop(n, sub, allow_sleep=allow_sleep)
+        worlds.append(sc)
+    return worlds
+
+
+def config5(n_chains: int = 512, links: int = 16, seed: int = 1, allow_sleep: bool = True) -> Scene:
+    """Revolute-joint chains (limits +/-30 degrees); a reduced stand-in of the joint stress world."""
+    return chains(n_chains, links, SplitMix64(seed), allow_sleep=allow_sleep)

@@ -1,0 +1,228 @@
+"""Oracle (test infrastructure only; never imported by the product).
+
+Two CPU implementations of the Box2D 2.3.2 step, driven through the same C-ABI shape:
+
+* ``ReferenceWorld`` - the UNMODIFIED reference (box2dref from the reference tree) compiled here by
+  ``oracle/Makefile`` into ``oracle/_ref/``; available only where the reference tree exists (it is
+  the source of the committed golden vectors under ``tests/golden/``). ``trig="libm"`` links glibc's
+  sinf/cosf, ``trig="project"`` links the project trig (``oracle/trig.c``) in their place.
+* ``PortWorld`` - the project's own CPU restatement (``oracle/port/``), built on any machine into
+  ``oracle/_build/liboracle.so``; ``trig`` selects the same two sin/cos choices.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg use this package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_TREE = os.environ.get("B2_REFERENCE_TREE", "/root/reference/Regression/box2d-ref")
+
+_f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+def build_port(quiet: bool = True) -> str:
+    """Compile the CPU restatement (runs make; cheap when up to date)."""
+    out = subprocess.run(["make", "-C", HERE, "port"], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle port build failed:\n" + out.stdout + out.stderr)
+    return os.path.join(HERE, "_build", "liboracle.so")
+
+
+def reference_available() -> bool:
+    return os.path.isdir(os.path.join(REF_TREE, "Box2DRef"))
+
+
+def build_reference() -> None:
+    """Compile the reference from its own sources (only where the reference tree exists)."""
+    if not reference_available():
+        raise RuntimeError("reference tree not present")
+    out = subprocess.run(["make", "-C", HERE, "ref", f"REF={REF_TREE}", "-j8"], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("reference build failed:\n" + out.stdout + out.stderr)
+
+
+_LIBS: dict = {}
+
+
+def _declare(lib, p: str) -> None:
+    vp = C.c_void_p
+    sig = {
+        "create": (vp, [C.c_float, C.c_float]),
+        "destroy": (None, [vp]),
+        "config": (None, [vp, C.c_int, C.c_int, C.c_int, C.c_int]),
+        "build": (None, [vp, C.c_int, _i32p, _f32p, _i32p, C.c_int, _i32p, _i32p, _f32p, _i32p, _f32p, _i32p,
+                         C.c_int, _i32p, _i32p, _f32p, _i32p]),
+        "step": (None, [vp, C.c_float, C.c_int, C.c_int]),
+        "body_count": (C.c_int, [vp]),
+        "contact_count": (C.c_int, [vp]),
+        "get_bodies": (None, [vp, _f32p]),
+        "get_contacts": (C.c_int, [vp, _i32p, _f32p, C.c_int]),
+        "get_proxies": (None, [vp, _i32p, _f32p]),
+        "collide": (C.c_int, [C.c_int, _f32p, C.c_int, _f32p, C.c_int, _f32p, C.c_int, _f32p, _i32p, _f32p]),
+        "polygon": (None, [C.c_int, _f32p, C.c_int, C.c_float, _f32p]),
+        "toi": (None, [C.c_int, _f32p, C.c_int, _f32p, C.c_int, _f32p, C.c_int, _f32p, C.c_float, _f32p]),
+        "sincosf": (None, [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+        "step_many": (None, [C.POINTER(vp), C.c_int, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int]),
+    }
+    if p == "po_":
+        sig["set_trig"] = (None, [C.c_int])
+        sig["record_events"] = (None, [vp, C.c_int])
+        sig["get_pairs"] = (C.c_int, [vp, _i32p, C.c_int])
+        sig["get_events"] = (C.c_int, [vp, _i32p, _f32p, C.c_int])
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, p + name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def load(kind: str = "port", trig: str = "project"):
+    """Return (ctypes library, symbol prefix) for kind 'port' or 'reference'."""
+    key = (kind, trig)
+    if key in _LIBS:
+        return _LIBS[key]
+    if kind == "port":
+        path = os.path.join(HERE, "_build", "liboracle.so")
+        if not os.path.exists(path):
+            build_port()
+        # one private copy per trig mode: the mode is a process-wide switch inside the library
+        lib = C.CDLL(path, mode=C.RTLD_LOCAL) if trig == "project" else C.CDLL(_copy_for(path, trig), mode=C.RTLD_LOCAL)
+        _declare(lib, "po_")
+        lib.po_set_trig(1 if trig == "project" else 0)
+        res = (lib, "po_")
+    elif kind == "reference":
+        name = "libref_proj.so" if trig == "project" else "libref_libm.so"
+        path = os.path.join(HERE, "_ref", name)
+        if not os.path.exists(path):
+            build_reference()
+        lib = C.CDLL(path, mode=C.RTLD_LOCAL)
+        _declare(lib, "rw_")
+        res = (lib, "rw_")
+    else:
+        raise ValueError(kind)
+    _LIBS[key] = res
+    return res
+
+
+def _copy_for(path: str, tag: str) -> str:
+    dst = path.replace(".so", f"_{tag}.so")
+    if not os.path.exists(dst) or os.path.getmtime(dst) < os.path.getmtime(path):
+        import shutil
+        shutil.copyfile(path, dst)
+    return dst
+
+
+class OracleWorld:
+    """One world of either CPU implementation, built from a ``box2dpp_gb300.scenes.Scene``."""
+
+    def __init__(self, scene, kind: str = "port", trig: str = "project"):
+        self.lib, self.p = load(kind, trig)
+        self.kind = kind
+        f = self._fn
+        self.h = f("create")(float(scene.gravity[0]), float(scene.gravity[1]))
+        f("config")(self.h, int(scene.allow_sleep), int(scene.warm_starting), int(scene.continuous),
+                    int(scene.sub_stepping))
+        a = scene.arrays()
+        f("build")(self.h, len(a["body_type"]), a["body_type"], a["body_f"], a["body_flags"],
+                   len(a["fix_body"]), a["fix_body"], a["fix_type"], a["fix_shape"], a["fix_n"], a["fix_mat"],
+                   a["fix_filt"], len(a["joint_a"]), a["joint_a"], a["joint_b"], a["joint_f"], a["joint_flags"])
+        self.n_fixtures = len(a["fix_body"])
+
+    def _fn(self, name):
+        return getattr(self.lib, self.p + name)
+
+    def __del__(self):
+        try:
+            self._fn("destroy")(self.h)
+        except Exception:
+            pass
+
+    def step(self, dt: float = 1.0 / 60.0, vi: int = 8, pi: int = 3) -> None:
+        self._fn("step")(self.h, dt, vi, pi)
+
+    def bodies(self) -> np.ndarray:
+        n = self._fn("body_count")(self.h)
+        out = np.zeros((n, 12), dtype=np.float32)
+        self._fn("get_bodies")(self.h, out)
+        return out
+
+    def contacts(self):
+        n = self._fn("contact_count")(self.h)
+        ints = np.zeros((max(n, 1), 8), dtype=np.int32)
+        flts = np.zeros((max(n, 1), 12), dtype=np.float32)
+        got = self._fn("get_contacts")(self.h, ints, flts, n)
+        return ints[:got], flts[:got]
+
+    def proxies(self):
+        ids = np.zeros(max(self.n_fixtures, 1), dtype=np.int32)
+        fat = np.zeros((max(self.n_fixtures, 1), 4), dtype=np.float32)
+        self._fn("get_proxies")(self.h, ids, fat)
+        return ids[:self.n_fixtures], fat[:self.n_fixtures]
+
+    def pairs(self) -> np.ndarray:
+        n = self._fn("get_pairs")(self.h, np.zeros(2, dtype=np.int32), 0)
+        out = np.zeros((max(n, 1), 2), dtype=np.int32)
+        self._fn("get_pairs")(self.h, out, n)
+        return out[:n]
+
+    def record_events(self, on: bool = True) -> None:
+        self._fn("record_events")(self.h, int(on))
+
+    def events(self):
+        n = self._fn("get_events")(self.h, np.zeros(3, dtype=np.int32), np.zeros(4, dtype=np.float32), 0)
+        ints = np.zeros((max(n, 1), 3), dtype=np.int32)
+        flts = np.zeros((max(n, 1), 4), dtype=np.float32)
+        self._fn("get_events")(self.h, ints, flts, n)
+        return ints[:n], flts[:n]
+
+
+def step_many(worlds: list, steps: int, threads: int, dt: float = 1.0 / 60.0, vi: int = 8, pi: int = 3) -> None:
+    """Step independent worlds of one kind on `threads` host threads (round-robin split)."""
+    if not worlds:
+        return
+    lib, p = worlds[0].lib, worlds[0].p
+    arr = (C.c_void_p * len(worlds))(*[w.h for w in worlds])
+    getattr(lib, p + "step_many")(arr, len(worlds), dt, vi, pi, steps, threads)
+
+
+def collide(kind: str, trig: str, typeA, shapeA, nA, xfA, typeB, shapeB, nB, xfB):
+    lib, p = load(kind, trig)
+    oi = np.zeros(4, dtype=np.int32)
+    of = np.zeros(12, dtype=np.float32)
+    sa = np.zeros(16, dtype=np.float32); sa[:len(shapeA)] = shapeA
+    sb = np.zeros(16, dtype=np.float32); sb[:len(shapeB)] = shapeB
+    r = getattr(lib, p + "collide")(typeA, sa, nA, np.asarray(xfA, dtype=np.float32), typeB, sb, nB,
+                                    np.asarray(xfB, dtype=np.float32), oi, of)
+    if r != 0:
+        raise ValueError("unsupported shape pair")
+    return oi, of
+
+
+def polygon(kind: str, type_, shape, n, density=1.0):
+    lib, p = load(kind, "project")
+    s = np.zeros(16, dtype=np.float32); s[:len(shape)] = shape
+    out = np.zeros(40, dtype=np.float32)
+    getattr(lib, p + "polygon")(type_, s, n, density, out)
+    return out
+
+
+def toi(kind: str, trig: str, typeA, shapeA, nA, sweepA, typeB, shapeB, nB, sweepB, tmax=1.0):
+    lib, p = load(kind, trig)
+    sa = np.zeros(16, dtype=np.float32); sa[:len(shapeA)] = shapeA
+    sb = np.zeros(16, dtype=np.float32); sb[:len(shapeB)] = shapeB
+    out = np.zeros(2, dtype=np.float32)
+    getattr(lib, p + "toi")(typeA, sa, nA, np.asarray(sweepA, dtype=np.float32), typeB, sb, nB,
+                            np.asarray(sweepB, dtype=np.float32), tmax, out)
+    return int(out[0]), float(out[1])
+
+
+def sincosf(kind: str, trig: str, x: float):
+    lib, p = load(kind, trig)
+    s, c = C.c_float(), C.c_float()
+    getattr(lib, p + "sincosf")(x, C.byref(s), C.byref(c))
+    return s.value, c.value

@@ -1,0 +1,1414 @@
+// Oracle (test infrastructure only): the CPU restatement of Box2D 2.3.2 b2World::Step with its
+// contact manager, island builder, island solver, contact solver, continuous (TOI) pass and revolute
+// joint. Paths are relative to the reference tree's Regression/box2d-ref/Box2DRef/.
+#include "world.h"
+
+#include <cstring>
+
+namespace b2o {
+
+// ---------------------------------------------------------------- bodies, fixtures, joints
+// b2World::CreateBody (Dynamics/b2World.cpp:115-140) + b2Body::b2Body (Dynamics/b2Body.cpp:27-107)
+int World::CreateBody(int type, const float* f, int fl)
+{
+    Body b;
+    b.flags = 0;
+    if (fl & 8) b.flags |= kBBullet;
+    if (fl & 4) b.flags |= kBFixedRot;
+    if (fl & 1) b.flags |= kBAutoSleep;
+    if (fl & 2) b.flags |= kBAwake;
+    if (fl & 16) b.flags |= kBActive;
+    b.xf.p = V(f[0], f[1]);
+    b.xf.q = RotOf(f[2]);
+    b.sweep.localCenter = V(0.0f, 0.0f);
+    b.sweep.c0 = b.xf.p;
+    b.sweep.c = b.xf.p;
+    b.sweep.a0 = f[2];
+    b.sweep.a = f[2];
+    b.sweep.alpha0 = 0.0f;
+    b.v = V(f[3], f[4]);
+    b.w = f[5];
+    b.linearDamping = f[6];
+    b.angularDamping = f[7];
+    b.gravityScale = f[8];
+    b.type = type;
+    if (type == kDynamic) { b.mass = 1.0f; b.invMass = 1.0f; }
+    int id = (int)bodies.size();
+    b.prev = kNull;
+    b.next = bodyList;
+    bodies.push_back(b);
+    if (bodyList != kNull) bodies[bodyList].prev = id;
+    bodyList = id;
+    ++bodyCount;
+    return id;
+}
+
+// b2Body::ResetMassData (Dynamics/b2Body.cpp:283-352)
+void World::ResetMassData(int bi)
+{
+    Body& b = bodies[bi];
+    b.mass = 0.0f; b.invMass = 0.0f; b.I = 0.0f; b.invI = 0.0f;
+    b.sweep.localCenter = V(0.0f, 0.0f);
+    if (b.type == kStatic || b.type == kKinematic) {
+        b.sweep.c0 = b.xf.p;
+        b.sweep.c = b.xf.p;
+        b.sweep.a0 = b.sweep.a;
+        return;
+    }
+    Vec2 localCenter = V(0.0f, 0.0f);
+    for (int f = b.fixtureList; f != kNull; f = fixtures[f].next) {
+        if (fixtures[f].density == 0.0f) continue;
+        MassData md;
+        ComputeMass(fixtures[f].shape, fixtures[f].density, &md);
+        b.mass += md.mass;
+        localCenter = localCenter + md.mass * md.center;
+        b.I += md.I;
+    }
+    if (b.mass > 0.0f) {
+        b.invMass = 1.0f / b.mass;
+        localCenter.x *= b.invMass;
+        localCenter.y *= b.invMass;
+    } else {
+        b.mass = 1.0f;
+        b.invMass = 1.0f;
+    }
+    if (b.I > 0.0f && (b.flags & kBFixedRot) == 0) {
+        b.I -= b.mass * Dot(localCenter, localCenter);
+        b.invI = 1.0f / b.I;
+    } else {
+        b.I = 0.0f;
+        b.invI = 0.0f;
+    }
+    Vec2 oldCenter = b.sweep.c;
+    b.sweep.localCenter = localCenter;
+    b.sweep.c = Mul(b.xf, b.sweep.localCenter);
+    b.sweep.c0 = b.sweep.c;
+    b.v = b.v + Cross(b.w, b.sweep.c - oldCenter);
+}
+
+// b2Body::CreateFixture (Dynamics/b2Body.cpp:165-201) + b2Fixture::CreateProxies (b2Fixture.cpp:121-137)
+int World::CreateFixture(int bi, const Shape& shape, float density, float friction, float restitution,
+                         int category, int mask, int group, bool sensor)
+{
+    Fixture fx;
+    fx.body = bi;
+    fx.shape = shape;
+    fx.density = density;
+    fx.friction = friction;
+    fx.restitution = restitution;
+    fx.category = (uint16_t)category;
+    fx.mask = (uint16_t)mask;
+    fx.group = (int16_t)group;
+    fx.sensor = sensor;
+    int id = (int)fixtures.size();
+    fixtures.push_back(fx);
+    Body& b = bodies[bi];
+    if (b.flags & kBActive) {
+        Fixture& f = fixtures[id];
+        f.proxyCount = 1;
+        ComputeAABB(f.shape, b.xf, &f.aabb);
+        f.proxyId = bp.CreateProxy(f.aabb, id);
+    }
+    fixtures[id].next = b.fixtureList;
+    b.fixtureList = id;
+    if (density > 0.0f) ResetMassData(bi);
+    wflags |= 0x1; // e_newFixture
+    return id;
+}
+
+// b2World::CreateJoint (Dynamics/b2World.cpp:212-269) + b2RevoluteJoint::b2RevoluteJoint (b2RevoluteJoint.cpp:44-63)
+int World::CreateRevolute(int a, int b, const float* f, int fl)
+{
+    Joint j;
+    j.bodyA = a; j.bodyB = b;
+    j.localAnchorA = V(f[0], f[1]);
+    j.localAnchorB = V(f[2], f[3]);
+    j.referenceAngle = f[4];
+    j.lowerAngle = f[5];
+    j.upperAngle = f[6];
+    j.motorSpeed = f[7];
+    j.maxMotorTorque = f[8];
+    j.enableLimit = (fl & 1) != 0;
+    j.enableMotor = (fl & 2) != 0;
+    j.collideConnected = (fl & 4) != 0;
+    int id = (int)joints.size();
+    j.prev = kNull;
+    j.next = jointList;
+    joints.push_back(j);
+    if (jointList != kNull) joints[jointList].prev = id;
+    jointList = id;
+    ++jointCount;
+    // edge 2*id is on bodyA's list (other = bodyB), 2*id+1 on bodyB's list (other = bodyA)
+    for (int side = 0; side < 2; ++side) {
+        Body& body = bodies[side == 0 ? a : b];
+        int e = 2 * id + side;
+        joints[id].ePrev[side] = kNull;
+        joints[id].eNext[side] = body.jointList;
+        if (body.jointList != kNull) joints[body.jointList >> 1].ePrev[body.jointList & 1] = e;
+        body.jointList = e;
+    }
+    if (!j.collideConnected) {
+        for (int e = bodies[b].contactList; e != kNull; e = contacts[e >> 1].eNext[e & 1])
+            if (EdgeOther(e) == a) contacts[e >> 1].flags |= kCFilter;
+    }
+    return id;
+}
+
+int World::EdgeOther(int e) const
+{
+    const Contact& c = contacts[e >> 1];
+    return (e & 1) == 0 ? fixtures[c.fB].body : fixtures[c.fA].body;
+}
+int World::JointEdgeOther(int e) const
+{
+    const Joint& j = joints[e >> 1];
+    return (e & 1) == 0 ? j.bodyB : j.bodyA;
+}
+
+// b2Body::SetAwake (Dynamics/b2Body.h:625-645)
+void World::SetAwake(int bi, bool flag)
+{
+    Body& b = bodies[bi];
+    if (flag) {
+        if ((b.flags & kBAwake) == 0) { b.flags |= kBAwake; b.sleepTime = 0.0f; }
+    } else {
+        b.flags &= ~kBAwake;
+        b.sleepTime = 0.0f;
+        b.v = V(0.0f, 0.0f);
+        b.w = 0.0f;
+        b.force = V(0.0f, 0.0f);
+        b.torque = 0.0f;
+    }
+}
+
+// b2Body::ShouldCollide (Dynamics/b2Body.cpp:354-375), called as bodyB->ShouldCollide(bodyA)
+bool World::ShouldCollide(int self, int other) const
+{
+    if (bodies[self].type != kDynamic && bodies[other].type != kDynamic) return false;
+    for (int e = bodies[self].jointList; e != kNull; e = joints[e >> 1].eNext[e & 1]) {
+        if (JointEdgeOther(e) == other && !joints[e >> 1].collideConnected) return false;
+    }
+    return true;
+}
+
+// b2Body::SynchronizeTransform (Dynamics/b2Body.h:850-854)
+void World::SynchronizeTransform(int bi)
+{
+    Body& b = bodies[bi];
+    b.xf.q = RotOf(b.sweep.a);
+    b.xf.p = b.sweep.c - Mul(b.xf.q, b.sweep.localCenter);
+}
+
+// b2Body::Advance (Dynamics/b2Body.h:856-864)
+void World::Advance(int bi, float alpha)
+{
+    Body& b = bodies[bi];
+    SweepAdvance(b.sweep, alpha);
+    b.sweep.c = b.sweep.c0;
+    b.sweep.a = b.sweep.a0;
+    b.xf.q = RotOf(b.sweep.a);
+    b.xf.p = b.sweep.c - Mul(b.xf.q, b.sweep.localCenter);
+}
+
+// b2Body::SynchronizeFixtures (Dynamics/b2Body.cpp:443-455) + b2Fixture::Synchronize (b2Fixture.cpp:154-177)
+void World::SynchronizeFixtures(int bi)
+{
+    Body& b = bodies[bi];
+    Xf xf1;
+    xf1.q = RotOf(b.sweep.a0);
+    xf1.p = b.sweep.c0 - Mul(xf1.q, b.sweep.localCenter);
+    for (int f = b.fixtureList; f != kNull; f = fixtures[f].next) {
+        Fixture& fx = fixtures[f];
+        if (fx.proxyCount == 0) continue;
+        AABB a1, a2;
+        ComputeAABB(fx.shape, xf1, &a1);
+        ComputeAABB(fx.shape, b.xf, &a2);
+        fx.aabb = Combine(a1, a2);
+        Vec2 displacement = b.xf.p - xf1.p;
+        bp.MoveProxy(fx.proxyId, fx.aabb, displacement);
+    }
+}
+
+// ---------------------------------------------------------------- contact manager
+// b2ContactManager::FindNewContacts (Dynamics/b2ContactManager.cpp:174-177) via UpdatePairs
+void World::FindNewContacts()
+{
+    std::vector<Pair> list;
+    bp.ComputePairs(list);
+    for (const Pair& p : list) stepPairs.push_back(p);
+    stepPairs.push_back(Pair{-1, -1});
+    for (const Pair& p : list) AddPair(p.a, p.b);
+}
+
+static bool PrimaryOrder(int t1, int t2, bool* exists)
+{
+    // b2Contact::InitializeRegisters (Dynamics/Contacts/b2Contact.cpp:40-49): primary (A-type, B-type)
+    // pairs are circle/circle, polygon/circle, polygon/polygon, edge/circle, edge/polygon.
+    *exists = !(t1 == kEdge && t2 == kEdge);
+    if (t1 == t2) return true;
+    if (t1 == kPolygon && t2 == kCircle) return true;
+    if (t1 == kEdge) return true;
+    return false;
+}
+
+// b2ContactManager::AddPair (Dynamics/b2ContactManager.cpp:179-294)
+void World::AddPair(int proxyA, int proxyB)
+{
+    int fixtureA = bp.tree.nodes[proxyA].user, fixtureB = bp.tree.nodes[proxyB].user;
+    int bodyA = fixtures[fixtureA].body, bodyB = fixtures[fixtureB].body;
+    if (bodyA == bodyB) return;
+    for (int e = bodies[bodyB].contactList; e != kNull; e = contacts[e >> 1].eNext[e & 1]) {
+        if (EdgeOther(e) == bodyA) {
+            const Contact& c = contacts[e >> 1];
+            if (c.fA == fixtureA && c.fB == fixtureB) return;
+            if (c.fA == fixtureB && c.fB == fixtureA) return;
+        }
+    }
+    if (!ShouldCollide(bodyB, bodyA)) return;
+    // default b2ContactFilter::ShouldCollide (Dynamics/b2WorldCallbacks.cpp:26-38)
+    const Fixture& fa = fixtures[fixtureA];
+    const Fixture& fb = fixtures[fixtureB];
+    if (fa.group == fb.group && fa.group != 0) {
+        if (!(fa.group > 0)) return;
+    } else if (!((fa.mask & fb.category) != 0 && (fa.category & fb.mask) != 0)) {
+        return;
+    }
+    bool exists;
+    bool primary = PrimaryOrder(fa.shape.type, fb.shape.type, &exists);
+    if (!exists) return;
+    int fA = primary ? fixtureA : fixtureB, fB = primary ? fixtureB : fixtureA;
+    int c;
+    if (!freeContacts.empty()) { c = freeContacts.back(); freeContacts.pop_back(); contacts[c] = Contact(); }
+    else { c = (int)contacts.size(); contacts.push_back(Contact()); }
+    Contact& ct = contacts[c];
+    ct.alive = true;
+    ct.flags = kCEnabled;
+    ct.fA = fA; ct.fB = fB;
+    ct.m.pointCount = 0;
+    ct.toiCount = 0;
+    ct.friction = sqrtf(fixtures[fA].friction * fixtures[fB].friction);
+    float ra = fixtures[fA].restitution, rb = fixtures[fB].restitution;
+    ct.restitution = ra > rb ? ra : rb;
+    ct.tangentSpeed = 0.0f;
+    Link(c);
+    if (!fixtures[fA].sensor && !fixtures[fB].sensor) {
+        SetAwake(fixtures[fA].body, true);
+        SetAwake(fixtures[fB].body, true);
+    }
+    ++contactCount;
+}
+
+// Prepend to the world list and both bodies' edge lists (b2ContactManager.cpp:255-290).
+int World::Link(int c)
+{
+    Contact& ct = contacts[c];
+    ct.prev = kNull;
+    ct.next = contactList;
+    if (contactList != kNull) contacts[contactList].prev = c;
+    contactList = c;
+    int bA = fixtures[ct.fA].body, bB = fixtures[ct.fB].body;
+    for (int side = 0; side < 2; ++side) {
+        Body& body = bodies[side == 0 ? bA : bB];
+        int e = 2 * c + side;
+        contacts[c].ePrev[side] = kNull;
+        contacts[c].eNext[side] = body.contactList;
+        if (body.contactList != kNull) contacts[body.contactList >> 1].ePrev[body.contactList & 1] = e;
+        body.contactList = e;
+    }
+    return c;
+}
+
+// b2ContactManager::Destroy (Dynamics/b2ContactManager.cpp:39-105) + b2Contact::Destroy (b2Contact.cpp:102-123)
+void World::Destroy(int c)
+{
+    Contact& ct = contacts[c];
+    int bA = fixtures[ct.fA].body, bB = fixtures[ct.fB].body;
+    if (ct.flags & kCTouching) {
+        if (recordEvents) events.push_back(Event{1, ct.fA, ct.fB, 0, 0, 0, 0});
+    }
+    if (ct.prev != kNull) contacts[ct.prev].next = ct.next;
+    if (ct.next != kNull) contacts[ct.next].prev = ct.prev;
+    if (c == contactList) contactList = ct.next;
+    for (int side = 0; side < 2; ++side) {
+        int body = side == 0 ? bA : bB;
+        int e = 2 * c + side;
+        int pe = ct.ePrev[side], ne = ct.eNext[side];
+        if (pe != kNull) contacts[pe >> 1].eNext[pe & 1] = ne;
+        if (ne != kNull) contacts[ne >> 1].ePrev[ne & 1] = pe;
+        if (bodies[body].contactList == e) bodies[body].contactList = ne;
+    }
+    if (ct.m.pointCount > 0 && !fixtures[ct.fA].sensor && !fixtures[ct.fB].sensor) {
+        SetAwake(bA, true);
+        SetAwake(bB, true);
+    }
+    ct.alive = false;
+    freeContacts.push_back(c);
+    --contactCount;
+}
+
+// b2Contact::Evaluate dispatch (Dynamics/Contacts/b2*Contact.cpp Evaluate)
+void World::Evaluate(int c, Manifold* m)
+{
+    const Contact& ct = contacts[c];
+    const Fixture& fa = fixtures[ct.fA];
+    const Fixture& fb = fixtures[ct.fB];
+    const Xf& xfA = bodies[fa.body].xf;
+    const Xf& xfB = bodies[fb.body].xf;
+    int ta = fa.shape.type, tb = fb.shape.type;
+    if (ta == kCircle) CollideCircles(m, fa.shape, xfA, fb.shape, xfB);
+    else if (ta == kPolygon && tb == kCircle) CollidePolygonAndCircle(m, fa.shape, xfA, fb.shape, xfB);
+    else if (ta == kPolygon) CollidePolygons(m, fa.shape, xfA, fb.shape, xfB);
+    else if (tb == kCircle) CollideEdgeAndCircle(m, fa.shape, xfA, fb.shape, xfB);
+    else CollideEdgeAndPolygon(m, fa.shape, xfA, fb.shape, xfB);
+}
+
+// b2Contact::Update (Dynamics/Contacts/b2Contact.cpp:164-245). Sensors: overlap test via GJK.
+void World::Update(int c)
+{
+    Contact& ct = contacts[c];
+    Manifold old = ct.m;
+    ct.flags |= kCEnabled;
+    bool touching = false;
+    bool wasTouching = (ct.flags & kCTouching) != 0;
+    const Fixture& fa = fixtures[ct.fA];
+    const Fixture& fb = fixtures[ct.fB];
+    bool sensor = fa.sensor || fb.sensor;
+    int bA = fa.body, bB = fb.body;
+    if (sensor) {
+        DistanceProxy pa, pb;
+        ProxyOf(&pa, fa.shape);
+        ProxyOf(&pb, fb.shape);
+        SimplexCache cache;
+        cache.count = 0;
+        DistanceOutput out;
+        Distance(&out, &cache, pa, bodies[bA].xf, pb, bodies[bB].xf, true);
+        touching = out.distance < 10.0f * kEpsilon;
+        ct.m.pointCount = 0;
+    } else {
+        Evaluate(c, &ct.m);
+        touching = ct.m.pointCount > 0;
+        for (int i = 0; i < ct.m.pointCount; ++i) {
+            ManifoldPoint* mp2 = ct.m.points + i;
+            mp2->normalImpulse = 0.0f;
+            mp2->tangentImpulse = 0.0f;
+            for (int j = 0; j < old.pointCount; ++j) {
+                if (old.points[j].id == mp2->id) {
+                    mp2->normalImpulse = old.points[j].normalImpulse;
+                    mp2->tangentImpulse = old.points[j].tangentImpulse;
+                    break;
+                }
+            }
+        }
+        if (touching != wasTouching) {
+            SetAwake(bA, true);
+            SetAwake(bB, true);
+        }
+    }
+    if (touching) ct.flags |= kCTouching;
+    else ct.flags &= ~kCTouching;
+    if (recordEvents) {
+        if (!wasTouching && touching) events.push_back(Event{0, ct.fA, ct.fB, 0, 0, 0, 0});
+        if (wasTouching && !touching) events.push_back(Event{1, ct.fA, ct.fB, 0, 0, 0, 0});
+        if (!sensor && touching) events.push_back(Event{2, ct.fA, ct.fB, 0, 0, 0, 0});
+    }
+}
+
+// b2ContactManager::Collide (Dynamics/b2ContactManager.cpp:107-172)
+void World::Collide()
+{
+    int c = contactList;
+    while (c != kNull) {
+        Contact& ct = contacts[c];
+        int bA = fixtures[ct.fA].body, bB = fixtures[ct.fB].body;
+        if (ct.flags & kCFilter) {
+            bool keep = ShouldCollide(bB, bA);
+            if (keep) {
+                const Fixture& fa = fixtures[ct.fA];
+                const Fixture& fb = fixtures[ct.fB];
+                if (fa.group == fb.group && fa.group != 0) keep = fa.group > 0;
+                else keep = (fa.mask & fb.category) != 0 && (fa.category & fb.mask) != 0;
+            }
+            if (!keep) { int nuke = c; c = ct.next; Destroy(nuke); continue; }
+            ct.flags &= ~kCFilter;
+        }
+        bool activeA = bodies[bA].IsAwake() && bodies[bA].type != kStatic;
+        bool activeB = bodies[bB].IsAwake() && bodies[bB].type != kStatic;
+        if (!activeA && !activeB) { c = ct.next; continue; }
+        bool overlap = bp.TestOverlap(fixtures[ct.fA].proxyId, fixtures[ct.fB].proxyId);
+        if (!overlap) { int nuke = c; c = ct.next; Destroy(nuke); continue; }
+        Update(c);
+        c = contacts[c].next;
+    }
+}
+
+// ---------------------------------------------------------------- contact solver
+namespace {
+struct Mat22 { Vec2 ex, ey; };
+inline Vec2 MulM(const Mat22& A, Vec2 v) { return V(A.ex.x * v.x + A.ey.x * v.y, A.ex.y * v.x + A.ey.y * v.y); }
+// b2Mat22::GetInverse (Common/b2Math.h:185-197)
+inline Mat22 Inverse(const Mat22& M)
+{
+    float a = M.ex.x, b = M.ey.x, c = M.ex.y, d = M.ey.y;
+    Mat22 B;
+    float det = a * d - b * c;
+    if (det != 0.0f) det = 1.0f / det;
+    B.ex.x = det * d; B.ey.x = -det * b;
+    B.ex.y = -det * c; B.ey.y = det * a;
+    return B;
+}
+
+struct VelPoint { Vec2 rA, rB; float normalImpulse, tangentImpulse, normalMass, tangentMass, velocityBias; };
+struct VelConstraint {
+    VelPoint points[2];
+    Vec2 normal;
+    Mat22 normalMass, K;
+    int indexA, indexB;
+    float invMassA, invMassB, invIA, invIB, friction, restitution, tangentSpeed;
+    int pointCount, contactIndex;
+};
+struct PosConstraint {
+    Vec2 localPoints[2], localNormal, localPoint;
+    int indexA, indexB;
+    float invMassA, invMassB;
+    Vec2 localCenterA, localCenterB;
+    float invIA, invIB;
+    int type;
+    float radiusA, radiusB;
+    int pointCount;
+};
+
+// b2ContactSolver (Dynamics/Contacts/b2ContactSolver.cpp)
+struct ContactSolver {
+    World* w;
+    StepInfo step;
+    std::vector<VelConstraint> vcs;
+    std::vector<PosConstraint> pcs;
+    const int* contactIds;
+    int count;
+    Position* positions;
+    Velocity* velocities;
+
+    // b2ContactSolver::b2ContactSolver (b2ContactSolver.cpp:49-141)
+    ContactSolver(World* world, const StepInfo& st, const int* ids, int n, Position* pos, Velocity* vel)
+        : w(world), step(st), contactIds(ids), count(n), positions(pos), velocities(vel)
+    {
+        vcs.resize(n);
+        pcs.resize(n);
+        for (int i = 0; i < n; ++i) {
+            const Contact& c = w->contacts[ids[i]];
+            const Fixture& fa = w->fixtures[c.fA];
+            const Fixture& fb = w->fixtures[c.fB];
+            const Body& bA = w->bodies[fa.body];
+            const Body& bB = w->bodies[fb.body];
+            const Manifold& m = c.m;
+            VelConstraint& vc = vcs[i];
+            vc.friction = c.friction;
+            vc.restitution = c.restitution;
+            vc.tangentSpeed = c.tangentSpeed;
+            vc.indexA = bA.islandIndex;
+            vc.indexB = bB.islandIndex;
+            vc.invMassA = bA.invMass; vc.invMassB = bB.invMass;
+            vc.invIA = bA.invI; vc.invIB = bB.invI;
+            vc.contactIndex = i;
+            vc.pointCount = m.pointCount;
+            vc.K = Mat22{V(0, 0), V(0, 0)};
+            vc.normalMass = Mat22{V(0, 0), V(0, 0)};
+            PosConstraint& pc = pcs[i];
+            pc.indexA = bA.islandIndex; pc.indexB = bB.islandIndex;
+            pc.invMassA = bA.invMass; pc.invMassB = bB.invMass;
+            pc.localCenterA = bA.sweep.localCenter; pc.localCenterB = bB.sweep.localCenter;
+            pc.invIA = bA.invI; pc.invIB = bB.invI;
+            pc.localNormal = m.localNormal;
+            pc.localPoint = m.localPoint;
+            pc.pointCount = m.pointCount;
+            pc.radiusA = fa.shape.radius;
+            pc.radiusB = fb.shape.radius;
+            pc.type = m.type;
+            for (int j = 0; j < m.pointCount; ++j) {
+                VelPoint& p = vc.points[j];
+                if (step.warmStarting) {
+                    p.normalImpulse = step.dtRatio * m.points[j].normalImpulse;
+                    p.tangentImpulse = step.dtRatio * m.points[j].tangentImpulse;
+                } else {
+                    p.normalImpulse = 0.0f;
+                    p.tangentImpulse = 0.0f;
+                }
+                p.rA = V(0, 0); p.rB = V(0, 0);
+                p.normalMass = 0.0f; p.tangentMass = 0.0f; p.velocityBias = 0.0f;
+                pc.localPoints[j] = m.points[j].localPoint;
+            }
+        }
+    }
+
+    // b2ContactSolver::InitializeVelocityConstraints (b2ContactSolver.cpp:143-252)
+    void InitVelocity()
+    {
+        for (int i = 0; i < count; ++i) {
+            VelConstraint& vc = vcs[i];
+            PosConstraint& pc = pcs[i];
+            float radiusA = pc.radiusA, radiusB = pc.radiusB;
+            const Manifold& m = w->contacts[contactIds[vc.contactIndex]].m;
+            int indexA = vc.indexA, indexB = vc.indexB;
+            float mA = vc.invMassA, mB = vc.invMassB, iA = vc.invIA, iB = vc.invIB;
+            Vec2 cA = positions[indexA].c; float aA = positions[indexA].a;
+            Vec2 vA = velocities[indexA].v; float wA = velocities[indexA].w;
+            Vec2 cB = positions[indexB].c; float aB = positions[indexB].a;
+            Vec2 vB = velocities[indexB].v; float wB = velocities[indexB].w;
+            Xf xfA, xfB;
+            xfA.q = RotOf(aA);
+            xfB.q = RotOf(aB);
+            xfA.p = cA - Mul(xfA.q, pc.localCenterA);
+            xfB.p = cB - Mul(xfB.q, pc.localCenterB);
+            WorldManifold wm;
+            WorldManifoldInit(&wm, &m, xfA, radiusA, xfB, radiusB);
+            vc.normal = wm.normal;
+            for (int j = 0; j < vc.pointCount; ++j) {
+                VelPoint& p = vc.points[j];
+                p.rA = wm.points[j] - cA;
+                p.rB = wm.points[j] - cB;
+                float rnA = Cross(p.rA, vc.normal), rnB = Cross(p.rB, vc.normal);
+                float kNormal = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
+                p.normalMass = kNormal > 0.0f ? 1.0f / kNormal : 0.0f;
+                Vec2 tangent = Cross(vc.normal, 1.0f);
+                float rtA = Cross(p.rA, tangent), rtB = Cross(p.rB, tangent);
+                float kTangent = mA + mB + iA * rtA * rtA + iB * rtB * rtB;
+                p.tangentMass = kTangent > 0.0f ? 1.0f / kTangent : 0.0f;
+                p.velocityBias = 0.0f;
+                float vRel = Dot(vc.normal, vB + Cross(wB, p.rB) - vA - Cross(wA, p.rA));
+                if (vRel < -kVelocityThreshold) p.velocityBias = -vc.restitution * vRel;
+            }
+            if (vc.pointCount == 2) {
+                VelPoint& p1 = vc.points[0];
+                VelPoint& p2 = vc.points[1];
+                float rn1A = Cross(p1.rA, vc.normal), rn1B = Cross(p1.rB, vc.normal);
+                float rn2A = Cross(p2.rA, vc.normal), rn2B = Cross(p2.rB, vc.normal);
+                float k11 = mA + mB + iA * rn1A * rn1A + iB * rn1B * rn1B;
+                float k22 = mA + mB + iA * rn2A * rn2A + iB * rn2B * rn2B;
+                float k12 = mA + mB + iA * rn1A * rn2A + iB * rn1B * rn2B;
+                const float k_maxConditionNumber = 1000.0f;
+                if (k11 * k11 < k_maxConditionNumber * (k11 * k22 - k12 * k12)) {
+                    vc.K.ex = V(k11, k12);
+                    vc.K.ey = V(k12, k22);
+                    vc.normalMass = Inverse(vc.K);
+                } else {
+                    vc.pointCount = 1;
+                }
+            }
+        }
+    }
+
+    // b2ContactSolver::WarmStart (b2ContactSolver.cpp:254-292)
+    void WarmStart()
+    {
+        for (int i = 0; i < count; ++i) {
+            VelConstraint& vc = vcs[i];
+            int indexA = vc.indexA, indexB = vc.indexB;
+            float mA = vc.invMassA, iA = vc.invIA, mB = vc.invMassB, iB = vc.invIB;
+            Vec2 vA = velocities[indexA].v; float wA = velocities[indexA].w;
+            Vec2 vB = velocities[indexB].v; float wB = velocities[indexB].w;
+            Vec2 normal = vc.normal, tangent = Cross(normal, 1.0f);
+            for (int j = 0; j < vc.pointCount; ++j) {
+                VelPoint& p = vc.points[j];
+                Vec2 P = p.normalImpulse * normal + p.tangentImpulse * tangent;
+                wA -= iA * Cross(p.rA, P);
+                vA = vA - mA * P;
+                wB += iB * Cross(p.rB, P);
+                vB = vB + mB * P;
+            }
+            velocities[indexA].v = vA; velocities[indexA].w = wA;
+            velocities[indexB].v = vB; velocities[indexB].w = wB;
+        }
+    }
+
+    // b2ContactSolver::SolveVelocityConstraints (b2ContactSolver.cpp:294-605)
+    void SolveVelocity()
+    {
+        for (int i = 0; i < count; ++i) {
+            VelConstraint& vc = vcs[i];
+            int indexA = vc.indexA, indexB = vc.indexB;
+            float mA = vc.invMassA, iA = vc.invIA, mB = vc.invMassB, iB = vc.invIB;
+            int pointCount = vc.pointCount;
+            Vec2 vA = velocities[indexA].v; float wA = velocities[indexA].w;
+            Vec2 vB = velocities[indexB].v; float wB = velocities[indexB].w;
+            Vec2 normal = vc.normal, tangent = Cross(normal, 1.0f);
+            float friction = vc.friction;
+            for (int j = 0; j < pointCount; ++j) {
+                VelPoint& p = vc.points[j];
+                Vec2 dv = vB + Cross(wB, p.rB) - vA - Cross(wA, p.rA);
+                float vt = Dot(dv, tangent) - vc.tangentSpeed;
+                float lambda = p.tangentMass * (-vt);
+                float maxFriction = friction * p.normalImpulse;
+                float newImpulse = Clamp(p.tangentImpulse + lambda, -maxFriction, maxFriction);
+                lambda = newImpulse - p.tangentImpulse;
+                p.tangentImpulse = newImpulse;
+                Vec2 P = lambda * tangent;
+                vA = vA - mA * P;
+                wA -= iA * Cross(p.rA, P);
+                vB = vB + mB * P;
+                wB += iB * Cross(p.rB, P);
+            }
+            if (pointCount == 1) {
+                VelPoint& p = vc.points[0];
+                Vec2 dv = vB + Cross(wB, p.rB) - vA - Cross(wA, p.rA);
+                float vn = Dot(dv, normal);
+                float lambda = -p.normalMass * (vn - p.velocityBias);
+                float newImpulse = Max(p.normalImpulse + lambda, 0.0f);
+                lambda = newImpulse - p.normalImpulse;
+                p.normalImpulse = newImpulse;
+                Vec2 P = lambda * normal;
+                vA = vA - mA * P;
+                wA -= iA * Cross(p.rA, P);
+                vB = vB + mB * P;
+                wB += iB * Cross(p.rB, P);
+            } else {
+                VelPoint& cp1 = vc.points[0];
+                VelPoint& cp2 = vc.points[1];
+                Vec2 a = V(cp1.normalImpulse, cp2.normalImpulse);
+                Vec2 dv1 = vB + Cross(wB, cp1.rB) - vA - Cross(wA, cp1.rA);
+                Vec2 dv2 = vB + Cross(wB, cp2.rB) - vA - Cross(wA, cp2.rA);
+                float vn1 = Dot(dv1, normal), vn2 = Dot(dv2, normal);
+                Vec2 b;
+                b.x = vn1 - cp1.velocityBias;
+                b.y = vn2 - cp2.velocityBias;
+                b = b - MulM(vc.K, a);
+                Vec2 x;
+                bool solved = false;
+                // Total enumeration of the 2-point LCP (b2ContactSolver.cpp:420-600)
+                x = -MulM(vc.normalMass, b);
+                if (x.x >= 0.0f && x.y >= 0.0f) solved = true;
+                if (!solved) {
+                    x.x = -cp1.normalMass * b.x;
+                    x.y = 0.0f;
+                    vn2 = vc.K.ex.y * x.x + b.y;
+                    if (x.x >= 0.0f && vn2 >= 0.0f) solved = true;
+                }
+                if (!solved) {
+                    x.x = 0.0f;
+                    x.y = -cp2.normalMass * b.y;
+                    vn1 = vc.K.ey.x * x.y + b.x;
+                    if (x.y >= 0.0f && vn1 >= 0.0f) solved = true;
+                }
+                if (!solved) {
+                    x.x = 0.0f;
+                    x.y = 0.0f;
+                    vn1 = b.x;
+                    vn2 = b.y;
+                    if (vn1 >= 0.0f && vn2 >= 0.0f) solved = true;
+                }
+                if (solved) {
+                    Vec2 d = x - a;
+                    Vec2 P1 = d.x * normal, P2 = d.y * normal;
+                    vA = vA - mA * (P1 + P2);
+                    wA -= iA * (Cross(cp1.rA, P1) + Cross(cp2.rA, P2));
+                    vB = vB + mB * (P1 + P2);
+                    wB += iB * (Cross(cp1.rB, P1) + Cross(cp2.rB, P2));
+                    cp1.normalImpulse = x.x;
+                    cp2.normalImpulse = x.y;
+                }
+            }
+            velocities[indexA].v = vA; velocities[indexA].w = wA;
+            velocities[indexB].v = vB; velocities[indexB].w = wB;
+        }
+    }
+
+    // b2ContactSolver::StoreImpulses (b2ContactSolver.cpp:607-620)
+    void StoreImpulses()
+    {
+        for (int i = 0; i < count; ++i) {
+            const VelConstraint& vc = vcs[i];
+            Manifold& m = w->contacts[contactIds[vc.contactIndex]].m;
+            for (int j = 0; j < vc.pointCount; ++j) {
+                m.points[j].normalImpulse = vc.points[j].normalImpulse;
+                m.points[j].tangentImpulse = vc.points[j].tangentImpulse;
+            }
+        }
+    }
+
+    // b2PositionSolverManifold::Initialize (b2ContactSolver.cpp:623-672)
+    static void PSM(const PosConstraint& pc, const Xf& xfA, const Xf& xfB, int index, Vec2* normal, Vec2* point, float* separation)
+    {
+        switch (pc.type) {
+        case kCircles: {
+            Vec2 pointA = Mul(xfA, pc.localPoint);
+            Vec2 pointB = Mul(xfB, pc.localPoints[0]);
+            *normal = pointB - pointA;
+            Normalize(*normal);
+            *point = 0.5f * (pointA + pointB);
+            *separation = Dot(pointB - pointA, *normal) - pc.radiusA - pc.radiusB;
+            break;
+        }
+        case kFaceA: {
+            *normal = Mul(xfA.q, pc.localNormal);
+            Vec2 planePoint = Mul(xfA, pc.localPoint);
+            Vec2 clipPoint = Mul(xfB, pc.localPoints[index]);
+            *separation = Dot(clipPoint - planePoint, *normal) - pc.radiusA - pc.radiusB;
+            *point = clipPoint;
+            break;
+        }
+        default: {
+            *normal = Mul(xfB.q, pc.localNormal);
+            Vec2 planePoint = Mul(xfB, pc.localPoint);
+            Vec2 clipPoint = Mul(xfA, pc.localPoints[index]);
+            *separation = Dot(clipPoint - planePoint, *normal) - pc.radiusA - pc.radiusB;
+            *point = clipPoint;
+            *normal = -*normal;
+            break;
+        }
+        }
+    }
+
+    // b2ContactSolver::SolvePositionConstraints (b2ContactSolver.cpp:674-751) and
+    // SolveTOIPositionConstraints (:753-836): toi == true uses the TOI Baumgarte, the TOI body masks
+    // and the -1.5 slop acceptance.
+    bool SolvePosition(bool toi, int toiA, int toiB)
+    {
+        float minSeparation = 0.0f;
+        for (int i = 0; i < count; ++i) {
+            const PosConstraint& pc = pcs[i];
+            int indexA = pc.indexA, indexB = pc.indexB;
+            Vec2 localCenterA = pc.localCenterA, localCenterB = pc.localCenterB;
+            float mA, iA, mB, iB;
+            if (!toi) { mA = pc.invMassA; iA = pc.invIA; mB = pc.invMassB; iB = pc.invIB; }
+            else {
+                mA = 0.0f; iA = 0.0f; mB = 0.0f; iB = 0.0f;
+                if (indexA == toiA || indexA == toiB) { mA = pc.invMassA; iA = pc.invIA; }
+                if (indexB == toiA || indexB == toiB) { mB = pc.invMassB; iB = pc.invIB; }
+            }
+            int pointCount = pc.pointCount;
+            Vec2 cA = positions[indexA].c; float aA = positions[indexA].a;
+            Vec2 cB = positions[indexB].c; float aB = positions[indexB].a;
+            for (int j = 0; j < pointCount; ++j) {
+                Xf xfA, xfB;
+                xfA.q = RotOf(aA);
+                xfB.q = RotOf(aB);
+                xfA.p = cA - Mul(xfA.q, localCenterA);
+                xfB.p = cB - Mul(xfB.q, localCenterB);
+                Vec2 normal, point;
+                float separation;
+                PSM(pc, xfA, xfB, j, &normal, &point, &separation);
+                Vec2 rA = point - cA, rB = point - cB;
+                minSeparation = Min(minSeparation, separation);
+                float C = toi ? Clamp(kToiBaumgarte * (separation + kLinearSlop), -kMaxLinearCorrection, 0.0f)
+                              : Clamp(kBaumgarte * (separation + kLinearSlop), -kMaxLinearCorrection, 0.0f);
+                float rnA = Cross(rA, normal), rnB = Cross(rB, normal);
+                float K = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
+                float impulse = K > 0.0f ? -C / K : 0.0f;
+                Vec2 P = impulse * normal;
+                cA = cA - mA * P;
+                aA -= iA * Cross(rA, P);
+                cB = cB + mB * P;
+                aB += iB * Cross(rB, P);
+            }
+            positions[indexA].c = cA; positions[indexA].a = aA;
+            positions[indexB].c = cB; positions[indexB].a = aB;
+        }
+        return toi ? minSeparation >= -1.5f * kLinearSlop : minSeparation >= -3.0f * kLinearSlop;
+    }
+
+    std::vector<float> ReportImpulses(int i) const
+    {
+        std::vector<float> r(4, 0.0f);
+        for (int j = 0; j < vcs[i].pointCount; ++j) { r[j] = vcs[i].points[j].normalImpulse; r[2 + j] = vcs[i].points[j].tangentImpulse; }
+        return r;
+    }
+};
+
+// ---------------------------------------------------------------- revolute joint
+inline Vec2 MulM33x(const float* m, Vec2 v)
+{
+    return V(m[0] * v.x + m[3] * v.y, m[1] * v.x + m[4] * v.y);
+}
+
+// b2RevoluteJoint::InitVelocityConstraints (Dynamics/Joints/b2RevoluteJoint.cpp:66-183)
+void RevInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel)
+{
+    const Body& A = w->bodies[j.bodyA];
+    const Body& B = w->bodies[j.bodyB];
+    j.indexA = A.islandIndex; j.indexB = B.islandIndex;
+    j.localCenterA = A.sweep.localCenter; j.localCenterB = B.sweep.localCenter;
+    j.invMassA = A.invMass; j.invMassB = B.invMass;
+    j.invIA = A.invI; j.invIB = B.invI;
+    float aA = pos[j.indexA].a;
+    Vec2 vA = vel[j.indexA].v; float wA = vel[j.indexA].w;
+    float aB = pos[j.indexB].a;
+    Vec2 vB = vel[j.indexB].v; float wB = vel[j.indexB].w;
+    Rot qA = RotOf(aA), qB = RotOf(aB);
+    j.rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    j.rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    bool fixedRotation = (iA + iB == 0.0f);
+    float* M = j.mass;
+    M[0] = mA + mB + j.rA.y * j.rA.y * iA + j.rB.y * j.rB.y * iB;
+    M[3] = -j.rA.y * j.rA.x * iA - j.rB.y * j.rB.x * iB;
+    M[6] = -j.rA.y * iA - j.rB.y * iB;
+    M[1] = M[3];
+    M[4] = mA + mB + j.rA.x * j.rA.x * iA + j.rB.x * j.rB.x * iB;
+    M[7] = j.rA.x * iA + j.rB.x * iB;
+    M[2] = M[6];
+    M[5] = M[7];
+    M[8] = iA + iB;
+    j.motorMass = iA + iB;
+    if (j.motorMass > 0.0f) j.motorMass = 1.0f / j.motorMass;
+    if (!j.enableMotor || fixedRotation) j.motorImpulse = 0.0f;
+    if (j.enableLimit && !fixedRotation) {
+        float jointAngle = aB - aA - j.referenceAngle;
+        if (Abs(j.upperAngle - j.lowerAngle) < 2.0f * kAngularSlop) j.limitState = 3;
+        else if (jointAngle <= j.lowerAngle) {
+            if (j.limitState != 1) j.impulse[2] = 0.0f;
+            j.limitState = 1;
+        } else if (jointAngle >= j.upperAngle) {
+            if (j.limitState != 2) j.impulse[2] = 0.0f;
+            j.limitState = 2;
+        } else {
+            j.limitState = 0;
+            j.impulse[2] = 0.0f;
+        }
+    } else {
+        j.limitState = 0;
+    }
+    if (step.warmStarting) {
+        j.impulse[0] *= step.dtRatio; j.impulse[1] *= step.dtRatio; j.impulse[2] *= step.dtRatio;
+        j.motorImpulse *= step.dtRatio;
+        Vec2 P = V(j.impulse[0], j.impulse[1]);
+        vA = vA - mA * P;
+        wA -= iA * (Cross(j.rA, P) + j.motorImpulse + j.impulse[2]);
+        vB = vB + mB * P;
+        wB += iB * (Cross(j.rB, P) + j.motorImpulse + j.impulse[2]);
+    } else {
+        j.impulse[0] = j.impulse[1] = j.impulse[2] = 0.0f;
+        j.motorImpulse = 0.0f;
+    }
+    vel[j.indexA].v = vA; vel[j.indexA].w = wA;
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+}
+
+// b2Mat33::Solve33 / Solve22 (Common/b2Math.cpp:24-56)
+inline void Solve33(const float* M, const float* b, float* x)
+{
+    // columns ex = M[0..2], ey = M[3..5], ez = M[6..8]
+    auto cross3 = [](const float* a, const float* c, float* o) {
+        o[0] = a[1] * c[2] - a[2] * c[1];
+        o[1] = a[2] * c[0] - a[0] * c[2];
+        o[2] = a[0] * c[1] - a[1] * c[0];
+    };
+    auto dot3 = [](const float* a, const float* c) { return a[0] * c[0] + a[1] * c[1] + a[2] * c[2]; };
+    float t[3];
+    cross3(M + 3, M + 6, t);
+    float det = dot3(M, t);
+    if (det != 0.0f) det = 1.0f / det;
+    x[0] = det * dot3(b, t);
+    cross3(b, M + 6, t);
+    x[1] = det * dot3(M, t);
+    cross3(M + 3, b, t);
+    x[2] = det * dot3(M, t);
+}
+inline Vec2 Solve22(const float* M, Vec2 b)
+{
+    float a11 = M[0], a12 = M[3], a21 = M[1], a22 = M[4];
+    float det = a11 * a22 - a12 * a21;
+    if (det != 0.0f) det = 1.0f / det;
+    return V(det * (a22 * b.x - a12 * b.y), det * (a11 * b.y - a21 * b.x));
+}
+
+// b2RevoluteJoint::SolveVelocityConstraints (b2RevoluteJoint.cpp:185-291)
+void RevSolveVelocity(Joint& j, const StepInfo& step, Velocity* vel)
+{
+    Vec2 vA = vel[j.indexA].v; float wA = vel[j.indexA].w;
+    Vec2 vB = vel[j.indexB].v; float wB = vel[j.indexB].w;
+    float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    bool fixedRotation = (iA + iB == 0.0f);
+    if (j.enableMotor && j.limitState != 3 && !fixedRotation) {
+        float Cdot = wB - wA - j.motorSpeed;
+        float impulse = -j.motorMass * Cdot;
+        float oldImpulse = j.motorImpulse;
+        float maxImpulse = step.dt * j.maxMotorTorque;
+        j.motorImpulse = Clamp(j.motorImpulse + impulse, -maxImpulse, maxImpulse);
+        impulse = j.motorImpulse - oldImpulse;
+        wA -= iA * impulse;
+        wB += iB * impulse;
+    }
+    if (j.enableLimit && j.limitState != 0 && !fixedRotation) {
+        Vec2 Cdot1 = vB + Cross(wB, j.rB) - vA - Cross(wA, j.rA);
+        float Cdot2 = wB - wA;
+        float Cdot[3] = {Cdot1.x, Cdot1.y, Cdot2};
+        float imp[3];
+        Solve33(j.mass, Cdot, imp);
+        imp[0] = -imp[0]; imp[1] = -imp[1]; imp[2] = -imp[2];
+        if (j.limitState == 3) {
+            j.impulse[0] += imp[0]; j.impulse[1] += imp[1]; j.impulse[2] += imp[2];
+        } else if (j.limitState == 1 || j.limitState == 2) {
+            float newImpulse = j.impulse[2] + imp[2];
+            bool clampIt = j.limitState == 1 ? newImpulse < 0.0f : newImpulse > 0.0f;
+            if (clampIt) {
+                Vec2 rhs = -Cdot1 + j.impulse[2] * V(j.mass[6], j.mass[7]);
+                Vec2 reduced = Solve22(j.mass, rhs);
+                imp[0] = reduced.x;
+                imp[1] = reduced.y;
+                imp[2] = -j.impulse[2];
+                j.impulse[0] += reduced.x;
+                j.impulse[1] += reduced.y;
+                j.impulse[2] = 0.0f;
+            } else {
+                j.impulse[0] += imp[0]; j.impulse[1] += imp[1]; j.impulse[2] += imp[2];
+            }
+        }
+        Vec2 P = V(imp[0], imp[1]);
+        vA = vA - mA * P;
+        wA -= iA * (Cross(j.rA, P) + imp[2]);
+        vB = vB + mB * P;
+        wB += iB * (Cross(j.rB, P) + imp[2]);
+    } else {
+        Vec2 Cdot = vB + Cross(wB, j.rB) - vA - Cross(wA, j.rA);
+        Vec2 impulse = Solve22(j.mass, -Cdot);
+        j.impulse[0] += impulse.x;
+        j.impulse[1] += impulse.y;
+        vA = vA - mA * impulse;
+        wA -= iA * Cross(j.rA, impulse);
+        vB = vB + mB * impulse;
+        wB += iB * Cross(j.rB, impulse);
+    }
+    vel[j.indexA].v = vA; vel[j.indexA].w = wA;
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+}
+
+// b2RevoluteJoint::SolvePositionConstraints (b2RevoluteJoint.cpp:293-380)
+bool RevSolvePosition(Joint& j, Position* pos)
+{
+    Vec2 cA = pos[j.indexA].c; float aA = pos[j.indexA].a;
+    Vec2 cB = pos[j.indexB].c; float aB = pos[j.indexB].a;
+    float angularError = 0.0f, positionError = 0.0f;
+    bool fixedRotation = (j.invIA + j.invIB == 0.0f);
+    if (j.enableLimit && j.limitState != 0 && !fixedRotation) {
+        float angle = aB - aA - j.referenceAngle;
+        float limitImpulse = 0.0f;
+        if (j.limitState == 3) {
+            float C = Clamp(angle - j.lowerAngle, -kMaxAngularCorrection, kMaxAngularCorrection);
+            limitImpulse = -j.motorMass * C;
+            angularError = Abs(C);
+        } else if (j.limitState == 1) {
+            float C = angle - j.lowerAngle;
+            angularError = -C;
+            C = Clamp(C + kAngularSlop, -kMaxAngularCorrection, 0.0f);
+            limitImpulse = -j.motorMass * C;
+        } else if (j.limitState == 2) {
+            float C = angle - j.upperAngle;
+            angularError = C;
+            C = Clamp(C - kAngularSlop, 0.0f, kMaxAngularCorrection);
+            limitImpulse = -j.motorMass * C;
+        }
+        aA -= j.invIA * limitImpulse;
+        aB += j.invIB * limitImpulse;
+    }
+    {
+        Rot qA = RotOf(aA), qB = RotOf(aB);
+        Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
+        Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
+        Vec2 C = cB + rB - cA - rA;
+        positionError = Length(C);
+        float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+        float K[9] = {0};
+        K[0] = mA + mB + iA * rA.y * rA.y + iB * rB.y * rB.y;
+        K[1] = -iA * rA.x * rA.y - iB * rB.x * rB.y;
+        K[3] = K[1];
+        K[4] = mA + mB + iA * rA.x * rA.x + iB * rB.x * rB.x;
+        Vec2 impulse = -Solve22(K, C);
+        cA = cA - mA * impulse;
+        aA -= iA * Cross(rA, impulse);
+        cB = cB + mB * impulse;
+        aB += iB * Cross(rB, impulse);
+    }
+    pos[j.indexA].c = cA; pos[j.indexA].a = aA;
+    pos[j.indexB].c = cB; pos[j.indexB].a = aB;
+    return positionError <= kLinearSlop && angularError <= kAngularSlop;
+}
+} // namespace
+
+// ---------------------------------------------------------------- island solve
+// b2Island::Solve (Dynamics/b2Island.cpp:185-384)
+void World::IslandSolve(const StepInfo& step)
+{
+    int nb = (int)iBodies.size();
+    positions.resize(nb);
+    velocities.resize(nb);
+    float h = step.dt;
+    for (int i = 0; i < nb; ++i) {
+        Body& b = bodies[iBodies[i]];
+        Vec2 c = b.sweep.c;
+        float a = b.sweep.a;
+        Vec2 v = b.v;
+        float w = b.w;
+        b.sweep.c0 = b.sweep.c;
+        b.sweep.a0 = b.sweep.a;
+        if (b.type == kDynamic) {
+            v = v + h * (b.gravityScale * gravity + b.invMass * b.force);
+            w += h * b.invI * b.torque;
+            v = (1.0f / (1.0f + h * b.linearDamping)) * v;
+            w *= 1.0f / (1.0f + h * b.angularDamping);
+        }
+        positions[i].c = c; positions[i].a = a;
+        velocities[i].v = v; velocities[i].w = w;
+    }
+    ContactSolver cs(this, step, iContacts.data(), (int)iContacts.size(), positions.data(), velocities.data());
+    cs.InitVelocity();
+    if (step.warmStarting) cs.WarmStart();
+    for (int jn : iJoints) RevInit(this, joints[jn], step, positions.data(), velocities.data());
+    for (int i = 0; i < step.velocityIterations; ++i) {
+        for (int jn : iJoints) RevSolveVelocity(joints[jn], step, velocities.data());
+        cs.SolveVelocity();
+    }
+    cs.StoreImpulses();
+    for (int i = 0; i < nb; ++i) {
+        Vec2 c = positions[i].c;
+        float a = positions[i].a;
+        Vec2 v = velocities[i].v;
+        float w = velocities[i].w;
+        Vec2 translation = h * v;
+        if (Dot(translation, translation) > kMaxTranslationSquared) {
+            float ratio = kMaxTranslation / Length(translation);
+            v.x *= ratio;
+            v.y *= ratio;
+        }
+        float rotation = h * w;
+        if (rotation * rotation > kMaxRotationSquared) {
+            float ratio = kMaxRotation / Abs(rotation);
+            w *= ratio;
+        }
+        c = c + h * v;
+        a += h * w;
+        positions[i].c = c; positions[i].a = a;
+        velocities[i].v = v; velocities[i].w = w;
+    }
+    bool positionSolved = false;
+    for (int i = 0; i < step.positionIterations; ++i) {
+        bool contactsOkay = cs.SolvePosition(false, -1, -1);
+        bool jointsOkay = true;
+        for (int jn : iJoints) {
+            bool ok = RevSolvePosition(joints[jn], positions.data());
+            jointsOkay = jointsOkay && ok;
+        }
+        if (contactsOkay && jointsOkay) { positionSolved = true; break; }
+    }
+    for (int i = 0; i < nb; ++i) {
+        int bi = iBodies[i];
+        Body& b = bodies[bi];
+        b.sweep.c = positions[i].c;
+        b.sweep.a = positions[i].a;
+        b.v = velocities[i].v;
+        b.w = velocities[i].w;
+        SynchronizeTransform(bi);
+    }
+    if (recordEvents) {
+        for (int i = 0; i < (int)iContacts.size(); ++i) {
+            std::vector<float> r = cs.ReportImpulses(i);
+            const Contact& c = contacts[iContacts[i]];
+            events.push_back(Event{3, c.fA, c.fB, r[0], r[1], r[2], r[3]});
+        }
+    }
+    if (allowSleep) {
+        float minSleepTime = kMaxFloat;
+        const float linTolSqr = kLinearSleepTolerance * kLinearSleepTolerance;
+        const float angTolSqr = kAngularSleepTolerance * kAngularSleepTolerance;
+        for (int i = 0; i < nb; ++i) {
+            Body& b = bodies[iBodies[i]];
+            if (b.type == kStatic) continue;
+            if ((b.flags & kBAutoSleep) == 0 || b.w * b.w > angTolSqr || Dot(b.v, b.v) > linTolSqr) {
+                b.sleepTime = 0.0f;
+                minSleepTime = 0.0f;
+            } else {
+                b.sleepTime += h;
+                minSleepTime = Min(minSleepTime, b.sleepTime);
+            }
+        }
+        if (minSleepTime >= kTimeToSleep && positionSolved) {
+            for (int i = 0; i < nb; ++i) SetAwake(iBodies[i], false);
+        }
+    }
+}
+
+// b2Island::SolveTOI (Dynamics/b2Island.cpp:386-485)
+void World::IslandSolveTOI(const StepInfo& sub, int toiA, int toiB)
+{
+    int nb = (int)iBodies.size();
+    positions.resize(nb);
+    velocities.resize(nb);
+    for (int i = 0; i < nb; ++i) {
+        const Body& b = bodies[iBodies[i]];
+        positions[i].c = b.sweep.c; positions[i].a = b.sweep.a;
+        velocities[i].v = b.v; velocities[i].w = b.w;
+    }
+    ContactSolver cs(this, sub, iContacts.data(), (int)iContacts.size(), positions.data(), velocities.data());
+    for (int i = 0; i < sub.positionIterations; ++i) {
+        if (cs.SolvePosition(true, toiA, toiB)) break;
+    }
+    bodies[iBodies[toiA]].sweep.c0 = positions[toiA].c;
+    bodies[iBodies[toiA]].sweep.a0 = positions[toiA].a;
+    bodies[iBodies[toiB]].sweep.c0 = positions[toiB].c;
+    bodies[iBodies[toiB]].sweep.a0 = positions[toiB].a;
+    cs.InitVelocity();
+    for (int i = 0; i < sub.velocityIterations; ++i) cs.SolveVelocity();
+    float h = sub.dt;
+    for (int i = 0; i < nb; ++i) {
+        Vec2 c = positions[i].c;
+        float a = positions[i].a;
+        Vec2 v = velocities[i].v;
+        float w = velocities[i].w;
+        Vec2 translation = h * v;
+        if (Dot(translation, translation) > kMaxTranslationSquared) {
+            float ratio = kMaxTranslation / Length(translation);
+            v.x *= ratio;
+            v.y *= ratio;
+        }
+        float rotation = h * w;
+        if (rotation * rotation > kMaxRotationSquared) {
+            float ratio = kMaxRotation / Abs(rotation);
+            w *= ratio;
+        }
+        c = c + h * v;
+        a += h * w;
+        positions[i].c = c; positions[i].a = a;
+        velocities[i].v = v; velocities[i].w = w;
+        int bi = iBodies[i];
+        Body& body = bodies[bi];
+        body.sweep.c = c;
+        body.sweep.a = a;
+        body.v = v;
+        body.w = w;
+        SynchronizeTransform(bi);
+    }
+    if (recordEvents) {
+        for (int i = 0; i < (int)iContacts.size(); ++i) {
+            std::vector<float> r = cs.ReportImpulses(i);
+            const Contact& c = contacts[iContacts[i]];
+            events.push_back(Event{3, c.fA, c.fB, r[0], r[1], r[2], r[3]});
+        }
+    }
+}
+
+// ---------------------------------------------------------------- world step
+// b2World::Solve (Dynamics/b2World.cpp:388-577)
+void World::Solve(const StepInfo& step)
+{
+    for (int b = bodyList; b != kNull; b = bodies[b].next) bodies[b].flags &= ~kBIsland;
+    for (int c = contactList; c != kNull; c = contacts[c].next) contacts[c].flags &= ~kCIsland;
+    for (int j = jointList; j != kNull; j = joints[j].next) joints[j].islandFlag = false;
+    stack.resize(bodyCount);
+    for (int seed = bodyList; seed != kNull; seed = bodies[seed].next) {
+        Body& sb = bodies[seed];
+        if (sb.flags & kBIsland) continue;
+        if (!sb.IsAwake() || (sb.flags & kBActive) == 0) continue;
+        if (sb.type == kStatic) continue;
+        iBodies.clear(); iContacts.clear(); iJoints.clear();
+        int stackCount = 0;
+        stack[stackCount++] = seed;
+        sb.flags |= kBIsland;
+        while (stackCount > 0) {
+            int bi = stack[--stackCount];
+            bodies[bi].islandIndex = (int)iBodies.size();
+            iBodies.push_back(bi);
+            SetAwake(bi, true);
+            if (bodies[bi].type == kStatic) continue;
+            for (int e = bodies[bi].contactList; e != kNull; e = contacts[e >> 1].eNext[e & 1]) {
+                int c = e >> 1;
+                Contact& ct = contacts[c];
+                if (ct.flags & kCIsland) continue;
+                if ((ct.flags & kCEnabled) == 0 || (ct.flags & kCTouching) == 0) continue;
+                if (fixtures[ct.fA].sensor || fixtures[ct.fB].sensor) continue;
+                iContacts.push_back(c);
+                ct.flags |= kCIsland;
+                int other = EdgeOther(e);
+                if (bodies[other].flags & kBIsland) continue;
+                stack[stackCount++] = other;
+                bodies[other].flags |= kBIsland;
+            }
+            for (int e = bodies[bi].jointList; e != kNull; e = joints[e >> 1].eNext[e & 1]) {
+                Joint& jt = joints[e >> 1];
+                if (jt.islandFlag) continue;
+                int other = JointEdgeOther(e);
+                if ((bodies[other].flags & kBActive) == 0) continue;
+                iJoints.push_back(e >> 1);
+                jt.islandFlag = true;
+                if (bodies[other].flags & kBIsland) continue;
+                stack[stackCount++] = other;
+                bodies[other].flags |= kBIsland;
+            }
+        }
+        IslandSolve(step);
+        for (int bi : iBodies)
+            if (bodies[bi].type == kStatic) bodies[bi].flags &= ~kBIsland;
+    }
+    for (int b = bodyList; b != kNull; b = bodies[b].next) {
+        if ((bodies[b].flags & kBIsland) == 0) continue;
+        if (bodies[b].type == kStatic) continue;
+        SynchronizeFixtures(b);
+    }
+    FindNewContacts();
+}
+
+// b2World::SolveTOI (Dynamics/b2World.cpp:579-896)
+void World::SolveTOI(const StepInfo& step)
+{
+    if (stepComplete) {
+        for (int b = bodyList; b != kNull; b = bodies[b].next) {
+            bodies[b].flags &= ~kBIsland;
+            bodies[b].sweep.alpha0 = 0.0f;
+        }
+        for (int c = contactList; c != kNull; c = contacts[c].next) {
+            contacts[c].flags &= ~(kCToi | kCIsland);
+            contacts[c].toiCount = 0;
+            contacts[c].toi = 1.0f;
+        }
+    }
+    for (;;) {
+        int minContact = kNull;
+        float minAlpha = 1.0f;
+        for (int c = contactList; c != kNull; c = contacts[c].next) {
+            Contact& ct = contacts[c];
+            if ((ct.flags & kCEnabled) == 0) continue;
+            if (ct.toiCount > kMaxSubSteps) continue;
+            float alpha = 1.0f;
+            if (ct.flags & kCToi) {
+                alpha = ct.toi;
+            } else {
+                const Fixture& fA = fixtures[ct.fA];
+                const Fixture& fB = fixtures[ct.fB];
+                if (fA.sensor || fB.sensor) continue;
+                Body& bA = bodies[fA.body];
+                Body& bB = bodies[fB.body];
+                bool activeA = bA.IsAwake() && bA.type != kStatic;
+                bool activeB = bB.IsAwake() && bB.type != kStatic;
+                if (!activeA && !activeB) continue;
+                bool collideA = (bA.flags & kBBullet) != 0 || bA.type != kDynamic;
+                bool collideB = (bB.flags & kBBullet) != 0 || bB.type != kDynamic;
+                if (!collideA && !collideB) continue;
+                float alpha0 = bA.sweep.alpha0;
+                if (bA.sweep.alpha0 < bB.sweep.alpha0) {
+                    alpha0 = bB.sweep.alpha0;
+                    SweepAdvance(bA.sweep, alpha0);
+                } else if (bB.sweep.alpha0 < bA.sweep.alpha0) {
+                    alpha0 = bA.sweep.alpha0;
+                    SweepAdvance(bB.sweep, alpha0);
+                }
+                DistanceProxy pa, pb;
+                ProxyOf(&pa, fA.shape);
+                ProxyOf(&pb, fB.shape);
+                int state;
+                float beta;
+                TimeOfImpact(&state, &beta, pa, pb, bA.sweep, bB.sweep, 1.0f);
+                if (state == kToiTouching) alpha = Min(alpha0 + (1.0f - alpha0) * beta, 1.0f);
+                else alpha = 1.0f;
+                ct.toi = alpha;
+                ct.flags |= kCToi;
+            }
+            if (alpha < minAlpha) { minContact = c; minAlpha = alpha; }
+        }
+        if (minContact == kNull || 1.0f - 10.0f * kEpsilon < minAlpha) {
+            stepComplete = true;
+            break;
+        }
+        int bA = fixtures[contacts[minContact].fA].body, bB = fixtures[contacts[minContact].fB].body;
+        Sweep backup1 = bodies[bA].sweep, backup2 = bodies[bB].sweep;
+        Advance(bA, minAlpha);
+        Advance(bB, minAlpha);
+        Update(minContact);
+        contacts[minContact].flags &= ~kCToi;
+        ++contacts[minContact].toiCount;
+        if ((contacts[minContact].flags & kCEnabled) == 0 || (contacts[minContact].flags & kCTouching) == 0) {
+            contacts[minContact].flags &= ~kCEnabled;
+            bodies[bA].sweep = backup1;
+            bodies[bB].sweep = backup2;
+            SynchronizeTransform(bA);
+            SynchronizeTransform(bB);
+            continue;
+        }
+        SetAwake(bA, true);
+        SetAwake(bB, true);
+        iBodies.clear(); iContacts.clear(); iJoints.clear();
+        const int bodyCap = 2 * kMaxTOIContacts, contactCap = kMaxTOIContacts;
+        bodies[bA].islandIndex = 0; iBodies.push_back(bA);
+        bodies[bB].islandIndex = 1; iBodies.push_back(bB);
+        iContacts.push_back(minContact);
+        bodies[bA].flags |= kBIsland;
+        bodies[bB].flags |= kBIsland;
+        contacts[minContact].flags |= kCIsland;
+        int pair[2] = {bA, bB};
+        for (int k = 0; k < 2; ++k) {
+            int body = pair[k];
+            if (bodies[body].type != kDynamic) continue;
+            for (int e = bodies[body].contactList; e != kNull; e = contacts[e >> 1].eNext[e & 1]) {
+                if ((int)iBodies.size() == bodyCap) break;
+                if ((int)iContacts.size() == contactCap) break;
+                int c = e >> 1;
+                Contact& ct = contacts[c];
+                if (ct.flags & kCIsland) continue;
+                int other = EdgeOther(e);
+                if (bodies[other].type == kDynamic && (bodies[body].flags & kBBullet) == 0 && (bodies[other].flags & kBBullet) == 0)
+                    continue;
+                if (fixtures[ct.fA].sensor || fixtures[ct.fB].sensor) continue;
+                Sweep backup = bodies[other].sweep;
+                if ((bodies[other].flags & kBIsland) == 0) Advance(other, minAlpha);
+                Update(c);
+                if ((contacts[c].flags & kCEnabled) == 0 || (contacts[c].flags & kCTouching) == 0) {
+                    bodies[other].sweep = backup;
+                    SynchronizeTransform(other);
+                    continue;
+                }
+                contacts[c].flags |= kCIsland;
+                iContacts.push_back(c);
+                if (bodies[other].flags & kBIsland) continue;
+                bodies[other].flags |= kBIsland;
+                if (bodies[other].type != kStatic) SetAwake(other, true);
+                bodies[other].islandIndex = (int)iBodies.size();
+                iBodies.push_back(other);
+            }
+        }
+        StepInfo sub;
+        sub.dt = (1.0f - minAlpha) * step.dt;
+        sub.inv_dt = 1.0f / sub.dt;
+        sub.dtRatio = 1.0f;
+        sub.positionIterations = 20;
+        sub.velocityIterations = step.velocityIterations;
+        sub.warmStarting = false;
+        IslandSolveTOI(sub, bodies[bA].islandIndex, bodies[bB].islandIndex);
+        for (int bi : iBodies) {
+            bodies[bi].flags &= ~kBIsland;
+            if (bodies[bi].type != kDynamic) continue;
+            SynchronizeFixtures(bi);
+            for (int e = bodies[bi].contactList; e != kNull; e = contacts[e >> 1].eNext[e & 1])
+                contacts[e >> 1].flags &= ~(kCToi | kCIsland);
+        }
+        FindNewContacts();
+        if (subStepping) { stepComplete = false; break; }
+    }
+}
+
+// b2World::Step (Dynamics/b2World.cpp:899-963)
+void World::Step(float dt, int vi, int pi)
+{
+    stepPairs.clear();
+    events.clear();
+    if (wflags & 0x1) {
+        FindNewContacts();
+        wflags &= ~0x1u;
+    }
+    wflags |= 0x2;
+    StepInfo step;
+    step.dt = dt;
+    step.velocityIterations = vi;
+    step.positionIterations = pi;
+    step.inv_dt = dt > 0.0f ? 1.0f / dt : 0.0f;
+    step.dtRatio = inv_dt0 * dt;
+    step.warmStarting = warmStarting;
+    Collide();
+    if (stepComplete && step.dt > 0.0f) Solve(step);
+    if (continuous && step.dt > 0.0f) SolveTOI(step);
+    if (step.dt > 0.0f) inv_dt0 = step.inv_dt;
+    if (wflags & 0x4) {
+        for (int b = bodyList; b != kNull; b = bodies[b].next) {
+            bodies[b].force = V(0.0f, 0.0f);
+            bodies[b].torque = 0.0f;
+        }
+    }
+    wflags &= ~0x2u;
+}
+
+} // namespace b2o

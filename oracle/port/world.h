@@ -1,0 +1,131 @@
+// Oracle (test infrastructure only): world, bodies, fixtures, contacts, joints, island and contact
+// solver declarations for the CPU restatement of Box2D 2.3.2 b2World::Step.
+#pragma once
+#include "tree.h"
+
+namespace b2o {
+
+enum BodyType { kStatic = 0, kKinematic = 1, kDynamic = 2 };
+// b2Body flags (Dynamics/b2Body.h:409-418)
+enum : uint32_t { kBIsland = 0x1, kBAwake = 0x2, kBAutoSleep = 0x4, kBBullet = 0x8, kBFixedRot = 0x10, kBActive = 0x20, kBToi = 0x40 };
+// b2Contact flags (Dynamics/Contacts/b2Contact.h:158-177)
+enum : uint32_t { kCIsland = 0x1, kCTouching = 0x2, kCEnabled = 0x4, kCFilter = 0x8, kCBulletHit = 0x10, kCToi = 0x20 };
+
+struct Body {
+    int type = kStatic;
+    uint32_t flags = 0;
+    int islandIndex = 0;
+    Xf xf{};
+    Sweep sweep{};
+    Vec2 v{0, 0};
+    float w = 0;
+    Vec2 force{0, 0};
+    float torque = 0;
+    float mass = 0, invMass = 0, I = 0, invI = 0;
+    float linearDamping = 0, angularDamping = 0, gravityScale = 1, sleepTime = 0;
+    int prev = kNull, next = kNull;
+    int fixtureList = kNull;
+    int contactList = kNull; // edge id: contact * 2 + side
+    int jointList = kNull;   // edge id: joint * 2 + side
+    bool IsAwake() const { return (flags & kBAwake) != 0; }
+};
+
+struct Fixture {
+    int body = kNull, next = kNull;
+    Shape shape;
+    float density = 0, friction = 0.2f, restitution = 0;
+    uint16_t category = 1, mask = 0xFFFF;
+    int16_t group = 0;
+    bool sensor = false;
+    int proxyId = kNull;
+    int proxyCount = 0;
+    AABB aabb{};
+};
+
+struct Contact {
+    uint32_t flags = 0;
+    int fA = kNull, fB = kNull, iA = 0, iB = 0;
+    Manifold m{};
+    int toiCount = 0;
+    float toi = 1.0f;
+    float friction = 0, restitution = 0, tangentSpeed = 0;
+    int prev = kNull, next = kNull;
+    int ePrev[2] = {kNull, kNull}, eNext[2] = {kNull, kNull};
+    bool alive = false;
+};
+
+struct Joint {
+    int bodyA = kNull, bodyB = kNull;
+    bool collideConnected = false, islandFlag = false;
+    int prev = kNull, next = kNull;
+    int ePrev[2] = {kNull, kNull}, eNext[2] = {kNull, kNull};
+    // revolute joint (Dynamics/Joints/b2RevoluteJoint.h)
+    Vec2 localAnchorA{0, 0}, localAnchorB{0, 0};
+    float referenceAngle = 0, lowerAngle = 0, upperAngle = 0, maxMotorTorque = 0, motorSpeed = 0;
+    bool enableLimit = false, enableMotor = false;
+    float impulse[3] = {0, 0, 0};
+    float motorImpulse = 0;
+    int limitState = 0; // 0 inactive, 1 lower, 2 upper, 3 equal
+    int indexA = 0, indexB = 0;
+    Vec2 rA{0, 0}, rB{0, 0}, localCenterA{0, 0}, localCenterB{0, 0};
+    float invMassA = 0, invMassB = 0, invIA = 0, invIB = 0;
+    float mass[9] = {0};     // b2Mat33 columns ex, ey, ez
+    float motorMass = 0;
+};
+
+struct Position { Vec2 c; float a; };
+struct Velocity { Vec2 v; float w; };
+struct StepInfo { float dt, inv_dt, dtRatio; int velocityIterations, positionIterations; bool warmStarting; };
+
+struct Event { int kind, fA, fB; float n0, n1, t0, t1; }; // kind: 0 begin, 1 end, 2 presolve, 3 postsolve
+
+struct World {
+    Vec2 gravity{0, -10};
+    std::vector<Body> bodies;
+    std::vector<Fixture> fixtures;
+    std::vector<Contact> contacts;
+    std::vector<int> freeContacts;
+    std::vector<Joint> joints;
+    int bodyList = kNull, contactList = kNull, jointList = kNull;
+    int bodyCount = 0, contactCount = 0, jointCount = 0;
+    uint32_t wflags = 0x4; // e_clearForces
+    bool allowSleep = true, warmStarting = true, continuous = true, subStepping = false, stepComplete = true;
+    float inv_dt0 = 0;
+    BroadPhase bp;
+    bool recordEvents = false;
+    std::vector<Event> events;
+    std::vector<Pair> stepPairs; // every UpdatePairs list of the last step, separated by {-1,-1}
+    // island scratch
+    std::vector<int> iBodies, iContacts, iJoints, stack;
+    std::vector<Position> positions;
+    std::vector<Velocity> velocities;
+
+    int CreateBody(int type, const float* f, int flags);
+    int CreateFixture(int body, const Shape& shape, float density, float friction, float restitution,
+                      int category, int mask, int group, bool sensor);
+    int CreateRevolute(int a, int b, const float* f, int flags);
+    void ResetMassData(int b);
+    void SetAwake(int b, bool flag);
+    bool ShouldCollide(int bodyB, int bodyA) const;
+    void SynchronizeFixtures(int b);
+    void SynchronizeTransform(int b);
+    void Advance(int b, float alpha);
+
+    void FindNewContacts();
+    void AddPair(int proxyA, int proxyB);
+    void Destroy(int c);
+    void Collide();
+    void Update(int c);
+    void Evaluate(int c, Manifold* m);
+    void Solve(const StepInfo& step);
+    void SolveTOI(const StepInfo& step);
+    void IslandSolve(const StepInfo& step);
+    void IslandSolveTOI(const StepInfo& sub, int toiA, int toiB);
+    void Step(float dt, int vi, int pi);
+
+    int EdgeOther(int e) const;
+    int JointEdgeOther(int e) const;
+    int Link(int c);
+};
+
+} // namespace b2o

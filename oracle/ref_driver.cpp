@@ -1,0 +1,368 @@
+// Oracle (test infrastructure only): a C-ABI driver around the UNMODIFIED reference Box2D 2.3.2
+// (namespace box2dref, Regression/box2d-ref/Box2DRef in the reference tree), compiled from the
+// reference sources in place by oracle/Makefile into oracle/_ref/. It builds scenes through the
+// reference's own public API (b2World::CreateBody, b2Body::CreateFixture, b2World::CreateJoint,
+// b2World::Step) and reads state back for golden-vector generation. Nothing here is product code.
+//
+// Private members are read (not written) for the dump: fat AABBs, proxy ids, contact flags.
+#include <algorithm>
+#include <cassert>
+#include <cfloat>
+#include <climits>
+#include <cmath>
+#include <cstddef>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <thread>
+#include <vector>
+#define private public
+#define protected public
+#include <Box2DRef/Box2D.h>
+#undef private
+#undef protected
+
+using namespace box2dref;
+
+namespace {
+
+struct RefWorld {
+    b2World world;
+    std::vector<b2Body*> bodies;      // creation order
+    std::vector<b2Fixture*> fixtures; // creation order
+    std::vector<b2Joint*> joints;
+    explicit RefWorld(const b2Vec2& g) : world(g) {}
+};
+
+int fixture_index(const b2Fixture* f) { return (int)(intptr_t)f->GetUserData() - 1; }
+int body_index(const b2Body* b) { return (int)(intptr_t)b->GetUserData() - 1; }
+
+} // namespace
+
+extern "C" {
+
+void* rw_create(float gx, float gy) { return new RefWorld(b2Vec2(gx, gy)); }
+void rw_destroy(void* h) { delete static_cast<RefWorld*>(h); }
+
+void rw_config(void* h, int allowSleep, int warmStarting, int continuous, int subStepping)
+{
+    RefWorld* w = static_cast<RefWorld*>(h);
+    w->world.SetAllowSleeping(allowSleep != 0);
+    w->world.SetWarmStarting(warmStarting != 0);
+    w->world.SetContinuousPhysics(continuous != 0);
+    w->world.SetSubStepping(subStepping != 0);
+}
+
+// f = {x, y, angle, vx, vy, w, linearDamping, angularDamping, gravityScale}
+// flags: 1 allowSleep, 2 awake, 4 fixedRotation, 8 bullet, 16 active
+int rw_body(void* h, int type, const float* f, int flags)
+{
+    RefWorld* w = static_cast<RefWorld*>(h);
+    b2BodyDef bd;
+    bd.type = (b2BodyType)type;
+    bd.position.Set(f[0], f[1]);
+    bd.angle = f[2];
+    bd.linearVelocity.Set(f[3], f[4]);
+    bd.angularVelocity = f[5];
+    bd.linearDamping = f[6];
+    bd.angularDamping = f[7];
+    bd.gravityScale = f[8];
+    bd.allowSleep = (flags & 1) != 0;
+    bd.awake = (flags & 2) != 0;
+    bd.fixedRotation = (flags & 4) != 0;
+    bd.bullet = (flags & 8) != 0;
+    bd.active = (flags & 16) != 0;
+    bd.userData = (void*)(intptr_t)(w->bodies.size() + 1);
+    b2Body* b = w->world.CreateBody(&bd);
+    w->bodies.push_back(b);
+    return (int)w->bodies.size() - 1;
+}
+
+// shapeType 0 circle: s = {px, py, radius}
+// shapeType 1 edge:   s = {v1x, v1y, v2x, v2y, v0x, v0y, v3x, v3y, hasV0, hasV3}
+// shapeType 2 polygon from points: s = n points (b2PolygonShape::Set)
+// shapeType 3 box:    s = {hx, hy} (SetAsBox(hx, hy)) or {hx, hy, cx, cy, angle} when n == 5
+// mat = {density, friction, restitution}; filt = {categoryBits, maskBits, groupIndex, isSensor}
+int rw_fixture(void* h, int body, int shapeType, const float* s, int n, const float* mat, const int* filt)
+{
+    RefWorld* w = static_cast<RefWorld*>(h);
+    b2FixtureDef fd;
+    b2CircleShape circle;
+    b2EdgeShape edge;
+    b2PolygonShape poly;
+    switch (shapeType) {
+    case 0:
+        circle.m_p.Set(s[0], s[1]);
+        circle.m_radius = s[2];
+        fd.shape = &circle;
+        break;
+    case 1:
+        edge.Set(b2Vec2(s[0], s[1]), b2Vec2(s[2], s[3]));
+        edge.m_vertex0.Set(s[4], s[5]);
+        edge.m_vertex3.Set(s[6], s[7]);
+        edge.m_hasVertex0 = s[8] != 0.0f;
+        edge.m_hasVertex3 = s[9] != 0.0f;
+        fd.shape = &edge;
+        break;
+    case 2: {
+        b2Vec2 pts[b2_maxPolygonVertices];
+        for (int i = 0; i < n && i < b2_maxPolygonVertices; ++i) pts[i].Set(s[2 * i], s[2 * i + 1]);
+        poly.Set(pts, n);
+        fd.shape = &poly;
+        break;
+    }
+    case 3:
+        if (n == 5) poly.SetAsBox(s[0], s[1], b2Vec2(s[2], s[3]), s[4]);
+        else poly.SetAsBox(s[0], s[1]);
+        fd.shape = &poly;
+        break;
+    default:
+        return -1;
+    }
+    fd.density = mat[0];
+    fd.friction = mat[1];
+    fd.restitution = mat[2];
+    fd.filter.categoryBits = (uint16)filt[0];
+    fd.filter.maskBits = (uint16)filt[1];
+    fd.filter.groupIndex = (int16)filt[2];
+    fd.isSensor = filt[3] != 0;
+    fd.userData = (void*)(intptr_t)(w->fixtures.size() + 1);
+    b2Fixture* fx = w->bodies[body]->CreateFixture(&fd);
+    w->fixtures.push_back(fx);
+    return (int)w->fixtures.size() - 1;
+}
+
+// f = {localAnchorA.x, .y, localAnchorB.x, .y, referenceAngle, lowerAngle, upperAngle, motorSpeed, maxMotorTorque}
+// flags: 1 enableLimit, 2 enableMotor, 4 collideConnected
+int rw_revolute(void* h, int bodyA, int bodyB, const float* f, int flags)
+{
+    RefWorld* w = static_cast<RefWorld*>(h);
+    b2RevoluteJointDef jd;
+    jd.bodyA = w->bodies[bodyA];
+    jd.bodyB = w->bodies[bodyB];
+    jd.localAnchorA.Set(f[0], f[1]);
+    jd.localAnchorB.Set(f[2], f[3]);
+    jd.referenceAngle = f[4];
+    jd.lowerAngle = f[5];
+    jd.upperAngle = f[6];
+    jd.motorSpeed = f[7];
+    jd.maxMotorTorque = f[8];
+    jd.enableLimit = (flags & 1) != 0;
+    jd.enableMotor = (flags & 2) != 0;
+    jd.collideConnected = (flags & 4) != 0;
+    w->joints.push_back(w->world.CreateJoint(&jd));
+    return (int)w->joints.size() - 1;
+}
+
+// Bulk scene build: body b is created, then its fixtures (fbody is non-decreasing), then all joints.
+void rw_build(void* h, int nb, const int* btype, const float* bf, const int* bflags, int nf, const int* fbody,
+              const int* ftype, const float* fshape, const int* fn, const float* fmat, const int* ffilt, int nj,
+              const int* ja, const int* jb, const float* jf, const int* jflags)
+{
+    int fi = 0;
+    for (int b = 0; b < nb; ++b) {
+        rw_body(h, btype[b], bf + 9 * b, bflags[b]);
+        while (fi < nf && fbody[fi] == b) {
+            rw_fixture(h, b, ftype[fi], fshape + 16 * fi, fn[fi], fmat + 3 * fi, ffilt + 4 * fi);
+            ++fi;
+        }
+    }
+    for (int j = 0; j < nj; ++j) rw_revolute(h, ja[j], jb[j], jf + 9 * j, jflags[j]);
+}
+
+void rw_step(void* h, float dt, int vi, int pi) { static_cast<RefWorld*>(h)->world.Step(dt, vi, pi); }
+
+int rw_body_count(void* h) { return (int)static_cast<RefWorld*>(h)->bodies.size(); }
+int rw_contact_count(void* h) { return static_cast<RefWorld*>(h)->world.GetContactCount(); }
+
+// Per body (creation order), 12 floats: xf.p.x, xf.p.y, sweep.a, sweep.c.x, sweep.c.y, v.x, v.y, w,
+// xf.q.s, xf.q.c, sleepTime, awake (0/1)
+void rw_get_bodies(void* h, float* out)
+{
+    RefWorld* w = static_cast<RefWorld*>(h);
+    for (size_t i = 0; i < w->bodies.size(); ++i) {
+        const b2Body* b = w->bodies[i];
+        float* o = out + 12 * i;
+        o[0] = b->m_xf.p.x; o[1] = b->m_xf.p.y; o[2] = b->m_sweep.a;
+        o[3] = b->m_sweep.c.x; o[4] = b->m_sweep.c.y;
+        o[5] = b->m_linearVelocity.x; o[6] = b->m_linearVelocity.y; o[7] = b->m_angularVelocity;
+        o[8] = b->m_xf.q.s; o[9] = b->m_xf.q.c; o[10] = b->m_sleepTime;
+        o[11] = b->IsAwake() ? 1.0f : 0.0f;
+    }
+}
+
+// Contacts in world-list order. ints (8 per contact): fixtureA, fixtureB, flags, pointCount,
+// manifold type, id0 key, id1 key, toiCount. floats (12 per contact): localNormal.xy,
+// localPoint.xy, then per point: localPoint.xy, normalImpulse, tangentImpulse.
+int rw_get_contacts(void* h, int* ints, float* flts, int cap)
+{
+    RefWorld* w = static_cast<RefWorld*>(h);
+    int n = 0;
+    for (b2Contact* c = w->world.GetContactList(); c; c = c->GetNext()) {
+        if (n < cap) {
+            int* i = ints + 8 * n;
+            float* f = flts + 12 * n;
+            const b2Manifold& m = c->m_manifold;
+            i[0] = fixture_index(c->m_fixtureA); i[1] = fixture_index(c->m_fixtureB);
+            i[2] = (int)c->m_flags; i[3] = m.pointCount; i[4] = m.pointCount > 0 ? (int)m.type : 0;
+            i[5] = m.pointCount > 0 ? (int)m.points[0].id.key : 0;
+            i[6] = m.pointCount > 1 ? (int)m.points[1].id.key : 0;
+            i[7] = c->m_toiCount;
+            // manifold fields are dead when pointCount == 0 (a collide may return early leaving them stale)
+            bool any = m.pointCount > 0;
+            f[0] = any ? m.localNormal.x : 0.0f; f[1] = any ? m.localNormal.y : 0.0f;
+            f[2] = any ? m.localPoint.x : 0.0f; f[3] = any ? m.localPoint.y : 0.0f;
+            for (int p = 0; p < 2; ++p) {
+                bool on = p < m.pointCount;
+                f[4 + 4 * p] = on ? m.points[p].localPoint.x : 0.0f;
+                f[5 + 4 * p] = on ? m.points[p].localPoint.y : 0.0f;
+                f[6 + 4 * p] = on ? m.points[p].normalImpulse : 0.0f;
+                f[7 + 4 * p] = on ? m.points[p].tangentImpulse : 0.0f;
+            }
+        }
+        ++n;
+    }
+    return n;
+}
+
+// Per fixture (creation order): proxy id and the broadphase fat AABB (lower.xy, upper.xy).
+void rw_get_proxies(void* h, int* proxyIds, float* fat)
+{
+    RefWorld* w = static_cast<RefWorld*>(h);
+    const b2BroadPhase& bp = w->world.m_contactManager.m_broadPhase;
+    for (size_t i = 0; i < w->fixtures.size(); ++i) {
+        const b2Fixture* f = w->fixtures[i];
+        int id = f->m_proxyCount > 0 ? f->m_proxies[0].proxyId : -1;
+        proxyIds[i] = id;
+        if (id >= 0) {
+            const b2AABB& a = bp.GetFatAABB(id);
+            fat[4 * i] = a.lowerBound.x; fat[4 * i + 1] = a.lowerBound.y;
+            fat[4 * i + 2] = a.upperBound.x; fat[4 * i + 3] = a.upperBound.y;
+        }
+    }
+}
+
+// Direct narrowphase call (b2Collide* from Collision/b2CollidePolygon.cpp, b2CollideCircle.cpp,
+// b2CollideEdge.cpp). Shapes use the rw_fixture encoding; xf = {p.x, p.y, q.s, q.c}.
+// Output: ints {type, pointCount, id0, id1}; floats as rw_get_contacts (impulses zero).
+int rw_collide(int typeA, const float* sA, int nA, const float* xfA,
+               int typeB, const float* sB, int nB, const float* xfB, int* oi, float* of)
+{
+    b2CircleShape cA, cB; b2EdgeShape eA; b2PolygonShape pA, pB;
+    auto make_poly = [](b2PolygonShape& p, int type, const float* s, int n) {
+        if (type == 3) { if (n == 5) p.SetAsBox(s[0], s[1], b2Vec2(s[2], s[3]), s[4]); else p.SetAsBox(s[0], s[1]); }
+        else { b2Vec2 pts[8]; for (int i = 0; i < n && i < 8; ++i) pts[i].Set(s[2*i], s[2*i+1]); p.Set(pts, n); }
+    };
+    b2Transform xa, xb;
+    xa.p.Set(xfA[0], xfA[1]); xa.q.s = xfA[2]; xa.q.c = xfA[3];
+    xb.p.Set(xfB[0], xfB[1]); xb.q.s = xfB[2]; xb.q.c = xfB[3];
+    b2Manifold m;
+    m.pointCount = 0;
+    bool polyA = typeA == 2 || typeA == 3, polyB = typeB == 2 || typeB == 3;
+    if (typeA == 0 && typeB == 0) {
+        cA.m_p.Set(sA[0], sA[1]); cA.m_radius = sA[2]; cB.m_p.Set(sB[0], sB[1]); cB.m_radius = sB[2];
+        b2CollideCircles(&m, &cA, xa, &cB, xb);
+    } else if (polyA && typeB == 0) {
+        make_poly(pA, typeA, sA, nA); cB.m_p.Set(sB[0], sB[1]); cB.m_radius = sB[2];
+        b2CollidePolygonAndCircle(&m, &pA, xa, &cB, xb);
+    } else if (polyA && polyB) {
+        make_poly(pA, typeA, sA, nA); make_poly(pB, typeB, sB, nB);
+        b2CollidePolygons(&m, &pA, xa, &pB, xb);
+    } else if (typeA == 1 && (typeB == 0 || polyB)) {
+        eA.Set(b2Vec2(sA[0], sA[1]), b2Vec2(sA[2], sA[3]));
+        eA.m_vertex0.Set(sA[4], sA[5]); eA.m_vertex3.Set(sA[6], sA[7]);
+        eA.m_hasVertex0 = sA[8] != 0.0f; eA.m_hasVertex3 = sA[9] != 0.0f;
+        if (typeB == 0) { cB.m_p.Set(sB[0], sB[1]); cB.m_radius = sB[2]; b2CollideEdgeAndCircle(&m, &eA, xa, &cB, xb); }
+        else { make_poly(pB, typeB, sB, nB); b2CollideEdgeAndPolygon(&m, &eA, xa, &pB, xb); }
+    } else {
+        return -1;
+    }
+    oi[0] = (int)m.type; oi[1] = m.pointCount;
+    oi[2] = m.pointCount > 0 ? (int)m.points[0].id.key : 0;
+    oi[3] = m.pointCount > 1 ? (int)m.points[1].id.key : 0;
+    of[0] = m.pointCount > 0 ? m.localNormal.x : 0.0f; of[1] = m.pointCount > 0 ? m.localNormal.y : 0.0f;
+    of[2] = m.pointCount > 0 ? m.localPoint.x : 0.0f; of[3] = m.pointCount > 0 ? m.localPoint.y : 0.0f;
+    for (int p = 0; p < 2; ++p) {
+        bool on = p < m.pointCount;
+        of[4 + 4 * p] = on ? m.points[p].localPoint.x : 0.0f;
+        of[5 + 4 * p] = on ? m.points[p].localPoint.y : 0.0f;
+        of[6 + 4 * p] = 0.0f; of[7 + 4 * p] = 0.0f;
+    }
+    return 0;
+}
+
+// Polygon construction as the reference does it (b2PolygonShape::Set / SetAsBox and ComputeMass):
+// out = {count, vertices (16), normals (16), centroid (2), mass, center (2), I} for density 1.
+void rw_polygon(int type, const float* s, int n, float density, float* out)
+{
+    b2PolygonShape p;
+    if (type == 3) { if (n == 5) p.SetAsBox(s[0], s[1], b2Vec2(s[2], s[3]), s[4]); else p.SetAsBox(s[0], s[1]); }
+    else { b2Vec2 pts[8]; for (int i = 0; i < n && i < 8; ++i) pts[i].Set(s[2*i], s[2*i+1]); p.Set(pts, n); }
+    std::memset(out, 0, sizeof(float) * 40);
+    out[0] = (float)p.m_count;
+    for (int i = 0; i < p.m_count; ++i) {
+        out[1 + 2 * i] = p.m_vertices[i].x; out[2 + 2 * i] = p.m_vertices[i].y;
+        out[17 + 2 * i] = p.m_normals[i].x; out[18 + 2 * i] = p.m_normals[i].y;
+    }
+    out[33] = p.m_centroid.x; out[34] = p.m_centroid.y;
+    b2MassData md;
+    p.ComputeMass(&md, density);
+    out[35] = md.mass; out[36] = md.center.x; out[37] = md.center.y; out[38] = md.I;
+}
+
+// b2TimeOfImpact (Collision/b2TimeOfImpact.cpp:257) on two shapes and sweeps.
+// sweep = {localCenter.xy, c0.xy, c.xy, a0, a, alpha0}; out = {state, t}.
+void rw_toi(int typeA, const float* sA, int nA, const float* swA,
+            int typeB, const float* sB, int nB, const float* swB, float tMax, float* out)
+{
+    b2CircleShape cA, cB; b2EdgeShape eA; b2PolygonShape pA, pB;
+    auto make = [&](int type, const float* s, int n, b2CircleShape& c, b2PolygonShape& p, b2EdgeShape* e) -> const b2Shape* {
+        if (type == 0) { c.m_p.Set(s[0], s[1]); c.m_radius = s[2]; return &c; }
+        if (type == 1 && e) { e->Set(b2Vec2(s[0], s[1]), b2Vec2(s[2], s[3])); return e; }
+        if (type == 3) { if (n == 5) p.SetAsBox(s[0], s[1], b2Vec2(s[2], s[3]), s[4]); else p.SetAsBox(s[0], s[1]); return &p; }
+        b2Vec2 pts[8]; for (int i = 0; i < n && i < 8; ++i) pts[i].Set(s[2*i], s[2*i+1]); p.Set(pts, n); return &p;
+    };
+    b2TOIInput in;
+    in.proxyA.Set(make(typeA, sA, nA, cA, pA, &eA), 0);
+    in.proxyB.Set(make(typeB, sB, nB, cB, pB, nullptr), 0);
+    auto sw = [](b2Sweep& s, const float* f) {
+        s.localCenter.Set(f[0], f[1]); s.c0.Set(f[2], f[3]); s.c.Set(f[4], f[5]);
+        s.a0 = f[6]; s.a = f[7]; s.alpha0 = f[8];
+    };
+    sw(in.sweepA, swA); sw(in.sweepB, swB);
+    in.tMax = tMax;
+    b2TOIOutput o;
+    b2TimeOfImpact(&o, &in);
+    out[0] = (float)o.state; out[1] = o.t;
+}
+
+void rw_sincosf(float x, float* s, float* c) { b2Rot q(x); *s = q.s; *c = q.c; }
+
+// Steps many independent reference worlds on `threads` host threads. The reference fills its
+// contact-type registry lazily on the first b2Contact::Create (Dynamics/Contacts/b2Contact.cpp:74-78),
+// so one contact is created on the calling thread first.
+void rw_step_many(void** hs, int n, float dt, int vi, int pi, int steps, int threads)
+{
+    {
+        b2World warm(b2Vec2(0.0f, -10.0f));
+        b2BodyDef bd;
+        bd.type = b2_dynamicBody;
+        b2CircleShape c;
+        c.m_radius = 1.0f;
+        warm.CreateBody(&bd)->CreateFixture(&c, 1.0f);
+        warm.CreateBody(&bd)->CreateFixture(&c, 1.0f);
+        warm.Step(1.0f / 60.0f, 1, 1);
+    }
+    if (threads < 1) threads = 1;
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t) {
+        pool.emplace_back([=]() {
+            for (int i = t; i < n; i += threads)
+                for (int s = 0; s < steps; ++s) static_cast<RefWorld*>(hs[i])->world.Step(dt, vi, pi);
+        });
+    }
+    for (std::thread& th : pool) th.join();
+}
+
+} // extern "C"
