@@ -1,0 +1,310 @@
+"""Benchmark of the GB300 Box2D step on the batched-worlds workload.
+
+One step = one b2World::Step of every world of the batch: 4096 independent worlds (per GPU) whose
+body counts are log-uniform in [16, 512], each a seeded pyramid, box stacks or a circle/polygon drop,
+dt 1/60, 8 velocity / 3 position iterations, float32, sleeping disabled (every body is simulated on
+every step). Metric: body-steps per second (dynamic bodies x steps / time) over the whole job.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--worlds n]
+
+value: device time of the K timed steps (CUDA events on the stream the step kernel runs on), state
+resident in HBM (several hundred MB, larger than L2, so no flush is needed between steps).
+e2e: the same K steps through the C-ABI with host buffers: every step uploads the force/torque
+accumulators of every body from pinned host memory (gb_set_forces), steps, and reads every body
+transform back into pinned host memory (gb_get_transforms), wall-clock timed.
+--impl reference: the reference CPU step (the compiled reference where its build exists, else the
+project's CPU restatement of it) on all host cores over a sample of the same worlds.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DT, VI, PI = 1.0 / 60.0, 8, 3
+METRIC = "body-steps/sec (batched worlds, plain solver)"
+UNIT = "body-steps/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=60)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--worlds", type=int, default=4096)
+    p.add_argument("--seed", type=int, default=1)
+    p.add_argument("--cpu-sample-every", type=int, default=8)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(args, rank: int):
+    from box2dpp_gb300 import scenes
+
+    return scenes.config3(args.worlds, seed=args.seed + 1000003 * rank, allow_sleep=False)
+
+
+def config_dict(args, worlds, extra=None):
+    n = sum(w.dynamic_count for w in worlds)
+    d = {
+        "workload": f"batched: {len(worlds)} independent worlds per GPU, bodies log-uniform in [16,512] "
+                    "(pyramid / box stacks / circle+polygon drop), dt 1/60, 8/3 iterations, sleep off",
+        "worlds_per_gpu": len(worlds),
+        "dynamic_bodies_per_gpu": n,
+        "step": "one b2World::Step of every world",
+        "l2": "state resident in HBM is larger than the 129 MB L2; no flush between steps",
+        "parallelism": "independent worlds sharded across GPUs, no collective",
+    }
+    if extra:
+        d.update(extra)
+    return d
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def algorithmic_bytes(t: dict) -> int:
+    """Minimum HBM bytes of one step if every persistent element is read and written once:
+    104 B per solved body (52 B read: c, a, v, w, invMass, invI, localCenter, gravityScale, damping;
+    24 B written c, a, v, w; 16 B transform; 12 B sweep c0, a0), 144 B per solved contact (manifold
+    64 B read + 64 B written, body/fixture indices 8 B, friction/restitution 8 B), 32 B per proxy
+    (fat AABB read + write), 8 B per broadphase pair."""
+    return 104 * t["solved_bodies"] + 144 * t["solved_contacts"] + 32 * t["proxies"] + 8 * t["pairs"]
+
+
+def cpu_baseline(worlds, steps: int, warmup: int, every: int, threads: int):
+    """The reference CPU step on `threads` host threads over every `every`-th world."""
+    import oracle
+
+    sample = worlds[::every]
+    kind = "reference" if oracle.reference_available() and os.path.exists(os.path.join(ROOT, "oracle", "_ref",
+                                                                                      "libref_libm.so")) else "port"
+    trig = "libm" if kind == "reference" else "project"
+    ws = [oracle.OracleWorld(s, kind, trig) for s in sample]
+    # costliest first so the round-robin split over threads balances
+    order = sorted(range(len(ws)), key=lambda i: -sample[i].dynamic_count)
+    ws = [ws[i] for i in order]
+    bodies = sum(s.dynamic_count for s in sample)
+    oracle.step_many(ws, warmup, threads, DT, VI, PI)
+    t0 = time.perf_counter()
+    oracle.step_many(ws, steps, threads, DT, VI, PI)
+    el = time.perf_counter() - t0
+    return {
+        "value": bodies * steps / el,
+        "unit": UNIT,
+        "cores": threads,
+        "kind": kind,
+        "sample": f"{len(sample)} of the {len(worlds)} worlds (every {every}th, {bodies} dynamic bodies), "
+                  f"{steps} steps after {warmup} warm-up steps, {el:.2f} s",
+    }
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    worlds = workload(args, 0)
+    threads = os.cpu_count() or 1
+    cb = cpu_baseline(worlds, args.steps, args.warmup, args.cpu_sample_every, threads)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": config_dict(args, worlds, {"sample": cb["sample"]}),
+        "cpu_baseline": cb,
+        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import torch
+
+    rank, world_size, local = dist_env()
+    torch.cuda.set_device(local)
+    if world_size > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from box2dpp_gb300.world import World
+
+    worlds = workload(args, rank)
+    w = World(worlds)
+    stream = torch.cuda.Stream()
+    w.set_stream(stream.cuda_stream)
+    w.upload()
+    n_dyn = w.dynamic_bodies
+    for _ in range(args.warmup):
+        w.step(DT, VI, PI)
+    w.sync()
+    t_before = w.totals()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world_size > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+            torch.cuda.synchronize()
+
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            start.record(stream)
+            for _ in range(args.steps):
+                w.step(DT, VI, PI)
+            end.record(stream)
+        end.synchronize()
+    barrier()
+    ms = start.elapsed_time(end)
+    w.sync()
+    t_after = w.totals()
+    ms_t = torch.tensor([ms], device="cuda")
+    if world_size > 1:
+        import torch.distributed as dist
+
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms_max = float(ms_t.item())
+    total_bodies = n_dyn * world_size
+    value = total_bodies * args.steps / (ms_max / 1e3)
+
+    # end-to-end through the C-ABI with pinned host buffers
+    nb = w.total_bodies
+    forces = torch.zeros((nb, 4), dtype=torch.float32).pin_memory()
+    xforms = torch.zeros((nb, 4), dtype=torch.float32).pin_memory()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        w.set_forces_ptr(forces.data_ptr())
+        w.step(DT, VI, PI)
+        w.get_transforms_ptr(xforms.data_ptr())
+    w.sync()
+    e2e_s = time.perf_counter() - t0
+    e2e_t = torch.tensor([e2e_s], device="cuda")
+    if world_size > 1:
+        import torch.distributed as dist
+
+        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
+    e2e_value = total_bodies * args.steps / float(e2e_t.item())
+
+    if rank == 0:
+        peak, peak_kind = measured_peaks()
+        step_bytes = (algorithmic_bytes(t_before) + algorithmic_bytes(t_after)) / 2.0
+        per_launch_ms = ms / args.steps
+        achieved = step_bytes / (per_launch_ms / 1e3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "peak_source": peak_kind, "kernel": "b2g::StepKernel",
+                "algorithmic_bytes_per_launch": step_bytes,
+                "launch_ms": per_launch_ms,
+                "counts_per_step": {k: (t_before[k] + t_after[k]) / 2.0 for k in
+                                    ("solved_bodies", "solved_contacts", "proxies", "pairs", "toi_events")}}
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_dict(args, worlds), "roofline": roof,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nb * 16, "d2h_bytes_per_step": nb * 16,
+                    "calls": "gb_set_forces + gb_world_step + gb_get_transforms per step, pinned host buffers"},
+            "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+        }
+        if not args.no_cpu_baseline and world_size == 1:
+            line["cpu_baseline"] = cpu_baseline(worlds, args.steps, args.warmup, args.cpu_sample_every,
+                                                os.cpu_count() or 1)
+        print(json.dumps(line), flush=True)
+    w.close()
+    if world_size > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

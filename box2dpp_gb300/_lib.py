@@ -1,0 +1,93 @@
+"""ctypes binding of ``libbox2d_gb300.so`` (the C-ABI in ``include/box2d_gb300.h``).
+
+The library is built in-tree by ``box2dpp_gb300.build``. There is no fallback: if the library is
+missing and cannot be built, importing the world API raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+GB_OK, GB_ERR_CAPACITY, GB_ERR_TIMEOUT, GB_ERR_INVALID, GB_ERR_CUDA = 0, 1, 2, 3, 4
+STATUS_NAMES = {0: "GB_OK", 1: "GB_ERR_CAPACITY", 2: "GB_ERR_TIMEOUT", 3: "GB_ERR_INVALID", 4: "GB_ERR_CUDA"}
+
+# Every symbol include/box2d_gb300.h declares.
+EXPORTS = [
+    "gb_world_create", "gb_world_destroy", "gb_create_bodies", "gb_create_fixtures", "gb_create_revolute_joints",
+    "gb_build_world", "gb_world_upload", "gb_world_step", "gb_world_sync", "gb_world_set_stream",
+    "gb_world_counts", "gb_get_bodies", "gb_get_contacts", "gb_get_proxies", "gb_world_stats", "gb_sincos",
+    "gb_collide", "gb_version", "gb_world_totals", "gb_set_forces", "gb_get_transforms",
+]
+
+
+class GbError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        super().__init__(f"{where} failed: {STATUS_NAMES.get(status, status)}")
+        self.status = status
+
+
+class WorldDef(C.Structure):
+    _fields_ = [("gravity_x", C.c_float), ("gravity_y", C.c_float), ("allow_sleep", C.c_int),
+                ("warm_starting", C.c_int), ("continuous_physics", C.c_int), ("sub_stepping", C.c_int)]
+
+
+_f32 = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+_i32 = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_LIB = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load the extension (building it first when it is absent or older than its sources)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if build_if_missing:
+        path = _build.build()
+    if not os.path.exists(path):
+        raise RuntimeError(f"box2dpp_gb300 extension not built: {path}")
+    lib = C.CDLL(path)
+    vp, i, f = C.c_void_p, C.c_int, C.c_float
+    sig = {
+        "gb_world_create": [i, C.POINTER(WorldDef), C.POINTER(vp)],
+        "gb_world_destroy": [vp],
+        "gb_create_bodies": [vp, i, i, _i32, _f32, _i32, _i32],
+        "gb_create_fixtures": [vp, i, i, _i32, _i32, _f32, _i32, _f32, _i32, _i32],
+        "gb_create_revolute_joints": [vp, i, i, _i32, _i32, _f32, _i32, _i32],
+        "gb_build_world": [vp, i, i, _i32, _f32, _i32, i, _i32, _i32, _f32, _i32, _f32, _i32, i, _i32, _i32, _f32, _i32],
+        "gb_world_upload": [vp],
+        "gb_world_step": [vp, f, i, i],
+        "gb_world_sync": [vp],
+        "gb_world_set_stream": [vp, vp],
+        "gb_world_counts": [vp, i, C.POINTER(i), C.POINTER(i), C.POINTER(i), C.POINTER(i)],
+        "gb_get_bodies": [vp, i, _f32],
+        "gb_get_contacts": [vp, i, _i32, _f32, i, C.POINTER(i)],
+        "gb_get_proxies": [vp, i, _i32, _f32],
+        "gb_world_stats": [vp, i, C.POINTER(i), C.POINTER(i)],
+        "gb_sincos": [_f32, _f32, _f32, i],
+        "gb_collide": [i, _i32, _f32, _i32, _f32, _i32, _f32, _i32, _f32, _i32, _f32],
+        "gb_world_totals": [vp, C.POINTER(C.c_longlong)],
+        "gb_set_forces": [vp, vp],
+        "gb_get_transforms": [vp, vp],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    lib.gb_version.argtypes = []
+    lib.gb_version.restype = C.c_char_p
+    _LIB = lib
+    return lib
+
+
+def check(status: int, where: str) -> None:
+    if status != GB_OK:
+        raise GbError(status, where)

@@ -1,0 +1,939 @@
+// Host runtime of the GB300 Box2D step and the C-ABI declared in include/box2d_gb300.h.
+//
+// The host keeps a mirror of each world's bodies, fixtures, proxies and joints. Creation calls
+// (b2World::CreateBody, b2Body::CreateFixture, b2World::CreateJoint) run their setup arithmetic here,
+// exactly as the reference does on its host: polygon hulls, mass data, initial transforms and AABBs,
+// proxy ids. The mirror is uploaded once into device columns (b2g_world.h); from then on every step
+// runs on the device and the host only reads state back when asked. A creation call after steps
+// first pulls the device state back, so the mirror stays authoritative for the next upload.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <vector>
+
+#include "../../include/box2d_gb300.h"
+#include "b2g_world.h"
+
+cudaError_t b2gLaunchStep(const b2g::Batch& B, const b2g::StepParams& P, const int* schedule, int threads,
+                          cudaStream_t stream);
+cudaError_t b2gLaunchSinCos(const float* x, float* s, float* c, int n, cudaStream_t stream);
+cudaError_t b2gLaunchCollide(int n, const b2g::Shape* a, const float4* xa, const b2g::Shape* b, const float4* xb,
+                             int4* oi, float4* of, cudaStream_t stream);
+
+using namespace b2g;
+
+namespace {
+
+struct HBody {
+    int type = kStatic, flags = 0;
+    Xf xf{};
+    Sweep sw{};
+    Vec2 v{0, 0};
+    float w = 0;
+    Vec2 force{0, 0};
+    float torque = 0;
+    float mass = 0, invMass = 0, I = 0, invI = 0;
+    float linDamp = 0, angDamp = 0, gravScale = 1, sleepTime = 0;
+    int fixtureList = kNullIdx, contactList = kNullIdx, jointList = kNullIdx, next = kNullIdx;
+};
+
+struct HFixture {
+    int body = kNullIdx, next = kNullIdx;
+    Shape shape{};
+    float density = 0, friction = 0.2f, restitution = 0;
+    int category = 1, mask = 0xFFFF, group = 0, sensor = 0;
+    int proxyId = kNullIdx;
+    float4 aabb{};
+};
+
+struct HContacts { // device contact columns of one world, pulled back before a host-side change
+    std::vector<int4> ci, ce, mh;
+    std::vector<float4> cp, mv, mp0, mp1;
+    std::vector<int> order, cnext;
+};
+
+struct HWorld {
+    gb_world_def def{};
+    int bodyList = kNullIdx, jointList = kNullIdx;
+    std::vector<HBody> bodies;
+    std::vector<HFixture> fixtures;
+    std::vector<Joint> joints;
+    std::vector<float4> fat;
+    std::vector<int> pfix, moved;
+    int nodeCount = 0, proxyCount = 0;
+    int newFixture = 0;
+    WorldState state{};
+    bool hasState = false; // state/contacts valid (pulled back from, or never sent to, the device)
+    HContacts contacts;
+};
+
+template <typename T> struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+};
+
+} // namespace
+
+struct gb_world {
+    std::vector<HWorld> worlds;
+    std::vector<WorldDesc> desc;
+    Batch batch{};
+    std::vector<void*> allocations;
+    int* dSchedule = nullptr;
+    cudaStream_t stream = nullptr;
+    bool ownStream = false;
+    bool onDevice = false;   // device columns hold the current state
+    bool hostDirty = true;   // host mirror has changes not yet uploaded
+    int threads = 64;
+    bool locked = false;
+};
+
+namespace {
+
+gb_status cudaErr(cudaError_t e)
+{
+    if (e == cudaSuccess) return GB_OK;
+    std::fprintf(stderr, "box2d_gb300: CUDA error: %s\n", cudaGetErrorString(e));
+    return GB_ERR_CUDA;
+}
+
+#define GB_CUDA(x)                                   \
+    do {                                             \
+        gb_status s_ = cudaErr(x);                   \
+        if (s_ != GB_OK) return s_;                  \
+    } while (0)
+
+// b2Body::ResetMassData (Box2D/Dynamics/b2Body.cpp:283-352)
+void ResetMassData(HWorld& W, int bi)
+{
+    HBody& b = W.bodies[bi];
+    b.mass = 0.0f; b.invMass = 0.0f; b.I = 0.0f; b.invI = 0.0f;
+    b.sw.localCenter = V(0.0f, 0.0f);
+    if (b.type == kStatic || b.type == kKinematic) {
+        b.sw.c0 = b.xf.p;
+        b.sw.c = b.xf.p;
+        b.sw.a0 = b.sw.a;
+        return;
+    }
+    Vec2 localCenter = V(0.0f, 0.0f);
+    for (int f = b.fixtureList; f != kNullIdx; f = W.fixtures[f].next) {
+        const HFixture& fx = W.fixtures[f];
+        if (fx.density == 0.0f) continue;
+        MassData md;
+        ComputeMass(fx.shape, fx.density, &md);
+        b.mass += md.mass;
+        localCenter = localCenter + md.mass * md.center;
+        b.I += md.I;
+    }
+    if (b.mass > 0.0f) {
+        b.invMass = 1.0f / b.mass;
+        localCenter.x *= b.invMass;
+        localCenter.y *= b.invMass;
+    } else {
+        b.mass = 1.0f;
+        b.invMass = 1.0f;
+    }
+    if (b.I > 0.0f && (b.flags & kBFixedRot) == 0) {
+        b.I -= b.mass * Dot(localCenter, localCenter);
+        b.invI = 1.0f / b.I;
+    } else {
+        b.I = 0.0f;
+        b.invI = 0.0f;
+    }
+    Vec2 oldCenter = b.sw.c;
+    b.sw.localCenter = localCenter;
+    b.sw.c = Mul(b.xf, b.sw.localCenter);
+    b.sw.c0 = b.sw.c;
+    b.v = b.v + Cross(b.w, b.sw.c - oldCenter);
+}
+
+// Proxy ids are node ids of the reference's b2DynamicTree: its free list hands out 0, 1, 2, ... and
+// every insertion after the first also takes one internal node (b2DynamicTree.cpp:56-105, 112-131),
+// so without removals the k-th proxy gets id 0 for k = 0 and 2k - 1 otherwise.
+int AllocateProxy(HWorld& W, float4 fatAabb, int fixture)
+{
+    int id = W.nodeCount++;
+    if (W.proxyCount > 0) W.nodeCount++;
+    ++W.proxyCount;
+    if ((int)W.fat.size() <= id) {
+        W.fat.resize(id + 1, make_float4(0, 0, 0, 0));
+        W.pfix.resize(id + 1, kNullIdx);
+        W.moved.resize(id + 1, 0);
+    }
+    W.fat[id] = fatAabb;
+    W.pfix[id] = fixture;
+    W.moved[id] = 1;
+    return id;
+}
+
+Shape MakeShape(int type, const float* s, int n)
+{
+    Shape sh;
+    std::memset(&sh, 0, sizeof(sh));
+    switch (type) {
+    case 0:
+        sh.type = kCircle; sh.count = 1; sh.v[0] = V(s[0], s[1]); sh.radius = s[2];
+        break;
+    case 1:
+        sh.type = kEdge; sh.count = 2; sh.radius = kPolygonRadius;
+        sh.v[0] = V(s[0], s[1]); sh.v[1] = V(s[2], s[3]); sh.v[2] = V(s[4], s[5]); sh.v[3] = V(s[6], s[7]);
+        sh.hasV0 = s[8] != 0.0f; sh.hasV3 = s[9] != 0.0f;
+        break;
+    case 2: {
+        Vec2 pts[kMaxPolyVerts];
+        int m = std::min(n, kMaxPolyVerts);
+        for (int i = 0; i < m; ++i) pts[i] = V(s[2 * i], s[2 * i + 1]);
+        PolygonSet(sh, pts, n);
+        break;
+    }
+    default:
+        if (n == 5) PolygonSetAsBox(sh, s[0], s[1], V(s[2], s[3]), s[4]);
+        else PolygonSetAsBox(sh, s[0], s[1]);
+        break;
+    }
+    return sh;
+}
+
+template <typename T> gb_status DevAlloc(gb_world* g, T** p, size_t n)
+{
+    *p = nullptr;
+    if (n == 0) n = 1;
+    void* ptr = nullptr;
+    GB_CUDA(cudaMalloc(&ptr, n * sizeof(T)));
+    g->allocations.push_back(ptr);
+    *p = static_cast<T*>(ptr);
+    return GB_OK;
+}
+
+void FreeDevice(gb_world* g)
+{
+    for (void* p : g->allocations) cudaFree(p);
+    g->allocations.clear();
+    std::memset(&g->batch, 0, sizeof(g->batch));
+    g->dSchedule = nullptr;
+}
+
+int NextPow2(int x)
+{
+    int p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+// Pull the device state of every world back into the host mirror.
+gb_status Download(gb_world* g)
+{
+    if (!g->onDevice) return GB_OK;
+    GB_CUDA(cudaStreamSynchronize(g->stream));
+    const Batch& B = g->batch;
+    for (size_t wi = 0; wi < g->worlds.size(); ++wi) {
+        HWorld& W = g->worlds[wi];
+        const WorldDesc& d = g->desc[wi];
+        int nb = d.bodyCount, nf = d.fixCount, np = d.proxyCap, nc = d.contactCap;
+        std::vector<float4> xf(nb), sw(nb), sw0(nb), vel(nb), frc(nb);
+        std::vector<int4> bi(nb), bj(nb);
+        GB_CUDA(cudaMemcpy(xf.data(), B.xf + d.bodyBase, nb * sizeof(float4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(sw.data(), B.sw + d.bodyBase, nb * sizeof(float4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(sw0.data(), B.sw0 + d.bodyBase, nb * sizeof(float4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(vel.data(), B.vel + d.bodyBase, nb * sizeof(float4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(frc.data(), B.frc + d.bodyBase, nb * sizeof(float4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(bi.data(), B.bi + d.bodyBase, nb * sizeof(int4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(bj.data(), B.bj + d.bodyBase, nb * sizeof(int4), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < nb; ++i) {
+            HBody& b = W.bodies[i];
+            b.xf.p = V(xf[i].x, xf[i].y); b.xf.q.s = xf[i].z; b.xf.q.c = xf[i].w;
+            b.sw.c = V(sw[i].x, sw[i].y); b.sw.a = sw[i].z; b.sw.alpha0 = sw[i].w;
+            b.sw.c0 = V(sw0[i].x, sw0[i].y); b.sw.a0 = sw0[i].z; b.sleepTime = sw0[i].w;
+            b.v = V(vel[i].x, vel[i].y); b.w = vel[i].z;
+            b.force = V(frc[i].x, frc[i].y); b.torque = frc[i].z;
+            b.flags = bi[i].y; b.contactList = bi[i].w;
+        }
+        std::vector<float4> faabb(nf);
+        GB_CUDA(cudaMemcpy(faabb.data(), B.faabb + d.fixBase, nf * sizeof(float4), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < nf; ++i) W.fixtures[i].aabb = faabb[i];
+        W.fat.resize(np); W.moved.resize(np);
+        GB_CUDA(cudaMemcpy(W.fat.data(), B.fat + d.proxyBase, np * sizeof(float4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(W.moved.data(), B.moved + d.proxyBase, np * sizeof(int), cudaMemcpyDeviceToHost));
+        HContacts& C = W.contacts;
+        C.ci.resize(nc); C.ce.resize(nc); C.mh.resize(nc); C.cp.resize(nc); C.mv.resize(nc); C.mp0.resize(nc);
+        C.mp1.resize(nc); C.order.resize(nc); C.cnext.resize(nc);
+        GB_CUDA(cudaMemcpy(C.ci.data(), B.ci + d.contactBase, nc * sizeof(int4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(C.ce.data(), B.ce + d.contactBase, nc * sizeof(int4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(C.mh.data(), B.mh + d.contactBase, nc * sizeof(int4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(C.cp.data(), B.cp + d.contactBase, nc * sizeof(float4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(C.mv.data(), B.mv + d.contactBase, nc * sizeof(float4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(C.mp0.data(), B.mp0 + d.contactBase, nc * sizeof(float4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(C.mp1.data(), B.mp1 + d.contactBase, nc * sizeof(float4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(C.order.data(), B.order + d.contactBase, nc * sizeof(int), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(C.cnext.data(), B.cnext + d.contactBase, nc * sizeof(int), cudaMemcpyDeviceToHost));
+        if (d.jointCount > 0)
+            GB_CUDA(cudaMemcpy(W.joints.data(), B.joint + d.jointBase, d.jointCount * sizeof(Joint), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(&W.state, B.state + wi, sizeof(WorldState), cudaMemcpyDeviceToHost));
+        W.newFixture = W.state.newFixture;
+        W.hasState = true;
+    }
+    g->onDevice = false;
+    return GB_OK;
+}
+
+template <typename T> gb_status Put(T* dst, const std::vector<T>& src, size_t n)
+{
+    if (n == 0) return GB_OK;
+    GB_CUDA(cudaMemcpy(dst, src.data(), n * sizeof(T), cudaMemcpyHostToDevice));
+    return GB_OK;
+}
+
+// (Re)allocate device columns for the current world sizes and copy the host mirror over.
+gb_status Upload(gb_world* g)
+{
+    if (!g->hostDirty && g->onDevice) return GB_OK;
+    if (!g->stream) {
+        GB_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+        g->ownStream = true;
+    }
+    if (g->onDevice) { gb_status s = Download(g); if (s != GB_OK) return s; }
+    FreeDevice(g);
+    const int nw = (int)g->worlds.size();
+    g->desc.assign(nw, WorldDesc{});
+    long long tb = 0, tf = 0, tp = 0, tc = 0, tj = 0, tq = 0, tr = 0;
+    for (int wi = 0; wi < nw; ++wi) {
+        HWorld& W = g->worlds[wi];
+        WorldDesc& d = g->desc[wi];
+        d.bodyBase = (int)tb; d.bodyCount = (int)W.bodies.size();
+        d.fixBase = (int)tf; d.fixCount = (int)W.fixtures.size();
+        d.proxyBase = (int)tp; d.proxyCap = std::max(1, (int)W.fat.size());
+        int oldCap = W.hasState ? (int)W.contacts.ci.size() : 0;
+        int cap = std::max(64, 8 * d.fixCount);
+        cap = std::max(cap, oldCap);
+        d.contactBase = (int)tc; d.contactCap = cap;
+        d.jointBase = (int)tj; d.jointCount = (int)W.joints.size();
+        d.pairBase = (int)tq; d.pairCap = NextPow2(std::max(256, cap));
+        d.rowBase = (int)tr; d.rowCap = d.bodyCount + cap + d.jointCount + 2 * kMaxTOIContacts;
+        tb += std::max(1, d.bodyCount); tf += std::max(1, d.fixCount); tp += d.proxyCap; tc += cap;
+        tj += std::max(1, d.jointCount); tq += d.pairCap; tr += d.rowCap;
+    }
+    if (tb > (1LL << 31) - 1 || tc > (1LL << 31) - 1 || tq > (1LL << 31) - 1 || tr > (1LL << 31) - 1)
+        return GB_ERR_CAPACITY;
+    Batch& B = g->batch;
+    B.worlds = nw;
+    gb_status s = GB_OK;
+#define ALLOC(field, n) if ((s = DevAlloc(g, &B.field, (size_t)(n))) != GB_OK) return s
+    ALLOC(desc, nw); ALLOC(state, nw);
+    ALLOC(xf, tb); ALLOC(sw, tb); ALLOC(sw0, tb); ALLOC(vel, tb); ALLOC(frc, tb); ALLOC(mas, tb); ALLOC(prop, tb);
+    ALLOC(bi, tb); ALLOC(bj, tb);
+    ALLOC(fi, tf); ALLOC(fm, tf); ALLOC(ff, tf); ALLOC(faabb, tf); ALLOC(shape, tf);
+    ALLOC(fat, tp); ALLOC(pfix, tp); ALLOC(moved, tp); ALLOC(movedList, tp);
+    ALLOC(ci, tc); ALLOC(ce, tc); ALLOC(cp, tc); ALLOC(mh, tc); ALLOC(mv, tc); ALLOC(mp0, tc); ALLOC(mp1, tc);
+    ALLOC(order, tc); ALLOC(cnext, tc);
+    ALLOC(joint, tj); ALLOC(sJoint, tj);
+    ALLOC(sBody, tr); ALLOC(sStack, tb); ALLOC(sWake, tb); ALLOC(sPos, tr); ALLOC(sVel, tr); ALLOC(islands, tb);
+    ALLOC(islandJ, tb); ALLOC(sleepOut, tb);
+    ALLOC(sContact, tc); ALLOC(sStatus, tc); ALLOC(vc, tc); ALLOC(pc, tc); ALLOC(toi, tc);
+    ALLOC(pairs, tq); ALLOC(pairKeep, tq);
+#undef ALLOC
+    GB_CUDA(cudaMemcpy(B.desc, g->desc.data(), nw * sizeof(WorldDesc), cudaMemcpyHostToDevice));
+    std::vector<WorldState> states(nw);
+    // Host staging of every column for all worlds, then one copy per column.
+    std::vector<float4> xf(tb), sw(tb), sw0(tb), vel(tb), frc(tb), mas(tb), prop(tb);
+    std::vector<int4> bi(tb, make_int4(0, 0, kNullIdx, kNullIdx)), bj(tb, make_int4(kNullIdx, kNullIdx, 0, 0));
+    std::vector<int4> fi(tf, make_int4(kNullIdx, kNullIdx, kNullIdx, 0)), ff(tf);
+    std::vector<float4> fm(tf), faabb(tf);
+    std::vector<Shape> shapes(tf);
+    std::vector<float4> fat(tp, make_float4(0, 0, 0, 0));
+    std::vector<int> pfix(tp, kNullIdx), moved(tp, 0);
+    std::vector<int4> ci(tc, make_int4(0, 0, 0, 0)), ce(tc, make_int4(-1, -1, -1, -1)), mh(tc, make_int4(0, 0, 0, 0));
+    std::vector<float4> cp(tc, make_float4(0, 0, 0, 1)), mv(tc), mp0(tc), mp1(tc);
+    std::vector<int> order(tc, 0), cnext(tc, kNullIdx);
+    std::vector<Joint> joints(tj);
+    for (int wi = 0; wi < nw; ++wi) {
+        HWorld& W = g->worlds[wi];
+        const WorldDesc& d = g->desc[wi];
+        for (int i = 0; i < d.bodyCount; ++i) {
+            const HBody& b = W.bodies[i];
+            const int r = d.bodyBase + i;
+            xf[r] = make_float4(b.xf.p.x, b.xf.p.y, b.xf.q.s, b.xf.q.c);
+            sw[r] = make_float4(b.sw.c.x, b.sw.c.y, b.sw.a, b.sw.alpha0);
+            sw0[r] = make_float4(b.sw.c0.x, b.sw.c0.y, b.sw.a0, b.sleepTime);
+            vel[r] = make_float4(b.v.x, b.v.y, b.w, 0.0f);
+            frc[r] = make_float4(b.force.x, b.force.y, b.torque, 0.0f);
+            mas[r] = make_float4(b.invMass, b.invI, b.sw.localCenter.x, b.sw.localCenter.y);
+            prop[r] = make_float4(b.linDamp, b.angDamp, b.gravScale, b.mass);
+            bi[r] = make_int4(b.type, b.flags, b.fixtureList, W.hasState ? b.contactList : kNullIdx);
+            bj[r] = make_int4(b.jointList, b.next, 0, 0);
+        }
+        for (int i = 0; i < d.fixCount; ++i) {
+            const HFixture& f = W.fixtures[i];
+            const int r = d.fixBase + i;
+            fi[r] = make_int4(f.body, f.next, f.proxyId, f.sensor);
+            fm[r] = make_float4(f.friction, f.restitution, f.density, f.shape.radius);
+            ff[r] = make_int4(f.category, f.mask, f.group, 0);
+            faabb[r] = f.aabb;
+            shapes[r] = f.shape;
+        }
+        const int np = d.proxyCap;
+        W.fat.resize(np, make_float4(0, 0, 0, 0)); W.pfix.resize(np, kNullIdx); W.moved.resize(np, 0);
+        std::copy(W.fat.begin(), W.fat.end(), fat.begin() + d.proxyBase);
+        std::copy(W.pfix.begin(), W.pfix.end(), pfix.begin() + d.proxyBase);
+        std::copy(W.moved.begin(), W.moved.end(), moved.begin() + d.proxyBase);
+        // contacts: previous slots keep their index; the rest of the capacity joins the free list
+        const int cap = d.contactCap;
+        HContacts& C = W.contacts;
+        const int old = W.hasState ? (int)C.ci.size() : 0;
+        for (int i = 0; i < old; ++i) {
+            const int r = d.contactBase + i;
+            ci[r] = C.ci[i]; ce[r] = C.ce[i]; mh[r] = C.mh[i]; cp[r] = C.cp[i]; mv[r] = C.mv[i];
+            mp0[r] = C.mp0[i]; mp1[r] = C.mp1[i]; order[r] = C.order[i]; cnext[r] = C.cnext[i];
+        }
+        WorldState st = W.hasState ? W.state : WorldState{};
+        int freeHead = W.hasState ? W.state.freeContact : kNullIdx;
+        for (int i = cap - 1; i >= old; --i) { cnext[d.contactBase + i] = freeHead; freeHead = i; }
+        if (!W.hasState) st.contactCount = 0;
+        st.freeContact = freeHead;
+        st.gx = W.def.gravity_x; st.gy = W.def.gravity_y;
+        st.bodyList = W.bodyList;
+        st.jointList = W.jointList;
+        st.newFixture = W.newFixture;
+        if (!W.hasState) { st.stepComplete = 1; st.inv_dt0 = 0.0f; }
+        st.allowSleep = W.def.allow_sleep; st.warmStarting = W.def.warm_starting;
+        st.continuous = W.def.continuous_physics; st.subStepping = W.def.sub_stepping;
+        st.error = 0;
+        states[wi] = st;
+        for (int j = 0; j < d.jointCount; ++j) joints[d.jointBase + j] = W.joints[j];
+        W.hasState = true;
+        W.state = st;
+        C = HContacts();
+    }
+    if ((s = Put(B.xf, xf, tb)) != GB_OK || (s = Put(B.sw, sw, tb)) != GB_OK || (s = Put(B.sw0, sw0, tb)) != GB_OK ||
+        (s = Put(B.vel, vel, tb)) != GB_OK || (s = Put(B.frc, frc, tb)) != GB_OK || (s = Put(B.mas, mas, tb)) != GB_OK ||
+        (s = Put(B.prop, prop, tb)) != GB_OK || (s = Put(B.bi, bi, tb)) != GB_OK || (s = Put(B.bj, bj, tb)) != GB_OK ||
+        (s = Put(B.fi, fi, tf)) != GB_OK || (s = Put(B.fm, fm, tf)) != GB_OK || (s = Put(B.ff, ff, tf)) != GB_OK ||
+        (s = Put(B.faabb, faabb, tf)) != GB_OK || (s = Put(B.shape, shapes, tf)) != GB_OK ||
+        (s = Put(B.fat, fat, tp)) != GB_OK || (s = Put(B.pfix, pfix, tp)) != GB_OK || (s = Put(B.moved, moved, tp)) != GB_OK ||
+        (s = Put(B.ci, ci, tc)) != GB_OK || (s = Put(B.ce, ce, tc)) != GB_OK || (s = Put(B.mh, mh, tc)) != GB_OK ||
+        (s = Put(B.cp, cp, tc)) != GB_OK || (s = Put(B.mv, mv, tc)) != GB_OK || (s = Put(B.mp0, mp0, tc)) != GB_OK ||
+        (s = Put(B.mp1, mp1, tc)) != GB_OK || (s = Put(B.order, order, tc)) != GB_OK ||
+        (s = Put(B.cnext, cnext, tc)) != GB_OK || (s = Put(B.joint, joints, tj)) != GB_OK)
+        return s;
+    GB_CUDA(cudaMemcpy(B.state, states.data(), nw * sizeof(WorldState), cudaMemcpyHostToDevice));
+    // Largest worlds first: with one CTA per world the longest step starts earliest.
+    std::vector<int> schedule(nw);
+    std::iota(schedule.begin(), schedule.end(), 0);
+    std::stable_sort(schedule.begin(), schedule.end(), [&](int a, int b) {
+        return g->desc[a].fixCount > g->desc[b].fixCount;
+    });
+    if ((s = DevAlloc(g, &g->dSchedule, nw)) != GB_OK) return s;
+    GB_CUDA(cudaMemcpy(g->dSchedule, schedule.data(), nw * sizeof(int), cudaMemcpyHostToDevice));
+    g->threads = nw == 1 ? 128 : 64; // StepKernel is compiled for at most 128 threads per CTA
+    g->onDevice = true;
+    g->hostDirty = false;
+    return GB_OK;
+}
+
+gb_status Mutable(gb_world* g, int w)
+{
+    if (!g || w < 0 || w >= (int)g->worlds.size() || g->locked) return GB_ERR_INVALID;
+    if (g->onDevice) {
+        gb_status s = Download(g);
+        if (s != GB_OK) return s;
+    }
+    g->hostDirty = true;
+    return GB_OK;
+}
+
+gb_status CreateBody(HWorld& W, int type, const float* f, int fl, int* id)
+{
+    if (type < 0 || type > 2) return GB_ERR_INVALID;
+    HBody b;
+    b.type = type;
+    b.flags = 0;
+    if (fl & 8) b.flags |= kBBullet;
+    if (fl & 4) b.flags |= kBFixedRot;
+    if (fl & 1) b.flags |= kBAutoSleep;
+    if (fl & 2) b.flags |= kBAwake;
+    if (fl & 16) b.flags |= kBActive;
+    // b2Body::b2Body (Box2D/Dynamics/b2Body.cpp:27-107)
+    b.xf.p = V(f[0], f[1]);
+    b.xf.q = RotOf(f[2]);
+    b.sw.localCenter = V(0.0f, 0.0f);
+    b.sw.c0 = b.xf.p; b.sw.c = b.xf.p;
+    b.sw.a0 = f[2]; b.sw.a = f[2]; b.sw.alpha0 = 0.0f;
+    b.v = V(f[3], f[4]); b.w = f[5];
+    b.linDamp = f[6]; b.angDamp = f[7]; b.gravScale = f[8];
+    if (type == kDynamic) { b.mass = 1.0f; b.invMass = 1.0f; }
+    int idx = (int)W.bodies.size();
+    b.next = W.bodyList;
+    W.bodyList = idx;
+    W.bodies.push_back(b);
+    if (id) *id = idx;
+    return GB_OK;
+}
+
+gb_status CreateFixture(HWorld& W, int body, int type, const float* s, int n, const float* mat, const int* filt, int* id)
+{
+    if (body < 0 || body >= (int)W.bodies.size() || type < 0 || type > 3) return GB_ERR_INVALID;
+    if ((type == 2 && (n < 3 || n > kMaxPolyVerts))) return GB_ERR_INVALID;
+    HFixture fx;
+    fx.body = body;
+    fx.shape = MakeShape(type, s, n);
+    fx.density = mat[0]; fx.friction = mat[1]; fx.restitution = mat[2];
+    fx.category = filt[0] & 0xFFFF; fx.mask = filt[1] & 0xFFFF; fx.group = (int16_t)filt[2]; fx.sensor = filt[3] != 0;
+    int idx = (int)W.fixtures.size();
+    HBody& b = W.bodies[body];
+    if (b.flags & kBActive) {
+        // b2Fixture::CreateProxies (Box2D/Dynamics/b2Fixture.cpp:121-137) + b2DynamicTree::CreateProxy
+        fx.aabb = ComputeAABB(fx.shape, b.xf);
+        float4 fat = make_float4(fx.aabb.x - kAabbExtension, fx.aabb.y - kAabbExtension,
+                                 fx.aabb.z + kAabbExtension, fx.aabb.w + kAabbExtension);
+        fx.proxyId = AllocateProxy(W, fat, idx);
+    }
+    fx.next = b.fixtureList;
+    b.fixtureList = idx;
+    W.fixtures.push_back(fx);
+    if (fx.density > 0.0f) ResetMassData(W, body);
+    W.newFixture = 1;
+    if (id) *id = idx;
+    return GB_OK;
+}
+
+gb_status CreateRevolute(HWorld& W, int a, int b, const float* f, int fl, int* id)
+{
+    int nb = (int)W.bodies.size();
+    if (a < 0 || a >= nb || b < 0 || b >= nb || a == b) return GB_ERR_INVALID;
+    Joint j;
+    std::memset(&j, 0, sizeof(j));
+    j.bodyA = a; j.bodyB = b;
+    j.localAnchorA = V(f[0], f[1]); j.localAnchorB = V(f[2], f[3]);
+    j.referenceAngle = f[4]; j.lowerAngle = f[5]; j.upperAngle = f[6]; j.motorSpeed = f[7]; j.maxMotorTorque = f[8];
+    j.enableLimit = (fl & 1) != 0; j.enableMotor = (fl & 2) != 0; j.collideConnected = (fl & 4) != 0;
+    int idx = (int)W.joints.size();
+    j.prev = kNullIdx;
+    j.next = W.jointList;
+    if (W.jointList != kNullIdx) W.joints[W.jointList].prev = idx;
+    W.jointList = idx;
+    // edge 2*idx on bodyA's joint list, 2*idx+1 on bodyB's (b2World.cpp:212-236)
+    for (int side = 0; side < 2; ++side) {
+        HBody& body = W.bodies[side == 0 ? a : b];
+        int e = 2 * idx + side;
+        j.ePrev[side] = kNullIdx;
+        j.eNext[side] = body.jointList;
+        if (body.jointList != kNullIdx) W.joints[body.jointList >> 1].ePrev[body.jointList & 1] = e;
+        body.jointList = e;
+    }
+    W.joints.push_back(j);
+    // Contacts between the two bodies are flagged for filtering (b2World.cpp:238-250).
+    if (!j.collideConnected && W.hasState) {
+        HContacts& C = W.contacts;
+        for (int e = W.bodies[b].contactList; e != kNullIdx;) {
+            int c = e >> 1;
+            int4 info = C.ci[c];
+            int other = (e & 1) == 0 ? W.fixtures[info.z].body : W.fixtures[info.y].body;
+            if (other == a) C.ci[c].x |= kCFilter;
+            int4 v = C.ce[c];
+            e = (e & 1) ? v.w : v.y;
+        }
+    }
+    if (id) *id = idx;
+    return GB_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+gb_status gb_world_create(int n_worlds, const gb_world_def* defs, gb_world** out)
+{
+    if (!out || n_worlds <= 0 || !defs) return GB_ERR_INVALID;
+    *out = nullptr;
+    gb_world* g = new (std::nothrow) gb_world();
+    if (!g) return GB_ERR_CAPACITY;
+    g->worlds.resize(n_worlds);
+    for (int i = 0; i < n_worlds; ++i) g->worlds[i].def = defs[i];
+    // The stream is created at the first upload, so building a world needs no device.
+    *out = g;
+    return GB_OK;
+}
+
+gb_status gb_world_destroy(gb_world* g)
+{
+    if (!g) return GB_ERR_INVALID;
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    FreeDevice(g);
+    if (g->ownStream && g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+    return GB_OK;
+}
+
+gb_status gb_create_bodies(gb_world* g, int w, int n, const int* type, const float* f, const int* flags, int* out_ids)
+{
+    gb_status s = Mutable(g, w);
+    if (s != GB_OK) return s;
+    for (int i = 0; i < n; ++i)
+        if ((s = CreateBody(g->worlds[w], type[i], f + 9 * i, flags[i], out_ids ? out_ids + i : nullptr)) != GB_OK) return s;
+    return GB_OK;
+}
+
+gb_status gb_create_fixtures(gb_world* g, int w, int n, const int* body, const int* shape_type, const float* shape,
+                             const int* shape_n, const float* mat, const int* filt, int* out_ids)
+{
+    gb_status s = Mutable(g, w);
+    if (s != GB_OK) return s;
+    for (int i = 0; i < n; ++i)
+        if ((s = CreateFixture(g->worlds[w], body[i], shape_type[i], shape + 16 * i, shape_n[i], mat + 3 * i, filt + 4 * i,
+                               out_ids ? out_ids + i : nullptr)) != GB_OK)
+            return s;
+    return GB_OK;
+}
+
+gb_status gb_create_revolute_joints(gb_world* g, int w, int n, const int* a, const int* b, const float* f,
+                                    const int* flags, int* out_ids)
+{
+    gb_status s = Mutable(g, w);
+    if (s != GB_OK) return s;
+    for (int i = 0; i < n; ++i)
+        if ((s = CreateRevolute(g->worlds[w], a[i], b[i], f + 9 * i, flags[i], out_ids ? out_ids + i : nullptr)) != GB_OK)
+            return s;
+    return GB_OK;
+}
+
+gb_status gb_build_world(gb_world* g, int w, int nb, const int* body_type, const float* body_f, const int* body_flags,
+                         int nf, const int* fix_body, const int* fix_type, const float* fix_shape, const int* fix_n,
+                         const float* fix_mat, const int* fix_filt, int nj, const int* joint_a, const int* joint_b,
+                         const float* joint_f, const int* joint_flags)
+{
+    gb_status s = Mutable(g, w);
+    if (s != GB_OK) return s;
+    HWorld& W = g->worlds[w];
+    const int base = (int)W.bodies.size();
+    int fi = 0;
+    for (int b = 0; b < nb; ++b) {
+        if ((s = CreateBody(W, body_type[b], body_f + 9 * b, body_flags[b], nullptr)) != GB_OK) return s;
+        while (fi < nf && fix_body[fi] == b) {
+            if ((s = CreateFixture(W, base + b, fix_type[fi], fix_shape + 16 * fi, fix_n[fi], fix_mat + 3 * fi,
+                                   fix_filt + 4 * fi, nullptr)) != GB_OK)
+                return s;
+            ++fi;
+        }
+    }
+    if (fi != nf) return GB_ERR_INVALID;
+    for (int j = 0; j < nj; ++j)
+        if ((s = CreateRevolute(W, base + joint_a[j], base + joint_b[j], joint_f + 9 * j, joint_flags[j], nullptr)) != GB_OK)
+            return s;
+    return GB_OK;
+}
+
+gb_status gb_world_upload(gb_world* g)
+{
+    if (!g) return GB_ERR_INVALID;
+    return Upload(g);
+}
+
+gb_status gb_world_step(gb_world* g, float dt, int vi, int pi)
+{
+    if (!g || vi < 0 || pi < 0) return GB_ERR_INVALID;
+    gb_status s = Upload(g);
+    if (s != GB_OK) return s;
+    StepParams P;
+    P.dt = dt;
+    P.velocityIterations = vi;
+    P.positionIterations = pi;
+    P.maxToiEvents = 4096;
+    return cudaErr(b2gLaunchStep(g->batch, P, g->dSchedule, g->threads, g->stream));
+}
+
+gb_status gb_world_sync(gb_world* g)
+{
+    if (!g) return GB_ERR_INVALID;
+    if (!g->onDevice) return GB_OK;
+    GB_CUDA(cudaStreamSynchronize(g->stream));
+    const int nw = (int)g->worlds.size();
+    std::vector<WorldState> st(nw);
+    GB_CUDA(cudaMemcpy(st.data(), g->batch.state, nw * sizeof(WorldState), cudaMemcpyDeviceToHost));
+    int err = 0;
+    for (const WorldState& s : st) err |= s.error;
+    if (err & kErrCapacity) return GB_ERR_CAPACITY;
+    if (err & kErrTimeout) return GB_ERR_TIMEOUT;
+    if (err & kErrInvalid) return GB_ERR_INVALID;
+    return GB_OK;
+}
+
+gb_status gb_world_set_stream(gb_world* g, void* stream)
+{
+    if (!g) return GB_ERR_INVALID;
+    if (g->stream) GB_CUDA(cudaStreamSynchronize(g->stream));
+    if (g->ownStream && g->stream) cudaStreamDestroy(g->stream);
+    if (stream) { g->stream = static_cast<cudaStream_t>(stream); g->ownStream = false; }
+    else {
+        GB_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+        g->ownStream = true;
+    }
+    return GB_OK;
+}
+
+gb_status gb_world_counts(gb_world* g, int w, int* bodies, int* fixtures, int* contacts, int* joints)
+{
+    if (!g || w < 0 || w >= (int)g->worlds.size()) return GB_ERR_INVALID;
+    HWorld& W = g->worlds[w];
+    if (bodies) *bodies = (int)W.bodies.size();
+    if (fixtures) *fixtures = (int)W.fixtures.size();
+    if (joints) *joints = (int)W.joints.size();
+    if (contacts) {
+        if (g->onDevice) {
+            GB_CUDA(cudaStreamSynchronize(g->stream));
+            WorldState st;
+            GB_CUDA(cudaMemcpy(&st, g->batch.state + w, sizeof(WorldState), cudaMemcpyDeviceToHost));
+            *contacts = st.contactCount;
+        } else {
+            *contacts = W.hasState ? W.state.contactCount : 0;
+        }
+    }
+    return GB_OK;
+}
+
+gb_status gb_get_bodies(gb_world* g, int w, float* out)
+{
+    if (!g || w < 0 || w >= (int)g->worlds.size() || !out) return GB_ERR_INVALID;
+    HWorld& W = g->worlds[w];
+    const int nb = (int)W.bodies.size();
+    if (g->onDevice) {
+        GB_CUDA(cudaStreamSynchronize(g->stream));
+        const WorldDesc& d = g->desc[w];
+        std::vector<float4> xf(nb), sw(nb), sw0(nb), vel(nb);
+        std::vector<int4> bi(nb);
+        GB_CUDA(cudaMemcpy(xf.data(), g->batch.xf + d.bodyBase, nb * sizeof(float4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(sw.data(), g->batch.sw + d.bodyBase, nb * sizeof(float4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(sw0.data(), g->batch.sw0 + d.bodyBase, nb * sizeof(float4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(vel.data(), g->batch.vel + d.bodyBase, nb * sizeof(float4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(bi.data(), g->batch.bi + d.bodyBase, nb * sizeof(int4), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < nb; ++i) {
+            float* o = out + 12 * i;
+            o[0] = xf[i].x; o[1] = xf[i].y; o[2] = sw[i].z; o[3] = sw[i].x; o[4] = sw[i].y;
+            o[5] = vel[i].x; o[6] = vel[i].y; o[7] = vel[i].z; o[8] = xf[i].z; o[9] = xf[i].w;
+            o[10] = sw0[i].w; o[11] = (bi[i].y & kBAwake) ? 1.0f : 0.0f;
+        }
+    } else {
+        for (int i = 0; i < nb; ++i) {
+            const HBody& b = W.bodies[i];
+            float* o = out + 12 * i;
+            o[0] = b.xf.p.x; o[1] = b.xf.p.y; o[2] = b.sw.a; o[3] = b.sw.c.x; o[4] = b.sw.c.y;
+            o[5] = b.v.x; o[6] = b.v.y; o[7] = b.w; o[8] = b.xf.q.s; o[9] = b.xf.q.c;
+            o[10] = b.sleepTime; o[11] = (b.flags & kBAwake) ? 1.0f : 0.0f;
+        }
+    }
+    return GB_OK;
+}
+
+gb_status gb_get_contacts(gb_world* g, int w, int* ints, float* floats, int cap, int* count)
+{
+    if (!g || w < 0 || w >= (int)g->worlds.size()) return GB_ERR_INVALID;
+    HWorld& W = g->worlds[w];
+    HContacts local;
+    const HContacts* C = &W.contacts;
+    int n = W.hasState ? W.state.contactCount : 0;
+    if (g->onDevice) {
+        GB_CUDA(cudaStreamSynchronize(g->stream));
+        const WorldDesc& d = g->desc[w];
+        WorldState st;
+        GB_CUDA(cudaMemcpy(&st, g->batch.state + w, sizeof(WorldState), cudaMemcpyDeviceToHost));
+        n = st.contactCount;
+        int nc = d.contactCap;
+        local.ci.resize(nc); local.mh.resize(nc); local.mv.resize(nc); local.mp0.resize(nc); local.mp1.resize(nc);
+        local.order.resize(std::max(n, 1));
+        GB_CUDA(cudaMemcpy(local.ci.data(), g->batch.ci + d.contactBase, nc * sizeof(int4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(local.mh.data(), g->batch.mh + d.contactBase, nc * sizeof(int4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(local.mv.data(), g->batch.mv + d.contactBase, nc * sizeof(float4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(local.mp0.data(), g->batch.mp0 + d.contactBase, nc * sizeof(float4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(local.mp1.data(), g->batch.mp1 + d.contactBase, nc * sizeof(float4), cudaMemcpyDeviceToHost));
+        if (n > 0)
+            GB_CUDA(cudaMemcpy(local.order.data(), g->batch.order + d.contactBase, n * sizeof(int), cudaMemcpyDeviceToHost));
+        C = &local;
+    }
+    if (count) *count = n;
+    for (int k = 0; k < n && k < cap; ++k) {
+        int c = C->order[k];
+        int4 info = C->ci[c], h = C->mh[c];
+        float4 v = C->mv[c], p0 = C->mp0[c], p1 = C->mp1[c];
+        bool any = h.y > 0;
+        int* I = ints + 8 * k;
+        float* F = floats + 12 * k;
+        // fixture indices, the b2Contact flags, the toi counter; dead manifold fields zeroed
+        I[0] = info.y; I[1] = info.z; I[2] = info.x; I[3] = h.y; I[4] = any ? h.x : 0;
+        I[5] = h.y > 0 ? h.z : 0; I[6] = h.y > 1 ? h.w : 0;
+        I[7] = info.w;
+        F[0] = any ? v.x : 0.0f; F[1] = any ? v.y : 0.0f; F[2] = any ? v.z : 0.0f; F[3] = any ? v.w : 0.0f;
+        F[4] = h.y > 0 ? p0.x : 0.0f; F[5] = h.y > 0 ? p0.y : 0.0f; F[6] = h.y > 0 ? p0.z : 0.0f; F[7] = h.y > 0 ? p0.w : 0.0f;
+        F[8] = h.y > 1 ? p1.x : 0.0f; F[9] = h.y > 1 ? p1.y : 0.0f; F[10] = h.y > 1 ? p1.z : 0.0f; F[11] = h.y > 1 ? p1.w : 0.0f;
+    }
+    return GB_OK;
+}
+
+gb_status gb_get_proxies(gb_world* g, int w, int* proxy_ids, float* fat_aabbs)
+{
+    if (!g || w < 0 || w >= (int)g->worlds.size()) return GB_ERR_INVALID;
+    HWorld& W = g->worlds[w];
+    std::vector<float4> fat = W.fat;
+    if (g->onDevice) {
+        GB_CUDA(cudaStreamSynchronize(g->stream));
+        const WorldDesc& d = g->desc[w];
+        fat.resize(d.proxyCap);
+        GB_CUDA(cudaMemcpy(fat.data(), g->batch.fat + d.proxyBase, d.proxyCap * sizeof(float4), cudaMemcpyDeviceToHost));
+    }
+    for (size_t i = 0; i < W.fixtures.size(); ++i) {
+        int id = W.fixtures[i].proxyId;
+        if (proxy_ids) proxy_ids[i] = id;
+        if (fat_aabbs && id >= 0) {
+            fat_aabbs[4 * i] = fat[id].x; fat_aabbs[4 * i + 1] = fat[id].y;
+            fat_aabbs[4 * i + 2] = fat[id].z; fat_aabbs[4 * i + 3] = fat[id].w;
+        }
+    }
+    return GB_OK;
+}
+
+gb_status gb_world_stats(gb_world* g, int w, int* islands, int* toi_events)
+{
+    if (!g || w < 0 || w >= (int)g->worlds.size()) return GB_ERR_INVALID;
+    WorldState st = g->worlds[w].state;
+    if (g->onDevice) {
+        GB_CUDA(cudaStreamSynchronize(g->stream));
+        GB_CUDA(cudaMemcpy(&st, g->batch.state + w, sizeof(WorldState), cudaMemcpyDeviceToHost));
+    }
+    if (islands) *islands = st.islands;
+    if (toi_events) *toi_events = st.toiEvents;
+    return GB_OK;
+}
+
+gb_status gb_world_totals(gb_world* g, long long* out)
+{
+    if (!g || !out) return GB_ERR_INVALID;
+    for (int i = 0; i < 8; ++i) out[i] = 0;
+    const int nw = (int)g->worlds.size();
+    std::vector<WorldState> st(nw);
+    if (g->onDevice) {
+        GB_CUDA(cudaStreamSynchronize(g->stream));
+        GB_CUDA(cudaMemcpy(st.data(), g->batch.state, nw * sizeof(WorldState), cudaMemcpyDeviceToHost));
+    } else {
+        for (int i = 0; i < nw; ++i) st[i] = g->worlds[i].state;
+    }
+    for (int i = 0; i < nw; ++i) {
+        const HWorld& W = g->worlds[i];
+        out[0] += st[i].contactCount;
+        out[1] += st[i].solvedBodies;
+        out[2] += st[i].solvedContacts;
+        out[3] += st[i].pairsFound;
+        out[4] += st[i].islands;
+        out[5] += st[i].toiEvents;
+        out[6] += W.proxyCount;
+        for (const HBody& b : W.bodies) out[7] += b.type == kDynamic ? 1 : 0;
+    }
+    return GB_OK;
+}
+
+// Bodies of consecutive worlds are consecutive rows of the body columns (one row of padding only
+// for a world without bodies), so whole-batch transfers are single copies.
+static bool BodyRowsContiguous(const gb_world* g)
+{
+    for (const WorldDesc& d : g->desc)
+        if (d.bodyCount == 0) return false;
+    return true;
+}
+
+gb_status gb_set_forces(gb_world* g, const float* forces)
+{
+    if (!g || !forces) return GB_ERR_INVALID;
+    gb_status s = Upload(g);
+    if (s != GB_OK) return s;
+    if (BodyRowsContiguous(g)) {
+        size_t n = 0;
+        for (const WorldDesc& d : g->desc) n += d.bodyCount;
+        GB_CUDA(cudaMemcpyAsync(g->batch.frc, forces, n * sizeof(float4), cudaMemcpyHostToDevice, g->stream));
+        return GB_OK;
+    }
+    size_t off = 0;
+    for (const WorldDesc& d : g->desc) {
+        if (d.bodyCount > 0)
+            GB_CUDA(cudaMemcpyAsync(g->batch.frc + d.bodyBase, forces + 4 * off, d.bodyCount * sizeof(float4),
+                                    cudaMemcpyHostToDevice, g->stream));
+        off += d.bodyCount;
+    }
+    return GB_OK;
+}
+
+gb_status gb_get_transforms(gb_world* g, float* xf)
+{
+    if (!g || !xf) return GB_ERR_INVALID;
+    gb_status s = Upload(g);
+    if (s != GB_OK) return s;
+    size_t off = 0;
+    if (BodyRowsContiguous(g)) {
+        for (const WorldDesc& d : g->desc) off += d.bodyCount;
+        GB_CUDA(cudaMemcpyAsync(xf, g->batch.xf, off * sizeof(float4), cudaMemcpyDeviceToHost, g->stream));
+    } else {
+        for (const WorldDesc& d : g->desc) {
+            if (d.bodyCount > 0)
+                GB_CUDA(cudaMemcpyAsync(xf + 4 * off, g->batch.xf + d.bodyBase, d.bodyCount * sizeof(float4),
+                                        cudaMemcpyDeviceToHost, g->stream));
+            off += d.bodyCount;
+        }
+    }
+    GB_CUDA(cudaStreamSynchronize(g->stream));
+    return GB_OK;
+}
+
+gb_status gb_sincos(const float* x, float* s, float* c, int n)
+{
+    if (n <= 0) return GB_OK;
+    float *dx = nullptr, *ds = nullptr, *dc = nullptr;
+    GB_CUDA(cudaMalloc(&dx, n * sizeof(float)));
+    GB_CUDA(cudaMalloc(&ds, n * sizeof(float)));
+    GB_CUDA(cudaMalloc(&dc, n * sizeof(float)));
+    cudaError_t e = cudaMemcpy(dx, x, n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = b2gLaunchSinCos(dx, ds, dc, n, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(s, ds, n * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(c, dc, n * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(dx); cudaFree(ds); cudaFree(dc);
+    return cudaErr(e);
+}
+
+gb_status gb_collide(int n, const int* type_a, const float* shape_a, const int* n_a, const float* xf_a,
+                     const int* type_b, const float* shape_b, const int* n_b, const float* xf_b,
+                     int* out_ints, float* out_floats)
+{
+    if (n <= 0) return GB_OK;
+    std::vector<Shape> sa(n), sb(n);
+    std::vector<float4> xa(n), xb(n);
+    for (int i = 0; i < n; ++i) {
+        if (type_a[i] < 0 || type_a[i] > 3 || type_b[i] < 0 || type_b[i] > 3) return GB_ERR_INVALID;
+        sa[i] = MakeShape(type_a[i], shape_a + 16 * i, n_a[i]);
+        sb[i] = MakeShape(type_b[i], shape_b + 16 * i, n_b[i]);
+        if (sa[i].type == kCircle && sb[i].type != kCircle) return GB_ERR_INVALID;
+        if (sa[i].type == kPolygon && sb[i].type == kEdge) return GB_ERR_INVALID;
+        if (sa[i].type == kEdge && sb[i].type == kEdge) return GB_ERR_INVALID;
+        xa[i] = make_float4(xf_a[4 * i], xf_a[4 * i + 1], xf_a[4 * i + 2], xf_a[4 * i + 3]);
+        xb[i] = make_float4(xf_b[4 * i], xf_b[4 * i + 1], xf_b[4 * i + 2], xf_b[4 * i + 3]);
+    }
+    Shape *dsa = nullptr, *dsb = nullptr;
+    float4 *dxa = nullptr, *dxb = nullptr, *dof = nullptr;
+    int4* doi = nullptr;
+    GB_CUDA(cudaMalloc(&dsa, n * sizeof(Shape)));
+    GB_CUDA(cudaMalloc(&dsb, n * sizeof(Shape)));
+    GB_CUDA(cudaMalloc(&dxa, n * sizeof(float4)));
+    GB_CUDA(cudaMalloc(&dxb, n * sizeof(float4)));
+    GB_CUDA(cudaMalloc(&doi, n * sizeof(int4)));
+    GB_CUDA(cudaMalloc(&dof, 3 * n * sizeof(float4)));
+    cudaError_t e = cudaMemcpy(dsa, sa.data(), n * sizeof(Shape), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dsb, sb.data(), n * sizeof(Shape), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dxa, xa.data(), n * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dxb, xb.data(), n * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = b2gLaunchCollide(n, dsa, dxa, dsb, dxb, doi, dof, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(out_ints, doi, n * sizeof(int4), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(out_floats, dof, 3 * n * sizeof(float4), cudaMemcpyDeviceToHost);
+    cudaFree(dsa); cudaFree(dsb); cudaFree(dxa); cudaFree(dxb); cudaFree(doi); cudaFree(dof);
+    return cudaErr(e);
+}
+
+const char* gb_version(void) { return "box2d_gb300 0.1 (Box2D 2.3.2 step semantics, sm_103a)"; }
+
+} // extern "C"

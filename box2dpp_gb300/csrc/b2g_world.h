@@ -1,0 +1,165 @@
+// Device-resident world state for the GB300 Box2D step.
+//
+// A batch holds W independent worlds; one world is a batch of one. Every per-body, per-fixture,
+// per-proxy and per-contact column lives in HBM for the whole run as a structure of arrays of 16-byte
+// vectors (float4/int4), indexed world-locally through the world's base offsets. The host writes it
+// at upload and reads it back on demand; a step never leaves the device.
+#pragma once
+
+#include <cstdint>
+#include <vector_types.h>
+
+#include "b2g_core.h"
+
+namespace b2g {
+
+constexpr int kNullIdx = -1;
+
+// b2Body flags (Dynamics/b2Body.h:409-418)
+enum : int { kBIsland = 0x1, kBAwake = 0x2, kBAutoSleep = 0x4, kBBullet = 0x8, kBFixedRot = 0x10, kBActive = 0x20 };
+// b2Contact flags (Dynamics/Contacts/b2Contact.h:158-177)
+enum : int { kCIsland = 0x1, kCTouching = 0x2, kCEnabled = 0x4, kCFilter = 0x8, kCToi = 0x20 };
+enum BodyType { kStatic = 0, kKinematic = 1, kDynamic = 2 };
+
+// Status words (the C-ABI's gb_status values are the host mirror of these bits).
+enum : int { kErrCapacity = 1, kErrTimeout = 2, kErrInvalid = 4 };
+
+// Per-world sizes and base offsets into the batch columns (immutable during a step).
+struct WorldDesc {
+    int bodyBase, bodyCount;
+    int fixBase, fixCount;
+    int proxyBase, proxyCap;
+    int contactBase, contactCap;
+    int jointBase, jointCount;
+    int pairBase, pairCap;
+    // island rows: a static body is a row of every island it touches, so rows can exceed bodies
+    int rowBase, rowCap;
+};
+
+// Per-world mutable scalars.
+struct WorldState {
+    float gx, gy;
+    float inv_dt0;
+    int bodyList;       // head of the body list (newest body first)
+    int jointList;
+    int contactCount;   // live contacts == length of the contact order list
+    int freeContact;    // head of the contact-slot free list
+    int newFixture;     // b2World::e_newFixture
+    int stepComplete;
+    int allowSleep, warmStarting, continuous, subStepping;
+    int error;          // kErr* bits
+    int toiEvents;      // TOI sub-steps taken in the last step (diagnostic)
+    int islands;        // islands solved in the last step (diagnostic)
+    int solvedBodies;   // non-static island rows solved in the last step
+    int solvedContacts; // island contacts solved in the last step
+    int pairsFound;     // broadphase pairs produced in the last step (all UpdatePairs calls)
+    int pad;
+};
+
+// Revolute joint (Dynamics/Joints/b2RevoluteJoint.h), stored whole: joints are few.
+struct Joint {
+    int bodyA, bodyB;
+    int collideConnected, islandFlag;
+    int prev, next;
+    int ePrev[2], eNext[2];
+    Vec2 localAnchorA, localAnchorB;
+    float referenceAngle, lowerAngle, upperAngle, maxMotorTorque, motorSpeed;
+    int enableLimit, enableMotor;
+    float impulse[3];
+    float motorImpulse;
+    int limitState;
+    int indexA, indexB;
+    Vec2 rA, rB, localCenterA, localCenterB;
+    float invMassA, invMassB, invIA, invIB;
+    float mass[9];
+    float motorMass;
+};
+
+// Island solver records (Dynamics/Contacts/b2ContactSolver.cpp:34-47, b2ContactSolver.h)
+struct VelPoint { Vec2 rA, rB; float normalImpulse, tangentImpulse, normalMass, tangentMass, velocityBias; };
+struct VelConstraint {
+    VelPoint p[2];
+    Vec2 normal;
+    float K[4];          // ex.x, ex.y, ey.x, ey.y
+    float normalMass[4];
+    int indexA, indexB;
+    float invMassA, invMassB, invIA, invIB;
+    float friction, restitution, tangentSpeed;
+    int pointCount, contact;
+};
+struct PosConstraint {
+    Vec2 localPoints[2], localNormal, localPoint;
+    int indexA, indexB;
+    float invMassA, invMassB;
+    Vec2 localCenterA, localCenterB;
+    float invIA, invIB;
+    int type;
+    float radiusA, radiusB;
+    int pointCount;
+};
+struct TOITask { int contact; int kind; float alpha0; Sweep sa, sb; };
+
+// All columns of a batch. Per world, column x of world w starts at x + desc[w].<kind>Base.
+struct Batch {
+    int worlds;
+    WorldDesc* desc;
+    WorldState* state;
+    // bodies
+    float4* xf;    // p.x, p.y, q.s, q.c
+    float4* sw;    // c.x, c.y, a, alpha0
+    float4* sw0;   // c0.x, c0.y, a0, sleepTime
+    float4* vel;   // v.x, v.y, w, 0
+    float4* frc;   // force.x, force.y, torque, 0
+    float4* mas;   // invMass, invI, localCenter.x, localCenter.y
+    float4* prop;  // linearDamping, angularDamping, gravityScale, mass
+    int4* bi;      // type, flags, fixtureList, contactList (edge id = 2*slot + side)
+    int4* bj;      // jointList (edge id = 2*joint + side), bodyNext, islandIndex, wake scratch
+    // fixtures
+    int4* fi;      // body, next, proxyId, isSensor
+    float4* fm;    // friction, restitution, density, radius
+    int4* ff;      // categoryBits, maskBits, groupIndex, 0
+    float4* faabb; // swept AABB last synchronised (b2FixtureProxy::aabb)
+    Shape* shape;
+    // proxies (indexed by proxy id, the reference's tree node id)
+    float4* fat;   // fat AABB
+    int* pfix;     // fixture of the proxy, -1 when free
+    int* moved;    // in the move buffer
+    // contacts (slots)
+    int4* ci;      // flags, fixtureA, fixtureB, toiCount
+    int4* ce;      // ePrev[0], eNext[0], ePrev[1], eNext[1]  (edge 0 on bodyA's list, 1 on bodyB's)
+    float4* cp;    // friction, restitution, tangentSpeed, toi
+    int4* mh;      // manifold type, pointCount, id0, id1
+    float4* mv;    // localNormal.xy, localPoint.xy
+    float4* mp0;   // point 0: localPoint.xy, normalImpulse, tangentImpulse
+    float4* mp1;   // point 1
+    int* order;    // live contacts in world-list order (newest first), length state.contactCount
+    int* cnext;    // free-list link of a free slot
+    // joints
+    Joint* joint;
+    // scratch (per world, same bases)
+    int* sBody;      // row-sized: island bodies
+    int* sStack;     // body-sized: DFS stack / wake positions
+    int* sWake;
+    float4* sPos;    // row-sized island positions c.x, c.y, a
+    float4* sVel;    // row-sized island velocities v.x, v.y, w
+    int* sContact;   // contact-sized: island contact list / collide status / pair keep flags
+    int* sStatus;
+    VelConstraint* vc;
+    PosConstraint* pc;
+    TOITask* toi;
+    int4* islands;   // body-sized: {bodyStart, bodyCount, contactStart, contactCount}
+    int2* islandJ;   // {jointStart, jointCount}
+    int* sJoint;     // joint-sized
+    int* sleepOut;   // per island: 1 when the island fell asleep
+    unsigned long long* pairs; // pair-sized sort keys (proxyA << 32 | proxyB)
+    int* pairKeep;
+    int* movedList;  // proxy-sized
+};
+
+struct StepParams {
+    float dt;
+    int velocityIterations, positionIterations;
+    int maxToiEvents;   // bound on TOI sub-steps per world per step (error bit on overflow)
+};
+
+} // namespace b2g

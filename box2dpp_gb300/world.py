@@ -1,0 +1,146 @@
+"""Python handle over the GB300 step: one ``World`` owns a batch of independent Box2D worlds.
+
+Built from ``scenes.Scene`` descriptions (the calls a b2World user makes), stepped on the GPU through
+the C-ABI, and read back in the same layouts the oracle uses so the two compare directly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .scenes import Scene
+
+
+class World:
+    """A batch of Box2D worlds resident on the GPU (a single world is a batch of one)."""
+
+    def __init__(self, scenes):
+        if isinstance(scenes, Scene):
+            scenes = [scenes]
+        self.lib = _lib.load()
+        self.n_worlds = len(scenes)
+        defs = (_lib.WorldDef * self.n_worlds)()
+        for i, s in enumerate(scenes):
+            defs[i].gravity_x, defs[i].gravity_y = float(s.gravity[0]), float(s.gravity[1])
+            defs[i].allow_sleep, defs[i].warm_starting = int(s.allow_sleep), int(s.warm_starting)
+            defs[i].continuous_physics, defs[i].sub_stepping = int(s.continuous), int(s.sub_stepping)
+        h = C.c_void_p()
+        _lib.check(self.lib.gb_world_create(self.n_worlds, defs, C.byref(h)), "gb_world_create")
+        self.h = h
+        self.n_fixtures = []
+        self.n_bodies = []
+        self.dynamic_bodies = 0
+        for i, s in enumerate(scenes):
+            a = s.arrays()
+            _lib.check(self.lib.gb_build_world(
+                self.h, i, len(a["body_type"]), a["body_type"], a["body_f"], a["body_flags"], len(a["fix_body"]),
+                a["fix_body"], a["fix_type"], a["fix_shape"], a["fix_n"], a["fix_mat"], a["fix_filt"],
+                len(a["joint_a"]), a["joint_a"], a["joint_b"], a["joint_f"], a["joint_flags"]), "gb_build_world")
+            self.n_fixtures.append(len(a["fix_body"]))
+            self.n_bodies.append(len(a["body_type"]))
+            self.dynamic_bodies += int((a["body_type"] == 2).sum())
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.gb_world_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------------ stepping
+    def upload(self) -> None:
+        _lib.check(self.lib.gb_world_upload(self.h), "gb_world_upload")
+
+    def step(self, dt: float = 1.0 / 60.0, vi: int = 8, pi: int = 3) -> None:
+        _lib.check(self.lib.gb_world_step(self.h, dt, vi, pi), "gb_world_step")
+
+    def sync(self) -> None:
+        _lib.check(self.lib.gb_world_sync(self.h), "gb_world_sync")
+
+    def set_stream(self, stream_handle: int) -> None:
+        _lib.check(self.lib.gb_world_set_stream(self.h, C.c_void_p(stream_handle)), "gb_world_set_stream")
+
+    # ------------------------------------------------------------------ read-back
+    def counts(self, w: int = 0):
+        b, f, c, j = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        _lib.check(self.lib.gb_world_counts(self.h, w, C.byref(b), C.byref(f), C.byref(c), C.byref(j)), "gb_world_counts")
+        return b.value, f.value, c.value, j.value
+
+    def bodies(self, w: int = 0) -> np.ndarray:
+        out = np.zeros((max(self.n_bodies[w], 1), 12), dtype=np.float32)
+        _lib.check(self.lib.gb_get_bodies(self.h, w, out), "gb_get_bodies")
+        return out[:self.n_bodies[w]]
+
+    def contacts(self, w: int = 0):
+        n = C.c_int()
+        probe_i, probe_f = np.zeros((1, 8), dtype=np.int32), np.zeros((1, 12), dtype=np.float32)
+        _lib.check(self.lib.gb_get_contacts(self.h, w, probe_i, probe_f, 0, C.byref(n)), "gb_get_contacts")
+        cnt = n.value
+        ints = np.zeros((max(cnt, 1), 8), dtype=np.int32)
+        flts = np.zeros((max(cnt, 1), 12), dtype=np.float32)
+        _lib.check(self.lib.gb_get_contacts(self.h, w, ints, flts, cnt, C.byref(n)), "gb_get_contacts")
+        return ints[:cnt], flts[:cnt]
+
+    def proxies(self, w: int = 0):
+        nf = self.n_fixtures[w]
+        ids = np.zeros(max(nf, 1), dtype=np.int32)
+        fat = np.zeros((max(nf, 1), 4), dtype=np.float32)
+        _lib.check(self.lib.gb_get_proxies(self.h, w, ids, fat), "gb_get_proxies")
+        return ids[:nf], fat[:nf]
+
+    def stats(self, w: int = 0):
+        isl, toi = C.c_int(), C.c_int()
+        _lib.check(self.lib.gb_world_stats(self.h, w, C.byref(isl), C.byref(toi)), "gb_world_stats")
+        return isl.value, toi.value
+
+    def totals(self) -> dict:
+        out = (C.c_longlong * 8)()
+        _lib.check(self.lib.gb_world_totals(self.h, out), "gb_world_totals")
+        keys = ["contacts", "solved_bodies", "solved_contacts", "pairs", "islands", "toi_events", "proxies",
+                "dynamic_bodies"]
+        return dict(zip(keys, list(out)))
+
+    @property
+    def total_bodies(self) -> int:
+        return int(sum(self.n_bodies))
+
+    def set_forces_ptr(self, host_ptr: int) -> None:
+        """Queue an upload of force/torque (float4 per body, all worlds) from a host pointer."""
+        _lib.check(self.lib.gb_set_forces(self.h, C.c_void_p(host_ptr)), "gb_set_forces")
+
+    def get_transforms_ptr(self, host_ptr: int) -> None:
+        """Copy every body transform (float4 per body, all worlds) into a host pointer."""
+        _lib.check(self.lib.gb_get_transforms(self.h, C.c_void_p(host_ptr)), "gb_get_transforms")
+
+    def get_transforms(self) -> np.ndarray:
+        out = np.zeros((self.total_bodies, 4), dtype=np.float32)
+        self.get_transforms_ptr(out.ctypes.data)
+        return out
+
+
+def sincos(x: np.ndarray):
+    """The project sin/cos evaluated on the GPU."""
+    lib = _lib.load()
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    s, c = np.zeros_like(x), np.zeros_like(x)
+    _lib.check(lib.gb_sincos(x, s, c, len(x)), "gb_sincos")
+    return s, c
+
+
+def collide(type_a, shape_a, n_a, xf_a, type_b, shape_b, n_b, xf_b):
+    """Narrowphase on the GPU for arrays of shape pairs (see gb_collide)."""
+    lib = _lib.load()
+    n = len(type_a)
+    f = lambda a, shp, dt: np.ascontiguousarray(np.asarray(a, dtype=dt).reshape(shp))
+    oi = np.zeros((n, 4), dtype=np.int32)
+    of = np.zeros((n, 12), dtype=np.float32)
+    _lib.check(lib.gb_collide(n, f(type_a, n, np.int32), f(shape_a, (n, 16), np.float32), f(n_a, n, np.int32),
+                              f(xf_a, (n, 4), np.float32), f(type_b, n, np.int32), f(shape_b, (n, 16), np.float32),
+                              f(n_b, n, np.int32), f(xf_b, (n, 4), np.float32), oi, of), "gb_collide")
+    return oi, of

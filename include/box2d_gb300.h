@@ -1,0 +1,149 @@
+/*
+ * C-ABI of the GB300 Box2D step (libbox2d_gb300.so).
+ *
+ * The reference Box2D 2.3.2 has no plugin or FFI layer: its boundary is the C++ class API of b2World
+ * (Box2D/Dynamics/b2World.h:43-288) with b2Body, b2Fixture, b2Contact and the listener classes. Each
+ * entry point below replaces the part of that API named in its comment; the C++ mirror in
+ * include/box2d_gb300.hpp (namespace box2d) and the Python package call only these functions.
+ *
+ * Conventions
+ *  - A gb_world handle owns a batch of one or more independent worlds (a single b2World is a batch of
+ *    one). World w of the batch is addressed by its index; bodies, fixtures and joints by their
+ *    creation index within their world, so index order is creation order.
+ *  - Every function returns a gb_status; no function throws or aborts. The library owns all device
+ *    memory; the caller owns every host array it passes and keeps it valid for the call only.
+ *  - Calls on one handle are not thread-safe (as b2World). Different handles are independent.
+ *  - gb_world_step is asynchronous on the handle's CUDA stream; getters and gb_world_sync wait for it.
+ */
+#ifndef BOX2D_GB300_H
+#define BOX2D_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int gb_status;
+#define GB_OK 0
+#define GB_ERR_CAPACITY 1 /* a fixed-capacity device buffer overflowed during a step */
+#define GB_ERR_TIMEOUT 2  /* a bounded device loop (TOI sub-steps) hit its limit */
+#define GB_ERR_INVALID 3  /* bad argument, or a call made while the world is locked */
+#define GB_ERR_CUDA 4     /* a CUDA runtime call failed (no device, launch error, ...) */
+
+typedef struct gb_world gb_world;
+
+/* b2World settings (b2World::b2World(gravity), SetAllowSleeping, SetWarmStarting,
+ * SetContinuousPhysics, SetSubStepping: Box2D/Dynamics/b2World.h:48,145-217). */
+typedef struct gb_world_def {
+    float gravity_x, gravity_y;
+    int allow_sleep;
+    int warm_starting;
+    int continuous_physics;
+    int sub_stepping;
+} gb_world_def;
+
+/* b2World::b2World (Box2D/Dynamics/b2World.cpp:34) for n_worlds independent worlds. */
+gb_status gb_world_create(int n_worlds, const gb_world_def* defs, gb_world** out);
+/* b2World::~b2World (Box2D/Dynamics/b2World.cpp:58) */
+gb_status gb_world_destroy(gb_world* world);
+
+/* b2World::CreateBody (Box2D/Dynamics/b2World.cpp:96). Per body: type (0 static, 1 kinematic,
+ * 2 dynamic); f[9] = position.x, position.y, angle, linearVelocity.x, .y, angularVelocity,
+ * linearDamping, angularDamping, gravityScale; flags: 1 allowSleep, 2 awake, 4 fixedRotation,
+ * 8 bullet, 16 active. out_ids (optional) receives the new body indices. */
+gb_status gb_create_bodies(gb_world* world, int w, int n, const int* type, const float* f, const int* flags,
+                           int* out_ids);
+
+/* b2Body::CreateFixture (Box2D/Dynamics/b2Body.cpp:151). Per fixture: body index; shape type
+ * 0 circle {p.x, p.y, radius}, 1 edge {v1.x, v1.y, v2.x, v2.y, v0.x, v0.y, v3.x, v3.y, hasV0, hasV3},
+ * 2 polygon from n points (b2PolygonShape::Set), 3 box {hx, hy} or, with n == 5, {hx, hy, center.x,
+ * center.y, angle} (b2PolygonShape::SetAsBox); shape[16] per fixture; mat[3] = density, friction,
+ * restitution; filt[4] = categoryBits, maskBits, groupIndex, isSensor. */
+gb_status gb_create_fixtures(gb_world* world, int w, int n, const int* body, const int* shape_type,
+                             const float* shape, const int* shape_n, const float* mat, const int* filt,
+                             int* out_ids);
+
+/* b2World::CreateJoint with a b2RevoluteJointDef (Box2D/Dynamics/b2World.cpp:185,
+ * Box2D/Dynamics/Joints/b2RevoluteJoint.h:36). f[9] = localAnchorA.x, .y, localAnchorB.x, .y,
+ * referenceAngle, lowerAngle, upperAngle, motorSpeed, maxMotorTorque; flags: 1 enableLimit,
+ * 2 enableMotor, 4 collideConnected. */
+gb_status gb_create_revolute_joints(gb_world* world, int w, int n, const int* body_a, const int* body_b,
+                                    const float* f, const int* flags, int* out_ids);
+
+/* Bulk scene build into world w: body b is created, then every fixture whose fix_body == b (the array
+ * is sorted by body), then all joints. Equivalent to the three calls above interleaved. */
+gb_status gb_build_world(gb_world* world, int w, int nb, const int* body_type, const float* body_f,
+                         const int* body_flags, int nf, const int* fix_body, const int* fix_type,
+                         const float* fix_shape, const int* fix_n, const float* fix_mat, const int* fix_filt,
+                         int nj, const int* joint_a, const int* joint_b, const float* joint_f,
+                         const int* joint_flags);
+
+/* Copies host-side changes (new bodies, fixtures, joints) to device memory. gb_world_step does this
+ * implicitly when needed; calling it explicitly moves the upload out of the first step. */
+gb_status gb_world_upload(gb_world* world);
+
+/* b2World::Step (Box2D/Dynamics/b2World.cpp:888): one step of every world of the batch, queued on
+ * the handle's stream. Listener events are recorded on the device when enabled. */
+gb_status gb_world_step(gb_world* world, float dt, int velocity_iterations, int position_iterations);
+
+/* Waits for queued steps and returns the first error any world raised since the last sync. */
+gb_status gb_world_sync(gb_world* world);
+
+/* Binds the handle to a caller-owned cudaStream_t (NULL = the handle's own stream). */
+gb_status gb_world_set_stream(gb_world* world, void* cuda_stream);
+
+/* Counts (b2World::GetBodyCount, GetContactCount, GetProxyCount: b2World.h:160-170). */
+gb_status gb_world_counts(gb_world* world, int w, int* bodies, int* fixtures, int* contacts, int* joints);
+
+/* Body state read-back in creation order, 12 floats per body: transform p.x, p.y, sweep angle a,
+ * world center c.x, c.y, linearVelocity.x, .y, angularVelocity, transform q.s, q.c, sleepTime,
+ * awake (0/1) (b2Body::GetPosition, GetAngle, GetWorldCenter, GetLinearVelocity,
+ * GetAngularVelocity, GetTransform, IsAwake: Box2D/Dynamics/b2Body.h). */
+gb_status gb_get_bodies(gb_world* world, int w, float* out);
+
+/* Contacts of world w in b2World::GetContactList order (b2World.h:124). ints[8] per contact:
+ * fixtureA, fixtureB, flags (b2Contact e_* bits), pointCount, manifold type, id0, id1, toiCount;
+ * floats[12]: localNormal.xy, localPoint.xy, then per point localPoint.xy, normalImpulse,
+ * tangentImpulse (b2Contact::GetManifold). *count receives the number of contacts (may exceed cap). */
+gb_status gb_get_contacts(gb_world* world, int w, int* ints, float* floats, int cap, int* count);
+
+/* Broadphase proxies per fixture: proxy id (b2FixtureProxy::proxyId) and fat AABB
+ * (b2BroadPhase::GetFatAABB, Box2D/Collision/b2BroadPhase.h:107). */
+gb_status gb_get_proxies(gb_world* world, int w, int* proxy_ids, float* fat_aabbs);
+
+/* Per-world diagnostics of the last step: islands solved, TOI sub-steps. */
+gb_status gb_world_stats(gb_world* world, int w, int* islands, int* toi_events);
+
+/* Batch totals over all worlds after the last step, out[8] = live contacts, bodies solved in
+ * islands, contacts solved in islands, broadphase pairs produced, islands, TOI sub-steps, proxies,
+ * dynamic bodies. */
+gb_status gb_world_totals(gb_world* world, long long* out);
+
+/* Whole-batch b2Body::ApplyForceToCenter + ApplyTorque for the next step (Box2D/Dynamics/b2Body.h:
+ * 437-468): forces[4] per body of every world in world order then creation order = force.x,
+ * force.y, torque, unused. The host array is copied to the device asynchronously on the handle's
+ * stream (pinned memory makes it a true async copy); it must stay valid until the next sync. */
+gb_status gb_set_forces(gb_world* world, const float* forces);
+
+/* Whole-batch b2Body::GetTransform (Box2D/Dynamics/b2Body.h:180): xf[4] per body of every world in
+ * world order then creation order = p.x, p.y, q.s, q.c. Waits for queued steps. */
+gb_status gb_get_transforms(gb_world* world, float* xf);
+
+/* The project sin/cos used for every b2Rot (b2Rot::Set, Box2D/Common/b2Math.h:305-312) evaluated on
+ * the device for n inputs (host arrays). */
+gb_status gb_sincos(const float* x, float* s, float* c, int n);
+
+/* Narrowphase on the device for n shape pairs (b2Collide*, Box2D/Collision/b2Collision.h:170-200):
+ * shapes in the gb_create_fixtures encoding, transforms xf[4] = p.x, p.y, q.s, q.c. Output per pair
+ * as gb_get_contacts without the first three ints (ints[4]: type, pointCount, id0, id1). */
+gb_status gb_collide(int n, const int* type_a, const float* shape_a, const int* n_a, const float* xf_a,
+                     const int* type_b, const float* shape_b, const int* n_b, const float* xf_b,
+                     int* out_ints, float* out_floats);
+
+/* Library version string. */
+const char* gb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BOX2D_GB300_H */

@@ -181,7 +181,8 @@ int po_collide(int typeA, const float* sA, int nA, const float* xfA, int typeB, 
     else if (a.type == kEdge && b.type == kCircle) CollideEdgeAndCircle(&m, a, xa, b, xb);
     else if (a.type == kEdge && polyB) CollideEdgeAndPolygon(&m, a, xa, b, xb);
     else return -1;
-    oi[0] = m.type; oi[1] = m.pointCount;
+    oi[0] = m.pointCount > 0 ? m.type : 0; // type is left unset when the shapes do not touch
+    oi[1] = m.pointCount;
     oi[2] = m.pointCount > 0 ? (int)m.points[0].id : 0;
     oi[3] = m.pointCount > 1 ? (int)m.points[1].id : 0;
     of[0] = m.pointCount > 0 ? m.localNormal.x : 0.0f; of[1] = m.pointCount > 0 ? m.localNormal.y : 0.0f;

@@ -1,0 +1,190 @@
+"""Generate the golden vectors under tests/golden/ from the UNMODIFIED reference (box2dref compiled by
+oracle/Makefile from the reference tree). Run where the reference tree exists:
+
+    python tests/golden/make_golden.py
+
+Two builds of the reference are used: ``libm`` (glibc sinf/cosf, the reference as shipped) and
+``project`` (the same objects with sinf/cosf/sincosf resolved to the project trig). Fixtures:
+
+* ``<case>_<trig>.npz``: for a scene stepped N times, the SHA-256 of every step's full state
+  (bodies 12 x float32 + contacts 8 x int32 + 12 x float32 in world-list order, as dumped by the
+  C-ABIs) and the full body/contact arrays at a few checkpoint steps.
+* ``collide.npz``: seeded shape pairs of every supported type pair with the reference manifolds.
+* ``toi.npz``: seeded sweeps with the reference b2TimeOfImpact result.
+* ``trig.npz``: glibc sinf/cosf on seeded angles (how far the project trig is from libm).
+"""
+from __future__ import annotations
+
+import hashlib
+import math
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
+
+import oracle  # noqa: E402
+from box2dpp_gb300 import scenes  # noqa: E402
+
+DT, VI, PI = 1.0 / 60.0, 8, 3
+
+
+def state_digest(bodies: np.ndarray, ints: np.ndarray, flts: np.ndarray) -> bytes:
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(bodies, dtype=np.float32).tobytes())
+    h.update(np.ascontiguousarray(ints, dtype=np.int32).tobytes())
+    h.update(np.ascontiguousarray(flts, dtype=np.float32).tobytes())
+    return h.digest()
+
+
+_BATCH = []
+
+
+def batch_world(i: int):
+    """World i of the 24-world batched sample (seed 9)."""
+    if not _BATCH:
+        _BATCH.extend(scenes.config3(24, seed=9))
+    return _BATCH[i]
+
+
+def cases():
+    """Named trajectory cases: (name, scene factory, steps, checkpoints)."""
+    return [
+        ("pyramid20", lambda: scenes.config1(), 600, [1, 10, 60, 120, 300, 600]),
+        ("drop300", lambda: scenes.drop(300, scenes.SplitMix64(7)), 300, [1, 30, 100, 300]),
+        ("drop1000_nosleep", lambda: scenes.drop(1000, scenes.SplitMix64(21), allow_sleep=False), 120, [1, 60, 120]),
+        ("stacks120", lambda: scenes.stacks(120, scenes.SplitMix64(5)), 300, [1, 150, 300]),
+        ("chains6x16", lambda: chains_with_load(), 300, [1, 100, 300]),
+    ] + [(f"batch{i}", (lambda i=i: batch_world(i)), 200, [200]) for i in range(24)]
+
+
+def chains_with_load():
+    """Joint chains with loose bodies falling onto them (contacts and joints in one island)."""
+    rng = scenes.SplitMix64(3)
+    s = scenes.chains(6, 16, rng)
+    for k in range(24):
+        x = -8.0 + 0.7 * k
+        b = s.body(scenes.DYNAMIC, x, 22.0 + 0.3 * (k % 5))
+        if k % 2:
+            s.fixture(b, scenes.CIRCLE, [0.0, 0.0, 0.3], density=1.0, friction=0.4)
+        else:
+            s.fixture(b, scenes.BOX, [0.25, 0.25], 2, density=1.0, friction=0.4)
+    return s
+
+
+def run_case(scene, steps, checkpoints, kind, trig):
+    w = oracle.OracleWorld(scene, kind, trig)
+    digests = np.zeros((steps, 32), dtype=np.uint8)
+    cps = {}
+    for s in range(1, steps + 1):
+        w.step(DT, VI, PI)
+        b = w.bodies()
+        ci, cf = w.contacts()
+        digests[s - 1] = np.frombuffer(state_digest(b, ci, cf), dtype=np.uint8)
+        if s in checkpoints:
+            cps[f"bodies_{s}"] = b
+            cps[f"cints_{s}"] = ci
+            cps[f"cflts_{s}"] = cf
+    return digests, cps
+
+
+def random_shape(rng: scenes.SplitMix64, kind: int):
+    """A shape in the C-ABI encoding: (type, shape list, n)."""
+    if kind == 0:
+        return 0, [rng.uniform(-0.3, 0.3), rng.uniform(-0.3, 0.3), rng.uniform(0.2, 1.0)], 0
+    if kind == 1:
+        x1, y1 = rng.uniform(-3, 3), rng.uniform(-1, 1)
+        x2, y2 = rng.uniform(-3, 3), rng.uniform(-1, 1)
+        has0, has3 = rng.randint(0, 1), rng.randint(0, 1)
+        return 1, [x1, y1, x2, y2, x1 - rng.uniform(0.5, 2), y1 + rng.uniform(-1, 1), x2 + rng.uniform(0.5, 2),
+                   y2 + rng.uniform(-1, 1), has0, has3], 0
+    if kind == 2:
+        k = rng.randint(3, 8)
+        r = rng.uniform(0.3, 1.2)
+        pts = []
+        for i in range(k):
+            a = 2 * math.pi * (i + rng.uniform(-0.3, 0.3)) / k
+            pts += [round(r * math.cos(a) * 1048576) / 1048576, round(r * math.sin(a) * 1048576) / 1048576]
+        return 2, pts, k
+    return 3, [rng.uniform(0.2, 1.0), rng.uniform(0.2, 1.0)], 2
+
+
+def xf_of(rng: scenes.SplitMix64, spread: float):
+    a = rng.uniform(-math.pi, math.pi)
+    s, c = oracle.sincosf("reference", "libm", a)
+    return [rng.uniform(-spread, spread), rng.uniform(-spread, spread), s, c]
+
+
+def make_collide(n: int = 4000):
+    rng = scenes.SplitMix64(2024)
+    pairs = [(0, 0), (2, 0), (3, 0), (2, 2), (3, 3), (2, 3), (1, 0), (1, 2), (1, 3)]
+    ta, sa, na, xa, tb, sb, nb, xb, oi, of = [], [], [], [], [], [], [], [], [], []
+    for k in range(n):
+        ka, kb = pairs[k % len(pairs)]
+        t1, s1, n1 = random_shape(rng, ka)
+        t2, s2, n2 = random_shape(rng, kb)
+        x1 = xf_of(rng, 0.2 if ka != 1 else 0.0)
+        x2 = xf_of(rng, 1.2)
+        i, f = oracle.collide("reference", "libm", t1, s1, n1, x1, t2, s2, n2, x2)
+        pad = lambda s: list(s) + [0.0] * (16 - len(s))
+        ta.append(t1); sa.append(pad(s1)); na.append(n1); xa.append(x1)
+        tb.append(t2); sb.append(pad(s2)); nb.append(n2); xb.append(x2)
+        oi.append(i); of.append(f)
+    np.savez_compressed(os.path.join(HERE, "collide.npz"),
+                        type_a=np.array(ta, np.int32), shape_a=np.array(sa, np.float32), n_a=np.array(na, np.int32),
+                        xf_a=np.array(xa, np.float32), type_b=np.array(tb, np.int32), shape_b=np.array(sb, np.float32),
+                        n_b=np.array(nb, np.int32), xf_b=np.array(xb, np.float32), out_ints=np.array(oi, np.int32),
+                        out_floats=np.array(of, np.float32))
+
+
+def make_toi(n: int = 1500):
+    rng = scenes.SplitMix64(77)
+    rows, outs = [], []
+    for k in range(n):
+        ta, sa, na = random_shape(rng, [0, 2, 3][k % 3])
+        tb, sb, nb = random_shape(rng, [0, 2, 3][(k // 3) % 3])
+        c0 = [rng.uniform(-0.5, 0.5), rng.uniform(2.0, 4.0)]
+        c = [c0[0] + rng.uniform(-1, 1), c0[1] - rng.uniform(1.0, 5.0)]
+        swa = [0.0, 0.0, c0[0], c0[1], c[0], c[1], rng.uniform(-1, 1), rng.uniform(-2, 2), 0.0]
+        swb = [0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0]
+        st, t = oracle.toi("reference", "project", ta, sa, na, swa, tb, sb, nb, swb)
+        pad = lambda s: list(s) + [0.0] * (16 - len(s))
+        rows.append((ta, pad(sa), na, swa, tb, pad(sb), nb, swb))
+        outs.append((st, t))
+    np.savez_compressed(os.path.join(HERE, "toi.npz"),
+                        type_a=np.array([r[0] for r in rows], np.int32), shape_a=np.array([r[1] for r in rows], np.float32),
+                        n_a=np.array([r[2] for r in rows], np.int32), sweep_a=np.array([r[3] for r in rows], np.float32),
+                        type_b=np.array([r[4] for r in rows], np.int32), shape_b=np.array([r[5] for r in rows], np.float32),
+                        n_b=np.array([r[6] for r in rows], np.int32), sweep_b=np.array([r[7] for r in rows], np.float32),
+                        state=np.array([o[0] for o in outs], np.int32), t=np.array([o[1] for o in outs], np.float32))
+
+
+def make_trig(n: int = 200000):
+    rng = np.random.default_rng(5)
+    x = np.concatenate([rng.uniform(-4, 4, n // 2), rng.uniform(-1e-3, 1e-3, n // 4),
+                        rng.uniform(-200, 200, n // 4)]).astype(np.float32)
+    s = np.zeros_like(x)
+    c = np.zeros_like(x)
+    for i, v in enumerate(x):
+        s[i], c[i] = oracle.sincosf("reference", "libm", float(v))
+    np.savez_compressed(os.path.join(HERE, "trig.npz"), x=x, sin=s, cos=c)
+
+
+def main():
+    oracle.build_reference()
+    for name, make, steps, cps in cases():
+        for trig in ("libm", "project"):
+            digests, snap = run_case(make(), steps, cps, "reference", trig)
+            np.savez_compressed(os.path.join(HERE, f"{name}_{trig}.npz"), digests=digests,
+                                checkpoints=np.array(cps, np.int32), steps=np.int32(steps), **snap)
+        print("wrote", name)
+    make_collide()
+    make_toi()
+    make_trig()
+    print("done")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,93 @@
+"""The CPU oracle restatement against golden vectors generated from the unmodified reference.
+
+Bit-exact: with glibc's sinf/cosf the restatement must reproduce the reference as shipped, and with
+the project trig it must reproduce the reference linked against the project trig, step by step."""
+import numpy as np
+import pytest
+
+import oracle
+from tests._util import golden, trajectory_cases, first_divergence
+
+CASES = trajectory_cases()
+
+
+@pytest.mark.parametrize("trig", ["project", "libm"])
+@pytest.mark.parametrize("name,make,steps", CASES, ids=[c[0] for c in CASES])
+def test_port_matches_reference_trajectory(name, make, steps, trig):
+    g = golden(f"{name}_{trig}")
+    w = oracle.OracleWorld(make(), "port", trig)
+    bad = first_divergence(w, steps, g["digests"])
+    if trig == "libm" and bad is not None:
+        # glibc's sinf differs between libc builds (x86-64 FMA variant vs others); the bit-exact
+        # claim for libm mode holds where the golden vectors were made.
+        import platform
+        if platform.machine() != "x86_64":
+            pytest.skip(f"libm trig differs on {platform.machine()} (first divergence at step {bad})")
+    assert bad is None, f"{name}/{trig}: first divergence at step {bad}"
+
+
+def test_port_checkpoints_exact():
+    g = golden("pyramid20_project")
+    w = oracle.OracleWorld(trajectory_cases()[0][1](), "port", "project")
+    for s in range(1, 61):
+        w.step()
+        if s in (1, 10, 60):
+            b = w.bodies()
+            ci, cf = w.contacts()
+            assert np.array_equal(b, g[f"bodies_{s}"])
+            assert np.array_equal(ci, g[f"cints_{s}"])
+            assert np.array_equal(cf.view(np.uint32), g[f"cflts_{s}"].view(np.uint32))
+
+
+def test_port_collide_matches_reference():
+    g = golden("collide")
+    n = len(g["type_a"])
+    mism = 0
+    for k in range(n):
+        oi, of = oracle.collide("port", "project", int(g["type_a"][k]), g["shape_a"][k], int(g["n_a"][k]), g["xf_a"][k],
+                                int(g["type_b"][k]), g["shape_b"][k], int(g["n_b"][k]), g["xf_b"][k])
+        if not (np.array_equal(oi, g["out_ints"][k]) and np.array_equal(of.view(np.uint32), g["out_floats"][k].view(np.uint32))):
+            mism += 1
+    assert mism == 0, f"{mism}/{n} manifolds differ"
+    # every supported type pair is exercised and a good share of the cases collide
+    assert (g["out_ints"][:, 1] > 0).mean() > 0.2
+
+
+def test_port_toi_matches_reference():
+    g = golden("toi")
+    n = len(g["state"])
+    for k in range(n):
+        st, t = oracle.toi("port", "project", int(g["type_a"][k]), g["shape_a"][k], int(g["n_a"][k]), g["sweep_a"][k],
+                           int(g["type_b"][k]), g["shape_b"][k], int(g["n_b"][k]), g["sweep_b"][k])
+        assert st == int(g["state"][k]) and np.float32(t) == g["t"][k], k
+    states = set(g["state"].tolist())
+    assert {3, 4} <= states  # touching and separated outcomes both covered
+
+
+def test_project_trig_close_to_glibc():
+    """The project sin/cos is within 1 ulp of glibc's and equal to it on the vast majority of inputs."""
+    g = golden("trig")
+    x = g["x"]
+    s = np.zeros_like(x)
+    c = np.zeros_like(x)
+    for i in range(0, len(x), 7):
+        s[i], c[i] = oracle.sincosf("port", "project", float(x[i]))
+    idx = np.arange(0, len(x), 7)
+    ds = np.abs(s[idx].view(np.int32).astype(np.int64) - g["sin"][idx].view(np.int32).astype(np.int64))
+    dc = np.abs(c[idx].view(np.int32).astype(np.int64) - g["cos"][idx].view(np.int32).astype(np.int64))
+    assert ds.max() <= 1 and dc.max() <= 1
+    assert (ds == 0).mean() > 0.95 and (dc == 0).mean() > 0.95
+
+
+def test_project_trig_nearly_correctly_rounded():
+    """Against long-double evaluation: misrounded results must be very rare."""
+    rng = np.random.default_rng(0)
+    x = np.concatenate([rng.uniform(-8, 8, 20000), rng.uniform(-1e-4, 1e-4, 2000)]).astype(np.float32)
+    xs = np.longdouble(x)
+    ref_s = np.sin(xs).astype(np.float32)
+    ref_c = np.cos(xs).astype(np.float32)
+    bad = 0
+    for i, v in enumerate(x):
+        s, c = oracle.sincosf("port", "project", float(v))
+        bad += (np.float32(s) != ref_s[i]) + (np.float32(c) != ref_c[i])
+    assert bad <= 2
