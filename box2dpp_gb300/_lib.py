@@ -20,7 +20,7 @@ EXPORTS = [
     "gb_world_create", "gb_world_destroy", "gb_create_bodies", "gb_create_fixtures", "gb_create_revolute_joints",
     "gb_build_world", "gb_world_upload", "gb_world_step", "gb_world_sync", "gb_world_set_stream",
     "gb_world_counts", "gb_get_bodies", "gb_get_contacts", "gb_get_proxies", "gb_world_stats", "gb_sincos",
-    "gb_collide", "gb_version", "gb_world_totals", "gb_set_forces", "gb_get_transforms",
+    "gb_collide", "gb_version", "gb_world_totals", "gb_set_forces", "gb_get_transforms", "gb_world_profile",
 ]
 
 
@@ -77,6 +77,7 @@ def load(build_if_missing: bool = True):
         "gb_world_totals": [vp, C.POINTER(C.c_longlong)],
         "gb_set_forces": [vp, vp],
         "gb_get_transforms": [vp, vp],
+        "gb_world_profile": [vp, np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

@@ -332,7 +332,7 @@ gb_status Upload(gb_world* g)
     ALLOC(joint, tj); ALLOC(sJoint, tj);
     ALLOC(sBody, tr); ALLOC(sStack, tb); ALLOC(sWake, tb); ALLOC(sPos, tr); ALLOC(sVel, tr); ALLOC(islands, tb);
     ALLOC(islandJ, tb); ALLOC(sleepOut, tb);
-    ALLOC(sContact, tc); ALLOC(sStatus, tc); ALLOC(vc, tc); ALLOC(pc, tc); ALLOC(toi, tc);
+    ALLOC(sContact, tc); ALLOC(sStatus, tc); ALLOC(vc, tc); ALLOC(pc, tc); ALLOC(vimp, tc); ALLOC(toi, tc);
     ALLOC(pairs, tq); ALLOC(pairKeep, tq);
 #undef ALLOC
     GB_CUDA(cudaMemcpy(B.desc, g->desc.data(), nw * sizeof(WorldDesc), cudaMemcpyHostToDevice));
@@ -828,6 +828,22 @@ gb_status gb_world_totals(gb_world* g, long long* out)
         out[6] += W.proxyCount;
         for (const HBody& b : W.bodies) out[7] += b.type == kDynamic ? 1 : 0;
     }
+    return GB_OK;
+}
+
+gb_status gb_world_profile(gb_world* g, unsigned long long* out)
+{
+    if (!g || !out) return GB_ERR_INVALID;
+    const int nw = (int)g->worlds.size();
+    std::vector<WorldState> st(nw);
+    if (g->onDevice) {
+        GB_CUDA(cudaStreamSynchronize(g->stream));
+        GB_CUDA(cudaMemcpy(st.data(), g->batch.state, nw * sizeof(WorldState), cudaMemcpyDeviceToHost));
+    } else {
+        for (int i = 0; i < nw; ++i) st[i] = g->worlds[i].state;
+    }
+    for (int i = 0; i < nw; ++i)
+        for (int k = 0; k < 16; ++k) out[16 * i + k] = st[i].cyc[k];
     return GB_OK;
 }
 

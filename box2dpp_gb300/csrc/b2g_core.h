@@ -11,6 +11,8 @@
 #include <cstdint>
 #include <vector_types.h>
 
+#include "b2g_trig_table.h"
+
 #ifdef __CUDACC__
 #define B2G_HD __host__ __device__ __forceinline__
 #define B2G_HDNI static __host__ __device__ __noinline__
@@ -47,52 +49,87 @@ constexpr float kLinearSleepTolerance = 0.01f;
 constexpr float kAngularSleepTolerance = 2.0f / 180.0f * kPi;
 
 // ------------------------------------------------------------------ project sin/cos
-// One deterministic float sin/cos evaluated identically on every device and host: Cody-Waite
-// reduction by pi/2 = P1 + P2 + P3 (P1, P2 with 26 significant bits so k*P1, k*P2 are exact for
-// |k| < 2^27), Taylor polynomials of sin/cos on |r| <= pi/4 (to r^17 / r^18) in Horner form with
-// separately rounded double multiplies and adds, quadrant select, one rounding to float. Error before
-// the final rounding is ~2^-51 relative, so results are the correctly rounded ones except with
-// probability ~2^-26 per call. |x| >= 2^27 is first reduced by an exact fmod with the double 2*pi.
-B2G_HD void SinCos(float xf, float* s_out, float* c_out)
+// One deterministic float sin/cos evaluated identically on every device and host, in float
+// arithmetic only (GB300's FP64 is far slower than FP32):
+//   1. k = rint(x * 256/pi); r = x - k*pi/256 as a float-float pair (rh, rl): pi/256 = C1 + C2 + C3,
+//      the products k*C1 and k*C2 made exact with fused multiply-adds, the differences with TwoSum.
+//   2. sin r = r + r^3(-1/6 + r^2/120) and cos r = 1 - r^2/2 + r^4/24 as float-float pairs
+//      (|r| <= pi/512, so the corrections are ~1e-6 relative and float precision suffices for them).
+//   3. sin x = S_j cos r + C_j sin r, cos x = C_j cos r - S_j sin r with float-float table values at
+//      j = k mod 512, exact products by fused multiply-add, one final rounding to float.
+// Within ~2^-41 of the exact value before the last rounding: the correctly rounded float except for
+// about one input in 10^5. The only fused operations are the explicit fmaf calls (the build disables
+// contraction everywhere else), so host and device round identically.
+#ifdef __CUDACC__
+static __device__ const float kTrigTableDev[512 * 4] = {B2G_TRIG_TABLE_ROWS};
+#endif
+static const float kTrigTableHost[512 * 4] = {B2G_TRIG_TABLE_ROWS};
+
+B2G_HD const float* TrigTable()
 {
-    if (xf == 0.0f) { *s_out = xf; *c_out = 1.0f; return; }
-    if (!(fabsf(xf) <= FLT_MAX)) { *s_out = xf - xf; *c_out = xf - xf; return; }
-    const double kTwoOverPi = 0x1.45f306dc9c883p-1;
-    const double kP1 = 0x1.921fb50000000p+0, kP2 = 0x1.110b460000000p-26, kP3 = 0x1.1a62633145c07p-54;
-    double x = (double)xf;
-    if (fabs(x) >= 134217728.0) x = fmod(x, 0x1.921fb54442d18p+2);
-    double k = rint(x * kTwoOverPi);
-    double r = x - k * kP1;
-    r = r - k * kP2;
-    r = r - k * kP3;
-    double r2 = r * r;
-    double ps = 0x1.952c77030ad4ap-49;
-    ps = ps * r2 + -0x1.ae7f3e733b81fp-41;
-    ps = ps * r2 + 0x1.6124613a86d09p-33;
-    ps = ps * r2 + -0x1.ae64567f544e4p-26;
-    ps = ps * r2 + 0x1.71de3a556c734p-19;
-    ps = ps * r2 + -0x1.a01a01a01a01ap-13;
-    ps = ps * r2 + 0x1.1111111111111p-7;
-    ps = ps * r2 + -0x1.5555555555555p-3;
-    double sn = r + (r * r2) * ps;
-    double pc = -0x1.6827863b97d97p-53;
-    pc = pc * r2 + 0x1.ae7f3e733b81fp-45;
-    pc = pc * r2 + -0x1.93974a8c07c9dp-37;
-    pc = pc * r2 + 0x1.1eed8eff8d898p-29;
-    pc = pc * r2 + -0x1.27e4fb7789f5cp-22;
-    pc = pc * r2 + 0x1.a01a01a01a01ap-16;
-    pc = pc * r2 + -0x1.6c16c16c16c17p-10;
-    pc = pc * r2 + 0x1.5555555555555p-5;
-    pc = pc * r2 + -0.5;
-    double cs = 1.0 + r2 * pc;
-    long long q = (long long)k & 3;
-    double s, c;
-    if (q == 0) { s = sn; c = cs; }
-    else if (q == 1) { s = cs; c = -sn; }
-    else if (q == 2) { s = -sn; c = -cs; }
-    else { s = -cs; c = sn; }
-    *s_out = (float)s;
-    *c_out = (float)c;
+#ifdef __CUDA_ARCH__
+    return kTrigTableDev;
+#else
+    return kTrigTableHost;
+#endif
+}
+
+B2G_HD void SinCos(float x, float* s_out, float* c_out)
+{
+    if (x == 0.0f) { *s_out = x; *c_out = 1.0f; return; }
+    if (!(fabsf(x) <= FLT_MAX)) { *s_out = x - x; *c_out = x - x; return; }
+    const float kf = rintf(x * B2G_INV_PIO256);
+    const int idx = fabsf(kf) < 16777216.0f ? ((int)kf) & 511 : ((int)fmodf(kf, 512.0f)) & 511;
+    // r = x - k*pi/256 in float-float
+    const float p = kf * B2G_PIO256_1;
+    const float pe = fmaf(kf, B2G_PIO256_1, -p);
+    const float t = x - p;
+    const float q = kf * B2G_PIO256_2;
+    const float qe = fmaf(kf, B2G_PIO256_2, -q);
+    const float s1 = t - pe;
+    const float b1 = s1 - t;
+    const float s1e = (t - (s1 - b1)) + (-pe - b1);
+    const float s2 = s1 - q;
+    const float b2 = s2 - s1;
+    const float s2e = (s1 - (s2 - b2)) + (-q - b2);
+    const float lo = ((s1e + s2e) - qe) - kf * B2G_PIO256_3;
+    const float rh = s2 + lo;
+    const float rl = lo - (rh - s2);
+    // sin r, cos r
+    const float r2 = rh * rh;
+    const float ts = (rh * r2) * (-0x1.555556p-3f + 0x1.111112p-7f * r2);
+    const float sh = rh;
+    const float sl = rl + ts;
+    const float pl = fmaf(rh, rh, -r2);
+    const float uh = 0.5f * r2;
+    const float ul = 0.5f * pl + rh * rl;
+    const float w = (r2 * r2) * 0x1.555556p-5f;
+    const float ch = 1.0f - uh;
+    const float b3 = ch - 1.0f;
+    const float che = (1.0f - (ch - b3)) + (-uh - b3);
+    const float cl = che + (w - ul);
+    // table
+    const float* T = TrigTable() + 4 * idx;
+    const float Sh = T[0], Sl = T[1], Ch = T[2], Cl = T[3];
+    // sin x = S cos r + C sin r
+    const float a1 = Sh * ch;
+    const float a1l = fmaf(Sh, ch, -a1) + (Sh * cl + Sl * ch);
+    const float a2 = Ch * sh;
+    const float a2l = fmaf(Ch, sh, -a2) + (Ch * sl + Cl * sh);
+    const float sa = a1 + a2;
+    const float b4 = sa - a1;
+    const float sae = (a1 - (sa - b4)) + (a2 - b4);
+    // cos x = C cos r - S sin r
+    const float c1 = Ch * ch;
+    const float c1l = fmaf(Ch, ch, -c1) + (Ch * cl + Cl * ch);
+    const float P = Sh * sh;
+    const float c2 = -P;
+    const float c2l = -fmaf(Sh, sh, -P) - (Sh * sl + Sl * sh);
+    const float ca = c1 + c2;
+    const float b5 = ca - c1;
+    const float cae = (c1 - (ca - b5)) + (c2 - b5);
+    *s_out = sa + ((sae + a1l) + a2l);
+    *c_out = ca + ((cae + c1l) + c2l);
 }
 
 // ------------------------------------------------------------------ vectors (Common/b2Math.h)

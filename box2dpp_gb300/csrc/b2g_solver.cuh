@@ -1,0 +1,680 @@
+// Contact solver, revolute joint and island solve of the GB300 Box2D step (included by b2g_step.cu
+// inside namespace b2g, after the world view Wd). Per-contact building blocks follow b2ContactSolver
+// (Dynamics/Contacts/b2ContactSolver.cpp) and b2RevoluteJoint (Dynamics/Joints/b2RevoluteJoint.cpp)
+// operation for operation. Island body rows (position, velocity) and the accumulated impulses are
+// staged in shared memory when the world's islands fit; the read-only constraint records stay in
+// global memory, are read with 128-bit loads, and the sequential sweeps prefetch the next record into
+// L1 while solving the current one.
+#pragma once
+
+__device__ inline void PrefetchL1(const void* p)
+{
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+template <typename T> __device__ inline void PrefetchRecord(const T* p)
+{
+    const char* c = reinterpret_cast<const char*>(p);
+    for (int off = 0; off < (int)sizeof(T); off += 128) PrefetchL1(c + off);
+}
+
+// b2ContactSolver::b2ContactSolver, one contact (b2ContactSolver.cpp:61-139). v.idx.x / v.idx.y
+// (body rows) are set when the island is built.
+__device__ void ContactSetup(const Wd& W, VelConstraint& v, PosConstraint& p, float4& imp, int c, bool warmStarting,
+                             float dtRatio)
+{
+    int4 info = W.ci[c];
+    int fA = info.y, fB = info.z;
+    int bA = W.fixBody(fA), bB = W.fixBody(fB);
+    float4 mA = W.mas[bA], mB = W.mas[bB];
+    float4 pp = W.cp[c];
+    int4 h = W.mh[c];
+    float4 mvv = W.mv[c], p0 = W.mp0[c], p1 = W.mp1[c];
+    const int rowA = v.idx.x, rowB = v.idx.y;
+    v.nf = make_float4(0.0f, 0.0f, pp.x, pp.z);
+    v.m = make_float4(mA.x, mA.y, mB.x, mB.y);
+    v.idx = make_int4(rowA, rowB, h.y, c);
+    v.K = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    v.NM = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    v.r0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    v.r1 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    v.c0 = make_float4(0.0f, 0.0f, 0.0f, pp.y);
+    v.c1 = make_float4(0.0f, 0.0f, 0.0f, pp.y);
+    if (warmStarting) {
+        imp = make_float4(dtRatio * p0.z, dtRatio * p0.w, h.y > 1 ? dtRatio * p1.z : 0.0f, h.y > 1 ? dtRatio * p1.w : 0.0f);
+    } else {
+        imp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    p.lp = make_float4(p0.x, p0.y, h.y > 1 ? p1.x : 0.0f, h.y > 1 ? p1.y : 0.0f);
+    p.ln = mvv;
+    p.idx = make_int4(rowA, rowB, h.y, h.x);
+    p.m = make_float4(mA.x, mA.y, mB.x, mB.y);
+    p.lc = make_float4(mA.z, mA.w, mB.z, mB.w);
+    p.rad = make_float4(W.fm[fA].w, W.fm[fB].w, 0.0f, 0.0f);
+}
+
+// b2ContactSolver::InitializeVelocityConstraints, one contact (b2ContactSolver.cpp:143-252)
+__device__ void ContactInitVelocity(const Wd& W, VelConstraint& v, const PosConstraint& p, const float4* pos,
+                                    const float4* vel)
+{
+    Manifold m;
+    W.loadManifold(v.idx.w, m);
+    const float mA = v.m.x, iA = v.m.y, mB = v.m.z, iB = v.m.w;
+    const float restitution = v.c0.w;
+    float4 pa = pos[v.idx.x], pb = pos[v.idx.y];
+    float4 va = vel[v.idx.x], vb = vel[v.idx.y];
+    Vec2 cA = V(pa.x, pa.y), cB = V(pb.x, pb.y);
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    Xf xfA, xfB;
+    xfA.q = RotOf(pa.z);
+    xfB.q = RotOf(pb.z);
+    xfA.p = cA - Mul(xfA.q, V(p.lc.x, p.lc.y));
+    xfB.p = cB - Mul(xfB.q, V(p.lc.z, p.lc.w));
+    WorldManifold wm;
+    WorldManifoldInit(&wm, m, xfA, p.rad.x, xfB, p.rad.y);
+    const Vec2 normal = wm.normal;
+    v.nf.x = normal.x;
+    v.nf.y = normal.y;
+    const int pointCount = v.idx.z;
+    Vec2 rA[2], rB[2];
+    for (int j = 0; j < pointCount; ++j) {
+        rA[j] = wm.pts[j] - cA;
+        rB[j] = wm.pts[j] - cB;
+        float rnA = Cross(rA[j], normal), rnB = Cross(rB[j], normal);
+        float kNormal = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
+        float normalMass = kNormal > 0.0f ? 1.0f / kNormal : 0.0f;
+        Vec2 tangent = Cross(normal, 1.0f);
+        float rtA = Cross(rA[j], tangent), rtB = Cross(rB[j], tangent);
+        float kTangent = mA + mB + iA * rtA * rtA + iB * rtB * rtB;
+        float tangentMass = kTangent > 0.0f ? 1.0f / kTangent : 0.0f;
+        float velocityBias = 0.0f;
+        float vRel = Dot(normal, vB + Cross(wB, rB[j]) - vA - Cross(wA, rA[j]));
+        if (vRel < -kVelocityThreshold) velocityBias = -restitution * vRel;
+        float4 r4 = make_float4(rA[j].x, rA[j].y, rB[j].x, rB[j].y);
+        float4 c4 = make_float4(normalMass, tangentMass, velocityBias, restitution);
+        if (j == 0) { v.r0 = r4; v.c0 = c4; } else { v.r1 = r4; v.c1 = c4; }
+    }
+    if (pointCount == 2) {
+        float rn1A = Cross(rA[0], normal), rn1B = Cross(rB[0], normal);
+        float rn2A = Cross(rA[1], normal), rn2B = Cross(rB[1], normal);
+        float k11 = mA + mB + iA * rn1A * rn1A + iB * rn1B * rn1B;
+        float k22 = mA + mB + iA * rn2A * rn2A + iB * rn2B * rn2B;
+        float k12 = mA + mB + iA * rn1A * rn2A + iB * rn1B * rn2B;
+        const float k_maxConditionNumber = 1000.0f;
+        if (k11 * k11 < k_maxConditionNumber * (k11 * k22 - k12 * k12)) {
+            v.K = make_float4(k11, k12, k12, k22);
+            // b2Mat22::GetInverse (Common/b2Math.h:185-197): a = ex.x, b = ey.x, c = ex.y, d = ey.y
+            float a = k11, b = k12, cc = k12, dd = k22;
+            float det = a * dd - b * cc;
+            if (det != 0.0f) det = 1.0f / det;
+            v.NM = make_float4(det * dd, -det * cc, -det * b, det * a);
+        } else {
+            v.idx.z = 1;
+        }
+    }
+}
+
+// b2ContactSolver::WarmStart, one contact (b2ContactSolver.cpp:254-292)
+__device__ void ContactWarmStart(const VelConstraint& v, const float4 imp, float4* vel)
+{
+    float4 va = vel[v.idx.x], vb = vel[v.idx.y];
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    Vec2 normal = V(v.nf.x, v.nf.y), tangent = Cross(normal, 1.0f);
+    for (int j = 0; j < v.idx.z; ++j) {
+        float4 r = j == 0 ? v.r0 : v.r1;
+        float ni = j == 0 ? imp.x : imp.z, ti = j == 0 ? imp.y : imp.w;
+        Vec2 P = ni * normal + ti * tangent;
+        wA -= v.m.y * Cross(V(r.x, r.y), P);
+        vA = vA - v.m.x * P;
+        wB += v.m.w * Cross(V(r.z, r.w), P);
+        vB = vB + v.m.z * P;
+    }
+    vel[v.idx.x] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[v.idx.y] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
+__device__ inline Vec2 MulM4(float4 A, Vec2 v) { return V(A.x * v.x + A.z * v.y, A.y * v.x + A.w * v.y); }
+
+// b2ContactSolver::SolveVelocityConstraints, one contact (b2ContactSolver.cpp:294-605): friction
+// per point, then the normal constraint, one point or the 2-point block LCP by total enumeration.
+__device__ __forceinline__ void ContactSolveVelocity(const VelConstraint& v, float4& imp, float4* vel)
+{
+    const float mA = v.m.x, iA = v.m.y, mB = v.m.z, iB = v.m.w;
+    const int ia = v.idx.x, ib = v.idx.y, pointCount = v.idx.z;
+    float4 va = vel[ia], vb = vel[ib];
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const Vec2 normal = V(v.nf.x, v.nf.y), tangent = Cross(normal, 1.0f);
+    const float friction = v.nf.z, tangentSpeed = v.nf.w;
+    const Vec2 rA0 = V(v.r0.x, v.r0.y), rB0 = V(v.r0.z, v.r0.w);
+    const Vec2 rA1 = V(v.r1.x, v.r1.y), rB1 = V(v.r1.z, v.r1.w);
+    float ni0 = imp.x, ti0 = imp.y, ni1 = imp.z, ti1 = imp.w;
+    // friction, point 0 then point 1
+    for (int j = 0; j < pointCount; ++j) {
+        const Vec2 rA = j == 0 ? rA0 : rA1, rB = j == 0 ? rB0 : rB1;
+        const float tangentMass = j == 0 ? v.c0.y : v.c1.y;
+        const float normalImpulse = j == 0 ? ni0 : ni1;
+        const float tangentImpulse = j == 0 ? ti0 : ti1;
+        Vec2 dv = vB + Cross(wB, rB) - vA - Cross(wA, rA);
+        float vt = Dot(dv, tangent) - tangentSpeed;
+        float lambda = tangentMass * (-vt);
+        float maxFriction = friction * normalImpulse;
+        float newImpulse = Clampf(tangentImpulse + lambda, -maxFriction, maxFriction);
+        lambda = newImpulse - tangentImpulse;
+        if (j == 0) ti0 = newImpulse; else ti1 = newImpulse;
+        Vec2 P = lambda * tangent;
+        vA = vA - mA * P;
+        wA -= iA * Cross(rA, P);
+        vB = vB + mB * P;
+        wB += iB * Cross(rB, P);
+    }
+    if (pointCount == 1) {
+        Vec2 dv = vB + Cross(wB, rB0) - vA - Cross(wA, rA0);
+        float vn = Dot(dv, normal);
+        float lambda = -v.c0.x * (vn - v.c0.z);
+        float newImpulse = Maxf(ni0 + lambda, 0.0f);
+        lambda = newImpulse - ni0;
+        ni0 = newImpulse;
+        Vec2 P = lambda * normal;
+        vA = vA - mA * P;
+        wA -= iA * Cross(rA0, P);
+        vB = vB + mB * P;
+        wB += iB * Cross(rB0, P);
+    } else {
+        Vec2 a = V(ni0, ni1);
+        Vec2 dv1 = vB + Cross(wB, rB0) - vA - Cross(wA, rA0);
+        Vec2 dv2 = vB + Cross(wB, rB1) - vA - Cross(wA, rA1);
+        float vn1 = Dot(dv1, normal), vn2 = Dot(dv2, normal);
+        Vec2 b;
+        b.x = vn1 - v.c0.z;
+        b.y = vn2 - v.c1.z;
+        b = b - MulM4(v.K, a);
+        Vec2 x = -MulM4(v.NM, b);
+        bool solved = x.x >= 0.0f && x.y >= 0.0f;
+        if (!solved) {
+            x.x = -v.c0.x * b.x;
+            x.y = 0.0f;
+            vn2 = v.K.y * x.x + b.y;
+            solved = x.x >= 0.0f && vn2 >= 0.0f;
+        }
+        if (!solved) {
+            x.x = 0.0f;
+            x.y = -v.c1.x * b.y;
+            vn1 = v.K.z * x.y + b.x;
+            solved = x.y >= 0.0f && vn1 >= 0.0f;
+        }
+        if (!solved) {
+            x.x = 0.0f;
+            x.y = 0.0f;
+            vn1 = b.x;
+            vn2 = b.y;
+            solved = vn1 >= 0.0f && vn2 >= 0.0f;
+        }
+        if (solved) {
+            Vec2 dd = x - a;
+            Vec2 P1 = dd.x * normal, P2 = dd.y * normal;
+            vA = vA - mA * (P1 + P2);
+            wA -= iA * (Cross(rA0, P1) + Cross(rA1, P2));
+            vB = vB + mB * (P1 + P2);
+            wB += iB * (Cross(rB0, P1) + Cross(rB1, P2));
+            ni0 = x.x;
+            ni1 = x.y;
+        }
+    }
+    imp = make_float4(ni0, ti0, ni1, ti1);
+    vel[ia] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[ib] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
+// b2ContactSolver::StoreImpulses, one contact (b2ContactSolver.cpp:607-620)
+__device__ void ContactStore(Wd& W, const VelConstraint& v, const float4 imp)
+{
+    const int c = v.idx.w;
+    if (v.idx.z > 0) { W.mp0[c].z = imp.x; W.mp0[c].w = imp.y; }
+    if (v.idx.z > 1) { W.mp1[c].z = imp.z; W.mp1[c].w = imp.w; }
+}
+
+// b2ContactSolver::SolvePositionConstraints (b2ContactSolver.cpp:674-751) and
+// SolveTOIPositionConstraints (:753-836) for one contact, with b2PositionSolverManifold (:623-672).
+__device__ __forceinline__ void ContactSolvePosition(const PosConstraint& p, float4* pos, bool toi, int toiA, int toiB,
+                                                     float& minSeparation)
+{
+    const int ia = p.idx.x, ib = p.idx.y, pointCount = p.idx.z, type = p.idx.w;
+    float mA, iA, mB, iB;
+    if (!toi) { mA = p.m.x; iA = p.m.y; mB = p.m.z; iB = p.m.w; }
+    else {
+        mA = 0.0f; iA = 0.0f; mB = 0.0f; iB = 0.0f;
+        if (ia == toiA || ia == toiB) { mA = p.m.x; iA = p.m.y; }
+        if (ib == toiA || ib == toiB) { mB = p.m.z; iB = p.m.w; }
+    }
+    const Vec2 localCenterA = V(p.lc.x, p.lc.y), localCenterB = V(p.lc.z, p.lc.w);
+    const Vec2 localNormal = V(p.ln.x, p.ln.y), localPoint = V(p.ln.z, p.ln.w);
+    const float radiusA = p.rad.x, radiusB = p.rad.y;
+    float4 pa = pos[ia], pb = pos[ib];
+    Vec2 cA = V(pa.x, pa.y), cB = V(pb.x, pb.y);
+    float aA = pa.z, aB = pb.z;
+    for (int j = 0; j < pointCount; ++j) {
+        Xf xfA, xfB;
+        xfA.q = RotOf(aA);
+        xfB.q = RotOf(aB);
+        xfA.p = cA - Mul(xfA.q, localCenterA);
+        xfB.p = cB - Mul(xfB.q, localCenterB);
+        const Vec2 lpj = j == 0 ? V(p.lp.x, p.lp.y) : V(p.lp.z, p.lp.w);
+        Vec2 normal, point;
+        float separation;
+        if (type == kCircles) {
+            Vec2 pA = Mul(xfA, localPoint), pB = Mul(xfB, V(p.lp.x, p.lp.y));
+            normal = pB - pA;
+            Normalize(normal);
+            point = 0.5f * (pA + pB);
+            separation = Dot(pB - pA, normal) - radiusA - radiusB;
+        } else if (type == kFaceA) {
+            normal = Mul(xfA.q, localNormal);
+            Vec2 plane = Mul(xfA, localPoint);
+            Vec2 clip = Mul(xfB, lpj);
+            separation = Dot(clip - plane, normal) - radiusA - radiusB;
+            point = clip;
+        } else {
+            normal = Mul(xfB.q, localNormal);
+            Vec2 plane = Mul(xfB, localPoint);
+            Vec2 clip = Mul(xfA, lpj);
+            separation = Dot(clip - plane, normal) - radiusA - radiusB;
+            point = clip;
+            normal = -normal;
+        }
+        Vec2 rA = point - cA, rB = point - cB;
+        minSeparation = Minf(minSeparation, separation);
+        float C = toi ? Clampf(kToiBaumgarte * (separation + kLinearSlop), -kMaxLinearCorrection, 0.0f)
+                      : Clampf(kBaumgarte * (separation + kLinearSlop), -kMaxLinearCorrection, 0.0f);
+        float rnA = Cross(rA, normal), rnB = Cross(rB, normal);
+        float K = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
+        float impulse = K > 0.0f ? -C / K : 0.0f;
+        Vec2 P = impulse * normal;
+        cA = cA - mA * P;
+        aA -= iA * Cross(rA, P);
+        cB = cB + mB * P;
+        aB += iB * Cross(rB, P);
+    }
+    pos[ia] = make_float4(cA.x, cA.y, aA, 0.0f);
+    pos[ib] = make_float4(cB.x, cB.y, aB, 0.0f);
+}
+
+// Sequential sweeps over one island's constraints [lo, hi), prefetching the next record.
+__device__ void SweepVelocity(const VelConstraint* vc, float4* imp, int lo, int hi, float4* vel)
+{
+    for (int i = lo; i < hi; ++i) {
+        if (i + 1 < hi) PrefetchRecord(vc + i + 1);
+        const VelConstraint v = vc[i];
+        float4 im = imp[i];
+        ContactSolveVelocity(v, im, vel);
+        imp[i] = im;
+    }
+}
+__device__ bool SweepPosition(const PosConstraint* pc, int lo, int hi, float4* pos, bool toi, int toiA, int toiB)
+{
+    float minSeparation = 0.0f;
+    for (int i = lo; i < hi; ++i) {
+        if (i + 1 < hi) PrefetchRecord(pc + i + 1);
+        const PosConstraint p = pc[i];
+        ContactSolvePosition(p, pos, toi, toiA, toiB, minSeparation);
+    }
+    return toi ? minSeparation >= -1.5f * kLinearSlop : minSeparation >= -3.0f * kLinearSlop;
+}
+
+// ------------------------------------------------------------------ revolute joint
+// b2RevoluteJoint (Dynamics/Joints/b2RevoluteJoint.cpp:66-380); pos/vel rows are indexA/indexB,
+// set when the island is built.
+__device__ void RevInit(const Wd& W, Joint& j, float4* pos, float4* vel, bool warmStarting, float dtRatio)
+{
+    int A = j.bodyA, B = j.bodyB;
+    float4 mA4 = W.mas[A], mB4 = W.mas[B];
+    j.localCenterA = V(mA4.z, mA4.w); j.localCenterB = V(mB4.z, mB4.w);
+    j.invMassA = mA4.x; j.invMassB = mB4.x; j.invIA = mA4.y; j.invIB = mB4.y;
+    float aA = pos[j.indexA].z, aB = pos[j.indexB].z;
+    float4 va = vel[j.indexA], vb = vel[j.indexB];
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    Rot qA = RotOf(aA), qB = RotOf(aB);
+    j.rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    j.rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    bool fixedRotation = (iA + iB == 0.0f);
+    float* M = j.mass;
+    M[0] = mA + mB + j.rA.y * j.rA.y * iA + j.rB.y * j.rB.y * iB;
+    M[3] = -j.rA.y * j.rA.x * iA - j.rB.y * j.rB.x * iB;
+    M[6] = -j.rA.y * iA - j.rB.y * iB;
+    M[1] = M[3];
+    M[4] = mA + mB + j.rA.x * j.rA.x * iA + j.rB.x * j.rB.x * iB;
+    M[7] = j.rA.x * iA + j.rB.x * iB;
+    M[2] = M[6];
+    M[5] = M[7];
+    M[8] = iA + iB;
+    j.motorMass = iA + iB;
+    if (j.motorMass > 0.0f) j.motorMass = 1.0f / j.motorMass;
+    if (!j.enableMotor || fixedRotation) j.motorImpulse = 0.0f;
+    if (j.enableLimit && !fixedRotation) {
+        float jointAngle = aB - aA - j.referenceAngle;
+        if (Absf(j.upperAngle - j.lowerAngle) < 2.0f * kAngularSlop) j.limitState = 3;
+        else if (jointAngle <= j.lowerAngle) {
+            if (j.limitState != 1) j.impulse[2] = 0.0f;
+            j.limitState = 1;
+        } else if (jointAngle >= j.upperAngle) {
+            if (j.limitState != 2) j.impulse[2] = 0.0f;
+            j.limitState = 2;
+        } else {
+            j.limitState = 0;
+            j.impulse[2] = 0.0f;
+        }
+    } else {
+        j.limitState = 0;
+    }
+    if (warmStarting) {
+        j.impulse[0] *= dtRatio; j.impulse[1] *= dtRatio; j.impulse[2] *= dtRatio;
+        j.motorImpulse *= dtRatio;
+        Vec2 P = V(j.impulse[0], j.impulse[1]);
+        vA = vA - mA * P;
+        wA -= iA * (Cross(j.rA, P) + j.motorImpulse + j.impulse[2]);
+        vB = vB + mB * P;
+        wB += iB * (Cross(j.rB, P) + j.motorImpulse + j.impulse[2]);
+    } else {
+        j.impulse[0] = j.impulse[1] = j.impulse[2] = 0.0f;
+        j.motorImpulse = 0.0f;
+    }
+    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
+// b2Mat33::Solve33 / Solve22 (Common/b2Math.cpp:24-56), columns ex = M[0..2], ey = M[3..5], ez = M[6..8]
+__device__ inline void Solve33(const float* M, const float* b, float* x)
+{
+    float t[3];
+    t[0] = M[4] * M[8] - M[5] * M[7]; t[1] = M[5] * M[6] - M[3] * M[8]; t[2] = M[3] * M[7] - M[4] * M[6];
+    float det = M[0] * t[0] + M[1] * t[1] + M[2] * t[2];
+    if (det != 0.0f) det = 1.0f / det;
+    x[0] = det * (b[0] * t[0] + b[1] * t[1] + b[2] * t[2]);
+    t[0] = b[1] * M[8] - b[2] * M[7]; t[1] = b[2] * M[6] - b[0] * M[8]; t[2] = b[0] * M[7] - b[1] * M[6];
+    x[1] = det * (M[0] * t[0] + M[1] * t[1] + M[2] * t[2]);
+    t[0] = M[4] * b[2] - M[5] * b[1]; t[1] = M[5] * b[0] - M[3] * b[2]; t[2] = M[3] * b[1] - M[4] * b[0];
+    x[2] = det * (M[0] * t[0] + M[1] * t[1] + M[2] * t[2]);
+}
+__device__ inline Vec2 Solve22(const float* M, Vec2 b)
+{
+    float a11 = M[0], a12 = M[3], a21 = M[1], a22 = M[4];
+    float det = a11 * a22 - a12 * a21;
+    if (det != 0.0f) det = 1.0f / det;
+    return V(det * (a22 * b.x - a12 * b.y), det * (a11 * b.y - a21 * b.x));
+}
+
+__device__ void RevSolveVelocity(Joint& j, float4* vel, float dt)
+{
+    float4 va = vel[j.indexA], vb = vel[j.indexB];
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    bool fixedRotation = (iA + iB == 0.0f);
+    if (j.enableMotor && j.limitState != 3 && !fixedRotation) {
+        float Cdot = wB - wA - j.motorSpeed;
+        float impulse = -j.motorMass * Cdot;
+        float oldImpulse = j.motorImpulse;
+        float maxImpulse = dt * j.maxMotorTorque;
+        j.motorImpulse = Clampf(j.motorImpulse + impulse, -maxImpulse, maxImpulse);
+        impulse = j.motorImpulse - oldImpulse;
+        wA -= iA * impulse;
+        wB += iB * impulse;
+    }
+    if (j.enableLimit && j.limitState != 0 && !fixedRotation) {
+        Vec2 Cdot1 = vB + Cross(wB, j.rB) - vA - Cross(wA, j.rA);
+        float Cdot2 = wB - wA;
+        float Cd[3] = {Cdot1.x, Cdot1.y, Cdot2};
+        float imp[3];
+        Solve33(j.mass, Cd, imp);
+        imp[0] = -imp[0]; imp[1] = -imp[1]; imp[2] = -imp[2];
+        if (j.limitState == 3) {
+            j.impulse[0] += imp[0]; j.impulse[1] += imp[1]; j.impulse[2] += imp[2];
+        } else {
+            float newImpulse = j.impulse[2] + imp[2];
+            bool clampIt = j.limitState == 1 ? newImpulse < 0.0f : newImpulse > 0.0f;
+            if (clampIt) {
+                Vec2 rhs = -Cdot1 + j.impulse[2] * V(j.mass[6], j.mass[7]);
+                Vec2 reduced = Solve22(j.mass, rhs);
+                imp[0] = reduced.x; imp[1] = reduced.y; imp[2] = -j.impulse[2];
+                j.impulse[0] += reduced.x; j.impulse[1] += reduced.y; j.impulse[2] = 0.0f;
+            } else {
+                j.impulse[0] += imp[0]; j.impulse[1] += imp[1]; j.impulse[2] += imp[2];
+            }
+        }
+        Vec2 P = V(imp[0], imp[1]);
+        vA = vA - mA * P;
+        wA -= iA * (Cross(j.rA, P) + imp[2]);
+        vB = vB + mB * P;
+        wB += iB * (Cross(j.rB, P) + imp[2]);
+    } else {
+        Vec2 Cdot = vB + Cross(wB, j.rB) - vA - Cross(wA, j.rA);
+        Vec2 impulse = Solve22(j.mass, -Cdot);
+        j.impulse[0] += impulse.x;
+        j.impulse[1] += impulse.y;
+        vA = vA - mA * impulse;
+        wA -= iA * Cross(j.rA, impulse);
+        vB = vB + mB * impulse;
+        wB += iB * Cross(j.rB, impulse);
+    }
+    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
+__device__ bool RevSolvePosition(Joint& j, float4* pos)
+{
+    float4 pa = pos[j.indexA], pb = pos[j.indexB];
+    Vec2 cA = V(pa.x, pa.y), cB = V(pb.x, pb.y);
+    float aA = pa.z, aB = pb.z;
+    float angularError = 0.0f, positionError = 0.0f;
+    bool fixedRotation = (j.invIA + j.invIB == 0.0f);
+    if (j.enableLimit && j.limitState != 0 && !fixedRotation) {
+        float angle = aB - aA - j.referenceAngle;
+        float limitImpulse = 0.0f;
+        if (j.limitState == 3) {
+            float C = Clampf(angle - j.lowerAngle, -kMaxAngularCorrection, kMaxAngularCorrection);
+            limitImpulse = -j.motorMass * C;
+            angularError = Absf(C);
+        } else if (j.limitState == 1) {
+            float C = angle - j.lowerAngle;
+            angularError = -C;
+            C = Clampf(C + kAngularSlop, -kMaxAngularCorrection, 0.0f);
+            limitImpulse = -j.motorMass * C;
+        } else if (j.limitState == 2) {
+            float C = angle - j.upperAngle;
+            angularError = C;
+            C = Clampf(C - kAngularSlop, 0.0f, kMaxAngularCorrection);
+            limitImpulse = -j.motorMass * C;
+        }
+        aA -= j.invIA * limitImpulse;
+        aB += j.invIB * limitImpulse;
+    }
+    {
+        Rot qA = RotOf(aA), qB = RotOf(aB);
+        Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
+        Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
+        Vec2 C = cB + rB - cA - rA;
+        positionError = Length(C);
+        float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+        float K[9] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        K[0] = mA + mB + iA * rA.y * rA.y + iB * rB.y * rB.y;
+        K[1] = -iA * rA.x * rA.y - iB * rB.x * rB.y;
+        K[3] = K[1];
+        K[4] = mA + mB + iA * rA.x * rA.x + iB * rB.x * rB.x;
+        Vec2 impulse = -Solve22(K, C);
+        cA = cA - mA * impulse;
+        aA -= iA * Cross(rA, impulse);
+        cB = cB + mB * impulse;
+        aB += iB * Cross(rB, impulse);
+    }
+    pos[j.indexA] = make_float4(cA.x, cA.y, aA, 0.0f);
+    pos[j.indexB] = make_float4(cB.x, cB.y, aB, 0.0f);
+    return positionError <= kLinearSlop && angularError <= kAngularSlop;
+}
+
+
+// b2Island::Solve velocity/position integration clamps (Dynamics/b2Island.cpp:263-296, 442-470)
+__device__ inline void IntegratePosition(float4& p4, float4& v4, float h)
+{
+    Vec2 c = V(p4.x, p4.y), v = V(v4.x, v4.y);
+    float a = p4.z, w = v4.z;
+    Vec2 translation = h * v;
+    if (Dot(translation, translation) > kMaxTranslationSquared) {
+        float ratio = kMaxTranslation / Length(translation);
+        v.x *= ratio;
+        v.y *= ratio;
+    }
+    float rotation = h * w;
+    if (rotation * rotation > kMaxRotationSquared) {
+        float ratio = kMaxRotation / Absf(rotation);
+        w *= ratio;
+    }
+    c = c + h * v;
+    a += h * w;
+    p4 = make_float4(c.x, c.y, a, 0.0f);
+    v4 = make_float4(v.x, v.y, w, 0.0f);
+}
+
+// ------------------------------------------------------------------ island solve
+// b2Island::Solve (Dynamics/b2Island.cpp:185-384) for all islands of the world at once. Per-body and
+// per-contact work that the reference does in independent loops (integration, constraint setup and
+// initialisation, impulse storage, write-back) is spread over the CTA; the order-dependent work (warm
+// start, velocity and position sweeps, joints, sleep) runs per island on one thread.
+__device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int nContacts, float4* smem, int smemRows,
+                                 int smemContacts)
+{
+    unsigned long long tStamp = clock64();
+    const float h = P.dt;
+    const float dtRatio = st->inv_dt0 * P.dt;
+    const bool warm = st->warmStarting != 0;
+    const float gx = st->gx, gy = st->gy;
+    const bool rowsInSmem = nRows <= smemRows;
+    float4* pos = rowsInSmem ? smem : sPos;
+    float4* vel = rowsInSmem ? smem + smemRows : sVel;
+    float4* imp = nContacts <= smemContacts ? smem + 2 * smemRows : vimp;
+    // velocity integration (b2Island.cpp:190-222); c0 = c, a0 = a for every island body
+    for (int r = tid(); r < nRows; r += nthreads()) {
+        int b = sBody[r];
+        float4 s = sw[b];
+        float4 v4 = vel_body(b);
+        Vec2 v = V(v4.x, v4.y);
+        float w = v4.z;
+        if (type(b) == kDynamic) {
+            float4 m = mas[b], pr = prop[b], f = frc[b];
+            Vec2 g = pr.z * V(gx, gy);
+            v = v + h * (g + m.x * V(f.x, f.y));
+            w += h * m.y * f.z;
+            v = (1.0f / (1.0f + h * pr.x)) * v;
+            w *= 1.0f / (1.0f + h * pr.y);
+        }
+        pos[r] = make_float4(s.x, s.y, s.z, 0.0f);
+        vel[r] = make_float4(v.x, v.y, w, 0.0f);
+        sw0[b] = make_float4(s.x, s.y, s.z, sw0[b].w);
+    }
+    __syncthreads();
+    // constraint setup and initialisation, every island contact in parallel
+    for (int i = tid(); i < nContacts; i += nthreads()) {
+        VelConstraint v;
+        v.idx = vc[i].idx;
+        PosConstraint p;
+        float4 im;
+        ContactSetup(*this, v, p, im, sContact[i], warm, dtRatio);
+        ContactInitVelocity(*this, v, p, pos, vel);
+        vc[i] = v;
+        pc[i] = p;
+        imp[i] = im;
+    }
+    __syncthreads();
+    if (tid() == 0) { unsigned long long now = clock64(); st->cyc[8] = now - tStamp; tStamp = now; }
+    // order-dependent velocity phase per island
+    for (int isl = tid(); isl < nIsl; isl += nthreads()) {
+        int4 I = islands[isl];
+        int2 J = islandJ[isl];
+        const int lo = I.z, hi = I.z + I.w;
+        if (warm)
+            for (int i = lo; i < hi; ++i) ContactWarmStart(vc[i], imp[i], vel);
+        for (int k = 0; k < J.y; ++k) RevInit(*this, jt[sJoint[J.x + k]], pos, vel, warm, dtRatio);
+        for (int it = 0; it < P.velocityIterations; ++it) {
+            for (int k = 0; k < J.y; ++k) RevSolveVelocity(jt[sJoint[J.x + k]], vel, h);
+            SweepVelocity(vc, imp, lo, hi, vel);
+        }
+    }
+    __syncthreads();
+    if (tid() == 0) { unsigned long long now = clock64(); st->cyc[9] = now - tStamp; tStamp = now; }
+    // impulses back to the manifolds, positions integrated, both in parallel
+    for (int i = tid(); i < nContacts; i += nthreads()) ContactStore(*this, vc[i], imp[i]);
+    for (int r = tid(); r < nRows; r += nthreads()) {
+        float4 p4 = pos[r], v4 = vel[r];
+        IntegratePosition(p4, v4, h);
+        pos[r] = p4;
+        vel[r] = v4;
+    }
+    __syncthreads();
+    if (tid() == 0) { unsigned long long now = clock64(); st->cyc[10] = now - tStamp; tStamp = now; }
+    // order-dependent position phase per island
+    for (int isl = tid(); isl < nIsl; isl += nthreads()) {
+        int4 I = islands[isl];
+        int2 J = islandJ[isl];
+        bool positionSolved = false;
+        for (int it = 0; it < P.positionIterations; ++it) {
+            bool contactsOkay = SweepPosition(pc, I.z, I.z + I.w, pos, false, -1, -1);
+            bool jointsOkay = true;
+            for (int k = 0; k < J.y; ++k) {
+                bool ok = RevSolvePosition(jt[sJoint[J.x + k]], pos);
+                jointsOkay = jointsOkay && ok;
+            }
+            if (contactsOkay && jointsOkay) { positionSolved = true; break; }
+        }
+        sleepOut[isl] = positionSolved ? 1 : 0;
+    }
+    __syncthreads();
+    if (tid() == 0) { unsigned long long now = clock64(); st->cyc[11] = now - tStamp; tStamp = now; }
+    // write back and SynchronizeTransform (static bodies never move: skipped)
+    for (int r = tid(); r < nRows; r += nthreads()) {
+        int b = sBody[r];
+        if (type(b) == kStatic) continue;
+        float4 p4 = pos[r], v4 = vel[r];
+        sw[b] = make_float4(p4.x, p4.y, p4.z, sw[b].w);
+        vel_body(b) = make_float4(v4.x, v4.y, v4.z, 0.0f);
+        syncTransform(b);
+    }
+    __syncthreads();
+    if (tid() == 0) { unsigned long long now = clock64(); st->cyc[12] = now - tStamp; tStamp = now; }
+    // sleep (b2Island.cpp:346-383), per island
+    for (int isl = tid(); isl < nIsl; isl += nthreads()) {
+        int slept = 0;
+        if (st->allowSleep) {
+            int4 I = islands[isl];
+            const bool positionSolved = sleepOut[isl] != 0;
+            float minSleepTime = kMaxFloat;
+            const float linTolSqr = kLinearSleepTolerance * kLinearSleepTolerance;
+            const float angTolSqr = kAngularSleepTolerance * kAngularSleepTolerance;
+            for (int r = I.x; r < I.x + I.y; ++r) {
+                int b = sBody[r];
+                if (type(b) == kStatic) continue;
+                float4 v4 = vel_body(b);
+                float st0 = sw0[b].w;
+                if ((flags(b) & kBAutoSleep) == 0 || v4.z * v4.z > angTolSqr || (v4.x * v4.x + v4.y * v4.y) > linTolSqr) {
+                    st0 = 0.0f;
+                    minSleepTime = 0.0f;
+                } else {
+                    st0 += h;
+                    minSleepTime = Minf(minSleepTime, st0);
+                }
+                sw0[b].w = st0;
+            }
+            if (minSleepTime >= kTimeToSleep && positionSolved) {
+                slept = 1;
+                for (int r = I.x; r < I.x + I.y; ++r) {
+                    int b = sBody[r];
+                    if (type(b) != kStatic) setAwake(b, false);
+                }
+            }
+        }
+        sleepOut[isl] = slept;
+    }
+    __syncthreads();
+    if (tid() == 0) { unsigned long long now = clock64(); st->cyc[13] = now - tStamp; tStamp = now; }
+}

@@ -47,6 +47,7 @@ struct Wd {
     int *sContact, *sStatus;
     VelConstraint* vc;
     PosConstraint* pc;
+    float4* vimp;
     TOITask* toi;
     int4* islands;
     int2* islandJ;
@@ -71,11 +72,12 @@ struct Wd {
         sBody = B.sBody + d.rowBase; sPos = B.sPos + d.rowBase; sVel = B.sVel + d.rowBase;
         sStack = B.sStack + b; sWake = B.sWake + b;
         islands = B.islands + b; islandJ = B.islandJ + b; sleepOut = B.sleepOut + b;
-        sContact = B.sContact + c; sStatus = B.sStatus + c; vc = B.vc + c; pc = B.pc + c; toi = B.toi + c;
+        sContact = B.sContact + c; sStatus = B.sStatus + c; vc = B.vc + c; pc = B.pc + c; vimp = B.vimp + c; toi = B.toi + c;
         pairs = B.pairs + q; pairKeep = B.pairKeep + q;
     }
 
     // ---------------------------------------------------------------- body helpers
+    __device__ float4& vel_body(int b) { return vel[b]; }
     __device__ int type(int b) const { return bi[b].x; }
     __device__ int flags(int b) const { return bi[b].y; }
     __device__ bool awake(int b) const { return (bi[b].y & kBAwake) != 0; }
@@ -280,15 +282,43 @@ struct Wd {
     // b2ContactManager::FindNewContacts -> b2BroadPhase::UpdatePairs -> AddPair, CTA-wide.
     __device__ void findNewContacts();
     __device__ void collide();
-    __device__ void solve(const StepParams& P);
+    __device__ void solve(const StepParams& P, float4* smem, int smemRows, int smemContacts);
+    __device__ void solveIslands(const StepParams& P, int nIsl, int nRows, int nContacts, float4* smem, int smemRows,
+                                 int smemContacts);
     __device__ void solveTOI(const StepParams& P);
     __device__ void destroyContact(int c);
-    __device__ void islandSolve(int island, const StepParams& P, float dt, float dtRatio);
 };
 
 // ------------------------------------------------------------------ CTA helpers
 __device__ inline int tid() { return threadIdx.x; }
 __device__ inline int nthreads() { return blockDim.x; }
+
+// Order-preserving compaction over the CTA: out receives in[k] for every k < n with keep(k), in k
+// order; returns the count (same value in every thread). Each thread takes one contiguous chunk.
+constexpr int kMaxCta = 128;
+template <typename Keep>
+__device__ int ctaCompact(const int* in, int n, int* out, Keep keep)
+{
+    __shared__ int sOff[kMaxCta + 1];
+    const int T = nthreads(), t = tid();
+    const int chunk = (n + T - 1) / T;
+    const int lo = min(n, t * chunk), hi = min(n, lo + chunk);
+    int cnt = 0;
+    for (int k = lo; k < hi; ++k) cnt += keep(k) ? 1 : 0;
+    sOff[t + 1] = cnt;
+    __syncthreads();
+    if (t == 0) {
+        sOff[0] = 0;
+        for (int i = 1; i <= T; ++i) sOff[i] += sOff[i - 1];
+    }
+    __syncthreads();
+    int o = sOff[t];
+    for (int k = lo; k < hi; ++k)
+        if (keep(k)) out[o++] = in[k];
+    const int total = sOff[T];
+    __syncthreads();
+    return total;
+}
 
 // Bitonic sort of n 64-bit keys in global memory (n <= capacity, capacity a power of two); the
 // padding keys are all-ones so they sort last.
@@ -405,15 +435,17 @@ __device__ void Wd::findNewContacts()
         sNew = created;
     }
     __syncthreads();
-    // order = reverse(new) ++ order
-    int created = sNew;
+    // order = reverse(new) ++ order (the pair-keep flags are dead now: reuse them as the copy buffer)
+    const int created = sNew;
     if (created > 0) {
-        int live = st->contactCount;
-        if (tid() == 0) {
-            for (int i = live - 1; i >= 0; --i) order[i + created] = order[i];
-            for (int i = 0; i < created; ++i) order[created - 1 - i] = sContact[i];
-            st->contactCount = live + created;
-        }
+        const int live = st->contactCount;
+        int* tmp = pairKeep;
+        for (int i = tid(); i < live; i += nthreads()) tmp[i] = order[i];
+        __syncthreads();
+        for (int i = tid(); i < live; i += nthreads()) order[i + created] = tmp[i];
+        for (int i = tid(); i < created; i += nthreads()) order[created - 1 - i] = sContact[i];
+        __syncthreads();
+        if (tid() == 0) st->contactCount = live + created;
     }
     for (int i = tid(); i < m; i += nthreads()) moved[movedList[i]] = 0;
     __syncthreads();
@@ -499,634 +531,29 @@ __device__ void Wd::collide()
         if (wk != -1 && wk != INT_MAX) setAwake(b, true);
     }
     __syncthreads();
+    // Survivors keep their relative order; destroyed contacts are unlinked in list order.
+    int* kept = sContact;
+    int* gone = pairKeep;
+    const int nKept = ctaCompact(order, n, kept, [&](int k) { return sStatus[k] != 2; });
+    const int nGone = ctaCompact(order, n, gone, [&](int k) { return sStatus[k] == 2; });
     if (tid() == 0) {
-        int out = 0;
-        for (int k = 0; k < n; ++k) {
-            int c = order[k];
-            if (sStatus[k] == 2) destroyContact(c);
-            else order[out++] = c;
-        }
-        st->contactCount = out;
+        for (int i = 0; i < nGone; ++i) destroyContact(gone[i]);
+        st->contactCount = nKept;
     }
+    for (int k = tid(); k < nKept; k += nthreads()) order[k] = kept[k];
     __syncthreads();
 }
 
-// ------------------------------------------------------------------ contact solver
-// b2ContactSolver (Dynamics/Contacts/b2ContactSolver.cpp) over one island's constraints.
-struct Solver {
-    VelConstraint* vc;
-    PosConstraint* pc;
-    int n;
-    float4* pos;
-    float4* vel;
-};
-
-__device__ inline Vec2 MulM(const float* A, Vec2 v) { return V(A[0] * v.x + A[2] * v.y, A[1] * v.x + A[3] * v.y); }
-
-// b2ContactSolver::b2ContactSolver (b2ContactSolver.cpp:49-141). islandBase maps island-local body
-// indices to rows of pos/vel.
-__device__ void SolverSetup(Wd& W, Solver& S, const int* contacts, bool warmStarting, float dtRatio)
-{
-    for (int i = 0; i < S.n; ++i) {
-        int c = contacts[i];
-        int4 info = W.ci[c];
-        int fA = info.y, fB = info.z;
-        int bA = W.fixBody(fA), bB = W.fixBody(fB);
-        float4 mA = W.mas[bA], mB = W.mas[bB];
-        float4 pp = W.cp[c];
-        int4 h = W.mh[c];
-        float4 mvv = W.mv[c], p0 = W.mp0[c], p1 = W.mp1[c];
-        VelConstraint& v = S.vc[i];
-        PosConstraint& p = S.pc[i];
-        v.friction = pp.x; v.restitution = pp.y; v.tangentSpeed = pp.z;
-        // v.indexA / v.indexB were set when the island was built
-        v.invMassA = mA.x; v.invMassB = mB.x; v.invIA = mA.y; v.invIB = mB.y;
-        v.contact = c;
-        v.pointCount = h.y;
-        v.K[0] = v.K[1] = v.K[2] = v.K[3] = 0.0f;
-        v.normalMass[0] = v.normalMass[1] = v.normalMass[2] = v.normalMass[3] = 0.0f;
-        p.indexA = v.indexA; p.indexB = v.indexB;
-        p.invMassA = mA.x; p.invMassB = mB.x;
-        p.localCenterA = V(mA.z, mA.w); p.localCenterB = V(mB.z, mB.w);
-        p.invIA = mA.y; p.invIB = mB.y;
-        p.localNormal = V(mvv.x, mvv.y);
-        p.localPoint = V(mvv.z, mvv.w);
-        p.pointCount = h.y;
-        p.radiusA = W.fm[fA].w; p.radiusB = W.fm[fB].w;
-        p.type = h.x;
-        for (int j = 0; j < h.y; ++j) {
-            float4 q = j == 0 ? p0 : p1;
-            VelPoint& vp = v.p[j];
-            if (warmStarting) {
-                vp.normalImpulse = dtRatio * q.z;
-                vp.tangentImpulse = dtRatio * q.w;
-            } else {
-                vp.normalImpulse = 0.0f;
-                vp.tangentImpulse = 0.0f;
-            }
-            vp.rA = V(0.0f, 0.0f); vp.rB = V(0.0f, 0.0f);
-            vp.normalMass = 0.0f; vp.tangentMass = 0.0f; vp.velocityBias = 0.0f;
-            p.localPoints[j] = V(q.x, q.y);
-        }
-    }
-}
-
-// b2ContactSolver::InitializeVelocityConstraints (b2ContactSolver.cpp:143-252)
-__device__ void SolverInitVelocity(Wd& W, Solver& S)
-{
-    for (int i = 0; i < S.n; ++i) {
-        VelConstraint& v = S.vc[i];
-        const PosConstraint& p = S.pc[i];
-        Manifold m;
-        W.loadManifold(v.contact, m);
-        float mA = v.invMassA, mB = v.invMassB, iA = v.invIA, iB = v.invIB;
-        float4 pa = S.pos[v.indexA], pb = S.pos[v.indexB];
-        float4 va = S.vel[v.indexA], vb = S.vel[v.indexB];
-        Vec2 cA = V(pa.x, pa.y), cB = V(pb.x, pb.y);
-        Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
-        float wA = va.z, wB = vb.z;
-        Xf xfA, xfB;
-        xfA.q = RotOf(pa.z);
-        xfB.q = RotOf(pb.z);
-        xfA.p = cA - Mul(xfA.q, p.localCenterA);
-        xfB.p = cB - Mul(xfB.q, p.localCenterB);
-        WorldManifold wm;
-        WorldManifoldInit(&wm, m, xfA, p.radiusA, xfB, p.radiusB);
-        v.normal = wm.normal;
-        for (int j = 0; j < v.pointCount; ++j) {
-            VelPoint& vp = v.p[j];
-            vp.rA = wm.pts[j] - cA;
-            vp.rB = wm.pts[j] - cB;
-            float rnA = Cross(vp.rA, v.normal), rnB = Cross(vp.rB, v.normal);
-            float kNormal = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
-            vp.normalMass = kNormal > 0.0f ? 1.0f / kNormal : 0.0f;
-            Vec2 tangent = Cross(v.normal, 1.0f);
-            float rtA = Cross(vp.rA, tangent), rtB = Cross(vp.rB, tangent);
-            float kTangent = mA + mB + iA * rtA * rtA + iB * rtB * rtB;
-            vp.tangentMass = kTangent > 0.0f ? 1.0f / kTangent : 0.0f;
-            vp.velocityBias = 0.0f;
-            float vRel = Dot(v.normal, vB + Cross(wB, vp.rB) - vA - Cross(wA, vp.rA));
-            if (vRel < -kVelocityThreshold) vp.velocityBias = -v.restitution * vRel;
-        }
-        if (v.pointCount == 2) {
-            const VelPoint& p1 = v.p[0];
-            const VelPoint& p2 = v.p[1];
-            float rn1A = Cross(p1.rA, v.normal), rn1B = Cross(p1.rB, v.normal);
-            float rn2A = Cross(p2.rA, v.normal), rn2B = Cross(p2.rB, v.normal);
-            float k11 = mA + mB + iA * rn1A * rn1A + iB * rn1B * rn1B;
-            float k22 = mA + mB + iA * rn2A * rn2A + iB * rn2B * rn2B;
-            float k12 = mA + mB + iA * rn1A * rn2A + iB * rn1B * rn2B;
-            const float k_maxConditionNumber = 1000.0f;
-            if (k11 * k11 < k_maxConditionNumber * (k11 * k22 - k12 * k12)) {
-                v.K[0] = k11; v.K[1] = k12; v.K[2] = k12; v.K[3] = k22;
-                // b2Mat22::GetInverse (Common/b2Math.h:185-197)
-                float a = v.K[0], b = v.K[2], cc = v.K[1], dd = v.K[3];
-                float det = a * dd - b * cc;
-                if (det != 0.0f) det = 1.0f / det;
-                v.normalMass[0] = det * dd; v.normalMass[2] = -det * b;
-                v.normalMass[1] = -det * cc; v.normalMass[3] = det * a;
-            } else {
-                v.pointCount = 1;
-            }
-        }
-    }
-}
-
-// b2ContactSolver::WarmStart (b2ContactSolver.cpp:254-292)
-__device__ void SolverWarmStart(Solver& S)
-{
-    for (int i = 0; i < S.n; ++i) {
-        const VelConstraint& v = S.vc[i];
-        float4 va = S.vel[v.indexA], vb = S.vel[v.indexB];
-        Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
-        float wA = va.z, wB = vb.z;
-        Vec2 normal = v.normal, tangent = Cross(normal, 1.0f);
-        for (int j = 0; j < v.pointCount; ++j) {
-            const VelPoint& p = v.p[j];
-            Vec2 P = p.normalImpulse * normal + p.tangentImpulse * tangent;
-            wA -= v.invIA * Cross(p.rA, P);
-            vA = vA - v.invMassA * P;
-            wB += v.invIB * Cross(p.rB, P);
-            vB = vB + v.invMassB * P;
-        }
-        S.vel[v.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
-        S.vel[v.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
-    }
-}
-
-// b2ContactSolver::SolveVelocityConstraints (b2ContactSolver.cpp:294-605): friction per point, then
-// the normal constraint: one point, or the 2-point block LCP solved by total enumeration.
-__device__ void SolverVelocity(Solver& S)
-{
-    for (int i = 0; i < S.n; ++i) {
-        VelConstraint& v = S.vc[i];
-        float mA = v.invMassA, iA = v.invIA, mB = v.invMassB, iB = v.invIB;
-        float4 va = S.vel[v.indexA], vb = S.vel[v.indexB];
-        Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
-        float wA = va.z, wB = vb.z;
-        Vec2 normal = v.normal, tangent = Cross(normal, 1.0f);
-        float friction = v.friction;
-        int pointCount = v.pointCount;
-        for (int j = 0; j < pointCount; ++j) {
-            VelPoint& p = v.p[j];
-            Vec2 dv = vB + Cross(wB, p.rB) - vA - Cross(wA, p.rA);
-            float vt = Dot(dv, tangent) - v.tangentSpeed;
-            float lambda = p.tangentMass * (-vt);
-            float maxFriction = friction * p.normalImpulse;
-            float newImpulse = Clampf(p.tangentImpulse + lambda, -maxFriction, maxFriction);
-            lambda = newImpulse - p.tangentImpulse;
-            p.tangentImpulse = newImpulse;
-            Vec2 P = lambda * tangent;
-            vA = vA - mA * P;
-            wA -= iA * Cross(p.rA, P);
-            vB = vB + mB * P;
-            wB += iB * Cross(p.rB, P);
-        }
-        if (pointCount == 1) {
-            VelPoint& p = v.p[0];
-            Vec2 dv = vB + Cross(wB, p.rB) - vA - Cross(wA, p.rA);
-            float vn = Dot(dv, normal);
-            float lambda = -p.normalMass * (vn - p.velocityBias);
-            float newImpulse = Maxf(p.normalImpulse + lambda, 0.0f);
-            lambda = newImpulse - p.normalImpulse;
-            p.normalImpulse = newImpulse;
-            Vec2 P = lambda * normal;
-            vA = vA - mA * P;
-            wA -= iA * Cross(p.rA, P);
-            vB = vB + mB * P;
-            wB += iB * Cross(p.rB, P);
-        } else {
-            VelPoint& cp1 = v.p[0];
-            VelPoint& cp2 = v.p[1];
-            Vec2 a = V(cp1.normalImpulse, cp2.normalImpulse);
-            Vec2 dv1 = vB + Cross(wB, cp1.rB) - vA - Cross(wA, cp1.rA);
-            Vec2 dv2 = vB + Cross(wB, cp2.rB) - vA - Cross(wA, cp2.rA);
-            float vn1 = Dot(dv1, normal), vn2 = Dot(dv2, normal);
-            Vec2 b;
-            b.x = vn1 - cp1.velocityBias;
-            b.y = vn2 - cp2.velocityBias;
-            b = b - MulM(v.K, a);
-            Vec2 x = -MulM(v.normalMass, b);
-            bool solved = x.x >= 0.0f && x.y >= 0.0f;
-            if (!solved) {
-                x.x = -cp1.normalMass * b.x;
-                x.y = 0.0f;
-                vn2 = v.K[1] * x.x + b.y;
-                solved = x.x >= 0.0f && vn2 >= 0.0f;
-            }
-            if (!solved) {
-                x.x = 0.0f;
-                x.y = -cp2.normalMass * b.y;
-                vn1 = v.K[2] * x.y + b.x;
-                solved = x.y >= 0.0f && vn1 >= 0.0f;
-            }
-            if (!solved) {
-                x.x = 0.0f;
-                x.y = 0.0f;
-                vn1 = b.x;
-                vn2 = b.y;
-                solved = vn1 >= 0.0f && vn2 >= 0.0f;
-            }
-            if (solved) {
-                Vec2 dd = x - a;
-                Vec2 P1 = dd.x * normal, P2 = dd.y * normal;
-                vA = vA - mA * (P1 + P2);
-                wA -= iA * (Cross(cp1.rA, P1) + Cross(cp2.rA, P2));
-                vB = vB + mB * (P1 + P2);
-                wB += iB * (Cross(cp1.rB, P1) + Cross(cp2.rB, P2));
-                cp1.normalImpulse = x.x;
-                cp2.normalImpulse = x.y;
-            }
-        }
-        S.vel[v.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
-        S.vel[v.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
-    }
-}
-
-// b2ContactSolver::StoreImpulses (b2ContactSolver.cpp:607-620)
-__device__ void SolverStore(Wd& W, Solver& S)
-{
-    for (int i = 0; i < S.n; ++i) {
-        const VelConstraint& v = S.vc[i];
-        if (v.pointCount > 0) { W.mp0[v.contact].z = v.p[0].normalImpulse; W.mp0[v.contact].w = v.p[0].tangentImpulse; }
-        if (v.pointCount > 1) { W.mp1[v.contact].z = v.p[1].normalImpulse; W.mp1[v.contact].w = v.p[1].tangentImpulse; }
-    }
-}
-
-// b2ContactSolver::SolvePositionConstraints (b2ContactSolver.cpp:674-751) and
-// SolveTOIPositionConstraints (:753-836) with b2PositionSolverManifold (:623-672).
-__device__ bool SolverPosition(Solver& S, bool toi, int toiA, int toiB)
-{
-    float minSeparation = 0.0f;
-    for (int i = 0; i < S.n; ++i) {
-        const PosConstraint& p = S.pc[i];
-        float mA, iA, mB, iB;
-        if (!toi) { mA = p.invMassA; iA = p.invIA; mB = p.invMassB; iB = p.invIB; }
-        else {
-            mA = 0.0f; iA = 0.0f; mB = 0.0f; iB = 0.0f;
-            if (p.indexA == toiA || p.indexA == toiB) { mA = p.invMassA; iA = p.invIA; }
-            if (p.indexB == toiA || p.indexB == toiB) { mB = p.invMassB; iB = p.invIB; }
-        }
-        float4 pa = S.pos[p.indexA], pb = S.pos[p.indexB];
-        Vec2 cA = V(pa.x, pa.y), cB = V(pb.x, pb.y);
-        float aA = pa.z, aB = pb.z;
-        for (int j = 0; j < p.pointCount; ++j) {
-            Xf xfA, xfB;
-            xfA.q = RotOf(aA);
-            xfB.q = RotOf(aB);
-            xfA.p = cA - Mul(xfA.q, p.localCenterA);
-            xfB.p = cB - Mul(xfB.q, p.localCenterB);
-            Vec2 normal, point;
-            float separation;
-            if (p.type == kCircles) {
-                Vec2 pA = Mul(xfA, p.localPoint), pB = Mul(xfB, p.localPoints[0]);
-                normal = pB - pA;
-                Normalize(normal);
-                point = 0.5f * (pA + pB);
-                separation = Dot(pB - pA, normal) - p.radiusA - p.radiusB;
-            } else if (p.type == kFaceA) {
-                normal = Mul(xfA.q, p.localNormal);
-                Vec2 plane = Mul(xfA, p.localPoint);
-                Vec2 clip = Mul(xfB, p.localPoints[j]);
-                separation = Dot(clip - plane, normal) - p.radiusA - p.radiusB;
-                point = clip;
-            } else {
-                normal = Mul(xfB.q, p.localNormal);
-                Vec2 plane = Mul(xfB, p.localPoint);
-                Vec2 clip = Mul(xfA, p.localPoints[j]);
-                separation = Dot(clip - plane, normal) - p.radiusA - p.radiusB;
-                point = clip;
-                normal = -normal;
-            }
-            Vec2 rA = point - cA, rB = point - cB;
-            minSeparation = Minf(minSeparation, separation);
-            float C = toi ? Clampf(kToiBaumgarte * (separation + kLinearSlop), -kMaxLinearCorrection, 0.0f)
-                          : Clampf(kBaumgarte * (separation + kLinearSlop), -kMaxLinearCorrection, 0.0f);
-            float rnA = Cross(rA, normal), rnB = Cross(rB, normal);
-            float K = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
-            float impulse = K > 0.0f ? -C / K : 0.0f;
-            Vec2 P = impulse * normal;
-            cA = cA - mA * P;
-            aA -= iA * Cross(rA, P);
-            cB = cB + mB * P;
-            aB += iB * Cross(rB, P);
-        }
-        S.pos[p.indexA] = make_float4(cA.x, cA.y, aA, 0.0f);
-        S.pos[p.indexB] = make_float4(cB.x, cB.y, aB, 0.0f);
-    }
-    return toi ? minSeparation >= -1.5f * kLinearSlop : minSeparation >= -3.0f * kLinearSlop;
-}
-
-// ------------------------------------------------------------------ revolute joint
-// b2RevoluteJoint (Dynamics/Joints/b2RevoluteJoint.cpp:66-380); pos/vel rows are indexA/indexB,
-// set when the island was built.
-__device__ void RevInit(Wd& W, Joint& j, float4* pos, float4* vel, bool warmStarting, float dtRatio)
-{
-    int A = j.bodyA, B = j.bodyB;
-    float4 mA4 = W.mas[A], mB4 = W.mas[B];
-    j.localCenterA = V(mA4.z, mA4.w); j.localCenterB = V(mB4.z, mB4.w);
-    j.invMassA = mA4.x; j.invMassB = mB4.x; j.invIA = mA4.y; j.invIB = mB4.y;
-    float aA = pos[j.indexA].z, aB = pos[j.indexB].z;
-    float4 va = vel[j.indexA], vb = vel[j.indexB];
-    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
-    float wA = va.z, wB = vb.z;
-    Rot qA = RotOf(aA), qB = RotOf(aB);
-    j.rA = Mul(qA, j.localAnchorA - j.localCenterA);
-    j.rB = Mul(qB, j.localAnchorB - j.localCenterB);
-    float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
-    bool fixedRotation = (iA + iB == 0.0f);
-    float* M = j.mass;
-    M[0] = mA + mB + j.rA.y * j.rA.y * iA + j.rB.y * j.rB.y * iB;
-    M[3] = -j.rA.y * j.rA.x * iA - j.rB.y * j.rB.x * iB;
-    M[6] = -j.rA.y * iA - j.rB.y * iB;
-    M[1] = M[3];
-    M[4] = mA + mB + j.rA.x * j.rA.x * iA + j.rB.x * j.rB.x * iB;
-    M[7] = j.rA.x * iA + j.rB.x * iB;
-    M[2] = M[6];
-    M[5] = M[7];
-    M[8] = iA + iB;
-    j.motorMass = iA + iB;
-    if (j.motorMass > 0.0f) j.motorMass = 1.0f / j.motorMass;
-    if (!j.enableMotor || fixedRotation) j.motorImpulse = 0.0f;
-    if (j.enableLimit && !fixedRotation) {
-        float jointAngle = aB - aA - j.referenceAngle;
-        if (Absf(j.upperAngle - j.lowerAngle) < 2.0f * kAngularSlop) j.limitState = 3;
-        else if (jointAngle <= j.lowerAngle) {
-            if (j.limitState != 1) j.impulse[2] = 0.0f;
-            j.limitState = 1;
-        } else if (jointAngle >= j.upperAngle) {
-            if (j.limitState != 2) j.impulse[2] = 0.0f;
-            j.limitState = 2;
-        } else {
-            j.limitState = 0;
-            j.impulse[2] = 0.0f;
-        }
-    } else {
-        j.limitState = 0;
-    }
-    if (warmStarting) {
-        j.impulse[0] *= dtRatio; j.impulse[1] *= dtRatio; j.impulse[2] *= dtRatio;
-        j.motorImpulse *= dtRatio;
-        Vec2 P = V(j.impulse[0], j.impulse[1]);
-        vA = vA - mA * P;
-        wA -= iA * (Cross(j.rA, P) + j.motorImpulse + j.impulse[2]);
-        vB = vB + mB * P;
-        wB += iB * (Cross(j.rB, P) + j.motorImpulse + j.impulse[2]);
-    } else {
-        j.impulse[0] = j.impulse[1] = j.impulse[2] = 0.0f;
-        j.motorImpulse = 0.0f;
-    }
-    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
-    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
-}
-
-// b2Mat33::Solve33 / Solve22 (Common/b2Math.cpp:24-56), columns ex = M[0..2], ey = M[3..5], ez = M[6..8]
-__device__ inline void Solve33(const float* M, const float* b, float* x)
-{
-    float t[3];
-    t[0] = M[4] * M[8] - M[5] * M[7]; t[1] = M[5] * M[6] - M[3] * M[8]; t[2] = M[3] * M[7] - M[4] * M[6];
-    float det = M[0] * t[0] + M[1] * t[1] + M[2] * t[2];
-    if (det != 0.0f) det = 1.0f / det;
-    x[0] = det * (b[0] * t[0] + b[1] * t[1] + b[2] * t[2]);
-    t[0] = b[1] * M[8] - b[2] * M[7]; t[1] = b[2] * M[6] - b[0] * M[8]; t[2] = b[0] * M[7] - b[1] * M[6];
-    x[1] = det * (M[0] * t[0] + M[1] * t[1] + M[2] * t[2]);
-    t[0] = M[4] * b[2] - M[5] * b[1]; t[1] = M[5] * b[0] - M[3] * b[2]; t[2] = M[3] * b[1] - M[4] * b[0];
-    x[2] = det * (M[0] * t[0] + M[1] * t[1] + M[2] * t[2]);
-}
-__device__ inline Vec2 Solve22(const float* M, Vec2 b)
-{
-    float a11 = M[0], a12 = M[3], a21 = M[1], a22 = M[4];
-    float det = a11 * a22 - a12 * a21;
-    if (det != 0.0f) det = 1.0f / det;
-    return V(det * (a22 * b.x - a12 * b.y), det * (a11 * b.y - a21 * b.x));
-}
-
-__device__ void RevSolveVelocity(Joint& j, float4* vel, float dt)
-{
-    float4 va = vel[j.indexA], vb = vel[j.indexB];
-    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
-    float wA = va.z, wB = vb.z;
-    float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
-    bool fixedRotation = (iA + iB == 0.0f);
-    if (j.enableMotor && j.limitState != 3 && !fixedRotation) {
-        float Cdot = wB - wA - j.motorSpeed;
-        float impulse = -j.motorMass * Cdot;
-        float oldImpulse = j.motorImpulse;
-        float maxImpulse = dt * j.maxMotorTorque;
-        j.motorImpulse = Clampf(j.motorImpulse + impulse, -maxImpulse, maxImpulse);
-        impulse = j.motorImpulse - oldImpulse;
-        wA -= iA * impulse;
-        wB += iB * impulse;
-    }
-    if (j.enableLimit && j.limitState != 0 && !fixedRotation) {
-        Vec2 Cdot1 = vB + Cross(wB, j.rB) - vA - Cross(wA, j.rA);
-        float Cdot2 = wB - wA;
-        float Cd[3] = {Cdot1.x, Cdot1.y, Cdot2};
-        float imp[3];
-        Solve33(j.mass, Cd, imp);
-        imp[0] = -imp[0]; imp[1] = -imp[1]; imp[2] = -imp[2];
-        if (j.limitState == 3) {
-            j.impulse[0] += imp[0]; j.impulse[1] += imp[1]; j.impulse[2] += imp[2];
-        } else {
-            float newImpulse = j.impulse[2] + imp[2];
-            bool clampIt = j.limitState == 1 ? newImpulse < 0.0f : newImpulse > 0.0f;
-            if (clampIt) {
-                Vec2 rhs = -Cdot1 + j.impulse[2] * V(j.mass[6], j.mass[7]);
-                Vec2 reduced = Solve22(j.mass, rhs);
-                imp[0] = reduced.x; imp[1] = reduced.y; imp[2] = -j.impulse[2];
-                j.impulse[0] += reduced.x; j.impulse[1] += reduced.y; j.impulse[2] = 0.0f;
-            } else {
-                j.impulse[0] += imp[0]; j.impulse[1] += imp[1]; j.impulse[2] += imp[2];
-            }
-        }
-        Vec2 P = V(imp[0], imp[1]);
-        vA = vA - mA * P;
-        wA -= iA * (Cross(j.rA, P) + imp[2]);
-        vB = vB + mB * P;
-        wB += iB * (Cross(j.rB, P) + imp[2]);
-    } else {
-        Vec2 Cdot = vB + Cross(wB, j.rB) - vA - Cross(wA, j.rA);
-        Vec2 impulse = Solve22(j.mass, -Cdot);
-        j.impulse[0] += impulse.x;
-        j.impulse[1] += impulse.y;
-        vA = vA - mA * impulse;
-        wA -= iA * Cross(j.rA, impulse);
-        vB = vB + mB * impulse;
-        wB += iB * Cross(j.rB, impulse);
-    }
-    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
-    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
-}
-
-__device__ bool RevSolvePosition(Joint& j, float4* pos)
-{
-    float4 pa = pos[j.indexA], pb = pos[j.indexB];
-    Vec2 cA = V(pa.x, pa.y), cB = V(pb.x, pb.y);
-    float aA = pa.z, aB = pb.z;
-    float angularError = 0.0f, positionError = 0.0f;
-    bool fixedRotation = (j.invIA + j.invIB == 0.0f);
-    if (j.enableLimit && j.limitState != 0 && !fixedRotation) {
-        float angle = aB - aA - j.referenceAngle;
-        float limitImpulse = 0.0f;
-        if (j.limitState == 3) {
-            float C = Clampf(angle - j.lowerAngle, -kMaxAngularCorrection, kMaxAngularCorrection);
-            limitImpulse = -j.motorMass * C;
-            angularError = Absf(C);
-        } else if (j.limitState == 1) {
-            float C = angle - j.lowerAngle;
-            angularError = -C;
-            C = Clampf(C + kAngularSlop, -kMaxAngularCorrection, 0.0f);
-            limitImpulse = -j.motorMass * C;
-        } else if (j.limitState == 2) {
-            float C = angle - j.upperAngle;
-            angularError = C;
-            C = Clampf(C - kAngularSlop, 0.0f, kMaxAngularCorrection);
-            limitImpulse = -j.motorMass * C;
-        }
-        aA -= j.invIA * limitImpulse;
-        aB += j.invIB * limitImpulse;
-    }
-    {
-        Rot qA = RotOf(aA), qB = RotOf(aB);
-        Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
-        Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
-        Vec2 C = cB + rB - cA - rA;
-        positionError = Length(C);
-        float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
-        float K[9] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-        K[0] = mA + mB + iA * rA.y * rA.y + iB * rB.y * rB.y;
-        K[1] = -iA * rA.x * rA.y - iB * rB.x * rB.y;
-        K[3] = K[1];
-        K[4] = mA + mB + iA * rA.x * rA.x + iB * rB.x * rB.x;
-        Vec2 impulse = -Solve22(K, C);
-        cA = cA - mA * impulse;
-        aA -= iA * Cross(rA, impulse);
-        cB = cB + mB * impulse;
-        aB += iB * Cross(rB, impulse);
-    }
-    pos[j.indexA] = make_float4(cA.x, cA.y, aA, 0.0f);
-    pos[j.indexB] = make_float4(cB.x, cB.y, aB, 0.0f);
-    return positionError <= kLinearSlop && angularError <= kAngularSlop;
-}
-
-// ------------------------------------------------------------------ island solve
-// b2Island::Solve (Dynamics/b2Island.cpp:185-384) for island `island`, by one thread.
-__device__ void Wd::islandSolve(int island, const StepParams& P, float h, float dtRatio)
-{
-    int4 isl = islands[island];
-    int2 ij = islandJ[island];
-    const int bBase = isl.x, nb = isl.y;
-    const float gx = st->gx, gy = st->gy;
-    for (int i = 0; i < nb; ++i) {
-        int b = sBody[bBase + i];
-        float4 s = sw[b];
-        float4 v4 = vel[b];
-        Vec2 v = V(v4.x, v4.y);
-        float w = v4.z;
-        sw0[b] = make_float4(s.x, s.y, s.z, sw0[b].w);
-        if (type(b) == kDynamic) {
-            float4 m = mas[b], pr = prop[b], f = frc[b];
-            Vec2 g = pr.z * V(gx, gy);
-            v = v + h * (g + m.x * V(f.x, f.y));
-            w += h * m.y * f.z;
-            v = (1.0f / (1.0f + h * pr.x)) * v;
-            w *= 1.0f / (1.0f + h * pr.y);
-        }
-        sPos[bBase + i] = make_float4(s.x, s.y, s.z, 0.0f);
-        sVel[bBase + i] = make_float4(v.x, v.y, w, 0.0f);
-    }
-    Solver S;
-    S.vc = vc + isl.z;
-    S.pc = pc + isl.z;
-    S.n = isl.w;
-    S.pos = sPos + bBase;
-    S.vel = sVel + bBase;
-    const bool warm = st->warmStarting != 0;
-    SolverSetup(*this, S, sContact + isl.z, warm, dtRatio);
-    SolverInitVelocity(*this, S);
-    if (warm) SolverWarmStart(S);
-    for (int k = 0; k < ij.y; ++k) RevInit(*this, jt[sJoint[ij.x + k]], S.pos, S.vel, warm, dtRatio);
-    for (int it = 0; it < P.velocityIterations; ++it) {
-        for (int k = 0; k < ij.y; ++k) RevSolveVelocity(jt[sJoint[ij.x + k]], S.vel, h);
-        SolverVelocity(S);
-    }
-    SolverStore(*this, S);
-    for (int i = 0; i < nb; ++i) {
-        float4 p4 = S.pos[i], v4 = S.vel[i];
-        Vec2 c = V(p4.x, p4.y), v = V(v4.x, v4.y);
-        float a = p4.z, w = v4.z;
-        Vec2 translation = h * v;
-        if (Dot(translation, translation) > kMaxTranslationSquared) {
-            float ratio = kMaxTranslation / Length(translation);
-            v.x *= ratio;
-            v.y *= ratio;
-        }
-        float rotation = h * w;
-        if (rotation * rotation > kMaxRotationSquared) {
-            float ratio = kMaxRotation / Absf(rotation);
-            w *= ratio;
-        }
-        c = c + h * v;
-        a += h * w;
-        S.pos[i] = make_float4(c.x, c.y, a, 0.0f);
-        S.vel[i] = make_float4(v.x, v.y, w, 0.0f);
-    }
-    bool positionSolved = false;
-    for (int it = 0; it < P.positionIterations; ++it) {
-        bool contactsOkay = SolverPosition(S, false, -1, -1);
-        bool jointsOkay = true;
-        for (int k = 0; k < ij.y; ++k) {
-            bool ok = RevSolvePosition(jt[sJoint[ij.x + k]], S.pos);
-            jointsOkay = jointsOkay && ok;
-        }
-        if (contactsOkay && jointsOkay) { positionSolved = true; break; }
-    }
-    // Write back (static bodies are shared between islands and never move: skipped).
-    for (int i = 0; i < nb; ++i) {
-        int b = sBody[bBase + i];
-        if (type(b) == kStatic) continue;
-        float4 p4 = S.pos[i], v4 = S.vel[i];
-        sw[b] = make_float4(p4.x, p4.y, p4.z, sw[b].w);
-        vel[b] = make_float4(v4.x, v4.y, v4.z, 0.0f);
-        syncTransform(b);
-    }
-    int slept = 0;
-    if (st->allowSleep) {
-        float minSleepTime = kMaxFloat;
-        const float linTolSqr = kLinearSleepTolerance * kLinearSleepTolerance;
-        const float angTolSqr = kAngularSleepTolerance * kAngularSleepTolerance;
-        for (int i = 0; i < nb; ++i) {
-            int b = sBody[bBase + i];
-            if (type(b) == kStatic) continue;
-            float4 v4 = vel[b];
-            float st0 = sw0[b].w;
-            if ((flags(b) & kBAutoSleep) == 0 || v4.z * v4.z > angTolSqr || (v4.x * v4.x + v4.y * v4.y) > linTolSqr) {
-                st0 = 0.0f;
-                minSleepTime = 0.0f;
-            } else {
-                st0 += h;
-                minSleepTime = Minf(minSleepTime, st0);
-            }
-            sw0[b].w = st0;
-        }
-        if (minSleepTime >= kTimeToSleep && positionSolved) {
-            slept = 1;
-            for (int i = 0; i < nb; ++i) {
-                int b = sBody[bBase + i];
-                if (type(b) != kStatic) setAwake(b, false);
-            }
-        }
-    }
-    sleepOut[island] = slept;
-}
+#include "b2g_solver.cuh"
 
 // ------------------------------------------------------------------ Solve
 // b2World::Solve (Dynamics/b2World.cpp:388-577). The island DFS runs on one thread (it fixes the
 // contact order inside every island); islands are then solved in parallel, one per thread, because
 // they share no dynamic body.
-__device__ void Wd::solve(const StepParams& P)
+__device__ void Wd::solve(const StepParams& P, float4* smem, int smemRows, int smemContacts)
 {
-    __shared__ int sIslands;
+    __shared__ int sIslands, sRows, sCons;
+    const unsigned long long tSolve0 = clock64();
     const int nb = d.bodyCount, nc = st->contactCount;
     for (int b = tid(); b < nb; b += nthreads()) bi[b].y &= ~kBIsland;
     for (int k = tid(); k < nc; k += nthreads()) ci[order[k]].x &= ~kCIsland;
@@ -1183,29 +610,32 @@ __device__ void Wd::solve(const StepParams& P)
             // in several islands and its island index is overwritten by each island's DFS.
             for (int i = cStart; i < cCur; ++i) {
                 int4 info = ci[sContact[i]];
-                vc[i].indexA = bj[fixBody(info.y)].z;
-                vc[i].indexB = bj[fixBody(info.z)].z;
+                vc[i].idx = make_int4(bStart + bj[fixBody(info.y)].z, bStart + bj[fixBody(info.z)].z, 0, 0);
             }
             for (int i = jStart; i < jCur; ++i) {
                 Joint& J = jt[sJoint[i]];
-                J.indexA = bj[J.bodyA].z;
-                J.indexB = bj[J.bodyB].z;
+                J.indexA = bStart + bj[J.bodyA].z;
+                J.indexB = bStart + bj[J.bodyB].z;
             }
             for (int i = bStart; i < bCur; ++i)
                 if (bi[sBody[i]].x == kStatic) bi[sBody[i]].y &= ~kBIsland;
         }
         sIslands = nIsl;
+        sRows = bCur;
+        sCons = cCur;
         st->islands = nIsl;
         st->solvedBodies = movers;
         st->solvedContacts = cCur;
     }
     __syncthreads();
+    unsigned long long t1 = clock64();
     const int nIsl = sIslands;
-    const float dtRatio = st->inv_dt0 * P.dt;
-    for (int i = tid(); i < nIsl; i += nthreads()) islandSolve(i, P, P.dt, dtRatio);
-    __syncthreads();
+    solveIslands(P, nIsl, sRows, sCons, smem, smemRows, smemContacts);
+    unsigned long long t2 = clock64();
     // A static body may sit in several islands; its awake flag ends as the last such island left it.
     if (tid() == 0) {
+        st->cyc[2] = t1 - tSolve0;
+        st->cyc[3] = t2 - t1;
         for (int i = 0; i < nIsl; ++i) {
             int4 isl = islands[i];
             for (int k = isl.x; k < isl.x + isl.y; ++k) {
@@ -1222,7 +652,12 @@ __device__ void Wd::solve(const StepParams& P)
         syncFixtures(b);
     }
     __syncthreads();
+    unsigned long long t3 = clock64();
     findNewContacts();
+    if (tid() == 0) {
+        st->cyc[4] = t3 - t2;
+        st->cyc[5] = clock64() - t3;
+    }
 }
 
 // ------------------------------------------------------------------ SolveTOI
@@ -1247,48 +682,77 @@ __device__ void Wd::solveTOI(const StepParams& P)
         }
     }
     __syncthreads();
+    __shared__ int sAdvance;
+    __shared__ float sBestA[kMaxCta];
+    __shared__ int sBestK[kMaxCta];
     for (int event = 0;; ++event) {
-        // scan (sequential: body sweeps are advanced in list order)
-        if (tid() == 0) {
-            const int n = st->contactCount;
-            for (int k = 0; k < n; ++k) {
-                int c = order[k];
-                TOITask& T = toi[k];
-                T.contact = c;
-                T.kind = 0;
-                int4 info = ci[c];
-                if ((info.x & kCEnabled) == 0) continue;
-                if (info.w > kMaxSubSteps) continue;
-                if (info.x & kCToi) { T.kind = 1; continue; }
-                if (fi[info.y].w != 0 || fi[info.z].w != 0) continue;
-                int bA = fixBody(info.y), bB = fixBody(info.z);
-                int tA = bi[bA].x, tB = bi[bB].x;
-                bool activeA = (bi[bA].y & kBAwake) && tA != kStatic;
-                bool activeB = (bi[bB].y & kBAwake) && tB != kStatic;
-                if (!activeA && !activeB) continue;
-                bool collideA = (bi[bA].y & kBBullet) || tA != kDynamic;
-                bool collideB = (bi[bB].y & kBBullet) || tB != kDynamic;
-                if (!collideA && !collideB) continue;
-                Sweep sA = sweep(bA), sB = sweep(bB);
-                float alpha0 = sA.alpha0;
-                if (sA.alpha0 < sB.alpha0) {
-                    alpha0 = sB.alpha0;
-                    SweepAdvance(sA, alpha0);
-                    setSweep(bA, sA);
-                } else if (sB.alpha0 < sA.alpha0) {
-                    alpha0 = sA.alpha0;
-                    SweepAdvance(sB, alpha0);
-                    setSweep(bB, sB);
+        const int n = st->contactCount;
+        if (tid() == 0) sAdvance = 0;
+        __syncthreads();
+        // Classify every contact of the list in parallel: 0 skipped, 1 cached TOI, 2 TOI needed.
+        // Whether a contact is skipped does not depend on the sweeps, so this is order-free.
+        for (int k = tid(); k < n; k += nthreads()) {
+            int c = order[k];
+            TOITask& T = toi[k];
+            T.contact = c;
+            int kind = 0;
+            int4 info = ci[c];
+            if ((info.x & kCEnabled) != 0 && info.w <= kMaxSubSteps) {
+                if (info.x & kCToi) kind = 1;
+                else if (fi[info.y].w == 0 && fi[info.z].w == 0) {
+                    int bA = fixBody(info.y), bB = fixBody(info.z);
+                    int4 iA = bi[bA], iB = bi[bB];
+                    bool activeA = (iA.y & kBAwake) && iA.x != kStatic;
+                    bool activeB = (iB.y & kBAwake) && iB.x != kStatic;
+                    bool collideA = (iA.y & kBBullet) || iA.x != kDynamic;
+                    bool collideB = (iB.y & kBBullet) || iB.x != kDynamic;
+                    if ((activeA || activeB) && (collideA || collideB)) {
+                        kind = 2;
+                        if (sw[bA].w != sw[bB].w) sAdvance = 1;
+                    }
                 }
-                T.kind = 2;
-                T.alpha0 = alpha0;
-                T.sa = sA;
-                T.sb = sB;
             }
-            sN = n;
+            T.kind = kind;
         }
         __syncthreads();
-        const int n = sN;
+        if (sAdvance) {
+            // Some pair has bodies at different sweep times: the reference advances the earlier body
+            // while it scans, in list order, and later pairs see the advanced sweep. Replay on one thread.
+            if (tid() == 0) {
+                for (int k = 0; k < n; ++k) {
+                    TOITask& T = toi[k];
+                    if (T.kind != 2) continue;
+                    int4 info = ci[T.contact];
+                    int bA = fixBody(info.y), bB = fixBody(info.z);
+                    Sweep sA = sweep(bA), sB = sweep(bB);
+                    float alpha0 = sA.alpha0;
+                    if (sA.alpha0 < sB.alpha0) {
+                        alpha0 = sB.alpha0;
+                        SweepAdvance(sA, alpha0);
+                        setSweep(bA, sA);
+                    } else if (sB.alpha0 < sA.alpha0) {
+                        alpha0 = sA.alpha0;
+                        SweepAdvance(sB, alpha0);
+                        setSweep(bB, sB);
+                    }
+                    T.alpha0 = alpha0;
+                    T.sa = sA;
+                    T.sb = sB;
+                }
+            }
+        } else {
+            // All pairs agree on alpha0, so no sweep changes during the scan: snapshot in parallel.
+            for (int k = tid(); k < n; k += nthreads()) {
+                TOITask& T = toi[k];
+                if (T.kind != 2) continue;
+                int4 info = ci[T.contact];
+                int bA = fixBody(info.y), bB = fixBody(info.z);
+                T.sa = sweep(bA);
+                T.sb = sweep(bB);
+                T.alpha0 = T.sa.alpha0;
+            }
+        }
+        __syncthreads();
         for (int k = tid(); k < n; k += nthreads()) {
             TOITask& T = toi[k];
             if (T.kind != 2) continue;
@@ -1301,14 +765,30 @@ __device__ void Wd::solveTOI(const StepParams& P)
             ci[T.contact].x = info.x | kCToi;
         }
         __syncthreads();
-        if (tid() == 0) {
-            int minC = kNullIdx;
-            float minAlpha = 1.0f;
-            for (int k = 0; k < n; ++k) {
+        // Earliest TOI, first in list order among equals (the reference keeps the first alpha <
+        // minAlpha): per-thread minimum over its strided positions, then a reduction on (alpha, k).
+        {
+            float best = 1.0f;
+            int bestK = INT_MAX;
+            for (int k = tid(); k < n; k += nthreads()) {
                 if (toi[k].kind == 0) continue;
                 float alpha = cp[toi[k].contact].w;
-                if (alpha < minAlpha) { minC = toi[k].contact; minAlpha = alpha; }
+                if (alpha < best) { best = alpha; bestK = k; }
             }
+            sBestA[tid()] = best;
+            sBestK[tid()] = bestK;
+        }
+        __syncthreads();
+        if (tid() == 0) {
+            float minAlpha = 1.0f;
+            int minK = INT_MAX;
+            for (int t = 0; t < nthreads(); ++t) {
+                if (sBestA[t] < minAlpha || (sBestA[t] == minAlpha && sBestK[t] < minK && sBestA[t] < 1.0f)) {
+                    minAlpha = sBestA[t];
+                    minK = sBestK[t];
+                }
+            }
+            int minC = minK == INT_MAX ? kNullIdx : toi[minK].contact;
             sMin = minC;
             sMinAlpha = minAlpha;
             sDone = 0;
@@ -1397,17 +877,21 @@ __device__ void Wd::solveTOI(const StepParams& P)
                     sPos[i] = make_float4(s.x, s.y, s.z, 0.0f);
                     sVel[i] = make_float4(v.x, v.y, v.z, 0.0f);
                 }
-                Solver S;
-                S.vc = vc; S.pc = pc; S.n = nContacts; S.pos = sPos; S.vel = sVel;
+                // rows 0..nBodies-1 of the scratch hold the mini island (island index == row)
                 for (int i = 0; i < nContacts; ++i) {
                     int4 ic = ci[sContact[i]];
-                    vc[i].indexA = bj[fixBody(ic.y)].z;
-                    vc[i].indexB = bj[fixBody(ic.z)].z;
+                    VelConstraint v;
+                    v.idx = make_int4(bj[fixBody(ic.y)].z, bj[fixBody(ic.z)].z, 0, 0);
+                    PosConstraint p;
+                    float4 im;
+                    ContactSetup(*this, v, p, im, sContact[i], false, 1.0f);
+                    vc[i] = v;
+                    pc[i] = p;
+                    vimp[i] = im;
                 }
-                SolverSetup(*this, S, sContact, false, 1.0f);
                 const int toiA = bj[bA].z, toiB = bj[bB].z;
                 for (int it = 0; it < 20; ++it)
-                    if (SolverPosition(S, true, toiA, toiB)) break;
+                    if (SweepPosition(pc, 0, nContacts, sPos, true, toiA, toiB)) break;
                 {
                     float4 pA = sPos[toiA], pB = sPos[toiB];
                     float4 a0 = sw0[bA];
@@ -1415,31 +899,17 @@ __device__ void Wd::solveTOI(const StepParams& P)
                     float4 b0 = sw0[bB];
                     sw0[bB] = make_float4(pB.x, pB.y, pB.z, b0.w);
                 }
-                SolverInitVelocity(*this, S);
-                for (int it = 0; it < P.velocityIterations; ++it) SolverVelocity(S);
-                float h = subDt;
+                for (int i = 0; i < nContacts; ++i) ContactInitVelocity(*this, vc[i], pc[i], sPos, sVel);
+                for (int it = 0; it < P.velocityIterations; ++it) SweepVelocity(vc, vimp, 0, nContacts, sVel);
+                const float h = subDt;
                 for (int i = 0; i < nBodies; ++i) {
                     float4 p4 = sPos[i], v4 = sVel[i];
-                    Vec2 c = V(p4.x, p4.y), v = V(v4.x, v4.y);
-                    float a = p4.z, w = v4.z;
-                    Vec2 translation = h * v;
-                    if (Dot(translation, translation) > kMaxTranslationSquared) {
-                        float ratio = kMaxTranslation / Length(translation);
-                        v.x *= ratio;
-                        v.y *= ratio;
-                    }
-                    float rotation = h * w;
-                    if (rotation * rotation > kMaxRotationSquared) {
-                        float ratio = kMaxRotation / Absf(rotation);
-                        w *= ratio;
-                    }
-                    c = c + h * v;
-                    a += h * w;
-                    sPos[i] = make_float4(c.x, c.y, a, 0.0f);
-                    sVel[i] = make_float4(v.x, v.y, w, 0.0f);
+                    IntegratePosition(p4, v4, h);
+                    sPos[i] = p4;
+                    sVel[i] = v4;
                     int b = sBody[i];
-                    sw[b] = make_float4(c.x, c.y, a, sw[b].w);
-                    vel[b] = make_float4(v.x, v.y, w, 0.0f);
+                    sw[b] = make_float4(p4.x, p4.y, p4.z, sw[b].w);
+                    vel[b] = make_float4(v4.x, v4.y, v4.z, 0.0f);
                     syncTransform(b);
                 }
                 for (int i = 0; i < nBodies; ++i) {
@@ -1466,11 +936,18 @@ __device__ void Wd::solveTOI(const StepParams& P)
 
 // ------------------------------------------------------------------ kernels
 // b2World::Step (Dynamics/b2World.cpp:899-963) for world schedule[blockIdx.x].
+// Shared memory stages the island body rows (positions, then velocities) when a world's rows fit,
+// and the accumulated impulses of its island contacts when they fit.
+constexpr int kSmemRows = 640;
+constexpr int kSmemContacts = 1024;
+
 __global__ void __launch_bounds__(128) StepKernel(Batch B, StepParams P, const int* schedule)
 {
+    extern __shared__ float4 smem[];
     Wd W;
     W.init(B, schedule ? schedule[blockIdx.x] : blockIdx.x);
     const bool newFixture = W.st->newFixture != 0;
+    const unsigned long long t0 = clock64();
     __syncthreads();
     if (tid() == 0) {
         W.st->toiEvents = 0;
@@ -1479,17 +956,28 @@ __global__ void __launch_bounds__(128) StepKernel(Batch B, StepParams P, const i
         W.st->solvedContacts = 0;
         W.st->pairsFound = 0;
         W.st->newFixture = 0;
+        for (int i = 0; i < 16; ++i) W.st->cyc[i] = 0;
     }
     __syncthreads();
     if (newFixture) W.findNewContacts();
     __syncthreads();
+    const unsigned long long t1 = clock64();
     W.collide();
-    if (W.st->stepComplete && P.dt > 0.0f) W.solve(P);
+    const unsigned long long t2 = clock64();
+    if (W.st->stepComplete && P.dt > 0.0f) W.solve(P, smem, kSmemRows, kSmemContacts);
     __syncthreads();
+    const unsigned long long t3 = clock64();
     if (W.st->continuous && P.dt > 0.0f) W.solveTOI(P);
     __syncthreads();
     for (int b = tid(); b < W.d.bodyCount; b += nthreads()) W.frc[b] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (tid() == 0 && P.dt > 0.0f) W.st->inv_dt0 = 1.0f / P.dt;
+    if (tid() == 0) {
+        if (P.dt > 0.0f) W.st->inv_dt0 = 1.0f / P.dt;
+        const unsigned long long t4 = clock64();
+        W.st->cyc[0] = t1 - t0;
+        W.st->cyc[1] = t2 - t1;
+        W.st->cyc[6] = t4 - t3;
+        W.st->cyc[7] = t4 - t0;
+    }
 }
 
 } // namespace b2g
@@ -1498,6 +986,7 @@ __global__ void __launch_bounds__(128) StepKernel(Batch B, StepParams P, const i
 cudaError_t b2gLaunchStep(const b2g::Batch& B, const b2g::StepParams& P, const int* schedule, int threads,
                           cudaStream_t stream)
 {
-    b2g::StepKernel<<<B.worlds, threads, 0, stream>>>(B, P, schedule);
+    const size_t smem = (2 * b2g::kSmemRows + b2g::kSmemContacts) * sizeof(float4);
+    b2g::StepKernel<<<B.worlds, threads, smem, stream>>>(B, P, schedule);
     return cudaGetLastError();
 }

@@ -54,6 +54,11 @@ struct WorldState {
     int solvedContacts; // island contacts solved in the last step
     int pairsFound;     // broadphase pairs produced in the last step (all UpdatePairs calls)
     int pad;
+    // SM clock cycles of the last step per phase: 0 new-fixture pairs, 1 collide, 2 island DFS,
+    // 3 island solve, 4 fixture sync, 5 pairs after solve, 6 TOI, 7 whole step; then the island solve
+    // split: 8 integrate + constraint init, 9 warm start + velocity sweeps, 10 impulses + position
+    // integration, 11 position sweeps, 12 write-back, 13 sleep, 14-15 unused
+    unsigned long long cyc[16];
 };
 
 // Revolute joint (Dynamics/Joints/b2RevoluteJoint.h), stored whole: joints are few.
@@ -75,27 +80,28 @@ struct Joint {
     float motorMass;
 };
 
-// Island solver records (Dynamics/Contacts/b2ContactSolver.cpp:34-47, b2ContactSolver.h)
-struct VelPoint { Vec2 rA, rB; float normalImpulse, tangentImpulse, normalMass, tangentMass, velocityBias; };
-struct VelConstraint {
-    VelPoint p[2];
-    Vec2 normal;
-    float K[4];          // ex.x, ex.y, ey.x, ey.y
-    float normalMass[4];
-    int indexA, indexB;
-    float invMassA, invMassB, invIA, invIB;
-    float friction, restitution, tangentSpeed;
-    int pointCount, contact;
+// Island solver records: the fields of b2ContactVelocityConstraint and b2ContactPositionConstraint
+// (Dynamics/Contacts/b2ContactSolver.h:35-56, b2ContactSolver.cpp:34-47) regrouped into 16-byte
+// vectors so a record loads with a few 128-bit loads. The accumulated impulses, the only part the
+// velocity sweeps write, live in a separate float4 per contact {normal0, tangent0, normal1, tangent1}.
+struct __align__(16) VelConstraint {
+    float4 nf;   // normal.x, normal.y, friction, tangentSpeed
+    float4 m;    // invMassA, invIA, invMassB, invIB
+    int4 idx;    // indexA (body row), indexB, pointCount, contact slot
+    float4 K;    // block matrix ex.x, ex.y, ey.x, ey.y
+    float4 NM;   // its inverse (normalMass)
+    float4 r0;   // point 0: rA.x, rA.y, rB.x, rB.y
+    float4 c0;   // point 0: normalMass, tangentMass, velocityBias, restitution
+    float4 r1;   // point 1
+    float4 c1;
 };
-struct PosConstraint {
-    Vec2 localPoints[2], localNormal, localPoint;
-    int indexA, indexB;
-    float invMassA, invMassB;
-    Vec2 localCenterA, localCenterB;
-    float invIA, invIB;
-    int type;
-    float radiusA, radiusB;
-    int pointCount;
+struct __align__(16) PosConstraint {
+    float4 lp;   // localPoints[0].xy, localPoints[1].xy
+    float4 ln;   // localNormal.xy, localPoint.xy
+    int4 idx;    // indexA, indexB, pointCount, manifold type
+    float4 m;    // invMassA, invIA, invMassB, invIB
+    float4 lc;   // localCenterA.xy, localCenterB.xy
+    float4 rad;  // radiusA, radiusB, 0, 0
 };
 struct TOITask { int contact; int kind; float alpha0; Sweep sa, sb; };
 
@@ -146,6 +152,7 @@ struct Batch {
     int* sStatus;
     VelConstraint* vc;
     PosConstraint* pc;
+    float4* vimp;    // contact-sized impulses of the island contacts (when not staged in shared memory)
     TOITask* toi;
     int4* islands;   // body-sized: {bodyStart, bodyCount, contactStart, contactCount}
     int2* islandJ;   // {jointStart, jointCount}

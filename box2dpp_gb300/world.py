@@ -106,6 +106,16 @@ class World:
                 "dynamic_bodies"]
         return dict(zip(keys, list(out)))
 
+    PHASES = ["new_pairs", "collide", "island_build", "island_solve", "fixture_sync", "pairs", "toi", "step",
+              "solve_init", "solve_velocity", "solve_store_integrate", "solve_position", "solve_writeback",
+              "solve_sleep", "unused14", "unused15"]
+
+    def profile(self) -> np.ndarray:
+        """SM clock cycles per world and phase of the last step, shape (worlds, 16) (see PHASES)."""
+        out = np.zeros(16 * self.n_worlds, dtype=np.uint64)
+        _lib.check(self.lib.gb_world_profile(self.h, out), "gb_world_profile")
+        return out.reshape(self.n_worlds, 16)
+
     @property
     def total_bodies(self) -> int:
         return int(sum(self.n_bodies))

@@ -118,6 +118,14 @@ gb_status gb_world_stats(gb_world* world, int w, int* islands, int* toi_events);
  * dynamic bodies. */
 gb_status gb_world_totals(gb_world* world, long long* out);
 
+/* Per-world SM clock cycles spent in the phases of the last step (the device counterpart of
+ * b2World::GetProfile, Box2D/Dynamics/b2World.h:196, b2Profile in b2TimeStep.h:27-37): out[16 * w + i]
+ * for i = 0 new-fixture pairs, 1 collide, 2 island build, 3 island solve, 4 fixture sync, 5 pairs,
+ * 6 continuous (TOI), 7 whole step, and the island solve split 8 integrate + constraint init,
+ * 9 warm start + velocity sweeps, 10 impulses + position integration, 11 position sweeps,
+ * 12 write-back, 13 sleep (14, 15 unused). */
+gb_status gb_world_profile(gb_world* world, unsigned long long* out);
+
 /* Whole-batch b2Body::ApplyForceToCenter + ApplyTorque for the next step (Box2D/Dynamics/b2Body.h:
  * 437-468): forces[4] per body of every world in world order then creation order = force.x,
  * force.y, torque, unused. The host array is copied to the device asynchronously on the handle's

@@ -233,6 +233,47 @@ void po_toi(int typeA, const float* sA, int nA, const float* swA, int typeB, con
 
 void po_sincosf(float x, float* s, float* c) { Rot q = RotOf(x); *s = q.s; *c = q.c; }
 
+// Island structure of the next Solve without stepping: for every island in solve order, its contacts
+// in solve order as (bodyA, bodyB, static flags). Used to study the Gauss-Seidel dependency chain.
+int po_island_contacts(void* h, int* out, int cap)
+{
+    World* w = static_cast<World*>(h);
+    int n = 0, island = 0;
+    std::vector<char> bodySeen(w->bodies.size(), 0), contactSeen(w->contacts.size(), 0);
+    std::vector<int> stack;
+    for (int seed = w->bodyList; seed != kNull; seed = w->bodies[seed].next) {
+        const Body& sb = w->bodies[seed];
+        if (bodySeen[seed] || !sb.IsAwake() || !(sb.flags & kBActive) || sb.type == kStatic) continue;
+        stack.assign(1, seed);
+        bodySeen[seed] = 1;
+        std::vector<int> statics;
+        while (!stack.empty()) {
+            int b = stack.back();
+            stack.pop_back();
+            if (w->bodies[b].type == kStatic) { statics.push_back(b); continue; }
+            for (int e = w->bodies[b].contactList; e != kNull; e = w->contacts[e >> 1].eNext[e & 1]) {
+                int c = e >> 1;
+                const Contact& ct = w->contacts[c];
+                if (contactSeen[c] || !(ct.flags & kCEnabled) || !(ct.flags & kCTouching)) continue;
+                contactSeen[c] = 1;
+                int bA = w->fixtures[ct.fA].body, bB = w->fixtures[ct.fB].body;
+                if (n < cap) {
+                    out[4 * n] = island; out[4 * n + 1] = bA; out[4 * n + 2] = bB;
+                    out[4 * n + 3] = (w->bodies[bA].type == kStatic) | ((w->bodies[bB].type == kStatic) << 1) | (ct.m.pointCount << 2);
+                }
+                ++n;
+                int other = w->EdgeOther(e);
+                if (bodySeen[other]) continue;
+                bodySeen[other] = 1;
+                stack.push_back(other);
+            }
+        }
+        for (int s : statics) bodySeen[s] = 0;
+        ++island;
+    }
+    return n;
+}
+
 void po_step_many(void** hs, int n, float dt, int vi, int pi, int steps, int threads)
 {
     if (threads < 1) threads = 1;

@@ -3,69 +3,86 @@
  *
  * The reference rotates bodies with libm's sinf/cosf (b2Rot::Set, Box2DRef/Common/b2Math.h:308-320).
  * glibc's sinf/cosf are not correctly rounded (about 1-3.6% of inputs in [2^-4, 64] differ from the
- * correctly rounded value), and a GPU cannot call glibc. So the project fixes ONE deterministic
- * float sin/cos that both the GPU kernels and this oracle evaluate identically:
+ * correctly rounded value), and a GPU cannot call glibc. So the project fixes ONE deterministic float
+ * sin/cos that the GPU kernels and this oracle evaluate identically, in float arithmetic only (GB300's
+ * FP64 is far slower than FP32):
  *
- *   1. Cody-Waite reduction in double: k = rint(x * 2/pi), r = ((x - k*P1) - k*P2) - k*P3, with
- *      pi/2 = P1 + P2 + P3, P1 and P2 holding 26 significant bits each so that k*P1 and k*P2 are
- *      exact for |k| < 2^27.
- *   2. Taylor polynomials of sin and cos on |r| <= pi/4 (terms to r^17 and r^18), Horner form,
- *      plain double multiplies and adds (no fused multiply-add, so every platform rounds alike).
- *   3. Quadrant selection by k mod 4, then one rounding to float.
+ *   1. k = rint(x * 256/pi); r = x - k*pi/256 as a float-float pair (rh, rl): pi/256 = C1 + C2 + C3,
+ *      the products k*C1 and k*C2 made exact with fused multiply-adds, the differences with TwoSum.
+ *   2. sin r = r + r^3(-1/6 + r^2/120) and cos r = 1 - r^2/2 + r^4/24 as float-float pairs
+ *      (|r| <= pi/512, so the corrections are ~1e-6 relative and float precision suffices for them).
+ *   3. sin x = S_j cos r + C_j sin r, cos x = C_j cos r - S_j sin r with the float-float table values
+ *      S_j, C_j at j = k mod 512, exact products by fused multiply-add, one final rounding to float.
  *
- * The double evaluation error is about 2^-51 relative, so the float result is the correctly rounded
- * one except with probability ~2^-26 per call. Inputs with |x| >= 2^27 are first reduced with an
- * exact fmod by the double nearest 2*pi (deterministic, not accurate: such angles are not physical).
- *
- * This file must be compiled with -ffp-contract=off. The GPU copy of this algorithm lives in the
- * package's CUDA sources; a GPU test checks the two agree bit for bit.
+ * The result is within ~2^-41 of the exact value before the last rounding, so it is the correctly
+ * rounded float except for about one input in 10^5. Inputs with |k| >= 2^24 keep the same steps
+ * (deterministic, not accurate: such angles are not physical). Compiled with -ffp-contract=off; the
+ * only fused operations are the explicit fmaf calls. The GPU copy of these steps lives in the
+ * package's CUDA sources; tests check both copies agree bit for bit.
  */
 #include <math.h>
 
+#include "trig_table.h"
+
 #define B2O_HIDDEN __attribute__((visibility("hidden")))
 
-static const double kTwoOverPi = 0x1.45f306dc9c883p-1;
-static const double kP1 = 0x1.921fb50000000p+0;
-static const double kP2 = 0x1.110b460000000p-26;
-static const double kP3 = 0x1.1a62633145c07p-54;
-static const double kTwoPi = 0x1.921fb54442d18p+2;
+static const float kTable[512 * 4] = {B2O_TRIG_TABLE_ROWS};
 
-static const double kS3 = -0x1.5555555555555p-3, kS5 = 0x1.1111111111111p-7, kS7 = -0x1.a01a01a01a01ap-13,
-                    kS9 = 0x1.71de3a556c734p-19, kS11 = -0x1.ae64567f544e4p-26, kS13 = 0x1.6124613a86d09p-33,
-                    kS15 = -0x1.ae7f3e733b81fp-41, kS17 = 0x1.952c77030ad4ap-49;
-static const double kC2 = -0.5, kC4 = 0x1.5555555555555p-5, kC6 = -0x1.6c16c16c16c17p-10,
-                    kC8 = 0x1.a01a01a01a01ap-16, kC10 = -0x1.27e4fb7789f5cp-22, kC12 = 0x1.1eed8eff8d898p-29,
-                    kC14 = -0x1.93974a8c07c9dp-37, kC16 = 0x1.ae7f3e733b81fp-45, kC18 = -0x1.6827863b97d97p-53;
-
-void b2o_sincosf(float xf, float* s_out, float* c_out)
+void b2o_sincosf(float x, float* s_out, float* c_out)
 {
-    if (xf == 0.0f) { *s_out = xf; *c_out = 1.0f; return; }
-    if (!(fabsf(xf) < INFINITY)) { *s_out = xf - xf; *c_out = xf - xf; return; }
-    double x = (double)xf;
-    if (fabs(x) >= 134217728.0) x = fmod(x, kTwoPi);
-    double k = rint(x * kTwoOverPi);
-    double r = x - k * kP1;
-    r = r - k * kP2;
-    r = r - k * kP3;
-    double r2 = r * r;
-    double ps = kS17;
-    ps = ps * r2 + kS15; ps = ps * r2 + kS13; ps = ps * r2 + kS11; ps = ps * r2 + kS9;
-    ps = ps * r2 + kS7;  ps = ps * r2 + kS5;  ps = ps * r2 + kS3;
-    double sn = r + (r * r2) * ps;
-    double pc = kC18;
-    pc = pc * r2 + kC16; pc = pc * r2 + kC14; pc = pc * r2 + kC12; pc = pc * r2 + kC10;
-    pc = pc * r2 + kC8;  pc = pc * r2 + kC6;  pc = pc * r2 + kC4;  pc = pc * r2 + kC2;
-    double cs = 1.0 + r2 * pc;
-    long long q = (long long)k & 3;
-    double s, c;
-    switch (q) {
-        case 0: s = sn;  c = cs;  break;
-        case 1: s = cs;  c = -sn; break;
-        case 2: s = -sn; c = -cs; break;
-        default: s = -cs; c = sn; break;
-    }
-    *s_out = (float)s;
-    *c_out = (float)c;
+    if (x == 0.0f) { *s_out = x; *c_out = 1.0f; return; }
+    if (!(fabsf(x) <= 3.40282347e38f)) { *s_out = x - x; *c_out = x - x; return; }
+    const float kf = rintf(x * B2O_INV_PIO256);
+    const int idx = fabsf(kf) < 16777216.0f ? ((int)kf) & 511 : ((int)fmodf(kf, 512.0f)) & 511;
+    /* r = x - k*pi/256 in float-float */
+    const float p = kf * B2O_PIO256_1;
+    const float pe = fmaf(kf, B2O_PIO256_1, -p);
+    const float t = x - p;
+    const float q = kf * B2O_PIO256_2;
+    const float qe = fmaf(kf, B2O_PIO256_2, -q);
+    const float s1 = t - pe;
+    const float b1 = s1 - t;
+    const float s1e = (t - (s1 - b1)) + (-pe - b1);
+    const float s2 = s1 - q;
+    const float b2 = s2 - s1;
+    const float s2e = (s1 - (s2 - b2)) + (-q - b2);
+    const float lo = ((s1e + s2e) - qe) - kf * B2O_PIO256_3;
+    const float rh = s2 + lo;
+    const float rl = lo - (rh - s2);
+    /* sin r, cos r */
+    const float r2 = rh * rh;
+    const float ts = (rh * r2) * (-0x1.555556p-3f + 0x1.111112p-7f * r2);
+    const float sh = rh;
+    const float sl = rl + ts;
+    const float pl = fmaf(rh, rh, -r2);
+    const float uh = 0.5f * r2;
+    const float ul = 0.5f * pl + rh * rl;
+    const float w = (r2 * r2) * 0x1.555556p-5f;
+    const float ch = 1.0f - uh;
+    const float b3 = ch - 1.0f;
+    const float che = (1.0f - (ch - b3)) + (-uh - b3);
+    const float cl = che + (w - ul);
+    /* table */
+    const float Sh = kTable[4 * idx], Sl = kTable[4 * idx + 1], Ch = kTable[4 * idx + 2], Cl = kTable[4 * idx + 3];
+    /* sin x = S cos r + C sin r */
+    const float a1 = Sh * ch;
+    const float a1l = fmaf(Sh, ch, -a1) + (Sh * cl + Sl * ch);
+    const float a2 = Ch * sh;
+    const float a2l = fmaf(Ch, sh, -a2) + (Ch * sl + Cl * sh);
+    const float sa = a1 + a2;
+    const float b4 = sa - a1;
+    const float sae = (a1 - (sa - b4)) + (a2 - b4);
+    /* cos x = C cos r - S sin r */
+    const float c1 = Ch * ch;
+    const float c1l = fmaf(Ch, ch, -c1) + (Ch * cl + Cl * ch);
+    const float P = Sh * sh;
+    const float c2 = -P;
+    const float c2l = -fmaf(Sh, sh, -P) - (Sh * sl + Sl * sh);
+    const float ca = c1 + c2;
+    const float b5 = ca - c1;
+    const float cae = (c1 - (ca - b5)) + (c2 - b5);
+    *s_out = sa + ((sae + a1l) + a2l);
+    *c_out = ca + ((cae + c1l) + c2l);
 }
 
 float b2o_sinf(float x) { float s, c; b2o_sincosf(x, &s, &c); return s; }
