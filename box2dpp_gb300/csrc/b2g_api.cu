@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <numeric>
 #include <vector>
@@ -953,3 +954,97 @@ gb_status gb_collide(int n, const int* type_a, const float* shape_a, const int* 
 const char* gb_version(void) { return "box2d_gb300 0.1 (Box2D 2.3.2 step semantics, sm_103a)"; }
 
 } // extern "C"
+
+// ------------------------------------------------------------------ narrowphase without allocation
+// gb_collide_noalloc stages its inputs and outputs in one fixed device buffer defined here (static
+// device storage for GB_COLLIDE_NOALLOC_MAX_PAIRS pairs) instead of allocating per call. The
+// buffer's address is resolved once per device, with that device current, and cached.
+namespace {
+
+constexpr int kNoAllocMaxDevices = 64;
+constexpr size_t RoundUp256(size_t x) { return (x + 255) & ~size_t(255); }
+constexpr size_t kNaShapes = RoundUp256(sizeof(Shape) * GB_COLLIDE_NOALLOC_MAX_PAIRS);
+constexpr size_t kNaXf = RoundUp256(sizeof(float4) * GB_COLLIDE_NOALLOC_MAX_PAIRS);
+constexpr size_t kNaOi = RoundUp256(sizeof(int4) * GB_COLLIDE_NOALLOC_MAX_PAIRS);
+constexpr size_t kNaOf = RoundUp256(3 * sizeof(float4) * GB_COLLIDE_NOALLOC_MAX_PAIRS);
+constexpr size_t kNaBytes = 2 * kNaShapes + 2 * kNaXf + kNaOi + kNaOf;
+
+} // namespace
+
+static __device__ __align__(256) unsigned char gCollideScratch[kNaBytes];
+
+namespace {
+
+std::mutex gCollideScratchMutex;
+unsigned char* gCollideScratchAddr[kNoAllocMaxDevices];
+
+gb_status CollideScratch(unsigned char** out)
+{
+    int dev = -1;
+    GB_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return GB_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(gCollideScratchMutex);
+    if (gCollideScratchAddr[dev] == nullptr) {
+        void* p = nullptr;
+        GB_CUDA(cudaGetSymbolAddress(&p, gCollideScratch));
+        gCollideScratchAddr[dev] = static_cast<unsigned char*>(p);
+    }
+    *out = gCollideScratchAddr[dev];
+    return GB_OK;
+}
+
+} // namespace
+
+extern "C" gb_status gb_collide_noalloc(int n, const int* type_a, const float* shape_a, const int* n_a,
+                                        const float* xf_a, const int* type_b, const float* shape_b, const int* n_b,
+                                        const float* xf_b, int* out_ints, float* out_floats)
+{
+    if (n <= 0) return GB_OK;
+    if (n > GB_COLLIDE_NOALLOC_MAX_PAIRS) {
+        std::fprintf(stderr, "box2d_gb300: gb_collide_noalloc: %d pairs exceed the fixed buffer of %d\n", n,
+                     GB_COLLIDE_NOALLOC_MAX_PAIRS);
+        return GB_ERR_CAPACITY;
+    }
+    if (!type_a || !shape_a || !n_a || !xf_a || !type_b || !shape_b || !n_b || !xf_b || !out_ints || !out_floats)
+        return GB_ERR_INVALID;
+    // the pair rules of gb_collide, checked before any device work
+    for (int i = 0; i < n; ++i) {
+        const int ta = type_a[i], tb = type_b[i];
+        if (ta < 0 || ta > 3 || tb < 0 || tb > 3) return GB_ERR_INVALID;
+        if (ta == 0 && tb != 0) return GB_ERR_INVALID;
+        if (ta >= 2 && tb == 1) return GB_ERR_INVALID;
+        if (ta == 1 && tb == 1) return GB_ERR_INVALID;
+    }
+    unsigned char* base = nullptr;
+    gb_status s = CollideScratch(&base);
+    if (s != GB_OK) return s;
+    Shape* dsa = reinterpret_cast<Shape*>(base);
+    Shape* dsb = reinterpret_cast<Shape*>(base + kNaShapes);
+    float4* dxa = reinterpret_cast<float4*>(base + 2 * kNaShapes);
+    float4* dxb = reinterpret_cast<float4*>(base + 2 * kNaShapes + kNaXf);
+    int4* doi = reinterpret_cast<int4*>(base + 2 * kNaShapes + 2 * kNaXf);
+    float4* dof = reinterpret_cast<float4*>(base + 2 * kNaShapes + 2 * kNaXf + kNaOi);
+    // host-side shape setup in chunks on the stack; a synchronous copy from pageable memory returns
+    // once the source has been consumed, so the chunk buffers are reused safely
+    constexpr int kChunk = 64;
+    Shape sa[kChunk], sb[kChunk];
+    float4 xa[kChunk], xb[kChunk];
+    for (int i0 = 0; i0 < n; i0 += kChunk) {
+        const int m = std::min(kChunk, n - i0);
+        for (int k = 0; k < m; ++k) {
+            const int i = i0 + k;
+            sa[k] = MakeShape(type_a[i], shape_a + 16 * i, n_a[i]);
+            sb[k] = MakeShape(type_b[i], shape_b + 16 * i, n_b[i]);
+            xa[k] = make_float4(xf_a[4 * i], xf_a[4 * i + 1], xf_a[4 * i + 2], xf_a[4 * i + 3]);
+            xb[k] = make_float4(xf_b[4 * i], xf_b[4 * i + 1], xf_b[4 * i + 2], xf_b[4 * i + 3]);
+        }
+        GB_CUDA(cudaMemcpy(dsa + i0, sa, m * sizeof(Shape), cudaMemcpyHostToDevice));
+        GB_CUDA(cudaMemcpy(dsb + i0, sb, m * sizeof(Shape), cudaMemcpyHostToDevice));
+        GB_CUDA(cudaMemcpy(dxa + i0, xa, m * sizeof(float4), cudaMemcpyHostToDevice));
+        GB_CUDA(cudaMemcpy(dxb + i0, xb, m * sizeof(float4), cudaMemcpyHostToDevice));
+    }
+    GB_CUDA(b2gLaunchCollide(n, dsa, dxa, dsb, dxb, doi, dof, 0));
+    GB_CUDA(cudaMemcpy(out_ints, doi, n * sizeof(int4), cudaMemcpyDeviceToHost));
+    GB_CUDA(cudaMemcpy(out_floats, dof, 3 * n * sizeof(float4), cudaMemcpyDeviceToHost));
+    return GB_OK;
+}

@@ -154,3 +154,18 @@ def collide(type_a, shape_a, n_a, xf_a, type_b, shape_b, n_b, xf_b):
                               f(xf_a, (n, 4), np.float32), f(type_b, n, np.int32), f(shape_b, (n, 16), np.float32),
                               f(n_b, n, np.int32), f(xf_b, (n, 4), np.float32), oi, of), "gb_collide")
     return oi, of
+
+
+def collide_noalloc(type_a, shape_a, n_a, xf_a, type_b, shape_b, n_b, xf_b):
+    """``collide`` through gb_collide_noalloc: the same narrowphase with inputs and outputs staged in
+    the library's fixed device buffer (at most ``_lib.COLLIDE_NOALLOC_MAX_PAIRS`` pairs per call)."""
+    lib = _lib.load()
+    n = len(type_a)
+    f = lambda a, shp, dt: np.ascontiguousarray(np.asarray(a, dtype=dt).reshape(shp))
+    oi = np.zeros((n, 4), dtype=np.int32)
+    of = np.zeros((n, 12), dtype=np.float32)
+    _lib.check(lib.gb_collide_noalloc(n, f(type_a, n, np.int32), f(shape_a, (n, 16), np.float32),
+                                      f(n_a, n, np.int32), f(xf_a, (n, 4), np.float32), f(type_b, n, np.int32),
+                                      f(shape_b, (n, 16), np.float32), f(n_b, n, np.int32),
+                                      f(xf_b, (n, 4), np.float32), oi, of), "gb_collide_noalloc")
+    return oi, of

@@ -147,6 +147,19 @@ gb_status gb_collide(int n, const int* type_a, const float* shape_a, const int* 
                      const int* type_b, const float* shape_b, const int* n_b, const float* xf_b,
                      int* out_ints, float* out_floats);
 
+/* No counterpart in the reference. gb_collide with no device memory allocation: inputs and outputs
+ * are staged in one fixed device buffer defined in the library (static device storage, about
+ * 1.7 MB, for at most GB_COLLIDE_NOALLOC_MAX_PAIRS pairs) instead of buffers allocated per call.
+ * Arguments, pair rules and output as gb_collide. n > GB_COLLIDE_NOALLOC_MAX_PAIRS returns
+ * GB_ERR_CAPACITY before any device work. The buffer is shared by every call on a device: calls
+ * whose device work overlaps (for example from several host threads) race on it, so the caller
+ * serialises them. The first call on each device resolves the buffer's address
+ * (cudaGetSymbolAddress) and should come before any CUDA stream capture. */
+#define GB_COLLIDE_NOALLOC_MAX_PAIRS 4096
+gb_status gb_collide_noalloc(int n, const int* type_a, const float* shape_a, const int* n_a, const float* xf_a,
+                             const int* type_b, const float* shape_b, const int* n_b, const float* xf_b,
+                             int* out_ints, float* out_floats);
+
 /* Library version string. */
 const char* gb_version(void);
 
