@@ -14,6 +14,7 @@ from . import build as _build
 
 GB_OK, GB_ERR_CAPACITY, GB_ERR_TIMEOUT, GB_ERR_INVALID, GB_ERR_CUDA = 0, 1, 2, 3, 4
 COLLIDE_NOALLOC_MAX_PAIRS = 4096  # GB_COLLIDE_NOALLOC_MAX_PAIRS
+SOLVER_PLAIN, SOLVER_COLOURED = 0, 1
 STATUS_NAMES = {0: "GB_OK", 1: "GB_ERR_CAPACITY", 2: "GB_ERR_TIMEOUT", 3: "GB_ERR_INVALID", 4: "GB_ERR_CUDA"}
 
 # Every symbol include/box2d_gb300.h declares.
@@ -22,7 +23,7 @@ EXPORTS = [
     "gb_build_world", "gb_world_upload", "gb_world_step", "gb_world_sync", "gb_world_set_stream",
     "gb_world_counts", "gb_get_bodies", "gb_get_contacts", "gb_get_proxies", "gb_world_stats", "gb_sincos",
     "gb_collide", "gb_version", "gb_world_totals", "gb_set_forces", "gb_get_transforms", "gb_world_profile",
-    "gb_collide_noalloc",
+    "gb_collide_noalloc", "gb_world_set_solver", "gb_world_solver_stats",
 ]
 
 
@@ -77,6 +78,8 @@ def load(build_if_missing: bool = True):
         "gb_sincos": [_f32, _f32, _f32, i],
         "gb_collide": [i, _i32, _f32, _i32, _f32, _i32, _f32, _i32, _f32, _i32, _f32],
         "gb_collide_noalloc": [i, _i32, _f32, _i32, _f32, _i32, _f32, _i32, _f32, _i32, _f32],
+        "gb_world_set_solver": [vp, i, f, i],
+        "gb_world_solver_stats": [vp, _i32, _i32, _f32],
         "gb_world_totals": [vp, C.POINTER(C.c_longlong)],
         "gb_set_forces": [vp, vp],
         "gb_get_transforms": [vp, vp],

@@ -91,6 +91,9 @@ struct gb_world {
     bool hostDirty = true;   // host mirror has changes not yet uploaded
     int threads = 64;
     bool locked = false;
+    int solver = kSolverPlain;
+    float tolerance = 0.0f;
+    int measureResidual = 0;
 };
 
 namespace {
@@ -332,8 +335,8 @@ gb_status Upload(gb_world* g)
     ALLOC(order, tc); ALLOC(cnext, tc);
     ALLOC(joint, tj); ALLOC(sJoint, tj);
     ALLOC(sBody, tr); ALLOC(sStack, tb); ALLOC(sWake, tb); ALLOC(sPos, tr); ALLOC(sVel, tr); ALLOC(islands, tb);
-    ALLOC(islandJ, tb); ALLOC(sleepOut, tb);
-    ALLOC(sContact, tc); ALLOC(sStatus, tc); ALLOC(vc, tc); ALLOC(pc, tc); ALLOC(vimp, tc); ALLOC(toi, tc);
+    ALLOC(islandJ, tb); ALLOC(sleepOut, tb); ALLOC(rowMask, tr);
+    ALLOC(sContact, tc); ALLOC(sStatus, tc); ALLOC(vc, tc); ALLOC(pc, tc); ALLOC(vimp, tc); ALLOC(toi, tc); ALLOC(cColour, tc); ALLOC(colourList, tc);
     ALLOC(pairs, tq); ALLOC(pairKeep, tq);
 #undef ALLOC
     GB_CUDA(cudaMemcpy(B.desc, g->desc.data(), nw * sizeof(WorldDesc), cudaMemcpyHostToDevice));
@@ -642,6 +645,10 @@ gb_status gb_world_step(gb_world* g, float dt, int vi, int pi)
     P.velocityIterations = vi;
     P.positionIterations = pi;
     P.maxToiEvents = 4096;
+    P.solver = g->solver;
+    P.tolerance = g->tolerance;
+    P.measureResidual = g->measureResidual;
+    P.pad = 0;
     return cudaErr(b2gLaunchStep(g->batch, P, g->dSchedule, g->threads, g->stream));
 }
 
@@ -658,6 +665,38 @@ gb_status gb_world_sync(gb_world* g)
     if (err & kErrCapacity) return GB_ERR_CAPACITY;
     if (err & kErrTimeout) return GB_ERR_TIMEOUT;
     if (err & kErrInvalid) return GB_ERR_INVALID;
+    return GB_OK;
+}
+
+gb_status gb_world_set_solver(gb_world* g, int solver, float tolerance, int measure_residual)
+{
+    if (!g || (solver != kSolverPlain && solver != kSolverColoured) || !(tolerance >= 0.0f)) return GB_ERR_INVALID;
+    g->solver = solver;
+    g->tolerance = tolerance;
+    g->measureResidual = measure_residual ? 1 : 0;
+    return GB_OK;
+}
+
+gb_status gb_world_solver_stats(gb_world* g, int* colours, int* vel_iters, float* residual)
+{
+    if (!g) return GB_ERR_INVALID;
+    const int nw = (int)g->worlds.size();
+    if (!g->onDevice) {
+        for (int i = 0; i < nw; ++i) {
+            if (colours) colours[i] = 0;
+            if (vel_iters) vel_iters[i] = 0;
+            if (residual) residual[i] = 0.0f;
+        }
+        return GB_OK;
+    }
+    GB_CUDA(cudaStreamSynchronize(g->stream));
+    std::vector<WorldState> st(nw);
+    GB_CUDA(cudaMemcpy(st.data(), g->batch.state, nw * sizeof(WorldState), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < nw; ++i) {
+        if (colours) colours[i] = st[i].colours;
+        if (vel_iters) vel_iters[i] = st[i].velIters;
+        if (residual) residual[i] = st[i].residual;
+    }
     return GB_OK;
 }
 

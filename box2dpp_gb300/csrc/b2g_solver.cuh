@@ -300,11 +300,18 @@ __device__ __forceinline__ void ContactSolvePosition(const PosConstraint& p, flo
     pos[ib] = make_float4(cB.x, cB.y, aB, 0.0f);
 }
 
-// Sequential sweeps over one island's constraints [lo, hi), prefetching the next record.
+// Sequential sweeps over one island's constraints [lo, hi). The records are read-only during a sweep
+// and their addresses are known ahead, so the records kSweepPrefetch places ahead are prefetched into
+// L1 while the current one is solved (an L2 round trip is longer than one contact solve).
+#ifndef B2G_SWEEP_PREFETCH
+#define B2G_SWEEP_PREFETCH 4
+#endif
+constexpr int kSweepPrefetch = B2G_SWEEP_PREFETCH;
 __device__ void SweepVelocity(const VelConstraint* vc, float4* imp, int lo, int hi, float4* vel)
 {
+    for (int i = lo; i < lo + kSweepPrefetch && i < hi; ++i) PrefetchRecord(vc + i);
     for (int i = lo; i < hi; ++i) {
-        if (i + 1 < hi) PrefetchRecord(vc + i + 1);
+        if (i + kSweepPrefetch < hi) PrefetchRecord(vc + i + kSweepPrefetch);
         const VelConstraint v = vc[i];
         float4 im = imp[i];
         ContactSolveVelocity(v, im, vel);
@@ -314,8 +321,9 @@ __device__ void SweepVelocity(const VelConstraint* vc, float4* imp, int lo, int 
 __device__ bool SweepPosition(const PosConstraint* pc, int lo, int hi, float4* pos, bool toi, int toiA, int toiB)
 {
     float minSeparation = 0.0f;
+    for (int i = lo; i < lo + kSweepPrefetch && i < hi; ++i) PrefetchRecord(pc + i);
     for (int i = lo; i < hi; ++i) {
-        if (i + 1 < hi) PrefetchRecord(pc + i + 1);
+        if (i + kSweepPrefetch < hi) PrefetchRecord(pc + i + kSweepPrefetch);
         const PosConstraint p = pc[i];
         ContactSolvePosition(p, pos, toi, toiA, toiB, minSeparation);
     }
@@ -537,20 +545,61 @@ __device__ inline void IntegratePosition(float4& p4, float4& v4, float h)
     v4 = make_float4(v.x, v.y, w, 0.0f);
 }
 
+// ------------------------------------------------------------------ residual
+// Velocity residual of one contact (m/s): for every point, |vn - velocityBias| where the normal
+// impulse is positive (active) and max(0, velocityBias - vn) where it is zero (the complementarity
+// violation), and |vt| where the friction impulse is below its bound (not saturated). Used to judge
+// solver variants at matched accuracy; it does not change the solution.
+__device__ float ContactResidual(const VelConstraint& v, const float4 imp, const float4* vel)
+{
+    const float4 va = vel[v.idx.x], vb = vel[v.idx.y];
+    const Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    const Vec2 normal = V(v.nf.x, v.nf.y), tangent = Cross(normal, 1.0f);
+    float r = 0.0f;
+    for (int j = 0; j < v.idx.z; ++j) {
+        const float4 rr = j == 0 ? v.r0 : v.r1;
+        const float4 cc = j == 0 ? v.c0 : v.c1;
+        const float ni = j == 0 ? imp.x : imp.z, ti = j == 0 ? imp.y : imp.w;
+        const Vec2 dv = vB + Cross(vb.z, V(rr.z, rr.w)) - vA - Cross(va.z, V(rr.x, rr.y));
+        const float vn = Dot(dv, normal);
+        const float rn = ni > 0.0f ? fabsf(vn - cc.z) : fmaxf(0.0f, cc.z - vn);
+        r = fmaxf(r, rn);
+        const float vt = Dot(dv, tangent) - v.nf.w;
+        if (fabsf(ti) < v.nf.z * ni) r = fmaxf(r, fabsf(vt));
+    }
+    return r;
+}
+
+// CTA-wide maximum of non-negative floats (their bit patterns order as integers).
+__device__ float ctaMaxNonNeg(float x, int* slot)
+{
+    __syncthreads();
+    if (tid() == 0) *slot = 0;
+    __syncthreads();
+    for (int o = 16; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
+    if ((tid() & 31) == 0 && x > 0.0f) atomicMax(slot, __float_as_int(x));
+    __syncthreads();
+    return __int_as_float(*slot);
+}
+
 // ------------------------------------------------------------------ island solve
 // b2Island::Solve (Dynamics/b2Island.cpp:185-384) for all islands of the world at once. Per-body and
 // per-contact work that the reference does in independent loops (integration, constraint setup and
-// initialisation, impulse storage, write-back) is spread over the CTA; the order-dependent work (warm
-// start, velocity and position sweeps, joints, sleep) runs per island on one thread.
+// initialisation, impulse storage, write-back) is spread over the CTA. The order-dependent work runs
+// either per island on one thread in the reference's order (kSolverPlain), or colour by colour with
+// the constraints of a colour spread over the CTA (kSolverColoured, colourStart != nullptr: contacts
+// colourList[colourStart[k] .. colourStart[k+1]) have colour k; joints stay per island).
 __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int nContacts, float4* smem, int smemRows,
-                                 int smemContacts)
+                                 int smemContacts, const int* colourStart)
 {
+    __shared__ int sFlag, sRes;
     unsigned long long tStamp = clock64();
     const float h = P.dt;
     const float dtRatio = st->inv_dt0 * P.dt;
     const bool warm = st->warmStarting != 0;
     const float gx = st->gx, gy = st->gy;
     const bool rowsInSmem = nRows <= smemRows;
+    const bool coloured = colourStart != nullptr;
     float4* pos = rowsInSmem ? smem : sPos;
     float4* vel = rowsInSmem ? smem + smemRows : sVel;
     float4* imp = nContacts <= smemContacts ? smem + 2 * smemRows : vimp;
@@ -588,19 +637,99 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
     }
     __syncthreads();
     if (tid() == 0) { unsigned long long now = clock64(); st->cyc[8] = now - tStamp; tStamp = now; }
-    // order-dependent velocity phase per island
-    for (int isl = tid(); isl < nIsl; isl += nthreads()) {
-        int4 I = islands[isl];
-        int2 J = islandJ[isl];
-        const int lo = I.z, hi = I.z + I.w;
-        if (warm)
-            for (int i = lo; i < hi; ++i) ContactWarmStart(vc[i], imp[i], vel);
-        for (int k = 0; k < J.y; ++k) RevInit(*this, jt[sJoint[J.x + k]], pos, vel, warm, dtRatio);
-        for (int it = 0; it < P.velocityIterations; ++it) {
-            for (int k = 0; k < J.y; ++k) RevSolveVelocity(jt[sJoint[J.x + k]], vel, h);
-            SweepVelocity(vc, imp, lo, hi, vel);
+    int itersRun = P.velocityIterations;
+    if (!coloured) {
+        // order-dependent velocity phase per island, the reference's order
+        if (tid() == 0) sFlag = 0;
+        __syncthreads();
+        for (int isl = tid(); isl < nIsl; isl += nthreads()) {
+            int4 I = islands[isl];
+            int2 J = islandJ[isl];
+            const int lo = I.z, hi = I.z + I.w;
+            if (warm)
+                for (int i = lo; i < hi; ++i) ContactWarmStart(vc[i], imp[i], vel);
+            for (int k = 0; k < J.y; ++k) RevInit(*this, jt[sJoint[J.x + k]], pos, vel, warm, dtRatio);
+            int it = 0;
+            for (; it < P.velocityIterations; ++it) {
+                if (P.tolerance > 0.0f) {
+                    float r = 0.0f;
+                    for (int i = lo; i < hi; ++i) r = fmaxf(r, ContactResidual(vc[i], imp[i], vel));
+                    if (r <= P.tolerance) break;
+                }
+                for (int k = 0; k < J.y; ++k) RevSolveVelocity(jt[sJoint[J.x + k]], vel, h);
+                SweepVelocity(vc, imp, lo, hi, vel);
+            }
+            atomicMax(&sFlag, it);
         }
+        __syncthreads();
+        itersRun = sFlag;
+    } else {
+        // colour by colour: warm start, joint initialisation per island, then the iterations
+        const int nCol = kColours;
+        if (warm) {
+            for (int k = 0; k < nCol; ++k) {
+                const int lo = colourStart[k], hi = colourStart[k + 1];
+                if (lo == hi) continue;
+                if (k == kSerialColour) {
+                    if (tid() == 0)
+                        for (int q = lo; q < hi; ++q) ContactWarmStart(vc[colourList[q]], imp[colourList[q]], vel);
+                } else {
+                    for (int q = lo + tid(); q < hi; q += nthreads()) ContactWarmStart(vc[colourList[q]], imp[colourList[q]], vel);
+                }
+                __syncthreads();
+            }
+        }
+        for (int isl = tid(); isl < nIsl; isl += nthreads()) {
+            int2 J = islandJ[isl];
+            for (int k = 0; k < J.y; ++k) RevInit(*this, jt[sJoint[J.x + k]], pos, vel, warm, dtRatio);
+        }
+        __syncthreads();
+        int it = 0;
+        for (; it < P.velocityIterations; ++it) {
+            if (P.tolerance > 0.0f) {
+                float r = 0.0f;
+                for (int i = tid(); i < nContacts; i += nthreads()) r = fmaxf(r, ContactResidual(vc[i], imp[i], vel));
+                if (ctaMaxNonNeg(r, &sRes) <= P.tolerance) break;
+            }
+            if (d.jointCount > 0) {
+                for (int isl = tid(); isl < nIsl; isl += nthreads()) {
+                    int2 J = islandJ[isl];
+                    for (int k = 0; k < J.y; ++k) RevSolveVelocity(jt[sJoint[J.x + k]], vel, h);
+                }
+                __syncthreads();
+            }
+            for (int k = 0; k < nCol; ++k) {
+                const int lo = colourStart[k], hi = colourStart[k + 1];
+                if (lo == hi) continue;
+                if (k == kSerialColour) {
+                    if (tid() == 0)
+                        for (int q = lo; q < hi; ++q) {
+                            const int i = colourList[q];
+                            float4 im = imp[i];
+                            ContactSolveVelocity(vc[i], im, vel);
+                            imp[i] = im;
+                        }
+                } else {
+                    for (int q = lo + tid(); q < hi; q += nthreads()) {
+                        const int i = colourList[q];
+                        const VelConstraint v = vc[i];
+                        float4 im = imp[i];
+                        ContactSolveVelocity(v, im, vel);
+                        imp[i] = im;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        itersRun = it;
     }
+    if (P.measureResidual) {
+        float r = 0.0f;
+        for (int i = tid(); i < nContacts; i += nthreads()) r = fmaxf(r, ContactResidual(vc[i], imp[i], vel));
+        r = ctaMaxNonNeg(r, &sRes);
+        if (tid() == 0) st->residual = r;
+    }
+    if (tid() == 0) st->velIters = itersRun;
     __syncthreads();
     if (tid() == 0) { unsigned long long now = clock64(); st->cyc[9] = now - tStamp; tStamp = now; }
     // impulses back to the manifolds, positions integrated, both in parallel
@@ -613,21 +742,58 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
     }
     __syncthreads();
     if (tid() == 0) { unsigned long long now = clock64(); st->cyc[10] = now - tStamp; tStamp = now; }
-    // order-dependent position phase per island
-    for (int isl = tid(); isl < nIsl; isl += nthreads()) {
-        int4 I = islands[isl];
-        int2 J = islandJ[isl];
+    if (!coloured) {
+        // order-dependent position phase per island
+        for (int isl = tid(); isl < nIsl; isl += nthreads()) {
+            int4 I = islands[isl];
+            int2 J = islandJ[isl];
+            bool positionSolved = false;
+            for (int it = 0; it < P.positionIterations; ++it) {
+                bool contactsOkay = SweepPosition(pc, I.z, I.z + I.w, pos, false, -1, -1);
+                bool jointsOkay = true;
+                for (int k = 0; k < J.y; ++k) {
+                    bool ok = RevSolvePosition(jt[sJoint[J.x + k]], pos);
+                    jointsOkay = jointsOkay && ok;
+                }
+                if (contactsOkay && jointsOkay) { positionSolved = true; break; }
+            }
+            sleepOut[isl] = positionSolved ? 1 : 0;
+        }
+    } else {
+        // colour by colour; the early exit is taken for the whole world at once
         bool positionSolved = false;
         for (int it = 0; it < P.positionIterations; ++it) {
-            bool contactsOkay = SweepPosition(pc, I.z, I.z + I.w, pos, false, -1, -1);
-            bool jointsOkay = true;
-            for (int k = 0; k < J.y; ++k) {
-                bool ok = RevSolvePosition(jt[sJoint[J.x + k]], pos);
-                jointsOkay = jointsOkay && ok;
+            float minSep = 0.0f;
+            for (int k = 0; k < kColours; ++k) {
+                const int lo = colourStart[k], hi = colourStart[k + 1];
+                if (lo == hi) continue;
+                if (k == kSerialColour) {
+                    if (tid() == 0)
+                        for (int q = lo; q < hi; ++q) ContactSolvePosition(pc[colourList[q]], pos, false, -1, -1, minSep);
+                } else {
+                    for (int q = lo + tid(); q < hi; q += nthreads()) {
+                        const PosConstraint p = pc[colourList[q]];
+                        ContactSolvePosition(p, pos, false, -1, -1, minSep);
+                    }
+                }
+                __syncthreads();
             }
-            if (contactsOkay && jointsOkay) { positionSolved = true; break; }
+            bool jointsOkay = true;
+            if (d.jointCount > 0) {
+                for (int isl = tid(); isl < nIsl; isl += nthreads()) {
+                    int2 J = islandJ[isl];
+                    for (int k = 0; k < J.y; ++k) {
+                        bool ok = RevSolvePosition(jt[sJoint[J.x + k]], pos);
+                        jointsOkay = jointsOkay && ok;
+                    }
+                }
+            }
+            // every thread reports its worst separation (as a violation >= 0) and joint state
+            const float violation = fmaxf(0.0f, -minSep);
+            const float worst = ctaMaxNonNeg(jointsOkay ? violation : 1e30f, &sRes);
+            if (worst <= 3.0f * kLinearSlop) { positionSolved = true; break; }
         }
-        sleepOut[isl] = positionSolved ? 1 : 0;
+        for (int isl = tid(); isl < nIsl; isl += nthreads()) sleepOut[isl] = positionSolved ? 1 : 0;
     }
     __syncthreads();
     if (tid() == 0) { unsigned long long now = clock64(); st->cyc[11] = now - tStamp; tStamp = now; }

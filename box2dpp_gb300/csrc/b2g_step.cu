@@ -53,6 +53,9 @@ struct Wd {
     int2* islandJ;
     int* sJoint;
     int* sleepOut;
+    int* cColour;
+    int* colourList;
+    unsigned long long* rowMask;
     unsigned long long* pairs;
     int* pairKeep;
     int* movedList;
@@ -70,9 +73,11 @@ struct Wd {
         order = B.order + c; cnext = B.cnext + c;
         jt = B.joint + j; sJoint = B.sJoint + j;
         sBody = B.sBody + d.rowBase; sPos = B.sPos + d.rowBase; sVel = B.sVel + d.rowBase;
+        rowMask = B.rowMask + d.rowBase;
         sStack = B.sStack + b; sWake = B.sWake + b;
         islands = B.islands + b; islandJ = B.islandJ + b; sleepOut = B.sleepOut + b;
         sContact = B.sContact + c; sStatus = B.sStatus + c; vc = B.vc + c; pc = B.pc + c; vimp = B.vimp + c; toi = B.toi + c;
+        cColour = B.cColour + c; colourList = B.colourList + c;
         pairs = B.pairs + q; pairKeep = B.pairKeep + q;
     }
 
@@ -284,7 +289,7 @@ struct Wd {
     __device__ void collide();
     __device__ void solve(const StepParams& P, float4* smem, int smemRows, int smemContacts);
     __device__ void solveIslands(const StepParams& P, int nIsl, int nRows, int nContacts, float4* smem, int smemRows,
-                                 int smemContacts);
+                                 int smemContacts, const int* colourStart);
     __device__ void solveTOI(const StepParams& P);
     __device__ void destroyContact(int c);
 };
@@ -553,12 +558,20 @@ __device__ void Wd::collide()
 __device__ void Wd::solve(const StepParams& P, float4* smem, int smemRows, int smemContacts)
 {
     __shared__ int sIslands, sRows, sCons;
+    __shared__ int sColourStart[kColours + 1], sColourCursor[kColours];
     const unsigned long long tSolve0 = clock64();
     const int nb = d.bodyCount, nc = st->contactCount;
+    const bool coloured = P.solver == kSolverColoured;
     for (int b = tid(); b < nb; b += nthreads()) bi[b].y &= ~kBIsland;
     for (int k = tid(); k < nc; k += nthreads()) ci[order[k]].x &= ~kCIsland;
     for (int j = tid(); j < d.jointCount; j += nthreads()) jt[j].islandFlag = 0;
+    for (int k = tid(); k <= kColours; k += nthreads()) sColourStart[k] = 0;
     __syncthreads();
+    // Colour masks of the island body rows while the DFS runs: in the (still unused) shared-memory
+    // row area when the row fits there, else in the global row scratch.
+    unsigned long long* smemMask = reinterpret_cast<unsigned long long*>(smem);
+    const int smemMaskRows = 2 * smemRows;
+    auto mask = [&](int r) -> unsigned long long& { return r < smemMaskRows ? smemMask[r] : rowMask[r]; };
     if (tid() == 0) {
         int nIsl = 0, bCur = 0, cCur = 0, jCur = 0, movers = 0;
         for (int seed = st->bodyList; seed != kNullIdx; seed = bj[seed].y) {
@@ -574,6 +587,7 @@ __device__ void Wd::solve(const StepParams& P, float4* smem, int smemRows, int s
                 int b = sStack[--stackCount];
                 if (bCur >= d.rowCap) { atomicOr(&st->error, kErrCapacity); stackCount = 0; break; }
                 bj[b].z = bCur - bStart;
+                if (coloured) mask(bCur) = 0ull;
                 sBody[bCur++] = b;
                 if (bi[b].x != kStatic) ++movers;
                 setAwake(b, true);
@@ -610,7 +624,23 @@ __device__ void Wd::solve(const StepParams& P, float4* smem, int smemRows, int s
             // in several islands and its island index is overwritten by each island's DFS.
             for (int i = cStart; i < cCur; ++i) {
                 int4 info = ci[sContact[i]];
-                vc[i].idx = make_int4(bStart + bj[fixBody(info.y)].z, bStart + bj[fixBody(info.z)].z, 0, 0);
+                const int bA = fixBody(info.y), bB = fixBody(info.z);
+                const int rA = bStart + bj[bA].z, rB = bStart + bj[bB].z;
+                vc[i].idx = make_int4(rA, rB, 0, 0);
+                if (coloured) {
+                    // Greedy colouring in island order: the lowest colour used by neither dynamic
+                    // body. Static and kinematic bodies take no impulse, so they constrain nothing.
+                    const bool dA = bi[bA].x == kDynamic, dB = bi[bB].x == kDynamic;
+                    const unsigned long long used = (dA ? mask(rA) : 0ull) | (dB ? mask(rB) : 0ull);
+                    const unsigned long long freeBits = ~used & ((1ull << kSerialColour) - 1ull);
+                    const int col = freeBits ? __ffsll((long long)freeBits) - 1 : kSerialColour;
+                    if (col != kSerialColour) {
+                        if (dA) mask(rA) |= 1ull << col;
+                        if (dB) mask(rB) |= 1ull << col;
+                    }
+                    cColour[i] = col;
+                    ++sColourStart[col + 1];
+                }
             }
             for (int i = jStart; i < jCur; ++i) {
                 Joint& J = jt[sJoint[i]];
@@ -628,9 +658,34 @@ __device__ void Wd::solve(const StepParams& P, float4* smem, int smemRows, int s
         st->solvedContacts = cCur;
     }
     __syncthreads();
+    if (coloured) {
+        // island contacts grouped by colour; the order inside a colour does not matter (its
+        // constraints are independent) except in the serial bucket, which is kept in island order
+        if (tid() == 0) {
+            for (int k = 0; k < kColours; ++k) sColourStart[k + 1] += sColourStart[k];
+            int used = 0;
+            for (int k = 0; k < kSerialColour; ++k)
+                if (sColourStart[k + 1] > sColourStart[k]) used = k + 1;
+            st->colours = used + (sColourStart[kColours] > sColourStart[kSerialColour] ? 1 : 0);
+        }
+        for (int k = tid(); k < kColours; k += nthreads()) sColourCursor[k] = 0;
+        __syncthreads();
+        const int n = sCons;
+        for (int i = tid(); i < n; i += nthreads()) {
+            const int col = cColour[i];
+            if (col == kSerialColour) continue;
+            colourList[sColourStart[col] + atomicAdd(&sColourCursor[col], 1)] = i;
+        }
+        if (tid() == 0 && sColourStart[kColours] > sColourStart[kSerialColour]) {
+            int w = sColourStart[kSerialColour];
+            for (int i = 0; i < n; ++i)
+                if (cColour[i] == kSerialColour) colourList[w++] = i;
+        }
+        __syncthreads();
+    }
     unsigned long long t1 = clock64();
     const int nIsl = sIslands;
-    solveIslands(P, nIsl, sRows, sCons, smem, smemRows, smemContacts);
+    solveIslands(P, nIsl, sRows, sCons, smem, smemRows, smemContacts, coloured ? sColourStart : nullptr);
     unsigned long long t2 = clock64();
     // A static body may sit in several islands; its awake flag ends as the last such island left it.
     if (tid() == 0) {
@@ -955,6 +1010,9 @@ __global__ void __launch_bounds__(128) StepKernel(Batch B, StepParams P, const i
         W.st->solvedBodies = 0;
         W.st->solvedContacts = 0;
         W.st->pairsFound = 0;
+        W.st->colours = 0;
+        W.st->velIters = 0;
+        W.st->residual = 0.0f;
         W.st->newFixture = 0;
         for (int i = 0; i < 16; ++i) W.st->cyc[i] = 0;
     }

@@ -53,6 +53,9 @@ struct WorldState {
     int solvedBodies;   // non-static island rows solved in the last step
     int solvedContacts; // island contacts solved in the last step
     int pairsFound;     // broadphase pairs produced in the last step (all UpdatePairs calls)
+    int colours;        // constraint colours used by the coloured solver in the last step
+    int velIters;       // velocity iterations run in the last step (fewer than asked when a tolerance is met)
+    float residual;     // velocity residual (m/s) after the last step's velocity iterations, when measured
     int pad;
     // SM clock cycles of the last step per phase: 0 new-fixture pairs, 1 collide, 2 island DFS,
     // 3 island solve, 4 fixture sync, 5 pairs after solve, 6 TOI, 7 whole step; then the island solve
@@ -158,15 +161,31 @@ struct Batch {
     int2* islandJ;   // {jointStart, jointCount}
     int* sJoint;     // joint-sized
     int* sleepOut;   // per island: 1 when the island fell asleep
+    int* cColour;    // contact-sized: colour of each island contact (coloured solver)
+    int* colourList; // contact-sized: island contacts grouped by colour
+    unsigned long long* rowMask; // row-sized: colours used at each island body row
     unsigned long long* pairs; // pair-sized sort keys (proxyA << 32 | proxyB)
     int* pairKeep;
     int* movedList;  // proxy-sized
 };
 
+// Island solver variants. kSolverPlain is the reference's per-island sequential Gauss-Seidel order
+// (bit-exact with the reference). kSolverColoured solves the same constraints colour by colour: the
+// constraints of one colour share no dynamic body and are solved in parallel across the CTA.
+enum : int { kSolverPlain = 0, kSolverColoured = 1 };
+// Colours 0..62 are solved in parallel; colour 63 collects the constraints for which no colour was
+// free and is solved by one thread in island order.
+constexpr int kColours = 64;
+constexpr int kSerialColour = kColours - 1;
+
 struct StepParams {
     float dt;
     int velocityIterations, positionIterations;
     int maxToiEvents;   // bound on TOI sub-steps per world per step (error bit on overflow)
+    int solver;         // kSolverPlain or kSolverColoured
+    float tolerance;    // > 0: stop the velocity iterations once the velocity residual is <= tolerance
+    int measureResidual;// 1: record the velocity residual after the velocity iterations
+    int pad;
 };
 
 } // namespace b2g

@@ -63,6 +63,21 @@ class World:
     def sync(self) -> None:
         _lib.check(self.lib.gb_world_sync(self.h), "gb_world_sync")
 
+    def set_solver(self, solver: str = "plain", tolerance: float = 0.0, measure_residual: bool = False) -> None:
+        """Island solver of the following steps: "plain" (the reference's sequential order, bit-exact)
+        or "coloured" (parallel per constraint colour); see gb_world_set_solver."""
+        code = {"plain": _lib.SOLVER_PLAIN, "coloured": _lib.SOLVER_COLOURED}[solver]
+        _lib.check(self.lib.gb_world_set_solver(self.h, code, float(tolerance), int(measure_residual)),
+                   "gb_world_set_solver")
+
+    def solver_stats(self):
+        """(colours, velocity iterations, velocity residual) per world of the last step."""
+        col = np.zeros(self.n_worlds, dtype=np.int32)
+        its = np.zeros(self.n_worlds, dtype=np.int32)
+        res = np.zeros(self.n_worlds, dtype=np.float32)
+        _lib.check(self.lib.gb_world_solver_stats(self.h, col, its, res), "gb_world_solver_stats")
+        return col, its, res
+
     def set_stream(self, stream_handle: int) -> None:
         _lib.check(self.lib.gb_world_set_stream(self.h, C.c_void_p(stream_handle)), "gb_world_set_stream")
 

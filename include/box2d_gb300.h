@@ -88,6 +88,23 @@ gb_status gb_world_step(gb_world* world, float dt, int velocity_iterations, int 
 /* Waits for queued steps and returns the first error any world raised since the last sync. */
 gb_status gb_world_sync(gb_world* world);
 
+/* Island solver of the following steps. GB_SOLVER_PLAIN (default) is b2Island::Solve's sequential
+ * per-island Gauss-Seidel order (Box2D/Dynamics/b2Island.cpp:185-384), bit-exact with the reference.
+ * GB_SOLVER_COLOURED solves the same contact constraints colour by colour (constraints of one colour
+ * share no dynamic body and are solved in parallel); it converges like Gauss-Seidel but its results
+ * are not the reference's bits. tolerance > 0 ends the velocity iterations of a world (plain: of an
+ * island) once its velocity residual is at most tolerance (m/s); velocity_iterations stays the
+ * maximum. measure_residual != 0 records each world's velocity residual after the velocity
+ * iterations (gb_world_solver_stats). The velocity residual is the largest of |vn - bias| over
+ * active normal points, max(0, bias - vn) over inactive ones and |vt| over unsaturated friction. */
+#define GB_SOLVER_PLAIN 0
+#define GB_SOLVER_COLOURED 1
+gb_status gb_world_set_solver(gb_world* world, int solver, float tolerance, int measure_residual);
+
+/* Per world of the last step (arrays of n_worlds, each may be NULL): colours used by the coloured
+ * solver, velocity iterations run, velocity residual (when measured). */
+gb_status gb_world_solver_stats(gb_world* world, int* colours, int* vel_iters, float* residual);
+
 /* Binds the handle to a caller-owned cudaStream_t (NULL = the handle's own stream). */
 gb_status gb_world_set_stream(gb_world* world, void* cuda_stream);
 
