@@ -23,7 +23,8 @@ EXPORTS = [
     "gb_build_world", "gb_world_upload", "gb_world_step", "gb_world_sync", "gb_world_set_stream",
     "gb_world_counts", "gb_get_bodies", "gb_get_contacts", "gb_get_proxies", "gb_world_stats", "gb_sincos",
     "gb_collide", "gb_version", "gb_world_totals", "gb_set_forces", "gb_get_transforms", "gb_world_profile",
-    "gb_collide_noalloc", "gb_world_set_solver", "gb_world_solver_stats",
+    "gb_collide_noalloc", "gb_world_set_solver", "gb_world_solver_stats", "gb_world_autotune",
+    "gb_world_launch_plan", "gb_world_set_launch_plan", "gb_world_graph_step",
 ]
 
 
@@ -80,6 +81,10 @@ def load(build_if_missing: bool = True):
         "gb_collide_noalloc": [i, _i32, _f32, _i32, _f32, _i32, _f32, _i32, _f32, _i32, _f32],
         "gb_world_set_solver": [vp, i, f, i],
         "gb_world_solver_stats": [vp, _i32, _i32, _f32],
+        "gb_world_autotune": [vp, i],
+        "gb_world_graph_step": [vp, f, i, i],
+        "gb_world_launch_plan": [vp, _i32, i, C.POINTER(i), _f32, i, C.POINTER(i)],
+        "gb_world_set_launch_plan": [vp, _i32, i],
         "gb_world_totals": [vp, C.POINTER(C.c_longlong)],
         "gb_set_forces": [vp, vp],
         "gb_get_transforms": [vp, vp],

@@ -19,8 +19,8 @@
 #include "../../include/box2d_gb300.h"
 #include "b2g_world.h"
 
-cudaError_t b2gLaunchStep(const b2g::Batch& B, const b2g::StepParams& P, const int* schedule, int threads,
-                          cudaStream_t stream);
+cudaError_t b2gLaunchStep(const b2g::Batch& B, const b2g::StepParams& P, const int* schedule, int first, int count,
+                          int threads, int smemRows, int smemContacts, cudaStream_t stream);
 cudaError_t b2gLaunchSinCos(const float* x, float* s, float* c, int n, cudaStream_t stream);
 cudaError_t b2gLaunchCollide(int n, const b2g::Shape* a, const float4* xa, const b2g::Shape* b, const float4* xb,
                              int4* oi, float4* of, cudaStream_t stream);
@@ -77,6 +77,13 @@ template <typename T> struct DevBuf {
     size_t n = 0;
 };
 
+// One launch of the step over a contiguous range of the schedule (worlds sorted largest first).
+struct LaunchClass {
+    int first, count, threads, rows, contacts;
+};
+using LaunchPlan = std::vector<LaunchClass>;
+constexpr int kMaxClasses = 4;
+
 } // namespace
 
 struct gb_world {
@@ -89,8 +96,24 @@ struct gb_world {
     bool ownStream = false;
     bool onDevice = false;   // device columns hold the current state
     bool hostDirty = true;   // host mirror has changes not yet uploaded
-    int threads = 64;
     bool locked = false;
+    // launch plan: size classes of worlds, each a launch with its own CTA size and shared memory
+    std::vector<int> schedule;      // world indices, largest first
+    std::vector<int> scheduleSize;  // body count of schedule[i]
+    LaunchPlan plan;
+    cudaStream_t side[kMaxClasses] = {};
+    cudaEvent_t fork = nullptr, join[kMaxClasses] = {};
+    // online autotuning of the plan over real steps (every plan gives identical results)
+    std::vector<LaunchPlan> candidates;
+    std::vector<float> candidateMs;
+    std::vector<cudaEvent_t> tuneEvents;
+    int tuneSteps = 0, tuneIndex = -1, tuneRep = 0;
+    // one captured step (every launch of the plan) replayed by gb_world_graph_step
+    cudaGraphExec_t graph = nullptr;
+    float graphDt = 0.0f;
+    int graphVi = -1, graphPi = -1, graphSolver = -1, graphMeasure = -1;
+    float graphTol = -1.0f;
+    LaunchPlan graphPlan;
     int solver = kSolverPlain;
     float tolerance = 0.0f;
     int measureResidual = 0;
@@ -215,6 +238,9 @@ template <typename T> gb_status DevAlloc(gb_world* g, T** p, size_t n)
 
 void FreeDevice(gb_world* g)
 {
+    // a captured step holds the device addresses being freed
+    if (g->graph) cudaGraphExecDestroy(g->graph);
+    g->graph = nullptr;
     for (void* p : g->allocations) cudaFree(p);
     g->allocations.clear();
     std::memset(&g->batch, 0, sizeof(g->batch));
@@ -291,6 +317,169 @@ template <typename T> gb_status Put(T* dst, const std::vector<T>& src, size_t n)
     return GB_OK;
 }
 
+// ------------------------------------------------------------------ launch plans
+int RoundUp(int x, int m) { return (x + m - 1) / m * m; }
+
+// A class over schedule[first, first + count): shared memory sized for its largest world (island rows
+// ~ bodies plus the static bodies repeated per island, contacts ~ 2.5 per body), within 36 KB.
+LaunchClass MakeClass(const gb_world* g, int first, int count, int threads)
+{
+    int maxBodies = 0;
+    for (int i = first; i < first + count; ++i) maxBodies = std::max(maxBodies, g->scheduleSize[i]);
+    LaunchClass c;
+    c.first = first;
+    c.count = count;
+    c.threads = threads;
+    c.rows = std::min(640, std::max(64, RoundUp(maxBodies + maxBodies / 4 + 16, 32)));
+    c.contacts = std::min(1024, std::max(128, RoundUp(maxBodies * 5 / 2 + 32, 32)));
+    return c;
+}
+
+// Split the schedule (largest first) at body-count thresholds (descending); one CTA size per class.
+LaunchPlan SplitPlan(const gb_world* g, const std::vector<int>& thresholds, const std::vector<int>& threads)
+{
+    LaunchPlan plan;
+    const int nw = (int)g->schedule.size();
+    int first = 0;
+    for (size_t k = 0; k <= thresholds.size() && first < nw; ++k) {
+        int end = nw;
+        if (k < thresholds.size()) {
+            end = first;
+            while (end < nw && g->scheduleSize[end] > thresholds[k]) ++end;
+        }
+        if (end > first) plan.push_back(MakeClass(g, first, end - first, threads[k]));
+        first = end;
+    }
+    return plan;
+}
+
+LaunchPlan DefaultPlan(const gb_world* g)
+{
+    const int nw = (int)g->schedule.size();
+    LaunchClass c{0, nw, nw == 1 ? 128 : 64, 640, 1024};
+    return LaunchPlan{c};
+}
+
+std::vector<LaunchPlan> CandidatePlans(const gb_world* g)
+{
+    std::vector<LaunchPlan> c;
+    c.push_back(DefaultPlan(g));
+    if (g->schedule.size() < 2) return c;
+    c.push_back(LaunchPlan{MakeClass(g, 0, (int)g->schedule.size(), 64)});
+    c.push_back(LaunchPlan{MakeClass(g, 0, (int)g->schedule.size(), 32)});
+    c.push_back(SplitPlan(g, {160}, {64, 32}));
+    c.push_back(SplitPlan(g, {160}, {64, 64}));
+    c.push_back(SplitPlan(g, {256, 64}, {64, 64, 32}));
+    c.push_back(SplitPlan(g, {256, 64}, {64, 32, 32}));
+    c.push_back(SplitPlan(g, {96}, {64, 32}));
+    c.push_back(SplitPlan(g, {320, 160, 64}, {128, 64, 32, 32}));
+    return c;
+}
+
+gb_status EnsureSideStreams(gb_world* g, int n)
+{
+    if (!g->fork) GB_CUDA(cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming));
+    for (int i = 1; i < n && i < kMaxClasses; ++i) {
+        if (!g->side[i]) GB_CUDA(cudaStreamCreateWithFlags(&g->side[i], cudaStreamNonBlocking));
+        if (!g->join[i]) GB_CUDA(cudaEventCreateWithFlags(&g->join[i], cudaEventDisableTiming));
+    }
+    return GB_OK;
+}
+
+// One step of every world with the given plan: class 0 (the largest worlds) on the handle's stream,
+// submitted first so its CTAs are dispatched first, the others on side streams forked from the same
+// point and joined back (a pattern stream capture records as one graph).
+gb_status LaunchPlanStep(gb_world* g, const StepParams& P, const LaunchPlan& plan)
+{
+    const int n = std::min((int)plan.size(), kMaxClasses);
+    if (n > 1) {
+        gb_status s = EnsureSideStreams(g, n);
+        if (s != GB_OK) return s;
+        GB_CUDA(cudaEventRecord(g->fork, g->stream));
+    }
+    if (n > 0) {
+        const LaunchClass& c = plan[0];
+        GB_CUDA(b2gLaunchStep(g->batch, P, g->dSchedule, c.first, c.count, c.threads, c.rows, c.contacts,
+                              g->stream));
+    }
+    for (int i = 1; i < n; ++i) {
+        const LaunchClass& c = plan[i];
+        GB_CUDA(cudaStreamWaitEvent(g->side[i], g->fork, 0));
+        GB_CUDA(b2gLaunchStep(g->batch, P, g->dSchedule, c.first, c.count, c.threads, c.rows, c.contacts,
+                              g->side[i]));
+        GB_CUDA(cudaEventRecord(g->join[i], g->side[i]));
+    }
+    for (int i = 1; i < n; ++i) GB_CUDA(cudaStreamWaitEvent(g->stream, g->join[i], 0));
+    return GB_OK;
+}
+
+// A step of the online autotuner: the candidate under trial, timed with events on the handle's
+// stream. Candidates take turns (rounds of one step each) so that the workload's drift over the
+// tuning steps reaches all of them alike; after the last round the candidate with the smallest
+// median time becomes the plan. tuneIndex is the candidate, tuneRep the round.
+gb_status TunedStep(gb_world* g, const StepParams& P)
+{
+    const int nc = (int)g->candidates.size();
+    const int trial = g->tuneIndex * g->tuneSteps + g->tuneRep;
+    cudaEvent_t e0 = g->tuneEvents[2 * trial], e1 = g->tuneEvents[2 * trial + 1];
+    GB_CUDA(cudaEventRecord(e0, g->stream));
+    gb_status s = LaunchPlanStep(g, P, g->candidates[g->tuneIndex]);
+    if (s != GB_OK) return s;
+    GB_CUDA(cudaEventRecord(e1, g->stream));
+    if (++g->tuneIndex == nc) { g->tuneIndex = 0; ++g->tuneRep; }
+    if (g->tuneRep < g->tuneSteps) return GB_OK;
+    g->tuneIndex = nc;
+    GB_CUDA(cudaEventSynchronize(e1));
+    int best = 0;
+    for (int c = 0; c < nc; ++c) {
+        std::vector<float> t(g->tuneSteps);
+        for (int r = 0; r < g->tuneSteps; ++r) {
+            const int k = c * g->tuneSteps + r;
+            GB_CUDA(cudaEventElapsedTime(&t[r], g->tuneEvents[2 * k], g->tuneEvents[2 * k + 1]));
+        }
+        std::sort(t.begin(), t.end());
+        g->candidateMs[c] = t[g->tuneSteps / 2];
+        if (g->candidateMs[c] < g->candidateMs[best]) best = c;
+    }
+    g->plan = g->candidates[best];
+    for (cudaEvent_t e : g->tuneEvents) cudaEventDestroy(e);
+    g->tuneEvents.clear();
+    g->tuneIndex = -1;
+    return GB_OK;
+}
+
+void ReleaseGraph(gb_world* g)
+{
+    if (g->graph) cudaGraphExecDestroy(g->graph);
+    g->graph = nullptr;
+}
+
+bool SamePlan(const LaunchPlan& a, const LaunchPlan& b)
+{
+    if (a.size() != b.size()) return false;
+    for (size_t i = 0; i < a.size(); ++i)
+        if (a[i].first != b[i].first || a[i].count != b[i].count || a[i].threads != b[i].threads ||
+            a[i].rows != b[i].rows || a[i].contacts != b[i].contacts)
+            return false;
+    return true;
+}
+
+void ReleaseLaunchResources(gb_world* g)
+{
+    ReleaseGraph(g);
+    for (int i = 0; i < kMaxClasses; ++i) {
+        if (g->side[i]) cudaStreamDestroy(g->side[i]);
+        if (g->join[i]) cudaEventDestroy(g->join[i]);
+        g->side[i] = nullptr;
+        g->join[i] = nullptr;
+    }
+    if (g->fork) cudaEventDestroy(g->fork);
+    g->fork = nullptr;
+    for (cudaEvent_t e : g->tuneEvents) cudaEventDestroy(e);
+    g->tuneEvents.clear();
+    g->tuneIndex = -1;
+}
+
 // (Re)allocate device columns for the current world sizes and copy the host mirror over.
 gb_status Upload(gb_world* g)
 {
@@ -337,7 +526,7 @@ gb_status Upload(gb_world* g)
     ALLOC(sBody, tr); ALLOC(sStack, tb); ALLOC(sWake, tb); ALLOC(sPos, tr); ALLOC(sVel, tr); ALLOC(islands, tb);
     ALLOC(islandJ, tb); ALLOC(sleepOut, tb); ALLOC(rowMask, tr);
     ALLOC(sContact, tc); ALLOC(sStatus, tc); ALLOC(vc, tc); ALLOC(pc, tc); ALLOC(vimp, tc); ALLOC(toi, tc); ALLOC(cColour, tc); ALLOC(colourList, tc);
-    ALLOC(pairs, tq); ALLOC(pairKeep, tq);
+    ALLOC(pairs, tq); ALLOC(pairKeep, tq); ALLOC(pairInfo, tq);
 #undef ALLOC
     GB_CUDA(cudaMemcpy(B.desc, g->desc.data(), nw * sizeof(WorldDesc), cudaMemcpyHostToDevice));
     std::vector<WorldState> states(nw);
@@ -431,7 +620,10 @@ gb_status Upload(gb_world* g)
     });
     if ((s = DevAlloc(g, &g->dSchedule, nw)) != GB_OK) return s;
     GB_CUDA(cudaMemcpy(g->dSchedule, schedule.data(), nw * sizeof(int), cudaMemcpyHostToDevice));
-    g->threads = nw == 1 ? 128 : 64; // StepKernel is compiled for at most 128 threads per CTA
+    g->schedule = schedule;
+    g->scheduleSize.resize(nw);
+    for (int i = 0; i < nw; ++i) g->scheduleSize[i] = g->desc[schedule[i]].bodyCount;
+    g->plan = DefaultPlan(g);
     g->onDevice = true;
     g->hostDirty = false;
     return GB_OK;
@@ -565,7 +757,10 @@ gb_status gb_world_destroy(gb_world* g)
 {
     if (!g) return GB_ERR_INVALID;
     if (g->stream) cudaStreamSynchronize(g->stream);
+    for (int i = 0; i < kMaxClasses; ++i)
+        if (g->side[i]) cudaStreamSynchronize(g->side[i]);
     FreeDevice(g);
+    ReleaseLaunchResources(g);
     if (g->ownStream && g->stream) cudaStreamDestroy(g->stream);
     delete g;
     return GB_OK;
@@ -649,7 +844,113 @@ gb_status gb_world_step(gb_world* g, float dt, int vi, int pi)
     P.tolerance = g->tolerance;
     P.measureResidual = g->measureResidual;
     P.pad = 0;
-    return cudaErr(b2gLaunchStep(g->batch, P, g->dSchedule, g->threads, g->stream));
+    if (g->tuneIndex >= 0) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        GB_CUDA(cudaStreamIsCapturing(g->stream, &cs));
+        if (cs == cudaStreamCaptureStatusNone) return TunedStep(g, P);
+    }
+    return LaunchPlanStep(g, P, g->plan);
+}
+
+gb_status gb_world_graph_step(gb_world* g, float dt, int vi, int pi)
+{
+    if (!g || vi < 0 || pi < 0) return GB_ERR_INVALID;
+    if (g->tuneIndex >= 0) return gb_world_step(g, dt, vi, pi);  // tuning steps are timed one by one
+    gb_status s = Upload(g);
+    if (s != GB_OK) return s;
+    const bool reuse = g->graph && g->graphDt == dt && g->graphVi == vi && g->graphPi == pi &&
+                       g->graphSolver == g->solver && g->graphTol == g->tolerance &&
+                       g->graphMeasure == g->measureResidual && SamePlan(g->graphPlan, g->plan);
+    if (!reuse) {
+        ReleaseGraph(g);
+        if (g->plan.size() > 1) {
+            s = EnsureSideStreams(g, (int)g->plan.size());
+            if (s != GB_OK) return s;
+        }
+        StepParams P;
+        P.dt = dt;
+        P.velocityIterations = vi;
+        P.positionIterations = pi;
+        P.maxToiEvents = 4096;
+        P.solver = g->solver;
+        P.tolerance = g->tolerance;
+        P.measureResidual = g->measureResidual;
+        P.pad = 0;
+        GB_CUDA(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
+        s = LaunchPlanStep(g, P, g->plan);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(g->stream, &graph);
+        if (s != GB_OK) { if (graph) cudaGraphDestroy(graph); return s; }
+        GB_CUDA(ec);
+        const cudaError_t ei = cudaGraphInstantiate(&g->graph, graph, 0);
+        cudaGraphDestroy(graph);
+        GB_CUDA(ei);
+        g->graphDt = dt; g->graphVi = vi; g->graphPi = pi; g->graphSolver = g->solver;
+        g->graphTol = g->tolerance; g->graphMeasure = g->measureResidual; g->graphPlan = g->plan;
+    }
+    GB_CUDA(cudaGraphLaunch(g->graph, g->stream));
+    return GB_OK;
+}
+
+gb_status gb_world_autotune(gb_world* g, int steps_per_candidate)
+{
+    if (!g || steps_per_candidate < 1 || steps_per_candidate > 64) return GB_ERR_INVALID;
+    gb_status s = Upload(g);
+    if (s != GB_OK) return s;
+    for (cudaEvent_t e : g->tuneEvents) cudaEventDestroy(e);
+    g->tuneEvents.clear();
+    g->candidates = CandidatePlans(g);
+    g->candidateMs.assign(g->candidates.size(), 0.0f);
+    const size_t n = 2 * g->candidates.size() * (size_t)steps_per_candidate;
+    for (size_t i = 0; i < n; ++i) {
+        cudaEvent_t e = nullptr;
+        GB_CUDA(cudaEventCreate(&e));
+        g->tuneEvents.push_back(e);
+    }
+    g->tuneSteps = steps_per_candidate;
+    g->tuneIndex = 0;
+    g->tuneRep = 0;
+    return GB_OK;
+}
+
+gb_status gb_world_launch_plan(gb_world* g, int* classes, int cap, int* n_classes, float* candidate_ms, int ms_cap,
+                               int* n_candidates)
+{
+    if (!g) return GB_ERR_INVALID;
+    if (n_classes) *n_classes = (int)g->plan.size();
+    if (classes)
+        for (int i = 0; i < (int)g->plan.size() && i < cap; ++i) {
+            const LaunchClass& c = g->plan[i];
+            classes[5 * i] = c.first; classes[5 * i + 1] = c.count; classes[5 * i + 2] = c.threads;
+            classes[5 * i + 3] = c.rows; classes[5 * i + 4] = c.contacts;
+        }
+    const int nc = g->tuneIndex < 0 ? (int)g->candidateMs.size() : 0;
+    if (n_candidates) *n_candidates = nc;
+    if (candidate_ms)
+        for (int i = 0; i < nc && i < ms_cap; ++i) candidate_ms[i] = g->candidateMs[i];
+    return GB_OK;
+}
+
+gb_status gb_world_set_launch_plan(gb_world* g, const int* classes, int n)
+{
+    if (!g || !classes || n < 1 || n > kMaxClasses) return GB_ERR_INVALID;
+    gb_status s = Upload(g);
+    if (s != GB_OK) return s;
+    LaunchPlan plan;
+    int next = 0;
+    for (int i = 0; i < n; ++i) {
+        LaunchClass c{classes[5 * i], classes[5 * i + 1], classes[5 * i + 2], classes[5 * i + 3], classes[5 * i + 4]};
+        const size_t smem = (2 * (size_t)std::max(c.rows, 0) + std::max(c.contacts, 0)) * sizeof(float4);
+        if (c.first != next || c.count < 1 || c.threads < 32 || c.threads > 128 || c.threads % 32 != 0 ||
+            c.rows < 0 || c.contacts < 0 || smem > 48 * 1024)
+            return GB_ERR_INVALID;
+        next += c.count;
+        plan.push_back(c);
+    }
+    if (next != (int)g->schedule.size()) return GB_ERR_INVALID;
+    g->plan = plan;
+    g->tuneIndex = -1;
+    return GB_OK;
 }
 
 gb_status gb_world_sync(gb_world* g)

@@ -59,6 +59,9 @@ struct Wd {
     unsigned long long* pairs;
     int* pairKeep;
     int* movedList;
+    int4* pairInfo;
+    float4* smemBase;   // the CTA's dynamic shared memory, free outside the island solve
+    int smemBytes;
 
     __device__ void init(const Batch& B, int w)
     {
@@ -78,7 +81,9 @@ struct Wd {
         islands = B.islands + b; islandJ = B.islandJ + b; sleepOut = B.sleepOut + b;
         sContact = B.sContact + c; sStatus = B.sStatus + c; vc = B.vc + c; pc = B.pc + c; vimp = B.vimp + c; toi = B.toi + c;
         cColour = B.cColour + c; colourList = B.colourList + c;
-        pairs = B.pairs + q; pairKeep = B.pairKeep + q;
+        pairs = B.pairs + q; pairKeep = B.pairKeep + q; pairInfo = B.pairInfo + q;
+        smemBase = nullptr;
+        smemBytes = 0;
     }
 
     // ---------------------------------------------------------------- body helpers
@@ -288,6 +293,7 @@ struct Wd {
     __device__ void findNewContacts();
     __device__ void collide();
     __device__ void solve(const StepParams& P, float4* smem, int smemRows, int smemContacts);
+    __device__ bool buildIslandsShared(bool coloured, int* colourCount, int& nIsl, int& nRows, int& nCons, int& movers);
     __device__ void solveIslands(const StepParams& P, int nIsl, int nRows, int nContacts, float4* smem, int smemRows,
                                  int smemContacts, const int* colourStart);
     __device__ void solveTOI(const StepParams& P);
@@ -352,23 +358,43 @@ __device__ void ctaSortKeys(unsigned long long* keys, int n, int capacity)
 // ------------------------------------------------------------------ FindNewContacts
 __device__ void Wd::findNewContacts()
 {
-    __shared__ int sMoved, sPairs, sNew;
+    __shared__ int sMoved, sPairs, sNew, sKept;
     if (tid() == 0) { sMoved = 0; sPairs = 0; sNew = 0; }
     __syncthreads();
+    const unsigned long long tPairs0 = clock64();
     const int np = d.proxyCap;
     for (int p = tid(); p < np; p += nthreads())
         if (moved[p]) movedList[atomicAdd(&sMoved, 1)] = p;
     __syncthreads();
     const int m = sMoved;
     // Query every moved proxy's fat AABB against all proxies (b2BroadPhase.h:188-217); a pair whose
-    // both proxies moved is emitted once, from the lower proxy id.
+    // both proxies moved is emitted once, from the lower proxy id. The proxies are staged in shared
+    // memory when they fit (each is read once per moved proxy): a free proxy gets an empty box that
+    // overlaps nothing, and a byte per proxy holds its moved flag.
+    const bool staged = np * (int)(sizeof(float4) + 1) <= smemBytes;
+    float4* sFat = smemBase;
+    unsigned char* sMovedFlag = reinterpret_cast<unsigned char*>(smemBase + np);
+    if (staged && m > 0) {
+        const float inf = __int_as_float(0x7f800000);
+        for (int p = tid(); p < np; p += nthreads()) {
+            sFat[p] = pfix[p] >= 0 ? fat[p] : make_float4(inf, inf, -inf, -inf);
+            sMovedFlag[p] = (unsigned char)(moved[p] != 0);
+        }
+        __syncthreads();
+    }
     const long long total = (long long)m * np;
     for (long long idx = tid(); idx < total; idx += nthreads()) {
-        int q = movedList[idx / np];
-        int p = (int)(idx % np);
-        if (p == q || pfix[p] < 0) continue;
-        if (moved[p] && p < q) continue;
-        if (!Overlap(fat[p], fat[q])) continue;
+        const int q = movedList[idx / np];
+        const int p = (int)(idx % np);
+        if (p == q) continue;
+        if (staged) {
+            if (sMovedFlag[p] && p < q) continue;
+            if (!Overlap(sFat[p], sFat[q])) continue;
+        } else {
+            if (pfix[p] < 0) continue;
+            if (moved[p] && p < q) continue;
+            if (!Overlap(fat[p], fat[q])) continue;
+        }
         int k = atomicAdd(&sPairs, 1);
         unsigned long long lo = (unsigned long long)(p < q ? p : q), hi = (unsigned long long)(p < q ? q : p);
         if (k < d.pairCap) pairs[k] = (lo << 32) | hi;
@@ -380,7 +406,21 @@ __device__ void Wd::findNewContacts()
         if (tid() == 0) atomicOr(&st->error, kErrCapacity);
         n = d.pairCap;
     }
-    ctaSortKeys(pairs, n, d.pairCap);
+    // sort (b2BroadPhase.h:220: std::sort by (proxyIdA, proxyIdB)); in shared memory when it fits
+    {
+        int P2 = 1;
+        while (P2 < n) P2 <<= 1;
+        if (n > 1 && P2 * (int)sizeof(unsigned long long) <= smemBytes) {
+            unsigned long long* sKeys = reinterpret_cast<unsigned long long*>(smemBase);
+            for (int i = tid(); i < n; i += nthreads()) sKeys[i] = pairs[i];
+            __syncthreads();
+            ctaSortKeys(sKeys, n, P2);
+            for (int i = tid(); i < n; i += nthreads()) pairs[i] = sKeys[i];
+            __syncthreads();
+        } else if (n > 1) {
+            ctaSortKeys(pairs, n, d.pairCap);
+        }
+    }
     // b2ContactManager::AddPair checks (Dynamics/b2ContactManager.cpp:179-227), independent per pair.
     for (int k = tid(); k < n; k += nthreads()) {
         int pA = (int)(pairs[k] >> 32), pB = (int)(pairs[k] & 0xffffffffu);
@@ -402,46 +442,98 @@ __device__ void Wd::findNewContacts()
         pairKeep[k] = keep;
     }
     __syncthreads();
-    // Create in sorted pair order; each new contact goes to the front of every list
-    // (b2ContactManager.cpp:229-293).
+    // kept pairs in sorted order, with everything a new contact needs that does not depend on the
+    // creation order worked out in parallel: fixtures in factory order, bodies, mixed friction and
+    // restitution, and whether the pair wakes its bodies
+    int* keptIdx = sContact;
+    {
+        // indices of the kept pairs, in sorted order (order-preserving compaction over the CTA)
+        const int T = nthreads(), t = tid();
+        const int chunk = (n + T - 1) / T;
+        const int lo = min(n, t * chunk), hi = min(n, lo + chunk);
+        __shared__ int sOff2[kMaxCta + 1];
+        int cnt = 0;
+        for (int k = lo; k < hi; ++k) cnt += pairKeep[k] != 0;
+        sOff2[t + 1] = cnt;
+        __syncthreads();
+        if (t == 0) {
+            sOff2[0] = 0;
+            for (int i = 1; i <= T; ++i) sOff2[i] += sOff2[i - 1];
+            sKept = sOff2[T];
+        }
+        __syncthreads();
+        int o = sOff2[t];
+        for (int k = lo; k < hi; ++k)
+            if (pairKeep[k] && o < d.contactCap) keptIdx[o++] = k;
+        __syncthreads();
+    }
+    // more new contacts than contact slots cannot be created: the free list runs dry below
+    const int nKept = min(sKept, d.contactCap);
+    int4* info = pairInfo;
+    for (int r = tid(); r < nKept; r += nthreads()) {
+        const int k = keptIdx[r];
+        const int pA = (int)(pairs[k] >> 32), pB = (int)(pairs[k] & 0xffffffffu);
+        int fa = pfix[pA], fb = pfix[pB];
+        if (!primaryOrder(shape[fa].type, shape[fb].type)) { int t = fa; fa = fb; fb = t; }
+        const int wake = (fi[fa].w == 0 && fi[fb].w == 0) ? 1 : 0;
+        info[r] = make_int4(fa | (wake << 30), fb, fixBody(fa), fixBody(fb));
+    }
+    __syncthreads();
+    const unsigned long long tCreate0 = clock64();
+    // Create in sorted pair order; each new contact goes to the front of both bodies' lists
+    // (b2ContactManager.cpp:229-293). The list heads of the bodies live in shared memory for the
+    // loop when they fit, so only the free-list pop reads global memory on the order-defining path.
+    const int nb = d.bodyCount;
+    const bool headsStaged = nKept > 0 && nb * (int)sizeof(int) <= smemBytes;
+    int* sHead = reinterpret_cast<int*>(smemBase);
+    if (headsStaged) {
+        for (int b = tid(); b < nb; b += nthreads()) sHead[b] = bi[b].w;
+        __syncthreads();
+    }
     if (tid() == 0) {
         int created = 0;
-        for (int k = 0; k < n; ++k) {
-            if (!pairKeep[k]) continue;
-            int pA = (int)(pairs[k] >> 32), pB = (int)(pairs[k] & 0xffffffffu);
-            int fa = pfix[pA], fb = pfix[pB];
-            if (!primaryOrder(shape[fa].type, shape[fb].type)) { int t = fa; fa = fb; fb = t; }
-            int c = st->freeContact;
+        int freeHead = st->freeContact;
+        for (int r = 0; r < nKept; ++r) {
+            const int4 I = info[r];
+            const int fa = I.x & 0x3fffffff, fb = I.y, bA = I.z, bB = I.w;
+            const int c = freeHead;
             if (c == kNullIdx) { atomicOr(&st->error, kErrCapacity); break; }
-            st->freeContact = cnext[c];
-            float4 ma = fm[fa], mb = fm[fb];
+            freeHead = cnext[c];
+            const float4 ma = fm[fa], mb = fm[fb];
             ci[c] = make_int4(kCEnabled, fa, fb, 0);
             cp[c] = make_float4(sqrtf(ma.x * mb.x), ma.y > mb.y ? ma.y : mb.y, 0.0f, 1.0f);
             mh[c] = make_int4(0, 0, 0, 0);
             mv[c] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             mp0[c] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             mp1[c] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            int bA = fixBody(fa), bB = fixBody(fb);
-            int eA = 2 * c, eB = 2 * c + 1;
-            int hA = bi[bA].w;
-            ce[c] = make_int4(kNullIdx, hA, kNullIdx, kNullIdx);
+            const int eA = 2 * c, eB = 2 * c + 1;
+            const int hA = headsStaged ? sHead[bA] : bi[bA].w;
             if (hA != kNullIdx) *ePrevP(hA) = eA;
-            bi[bA].w = eA;
-            int hB = bi[bB].w;
-            ce[c].w = hB;
+            if (headsStaged) sHead[bA] = eA; else bi[bA].w = eA;
+            const int hB = headsStaged ? sHead[bB] : bi[bB].w;
+            ce[c] = make_int4(kNullIdx, hA, kNullIdx, hB);
             if (hB != kNullIdx) *ePrevP(hB) = eB;
-            bi[bB].w = eB;
-            if (fi[fa].w == 0 && fi[fb].w == 0) {
-                setAwake(bA, true);
-                setAwake(bB, true);
-            }
+            if (headsStaged) sHead[bB] = eB; else bi[bB].w = eB;
             sContact[created++] = c;
         }
+        st->freeContact = freeHead;
         sNew = created;
     }
     __syncthreads();
-    // order = reverse(new) ++ order (the pair-keep flags are dead now: reuse them as the copy buffer)
     const int created = sNew;
+    if (headsStaged) {
+        for (int b = tid(); b < nb; b += nthreads()) bi[b].w = sHead[b];
+    }
+    // b2Body::SetAwake(true) of both bodies of every non-sensor pair: idempotent, so in parallel
+    for (int r = tid(); r < created; r += nthreads()) {
+        const int4 I = info[r];
+        if ((I.x >> 30) & 1) {
+            setAwake(I.z, true);
+            setAwake(I.w, true);
+        }
+    }
+    __syncthreads();
+    // order = reverse(new) ++ order (the pair-keep flags are dead now: reuse them as the copy buffer)
     if (created > 0) {
         const int live = st->contactCount;
         int* tmp = pairKeep;
@@ -454,6 +546,11 @@ __device__ void Wd::findNewContacts()
     }
     for (int i = tid(); i < m; i += nthreads()) moved[movedList[i]] = 0;
     __syncthreads();
+    if (tid() == 0) {
+        const unsigned long long now = clock64();
+        st->cyc[14] += tCreate0 - tPairs0;
+        st->cyc[15] += now - tCreate0;
+    }
 }
 
 // ------------------------------------------------------------------ destroy
@@ -555,6 +652,194 @@ __device__ void Wd::collide()
 // b2World::Solve (Dynamics/b2World.cpp:388-577). The island DFS runs on one thread (it fixes the
 // contact order inside every island); islands are then solved in parallel, one per thread, because
 // they share no dynamic body.
+// The island DFS of b2World::Solve (Dynamics/b2World.cpp:422-510) with its working set in shared
+// memory, for worlds whose set fits. A parallel pre-pass flattens the edge list of every non-static
+// body into a table of its eligible contacts (enabled, touching, no sensor) in list order, and copies
+// the body-list links and body flags; thread 0 then runs the DFS on that table. Contacts, joints and
+// bodies are visited in exactly the order of the global DFS, so islands, rows and contact order (and
+// colours) are the same; island flags, wakes and contact island flags are written back in parallel
+// afterwards (they are idempotent and nothing in the DFS reads them back from global memory).
+// Returns false (nothing written outside shared memory) when the world does not fit.
+__device__ bool Wd::buildIslandsShared(bool coloured, int* colourCount, int& nIslOut, int& nRowsOut, int& nConsOut,
+                                       int& moversOut)
+{
+    __shared__ int sE, sOk, sIsl, sRowsS, sConsS, sMovers;
+    enum : unsigned char { fIsl = 1, fStatic = 2, fAwake = 4, fActive = 8, fDynamic = 16, fJoints = 32 };
+    const int nb = d.bodyCount, C = d.contactCap;
+    if (nb >= 65536 || C >= 32768 || nb == 0) return false;
+    // layout (bytes): masks 8nb | off 4(nb+1) | next 4nb | stack 4nb | cbits 4ceil(C/32) | local 2nb |
+    // statics 2nb | bflag nb | entries 4E | island contact pairs 4E (a contact with a static body has one entry)
+    auto up4 = [](int x) { return (x + 3) & ~3; };
+    const int oMask = 0;
+    const int oOff = oMask + (coloured ? 8 * nb : 0);
+    const int oNext = oOff + 4 * (nb + 1);
+    const int oStack = oNext + 4 * nb;
+    const int oBits = oStack + 4 * nb;
+    const int oLocal = oBits + 4 * ((C + 31) / 32);
+    const int oStatics = oLocal + up4(2 * nb);
+    const int oFlag = oStatics + up4(2 * nb);
+    const int oEntries = oFlag + up4(nb);
+    if (oEntries > smemBytes) return false;
+    unsigned char* base = reinterpret_cast<unsigned char*>(smemBase);
+    unsigned long long* mask = reinterpret_cast<unsigned long long*>(base + oMask);
+    int* off = reinterpret_cast<int*>(base + oOff);
+    int* next = reinterpret_cast<int*>(base + oNext);
+    int* stack = reinterpret_cast<int*>(base + oStack);
+    unsigned* cbits = reinterpret_cast<unsigned*>(base + oBits);
+    unsigned short* local = reinterpret_cast<unsigned short*>(base + oLocal);
+    unsigned short* statics = reinterpret_cast<unsigned short*>(base + oStatics);
+    unsigned char* bflag = base + oFlag;
+    unsigned* entries = reinterpret_cast<unsigned*>(base + oEntries);
+    auto eligible = [&](int e, int& other) {
+        const int4 info = ci[e >> 1];
+        other = (e & 1) == 0 ? fixBody(info.z) : fixBody(info.y);
+        return (info.x & kCEnabled) != 0 && (info.x & kCTouching) != 0 && fi[info.y].w == 0 && fi[info.z].w == 0;
+    };
+    // pre-pass 1: flags, links, eligible-edge counts
+    for (int b = tid(); b < nb; b += nthreads()) {
+        const int4 B = bi[b];
+        unsigned char f = 0;
+        if (B.x == kStatic) f |= fStatic;
+        if (B.x == kDynamic) f |= fDynamic;
+        if (B.y & kBAwake) f |= fAwake;
+        if (B.y & kBActive) f |= fActive;
+        if (bj[b].x != kNullIdx) f |= fJoints;
+        bflag[b] = f;
+        next[b] = bj[b].y;
+        int cnt = 0;
+        if (B.x != kStatic) {
+            B2G_WALK(e, B.w, eNext(e), 2 * C + 2) {
+                int other;
+                if (eligible(e, other)) ++cnt;
+            }
+        }
+        off[b + 1] = cnt;
+    }
+    for (int k = tid(); k < (C + 31) / 32; k += nthreads()) cbits[k] = 0u;
+    __syncthreads();
+    if (tid() == 0) {
+        off[0] = 0;
+        for (int b = 0; b < nb; ++b) off[b + 1] += off[b];
+        const int E = off[nb];
+        sE = E;
+        sOk = oEntries + 8 * E + 4 <= smemBytes ? 1 : 0;  // the table, then one pair slot per possible island contact
+    }
+    __syncthreads();
+    if (!sOk) return false;
+    const int E = sE;
+    unsigned* icPairs = entries + E;
+    // pre-pass 2: the table, (contact << 17) | (side << 16) | other body, in list order
+    for (int b = tid(); b < nb; b += nthreads()) {
+        if (bflag[b] & fStatic) continue;
+        int k = off[b];
+        B2G_WALK(e, bi[b].w, eNext(e), 2 * C + 2) {
+            int other;
+            if (eligible(e, other)) entries[k++] = ((unsigned)(e >> 1) << 17) | ((unsigned)(e & 1) << 16) | (unsigned)other;
+        }
+    }
+    __syncthreads();
+    if (tid() == 0) {
+        int nIsl = 0, bCur = 0, cCur = 0, jCur = 0, movers = 0, guard = 0;
+        for (int seed = st->bodyList; seed != kNullIdx; seed = next[seed]) {
+            if (++guard > nb) { atomicOr(&st->error, kErrInvalid); break; }
+            const unsigned char fl = bflag[seed];
+            if (fl & fIsl) continue;
+            if ((fl & fAwake) == 0 || (fl & fActive) == 0) continue;
+            if (fl & fStatic) continue;
+            const int bStart = bCur, cStart = cCur, jStart = jCur;
+            int stackCount = 0, nStatics = 0;
+            stack[stackCount++] = seed;
+            bflag[seed] = fl | fIsl;
+            while (stackCount > 0) {
+                const int b = stack[--stackCount];
+                if (bCur >= d.rowCap) { atomicOr(&st->error, kErrCapacity); stackCount = 0; break; }
+                const int loc = bCur - bStart;
+                local[b] = (unsigned short)loc;
+                bj[b].z = loc;
+                if (coloured) mask[loc] = 0ull;
+                sBody[bCur++] = b;
+                const unsigned char fb = bflag[b];
+                if (fb & fStatic) { statics[nStatics++] = (unsigned short)b; continue; }
+                ++movers;
+                for (int k = off[b], ke = off[b + 1]; k < ke; ++k) {
+                    const unsigned u = entries[k];
+                    const int c = (int)(u >> 17), other = (int)(u & 0xffffu);
+                    const unsigned bit = 1u << (c & 31);
+                    if (cbits[c >> 5] & bit) continue;
+                    cbits[c >> 5] |= bit;
+                    icPairs[cCur - cStart] = (u >> 16) & 1u ? ((unsigned)other | ((unsigned)b << 16))
+                                                            : ((unsigned)b | ((unsigned)other << 16));
+                    sContact[cCur++] = c;
+                    if (bflag[other] & fIsl) continue;
+                    stack[stackCount++] = other;
+                    bflag[other] |= fIsl;
+                }
+                if (fb & fJoints) {
+                    B2G_WALK(e, bj[b].x, jNext(e), 2 * d.jointCount + 2) {
+                        Joint& J = jt[e >> 1];
+                        if (J.islandFlag) continue;
+                        const int other = jOther(e);
+                        if ((bflag[other] & fActive) == 0) continue;
+                        sJoint[jCur++] = e >> 1;
+                        J.islandFlag = 1;
+                        if (bflag[other] & fIsl) continue;
+                        stack[stackCount++] = other;
+                        bflag[other] |= fIsl;
+                    }
+                }
+            }
+            islands[nIsl] = make_int4(bStart, bCur - bStart, cStart, cCur - cStart);
+            islandJ[nIsl] = make_int2(jStart, jCur - jStart);
+            ++nIsl;
+            for (int i = cStart; i < cCur; ++i) {
+                const unsigned pr = icPairs[i - cStart];
+                const int bA = (int)(pr & 0xffffu), bB = (int)(pr >> 16);
+                const int lA = local[bA], lB = local[bB];
+                vc[i].idx = make_int4(bStart + lA, bStart + lB, 0, 0);
+                if (coloured) {
+                    const bool dA = (bflag[bA] & fDynamic) != 0, dB = (bflag[bB] & fDynamic) != 0;
+                    const unsigned long long used = (dA ? mask[lA] : 0ull) | (dB ? mask[lB] : 0ull);
+                    const unsigned long long freeBits = ~used & ((1ull << kSerialColour) - 1ull);
+                    const int col = freeBits ? __ffsll((long long)freeBits) - 1 : kSerialColour;
+                    if (col != kSerialColour) {
+                        if (dA) mask[lA] |= 1ull << col;
+                        if (dB) mask[lB] |= 1ull << col;
+                    }
+                    cColour[i] = col;
+                    ++colourCount[col];
+                }
+            }
+            for (int i = jStart; i < jCur; ++i) {
+                Joint& J = jt[sJoint[i]];
+                J.indexA = bStart + local[J.bodyA];
+                J.indexB = bStart + local[J.bodyB];
+            }
+            for (int i = 0; i < nStatics; ++i) bflag[statics[i]] &= (unsigned char)~fIsl;
+        }
+        sIsl = nIsl;
+        sRowsS = bCur;
+        sConsS = cCur;
+        sMovers = movers;
+    }
+    __syncthreads();
+    const int nRows = sRowsS, nCons = sConsS;
+    // write-back: body island flags, then wakes (b2Body::SetAwake(true) of every island body), then
+    // the island flag of every island contact
+    for (int b = tid(); b < nb; b += nthreads()) {
+        const int y = bi[b].y;
+        bi[b].y = (bflag[b] & fIsl) ? (y | kBIsland) : (y & ~kBIsland);
+    }
+    __syncthreads();
+    for (int r = tid(); r < nRows; r += nthreads()) setAwake(sBody[r], true);
+    for (int i = tid(); i < nCons; i += nthreads()) ci[sContact[i]].x |= kCIsland;
+    __syncthreads();
+    nIslOut = sIsl;
+    nRowsOut = nRows;
+    nConsOut = nCons;
+    moversOut = sMovers;
+    return true;
+}
+
 __device__ void Wd::solve(const StepParams& P, float4* smem, int smemRows, int smemContacts)
 {
     __shared__ int sIslands, sRows, sCons;
@@ -572,7 +857,18 @@ __device__ void Wd::solve(const StepParams& P, float4* smem, int smemRows, int s
     unsigned long long* smemMask = reinterpret_cast<unsigned long long*>(smem);
     const int smemMaskRows = 2 * smemRows;
     auto mask = [&](int r) -> unsigned long long& { return r < smemMaskRows ? smemMask[r] : rowMask[r]; };
-    if (tid() == 0) {
+    int fIsl = 0, fRows = 0, fCons = 0, fMovers = 0;
+    const bool fast = buildIslandsShared(coloured, sColourStart + 1, fIsl, fRows, fCons, fMovers);
+    if (fast) {
+        if (tid() == 0) {
+            sIslands = fIsl;
+            sRows = fRows;
+            sCons = fCons;
+            st->islands = fIsl;
+            st->solvedBodies = fMovers;
+            st->solvedContacts = fCons;
+        }
+    } else if (tid() == 0) {
         int nIsl = 0, bCur = 0, cCur = 0, jCur = 0, movers = 0;
         for (int seed = st->bodyList; seed != kNullIdx; seed = bj[seed].y) {
             int fl = bi[seed].y;
@@ -990,17 +1286,18 @@ __device__ void Wd::solveTOI(const StepParams& P)
 }
 
 // ------------------------------------------------------------------ kernels
-// b2World::Step (Dynamics/b2World.cpp:899-963) for world schedule[blockIdx.x].
-// Shared memory stages the island body rows (positions, then velocities) when a world's rows fit,
-// and the accumulated impulses of its island contacts when they fit.
-constexpr int kSmemRows = 640;
-constexpr int kSmemContacts = 1024;
-
-__global__ void __launch_bounds__(128) StepKernel(Batch B, StepParams P, const int* schedule)
+// b2World::Step (Dynamics/b2World.cpp:899-963) for world schedule[blockIdx.x], one CTA per world.
+// Shared memory (its size is the launch's choice, LaunchShape) stages the island body rows
+// (positions, then velocities) and the accumulated impulses of the island contacts when a world's
+// fit, and the broadphase proxies, pair keys and list heads outside the island solve; every use
+// falls back to global memory when the world is larger, so the shape changes speed, never results.
+__global__ void __launch_bounds__(128) StepKernel(Batch B, StepParams P, const int* schedule, LaunchShape L)
 {
     extern __shared__ float4 smem[];
     Wd W;
     W.init(B, schedule ? schedule[blockIdx.x] : blockIdx.x);
+    W.smemBase = smem;
+    W.smemBytes = (2 * L.smemRows + L.smemContacts) * (int)sizeof(float4);
     const bool newFixture = W.st->newFixture != 0;
     const unsigned long long t0 = clock64();
     __syncthreads();
@@ -1022,7 +1319,7 @@ __global__ void __launch_bounds__(128) StepKernel(Batch B, StepParams P, const i
     const unsigned long long t1 = clock64();
     W.collide();
     const unsigned long long t2 = clock64();
-    if (W.st->stepComplete && P.dt > 0.0f) W.solve(P, smem, kSmemRows, kSmemContacts);
+    if (W.st->stepComplete && P.dt > 0.0f) W.solve(P, smem, L.smemRows, L.smemContacts);
     __syncthreads();
     const unsigned long long t3 = clock64();
     if (W.st->continuous && P.dt > 0.0f) W.solveTOI(P);
@@ -1041,10 +1338,14 @@ __global__ void __launch_bounds__(128) StepKernel(Batch B, StepParams P, const i
 } // namespace b2g
 
 // Launch entry used by the host runtime (b2g_api.cu).
-cudaError_t b2gLaunchStep(const b2g::Batch& B, const b2g::StepParams& P, const int* schedule, int threads,
-                          cudaStream_t stream)
+cudaError_t b2gLaunchStep(const b2g::Batch& B, const b2g::StepParams& P, const int* schedule, int first, int count,
+                          int threads, int smemRows, int smemContacts, cudaStream_t stream)
 {
-    const size_t smem = (2 * b2g::kSmemRows + b2g::kSmemContacts) * sizeof(float4);
-    b2g::StepKernel<<<B.worlds, threads, smem, stream>>>(B, P, schedule);
+    if (count <= 0) return cudaSuccess;
+    b2g::LaunchShape L;
+    L.smemRows = smemRows;
+    L.smemContacts = smemContacts;
+    const size_t smem = (2 * (size_t)smemRows + smemContacts) * sizeof(float4);
+    b2g::StepKernel<<<count, threads, smem, stream>>>(B, P, schedule + first, L);
     return cudaGetLastError();
 }

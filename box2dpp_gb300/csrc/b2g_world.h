@@ -60,7 +60,8 @@ struct WorldState {
     // SM clock cycles of the last step per phase: 0 new-fixture pairs, 1 collide, 2 island DFS,
     // 3 island solve, 4 fixture sync, 5 pairs after solve, 6 TOI, 7 whole step; then the island solve
     // split: 8 integrate + constraint init, 9 warm start + velocity sweeps, 10 impulses + position
-    // integration, 11 position sweeps, 12 write-back, 13 sleep, 14-15 unused
+    // integration, 11 position sweeps, 12 write-back, 13 sleep; 14 pair finding and sorting, 15 contact
+    // creation (both summed over every UpdatePairs call of the step)
     unsigned long long cyc[16];
 };
 
@@ -166,6 +167,7 @@ struct Batch {
     unsigned long long* rowMask; // row-sized: colours used at each island body row
     unsigned long long* pairs; // pair-sized sort keys (proxyA << 32 | proxyB)
     int* pairKeep;
+    int4* pairInfo;  // pair-sized: a new contact's fixtures and bodies, worked out before creation
     int* movedList;  // proxy-sized
 };
 
@@ -177,6 +179,11 @@ enum : int { kSolverPlain = 0, kSolverColoured = 1 };
 // free and is solved by one thread in island order.
 constexpr int kColours = 64;
 constexpr int kSerialColour = kColours - 1;
+
+// Shared-memory shape of one step launch: island rows and contacts staged per CTA.
+struct LaunchShape {
+    int smemRows, smemContacts;
+};
 
 struct StepParams {
     float dt;

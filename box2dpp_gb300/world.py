@@ -60,6 +60,10 @@ class World:
     def step(self, dt: float = 1.0 / 60.0, vi: int = 8, pi: int = 3) -> None:
         _lib.check(self.lib.gb_world_step(self.h, dt, vi, pi), "gb_world_step")
 
+    def graph_step(self, dt: float = 1.0 / 60.0, vi: int = 8, pi: int = 3) -> None:
+        """One step replayed from a captured CUDA graph (see gb_world_graph_step)."""
+        _lib.check(self.lib.gb_world_graph_step(self.h, dt, vi, pi), "gb_world_graph_step")
+
     def sync(self) -> None:
         _lib.check(self.lib.gb_world_sync(self.h), "gb_world_sync")
 
@@ -77,6 +81,23 @@ class World:
         res = np.zeros(self.n_worlds, dtype=np.float32)
         _lib.check(self.lib.gb_world_solver_stats(self.h, col, its, res), "gb_world_solver_stats")
         return col, its, res
+
+    def autotune(self, steps_per_candidate: int = 2) -> None:
+        """Arm the online launch-plan autotuner over the next steps (see gb_world_autotune)."""
+        _lib.check(self.lib.gb_world_autotune(self.h, int(steps_per_candidate)), "gb_world_autotune")
+
+    def launch_plan(self):
+        """(classes as rows of first, count, threads, smem rows, smem contacts; best ms per candidate)."""
+        cls = np.zeros(5 * 8, dtype=np.int32)
+        ms = np.zeros(32, dtype=np.float32)
+        n, nc = C.c_int(), C.c_int()
+        _lib.check(self.lib.gb_world_launch_plan(self.h, cls, 8, C.byref(n), ms, 32, C.byref(nc)),
+                   "gb_world_launch_plan")
+        return cls[:5 * n.value].reshape(n.value, 5), ms[:nc.value]
+
+    def set_launch_plan(self, classes) -> None:
+        arr = np.ascontiguousarray(np.asarray(classes, dtype=np.int32).reshape(-1, 5))
+        _lib.check(self.lib.gb_world_set_launch_plan(self.h, arr.reshape(-1), len(arr)), "gb_world_set_launch_plan")
 
     def set_stream(self, stream_handle: int) -> None:
         _lib.check(self.lib.gb_world_set_stream(self.h, C.c_void_p(stream_handle)), "gb_world_set_stream")
@@ -123,7 +144,7 @@ class World:
 
     PHASES = ["new_pairs", "collide", "island_build", "island_solve", "fixture_sync", "pairs", "toi", "step",
               "solve_init", "solve_velocity", "solve_store_integrate", "solve_position", "solve_writeback",
-              "solve_sleep", "unused14", "unused15"]
+              "solve_sleep", "pairs_find_sort", "pairs_create"]
 
     def profile(self) -> np.ndarray:
         """SM clock cycles per world and phase of the last step, shape (worlds, 16) (see PHASES)."""

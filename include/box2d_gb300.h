@@ -105,6 +105,28 @@ gb_status gb_world_set_solver(gb_world* world, int solver, float tolerance, int 
  * solver, velocity iterations run, velocity residual (when measured). */
 gb_status gb_world_solver_stats(gb_world* world, int* colours, int* vel_iters, float* residual);
 
+/* Launch plan of the step (no counterpart in the reference, which steps one world on one thread).
+ * Worlds are scheduled largest first (by fixture count) and split into up to 4 classes, contiguous
+ * ranges of that schedule; each class is one launch with one CTA per world, its own CTA size and
+ * shared-memory shape, the launches forked onto side streams and joined back to the handle's stream.
+ * Every plan computes identical results; plans differ only in speed.
+ * gb_world_autotune arms the online autotuner: the next steps_per_candidate x (number of candidate
+ * plans) calls of gb_world_step run the candidates in turn, one step each per round (they are real
+ * steps), timed with CUDA events; then the candidate with the smallest median time becomes the plan.
+ * Tuning is skipped while the stream is being captured.
+ * gb_world_launch_plan reports the plan, classes[5 * i] = first schedule slot, count, threads per
+ * CTA, shared-memory island rows, shared-memory contacts, and after tuning the best time (ms) each
+ * candidate took. gb_world_set_launch_plan sets a plan in the same layout (classes must cover the
+ * schedule in order; threads a multiple of 32 in [32, 128]; at most 48 KB of shared memory). */
+gb_status gb_world_autotune(gb_world* world, int steps_per_candidate);
+/* gb_world_step as a CUDA graph: the first call (and any call after the step's parameters, solver
+ * or plan changed, or device memory was reallocated) captures one step, every launch of the plan,
+ * from the handle's stream into a graph; every call launches that graph once on the stream. */
+gb_status gb_world_graph_step(gb_world* world, float dt, int velocity_iterations, int position_iterations);
+gb_status gb_world_launch_plan(gb_world* world, int* classes, int cap, int* n_classes, float* candidate_ms,
+                               int ms_cap, int* n_candidates);
+gb_status gb_world_set_launch_plan(gb_world* world, const int* classes, int n);
+
 /* Binds the handle to a caller-owned cudaStream_t (NULL = the handle's own stream). */
 gb_status gb_world_set_stream(gb_world* world, void* cuda_stream);
 
@@ -140,7 +162,7 @@ gb_status gb_world_totals(gb_world* world, long long* out);
  * for i = 0 new-fixture pairs, 1 collide, 2 island build, 3 island solve, 4 fixture sync, 5 pairs,
  * 6 continuous (TOI), 7 whole step, and the island solve split 8 integrate + constraint init,
  * 9 warm start + velocity sweeps, 10 impulses + position integration, 11 position sweeps,
- * 12 write-back, 13 sleep (14, 15 unused). */
+ * 12 write-back, 13 sleep, 14 broadphase pair finding and sorting, 15 contact creation. */
 gb_status gb_world_profile(gb_world* world, unsigned long long* out);
 
 /* Whole-batch b2Body::ApplyForceToCenter + ApplyTorque for the next step (Box2D/Dynamics/b2Body.h:

@@ -19,14 +19,15 @@ pytestmark = pytest.mark.gpu
 def _run(scene_list, solver, steps, tolerance=0.0, vi=VI):
     w = World(scene_list)
     w.set_solver(solver, tolerance=tolerance, measure_residual=True)
-    res, its = [], []
+    res, its, cols = [], [], []
     for _ in range(steps):
         w.step(DT, vi, PI)
         col, it, r = w.solver_stats()
         res.append(r.copy())
         its.append(it.copy())
+        cols.append(col.copy())
     w.sync()
-    return w, np.array(res), np.array(its), col
+    return w, np.array(res), np.array(its), np.array(cols)
 
 
 def test_coloured_pyramid_stands_like_plain(gpu):
@@ -39,7 +40,7 @@ def test_coloured_pyramid_stands_like_plain(gpu):
     # Gauss-Seidel orders drift apart by a few millimetres per row of a 20-row stack)
     assert np.max(np.abs(bp[:, 0:2] - bc[:, 0:2])) < 0.05
     assert np.max(np.abs(bc[:, 5:8])) < 0.05  # at rest
-    assert 2 <= col[0] < 63
+    assert 2 <= col[:, 0].max() < 63  # colours while awake (the pile may fall asleep)
     # matched accuracy: the coloured solver's residual over the settled steps is no worse than 2x plain's
     assert np.median(rc[100:]) <= 2.0 * np.median(rp[100:]) + 1e-5
 
