@@ -2,18 +2,22 @@
 
 One step = one b2World::Step of every world of the batch: 4096 independent worlds (per GPU) whose
 body counts are log-uniform in [16, 512], each a seeded pyramid, box stacks or a circle/polygon drop,
-dt 1/60, 8 velocity / 3 position iterations, float32, sleeping disabled (every body is simulated on
-every step). Metric: body-steps per second (dynamic bodies x steps / time) over the whole job.
+dt 1/60, float32, sleeping disabled (every body is simulated on every step). Metric: body-steps per
+second (dynamic bodies x steps / time) over the whole job, at a stated velocity residual.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--worlds n]
 
-value: device time of the K timed steps (CUDA events on the stream the step kernel runs on), state
-resident in HBM (several hundred MB, larger than L2, so no flush is needed between steps).
-e2e: the same K steps through the C-ABI with host buffers: every step uploads the force/torque
-accumulators of every body from pinned host memory (gb_set_forces), steps, and reads every body
-transform back into pinned host memory (gb_get_transforms), wall-clock timed.
+value: the batched step as shipped for throughput: the graph-coloured island solver (8/3 iterations
+unless --coloured-vi says otherwise), launch plan picked by the online autotuner, each step replayed
+from a captured CUDA graph; device time of the K timed steps (CUDA events on the stream the step
+runs on), state resident in HBM (several hundred MB, larger than L2, so no flush between steps).
+plain: the same measurement with the reference-order solver (bit-exact with the reference).
+residual: the velocity residual (m/s, median over worlds of the last timed step) each solver leaves.
+e2e: the same K coloured steps through the C-ABI with host buffers: every step uploads the force
+and torque of every body from pinned host memory (gb_set_forces), steps (gb_world_graph_step) and
+reads every body transform back into pinned host memory (gb_get_transforms), wall-clock timed.
 --impl reference: the reference CPU step (the compiled reference where its build exists, else the
-project's CPU restatement of it) on all host cores over a sample of the same worlds.
+project's CPU restatement of it) on all host cores over the same worlds.
 """
 from __future__ import annotations
 
@@ -30,7 +34,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 DT, VI, PI = 1.0 / 60.0, 8, 3
-METRIC = "body-steps/sec (batched worlds, plain solver)"
+METRIC = "body-steps/sec at fixed residual (batched worlds)"
 UNIT = "body-steps/s"
 
 
@@ -42,8 +46,10 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--worlds", type=int, default=4096)
     p.add_argument("--seed", type=int, default=1)
-    p.add_argument("--cpu-sample-every", type=int, default=8)
+    p.add_argument("--cpu-steps", type=int, default=200, help="steps of the CPU baseline sample")
+    p.add_argument("--coloured-vi", type=int, default=8, help="velocity iterations of the coloured solver")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-plain", action="store_true")
     return p.parse_args()
 
 
@@ -150,11 +156,11 @@ def algorithmic_bytes(t: dict) -> int:
     return 104 * t["solved_bodies"] + 144 * t["solved_contacts"] + 32 * t["proxies"] + 8 * t["pairs"]
 
 
-def cpu_baseline(worlds, steps: int, warmup: int, every: int, threads: int):
-    """The reference CPU step on `threads` host threads over every `every`-th world."""
+def cpu_baseline(worlds, steps: int, warmup: int, threads: int):
+    """The reference CPU step (plain solver order) on `threads` host threads over all the worlds."""
     import oracle
 
-    sample = worlds[::every]
+    sample = worlds
     kind = "reference" if oracle.reference_available() and os.path.exists(os.path.join(ROOT, "oracle", "_ref",
                                                                                       "libref_libm.so")) else "port"
     trig = "libm" if kind == "reference" else "project"
@@ -172,8 +178,8 @@ def cpu_baseline(worlds, steps: int, warmup: int, every: int, threads: int):
         "unit": UNIT,
         "cores": threads,
         "kind": kind,
-        "sample": f"{len(sample)} of the {len(worlds)} worlds (every {every}th, {bodies} dynamic bodies), "
-                  f"{steps} steps after {warmup} warm-up steps, {el:.2f} s",
+        "sample": f"all {len(sample)} worlds ({bodies} dynamic bodies), {steps} steps after {warmup} warm-up "
+                  f"steps, {el:.2f} s, 8/3 iterations (the reference's solver order)",
     }
 
 
@@ -183,7 +189,7 @@ def run_reference(args):
         return
     worlds = workload(args, 0)
     threads = os.cpu_count() or 1
-    cb = cpu_baseline(worlds, args.steps, args.warmup, args.cpu_sample_every, threads)
+    cb = cpu_baseline(worlds, args.steps, args.warmup, threads)
     line = {
         "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
@@ -195,7 +201,40 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _timed_steps(w, stream, steps: int, vi: int, clk=None):
+    """K graph-replayed steps between two CUDA events on the step's stream; returns ms."""
+    import torch
+
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(steps):
+        w.graph_step(DT, vi, PI)
+    end.record(stream)
+    end.synchronize()
+    return start.elapsed_time(end)
+
+
+def _prepare(worlds, stream, solver: str, vi: int, warmup: int):
+    """World batch on the GPU with the given solver, autotuned launch plan and warm-up steps."""
+    from box2dpp_gb300.world import World
+
+    w = World(worlds)
+    w.set_stream(stream.cuda_stream)
+    w.set_solver(solver, measure_residual=True)
+    w.upload()
+    w.autotune(2)
+    tune_steps = 0
+    while len(w.launch_plan()[1]) == 0 and tune_steps < 256:
+        w.step(DT, vi, PI)
+        tune_steps += 1
+    for _ in range(warmup):
+        w.graph_step(DT, vi, PI)
+    w.sync()
+    return w, tune_steps
+
+
 def run_gpu(args):
+    import numpy as np
     import torch
 
     rank, world_size, local = dist_env()
@@ -204,18 +243,8 @@ def run_gpu(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    from box2dpp_gb300.world import World
-
     worlds = workload(args, rank)
-    w = World(worlds)
     stream = torch.cuda.Stream()
-    w.set_stream(stream.cuda_stream)
-    w.upload()
-    n_dyn = w.dynamic_bodies
-    for _ in range(args.warmup):
-        w.step(DT, VI, PI)
-    w.sync()
-    t_before = w.totals()
 
     def barrier():
         torch.cuda.synchronize()
@@ -225,25 +254,27 @@ def run_gpu(args):
             dist.barrier()
             torch.cuda.synchronize()
 
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    def max_over_ranks(x: float) -> float:
+        t = torch.tensor([x], device="cuda")
+        if world_size > 1:
+            import torch.distributed as dist
+
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    vi = args.coloured_vi
+    w, tune_steps = _prepare(worlds, stream, "coloured", vi, args.warmup)
+    n_dyn = w.dynamic_bodies
+    t_before = w.totals()
+    plan, cand_ms = w.launch_plan()
     barrier()
     with ClockSampler(local) as clk:
-        with torch.cuda.stream(stream):
-            start.record(stream)
-            for _ in range(args.steps):
-                w.step(DT, VI, PI)
-            end.record(stream)
-        end.synchronize()
+        ms = _timed_steps(w, stream, args.steps, vi)
     barrier()
-    ms = start.elapsed_time(end)
     w.sync()
     t_after = w.totals()
-    ms_t = torch.tensor([ms], device="cuda")
-    if world_size > 1:
-        import torch.distributed as dist
-
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms_max = float(ms_t.item())
+    _, _, res = w.solver_stats()
+    ms_max = max_over_ranks(ms)
     total_bodies = n_dyn * world_size
     value = total_bodies * args.steps / (ms_max / 1e3)
 
@@ -255,16 +286,25 @@ def run_gpu(args):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         w.set_forces_ptr(forces.data_ptr())
-        w.step(DT, VI, PI)
+        w.graph_step(DT, vi, PI)
         w.get_transforms_ptr(xforms.data_ptr())
     w.sync()
-    e2e_s = time.perf_counter() - t0
-    e2e_t = torch.tensor([e2e_s], device="cuda")
-    if world_size > 1:
-        import torch.distributed as dist
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_value = total_bodies * args.steps / e2e_s
+    w.close()
 
-        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-    e2e_value = total_bodies * args.steps / float(e2e_t.item())
+    plain = None
+    if not args.no_plain:
+        wp, _ = _prepare(worlds, stream, "plain", VI, args.warmup)
+        barrier()
+        ms_p = max_over_ranks(_timed_steps(wp, stream, args.steps, VI))
+        _, _, res_p = wp.solver_stats()
+        plain_plan, _ = wp.launch_plan()
+        plain = {"value": total_bodies * args.steps / (ms_p / 1e3), "unit": UNIT, "ms_per_step": ms_p / args.steps,
+                 "velocity_iterations": VI, "residual_median": float(np.median(res_p)),
+                 "launch_plan": plain_plan.tolist(),
+                 "note": "reference-order per-island Gauss-Seidel, bit-exact with the reference"}
+        wp.close()
 
     if rank == 0:
         peak, peak_kind = measured_peaks()
@@ -275,23 +315,30 @@ def run_gpu(args):
                 "traffic": None, "peak_source": peak_kind, "kernel": "b2g::StepKernel",
                 "algorithmic_bytes_per_launch": step_bytes,
                 "launch_ms": per_launch_ms,
+                "note": "one step = the launches of the plan (one per class); bytes and time are per step",
                 "counts_per_step": {k: (t_before[k] + t_after[k]) / 2.0 for k in
                                     ("solved_bodies", "solved_contacts", "proxies", "pairs", "toi_events")}}
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config_dict(args, worlds), "roofline": roof,
+            "config": config_dict(args, worlds, {
+                "solver": f"graph-coloured, {vi}/3 iterations",
+                "launch_plan": plan.tolist(), "autotune_candidate_ms": [round(float(x), 3) for x in cand_ms],
+                "autotune_steps": tune_steps, "cuda_graph": "one captured step replayed per step"}),
+            "residual": {"coloured_median": float(np.median(res)), "unit": "m/s",
+                         "definition": "max over contacts of |vn - bias| (active normal), max(0, bias - vn) "
+                                       "(inactive), |vt| (unsaturated friction), after the velocity iterations"},
+            "plain": plain,
+            "roofline": roof,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nb * 16, "d2h_bytes_per_step": nb * 16,
-                    "calls": "gb_set_forces + gb_world_step + gb_get_transforms per step, pinned host buffers"},
-            "gpu_launches": args.steps,
+                    "calls": "gb_set_forces + gb_world_graph_step + gb_get_transforms per step, pinned host buffers"},
+            "gpu_launches": args.steps * len(plan),
             "clocks": clk.summary(),
         }
         if not args.no_cpu_baseline and world_size == 1:
-            line["cpu_baseline"] = cpu_baseline(worlds, args.steps, args.warmup, args.cpu_sample_every,
-                                                os.cpu_count() or 1)
+            line["cpu_baseline"] = cpu_baseline(worlds, args.cpu_steps, args.warmup, os.cpu_count() or 1)
         print(json.dumps(line), flush=True)
-    w.close()
     if world_size > 1:
         import torch.distributed as dist
 

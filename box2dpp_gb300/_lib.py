@@ -15,6 +15,7 @@ from . import build as _build
 GB_OK, GB_ERR_CAPACITY, GB_ERR_TIMEOUT, GB_ERR_INVALID, GB_ERR_CUDA = 0, 1, 2, 3, 4
 COLLIDE_NOALLOC_MAX_PAIRS = 4096  # GB_COLLIDE_NOALLOC_MAX_PAIRS
 SOLVER_PLAIN, SOLVER_COLOURED = 0, 1
+WARM_REFERENCE, WARM_LEARNED = 0, 1
 STATUS_NAMES = {0: "GB_OK", 1: "GB_ERR_CAPACITY", 2: "GB_ERR_TIMEOUT", 3: "GB_ERR_INVALID", 4: "GB_ERR_CUDA"}
 
 # Every symbol include/box2d_gb300.h declares.
@@ -25,6 +26,9 @@ EXPORTS = [
     "gb_collide", "gb_version", "gb_world_totals", "gb_set_forces", "gb_get_transforms", "gb_world_profile",
     "gb_collide_noalloc", "gb_world_set_solver", "gb_world_solver_stats", "gb_world_autotune",
     "gb_world_launch_plan", "gb_world_set_launch_plan", "gb_world_graph_step",
+    "gb_mlp_create", "gb_mlp_destroy", "gb_mlp_param_count", "gb_mlp_set_params", "gb_mlp_get_params",
+    "gb_mlp_forward", "gb_mlp_gradients", "gb_mlp_train", "gb_world_set_warm_start", "gb_world_warm_stats",
+    "gb_world_set_contact_log", "gb_world_read_contact_log",
 ]
 
 
@@ -41,6 +45,19 @@ class WorldDef(C.Structure):
 
 _f32 = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 _i32 = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+class _NullableF32:
+    """ctypes argtype: a C-contiguous float32 array, or None for NULL."""
+
+    @classmethod
+    def from_param(cls, obj):
+        if obj is None:
+            return None
+        return _f32.from_param(obj)
+
+
+_f32n = _NullableF32
 _LIB = None
 
 
@@ -83,6 +100,17 @@ def load(build_if_missing: bool = True):
         "gb_world_solver_stats": [vp, _i32, _i32, _f32],
         "gb_world_autotune": [vp, i],
         "gb_world_graph_step": [vp, f, i, i],
+        "gb_mlp_create": [C.c_ulonglong, C.POINTER(vp)],
+        "gb_world_set_warm_start": [vp, vp, i],
+        "gb_world_warm_stats": [vp, _i32],
+        "gb_world_set_contact_log": [vp, i],
+        "gb_world_read_contact_log": [vp, _f32, _f32, i, C.POINTER(i)],
+        "gb_mlp_destroy": [vp],
+        "gb_mlp_set_params": [vp, _f32n, _f32n, _f32n],
+        "gb_mlp_get_params": [vp, _f32, _f32, _f32],
+        "gb_mlp_forward": [vp, _f32, i, _f32],
+        "gb_mlp_gradients": [vp, _f32, _f32, i, _f32, C.POINTER(f)],
+        "gb_mlp_train": [vp, _f32, _f32, i, i, i, f, C.c_ulonglong, _f32],
         "gb_world_launch_plan": [vp, _i32, i, C.POINTER(i), _f32, i, C.POINTER(i)],
         "gb_world_set_launch_plan": [vp, _i32, i],
         "gb_world_totals": [vp, C.POINTER(C.c_longlong)],
@@ -94,6 +122,8 @@ def load(build_if_missing: bool = True):
         fn = getattr(lib, name)
         fn.argtypes = args
         fn.restype = C.c_int
+    lib.gb_mlp_param_count.argtypes = []
+    lib.gb_mlp_param_count.restype = C.c_int
     lib.gb_version.argtypes = []
     lib.gb_version.restype = C.c_char_p
     _LIB = lib

@@ -22,6 +22,7 @@
 cudaError_t b2gLaunchStep(const b2g::Batch& B, const b2g::StepParams& P, const int* schedule, int first, int count,
                           int threads, int smemRows, int smemContacts, cudaStream_t stream);
 cudaError_t b2gLaunchSinCos(const float* x, float* s, float* c, int n, cudaStream_t stream);
+b2g::MlpView b2gMlpView(const gb_mlp* m);
 cudaError_t b2gLaunchCollide(int n, const b2g::Shape* a, const float4* xa, const b2g::Shape* b, const float4* xb,
                              int4* oi, float4* of, cudaStream_t stream);
 
@@ -111,12 +112,19 @@ struct gb_world {
     // one captured step (every launch of the plan) replayed by gb_world_graph_step
     cudaGraphExec_t graph = nullptr;
     float graphDt = 0.0f;
-    int graphVi = -1, graphPi = -1, graphSolver = -1, graphMeasure = -1;
+    int graphVi = -1, graphPi = -1, graphSolver = -1, graphMeasure = -1, graphWarm = -1;
+    const float* graphLog = nullptr;
     float graphTol = -1.0f;
     LaunchPlan graphPlan;
     int solver = kSolverPlain;
     float tolerance = 0.0f;
     int measureResidual = 0;
+    int warmMode = kWarmReference;
+    MlpView mlp{};
+    float* logX = nullptr;   // contact-point log (device), see gb_world_set_contact_log
+    float* logT = nullptr;
+    int* logCount = nullptr;
+    int logCap = 0;
 };
 
 namespace {
@@ -376,6 +384,36 @@ std::vector<LaunchPlan> CandidatePlans(const gb_world* g)
     return c;
 }
 
+StepParams MakeParams(const gb_world* g, float dt, int vi, int pi)
+{
+    StepParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.dt = dt;
+    P.velocityIterations = vi;
+    P.positionIterations = pi;
+    P.maxToiEvents = 4096;
+    P.solver = g->solver;
+    P.tolerance = g->tolerance;
+    P.measureResidual = g->measureResidual;
+    P.warmMode = g->warmMode;
+    P.mlp = g->mlp;
+    P.logX = g->logX;
+    P.logT = g->logT;
+    P.logCount = g->logCount;
+    P.logCap = g->logCap;
+    return P;
+}
+
+void FreeLog(gb_world* g)
+{
+    if (g->logX) cudaFree(g->logX);
+    if (g->logT) cudaFree(g->logT);
+    if (g->logCount) cudaFree(g->logCount);
+    g->logX = g->logT = nullptr;
+    g->logCount = nullptr;
+    g->logCap = 0;
+}
+
 gb_status EnsureSideStreams(gb_world* g, int n)
 {
     if (!g->fork) GB_CUDA(cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming));
@@ -524,8 +562,8 @@ gb_status Upload(gb_world* g)
     ALLOC(order, tc); ALLOC(cnext, tc);
     ALLOC(joint, tj); ALLOC(sJoint, tj);
     ALLOC(sBody, tr); ALLOC(sStack, tb); ALLOC(sWake, tb); ALLOC(sPos, tr); ALLOC(sVel, tr); ALLOC(islands, tb);
-    ALLOC(islandJ, tb); ALLOC(sleepOut, tb); ALLOC(rowMask, tr);
-    ALLOC(sContact, tc); ALLOC(sStatus, tc); ALLOC(vc, tc); ALLOC(pc, tc); ALLOC(vimp, tc); ALLOC(toi, tc); ALLOC(cColour, tc); ALLOC(colourList, tc);
+    ALLOC(islandJ, tb); ALLOC(sleepOut, tb); ALLOC(rowMask, tr); ALLOC(sVelL, tr);
+    ALLOC(sContact, tc); ALLOC(sStatus, tc); ALLOC(vc, tc); ALLOC(pc, tc); ALLOC(vimp, tc); ALLOC(vimpL, tc); ALLOC(vsep, tc); ALLOC(toi, tc); ALLOC(cColour, tc); ALLOC(colourList, tc);
     ALLOC(pairs, tq); ALLOC(pairKeep, tq); ALLOC(pairInfo, tq);
 #undef ALLOC
     GB_CUDA(cudaMemcpy(B.desc, g->desc.data(), nw * sizeof(WorldDesc), cudaMemcpyHostToDevice));
@@ -761,6 +799,7 @@ gb_status gb_world_destroy(gb_world* g)
         if (g->side[i]) cudaStreamSynchronize(g->side[i]);
     FreeDevice(g);
     ReleaseLaunchResources(g);
+    FreeLog(g);
     if (g->ownStream && g->stream) cudaStreamDestroy(g->stream);
     delete g;
     return GB_OK;
@@ -835,15 +874,7 @@ gb_status gb_world_step(gb_world* g, float dt, int vi, int pi)
     if (!g || vi < 0 || pi < 0) return GB_ERR_INVALID;
     gb_status s = Upload(g);
     if (s != GB_OK) return s;
-    StepParams P;
-    P.dt = dt;
-    P.velocityIterations = vi;
-    P.positionIterations = pi;
-    P.maxToiEvents = 4096;
-    P.solver = g->solver;
-    P.tolerance = g->tolerance;
-    P.measureResidual = g->measureResidual;
-    P.pad = 0;
+    const StepParams P = MakeParams(g, dt, vi, pi);
     if (g->tuneIndex >= 0) {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         GB_CUDA(cudaStreamIsCapturing(g->stream, &cs));
@@ -860,22 +891,15 @@ gb_status gb_world_graph_step(gb_world* g, float dt, int vi, int pi)
     if (s != GB_OK) return s;
     const bool reuse = g->graph && g->graphDt == dt && g->graphVi == vi && g->graphPi == pi &&
                        g->graphSolver == g->solver && g->graphTol == g->tolerance &&
-                       g->graphMeasure == g->measureResidual && SamePlan(g->graphPlan, g->plan);
+                       g->graphMeasure == g->measureResidual && g->graphWarm == g->warmMode &&
+                       g->graphLog == g->logX && SamePlan(g->graphPlan, g->plan);
     if (!reuse) {
         ReleaseGraph(g);
         if (g->plan.size() > 1) {
             s = EnsureSideStreams(g, (int)g->plan.size());
             if (s != GB_OK) return s;
         }
-        StepParams P;
-        P.dt = dt;
-        P.velocityIterations = vi;
-        P.positionIterations = pi;
-        P.maxToiEvents = 4096;
-        P.solver = g->solver;
-        P.tolerance = g->tolerance;
-        P.measureResidual = g->measureResidual;
-        P.pad = 0;
+        const StepParams P = MakeParams(g, dt, vi, pi);
         GB_CUDA(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
         s = LaunchPlanStep(g, P, g->plan);
         cudaGraph_t graph = nullptr;
@@ -887,6 +911,7 @@ gb_status gb_world_graph_step(gb_world* g, float dt, int vi, int pi)
         GB_CUDA(ei);
         g->graphDt = dt; g->graphVi = vi; g->graphPi = pi; g->graphSolver = g->solver;
         g->graphTol = g->tolerance; g->graphMeasure = g->measureResidual; g->graphPlan = g->plan;
+        g->graphWarm = g->warmMode; g->graphLog = g->logX;
     }
     GB_CUDA(cudaGraphLaunch(g->graph, g->stream));
     return GB_OK;
@@ -978,6 +1003,44 @@ gb_status gb_world_set_solver(gb_world* g, int solver, float tolerance, int meas
     return GB_OK;
 }
 
+gb_status gb_world_set_warm_start(gb_world* g, gb_mlp* mlp, int mode)
+{
+    if (!g || (mode != kWarmReference && mode != kWarmLearned) || (mode == kWarmLearned && !mlp)) return GB_ERR_INVALID;
+    g->warmMode = mode;
+    g->mlp = mode == kWarmLearned ? b2gMlpView(mlp) : MlpView{};
+    return GB_OK;
+}
+
+gb_status gb_world_set_contact_log(gb_world* g, int capacity)
+{
+    if (!g || capacity < 0) return GB_ERR_INVALID;
+    if (g->stream) GB_CUDA(cudaStreamSynchronize(g->stream));
+    FreeLog(g);
+    if (capacity == 0) return GB_OK;
+    GB_CUDA(cudaMalloc(&g->logX, (size_t)capacity * 14 * sizeof(float)));
+    GB_CUDA(cudaMalloc(&g->logT, (size_t)capacity * 2 * sizeof(float)));
+    GB_CUDA(cudaMalloc(&g->logCount, sizeof(int)));
+    GB_CUDA(cudaMemset(g->logCount, 0, sizeof(int)));
+    g->logCap = capacity;
+    return GB_OK;
+}
+
+gb_status gb_world_read_contact_log(gb_world* g, float* x, float* t, int cap, int* n)
+{
+    if (!g || !n || cap < 0) return GB_ERR_INVALID;
+    *n = 0;
+    if (!g->logCount) return GB_OK;
+    if (g->stream) GB_CUDA(cudaStreamSynchronize(g->stream));
+    int count = 0;
+    GB_CUDA(cudaMemcpy(&count, g->logCount, sizeof(int), cudaMemcpyDeviceToHost));
+    const int m = std::min(std::min(count, g->logCap), cap);
+    if (m > 0 && x) GB_CUDA(cudaMemcpy(x, g->logX, (size_t)m * 14 * sizeof(float), cudaMemcpyDeviceToHost));
+    if (m > 0 && t) GB_CUDA(cudaMemcpy(t, g->logT, (size_t)m * 2 * sizeof(float), cudaMemcpyDeviceToHost));
+    GB_CUDA(cudaMemset(g->logCount, 0, sizeof(int)));
+    *n = m;
+    return count > g->logCap ? GB_ERR_CAPACITY : GB_OK;
+}
+
 gb_status gb_world_solver_stats(gb_world* g, int* colours, int* vel_iters, float* residual)
 {
     if (!g) return GB_ERR_INVALID;
@@ -998,6 +1061,21 @@ gb_status gb_world_solver_stats(gb_world* g, int* colours, int* vel_iters, float
         if (vel_iters) vel_iters[i] = st[i].velIters;
         if (residual) residual[i] = st[i].residual;
     }
+    return GB_OK;
+}
+
+gb_status gb_world_warm_stats(gb_world* g, int* learned_used)
+{
+    if (!g || !learned_used) return GB_ERR_INVALID;
+    const int nw = (int)g->worlds.size();
+    if (!g->onDevice) {
+        for (int i = 0; i < nw; ++i) learned_used[i] = 0;
+        return GB_OK;
+    }
+    GB_CUDA(cudaStreamSynchronize(g->stream));
+    std::vector<WorldState> st(nw);
+    GB_CUDA(cudaMemcpy(st.data(), g->batch.state, nw * sizeof(WorldState), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < nw; ++i) learned_used[i] = st[i].warmLearned;
     return GB_OK;
 }
 
@@ -1184,7 +1262,7 @@ gb_status gb_world_profile(gb_world* g, unsigned long long* out)
         for (int i = 0; i < nw; ++i) st[i] = g->worlds[i].state;
     }
     for (int i = 0; i < nw; ++i)
-        for (int k = 0; k < 16; ++k) out[16 * i + k] = st[i].cyc[k];
+        for (int k = 0; k < kProfileSlots; ++k) out[(size_t)kProfileSlots * i + k] = st[i].cyc[k];
     return GB_OK;
 }
 

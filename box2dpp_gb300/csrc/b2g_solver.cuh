@@ -54,7 +54,7 @@ __device__ void ContactSetup(const Wd& W, VelConstraint& v, PosConstraint& p, fl
 
 // b2ContactSolver::InitializeVelocityConstraints, one contact (b2ContactSolver.cpp:143-252)
 __device__ void ContactInitVelocity(const Wd& W, VelConstraint& v, const PosConstraint& p, const float4* pos,
-                                    const float4* vel)
+                                    const float4* vel, float2* sepOut = nullptr)
 {
     Manifold m;
     W.loadManifold(v.idx.w, m);
@@ -72,6 +72,7 @@ __device__ void ContactInitVelocity(const Wd& W, VelConstraint& v, const PosCons
     xfB.p = cB - Mul(xfB.q, V(p.lc.z, p.lc.w));
     WorldManifold wm;
     WorldManifoldInit(&wm, m, xfA, p.rad.x, xfB, p.rad.y);
+    if (sepOut) *sepOut = make_float2(v.idx.z > 0 ? wm.sep[0] : 0.0f, v.idx.z > 1 ? wm.sep[1] : 0.0f);
     const Vec2 normal = wm.normal;
     v.nf.x = normal.x;
     v.nf.y = normal.y;
@@ -582,6 +583,110 @@ __device__ float ctaMaxNonNeg(float x, int* slot)
     return __int_as_float(*slot);
 }
 
+// ------------------------------------------------------------------ learned warm start
+// The 14 features of point j of a contact at the start of the velocity solve (after velocity
+// integration, before any warm start): world normal (2), relative normal and tangent velocity of
+// the point, its separation, the four inverse masses and inertias, the reference warm-start normal
+// and tangent impulses (the previous step's, scaled by dtRatio; zero for new points) expressed as
+// velocities (impulse / effective mass), the effective inverse normal mass, the friction
+// coefficient, and whether the manifold has two points. The network predicts the point's final
+// normal and tangent impulses in the same velocity units.
+__device__ void PointFeatures(const VelConstraint& v, const float4 imp, const float2 sep, const float4* vel, int j,
+                              float (&f)[kMlpIn])
+{
+    const float4 va = vel[v.idx.x], vb = vel[v.idx.y];
+    const float4 r = j == 0 ? v.r0 : v.r1;
+    const float4 c = j == 0 ? v.c0 : v.c1;
+    const Vec2 n = V(v.nf.x, v.nf.y), t = Cross(n, 1.0f);
+    const Vec2 dv = V(vb.x, vb.y) + Cross(vb.z, V(r.z, r.w)) - V(va.x, va.y) - Cross(va.z, V(r.x, r.y));
+    const float kn = c.x > 0.0f ? 1.0f / c.x : 0.0f, kt = c.y > 0.0f ? 1.0f / c.y : 0.0f;
+    f[0] = n.x; f[1] = n.y;
+    f[2] = Dot(dv, n);
+    f[3] = Dot(dv, t) - v.nf.w;
+    f[4] = j == 0 ? sep.x : sep.y;
+    f[5] = v.m.x; f[6] = v.m.y; f[7] = v.m.z; f[8] = v.m.w;
+    f[9] = (j == 0 ? imp.x : imp.z) * kn;
+    f[10] = (j == 0 ? imp.y : imp.w) * kt;
+    f[11] = kn;
+    f[12] = v.nf.z;
+    f[13] = v.idx.z == 2 ? 1.0f : 0.0f;
+}
+
+// Network predictions for every island contact point, written to vimpL: one 16-row tile (8
+// contacts, 2 points each) per warp at a time; rows of absent points are zero and ignored. The
+// prediction is decoded as normal impulse max(0, y0 * normalMass) and tangent impulse y1 *
+// tangentMass clamped to the friction cone.
+__device__ __noinline__ void Wd::learnedImpulses(const StepParams& P, int nContacts, const float4* imp, const float4* vel)
+{
+    __shared__ __align__(16) __nv_bfloat16 xTile[kMaxCta / 32][16 * kMlpInPad];
+    const int warp = tid() >> 5, lane = tid() & 31, g = lane >> 2, t = lane & 3;
+    const int warps = nthreads() >> 5;
+    const int tiles = (nContacts + 7) / 8;
+    __nv_bfloat16* x = xTile[warp];
+    for (int tile = warp; tile < tiles; tile += warps) {
+        if (lane < 16) {
+            const int i = 8 * tile + (lane >> 1), j = lane & 1;
+            float f[kMlpIn];
+            bool ok = false;
+            if (i < nContacts) {
+                const VelConstraint v = vc[i];
+                if (j < v.idx.z) {
+                    PointFeatures(v, imp[i], vsep[i], vel, j, f);
+                    ok = true;
+                }
+            }
+            for (int k = 0; k < kMlpInPad; ++k) {
+                const float val = (ok && k < kMlpIn) ? (f[k] - P.mlp.mu[k]) / P.mlp.sigma[k] : 0.0f;
+                x[lane * kMlpInPad + k] = __float2bfloat16_rn(val);
+            }
+        }
+        __syncwarp();
+        float out[4];
+        MlpForwardTile(P.mlp, x, out);
+        if (t == 0) {
+            for (int h = 0; h < 2; ++h) {
+                const int row = g + 8 * h, i = 8 * tile + (row >> 1), j = row & 1;
+                if (i >= nContacts) continue;
+                const VelConstraint v = vc[i];
+                if (j >= v.idx.z) continue;
+                const float4 c = j == 0 ? v.c0 : v.c1;
+                const float ni = fmaxf(0.0f, out[2 * h] * c.x);
+                const float bound = v.nf.z * ni;
+                const float ti = fminf(fmaxf(out[2 * h + 1] * c.y, -bound), bound);
+                float* dst = reinterpret_cast<float*>(&vimpL[i]) + 2 * j;
+                dst[0] = ni;
+                dst[1] = ti;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Warm start of every island contact with impulses im on velocities v: per island in the reference
+// order (plain), or colour by colour (coloured).
+__device__ void Wd::warmStartAll(int nIsl, const int* colourStart, const float4* im, float4* v)
+{
+    if (colourStart == nullptr) {
+        for (int isl = tid(); isl < nIsl; isl += nthreads()) {
+            const int4 I = islands[isl];
+            for (int i = I.z; i < I.z + I.w; ++i) ContactWarmStart(vc[i], im[i], v);
+        }
+        __syncthreads();
+        return;
+    }
+    for (int k = 0; k < kColours; ++k) {
+        const int lo = colourStart[k], hi = colourStart[k + 1];
+        if (lo == hi) continue;
+        if (k == kSerialColour) {
+            if (tid() == 0)
+                for (int q = lo; q < hi; ++q) ContactWarmStart(vc[colourList[q]], im[colourList[q]], v);
+        } else {
+            for (int q = lo + tid(); q < hi; q += nthreads()) ContactWarmStart(vc[colourList[q]], im[colourList[q]], v);
+        }
+        __syncthreads();
+    }
+}
+
 // ------------------------------------------------------------------ island solve
 // b2Island::Solve (Dynamics/b2Island.cpp:185-384) for all islands of the world at once. Per-body and
 // per-contact work that the reference does in independent loops (integration, constraint setup and
@@ -600,6 +705,9 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
     const float gx = st->gx, gy = st->gy;
     const bool rowsInSmem = nRows <= smemRows;
     const bool coloured = colourStart != nullptr;
+    const bool learned = P.warmMode == kWarmLearned && warm;
+    const bool logging = P.logX != nullptr && !coloured;
+    const bool needSep = learned || logging;
     float4* pos = rowsInSmem ? smem : sPos;
     float4* vel = rowsInSmem ? smem + smemRows : sVel;
     float4* imp = nContacts <= smemContacts ? smem + 2 * smemRows : vimp;
@@ -630,12 +738,46 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
         PosConstraint p;
         float4 im;
         ContactSetup(*this, v, p, im, sContact[i], warm, dtRatio);
-        ContactInitVelocity(*this, v, p, pos, vel);
+        ContactInitVelocity(*this, v, p, pos, vel, needSep ? &vsep[i] : nullptr);
         vc[i] = v;
         pc[i] = p;
         imp[i] = im;
+        if (logging) {
+            // reserve the contact's log rows and write its features now (start of the solve)
+            const int base = atomicAdd(P.logCount, v.idx.z);
+            sStatus[i] = base;
+            for (int j = 0; j < v.idx.z && base + j < P.logCap; ++j) {
+                float f[kMlpIn];
+                PointFeatures(v, im, vsep[i], vel, j, f);
+                for (int k = 0; k < kMlpIn; ++k) P.logX[(size_t)(base + j) * kMlpIn + k] = f[k];
+            }
+        }
     }
     __syncthreads();
+    // learned warm start: predictions, then both warm starts on their own velocity copies; the world
+    // keeps the one whose velocity residual is smaller (the reference's on a tie)
+    bool warmDone = false;
+    if (learned && nContacts > 0) {
+        learnedImpulses(P, nContacts, imp, vel);
+        for (int r = tid(); r < nRows; r += nthreads()) sVelL[r] = vel[r];
+        __syncthreads();
+        warmStartAll(nIsl, colourStart, imp, vel);
+        warmStartAll(nIsl, colourStart, vimpL, sVelL);
+        float rRef = 0.0f, rL = 0.0f;
+        for (int i = tid(); i < nContacts; i += nthreads()) {
+            rRef = fmaxf(rRef, ContactResidual(vc[i], imp[i], vel));
+            rL = fmaxf(rL, ContactResidual(vc[i], vimpL[i], sVelL));
+        }
+        rRef = ctaMaxNonNeg(rRef, &sRes);
+        rL = ctaMaxNonNeg(rL, &sRes);
+        if (rL < rRef) {
+            for (int r = tid(); r < nRows; r += nthreads()) vel[r] = sVelL[r];
+            for (int i = tid(); i < nContacts; i += nthreads()) imp[i] = vimpL[i];
+            if (tid() == 0) st->warmLearned = 1;
+        }
+        __syncthreads();
+        warmDone = true;
+    }
     if (tid() == 0) { unsigned long long now = clock64(); st->cyc[8] = now - tStamp; tStamp = now; }
     int itersRun = P.velocityIterations;
     if (!coloured) {
@@ -646,7 +788,7 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
             int4 I = islands[isl];
             int2 J = islandJ[isl];
             const int lo = I.z, hi = I.z + I.w;
-            if (warm)
+            if (warm && !warmDone)
                 for (int i = lo; i < hi; ++i) ContactWarmStart(vc[i], imp[i], vel);
             for (int k = 0; k < J.y; ++k) RevInit(*this, jt[sJoint[J.x + k]], pos, vel, warm, dtRatio);
             int it = 0;
@@ -666,7 +808,7 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
     } else {
         // colour by colour: warm start, joint initialisation per island, then the iterations
         const int nCol = kColours;
-        if (warm) {
+        if (warm && !warmDone) {
             for (int k = 0; k < nCol; ++k) {
                 const int lo = colourStart[k], hi = colourStart[k + 1];
                 if (lo == hi) continue;
@@ -730,6 +872,19 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
         if (tid() == 0) st->residual = r;
     }
     if (tid() == 0) st->velIters = itersRun;
+    if (logging) {
+        for (int i = tid(); i < nContacts; i += nthreads()) {
+            const VelConstraint v = vc[i];
+            const float4 im = imp[i];
+            const int base = sStatus[i];
+            for (int j = 0; j < v.idx.z && base + j < P.logCap; ++j) {
+                const float4 c = j == 0 ? v.c0 : v.c1;
+                const float kn = c.x > 0.0f ? 1.0f / c.x : 0.0f, kt = c.y > 0.0f ? 1.0f / c.y : 0.0f;
+                P.logT[2 * (size_t)(base + j)] = (j == 0 ? im.x : im.z) * kn;
+                P.logT[2 * (size_t)(base + j) + 1] = (j == 0 ? im.y : im.w) * kt;
+            }
+        }
+    }
     __syncthreads();
     if (tid() == 0) { unsigned long long now = clock64(); st->cyc[9] = now - tStamp; tStamp = now; }
     // impulses back to the manifolds, positions integrated, both in parallel

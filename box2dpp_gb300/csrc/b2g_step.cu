@@ -48,6 +48,9 @@ struct Wd {
     VelConstraint* vc;
     PosConstraint* pc;
     float4* vimp;
+    float4* vimpL;
+    float2* vsep;
+    float4* sVelL;
     TOITask* toi;
     int4* islands;
     int2* islandJ;
@@ -76,10 +79,11 @@ struct Wd {
         order = B.order + c; cnext = B.cnext + c;
         jt = B.joint + j; sJoint = B.sJoint + j;
         sBody = B.sBody + d.rowBase; sPos = B.sPos + d.rowBase; sVel = B.sVel + d.rowBase;
-        rowMask = B.rowMask + d.rowBase;
+        rowMask = B.rowMask + d.rowBase; sVelL = B.sVelL + d.rowBase;
         sStack = B.sStack + b; sWake = B.sWake + b;
         islands = B.islands + b; islandJ = B.islandJ + b; sleepOut = B.sleepOut + b;
         sContact = B.sContact + c; sStatus = B.sStatus + c; vc = B.vc + c; pc = B.pc + c; vimp = B.vimp + c; toi = B.toi + c;
+        vimpL = B.vimpL + c; vsep = B.vsep + c;
         cColour = B.cColour + c; colourList = B.colourList + c;
         pairs = B.pairs + q; pairKeep = B.pairKeep + q; pairInfo = B.pairInfo + q;
         smemBase = nullptr;
@@ -297,6 +301,8 @@ struct Wd {
     __device__ void solveIslands(const StepParams& P, int nIsl, int nRows, int nContacts, float4* smem, int smemRows,
                                  int smemContacts, const int* colourStart);
     __device__ void solveTOI(const StepParams& P);
+    __device__ void warmStartAll(int nIsl, const int* colourStart, const float4* im, float4* v);
+    __device__ void learnedImpulses(const StepParams& P, int nContacts, const float4* imp, const float4* vel);
     __device__ void destroyContact(int c);
 };
 
@@ -1036,6 +1042,14 @@ __device__ void Wd::solveTOI(const StepParams& P)
     __shared__ int sAdvance;
     __shared__ float sBestA[kMaxCta];
     __shared__ int sBestK[kMaxCta];
+    unsigned long long tMark = clock64();
+    auto stamp = [&](int slot) {
+        if (tid() == 0) {
+            const unsigned long long now = clock64();
+            st->cyc[slot] += now - tMark;
+            tMark = now;
+        }
+    };
     for (int event = 0;; ++event) {
         const int n = st->contactCount;
         if (tid() == 0) sAdvance = 0;
@@ -1116,6 +1130,7 @@ __device__ void Wd::solveTOI(const StepParams& P)
             ci[T.contact].x = info.x | kCToi;
         }
         __syncthreads();
+        stamp(16);
         // Earliest TOI, first in list order among equals (the reference keeps the first alpha <
         // minAlpha): per-thread minimum over its strided positions, then a reduction on (alpha, k).
         {
@@ -1153,6 +1168,7 @@ __device__ void Wd::solveTOI(const StepParams& P)
             }
         }
         __syncthreads();
+        stamp(17);
         if (sDone) break;
         if (tid() == 0) {
             st->toiEvents = event + 1;
@@ -1220,6 +1236,7 @@ __device__ void Wd::solveTOI(const StepParams& P)
                         sBody[nBodies++] = other;
                     }
                 }
+                stamp(18);
                 // b2Island::SolveTOI (Dynamics/b2Island.cpp:386-485)
                 float subDt = (1.0f - minAlpha) * P.dt;
                 for (int i = 0; i < nBodies; ++i) {
@@ -1263,6 +1280,7 @@ __device__ void Wd::solveTOI(const StepParams& P)
                     vel[b] = make_float4(v4.x, v4.y, v4.z, 0.0f);
                     syncTransform(b);
                 }
+                stamp(19);
                 for (int i = 0; i < nBodies; ++i) {
                     int b = sBody[i];
                     bi[b].y &= ~kBIsland;
@@ -1274,8 +1292,10 @@ __device__ void Wd::solveTOI(const StepParams& P)
             sDone = skip ? 2 : 0;
         }
         __syncthreads();
+        stamp(20);
         if (sDone == 2) continue;
         findNewContacts();
+        stamp(21);
         if (st->subStepping) {
             if (tid() == 0) st->stepComplete = 0;
             __syncthreads();
@@ -1310,8 +1330,9 @@ __global__ void __launch_bounds__(128) StepKernel(Batch B, StepParams P, const i
         W.st->colours = 0;
         W.st->velIters = 0;
         W.st->residual = 0.0f;
+        W.st->warmLearned = 0;
         W.st->newFixture = 0;
-        for (int i = 0; i < 16; ++i) W.st->cyc[i] = 0;
+        for (int i = 0; i < kProfileSlots; ++i) W.st->cyc[i] = 0;
     }
     __syncthreads();
     if (newFixture) W.findNewContacts();

@@ -10,6 +10,7 @@
 #include <vector_types.h>
 
 #include "b2g_core.h"
+#include "b2g_mlp.cuh"
 
 namespace b2g {
 
@@ -36,6 +37,8 @@ struct WorldDesc {
     int rowBase, rowCap;
 };
 
+constexpr int kProfileSlots = 24;
+
 // Per-world mutable scalars.
 struct WorldState {
     float gx, gy;
@@ -56,13 +59,16 @@ struct WorldState {
     int colours;        // constraint colours used by the coloured solver in the last step
     int velIters;       // velocity iterations run in the last step (fewer than asked when a tolerance is met)
     float residual;     // velocity residual (m/s) after the last step's velocity iterations, when measured
-    int pad;
+    int warmLearned;    // 1 when the last step used the learned warm start (its residual was smaller)
     // SM clock cycles of the last step per phase: 0 new-fixture pairs, 1 collide, 2 island DFS,
     // 3 island solve, 4 fixture sync, 5 pairs after solve, 6 TOI, 7 whole step; then the island solve
     // split: 8 integrate + constraint init, 9 warm start + velocity sweeps, 10 impulses + position
     // integration, 11 position sweeps, 12 write-back, 13 sleep; 14 pair finding and sorting, 15 contact
-    // creation (both summed over every UpdatePairs call of the step)
-    unsigned long long cyc[16];
+    // creation (both summed over every UpdatePairs call of the step); the TOI split (summed over its
+    // events): 16 contact classification and time of impact, 17 earliest-event selection, 18 event
+    // mini-island build, 19 mini-island solve, 20 fixture sync and contact invalidation, 21 pair
+    // finding after events; 22, 23 unused
+    unsigned long long cyc[kProfileSlots];
 };
 
 // Revolute joint (Dynamics/Joints/b2RevoluteJoint.h), stored whole: joints are few.
@@ -157,6 +163,9 @@ struct Batch {
     VelConstraint* vc;
     PosConstraint* pc;
     float4* vimp;    // contact-sized impulses of the island contacts (when not staged in shared memory)
+    float4* vimpL;   // contact-sized learned warm-start impulses
+    float2* vsep;    // contact-sized separations of the points at the start of the velocity solve
+    float4* sVelL;   // row-sized velocities under the learned warm start
     TOITask* toi;
     int4* islands;   // body-sized: {bodyStart, bodyCount, contactStart, contactCount}
     int2* islandJ;   // {jointStart, jointCount}
@@ -175,6 +184,7 @@ struct Batch {
 // (bit-exact with the reference). kSolverColoured solves the same constraints colour by colour: the
 // constraints of one colour share no dynamic body and are solved in parallel across the CTA.
 enum : int { kSolverPlain = 0, kSolverColoured = 1 };
+enum : int { kWarmReference = 0, kWarmLearned = 1 };
 // Colours 0..62 are solved in parallel; colour 63 collects the constraints for which no colour was
 // free and is solved by one thread in island order.
 constexpr int kColours = 64;
@@ -192,7 +202,14 @@ struct StepParams {
     int solver;         // kSolverPlain or kSolverColoured
     float tolerance;    // > 0: stop the velocity iterations once the velocity residual is <= tolerance
     int measureResidual;// 1: record the velocity residual after the velocity iterations
-    int pad;
+    int warmMode;       // kWarmReference, or kWarmLearned (the network below, reference as fallback)
+    MlpView mlp;
+    // contact-point log (plain solver): features at the start of the velocity solve, then the
+    // scaled impulses the velocity iterations end with; logX == nullptr disables it
+    float* logX;        // [logCap][14]
+    float* logT;        // [logCap][2]
+    int* logCount;
+    int logCap;
 };
 
 } // namespace b2g

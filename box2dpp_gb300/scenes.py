@@ -265,6 +265,14 @@ def config2(n_bodies: int = 10000, seed: int = 1, allow_sleep: bool = True) -> S
     return drop(n_bodies, SplitMix64(seed), half_size=100.0, allow_sleep=allow_sleep)
 
 
+def config4(n_worlds: int, first_seed: int, n_bodies: int = 256, allow_sleep: bool = False) -> list:
+    """Worlds of the config-2 mix (circles / convex polygons dropped into an edge container), one per
+    seed first_seed, first_seed + 1, ...: the scenes the learned warm start is trained and judged on.
+    n_bodies per world (the full-size mix has 10,000 in a 200 m box; the container here scales with
+    the body count as in drop())."""
+    return [drop(n_bodies, SplitMix64(first_seed + k), allow_sleep=allow_sleep) for k in range(n_worlds)]
+
+
 def config3(n_worlds: int = 4096, seed: int = 1, allow_sleep: bool = True, min_bodies: int = 16,
             max_bodies: int = 512) -> list:
     """Independent worlds with log-uniform body counts in [min, max] and a seeded kind among

@@ -1,0 +1,130 @@
+"""Train the learned warm start and measure what it saves.
+
+  python -m box2dpp_gb300.train_warmstart [--seeds 1000] [--steps 20000] [--batch 65536] [--out PATH]
+
+1. Data: worlds of the config-2 mix (circles and convex polygons dropped into an edge container,
+   ``scenes.config4``), one per seed over ``--seeds`` held-out seeds, stepped with the plain
+   (reference-order) solver. After ``--settle`` steps at 8/3 iterations the contact-point log records,
+   for ``--log-steps`` steps at ``--log-vi`` velocity iterations, each island contact point's 14
+   features at the start of the velocity solve and the impulses the iterations end with (the
+   targets, in velocity units).
+2. Training: the library's tensor-core kernels, Adam for ``--steps`` steps on batches of ``--batch``
+   points drawn from the log.
+3. Evaluation on other seeds: the plain solver with a velocity-residual tolerance (``--tol``, at most
+   ``--max-vi`` iterations) counts the iterations each world needs with the reference warm start and
+   with the learned one (which falls back to the reference warm start whenever its residual is
+   worse).
+
+The trained parameters and normaliser are written to ``--out`` (``box2dpp_gb300/data/warmstart_mlp.npz``
+by default) together with the evaluation numbers.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DEFAULT_OUT = os.path.join(HERE, "data", "warmstart_mlp.npz")
+DT, PI = 1.0 / 60.0, 3
+
+
+def log_points(first_seed: int, n_seeds: int, bodies: int, settle: int, log_steps: int, log_vi: int,
+               chunk: int = 250):
+    from . import scenes
+    from .world import World
+
+    xs, ts = [], []
+    for s0 in range(first_seed, first_seed + n_seeds, chunk):
+        n = min(chunk, first_seed + n_seeds - s0)
+        w = World(scenes.config4(n, s0, bodies))
+        w.set_solver("plain")
+        for _ in range(settle):
+            w.step(DT, 8, PI)
+        w.set_contact_log(4_000_000)
+        for _ in range(log_steps):
+            w.step(DT, log_vi, PI)
+            x, t = w.read_contact_log()
+            xs.append(x)
+            ts.append(t)
+        w.close()
+    return np.concatenate(xs), np.concatenate(ts)
+
+
+def iterations_to_tolerance(mlp, first_seed: int, n_seeds: int, bodies: int, settle: int, steps: int, tol: float,
+                            max_vi: int):
+    """Mean over worlds and steps of the velocity iterations the plain solver runs to reach tol, and
+    the share of world-steps that kept the learned prediction (None without a network)."""
+    from . import scenes
+    from .world import World
+
+    w = World(scenes.config4(n_seeds, first_seed, bodies))
+    w.set_solver("plain", tolerance=tol, measure_residual=True)
+    for _ in range(settle):
+        w.step(DT, 8, PI)
+    w.set_warm_start(mlp)
+    its, used, res = [], [], []
+    for _ in range(steps):
+        w.step(DT, max_vi, PI)
+        _, it, r = w.solver_stats()
+        its.append(it.copy())
+        res.append(r.copy())
+        if mlp is not None:
+            used.append(w.warm_stats().copy())
+    w.close()
+    its, res = np.array(its), np.array(res)
+    return float(its.mean()), (float(np.array(used).mean()) if used else None), float(np.median(res))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--seeds", type=int, default=1000)
+    ap.add_argument("--first-seed", type=int, default=1_000_000)
+    ap.add_argument("--bodies", type=int, default=256)
+    ap.add_argument("--settle", type=int, default=60)
+    ap.add_argument("--log-steps", type=int, default=8)
+    ap.add_argument("--log-vi", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=20000)
+    ap.add_argument("--batch", type=int, default=65536)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--eval-seeds", type=int, default=64)
+    ap.add_argument("--eval-first-seed", type=int, default=2_000_000)
+    ap.add_argument("--tol", type=float, default=1e-4)
+    ap.add_argument("--max-vi", type=int, default=50)
+    ap.add_argument("--out", default=DEFAULT_OUT)
+    args = ap.parse_args()
+
+    from .learn import Mlp
+
+    t0 = time.time()
+    x, t = log_points(args.first_seed, args.seeds, args.bodies, args.settle, args.log_steps, args.log_vi)
+    t_log = time.time() - t0
+    m = Mlp(1)
+    m.fit_normaliser(x)
+    t0 = time.time()
+    losses = m.train(x, t, steps=args.steps, batch=args.batch, lr=args.lr, seed=1)
+    t_train = time.time() - t0
+    ref_its, _, ref_res = iterations_to_tolerance(None, args.eval_first_seed, args.eval_seeds, args.bodies,
+                                                  args.settle, 30, args.tol, args.max_vi)
+    lrn_its, used, lrn_res = iterations_to_tolerance(m, args.eval_first_seed, args.eval_seeds, args.bodies,
+                                                     args.settle, 30, args.tol, args.max_vi)
+    report = {
+        "points": int(len(x)), "log_seconds": round(t_log, 1), "train_steps": args.steps, "batch": args.batch,
+        "train_seconds": round(t_train, 1), "loss_first": float(losses[:10].mean()),
+        "loss_last": float(losses[-100:].mean()), "tolerance": args.tol, "max_vi": args.max_vi,
+        "iterations_reference": ref_its, "iterations_learned": lrn_its, "ratio": lrn_its / ref_its,
+        "learned_kept_share": used, "residual_median_reference": ref_res, "residual_median_learned": lrn_res,
+        "train_seeds": [args.first_seed, args.first_seed + args.seeds - 1],
+        "eval_seeds": [args.eval_first_seed, args.eval_first_seed + args.eval_seeds - 1],
+    }
+    os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
+    p, mu, sigma = m.params()
+    np.savez(args.out, params=p, mu=mu, sigma=sigma, report=json.dumps(report))
+    print(json.dumps(report), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -99,6 +99,33 @@ class World:
         arr = np.ascontiguousarray(np.asarray(classes, dtype=np.int32).reshape(-1, 5))
         _lib.check(self.lib.gb_world_set_launch_plan(self.h, arr.reshape(-1), len(arr)), "gb_world_set_launch_plan")
 
+    def set_warm_start(self, mlp=None) -> None:
+        """Learned warm start with the given network (reference warm start as fallback); None: the
+        reference warm start only. The network must outlive its use by this world."""
+        if mlp is None:
+            _lib.check(self.lib.gb_world_set_warm_start(self.h, None, _lib.WARM_REFERENCE), "gb_world_set_warm_start")
+        else:
+            _lib.check(self.lib.gb_world_set_warm_start(self.h, mlp.h, _lib.WARM_LEARNED), "gb_world_set_warm_start")
+        self._mlp = mlp
+
+    def warm_stats(self) -> np.ndarray:
+        used = np.zeros(self.n_worlds, dtype=np.int32)
+        _lib.check(self.lib.gb_world_warm_stats(self.h, used), "gb_world_warm_stats")
+        return used
+
+    def set_contact_log(self, capacity: int) -> None:
+        _lib.check(self.lib.gb_world_set_contact_log(self.h, int(capacity)), "gb_world_set_contact_log")
+        self._log_cap = int(capacity)
+
+    def read_contact_log(self):
+        """(features [n][14], targets [n][2]) logged since the last read; empties the log."""
+        cap = getattr(self, "_log_cap", 0)
+        x = np.zeros((max(cap, 1), 14), dtype=np.float32)
+        t = np.zeros((max(cap, 1), 2), dtype=np.float32)
+        n = C.c_int()
+        _lib.check(self.lib.gb_world_read_contact_log(self.h, x, t, cap, C.byref(n)), "gb_world_read_contact_log")
+        return x[:n.value], t[:n.value]
+
     def set_stream(self, stream_handle: int) -> None:
         _lib.check(self.lib.gb_world_set_stream(self.h, C.c_void_p(stream_handle)), "gb_world_set_stream")
 
@@ -144,13 +171,14 @@ class World:
 
     PHASES = ["new_pairs", "collide", "island_build", "island_solve", "fixture_sync", "pairs", "toi", "step",
               "solve_init", "solve_velocity", "solve_store_integrate", "solve_position", "solve_writeback",
-              "solve_sleep", "pairs_find_sort", "pairs_create"]
+              "solve_sleep", "pairs_find_sort", "pairs_create", "toi_classify", "toi_select", "toi_island",
+              "toi_solve", "toi_sync", "toi_pairs", "unused22", "unused23"]
 
     def profile(self) -> np.ndarray:
-        """SM clock cycles per world and phase of the last step, shape (worlds, 16) (see PHASES)."""
-        out = np.zeros(16 * self.n_worlds, dtype=np.uint64)
+        """SM clock cycles per world and phase of the last step, shape (worlds, 24) (see PHASES)."""
+        out = np.zeros(len(self.PHASES) * self.n_worlds, dtype=np.uint64)
         _lib.check(self.lib.gb_world_profile(self.h, out), "gb_world_profile")
-        return out.reshape(self.n_worlds, 16)
+        return out.reshape(self.n_worlds, len(self.PHASES))
 
     @property
     def total_bodies(self) -> int:

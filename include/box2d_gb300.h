@@ -30,6 +30,7 @@ typedef int gb_status;
 #define GB_ERR_CUDA 4     /* a CUDA runtime call failed (no device, launch error, ...) */
 
 typedef struct gb_world gb_world;
+typedef struct gb_mlp gb_mlp;
 
 /* b2World settings (b2World::b2World(gravity), SetAllowSleeping, SetWarmStarting,
  * SetContinuousPhysics, SetSubStepping: Box2D/Dynamics/b2World.h:48,145-217). */
@@ -158,11 +159,15 @@ gb_status gb_world_stats(gb_world* world, int w, int* islands, int* toi_events);
 gb_status gb_world_totals(gb_world* world, long long* out);
 
 /* Per-world SM clock cycles spent in the phases of the last step (the device counterpart of
- * b2World::GetProfile, Box2D/Dynamics/b2World.h:196, b2Profile in b2TimeStep.h:27-37): out[16 * w + i]
- * for i = 0 new-fixture pairs, 1 collide, 2 island build, 3 island solve, 4 fixture sync, 5 pairs,
- * 6 continuous (TOI), 7 whole step, and the island solve split 8 integrate + constraint init,
- * 9 warm start + velocity sweeps, 10 impulses + position integration, 11 position sweeps,
- * 12 write-back, 13 sleep, 14 broadphase pair finding and sorting, 15 contact creation. */
+ * b2World::GetProfile, Box2D/Dynamics/b2World.h:196, b2Profile in b2TimeStep.h:27-37):
+ * out[GB_PROFILE_SLOTS * w + i] for i = 0 new-fixture pairs, 1 collide, 2 island build, 3 island
+ * solve, 4 fixture sync, 5 pairs, 6 continuous (TOI), 7 whole step; the island solve split 8
+ * integrate + constraint init, 9 warm start + velocity sweeps, 10 impulses + position integration,
+ * 11 position sweeps, 12 write-back, 13 sleep; 14 broadphase pair finding and sorting, 15 contact
+ * creation; the continuous split 16 classification + time of impact, 17 earliest-event selection,
+ * 18 event mini-island build, 19 mini-island solve, 20 fixture sync + contact invalidation,
+ * 21 pair finding after events (22, 23 unused). */
+#define GB_PROFILE_SLOTS 24
 gb_status gb_world_profile(gb_world* world, unsigned long long* out);
 
 /* Whole-batch b2Body::ApplyForceToCenter + ApplyTorque for the next step (Box2D/Dynamics/b2Body.h:
@@ -198,6 +203,55 @@ gb_status gb_collide(int n, const int* type_a, const float* shape_a, const int* 
 gb_status gb_collide_noalloc(int n, const int* type_a, const float* shape_a, const int* n_a, const float* xf_a,
                              const int* type_b, const float* shape_b, const int* n_b, const float* xf_b,
                              int* out_ints, float* out_floats);
+
+/* ---------------------------------------------------------------- learned warm start
+ * No counterpart in the reference. A BF16 MLP 14 -> 64 -> 64 -> 2 (ReLU, FP32 accumulation, tensor
+ * cores) that predicts the accumulated normal and tangent impulse of a contact point from 14
+ * features of the point at the start of the velocity solve; see gb_world_set_warm_start for the
+ * features and how the prediction is used. Parameters are f32 masters, gb_mlp_param_count() of
+ * them: W1 [64][16] (inputs 14, 15 zero), b1 [64], W2 [64][64], b2 [64], W3 [8][64] (rows 2..7
+ * zero), b3 [8] (2..7 zero), row major [out][in]; features are normalised as (x - mu) / sigma.
+ * gb_mlp_forward: y[n][2] for raw features x[n][14] (host arrays). gb_mlp_gradients: loss (mean
+ * over rows of the squared error summed over both outputs) and its gradient (param layout) for
+ * targets t[n][2], n a multiple of 16, without changing the network. gb_mlp_train: steps of Adam
+ * (lr, beta 0.9/0.999) on batches of `batch` rows (a multiple of 16) drawn with a seeded hash from
+ * the n rows; losses[steps] (optional) receives each batch's loss. */
+gb_status gb_mlp_create(unsigned long long seed, gb_mlp** out);
+gb_status gb_mlp_destroy(gb_mlp* mlp);
+int gb_mlp_param_count(void);
+gb_status gb_mlp_set_params(gb_mlp* mlp, const float* params, const float* mu, const float* sigma);
+gb_status gb_mlp_get_params(gb_mlp* mlp, float* params, float* mu, float* sigma);
+gb_status gb_mlp_forward(gb_mlp* mlp, const float* x, int n, float* y);
+gb_status gb_mlp_gradients(gb_mlp* mlp, const float* x, const float* t, int n, float* grad, float* loss);
+gb_status gb_mlp_train(gb_mlp* mlp, const float* x, const float* t, int n, int steps, int batch, float lr,
+                       unsigned long long seed, float* losses);
+
+/* Warm start of the following steps (no counterpart in the reference). GB_WARM_REFERENCE (default)
+ * is b2ContactSolver's: each point starts from its previous impulses scaled by dtRatio
+ * (Box2D/Dynamics/Contacts/b2ContactSolver.cpp:100-110, 254-292). GB_WARM_LEARNED evaluates the
+ * network for every island contact point after the constraints are initialised, from 14 features:
+ * world normal (2); relative normal and tangent velocity at the point; its separation; inverse mass
+ * and inertia of both bodies (4); the reference warm-start normal and tangent impulses divided by
+ * the point's normal and tangent effective mass; the effective inverse normal mass; the friction
+ * coefficient; 1 for a two-point manifold. The outputs, multiplied by the normal and tangent
+ * effective mass, are the predicted impulses (normal clamped at 0, tangent to the friction cone).
+ * Each world then warm-starts its velocities both ways and keeps the one whose velocity residual is
+ * smaller, so a world falls back to the reference warm start whenever the prediction is worse. The
+ * network must outlive its use by the world. */
+#define GB_WARM_REFERENCE 0
+#define GB_WARM_LEARNED 1
+gb_status gb_world_set_warm_start(gb_world* world, gb_mlp* mlp, int mode);
+/* Per world: 1 when the last step used the learned warm start. */
+gb_status gb_world_warm_stats(gb_world* world, int* learned_used);
+
+/* Contact-point log for training the network (plain solver only): capacity > 0 allocates a device
+ * log of that many points and starts recording, 0 stops and frees it. Every step appends, for each
+ * island contact point of every world, its 14 features at the start of the velocity solve (x) and
+ * the normal and tangent impulses the velocity iterations end with divided by the effective masses
+ * (t, the network's targets). gb_world_read_contact_log copies up to cap points to the host, sets *n,
+ * empties the log and returns GB_ERR_CAPACITY when points were dropped for lack of room. */
+gb_status gb_world_set_contact_log(gb_world* world, int capacity);
+gb_status gb_world_read_contact_log(gb_world* world, float* x, float* t, int cap, int* n);
 
 /* Library version string. */
 const char* gb_version(void);

@@ -1,0 +1,493 @@
+// C++ mirror of the reference's host API (Box2D 2.3.2 b2World, b2Body, b2Fixture, b2Contact, shapes,
+// b2RevoluteJointDef, b2ContactListener: Box2D/Dynamics/b2World.h:43-288, b2Body.h, b2Fixture.h,
+// Contacts/b2Contact.h, b2WorldCallbacks.h) over the C-ABI of libbox2d_gb300.so, header only.
+//
+// The signatures and semantics a b2World user relies on are kept: a world owns its bodies, fixtures
+// and joints (stable pointers until the world is destroyed), definitions are copied, Step(dt,
+// velocityIterations, positionIterations) advances the world, and body state is read through the
+// b2Body getters. Differences, all of them consequences of the state living on the GPU:
+//  - a Step is queued on the device; the first getter after it waits for it and reads every body
+//    once (the getters of that step are then host reads);
+//  - the world settings (SetAllowSleeping, SetWarmStarting, SetContinuousPhysics, SetSubStepping)
+//    take effect when the device world is created, at the first Step;
+//  - bodies, fixtures and joints are created but never destroyed (the reference's Destroy* calls
+//    are not part of this API);
+//  - b2ContactListener receives BeginContact/EndContact after each Step, derived from which fixture
+//    pairs touch before and after the step: all EndContact calls first, in the previous contact list
+//    order, then all BeginContact calls in the new list order (the reference interleaves them inside
+//    Step); PreSolve and PostSolve are not called.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <utility>
+#include <vector>
+
+#include "box2d_gb300.h"
+
+namespace box2d {
+
+struct b2Vec2 {
+    float x = 0.0f, y = 0.0f;
+    b2Vec2() = default;
+    b2Vec2(float x_, float y_) : x(x_), y(y_) {}
+    void Set(float x_, float y_) { x = x_; y = y_; }
+    void SetZero() { x = 0.0f; y = 0.0f; }
+};
+struct b2Rot {
+    float s = 0.0f, c = 1.0f;
+    float GetAngle() const { return std::atan2(s, c); }
+};
+struct b2Transform {
+    b2Vec2 p;
+    b2Rot q;
+};
+
+enum b2BodyType { b2_staticBody = 0, b2_kinematicBody = 1, b2_dynamicBody = 2 };
+
+struct b2BodyDef {
+    b2BodyType type = b2_staticBody;
+    b2Vec2 position;
+    float angle = 0.0f;
+    b2Vec2 linearVelocity;
+    float angularVelocity = 0.0f;
+    float linearDamping = 0.0f;
+    float angularDamping = 0.0f;
+    bool allowSleep = true;
+    bool awake = true;
+    bool fixedRotation = false;
+    bool bullet = false;
+    bool active = true;
+    float gravityScale = 1.0f;
+    void* userData = nullptr;
+};
+
+// ---------------------------------------------------------------- shapes (Collision/Shapes/*.h)
+class b2Shape {
+public:
+    enum Type { e_circle = 0, e_edge = 1, e_polygon = 2 };
+    virtual ~b2Shape() = default;
+    Type GetType() const { return m_type; }
+    // C-ABI encoding (gb_create_fixtures): type code, 16 floats, count
+    virtual void Encode(int* type, float* shape, int* n) const = 0;
+    Type m_type = e_circle;
+    float m_radius = 0.0f;
+};
+
+class b2CircleShape : public b2Shape {
+public:
+    b2CircleShape() { m_type = e_circle; }
+    void Encode(int* type, float* shape, int* n) const override
+    {
+        *type = 0; *n = 1;
+        shape[0] = m_p.x; shape[1] = m_p.y; shape[2] = m_radius;
+    }
+    b2Vec2 m_p;
+};
+
+class b2EdgeShape : public b2Shape {
+public:
+    b2EdgeShape() { m_type = e_edge; }
+    void Set(const b2Vec2& v1, const b2Vec2& v2) { m_vertex1 = v1; m_vertex2 = v2; m_hasVertex0 = m_hasVertex3 = false; }
+    void Encode(int* type, float* shape, int* n) const override
+    {
+        *type = 1; *n = 2;
+        const float v[10] = {m_vertex1.x, m_vertex1.y, m_vertex2.x, m_vertex2.y, m_vertex0.x, m_vertex0.y,
+                             m_vertex3.x, m_vertex3.y, m_hasVertex0 ? 1.0f : 0.0f, m_hasVertex3 ? 1.0f : 0.0f};
+        for (int i = 0; i < 10; ++i) shape[i] = v[i];
+    }
+    b2Vec2 m_vertex1, m_vertex2, m_vertex0, m_vertex3;
+    bool m_hasVertex0 = false, m_hasVertex3 = false;
+};
+
+class b2PolygonShape : public b2Shape {
+public:
+    b2PolygonShape() { m_type = e_polygon; }
+    // b2PolygonShape::Set: the hull is computed by the library exactly as the reference does
+    void Set(const b2Vec2* points, int count)
+    {
+        m_mode = kPoints;
+        m_count = count < 8 ? count : 8;
+        for (int i = 0; i < m_count; ++i) m_points[i] = points[i];
+    }
+    void SetAsBox(float hx, float hy)
+    {
+        m_mode = kBox; m_hx = hx; m_hy = hy; m_oriented = false;
+    }
+    void SetAsBox(float hx, float hy, const b2Vec2& center, float angle)
+    {
+        m_mode = kBox; m_hx = hx; m_hy = hy; m_center = center; m_angle = angle; m_oriented = true;
+    }
+    void Encode(int* type, float* shape, int* n) const override
+    {
+        if (m_mode == kBox) {
+            *type = 3;
+            shape[0] = m_hx; shape[1] = m_hy;
+            if (m_oriented) { shape[2] = m_center.x; shape[3] = m_center.y; shape[4] = m_angle; *n = 5; }
+            else *n = 2;
+        } else {
+            *type = 2; *n = m_count;
+            for (int i = 0; i < m_count; ++i) { shape[2 * i] = m_points[i].x; shape[2 * i + 1] = m_points[i].y; }
+        }
+    }
+
+private:
+    enum Mode { kPoints, kBox } m_mode = kBox;
+    b2Vec2 m_points[8];
+    int m_count = 0;
+    float m_hx = 0.0f, m_hy = 0.0f, m_angle = 0.0f;
+    b2Vec2 m_center;
+    bool m_oriented = false;
+};
+
+struct b2Filter {
+    uint16_t categoryBits = 0x0001;
+    uint16_t maskBits = 0xFFFF;
+    int16_t groupIndex = 0;
+};
+
+struct b2FixtureDef {
+    const b2Shape* shape = nullptr;
+    void* userData = nullptr;
+    float friction = 0.2f;
+    float restitution = 0.0f;
+    float density = 0.0f;
+    bool isSensor = false;
+    b2Filter filter;
+};
+
+class b2World;
+class b2Body;
+
+class b2Fixture {
+public:
+    b2Body* GetBody() const { return m_body; }
+    int GetIndex() const { return m_index; }
+    float GetFriction() const { return m_def.friction; }
+    float GetRestitution() const { return m_def.restitution; }
+    float GetDensity() const { return m_def.density; }
+    bool IsSensor() const { return m_def.isSensor; }
+    void* GetUserData() const { return m_def.userData; }
+    b2Shape::Type GetType() const { return m_type; }
+
+private:
+    friend class b2World;
+    b2Body* m_body = nullptr;
+    int m_index = -1;
+    b2FixtureDef m_def;
+    b2Shape::Type m_type = b2Shape::e_circle;
+};
+
+class b2Body {
+public:
+    b2Fixture* CreateFixture(const b2FixtureDef* def);
+    b2Fixture* CreateFixture(const b2Shape* shape, float density)
+    {
+        b2FixtureDef d;
+        d.shape = shape;
+        d.density = density;
+        return CreateFixture(&d);
+    }
+    b2BodyType GetType() const { return m_type; }
+    int GetIndex() const { return m_index; }
+    b2World* GetWorld() const { return m_world; }
+    void* GetUserData() const { return m_userData; }
+    const b2Vec2 GetPosition() const { const float* s = State(); return b2Vec2(s[0], s[1]); }
+    float GetAngle() const { return State()[2]; }
+    const b2Vec2 GetWorldCenter() const { const float* s = State(); return b2Vec2(s[3], s[4]); }
+    const b2Vec2 GetLinearVelocity() const { const float* s = State(); return b2Vec2(s[5], s[6]); }
+    float GetAngularVelocity() const { return State()[7]; }
+    const b2Transform GetTransform() const
+    {
+        const float* s = State();
+        b2Transform t;
+        t.p = b2Vec2(s[0], s[1]);
+        t.q.s = s[8];
+        t.q.c = s[9];
+        return t;
+    }
+    bool IsAwake() const { return State()[11] != 0.0f; }
+    // b2Body::ApplyForceToCenter / ApplyTorque: accumulated for the next Step (the reference
+    // applies them only to awake bodies and wakes the body when wake is true; here the force is
+    // recorded and the device step applies it like the reference's integration does)
+    void ApplyForceToCenter(const b2Vec2& force, bool wake);
+    void ApplyTorque(float torque, bool wake);
+
+private:
+    friend class b2World;
+    const float* State() const;
+    b2World* m_world = nullptr;
+    int m_index = -1;
+    b2BodyType m_type = b2_staticBody;
+    void* m_userData = nullptr;
+};
+
+struct b2RevoluteJointDef {
+    b2Body* bodyA = nullptr;
+    b2Body* bodyB = nullptr;
+    bool collideConnected = false;
+    b2Vec2 localAnchorA, localAnchorB;
+    float referenceAngle = 0.0f;
+    bool enableLimit = false;
+    float lowerAngle = 0.0f, upperAngle = 0.0f;
+    bool enableMotor = false;
+    float motorSpeed = 0.0f, maxMotorTorque = 0.0f;
+};
+
+class b2Joint {
+public:
+    int GetIndex() const { return m_index; }
+    b2Body* GetBodyA() const { return m_a; }
+    b2Body* GetBodyB() const { return m_b; }
+
+private:
+    friend class b2World;
+    int m_index = -1;
+    b2Body *m_a = nullptr, *m_b = nullptr;
+};
+
+struct b2ManifoldPoint {
+    b2Vec2 localPoint;
+    float normalImpulse = 0.0f, tangentImpulse = 0.0f;
+    uint32_t id = 0;
+};
+struct b2Manifold {
+    enum Type { e_circles = 0, e_faceA = 1, e_faceB = 2 };
+    b2ManifoldPoint points[2];
+    b2Vec2 localNormal, localPoint;
+    Type type = e_circles;
+    int pointCount = 0;
+};
+
+class b2Contact {
+public:
+    b2Fixture* GetFixtureA() const { return m_a; }
+    b2Fixture* GetFixtureB() const { return m_b; }
+    bool IsTouching() const { return (m_flags & 2) != 0; }
+    bool IsEnabled() const { return (m_flags & 4) != 0; }
+    const b2Manifold* GetManifold() const { return &m_manifold; }
+
+private:
+    friend class b2World;
+    b2Fixture *m_a = nullptr, *m_b = nullptr;
+    int m_flags = 0;
+    b2Manifold m_manifold;
+};
+
+class b2ContactListener {
+public:
+    virtual ~b2ContactListener() = default;
+    virtual void BeginContact(b2Contact*) {}
+    virtual void EndContact(b2Contact*) {}
+};
+
+class b2World {
+public:
+    explicit b2World(const b2Vec2& gravity) : m_gravity(gravity) {}
+    ~b2World()
+    {
+        if (m_h) gb_world_destroy(m_h);
+    }
+    b2World(const b2World&) = delete;
+    b2World& operator=(const b2World&) = delete;
+
+    void SetAllowSleeping(bool flag) { m_def.allow_sleep = flag; }
+    void SetWarmStarting(bool flag) { m_def.warm_starting = flag; }
+    void SetContinuousPhysics(bool flag) { m_def.continuous_physics = flag; }
+    void SetSubStepping(bool flag) { m_def.sub_stepping = flag; }
+    bool GetAllowSleeping() const { return m_def.allow_sleep != 0; }
+    b2Vec2 GetGravity() const { return m_gravity; }
+    void SetContactListener(b2ContactListener* listener) { m_listener = listener; }
+
+    b2Body* CreateBody(const b2BodyDef* def)
+    {
+        if (!Handle()) return nullptr;
+        const float f[9] = {def->position.x, def->position.y, def->angle, def->linearVelocity.x, def->linearVelocity.y,
+                            def->angularVelocity, def->linearDamping, def->angularDamping, def->gravityScale};
+        const int flags = (def->allowSleep ? 1 : 0) | (def->awake ? 2 : 0) | (def->fixedRotation ? 4 : 0) |
+                          (def->bullet ? 8 : 0) | (def->active ? 16 : 0);
+        const int type = def->type;
+        int id = -1;
+        if (gb_create_bodies(m_h, 0, 1, &type, f, &flags, &id) != GB_OK) return nullptr;
+        std::unique_ptr<b2Body> b(new b2Body());
+        b->m_world = this;
+        b->m_index = id;
+        b->m_type = def->type;
+        b->m_userData = def->userData;
+        m_bodies.push_back(std::move(b));
+        m_forces.resize(4 * m_bodies.size(), 0.0f);
+        m_stale = true;
+        return m_bodies.back().get();
+    }
+
+    b2Joint* CreateJoint(const b2RevoluteJointDef* def)
+    {
+        if (!Handle() || !def->bodyA || !def->bodyB) return nullptr;
+        const float f[9] = {def->localAnchorA.x, def->localAnchorA.y, def->localAnchorB.x, def->localAnchorB.y,
+                            def->referenceAngle, def->lowerAngle, def->upperAngle, def->motorSpeed,
+                            def->maxMotorTorque};
+        const int flags = (def->enableLimit ? 1 : 0) | (def->enableMotor ? 2 : 0) | (def->collideConnected ? 4 : 0);
+        const int a = def->bodyA->m_index, b = def->bodyB->m_index;
+        int id = -1;
+        if (gb_create_revolute_joints(m_h, 0, 1, &a, &b, f, &flags, &id) != GB_OK) return nullptr;
+        std::unique_ptr<b2Joint> j(new b2Joint());
+        j->m_index = id;
+        j->m_a = def->bodyA;
+        j->m_b = def->bodyB;
+        m_joints.push_back(std::move(j));
+        return m_joints.back().get();
+    }
+
+    void Step(float timeStep, int velocityIterations, int positionIterations)
+    {
+        if (!Handle()) return;
+        if (m_listener && m_contacts.empty()) ReadContacts();  // the touching state before the step
+        if (m_forcesDirty) {
+            gb_world_upload(m_h);
+            gb_set_forces(m_h, m_forces.data());
+        }
+        gb_world_step(m_h, timeStep, velocityIterations, positionIterations);
+        if (m_forcesDirty) {
+            gb_world_sync(m_h);  // the force upload reads the host array
+            std::fill(m_forces.begin(), m_forces.end(), 0.0f);
+            m_forcesDirty = false;
+        }
+        m_stale = true;
+        if (m_listener) Report();
+    }
+
+    int GetBodyCount() const { return (int)m_bodies.size(); }
+    int GetJointCount() const { return (int)m_joints.size(); }
+    int GetContactCount()
+    {
+        int b = 0, f = 0, c = 0, j = 0;
+        if (m_h) gb_world_counts(m_h, 0, &b, &f, &c, &j);
+        return c;
+    }
+    // b2World::GetContactList as a vector in list order (newest first)
+    const std::vector<b2Contact*>& GetContactList()
+    {
+        ReadContacts();
+        m_contactView.clear();
+        for (auto& c : m_contacts) m_contactView.push_back(c.get());
+        return m_contactView;
+    }
+
+    // raw access used by b2Body
+    const float* BodyState(int index)
+    {
+        if (m_stale) {
+            m_state.assign(12 * m_bodies.size(), 0.0f);
+            if (!m_bodies.empty()) gb_get_bodies(m_h, 0, m_state.data());
+            m_stale = false;
+        }
+        return m_state.data() + 12 * index;
+    }
+    b2Fixture* AddFixture(b2Body* body, const b2FixtureDef* def)
+    {
+        if (!Handle() || !def->shape) return nullptr;
+        int type = 0, n = 0;
+        float shape[16] = {0};
+        def->shape->Encode(&type, shape, &n);
+        const float mat[3] = {def->density, def->friction, def->restitution};
+        const int filt[4] = {def->filter.categoryBits, def->filter.maskBits, def->filter.groupIndex, def->isSensor ? 1 : 0};
+        const int b = body->GetIndex();
+        int id = -1;
+        if (gb_create_fixtures(m_h, 0, 1, &b, &type, shape, &n, mat, filt, &id) != GB_OK) return nullptr;
+        std::unique_ptr<b2Fixture> fx(new b2Fixture());
+        fx->m_body = body;
+        fx->m_index = id;
+        fx->m_def = *def;
+        fx->m_def.shape = nullptr;
+        fx->m_type = def->shape->GetType();
+        m_fixtures.push_back(std::move(fx));
+        m_stale = true;
+        return m_fixtures.back().get();
+    }
+    void AddForce(int index, float fx, float fy, float torque)
+    {
+        m_forces[4 * index] += fx;
+        m_forces[4 * index + 1] += fy;
+        m_forces[4 * index + 2] += torque;
+        m_forcesDirty = true;
+    }
+
+private:
+    gb_world* Handle()
+    {
+        if (!m_h) {
+            m_def.gravity_x = m_gravity.x;
+            m_def.gravity_y = m_gravity.y;
+            if (gb_world_create(1, &m_def, &m_h) != GB_OK) m_h = nullptr;
+        }
+        return m_h;
+    }
+    void ReadContacts()
+    {
+        int n = 0;
+        std::vector<int> ints(8);
+        std::vector<float> flts(12);
+        if (gb_get_contacts(m_h, 0, ints.data(), flts.data(), 0, &n) != GB_OK && n == 0) n = 0;
+        ints.assign(8 * (size_t)(n > 0 ? n : 1), 0);
+        flts.assign(12 * (size_t)(n > 0 ? n : 1), 0.0f);
+        if (n > 0) gb_get_contacts(m_h, 0, ints.data(), flts.data(), n, &n);
+        m_contacts.clear();
+        for (int i = 0; i < n; ++i) {
+            std::unique_ptr<b2Contact> c(new b2Contact());
+            const int* I = &ints[8 * (size_t)i];
+            const float* F = &flts[12 * (size_t)i];
+            c->m_a = m_fixtures[I[0]].get();
+            c->m_b = m_fixtures[I[1]].get();
+            c->m_flags = I[2];
+            b2Manifold& m = c->m_manifold;
+            m.pointCount = I[3];
+            m.type = (b2Manifold::Type)I[4];
+            m.localNormal = b2Vec2(F[0], F[1]);
+            m.localPoint = b2Vec2(F[2], F[3]);
+            for (int p = 0; p < 2; ++p) {
+                m.points[p].localPoint = b2Vec2(F[4 + 4 * p], F[5 + 4 * p]);
+                m.points[p].normalImpulse = F[6 + 4 * p];
+                m.points[p].tangentImpulse = F[7 + 4 * p];
+                m.points[p].id = (uint32_t)I[5 + p];
+            }
+            m_contacts.push_back(std::move(c));
+        }
+    }
+    void Report()
+    {
+        std::map<std::pair<int, int>, int> before;
+        std::vector<std::unique_ptr<b2Contact>> old = std::move(m_contacts);
+        auto key = [](const b2Contact& c) { return std::make_pair(c.m_a->GetIndex(), c.m_b->GetIndex()); };
+        for (size_t i = 0; i < old.size(); ++i)
+            if (old[i]->IsTouching()) before[key(*old[i])] = (int)i;
+        ReadContacts();
+        std::map<std::pair<int, int>, bool> after;
+        for (auto& c : m_contacts)
+            if (c->IsTouching()) after[key(*c)] = true;
+        for (auto& c : old)
+            if (c->IsTouching() && !after.count(key(*c))) m_listener->EndContact(c.get());
+        for (auto& c : m_contacts)
+            if (c->IsTouching() && !before.count(key(*c))) m_listener->BeginContact(c.get());
+    }
+
+    b2Vec2 m_gravity;
+    gb_world_def m_def{0.0f, 0.0f, 1, 1, 1, 0};
+    gb_world* m_h = nullptr;
+    b2ContactListener* m_listener = nullptr;
+    std::vector<std::unique_ptr<b2Body>> m_bodies;
+    std::vector<std::unique_ptr<b2Fixture>> m_fixtures;
+    std::vector<std::unique_ptr<b2Joint>> m_joints;
+    std::vector<std::unique_ptr<b2Contact>> m_contacts;
+    std::vector<b2Contact*> m_contactView;
+    std::vector<float> m_state, m_forces;
+    bool m_stale = true, m_forcesDirty = false;
+};
+
+inline b2Fixture* b2Body::CreateFixture(const b2FixtureDef* def) { return m_world->AddFixture(this, def); }
+inline const float* b2Body::State() const { return m_world->BodyState(m_index); }
+inline void b2Body::ApplyForceToCenter(const b2Vec2& force, bool) { m_world->AddForce(m_index, force.x, force.y, 0.0f); }
+inline void b2Body::ApplyTorque(float torque, bool) { m_world->AddForce(m_index, 0.0f, 0.0f, torque); }
+
+} // namespace box2d

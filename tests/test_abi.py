@@ -16,7 +16,7 @@ HEADER = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "include
 
 def declared_symbols():
     text = open(HEADER).read()
-    return sorted(set(re.findall(r"^(?:gb_status|const char\*)\s+(gb_\w+)\(", text, re.M)))
+    return sorted(set(re.findall(r"^(?:gb_status|const char\*|int)\s+(gb_\w+)\(", text, re.M)))
 
 
 def test_header_matches_binding_list():

@@ -1,0 +1,57 @@
+"""The C++ mirror of b2World (include/box2d_gb300.hpp) builds against the library and, on the GPU,
+runs the Box2D manual's HelloWorld bit for bit like the CPU oracle."""
+from __future__ import annotations
+
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from box2dpp_gb300 import _lib, scenes
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+SRC = os.path.join(ROOT, "tests", "cpp", "hello_world.cpp")
+
+
+def _compile(tmp_path):
+    lib = _lib.library_path()
+    if not os.path.exists(lib):
+        from box2dpp_gb300 import build
+        build.build()
+    exe = str(tmp_path / "hello_world")
+    libdir = os.path.dirname(lib)
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "include"), SRC, "-o", exe,
+           "-L", libdir, "-lbox2d_gb300", f"-Wl,-rpath,{libdir}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return exe
+
+
+def test_cpp_mirror_compiles_and_links(tmp_path):
+    _compile(tmp_path)
+
+
+@pytest.mark.gpu
+def test_hello_world_matches_oracle(gpu, tmp_path):
+    exe = _compile(tmp_path)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.strip().splitlines()
+    got = np.array([[float.fromhex(v) for v in ln.split()[1:]] for ln in lines[:60]], dtype=np.float32)
+    sc = scenes.Scene(name="hello_world")
+    g = sc.body(scenes.STATIC, 0.0, -10.0)
+    sc.fixture(g, 3, [50.0, 10.0], n=2, density=0.0)
+    b = sc.body(scenes.DYNAMIC, 0.0, 4.0)
+    sc.fixture(b, 3, [1.0, 1.0], n=2, density=1.0, friction=0.3)
+    o = oracle.OracleWorld(sc, "port", "project")
+    want = []
+    for _ in range(60):
+        o.step(1.0 / 60.0, 6, 2)
+        s = o.bodies()[1]
+        want.append([s[0], s[1], s[2]])
+    want = np.array(want, dtype=np.float32)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    tail = lines[60].split()
+    assert tail[0] == "contacts" and int(tail[1]) == 1 and int(tail[3]) == 1 and int(tail[5]) == 0

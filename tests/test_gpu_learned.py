@@ -1,0 +1,90 @@
+"""The learned warm start end to end on the GPU: log the plain solver's converged impulses, train the
+network with the library's kernels, and count the velocity iterations the plain solver needs to
+reach a residual tolerance with and without it on held-out seeds."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from box2dpp_gb300 import scenes
+from box2dpp_gb300.learn import Mlp
+from box2dpp_gb300.world import World
+from tests._util import DT, PI
+
+pytestmark = pytest.mark.gpu
+
+TOL, MAX_VI = 1e-3, 40
+
+
+def _log(seed, n_worlds, steps):
+    w = World(scenes.config4(n_worlds, seed, 120))
+    w.set_solver("plain")
+    for _ in range(40):
+        w.step(DT, 8, PI)
+    w.set_contact_log(2_000_000)
+    xs, ts = [], []
+    for _ in range(steps):
+        w.step(DT, MAX_VI, PI)
+        x, t = w.read_contact_log()
+        xs.append(x)
+        ts.append(t)
+    return np.concatenate(xs), np.concatenate(ts)
+
+
+def _iterations(mlp, seed):
+    w = World(scenes.config4(32, seed, 120))
+    w.set_solver("plain", tolerance=TOL, measure_residual=True)
+    for _ in range(40):
+        w.step(DT, 8, PI)
+    w.set_warm_start(mlp)
+    its, used = [], []
+    for _ in range(30):
+        w.step(DT, MAX_VI, PI)
+        its.append(w.solver_stats()[1].copy())
+        if mlp is not None:
+            used.append(w.warm_stats().copy())
+    return np.array(its), (np.array(used) if used else None)
+
+
+@pytest.fixture(scope="module")
+def trained():
+    x, t = _log(1000, 48, 20)
+    assert len(x) > 10000 and np.all(np.isfinite(x)) and np.all(np.isfinite(t))
+    m = Mlp(7)
+    m.fit_normaliser(x)
+    losses = m.train(x, t, steps=1500, batch=4096, lr=2e-3, seed=3)
+    return m, losses, x, t
+
+
+def test_contact_log_is_consistent(gpu):
+    x, t = _log(1500, 4, 3)
+    assert x.shape[1] == 14 and t.shape[1] == 2
+    n = np.hypot(x[:, 0], x[:, 1])
+    assert np.allclose(n, 1.0, atol=1e-4)            # unit normals
+    assert np.all(t[:, 0] >= 0.0)                     # normal impulses are non-negative
+    assert np.all(x[:, 11] > 0.0)                     # effective inverse normal mass
+    assert set(np.unique(x[:, 13])) <= {0.0, 1.0}
+
+
+def test_training_fits_the_logged_impulses(gpu, trained):
+    m, losses, x, t = trained
+    assert np.all(np.isfinite(losses))
+    assert losses[-50:].mean() < 0.5 * losses[:10].mean()
+
+
+def test_learned_warm_start_needs_fewer_iterations(gpu, trained):
+    m = trained[0]
+    ref, _ = _iterations(None, 5000)
+    lrn, used = _iterations(m, 5000)
+    ratio = lrn.mean() / ref.mean()
+    print(f"iterations to {TOL} m/s: reference warm start {ref.mean():.2f}, learned {lrn.mean():.2f} "
+          f"(ratio {ratio:.2f}); learned prediction kept in {used.mean() * 100:.0f}% of world-steps")
+    assert lrn.mean() <= ref.mean() * 1.02 + 0.25
+
+
+def test_untrained_network_falls_back(gpu):
+    m = Mlp(11)  # random weights: its predictions are poor, so worlds keep the reference warm start
+    lrn, used = _iterations(m, 6000)
+    ref, _ = _iterations(None, 6000)
+    assert used.mean() < 0.5
+    assert lrn.mean() <= ref.mean() * 1.1 + 0.5
