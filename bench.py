@@ -54,16 +54,16 @@ def parse():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    from box2dpp_gb300 import shard
+
+    return shard.dist_env()
 
 
 def workload(args, rank: int):
-    from box2dpp_gb300 import scenes
+    """This rank's shard: its own args.worlds worlds (weak scaling, no data-path collective)."""
+    from box2dpp_gb300 import shard
 
-    return scenes.config3(args.worlds, seed=args.seed + 1000003 * rank, allow_sleep=False)
+    return shard.shard_workload(args.worlds, args.seed, rank, allow_sleep=False)
 
 
 def config_dict(args, worlds, extra=None):
@@ -255,12 +255,9 @@ def run_gpu(args):
             torch.cuda.synchronize()
 
     def max_over_ranks(x: float) -> float:
-        t = torch.tensor([x], device="cuda")
-        if world_size > 1:
-            import torch.distributed as dist
+        from box2dpp_gb300 import shard
 
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return shard.max_over_ranks(x, world_size, device="cuda")
 
     vi = args.coloured_vi
     w, tune_steps = _prepare(worlds, stream, "coloured", vi, args.warmup)
