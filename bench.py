@@ -175,6 +175,7 @@ def cpu_baseline(worlds, steps: int, warmup: int, threads: int):
     el = time.perf_counter() - t0
     return {
         "value": bodies * steps / el,
+        "ms_per_step": el * 1e3 / max(steps, 1),
         "unit": UNIT,
         "cores": threads,
         "kind": kind,
@@ -192,7 +193,7 @@ def run_reference(args):
     cb = cpu_baseline(worlds, args.steps, args.warmup, threads)
     line = {
         "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": config_dict(args, worlds, {"sample": cb["sample"]}),
         "cpu_baseline": cb,
@@ -324,8 +325,9 @@ def run_gpu(args):
                 "launch_plan": plan.tolist(), "autotune_candidate_ms": [round(float(x), 3) for x in cand_ms],
                 "autotune_steps": tune_steps, "cuda_graph": "one captured step replayed per step"}),
             "residual": {"coloured_median": float(np.median(res)), "unit": "m/s",
-                         "definition": "max over contacts of |vn - bias| (active normal), max(0, bias - vn) "
-                                       "(inactive), |vt| (unsaturated friction), after the velocity iterations"},
+                         "definition": "max over contact points of the natural-map residual in m/s: |vn - bias| on "
+                                       "active normal points, |vt| on friction inside its cone, 0 at a solution; "
+                                       "after the velocity iterations"},
             "plain": plain,
             "roofline": roof,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nb * 16, "d2h_bytes_per_step": nb * 16,

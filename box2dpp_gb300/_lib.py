@@ -102,7 +102,7 @@ def load(build_if_missing: bool = True):
         "gb_world_graph_step": [vp, f, i, i],
         "gb_mlp_create": [C.c_ulonglong, C.POINTER(vp)],
         "gb_world_set_warm_start": [vp, vp, i],
-        "gb_world_warm_stats": [vp, _i32],
+        "gb_world_warm_stats": [vp, _i32, _i32],
         "gb_world_set_contact_log": [vp, i],
         "gb_world_read_contact_log": [vp, _f32, _f32, i, C.POINTER(i)],
         "gb_mlp_destroy": [vp],

@@ -1064,18 +1064,24 @@ gb_status gb_world_solver_stats(gb_world* g, int* colours, int* vel_iters, float
     return GB_OK;
 }
 
-gb_status gb_world_warm_stats(gb_world* g, int* learned_used)
+gb_status gb_world_warm_stats(gb_world* g, int* learned_islands, int* vel_iters_sum)
 {
-    if (!g || !learned_used) return GB_ERR_INVALID;
+    if (!g) return GB_ERR_INVALID;
     const int nw = (int)g->worlds.size();
     if (!g->onDevice) {
-        for (int i = 0; i < nw; ++i) learned_used[i] = 0;
+        for (int i = 0; i < nw; ++i) {
+            if (learned_islands) learned_islands[i] = 0;
+            if (vel_iters_sum) vel_iters_sum[i] = 0;
+        }
         return GB_OK;
     }
     GB_CUDA(cudaStreamSynchronize(g->stream));
     std::vector<WorldState> st(nw);
     GB_CUDA(cudaMemcpy(st.data(), g->batch.state, nw * sizeof(WorldState), cudaMemcpyDeviceToHost));
-    for (int i = 0; i < nw; ++i) learned_used[i] = st[i].warmLearned;
+    for (int i = 0; i < nw; ++i) {
+        if (learned_islands) learned_islands[i] = st[i].warmLearned;
+        if (vel_iters_sum) vel_iters_sum[i] = st[i].velItersSum;
+    }
     return GB_OK;
 }
 

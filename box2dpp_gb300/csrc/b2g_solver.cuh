@@ -547,10 +547,14 @@ __device__ inline void IntegratePosition(float4& p4, float4& v4, float h)
 }
 
 // ------------------------------------------------------------------ residual
-// Velocity residual of one contact (m/s): for every point, |vn - velocityBias| where the normal
-// impulse is positive (active) and max(0, velocityBias - vn) where it is zero (the complementarity
-// violation), and |vt| where the friction impulse is below its bound (not saturated). Used to judge
-// solver variants at matched accuracy; it does not change the solution.
+// Velocity residual of one contact (m/s): the natural-map residual of the contact's complementarity
+// conditions in velocity units, i.e. for every point how far one projected Gauss-Seidel update of its
+// impulse would move it, divided by the effective mass:
+//   normal  |ni - max(0, ni - mn (vn - bias))| / mn  (= |vn - bias| for an active point that stays
+//           active, = max(0, bias - vn) for an inactive one, = ni / mn for one that would separate)
+//   tangent |ti - clamp(ti - mt vt, -mu ni, mu ni)| / mt  (= |vt| strictly inside the friction cone,
+//           0 for a contact sliding at the bound in the direction its impulse opposes)
+// It is zero exactly at a solution of the contact problem and does not change the solution.
 __device__ float ContactResidual(const VelConstraint& v, const float4 imp, const float4* vel)
 {
     const float4 va = vel[v.idx.x], vb = vel[v.idx.y];
@@ -563,10 +567,11 @@ __device__ float ContactResidual(const VelConstraint& v, const float4 imp, const
         const float ni = j == 0 ? imp.x : imp.z, ti = j == 0 ? imp.y : imp.w;
         const Vec2 dv = vB + Cross(vb.z, V(rr.z, rr.w)) - vA - Cross(va.z, V(rr.x, rr.y));
         const float vn = Dot(dv, normal);
-        const float rn = ni > 0.0f ? fabsf(vn - cc.z) : fmaxf(0.0f, cc.z - vn);
-        r = fmaxf(r, rn);
+        const float mn = cc.x, mt = cc.y;
+        if (mn > 0.0f) r = fmaxf(r, fabsf(ni - fmaxf(0.0f, ni - mn * (vn - cc.z))) / mn);
         const float vt = Dot(dv, tangent) - v.nf.w;
-        if (fabsf(ti) < v.nf.z * ni) r = fmaxf(r, fabsf(vt));
+        const float bound = v.nf.z * ni;
+        if (mt > 0.0f) r = fmaxf(r, fabsf(ti - fminf(fmaxf(ti - mt * vt, -bound), bound)) / mt);
     }
     return r;
 }
@@ -589,8 +594,8 @@ __device__ float ctaMaxNonNeg(float x, int* slot)
 // the point, its separation, the four inverse masses and inertias, the reference warm-start normal
 // and tangent impulses (the previous step's, scaled by dtRatio; zero for new points) expressed as
 // velocities (impulse / effective mass), the effective inverse normal mass, the friction
-// coefficient, and whether the manifold has two points. The network predicts the point's final
-// normal and tangent impulses in the same velocity units.
+// coefficient, and whether the manifold has two points. The network predicts how far the point's
+// final normal and tangent impulses are from the reference warm start, in the same velocity units.
 __device__ void PointFeatures(const VelConstraint& v, const float4 imp, const float2 sep, const float4* vel, int j,
                               float (&f)[kMlpIn])
 {
@@ -614,8 +619,9 @@ __device__ void PointFeatures(const VelConstraint& v, const float4 imp, const fl
 
 // Network predictions for every island contact point, written to vimpL: one 16-row tile (8
 // contacts, 2 points each) per warp at a time; rows of absent points are zero and ignored. The
-// prediction is decoded as normal impulse max(0, y0 * normalMass) and tangent impulse y1 *
-// tangentMass clamped to the friction cone.
+// outputs are corrections to the reference warm start in velocity units: normal impulse
+// max(0, ref + y0 * normalMass), tangent impulse ref + y1 * tangentMass clamped to the friction
+// cone (an output of zero reproduces the reference warm start).
 __device__ __noinline__ void Wd::learnedImpulses(const StepParams& P, int nContacts, const float4* imp, const float4* vel)
 {
     __shared__ __align__(16) __nv_bfloat16 xTile[kMaxCta / 32][16 * kMlpInPad];
@@ -650,9 +656,10 @@ __device__ __noinline__ void Wd::learnedImpulses(const StepParams& P, int nConta
                 const VelConstraint v = vc[i];
                 if (j >= v.idx.z) continue;
                 const float4 c = j == 0 ? v.c0 : v.c1;
-                const float ni = fmaxf(0.0f, out[2 * h] * c.x);
+                const float4 ref = imp[i];
+                const float ni = fmaxf(0.0f, (j == 0 ? ref.x : ref.z) + out[2 * h] * c.x);
                 const float bound = v.nf.z * ni;
-                const float ti = fminf(fmaxf(out[2 * h + 1] * c.y, -bound), bound);
+                const float ti = fminf(fmaxf((j == 0 ? ref.y : ref.w) + out[2 * h + 1] * c.y, -bound), bound);
                 float* dst = reinterpret_cast<float*>(&vimpL[i]) + 2 * j;
                 dst[0] = ni;
                 dst[1] = ti;
@@ -708,6 +715,10 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
     const bool learned = P.warmMode == kWarmLearned && warm;
     const bool logging = P.logX != nullptr && !coloured;
     const bool needSep = learned || logging;
+    // island of each island contact during the learned warm-start choice (contact-sized scratch that
+    // is free during the island solve)
+    int* contactIsland = pairKeep;
+    auto cColourIsland = [&](int i) -> int& { return contactIsland[i]; };
     float4* pos = rowsInSmem ? smem : sPos;
     float4* vel = rowsInSmem ? smem + smemRows : sVel;
     float4* imp = nContacts <= smemContacts ? smem + 2 * smemRows : vimp;
@@ -763,19 +774,35 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
         __syncthreads();
         warmStartAll(nIsl, colourStart, imp, vel);
         warmStartAll(nIsl, colourStart, vimpL, sVelL);
-        float rRef = 0.0f, rL = 0.0f;
-        for (int i = tid(); i < nContacts; i += nthreads()) {
-            rRef = fmaxf(rRef, ContactResidual(vc[i], imp[i], vel));
-            rL = fmaxf(rL, ContactResidual(vc[i], vimpL[i], sVelL));
-        }
-        rRef = ctaMaxNonNeg(rRef, &sRes);
-        rL = ctaMaxNonNeg(rL, &sRes);
-        if (rL < rRef) {
-            for (int r = tid(); r < nRows; r += nthreads()) vel[r] = sVelL[r];
-            for (int i = tid(); i < nContacts; i += nthreads()) imp[i] = vimpL[i];
-            if (tid() == 0) st->warmLearned = 1;
+        // per-island residuals (islands are independent): each contact's residual both ways, reduced
+        // into two per-island maxima (non-negative floats order as integers)
+        int* islRef = sStack;
+        int* islL = sWake;
+        for (int isl = tid(); isl < nIsl; isl += nthreads()) { islRef[isl] = 0; islL[isl] = 0; }
+        __syncthreads();
+        for (int isl = tid(); isl < nIsl; isl += nthreads()) {
+            const int4 I = islands[isl];
+            for (int i = I.z; i < I.z + I.w; ++i) cColourIsland(i) = isl;
         }
         __syncthreads();
+        for (int i = tid(); i < nContacts; i += nthreads()) {
+            const int isl = cColourIsland(i);
+            atomicMax(&islRef[isl], __float_as_int(ContactResidual(vc[i], imp[i], vel)));
+            atomicMax(&islL[isl], __float_as_int(ContactResidual(vc[i], vimpL[i], sVelL)));
+        }
+        __syncthreads();
+        // each island keeps the warm start with the smaller residual (the reference's on a tie)
+        for (int isl = tid(); isl < nIsl; isl += nthreads()) {
+            if (!(__int_as_float(islL[isl]) < __int_as_float(islRef[isl]))) continue;
+            const int4 I = islands[isl];
+            for (int r = I.x; r < I.x + I.y; ++r) vel[r] = sVelL[r];
+            for (int i = I.z; i < I.z + I.w; ++i) imp[i] = vimpL[i];
+            atomicAdd(&st->warmLearned, 1);
+        }
+        __syncthreads();
+        float rRef = 0.0f, rL = 0.0f;
+        (void)rRef;
+        (void)rL;
         warmDone = true;
     }
     if (tid() == 0) { unsigned long long now = clock64(); st->cyc[8] = now - tStamp; tStamp = now; }
@@ -802,6 +829,7 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
                 SweepVelocity(vc, imp, lo, hi, vel);
             }
             atomicMax(&sFlag, it);
+            atomicAdd(&st->velItersSum, it * I.w);
         }
         __syncthreads();
         itersRun = sFlag;
@@ -864,6 +892,7 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
             }
         }
         itersRun = it;
+        if (tid() == 0) st->velItersSum = it * nContacts;
     }
     if (P.measureResidual) {
         float r = 0.0f;

@@ -212,7 +212,19 @@ struct Wd {
 
     // b2Contact::Update (Dynamics/Contacts/b2Contact.cpp:164-245). Returns true when the touching
     // state of a non-sensor contact changed (the caller wakes both bodies).
-    __device__ bool update(int c)
+    // Copies the shape of fixture f to dst, 8 bytes at a time (shapes are 8-byte aligned).
+    __device__ void stageShape(int f, Shape* dst) const
+    {
+        static_assert(sizeof(Shape) % 8 == 0, "shapes are copied as float2");
+        const float2* src = reinterpret_cast<const float2*>(shape + f);
+        float2* out = reinterpret_cast<float2*>(dst);
+#pragma unroll
+        for (int k = 0; k < (int)(sizeof(Shape) / 8); ++k) out[k] = src[k];
+    }
+
+    // stage (optional): this thread's two shape slots in shared memory; the narrowphase then reads
+    // both shapes there instead of re-reading them from global memory in its loops
+    __device__ bool update(int c, Shape* stage = nullptr)
     {
         int4 info = ci[c];
         int fl = info.x | kCEnabled;
@@ -239,7 +251,13 @@ struct Wd {
             m.type = old.type;
             m.localNormal = old.localNormal;
             m.localPoint = old.localPoint;
-            Evaluate(&m, shape[fA], xfA, shape[fB], xfB);
+            if (stage) {
+                stageShape(fA, stage);
+                stageShape(fB, stage + 1);
+                Evaluate(&m, stage[0], xfA, stage[1], xfB);
+            } else {
+                Evaluate(&m, shape[fA], xfA, shape[fB], xfB);
+            }
             for (int i = 0; i < m.count; ++i) {
                 m.p[i].ni = 0.0f;
                 m.p[i].ti = 0.0f;
@@ -590,6 +608,8 @@ __device__ void Wd::collide()
 {
     __shared__ int sChanged;
     const int n = st->contactCount;
+    // two shape slots per thread in the dynamic shared memory (free during this phase) when it fits
+    Shape* shapeSlots = (int)(2 * sizeof(Shape)) * nthreads() <= smemBytes ? reinterpret_cast<Shape*>(smemBase) : nullptr;
     for (int b = tid(); b < d.bodyCount; b += nthreads()) sWake[b] = awake(b) ? -1 : INT_MAX;
     for (int k = tid(); k < n; k += nthreads()) sStatus[k] = 0;
     __syncthreads();
@@ -626,7 +646,7 @@ __device__ void Wd::collide()
                 continue;
             }
             sStatus[k] = 1;
-            if (update(c)) {
+            if (update(c, shapeSlots ? shapeSlots + 2 * tid() : nullptr)) {
                 if (atomicMin(&sWake[bA], k) > k) sChanged = 1;
                 if (atomicMin(&sWake[bB], k) > k) sChanged = 1;
             }
@@ -1055,29 +1075,55 @@ __device__ void Wd::solveTOI(const StepParams& P)
         if (tid() == 0) sAdvance = 0;
         __syncthreads();
         // Classify every contact of the list in parallel: 0 skipped, 1 cached TOI, 2 TOI needed.
-        // Whether a contact is skipped does not depend on the sweeps, so this is order-free.
-        for (int k = tid(); k < n; k += nthreads()) {
-            int c = order[k];
-            TOITask& T = toi[k];
-            T.contact = c;
-            int kind = 0;
-            int4 info = ci[c];
-            if ((info.x & kCEnabled) != 0 && info.w <= kMaxSubSteps) {
-                if (info.x & kCToi) kind = 1;
-                else if (fi[info.y].w == 0 && fi[info.z].w == 0) {
-                    int bA = fixBody(info.y), bB = fixBody(info.z);
-                    int4 iA = bi[bA], iB = bi[bB];
-                    bool activeA = (iA.y & kBAwake) && iA.x != kStatic;
-                    bool activeB = (iB.y & kBAwake) && iB.x != kStatic;
-                    bool collideA = (iA.y & kBBullet) || iA.x != kDynamic;
-                    bool collideB = (iB.y & kBBullet) || iB.x != kDynamic;
-                    if ((activeA || activeB) && (collideA || collideB)) {
-                        kind = 2;
-                        if (sw[bA].w != sw[bB].w) sAdvance = 1;
+        // Whether a contact is skipped does not depend on the sweeps, so this is order-free. Each
+        // thread gathers kBatch contacts one dependency level at a time (list slot, contact, its
+        // fixtures, their bodies), so the global loads of a level overlap instead of queueing.
+        constexpr int kBatch = 8;
+        for (int k0 = tid(); k0 < n; k0 += kBatch * nthreads()) {
+            int c[kBatch];
+            int4 info[kBatch];
+            int fA[kBatch], fB[kBatch];
+            bool live[kBatch];
+#pragma unroll
+            for (int j = 0; j < kBatch; ++j) {
+                const int k = k0 + j * nthreads();
+                c[j] = k < n ? order[k] : -1;
+            }
+#pragma unroll
+            for (int j = 0; j < kBatch; ++j) info[j] = c[j] >= 0 ? ci[c[j]] : make_int4(0, 0, 0, 0);
+#pragma unroll
+            for (int j = 0; j < kBatch; ++j) {
+                live[j] = c[j] >= 0 && (info[j].x & kCEnabled) != 0 && info[j].w <= kMaxSubSteps &&
+                          (info[j].x & kCToi) == 0;
+                const int4 a = live[j] ? fi[info[j].y] : make_int4(0, 0, 0, 1);
+                const int4 b = live[j] ? fi[info[j].z] : make_int4(0, 0, 0, 1);
+                fA[j] = a.w == 0 && b.w == 0 ? a.x : -1;  // body of fixture A, -1 when a sensor
+                fB[j] = b.x;
+            }
+#pragma unroll
+            for (int j = 0; j < kBatch; ++j) {
+                const int k = k0 + j * nthreads();
+                if (c[j] < 0) continue;
+                int kind = 0;
+                if ((info[j].x & kCEnabled) != 0 && info[j].w <= kMaxSubSteps) {
+                    if (info[j].x & kCToi) kind = 1;
+                    else if (fA[j] >= 0) {
+                        const int bA = fA[j], bB = fB[j];
+                        const int4 iA = bi[bA], iB = bi[bB];
+                        const bool activeA = (iA.y & kBAwake) && iA.x != kStatic;
+                        const bool activeB = (iB.y & kBAwake) && iB.x != kStatic;
+                        const bool collideA = (iA.y & kBBullet) || iA.x != kDynamic;
+                        const bool collideB = (iB.y & kBBullet) || iB.x != kDynamic;
+                        if ((activeA || activeB) && (collideA || collideB)) {
+                            kind = 2;
+                            if (sw[bA].w != sw[bB].w) sAdvance = 1;
+                        }
                     }
                 }
+                TOITask& T = toi[k];
+                T.contact = c[j];
+                T.kind = kind;
             }
-            T.kind = kind;
         }
         __syncthreads();
         if (sAdvance) {
@@ -1237,13 +1283,23 @@ __device__ void Wd::solveTOI(const StepParams& P)
                     }
                 }
                 stamp(18);
-                // b2Island::SolveTOI (Dynamics/b2Island.cpp:386-485)
+                // b2Island::SolveTOI (Dynamics/b2Island.cpp:386-485). The mini island's rows and
+                // constraint records live in shared memory when they fit (the CTA's dynamic shared
+                // memory is free during the continuous phase), else in the global scratch.
+                const int miniBytes = (2 * bodyCap) * (int)sizeof(float4) +
+                                      kMaxTOIContacts * (int)(sizeof(VelConstraint) + sizeof(PosConstraint) + sizeof(float4));
+                const bool miniShared = miniBytes <= smemBytes;
+                float4* mPos = miniShared ? smemBase : sPos;
+                float4* mVel = miniShared ? smemBase + bodyCap : sVel;
+                VelConstraint* mVc = miniShared ? reinterpret_cast<VelConstraint*>(smemBase + 2 * bodyCap) : vc;
+                PosConstraint* mPc = miniShared ? reinterpret_cast<PosConstraint*>(mVc + kMaxTOIContacts) : pc;
+                float4* mImp = miniShared ? reinterpret_cast<float4*>(mPc + kMaxTOIContacts) : vimp;
                 float subDt = (1.0f - minAlpha) * P.dt;
                 for (int i = 0; i < nBodies; ++i) {
                     int b = sBody[i];
                     float4 s = sw[b], v = vel[b];
-                    sPos[i] = make_float4(s.x, s.y, s.z, 0.0f);
-                    sVel[i] = make_float4(v.x, v.y, v.z, 0.0f);
+                    mPos[i] = make_float4(s.x, s.y, s.z, 0.0f);
+                    mVel[i] = make_float4(v.x, v.y, v.z, 0.0f);
                 }
                 // rows 0..nBodies-1 of the scratch hold the mini island (island index == row)
                 for (int i = 0; i < nContacts; ++i) {
@@ -1253,28 +1309,28 @@ __device__ void Wd::solveTOI(const StepParams& P)
                     PosConstraint p;
                     float4 im;
                     ContactSetup(*this, v, p, im, sContact[i], false, 1.0f);
-                    vc[i] = v;
-                    pc[i] = p;
-                    vimp[i] = im;
+                    mVc[i] = v;
+                    mPc[i] = p;
+                    mImp[i] = im;
                 }
                 const int toiA = bj[bA].z, toiB = bj[bB].z;
                 for (int it = 0; it < 20; ++it)
-                    if (SweepPosition(pc, 0, nContacts, sPos, true, toiA, toiB)) break;
+                    if (SweepPosition(mPc, 0, nContacts, mPos, true, toiA, toiB)) break;
                 {
-                    float4 pA = sPos[toiA], pB = sPos[toiB];
+                    float4 pA = mPos[toiA], pB = mPos[toiB];
                     float4 a0 = sw0[bA];
                     sw0[bA] = make_float4(pA.x, pA.y, pA.z, a0.w);
                     float4 b0 = sw0[bB];
                     sw0[bB] = make_float4(pB.x, pB.y, pB.z, b0.w);
                 }
-                for (int i = 0; i < nContacts; ++i) ContactInitVelocity(*this, vc[i], pc[i], sPos, sVel);
-                for (int it = 0; it < P.velocityIterations; ++it) SweepVelocity(vc, vimp, 0, nContacts, sVel);
+                for (int i = 0; i < nContacts; ++i) ContactInitVelocity(*this, mVc[i], mPc[i], mPos, mVel);
+                for (int it = 0; it < P.velocityIterations; ++it) SweepVelocity(mVc, mImp, 0, nContacts, mVel);
                 const float h = subDt;
                 for (int i = 0; i < nBodies; ++i) {
-                    float4 p4 = sPos[i], v4 = sVel[i];
+                    float4 p4 = mPos[i], v4 = mVel[i];
                     IntegratePosition(p4, v4, h);
-                    sPos[i] = p4;
-                    sVel[i] = v4;
+                    mPos[i] = p4;
+                    mVel[i] = v4;
                     int b = sBody[i];
                     sw[b] = make_float4(p4.x, p4.y, p4.z, sw[b].w);
                     vel[b] = make_float4(v4.x, v4.y, v4.z, 0.0f);
@@ -1311,7 +1367,11 @@ __device__ void Wd::solveTOI(const StepParams& P)
 // (positions, then velocities) and the accumulated impulses of the island contacts when a world's
 // fit, and the broadphase proxies, pair keys and list heads outside the island solve; every use
 // falls back to global memory when the world is larger, so the shape changes speed, never results.
-__global__ void __launch_bounds__(128) StepKernel(Batch B, StepParams P, const int* schedule, LaunchShape L)
+// Minimum resident CTAs per SM the register allocation must allow at 128 threads (1: no cap).
+#ifndef B2G_STEP_MIN_BLOCKS
+#define B2G_STEP_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(128, B2G_STEP_MIN_BLOCKS) StepKernel(Batch B, StepParams P, const int* schedule, LaunchShape L)
 {
     extern __shared__ float4 smem[];
     Wd W;
@@ -1331,6 +1391,7 @@ __global__ void __launch_bounds__(128) StepKernel(Batch B, StepParams P, const i
         W.st->velIters = 0;
         W.st->residual = 0.0f;
         W.st->warmLearned = 0;
+        W.st->velItersSum = 0;
         W.st->newFixture = 0;
         for (int i = 0; i < kProfileSlots; ++i) W.st->cyc[i] = 0;
     }

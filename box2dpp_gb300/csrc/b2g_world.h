@@ -59,7 +59,8 @@ struct WorldState {
     int colours;        // constraint colours used by the coloured solver in the last step
     int velIters;       // velocity iterations run in the last step (fewer than asked when a tolerance is met)
     float residual;     // velocity residual (m/s) after the last step's velocity iterations, when measured
-    int warmLearned;    // 1 when the last step used the learned warm start (its residual was smaller)
+    int warmLearned;    // islands of the last step that kept the learned warm start (its residual was smaller)
+    int velItersSum;    // velocity iterations of the last step x island contacts, summed over islands
     // SM clock cycles of the last step per phase: 0 new-fixture pairs, 1 collide, 2 island DFS,
     // 3 island solve, 4 fixture sync, 5 pairs after solve, 6 TOI, 7 whole step; then the island solve
     // split: 8 integrate + constraint init, 9 warm start + velocity sweeps, 10 impulses + position

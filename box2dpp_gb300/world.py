@@ -108,10 +108,12 @@ class World:
             _lib.check(self.lib.gb_world_set_warm_start(self.h, mlp.h, _lib.WARM_LEARNED), "gb_world_set_warm_start")
         self._mlp = mlp
 
-    def warm_stats(self) -> np.ndarray:
+    def warm_stats(self):
+        """(islands that kept the learned warm start, velocity iterations summed over islands) per world."""
         used = np.zeros(self.n_worlds, dtype=np.int32)
-        _lib.check(self.lib.gb_world_warm_stats(self.h, used), "gb_world_warm_stats")
-        return used
+        its = np.zeros(self.n_worlds, dtype=np.int32)
+        _lib.check(self.lib.gb_world_warm_stats(self.h, used, its), "gb_world_warm_stats")
+        return used, its
 
     def set_contact_log(self, capacity: int) -> None:
         _lib.check(self.lib.gb_world_set_contact_log(self.h, int(capacity)), "gb_world_set_contact_log")

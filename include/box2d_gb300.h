@@ -96,8 +96,11 @@ gb_status gb_world_sync(gb_world* world);
  * are not the reference's bits. tolerance > 0 ends the velocity iterations of a world (plain: of an
  * island) once its velocity residual is at most tolerance (m/s); velocity_iterations stays the
  * maximum. measure_residual != 0 records each world's velocity residual after the velocity
- * iterations (gb_world_solver_stats). The velocity residual is the largest of |vn - bias| over
- * active normal points, max(0, bias - vn) over inactive ones and |vt| over unsaturated friction. */
+ * iterations (gb_world_solver_stats). The velocity residual is the largest over contact points of
+ * the natural-map residual of the contact conditions in velocity units: |ni - max(0, ni - mn (vn -
+ * bias))| / mn for the normal impulse ni (effective mass mn) and |ti - clamp(ti - mt vt, -mu ni,
+ * mu ni)| / mt for the tangent impulse ti; it is |vn - bias| on active normal points, |vt| on friction
+ * strictly inside its cone, and zero exactly at a solution. */
 #define GB_SOLVER_PLAIN 0
 #define GB_SOLVER_COLOURED 1
 gb_status gb_world_set_solver(gb_world* world, int solver, float tolerance, int measure_residual);
@@ -234,15 +237,20 @@ gb_status gb_mlp_train(gb_mlp* mlp, const float* x, const float* t, int n, int s
  * and inertia of both bodies (4); the reference warm-start normal and tangent impulses divided by
  * the point's normal and tangent effective mass; the effective inverse normal mass; the friction
  * coefficient; 1 for a two-point manifold. The outputs, multiplied by the normal and tangent
- * effective mass, are the predicted impulses (normal clamped at 0, tangent to the friction cone).
+ * effective mass, are corrections added to the reference warm-start impulses (the normal result
+ * clamped at 0, the tangent one to the friction cone); the network is trained on the logged final
+ * impulses minus the reference warm start (t - x[9..10] in the log's units).
  * Each world then warm-starts its velocities both ways and keeps the one whose velocity residual is
- * smaller, so a world falls back to the reference warm start whenever the prediction is worse. The
- * network must outlive its use by the world. */
+ * smaller, island by island (islands share no dynamic body), so an island falls back to the reference
+ * warm start whenever the prediction is worse. The network must outlive its use by the world. */
 #define GB_WARM_REFERENCE 0
 #define GB_WARM_LEARNED 1
 gb_status gb_world_set_warm_start(gb_world* world, gb_mlp* mlp, int mode);
-/* Per world: 1 when the last step used the learned warm start. */
-gb_status gb_world_warm_stats(gb_world* world, int* learned_used);
+/* Per world of the last step (arrays of n_worlds, each may be NULL): islands that kept the learned
+ * warm start, and the contact-iterations of the velocity solve (each island's iterations times its
+ * contacts, summed): divided by the solved contacts (gb_world_totals), the mean iterations a contact
+ * went through, e.g. to reach a residual tolerance. */
+gb_status gb_world_warm_stats(gb_world* world, int* learned_islands, int* vel_iters_sum);
 
 /* Contact-point log for training the network (plain solver only): capacity > 0 allocates a device
  * log of that many points and starts recording, 0 stops and frees it. Every step appends, for each

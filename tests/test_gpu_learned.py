@@ -32,27 +32,21 @@ def _log(seed, n_worlds, steps):
 
 
 def _iterations(mlp, seed):
-    w = World(scenes.config4(32, seed, 120))
-    w.set_solver("plain", tolerance=TOL, measure_residual=True)
-    for _ in range(40):
-        w.step(DT, 8, PI)
-    w.set_warm_start(mlp)
-    its, used = [], []
-    for _ in range(30):
-        w.step(DT, MAX_VI, PI)
-        its.append(w.solver_stats()[1].copy())
-        if mlp is not None:
-            used.append(w.warm_stats().copy())
-    return np.array(its), (np.array(used) if used else None)
+    from box2dpp_gb300.train_warmstart import iterations_to_tolerance
+
+    its, kept, _ = iterations_to_tolerance(mlp, seed, 32, 120, 40, 30, TOL, MAX_VI)
+    return its, kept
 
 
 @pytest.fixture(scope="module")
 def trained():
     x, t = _log(1000, 48, 20)
     assert len(x) > 10000 and np.all(np.isfinite(x)) and np.all(np.isfinite(t))
+    from box2dpp_gb300.train_warmstart import correction_targets
+
     m = Mlp(7)
     m.fit_normaliser(x)
-    losses = m.train(x, t, steps=1500, batch=4096, lr=2e-3, seed=3)
+    losses = m.train(x, correction_targets(x, t), steps=1500, batch=4096, lr=2e-3, seed=3)
     return m, losses, x, t
 
 
@@ -75,16 +69,15 @@ def test_training_fits_the_logged_impulses(gpu, trained):
 def test_learned_warm_start_needs_fewer_iterations(gpu, trained):
     m = trained[0]
     ref, _ = _iterations(None, 5000)
-    lrn, used = _iterations(m, 5000)
-    ratio = lrn.mean() / ref.mean()
-    print(f"iterations to {TOL} m/s: reference warm start {ref.mean():.2f}, learned {lrn.mean():.2f} "
-          f"(ratio {ratio:.2f}); learned prediction kept in {used.mean() * 100:.0f}% of world-steps")
-    assert lrn.mean() <= ref.mean() * 1.02 + 0.25
+    lrn, kept = _iterations(m, 5000)
+    print(f"iterations per contact to {TOL} m/s: reference warm start {ref:.2f}, learned {lrn:.2f} "
+          f"(ratio {lrn / ref:.2f}); learned prediction kept by {kept * 100:.0f}% of islands")
+    assert lrn <= ref * 1.02 + 0.25
 
 
 def test_untrained_network_falls_back(gpu):
-    m = Mlp(11)  # random weights: its predictions are poor, so worlds keep the reference warm start
-    lrn, used = _iterations(m, 6000)
+    m = Mlp(11)  # random weights: its predictions are poor, so islands keep the reference warm start
+    lrn, kept = _iterations(m, 6000)
     ref, _ = _iterations(None, 6000)
-    assert used.mean() < 0.5
-    assert lrn.mean() <= ref.mean() * 1.1 + 0.5
+    assert kept < 0.5
+    assert lrn <= ref * 1.1 + 0.5
