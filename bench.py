@@ -147,6 +147,12 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+# DRAM bytes (read + write) per algorithmic byte of the coloured StepKernel, from one full ncu capture
+# of the 1024-world case of this workload (275.6 MB of traffic for 41.4 MB algorithmic); traffic
+# grows with the units processed, so the full launch's traffic is this ratio x its algorithmic bytes.
+TRAFFIC_PER_ALGORITHMIC_BYTE = 275.6 / 41.4
+
+
 def algorithmic_bytes(t: dict) -> int:
     """Minimum HBM bytes of one step if every persistent element is read and written once:
     104 B per solved body (52 B read: c, a, v, w, invMass, invI, localCenter, gravityScale, damping;
@@ -310,7 +316,9 @@ def run_gpu(args):
         per_launch_ms = ms / args.steps
         achieved = step_bytes / (per_launch_ms / 1e3) / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "peak_source": peak_kind, "kernel": "b2g::StepKernel",
+                "traffic": step_bytes * TRAFFIC_PER_ALGORITHMIC_BYTE, "peak_source": peak_kind,
+                "traffic_note": "bytes per step, scaled from an ncu capture of the 1024-world case",
+                "kernel": "b2g::StepKernel",
                 "algorithmic_bytes_per_launch": step_bytes,
                 "launch_ms": per_launch_ms,
                 "note": "one step = the launches of the plan (one per class); bytes and time are per step",

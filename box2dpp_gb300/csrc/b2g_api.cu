@@ -557,7 +557,7 @@ gb_status Upload(gb_world* g)
     ALLOC(xf, tb); ALLOC(sw, tb); ALLOC(sw0, tb); ALLOC(vel, tb); ALLOC(frc, tb); ALLOC(mas, tb); ALLOC(prop, tb);
     ALLOC(bi, tb); ALLOC(bj, tb);
     ALLOC(fi, tf); ALLOC(fm, tf); ALLOC(ff, tf); ALLOC(faabb, tf); ALLOC(shape, tf);
-    ALLOC(fat, tp); ALLOC(pfix, tp); ALLOC(moved, tp); ALLOC(movedList, tp);
+    ALLOC(fat, tp); ALLOC(pfix, tp); ALLOC(moved, tp); ALLOC(movedList, tp); ALLOC(sweepRank, tp);
     ALLOC(ci, tc); ALLOC(ce, tc); ALLOC(cp, tc); ALLOC(mh, tc); ALLOC(mv, tc); ALLOC(mp0, tc); ALLOC(mp1, tc);
     ALLOC(order, tc); ALLOC(cnext, tc);
     ALLOC(joint, tj); ALLOC(sJoint, tj);
@@ -1061,6 +1061,21 @@ gb_status gb_world_solver_stats(gb_world* g, int* colours, int* vel_iters, float
         if (vel_iters) vel_iters[i] = st[i].velIters;
         if (residual) residual[i] = st[i].residual;
     }
+    return GB_OK;
+}
+
+gb_status gb_world_contact_stats(gb_world* g, float* max_penetration)
+{
+    if (!g || !max_penetration) return GB_ERR_INVALID;
+    const int nw = (int)g->worlds.size();
+    if (!g->onDevice) {
+        for (int i = 0; i < nw; ++i) max_penetration[i] = 0.0f;
+        return GB_OK;
+    }
+    GB_CUDA(cudaStreamSynchronize(g->stream));
+    std::vector<WorldState> st(nw);
+    GB_CUDA(cudaMemcpy(st.data(), g->batch.state, nw * sizeof(WorldState), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < nw; ++i) max_penetration[i] = st[i].maxPenetration;
     return GB_OK;
 }
 

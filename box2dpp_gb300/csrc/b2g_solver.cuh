@@ -319,7 +319,8 @@ __device__ void SweepVelocity(const VelConstraint* vc, float4* imp, int lo, int 
         imp[i] = im;
     }
 }
-__device__ bool SweepPosition(const PosConstraint* pc, int lo, int hi, float4* pos, bool toi, int toiA, int toiB)
+__device__ bool SweepPosition(const PosConstraint* pc, int lo, int hi, float4* pos, bool toi, int toiA, int toiB,
+                              float* minSepOut = nullptr)
 {
     float minSeparation = 0.0f;
     for (int i = lo; i < lo + kSweepPrefetch && i < hi; ++i) PrefetchRecord(pc + i);
@@ -328,6 +329,7 @@ __device__ bool SweepPosition(const PosConstraint* pc, int lo, int hi, float4* p
         const PosConstraint p = pc[i];
         ContactSolvePosition(p, pos, toi, toiA, toiB, minSeparation);
     }
+    if (minSepOut) *minSepOut = minSeparation;
     return toi ? minSeparation >= -1.5f * kLinearSlop : minSeparation >= -3.0f * kLinearSlop;
 }
 
@@ -621,7 +623,9 @@ __device__ void PointFeatures(const VelConstraint& v, const float4 imp, const fl
 // contacts, 2 points each) per warp at a time; rows of absent points are zero and ignored. The
 // outputs are corrections to the reference warm start in velocity units: normal impulse
 // max(0, ref + y0 * normalMass), tangent impulse ref + y1 * tangentMass clamped to the friction
-// cone (an output of zero reproduces the reference warm start).
+// cone (an output of zero reproduces the reference warm start). Points the reference starts warm
+// (a positive normal impulse carried over) keep it: the network is used where the reference has
+// nothing to offer, new or previously inactive points.
 __device__ __noinline__ void Wd::learnedImpulses(const StepParams& P, int nContacts, const float4* imp, const float4* vel)
 {
     __shared__ __align__(16) __nv_bfloat16 xTile[kMaxCta / 32][16 * kMlpInPad];
@@ -657,9 +661,13 @@ __device__ __noinline__ void Wd::learnedImpulses(const StepParams& P, int nConta
                 if (j >= v.idx.z) continue;
                 const float4 c = j == 0 ? v.c0 : v.c1;
                 const float4 ref = imp[i];
-                const float ni = fmaxf(0.0f, (j == 0 ? ref.x : ref.z) + out[2 * h] * c.x);
-                const float bound = v.nf.z * ni;
-                const float ti = fminf(fmaxf((j == 0 ? ref.y : ref.w) + out[2 * h + 1] * c.y, -bound), bound);
+                const float niRef = j == 0 ? ref.x : ref.z, tiRef = j == 0 ? ref.y : ref.w;
+                float ni = niRef, ti = tiRef;
+                if (!(niRef > 0.0f)) {
+                    ni = fmaxf(0.0f, niRef + out[2 * h] * c.x);
+                    const float bound = v.nf.z * ni;
+                    ti = fminf(fmaxf(tiRef + out[2 * h + 1] * c.y, -bound), bound);
+                }
                 float* dst = reinterpret_cast<float*>(&vimpL[i]) + 2 * j;
                 dst[0] = ni;
                 dst[1] = ti;
@@ -933,7 +941,9 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
             int2 J = islandJ[isl];
             bool positionSolved = false;
             for (int it = 0; it < P.positionIterations; ++it) {
-                bool contactsOkay = SweepPosition(pc, I.z, I.z + I.w, pos, false, -1, -1);
+                float minSep = 0.0f;
+                bool contactsOkay = SweepPosition(pc, I.z, I.z + I.w, pos, false, -1, -1, &minSep);
+                if (it == 0 && minSep < 0.0f) atomicMax(reinterpret_cast<int*>(&st->maxPenetration), __float_as_int(-minSep));
                 bool jointsOkay = true;
                 for (int k = 0; k < J.y; ++k) {
                     bool ok = RevSolvePosition(jt[sJoint[J.x + k]], pos);
@@ -974,6 +984,7 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
             }
             // every thread reports its worst separation (as a violation >= 0) and joint state
             const float violation = fmaxf(0.0f, -minSep);
+            if (it == 0 && violation > 0.0f) atomicMax(reinterpret_cast<int*>(&st->maxPenetration), __float_as_int(violation));
             const float worst = ctaMaxNonNeg(jointsOkay ? violation : 1e30f, &sRes);
             if (worst <= 3.0f * kLinearSlop) { positionSolved = true; break; }
         }

@@ -62,6 +62,7 @@ struct Wd {
     unsigned long long* pairs;
     int* pairKeep;
     int* movedList;
+    int* sweepRank;
     int4* pairInfo;
     float4* smemBase;   // the CTA's dynamic shared memory, free outside the island solve
     int smemBytes;
@@ -74,7 +75,7 @@ struct Wd {
         xf = B.xf + b; sw = B.sw + b; sw0 = B.sw0 + b; vel = B.vel + b; frc = B.frc + b; mas = B.mas + b;
         prop = B.prop + b; bi = B.bi + b; bj = B.bj + b;
         fi = B.fi + f; fm = B.fm + f; ff = B.ff + f; faabb = B.faabb + f; shape = B.shape + f;
-        fat = B.fat + p; pfix = B.pfix + p; moved = B.moved + p; movedList = B.movedList + p;
+        fat = B.fat + p; pfix = B.pfix + p; moved = B.moved + p; movedList = B.movedList + p; sweepRank = B.sweepRank + p;
         ci = B.ci + c; ce = B.ce + c; cp = B.cp + c; mh = B.mh + c; mv = B.mv + c; mp0 = B.mp0 + c; mp1 = B.mp1 + c;
         order = B.order + c; cnext = B.cnext + c;
         jt = B.joint + j; sJoint = B.sJoint + j;
@@ -313,6 +314,7 @@ struct Wd {
 
     // b2ContactManager::FindNewContacts -> b2BroadPhase::UpdatePairs -> AddPair, CTA-wide.
     __device__ void findNewContacts();
+    __device__ void sweepPairs(int m, int* pairCount);
     __device__ void collide();
     __device__ void solve(const StepParams& P, float4* smem, int smemRows, int smemContacts);
     __device__ bool buildIslandsShared(bool coloured, int* colourCount, int& nIsl, int& nRows, int& nCons, int& movers);
@@ -380,6 +382,110 @@ __device__ void ctaSortKeys(unsigned long long* keys, int n, int capacity)
 }
 
 // ------------------------------------------------------------------ FindNewContacts
+// Above this many moved x all proxy tests, pair finding sorts and sweeps instead.
+constexpr long long kSweepThreshold = 1ll << 20;
+
+__device__ inline unsigned OrderedBits(float x)
+{
+    const unsigned u = __float_as_uint(x);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ inline float FromOrderedBits(unsigned o)
+{
+    return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
+
+// The pairs of b2BroadPhase::UpdatePairs for large worlds, the same set the all-pairs test finds
+// (the overlap test is b2TestOverlap, only the candidates differ): live proxies sorted by fat lower
+// x, each moved proxy scans forward while candidates start before its upper x and backward while
+// they start after its lower x minus the widest proxy's width. Proxies more than 4x wider than the
+// mean (container edges, ground) are kept out of the scans and tested against every moved proxy.
+// Keys live in the pair-info scratch (free until contact creation), ranks in sweepRank.
+__device__ void Wd::sweepPairs(int m, int* pairCount)
+{
+    __shared__ float sWidthSum;
+    __shared__ int sLive, sSmall;
+    __shared__ unsigned sMaxW;
+    const int np = d.proxyCap;
+    if (tid() == 0) { sWidthSum = 0.0f; sLive = 0; sSmall = 0; sMaxW = 0u; }
+    __syncthreads();
+    float wsum = 0.0f;
+    int live = 0;
+    for (int p = tid(); p < np; p += nthreads())
+        if (pfix[p] >= 0) { const float4 f = fat[p]; wsum += f.z - f.x; ++live; }
+    atomicAdd(&sWidthSum, wsum);
+    atomicAdd(&sLive, live);
+    __syncthreads();
+    const int nLive = sLive;
+    const float wLarge = 4.0f * (sWidthSum / (float)max(nLive, 1));
+    unsigned long long* keys = reinterpret_cast<unsigned long long*>(pairInfo);
+    // keys: (ordered lower x) << 32 | proxy for the small proxies, all-ones << 32 | proxy for the wide
+    // ones so they sort last
+    __shared__ int sCursor;
+    if (tid() == 0) sCursor = 0;
+    __syncthreads();
+    for (int p = tid(); p < np; p += nthreads()) {
+        if (pfix[p] < 0) continue;
+        const float4 f = fat[p];
+        const float w = f.z - f.x;
+        const bool large = w > wLarge;
+        const unsigned hi = large ? 0xffffffffu : OrderedBits(f.x);
+        keys[atomicAdd(&sCursor, 1)] = ((unsigned long long)hi << 32) | (unsigned)p;
+        if (!large) {
+            atomicAdd(&sSmall, 1);
+            atomicMax(&sMaxW, __float_as_uint(fmaxf(w, 0.0f)));
+        }
+    }
+    __syncthreads();
+    const int cap = 2 * d.pairCap;
+    int P2 = 1;
+    while (P2 < nLive) P2 <<= 1;
+    if (P2 * (int)sizeof(unsigned long long) <= smemBytes) {
+        unsigned long long* sk = reinterpret_cast<unsigned long long*>(smemBase);
+        for (int i = tid(); i < nLive; i += nthreads()) sk[i] = keys[i];
+        __syncthreads();
+        ctaSortKeys(sk, nLive, P2);
+        for (int i = tid(); i < nLive; i += nthreads()) keys[i] = sk[i];
+        __syncthreads();
+    } else {
+        ctaSortKeys(keys, nLive, cap);
+    }
+    for (int i = tid(); i < nLive; i += nthreads()) sweepRank[(int)(keys[i] & 0xffffffffu)] = i;
+    __syncthreads();
+    const int nSmall = sSmall;
+    const float W = __uint_as_float(sMaxW) * 1.0001f + 1e-4f;
+    for (int t = tid(); t < m; t += nthreads()) {
+        const int q = movedList[t];
+        const float4 Fq = fat[q];
+        const int r = sweepRank[q];
+        auto test = [&](int p) {
+            if (p == q) return;
+            if (moved[p] && p < q) return;
+            if (!Overlap(fat[p], Fq)) return;
+            const int k = atomicAdd(pairCount, 1);
+            const unsigned long long lo = (unsigned long long)(p < q ? p : q), hi = (unsigned long long)(p < q ? q : p);
+            if (k < d.pairCap) pairs[k] = (lo << 32) | hi;
+        };
+        if (r >= nSmall) {
+            for (int j = 0; j < nLive; ++j) test((int)(keys[j] & 0xffffffffu));
+            continue;
+        }
+        for (int j = r + 1; j < nSmall; ++j) {
+            const unsigned long long key = keys[j];
+            if (FromOrderedBits((unsigned)(key >> 32)) > Fq.z) break;
+            test((int)(key & 0xffffffffu));
+        }
+        const float lowest = Fq.x - W - 1e-4f * fabsf(Fq.x);
+        for (int j = r - 1; j >= 0; --j) {
+            const unsigned long long key = keys[j];
+            if (FromOrderedBits((unsigned)(key >> 32)) < lowest) break;
+            test((int)(key & 0xffffffffu));
+        }
+        for (int j = nSmall; j < nLive; ++j) test((int)(keys[j] & 0xffffffffu));
+    }
+    __syncthreads();
+}
+
 __device__ void Wd::findNewContacts()
 {
     __shared__ int sMoved, sPairs, sNew, sKept;
@@ -407,6 +513,9 @@ __device__ void Wd::findNewContacts()
         __syncthreads();
     }
     const long long total = (long long)m * np;
+    if (total > kSweepThreshold) {
+        sweepPairs(m, &sPairs);
+    } else
     for (long long idx = tid(); idx < total; idx += nthreads()) {
         const int q = movedList[idx / np];
         const int p = (int)(idx % np);
@@ -1367,9 +1476,11 @@ __device__ void Wd::solveTOI(const StepParams& P)
 // (positions, then velocities) and the accumulated impulses of the island contacts when a world's
 // fit, and the broadphase proxies, pair keys and list heads outside the island solve; every use
 // falls back to global memory when the world is larger, so the shape changes speed, never results.
-// Minimum resident CTAs per SM the register allocation must allow at 128 threads (1: no cap).
+// Minimum resident CTAs per SM the register allocation must allow at 128 threads: 3 caps the
+// kernel at 170 registers (measured fastest; uncapped it takes 255, and 128 or fewer cost more in
+// spills than the extra resident worlds gain).
 #ifndef B2G_STEP_MIN_BLOCKS
-#define B2G_STEP_MIN_BLOCKS 1
+#define B2G_STEP_MIN_BLOCKS 3
 #endif
 __global__ void __launch_bounds__(128, B2G_STEP_MIN_BLOCKS) StepKernel(Batch B, StepParams P, const int* schedule, LaunchShape L)
 {
@@ -1392,6 +1503,7 @@ __global__ void __launch_bounds__(128, B2G_STEP_MIN_BLOCKS) StepKernel(Batch B, 
         W.st->residual = 0.0f;
         W.st->warmLearned = 0;
         W.st->velItersSum = 0;
+        W.st->maxPenetration = 0.0f;
         W.st->newFixture = 0;
         for (int i = 0; i < kProfileSlots; ++i) W.st->cyc[i] = 0;
     }

@@ -61,6 +61,7 @@ struct WorldState {
     float residual;     // velocity residual (m/s) after the last step's velocity iterations, when measured
     int warmLearned;    // islands of the last step that kept the learned warm start (its residual was smaller)
     int velItersSum;    // velocity iterations of the last step x island contacts, summed over islands
+    float maxPenetration; // deepest contact penetration (m) before the last step's position correction
     // SM clock cycles of the last step per phase: 0 new-fixture pairs, 1 collide, 2 island DFS,
     // 3 island solve, 4 fixture sync, 5 pairs after solve, 6 TOI, 7 whole step; then the island solve
     // split: 8 integrate + constraint init, 9 warm start + velocity sweeps, 10 impulses + position
@@ -179,6 +180,7 @@ struct Batch {
     int* pairKeep;
     int4* pairInfo;  // pair-sized: a new contact's fixtures and bodies, worked out before creation
     int* movedList;  // proxy-sized
+    int* sweepRank;  // proxy-sized: position of a proxy in the sweep order (large worlds)
 };
 
 // Island solver variants. kSolverPlain is the reference's per-island sequential Gauss-Seidel order

@@ -294,6 +294,71 @@ def config3(n_worlds: int = 4096, seed: int = 1, allow_sleep: bool = True, min_b
     return worlds
 
 
-def config5(n_chains: int = 512, links: int = 16, seed: int = 1, allow_sleep: bool = True) -> Scene:
-    """Revolute-joint chains (limits +/-30 degrees); a reduced stand-in of the joint stress world."""
-    return chains(n_chains, links, SplitMix64(seed), allow_sleep=allow_sleep)
+def config5(n_bodies: int = 65536, n_chains: int = 512, links: int = 16, half: float = 150.0, seed: int = 1,
+            omega: float = 0.05, allow_sleep: bool = True) -> Scene:
+    """The joint stress world: a 2*half square container of 4 edges on one kinematic body spinning
+    at omega rad/s about the container's centre, holding n_bodies dynamic bodies: n_chains chains of
+    `links` revolute-jointed 0.1 x 0.5 m box links (limits +/-30 degrees, no collision inside a
+    chain), and loose bodies, 60% boxes (half-extent U[0.2, 0.8]) and 40% circles (radius
+    U[0.2, 0.8]). Bodies start on a square grid filling the container, one per cell (cell pitch
+    2*half / ceil(sqrt(n_bodies))): a loose body's size is capped at 0.47 of the pitch so none
+    overlap (at 65,536 bodies in 300 m the pitch is 1.17 m, so sizes above 0.55 m are capped), and
+    each chain fills `links` consecutive cells of a grid column, its joints halfway between cells."""
+    rng = SplitMix64(seed)
+    s = Scene(name=f"stress{n_bodies}")
+    cx, cy = 0.0, half
+    k = s.body(KINEMATIC, cx, cy, w=omega)
+    for v in ([-half, -half, half, -half], [half, -half, half, half], [half, half, -half, half], [-half, half, -half, -half]):
+        s.fixture(k, EDGE, v + [0, 0, 0, 0, 0, 0], friction=0.6)
+    g = int(math.ceil(math.sqrt(n_bodies)))
+    pitch = 2.0 * half / g
+    cap = 0.47 * pitch
+    cell = lambda i, j: (_q(cx - half + (i + 0.5) * pitch), _q(cy - half + (j + 0.5) * pitch))
+    rows_per_chain = links
+    chain_cells = set()
+    chains_made = 0
+    col, row = 0, 0
+    while chains_made < n_chains and col < g:
+        if row + rows_per_chain > g:
+            col += 2
+            row = 0
+            continue
+        for r in range(rows_per_chain):
+            chain_cells.add((col, row + r))
+        chains_made += 1
+        row += rows_per_chain + 1
+    # chains first (bodies then joints per chain), then the loose bodies in grid order
+    placed = 0
+    made = 0
+    col, row = 0, 0
+    while made < chains_made:
+        if row + rows_per_chain > g:
+            col += 2
+            row = 0
+            continue
+        prev = None
+        for r in range(rows_per_chain):
+            x, y = cell(col, row + rows_per_chain - 1 - r)
+            b = s.body(DYNAMIC, x, y)
+            s.fixture(b, BOX, [0.1, 0.5], 2, density=1.0, friction=0.4, group=-(made + 1))
+            if prev is not None:
+                s.revolute(prev, b, (0.0, -0.5 * pitch), (0.0, 0.5 * pitch), 0.0, -math.pi / 6.0, math.pi / 6.0, flags=1)
+            prev = b
+            placed += 1
+        made += 1
+        row += rows_per_chain + 1
+    for j in range(g):
+        for i in range(g):
+            if placed >= n_bodies:
+                break
+            if (i, j) in chain_cells:
+                continue
+            x, y = cell(i, j)
+            size = min(rng.uniform(0.2, 0.8), cap)
+            b = s.body(DYNAMIC, x, y, angle=_q(rng.uniform(0.0, 2.0 * math.pi)))
+            if rng.uniform() < 0.6:
+                s.fixture(b, BOX, [_q(size), _q(size)], 2, density=1.0, friction=0.4)
+            else:
+                s.fixture(b, CIRCLE, [0.0, 0.0, _q(size)], 1, density=1.0, friction=0.4)
+            placed += 1
+    return _settings(s, allow_sleep)

@@ -128,6 +128,12 @@ class World:
         _lib.check(self.lib.gb_world_read_contact_log(self.h, x, t, cap, C.byref(n)), "gb_world_read_contact_log")
         return x[:n.value], t[:n.value]
 
+    def max_penetration(self) -> np.ndarray:
+        """Per world: the deepest penetration (m) the last step's position solver started from."""
+        out = np.zeros(self.n_worlds, dtype=np.float32)
+        _lib.check(self.lib.gb_world_contact_stats(self.h, out), "gb_world_contact_stats")
+        return out
+
     def set_stream(self, stream_handle: int) -> None:
         _lib.check(self.lib.gb_world_set_stream(self.h, C.c_void_p(stream_handle)), "gb_world_set_stream")
 

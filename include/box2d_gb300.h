@@ -131,6 +131,10 @@ gb_status gb_world_launch_plan(gb_world* world, int* classes, int cap, int* n_cl
                                int ms_cap, int* n_candidates);
 gb_status gb_world_set_launch_plan(gb_world* world, const int* classes, int n);
 
+/* Per world of the last step (array of n_worlds): the deepest contact penetration (m) the position
+ * solver started from, i.e. minus the smallest separation of its first iteration (0 when none). */
+gb_status gb_world_contact_stats(gb_world* world, float* max_penetration);
+
 /* Binds the handle to a caller-owned cudaStream_t (NULL = the handle's own stream). */
 gb_status gb_world_set_stream(gb_world* world, void* cuda_stream);
 
@@ -238,7 +242,8 @@ gb_status gb_mlp_train(gb_mlp* mlp, const float* x, const float* t, int n, int s
  * the point's normal and tangent effective mass; the effective inverse normal mass; the friction
  * coefficient; 1 for a two-point manifold. The outputs, multiplied by the normal and tangent
  * effective mass, are corrections added to the reference warm-start impulses (the normal result
- * clamped at 0, the tangent one to the friction cone); the network is trained on the logged final
+ * clamped at 0, the tangent one to the friction cone), applied at the points the reference starts
+ * cold (no normal impulse carried over); the network is trained on such logged points, on the final
  * impulses minus the reference warm start (t - x[9..10] in the log's units).
  * Each world then warm-starts its velocities both ways and keeps the one whose velocity residual is
  * smaller, island by island (islands share no dynamic body), so an island falls back to the reference
