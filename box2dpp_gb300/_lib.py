@@ -28,7 +28,8 @@ EXPORTS = [
     "gb_world_launch_plan", "gb_world_set_launch_plan", "gb_world_graph_step",
     "gb_mlp_create", "gb_mlp_destroy", "gb_mlp_param_count", "gb_mlp_set_params", "gb_mlp_get_params",
     "gb_mlp_forward", "gb_mlp_gradients", "gb_mlp_train", "gb_world_set_warm_start", "gb_world_warm_stats",
-    "gb_world_set_contact_log", "gb_world_read_contact_log", "gb_world_contact_stats",
+    "gb_world_set_contact_log", "gb_world_read_contact_log", "gb_world_contact_stats", "gb_world_set_events",
+    "gb_world_read_events", "gb_world_query_aabb", "gb_world_raycast",
 ]
 
 
@@ -105,6 +106,10 @@ def load(build_if_missing: bool = True):
         "gb_world_warm_stats": [vp, _i32, _i32],
         "gb_world_set_contact_log": [vp, i],
         "gb_world_contact_stats": [vp, _f32],
+        "gb_world_set_events": [vp, i],
+        "gb_world_query_aabb": [vp, i, i, _f32, _i32, _i32, i, C.POINTER(i)],
+        "gb_world_raycast": [vp, i, i, _f32, _i32, _f32],
+        "gb_world_read_events": [vp, i, _i32, _f32, i, C.POINTER(i)],
         "gb_world_read_contact_log": [vp, _f32, _f32, i, C.POINTER(i)],
         "gb_mlp_destroy": [vp],
         "gb_mlp_set_params": [vp, _f32n, _f32n, _f32n],

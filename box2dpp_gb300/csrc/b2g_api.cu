@@ -23,6 +23,10 @@ cudaError_t b2gLaunchStep(const b2g::Batch& B, const b2g::StepParams& P, const i
                           int threads, int smemRows, int smemContacts, cudaStream_t stream);
 cudaError_t b2gLaunchSinCos(const float* x, float* s, float* c, int n, cudaStream_t stream);
 b2g::MlpView b2gMlpView(const gb_mlp* m);
+cudaError_t b2gLaunchQueryAabb(const b2g::Batch& B, int w, const float4* boxes, int n, const int* offsets, int* counts,
+                               int* fill, int cap, cudaStream_t stream);
+cudaError_t b2gLaunchRayCast(const b2g::Batch& B, int w, const float4* rays, int n, int* fixture, float* hit,
+                             cudaStream_t stream);
 cudaError_t b2gLaunchCollide(int n, const b2g::Shape* a, const float4* xa, const b2g::Shape* b, const float4* xb,
                              int4* oi, float4* of, cudaStream_t stream);
 
@@ -120,6 +124,7 @@ struct gb_world {
     float tolerance = 0.0f;
     int measureResidual = 0;
     int warmMode = kWarmReference;
+    bool eventsEnabled = false;
     MlpView mlp{};
     float* logX = nullptr;   // contact-point log (device), see gb_world_set_contact_log
     float* logT = nullptr;
@@ -401,6 +406,7 @@ StepParams MakeParams(const gb_world* g, float dt, int vi, int pi)
     P.logT = g->logT;
     P.logCount = g->logCount;
     P.logCap = g->logCap;
+    P.recordEvents = g->eventsEnabled ? 1 : 0;
     return P;
 }
 
@@ -564,6 +570,8 @@ gb_status Upload(gb_world* g)
     ALLOC(sBody, tr); ALLOC(sStack, tb); ALLOC(sWake, tb); ALLOC(sPos, tr); ALLOC(sVel, tr); ALLOC(islands, tb);
     ALLOC(islandJ, tb); ALLOC(sleepOut, tb); ALLOC(rowMask, tr); ALLOC(sVelL, tr);
     ALLOC(sContact, tc); ALLOC(sStatus, tc); ALLOC(vc, tc); ALLOC(pc, tc); ALLOC(vimp, tc); ALLOC(vimpL, tc); ALLOC(vsep, tc); ALLOC(toi, tc); ALLOC(cColour, tc); ALLOC(colourList, tc);
+    ALLOC(evType, tc);
+    if (g->eventsEnabled) { ALLOC(evLog, 8 * tc); } else { B.evLog = nullptr; }
     ALLOC(pairs, tq); ALLOC(pairKeep, tq); ALLOC(pairInfo, tq);
 #undef ALLOC
     GB_CUDA(cudaMemcpy(B.desc, g->desc.data(), nw * sizeof(WorldDesc), cudaMemcpyHostToDevice));
@@ -1009,6 +1017,103 @@ gb_status gb_world_set_warm_start(gb_world* g, gb_mlp* mlp, int mode)
     g->warmMode = mode;
     g->mlp = mode == kWarmLearned ? b2gMlpView(mlp) : MlpView{};
     return GB_OK;
+}
+
+gb_status gb_world_query_aabb(gb_world* g, int w, int n, const float* aabbs, int* offsets, int* fixtures, int cap,
+                             int* total)
+{
+    if (!g || w < 0 || w >= (int)g->worlds.size() || n < 0 || !offsets || !total || cap < 0 || (n > 0 && !aabbs))
+        return GB_ERR_INVALID;
+    gb_status s = Upload(g);
+    if (s != GB_OK) return s;
+    *total = 0;
+    offsets[0] = 0;
+    if (n == 0) return GB_OK;
+    float4* dBoxes = nullptr;
+    int *dCounts = nullptr, *dOffsets = nullptr, *dFill = nullptr;
+    std::vector<int> counts(n);
+    cudaError_t e = cudaMalloc(&dBoxes, n * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc(&dCounts, n * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&dOffsets, (n + 1) * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dBoxes, aabbs, n * sizeof(float4), cudaMemcpyHostToDevice, g->stream);
+    if (e == cudaSuccess) e = b2gLaunchQueryAabb(g->batch, w, dBoxes, n, nullptr, dCounts, nullptr, 0, g->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(counts.data(), dCounts, n * sizeof(int), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e == cudaSuccess) {
+        for (int i = 0; i < n; ++i) offsets[i + 1] = offsets[i] + counts[i];
+        *total = offsets[n];
+        const int m = std::min(*total, cap);
+        if (m > 0 && fixtures) {
+            e = cudaMalloc(&dFill, m * sizeof(int));
+            if (e == cudaSuccess) e = cudaMemcpyAsync(dOffsets, offsets, (n + 1) * sizeof(int), cudaMemcpyHostToDevice, g->stream);
+            if (e == cudaSuccess) e = b2gLaunchQueryAabb(g->batch, w, dBoxes, n, dOffsets, dCounts, dFill, m, g->stream);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(fixtures, dFill, m * sizeof(int), cudaMemcpyDeviceToHost, g->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+        }
+    }
+    cudaFree(dBoxes); cudaFree(dCounts); cudaFree(dOffsets); cudaFree(dFill);
+    GB_CUDA(e);
+    return *total > cap ? GB_ERR_CAPACITY : GB_OK;
+}
+
+gb_status gb_world_raycast(gb_world* g, int w, int n, const float* rays, int* fixture, float* hit)
+{
+    if (!g || w < 0 || w >= (int)g->worlds.size() || n < 0 || (n > 0 && (!rays || !fixture || !hit)))
+        return GB_ERR_INVALID;
+    gb_status s = Upload(g);
+    if (s != GB_OK) return s;
+    if (n == 0) return GB_OK;
+    float4* dRays = nullptr;
+    int* dFix = nullptr;
+    float* dHit = nullptr;
+    cudaError_t e = cudaMalloc(&dRays, n * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc(&dFix, n * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&dHit, 5 * (size_t)n * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dRays, rays, n * sizeof(float4), cudaMemcpyHostToDevice, g->stream);
+    if (e == cudaSuccess) e = b2gLaunchRayCast(g->batch, w, dRays, n, dFix, dHit, g->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fixture, dFix, n * sizeof(int), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hit, dHit, 5 * (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    cudaFree(dRays); cudaFree(dFix); cudaFree(dHit);
+    GB_CUDA(e);
+    return GB_OK;
+}
+
+gb_status gb_world_set_events(gb_world* g, int enable)
+{
+    if (!g) return GB_ERR_INVALID;
+    const bool on = enable != 0;
+    if (on == g->eventsEnabled) return GB_OK;
+    g->eventsEnabled = on;
+    // the log is sized with the device columns: reallocate them (the state is preserved)
+    g->hostDirty = true;
+    return Upload(g);
+}
+
+gb_status gb_world_read_events(gb_world* g, int w, int* records, float* impulses, int cap, int* n)
+{
+    if (!g || !n || cap < 0 || w < 0 || w >= (int)g->worlds.size()) return GB_ERR_INVALID;
+    *n = 0;
+    if (!g->onDevice || !g->eventsEnabled) return GB_OK;
+    GB_CUDA(cudaStreamSynchronize(g->stream));
+    WorldState st;
+    GB_CUDA(cudaMemcpy(&st, g->batch.state + w, sizeof(WorldState), cudaMemcpyDeviceToHost));
+    const int count = std::min(st.eventCount, 4 * g->desc[w].contactCap);
+    *n = count;
+    const int m = std::min(count, cap);
+    if (m > 0) {
+        std::vector<int4> raw(2 * (size_t)m);
+        GB_CUDA(cudaMemcpy(raw.data(), g->batch.evLog + 8 * (size_t)g->desc[w].contactBase, raw.size() * sizeof(int4),
+                           cudaMemcpyDeviceToHost));
+        for (int i = 0; i < m; ++i) {
+            if (records) {
+                records[4 * i] = raw[2 * i].x; records[4 * i + 1] = raw[2 * i].y;
+                records[4 * i + 2] = raw[2 * i].z; records[4 * i + 3] = raw[2 * i].w;
+            }
+            if (impulses) std::memcpy(impulses + 4 * (size_t)i, &raw[2 * i + 1], 4 * sizeof(float));
+        }
+    }
+    return st.eventsDropped ? GB_ERR_CAPACITY : GB_OK;
 }
 
 gb_status gb_world_set_contact_log(gb_world* g, int capacity)

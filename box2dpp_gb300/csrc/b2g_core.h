@@ -853,6 +853,79 @@ B2G_HD void Evaluate(Manifold* m, const Shape& a, const Xf& xfA, const Shape& b,
 }
 
 // ------------------------------------------------------------------ GJK distance (Collision/b2Distance.cpp)
+// ------------------------------------------------------------------ shape ray casts
+// b2Shape::RayCast for one fixture (Collision/Shapes/b2CircleShape.cpp:49-84, b2EdgeShape.cpp:56-116,
+// b2PolygonShape.cpp:270-340), segment p1 -> p2 with maxFraction, shape at transform xf. Returns
+// whether the segment hits the shape, the fraction along it and the world normal.
+B2G_HD bool RayCastShape(const Shape& sh, const Xf& xf, Vec2 p1, Vec2 p2, float maxFraction, float* fraction,
+                         Vec2* normal)
+{
+    if (sh.type == kCircle) {
+        const Vec2 position = xf.p + Mul(xf.q, sh.v[0]);
+        const Vec2 s = p1 - position;
+        const float b = Dot(s, s) - sh.radius * sh.radius;
+        const Vec2 r = p2 - p1;
+        const float c = Dot(s, r);
+        const float rr = Dot(r, r);
+        const float sigma = c * c - rr * b;
+        if (sigma < 0.0f || rr < kEpsilon) return false;
+        float a = -(c + sqrtf(sigma));
+        if (0.0f <= a && a <= maxFraction * rr) {
+            a /= rr;
+            *fraction = a;
+            Vec2 n = s + a * r;
+            Normalize(n);
+            *normal = n;
+            return true;
+        }
+        return false;
+    }
+    const Vec2 q1 = MulT(xf.q, p1 - xf.p);
+    const Vec2 q2 = MulT(xf.q, p2 - xf.p);
+    const Vec2 d = q2 - q1;
+    if (sh.type == kEdge) {
+        const Vec2 v1 = sh.v[0], v2 = sh.v[1];
+        const Vec2 e = v2 - v1;
+        Vec2 n = V(e.y, -e.x);
+        Normalize(n);
+        const float numerator = Dot(n, v1 - q1);
+        const float denominator = Dot(n, d);
+        if (denominator == 0.0f) return false;
+        const float t = numerator / denominator;
+        if (t < 0.0f || maxFraction < t) return false;
+        const Vec2 q = q1 + t * d;
+        const Vec2 r = v2 - v1;
+        const float rr = Dot(r, r);
+        if (rr == 0.0f) return false;
+        const float sEdge = Dot(q - v1, r) / rr;
+        if (sEdge < 0.0f || 1.0f < sEdge) return false;
+        *fraction = t;
+        *normal = numerator > 0.0f ? -Mul(xf.q, n) : Mul(xf.q, n);
+        return true;
+    }
+    float lower = 0.0f, upper = maxFraction;
+    int index = -1;
+    for (int i = 0; i < sh.count; ++i) {
+        const float numerator = Dot(sh.n[i], sh.v[i] - q1);
+        const float denominator = Dot(sh.n[i], d);
+        if (denominator == 0.0f) {
+            if (numerator < 0.0f) return false;
+        } else if (denominator < 0.0f && numerator < lower * denominator) {
+            lower = numerator / denominator;
+            index = i;
+        } else if (denominator > 0.0f && numerator < upper * denominator) {
+            upper = numerator / denominator;
+        }
+        if (upper < lower) return false;
+    }
+    if (index >= 0) {
+        *fraction = lower;
+        *normal = Mul(xf.q, sh.n[index]);
+        return true;
+    }
+    return false;
+}
+
 struct Proxy { const Vec2* v; int count; float radius; };
 B2G_HD Proxy ProxyOf(const Shape& s)
 {

@@ -1001,6 +1001,21 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
         vel_body(b) = make_float4(v4.x, v4.y, v4.z, 0.0f);
         syncTransform(b);
     }
+    // b2Island::Report (b2Island.cpp:344, 518-541): PostSolve for every island contact, islands in
+    // order, with the impulses the velocity iterations ended with
+    if (evLog) {
+        const int base = st->eventCount;
+        __syncthreads();
+        for (int i = tid(); i < nContacts; i += nthreads()) {
+            const int4 info = ci[sContact[i]];
+            const float4 im = imp[i];
+            const int n = vc[i].idx.z;
+            putEvent(base + i, kEvPostSolve, info.y, info.z, n, n > 0 ? im.x : 0.0f, n > 1 ? im.z : 0.0f,
+                     n > 0 ? im.y : 0.0f, n > 1 ? im.w : 0.0f);
+        }
+        __syncthreads();
+        if (tid() == 0) st->eventCount = base + nContacts;
+    }
     __syncthreads();
     if (tid() == 0) { unsigned long long now = clock64(); st->cyc[12] = now - tStamp; tStamp = now; }
     // sleep (b2Island.cpp:346-383), per island

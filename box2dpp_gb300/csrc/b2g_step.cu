@@ -58,6 +58,9 @@ struct Wd {
     int* sleepOut;
     int* cColour;
     int* colourList;
+    int* evType;
+    int4* evLog;
+    int evCap;
     unsigned long long* rowMask;
     unsigned long long* pairs;
     int* pairKeep;
@@ -85,10 +88,34 @@ struct Wd {
         islands = B.islands + b; islandJ = B.islandJ + b; sleepOut = B.sleepOut + b;
         sContact = B.sContact + c; sStatus = B.sStatus + c; vc = B.vc + c; pc = B.pc + c; vimp = B.vimp + c; toi = B.toi + c;
         vimpL = B.vimpL + c; vsep = B.vsep + c;
-        cColour = B.cColour + c; colourList = B.colourList + c;
+        cColour = B.cColour + c; colourList = B.colourList + c; evType = B.evType + c;
+        evLog = B.evLog ? B.evLog + 8 * (size_t)c : nullptr;
+        evCap = 4 * d.contactCap;
         pairs = B.pairs + q; pairKeep = B.pairKeep + q; pairInfo = B.pairInfo + q;
         smemBase = nullptr;
         smemBytes = 0;
+    }
+
+    // ---------------------------------------------------------------- listener event log
+    __device__ void putEvent(int slot, int kind, int fA, int fB, int count = 0, float n0 = 0.0f, float n1 = 0.0f,
+                             float t0 = 0.0f, float t1 = 0.0f)
+    {
+        if (slot >= evCap) { st->eventsDropped = 1; return; }
+        evLog[2 * slot] = make_int4(kind, fA, fB, count);
+        evLog[2 * slot + 1] = make_int4(__float_as_int(n0), __float_as_int(n1), __float_as_int(t0), __float_as_int(t1));
+    }
+    // the calls b2Contact::Update makes (Dynamics/Contacts/b2Contact.cpp:164-236), as bits: 1 begin,
+    // 2 end, 4 pre-solve
+    __device__ static int updateEventBits(bool wasTouching, bool touching, bool sensor)
+    {
+        return (!wasTouching && touching ? 1 : 0) | (wasTouching && !touching ? 2 : 0) | (!sensor && touching ? 4 : 0);
+    }
+    // serial append of a contact's update calls (one thread)
+    __device__ void appendUpdateEvents(int c, int bits)
+    {
+        const int4 info = ci[c];
+        for (int b = 0; b < 3; ++b)
+            if (bits & (1 << b)) putEvent(st->eventCount++, b, info.y, info.z);
     }
 
     // ---------------------------------------------------------------- body helpers
@@ -720,7 +747,8 @@ __device__ void Wd::collide()
     // two shape slots per thread in the dynamic shared memory (free during this phase) when it fits
     Shape* shapeSlots = (int)(2 * sizeof(Shape)) * nthreads() <= smemBytes ? reinterpret_cast<Shape*>(smemBase) : nullptr;
     for (int b = tid(); b < d.bodyCount; b += nthreads()) sWake[b] = awake(b) ? -1 : INT_MAX;
-    for (int k = tid(); k < n; k += nthreads()) sStatus[k] = 0;
+    const bool rec = evLog != nullptr;
+    for (int k = tid(); k < n; k += nthreads()) { sStatus[k] = 0; evType[k] = 0; }
     __syncthreads();
     for (int round = 0; round <= n + 1; ++round) {
         if (tid() == 0) sChanged = 0;
@@ -735,6 +763,7 @@ __device__ void Wd::collide()
                 bool keep = shouldCollide(bB, bA) && filterCollide(info.y, info.z);
                 if (!keep) {
                     sStatus[k] = 2;
+                    if (rec && (info.x & kCTouching)) evType[k] = 2;
                     if (mh[c].y > 0 && !sensor) {
                         if (atomicMin(&sWake[bA], k) > k) sChanged = 1;
                         if (atomicMin(&sWake[bB], k) > k) sChanged = 1;
@@ -748,6 +777,7 @@ __device__ void Wd::collide()
             if (!activeA && !activeB) continue;
             if (!Overlap(fat[fi[info.y].z], fat[fi[info.z].z])) {
                 sStatus[k] = 2;
+                if (rec && (info.x & kCTouching)) evType[k] = 2;
                 if (mh[c].y > 0 && !sensor) {
                     if (atomicMin(&sWake[bA], k) > k) sChanged = 1;
                     if (atomicMin(&sWake[bB], k) > k) sChanged = 1;
@@ -755,7 +785,9 @@ __device__ void Wd::collide()
                 continue;
             }
             sStatus[k] = 1;
-            if (update(c, shapeSlots ? shapeSlots + 2 * tid() : nullptr)) {
+            const bool updated = update(c, shapeSlots ? shapeSlots + 2 * tid() : nullptr);
+            if (rec) evType[k] = updateEventBits((info.x & kCTouching) != 0, (ci[c].x & kCTouching) != 0, sensor);
+            if (updated) {
                 if (atomicMin(&sWake[bA], k) > k) sChanged = 1;
                 if (atomicMin(&sWake[bB], k) > k) sChanged = 1;
             }
@@ -768,6 +800,34 @@ __device__ void Wd::collide()
         if (wk != -1 && wk != INT_MAX) setAwake(b, true);
     }
     __syncthreads();
+    // Listener calls of the collide phase in list order (b2ContactManager::Collide visits the list in
+    // order; each contact's Update or Destroy makes its calls), appended to the event log.
+    if (rec) {
+        __shared__ int sEvOff[kMaxCta + 1];
+        const int T = nthreads(), t = tid();
+        const int chunk = (n + T - 1) / T;
+        const int lo = min(n, t * chunk), hi = min(n, lo + chunk);
+        int cnt = 0;
+        for (int k = lo; k < hi; ++k) cnt += __popc(evType[k] & 7);
+        sEvOff[t + 1] = cnt;
+        __syncthreads();
+        if (t == 0) {
+            sEvOff[0] = st->eventCount;
+            for (int i = 1; i <= T; ++i) sEvOff[i] += sEvOff[i - 1];
+        }
+        __syncthreads();
+        int slot = sEvOff[t];
+        for (int k = lo; k < hi; ++k) {
+            const int bits = evType[k] & 7;
+            if (!bits) continue;
+            const int4 info = ci[order[k]];
+            for (int b = 0; b < 3; ++b)
+                if (bits & (1 << b)) putEvent(slot++, b, info.y, info.z);
+        }
+        __syncthreads();
+        if (t == 0) st->eventCount = sEvOff[T];
+        __syncthreads();
+    }
     // Survivors keep their relative order; destroyed contacts are unlinked in list order.
     int* kept = sContact;
     int* gone = pairKeep;
@@ -1334,7 +1394,13 @@ __device__ void Wd::solveTOI(const StepParams& P)
             Sweep backup1 = sweep(bA), backup2 = sweep(bB);
             advance(bA, minAlpha);
             advance(bB, minAlpha);
-            update(mc);
+            {
+                const int before = ci[mc].x;
+                update(mc);
+                if (evLog)
+                    appendUpdateEvents(mc, updateEventBits((before & kCTouching) != 0, (ci[mc].x & kCTouching) != 0,
+                                                           fi[ci[mc].y].w != 0 || fi[ci[mc].z].w != 0));
+            }
             ci[mc].x &= ~kCToi;
             ci[mc].w += 1;
             int fl = ci[mc].x;
@@ -1376,6 +1442,9 @@ __device__ void Wd::solveTOI(const StepParams& P)
                         Sweep backup = sweep(other);
                         if ((bi[other].y & kBIsland) == 0) advance(other, minAlpha);
                         update(c);
+                        if (evLog)
+                            appendUpdateEvents(c, updateEventBits((ic.x & kCTouching) != 0, (ci[c].x & kCTouching) != 0,
+                                                                  fi[ic.y].w != 0 || fi[ic.z].w != 0));
                         int fc = ci[c].x;
                         if ((fc & kCEnabled) == 0 || (fc & kCTouching) == 0) {
                             setSweep(other, backup);
@@ -1445,6 +1514,16 @@ __device__ void Wd::solveTOI(const StepParams& P)
                     vel[b] = make_float4(v4.x, v4.y, v4.z, 0.0f);
                     syncTransform(b);
                 }
+                // b2Island::Report of the sub-step island (b2Island.cpp:515): PostSolve with the TOI
+                // velocity impulses, which are not stored in the manifolds
+                if (evLog)
+                    for (int i = 0; i < nContacts; ++i) {
+                        const int4 ic = ci[sContact[i]];
+                        const float4 im = mImp[i];
+                        const int pcn = mVc[i].idx.z;
+                        putEvent(st->eventCount++, kEvPostSolve, ic.y, ic.z, pcn, pcn > 0 ? im.x : 0.0f,
+                                 pcn > 1 ? im.z : 0.0f, pcn > 0 ? im.y : 0.0f, pcn > 1 ? im.w : 0.0f);
+                    }
                 stamp(19);
                 for (int i = 0; i < nBodies; ++i) {
                     int b = sBody[i];
@@ -1504,6 +1583,8 @@ __global__ void __launch_bounds__(128, B2G_STEP_MIN_BLOCKS) StepKernel(Batch B, 
         W.st->warmLearned = 0;
         W.st->velItersSum = 0;
         W.st->maxPenetration = 0.0f;
+        W.st->eventCount = 0;
+        W.st->eventsDropped = 0;
         W.st->newFixture = 0;
         for (int i = 0; i < kProfileSlots; ++i) W.st->cyc[i] = 0;
     }

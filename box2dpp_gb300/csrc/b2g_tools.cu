@@ -60,3 +60,85 @@ cudaError_t b2gLaunchCollide(int n, const b2g::Shape* a, const float4* xa, const
     if (e != cudaSuccess) return e;
     return cudaStreamSynchronize(stream);
 }
+
+// ------------------------------------------------------------------ world queries
+// b2World::QueryAABB and b2World::RayCast (Dynamics/b2World.cpp:965-1020) over one world of a batch,
+// one thread per query.
+#include "b2g_world.h"
+
+namespace b2g {
+
+// The fixtures whose broadphase fat AABB overlaps the query box (b2DynamicTree::Query reports every
+// leaf whose box passes b2TestOverlap), in fixture order; fill == nullptr only counts them.
+__global__ void QueryAabbKernel(Batch B, int w, const float4* boxes, int n, const int* offsets, int* counts,
+                                int* fill, int cap)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const WorldDesc d = B.desc[w];
+    const float4 q = boxes[i];
+    int k = 0;
+    for (int f = 0; f < d.fixCount; ++f) {
+        const int proxy = B.fi[d.fixBase + f].z;
+        if (proxy < 0) continue;
+        if (!Overlap(B.fat[d.proxyBase + proxy], q)) continue;
+        if (fill) {
+            const int slot = offsets[i] + k;
+            if (slot < cap) fill[slot] = f;
+        }
+        ++k;
+    }
+    if (!fill) counts[i] = k;
+}
+
+// The closest fixture hit by each segment p1 -> p2 (b2World::RayCast with a callback that clips the
+// ray to every reported fraction): the smallest fraction over all fixtures, ties to the lowest
+// fixture index; hit = fraction, point (1 - f) p1 + f p2, normal.
+__global__ void RayCastKernel(Batch B, int w, const float4* rays, int n, int* fixture, float* hit)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const WorldDesc d = B.desc[w];
+    const float4 r = rays[i];
+    const Vec2 p1 = V(r.x, r.y), p2 = V(r.z, r.w);
+    int best = -1;
+    float bestF = 0.0f;
+    Vec2 bestN = V(0.0f, 0.0f);
+    for (int f = 0; f < d.fixCount; ++f) {
+        const int body = B.fi[d.fixBase + f].x;
+        const float4 x = B.xf[d.bodyBase + body];
+        Xf xf;
+        xf.p = V(x.x, x.y);
+        xf.q.s = x.z;
+        xf.q.c = x.w;
+        float fr;
+        Vec2 nrm;
+        if (!RayCastShape(B.shape[d.fixBase + f], xf, p1, p2, 1.0f, &fr, &nrm)) continue;
+        if (best < 0 || fr < bestF) { best = f; bestF = fr; bestN = nrm; }
+    }
+    fixture[i] = best;
+    const Vec2 pt = best >= 0 ? (1.0f - bestF) * p1 + bestF * p2 : V(0.0f, 0.0f);
+    hit[5 * i] = bestF;
+    hit[5 * i + 1] = pt.x;
+    hit[5 * i + 2] = pt.y;
+    hit[5 * i + 3] = bestN.x;
+    hit[5 * i + 4] = bestN.y;
+}
+
+} // namespace b2g
+
+cudaError_t b2gLaunchQueryAabb(const b2g::Batch& B, int w, const float4* boxes, int n, const int* offsets, int* counts,
+                               int* fill, int cap, cudaStream_t stream)
+{
+    if (n <= 0) return cudaSuccess;
+    b2g::QueryAabbKernel<<<(n + 127) / 128, 128, 0, stream>>>(B, w, boxes, n, offsets, counts, fill, cap);
+    return cudaGetLastError();
+}
+
+cudaError_t b2gLaunchRayCast(const b2g::Batch& B, int w, const float4* rays, int n, int* fixture, float* hit,
+                             cudaStream_t stream)
+{
+    if (n <= 0) return cudaSuccess;
+    b2g::RayCastKernel<<<(n + 127) / 128, 128, 0, stream>>>(B, w, rays, n, fixture, hit);
+    return cudaGetLastError();
+}

@@ -62,6 +62,8 @@ struct WorldState {
     int warmLearned;    // islands of the last step that kept the learned warm start (its residual was smaller)
     int velItersSum;    // velocity iterations of the last step x island contacts, summed over islands
     float maxPenetration; // deepest contact penetration (m) before the last step's position correction
+    int eventCount;     // listener records of the last step in the world's event log
+    int eventsDropped;  // 1 when the log ran out of room
     // SM clock cycles of the last step per phase: 0 new-fixture pairs, 1 collide, 2 island DFS,
     // 3 island solve, 4 fixture sync, 5 pairs after solve, 6 TOI, 7 whole step; then the island solve
     // split: 8 integrate + constraint init, 9 warm start + velocity sweeps, 10 impulses + position
@@ -174,6 +176,10 @@ struct Batch {
     int* sJoint;     // joint-sized
     int* sleepOut;   // per island: 1 when the island fell asleep
     int* cColour;    // contact-sized: colour of each island contact (coloured solver)
+    int* evType;     // contact-sized: listener calls of each list position in the collide phase
+    int4* evLog;     // 4 x contact-sized records of 2 int4, or nullptr when events are off: the step's
+                     // listener calls {kind 0 begin, 1 end, 2 pre-solve, 3 post-solve, fixtureA,
+                     // fixtureB, impulse points} {normal impulse 0, 1, tangent impulse 0, 1}
     int* colourList; // contact-sized: island contacts grouped by colour
     unsigned long long* rowMask; // row-sized: colours used at each island body row
     unsigned long long* pairs; // pair-sized sort keys (proxyA << 32 | proxyB)
@@ -188,6 +194,8 @@ struct Batch {
 // constraints of one colour share no dynamic body and are solved in parallel across the CTA.
 enum : int { kSolverPlain = 0, kSolverColoured = 1 };
 enum : int { kWarmReference = 0, kWarmLearned = 1 };
+// b2ContactListener calls (Dynamics/b2WorldCallbacks.h:84-130) as event log kinds
+enum : int { kEvBegin = 0, kEvEnd = 1, kEvPreSolve = 2, kEvPostSolve = 3 };
 // Colours 0..62 are solved in parallel; colour 63 collects the constraints for which no colour was
 // free and is solved by one thread in island order.
 constexpr int kColours = 64;
@@ -205,6 +213,7 @@ struct StepParams {
     int solver;         // kSolverPlain or kSolverColoured
     float tolerance;    // > 0: stop the velocity iterations once the velocity residual is <= tolerance
     int measureResidual;// 1: record the velocity residual after the velocity iterations
+    int recordEvents;   // 1: record the listener calls of the step in the event log
     int warmMode;       // kWarmReference, or kWarmLearned (the network below, reference as fallback)
     MlpView mlp;
     // contact-point log (plain solver): features at the start of the velocity solve, then the

@@ -134,6 +134,47 @@ class World:
         _lib.check(self.lib.gb_world_contact_stats(self.h, out), "gb_world_contact_stats")
         return out
 
+    def set_events(self, on: bool = True) -> None:
+        """Record the listener calls of every step on the device (see gb_world_set_events)."""
+        _lib.check(self.lib.gb_world_set_events(self.h, int(on)), "gb_world_set_events")
+
+    def events(self, w: int = 0):
+        """(records [n][4] = kind, fixtureA, fixtureB, impulse points; impulses [n][4] = n0, n1, t0, t1) of
+        the last step."""
+        n = C.c_int()
+        _lib.check(self.lib.gb_world_read_events(self.h, w, np.zeros(4, np.int32), np.zeros(4, np.float32), 0,
+                                                 C.byref(n)), "gb_world_read_events")
+        cnt = n.value
+        rec = np.zeros((max(cnt, 1), 4), dtype=np.int32)
+        imp = np.zeros((max(cnt, 1), 4), dtype=np.float32)
+        _lib.check(self.lib.gb_world_read_events(self.h, w, rec, imp, cnt, C.byref(n)), "gb_world_read_events")
+        return rec[:cnt], imp[:cnt]
+
+    def query_aabb(self, boxes, w: int = 0):
+        """Fixture indices whose fat AABB overlaps each box (lower.x, lower.y, upper.x, upper.y): a list
+        of arrays, one per box (see gb_world_query_aabb)."""
+        boxes = np.ascontiguousarray(np.asarray(boxes, dtype=np.float32).reshape(-1, 4))
+        n = len(boxes)
+        offsets = np.zeros(n + 1, dtype=np.int32)
+        total = C.c_int()
+        status = self.lib.gb_world_query_aabb(self.h, w, n, boxes, offsets, np.zeros(1, np.int32), 0, C.byref(total))
+        if status not in (_lib.GB_OK, _lib.GB_ERR_CAPACITY):
+            _lib.check(status, "gb_world_query_aabb")
+        fixtures = np.zeros(max(total.value, 1), dtype=np.int32)
+        _lib.check(self.lib.gb_world_query_aabb(self.h, w, n, boxes, offsets, fixtures, total.value, C.byref(total)),
+                   "gb_world_query_aabb")
+        return [fixtures[offsets[i]:offsets[i + 1]].copy() for i in range(n)]
+
+    def raycast(self, rays, w: int = 0):
+        """Closest hit per segment (p1.x, p1.y, p2.x, p2.y): (fixture or -1, [fraction, point.x, point.y,
+        normal.x, normal.y]) arrays (see gb_world_raycast)."""
+        rays = np.ascontiguousarray(np.asarray(rays, dtype=np.float32).reshape(-1, 4))
+        n = len(rays)
+        fixture = np.zeros(max(n, 1), dtype=np.int32)
+        hit = np.zeros((max(n, 1), 5), dtype=np.float32)
+        _lib.check(self.lib.gb_world_raycast(self.h, w, n, rays, fixture, hit), "gb_world_raycast")
+        return fixture[:n], hit[:n]
+
     def set_stream(self, stream_handle: int) -> None:
         _lib.check(self.lib.gb_world_set_stream(self.h, C.c_void_p(stream_handle)), "gb_world_set_stream")
 

@@ -138,6 +138,33 @@ gb_status gb_world_contact_stats(gb_world* world, float* max_penetration);
 /* Binds the handle to a caller-owned cudaStream_t (NULL = the handle's own stream). */
 gb_status gb_world_set_stream(gb_world* world, void* cuda_stream);
 
+/* b2ContactListener (Box2D/Dynamics/b2WorldCallbacks.h:84-130) as a device event log. With events
+ * on, every step records, per world and in the reference's call order, the listener calls
+ * b2World::Step would make: records[4] = kind (0 BeginContact, 1 EndContact, 2 PreSolve,
+ * 3 PostSolve), fixtureA, fixtureB, and for a PostSolve b2ContactImpulse::count; impulses[4] = the
+ * PostSolve's normal impulses 0, 1 and tangent impulses 0, 1 (zero otherwise). Order: the collide phase in contact-list order
+ * (Update's Begin/End then PreSolve, or Destroy's End), then PostSolve per solved island in island
+ * order, then the continuous phase's calls in event order. gb_world_set_events(1) reallocates the
+ * device columns (the state is kept); gb_world_read_events reads the last step's records of world w
+ * (up to cap; *n receives the count) and returns GB_ERR_CAPACITY if the log overflowed. PreSolve is
+ * recorded as a notification: a listener sees it after the step and cannot change the contact. */
+gb_status gb_world_set_events(gb_world* world, int enable);
+gb_status gb_world_read_events(gb_world* world, int w, int* records, float* impulses, int cap, int* n);
+
+/* World queries on the device (b2World::QueryAABB, b2World::RayCast: Box2D/Dynamics/b2World.h:116-124,
+ * b2World.cpp:965-1020), run after the queued steps. gb_world_query_aabb: for n boxes aabbs[4] =
+ * lower.x, lower.y, upper.x, upper.y, the fixtures whose broadphase fat AABB overlaps the box (the
+ * leaves b2DynamicTree::Query reports), in fixture order: query i's fixtures are
+ * fixtures[offsets[i] .. offsets[i + 1]) (offsets has n + 1 entries); *total receives the number of
+ * results, GB_ERR_CAPACITY when it exceeds cap (offsets stay valid). gb_world_raycast: for n segments
+ * rays[4] = p1.x, p1.y, p2.x, p2.y, the closest hit as a callback that returns each reported
+ * fraction gets it: fixture[i] (-1 when none), hit[5] = fraction, point.x, point.y, normal.x,
+ * normal.y (b2RayCastOutput and the reported point); equal fractions resolve to the lowest fixture
+ * index (the reference keeps the last one its tree traversal reports). Sensors are included. */
+gb_status gb_world_query_aabb(gb_world* world, int w, int n, const float* aabbs, int* offsets, int* fixtures, int cap,
+                             int* total);
+gb_status gb_world_raycast(gb_world* world, int w, int n, const float* rays, int* fixture, float* hit);
+
 /* Counts (b2World::GetBodyCount, GetContactCount, GetProxyCount: b2World.h:160-170). */
 gb_status gb_world_counts(gb_world* world, int w, int* bodies, int* fixtures, int* contacts, int* joints);
 

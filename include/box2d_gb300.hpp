@@ -12,10 +12,9 @@
 //    take effect when the device world is created, at the first Step;
 //  - bodies, fixtures and joints are created but never destroyed (the reference's Destroy* calls
 //    are not part of this API);
-//  - b2ContactListener receives BeginContact/EndContact after each Step, derived from which fixture
-//    pairs touch before and after the step: all EndContact calls first, in the previous contact list
-//    order, then all BeginContact calls in the new list order (the reference interleaves them inside
-//    Step); PreSolve and PostSolve are not called.
+//  - b2ContactListener calls are recorded on the device during the step, in the reference's order,
+//    and made after it: BeginContact, EndContact, PreSolve (a notification: the contact can no longer
+//    be changed for this step) and PostSolve with the solver's impulses.
 #pragma once
 
 #include <cmath>
@@ -276,11 +275,19 @@ private:
     b2Manifold m_manifold;
 };
 
+struct b2ContactImpulse {
+    float normalImpulses[2] = {0.0f, 0.0f};
+    float tangentImpulses[2] = {0.0f, 0.0f};
+    int count = 0;
+};
+
 class b2ContactListener {
 public:
     virtual ~b2ContactListener() = default;
     virtual void BeginContact(b2Contact*) {}
     virtual void EndContact(b2Contact*) {}
+    virtual void PreSolve(b2Contact*, const b2Manifold*) {}
+    virtual void PostSolve(b2Contact*, const b2ContactImpulse*) {}
 };
 
 class b2World {
@@ -343,7 +350,10 @@ public:
     void Step(float timeStep, int velocityIterations, int positionIterations)
     {
         if (!Handle()) return;
-        if (m_listener && m_contacts.empty()) ReadContacts();  // the touching state before the step
+        if (m_listener) {
+            if (!m_eventsOn) m_eventsOn = gb_world_set_events(m_h, 1) == GB_OK;
+            ReadContacts();  // the contacts before the step: destroyed contacts and old manifolds
+        }
         if (m_forcesDirty) {
             gb_world_upload(m_h);
             gb_set_forces(m_h, m_forces.data());
@@ -457,19 +467,37 @@ private:
     }
     void Report()
     {
-        std::map<std::pair<int, int>, int> before;
         std::vector<std::unique_ptr<b2Contact>> old = std::move(m_contacts);
-        auto key = [](const b2Contact& c) { return std::make_pair(c.m_a->GetIndex(), c.m_b->GetIndex()); };
-        for (size_t i = 0; i < old.size(); ++i)
-            if (old[i]->IsTouching()) before[key(*old[i])] = (int)i;
         ReadContacts();
-        std::map<std::pair<int, int>, bool> after;
-        for (auto& c : m_contacts)
-            if (c->IsTouching()) after[key(*c)] = true;
-        for (auto& c : old)
-            if (c->IsTouching() && !after.count(key(*c))) m_listener->EndContact(c.get());
-        for (auto& c : m_contacts)
-            if (c->IsTouching() && !before.count(key(*c))) m_listener->BeginContact(c.get());
+        std::map<std::pair<int, int>, b2Contact*> now, before;
+        for (auto& c : m_contacts) now[{c->m_a->GetIndex(), c->m_b->GetIndex()}] = c.get();
+        for (auto& c : old) before[{c->m_a->GetIndex(), c->m_b->GetIndex()}] = c.get();
+        int n = 0;
+        gb_world_read_events(m_h, 0, nullptr, nullptr, 0, &n);
+        std::vector<int> rec(4 * (size_t)(n > 0 ? n : 1));
+        std::vector<float> imp(4 * (size_t)(n > 0 ? n : 1));
+        if (n > 0) gb_world_read_events(m_h, 0, rec.data(), imp.data(), n, &n);
+        const b2Manifold empty;
+        for (int i = 0; i < n; ++i) {
+            const std::pair<int, int> key{rec[4 * i + 1], rec[4 * i + 2]};
+            auto itNow = now.find(key);
+            auto itOld = before.find(key);
+            b2Contact* c = itNow != now.end() ? itNow->second : (itOld != before.end() ? itOld->second : nullptr);
+            if (!c) continue;
+            switch (rec[4 * i]) {
+            case 0: m_listener->BeginContact(c); break;
+            case 1: m_listener->EndContact(itOld != before.end() && itNow == now.end() ? itOld->second : c); break;
+            case 2: m_listener->PreSolve(c, itOld != before.end() ? &itOld->second->m_manifold : &empty); break;
+            default: {
+                b2ContactImpulse ci;
+                ci.count = rec[4 * i + 3];
+                ci.normalImpulses[0] = imp[4 * i]; ci.normalImpulses[1] = imp[4 * i + 1];
+                ci.tangentImpulses[0] = imp[4 * i + 2]; ci.tangentImpulses[1] = imp[4 * i + 3];
+                m_listener->PostSolve(c, &ci);
+            }
+            }
+        }
+        m_old = std::move(old);  // kept alive: a listener may hold the pointers until the next Step
     }
 
     b2Vec2 m_gravity;
@@ -479,7 +507,8 @@ private:
     std::vector<std::unique_ptr<b2Body>> m_bodies;
     std::vector<std::unique_ptr<b2Fixture>> m_fixtures;
     std::vector<std::unique_ptr<b2Joint>> m_joints;
-    std::vector<std::unique_ptr<b2Contact>> m_contacts;
+    std::vector<std::unique_ptr<b2Contact>> m_contacts, m_old;
+    bool m_eventsOn = false;
     std::vector<b2Contact*> m_contactView;
     std::vector<float> m_state, m_forces;
     bool m_stale = true, m_forcesDirty = false;

@@ -70,6 +70,9 @@ def _declare(lib, p: str) -> None:
         "sincosf": (None, [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
         "step_many": (None, [C.POINTER(vp), C.c_int, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int]),
     }
+    if p == "rw_":
+        sig["query_aabb"] = (C.c_int, [vp, _f32p, _i32p, C.c_int])
+        sig["raycast"] = (C.c_int, [vp, _f32p, _f32p])
     if p == "po_":
         sig["set_trig"] = (None, [C.c_int])
         sig["record_events"] = (None, [vp, C.c_int])
@@ -169,6 +172,23 @@ class OracleWorld:
         out = np.zeros((max(n, 1), 2), dtype=np.int32)
         self._fn("get_pairs")(self.h, out, n)
         return out[:n]
+
+    def query_aabb(self, box):
+        """Fixture indices the reference reports for the box (lower.x, lower.y, upper.x, upper.y), sorted
+        (reference build only)."""
+        box = np.ascontiguousarray(box, dtype=np.float32)
+        fn = self._fn("query_aabb")
+        n = fn(self.h, box, np.zeros(1, np.int32), 0)
+        out = np.zeros(max(n, 1), dtype=np.int32)
+        fn(self.h, box, out, n)
+        return out[:n]
+
+    def raycast(self, ray):
+        """(fixture or -1, [fraction, point.x, point.y, normal.x, normal.y]) of the closest hit
+        (reference build only)."""
+        hit = np.zeros(5, dtype=np.float32)
+        f = self._fn("raycast")(self.h, np.ascontiguousarray(ray, dtype=np.float32), hit)
+        return f, hit
 
     def record_events(self, on: bool = True) -> None:
         self._fn("record_events")(self.h, int(on))

@@ -340,6 +340,40 @@ void rw_toi(int typeA, const float* sA, int nA, const float* swA,
 
 void rw_sincosf(float x, float* s, float* c) { b2Rot q(x); *s = q.s; *c = q.c; }
 
+// b2World::QueryAABB: the fixtures the reference reports for the box, sorted by creation index.
+int rw_query_aabb(void* h, const float* box, int* out, int cap)
+{
+    struct Collect : b2QueryCallback {
+        std::vector<int> hits;
+        bool ReportFixture(b2Fixture* f) override { hits.push_back(fixture_index(f)); return true; }
+    } cb;
+    b2AABB aabb;
+    aabb.lowerBound.Set(box[0], box[1]);
+    aabb.upperBound.Set(box[2], box[3]);
+    static_cast<RefWorld*>(h)->world.QueryAABB(&cb, aabb);
+    std::sort(cb.hits.begin(), cb.hits.end());
+    for (int i = 0; i < (int)cb.hits.size() && i < cap; ++i) out[i] = cb.hits[i];
+    return (int)cb.hits.size();
+}
+
+// b2World::RayCast with a closest-hit callback (returns each reported fraction): the last report.
+int rw_raycast(void* h, const float* ray, float* hit)
+{
+    struct Closest : b2RayCastCallback {
+        int fixture = -1;
+        float out[5] = {0, 0, 0, 0, 0};
+        float32 ReportFixture(b2Fixture* f, const b2Vec2& point, const b2Vec2& normal, float32 fraction) override
+        {
+            fixture = fixture_index(f);
+            out[0] = fraction; out[1] = point.x; out[2] = point.y; out[3] = normal.x; out[4] = normal.y;
+            return fraction;
+        }
+    } cb;
+    static_cast<RefWorld*>(h)->world.RayCast(&cb, b2Vec2(ray[0], ray[1]), b2Vec2(ray[2], ray[3]));
+    for (int i = 0; i < 5; ++i) hit[i] = cb.out[i];
+    return cb.fixture;
+}
+
 // Steps many independent reference worlds on `threads` host threads. The reference fills its
 // contact-type registry lazily on the first b2Contact::Create (Dynamics/Contacts/b2Contact.cpp:74-78),
 // so one contact is created on the calling thread first.

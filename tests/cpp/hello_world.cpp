@@ -9,9 +9,16 @@
 using namespace box2d;
 
 struct Counter : b2ContactListener {
-    int begins = 0, ends = 0;
+    int begins = 0, ends = 0, presolves = 0, postsolves = 0;
+    float lastNormalImpulse = 0.0f;
     void BeginContact(b2Contact*) override { ++begins; }
     void EndContact(b2Contact*) override { ++ends; }
+    void PreSolve(b2Contact*, const b2Manifold*) override { ++presolves; }
+    void PostSolve(b2Contact*, const b2ContactImpulse* impulse) override
+    {
+        ++postsolves;
+        lastNormalImpulse = impulse->normalImpulses[0];
+    }
 };
 
 int main()
@@ -45,7 +52,8 @@ int main()
         const b2Vec2 p = body->GetPosition();
         std::printf("%d %a %a %a\n", i, p.x, p.y, body->GetAngle());
     }
-    std::printf("contacts %d begin %d end %d awake %d\n", world.GetContactCount(), counter.begins, counter.ends,
-                body->IsAwake() ? 1 : 0);
+    std::printf("contacts %d begin %d end %d awake %d presolve %d postsolve %d impulse %a\n", world.GetContactCount(),
+                counter.begins, counter.ends, body->IsAwake() ? 1 : 0, counter.presolves, counter.postsolves,
+                counter.lastNormalImpulse);
     return 0;
 }

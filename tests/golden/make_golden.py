@@ -1,7 +1,7 @@
 """Generate the golden vectors under tests/golden/ from the UNMODIFIED reference (box2dref compiled by
 oracle/Makefile from the reference tree). Run where the reference tree exists:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [--queries]
 
 Two builds of the reference are used: ``libm`` (glibc sinf/cosf, the reference as shipped) and
 ``project`` (the same objects with sinf/cosf/sincosf resolved to the project trig). Fixtures:
@@ -12,11 +12,14 @@ Two builds of the reference are used: ``libm`` (glibc sinf/cosf, the reference a
 * ``collide.npz``: seeded shape pairs of every supported type pair with the reference manifolds.
 * ``toi.npz``: seeded sweeps with the reference b2TimeOfImpact result.
 * ``trig.npz``: glibc sinf/cosf on seeded angles (how far the project trig is from libm).
+* ``query_<scene>.npz``: b2World::QueryAABB and closest-hit b2World::RayCast results on a stepped
+  scene (project trig) for seeded boxes and segments (``--queries`` writes only these).
 """
 from __future__ import annotations
 
 import hashlib
 import math
+import zlib
 import os
 import sys
 
@@ -161,6 +164,55 @@ def make_toi(n: int = 1500):
                         state=np.array([o[0] for o in outs], np.int32), t=np.array([o[1] for o in outs], np.float32))
 
 
+def query_scenes():
+    """Scenes the world-query golden vectors are taken on, with the steps run before the queries."""
+    return [
+        ("drop300", lambda: scenes.drop(300, scenes.SplitMix64(7)), 90),
+        ("pyramid20", lambda: scenes.config1(), 60),
+        ("chains", lambda: chains_with_load(), 60),
+        ("batch3", lambda: batch_world(3), 60),
+    ]
+
+
+def make_queries(n_boxes: int = 300, n_rays: int = 600):
+    """b2World::QueryAABB and closest-hit b2World::RayCast results of the reference (project trig) on
+    stepped scenes, for seeded boxes and segments over each scene's extent."""
+    out = {}
+    for name, make, steps in query_scenes():
+        sc = make()
+        w = oracle.OracleWorld(sc, "reference", "project")
+        for _ in range(steps):
+            w.step(DT, VI, PI)
+        b = w.bodies()
+        lo, hi = b[:, 0:2].min(axis=0) - 2.0, b[:, 0:2].max(axis=0) + 2.0
+        rng = scenes.SplitMix64(zlib.crc32(name.encode()))
+        boxes, rays = [], []
+        for _ in range(n_boxes):
+            cx, cy = rng.uniform(lo[0], hi[0]), rng.uniform(lo[1], hi[1])
+            hx, hy = rng.uniform(0.1, 6.0), rng.uniform(0.1, 6.0)
+            boxes.append([cx - hx, cy - hy, cx + hx, cy + hy])
+        for _ in range(n_rays):
+            rays.append([rng.uniform(lo[0], hi[0]), rng.uniform(lo[1], hi[1]), rng.uniform(lo[0], hi[0]),
+                         rng.uniform(lo[1], hi[1])])
+        boxes = np.array(boxes, dtype=np.float32)
+        rays = np.array(rays, dtype=np.float32)
+        counts, fixtures = [], []
+        for bx in boxes:
+            f = w.query_aabb(bx)
+            counts.append(len(f))
+            fixtures.extend(f.tolist())
+        ray_fix, ray_hit = [], []
+        for r in rays:
+            f, h = w.raycast(r)
+            ray_fix.append(f)
+            ray_hit.append(h)
+        out[name] = dict(boxes=boxes, counts=np.array(counts, np.int32), fixtures=np.array(fixtures, np.int32),
+                         rays=rays, ray_fixture=np.array(ray_fix, np.int32), ray_hit=np.array(ray_hit, np.float32),
+                         steps=np.int32(steps))
+    for name, d in out.items():
+        np.savez_compressed(os.path.join(HERE, f"query_{name}.npz"), **d)
+
+
 def make_trig(n: int = 200000):
     rng = np.random.default_rng(5)
     x = np.concatenate([rng.uniform(-4, 4, n // 2), rng.uniform(-1e-3, 1e-3, n // 4),
@@ -174,6 +226,10 @@ def make_trig(n: int = 200000):
 
 def main():
     oracle.build_reference()
+    if "--queries" in sys.argv:
+        make_queries()
+        print("done")
+        return
     for name, make, steps, cps in cases():
         for trig in ("libm", "project"):
             digests, snap = run_case(make(), steps, cps, "reference", trig)
@@ -183,6 +239,7 @@ def main():
     make_collide()
     make_toi()
     make_trig()
+    make_queries()
     print("done")
 
 

@@ -46,12 +46,24 @@ def test_hello_world_matches_oracle(gpu, tmp_path):
     b = sc.body(scenes.DYNAMIC, 0.0, 4.0)
     sc.fixture(b, 3, [1.0, 1.0], n=2, density=1.0, friction=0.3)
     o = oracle.OracleWorld(sc, "port", "project")
+    o.record_events(True)
     want = []
+    kinds = np.zeros(4, dtype=np.int64)
+    last_post = None
     for _ in range(60):
         o.step(1.0 / 60.0, 6, 2)
         s = o.bodies()[1]
         want.append([s[0], s[1], s[2]])
+        ev, imp = o.events()
+        for k, row in zip(ev[:, 0], imp):
+            kinds[k] += 1
+            if k == 3:
+                last_post = row[0]
     want = np.array(want, dtype=np.float32)
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    # the listener saw the reference's calls: counts per kind and the last PostSolve impulse
     tail = lines[60].split()
-    assert tail[0] == "contacts" and int(tail[1]) == 1 and int(tail[3]) == 1 and int(tail[5]) == 0
+    assert tail[0] == "contacts" and int(tail[1]) == 1
+    assert [int(tail[3]), int(tail[5]), int(tail[9]), int(tail[11])] == [kinds[0], kinds[1], kinds[2], kinds[3]]
+    assert kinds[3] > 0
+    assert np.float32(float.fromhex(tail[13])).view(np.uint32) == np.float32(last_post).view(np.uint32)
