@@ -29,7 +29,7 @@ EXPORTS = [
     "gb_mlp_create", "gb_mlp_destroy", "gb_mlp_param_count", "gb_mlp_set_params", "gb_mlp_get_params",
     "gb_mlp_forward", "gb_mlp_gradients", "gb_mlp_train", "gb_world_set_warm_start", "gb_world_warm_stats",
     "gb_world_set_contact_log", "gb_world_read_contact_log", "gb_world_contact_stats", "gb_world_set_events",
-    "gb_world_read_events", "gb_world_query_aabb", "gb_world_raycast",
+    "gb_world_read_events", "gb_world_query_aabb", "gb_world_raycast", "gb_create_joints",
 ]
 
 
@@ -84,7 +84,9 @@ def load(build_if_missing: bool = True):
         "gb_create_bodies": [vp, i, i, _i32, _f32, _i32, _i32],
         "gb_create_fixtures": [vp, i, i, _i32, _i32, _f32, _i32, _f32, _i32, _i32],
         "gb_create_revolute_joints": [vp, i, i, _i32, _i32, _f32, _i32, _i32],
-        "gb_build_world": [vp, i, i, _i32, _f32, _i32, i, _i32, _i32, _f32, _i32, _f32, _i32, i, _i32, _i32, _f32, _i32],
+        "gb_build_world": [vp, i, i, _i32, _f32, _i32, i, _i32, _i32, _f32, _i32, _f32, _i32, i, _i32, _i32, _i32, _f32,
+                           _i32],
+        "gb_create_joints": [vp, i, i, _i32, _i32, _i32, _f32, _i32, _i32],
         "gb_world_upload": [vp],
         "gb_world_step": [vp, f, i, i],
         "gb_world_sync": [vp],

@@ -741,16 +741,29 @@ gb_status CreateFixture(HWorld& W, int body, int type, const float* s, int n, co
     return GB_OK;
 }
 
-gb_status CreateRevolute(HWorld& W, int a, int b, const float* f, int fl, int* id)
+// b2World::CreateJoint (Dynamics/b2World.cpp:185-250) for a revolute, distance or weld joint
+// definition. f[9]: revolute localAnchorA, localAnchorB, referenceAngle, lowerAngle, upperAngle,
+// motorSpeed, maxMotorTorque; distance localAnchorA, localAnchorB, length, frequencyHz,
+// dampingRatio; weld localAnchorA, localAnchorB, referenceAngle, frequencyHz, dampingRatio.
+gb_status CreateJoint(HWorld& W, int type, int a, int b, const float* f, int fl, int* id)
 {
     int nb = (int)W.bodies.size();
     if (a < 0 || a >= nb || b < 0 || b >= nb || a == b) return GB_ERR_INVALID;
+    if (type != kJointRevolute && type != kJointDistance && type != kJointWeld) return GB_ERR_INVALID;
     Joint j;
     std::memset(&j, 0, sizeof(j));
+    j.type = type;
     j.bodyA = a; j.bodyB = b;
     j.localAnchorA = V(f[0], f[1]); j.localAnchorB = V(f[2], f[3]);
-    j.referenceAngle = f[4]; j.lowerAngle = f[5]; j.upperAngle = f[6]; j.motorSpeed = f[7]; j.maxMotorTorque = f[8];
-    j.enableLimit = (fl & 1) != 0; j.enableMotor = (fl & 2) != 0; j.collideConnected = (fl & 4) != 0;
+    if (type == kJointRevolute) {
+        j.referenceAngle = f[4]; j.lowerAngle = f[5]; j.upperAngle = f[6]; j.motorSpeed = f[7]; j.maxMotorTorque = f[8];
+        j.enableLimit = (fl & 1) != 0; j.enableMotor = (fl & 2) != 0;
+    } else if (type == kJointDistance) {
+        j.length = f[4]; j.frequencyHz = f[5]; j.dampingRatio = f[6];
+    } else {
+        j.referenceAngle = f[4]; j.frequencyHz = f[5]; j.dampingRatio = f[6];
+    }
+    j.collideConnected = (fl & 4) != 0;
     int idx = (int)W.joints.size();
     j.prev = kNullIdx;
     j.next = W.jointList;
@@ -840,15 +853,27 @@ gb_status gb_create_revolute_joints(gb_world* g, int w, int n, const int* a, con
     gb_status s = Mutable(g, w);
     if (s != GB_OK) return s;
     for (int i = 0; i < n; ++i)
-        if ((s = CreateRevolute(g->worlds[w], a[i], b[i], f + 9 * i, flags[i], out_ids ? out_ids + i : nullptr)) != GB_OK)
+        if ((s = CreateJoint(g->worlds[w], kJointRevolute, a[i], b[i], f + 9 * i, flags[i], out_ids ? out_ids + i : nullptr)) != GB_OK)
+            return s;
+    return GB_OK;
+}
+
+gb_status gb_create_joints(gb_world* g, int w, int n, const int* type, const int* a, const int* b, const float* f,
+                           const int* flags, int* out_ids)
+{
+    gb_status s = Mutable(g, w);
+    if (s != GB_OK) return s;
+    if (n > 0 && (!type || !a || !b || !f || !flags)) return GB_ERR_INVALID;
+    for (int i = 0; i < n; ++i)
+        if ((s = CreateJoint(g->worlds[w], type[i], a[i], b[i], f + 9 * i, flags[i], out_ids ? out_ids + i : nullptr)) != GB_OK)
             return s;
     return GB_OK;
 }
 
 gb_status gb_build_world(gb_world* g, int w, int nb, const int* body_type, const float* body_f, const int* body_flags,
                          int nf, const int* fix_body, const int* fix_type, const float* fix_shape, const int* fix_n,
-                         const float* fix_mat, const int* fix_filt, int nj, const int* joint_a, const int* joint_b,
-                         const float* joint_f, const int* joint_flags)
+                         const float* fix_mat, const int* fix_filt, int nj, const int* joint_type, const int* joint_a,
+                         const int* joint_b, const float* joint_f, const int* joint_flags)
 {
     gb_status s = Mutable(g, w);
     if (s != GB_OK) return s;
@@ -866,7 +891,8 @@ gb_status gb_build_world(gb_world* g, int w, int nb, const int* body_type, const
     }
     if (fi != nf) return GB_ERR_INVALID;
     for (int j = 0; j < nj; ++j)
-        if ((s = CreateRevolute(W, base + joint_a[j], base + joint_b[j], joint_f + 9 * j, joint_flags[j], nullptr)) != GB_OK)
+        if ((s = CreateJoint(W, joint_type ? joint_type[j] : kJointRevolute, base + joint_a[j], base + joint_b[j],
+                             joint_f + 9 * j, joint_flags[j], nullptr)) != GB_OK)
             return s;
     return GB_OK;
 }

@@ -526,6 +526,509 @@ __device__ bool RevSolvePosition(Joint& j, float4* pos)
 }
 
 
+// ------------------------------------------------------------------ distance joint
+// b2DistanceJoint (Dynamics/Joints/b2DistanceJoint.cpp:61-225): a rod, or a spring when frequencyHz > 0.
+__device__ void DistInit(const Wd& W, Joint& j, float4* pos, float4* vel, bool warmStarting, float dtRatio, float dt)
+{
+    const float4 mA4 = W.mas[j.bodyA], mB4 = W.mas[j.bodyB];
+    j.localCenterA = V(mA4.z, mA4.w); j.localCenterB = V(mB4.z, mB4.w);
+    j.invMassA = mA4.x; j.invMassB = mB4.x; j.invIA = mA4.y; j.invIB = mB4.y;
+    const float4 pa = pos[j.indexA], pb = pos[j.indexB], va = vel[j.indexA], vb = vel[j.indexB];
+    const Vec2 cA = V(pa.x, pa.y), cB = V(pb.x, pb.y);
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const Rot qA = RotOf(pa.z), qB = RotOf(pb.z);
+    j.rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    j.rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    j.u = cB + j.rB - cA - j.rA;
+    const float length = Length(j.u);
+    if (length > kLinearSlop) {
+        const float inv = 1.0f / length;
+        j.u.x *= inv;
+        j.u.y *= inv;
+    } else {
+        j.u = V(0.0f, 0.0f);
+    }
+    const float crAu = Cross(j.rA, j.u), crBu = Cross(j.rB, j.u);
+    float invMass = j.invMassA + j.invIA * crAu * crAu + j.invMassB + j.invIB * crBu * crBu;
+    j.motorMass = invMass != 0.0f ? 1.0f / invMass : 0.0f;
+    if (j.frequencyHz > 0.0f) {
+        const float C = length - j.length;
+        const float omega = 2.0f * kPi * j.frequencyHz;
+        const float d = 2.0f * j.motorMass * j.dampingRatio * omega;
+        const float k = j.motorMass * omega * omega;
+        const float h = dt;
+        j.gamma = h * (d + h * k);
+        j.gamma = j.gamma != 0.0f ? 1.0f / j.gamma : 0.0f;
+        j.bias = C * h * k * j.gamma;
+        invMass += j.gamma;
+        j.motorMass = invMass != 0.0f ? 1.0f / invMass : 0.0f;
+    } else {
+        j.gamma = 0.0f;
+        j.bias = 0.0f;
+    }
+    if (warmStarting) {
+        j.impulse[0] *= dtRatio;
+        const Vec2 P = j.impulse[0] * j.u;
+        vA = vA - j.invMassA * P;
+        wA -= j.invIA * Cross(j.rA, P);
+        vB = vB + j.invMassB * P;
+        wB += j.invIB * Cross(j.rB, P);
+    } else {
+        j.impulse[0] = 0.0f;
+    }
+    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
+__device__ void DistSolveVelocity(Joint& j, float4* vel)
+{
+    const float4 va = vel[j.indexA], vb = vel[j.indexB];
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const Vec2 vpA = vA + Cross(wA, j.rA);
+    const Vec2 vpB = vB + Cross(wB, j.rB);
+    const float Cdot = Dot(j.u, vpB - vpA);
+    const float impulse = -j.motorMass * (Cdot + j.bias + j.gamma * j.impulse[0]);
+    j.impulse[0] += impulse;
+    const Vec2 P = impulse * j.u;
+    vA = vA - j.invMassA * P;
+    wA -= j.invIA * Cross(j.rA, P);
+    vB = vB + j.invMassB * P;
+    wB += j.invIB * Cross(j.rB, P);
+    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
+__device__ bool DistSolvePosition(Joint& j, float4* pos)
+{
+    if (j.frequencyHz > 0.0f) return true;
+    const float4 pa = pos[j.indexA], pb = pos[j.indexB];
+    Vec2 cA = V(pa.x, pa.y), cB = V(pb.x, pb.y);
+    float aA = pa.z, aB = pb.z;
+    const Rot qA = RotOf(aA), qB = RotOf(aB);
+    const Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    const Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    Vec2 u = cB + rB - cA - rA;
+    const float length = Normalize(u);
+    float C = length - j.length;
+    C = Clampf(C, -kMaxLinearCorrection, kMaxLinearCorrection);
+    const float impulse = -j.motorMass * C;
+    const Vec2 P = impulse * u;
+    cA = cA - j.invMassA * P;
+    aA -= j.invIA * Cross(rA, P);
+    cB = cB + j.invMassB * P;
+    aB += j.invIB * Cross(rB, P);
+    pos[j.indexA] = make_float4(cA.x, cA.y, aA, 0.0f);
+    pos[j.indexB] = make_float4(cB.x, cB.y, aB, 0.0f);
+    return Absf(C) < kLinearSlop;
+}
+
+// ------------------------------------------------------------------ weld joint
+// b2WeldJoint (Dynamics/Joints/b2WeldJoint.cpp:69-316); mass[] holds m_mass with columns ex = mass[0..2],
+// ey = mass[3..5], ez = mass[6..8] (the Solve33 layout).
+__device__ inline void WeldK(const Joint& j, Vec2 rA, Vec2 rB, float* K)
+{
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    K[0] = mA + mB + rA.y * rA.y * iA + rB.y * rB.y * iB;
+    K[3] = -rA.y * rA.x * iA - rB.y * rB.x * iB;
+    K[6] = -rA.y * iA - rB.y * iB;
+    K[1] = K[3];
+    K[4] = mA + mB + rA.x * rA.x * iA + rB.x * rB.x * iB;
+    K[7] = rA.x * iA + rB.x * iB;
+    K[2] = K[6];
+    K[5] = K[7];
+    K[8] = iA + iB;
+}
+// b2Mat33::GetInverse22 and GetSymInverse33 (Common/b2Math.cpp:59-97)
+__device__ inline void Inverse22(const float* K, float* M)
+{
+    const float a = K[0], b = K[3], c = K[1], d = K[4];
+    float det = a * d - b * c;
+    if (det != 0.0f) det = 1.0f / det;
+    M[0] = det * d; M[3] = -det * b; M[2] = 0.0f;
+    M[1] = -det * c; M[4] = det * a; M[5] = 0.0f;
+    M[6] = 0.0f; M[7] = 0.0f; M[8] = 0.0f;
+}
+__device__ inline void SymInverse33(const float* K, float* M)
+{
+    // det = dot(ex, cross(ey, ez))
+    const float cx = K[4] * K[8] - K[5] * K[7], cy = K[5] * K[6] - K[3] * K[8], cz = K[3] * K[7] - K[4] * K[6];
+    float det = K[0] * cx + K[1] * cy + K[2] * cz;
+    if (det != 0.0f) det = 1.0f / det;
+    const float a11 = K[0], a12 = K[3], a13 = K[6];
+    const float a22 = K[4], a23 = K[7];
+    const float a33 = K[8];
+    M[0] = det * (a22 * a33 - a23 * a23);
+    M[1] = det * (a13 * a23 - a12 * a33);
+    M[2] = det * (a12 * a23 - a13 * a22);
+    M[3] = M[1];
+    M[4] = det * (a11 * a33 - a13 * a13);
+    M[5] = det * (a13 * a12 - a11 * a23);
+    M[6] = M[2];
+    M[7] = M[5];
+    M[8] = det * (a11 * a22 - a12 * a12);
+}
+
+__device__ void WeldInit(const Wd& W, Joint& j, float4* pos, float4* vel, bool warmStarting, float dtRatio, float dt)
+{
+    const float4 mA4 = W.mas[j.bodyA], mB4 = W.mas[j.bodyB];
+    j.localCenterA = V(mA4.z, mA4.w); j.localCenterB = V(mB4.z, mB4.w);
+    j.invMassA = mA4.x; j.invMassB = mB4.x; j.invIA = mA4.y; j.invIB = mB4.y;
+    const float aA = pos[j.indexA].z, aB = pos[j.indexB].z;
+    const float4 va = vel[j.indexA], vb = vel[j.indexB];
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const Rot qA = RotOf(aA), qB = RotOf(aB);
+    j.rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    j.rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    float K[9];
+    WeldK(j, j.rA, j.rB, K);
+    if (j.frequencyHz > 0.0f) {
+        Inverse22(K, j.mass);
+        float invM = iA + iB;
+        const float m = invM > 0.0f ? 1.0f / invM : 0.0f;
+        const float C = aB - aA - j.referenceAngle;
+        const float omega = 2.0f * kPi * j.frequencyHz;
+        const float d = 2.0f * m * j.dampingRatio * omega;
+        const float k = m * omega * omega;
+        const float h = dt;
+        j.gamma = h * (d + h * k);
+        j.gamma = j.gamma != 0.0f ? 1.0f / j.gamma : 0.0f;
+        j.bias = C * h * k * j.gamma;
+        invM += j.gamma;
+        j.mass[8] = invM != 0.0f ? 1.0f / invM : 0.0f;
+    } else if (K[8] == 0.0f) {
+        Inverse22(K, j.mass);
+        j.gamma = 0.0f;
+        j.bias = 0.0f;
+    } else {
+        SymInverse33(K, j.mass);
+        j.gamma = 0.0f;
+        j.bias = 0.0f;
+    }
+    if (warmStarting) {
+        j.impulse[0] *= dtRatio; j.impulse[1] *= dtRatio; j.impulse[2] *= dtRatio;
+        const Vec2 P = V(j.impulse[0], j.impulse[1]);
+        vA = vA - mA * P;
+        wA -= iA * (Cross(j.rA, P) + j.impulse[2]);
+        vB = vB + mB * P;
+        wB += iB * (Cross(j.rB, P) + j.impulse[2]);
+    } else {
+        j.impulse[0] = j.impulse[1] = j.impulse[2] = 0.0f;
+    }
+    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
+__device__ void WeldSolveVelocity(Joint& j, float4* vel)
+{
+    const float4 va = vel[j.indexA], vb = vel[j.indexB];
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    const float* M = j.mass;
+    if (j.frequencyHz > 0.0f) {
+        const float Cdot2 = wB - wA;
+        const float impulse2 = -M[8] * (Cdot2 + j.bias + j.gamma * j.impulse[2]);
+        j.impulse[2] += impulse2;
+        wA -= iA * impulse2;
+        wB += iB * impulse2;
+        const Vec2 Cdot1 = vB + Cross(wB, j.rB) - vA - Cross(wA, j.rA);
+        // b2Mul22(m_mass, Cdot1)
+        const Vec2 impulse1 = -V(M[0] * Cdot1.x + M[3] * Cdot1.y, M[1] * Cdot1.x + M[4] * Cdot1.y);
+        j.impulse[0] += impulse1.x;
+        j.impulse[1] += impulse1.y;
+        const Vec2 P = impulse1;
+        vA = vA - mA * P;
+        wA -= iA * Cross(j.rA, P);
+        vB = vB + mB * P;
+        wB += iB * Cross(j.rB, P);
+    } else {
+        const Vec2 Cdot1 = vB + Cross(wB, j.rB) - vA - Cross(wA, j.rA);
+        const float Cdot2 = wB - wA;
+        // b2Mul(m_mass, Cdot) = Cdot.x * ex + Cdot.y * ey + Cdot.z * ez
+        const float ix = -((Cdot1.x * M[0] + Cdot1.y * M[3]) + Cdot2 * M[6]);
+        const float iy = -((Cdot1.x * M[1] + Cdot1.y * M[4]) + Cdot2 * M[7]);
+        const float iz = -((Cdot1.x * M[2] + Cdot1.y * M[5]) + Cdot2 * M[8]);
+        j.impulse[0] += ix;
+        j.impulse[1] += iy;
+        j.impulse[2] += iz;
+        const Vec2 P = V(ix, iy);
+        vA = vA - mA * P;
+        wA -= iA * (Cross(j.rA, P) + iz);
+        vB = vB + mB * P;
+        wB += iB * (Cross(j.rB, P) + iz);
+    }
+    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
+__device__ bool WeldSolvePosition(Joint& j, float4* pos)
+{
+    const float4 pa = pos[j.indexA], pb = pos[j.indexB];
+    Vec2 cA = V(pa.x, pa.y), cB = V(pb.x, pb.y);
+    float aA = pa.z, aB = pb.z;
+    const Rot qA = RotOf(aA), qB = RotOf(aB);
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    const Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    const Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    float K[9];
+    WeldK(j, rA, rB, K);
+    float positionError, angularError;
+    if (j.frequencyHz > 0.0f) {
+        const Vec2 C1 = cB + rB - cA - rA;
+        positionError = Length(C1);
+        angularError = 0.0f;
+        const Vec2 P = -Solve22(K, C1);
+        cA = cA - mA * P;
+        aA -= iA * Cross(rA, P);
+        cB = cB + mB * P;
+        aB += iB * Cross(rB, P);
+    } else {
+        const Vec2 C1 = cB + rB - cA - rA;
+        const float C2 = aB - aA - j.referenceAngle;
+        positionError = Length(C1);
+        angularError = Absf(C2);
+        float imp[3];
+        if (K[8] > 0.0f) {
+            const float Cv[3] = {C1.x, C1.y, C2};
+            Solve33(K, Cv, imp);
+            imp[0] = -imp[0]; imp[1] = -imp[1]; imp[2] = -imp[2];
+        } else {
+            const Vec2 i2 = -Solve22(K, C1);
+            imp[0] = i2.x; imp[1] = i2.y; imp[2] = 0.0f;
+        }
+        const Vec2 P = V(imp[0], imp[1]);
+        cA = cA - mA * P;
+        aA -= iA * (Cross(rA, P) + imp[2]);
+        cB = cB + mB * P;
+        aB += iB * (Cross(rB, P) + imp[2]);
+    }
+    pos[j.indexA] = make_float4(cA.x, cA.y, aA, 0.0f);
+    pos[j.indexB] = make_float4(cB.x, cB.y, aB, 0.0f);
+    return positionError <= kLinearSlop && angularError <= kAngularSlop;
+}
+
+// ------------------------------------------------------------------ prismatic joint
+// b2PrismaticJoint (Dynamics/Joints/b2PrismaticJoint.cpp:128-487): body B slides along an axis fixed
+// in body A, with a translation limit and a motor. lowerAngle/upperAngle hold the translation limits,
+// maxMotorTorque the maximum motor force, u the axis of the step, mass[] the 3x3 K (Solve33 layout).
+__device__ void PrisInit(const Wd& W, Joint& j, float4* pos, float4* vel, bool warmStarting, float dtRatio)
+{
+    const float4 mA4 = W.mas[j.bodyA], mB4 = W.mas[j.bodyB];
+    j.localCenterA = V(mA4.z, mA4.w); j.localCenterB = V(mB4.z, mB4.w);
+    j.invMassA = mA4.x; j.invMassB = mB4.x; j.invIA = mA4.y; j.invIB = mB4.y;
+    const float4 pa = pos[j.indexA], pb = pos[j.indexB], va = vel[j.indexA], vb = vel[j.indexB];
+    const Vec2 cA = V(pa.x, pa.y), cB = V(pb.x, pb.y);
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const Rot qA = RotOf(pa.z), qB = RotOf(pb.z);
+    const Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    const Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    const Vec2 d = (cB - cA) + rB - rA;
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    j.u = Mul(qA, j.localXAxisA);
+    j.a1 = Cross(d + rA, j.u);
+    j.a2 = Cross(rB, j.u);
+    j.motorMass = mA + mB + iA * j.a1 * j.a1 + iB * j.a2 * j.a2;
+    if (j.motorMass > 0.0f) j.motorMass = 1.0f / j.motorMass;
+    j.perp = Mul(qA, j.localYAxisA);
+    j.s1 = Cross(d + rA, j.perp);
+    j.s2 = Cross(rB, j.perp);
+    float* K = j.mass;
+    K[0] = mA + mB + iA * j.s1 * j.s1 + iB * j.s2 * j.s2;
+    K[1] = iA * j.s1 + iB * j.s2;
+    K[2] = iA * j.s1 * j.a1 + iB * j.s2 * j.a2;
+    K[4] = iA + iB;
+    if (K[4] == 0.0f) K[4] = 1.0f;  // fixed rotation
+    K[5] = iA * j.a1 + iB * j.a2;
+    K[8] = mA + mB + iA * j.a1 * j.a1 + iB * j.a2 * j.a2;
+    K[3] = K[1]; K[6] = K[2]; K[7] = K[5];
+    if (j.enableLimit) {
+        const float translation = Dot(j.u, d);
+        if (Absf(j.upperAngle - j.lowerAngle) < 2.0f * kLinearSlop) {
+            j.limitState = 3;
+        } else if (translation <= j.lowerAngle) {
+            if (j.limitState != 1) { j.limitState = 1; j.impulse[2] = 0.0f; }
+        } else if (translation >= j.upperAngle) {
+            if (j.limitState != 2) { j.limitState = 2; j.impulse[2] = 0.0f; }
+        } else {
+            j.limitState = 0;
+            j.impulse[2] = 0.0f;
+        }
+    } else {
+        j.limitState = 0;
+        j.impulse[2] = 0.0f;
+    }
+    if (!j.enableMotor) j.motorImpulse = 0.0f;
+    if (warmStarting) {
+        j.impulse[0] *= dtRatio; j.impulse[1] *= dtRatio; j.impulse[2] *= dtRatio;
+        j.motorImpulse *= dtRatio;
+        const float axial = j.motorImpulse + j.impulse[2];
+        const Vec2 P = j.impulse[0] * j.perp + axial * j.u;
+        const float LA = j.impulse[0] * j.s1 + j.impulse[1] + axial * j.a1;
+        const float LB = j.impulse[0] * j.s2 + j.impulse[1] + axial * j.a2;
+        vA = vA - mA * P;
+        wA -= iA * LA;
+        vB = vB + mB * P;
+        wB += iB * LB;
+    } else {
+        j.impulse[0] = j.impulse[1] = j.impulse[2] = 0.0f;
+        j.motorImpulse = 0.0f;
+    }
+    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
+__device__ void PrisSolveVelocity(Joint& j, float4* vel, float dt)
+{
+    const float4 va = vel[j.indexA], vb = vel[j.indexB];
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    if (j.enableMotor && j.limitState != 3) {
+        const float Cdot = Dot(j.u, vB - vA) + j.a2 * wB - j.a1 * wA;
+        float impulse = j.motorMass * (j.motorSpeed - Cdot);
+        const float oldImpulse = j.motorImpulse;
+        const float maxImpulse = dt * j.maxMotorTorque;
+        j.motorImpulse = Clampf(j.motorImpulse + impulse, -maxImpulse, maxImpulse);
+        impulse = j.motorImpulse - oldImpulse;
+        const Vec2 P = impulse * j.u;
+        const float LA = impulse * j.a1, LB = impulse * j.a2;
+        vA = vA - mA * P;
+        wA -= iA * LA;
+        vB = vB + mB * P;
+        wB += iB * LB;
+    }
+    const Vec2 Cdot1 = V(Dot(j.perp, vB - vA) + j.s2 * wB - j.s1 * wA, wB - wA);
+    if (j.enableLimit && j.limitState != 0) {
+        const float Cdot2 = Dot(j.u, vB - vA) + j.a2 * wB - j.a1 * wA;
+        const float negCdot[3] = {-Cdot1.x, -Cdot1.y, -Cdot2};
+        const float f1[3] = {j.impulse[0], j.impulse[1], j.impulse[2]};
+        float df[3];
+        Solve33(j.mass, negCdot, df);
+        j.impulse[0] += df[0]; j.impulse[1] += df[1]; j.impulse[2] += df[2];
+        if (j.limitState == 1) j.impulse[2] = Maxf(j.impulse[2], 0.0f);
+        else if (j.limitState == 2) j.impulse[2] = Minf(j.impulse[2], 0.0f);
+        // The 2x2 part re-solved with the clamped axial impulse (b2PrismaticJoint.cpp:322-327).
+        const float dz = j.impulse[2] - f1[2];
+        const Vec2 b = V(-Cdot1.x - dz * j.mass[6], -Cdot1.y - dz * j.mass[7]);
+        const Vec2 f2r = Solve22(j.mass, b) + V(f1[0], f1[1]);
+        j.impulse[0] = f2r.x;
+        j.impulse[1] = f2r.y;
+        df[0] = j.impulse[0] - f1[0]; df[1] = j.impulse[1] - f1[1]; df[2] = j.impulse[2] - f1[2];
+        const Vec2 P = df[0] * j.perp + df[2] * j.u;
+        const float LA = df[0] * j.s1 + df[1] + df[2] * j.a1;
+        const float LB = df[0] * j.s2 + df[1] + df[2] * j.a2;
+        vA = vA - mA * P;
+        wA -= iA * LA;
+        vB = vB + mB * P;
+        wB += iB * LB;
+    } else {
+        const Vec2 df = Solve22(j.mass, -Cdot1);
+        j.impulse[0] += df.x;
+        j.impulse[1] += df.y;
+        const Vec2 P = df.x * j.perp;
+        const float LA = df.x * j.s1 + df.y, LB = df.x * j.s2 + df.y;
+        vA = vA - mA * P;
+        wA -= iA * LA;
+        vB = vB + mB * P;
+        wB += iB * LB;
+    }
+    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
+__device__ bool PrisSolvePosition(Joint& j, float4* pos)
+{
+    const float4 pa = pos[j.indexA], pb = pos[j.indexB];
+    Vec2 cA = V(pa.x, pa.y), cB = V(pb.x, pb.y);
+    float aA = pa.z, aB = pb.z;
+    const Rot qA = RotOf(aA), qB = RotOf(aB);
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    const Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    const Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    const Vec2 d = cB + rB - cA - rA;
+    const Vec2 axis = Mul(qA, j.localXAxisA);
+    const float a1 = Cross(d + rA, axis), a2 = Cross(rB, axis);
+    const Vec2 perp = Mul(qA, j.localYAxisA);
+    const float s1 = Cross(d + rA, perp), s2 = Cross(rB, perp);
+    const Vec2 C1 = V(Dot(perp, d), aB - aA - j.referenceAngle);
+    float linearError = Absf(C1.x);
+    const float angularError = Absf(C1.y);
+    bool active = false;
+    float C2 = 0.0f;
+    if (j.enableLimit) {
+        const float translation = Dot(axis, d);
+        if (Absf(j.upperAngle - j.lowerAngle) < 2.0f * kLinearSlop) {
+            C2 = Clampf(translation, -kMaxLinearCorrection, kMaxLinearCorrection);
+            linearError = Maxf(linearError, Absf(translation));
+            active = true;
+        } else if (translation <= j.lowerAngle) {
+            C2 = Clampf(translation - j.lowerAngle + kLinearSlop, -kMaxLinearCorrection, 0.0f);
+            linearError = Maxf(linearError, j.lowerAngle - translation);
+            active = true;
+        } else if (translation >= j.upperAngle) {
+            C2 = Clampf(translation - j.upperAngle - kLinearSlop, 0.0f, kMaxLinearCorrection);
+            linearError = Maxf(linearError, translation - j.upperAngle);
+            active = true;
+        }
+    }
+    float imp[3];
+    float K[9];
+    K[0] = mA + mB + iA * s1 * s1 + iB * s2 * s2;
+    K[1] = iA * s1 + iB * s2;
+    K[4] = iA + iB;
+    if (K[4] == 0.0f) K[4] = 1.0f;
+    K[3] = K[1];
+    if (active) {
+        K[2] = iA * s1 * a1 + iB * s2 * a2;
+        K[5] = iA * a1 + iB * a2;
+        K[8] = mA + mB + iA * a1 * a1 + iB * a2 * a2;
+        K[6] = K[2]; K[7] = K[5];
+        const float negC[3] = {-C1.x, -C1.y, -C2};
+        Solve33(K, negC, imp);
+    } else {
+        const Vec2 i1 = Solve22(K, -C1);
+        imp[0] = i1.x; imp[1] = i1.y; imp[2] = 0.0f;
+    }
+    const Vec2 P = imp[0] * perp + imp[2] * axis;
+    const float LA = imp[0] * s1 + imp[1] + imp[2] * a1;
+    const float LB = imp[0] * s2 + imp[1] + imp[2] * a2;
+    cA = cA - mA * P;
+    aA -= iA * LA;
+    cB = cB + mB * P;
+    aB += iB * LB;
+    pos[j.indexA] = make_float4(cA.x, cA.y, aA, 0.0f);
+    pos[j.indexB] = make_float4(cB.x, cB.y, aB, 0.0f);
+    return linearError <= kLinearSlop && angularError <= kAngularSlop;
+}
+
+// ------------------------------------------------------------------ joint dispatch
+__device__ void JointInit(const Wd& W, Joint& j, float4* pos, float4* vel, bool warmStarting, float dtRatio, float dt)
+{
+    if (j.type == kJointDistance) DistInit(W, j, pos, vel, warmStarting, dtRatio, dt);
+    else if (j.type == kJointWeld) WeldInit(W, j, pos, vel, warmStarting, dtRatio, dt);
+    else if (j.type == kJointPrismatic) PrisInit(W, j, pos, vel, warmStarting, dtRatio);
+    else RevInit(W, j, pos, vel, warmStarting, dtRatio);
+}
+__device__ void JointSolveVelocity(Joint& j, float4* vel, float dt)
+{
+    if (j.type == kJointDistance) DistSolveVelocity(j, vel);
+    else if (j.type == kJointWeld) WeldSolveVelocity(j, vel);
+    else if (j.type == kJointPrismatic) PrisSolveVelocity(j, vel, dt);
+    else RevSolveVelocity(j, vel, dt);
+}
+__device__ bool JointSolvePosition(Joint& j, float4* pos)
+{
+    if (j.type == kJointDistance) return DistSolvePosition(j, pos);
+    if (j.type == kJointWeld) return WeldSolvePosition(j, pos);
+    if (j.type == kJointPrismatic) return PrisSolvePosition(j, pos);
+    return RevSolvePosition(j, pos);
+}
+
 // b2Island::Solve velocity/position integration clamps (Dynamics/b2Island.cpp:263-296, 442-470)
 __device__ inline void IntegratePosition(float4& p4, float4& v4, float h)
 {
@@ -825,7 +1328,7 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
             const int lo = I.z, hi = I.z + I.w;
             if (warm && !warmDone)
                 for (int i = lo; i < hi; ++i) ContactWarmStart(vc[i], imp[i], vel);
-            for (int k = 0; k < J.y; ++k) RevInit(*this, jt[sJoint[J.x + k]], pos, vel, warm, dtRatio);
+            for (int k = 0; k < J.y; ++k) JointInit(*this, jt[sJoint[J.x + k]], pos, vel, warm, dtRatio, h);
             int it = 0;
             for (; it < P.velocityIterations; ++it) {
                 if (P.tolerance > 0.0f) {
@@ -833,7 +1336,7 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
                     for (int i = lo; i < hi; ++i) r = fmaxf(r, ContactResidual(vc[i], imp[i], vel));
                     if (r <= P.tolerance) break;
                 }
-                for (int k = 0; k < J.y; ++k) RevSolveVelocity(jt[sJoint[J.x + k]], vel, h);
+                for (int k = 0; k < J.y; ++k) JointSolveVelocity(jt[sJoint[J.x + k]], vel, h);
                 SweepVelocity(vc, imp, lo, hi, vel);
             }
             atomicMax(&sFlag, it);
@@ -859,7 +1362,7 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
         }
         for (int isl = tid(); isl < nIsl; isl += nthreads()) {
             int2 J = islandJ[isl];
-            for (int k = 0; k < J.y; ++k) RevInit(*this, jt[sJoint[J.x + k]], pos, vel, warm, dtRatio);
+            for (int k = 0; k < J.y; ++k) JointInit(*this, jt[sJoint[J.x + k]], pos, vel, warm, dtRatio, h);
         }
         __syncthreads();
         int it = 0;
@@ -872,7 +1375,7 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
             if (d.jointCount > 0) {
                 for (int isl = tid(); isl < nIsl; isl += nthreads()) {
                     int2 J = islandJ[isl];
-                    for (int k = 0; k < J.y; ++k) RevSolveVelocity(jt[sJoint[J.x + k]], vel, h);
+                    for (int k = 0; k < J.y; ++k) JointSolveVelocity(jt[sJoint[J.x + k]], vel, h);
                 }
                 __syncthreads();
             }
@@ -946,7 +1449,7 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
                 if (it == 0 && minSep < 0.0f) atomicMax(reinterpret_cast<int*>(&st->maxPenetration), __float_as_int(-minSep));
                 bool jointsOkay = true;
                 for (int k = 0; k < J.y; ++k) {
-                    bool ok = RevSolvePosition(jt[sJoint[J.x + k]], pos);
+                    bool ok = JointSolvePosition(jt[sJoint[J.x + k]], pos);
                     jointsOkay = jointsOkay && ok;
                 }
                 if (contactsOkay && jointsOkay) { positionSolved = true; break; }
@@ -977,7 +1480,7 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
                 for (int isl = tid(); isl < nIsl; isl += nthreads()) {
                     int2 J = islandJ[isl];
                     for (int k = 0; k < J.y; ++k) {
-                        bool ok = RevSolvePosition(jt[sJoint[J.x + k]], pos);
+                        bool ok = JointSolvePosition(jt[sJoint[J.x + k]], pos);
                         jointsOkay = jointsOkay && ok;
                     }
                 }

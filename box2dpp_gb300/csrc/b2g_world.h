@@ -75,8 +75,14 @@ struct WorldState {
     unsigned long long cyc[kProfileSlots];
 };
 
-// Revolute joint (Dynamics/Joints/b2RevoluteJoint.h), stored whole: joints are few.
+// Joint types (b2JointType, Dynamics/Joints/b2Joint.h:28-42, those built here).
+enum : int { kJointRevolute = 0, kJointDistance = 1, kJointWeld = 2, kJointPrismatic = 3 };
+
+// A joint (Dynamics/Joints/b2RevoluteJoint.h, b2DistanceJoint.h, b2WeldJoint.h), stored whole: joints
+// are few. Fields a type does not use stay zero; the distance joint keeps its scalar impulse in
+// impulse[0] and its effective mass in motorMass, the weld joint its 3x3 effective mass in mass[].
 struct Joint {
+    int type;
     int bodyA, bodyB;
     int collideConnected, islandFlag;
     int prev, next;
@@ -92,6 +98,12 @@ struct Joint {
     float invMassA, invMassB, invIA, invIB;
     float mass[9];
     float motorMass;
+    float length, frequencyHz, dampingRatio;  // distance: length; distance, weld: spring
+    float gamma, bias;                        // soft constraint terms of the step
+    Vec2 u;                                   // distance: unit axis of the step; prismatic: axis
+    Vec2 localXAxisA, localYAxisA;            // prismatic: unit axis in body A and its normal
+    Vec2 perp;                                // prismatic: normal of the axis, this step
+    float s1, s2, a1, a2;                     // prismatic: lever arms of the step
 };
 
 // Island solver records: the fields of b2ContactVelocityConstraint and b2ContactPositionConstraint

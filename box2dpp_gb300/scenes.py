@@ -12,9 +12,11 @@ each followed by its fixtures, then joints. It is stored as numpy arrays so that
   ``b2PolygonShape::Set``); 3 box {hx, hy} or {hx, hy, cx, cy, angle}), ``fix_shape`` float32[M, 16],
   ``fix_n`` int32[M], ``fix_mat`` float32[M, 3] = (density, friction, restitution), ``fix_filt``
   int32[M, 4] = (categoryBits, maskBits, groupIndex, isSensor).
-* ``joint_a``/``joint_b`` int32[J], ``joint_f`` float32[J, 9] = (localAnchorA, localAnchorB,
-  referenceAngle, lowerAngle, upperAngle, motorSpeed, maxMotorTorque), ``joint_flags`` int32[J]
-  (1 limit, 2 motor, 4 collideConnected) - revolute joints.
+* ``joint_type`` int32[J] (0 revolute, 1 distance, 2 weld), ``joint_a``/``joint_b`` int32[J],
+  ``joint_f`` float32[J, 9] = revolute (localAnchorA, localAnchorB, referenceAngle, lowerAngle,
+  upperAngle, motorSpeed, maxMotorTorque), distance (localAnchorA, localAnchorB, length,
+  frequencyHz, dampingRatio), weld (localAnchorA, localAnchorB, referenceAngle, frequencyHz,
+  dampingRatio); ``joint_flags`` int32[J] (1 limit, 2 motor, 4 collideConnected).
 
 Random numbers come from splitmix64 on Python integers, so a seed gives the same scene on every
 machine. No public benchmark scene set exists for Box2D; these follow the workload descriptions:
@@ -32,6 +34,7 @@ import numpy as np
 STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 # shape encodings of the bulk build call
 CIRCLE, EDGE, POLYGON, BOX = 0, 1, 2, 3
+REVOLUTE, DISTANCE, WELD = 0, 1, 2
 DEFAULT_FLAGS = 1 | 2 | 16  # allowSleep, awake, active
 
 
@@ -90,8 +93,22 @@ class Scene:
     def revolute(self, a, b, anchor_a, anchor_b, ref_angle=0.0, lower=0.0, upper=0.0, motor_speed=0.0,
                  max_motor_torque=0.0, flags=0) -> int:
         self.joints.append((a, b, [anchor_a[0], anchor_a[1], anchor_b[0], anchor_b[1], ref_angle, lower,
-                                   upper, motor_speed, max_motor_torque], flags))
+                                   upper, motor_speed, max_motor_torque], flags, REVOLUTE))
         return len(self.joints) - 1
+
+    def distance(self, a, b, anchor_a, anchor_b, length, frequency_hz=0.0, damping_ratio=0.0, flags=0) -> int:
+        self.joints.append((a, b, [anchor_a[0], anchor_a[1], anchor_b[0], anchor_b[1], length, frequency_hz,
+                                   damping_ratio, 0.0, 0.0], flags, DISTANCE))
+        return len(self.joints) - 1
+
+    def weld(self, a, b, anchor_a, anchor_b, ref_angle=0.0, frequency_hz=0.0, damping_ratio=0.0, flags=0) -> int:
+        self.joints.append((a, b, [anchor_a[0], anchor_a[1], anchor_b[0], anchor_b[1], ref_angle, frequency_hz,
+                                   damping_ratio, 0.0, 0.0], flags, WELD))
+        return len(self.joints) - 1
+
+    @property
+    def joint_types(self) -> set:
+        return {j[4] for j in self.joints}
 
     # ------------------------------------------------------------------ arrays
     def arrays(self) -> dict:
@@ -106,6 +123,7 @@ class Scene:
             "fix_n": np.array([f[3] for f in self.fixtures], dtype=np.int32).reshape(nf),
             "fix_mat": np.array([f[4] for f in self.fixtures], dtype=np.float32).reshape(nf, 3),
             "fix_filt": np.array([f[5] for f in self.fixtures], dtype=np.int32).reshape(nf, 4),
+            "joint_type": np.array([j[4] for j in self.joints], dtype=np.int32).reshape(nj),
             "joint_a": np.array([j[0] for j in self.joints], dtype=np.int32).reshape(nj),
             "joint_b": np.array([j[1] for j in self.joints], dtype=np.int32).reshape(nj),
             "joint_f": np.array([j[2] for j in self.joints], dtype=np.float32).reshape(nj, 9),
@@ -251,6 +269,42 @@ def chains(n_chains: int, links: int, rng: SplitMix64, allow_sleep: bool = True,
                 la = (0.0, -0.5)
             s.revolute(prev, b, la, (0.0, 0.5), 0.0, -limit, limit, flags=1)
             prev = b
+    return _settings(s, allow_sleep)
+
+
+def joint_mix(rng: SplitMix64, allow_sleep: bool = True) -> Scene:
+    """Distance, weld and revolute joints together: pendulums on rigid and soft distance joints,
+    rigid and soft weld chains of boxes, a revolute hinge, over a ground edge they fall onto."""
+    s = Scene(name="joint_mix")
+    g = s.body(STATIC, 0.0, 0.0)
+    s.fixture(g, EDGE, [-40.0, 0.0, 40.0, 0.0, 0, 0, 0, 0, 0, 0], friction=0.6)
+    anchor = s.body(STATIC, 0.0, 20.0)
+    s.fixture(anchor, BOX, [0.5, 0.5], 2)
+    # pendulums: rigid rods and springs of decreasing stiffness
+    for k, (hz, zeta) in enumerate([(0.0, 0.0), (4.0, 0.5), (1.5, 0.1), (0.0, 0.0)]):
+        x = -12.0 + 4.0 * k
+        b = s.body(DYNAMIC, _q(x + rng.uniform(-1.0, 1.0)), 12.0, angle=_q(rng.uniform(-0.5, 0.5)))
+        s.fixture(b, CIRCLE if k % 2 else BOX, [0.0, 0.0, 0.6] if k % 2 else [0.5, 0.4], 1 if k % 2 else 2,
+                  density=1.0 + k, friction=0.4)
+        length = math.hypot(x - 0.0, 8.0)
+        s.distance(anchor, b, (x * 0.05, -0.5), (0.0, 0.0), _q(length), hz, zeta)
+    # weld chains: rigid and soft, hanging from the anchor's neighbours, loose at the end
+    for c, (hz, zeta) in enumerate([(0.0, 0.0), (6.0, 0.7)]):
+        x0 = 6.0 + 6.0 * c
+        top = s.body(STATIC, x0, 18.0)
+        s.fixture(top, BOX, [0.2, 0.2], 2)
+        prev = top
+        for i in range(5):
+            b = s.body(DYNAMIC, x0 + 1.0 * (i + 1), 18.0)
+            s.fixture(b, BOX, [0.5, 0.12], 2, density=2.0, friction=0.3, group=-(c + 1))
+            s.weld(prev, b, (0.5 if prev != top else 0.2, 0.0), (-0.5, 0.0), 0.0, hz, zeta)
+            prev = b
+    # a hinge with a limit, a box falling onto the arm
+    arm = s.body(DYNAMIC, -20.0, 6.0)
+    s.fixture(arm, BOX, [3.0, 0.2], 2, density=1.0)
+    s.revolute(g, arm, (-20.0, 6.0), (0.0, 0.0), 0.0, -0.4, 0.4, flags=1)
+    box = s.body(DYNAMIC, -18.0, 10.0, angle=0.3)
+    s.fixture(box, BOX, [0.6, 0.6], 2, density=3.0)
     return _settings(s, allow_sleep)
 
 

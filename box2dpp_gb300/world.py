@@ -37,7 +37,8 @@ class World:
             _lib.check(self.lib.gb_build_world(
                 self.h, i, len(a["body_type"]), a["body_type"], a["body_f"], a["body_flags"], len(a["fix_body"]),
                 a["fix_body"], a["fix_type"], a["fix_shape"], a["fix_n"], a["fix_mat"], a["fix_filt"],
-                len(a["joint_a"]), a["joint_a"], a["joint_b"], a["joint_f"], a["joint_flags"]), "gb_build_world")
+                len(a["joint_a"]), a["joint_type"], a["joint_a"], a["joint_b"], a["joint_f"], a["joint_flags"]),
+                "gb_build_world")
             self.n_fixtures.append(len(a["fix_body"]))
             self.n_bodies.append(len(a["body_type"]))
             self.dynamic_bodies += int((a["body_type"] == 2).sum())

@@ -235,6 +235,24 @@ struct b2RevoluteJointDef {
     float motorSpeed = 0.0f, maxMotorTorque = 0.0f;
 };
 
+struct b2DistanceJointDef {
+    b2Body* bodyA = nullptr;
+    b2Body* bodyB = nullptr;
+    bool collideConnected = false;
+    b2Vec2 localAnchorA, localAnchorB;
+    float length = 1.0f;
+    float frequencyHz = 0.0f, dampingRatio = 0.0f;
+};
+
+struct b2WeldJointDef {
+    b2Body* bodyA = nullptr;
+    b2Body* bodyB = nullptr;
+    bool collideConnected = false;
+    b2Vec2 localAnchorA, localAnchorB;
+    float referenceAngle = 0.0f;
+    float frequencyHz = 0.0f, dampingRatio = 0.0f;
+};
+
 class b2Joint {
 public:
     int GetIndex() const { return m_index; }
@@ -347,6 +365,19 @@ public:
         return m_joints.back().get();
     }
 
+    b2Joint* CreateJoint(const b2DistanceJointDef* def)
+    {
+        const float f[9] = {def->localAnchorA.x, def->localAnchorA.y, def->localAnchorB.x, def->localAnchorB.y,
+                            def->length, def->frequencyHz, def->dampingRatio, 0.0f, 0.0f};
+        return AddJoint(GB_JOINT_DISTANCE, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
+    }
+    b2Joint* CreateJoint(const b2WeldJointDef* def)
+    {
+        const float f[9] = {def->localAnchorA.x, def->localAnchorA.y, def->localAnchorB.x, def->localAnchorB.y,
+                            def->referenceAngle, def->frequencyHz, def->dampingRatio, 0.0f, 0.0f};
+        return AddJoint(GB_JOINT_WELD, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
+    }
+
     void Step(float timeStep, int velocityIterations, int positionIterations)
     {
         if (!Handle()) return;
@@ -425,6 +456,19 @@ public:
     }
 
 private:
+    b2Joint* AddJoint(int type, b2Body* a, b2Body* b, const float* f, int flags)
+    {
+        if (!Handle() || !a || !b) return nullptr;
+        const int ia = a->m_index, ib = b->m_index;
+        int id = -1;
+        if (gb_create_joints(m_h, 0, 1, &type, &ia, &ib, f, &flags, &id) != GB_OK) return nullptr;
+        std::unique_ptr<b2Joint> j(new b2Joint());
+        j->m_index = id;
+        j->m_a = a;
+        j->m_b = b;
+        m_joints.push_back(std::move(j));
+        return m_joints.back().get();
+    }
     gb_world* Handle()
     {
         if (!m_h) {

@@ -71,6 +71,7 @@ def _declare(lib, p: str) -> None:
         "step_many": (None, [C.POINTER(vp), C.c_int, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int]),
     }
     if p == "rw_":
+        sig["joint"] = (C.c_int, [vp, C.c_int, C.c_int, C.c_int, _f32p, C.c_int])
         sig["query_aabb"] = (C.c_int, [vp, _f32p, _i32p, C.c_int])
         sig["raycast"] = (C.c_int, [vp, _f32p, _f32p])
     if p == "po_":
@@ -131,9 +132,17 @@ class OracleWorld:
         f("config")(self.h, int(scene.allow_sleep), int(scene.warm_starting), int(scene.continuous),
                     int(scene.sub_stepping))
         a = scene.arrays()
+        typed = bool(len(a["joint_type"])) and bool((a["joint_type"] != 0).any())
+        if typed and kind == "port":
+            raise NotImplementedError("the CPU restatement builds revolute joints only")
+        nj = 0 if typed else len(a["joint_a"])
         f("build")(self.h, len(a["body_type"]), a["body_type"], a["body_f"], a["body_flags"],
                    len(a["fix_body"]), a["fix_body"], a["fix_type"], a["fix_shape"], a["fix_n"], a["fix_mat"],
-                   a["fix_filt"], len(a["joint_a"]), a["joint_a"], a["joint_b"], a["joint_f"], a["joint_flags"])
+                   a["fix_filt"], nj, a["joint_a"], a["joint_b"], a["joint_f"], a["joint_flags"])
+        if typed:
+            for j in range(len(a["joint_a"])):
+                f("joint")(self.h, int(a["joint_type"][j]), int(a["joint_a"][j]), int(a["joint_b"][j]),
+                           np.ascontiguousarray(a["joint_f"][j]), int(a["joint_flags"][j]))
         self.n_fixtures = len(a["fix_body"])
 
     def _fn(self, name):

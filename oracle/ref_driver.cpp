@@ -155,6 +155,37 @@ int rw_revolute(void* h, int bodyA, int bodyB, const float* f, int flags)
     return (int)w->joints.size() - 1;
 }
 
+// b2World::CreateJoint with a distance (type 1) or weld (type 2) definition; f as gb_create_joints.
+int rw_joint(void* h, int type, int bodyA, int bodyB, const float* f, int flags)
+{
+    RefWorld* w = static_cast<RefWorld*>(h);
+    if (type == 0) return rw_revolute(h, bodyA, bodyB, f, flags);
+    if (type == 1) {
+        b2DistanceJointDef jd;
+        jd.bodyA = w->bodies[bodyA];
+        jd.bodyB = w->bodies[bodyB];
+        jd.localAnchorA.Set(f[0], f[1]);
+        jd.localAnchorB.Set(f[2], f[3]);
+        jd.length = f[4];
+        jd.frequencyHz = f[5];
+        jd.dampingRatio = f[6];
+        jd.collideConnected = (flags & 4) != 0;
+        w->joints.push_back(w->world.CreateJoint(&jd));
+    } else {
+        b2WeldJointDef jd;
+        jd.bodyA = w->bodies[bodyA];
+        jd.bodyB = w->bodies[bodyB];
+        jd.localAnchorA.Set(f[0], f[1]);
+        jd.localAnchorB.Set(f[2], f[3]);
+        jd.referenceAngle = f[4];
+        jd.frequencyHz = f[5];
+        jd.dampingRatio = f[6];
+        jd.collideConnected = (flags & 4) != 0;
+        w->joints.push_back(w->world.CreateJoint(&jd));
+    }
+    return (int)w->joints.size() - 1;
+}
+
 // Bulk scene build: body b is created, then its fixtures (fbody is non-decreasing), then all joints.
 void rw_build(void* h, int nb, const int* btype, const float* bf, const int* bflags, int nf, const int* fbody,
               const int* ftype, const float* fshape, const int* fn, const float* fmat, const int* ffilt, int nj,

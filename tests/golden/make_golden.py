@@ -60,6 +60,7 @@ def cases():
         ("drop1000_nosleep", lambda: scenes.drop(1000, scenes.SplitMix64(21), allow_sleep=False), 120, [1, 60, 120]),
         ("stacks120", lambda: scenes.stacks(120, scenes.SplitMix64(5)), 300, [1, 150, 300]),
         ("chains6x16", lambda: chains_with_load(), 300, [1, 100, 300]),
+        ("joint_mix", lambda: scenes.joint_mix(scenes.SplitMix64(3)), 300, [1, 60, 150, 300]),
     ] + [(f"batch{i}", (lambda i=i: batch_world(i)), 200, [200]) for i in range(24)]
 
 

@@ -15,7 +15,10 @@ CASES = trajectory_cases()
 @pytest.mark.parametrize("name,make,steps", CASES, ids=[c[0] for c in CASES])
 def test_port_matches_reference_trajectory(name, make, steps, trig):
     g = golden(f"{name}_{trig}")
-    w = oracle.OracleWorld(make(), "port", trig)
+    sc = make()
+    if sc.joint_types - {0}:
+        pytest.skip("the CPU restatement builds revolute joints only; the GPU test checks this case")
+    w = oracle.OracleWorld(sc, "port", trig)
     bad = first_divergence(w, steps, g["digests"])
     if trig == "libm" and bad is not None:
         # glibc's sinf differs between libc builds (x86-64 FMA variant vs others); the bit-exact
