@@ -19,8 +19,12 @@
 #include "../../include/box2d_gb300.h"
 #include "b2g_world.h"
 
+cudaError_t b2gLaunchNarrowphase(const b2g::Batch& B, cudaStream_t stream);
 cudaError_t b2gLaunchStep(const b2g::Batch& B, const b2g::StepParams& P, const int* schedule, int first, int count,
                           int threads, int smemRows, int smemContacts, cudaStream_t stream);
+cudaError_t b2gLaunchToi(const b2g::Batch& B, const b2g::StepParams& P, cudaStream_t stream);
+cudaError_t b2gLaunchStepToi(const b2g::Batch& B, const b2g::StepParams& P, const int* schedule, int first, int count,
+                             int threads, int smemRows, int smemContacts, cudaStream_t stream);
 cudaError_t b2gLaunchSinCos(const float* x, float* s, float* c, int n, cudaStream_t stream);
 b2g::MlpView b2gMlpView(const gb_mlp* m);
 cudaError_t b2gLaunchQueryAabb(const b2g::Batch& B, int w, const float4* boxes, int n, const int* offsets, int* counts,
@@ -430,10 +434,11 @@ gb_status EnsureSideStreams(gb_world* g, int n)
     return GB_OK;
 }
 
-// One step of every world with the given plan: class 0 (the largest worlds) on the handle's stream,
+// One per-world launch per class of the plan: class 0 (the largest worlds) on the handle's stream,
 // submitted first so its CTAs are dispatched first, the others on side streams forked from the same
 // point and joined back (a pattern stream capture records as one graph).
-gb_status LaunchPlanStep(gb_world* g, const StepParams& P, const LaunchPlan& plan)
+using ClassLaunch = cudaError_t (*)(const Batch&, const StepParams&, const int*, int, int, int, int, int, cudaStream_t);
+gb_status LaunchClasses(gb_world* g, const StepParams& P, const LaunchPlan& plan, ClassLaunch launch)
 {
     const int n = std::min((int)plan.size(), kMaxClasses);
     if (n > 1) {
@@ -443,18 +448,27 @@ gb_status LaunchPlanStep(gb_world* g, const StepParams& P, const LaunchPlan& pla
     }
     if (n > 0) {
         const LaunchClass& c = plan[0];
-        GB_CUDA(b2gLaunchStep(g->batch, P, g->dSchedule, c.first, c.count, c.threads, c.rows, c.contacts,
-                              g->stream));
+        GB_CUDA(launch(g->batch, P, g->dSchedule, c.first, c.count, c.threads, c.rows, c.contacts, g->stream));
     }
     for (int i = 1; i < n; ++i) {
         const LaunchClass& c = plan[i];
         GB_CUDA(cudaStreamWaitEvent(g->side[i], g->fork, 0));
-        GB_CUDA(b2gLaunchStep(g->batch, P, g->dSchedule, c.first, c.count, c.threads, c.rows, c.contacts,
-                              g->side[i]));
+        GB_CUDA(launch(g->batch, P, g->dSchedule, c.first, c.count, c.threads, c.rows, c.contacts, g->side[i]));
         GB_CUDA(cudaEventRecord(g->join[i], g->side[i]));
     }
     for (int i = 1; i < n; ++i) GB_CUDA(cudaStreamWaitEvent(g->stream, g->join[i], 0));
     return GB_OK;
+}
+
+// One step of every world with the given plan: the flat narrowphase pre-pass, the per-world step up
+// to the continuous phase, the flat time-of-impact pre-pass, the per-world continuous phase.
+gb_status LaunchPlanStep(gb_world* g, const StepParams& P, const LaunchPlan& plan)
+{
+    GB_CUDA(b2gLaunchNarrowphase(g->batch, g->stream));
+    gb_status s = LaunchClasses(g, P, plan, b2gLaunchStep);
+    if (s != GB_OK) return s;
+    GB_CUDA(b2gLaunchToi(g->batch, P, g->stream));
+    return LaunchClasses(g, P, plan, b2gLaunchStepToi);
 }
 
 // A step of the online autotuner: the candidate under trial, timed with events on the handle's
@@ -559,7 +573,9 @@ gb_status Upload(gb_world* g)
     B.worlds = nw;
     gb_status s = GB_OK;
 #define ALLOC(field, n) if ((s = DevAlloc(g, &B.field, (size_t)(n))) != GB_OK) return s
-    ALLOC(desc, nw); ALLOC(state, nw);
+    ALLOC(desc, nw); ALLOC(state, nw); ALLOC(bWorld, tb); ALLOC(cWorld, tc);
+    B.bodyRows = (int)tb;
+    B.contactRows = (int)tc;
     ALLOC(xf, tb); ALLOC(sw, tb); ALLOC(sw0, tb); ALLOC(vel, tb); ALLOC(frc, tb); ALLOC(mas, tb); ALLOC(prop, tb);
     ALLOC(bi, tb); ALLOC(bj, tb);
     ALLOC(fi, tf); ALLOC(fm, tf); ALLOC(ff, tf); ALLOC(faabb, tf); ALLOC(shape, tf);
@@ -658,6 +674,16 @@ gb_status Upload(gb_world* g)
         (s = Put(B.cnext, cnext, tc)) != GB_OK || (s = Put(B.joint, joints, tj)) != GB_OK)
         return s;
     GB_CUDA(cudaMemcpy(B.state, states.data(), nw * sizeof(WorldState), cudaMemcpyHostToDevice));
+    {
+        // row -> world maps of the body and contact columns (padding rows belong to their world)
+        std::vector<int> bw(tb), cw(tc);
+        for (int wi = 0; wi < nw; ++wi) {
+            const WorldDesc& d = g->desc[wi];
+            std::fill(bw.begin() + d.bodyBase, bw.begin() + d.bodyBase + std::max(1, d.bodyCount), wi);
+            std::fill(cw.begin() + d.contactBase, cw.begin() + d.contactBase + d.contactCap, wi);
+        }
+        if ((s = Put(B.bWorld, bw, tb)) != GB_OK || (s = Put(B.cWorld, cw, tc)) != GB_OK) return s;
+    }
     // Largest worlds first: with one CTA per world the longest step starts earliest.
     std::vector<int> schedule(nw);
     std::iota(schedule.begin(), schedule.end(), 0);

@@ -238,8 +238,6 @@ struct Wd {
         mp1[c] = make_float4(m.p[1].lp.x, m.p[1].lp.y, m.p[1].ni, m.p[1].ti);
     }
 
-    // b2Contact::Update (Dynamics/Contacts/b2Contact.cpp:164-245). Returns true when the touching
-    // state of a non-sensor contact changed (the caller wakes both bodies).
     // Copies the shape of fixture f to dst, 8 bytes at a time (shapes are 8-byte aligned).
     __device__ void stageShape(int f, Shape* dst) const
     {
@@ -250,20 +248,69 @@ struct Wd {
         for (int k = 0; k < (int)(sizeof(Shape) / 8); ++k) out[k] = src[k];
     }
 
-    // stage (optional): this thread's two shape slots in shared memory; the narrowphase then reads
-    // both shapes there instead of re-reading them from global memory in its loops
-    __device__ bool update(int c, Shape* stage = nullptr)
+    // b2Contact::Update's evaluation of a non-sensor contact (Dynamics/Contacts/b2Contact.cpp:176-209):
+    // the manifold at the bodies' current transforms, each new point taking the impulses of the old
+    // point with the same id. stage (optional): this thread's two shape slots in shared memory; the
+    // narrowphase then reads both shapes there instead of re-reading them from global memory.
+    __device__ void evaluateManifold(int c, Manifold& m, Shape* stage) const
+    {
+        const int4 info = ci[c];
+        const int fA = info.y, fB = info.z;
+        const Xf xfA = xform(fixBody(fA)), xfB = xform(fixBody(fB));
+        Manifold old;
+        loadManifold(c, old);
+        m.count = 0;
+        m.type = old.type;
+        m.localNormal = old.localNormal;
+        m.localPoint = old.localPoint;
+        if (stage) {
+            stageShape(fA, stage);
+            stageShape(fB, stage + 1);
+            Evaluate(&m, stage[0], xfA, stage[1], xfB);
+        } else {
+            Evaluate(&m, shape[fA], xfA, shape[fB], xfB);
+        }
+        for (int i = 0; i < m.count; ++i) {
+            m.p[i].ni = 0.0f;
+            m.p[i].ti = 0.0f;
+            for (int j = 0; j < old.count; ++j) {
+                if (old.p[j].id == m.p[i].id) {
+                    m.p[i].ni = old.p[j].ni;
+                    m.p[i].ti = old.p[j].ti;
+                    break;
+                }
+            }
+        }
+        for (int i = m.count; i < 2; ++i) { m.p[i].lp = V(0.0f, 0.0f); m.p[i].ni = 0.0f; m.p[i].ti = 0.0f; m.p[i].id = 0; }
+    }
+
+    // Stage record of contact c (see ManifoldStage; it shares the contact's VelConstraint slot).
+    __device__ ManifoldStage* stageOf(int c) const { return reinterpret_cast<ManifoldStage*>(vc) + c; }
+    __device__ void writeStage(int c, const Manifold& m) const
+    {
+        ManifoldStage* S = stageOf(c);
+        S->h = make_int4(m.type, m.count, (int)m.p[0].id, (int)m.p[1].id);
+        S->v = make_float4(m.localNormal.x, m.localNormal.y, m.localPoint.x, m.localPoint.y);
+        S->p0 = make_float4(m.p[0].lp.x, m.p[0].lp.y, m.p[0].ni, m.p[0].ti);
+        S->p1 = make_float4(m.p[1].lp.x, m.p[1].lp.y, m.p[1].ni, m.p[1].ti);
+    }
+
+    // b2Contact::Update (Dynamics/Contacts/b2Contact.cpp:164-245). Returns true when the touching
+    // state of a non-sensor contact changed (the caller wakes both bodies). staged: this step's
+    // NarrowphaseKernel ran for the world, so a contact it evaluated (tag 1) commits that record,
+    // the same values the evaluation here would give.
+    __device__ bool update(int c, Shape* stage = nullptr, bool staged = false)
     {
         int4 info = ci[c];
         int fl = info.x | kCEnabled;
         bool wasTouching = (fl & kCTouching) != 0;
         int fA = info.y, fB = info.z;
         bool sensor = fi[fA].w != 0 || fi[fB].w != 0;
-        int bA = fixBody(fA), bB = fixBody(fB);
-        Xf xfA = xform(bA), xfB = xform(bB);
         bool touching;
         bool changed = false;
         if (sensor) {
+            int bA = fixBody(fA), bB = fixBody(fB);
+            Xf xfA = xform(bA), xfB = xform(bB);
             Proxy pa = ProxyOf(shape[fA]), pb = ProxyOf(shape[fB]);
             SimplexCache cache;
             cache.count = 0;
@@ -272,34 +319,20 @@ struct Wd {
             touching = Distance(&a, &b, &cache, pa, xfA, pb, xfB, true) < 10.0f * kEpsilon;
             mh[c].y = 0;
         } else {
-            Manifold old;
-            loadManifold(c, old);
-            Manifold m;
-            m.count = 0;
-            m.type = old.type;
-            m.localNormal = old.localNormal;
-            m.localPoint = old.localPoint;
-            if (stage) {
-                stageShape(fA, stage);
-                stageShape(fB, stage + 1);
-                Evaluate(&m, stage[0], xfA, stage[1], xfB);
+            const ManifoldStage* S = stageOf(c);
+            if (staged && S->tag == 1) {
+                const int4 h = S->h;
+                mh[c] = h;
+                mv[c] = S->v;
+                mp0[c] = S->p0;
+                mp1[c] = S->p1;
+                touching = h.y > 0;
             } else {
-                Evaluate(&m, shape[fA], xfA, shape[fB], xfB);
+                Manifold m;
+                evaluateManifold(c, m, stage);
+                storeManifold(c, m);
+                touching = m.count > 0;
             }
-            for (int i = 0; i < m.count; ++i) {
-                m.p[i].ni = 0.0f;
-                m.p[i].ti = 0.0f;
-                for (int j = 0; j < old.count; ++j) {
-                    if (old.p[j].id == m.p[i].id) {
-                        m.p[i].ni = old.p[j].ni;
-                        m.p[i].ti = old.p[j].ti;
-                        break;
-                    }
-                }
-            }
-            for (int i = m.count; i < 2; ++i) { m.p[i].lp = V(0.0f, 0.0f); m.p[i].ni = 0.0f; m.p[i].ti = 0.0f; m.p[i].id = 0; }
-            storeManifold(c, m);
-            touching = m.count > 0;
             changed = touching != wasTouching;
         }
         if (touching) fl |= kCTouching;
@@ -348,6 +381,8 @@ struct Wd {
     __device__ void solveIslands(const StepParams& P, int nIsl, int nRows, int nContacts, float4* smem, int smemRows,
                                  int smemContacts, const int* colourStart);
     __device__ void solveTOI(const StepParams& P);
+    __device__ void resetToi();
+    __device__ int toiKind(const int4& info) const;
     __device__ void warmStartAll(int nIsl, const int* colourStart, const float4* im, float4* v);
     __device__ void learnedImpulses(const StepParams& P, int nContacts, const float4* imp, const float4* vel);
     __device__ void destroyContact(int c);
@@ -515,7 +550,7 @@ __device__ void Wd::sweepPairs(int m, int* pairCount)
 
 __device__ void Wd::findNewContacts()
 {
-    __shared__ int sMoved, sPairs, sNew, sKept;
+    __shared__ int sMoved, sPairs, sNew, sKept, sLive;
     if (tid() == 0) { sMoved = 0; sPairs = 0; sNew = 0; }
     __syncthreads();
     const unsigned long long tPairs0 = clock64();
@@ -525,33 +560,45 @@ __device__ void Wd::findNewContacts()
     __syncthreads();
     const int m = sMoved;
     // Query every moved proxy's fat AABB against all proxies (b2BroadPhase.h:188-217); a pair whose
-    // both proxies moved is emitted once, from the lower proxy id. The proxies are staged in shared
-    // memory when they fit (each is read once per moved proxy): a free proxy gets an empty box that
-    // overlaps nothing, and a byte per proxy holds its moved flag.
-    const bool staged = np * (int)(sizeof(float4) + 1) <= smemBytes;
+    // both proxies moved is emitted once, from the lower proxy id. Proxy ids are tree node ids, so
+    // about half the id range is internal nodes: the live proxies (those with a fixture) are listed
+    // first and only they are tested. When they fit, their boxes, ids and moved flags are staged in
+    // shared memory (each is read once per moved proxy). The list's order is free: the pairs are
+    // sorted below.
+    const bool staged = np * (int)(sizeof(float4) + sizeof(int) + 1) <= smemBytes;
     float4* sFat = smemBase;
-    unsigned char* sMovedFlag = reinterpret_cast<unsigned char*>(smemBase + np);
-    if (staged && m > 0) {
-        const float inf = __int_as_float(0x7f800000);
+    int* sId = reinterpret_cast<int*>(smemBase + np);
+    unsigned char* sMovedFlag = reinterpret_cast<unsigned char*>(sId + np);
+    int* liveList = staged ? sId : sweepRank;  // sweepRank is free outside sweepPairs
+    if (tid() == 0) sLive = 0;
+    __syncthreads();
+    if (m > 0) {
         for (int p = tid(); p < np; p += nthreads()) {
-            sFat[p] = pfix[p] >= 0 ? fat[p] : make_float4(inf, inf, -inf, -inf);
-            sMovedFlag[p] = (unsigned char)(moved[p] != 0);
+            if (pfix[p] < 0) continue;
+            const int i = atomicAdd(&sLive, 1);
+            liveList[i] = p;
+            if (staged) {
+                sFat[i] = fat[p];
+                sMovedFlag[i] = (unsigned char)(moved[p] != 0);
+            }
         }
-        __syncthreads();
     }
-    const long long total = (long long)m * np;
+    __syncthreads();
+    const int nLive = sLive;
+    const long long total = (long long)m * nLive;
     if (total > kSweepThreshold) {
+        __syncthreads();
         sweepPairs(m, &sPairs);
     } else
     for (long long idx = tid(); idx < total; idx += nthreads()) {
-        const int q = movedList[idx / np];
-        const int p = (int)(idx % np);
+        const int q = movedList[idx / nLive];
+        const int i = (int)(idx % nLive);
+        const int p = liveList[i];
         if (p == q) continue;
         if (staged) {
-            if (sMovedFlag[p] && p < q) continue;
-            if (!Overlap(sFat[p], sFat[q])) continue;
+            if (sMovedFlag[i] && p < q) continue;
+            if (!Overlap(sFat[i], fat[q])) continue;
         } else {
-            if (pfix[p] < 0) continue;
             if (moved[p] && p < q) continue;
             if (!Overlap(fat[p], fat[q])) continue;
         }
@@ -744,6 +791,8 @@ __device__ void Wd::collide()
 {
     __shared__ int sChanged;
     const int n = st->contactCount;
+    // manifolds NarrowphaseKernel evaluated for this step (cleared below once committed)
+    const bool staged = st->staged != 0;
     // two shape slots per thread in the dynamic shared memory (free during this phase) when it fits
     Shape* shapeSlots = (int)(2 * sizeof(Shape)) * nthreads() <= smemBytes ? reinterpret_cast<Shape*>(smemBase) : nullptr;
     for (int b = tid(); b < d.bodyCount; b += nthreads()) sWake[b] = awake(b) ? -1 : INT_MAX;
@@ -785,7 +834,7 @@ __device__ void Wd::collide()
                 continue;
             }
             sStatus[k] = 1;
-            const bool updated = update(c, shapeSlots ? shapeSlots + 2 * tid() : nullptr);
+            const bool updated = update(c, shapeSlots ? shapeSlots + 2 * tid() : nullptr, staged);
             if (rec) evType[k] = updateEventBits((info.x & kCTouching) != 0, (ci[c].x & kCTouching) != 0, sensor);
             if (updated) {
                 if (atomicMin(&sWake[bA], k) > k) sChanged = 1;
@@ -836,6 +885,7 @@ __device__ void Wd::collide()
     if (tid() == 0) {
         for (int i = 0; i < nGone; ++i) destroyContact(gone[i]);
         st->contactCount = nKept;
+        st->staged = 0;
     }
     for (int k = tid(); k < nKept; k += nthreads()) order[k] = kept[k];
     __syncthreads();
@@ -1210,24 +1260,50 @@ __device__ void Wd::solve(const StepParams& P, float4* smem, int smemRows, int s
 // b2World::SolveTOI (Dynamics/b2World.cpp:579-896). One event at a time, as the reference: thread 0
 // scans the contact list in order (mutating sweeps as the reference does), the time of impact of every
 // contact that needs one is computed in parallel, thread 0 takes the earliest, and sub-steps it.
+// The reset at the start of a completed step's continuous phase (b2World.cpp:583-599): island flags
+// and sweep times of the bodies, TOI flags, counts and cached times of the contacts.
+__device__ void Wd::resetToi()
+{
+    for (int b = tid(); b < d.bodyCount; b += nthreads()) {
+        bi[b].y &= ~kBIsland;
+        sw[b].w = 0.0f;
+    }
+    const int nc = st->contactCount;
+    for (int k = tid(); k < nc; k += nthreads()) {
+        int c = order[k];
+        ci[c].x &= ~(kCToi | kCIsland);
+        ci[c].w = 0;
+        cp[c].w = 1.0f;
+    }
+}
+
+// What the scan of b2World::SolveTOI (b2World.cpp:609-650) does with a contact whose ci record is
+// info: 0 skipped (disabled,
+// too many sub-steps, a sensor, no awake non-static body, or neither body a bullet, static or
+// kinematic), 1 its cached time of impact, 2 a time of impact to compute.
+__device__ int Wd::toiKind(const int4& info) const
+{
+    if ((info.x & kCEnabled) == 0 || info.w > kMaxSubSteps) return 0;
+    if (info.x & kCToi) return 1;
+    const int4 a = fi[info.y], b = fi[info.z];
+    if (a.w != 0 || b.w != 0) return 0;
+    const int4 iA = bi[a.x], iB = bi[b.x];
+    const bool activeA = (iA.y & kBAwake) && iA.x != kStatic;
+    const bool activeB = (iB.y & kBAwake) && iB.x != kStatic;
+    const bool collideA = (iA.y & kBBullet) || iA.x != kDynamic;
+    const bool collideB = (iB.y & kBBullet) || iB.x != kDynamic;
+    return (activeA || activeB) && (collideA || collideB) ? 2 : 0;
+}
+
 __device__ void Wd::solveTOI(const StepParams& P)
 {
     __shared__ int sN, sDone, sMin;
     __shared__ float sMinAlpha;
-    if (st->stepComplete) {
-        for (int b = tid(); b < d.bodyCount; b += nthreads()) {
-            bi[b].y &= ~kBIsland;
-            sw[b].w = 0.0f;
-        }
-        const int nc = st->contactCount;
-        for (int k = tid(); k < nc; k += nthreads()) {
-            int c = order[k];
-            ci[c].x &= ~(kCToi | kCIsland);
-            ci[c].w = 0;
-            cp[c].w = 1.0f;
-        }
-    }
+    // ToiKernel may have done the reset and the first pass's times of impact already
+    const bool prepared = st->toiPrepared != 0;
+    if (st->stepComplete && !prepared) resetToi();
     __syncthreads();
+    if (tid() == 0) st->toiPrepared = 0;
     __shared__ int sAdvance;
     __shared__ float sBestA[kMaxCta];
     __shared__ int sBestK[kMaxCta];
@@ -1239,16 +1315,54 @@ __device__ void Wd::solveTOI(const StepParams& P)
             tMark = now;
         }
     };
+    // The scan's outcome is kept per contact between events, indexed by the contact's position from
+    // the list tail (vsep[t] = {alpha, or 2 when the scan skips it; contact slot}, cColour[c] = t):
+    // no contact leaves the list during the continuous phase and new ones are prepended, so that
+    // index is stable and list order is descending t. An event changes the outcome only of the
+    // contacts it touches: the event contact, the contacts of the non-static bodies of its mini
+    // island (invalidated, woken or moved) and the contacts it creates. Those (the dirty list in
+    // colourList, deduplicated by the event stamp in evType) are the only ones classified again; the
+    // first pass classifies the whole list. These scratch columns belong to the collide and solve
+    // phases, which set them before use.
+    __shared__ int sDirty;
+    __shared__ int sSortT[kMaxCta * 2], sSortC[kMaxCta * 2];
+    if (tid() == 0) sDirty = 0;
     for (int event = 0;; ++event) {
         const int n = st->contactCount;
+        const int nTask = event == 0 ? n : sDirty;
+        const int* task = event == 0 ? order : colourList;
         if (tid() == 0) sAdvance = 0;
+        if (event > 0 && nTask > 1) {
+            // dirty contacts into list order (descending tail index), for the sweep advances below
+            if (nTask <= 2 * kMaxCta) {
+                for (int i = tid(); i < nTask; i += nthreads()) {
+                    const int c = colourList[i];
+                    sSortC[i] = c;
+                    sSortT[i] = cColour[c];
+                }
+                __syncthreads();
+                for (int i = tid(); i < nTask; i += nthreads()) {
+                    const int ti = sSortT[i];
+                    int r = 0;
+                    for (int j = 0; j < nTask; ++j) r += sSortT[j] > ti ? 1 : 0;
+                    colourList[r] = sSortC[i];
+                }
+            } else if (tid() == 0) {
+                for (int i = 1; i < nTask; ++i) {
+                    const int x = colourList[i], tx = cColour[x];
+                    int j = i - 1;
+                    while (j >= 0 && cColour[colourList[j]] < tx) { colourList[j + 1] = colourList[j]; --j; }
+                    colourList[j + 1] = x;
+                }
+            }
+        }
         __syncthreads();
-        // Classify every contact of the list in parallel: 0 skipped, 1 cached TOI, 2 TOI needed.
-        // Whether a contact is skipped does not depend on the sweeps, so this is order-free. Each
-        // thread gathers kBatch contacts one dependency level at a time (list slot, contact, its
-        // fixtures, their bodies), so the global loads of a level overlap instead of queueing.
+        // Classify the contacts in parallel: 0 skipped, 1 cached TOI, 2 TOI needed. Whether a
+        // contact is skipped does not depend on the sweeps, so this is order-free. Each thread
+        // gathers kBatch contacts one dependency level at a time (list slot, contact, its fixtures,
+        // their bodies), so the global loads of a level overlap instead of queueing.
         constexpr int kBatch = 8;
-        for (int k0 = tid(); k0 < n; k0 += kBatch * nthreads()) {
+        for (int k0 = tid(); k0 < nTask; k0 += kBatch * nthreads()) {
             int c[kBatch];
             int4 info[kBatch];
             int fA[kBatch], fB[kBatch];
@@ -1256,7 +1370,7 @@ __device__ void Wd::solveTOI(const StepParams& P)
 #pragma unroll
             for (int j = 0; j < kBatch; ++j) {
                 const int k = k0 + j * nthreads();
-                c[j] = k < n ? order[k] : -1;
+                c[j] = k < nTask ? task[k] : -1;
             }
 #pragma unroll
             for (int j = 0; j < kBatch; ++j) info[j] = c[j] >= 0 ? ci[c[j]] : make_int4(0, 0, 0, 0);
@@ -1297,9 +1411,10 @@ __device__ void Wd::solveTOI(const StepParams& P)
         __syncthreads();
         if (sAdvance) {
             // Some pair has bodies at different sweep times: the reference advances the earlier body
-            // while it scans, in list order, and later pairs see the advanced sweep. Replay on one thread.
+            // while it scans, in list order, and later pairs see the advanced sweep. Replay on one
+            // thread (contacts the scan skips or finds cached advance nothing).
             if (tid() == 0) {
-                for (int k = 0; k < n; ++k) {
+                for (int k = 0; k < nTask; ++k) {
                     TOITask& T = toi[k];
                     if (T.kind != 2) continue;
                     int4 info = ci[T.contact];
@@ -1322,7 +1437,7 @@ __device__ void Wd::solveTOI(const StepParams& P)
             }
         } else {
             // All pairs agree on alpha0, so no sweep changes during the scan: snapshot in parallel.
-            for (int k = tid(); k < n; k += nthreads()) {
+            for (int k = tid(); k < nTask; k += nthreads()) {
                 TOITask& T = toi[k];
                 if (T.kind != 2) continue;
                 int4 info = ci[T.contact];
@@ -1333,7 +1448,7 @@ __device__ void Wd::solveTOI(const StepParams& P)
             }
         }
         __syncthreads();
-        for (int k = tid(); k < n; k += nthreads()) {
+        for (int k = tid(); k < nTask; k += nthreads()) {
             TOITask& T = toi[k];
             if (T.kind != 2) continue;
             int4 info = ci[T.contact];
@@ -1345,31 +1460,47 @@ __device__ void Wd::solveTOI(const StepParams& P)
             ci[T.contact].x = info.x | kCToi;
         }
         __syncthreads();
+        // the outcomes by tail index (the first pass also numbers the list and clears the stamps)
+        for (int k = tid(); k < nTask; k += nthreads()) {
+            const TOITask& T = toi[k];
+            const int c = T.contact;
+            int t;
+            if (event == 0) {
+                t = n - 1 - k;
+                cColour[c] = t;
+                evType[c] = 0;
+            } else {
+                t = cColour[c];
+            }
+            vsep[t] = make_float2(T.kind != 0 ? cp[c].w : 2.0f, __int_as_float(c));
+        }
+        __syncthreads();
         stamp(16);
         // Earliest TOI, first in list order among equals (the reference keeps the first alpha <
-        // minAlpha): per-thread minimum over its strided positions, then a reduction on (alpha, k).
+        // minAlpha): per-thread minimum over its strided tail indices (a later index is earlier in
+        // the list, so it wins a tie), then a reduction on (alpha, -t).
         {
             float best = 1.0f;
-            int bestK = INT_MAX;
-            for (int k = tid(); k < n; k += nthreads()) {
-                if (toi[k].kind == 0) continue;
-                float alpha = cp[toi[k].contact].w;
-                if (alpha < best) { best = alpha; bestK = k; }
+            int bestT = -1;
+            for (int t = tid(); t < n; t += nthreads()) {
+                const float alpha = vsep[t].x;
+                if (alpha < 1.0f && alpha <= best) { best = alpha; bestT = t; }
             }
             sBestA[tid()] = best;
-            sBestK[tid()] = bestK;
+            sBestK[tid()] = bestT;
         }
         __syncthreads();
         if (tid() == 0) {
             float minAlpha = 1.0f;
-            int minK = INT_MAX;
+            int minT = -1;
             for (int t = 0; t < nthreads(); ++t) {
-                if (sBestA[t] < minAlpha || (sBestA[t] == minAlpha && sBestK[t] < minK && sBestA[t] < 1.0f)) {
+                if (sBestK[t] < 0) continue;
+                if (sBestA[t] < minAlpha || (sBestA[t] == minAlpha && sBestK[t] > minT)) {
                     minAlpha = sBestA[t];
-                    minK = sBestK[t];
+                    minT = sBestK[t];
                 }
             }
-            int minC = minK == INT_MAX ? kNullIdx : toi[minK].contact;
+            int minC = minT < 0 ? kNullIdx : __float_as_int(vsep[minT].y);
             sMin = minC;
             sMinAlpha = minAlpha;
             sDone = 0;
@@ -1387,6 +1518,7 @@ __device__ void Wd::solveTOI(const StepParams& P)
         if (sDone) break;
         if (tid() == 0) {
             st->toiEvents = event + 1;
+            sDirty = 0;
             const int mc = sMin;
             const float minAlpha = sMinAlpha;
             int4 info = ci[mc];
@@ -1525,13 +1657,28 @@ __device__ void Wd::solveTOI(const StepParams& P)
                                  pcn > 1 ? im.z : 0.0f, pcn > 0 ? im.y : 0.0f, pcn > 1 ? im.w : 0.0f);
                     }
                 stamp(19);
+                // dynamic bodies: fixtures synchronised, contacts' TOIs invalidated; every contact of
+                // a non-static island body joins the dirty list (a woken kinematic body's contacts
+                // may now need a TOI)
                 for (int i = 0; i < nBodies; ++i) {
                     int b = sBody[i];
                     bi[b].y &= ~kBIsland;
-                    if (bi[b].x != kDynamic) continue;
-                    syncFixtures(b);
-                    B2G_WALK(e, bi[b].w, eNext(e), 2 * d.contactCap + 2) ci[e >> 1].x &= ~(kCToi | kCIsland);
+                    if (bi[b].x == kStatic) continue;
+                    const bool dynamic = bi[b].x == kDynamic;
+                    if (dynamic) syncFixtures(b);
+                    B2G_WALK(e, bi[b].w, eNext(e), 2 * d.contactCap + 2) {
+                        const int c = e >> 1;
+                        if (dynamic) ci[c].x &= ~(kCToi | kCIsland);
+                        if (evType[c] != event + 1) {
+                            evType[c] = event + 1;
+                            colourList[sDirty++] = c;
+                        }
+                    }
                 }
+            }
+            if (evType[mc] != event + 1) {
+                evType[mc] = event + 1;
+                colourList[sDirty++] = mc;
             }
             sDone = skip ? 2 : 0;
         }
@@ -1539,6 +1686,19 @@ __device__ void Wd::solveTOI(const StepParams& P)
         stamp(20);
         if (sDone == 2) continue;
         findNewContacts();
+        __syncthreads();
+        {
+            // the contacts the event created sit at the head of the list
+            const int n2 = st->contactCount, nNew = n2 - n, base = sDirty;
+            for (int k = tid(); k < nNew; k += nthreads()) {
+                const int c = order[k];
+                cColour[c] = n2 - 1 - k;
+                evType[c] = event + 1;
+                colourList[base + k] = c;
+            }
+            __syncthreads();
+            if (tid() == 0) sDirty = base + nNew;
+        }
         stamp(21);
         if (st->subStepping) {
             if (tid() == 0) st->stepComplete = 0;
@@ -1550,7 +1710,82 @@ __device__ void Wd::solveTOI(const StepParams& P)
 }
 
 // ------------------------------------------------------------------ kernels
-// b2World::Step (Dynamics/b2World.cpp:899-963) for world schedule[blockIdx.x], one CTA per world.
+// One step of a batch is, in stream order:
+//   NarrowphaseKernel  (flat, every contact row of the batch) per-step counters reset; manifolds of
+//                      the collide phase evaluated ahead
+//   StepKernel         (per world, per launch class) new-fixture pairs, collide (commits the staged
+//                      manifolds), island solve, fixture sync and pair finding
+//   ToiKernel          (flat, every body and contact row) the continuous phase's reset and the first
+//                      pass of times of impact
+//   StepToiKernel      (per world, per launch class) the continuous phase's event loop, force clearing
+// The flat pre-passes compute, per contact and in any order, values the reference computes while it
+// walks the contact list; the per-world kernels consume them in list order, so the results are the
+// reference's bit for bit. One thread per contact row keeps every SM busy with short independent
+// work (most rows are spare capacity and return at once), where the per-world kernels hold a
+// world's sequential phases.
+
+// Per-step counters of the world, zeroed before the step (profile slots included).
+__device__ void ResetStepCounters(WorldState* st)
+{
+    st->toiEvents = 0;
+    st->islands = 0;
+    st->solvedBodies = 0;
+    st->solvedContacts = 0;
+    st->pairsFound = 0;
+    st->colours = 0;
+    st->velIters = 0;
+    st->residual = 0.0f;
+    st->warmLearned = 0;
+    st->velItersSum = 0;
+    st->maxPenetration = 0.0f;
+    st->eventCount = 0;
+    st->eventsDropped = 0;
+    for (int i = 0; i < kProfileSlots; ++i) st->cyc[i] = 0;
+}
+
+// The evaluations of b2ContactManager::Collide (Dynamics/b2ContactManager.cpp:107-172), ahead of the
+// step, one thread per contact row of the batch: the k-th live contact of a world's list, if it is a
+// non-sensor contact with an awake non-static body whose fat AABBs overlap, gets the manifold
+// b2Contact::Update would compute (evaluation at the current transforms, impulses matched by id) in
+// its stage record. Nothing the collide phase does before it updates a contact changes those
+// inputs, so the collide phase commits the record when it reaches the contact; contacts left out
+// (tag 0: asleep, sensors, apart) it evaluates itself. Worlds with new fixtures create contacts
+// before their collide phase and are left out whole. Row 0 of each world resets its counters.
+__global__ void __launch_bounds__(256) NarrowphaseKernel(Batch B)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= B.contactRows) return;
+    const int w = B.cWorld[r];
+    WorldState* st = B.state + w;
+    const int k = r - B.desc[w].contactBase;
+    const bool newFixture = st->newFixture != 0;
+    if (k == 0) {
+        ResetStepCounters(st);
+        st->staged = newFixture ? 0 : 1;
+    }
+    if (newFixture || k >= st->contactCount) return;
+    Wd W;
+    W.init(B, w);
+    const int c = W.order[k];
+    const int4 info = W.ci[c];
+    const int4 a = W.fi[info.y], b = W.fi[info.z];
+    int tag = 0;
+    if (a.w == 0 && b.w == 0) {
+        const bool activeA = W.type(a.x) != kStatic && W.awake(a.x);
+        const bool activeB = W.type(b.x) != kStatic && W.awake(b.x);
+        if ((activeA || activeB) && Overlap(W.fat[a.z], W.fat[b.z])) {
+            Manifold m;
+            W.evaluateManifold(c, m, nullptr);
+            W.writeStage(c, m);
+            tag = 1;
+        }
+    }
+    W.stageOf(c)->tag = tag;
+}
+
+// b2World::Step (Dynamics/b2World.cpp:899-963) for world schedule[blockIdx.x], one CTA per world, up
+// to the continuous phase: new-fixture pairs, collide, island solve (with fixture synchronisation and
+// pair finding at its end).
 // Shared memory (its size is the launch's choice, LaunchShape) stages the island body rows
 // (positions, then velocities) and the accumulated impulses of the island contacts when a world's
 // fit, and the broadphase proxies, pair keys and list heads outside the island solve; every use
@@ -1571,24 +1806,7 @@ __global__ void __launch_bounds__(128, B2G_STEP_MIN_BLOCKS) StepKernel(Batch B, 
     const bool newFixture = W.st->newFixture != 0;
     const unsigned long long t0 = clock64();
     __syncthreads();
-    if (tid() == 0) {
-        W.st->toiEvents = 0;
-        W.st->islands = 0;
-        W.st->solvedBodies = 0;
-        W.st->solvedContacts = 0;
-        W.st->pairsFound = 0;
-        W.st->colours = 0;
-        W.st->velIters = 0;
-        W.st->residual = 0.0f;
-        W.st->warmLearned = 0;
-        W.st->velItersSum = 0;
-        W.st->maxPenetration = 0.0f;
-        W.st->eventCount = 0;
-        W.st->eventsDropped = 0;
-        W.st->newFixture = 0;
-        for (int i = 0; i < kProfileSlots; ++i) W.st->cyc[i] = 0;
-    }
-    __syncthreads();
+    if (tid() == 0) W.st->newFixture = 0;
     if (newFixture) W.findNewContacts();
     __syncthreads();
     const unsigned long long t1 = clock64();
@@ -1596,31 +1814,128 @@ __global__ void __launch_bounds__(128, B2G_STEP_MIN_BLOCKS) StepKernel(Batch B, 
     const unsigned long long t2 = clock64();
     if (W.st->stepComplete && P.dt > 0.0f) W.solve(P, smem, L.smemRows, L.smemContacts);
     __syncthreads();
-    const unsigned long long t3 = clock64();
+    if (tid() == 0) {
+        const unsigned long long t3 = clock64();
+        W.st->cyc[0] = t1 - t0;
+        W.st->cyc[1] = t2 - t1;
+        W.st->cyc[7] = t3 - t0;
+    }
+}
+
+// The first pass of b2World::SolveTOI (Dynamics/b2World.cpp:579-680) after a completed step, one
+// thread per body row and per contact row of the batch: the reset (body island flags and sweep
+// times, contact TOI flags, counts and cached times), then for every contact the scan would compute
+// a time of impact for, that time, cached on the contact as the scan caches it. After the reset every
+// sweep starts at alpha0 = 0 (a contact thread takes that value instead of waiting for its bodies'
+// reset), so the scan advances no sweep and each time of impact depends on its contact alone.
+// StepToiKernel's event loop then finds them cached. The body-flag bits the classification reads
+// (type, awake, bullet) are not the ones the reset clears.
+__global__ void __launch_bounds__(256, 2) ToiKernel(Batch B, float dt)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < B.bodyRows) {
+        const int w = B.bWorld[r];
+        WorldState* st = B.state + w;
+        if (!(st->continuous && dt > 0.0f && st->stepComplete)) return;
+        const int b = r - B.desc[w].bodyBase;
+        if (b == 0) st->toiPrepared = 1;
+        if (b < B.desc[w].bodyCount) {
+            B.bi[r].y &= ~kBIsland;
+            B.sw[r].w = 0.0f;
+        }
+        return;
+    }
+    const int q = r - B.bodyRows;
+    if (q >= B.contactRows) return;
+    const int w = B.cWorld[q];
+    WorldState* st = B.state + w;
+    if (!(st->continuous && dt > 0.0f && st->stepComplete)) return;
+    const int k = q - B.desc[w].contactBase;
+    if (k >= st->contactCount) return;
+    Wd W;
+    W.init(B, w);
+    const int c = W.order[k];
+    int4 info = W.ci[c];
+    info.x &= ~(kCToi | kCIsland);
+    info.w = 0;
+    float alpha = 1.0f;
+    if (W.toiKind(info) == 2) {
+        Sweep sA = W.sweep(W.fixBody(info.y)), sB = W.sweep(W.fixBody(info.z));
+        sA.alpha0 = 0.0f;
+        sB.alpha0 = 0.0f;
+        const float alpha0 = sA.alpha0;
+        int state;
+        float beta;
+        TimeOfImpact(&state, &beta, ProxyOf(W.shape[info.y]), ProxyOf(W.shape[info.z]), sA, sB, 1.0f);
+        alpha = state == kToiTouching ? Minf(alpha0 + (1.0f - alpha0) * beta, 1.0f) : 1.0f;
+        info.x |= kCToi;
+    }
+    W.cp[c].w = alpha;
+    W.ci[c] = info;
+}
+
+// The continuous phase of b2World::Step (b2World.cpp:948-958) and the end of the step: the TOI
+// event loop, force clearing, inv_dt0.
+__global__ void __launch_bounds__(128, B2G_STEP_MIN_BLOCKS) StepToiKernel(Batch B, StepParams P, const int* schedule, LaunchShape L)
+{
+    extern __shared__ float4 smem[];
+    Wd W;
+    W.init(B, schedule ? schedule[blockIdx.x] : blockIdx.x);
+    W.smemBase = smem;
+    W.smemBytes = (2 * L.smemRows + L.smemContacts) * (int)sizeof(float4);
+    const unsigned long long t0 = clock64();
     if (W.st->continuous && P.dt > 0.0f) W.solveTOI(P);
     __syncthreads();
     for (int b = tid(); b < W.d.bodyCount; b += nthreads()) W.frc[b] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (tid() == 0) {
         if (P.dt > 0.0f) W.st->inv_dt0 = 1.0f / P.dt;
-        const unsigned long long t4 = clock64();
-        W.st->cyc[0] = t1 - t0;
-        W.st->cyc[1] = t2 - t1;
-        W.st->cyc[6] = t4 - t3;
-        W.st->cyc[7] = t4 - t0;
+        const unsigned long long t1 = clock64();
+        W.st->cyc[6] = t1 - t0;
+        W.st->cyc[7] += t1 - t0;
     }
 }
 
 } // namespace b2g
 
-// Launch entry used by the host runtime (b2g_api.cu).
+// Launch entries used by the host runtime (b2g_api.cu). A step is b2gLaunchNarrowphase, then
+// b2gLaunchStep for every launch class, then b2gLaunchToi, then b2gLaunchStepToi for every class.
+cudaError_t b2gLaunchNarrowphase(const b2g::Batch& B, cudaStream_t stream)
+{
+    if (B.contactRows <= 0) return cudaSuccess;
+    b2g::NarrowphaseKernel<<<(B.contactRows + 255) / 256, 256, 0, stream>>>(B);
+    return cudaGetLastError();
+}
+
+cudaError_t b2gLaunchToi(const b2g::Batch& B, const b2g::StepParams& P, cudaStream_t stream)
+{
+    if (!(P.dt > 0.0f)) return cudaSuccess;
+    const long long rows = (long long)B.bodyRows + B.contactRows;
+    b2g::ToiKernel<<<(unsigned)((rows + 255) / 256), 256, 0, stream>>>(B, P.dt);
+    return cudaGetLastError();
+}
+
+static b2g::LaunchShape Shape(int smemRows, int smemContacts)
+{
+    b2g::LaunchShape L;
+    L.smemRows = smemRows;
+    L.smemContacts = smemContacts;
+    return L;
+}
+
 cudaError_t b2gLaunchStep(const b2g::Batch& B, const b2g::StepParams& P, const int* schedule, int first, int count,
                           int threads, int smemRows, int smemContacts, cudaStream_t stream)
 {
     if (count <= 0) return cudaSuccess;
-    b2g::LaunchShape L;
-    L.smemRows = smemRows;
-    L.smemContacts = smemContacts;
     const size_t smem = (2 * (size_t)smemRows + smemContacts) * sizeof(float4);
-    b2g::StepKernel<<<count, threads, smem, stream>>>(B, P, schedule + first, L);
+    b2g::StepKernel<<<count, threads, smem, stream>>>(B, P, schedule + first, Shape(smemRows, smemContacts));
+    return cudaGetLastError();
+}
+
+cudaError_t b2gLaunchStepToi(const b2g::Batch& B, const b2g::StepParams& P, const int* schedule, int first, int count,
+                             int threads, int smemRows, int smemContacts, cudaStream_t stream)
+{
+    if (count <= 0) return cudaSuccess;
+    const size_t smem = (2 * (size_t)smemRows + smemContacts) * sizeof(float4);
+    b2g::StepToiKernel<<<count, threads, smem, stream>>>(B, P, schedule + first, Shape(smemRows, smemContacts));
     return cudaGetLastError();
 }

@@ -64,6 +64,8 @@ struct WorldState {
     float maxPenetration; // deepest contact penetration (m) before the last step's position correction
     int eventCount;     // listener records of the last step in the world's event log
     int eventsDropped;  // 1 when the log ran out of room
+    int staged;         // 1 while this step's manifolds wait in the stage (NarrowphaseKernel -> collide)
+    int toiPrepared;    // 1 while this step's first time-of-impact pass is done (ToiKernel -> solveTOI)
     // SM clock cycles of the last step per phase: 0 new-fixture pairs, 1 collide, 2 island DFS,
     // 3 island solve, 4 fixture sync, 5 pairs after solve, 6 TOI, 7 whole step; then the island solve
     // split: 8 integrate + constraint init, 9 warm start + velocity sweeps, 10 impulses + position
@@ -71,7 +73,7 @@ struct WorldState {
     // creation (both summed over every UpdatePairs call of the step); the TOI split (summed over its
     // events): 16 contact classification and time of impact, 17 earliest-event selection, 18 event
     // mini-island build, 19 mini-island solve, 20 fixture sync and contact invalidation, 21 pair
-    // finding after events; 22, 23 unused
+    // finding after events; 22, 23 unused (the flat pre-pass kernels are not counted per world)
     unsigned long long cyc[kProfileSlots];
 };
 
@@ -131,11 +133,27 @@ struct __align__(16) PosConstraint {
 };
 struct TOITask { int contact; int kind; float alpha0; Sweep sa, sb; };
 
+// A contact's manifold as b2Contact::Update would leave it (evaluated, impulses matched by id) but
+// not yet committed, written by NarrowphaseKernel before the step and read by the collide phase.
+// It lives in the contact's VelConstraint slot, which is free until the island solve. tag is 1 when
+// the record belongs to this step; 0 when the contact was left to the collide phase.
+struct __align__(16) ManifoldStage {
+    int4 h;      // type, pointCount, id0, id1
+    float4 v;    // localNormal.xy, localPoint.xy
+    float4 p0;   // point 0: localPoint.xy, normalImpulse, tangentImpulse
+    float4 p1;   // point 1
+    int tag;
+};
+static_assert(sizeof(ManifoldStage) <= sizeof(VelConstraint), "the stage reuses a VelConstraint slot");
+
 // All columns of a batch. Per world, column x of world w starts at x + desc[w].<kind>Base.
 struct Batch {
     int worlds;
+    int bodyRows, contactRows;  // lengths of the body and contact columns (all worlds, padding included)
     WorldDesc* desc;
     WorldState* state;
+    int* bWorld;   // body-column row -> its world (the flat pre-pass kernels' map)
+    int* cWorld;   // contact-column row -> its world
     // bodies
     float4* xf;    // p.x, p.y, q.s, q.c
     float4* sw;    // c.x, c.y, a, alpha0

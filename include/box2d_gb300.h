@@ -213,7 +213,8 @@ gb_status gb_world_totals(gb_world* world, long long* out);
  * 11 position sweeps, 12 write-back, 13 sleep; 14 broadphase pair finding and sorting, 15 contact
  * creation; the continuous split 16 classification + time of impact, 17 earliest-event selection,
  * 18 event mini-island build, 19 mini-island solve, 20 fixture sync + contact invalidation,
- * 21 pair finding after events (22, 23 unused). */
+ * 21 pair finding after events (22, 23 unused). The narrowphase and time-of-impact pre-passes run
+ * flat over all worlds' contacts before the collide and continuous phases and are not counted. */
 #define GB_PROFILE_SLOTS 24
 gb_status gb_world_profile(gb_world* world, unsigned long long* out);
 

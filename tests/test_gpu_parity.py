@@ -106,3 +106,27 @@ def test_gpu_large_world_sweep_pairs_match_oracle(gpu):
             assert np.array_equal(gi, oi), f"contacts differ at step {s}"
             assert np.array_equal(gf.view(np.uint32), of.view(np.uint32)), f"manifolds differ at step {s}"
     w.sync()
+
+
+def test_gpu_toi_event_loop_matches_oracle(gpu):
+    """A drop whose fast bodies hit the container: many steps take several time-of-impact events, so
+    the event loop's later events (only the contacts an event touched are classified again) run
+    often; every body and contact matches the CPU oracle bit for bit after every step."""
+    sc = scenes.drop(400, scenes.SplitMix64(11), allow_sleep=False)
+    w = World(sc)
+    o = oracle.OracleWorld(sc, "port", "project")
+    events, multi = 0, 0
+    for s in range(1, 121):
+        w.step(DT, VI, PI)
+        o.step(DT, VI, PI)
+        e = w.stats(0)[1]
+        events += e
+        multi += e >= 2
+        gb, ob = w.bodies(0), o.bodies()
+        assert np.array_equal(gb.view(np.uint32), ob.view(np.uint32)), f"bodies differ at step {s}"
+        gi, gf = w.contacts(0)
+        oi, of = o.contacts()
+        assert np.array_equal(gi, oi), f"contacts differ at step {s}"
+        assert np.array_equal(gf.view(np.uint32), of.view(np.uint32)), f"manifolds differ at step {s}"
+    w.sync()
+    assert events >= 20 and multi >= 5, (events, multi)
