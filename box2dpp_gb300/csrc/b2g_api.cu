@@ -390,6 +390,10 @@ std::vector<LaunchPlan> CandidatePlans(const gb_world* g)
     c.push_back(SplitPlan(g, {256, 64}, {64, 32, 32}));
     c.push_back(SplitPlan(g, {96}, {64, 32}));
     c.push_back(SplitPlan(g, {320, 160, 64}, {128, 64, 32, 32}));
+    // the largest worlds set the step's critical path: a small first class with wider CTAs
+    c.push_back(SplitPlan(g, {400, 96}, {128, 64, 32}));
+    c.push_back(SplitPlan(g, {320, 96}, {128, 64, 32}));
+    c.push_back(SplitPlan(g, {400, 160}, {128, 64, 32}));
     return c;
 }
 

@@ -1324,14 +1324,14 @@ __device__ void Wd::solveTOI(const StepParams& P)
     // colourList, deduplicated by the event stamp in evType) are the only ones classified again; the
     // first pass classifies the whole list. These scratch columns belong to the collide and solve
     // phases, which set them before use.
-    __shared__ int sDirty;
+    __shared__ int sDirty, sNeed;
     __shared__ int sSortT[kMaxCta * 2], sSortC[kMaxCta * 2];
     if (tid() == 0) sDirty = 0;
     for (int event = 0;; ++event) {
         const int n = st->contactCount;
         const int nTask = event == 0 ? n : sDirty;
         const int* task = event == 0 ? order : colourList;
-        if (tid() == 0) sAdvance = 0;
+        if (tid() == 0) { sAdvance = 0; sNeed = 0; }
         if (event > 0 && nTask > 1) {
             // dirty contacts into list order (descending tail index), for the sweep advances below
             if (nTask <= 2 * kMaxCta) {
@@ -1400,6 +1400,7 @@ __device__ void Wd::solveTOI(const StepParams& P)
                         if ((activeA || activeB) && (collideA || collideB)) {
                             kind = 2;
                             if (sw[bA].w != sw[bB].w) sAdvance = 1;
+                            sStatus[atomicAdd(&sNeed, 1)] = k;
                         }
                     }
                 }
@@ -1448,9 +1449,10 @@ __device__ void Wd::solveTOI(const StepParams& P)
             }
         }
         __syncthreads();
-        for (int k = tid(); k < nTask; k += nthreads()) {
-            TOITask& T = toi[k];
-            if (T.kind != 2) continue;
+        // the times of impact, over the compacted list of tasks that need one (sStatus, filled by
+        // the classification in any order) so that every thread gets a share
+        for (int i = tid(); i < sNeed; i += nthreads()) {
+            TOITask& T = toi[sStatus[i]];
             int4 info = ci[T.contact];
             int state;
             float beta;
