@@ -138,6 +138,11 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# steps timed stage by stage after the timed region (gb_world_stage_times)
+STAGE_STEPS = 5
+STAGE_KERNELS = ["b2g::NarrowphaseKernel", "b2g::StepKernel", "b2g::ToiKernel", "b2g::StepToiKernel"]
+
+
 def launches_per_step(n_classes: int) -> int:
     """Kernel launches of one step: the flat NarrowphaseKernel and ToiKernel, and StepKernel and
     StepToiKernel once per class of the launch plan."""
@@ -154,10 +159,11 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-# DRAM bytes (read + write) per algorithmic byte of the coloured StepKernel, from one full ncu capture
-# of the 1024-world case of this workload (275.6 MB of traffic for 41.4 MB algorithmic); traffic
-# grows with the units processed, so the full launch's traffic is this ratio x its algorithmic bytes.
-TRAFFIC_PER_ALGORITHMIC_BYTE = 275.6 / 41.4
+# DRAM bytes (read + write) per algorithmic byte of StepKernel (coloured solver), from one full ncu
+# capture of the 1024-world case of this workload (109.6 MB read + 78.9 MB written for 41.4 MB
+# algorithmic, profiles/StepKernel_coloured_1024_worlds.md); traffic grows with the units processed,
+# so the full launch's traffic is this ratio x its algorithmic bytes.
+TRAFFIC_PER_ALGORITHMIC_BYTE = 188.5 / 41.4
 
 
 def algorithmic_bytes(t: dict) -> int:
@@ -285,6 +291,14 @@ def run_gpu(args):
     w.sync()
     t_after = w.totals()
     _, _, res = w.solver_stats()
+    # per-stage device times of a few more steps (CUDA events between the step's launch stages), with
+    # the same steps' work counts for the roofline of the stage that carries the step's state traffic
+    stage_ms = np.zeros(4)
+    stage_bytes = []
+    for _ in range(STAGE_STEPS):
+        stage_ms += w.stage_times(DT, vi, PI)
+        stage_bytes.append(algorithmic_bytes(w.totals()))
+    stage_ms /= STAGE_STEPS
     ms_max = max_over_ranks(ms)
     total_bodies = n_dyn * world_size
     value = total_bodies * args.steps / (ms_max / 1e3)
@@ -337,16 +351,23 @@ def run_gpu(args):
 
     if rank == 0:
         peak, peak_kind = measured_peaks()
-        step_bytes = (algorithmic_bytes(t_before) + algorithmic_bytes(t_after)) / 2.0
-        per_launch_ms = ms / args.steps
-        achieved = step_bytes / (per_launch_ms / 1e3) / 1e9
+        step_bytes = float(np.mean(stage_bytes))
+        kernel_ms = float(stage_ms[1])
+        achieved = step_bytes / (kernel_ms / 1e3) / 1e9
+        total_stage = float(stage_ms.sum())
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": step_bytes * TRAFFIC_PER_ALGORITHMIC_BYTE, "peak_source": peak_kind,
-                "traffic_note": "bytes per step, scaled from an ncu capture of the 1024-world case",
+                "traffic_note": "DRAM bytes per launch stage, scaled from an ncu capture of StepKernel on the "
+                                "1024-world case (traffic per algorithmic byte)",
                 "kernel": "b2g::StepKernel",
                 "algorithmic_bytes_per_launch": step_bytes,
-                "launch_ms": per_launch_ms,
-                "note": "one step = the launches of the plan (one per class); bytes and time are per step",
+                "launch_ms": kernel_ms,
+                "note": "StepKernel's stage (every class of the plan) carries the step's persistent-state "
+                        "traffic (collide commit, island solve, fixture sync, pair finding); its bytes per "
+                        f"step over its CUDA-event duration, averaged over {STAGE_STEPS} steps after the timed "
+                        "region",
+                "stages": {k: {"ms": float(m), "share": float(m) / total_stage}
+                           for k, m in zip(STAGE_KERNELS, stage_ms)},
                 "counts_per_step": {k: (t_before[k] + t_after[k]) / 2.0 for k in
                                     ("solved_bodies", "solved_contacts", "proxies", "pairs", "toi_events")}}
         line = {

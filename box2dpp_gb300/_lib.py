@@ -30,6 +30,7 @@ EXPORTS = [
     "gb_mlp_forward", "gb_mlp_gradients", "gb_mlp_train", "gb_world_set_warm_start", "gb_world_warm_stats",
     "gb_world_set_contact_log", "gb_world_read_contact_log", "gb_world_contact_stats", "gb_world_set_events",
     "gb_world_read_events", "gb_world_query_aabb", "gb_world_raycast", "gb_create_joints",
+    "gb_world_stage_times",
 ]
 
 
@@ -125,6 +126,7 @@ def load(build_if_missing: bool = True):
         "gb_set_forces": [vp, vp],
         "gb_get_transforms": [vp, vp],
         "gb_world_profile": [vp, np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")],
+        "gb_world_stage_times": [vp, f, i, i, _f32],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

@@ -1448,6 +1448,32 @@ gb_status gb_world_profile(gb_world* g, unsigned long long* out)
     return GB_OK;
 }
 
+gb_status gb_world_stage_times(gb_world* g, float dt, int vi, int pi, float* ms)
+{
+    if (!g || !ms || vi < 0 || pi < 0 || g->tuneIndex >= 0) return GB_ERR_INVALID;
+    gb_status s = Upload(g);
+    if (s != GB_OK) return s;
+    cudaEvent_t e[5] = {};
+    cudaError_t err = cudaSuccess;
+    for (int i = 0; i < 5 && err == cudaSuccess; ++i) err = cudaEventCreate(&e[i]);
+    const StepParams P = MakeParams(g, dt, vi, pi);
+    if (err == cudaSuccess) err = cudaEventRecord(e[0], g->stream);
+    if (err == cudaSuccess) err = b2gLaunchNarrowphase(g->batch, g->stream);
+    if (err == cudaSuccess) err = cudaEventRecord(e[1], g->stream);
+    if (err == cudaSuccess) s = LaunchClasses(g, P, g->plan, b2gLaunchStep);
+    if (err == cudaSuccess && s == GB_OK) err = cudaEventRecord(e[2], g->stream);
+    if (err == cudaSuccess && s == GB_OK) err = b2gLaunchToi(g->batch, P, g->stream);
+    if (err == cudaSuccess && s == GB_OK) err = cudaEventRecord(e[3], g->stream);
+    if (err == cudaSuccess && s == GB_OK) s = LaunchClasses(g, P, g->plan, b2gLaunchStepToi);
+    if (err == cudaSuccess && s == GB_OK) err = cudaEventRecord(e[4], g->stream);
+    if (err == cudaSuccess && s == GB_OK) err = cudaEventSynchronize(e[4]);
+    for (int i = 0; i < 4 && err == cudaSuccess && s == GB_OK; ++i) err = cudaEventElapsedTime(&ms[i], e[i], e[i + 1]);
+    for (cudaEvent_t x : e)
+        if (x) cudaEventDestroy(x);
+    if (err != cudaSuccess) return GB_ERR_CUDA;
+    return s;
+}
+
 // Bodies of consecutive worlds are consecutive rows of the body columns (one row of padding only
 // for a world without bodies), so whole-batch transfers are single copies.
 static bool BodyRowsContiguous(const gb_world* g)

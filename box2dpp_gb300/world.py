@@ -230,6 +230,14 @@ class World:
         _lib.check(self.lib.gb_world_profile(self.h, out), "gb_world_profile")
         return out.reshape(self.n_worlds, len(self.PHASES))
 
+    STAGES = ["narrowphase_prepass", "step", "toi_prepass", "continuous"]
+
+    def stage_times(self, dt: float = 1.0 / 60.0, vi: int = 8, pi: int = 3) -> np.ndarray:
+        """Milliseconds of the four launch stages of one (real) step, see STAGES and gb_world_stage_times."""
+        out = np.zeros(4, dtype=np.float32)
+        _lib.check(self.lib.gb_world_stage_times(self.h, float(dt), int(vi), int(pi), out), "gb_world_stage_times")
+        return out
+
     @property
     def total_bodies(self) -> int:
         return int(sum(self.n_bodies))

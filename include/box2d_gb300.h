@@ -218,6 +218,15 @@ gb_status gb_world_totals(gb_world* world, long long* out);
 #define GB_PROFILE_SLOTS 24
 gb_status gb_world_profile(gb_world* world, unsigned long long* out);
 
+/* One b2World::Step of every world (a real step, with the current plan, not from the captured
+ * graph), timed stage by stage with CUDA events on the handle's stream: ms[0] the narrowphase
+ * pre-pass, ms[1] the per-world step up to the continuous phase (every class), ms[2] the
+ * time-of-impact pre-pass, ms[3] the per-world continuous phase (every class). The whole-batch
+ * counterpart of b2World::GetProfile's step timings (Box2D/Dynamics/b2World.h:196, b2Profile in
+ * b2TimeStep.h:27-37); blocks until the step is done. */
+gb_status gb_world_stage_times(gb_world* world, float dt, int velocity_iterations, int position_iterations,
+                               float* ms);
+
 /* Whole-batch b2Body::ApplyForceToCenter + ApplyTorque for the next step (Box2D/Dynamics/b2Body.h:
  * 437-468): forces[4] per body of every world in world order then creation order = force.x,
  * force.y, torque, unused. The host array is copied to the device asynchronously on the handle's
