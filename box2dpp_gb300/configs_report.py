@@ -1,0 +1,95 @@
+"""Throughput of the single-world configurations on the GPU, beside the CPU restatement of the
+reference step on one host core, on the same seeded scenes.
+
+  python -m box2dpp_gb300.configs_report [--configs 1,2,5] [--cpu-seconds 15]
+
+Configurations (the batched one is bench.py's):
+  1  the 210-box pyramid on an edge ground, sleep on (the reference default), 600 steps;
+  2  10,000 circles and convex polygons dropped into a 200 m edge box, sleep off, steps 1..200;
+  5  65,536 bodies with 512 revolute chains of 16 links in a 300 m container spinning at 0.05 rad/s,
+     sleep off, steps 1..60.
+
+GPU: one world per handle, the plain (reference-order, bit-exact) and the graph-coloured solver,
+8/3 iterations, each step timed with CUDA events on the handle's stream; body-steps/s over the timed
+steps. CPU: the oracle's restatement of b2World::Step (plain order, project trig) on one thread,
+stepped from the same initial state for as many of the same steps as fit in --cpu-seconds. Prints
+one JSON line per configuration.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+DT, VI, PI = 1.0 / 60.0, 8, 3
+
+
+def scene(cfg: int):
+    from . import scenes
+
+    if cfg == 1:
+        return scenes.config1(), 600
+    if cfg == 2:
+        return scenes.config2(10000, seed=1, allow_sleep=False), 200
+    if cfg == 5:
+        return scenes.config5(allow_sleep=False), 60
+    raise ValueError(cfg)
+
+
+def gpu_rate(sc, steps: int, solver: str) -> dict:
+    import torch
+
+    from .world import World
+
+    w = World(sc)
+    w.set_solver(solver)
+    stream = torch.cuda.Stream()
+    w.set_stream(stream.cuda_stream)
+    w.upload()
+    ms = []
+    for _ in range(steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        w.step(DT, VI, PI)
+        b.record(stream)
+        b.synchronize()
+        ms.append(a.elapsed_time(b))
+    w.sync()
+    n = w.dynamic_bodies
+    w.close()
+    return {"solver": solver, "steps": steps, "ms_per_step_mean": float(np.mean(ms)),
+            "ms_per_step_median": float(np.median(ms)), "body_steps_per_s": n * steps / (sum(ms) / 1e3)}
+
+
+def cpu_rate(sc, steps: int, budget_s: float) -> dict:
+    import oracle
+
+    w = oracle.OracleWorld(sc, "port", "project")
+    n = sum(1 for b in sc.bodies if b[0] == 2)
+    done, t0 = 0, time.perf_counter()
+    while done < steps and time.perf_counter() - t0 < budget_s:
+        w.step(DT, VI, PI)
+        done += 1
+    el = time.perf_counter() - t0
+    return {"cores": 1, "kind": "port", "steps": done, "seconds": round(el, 2), "body_steps_per_s": n * done / el,
+            "sample": f"steps 1..{done} of the same scene on one thread"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--configs", default="1,2,5")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    a = ap.parse_args()
+    for cfg in [int(c) for c in a.configs.split(",")]:
+        sc, steps = scene(cfg)
+        n = sum(1 for b in sc.bodies if b[0] == 2)
+        line = {"config": cfg, "dynamic_bodies": n, "joints": len(sc.joints), "sleep": bool(sc.allow_sleep),
+                "gpu": [gpu_rate(sc, steps, s) for s in ("plain", "coloured")],
+                "cpu": cpu_rate(sc, steps, a.cpu_seconds)}
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()
