@@ -554,7 +554,7 @@ gb_status Upload(gb_world* g)
     FreeDevice(g);
     const int nw = (int)g->worlds.size();
     g->desc.assign(nw, WorldDesc{});
-    long long tb = 0, tf = 0, tp = 0, tc = 0, tj = 0, tq = 0, tr = 0;
+    long long tb = 0, tf = 0, tp = 0, tc = 0, tj = 0, tq = 0, tr = 0, tt = 0;
     for (int wi = 0; wi < nw; ++wi) {
         HWorld& W = g->worlds[wi];
         WorldDesc& d = g->desc[wi];
@@ -568,8 +568,13 @@ gb_status Upload(gb_world* g)
         d.jointBase = (int)tj; d.jointCount = (int)W.joints.size();
         d.pairBase = (int)tq; d.pairCap = NextPow2(std::max(256, cap));
         d.rowBase = (int)tr; d.rowCap = d.bodyCount + cap + d.jointCount + 2 * kMaxTOIContacts;
+        // island-DFS table: 29 bytes per body, a bit per contact slot, 16 bytes per table entry for up
+        // to 8 entries per body (a world that needs more takes the DFS without a table)
+        const long long islBytes = ((29ll * d.bodyCount + 4ll * ((cap + 31) / 32) + 16ll * (8ll * d.bodyCount + 64) +
+                                     128) + 15) & ~15ll;
+        d.islTabBase = tt; d.islTabBytes = (int)std::min<long long>(islBytes, 1ll << 30);
         tb += std::max(1, d.bodyCount); tf += std::max(1, d.fixCount); tp += d.proxyCap; tc += cap;
-        tj += std::max(1, d.jointCount); tq += d.pairCap; tr += d.rowCap;
+        tj += std::max(1, d.jointCount); tq += d.pairCap; tr += d.rowCap; tt += d.islTabBytes;
     }
     if (tb > (1LL << 31) - 1 || tc > (1LL << 31) - 1 || tq > (1LL << 31) - 1 || tr > (1LL << 31) - 1)
         return GB_ERR_CAPACITY;
@@ -592,7 +597,7 @@ gb_status Upload(gb_world* g)
     ALLOC(sContact, tc); ALLOC(sStatus, tc); ALLOC(vc, tc); ALLOC(pc, tc); ALLOC(vimp, tc); ALLOC(vimpL, tc); ALLOC(vsep, tc); ALLOC(toi, tc); ALLOC(cColour, tc); ALLOC(colourList, tc);
     ALLOC(evType, tc);
     if (g->eventsEnabled) { ALLOC(evLog, 8 * tc); } else { B.evLog = nullptr; }
-    ALLOC(pairs, tq); ALLOC(pairKeep, tq); ALLOC(pairInfo, tq);
+    ALLOC(pairs, tq); ALLOC(pairKeep, tq); ALLOC(pairInfo, tq); ALLOC(islTab, tt);
 #undef ALLOC
     GB_CUDA(cudaMemcpy(B.desc, g->desc.data(), nw * sizeof(WorldDesc), cudaMemcpyHostToDevice));
     std::vector<WorldState> states(nw);

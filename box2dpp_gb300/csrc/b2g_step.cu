@@ -67,6 +67,7 @@ struct Wd {
     int* movedList;
     int* sweepRank;
     int4* pairInfo;
+    unsigned char* islTab; // the world's global island-table region (d.islTabBytes bytes)
     float4* smemBase;   // the CTA's dynamic shared memory, free outside the island solve
     int smemBytes;
 
@@ -92,6 +93,7 @@ struct Wd {
         evLog = B.evLog ? B.evLog + 8 * (size_t)c : nullptr;
         evCap = 4 * d.contactCap;
         pairs = B.pairs + q; pairKeep = B.pairKeep + q; pairInfo = B.pairInfo + q;
+        islTab = B.islTab ? B.islTab + d.islTabBase : nullptr;
         smemBase = nullptr;
         smemBytes = 0;
     }
@@ -377,7 +379,9 @@ struct Wd {
     __device__ void sweepPairs(int m, int* pairCount);
     __device__ void collide();
     __device__ void solve(const StepParams& P, float4* smem, int smemRows, int smemContacts);
-    __device__ bool buildIslandsShared(bool coloured, int* colourCount, int& nIsl, int& nRows, int& nCons, int& movers);
+    template <class L>
+    __device__ bool buildIslandsTable(unsigned char* base, int capacity, bool coloured, int* colourCount, int& nIsl,
+                                      int& nRows, int& nCons, int& movers);
     __device__ void solveIslands(const StepParams& P, int nIsl, int nRows, int nContacts, float4* smem, int smemRows,
                                  int smemContacts, const int* colourStart);
     __device__ void solveTOI(const StepParams& P);
@@ -443,6 +447,89 @@ __device__ void ctaSortKeys(unsigned long long* keys, int n, int capacity)
     }
 }
 
+// Stable LSD radix sort (8-bit digits) of n 64-bit keys in global memory over the CTA, ping-ponging
+// between keys and tmp (n slots each); the sorted keys end in keys. A digit position where every key
+// has the same byte is skipped (its pass would not move anything). For arrays too large for shared
+// memory this replaces the bitonic network, whose log^2 n passes over global memory dominate large
+// worlds; both give the same order (equal keys are equal values). work: kRadixWork ints of shared
+// memory (the digit bases and the per-warp tile counts); the caller checks RadixSortFits first.
+constexpr int kRadixWork = 256 + (kMaxCta / 32) * 256;
+__device__ inline bool RadixSortFits(int n, int workBytes)
+{
+    // tile stamps are packed with a 6-bit count into an int: at most 2^24 tiles over all passes
+    return workBytes >= kRadixWork * (int)sizeof(int) && (long long)((n + 31) / 32) * 8 < (1ll << 24);
+}
+__device__ void ctaRadixSort(unsigned long long* keys, unsigned long long* tmp, int n, int* work)
+{
+    __shared__ unsigned long long sOr, sAnd;
+    int* sBase = work;
+    int (*sTileCnt)[256] = reinterpret_cast<int (*)[256]>(work + 256);
+    if (n <= 1) return;
+    const int T = nthreads(), t = tid(), lane = t & 31, warp = t >> 5;
+    if (t == 0) { sOr = 0ull; sAnd = ~0ull; }
+    for (int i = t; i < (kMaxCta / 32) * 256; i += T) work[256 + i] = -1;
+    __syncthreads();
+    {
+        unsigned long long o = 0ull, a = ~0ull;
+        for (int i = t; i < n; i += T) { o |= keys[i]; a &= keys[i]; }
+        atomicOr(&sOr, o);
+        atomicAnd(&sAnd, a);
+    }
+    __syncthreads();
+    const unsigned long long varying = sOr ^ sAnd;
+    const int nTiles = (n + T - 1) / T;
+    unsigned long long* src = keys;
+    unsigned long long* dst = tmp;
+    int stampBase = 0;
+    for (int shift = 0; shift < 64; shift += 8) {
+        if (((varying >> shift) & 0xffull) == 0ull) continue;
+        for (int dg = t; dg < 256; dg += T) sBase[dg] = 0;
+        __syncthreads();
+        for (int i = t; i < n; i += T) atomicAdd(&sBase[(int)((src[i] >> shift) & 0xffull)], 1);
+        __syncthreads();
+        if (t == 0) {
+            int run = 0;
+            for (int dg = 0; dg < 256; ++dg) { const int c = sBase[dg]; sBase[dg] = run; run += c; }
+        }
+        __syncthreads();
+        // tiles of T consecutive keys: a key's place is its digit's base, plus the keys with the same
+        // digit in earlier warps of the tile (sTileCnt, stamped with the tile), plus its rank in its
+        // warp (lanes in index order), which keeps the pass stable
+        for (int tile = 0; tile < nTiles; ++tile) {
+            const int i = tile * T + t;
+            const bool valid = i < n;
+            const unsigned long long key = valid ? src[i] : 0ull;
+            const int dg = valid ? (int)((key >> shift) & 0xffull) : 256;
+            const unsigned peers = __match_any_sync(0xffffffffu, dg);
+            const int rank = __popc(peers & ((1u << lane) - 1u));
+            const bool leader = rank == 0;
+            const int cnt = __popc(peers);
+            const int stamp = stampBase + tile;
+            if (valid && leader) sTileCnt[warp][dg] = (stamp << 6) | cnt;
+            __syncthreads();
+            if (valid) {
+                int off = 0;
+                for (int w2 = 0; w2 < warp; ++w2) {
+                    const int v = sTileCnt[w2][dg];
+                    if ((v >> 6) == stamp) off += v & 63;
+                }
+                dst[sBase[dg] + off + rank] = key;
+            }
+            __syncthreads();
+            if (valid && leader) atomicAdd(&sBase[dg], cnt);
+            __syncthreads();
+        }
+        stampBase += nTiles;
+        unsigned long long* x = src;
+        src = dst;
+        dst = x;
+    }
+    if (src != keys) {
+        for (int i = t; i < n; i += T) keys[i] = src[i];
+        __syncthreads();
+    }
+}
+
 // ------------------------------------------------------------------ FindNewContacts
 // Above this many moved x all proxy tests, pair finding sorts and sweeps instead.
 constexpr long long kSweepThreshold = 1ll << 20;
@@ -500,6 +587,7 @@ __device__ void Wd::sweepPairs(int m, int* pairCount)
     }
     __syncthreads();
     const int cap = 2 * d.pairCap;
+    int* radixWork = reinterpret_cast<int*>(smemBase);
     int P2 = 1;
     while (P2 < nLive) P2 <<= 1;
     if (P2 * (int)sizeof(unsigned long long) <= smemBytes) {
@@ -509,6 +597,9 @@ __device__ void Wd::sweepPairs(int m, int* pairCount)
         ctaSortKeys(sk, nLive, P2);
         for (int i = tid(); i < nLive; i += nthreads()) keys[i] = sk[i];
         __syncthreads();
+    } else if (RadixSortFits(nLive, smemBytes)) {
+        // the second half of the pair-info scratch (2 x pairCap keys, nLive <= pairCap) as the buffer
+        ctaRadixSort(keys, keys + d.pairCap, nLive, radixWork);
     } else {
         ctaSortKeys(keys, nLive, cap);
     }
@@ -624,6 +715,10 @@ __device__ void Wd::findNewContacts()
             ctaSortKeys(sKeys, n, P2);
             for (int i = tid(); i < n; i += nthreads()) pairs[i] = sKeys[i];
             __syncthreads();
+        } else if (n > 1 && RadixSortFits(n, smemBytes)) {
+            // the pair-info scratch is free until contact creation: the radix sort's buffer; its work
+            // arrays in the shared memory (free again once the pairs are found)
+            ctaRadixSort(pairs, reinterpret_cast<unsigned long long*>(pairInfo), n, reinterpret_cast<int*>(smemBase));
         } else if (n > 1) {
             ctaSortKeys(pairs, n, d.pairCap);
         }
@@ -897,44 +992,77 @@ __device__ void Wd::collide()
 // b2World::Solve (Dynamics/b2World.cpp:388-577). The island DFS runs on one thread (it fixes the
 // contact order inside every island); islands are then solved in parallel, one per thread, because
 // they share no dynamic body.
-// The island DFS of b2World::Solve (Dynamics/b2World.cpp:422-510) with its working set in shared
-// memory, for worlds whose set fits. A parallel pre-pass flattens the edge list of every non-static
-// body into a table of its eligible contacts (enabled, touching, no sensor) in list order, and copies
-// the body-list links and body flags; thread 0 then runs the DFS on that table. Contacts, joints and
-// bodies are visited in exactly the order of the global DFS, so islands, rows and contact order (and
-// colours) are the same; island flags, wakes and contact island flags are written back in parallel
-// afterwards (they are idempotent and nothing in the DFS reads them back from global memory).
-// Returns false (nothing written outside shared memory) when the world does not fit.
-__device__ bool Wd::buildIslandsShared(bool coloured, int* colourCount, int& nIslOut, int& nRowsOut, int& nConsOut,
-                                       int& moversOut)
+// The island DFS of b2World::Solve (Dynamics/b2World.cpp:422-510) from a table: a parallel pre-pass
+// flattens the edge list of every non-static body into a table of its eligible contacts (enabled,
+// touching, no sensor) in list order, and copies the body-list links and body flags; thread 0 then
+// runs the DFS on that table. Contacts, joints and bodies are visited in exactly the order of the
+// global DFS, so islands, rows and contact order (and colours) are the same; island flags, wakes and
+// contact island flags are written back in parallel afterwards (they are idempotent and nothing in
+// the DFS reads them back from global memory).
+// Two table layouts: IslPacked (16-bit body and 15-bit contact indices, four bytes per entry) in the
+// CTA's shared memory, and IslWide (32-bit indices) in the world's global table region, for worlds
+// whose packed table does not fit or whose indices do not pack.
+// Returns false (nothing written outside the table region) when the world does not fit the layout.
+struct IslPacked {
+    using Idx = unsigned short;
+    using Entry = unsigned;
+    using Pair = unsigned;
+    static constexpr int kMaxBodies = 65536, kMaxContacts = 32768;
+    __device__ static Entry entry(int c, int side, int other) { return ((unsigned)c << 17) | ((unsigned)side << 16) | (unsigned)other; }
+    __device__ static int contact(Entry u) { return (int)(u >> 17); }
+    __device__ static int side(Entry u) { return (int)((u >> 16) & 1u); }
+    __device__ static int other(Entry u) { return (int)(u & 0xffffu); }
+    __device__ static Pair pair(int a, int b) { return (unsigned)a | ((unsigned)b << 16); }
+    __device__ static int pairA(Pair p) { return (int)(p & 0xffffu); }
+    __device__ static int pairB(Pair p) { return (int)(p >> 16); }
+};
+struct IslWide {
+    using Idx = int;
+    using Entry = int2;
+    using Pair = int2;
+    static constexpr int kMaxBodies = 1 << 30, kMaxContacts = 1 << 29;
+    __device__ static Entry entry(int c, int side, int other) { return make_int2((c << 1) | side, other); }
+    __device__ static int contact(Entry u) { return u.x >> 1; }
+    __device__ static int side(Entry u) { return u.x & 1; }
+    __device__ static int other(Entry u) { return u.y; }
+    __device__ static Pair pair(int a, int b) { return make_int2(a, b); }
+    __device__ static int pairA(Pair p) { return p.x; }
+    __device__ static int pairB(Pair p) { return p.y; }
+};
+
+template <class L>
+__device__ bool Wd::buildIslandsTable(unsigned char* base, int capacity, bool coloured, int* colourCount, int& nIslOut,
+                                      int& nRowsOut, int& nConsOut, int& moversOut)
 {
+    using Idx = typename L::Idx;
+    using Entry = typename L::Entry;
+    using Pair = typename L::Pair;
     __shared__ int sE, sOk, sIsl, sRowsS, sConsS, sMovers;
     enum : unsigned char { fIsl = 1, fStatic = 2, fAwake = 4, fActive = 8, fDynamic = 16, fJoints = 32 };
     const int nb = d.bodyCount, C = d.contactCap;
-    if (nb >= 65536 || C >= 32768 || nb == 0) return false;
-    // layout (bytes): masks 8nb | off 4(nb+1) | next 4nb | stack 4nb | cbits 4ceil(C/32) | local 2nb |
-    // statics 2nb | bflag nb | entries 4E | island contact pairs 4E (a contact with a static body has one entry)
-    auto up4 = [](int x) { return (x + 3) & ~3; };
-    const int oMask = 0;
-    const int oOff = oMask + (coloured ? 8 * nb : 0);
-    const int oNext = oOff + 4 * (nb + 1);
-    const int oStack = oNext + 4 * nb;
-    const int oBits = oStack + 4 * nb;
-    const int oLocal = oBits + 4 * ((C + 31) / 32);
-    const int oStatics = oLocal + up4(2 * nb);
-    const int oFlag = oStatics + up4(2 * nb);
-    const int oEntries = oFlag + up4(nb);
-    if (oEntries > smemBytes) return false;
-    unsigned char* base = reinterpret_cast<unsigned char*>(smemBase);
+    if (!base || nb >= L::kMaxBodies || C >= L::kMaxContacts || nb == 0) return false;
+    // layout (bytes): masks 8nb | off 4(nb+1) | next 4nb | stack 4nb | cbits 4ceil(C/32) | local |
+    // statics | bflag nb | entries E | island contact pairs E (a contact with a static body has one entry)
+    auto up = [](long long x) { return (x + 7) & ~7ll; };
+    const long long oMask = 0;
+    const long long oOff = oMask + (coloured ? 8ll * nb : 0);
+    const long long oNext = oOff + 4ll * (nb + 1);
+    const long long oStack = oNext + 4ll * nb;
+    const long long oBits = oStack + 4ll * nb;
+    const long long oLocal = up(oBits + 4ll * ((C + 31) / 32));
+    const long long oStatics = up(oLocal + (long long)sizeof(Idx) * nb);
+    const long long oFlag = up(oStatics + (long long)sizeof(Idx) * nb);
+    const long long oEntries = up(oFlag + nb);
+    if (oEntries > capacity) return false;
     unsigned long long* mask = reinterpret_cast<unsigned long long*>(base + oMask);
     int* off = reinterpret_cast<int*>(base + oOff);
     int* next = reinterpret_cast<int*>(base + oNext);
     int* stack = reinterpret_cast<int*>(base + oStack);
     unsigned* cbits = reinterpret_cast<unsigned*>(base + oBits);
-    unsigned short* local = reinterpret_cast<unsigned short*>(base + oLocal);
-    unsigned short* statics = reinterpret_cast<unsigned short*>(base + oStatics);
+    Idx* local = reinterpret_cast<Idx*>(base + oLocal);
+    Idx* statics = reinterpret_cast<Idx*>(base + oStatics);
     unsigned char* bflag = base + oFlag;
-    unsigned* entries = reinterpret_cast<unsigned*>(base + oEntries);
+    Entry* entries = reinterpret_cast<Entry*>(base + oEntries);
     auto eligible = [&](int e, int& other) {
         const int4 info = ci[e >> 1];
         other = (e & 1) == 0 ? fixBody(info.z) : fixBody(info.y);
@@ -965,21 +1093,22 @@ __device__ bool Wd::buildIslandsShared(bool coloured, int* colourCount, int& nIs
     if (tid() == 0) {
         off[0] = 0;
         for (int b = 0; b < nb; ++b) off[b + 1] += off[b];
-        const int E = off[nb];
-        sE = E;
-        sOk = oEntries + 8 * E + 4 <= smemBytes ? 1 : 0;  // the table, then one pair slot per possible island contact
+        const long long E = off[nb];
+        sE = (int)E;
+        // the table, then one pair slot per possible island contact
+        sOk = oEntries + (long long)(sizeof(Entry) + sizeof(Pair)) * E + 8 <= capacity ? 1 : 0;
     }
     __syncthreads();
     if (!sOk) return false;
     const int E = sE;
-    unsigned* icPairs = entries + E;
-    // pre-pass 2: the table, (contact << 17) | (side << 16) | other body, in list order
+    Pair* icPairs = reinterpret_cast<Pair*>(entries + E);
+    // pre-pass 2: the table, {contact, side, other body} in list order
     for (int b = tid(); b < nb; b += nthreads()) {
         if (bflag[b] & fStatic) continue;
         int k = off[b];
         B2G_WALK(e, bi[b].w, eNext(e), 2 * C + 2) {
             int other;
-            if (eligible(e, other)) entries[k++] = ((unsigned)(e >> 1) << 17) | ((unsigned)(e & 1) << 16) | (unsigned)other;
+            if (eligible(e, other)) entries[k++] = L::entry(e >> 1, e & 1, other);
         }
     }
     __syncthreads();
@@ -999,21 +1128,20 @@ __device__ bool Wd::buildIslandsShared(bool coloured, int* colourCount, int& nIs
                 const int b = stack[--stackCount];
                 if (bCur >= d.rowCap) { atomicOr(&st->error, kErrCapacity); stackCount = 0; break; }
                 const int loc = bCur - bStart;
-                local[b] = (unsigned short)loc;
+                local[b] = (Idx)loc;
                 bj[b].z = loc;
                 if (coloured) mask[loc] = 0ull;
                 sBody[bCur++] = b;
                 const unsigned char fb = bflag[b];
-                if (fb & fStatic) { statics[nStatics++] = (unsigned short)b; continue; }
+                if (fb & fStatic) { statics[nStatics++] = (Idx)b; continue; }
                 ++movers;
                 for (int k = off[b], ke = off[b + 1]; k < ke; ++k) {
-                    const unsigned u = entries[k];
-                    const int c = (int)(u >> 17), other = (int)(u & 0xffffu);
+                    const Entry u = entries[k];
+                    const int c = L::contact(u), other = L::other(u);
                     const unsigned bit = 1u << (c & 31);
                     if (cbits[c >> 5] & bit) continue;
                     cbits[c >> 5] |= bit;
-                    icPairs[cCur - cStart] = (u >> 16) & 1u ? ((unsigned)other | ((unsigned)b << 16))
-                                                            : ((unsigned)b | ((unsigned)other << 16));
+                    icPairs[cCur - cStart] = L::side(u) ? L::pair(other, b) : L::pair(b, other);
                     sContact[cCur++] = c;
                     if (bflag[other] & fIsl) continue;
                     stack[stackCount++] = other;
@@ -1037,8 +1165,8 @@ __device__ bool Wd::buildIslandsShared(bool coloured, int* colourCount, int& nIs
             islandJ[nIsl] = make_int2(jStart, jCur - jStart);
             ++nIsl;
             for (int i = cStart; i < cCur; ++i) {
-                const unsigned pr = icPairs[i - cStart];
-                const int bA = (int)(pr & 0xffffu), bB = (int)(pr >> 16);
+                const Pair pr = icPairs[i - cStart];
+                const int bA = L::pairA(pr), bB = L::pairB(pr);
                 const int lA = local[bA], lB = local[bB];
                 vc[i].idx = make_int4(bStart + lA, bStart + lB, 0, 0);
                 if (coloured) {
@@ -1103,7 +1231,11 @@ __device__ void Wd::solve(const StepParams& P, float4* smem, int smemRows, int s
     const int smemMaskRows = 2 * smemRows;
     auto mask = [&](int r) -> unsigned long long& { return r < smemMaskRows ? smemMask[r] : rowMask[r]; };
     int fIsl = 0, fRows = 0, fCons = 0, fMovers = 0;
-    const bool fast = buildIslandsShared(coloured, sColourStart + 1, fIsl, fRows, fCons, fMovers);
+    bool fast = buildIslandsTable<IslPacked>(reinterpret_cast<unsigned char*>(smemBase), smemBytes, coloured,
+                                             sColourStart + 1, fIsl, fRows, fCons, fMovers);
+    if (!fast)
+        fast = buildIslandsTable<IslWide>(islTab, d.islTabBytes, coloured, sColourStart + 1, fIsl, fRows, fCons,
+                                          fMovers);
     if (fast) {
         if (tid() == 0) {
             sIslands = fIsl;

@@ -35,6 +35,9 @@ struct WorldDesc {
     int pairBase, pairCap;
     // island rows: a static body is a row of every island it touches, so rows can exceed bodies
     int rowBase, rowCap;
+    // island-table region (bytes) for the DFS when its table does not fit in shared memory
+    long long islTabBase;
+    int islTabBytes;
 };
 
 constexpr int kProfileSlots = 24;
@@ -217,6 +220,7 @@ struct Batch {
     int4* pairInfo;  // pair-sized: a new contact's fixtures and bodies, worked out before creation
     int* movedList;  // proxy-sized
     int* sweepRank;  // proxy-sized: position of a proxy in the sweep order (large worlds)
+    unsigned char* islTab; // island-DFS tables of the worlds whose table does not fit in shared memory
 };
 
 // Island solver variants. kSolverPlain is the reference's per-island sequential Gauss-Seidel order
