@@ -396,6 +396,18 @@ struct Wd {
 __device__ inline int tid() { return threadIdx.x; }
 __device__ inline int nthreads() { return blockDim.x; }
 
+// Appends to a list counted by *count (shared memory) with one atomic per warp: returns this lane's
+// slot when keep, else -1. Every lane of the warp must call it (CTA sizes are multiples of 32).
+__device__ inline int WarpAppend(bool keep, int* count)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    int base = 0;
+    if (lane == 0 && bal) base = atomicAdd(count, __popc(bal));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    return keep ? base + __popc(bal & ((1u << lane) - 1u)) : -1;
+}
+
 // Order-preserving compaction over the CTA: out receives in[k] for every k < n with keep(k), in k
 // order; returns the count (same value in every thread). Each thread takes one contiguous chunk.
 constexpr int kMaxCta = 128;
@@ -646,8 +658,11 @@ __device__ void Wd::findNewContacts()
     __syncthreads();
     const unsigned long long tPairs0 = clock64();
     const int np = d.proxyCap;
-    for (int p = tid(); p < np; p += nthreads())
-        if (moved[p]) movedList[atomicAdd(&sMoved, 1)] = p;
+    for (int p0 = 0; p0 < np; p0 += nthreads()) {
+        const int p = p0 + tid();
+        const int i = WarpAppend(p < np && moved[p] != 0, &sMoved);
+        if (i >= 0) movedList[i] = p;
+    }
     __syncthreads();
     const int m = sMoved;
     // Query every moved proxy's fat AABB against all proxies (b2BroadPhase.h:188-217); a pair whose
@@ -664,9 +679,10 @@ __device__ void Wd::findNewContacts()
     if (tid() == 0) sLive = 0;
     __syncthreads();
     if (m > 0) {
-        for (int p = tid(); p < np; p += nthreads()) {
-            if (pfix[p] < 0) continue;
-            const int i = atomicAdd(&sLive, 1);
+        for (int p0 = 0; p0 < np; p0 += nthreads()) {
+            const int p = p0 + tid();
+            const int i = WarpAppend(p < np && pfix[p] >= 0, &sLive);
+            if (i < 0) continue;
             liveList[i] = p;
             if (staged) {
                 sFat[i] = fat[p];
@@ -1427,6 +1443,9 @@ __device__ int Wd::toiKind(const int4& info) const
     return (activeA || activeB) && (collideA || collideB) ? 2 : 0;
 }
 
+// Tail indices per block of the earliest-event selection in Wd::solveTOI.
+constexpr int kSelBlock = 256;
+
 __device__ void Wd::solveTOI(const StepParams& P)
 {
     __shared__ int sN, sDone, sMin;
@@ -1605,20 +1624,42 @@ __device__ void Wd::solveTOI(const StepParams& P)
                 evType[c] = 0;
             } else {
                 t = cColour[c];
+                vimpL[t / kSelBlock].z = 1.0f;  // its block's minimum is stale
             }
             vsep[t] = make_float2(T.kind != 0 ? cp[c].w : 2.0f, __int_as_float(c));
         }
         __syncthreads();
         stamp(16);
         // Earliest TOI, first in list order among equals (the reference keeps the first alpha <
-        // minAlpha): per-thread minimum over its strided tail indices (a later index is earlier in
-        // the list, so it wins a tie), then a reduction on (alpha, -t).
+        // minAlpha): the argmin over (alpha, -t) of the outcomes with alpha < 1 (a later tail index
+        // is earlier in the list, so it wins a tie). Two levels: the minimum of every block of
+        // kSelBlock tail indices is kept in vimpL {alpha, t, stale} (free scratch in this phase) and
+        // recomputed, one warp per block, only where an outcome changed; then the blocks' minima.
         {
+            const int nBlk = (n + kSelBlock - 1) / kSelBlock;
+            const int lane = tid() & 31, nWarps = nthreads() >> 5;
+            for (int bk = tid() >> 5; bk < nBlk; bk += nWarps) {
+                if (event > 0 && vimpL[bk].z == 0.0f) continue;
+                float ba = 1.0f;
+                int bt = -1;
+                for (int t = bk * kSelBlock + lane; t < min(n, (bk + 1) * kSelBlock); t += 32) {
+                    const float alpha = vsep[t].x;
+                    if (alpha < 1.0f && (bt < 0 || alpha < ba || (alpha == ba && t > bt))) { ba = alpha; bt = t; }
+                }
+                for (int o = 16; o > 0; o >>= 1) {
+                    const float oa = __shfl_down_sync(0xffffffffu, ba, o);
+                    const int ot = __shfl_down_sync(0xffffffffu, bt, o);
+                    if (ot >= 0 && (bt < 0 || oa < ba || (oa == ba && ot > bt))) { ba = oa; bt = ot; }
+                }
+                if (lane == 0) vimpL[bk] = make_float4(ba, __int_as_float(bt), 0.0f, 0.0f);
+            }
+            __syncthreads();
             float best = 1.0f;
             int bestT = -1;
-            for (int t = tid(); t < n; t += nthreads()) {
-                const float alpha = vsep[t].x;
-                if (alpha < 1.0f && alpha <= best) { best = alpha; bestT = t; }
+            for (int bk = tid(); bk < nBlk; bk += nthreads()) {
+                const float4 m = vimpL[bk];
+                const int t = __float_as_int(m.y);
+                if (t >= 0 && (bestT < 0 || m.x < best || (m.x == best && t > bestT))) { best = m.x; bestT = t; }
             }
             sBestA[tid()] = best;
             sBestK[tid()] = bestT;
@@ -1680,6 +1721,12 @@ __device__ void Wd::solveTOI(const StepParams& P)
                 skip = true;
             }
             if (!skip) {
+                // island bodies (bit = island position) this event woke: a woken kinematic body's
+                // contacts join the dirty list below (an awake one's cannot change their outcome)
+                static_assert(2 * kMaxTOIContacts <= 64, "one bit per mini-island body");
+                unsigned long long woke = 0ull;
+                if ((bi[bA].y & kBAwake) == 0) woke |= 1ull;
+                if ((bi[bB].y & kBAwake) == 0) woke |= 2ull;
                 setAwake(bA, true);
                 setAwake(bB, true);
                 // mini island in the scratch rows (b2World.cpp:700-780)
@@ -1721,7 +1768,10 @@ __device__ void Wd::solveTOI(const StepParams& P)
                         sContact[nContacts++] = c;
                         if (bi[other].y & kBIsland) continue;
                         bi[other].y |= kBIsland;
-                        if (bi[other].x != kStatic) setAwake(other, true);
+                        if (bi[other].x != kStatic) {
+                            if ((bi[other].y & kBAwake) == 0) woke |= 1ull << nBodies;
+                            setAwake(other, true);
+                        }
                         bj[other].z = nBodies;
                         sBody[nBodies++] = other;
                     }
@@ -1791,15 +1841,16 @@ __device__ void Wd::solveTOI(const StepParams& P)
                                  pcn > 1 ? im.z : 0.0f, pcn > 0 ? im.y : 0.0f, pcn > 1 ? im.w : 0.0f);
                     }
                 stamp(19);
-                // dynamic bodies: fixtures synchronised, contacts' TOIs invalidated; every contact of
-                // a non-static island body joins the dirty list (a woken kinematic body's contacts
-                // may now need a TOI)
+                // dynamic bodies: fixtures synchronised, contacts' TOIs invalidated; the contacts of
+                // every dynamic island body and of every kinematic one this event woke join the dirty
+                // list
                 for (int i = 0; i < nBodies; ++i) {
                     int b = sBody[i];
                     bi[b].y &= ~kBIsland;
                     if (bi[b].x == kStatic) continue;
                     const bool dynamic = bi[b].x == kDynamic;
                     if (dynamic) syncFixtures(b);
+                    else if (((woke >> i) & 1ull) == 0ull) continue;
                     B2G_WALK(e, bi[b].w, eNext(e), 2 * d.contactCap + 2) {
                         const int c = e >> 1;
                         if (dynamic) ci[c].x &= ~(kCToi | kCIsland);
