@@ -588,7 +588,7 @@ gb_status Upload(gb_world* g)
     ALLOC(xf, tb); ALLOC(sw, tb); ALLOC(sw0, tb); ALLOC(vel, tb); ALLOC(frc, tb); ALLOC(mas, tb); ALLOC(prop, tb);
     ALLOC(bi, tb); ALLOC(bj, tb);
     ALLOC(fi, tf); ALLOC(fm, tf); ALLOC(ff, tf); ALLOC(faabb, tf); ALLOC(shape, tf);
-    ALLOC(fat, tp); ALLOC(pfix, tp); ALLOC(moved, tp); ALLOC(movedList, tp); ALLOC(sweepRank, tp);
+    ALLOC(fat, tp); ALLOC(pfix, tp); ALLOC(moved, tp); ALLOC(movedList, tp); ALLOC(liveProxies, tp);
     ALLOC(ci, tc); ALLOC(ce, tc); ALLOC(cp, tc); ALLOC(mh, tc); ALLOC(mv, tc); ALLOC(mp0, tc); ALLOC(mp1, tc);
     ALLOC(order, tc); ALLOC(cnext, tc);
     ALLOC(joint, tj); ALLOC(sJoint, tj);

@@ -65,7 +65,7 @@ struct Wd {
     unsigned long long* pairs;
     int* pairKeep;
     int* movedList;
-    int* sweepRank;
+    int* liveProxies;
     int4* pairInfo;
     unsigned char* islTab; // the world's global island-table region (d.islTabBytes bytes)
     float4* smemBase;   // the CTA's dynamic shared memory, free outside the island solve
@@ -79,7 +79,7 @@ struct Wd {
         xf = B.xf + b; sw = B.sw + b; sw0 = B.sw0 + b; vel = B.vel + b; frc = B.frc + b; mas = B.mas + b;
         prop = B.prop + b; bi = B.bi + b; bj = B.bj + b;
         fi = B.fi + f; fm = B.fm + f; ff = B.ff + f; faabb = B.faabb + f; shape = B.shape + f;
-        fat = B.fat + p; pfix = B.pfix + p; moved = B.moved + p; movedList = B.movedList + p; sweepRank = B.sweepRank + p;
+        fat = B.fat + p; pfix = B.pfix + p; moved = B.moved + p; movedList = B.movedList + p; liveProxies = B.liveProxies + p;
         ci = B.ci + c; ce = B.ce + c; cp = B.cp + c; mh = B.mh + c; mv = B.mv + c; mp0 = B.mp0 + c; mp1 = B.mp1 + c;
         order = B.order + c; cnext = B.cnext + c;
         jt = B.joint + j; sJoint = B.sJoint + j;
@@ -376,7 +376,7 @@ struct Wd {
 
     // b2ContactManager::FindNewContacts -> b2BroadPhase::UpdatePairs -> AddPair, CTA-wide.
     __device__ void findNewContacts();
-    __device__ void sweepPairs(int m, int* pairCount);
+    __device__ void gridPairs(int m, int* pairCount);
     __device__ void collide();
     __device__ void solve(const StepParams& P, float4* smem, int smemRows, int smemContacts);
     template <class L>
@@ -543,7 +543,7 @@ __device__ void ctaRadixSort(unsigned long long* keys, unsigned long long* tmp, 
 }
 
 // ------------------------------------------------------------------ FindNewContacts
-// Above this many moved x all proxy tests, pair finding sorts and sweeps instead.
+// Above this many moved x live proxy tests, pair finding bins the proxies into a grid instead.
 constexpr long long kSweepThreshold = 1ll << 20;
 
 __device__ inline unsigned OrderedBits(float x)
@@ -557,49 +557,85 @@ __device__ inline float FromOrderedBits(unsigned o)
 }
 
 // The pairs of b2BroadPhase::UpdatePairs for large worlds, the same set the all-pairs test finds
-// (the overlap test is b2TestOverlap, only the candidates differ): live proxies sorted by fat lower
-// x, each moved proxy scans forward while candidates start before its upper x and backward while
-// they start after its lower x minus the widest proxy's width. Proxies more than 4x wider than the
-// mean (container edges, ground) are kept out of the scans and tested against every moved proxy.
-// Keys live in the pair-info scratch (free until contact creation), ranks in sweepRank.
-__device__ void Wd::sweepPairs(int m, int* pairCount)
+// (the overlap test is b2TestOverlap, only the candidates differ): live proxies are binned by the
+// lower corner of their fat AABB into a uniform grid whose cells are at least as wide and as tall as
+// the largest proxy, and sorted by cell; each moved proxy tests the proxies of the cells that its box,
+// grown by that size down and left, covers. A proxy overlapping it has its lower corner in that grown
+// box, and the cell of a coordinate, floor((x - origin) / h), never decreases with x, so those cells
+// hold every candidate. Proxies more than 4x larger than the mean (container edges, ground) stay out
+// of the grid and are tested against every moved proxy. Keys live in the pair-info scratch (free
+// until contact creation), the cell ranges after them.
+__device__ void Wd::gridPairs(int m, int* pairCount)
 {
-    __shared__ float sWidthSum;
-    __shared__ int sLive, sSmall;
-    __shared__ unsigned sMaxW;
+    __shared__ float sSizeSum;
+    __shared__ int sLive, sSmall, sCursor;
+    __shared__ unsigned sMaxW, sMinX, sMinY, sMaxX, sMaxY;
     const int np = d.proxyCap;
-    if (tid() == 0) { sWidthSum = 0.0f; sLive = 0; sSmall = 0; sMaxW = 0u; }
+    if (tid() == 0) {
+        sSizeSum = 0.0f; sLive = 0; sSmall = 0; sCursor = 0; sMaxW = 0u;
+        sMinX = sMinY = 0xffffffffu; sMaxX = sMaxY = 0u;
+    }
     __syncthreads();
-    float wsum = 0.0f;
-    int live = 0;
-    for (int p = tid(); p < np; p += nthreads())
-        if (pfix[p] >= 0) { const float4 f = fat[p]; wsum += f.z - f.x; ++live; }
-    atomicAdd(&sWidthSum, wsum);
-    atomicAdd(&sLive, live);
+    auto size = [](const float4& f) { return fmaxf(f.z - f.x, f.w - f.y); };
+    {
+        float wsum = 0.0f;
+        int live = 0;
+        for (int p = tid(); p < np; p += nthreads())
+            if (pfix[p] >= 0) { wsum += size(fat[p]); ++live; }
+        atomicAdd(&sSizeSum, wsum);
+        atomicAdd(&sLive, live);
+    }
     __syncthreads();
     const int nLive = sLive;
-    const float wLarge = 4.0f * (sWidthSum / (float)max(nLive, 1));
-    unsigned long long* keys = reinterpret_cast<unsigned long long*>(pairInfo);
-    // keys: (ordered lower x) << 32 | proxy for the small proxies, all-ones << 32 | proxy for the wide
-    // ones so they sort last
-    __shared__ int sCursor;
-    if (tid() == 0) sCursor = 0;
-    __syncthreads();
+    const float wLarge = 4.0f * (sSizeSum / (float)max(nLive, 1));
     for (int p = tid(); p < np; p += nthreads()) {
         if (pfix[p] < 0) continue;
         const float4 f = fat[p];
-        const float w = f.z - f.x;
-        const bool large = w > wLarge;
-        const unsigned hi = large ? 0xffffffffu : OrderedBits(f.x);
-        keys[atomicAdd(&sCursor, 1)] = ((unsigned long long)hi << 32) | (unsigned)p;
-        if (!large) {
-            atomicAdd(&sSmall, 1);
-            atomicMax(&sMaxW, __float_as_uint(fmaxf(w, 0.0f)));
-        }
+        if (size(f) > wLarge) continue;
+        atomicMax(&sMaxW, __float_as_uint(fmaxf(size(f), 0.0f)));
+        atomicMin(&sMinX, OrderedBits(f.x));
+        atomicMin(&sMinY, OrderedBits(f.y));
+        atomicMax(&sMaxX, OrderedBits(f.x));
+        atomicMax(&sMaxY, OrderedBits(f.y));
     }
     __syncthreads();
-    const int cap = 2 * d.pairCap;
-    int* radixWork = reinterpret_cast<int*>(smemBase);
+    // the grid: cell size h >= the largest small proxy, at most cellCap cells (h grows to fit)
+    const float W = __uint_as_float(sMaxW) * 1.0001f + 1e-4f;
+    const bool anySmall = sMinX <= sMaxX;
+    const float ox = anySmall ? FromOrderedBits(sMinX) : 0.0f, oy = anySmall ? FromOrderedBits(sMinY) : 0.0f;
+    float spanX = anySmall ? FromOrderedBits(sMaxX) - ox : 0.0f;
+    float spanY = anySmall ? FromOrderedBits(sMaxY) - oy : 0.0f;
+    if (!(spanX < 1e30f) || !(spanY < 1e30f)) spanX = spanY = 0.0f;  // non-finite boxes: one cell (all-pairs)
+    const int cellCap = min(d.pairCap, 4 * max(nLive, 1));
+    float h = fmaxf(W, 1e-3f), invH, fx, fy;
+    for (;;) {
+        invH = 1.0f / h;
+        fx = floorf(spanX * invH) + 1.0f;
+        fy = floorf(spanY * invH) + 1.0f;
+        if (fx * fy <= (float)cellCap) break;
+        h *= 1.5f;
+    }
+    const int nx = (int)fx, ny = (int)fy;
+    auto cellOf = [&](float x, float o, int n) {
+        const float c = fminf(fmaxf(floorf((x - o) * invH), -1.0f), (float)n);
+        return (int)c;
+    };
+    unsigned long long* keys = reinterpret_cast<unsigned long long*>(pairInfo);
+    // keys: cell << 32 | proxy for the small proxies, all-ones << 32 | proxy for the large ones, so
+    // they sort last
+    for (int p = tid(); p < np; p += nthreads()) {
+        if (pfix[p] < 0) continue;
+        const float4 f = fat[p];
+        const bool large = size(f) > wLarge;
+        unsigned hi = 0xffffffffu;
+        if (!large) {
+            const int cx = min(max(cellOf(f.x, ox, nx), 0), nx - 1), cy = min(max(cellOf(f.y, oy, ny), 0), ny - 1);
+            hi = (unsigned)(cy * nx + cx);
+            atomicAdd(&sSmall, 1);
+        }
+        keys[atomicAdd(&sCursor, 1)] = ((unsigned long long)hi << 32) | (unsigned)p;
+    }
+    __syncthreads();
     int P2 = 1;
     while (P2 < nLive) P2 <<= 1;
     if (P2 * (int)sizeof(unsigned long long) <= smemBytes) {
@@ -611,18 +647,25 @@ __device__ void Wd::sweepPairs(int m, int* pairCount)
         __syncthreads();
     } else if (RadixSortFits(nLive, smemBytes)) {
         // the second half of the pair-info scratch (2 x pairCap keys, nLive <= pairCap) as the buffer
-        ctaRadixSort(keys, keys + d.pairCap, nLive, radixWork);
+        ctaRadixSort(keys, keys + d.pairCap, nLive, reinterpret_cast<int*>(smemBase));
     } else {
-        ctaSortKeys(keys, nLive, cap);
+        ctaSortKeys(keys, nLive, 2 * d.pairCap);
     }
-    for (int i = tid(); i < nLive; i += nthreads()) sweepRank[(int)(keys[i] & 0xffffffffu)] = i;
+    // cell ranges [start, end) in the second half of the scratch (2 x pairCap ints >= 2 x cellCap)
+    const int nSmall = sSmall, nCells = nx * ny;
+    int* cellStart = reinterpret_cast<int*>(keys + d.pairCap);
+    int* cellEnd = cellStart + nCells;
+    for (int c = tid(); c < nCells; c += nthreads()) { cellStart[c] = 0; cellEnd[c] = 0; }
     __syncthreads();
-    const int nSmall = sSmall;
-    const float W = __uint_as_float(sMaxW) * 1.0001f + 1e-4f;
+    for (int i = tid(); i < nSmall; i += nthreads()) {
+        const unsigned c = (unsigned)(keys[i] >> 32);
+        if (i == 0 || (unsigned)(keys[i - 1] >> 32) != c) cellStart[c] = i;
+        if (i == nSmall - 1 || (unsigned)(keys[i + 1] >> 32) != c) cellEnd[c] = i + 1;
+    }
+    __syncthreads();
     for (int t = tid(); t < m; t += nthreads()) {
         const int q = movedList[t];
         const float4 Fq = fat[q];
-        const int r = sweepRank[q];
         auto test = [&](int p) {
             if (p == q) return;
             if (moved[p] && p < q) return;
@@ -631,21 +674,18 @@ __device__ void Wd::sweepPairs(int m, int* pairCount)
             const unsigned long long lo = (unsigned long long)(p < q ? p : q), hi = (unsigned long long)(p < q ? q : p);
             if (k < d.pairCap) pairs[k] = (lo << 32) | hi;
         };
-        if (r >= nSmall) {
+        if (size(Fq) > wLarge) {
             for (int j = 0; j < nLive; ++j) test((int)(keys[j] & 0xffffffffu));
             continue;
         }
-        for (int j = r + 1; j < nSmall; ++j) {
-            const unsigned long long key = keys[j];
-            if (FromOrderedBits((unsigned)(key >> 32)) > Fq.z) break;
-            test((int)(key & 0xffffffffu));
-        }
-        const float lowest = Fq.x - W - 1e-4f * fabsf(Fq.x);
-        for (int j = r - 1; j >= 0; --j) {
-            const unsigned long long key = keys[j];
-            if (FromOrderedBits((unsigned)(key >> 32)) < lowest) break;
-            test((int)(key & 0xffffffffu));
-        }
+        const float lowX = Fq.x - W - 1e-4f * fabsf(Fq.x), lowY = Fq.y - W - 1e-4f * fabsf(Fq.y);
+        const int cx0 = max(cellOf(lowX, ox, nx), 0), cx1 = min(cellOf(Fq.z, ox, nx), nx - 1);
+        const int cy0 = max(cellOf(lowY, oy, ny), 0), cy1 = min(cellOf(Fq.w, oy, ny), ny - 1);
+        for (int cy = cy0; cy <= cy1; ++cy)
+            for (int cx = cx0; cx <= cx1; ++cx) {
+                const int c = cy * nx + cx;
+                for (int i = cellStart[c], e = cellEnd[c]; i < e; ++i) test((int)(keys[i] & 0xffffffffu));
+            }
         for (int j = nSmall; j < nLive; ++j) test((int)(keys[j] & 0xffffffffu));
     }
     __syncthreads();
@@ -675,7 +715,7 @@ __device__ void Wd::findNewContacts()
     float4* sFat = smemBase;
     int* sId = reinterpret_cast<int*>(smemBase + np);
     unsigned char* sMovedFlag = reinterpret_cast<unsigned char*>(sId + np);
-    int* liveList = staged ? sId : sweepRank;  // sweepRank is free outside sweepPairs
+    int* liveList = staged ? sId : liveProxies;
     if (tid() == 0) sLive = 0;
     __syncthreads();
     if (m > 0) {
@@ -695,7 +735,7 @@ __device__ void Wd::findNewContacts()
     const long long total = (long long)m * nLive;
     if (total > kSweepThreshold) {
         __syncthreads();
-        sweepPairs(m, &sPairs);
+        gridPairs(m, &sPairs);
     } else
     for (long long idx = tid(); idx < total; idx += nthreads()) {
         const int q = movedList[idx / nLive];

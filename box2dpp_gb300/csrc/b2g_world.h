@@ -219,7 +219,7 @@ struct Batch {
     int* pairKeep;
     int4* pairInfo;  // pair-sized: a new contact's fixtures and bodies, worked out before creation
     int* movedList;  // proxy-sized
-    int* sweepRank;  // proxy-sized: position of a proxy in the sweep order (large worlds)
+    int* liveProxies; // proxy-sized: pair finding's list of live proxies when it is not in shared memory
     unsigned char* islTab; // island-DFS tables of the worlds whose table does not fit in shared memory
 };
 

@@ -130,3 +130,23 @@ def test_gpu_toi_event_loop_matches_oracle(gpu):
         assert np.array_equal(gf.view(np.uint32), of.view(np.uint32)), f"manifolds differ at step {s}"
     w.sync()
     assert events >= 20 and multi >= 5, (events, multi)
+
+
+def test_gpu_grid_pair_finding_matches_oracle(gpu):
+    """3,000 bodies dropped into the edge container with sleep off: every step's pair finding has more
+    than 2^20 candidate tests and bins the proxies into a grid; the pair set, and so every body and
+    contact, must match the CPU oracle bit for bit through the fall and the pile-up."""
+    sc = scenes.config2(3000, seed=4, allow_sleep=False)
+    w = World(sc)
+    o = oracle.OracleWorld(sc, "port", "project")
+    for s in range(1, 151):
+        w.step(DT, VI, PI)
+        o.step(DT, VI, PI)
+        if s % 15 == 0:
+            gb, ob = w.bodies(0), o.bodies()
+            assert np.array_equal(gb.view(np.uint32), ob.view(np.uint32)), f"bodies differ at step {s}"
+            gi, gf = w.contacts(0)
+            oi, of = o.contacts()
+            assert np.array_equal(gi, oi), f"contacts differ at step {s}"
+            assert np.array_equal(gf.view(np.uint32), of.view(np.uint32)), f"manifolds differ at step {s}"
+    w.sync()
