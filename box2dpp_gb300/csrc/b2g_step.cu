@@ -1416,19 +1416,27 @@ __device__ void Wd::solve(const StepParams& P, float4* smem, int smemRows, int s
     const int nIsl = sIslands;
     solveIslands(P, nIsl, sRows, sCons, smem, smemRows, smemContacts, coloured ? sColourStart : nullptr);
     unsigned long long t2 = clock64();
-    // A static body may sit in several islands; its awake flag ends as the last such island left it.
+    // A static body may sit in several islands; its awake flag ends as the last such island left it:
+    // the largest island index per static body (sWake, free after the collide phase), then its flag.
     if (tid() == 0) {
         st->cyc[2] = t1 - tSolve0;
         st->cyc[3] = t2 - t1;
-        for (int i = 0; i < nIsl; ++i) {
-            int4 isl = islands[i];
-            for (int k = isl.x; k < isl.x + isl.y; ++k) {
-                int b = sBody[k];
-                if (bi[b].x != kStatic) continue;
-                if (sleepOut[i]) bi[b].y &= ~kBAwake;
-                else bi[b].y |= kBAwake;
-            }
+    }
+    for (int b = tid(); b < nb; b += nthreads()) sWake[b] = -1;
+    __syncthreads();
+    for (int i = tid(); i < nIsl; i += nthreads()) {
+        const int4 isl = islands[i];
+        for (int k = isl.x; k < isl.x + isl.y; ++k) {
+            const int b = sBody[k];
+            if (bi[b].x == kStatic) atomicMax(&sWake[b], i);
         }
+    }
+    __syncthreads();
+    for (int b = tid(); b < nb; b += nthreads()) {
+        const int i = sWake[b];
+        if (i < 0) continue;
+        if (sleepOut[i]) bi[b].y &= ~kBAwake;
+        else bi[b].y |= kBAwake;
     }
     __syncthreads();
     for (int b = tid(); b < nb; b += nthreads()) {
