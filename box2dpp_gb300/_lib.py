@@ -30,8 +30,16 @@ EXPORTS = [
     "gb_mlp_forward", "gb_mlp_gradients", "gb_mlp_train", "gb_world_set_warm_start", "gb_world_warm_stats",
     "gb_world_set_contact_log", "gb_world_read_contact_log", "gb_world_contact_stats", "gb_world_set_events",
     "gb_world_read_events", "gb_world_query_aabb", "gb_world_raycast", "gb_create_joints",
-    "gb_world_stage_times",
+    "gb_world_stage_times", "gb_body_edits",
 ]
+
+
+# gb_body_edit ops (GB_EDIT_*) and the record layout: world, body, op, wake (int32), v[4] (float32)
+EDIT_OPS = {"set_transform": 0, "set_linear_velocity": 1, "set_angular_velocity": 2, "set_awake": 3,
+            "apply_force": 4, "apply_force_to_center": 5, "apply_torque": 6, "apply_linear_impulse": 7,
+            "apply_angular_impulse": 8}
+EDIT_DTYPE = np.dtype([("world", np.int32), ("body", np.int32), ("op", np.int32), ("wake", np.int32),
+                       ("v", np.float32, 4)])
 
 
 class GbError(RuntimeError):
@@ -127,6 +135,7 @@ def load(build_if_missing: bool = True):
         "gb_get_transforms": [vp, vp],
         "gb_world_profile": [vp, np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")],
         "gb_world_stage_times": [vp, f, i, i, _f32],
+        "gb_body_edits": [vp, i, vp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

@@ -23,6 +23,7 @@ cudaError_t b2gLaunchNarrowphase(const b2g::Batch& B, cudaStream_t stream);
 cudaError_t b2gLaunchStep(const b2g::Batch& B, const b2g::StepParams& P, const int* schedule, int first, int count,
                           int threads, int smemRows, int smemContacts, cudaStream_t stream);
 cudaError_t b2gLaunchToi(const b2g::Batch& B, const b2g::StepParams& P, cudaStream_t stream);
+cudaError_t b2gLaunchBodyEdits(const b2g::Batch& B, const b2g::BodyEdit* edits, int n, cudaStream_t stream);
 cudaError_t b2gLaunchStepToi(const b2g::Batch& B, const b2g::StepParams& P, const int* schedule, int first, int count,
                              int threads, int smemRows, int smemContacts, cudaStream_t stream);
 cudaError_t b2gLaunchSinCos(const float* x, float* s, float* c, int n, cudaStream_t stream);
@@ -130,6 +131,8 @@ struct gb_world {
     int warmMode = kWarmReference;
     bool eventsEnabled = false;
     MlpView mlp{};
+    BodyEdit* dEdits = nullptr;  // device copy of the last gb_body_edits call
+    int editCap = 0;
     float* logX = nullptr;   // contact-point log (device), see gb_world_set_contact_log
     float* logT = nullptr;
     int* logCount = nullptr;
@@ -856,8 +859,38 @@ gb_status gb_world_destroy(gb_world* g)
     FreeDevice(g);
     ReleaseLaunchResources(g);
     FreeLog(g);
+    if (g->dEdits) cudaFree(g->dEdits);
     if (g->ownStream && g->stream) cudaStreamDestroy(g->stream);
     delete g;
+    return GB_OK;
+}
+
+static_assert(sizeof(gb_body_edit) == sizeof(BodyEdit), "gb_body_edit and its device copy share a layout");
+
+gb_status gb_body_edits(gb_world* g, int n, const gb_body_edit* edits)
+{
+    if (!g || n < 0 || (n > 0 && !edits)) return GB_ERR_INVALID;
+    if (n == 0) return GB_OK;
+    for (int i = 0; i < n; ++i) {
+        const gb_body_edit& e = edits[i];
+        if (e.world < 0 || e.world >= (int)g->worlds.size()) return GB_ERR_INVALID;
+        if (e.body < 0 || e.body >= (int)g->worlds[e.world].bodies.size()) return GB_ERR_INVALID;
+        if (e.op < 0 || e.op >= kEditOps) return GB_ERR_INVALID;
+    }
+    gb_status s = Upload(g);
+    if (s != GB_OK) return s;
+    if (g->editCap < n) {
+        // freeing waits for the device, so an earlier call's edits are no longer read
+        if (g->dEdits) GB_CUDA(cudaFree(g->dEdits));
+        g->dEdits = nullptr;
+        g->editCap = 0;
+        GB_CUDA(cudaMalloc(&g->dEdits, (size_t)n * sizeof(BodyEdit)));
+        g->editCap = n;
+    }
+    // from pageable memory the copy has left the caller's array when the call returns; stream order
+    // keeps an earlier call's kernel ahead of this copy
+    GB_CUDA(cudaMemcpyAsync(g->dEdits, edits, (size_t)n * sizeof(BodyEdit), cudaMemcpyHostToDevice, g->stream));
+    GB_CUDA(b2gLaunchBodyEdits(g->batch, g->dEdits, n, g->stream));
     return GB_OK;
 }
 

@@ -351,7 +351,14 @@ struct Wd {
         Xf xf1;
         xf1.q = RotOf(s0.z);
         xf1.p = V(s0.x, s0.y) - Mul(xf1.q, V(m.z, m.w));
-        Xf xf2 = xform(b);
+        syncFixturesFrom(b, xf1, xform(b));
+    }
+
+    // b2Fixture::Synchronize (Dynamics/b2Fixture.cpp:154-177) of every fixture of body b between two
+    // transforms, with b2BroadPhase::MoveProxy (b2DynamicTree.cpp:133-177): the swept AABB, and a
+    // new fat AABB (grown by the extension and the predicted displacement) when it left the old one.
+    __device__ void syncFixturesFrom(int b, const Xf& xf1, const Xf& xf2)
+    {
         B2G_WALK(f, bi[b].z, fi[f].y, d.fixCount + 1) {
             int pid = fi[f].z;
             if (pid < 0) continue;
@@ -368,6 +375,89 @@ struct Wd {
             if (dd.y < 0.0f) nb.y += dd.y; else nb.w += dd.y;
             fat[pid] = nb;
             moved[pid] = 1;
+        }
+    }
+
+    // One b2Body state change between steps (the methods gb_body_edits lists, Dynamics/b2Body.cpp:
+    // 419-441 and b2Body.h:501-830), with the reference's type checks, wakes and sleep rules.
+    __device__ void applyEdit(const BodyEdit& e)
+    {
+        const int b = e.body;
+        const int type = bi[b].x;
+        auto wakeOnRequest = [&]() {
+            if (e.wake && !awake(b)) setAwake(b, true);
+        };
+        switch (e.op) {
+        case kEditSetTransform: {
+            Xf x;
+            x.q = RotOf(e.v[2]);
+            x.p = V(e.v[0], e.v[1]);
+            const float4 m = mas[b];
+            const Vec2 c = Mul(x, V(m.z, m.w));
+            setXform(b, x);
+            sw[b] = make_float4(c.x, c.y, e.v[2], sw[b].w);
+            sw0[b] = make_float4(c.x, c.y, e.v[2], sw0[b].w);
+            syncFixturesFrom(b, x, x);
+            break;
+        }
+        case kEditSetLinearVelocity: {
+            if (type == kStatic) break;
+            const Vec2 v = V(e.v[0], e.v[1]);
+            if (Dot(v, v) > 0.0f) setAwake(b, true);
+            float4 q = vel[b];
+            q.x = v.x;
+            q.y = v.y;
+            vel[b] = q;
+            break;
+        }
+        case kEditSetAngularVelocity:
+            if (type == kStatic) break;
+            if (e.v[0] * e.v[0] > 0.0f) setAwake(b, true);
+            vel[b].z = e.v[0];
+            break;
+        case kEditSetAwake:
+            setAwake(b, e.v[0] != 0.0f);
+            break;
+        case kEditApplyForce:
+        case kEditApplyForceToCenter:
+        case kEditApplyTorque: {
+            if (type != kDynamic) break;
+            wakeOnRequest();
+            if (!awake(b)) break;
+            float4 f = frc[b];
+            if (e.op == kEditApplyTorque) {
+                f.z += e.v[0];
+            } else {
+                f.x += e.v[0];
+                f.y += e.v[1];
+                if (e.op == kEditApplyForce) {
+                    const float4 s = sw[b];
+                    f.z += Cross(V(e.v[2], e.v[3]) - V(s.x, s.y), V(e.v[0], e.v[1]));
+                }
+            }
+            frc[b] = f;
+            break;
+        }
+        case kEditApplyLinearImpulse:
+        case kEditApplyAngularImpulse: {
+            if (type != kDynamic) break;
+            wakeOnRequest();
+            if (!awake(b)) break;
+            const float4 m = mas[b];
+            float4 q = vel[b];
+            if (e.op == kEditApplyLinearImpulse) {
+                const float4 s = sw[b];
+                q.x += m.x * e.v[0];
+                q.y += m.x * e.v[1];
+                q.z += m.y * Cross(V(e.v[2], e.v[3]) - V(s.x, s.y), V(e.v[0], e.v[1]));
+            } else {
+                q.z += m.y * e.v[0];
+            }
+            vel[b] = q;
+            break;
+        }
+        default:
+            break;
         }
     }
 
@@ -2128,6 +2218,19 @@ __global__ void __launch_bounds__(128, B2G_STEP_MIN_BLOCKS) StepToiKernel(Batch 
     }
 }
 
+// gb_body_edits: the edits in array order on one thread (they may repeat a body, and their order
+// is the caller's call order).
+__global__ void BodyEditKernel(Batch B, const BodyEdit* edits, int n)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    for (int i = 0; i < n; ++i) {
+        const BodyEdit e = edits[i];
+        Wd W;
+        W.init(B, e.world);
+        W.applyEdit(e);
+    }
+}
+
 } // namespace b2g
 
 // Launch entries used by the host runtime (b2g_api.cu). A step is b2gLaunchNarrowphase, then
@@ -2136,6 +2239,13 @@ cudaError_t b2gLaunchNarrowphase(const b2g::Batch& B, cudaStream_t stream)
 {
     if (B.contactRows <= 0) return cudaSuccess;
     b2g::NarrowphaseKernel<<<(B.contactRows + 255) / 256, 256, 0, stream>>>(B);
+    return cudaGetLastError();
+}
+
+cudaError_t b2gLaunchBodyEdits(const b2g::Batch& B, const b2g::BodyEdit* edits, int n, cudaStream_t stream)
+{
+    if (n <= 0) return cudaSuccess;
+    b2g::BodyEditKernel<<<1, 32, 0, stream>>>(B, edits, n);
     return cudaGetLastError();
 }
 

@@ -223,6 +223,14 @@ struct Batch {
     unsigned char* islTab; // island-DFS tables of the worlds whose table does not fit in shared memory
 };
 
+// A b2Body state change between steps (the device copy of the C-ABI's gb_body_edit, same layout).
+enum : int { kEditSetTransform = 0, kEditSetLinearVelocity, kEditSetAngularVelocity, kEditSetAwake, kEditApplyForce,
+             kEditApplyForceToCenter, kEditApplyTorque, kEditApplyLinearImpulse, kEditApplyAngularImpulse, kEditOps };
+struct BodyEdit {
+    int world, body, op, wake;
+    float v[4];
+};
+
 // Island solver variants. kSolverPlain is the reference's per-island sequential Gauss-Seidel order
 // (bit-exact with the reference). kSolverColoured solves the same constraints colour by colour: the
 // constraints of one colour share no dynamic body and are solved in parallel across the CTA.

@@ -230,6 +230,19 @@ class World:
         _lib.check(self.lib.gb_world_profile(self.h, out), "gb_world_profile")
         return out.reshape(self.n_worlds, len(self.PHASES))
 
+    def body_edits(self, edits) -> None:
+        """b2Body state changes before the next step, in order: edits is a sequence of (world, body,
+        op name or code, values, wake) with op names from _lib.EDIT_OPS (see gb_body_edits)."""
+        arr = np.zeros(len(edits), dtype=_lib.EDIT_DTYPE)
+        for i, (w, b, op, vals, wake) in enumerate(edits):
+            arr[i]["world"], arr[i]["body"] = w, b
+            arr[i]["op"] = _lib.EDIT_OPS[op] if isinstance(op, str) else int(op)
+            arr[i]["wake"] = int(bool(wake))
+            v = np.zeros(4, dtype=np.float32)
+            v[:len(vals)] = vals
+            arr[i]["v"] = v
+        _lib.check(self.lib.gb_body_edits(self.h, len(arr), arr.ctypes.data_as(C.c_void_p)), "gb_body_edits")
+
     STAGES = ["narrowphase_prepass", "step", "toi_prepass", "continuous"]
 
     def stage_times(self, dt: float = 1.0 / 60.0, vi: int = 8, pi: int = 3) -> np.ndarray:

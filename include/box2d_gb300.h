@@ -227,6 +227,32 @@ gb_status gb_world_profile(gb_world* world, unsigned long long* out);
 gb_status gb_world_stage_times(gb_world* world, float dt, int velocity_iterations, int position_iterations,
                                float* ms);
 
+/* b2Body state changes between steps, each with the reference method's semantics (Box2D/Dynamics/
+ * b2Body.cpp:419-441 SetTransform; b2Body.h:501-530 SetLinearVelocity, SetAngularVelocity; 635-655
+ * SetAwake; 739-830 ApplyForce, ApplyForceToCenter, ApplyTorque, ApplyLinearImpulse,
+ * ApplyAngularImpulse: no effect on bodies of the wrong type, wake on request, no accumulation on a
+ * sleeping body; SetTransform moves the fixtures' proxies as b2Fixture::Synchronize does).
+ * gb_body_edits applies n edits in array order on the device, queued on the handle's stream before
+ * the next step (one thread applies them: meant for the sparse changes of a game loop; the whole
+ * batch's forces go through gb_set_forces). The edit array may be reused when the call returns. */
+#define GB_EDIT_SET_TRANSFORM 0        /* v: position.x, position.y, angle */
+#define GB_EDIT_SET_LINEAR_VELOCITY 1  /* v: v.x, v.y */
+#define GB_EDIT_SET_ANGULAR_VELOCITY 2 /* v: w */
+#define GB_EDIT_SET_AWAKE 3            /* v[0] != 0: awake */
+#define GB_EDIT_APPLY_FORCE 4          /* v: force.x, force.y, point.x, point.y (world) */
+#define GB_EDIT_APPLY_FORCE_TO_CENTER 5 /* v: force.x, force.y */
+#define GB_EDIT_APPLY_TORQUE 6         /* v: torque */
+#define GB_EDIT_APPLY_LINEAR_IMPULSE 7 /* v: impulse.x, impulse.y, point.x, point.y (world) */
+#define GB_EDIT_APPLY_ANGULAR_IMPULSE 8 /* v: impulse */
+typedef struct gb_body_edit {
+    int world;  /* world index in the batch */
+    int body;   /* body index (creation order) */
+    int op;     /* GB_EDIT_* */
+    int wake;   /* the Apply* methods' wake argument */
+    float v[4];
+} gb_body_edit;
+gb_status gb_body_edits(gb_world* world, int n, const gb_body_edit* edits);
+
 /* Whole-batch b2Body::ApplyForceToCenter + ApplyTorque for the next step (Box2D/Dynamics/b2Body.h:
  * 437-468): forces[4] per body of every world in world order then creation order = force.x,
  * force.y, torque, unused. The host array is copied to the device asynchronously on the handle's

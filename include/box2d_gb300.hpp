@@ -208,11 +208,18 @@ public:
         return t;
     }
     bool IsAwake() const { return State()[11] != 0.0f; }
-    // b2Body::ApplyForceToCenter / ApplyTorque: accumulated for the next Step (the reference
-    // applies them only to awake bodies and wakes the body when wake is true; here the force is
-    // recorded and the device step applies it like the reference's integration does)
+    // State changes between steps (Box2D/Dynamics/b2Body.cpp:419, b2Body.h:501-830), each one
+    // gb_body_edits record applied on the device in call order before the next Step, with the
+    // reference's semantics (type checks, wakes, no accumulation on sleeping bodies).
+    void SetTransform(const b2Vec2& position, float angle);
+    void SetLinearVelocity(const b2Vec2& v);
+    void SetAngularVelocity(float omega);
+    void SetAwake(bool flag);
+    void ApplyForce(const b2Vec2& force, const b2Vec2& point, bool wake);
     void ApplyForceToCenter(const b2Vec2& force, bool wake);
     void ApplyTorque(float torque, bool wake);
+    void ApplyLinearImpulse(const b2Vec2& impulse, const b2Vec2& point, bool wake);
+    void ApplyAngularImpulse(float impulse, bool wake);
 
 private:
     friend class b2World;
@@ -342,7 +349,6 @@ public:
         b->m_type = def->type;
         b->m_userData = def->userData;
         m_bodies.push_back(std::move(b));
-        m_forces.resize(4 * m_bodies.size(), 0.0f);
         m_stale = true;
         return m_bodies.back().get();
     }
@@ -385,16 +391,7 @@ public:
             if (!m_eventsOn) m_eventsOn = gb_world_set_events(m_h, 1) == GB_OK;
             ReadContacts();  // the contacts before the step: destroyed contacts and old manifolds
         }
-        if (m_forcesDirty) {
-            gb_world_upload(m_h);
-            gb_set_forces(m_h, m_forces.data());
-        }
         gb_world_step(m_h, timeStep, velocityIterations, positionIterations);
-        if (m_forcesDirty) {
-            gb_world_sync(m_h);  // the force upload reads the host array
-            std::fill(m_forces.begin(), m_forces.end(), 0.0f);
-            m_forcesDirty = false;
-        }
         m_stale = true;
         if (m_listener) Report();
     }
@@ -447,12 +444,17 @@ public:
         m_stale = true;
         return m_fixtures.back().get();
     }
-    void AddForce(int index, float fx, float fy, float torque)
+    void Edit(int index, int op, float v0, float v1, float v2, float v3, bool wake)
     {
-        m_forces[4 * index] += fx;
-        m_forces[4 * index + 1] += fy;
-        m_forces[4 * index + 2] += torque;
-        m_forcesDirty = true;
+        if (!Handle()) return;
+        gb_body_edit e;
+        e.world = 0;
+        e.body = index;
+        e.op = op;
+        e.wake = wake ? 1 : 0;
+        e.v[0] = v0; e.v[1] = v1; e.v[2] = v2; e.v[3] = v3;
+        gb_body_edits(m_h, 1, &e);
+        m_stale = true;
     }
 
 private:
@@ -554,13 +556,20 @@ private:
     std::vector<std::unique_ptr<b2Contact>> m_contacts, m_old;
     bool m_eventsOn = false;
     std::vector<b2Contact*> m_contactView;
-    std::vector<float> m_state, m_forces;
-    bool m_stale = true, m_forcesDirty = false;
+    std::vector<float> m_state;
+    bool m_stale = true;
 };
 
 inline b2Fixture* b2Body::CreateFixture(const b2FixtureDef* def) { return m_world->AddFixture(this, def); }
 inline const float* b2Body::State() const { return m_world->BodyState(m_index); }
-inline void b2Body::ApplyForceToCenter(const b2Vec2& force, bool) { m_world->AddForce(m_index, force.x, force.y, 0.0f); }
-inline void b2Body::ApplyTorque(float torque, bool) { m_world->AddForce(m_index, 0.0f, 0.0f, torque); }
+inline void b2Body::SetTransform(const b2Vec2& p, float angle) { m_world->Edit(m_index, GB_EDIT_SET_TRANSFORM, p.x, p.y, angle, 0.0f, true); }
+inline void b2Body::SetLinearVelocity(const b2Vec2& v) { m_world->Edit(m_index, GB_EDIT_SET_LINEAR_VELOCITY, v.x, v.y, 0.0f, 0.0f, true); }
+inline void b2Body::SetAngularVelocity(float w) { m_world->Edit(m_index, GB_EDIT_SET_ANGULAR_VELOCITY, w, 0.0f, 0.0f, 0.0f, true); }
+inline void b2Body::SetAwake(bool flag) { m_world->Edit(m_index, GB_EDIT_SET_AWAKE, flag ? 1.0f : 0.0f, 0.0f, 0.0f, 0.0f, true); }
+inline void b2Body::ApplyForce(const b2Vec2& f, const b2Vec2& p, bool wake) { m_world->Edit(m_index, GB_EDIT_APPLY_FORCE, f.x, f.y, p.x, p.y, wake); }
+inline void b2Body::ApplyForceToCenter(const b2Vec2& f, bool wake) { m_world->Edit(m_index, GB_EDIT_APPLY_FORCE_TO_CENTER, f.x, f.y, 0.0f, 0.0f, wake); }
+inline void b2Body::ApplyTorque(float torque, bool wake) { m_world->Edit(m_index, GB_EDIT_APPLY_TORQUE, torque, 0.0f, 0.0f, 0.0f, wake); }
+inline void b2Body::ApplyLinearImpulse(const b2Vec2& i, const b2Vec2& p, bool wake) { m_world->Edit(m_index, GB_EDIT_APPLY_LINEAR_IMPULSE, i.x, i.y, p.x, p.y, wake); }
+inline void b2Body::ApplyAngularImpulse(float impulse, bool wake) { m_world->Edit(m_index, GB_EDIT_APPLY_ANGULAR_IMPULSE, impulse, 0.0f, 0.0f, 0.0f, wake); }
 
 } // namespace box2d

@@ -69,6 +69,7 @@ def _declare(lib, p: str) -> None:
         "toi": (None, [C.c_int, _f32p, C.c_int, _f32p, C.c_int, _f32p, C.c_int, _f32p, C.c_float, _f32p]),
         "sincosf": (None, [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
         "step_many": (None, [C.POINTER(vp), C.c_int, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int]),
+        "body_edit": (None, [vp, C.c_int, C.c_int, C.c_int, _f32p]),
     }
     if p == "rw_":
         sig["joint"] = (C.c_int, [vp, C.c_int, C.c_int, C.c_int, _f32p, C.c_int])
@@ -156,6 +157,12 @@ class OracleWorld:
 
     def step(self, dt: float = 1.0 / 60.0, vi: int = 8, pi: int = 3) -> None:
         self._fn("step")(self.h, dt, vi, pi)
+
+    def body_edit(self, op: int, body: int, values, wake: bool = True) -> None:
+        """A b2Body state change between steps (op: the C-ABI's GB_EDIT_* code)."""
+        v = np.zeros(4, dtype=np.float32)
+        v[:len(values)] = values
+        self._fn("body_edit")(self.h, int(op), int(body), int(bool(wake)), v)
 
     def bodies(self) -> np.ndarray:
         n = self._fn("body_count")(self.h)

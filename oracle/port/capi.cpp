@@ -79,6 +79,7 @@ void po_build(void* h, int nb, const int* btype, const float* bf, const int* bfl
 }
 
 void po_step(void* h, float dt, int vi, int pi) { static_cast<World*>(h)->Step(dt, vi, pi); }
+void po_body_edit(void* h, int op, int body, int wake, const float* v) { static_cast<World*>(h)->ApplyEdit(op, body, wake, v); }
 
 // Steps many independent worlds on `threads` host threads (static round-robin split of the worlds,
 // which the caller orders by estimated cost). Used for the all-cores CPU baseline.

@@ -217,15 +217,84 @@ void World::SynchronizeFixtures(int bi)
     Xf xf1;
     xf1.q = RotOf(b.sweep.a0);
     xf1.p = b.sweep.c0 - Mul(xf1.q, b.sweep.localCenter);
+    SynchronizeFixturesFrom(bi, xf1, b.xf);
+}
+
+// b2Fixture::Synchronize (Dynamics/b2Fixture.cpp:154-177) of every fixture of body bi from xf1 to xf2
+void World::SynchronizeFixturesFrom(int bi, const Xf& xf1, const Xf& xf2)
+{
+    Body& b = bodies[bi];
     for (int f = b.fixtureList; f != kNull; f = fixtures[f].next) {
         Fixture& fx = fixtures[f];
         if (fx.proxyCount == 0) continue;
         AABB a1, a2;
         ComputeAABB(fx.shape, xf1, &a1);
-        ComputeAABB(fx.shape, b.xf, &a2);
+        ComputeAABB(fx.shape, xf2, &a2);
         fx.aabb = Combine(a1, a2);
-        Vec2 displacement = b.xf.p - xf1.p;
+        Vec2 displacement = xf2.p - xf1.p;
         bp.MoveProxy(fx.proxyId, fx.aabb, displacement);
+    }
+}
+
+// b2Body state changes between steps: SetTransform (Dynamics/b2Body.cpp:419-441), SetLinearVelocity,
+// SetAngularVelocity (b2Body.h:501-530), SetAwake (b2Body.h:635-655), ApplyForce, ApplyForceToCenter,
+// ApplyTorque, ApplyLinearImpulse, ApplyAngularImpulse (b2Body.h:739-830). op: the C-ABI's GB_EDIT_*.
+void World::ApplyEdit(int op, int bi, int wake, const float* v)
+{
+    Body& b = bodies[bi];
+    auto wakeOnRequest = [&]() {
+        if (wake && (b.flags & kBAwake) == 0) SetAwake(bi, true);
+    };
+    switch (op) {
+    case 0: {
+        b.xf.q = RotOf(v[2]);
+        b.xf.p = V(v[0], v[1]);
+        b.sweep.c = Mul(b.xf, b.sweep.localCenter);
+        b.sweep.a = v[2];
+        b.sweep.c0 = b.sweep.c;
+        b.sweep.a0 = v[2];
+        SynchronizeFixturesFrom(bi, b.xf, b.xf);
+        break;
+    }
+    case 1: {
+        if (b.type == kStatic) break;
+        const Vec2 vel = V(v[0], v[1]);
+        if (Dot(vel, vel) > 0.0f) SetAwake(bi, true);
+        b.v = vel;
+        break;
+    }
+    case 2:
+        if (b.type == kStatic) break;
+        if (v[0] * v[0] > 0.0f) SetAwake(bi, true);
+        b.w = v[0];
+        break;
+    case 3:
+        SetAwake(bi, v[0] != 0.0f);
+        break;
+    case 4: case 5: case 6:
+        if (b.type != kDynamic) break;
+        wakeOnRequest();
+        if ((b.flags & kBAwake) == 0) break;
+        if (op == 6) {
+            b.torque += v[0];
+        } else {
+            b.force = b.force + V(v[0], v[1]);
+            if (op == 4) b.torque += Cross(V(v[2], v[3]) - b.sweep.c, V(v[0], v[1]));
+        }
+        break;
+    case 7: case 8:
+        if (b.type != kDynamic) break;
+        wakeOnRequest();
+        if ((b.flags & kBAwake) == 0) break;
+        if (op == 7) {
+            b.v = b.v + b.invMass * V(v[0], v[1]);
+            b.w += b.invI * Cross(V(v[2], v[3]) - b.sweep.c, V(v[0], v[1]));
+        } else {
+            b.w += b.invI * v[0];
+        }
+        break;
+    default:
+        break;
     }
 }
 

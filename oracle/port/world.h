@@ -108,6 +108,8 @@ struct World {
     void SetAwake(int b, bool flag);
     bool ShouldCollide(int bodyB, int bodyA) const;
     void SynchronizeFixtures(int b);
+    void SynchronizeFixturesFrom(int b, const Xf& xf1, const Xf& xf2);
+    void ApplyEdit(int op, int b, int wake, const float* v);
     void SynchronizeTransform(int b);
     void Advance(int b, float alpha);
 

@@ -204,6 +204,25 @@ void rw_build(void* h, int nb, const int* btype, const float* bf, const int* bfl
 
 void rw_step(void* h, float dt, int vi, int pi) { static_cast<RefWorld*>(h)->world.Step(dt, vi, pi); }
 
+// A b2Body state change between steps through the reference's own methods. op: the C-ABI's GB_EDIT_*.
+void rw_body_edit(void* h, int op, int body, int wake, const float* v)
+{
+    b2Body* b = static_cast<RefWorld*>(h)->bodies[body];
+    const bool w = wake != 0;
+    switch (op) {
+    case 0: b->SetTransform(b2Vec2(v[0], v[1]), v[2]); break;
+    case 1: b->SetLinearVelocity(b2Vec2(v[0], v[1])); break;
+    case 2: b->SetAngularVelocity(v[0]); break;
+    case 3: b->SetAwake(v[0] != 0.0f); break;
+    case 4: b->ApplyForce(b2Vec2(v[0], v[1]), b2Vec2(v[2], v[3]), w); break;
+    case 5: b->ApplyForceToCenter(b2Vec2(v[0], v[1]), w); break;
+    case 6: b->ApplyTorque(v[0], w); break;
+    case 7: b->ApplyLinearImpulse(b2Vec2(v[0], v[1]), b2Vec2(v[2], v[3]), w); break;
+    case 8: b->ApplyAngularImpulse(v[0], w); break;
+    default: break;
+    }
+}
+
 int rw_body_count(void* h) { return (int)static_cast<RefWorld*>(h)->bodies.size(); }
 int rw_contact_count(void* h) { return static_cast<RefWorld*>(h)->world.GetContactCount(); }
 

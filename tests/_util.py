@@ -42,3 +42,37 @@ def first_divergence(world, steps: int, golden_digests: np.ndarray):
         if not np.array_equal(digest(b, ci, cf), golden_digests[s - 1]):
             return s
     return None
+
+
+# op codes of gb_body_edit (GB_EDIT_*)
+SET_TRANSFORM, SET_LINEAR_VELOCITY, SET_ANGULAR_VELOCITY, SET_AWAKE = 0, 1, 2, 3
+APPLY_FORCE, APPLY_FORCE_TO_CENTER, APPLY_TORQUE, APPLY_LINEAR_IMPULSE, APPLY_ANGULAR_IMPULSE = 4, 5, 6, 7, 8
+
+
+def edit_scene():
+    """A 10-row pyramid on an edge ground with a kinematic paddle, sleep on: the b2Body edit cases."""
+    from box2dpp_gb300 import scenes
+
+    s = scenes.pyramid(10)
+    k = s.body(scenes.KINEMATIC, -15.0, 3.0, vx=1.0)
+    s.fixture(k, scenes.BOX, [2.0, 0.25], 2)
+    return s
+
+
+def edit_script():
+    """{step: [(op, body, values, wake)]} applied before that step: every edit kind, on dynamic,
+    static (body 0) and kinematic (the last body) targets, on awake and sleeping bodies."""
+    kin = 56  # 1 ground + 55 boxes, then the paddle
+    return {
+        5: [(APPLY_LINEAR_IMPULSE, 3, (2.0, 9.0, 0.3, 0.9), True), (APPLY_ANGULAR_IMPULSE, 8, (1.5,), True),
+            (SET_LINEAR_VELOCITY, 0, (3.0, 0.0), True)],
+        20: [(SET_TRANSFORM, 55, (6.0, 14.0, 0.7), True), (SET_ANGULAR_VELOCITY, 55, (2.0,), True),
+             (APPLY_FORCE, 12, (300.0, 40.0, 0.2, 1.0), True), (APPLY_TORQUE, 13, (25.0,), False),
+             (APPLY_FORCE_TO_CENTER, 14, (-200.0, 0.0), True)],
+        40: [(SET_LINEAR_VELOCITY, kin, (-2.0, 0.5), True), (SET_ANGULAR_VELOCITY, kin, (0.3,), True),
+             (SET_AWAKE, 20, (0.0,), True), (SET_TRANSFORM, 30, (-8.0, 0.6, 0.0), True)],
+        60: [(APPLY_LINEAR_IMPULSE, 20, (0.0, 5.0, 0.0, 0.0), False), (APPLY_FORCE, 21, (0.0, 500.0, 0.0, 0.0), True)],
+        300: [(APPLY_LINEAR_IMPULSE, 25, (4.0, 4.0, 0.0, 0.0), False), (APPLY_TORQUE, 26, (10.0,), False),
+              (SET_AWAKE, 27, (1.0,), True), (APPLY_ANGULAR_IMPULSE, 28, (3.0,), True)],
+        310: [(SET_TRANSFORM, kin, (15.0, 3.0, 0.2), True), (SET_LINEAR_VELOCITY, 40, (0.0, 0.0), True)],
+    }

@@ -67,3 +67,54 @@ def test_hello_world_matches_oracle(gpu, tmp_path):
     assert [int(tail[3]), int(tail[5]), int(tail[9]), int(tail[11])] == [kinds[0], kinds[1], kinds[2], kinds[3]]
     assert kinds[3] > 0
     assert np.float32(float.fromhex(tail[13])).view(np.uint32) == np.float32(last_post).view(np.uint32)
+
+
+EDITS_SRC = os.path.join(ROOT, "tests", "cpp", "body_edits.cpp")
+
+
+def _compile_edits(tmp_path):
+    lib = _lib.library_path()
+    exe = str(tmp_path / "body_edits")
+    libdir = os.path.dirname(lib)
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "include"), EDITS_SRC, "-o",
+           exe, "-L", libdir, "-lbox2d_gb300", f"-Wl,-rpath,{libdir}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return exe
+
+
+def test_cpp_body_edits_compile(tmp_path):
+    _compile_edits(tmp_path)
+
+
+@pytest.mark.gpu
+def test_cpp_body_edits_match_oracle(gpu, tmp_path):
+    """b2Body::ApplyLinearImpulse, SetTransform, SetAngularVelocity, ApplyForce, ApplyTorque,
+    SetLinearVelocity and SetAwake through the C++ mirror, bit for bit like the CPU oracle."""
+    from tests._util import (APPLY_FORCE, APPLY_LINEAR_IMPULSE, APPLY_TORQUE, SET_ANGULAR_VELOCITY, SET_AWAKE,
+                             SET_LINEAR_VELOCITY, SET_TRANSFORM)
+
+    exe = _compile_edits(tmp_path)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    got = np.array([[float.fromhex(v) for v in ln.split()[1:4]] for ln in r.stdout.strip().splitlines()],
+                   dtype=np.float32)
+    sc = scenes.Scene(name="body_edits")
+    g = sc.body(scenes.STATIC, 0.0, -10.0)
+    sc.fixture(g, 3, [50.0, 10.0], n=2, density=0.0)
+    b = sc.body(scenes.DYNAMIC, 0.0, 4.0)
+    sc.fixture(b, 3, [1.0, 1.0], n=2, density=1.0, friction=0.3)
+    o = oracle.OracleWorld(sc, "port", "project")
+    script = {10: (APPLY_LINEAR_IMPULSE, (3.0, 6.0, 0.5, 3.0)), 25: (SET_TRANSFORM, (-4.0, 6.0, 0.6)),
+              30: (SET_ANGULAR_VELOCITY, (3.0,)), 40: (APPLY_FORCE, (50.0, 0.0, -4.0, 1.0)),
+              41: (APPLY_TORQUE, (-20.0,)), 60: (SET_LINEAR_VELOCITY, (1.0, 0.0)), 75: (SET_AWAKE, (0.0,))}
+    want = []
+    for i in range(90):
+        if i in script:
+            op, vals = script[i]
+            o.body_edit(op, 1, vals, True)
+        o.step(1.0 / 60.0, 8, 3)
+        s = o.bodies()[1]
+        want.append([s[0], s[1], s[2]])
+    want = np.array(want, dtype=np.float32)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
