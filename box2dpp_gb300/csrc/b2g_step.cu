@@ -2113,11 +2113,12 @@ __global__ void __launch_bounds__(256) NarrowphaseKernel(Batch B)
 // (positions, then velocities) and the accumulated impulses of the island contacts when a world's
 // fit, and the broadphase proxies, pair keys and list heads outside the island solve; every use
 // falls back to global memory when the world is larger, so the shape changes speed, never results.
-// Minimum resident CTAs per SM the register allocation must allow at 128 threads: 3 caps the
-// kernel at 170 registers (measured fastest; uncapped it takes 255, and 128 or fewer cost more in
-// spills than the extra resident worlds gain).
+// Minimum resident CTAs per SM the register allocation must allow at 128 threads: StepKernel 4
+// (128 registers), StepToiKernel 3 (168; its time-of-impact code spills more when capped lower).
+// Measured on the bench batch: 4/3 3.89 ms per step coloured, 10.20 plain; 3/3 4.05, 10.51; 4/4
+// 4.01, 10.33; 5/4 4.24, 11.37.
 #ifndef B2G_STEP_MIN_BLOCKS
-#define B2G_STEP_MIN_BLOCKS 3
+#define B2G_STEP_MIN_BLOCKS 4
 #endif
 __global__ void __launch_bounds__(128, B2G_STEP_MIN_BLOCKS) StepKernel(Batch B, StepParams P, const int* schedule, LaunchShape L)
 {
@@ -2199,7 +2200,10 @@ __global__ void __launch_bounds__(256, 2) ToiKernel(Batch B, float dt)
 
 // The continuous phase of b2World::Step (b2World.cpp:948-958) and the end of the step: the TOI
 // event loop, force clearing, inv_dt0.
-__global__ void __launch_bounds__(128, B2G_STEP_MIN_BLOCKS) StepToiKernel(Batch B, StepParams P, const int* schedule, LaunchShape L)
+#ifndef B2G_TOI_MIN_BLOCKS
+#define B2G_TOI_MIN_BLOCKS 3
+#endif
+__global__ void __launch_bounds__(128, B2G_TOI_MIN_BLOCKS) StepToiKernel(Batch B, StepParams P, const int* schedule, LaunchShape L)
 {
     extern __shared__ float4 smem[];
     Wd W;
