@@ -71,8 +71,8 @@ def _declare(lib, p: str) -> None:
         "step_many": (None, [C.POINTER(vp), C.c_int, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int]),
         "body_edit": (None, [vp, C.c_int, C.c_int, C.c_int, _f32p]),
     }
+    sig["joint"] = (C.c_int, [vp, C.c_int, C.c_int, C.c_int, _f32p, C.c_int])
     if p == "rw_":
-        sig["joint"] = (C.c_int, [vp, C.c_int, C.c_int, C.c_int, _f32p, C.c_int])
         sig["query_aabb"] = (C.c_int, [vp, _f32p, _i32p, C.c_int])
         sig["raycast"] = (C.c_int, [vp, _f32p, _f32p])
     if p == "po_":
@@ -134,8 +134,6 @@ class OracleWorld:
                     int(scene.sub_stepping))
         a = scene.arrays()
         typed = bool(len(a["joint_type"])) and bool((a["joint_type"] != 0).any())
-        if typed and kind == "port":
-            raise NotImplementedError("the CPU restatement builds revolute joints only")
         nj = 0 if typed else len(a["joint_a"])
         f("build")(self.h, len(a["body_type"]), a["body_type"], a["body_f"], a["body_flags"],
                    len(a["fix_body"]), a["fix_body"], a["fix_type"], a["fix_shape"], a["fix_n"], a["fix_mat"],

@@ -62,6 +62,7 @@ int po_fixture(void* h, int body, int shapeType, const float* s, int n, const fl
     return w->CreateFixture(body, MakeShape(shapeType, s, n), mat[0], mat[1], mat[2], filt[0], filt[1], filt[2], filt[3] != 0);
 }
 int po_revolute(void* h, int a, int b, const float* f, int flags) { return static_cast<World*>(h)->CreateRevolute(a, b, f, flags); }
+int po_joint(void* h, int type, int a, int b, const float* f, int flags) { return static_cast<World*>(h)->CreateJoint(type, a, b, f, flags); }
 // Bulk scene build: body b is created, then its fixtures (fbody is non-decreasing), then all joints.
 void po_build(void* h, int nb, const int* btype, const float* bf, const int* bflags, int nf, const int* fbody,
               const int* ftype, const float* fshape, const int* fn, const float* fmat, const int* ffilt, int nj,

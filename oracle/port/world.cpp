@@ -131,6 +131,33 @@ int World::CreateRevolute(int a, int b, const float* f, int fl)
     j.enableLimit = (fl & 1) != 0;
     j.enableMotor = (fl & 2) != 0;
     j.collideConnected = (fl & 4) != 0;
+    return LinkJoint(j, a, b);
+}
+
+// b2World::CreateJoint for a revolute, distance (b2DistanceJoint.cpp:52-63) or weld (b2WeldJoint.cpp:
+// 48-58) definition; f as the C-ABI's gb_create_joints: revolute as CreateRevolute, distance
+// localAnchorA, localAnchorB, length, frequencyHz, dampingRatio, weld localAnchorA, localAnchorB,
+// referenceAngle, frequencyHz, dampingRatio; flags bit 4 collideConnected.
+int World::CreateJoint(int type, int a, int b, const float* f, int fl)
+{
+    if (type == kRevoluteJoint) return CreateRevolute(a, b, f, fl);
+    Joint j;
+    j.type = type;
+    j.bodyA = a; j.bodyB = b;
+    j.localAnchorA = V(f[0], f[1]);
+    j.localAnchorB = V(f[2], f[3]);
+    if (type == kDistanceJoint) j.length = f[4];
+    else j.referenceAngle = f[4];
+    j.frequencyHz = f[5];
+    j.dampingRatio = f[6];
+    j.collideConnected = (fl & 4) != 0;
+    return LinkJoint(j, a, b);
+}
+
+// b2World::CreateJoint (Dynamics/b2World.cpp:212-269): the joint list, both bodies' joint edges, and
+// the filter flag on contacts between the bodies when they may not collide.
+int World::LinkJoint(Joint& j, int a, int b)
+{
     int id = (int)joints.size();
     j.prev = kNull;
     j.next = jointList;
@@ -951,6 +978,14 @@ void RevInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* 
     vel[j.indexB].v = vB; vel[j.indexB].w = wB;
 }
 
+// forward declarations of the joint kinds other than revolute (below)
+void DistInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel);
+void DistSolveVelocity(Joint& j, Velocity* vel);
+bool DistSolvePosition(Joint& j, Position* pos);
+void WeldInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel);
+void WeldSolveVelocity(Joint& j, Velocity* vel);
+bool WeldSolvePosition(Joint& j, Position* pos);
+
 // b2Mat33::Solve33 / Solve22 (Common/b2Math.cpp:24-56)
 inline void Solve33(const float* M, const float* b, float* x)
 {
@@ -1090,6 +1125,297 @@ bool RevSolvePosition(Joint& j, Position* pos)
     pos[j.indexB].c = cB; pos[j.indexB].a = aB;
     return positionError <= kLinearSlop && angularError <= kAngularSlop;
 }
+
+// ---------------------------------------------------------------- distance joint
+// b2DistanceJoint::InitVelocityConstraints (Dynamics/Joints/b2DistanceJoint.cpp:65-158)
+void DistInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel)
+{
+    const Body& A = w->bodies[j.bodyA];
+    const Body& B = w->bodies[j.bodyB];
+    j.indexA = A.islandIndex; j.indexB = B.islandIndex;
+    j.localCenterA = A.sweep.localCenter; j.localCenterB = B.sweep.localCenter;
+    j.invMassA = A.invMass; j.invMassB = B.invMass;
+    j.invIA = A.invI; j.invIB = B.invI;
+    const Vec2 cA = pos[j.indexA].c, cB = pos[j.indexB].c;
+    const float aA = pos[j.indexA].a, aB = pos[j.indexB].a;
+    Vec2 vA = vel[j.indexA].v, vB = vel[j.indexB].v;
+    float wA = vel[j.indexA].w, wB = vel[j.indexB].w;
+    const Rot qA = RotOf(aA), qB = RotOf(aB);
+    j.rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    j.rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    j.u = cB + j.rB - cA - j.rA;
+    const float length = Length(j.u);
+    if (length > kLinearSlop) {
+        j.u.x *= 1.0f / length;
+        j.u.y *= 1.0f / length;
+    } else {
+        j.u = V(0.0f, 0.0f);
+    }
+    const float crAu = Cross(j.rA, j.u), crBu = Cross(j.rB, j.u);
+    float invMass = j.invMassA + j.invIA * crAu * crAu + j.invMassB + j.invIB * crBu * crBu;
+    j.motorMass = invMass != 0.0f ? 1.0f / invMass : 0.0f;
+    if (j.frequencyHz > 0.0f) {
+        const float C = length - j.length;
+        const float omega = 2.0f * kPi * j.frequencyHz;
+        const float d = 2.0f * j.motorMass * j.dampingRatio * omega;
+        const float k = j.motorMass * omega * omega;
+        const float h = step.dt;
+        j.gamma = h * (d + h * k);
+        j.gamma = j.gamma != 0.0f ? 1.0f / j.gamma : 0.0f;
+        j.bias = C * h * k * j.gamma;
+        invMass += j.gamma;
+        j.motorMass = invMass != 0.0f ? 1.0f / invMass : 0.0f;
+    } else {
+        j.gamma = 0.0f;
+        j.bias = 0.0f;
+    }
+    if (step.warmStarting) {
+        j.impulse[0] *= step.dtRatio;
+        const Vec2 P = j.impulse[0] * j.u;
+        vA = vA - j.invMassA * P;
+        wA -= j.invIA * Cross(j.rA, P);
+        vB = vB + j.invMassB * P;
+        wB += j.invIB * Cross(j.rB, P);
+    } else {
+        j.impulse[0] = 0.0f;
+    }
+    vel[j.indexA].v = vA; vel[j.indexA].w = wA;
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+}
+
+// b2DistanceJoint::SolveVelocityConstraints (b2DistanceJoint.cpp:160-185)
+void DistSolveVelocity(Joint& j, Velocity* vel)
+{
+    Vec2 vA = vel[j.indexA].v, vB = vel[j.indexB].v;
+    float wA = vel[j.indexA].w, wB = vel[j.indexB].w;
+    const Vec2 vpA = vA + Cross(wA, j.rA);
+    const Vec2 vpB = vB + Cross(wB, j.rB);
+    const float Cdot = Dot(j.u, vpB - vpA);
+    const float impulse = -j.motorMass * (Cdot + j.bias + j.gamma * j.impulse[0]);
+    j.impulse[0] += impulse;
+    const Vec2 P = impulse * j.u;
+    vA = vA - j.invMassA * P;
+    wA -= j.invIA * Cross(j.rA, P);
+    vB = vB + j.invMassB * P;
+    wB += j.invIB * Cross(j.rB, P);
+    vel[j.indexA].v = vA; vel[j.indexA].w = wA;
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+}
+
+// b2DistanceJoint::SolvePositionConstraints (b2DistanceJoint.cpp:187-226)
+bool DistSolvePosition(Joint& j, Position* pos)
+{
+    if (j.frequencyHz > 0.0f) return true;
+    Vec2 cA = pos[j.indexA].c, cB = pos[j.indexB].c;
+    float aA = pos[j.indexA].a, aB = pos[j.indexB].a;
+    const Rot qA = RotOf(aA), qB = RotOf(aB);
+    const Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    const Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    Vec2 u = cB + rB - cA - rA;
+    const float length = Normalize(u);
+    float C = length - j.length;
+    C = Clamp(C, -kMaxLinearCorrection, kMaxLinearCorrection);
+    const float impulse = -j.motorMass * C;
+    const Vec2 P = impulse * u;
+    cA = cA - j.invMassA * P;
+    aA -= j.invIA * Cross(rA, P);
+    cB = cB + j.invMassB * P;
+    aB += j.invIB * Cross(rB, P);
+    pos[j.indexA].c = cA; pos[j.indexA].a = aA;
+    pos[j.indexB].c = cB; pos[j.indexB].a = aB;
+    return Abs(C) < kLinearSlop;
+}
+
+// ---------------------------------------------------------------- weld joint
+// K of b2WeldJoint (b2WeldJoint.cpp:95-105 and 245-254), columns ex = K[0..2], ey = K[3..5], ez = K[6..8]
+void WeldK(const Joint& j, Vec2 rA, Vec2 rB, float* K)
+{
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    K[0] = mA + mB + rA.y * rA.y * iA + rB.y * rB.y * iB;
+    K[3] = -rA.y * rA.x * iA - rB.y * rB.x * iB;
+    K[6] = -rA.y * iA - rB.y * iB;
+    K[1] = K[3];
+    K[4] = mA + mB + rA.x * rA.x * iA + rB.x * rB.x * iB;
+    K[7] = rA.x * iA + rB.x * iB;
+    K[2] = K[6];
+    K[5] = K[7];
+    K[8] = iA + iB;
+}
+
+// b2Mat33::GetInverse22 (Common/b2Math.cpp:59-72): the 2x2 block's inverse, the rest zero
+void Inverse22(const float* K, float* M)
+{
+    const float a = K[0], b = K[3], c = K[1], d = K[4];
+    float det = a * d - b * c;
+    if (det != 0.0f) det = 1.0f / det;
+    M[0] = det * d; M[3] = -det * b; M[2] = 0.0f;
+    M[1] = -det * c; M[4] = det * a; M[5] = 0.0f;
+    M[6] = 0.0f; M[7] = 0.0f; M[8] = 0.0f;
+}
+
+// b2Mat33::GetSymInverse33 (Common/b2Math.cpp:74-97)
+void SymInverse33(const float* K, float* M)
+{
+    const float cx = K[4] * K[8] - K[5] * K[7], cy = K[5] * K[6] - K[3] * K[8], cz = K[3] * K[7] - K[4] * K[6];
+    float det = K[0] * cx + K[1] * cy + K[2] * cz;
+    if (det != 0.0f) det = 1.0f / det;
+    const float a11 = K[0], a12 = K[3], a13 = K[6];
+    const float a22 = K[4], a23 = K[7];
+    const float a33 = K[8];
+    M[0] = det * (a22 * a33 - a23 * a23);
+    M[1] = det * (a13 * a23 - a12 * a33);
+    M[2] = det * (a12 * a23 - a13 * a22);
+    M[3] = M[1];
+    M[4] = det * (a11 * a33 - a13 * a13);
+    M[5] = det * (a13 * a12 - a11 * a23);
+    M[6] = M[2];
+    M[7] = M[5];
+    M[8] = det * (a11 * a22 - a12 * a12);
+}
+
+// b2WeldJoint::InitVelocityConstraints (Dynamics/Joints/b2WeldJoint.cpp:60-169)
+void WeldInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel)
+{
+    const Body& A = w->bodies[j.bodyA];
+    const Body& B = w->bodies[j.bodyB];
+    j.indexA = A.islandIndex; j.indexB = B.islandIndex;
+    j.localCenterA = A.sweep.localCenter; j.localCenterB = B.sweep.localCenter;
+    j.invMassA = A.invMass; j.invMassB = B.invMass;
+    j.invIA = A.invI; j.invIB = B.invI;
+    const float aA = pos[j.indexA].a, aB = pos[j.indexB].a;
+    Vec2 vA = vel[j.indexA].v, vB = vel[j.indexB].v;
+    float wA = vel[j.indexA].w, wB = vel[j.indexB].w;
+    const Rot qA = RotOf(aA), qB = RotOf(aB);
+    j.rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    j.rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    float K[9];
+    WeldK(j, j.rA, j.rB, K);
+    if (j.frequencyHz > 0.0f) {
+        Inverse22(K, j.mass);
+        float invM = iA + iB;
+        const float m = invM > 0.0f ? 1.0f / invM : 0.0f;
+        const float C = aB - aA - j.referenceAngle;
+        const float omega = 2.0f * kPi * j.frequencyHz;
+        const float d = 2.0f * m * j.dampingRatio * omega;
+        const float k = m * omega * omega;
+        const float h = step.dt;
+        j.gamma = h * (d + h * k);
+        j.gamma = j.gamma != 0.0f ? 1.0f / j.gamma : 0.0f;
+        j.bias = C * h * k * j.gamma;
+        invM += j.gamma;
+        j.mass[8] = invM != 0.0f ? 1.0f / invM : 0.0f;
+    } else if (K[8] == 0.0f) {
+        Inverse22(K, j.mass);
+        j.gamma = 0.0f;
+        j.bias = 0.0f;
+    } else {
+        SymInverse33(K, j.mass);
+        j.gamma = 0.0f;
+        j.bias = 0.0f;
+    }
+    if (step.warmStarting) {
+        j.impulse[0] *= step.dtRatio; j.impulse[1] *= step.dtRatio; j.impulse[2] *= step.dtRatio;
+        const Vec2 P = V(j.impulse[0], j.impulse[1]);
+        vA = vA - mA * P;
+        wA -= iA * (Cross(j.rA, P) + j.impulse[2]);
+        vB = vB + mB * P;
+        wB += iB * (Cross(j.rB, P) + j.impulse[2]);
+    } else {
+        j.impulse[0] = j.impulse[1] = j.impulse[2] = 0.0f;
+    }
+    vel[j.indexA].v = vA; vel[j.indexA].w = wA;
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+}
+
+// b2WeldJoint::SolveVelocityConstraints (b2WeldJoint.cpp:171-227)
+void WeldSolveVelocity(Joint& j, Velocity* vel)
+{
+    Vec2 vA = vel[j.indexA].v, vB = vel[j.indexB].v;
+    float wA = vel[j.indexA].w, wB = vel[j.indexB].w;
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    const float* M = j.mass;
+    if (j.frequencyHz > 0.0f) {
+        const float Cdot2 = wB - wA;
+        const float impulse2 = -M[8] * (Cdot2 + j.bias + j.gamma * j.impulse[2]);
+        j.impulse[2] += impulse2;
+        wA -= iA * impulse2;
+        wB += iB * impulse2;
+        const Vec2 Cdot1 = vB + Cross(wB, j.rB) - vA - Cross(wA, j.rA);
+        const Vec2 impulse1 = -MulM33x(M, Cdot1);
+        j.impulse[0] += impulse1.x;
+        j.impulse[1] += impulse1.y;
+        const Vec2 P = impulse1;
+        vA = vA - mA * P;
+        wA -= iA * Cross(j.rA, P);
+        vB = vB + mB * P;
+        wB += iB * Cross(j.rB, P);
+    } else {
+        const Vec2 Cdot1 = vB + Cross(wB, j.rB) - vA - Cross(wA, j.rA);
+        const float Cdot2 = wB - wA;
+        // b2Mul(b2Mat33, b2Vec3) = Cdot.x * ex + Cdot.y * ey + Cdot.z * ez
+        const float ix = -((Cdot1.x * M[0] + Cdot1.y * M[3]) + Cdot2 * M[6]);
+        const float iy = -((Cdot1.x * M[1] + Cdot1.y * M[4]) + Cdot2 * M[7]);
+        const float iz = -((Cdot1.x * M[2] + Cdot1.y * M[5]) + Cdot2 * M[8]);
+        j.impulse[0] += ix;
+        j.impulse[1] += iy;
+        j.impulse[2] += iz;
+        const Vec2 P = V(ix, iy);
+        vA = vA - mA * P;
+        wA -= iA * (Cross(j.rA, P) + iz);
+        vB = vB + mB * P;
+        wB += iB * (Cross(j.rB, P) + iz);
+    }
+    vel[j.indexA].v = vA; vel[j.indexA].w = wA;
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+}
+
+// b2WeldJoint::SolvePositionConstraints (b2WeldJoint.cpp:229-316)
+bool WeldSolvePosition(Joint& j, Position* pos)
+{
+    Vec2 cA = pos[j.indexA].c, cB = pos[j.indexB].c;
+    float aA = pos[j.indexA].a, aB = pos[j.indexB].a;
+    const Rot qA = RotOf(aA), qB = RotOf(aB);
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    const Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    const Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    float K[9];
+    WeldK(j, rA, rB, K);
+    float positionError, angularError;
+    if (j.frequencyHz > 0.0f) {
+        const Vec2 C1 = cB + rB - cA - rA;
+        positionError = Length(C1);
+        angularError = 0.0f;
+        const Vec2 P = -Solve22(K, C1);
+        cA = cA - mA * P;
+        aA -= iA * Cross(rA, P);
+        cB = cB + mB * P;
+        aB += iB * Cross(rB, P);
+    } else {
+        const Vec2 C1 = cB + rB - cA - rA;
+        const float C2 = aB - aA - j.referenceAngle;
+        positionError = Length(C1);
+        angularError = Abs(C2);
+        float imp[3];
+        if (K[8] > 0.0f) {
+            const float Cv[3] = {C1.x, C1.y, C2};
+            Solve33(K, Cv, imp);
+            imp[0] = -imp[0]; imp[1] = -imp[1]; imp[2] = -imp[2];
+        } else {
+            const Vec2 i2 = -Solve22(K, C1);
+            imp[0] = i2.x; imp[1] = i2.y; imp[2] = 0.0f;
+        }
+        const Vec2 P = V(imp[0], imp[1]);
+        cA = cA - mA * P;
+        aA -= iA * (Cross(rA, P) + imp[2]);
+        cB = cB + mB * P;
+        aB += iB * (Cross(rB, P) + imp[2]);
+    }
+    pos[j.indexA].c = cA; pos[j.indexA].a = aA;
+    pos[j.indexB].c = cB; pos[j.indexB].a = aB;
+    return positionError <= kLinearSlop && angularError <= kAngularSlop;
+}
+
 } // namespace
 
 // ---------------------------------------------------------------- island solve
@@ -1120,9 +1446,19 @@ void World::IslandSolve(const StepInfo& step)
     ContactSolver cs(this, step, iContacts.data(), (int)iContacts.size(), positions.data(), velocities.data());
     cs.InitVelocity();
     if (step.warmStarting) cs.WarmStart();
-    for (int jn : iJoints) RevInit(this, joints[jn], step, positions.data(), velocities.data());
+    for (int jn : iJoints) {
+        Joint& j = joints[jn];
+        if (j.type == kDistanceJoint) DistInit(this, j, step, positions.data(), velocities.data());
+        else if (j.type == kWeldJoint) WeldInit(this, j, step, positions.data(), velocities.data());
+        else RevInit(this, j, step, positions.data(), velocities.data());
+    }
     for (int i = 0; i < step.velocityIterations; ++i) {
-        for (int jn : iJoints) RevSolveVelocity(joints[jn], step, velocities.data());
+        for (int jn : iJoints) {
+            Joint& j = joints[jn];
+            if (j.type == kDistanceJoint) DistSolveVelocity(j, velocities.data());
+            else if (j.type == kWeldJoint) WeldSolveVelocity(j, velocities.data());
+            else RevSolveVelocity(j, step, velocities.data());
+        }
         cs.SolveVelocity();
     }
     cs.StoreImpulses();
@@ -1152,7 +1488,10 @@ void World::IslandSolve(const StepInfo& step)
         bool contactsOkay = cs.SolvePosition(false, -1, -1);
         bool jointsOkay = true;
         for (int jn : iJoints) {
-            bool ok = RevSolvePosition(joints[jn], positions.data());
+            Joint& j = joints[jn];
+            bool ok = j.type == kDistanceJoint ? DistSolvePosition(j, positions.data())
+                      : j.type == kWeldJoint   ? WeldSolvePosition(j, positions.data())
+                                               : RevSolvePosition(j, positions.data());
             jointsOkay = jointsOkay && ok;
         }
         if (contactsOkay && jointsOkay) { positionSolved = true; break; }

@@ -54,7 +54,11 @@ struct Contact {
     bool alive = false;
 };
 
+// joint types (b2JointType, Dynamics/Joints/b2Joint.h:28-42, those restated here)
+enum JointType { kRevoluteJoint = 0, kDistanceJoint = 1, kWeldJoint = 2 };
+
 struct Joint {
+    int type = kRevoluteJoint;
     int bodyA = kNull, bodyB = kNull;
     bool collideConnected = false, islandFlag = false;
     int prev = kNull, next = kNull;
@@ -71,6 +75,11 @@ struct Joint {
     float invMassA = 0, invMassB = 0, invIA = 0, invIB = 0;
     float mass[9] = {0};     // b2Mat33 columns ex, ey, ez
     float motorMass = 0;
+    // distance joint (b2DistanceJoint.h): length, spring; weld joint (b2WeldJoint.h): spring (the
+    // weld's reference angle is referenceAngle, its impulse impulse[0..2], its mass mass[])
+    float length = 0, frequencyHz = 0, dampingRatio = 0;
+    float gamma = 0, bias = 0;
+    Vec2 u{0, 0};            // distance: unit axis of the step (its effective mass in motorMass)
 };
 
 struct Position { Vec2 c; float a; };
@@ -104,6 +113,8 @@ struct World {
     int CreateFixture(int body, const Shape& shape, float density, float friction, float restitution,
                       int category, int mask, int group, bool sensor);
     int CreateRevolute(int a, int b, const float* f, int flags);
+    int CreateJoint(int type, int a, int b, const float* f, int flags);
+    int LinkJoint(Joint& j, int a, int b);
     void ResetMassData(int b);
     void SetAwake(int b, bool flag);
     bool ShouldCollide(int bodyB, int bodyA) const;

@@ -16,8 +16,6 @@ CASES = trajectory_cases()
 def test_port_matches_reference_trajectory(name, make, steps, trig):
     g = golden(f"{name}_{trig}")
     sc = make()
-    if sc.joint_types - {0}:
-        pytest.skip("the CPU restatement builds revolute joints only; the GPU test checks this case")
     w = oracle.OracleWorld(sc, "port", trig)
     bad = first_divergence(w, steps, g["digests"])
     if trig == "libm" and bad is not None:
