@@ -781,15 +781,14 @@ gb_status CreateFixture(HWorld& W, int body, int type, const float* s, int n, co
     return GB_OK;
 }
 
-// b2World::CreateJoint (Dynamics/b2World.cpp:185-250) for a revolute, distance or weld joint
-// definition. f[9]: revolute localAnchorA, localAnchorB, referenceAngle, lowerAngle, upperAngle,
-// motorSpeed, maxMotorTorque; distance localAnchorA, localAnchorB, length, frequencyHz,
-// dampingRatio; weld localAnchorA, localAnchorB, referenceAngle, frequencyHz, dampingRatio.
+// b2World::CreateJoint (Dynamics/b2World.cpp:185-250) for a revolute, distance, weld or prismatic
+// joint definition; f as gb_create_joints documents (revolute, distance and weld use f[0..8]).
 gb_status CreateJoint(HWorld& W, int type, int a, int b, const float* f, int fl, int* id)
 {
     int nb = (int)W.bodies.size();
     if (a < 0 || a >= nb || b < 0 || b >= nb || a == b) return GB_ERR_INVALID;
-    if (type != kJointRevolute && type != kJointDistance && type != kJointWeld) return GB_ERR_INVALID;
+    if (type != kJointRevolute && type != kJointDistance && type != kJointWeld && type != kJointPrismatic)
+        return GB_ERR_INVALID;
     Joint j;
     std::memset(&j, 0, sizeof(j));
     j.type = type;
@@ -800,8 +799,19 @@ gb_status CreateJoint(HWorld& W, int type, int a, int b, const float* f, int fl,
         j.enableLimit = (fl & 1) != 0; j.enableMotor = (fl & 2) != 0;
     } else if (type == kJointDistance) {
         j.length = f[4]; j.frequencyHz = f[5]; j.dampingRatio = f[6];
-    } else {
+    } else if (type == kJointWeld) {
         j.referenceAngle = f[4]; j.frequencyHz = f[5]; j.dampingRatio = f[6];
+    } else {
+        // b2PrismaticJoint::b2PrismaticJoint (Dynamics/Joints/b2PrismaticJoint.cpp:102-126): the unit
+        // axis (b2Vec2::Normalize), its normal b2Cross(1, axis); the translation limits and the motor
+        // force sit in the angle-limit and motor-torque fields
+        Vec2 axis = V(f[4], f[5]);
+        Normalize(axis);
+        j.localXAxisA = axis;
+        j.localYAxisA = Cross(1.0f, axis);
+        j.referenceAngle = f[6]; j.lowerAngle = f[7]; j.upperAngle = f[8];
+        j.maxMotorTorque = f[9]; j.motorSpeed = f[10];
+        j.enableLimit = (fl & 1) != 0; j.enableMotor = (fl & 2) != 0;
     }
     j.collideConnected = (fl & 4) != 0;
     int idx = (int)W.joints.size();
@@ -935,7 +945,7 @@ gb_status gb_create_joints(gb_world* g, int w, int n, const int* type, const int
     if (s != GB_OK) return s;
     if (n > 0 && (!type || !a || !b || !f || !flags)) return GB_ERR_INVALID;
     for (int i = 0; i < n; ++i)
-        if ((s = CreateJoint(g->worlds[w], type[i], a[i], b[i], f + 9 * i, flags[i], out_ids ? out_ids + i : nullptr)) != GB_OK)
+        if ((s = CreateJoint(g->worlds[w], type[i], a[i], b[i], f + GB_JOINT_FLOATS * i, flags[i], out_ids ? out_ids + i : nullptr)) != GB_OK)
             return s;
     return GB_OK;
 }
@@ -962,7 +972,7 @@ gb_status gb_build_world(gb_world* g, int w, int nb, const int* body_type, const
     if (fi != nf) return GB_ERR_INVALID;
     for (int j = 0; j < nj; ++j)
         if ((s = CreateJoint(W, joint_type ? joint_type[j] : kJointRevolute, base + joint_a[j], base + joint_b[j],
-                             joint_f + 9 * j, joint_flags[j], nullptr)) != GB_OK)
+                             joint_f + GB_JOINT_FLOATS * j, joint_flags[j], nullptr)) != GB_OK)
             return s;
     return GB_OK;
 }

@@ -12,11 +12,12 @@ each followed by its fixtures, then joints. It is stored as numpy arrays so that
   ``b2PolygonShape::Set``); 3 box {hx, hy} or {hx, hy, cx, cy, angle}), ``fix_shape`` float32[M, 16],
   ``fix_n`` int32[M], ``fix_mat`` float32[M, 3] = (density, friction, restitution), ``fix_filt``
   int32[M, 4] = (categoryBits, maskBits, groupIndex, isSensor).
-* ``joint_type`` int32[J] (0 revolute, 1 distance, 2 weld), ``joint_a``/``joint_b`` int32[J],
-  ``joint_f`` float32[J, 9] = revolute (localAnchorA, localAnchorB, referenceAngle, lowerAngle,
-  upperAngle, motorSpeed, maxMotorTorque), distance (localAnchorA, localAnchorB, length,
+* ``joint_type`` int32[J] (0 revolute, 1 distance, 2 weld, 3 prismatic), ``joint_a``/``joint_b``
+  int32[J], ``joint_f`` float32[J, 12] = revolute (localAnchorA, localAnchorB, referenceAngle,
+  lowerAngle, upperAngle, motorSpeed, maxMotorTorque), distance (localAnchorA, localAnchorB, length,
   frequencyHz, dampingRatio), weld (localAnchorA, localAnchorB, referenceAngle, frequencyHz,
-  dampingRatio); ``joint_flags`` int32[J] (1 limit, 2 motor, 4 collideConnected).
+  dampingRatio), prismatic (localAnchorA, localAnchorB, localAxisA, referenceAngle,
+  lowerTranslation, upperTranslation, maxMotorForce, motorSpeed), zero-padded; ``joint_flags`` int32[J] (1 limit, 2 motor, 4 collideConnected).
 
 Random numbers come from splitmix64 on Python integers, so a seed gives the same scene on every
 machine. No public benchmark scene set exists for Box2D; these follow the workload descriptions:
@@ -34,7 +35,7 @@ import numpy as np
 STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 # shape encodings of the bulk build call
 CIRCLE, EDGE, POLYGON, BOX = 0, 1, 2, 3
-REVOLUTE, DISTANCE, WELD = 0, 1, 2
+REVOLUTE, DISTANCE, WELD, PRISMATIC = 0, 1, 2, 3
 DEFAULT_FLAGS = 1 | 2 | 16  # allowSleep, awake, active
 
 
@@ -93,17 +94,25 @@ class Scene:
     def revolute(self, a, b, anchor_a, anchor_b, ref_angle=0.0, lower=0.0, upper=0.0, motor_speed=0.0,
                  max_motor_torque=0.0, flags=0) -> int:
         self.joints.append((a, b, [anchor_a[0], anchor_a[1], anchor_b[0], anchor_b[1], ref_angle, lower,
-                                   upper, motor_speed, max_motor_torque], flags, REVOLUTE))
+                                   upper, motor_speed, max_motor_torque, 0.0, 0.0, 0.0], flags, REVOLUTE))
         return len(self.joints) - 1
 
     def distance(self, a, b, anchor_a, anchor_b, length, frequency_hz=0.0, damping_ratio=0.0, flags=0) -> int:
         self.joints.append((a, b, [anchor_a[0], anchor_a[1], anchor_b[0], anchor_b[1], length, frequency_hz,
-                                   damping_ratio, 0.0, 0.0], flags, DISTANCE))
+                                   damping_ratio, 0.0, 0.0, 0.0, 0.0, 0.0], flags, DISTANCE))
         return len(self.joints) - 1
 
     def weld(self, a, b, anchor_a, anchor_b, ref_angle=0.0, frequency_hz=0.0, damping_ratio=0.0, flags=0) -> int:
         self.joints.append((a, b, [anchor_a[0], anchor_a[1], anchor_b[0], anchor_b[1], ref_angle, frequency_hz,
-                                   damping_ratio, 0.0, 0.0], flags, WELD))
+                                   damping_ratio, 0.0, 0.0, 0.0, 0.0, 0.0], flags, WELD))
+        return len(self.joints) - 1
+
+    def prismatic(self, a, b, anchor_a, anchor_b, axis, ref_angle=0.0, lower=0.0, upper=0.0, max_motor_force=0.0,
+                  motor_speed=0.0, flags=0) -> int:
+        """b2PrismaticJointDef: body B slides along axis (in body A's frame); flags 1 limit, 2 motor,
+        4 collideConnected."""
+        self.joints.append((a, b, [anchor_a[0], anchor_a[1], anchor_b[0], anchor_b[1], axis[0], axis[1], ref_angle,
+                                   lower, upper, max_motor_force, motor_speed, 0.0], flags, PRISMATIC))
         return len(self.joints) - 1
 
     @property
@@ -126,7 +135,7 @@ class Scene:
             "joint_type": np.array([j[4] for j in self.joints], dtype=np.int32).reshape(nj),
             "joint_a": np.array([j[0] for j in self.joints], dtype=np.int32).reshape(nj),
             "joint_b": np.array([j[1] for j in self.joints], dtype=np.int32).reshape(nj),
-            "joint_f": np.array([j[2] for j in self.joints], dtype=np.float32).reshape(nj, 9),
+            "joint_f": np.array([j[2] for j in self.joints], dtype=np.float32).reshape(nj, 12),
             "joint_flags": np.array([j[3] for j in self.joints], dtype=np.int32).reshape(nj),
         }
         for i, f in enumerate(self.fixtures):
@@ -305,6 +314,48 @@ def joint_mix(rng: SplitMix64, allow_sleep: bool = True) -> Scene:
     s.revolute(g, arm, (-20.0, 6.0), (0.0, 0.0), 0.0, -0.4, 0.4, flags=1)
     box = s.body(DYNAMIC, -18.0, 10.0, angle=0.3)
     s.fixture(box, BOX, [0.6, 0.6], 2, density=3.0)
+    return _settings(s, allow_sleep)
+
+
+def prismatic_mix(rng: SplitMix64, allow_sleep: bool = True) -> Scene:
+    """Prismatic joints: sliders on the ground with motors against limits, a locked slider, an
+    elevator lifting a platform of boxes, a slider on an unnormalised oblique axis, a piston between
+    two dynamic bodies on a hinge, and boxes falling onto them."""
+    s = Scene(name="prismatic_mix")
+    g = s.body(STATIC, 0.0, 0.0)
+    s.fixture(g, EDGE, [-40.0, 0.0, 40.0, 0.0, 0, 0, 0, 0, 0, 0], friction=0.6)
+    # ground sliders: limits [-3, 3], motors pushing toward a limit, one without a motor, one locked
+    for k, (speed, force, flags) in enumerate([(2.0, 60.0, 3), (-1.5, 30.0, 3), (0.0, 0.0, 1), (1.0, 40.0, 3)]):
+        x = -24.0 + 5.0 * k
+        b = s.body(DYNAMIC, x, 0.6 + 0.01 * k)
+        s.fixture(b, BOX, [0.8, 0.5], 2, density=2.0, friction=0.2)
+        lower, upper = (-3.0, 3.0) if k != 3 else (0.0, 0.0)
+        s.prismatic(g, b, (x, 0.6), (0.0, 0.0), (1.0, 0.0), 0.0, lower, upper, force, speed, flags)
+    # elevator: a platform driven up a vertical axis, boxes resting on it
+    plat = s.body(DYNAMIC, 0.0, 2.0)
+    s.fixture(plat, BOX, [2.5, 0.2], 2, density=3.0, friction=0.8)
+    s.prismatic(g, plat, (0.0, 2.0), (0.0, 0.0), (0.0, 1.0), 0.0, -1.0, 6.0, 400.0, 1.2, 3)
+    for i in range(3):
+        b = s.body(DYNAMIC, _q(-1.5 + 1.5 * i + rng.uniform(-0.2, 0.2)), 2.75)
+        s.fixture(b, BOX, [0.5, 0.5], 2, density=1.0, friction=0.6)
+    # oblique slider: axis (2, 1) given unnormalised, no limit, gravity pulls it down the axis
+    ob = s.body(DYNAMIC, 12.0, 8.0, angle=0.3)
+    s.fixture(ob, BOX, [0.6, 0.3], 2, density=1.5)
+    s.prismatic(g, ob, (12.0, 8.0), (0.0, 0.0), (2.0, 1.0), 0.3, 0.0, 0.0, 0.0, 0.0, 0)
+    # piston: a cylinder hinged to the ground, a rod sliding in it (collide connected), a load on top
+    cyl = s.body(DYNAMIC, 20.0, 3.0)
+    s.fixture(cyl, BOX, [0.3, 1.5], 2, density=1.0, group=-3)
+    s.revolute(g, cyl, (20.0, 1.5), (0.0, -1.5), 0.0, -0.3, 0.3, flags=1)
+    rod = s.body(DYNAMIC, 20.0, 5.0)
+    s.fixture(rod, BOX, [0.15, 1.2], 2, density=1.0, group=-3)
+    s.prismatic(cyl, rod, (0.0, 1.0), (0.0, -1.0), (0.0, 1.0), 0.0, -0.5, 1.5, 80.0, 2.0, 3)
+    load = s.body(DYNAMIC, _q(20.0 + rng.uniform(-0.3, 0.3)), 8.5)
+    s.fixture(load, BOX, [0.7, 0.4], 2, density=2.0)
+    # boxes falling on the sliders
+    for i in range(6):
+        b = s.body(DYNAMIC, _q(-25.0 + 3.5 * i + rng.uniform(-0.5, 0.5)), _q(4.0 + 1.2 * i), angle=_q(rng.uniform(-0.4, 0.4)))
+        s.fixture(b, CIRCLE if i % 2 else BOX, [0.0, 0.0, 0.4] if i % 2 else [0.4, 0.4], 1 if i % 2 else 2,
+                  density=1.0, friction=0.5)
     return _settings(s, allow_sleep)
 
 

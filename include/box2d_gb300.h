@@ -70,21 +70,26 @@ gb_status gb_create_fixtures(gb_world* world, int w, int n, const int* body, con
 gb_status gb_create_revolute_joints(gb_world* world, int w, int n, const int* body_a, const int* body_b,
                                     const float* f, const int* flags, int* out_ids);
 
-/* b2World::CreateJoint for revolute, distance and weld joint definitions (Box2D/Dynamics/b2World.cpp:185,
- * Box2D/Dynamics/Joints/b2RevoluteJoint.h:36, b2DistanceJoint.h:30, b2WeldJoint.h:28). type: 0
- * revolute, 1 distance, 2 weld. f[9]: revolute as gb_create_revolute_joints; distance localAnchorA.x,
- * .y, localAnchorB.x, .y, length, frequencyHz, dampingRatio; weld localAnchorA.x, .y, localAnchorB.x,
- * .y, referenceAngle, frequencyHz, dampingRatio. flags: 1 enableLimit, 2 enableMotor (revolute),
- * 4 collideConnected. */
+/* b2World::CreateJoint for revolute, distance, weld and prismatic joint definitions
+ * (Box2D/Dynamics/b2World.cpp:185, Box2D/Dynamics/Joints/b2RevoluteJoint.h:36, b2DistanceJoint.h:30,
+ * b2WeldJoint.h:28, b2PrismaticJoint.h:30). type: GB_JOINT_*. f[GB_JOINT_FLOATS] per joint: revolute
+ * as gb_create_revolute_joints (f[0..8]); distance localAnchorA.x, .y, localAnchorB.x, .y, length,
+ * frequencyHz, dampingRatio; weld localAnchorA.x, .y, localAnchorB.x, .y, referenceAngle,
+ * frequencyHz, dampingRatio; prismatic localAnchorA.x, .y, localAnchorB.x, .y, localAxisA.x, .y
+ * (normalised as the reference's constructor does), referenceAngle, lowerTranslation,
+ * upperTranslation, maxMotorForce, motorSpeed. Unused trailing floats are ignored. flags: 1
+ * enableLimit, 2 enableMotor (revolute, prismatic), 4 collideConnected. */
 #define GB_JOINT_REVOLUTE 0
 #define GB_JOINT_DISTANCE 1
 #define GB_JOINT_WELD 2
+#define GB_JOINT_PRISMATIC 3
+#define GB_JOINT_FLOATS 12
 gb_status gb_create_joints(gb_world* world, int w, int n, const int* type, const int* body_a, const int* body_b,
                            const float* f, const int* flags, int* out_ids);
 
 /* Bulk scene build into world w: body b is created, then every fixture whose fix_body == b (the array
- * is sorted by body), then all joints (joint_type NULL: all revolute). Equivalent to the calls above
- * interleaved. */
+ * is sorted by body), then all joints (joint_type NULL: all revolute), GB_JOINT_FLOATS floats each as
+ * gb_create_joints. Equivalent to the calls above interleaved. */
 gb_status gb_build_world(gb_world* world, int w, int nb, const int* body_type, const float* body_f,
                          const int* body_flags, int nf, const int* fix_body, const int* fix_type,
                          const float* fix_shape, const int* fix_n, const float* fix_mat, const int* fix_filt,

@@ -260,6 +260,20 @@ struct b2WeldJointDef {
     float frequencyHz = 0.0f, dampingRatio = 0.0f;
 };
 
+// b2PrismaticJointDef (Box2D/Dynamics/Joints/b2PrismaticJoint.h:30-88)
+struct b2PrismaticJointDef {
+    b2Body* bodyA = nullptr;
+    b2Body* bodyB = nullptr;
+    bool collideConnected = false;
+    b2Vec2 localAnchorA, localAnchorB;
+    b2Vec2 localAxisA{1.0f, 0.0f};
+    float referenceAngle = 0.0f;
+    bool enableLimit = false;
+    float lowerTranslation = 0.0f, upperTranslation = 0.0f;
+    bool enableMotor = false;
+    float maxMotorForce = 0.0f, motorSpeed = 0.0f;
+};
+
 class b2Joint {
 public:
     int GetIndex() const { return m_index; }
@@ -373,15 +387,25 @@ public:
 
     b2Joint* CreateJoint(const b2DistanceJointDef* def)
     {
-        const float f[9] = {def->localAnchorA.x, def->localAnchorA.y, def->localAnchorB.x, def->localAnchorB.y,
-                            def->length, def->frequencyHz, def->dampingRatio, 0.0f, 0.0f};
+        const float f[GB_JOINT_FLOATS] = {def->localAnchorA.x, def->localAnchorA.y, def->localAnchorB.x,
+                                          def->localAnchorB.y, def->length, def->frequencyHz, def->dampingRatio};
         return AddJoint(GB_JOINT_DISTANCE, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
     }
     b2Joint* CreateJoint(const b2WeldJointDef* def)
     {
-        const float f[9] = {def->localAnchorA.x, def->localAnchorA.y, def->localAnchorB.x, def->localAnchorB.y,
-                            def->referenceAngle, def->frequencyHz, def->dampingRatio, 0.0f, 0.0f};
+        const float f[GB_JOINT_FLOATS] = {def->localAnchorA.x, def->localAnchorA.y, def->localAnchorB.x,
+                                          def->localAnchorB.y, def->referenceAngle, def->frequencyHz,
+                                          def->dampingRatio};
         return AddJoint(GB_JOINT_WELD, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
+    }
+    b2Joint* CreateJoint(const b2PrismaticJointDef* def)
+    {
+        const float f[GB_JOINT_FLOATS] = {def->localAnchorA.x, def->localAnchorA.y, def->localAnchorB.x,
+                                          def->localAnchorB.y, def->localAxisA.x, def->localAxisA.y,
+                                          def->referenceAngle, def->lowerTranslation, def->upperTranslation,
+                                          def->maxMotorForce, def->motorSpeed};
+        const int flags = (def->enableLimit ? 1 : 0) | (def->enableMotor ? 2 : 0) | (def->collideConnected ? 4 : 0);
+        return AddJoint(GB_JOINT_PRISMATIC, def->bodyA, def->bodyB, f, flags);
     }
 
     void Step(float timeStep, int velocityIterations, int positionIterations)

@@ -76,7 +76,7 @@ void po_build(void* h, int nb, const int* btype, const float* bf, const int* bfl
             ++fi;
         }
     }
-    for (int j = 0; j < nj; ++j) po_revolute(h, ja[j], jb[j], jf + 9 * j, jflags[j]);
+    for (int j = 0; j < nj; ++j) po_revolute(h, ja[j], jb[j], jf + 12 * j, jflags[j]);
 }
 
 void po_step(void* h, float dt, int vi, int pi) { static_cast<World*>(h)->Step(dt, vi, pi); }

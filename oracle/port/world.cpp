@@ -146,10 +146,24 @@ int World::CreateJoint(int type, int a, int b, const float* f, int fl)
     j.bodyA = a; j.bodyB = b;
     j.localAnchorA = V(f[0], f[1]);
     j.localAnchorB = V(f[2], f[3]);
-    if (type == kDistanceJoint) j.length = f[4];
-    else j.referenceAngle = f[4];
-    j.frequencyHz = f[5];
-    j.dampingRatio = f[6];
+    if (type == kPrismaticJoint) {
+        // b2PrismaticJoint::b2PrismaticJoint (b2PrismaticJoint.cpp:102-126)
+        j.localXAxisA = V(f[4], f[5]);
+        Normalize(j.localXAxisA);
+        j.localYAxisA = Cross(1.0f, j.localXAxisA);
+        j.referenceAngle = f[6];
+        j.lowerAngle = f[7];
+        j.upperAngle = f[8];
+        j.maxMotorTorque = f[9];
+        j.motorSpeed = f[10];
+        j.enableLimit = (fl & 1) != 0;
+        j.enableMotor = (fl & 2) != 0;
+    } else {
+        if (type == kDistanceJoint) j.length = f[4];
+        else j.referenceAngle = f[4];
+        j.frequencyHz = f[5];
+        j.dampingRatio = f[6];
+    }
     j.collideConnected = (fl & 4) != 0;
     return LinkJoint(j, a, b);
 }
@@ -985,6 +999,9 @@ bool DistSolvePosition(Joint& j, Position* pos);
 void WeldInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel);
 void WeldSolveVelocity(Joint& j, Velocity* vel);
 bool WeldSolvePosition(Joint& j, Position* pos);
+void PrisInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel);
+void PrisSolveVelocity(Joint& j, const StepInfo& step, Velocity* vel);
+bool PrisSolvePosition(Joint& j, Position* pos);
 
 // b2Mat33::Solve33 / Solve22 (Common/b2Math.cpp:24-56)
 inline void Solve33(const float* M, const float* b, float* x)
@@ -1416,6 +1433,207 @@ bool WeldSolvePosition(Joint& j, Position* pos)
     return positionError <= kLinearSlop && angularError <= kAngularSlop;
 }
 
+
+// ---------------------------------------------------------------- prismatic joint
+// b2PrismaticJoint::InitVelocityConstraints (Dynamics/Joints/b2PrismaticJoint.cpp:128-266)
+void PrisInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel)
+{
+    const Body& A = w->bodies[j.bodyA];
+    const Body& B = w->bodies[j.bodyB];
+    j.indexA = A.islandIndex; j.indexB = B.islandIndex;
+    j.localCenterA = A.sweep.localCenter; j.localCenterB = B.sweep.localCenter;
+    j.invMassA = A.invMass; j.invMassB = B.invMass;
+    j.invIA = A.invI; j.invIB = B.invI;
+    const Vec2 cA = pos[j.indexA].c, cB = pos[j.indexB].c;
+    const float aA = pos[j.indexA].a, aB = pos[j.indexB].a;
+    Vec2 vA = vel[j.indexA].v, vB = vel[j.indexB].v;
+    float wA = vel[j.indexA].w, wB = vel[j.indexB].w;
+    const Rot qA = RotOf(aA), qB = RotOf(aB);
+    const Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    const Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    const Vec2 d = (cB - cA) + rB - rA;
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    j.u = Mul(qA, j.localXAxisA);
+    j.a1 = Cross(d + rA, j.u);
+    j.a2 = Cross(rB, j.u);
+    j.motorMass = mA + mB + iA * j.a1 * j.a1 + iB * j.a2 * j.a2;
+    if (j.motorMass > 0.0f) j.motorMass = 1.0f / j.motorMass;
+    j.perp = Mul(qA, j.localYAxisA);
+    j.s1 = Cross(d + rA, j.perp);
+    j.s2 = Cross(rB, j.perp);
+    float* K = j.mass;
+    K[0] = mA + mB + iA * j.s1 * j.s1 + iB * j.s2 * j.s2;
+    K[1] = iA * j.s1 + iB * j.s2;
+    K[2] = iA * j.s1 * j.a1 + iB * j.s2 * j.a2;
+    float k22 = iA + iB;
+    if (k22 == 0.0f) k22 = 1.0f;
+    K[4] = k22;
+    K[5] = iA * j.a1 + iB * j.a2;
+    K[8] = mA + mB + iA * j.a1 * j.a1 + iB * j.a2 * j.a2;
+    K[3] = K[1]; K[6] = K[2]; K[7] = K[5];
+    if (j.enableLimit) {
+        const float translation = Dot(j.u, d);
+        if (Abs(j.upperAngle - j.lowerAngle) < 2.0f * kLinearSlop) {
+            j.limitState = 3;
+        } else if (translation <= j.lowerAngle) {
+            if (j.limitState != 1) { j.limitState = 1; j.impulse[2] = 0.0f; }
+        } else if (translation >= j.upperAngle) {
+            if (j.limitState != 2) { j.limitState = 2; j.impulse[2] = 0.0f; }
+        } else {
+            j.limitState = 0;
+            j.impulse[2] = 0.0f;
+        }
+    } else {
+        j.limitState = 0;
+        j.impulse[2] = 0.0f;
+    }
+    if (!j.enableMotor) j.motorImpulse = 0.0f;
+    if (step.warmStarting) {
+        j.impulse[0] *= step.dtRatio; j.impulse[1] *= step.dtRatio; j.impulse[2] *= step.dtRatio;
+        j.motorImpulse *= step.dtRatio;
+        const Vec2 P = j.impulse[0] * j.perp + (j.motorImpulse + j.impulse[2]) * j.u;
+        const float LA = j.impulse[0] * j.s1 + j.impulse[1] + (j.motorImpulse + j.impulse[2]) * j.a1;
+        const float LB = j.impulse[0] * j.s2 + j.impulse[1] + (j.motorImpulse + j.impulse[2]) * j.a2;
+        vA = vA - mA * P;
+        wA -= iA * LA;
+        vB = vB + mB * P;
+        wB += iB * LB;
+    } else {
+        j.impulse[0] = j.impulse[1] = j.impulse[2] = 0.0f;
+        j.motorImpulse = 0.0f;
+    }
+    vel[j.indexA].v = vA; vel[j.indexA].w = wA;
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+}
+
+// b2PrismaticJoint::SolveVelocityConstraints (b2PrismaticJoint.cpp:268-363)
+void PrisSolveVelocity(Joint& j, const StepInfo& step, Velocity* vel)
+{
+    Vec2 vA = vel[j.indexA].v, vB = vel[j.indexB].v;
+    float wA = vel[j.indexA].w, wB = vel[j.indexB].w;
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    if (j.enableMotor && j.limitState != 3) {
+        const float Cdot = Dot(j.u, vB - vA) + j.a2 * wB - j.a1 * wA;
+        float impulse = j.motorMass * (j.motorSpeed - Cdot);
+        const float oldImpulse = j.motorImpulse;
+        const float maxImpulse = step.dt * j.maxMotorTorque;
+        j.motorImpulse = Clamp(j.motorImpulse + impulse, -maxImpulse, maxImpulse);
+        impulse = j.motorImpulse - oldImpulse;
+        const Vec2 P = impulse * j.u;
+        const float LA = impulse * j.a1, LB = impulse * j.a2;
+        vA = vA - mA * P;
+        wA -= iA * LA;
+        vB = vB + mB * P;
+        wB += iB * LB;
+    }
+    Vec2 Cdot1;
+    Cdot1.x = Dot(j.perp, vB - vA) + j.s2 * wB - j.s1 * wA;
+    Cdot1.y = wB - wA;
+    if (j.enableLimit && j.limitState != 0) {
+        const float Cdot2 = Dot(j.u, vB - vA) + j.a2 * wB - j.a1 * wA;
+        const float negCdot[3] = {-Cdot1.x, -Cdot1.y, -Cdot2};
+        const float f1[3] = {j.impulse[0], j.impulse[1], j.impulse[2]};
+        float df[3];
+        Solve33(j.mass, negCdot, df);
+        j.impulse[0] += df[0]; j.impulse[1] += df[1]; j.impulse[2] += df[2];
+        if (j.limitState == 1) j.impulse[2] = Max(j.impulse[2], 0.0f);
+        else if (j.limitState == 2) j.impulse[2] = Min(j.impulse[2], 0.0f);
+        const Vec2 b = -Cdot1 - (j.impulse[2] - f1[2]) * V(j.mass[6], j.mass[7]);
+        const Vec2 f2r = Solve22(j.mass, b) + V(f1[0], f1[1]);
+        j.impulse[0] = f2r.x;
+        j.impulse[1] = f2r.y;
+        df[0] = j.impulse[0] - f1[0]; df[1] = j.impulse[1] - f1[1]; df[2] = j.impulse[2] - f1[2];
+        const Vec2 P = df[0] * j.perp + df[2] * j.u;
+        const float LA = df[0] * j.s1 + df[1] + df[2] * j.a1;
+        const float LB = df[0] * j.s2 + df[1] + df[2] * j.a2;
+        vA = vA - mA * P;
+        wA -= iA * LA;
+        vB = vB + mB * P;
+        wB += iB * LB;
+    } else {
+        const Vec2 df = Solve22(j.mass, -Cdot1);
+        j.impulse[0] += df.x;
+        j.impulse[1] += df.y;
+        const Vec2 P = df.x * j.perp;
+        const float LA = df.x * j.s1 + df.y;
+        const float LB = df.x * j.s2 + df.y;
+        vA = vA - mA * P;
+        wA -= iA * LA;
+        vB = vB + mB * P;
+        wB += iB * LB;
+    }
+    vel[j.indexA].v = vA; vel[j.indexA].w = wA;
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+}
+
+// b2PrismaticJoint::SolvePositionConstraints (b2PrismaticJoint.cpp:365-487)
+bool PrisSolvePosition(Joint& j, Position* pos)
+{
+    Vec2 cA = pos[j.indexA].c, cB = pos[j.indexB].c;
+    float aA = pos[j.indexA].a, aB = pos[j.indexB].a;
+    const Rot qA = RotOf(aA), qB = RotOf(aB);
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    const Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    const Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    const Vec2 d = cB + rB - cA - rA;
+    const Vec2 axis = Mul(qA, j.localXAxisA);
+    const float a1 = Cross(d + rA, axis), a2 = Cross(rB, axis);
+    const Vec2 perp = Mul(qA, j.localYAxisA);
+    const float s1 = Cross(d + rA, perp), s2 = Cross(rB, perp);
+    Vec2 C1;
+    C1.x = Dot(perp, d);
+    C1.y = aB - aA - j.referenceAngle;
+    float linearError = Abs(C1.x);
+    const float angularError = Abs(C1.y);
+    bool active = false;
+    float C2 = 0.0f;
+    if (j.enableLimit) {
+        const float translation = Dot(axis, d);
+        if (Abs(j.upperAngle - j.lowerAngle) < 2.0f * kLinearSlop) {
+            C2 = Clamp(translation, -kMaxLinearCorrection, kMaxLinearCorrection);
+            linearError = Max(linearError, Abs(translation));
+            active = true;
+        } else if (translation <= j.lowerAngle) {
+            C2 = Clamp(translation - j.lowerAngle + kLinearSlop, -kMaxLinearCorrection, 0.0f);
+            linearError = Max(linearError, j.lowerAngle - translation);
+            active = true;
+        } else if (translation >= j.upperAngle) {
+            C2 = Clamp(translation - j.upperAngle - kLinearSlop, 0.0f, kMaxLinearCorrection);
+            linearError = Max(linearError, translation - j.upperAngle);
+            active = true;
+        }
+    }
+    float imp[3];
+    float K[9];
+    K[0] = mA + mB + iA * s1 * s1 + iB * s2 * s2;
+    K[1] = iA * s1 + iB * s2;
+    float k22 = iA + iB;
+    if (k22 == 0.0f) k22 = 1.0f;
+    K[4] = k22;
+    K[3] = K[1];
+    if (active) {
+        K[2] = iA * s1 * a1 + iB * s2 * a2;
+        K[5] = iA * a1 + iB * a2;
+        K[8] = mA + mB + iA * a1 * a1 + iB * a2 * a2;
+        K[6] = K[2]; K[7] = K[5];
+        const float negC[3] = {-C1.x, -C1.y, -C2};
+        Solve33(K, negC, imp);
+    } else {
+        const Vec2 i2 = Solve22(K, -C1);
+        imp[0] = i2.x; imp[1] = i2.y; imp[2] = 0.0f;
+    }
+    const Vec2 P = imp[0] * perp + imp[2] * axis;
+    const float LA = imp[0] * s1 + imp[1] + imp[2] * a1;
+    const float LB = imp[0] * s2 + imp[1] + imp[2] * a2;
+    cA = cA - mA * P;
+    aA -= iA * LA;
+    cB = cB + mB * P;
+    aB += iB * LB;
+    pos[j.indexA].c = cA; pos[j.indexA].a = aA;
+    pos[j.indexB].c = cB; pos[j.indexB].a = aB;
+    return linearError <= kLinearSlop && angularError <= kAngularSlop;
+}
+
 } // namespace
 
 // ---------------------------------------------------------------- island solve
@@ -1450,6 +1668,7 @@ void World::IslandSolve(const StepInfo& step)
         Joint& j = joints[jn];
         if (j.type == kDistanceJoint) DistInit(this, j, step, positions.data(), velocities.data());
         else if (j.type == kWeldJoint) WeldInit(this, j, step, positions.data(), velocities.data());
+        else if (j.type == kPrismaticJoint) PrisInit(this, j, step, positions.data(), velocities.data());
         else RevInit(this, j, step, positions.data(), velocities.data());
     }
     for (int i = 0; i < step.velocityIterations; ++i) {
@@ -1457,6 +1676,7 @@ void World::IslandSolve(const StepInfo& step)
             Joint& j = joints[jn];
             if (j.type == kDistanceJoint) DistSolveVelocity(j, velocities.data());
             else if (j.type == kWeldJoint) WeldSolveVelocity(j, velocities.data());
+            else if (j.type == kPrismaticJoint) PrisSolveVelocity(j, step, velocities.data());
             else RevSolveVelocity(j, step, velocities.data());
         }
         cs.SolveVelocity();
@@ -1491,6 +1711,7 @@ void World::IslandSolve(const StepInfo& step)
             Joint& j = joints[jn];
             bool ok = j.type == kDistanceJoint ? DistSolvePosition(j, positions.data())
                       : j.type == kWeldJoint   ? WeldSolvePosition(j, positions.data())
+                      : j.type == kPrismaticJoint ? PrisSolvePosition(j, positions.data())
                                                : RevSolvePosition(j, positions.data());
             jointsOkay = jointsOkay && ok;
         }

@@ -55,7 +55,7 @@ struct Contact {
 };
 
 // joint types (b2JointType, Dynamics/Joints/b2Joint.h:28-42, those restated here)
-enum JointType { kRevoluteJoint = 0, kDistanceJoint = 1, kWeldJoint = 2 };
+enum JointType { kRevoluteJoint = 0, kDistanceJoint = 1, kWeldJoint = 2, kPrismaticJoint = 3 };
 
 struct Joint {
     int type = kRevoluteJoint;
@@ -79,7 +79,11 @@ struct Joint {
     // weld's reference angle is referenceAngle, its impulse impulse[0..2], its mass mass[])
     float length = 0, frequencyHz = 0, dampingRatio = 0;
     float gamma = 0, bias = 0;
-    Vec2 u{0, 0};            // distance: unit axis of the step (its effective mass in motorMass)
+    Vec2 u{0, 0};            // distance: unit axis of the step (its effective mass in motorMass); prismatic: axis
+    // prismatic joint (b2PrismaticJoint.h): translation limits in lowerAngle/upperAngle, maximum motor
+    // force in maxMotorTorque, the 3x3 K in mass[]
+    Vec2 localXAxisA{0, 0}, localYAxisA{0, 0}, perp{0, 0};
+    float s1 = 0, s2 = 0, a1 = 0, a2 = 0;
 };
 
 struct Position { Vec2 c; float a; };

@@ -171,7 +171,7 @@ int rw_joint(void* h, int type, int bodyA, int bodyB, const float* f, int flags)
         jd.dampingRatio = f[6];
         jd.collideConnected = (flags & 4) != 0;
         w->joints.push_back(w->world.CreateJoint(&jd));
-    } else {
+    } else if (type == 2) {
         b2WeldJointDef jd;
         jd.bodyA = w->bodies[bodyA];
         jd.bodyB = w->bodies[bodyB];
@@ -180,6 +180,22 @@ int rw_joint(void* h, int type, int bodyA, int bodyB, const float* f, int flags)
         jd.referenceAngle = f[4];
         jd.frequencyHz = f[5];
         jd.dampingRatio = f[6];
+        jd.collideConnected = (flags & 4) != 0;
+        w->joints.push_back(w->world.CreateJoint(&jd));
+    } else {
+        b2PrismaticJointDef jd;
+        jd.bodyA = w->bodies[bodyA];
+        jd.bodyB = w->bodies[bodyB];
+        jd.localAnchorA.Set(f[0], f[1]);
+        jd.localAnchorB.Set(f[2], f[3]);
+        jd.localAxisA.Set(f[4], f[5]);
+        jd.referenceAngle = f[6];
+        jd.lowerTranslation = f[7];
+        jd.upperTranslation = f[8];
+        jd.maxMotorForce = f[9];
+        jd.motorSpeed = f[10];
+        jd.enableLimit = (flags & 1) != 0;
+        jd.enableMotor = (flags & 2) != 0;
         jd.collideConnected = (flags & 4) != 0;
         w->joints.push_back(w->world.CreateJoint(&jd));
     }
@@ -199,7 +215,7 @@ void rw_build(void* h, int nb, const int* btype, const float* bf, const int* bfl
             ++fi;
         }
     }
-    for (int j = 0; j < nj; ++j) rw_revolute(h, ja[j], jb[j], jf + 9 * j, jflags[j]);
+    for (int j = 0; j < nj; ++j) rw_revolute(h, ja[j], jb[j], jf + 12 * j, jflags[j]);
 }
 
 void rw_step(void* h, float dt, int vi, int pi) { static_cast<RefWorld*>(h)->world.Step(dt, vi, pi); }

@@ -61,6 +61,7 @@ def cases():
         ("stacks120", lambda: scenes.stacks(120, scenes.SplitMix64(5)), 300, [1, 150, 300]),
         ("chains6x16", lambda: chains_with_load(), 300, [1, 100, 300]),
         ("joint_mix", lambda: scenes.joint_mix(scenes.SplitMix64(3)), 300, [1, 60, 150, 300]),
+        ("prismatic_mix", lambda: scenes.prismatic_mix(scenes.SplitMix64(5)), 300, [1, 60, 150, 300]),
     ] + [(f"batch{i}", (lambda i=i: batch_world(i)), 200, [200]) for i in range(24)]
 
 
@@ -231,12 +232,17 @@ def main():
         make_queries()
         print("done")
         return
+    only = sys.argv[sys.argv.index("--case") + 1] if "--case" in sys.argv else None
     for name, make, steps, cps in cases():
+        if only and name != only:
+            continue
         for trig in ("libm", "project"):
             digests, snap = run_case(make(), steps, cps, "reference", trig)
             np.savez_compressed(os.path.join(HERE, f"{name}_{trig}.npz"), digests=digests,
                                 checkpoints=np.array(cps, np.int32), steps=np.int32(steps), **snap)
         print("wrote", name)
+    if only:
+        return
     make_collide()
     make_toi()
     make_trig()
