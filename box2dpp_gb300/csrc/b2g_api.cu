@@ -787,8 +787,7 @@ gb_status CreateJoint(HWorld& W, int type, int a, int b, const float* f, int fl,
 {
     int nb = (int)W.bodies.size();
     if (a < 0 || a >= nb || b < 0 || b >= nb || a == b) return GB_ERR_INVALID;
-    if (type != kJointRevolute && type != kJointDistance && type != kJointWeld && type != kJointPrismatic)
-        return GB_ERR_INVALID;
+    if (type < 0 || type >= kJointTypes) return GB_ERR_INVALID;
     Joint j;
     std::memset(&j, 0, sizeof(j));
     j.type = type;
@@ -801,6 +800,22 @@ gb_status CreateJoint(HWorld& W, int type, int a, int b, const float* f, int fl,
         j.length = f[4]; j.frequencyHz = f[5]; j.dampingRatio = f[6];
     } else if (type == kJointWeld) {
         j.referenceAngle = f[4]; j.frequencyHz = f[5]; j.dampingRatio = f[6];
+    } else if (type == kJointWheel) {
+        // b2WheelJoint::b2WheelJoint (Dynamics/Joints/b2WheelJoint.cpp:39-64): the axis as given, its
+        // normal b2Cross(1, axis)
+        j.localXAxisA = V(f[4], f[5]);
+        j.localYAxisA = Cross(1.0f, j.localXAxisA);
+        j.maxMotorTorque = f[6]; j.motorSpeed = f[7]; j.frequencyHz = f[8]; j.dampingRatio = f[9];
+        j.enableMotor = (fl & 2) != 0;
+    } else if (type == kJointRope) {
+        j.maxLength = f[4];  // b2RopeJoint::b2RopeJoint (b2RopeJoint.cpp:35-45)
+    } else if (type == kJointFriction) {
+        j.maxForce = f[4]; j.maxTorque = f[5];  // b2FrictionJoint::b2FrictionJoint (b2FrictionJoint.cpp:35-45)
+    } else if (type == kJointMotor) {
+        // b2MotorJoint::b2MotorJoint (b2MotorJoint.cpp:43-56): no anchors; the offsets in f[0..2]
+        j.localAnchorA = V(0.0f, 0.0f); j.localAnchorB = V(0.0f, 0.0f);
+        j.linearOffset = V(f[0], f[1]); j.angularOffset = f[2];
+        j.maxForce = f[3]; j.maxTorque = f[4]; j.correctionFactor = f[5];
     } else {
         // b2PrismaticJoint::b2PrismaticJoint (Dynamics/Joints/b2PrismaticJoint.cpp:102-126): the unit
         // axis (b2Vec2::Normalize), its normal b2Cross(1, axis); the translation limits and the motor

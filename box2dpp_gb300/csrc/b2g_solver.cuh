@@ -1006,23 +1006,377 @@ __device__ bool PrisSolvePosition(Joint& j, float4* pos)
     return linearError <= kLinearSlop && angularError <= kAngularSlop;
 }
 
+// ------------------------------------------------------------------ wheel joint
+// b2WheelJoint (Dynamics/Joints/b2WheelJoint.cpp:66-302): point-on-line with a spring along the axis
+// and a rotational motor. The axis is taken as given (the reference's constructor does not normalise it).
+__device__ void WheelInit(const Wd& W, Joint& j, float4* pos, float4* vel, bool warmStarting, float dtRatio, float dt)
+{
+    const float4 mA4 = W.mas[j.bodyA], mB4 = W.mas[j.bodyB];
+    j.localCenterA = V(mA4.z, mA4.w); j.localCenterB = V(mB4.z, mB4.w);
+    j.invMassA = mA4.x; j.invMassB = mB4.x; j.invIA = mA4.y; j.invIB = mB4.y;
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    const float4 pa = pos[j.indexA], pb = pos[j.indexB], va = vel[j.indexA], vb = vel[j.indexB];
+    const Vec2 cA = V(pa.x, pa.y), cB = V(pb.x, pb.y);
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const Rot qA = RotOf(pa.z), qB = RotOf(pb.z);
+    const Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    const Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    const Vec2 d = cB + rB - cA - rA;
+    j.ay = Mul(qA, j.localYAxisA);
+    j.sAy = Cross(d + rA, j.ay);
+    j.sBy = Cross(rB, j.ay);
+    // the point-on-line mass (m_mass) is kept in mass[0]
+    j.mass[0] = mA + mB + iA * j.sAy * j.sAy + iB * j.sBy * j.sBy;
+    if (j.mass[0] > 0.0f) j.mass[0] = 1.0f / j.mass[0];
+    j.springMass = 0.0f;
+    j.bias = 0.0f;
+    j.gamma = 0.0f;
+    if (j.frequencyHz > 0.0f) {
+        j.ax = Mul(qA, j.localXAxisA);
+        j.sAx = Cross(d + rA, j.ax);
+        j.sBx = Cross(rB, j.ax);
+        const float invMass = mA + mB + iA * j.sAx * j.sAx + iB * j.sBx * j.sBx;
+        if (invMass > 0.0f) {
+            j.springMass = 1.0f / invMass;
+            const float C = Dot(d, j.ax);
+            const float omega = 2.0f * kPi * j.frequencyHz;
+            const float damp = 2.0f * j.springMass * j.dampingRatio * omega;
+            const float k = j.springMass * omega * omega;
+            const float h = dt;
+            j.gamma = h * (damp + h * k);
+            if (j.gamma > 0.0f) j.gamma = 1.0f / j.gamma;
+            j.bias = C * h * k * j.gamma;
+            j.springMass = invMass + j.gamma;
+            if (j.springMass > 0.0f) j.springMass = 1.0f / j.springMass;
+        }
+    } else {
+        j.springImpulse = 0.0f;
+    }
+    if (j.enableMotor) {
+        j.motorMass = iA + iB;
+        if (j.motorMass > 0.0f) j.motorMass = 1.0f / j.motorMass;
+    } else {
+        j.motorMass = 0.0f;
+        j.motorImpulse = 0.0f;
+    }
+    if (warmStarting) {
+        j.impulse[0] *= dtRatio;
+        j.springImpulse *= dtRatio;
+        j.motorImpulse *= dtRatio;
+        const Vec2 P = j.impulse[0] * j.ay + j.springImpulse * j.ax;
+        const float LA = j.impulse[0] * j.sAy + j.springImpulse * j.sAx + j.motorImpulse;
+        const float LB = j.impulse[0] * j.sBy + j.springImpulse * j.sBx + j.motorImpulse;
+        vA = vA - j.invMassA * P;
+        wA -= j.invIA * LA;
+        vB = vB + j.invMassB * P;
+        wB += j.invIB * LB;
+    } else {
+        j.impulse[0] = 0.0f;
+        j.springImpulse = 0.0f;
+        j.motorImpulse = 0.0f;
+    }
+    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
+__device__ void WheelSolveVelocity(Joint& j, float4* vel, float dt)
+{
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    const float4 va = vel[j.indexA], vb = vel[j.indexB];
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    {   // spring
+        const float Cdot = Dot(j.ax, vB - vA) + j.sBx * wB - j.sAx * wA;
+        const float impulse = -j.springMass * (Cdot + j.bias + j.gamma * j.springImpulse);
+        j.springImpulse += impulse;
+        const Vec2 P = impulse * j.ax;
+        const float LA = impulse * j.sAx, LB = impulse * j.sBx;
+        vA = vA - mA * P;
+        wA -= iA * LA;
+        vB = vB + mB * P;
+        wB += iB * LB;
+    }
+    {   // rotational motor
+        const float Cdot = wB - wA - j.motorSpeed;
+        float impulse = -j.motorMass * Cdot;
+        const float oldImpulse = j.motorImpulse;
+        const float maxImpulse = dt * j.maxMotorTorque;
+        j.motorImpulse = Clampf(j.motorImpulse + impulse, -maxImpulse, maxImpulse);
+        impulse = j.motorImpulse - oldImpulse;
+        wA -= iA * impulse;
+        wB += iB * impulse;
+    }
+    {   // point to line
+        const float Cdot = Dot(j.ay, vB - vA) + j.sBy * wB - j.sAy * wA;
+        const float impulse = -j.mass[0] * Cdot;
+        j.impulse[0] += impulse;
+        const Vec2 P = impulse * j.ay;
+        const float LA = impulse * j.sAy, LB = impulse * j.sBy;
+        vA = vA - mA * P;
+        wA -= iA * LA;
+        vB = vB + mB * P;
+        wB += iB * LB;
+    }
+    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
+__device__ bool WheelSolvePosition(Joint& j, float4* pos)
+{
+    const float4 pa = pos[j.indexA], pb = pos[j.indexB];
+    Vec2 cA = V(pa.x, pa.y), cB = V(pb.x, pb.y);
+    float aA = pa.z, aB = pb.z;
+    const Rot qA = RotOf(aA), qB = RotOf(aB);
+    const Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    const Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    const Vec2 d = (cB - cA) + rB - rA;
+    const Vec2 ay = Mul(qA, j.localYAxisA);
+    const float sAy = Cross(d + rA, ay), sBy = Cross(rB, ay);
+    const float C = Dot(d, ay);
+    // the reference's mass here uses the lever arms of the velocity step (m_sAy, m_sBy)
+    const float k = j.invMassA + j.invMassB + j.invIA * j.sAy * j.sAy + j.invIB * j.sBy * j.sBy;
+    const float impulse = k != 0.0f ? -C / k : 0.0f;
+    const Vec2 P = impulse * ay;
+    const float LA = impulse * sAy, LB = impulse * sBy;
+    cA = cA - j.invMassA * P;
+    aA -= j.invIA * LA;
+    cB = cB + j.invMassB * P;
+    aB += j.invIB * LB;
+    pos[j.indexA] = make_float4(cA.x, cA.y, aA, 0.0f);
+    pos[j.indexB] = make_float4(cB.x, cB.y, aB, 0.0f);
+    return Absf(C) <= kLinearSlop;
+}
+
+// ------------------------------------------------------------------ rope joint
+// b2RopeJoint (Dynamics/Joints/b2RopeJoint.cpp:45-198): a maximum distance between the anchors.
+__device__ void RopeInit(const Wd& W, Joint& j, float4* pos, float4* vel, bool warmStarting, float dtRatio)
+{
+    const float4 mA4 = W.mas[j.bodyA], mB4 = W.mas[j.bodyB];
+    j.localCenterA = V(mA4.z, mA4.w); j.localCenterB = V(mB4.z, mB4.w);
+    j.invMassA = mA4.x; j.invMassB = mB4.x; j.invIA = mA4.y; j.invIB = mB4.y;
+    const float4 pa = pos[j.indexA], pb = pos[j.indexB], va = vel[j.indexA], vb = vel[j.indexB];
+    const Vec2 cA = V(pa.x, pa.y), cB = V(pb.x, pb.y);
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const Rot qA = RotOf(pa.z), qB = RotOf(pb.z);
+    j.rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    j.rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    j.u = cB + j.rB - cA - j.rA;
+    j.ropeLength = Length(j.u);
+    const float C = j.ropeLength - j.maxLength;
+    j.limitState = C > 0.0f ? 2 : 0;
+    if (j.ropeLength > kLinearSlop) {
+        const float inv = 1.0f / j.ropeLength;
+        j.u.x *= inv;
+        j.u.y *= inv;
+    } else {
+        j.u = V(0.0f, 0.0f);
+        j.motorMass = 0.0f;
+        j.impulse[0] = 0.0f;
+        return;
+    }
+    const float crA = Cross(j.rA, j.u), crB = Cross(j.rB, j.u);
+    const float invMass = j.invMassA + j.invIA * crA * crA + j.invMassB + j.invIB * crB * crB;
+    j.motorMass = invMass != 0.0f ? 1.0f / invMass : 0.0f;
+    if (warmStarting) {
+        j.impulse[0] *= dtRatio;
+        const Vec2 P = j.impulse[0] * j.u;
+        vA = vA - j.invMassA * P;
+        wA -= j.invIA * Cross(j.rA, P);
+        vB = vB + j.invMassB * P;
+        wB += j.invIB * Cross(j.rB, P);
+    } else {
+        j.impulse[0] = 0.0f;
+    }
+    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
+__device__ void RopeSolveVelocity(Joint& j, float4* vel, float dt)
+{
+    const float4 va = vel[j.indexA], vb = vel[j.indexB];
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const Vec2 vpA = vA + Cross(wA, j.rA);
+    const Vec2 vpB = vB + Cross(wB, j.rB);
+    const float C = j.ropeLength - j.maxLength;
+    float Cdot = Dot(j.u, vpB - vpA);
+    if (C < 0.0f) Cdot += (1.0f / dt) * C;  // predictive: the step's inv_dt
+    float impulse = -j.motorMass * Cdot;
+    const float oldImpulse = j.impulse[0];
+    j.impulse[0] = Minf(0.0f, j.impulse[0] + impulse);
+    impulse = j.impulse[0] - oldImpulse;
+    const Vec2 P = impulse * j.u;
+    vA = vA - j.invMassA * P;
+    wA -= j.invIA * Cross(j.rA, P);
+    vB = vB + j.invMassB * P;
+    wB += j.invIB * Cross(j.rB, P);
+    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
+__device__ bool RopeSolvePosition(Joint& j, float4* pos)
+{
+    const float4 pa = pos[j.indexA], pb = pos[j.indexB];
+    Vec2 cA = V(pa.x, pa.y), cB = V(pb.x, pb.y);
+    float aA = pa.z, aB = pb.z;
+    const Rot qA = RotOf(aA), qB = RotOf(aB);
+    const Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    const Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    Vec2 u = cB + rB - cA - rA;
+    const float length = Normalize(u);
+    float C = length - j.maxLength;
+    C = Clampf(C, 0.0f, kMaxLinearCorrection);
+    const float impulse = -j.motorMass * C;
+    const Vec2 P = impulse * u;
+    cA = cA - j.invMassA * P;
+    aA -= j.invIA * Cross(rA, P);
+    cB = cB + j.invMassB * P;
+    aB += j.invIB * Cross(rB, P);
+    pos[j.indexA] = make_float4(cA.x, cA.y, aA, 0.0f);
+    pos[j.indexB] = make_float4(cB.x, cB.y, aB, 0.0f);
+    return length - j.maxLength < kLinearSlop;
+}
+
+// ------------------------------------------------------------------ friction and motor joints
+// b2FrictionJoint (Dynamics/Joints/b2FrictionJoint.cpp:45-170): top-down friction, linear and angular
+// impulses bounded by maxForce and maxTorque. b2MotorJoint (b2MotorJoint.cpp:58-200): drives body B
+// to an offset from body A with bounded force and torque. Both have no position constraint.
+// b2Mat22::GetInverse (Common/b2Math.h:245-257) of K (ex.x, ex.y, ey.x, ey.y in K[0..3]) into M.
+__device__ inline void Mat22Inverse(const float* K, float* M)
+{
+    const float a = K[0], b = K[2], c = K[1], d = K[3];
+    float det = a * d - b * c;
+    if (det != 0.0f) det = 1.0f / det;
+    M[0] = det * d; M[2] = -det * b;
+    M[1] = -det * c; M[3] = det * a;
+}
+
+// the 2x2 linear mass and the angular mass of a friction or motor joint at this step's lever arms
+__device__ inline void PointMasses(Joint& j)
+{
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    float K[4];
+    K[0] = mA + mB + iA * j.rA.y * j.rA.y + iB * j.rB.y * j.rB.y;
+    K[1] = -iA * j.rA.x * j.rA.y - iB * j.rB.x * j.rB.y;
+    K[2] = K[1];
+    K[3] = mA + mB + iA * j.rA.x * j.rA.x + iB * j.rB.x * j.rB.x;
+    Mat22Inverse(K, j.mass);
+    j.motorMass = iA + iB;
+    if (j.motorMass > 0.0f) j.motorMass = 1.0f / j.motorMass;
+}
+
+__device__ void FrictionMotorInit(const Wd& W, Joint& j, float4* pos, float4* vel, bool warmStarting, float dtRatio)
+{
+    const float4 mA4 = W.mas[j.bodyA], mB4 = W.mas[j.bodyB];
+    j.localCenterA = V(mA4.z, mA4.w); j.localCenterB = V(mB4.z, mB4.w);
+    j.invMassA = mA4.x; j.invMassB = mB4.x; j.invIA = mA4.y; j.invIB = mB4.y;
+    const float4 pa = pos[j.indexA], pb = pos[j.indexB], va = vel[j.indexA], vb = vel[j.indexB];
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const Rot qA = RotOf(pa.z), qB = RotOf(pb.z);
+    if (j.type == kJointMotor) {
+        j.rA = Mul(qA, -j.localCenterA);
+        j.rB = Mul(qB, -j.localCenterB);
+    } else {
+        j.rA = Mul(qA, j.localAnchorA - j.localCenterA);
+        j.rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    }
+    PointMasses(j);
+    if (j.type == kJointMotor) {
+        const Vec2 cA = V(pa.x, pa.y), cB = V(pb.x, pb.y);
+        j.linearError = cB + j.rB - cA - j.rA - Mul(qA, j.linearOffset);
+        j.angularError = pb.z - pa.z - j.angularOffset;
+    }
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    if (warmStarting) {
+        j.impulse[0] *= dtRatio; j.impulse[1] *= dtRatio;
+        j.impulse[2] *= dtRatio;
+        const Vec2 P = V(j.impulse[0], j.impulse[1]);
+        vA = vA - mA * P;
+        wA -= iA * (Cross(j.rA, P) + j.impulse[2]);
+        vB = vB + mB * P;
+        wB += iB * (Cross(j.rB, P) + j.impulse[2]);
+    } else {
+        j.impulse[0] = j.impulse[1] = 0.0f;
+        j.impulse[2] = 0.0f;
+    }
+    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
+__device__ void FrictionMotorSolveVelocity(Joint& j, float4* vel, float dt)
+{
+    const float4 va = vel[j.indexA], vb = vel[j.indexB];
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    const float h = dt;
+    const bool motor = j.type == kJointMotor;
+    const float invH = 1.0f / dt;
+    {   // angular
+        float Cdot = wB - wA;
+        if (motor) Cdot = Cdot + invH * j.correctionFactor * j.angularError;
+        float impulse = -j.motorMass * Cdot;
+        const float oldImpulse = j.impulse[2];
+        const float maxImpulse = h * j.maxTorque;
+        j.impulse[2] = Clampf(j.impulse[2] + impulse, -maxImpulse, maxImpulse);
+        impulse = j.impulse[2] - oldImpulse;
+        wA -= iA * impulse;
+        wB += iB * impulse;
+    }
+    {   // linear
+        Vec2 Cdot = vB + Cross(wB, j.rB) - vA - Cross(wA, j.rA);
+        if (motor) Cdot = Cdot + (invH * j.correctionFactor) * j.linearError;
+        const float* M = j.mass;
+        Vec2 impulse = -V(M[0] * Cdot.x + M[2] * Cdot.y, M[1] * Cdot.x + M[3] * Cdot.y);
+        const Vec2 oldImpulse = V(j.impulse[0], j.impulse[1]);
+        Vec2 li = oldImpulse + impulse;
+        const float maxImpulse = h * j.maxForce;
+        if (LengthSq(li) > maxImpulse * maxImpulse) {
+            Normalize(li);
+            li.x *= maxImpulse;
+            li.y *= maxImpulse;
+        }
+        j.impulse[0] = li.x;
+        j.impulse[1] = li.y;
+        impulse = li - oldImpulse;
+        vA = vA - mA * impulse;
+        wA -= iA * Cross(j.rA, impulse);
+        vB = vB + mB * impulse;
+        wB += iB * Cross(j.rB, impulse);
+    }
+    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
 // ------------------------------------------------------------------ joint dispatch
 __device__ void JointInit(const Wd& W, Joint& j, float4* pos, float4* vel, bool warmStarting, float dtRatio, float dt)
 {
-    if (j.type == kJointDistance) DistInit(W, j, pos, vel, warmStarting, dtRatio, dt);
+    if (j.type == kJointWheel) WheelInit(W, j, pos, vel, warmStarting, dtRatio, dt);
+    else if (j.type == kJointRope) RopeInit(W, j, pos, vel, warmStarting, dtRatio);
+    else if (j.type == kJointFriction || j.type == kJointMotor) FrictionMotorInit(W, j, pos, vel, warmStarting, dtRatio);
+    else if (j.type == kJointDistance) DistInit(W, j, pos, vel, warmStarting, dtRatio, dt);
     else if (j.type == kJointWeld) WeldInit(W, j, pos, vel, warmStarting, dtRatio, dt);
     else if (j.type == kJointPrismatic) PrisInit(W, j, pos, vel, warmStarting, dtRatio);
     else RevInit(W, j, pos, vel, warmStarting, dtRatio);
 }
 __device__ void JointSolveVelocity(Joint& j, float4* vel, float dt)
 {
-    if (j.type == kJointDistance) DistSolveVelocity(j, vel);
+    if (j.type == kJointWheel) WheelSolveVelocity(j, vel, dt);
+    else if (j.type == kJointRope) RopeSolveVelocity(j, vel, dt);
+    else if (j.type == kJointFriction || j.type == kJointMotor) FrictionMotorSolveVelocity(j, vel, dt);
+    else if (j.type == kJointDistance) DistSolveVelocity(j, vel);
     else if (j.type == kJointWeld) WeldSolveVelocity(j, vel);
     else if (j.type == kJointPrismatic) PrisSolveVelocity(j, vel, dt);
     else RevSolveVelocity(j, vel, dt);
 }
 __device__ bool JointSolvePosition(Joint& j, float4* pos)
 {
+    if (j.type == kJointWheel) return WheelSolvePosition(j, pos);
+    if (j.type == kJointRope) return RopeSolvePosition(j, pos);
+    if (j.type == kJointFriction || j.type == kJointMotor) return true;
     if (j.type == kJointDistance) return DistSolvePosition(j, pos);
     if (j.type == kJointWeld) return WeldSolvePosition(j, pos);
     if (j.type == kJointPrismatic) return PrisSolvePosition(j, pos);

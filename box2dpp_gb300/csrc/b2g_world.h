@@ -81,7 +81,8 @@ struct WorldState {
 };
 
 // Joint types (b2JointType, Dynamics/Joints/b2Joint.h:28-42, those built here).
-enum : int { kJointRevolute = 0, kJointDistance = 1, kJointWeld = 2, kJointPrismatic = 3 };
+enum : int { kJointRevolute = 0, kJointDistance = 1, kJointWeld = 2, kJointPrismatic = 3, kJointWheel = 4,
+             kJointRope = 5, kJointFriction = 6, kJointMotor = 7, kJointTypes };
 
 // A joint (Dynamics/Joints/b2RevoluteJoint.h, b2DistanceJoint.h, b2WeldJoint.h), stored whole: joints
 // are few. Fields a type does not use stay zero; the distance joint keeps its scalar impulse in
@@ -109,6 +110,20 @@ struct Joint {
     Vec2 localXAxisA, localYAxisA;            // prismatic: unit axis in body A and its normal
     Vec2 perp;                                // prismatic: normal of the axis, this step
     float s1, s2, a1, a2;                     // prismatic: lever arms of the step
+    // wheel (b2WheelJoint.h): the axis in localXAxisA/localYAxisA, this step's axes and lever arms,
+    // spring and motor state (the motor's maximum torque and speed in maxMotorTorque, motorSpeed)
+    Vec2 ax, ay;
+    float sAx, sBx, sAy, sBy;
+    float springMass, springImpulse;
+    // rope (b2RopeJoint.h): maximum length, this step's length; its impulse in impulse[0], mass in
+    // motorMass, state in limitState
+    float maxLength, ropeLength;
+    // friction and motor (b2FrictionJoint.h, b2MotorJoint.h): linear impulse in impulse[0..1], angular
+    // in impulse[2], the 2x2 linear mass in mass[0..3] (b2Mat22 columns ex, ey), angular mass in
+    // motorMass
+    float maxForce, maxTorque;
+    Vec2 linearOffset, linearError;           // motor
+    float angularOffset, angularError, correctionFactor;
 };
 
 // Island solver records: the fields of b2ContactVelocityConstraint and b2ContactPositionConstraint

@@ -35,7 +35,7 @@ import numpy as np
 STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 # shape encodings of the bulk build call
 CIRCLE, EDGE, POLYGON, BOX = 0, 1, 2, 3
-REVOLUTE, DISTANCE, WELD, PRISMATIC = 0, 1, 2, 3
+REVOLUTE, DISTANCE, WELD, PRISMATIC, WHEEL, ROPE, FRICTION, MOTOR = 0, 1, 2, 3, 4, 5, 6, 7
 DEFAULT_FLAGS = 1 | 2 | 16  # allowSleep, awake, active
 
 
@@ -105,6 +105,32 @@ class Scene:
     def weld(self, a, b, anchor_a, anchor_b, ref_angle=0.0, frequency_hz=0.0, damping_ratio=0.0, flags=0) -> int:
         self.joints.append((a, b, [anchor_a[0], anchor_a[1], anchor_b[0], anchor_b[1], ref_angle, frequency_hz,
                                    damping_ratio, 0.0, 0.0, 0.0, 0.0, 0.0], flags, WELD))
+        return len(self.joints) - 1
+
+    def wheel(self, a, b, anchor_a, anchor_b, axis, max_motor_torque=0.0, motor_speed=0.0, frequency_hz=2.0,
+              damping_ratio=0.7, flags=0) -> int:
+        """b2WheelJointDef (axis in body A's frame, not normalised); flags 2 motor, 4 collideConnected."""
+        self.joints.append((a, b, [anchor_a[0], anchor_a[1], anchor_b[0], anchor_b[1], axis[0], axis[1],
+                                   max_motor_torque, motor_speed, frequency_hz, damping_ratio, 0.0, 0.0], flags, WHEEL))
+        return len(self.joints) - 1
+
+    def rope(self, a, b, anchor_a, anchor_b, max_length, flags=0) -> int:
+        """b2RopeJointDef: at most max_length between the anchors."""
+        self.joints.append((a, b, [anchor_a[0], anchor_a[1], anchor_b[0], anchor_b[1], max_length] + [0.0] * 7,
+                            flags, ROPE))
+        return len(self.joints) - 1
+
+    def friction(self, a, b, anchor_a, anchor_b, max_force, max_torque, flags=0) -> int:
+        """b2FrictionJointDef: relative motion resisted up to max_force and max_torque."""
+        self.joints.append((a, b, [anchor_a[0], anchor_a[1], anchor_b[0], anchor_b[1], max_force, max_torque]
+                            + [0.0] * 6, flags, FRICTION))
+        return len(self.joints) - 1
+
+    def motor(self, a, b, linear_offset, angular_offset=0.0, max_force=1.0, max_torque=1.0, correction_factor=0.3,
+              flags=0) -> int:
+        """b2MotorJointDef: drives body B to linear_offset and angular_offset in body A's frame."""
+        self.joints.append((a, b, [linear_offset[0], linear_offset[1], angular_offset, max_force, max_torque,
+                                   correction_factor] + [0.0] * 6, flags, MOTOR))
         return len(self.joints) - 1
 
     def prismatic(self, a, b, anchor_a, anchor_b, axis, ref_angle=0.0, lower=0.0, upper=0.0, max_motor_force=0.0,
@@ -355,6 +381,47 @@ def prismatic_mix(rng: SplitMix64, allow_sleep: bool = True) -> Scene:
     for i in range(6):
         b = s.body(DYNAMIC, _q(-25.0 + 3.5 * i + rng.uniform(-0.5, 0.5)), _q(4.0 + 1.2 * i), angle=_q(rng.uniform(-0.4, 0.4)))
         s.fixture(b, CIRCLE if i % 2 else BOX, [0.0, 0.0, 0.4] if i % 2 else [0.4, 0.4], 1 if i % 2 else 2,
+                  density=1.0, friction=0.5)
+    return _settings(s, allow_sleep)
+
+
+def joint_zoo(rng: SplitMix64, allow_sleep: bool = True) -> Scene:
+    """Wheel, rope, friction and motor joints: a car on sprung wheel joints (rear motor) driving over a
+    bump, a rope-jointed chain swinging from an anchor, boxes held back by friction joints, a body
+    pulled to an offset by a motor joint, and boxes falling among them."""
+    s = Scene(name="joint_zoo")
+    g = s.body(STATIC, 0.0, 0.0)
+    s.fixture(g, EDGE, [-40.0, 0.0, 40.0, 0.0, 0, 0, 0, 0, 0, 0], friction=0.8)
+    s.fixture(g, BOX, [1.0, 0.25, -8.0, 0.0, 0.3], 5, friction=0.8)
+    # car: chassis and two wheels on wheel joints, axis up, springs, rear motor
+    car = s.body(DYNAMIC, -20.0, 1.2)
+    s.fixture(car, BOX, [1.5, 0.3], 2, density=1.0, group=-1)
+    for k, (dx, flags) in enumerate([(-1.0, 2), (1.0, 0)]):
+        wh = s.body(DYNAMIC, -20.0 + dx, 0.5)
+        s.fixture(wh, CIRCLE, [0.0, 0.0, 0.45], 1, density=1.0, friction=0.9, group=-1)
+        s.wheel(car, wh, (dx, -0.7), (0.0, 0.0), (0.0, 1.0), 40.0, -12.0, 4.0 + k, 0.7, flags)
+    # rope chain: a static anchor, five boxes, rope joints of slack length
+    anchor = s.body(STATIC, 5.0, 14.0)
+    s.fixture(anchor, BOX, [0.3, 0.3], 2)
+    prev = anchor
+    for i in range(5):
+        b = s.body(DYNAMIC, _q(6.2 + 1.2 * i), 14.0)
+        s.fixture(b, BOX, [0.3, 0.2], 2, density=1.0, group=-2)
+        s.rope(prev, b, (0.0, 0.0), (0.0, 0.0), _q(1.3 + 0.1 * rng.uniform(0.0, 1.0)))
+        prev = b
+    # friction joints: boxes sliding on the ground with a push (collide connected), dragged to rest
+    for i, (fmax, tmax) in enumerate([(5.0, 1.0), (20.0, 4.0), (0.0, 0.0)]):
+        b = s.body(DYNAMIC, 14.0 + 3.0 * i, 0.5, vx=6.0, w=3.0)
+        s.fixture(b, BOX, [0.5, 0.5], 2, density=1.0, friction=0.1)
+        s.friction(g, b, (14.0 + 3.0 * i, 0.5), (0.0, 0.0), fmax, tmax, flags=4)
+    # motor joint: a body pulled to an offset above the ground, bounded force and torque
+    m = s.body(DYNAMIC, 26.0, 1.0, angle=0.5)
+    s.fixture(m, BOX, [0.8, 0.3], 2, density=2.0)
+    s.motor(g, m, (28.0, 4.0), 1.0, 60.0, 10.0, 0.3)
+    for i in range(5):
+        b = s.body(DYNAMIC, _q(-12.0 + 5.0 * i + rng.uniform(-0.5, 0.5)), _q(6.0 + rng.uniform(0.0, 3.0)),
+                   angle=_q(rng.uniform(-0.5, 0.5)))
+        s.fixture(b, CIRCLE if i % 2 else BOX, [0.0, 0.0, 0.35] if i % 2 else [0.35, 0.35], 1 if i % 2 else 2,
                   density=1.0, friction=0.5)
     return _settings(s, allow_sleep)
 

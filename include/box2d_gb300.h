@@ -70,19 +70,33 @@ gb_status gb_create_fixtures(gb_world* world, int w, int n, const int* body, con
 gb_status gb_create_revolute_joints(gb_world* world, int w, int n, const int* body_a, const int* body_b,
                                     const float* f, const int* flags, int* out_ids);
 
-/* b2World::CreateJoint for revolute, distance, weld and prismatic joint definitions
- * (Box2D/Dynamics/b2World.cpp:185, Box2D/Dynamics/Joints/b2RevoluteJoint.h:36, b2DistanceJoint.h:30,
- * b2WeldJoint.h:28, b2PrismaticJoint.h:30). type: GB_JOINT_*. f[GB_JOINT_FLOATS] per joint: revolute
- * as gb_create_revolute_joints (f[0..8]); distance localAnchorA.x, .y, localAnchorB.x, .y, length,
- * frequencyHz, dampingRatio; weld localAnchorA.x, .y, localAnchorB.x, .y, referenceAngle,
- * frequencyHz, dampingRatio; prismatic localAnchorA.x, .y, localAnchorB.x, .y, localAxisA.x, .y
- * (normalised as the reference's constructor does), referenceAngle, lowerTranslation,
- * upperTranslation, maxMotorForce, motorSpeed. Unused trailing floats are ignored. flags: 1
- * enableLimit, 2 enableMotor (revolute, prismatic), 4 collideConnected. */
+/* b2World::CreateJoint for the joint definitions built here (Box2D/Dynamics/b2World.cpp:185;
+ * Box2D/Dynamics/Joints/b2RevoluteJoint.h:36, b2DistanceJoint.h:30, b2WeldJoint.h:28,
+ * b2PrismaticJoint.h:30, b2WheelJoint.h:30, b2RopeJoint.h:28, b2FrictionJoint.h:25,
+ * b2MotorJoint.h:26). type: GB_JOINT_*. f[GB_JOINT_FLOATS] per joint (the fields of the definition;
+ * anchors and axes in body-local coordinates):
+ *   revolute   localAnchorA.x, .y, localAnchorB.x, .y, referenceAngle, lowerAngle, upperAngle,
+ *              motorSpeed, maxMotorTorque (as gb_create_revolute_joints)
+ *   distance   localAnchorA.x, .y, localAnchorB.x, .y, length, frequencyHz, dampingRatio
+ *   weld       localAnchorA.x, .y, localAnchorB.x, .y, referenceAngle, frequencyHz, dampingRatio
+ *   prismatic  localAnchorA.x, .y, localAnchorB.x, .y, localAxisA.x, .y (normalised as the
+ *              reference's constructor does), referenceAngle, lowerTranslation, upperTranslation,
+ *              maxMotorForce, motorSpeed
+ *   wheel      localAnchorA.x, .y, localAnchorB.x, .y, localAxisA.x, .y (taken as given, as the
+ *              reference does), maxMotorTorque, motorSpeed, frequencyHz, dampingRatio
+ *   rope       localAnchorA.x, .y, localAnchorB.x, .y, maxLength
+ *   friction   localAnchorA.x, .y, localAnchorB.x, .y, maxForce, maxTorque
+ *   motor      linearOffset.x, .y, angularOffset, maxForce, maxTorque, correctionFactor
+ * Unused trailing floats are ignored. flags: 1 enableLimit (revolute, prismatic), 2 enableMotor
+ * (revolute, prismatic, wheel), 4 collideConnected. */
 #define GB_JOINT_REVOLUTE 0
 #define GB_JOINT_DISTANCE 1
 #define GB_JOINT_WELD 2
 #define GB_JOINT_PRISMATIC 3
+#define GB_JOINT_WHEEL 4
+#define GB_JOINT_ROPE 5
+#define GB_JOINT_FRICTION 6
+#define GB_JOINT_MOTOR 7
 #define GB_JOINT_FLOATS 12
 gb_status gb_create_joints(gb_world* world, int w, int n, const int* type, const int* body_a, const int* body_b,
                            const float* f, const int* flags, int* out_ids);

@@ -260,6 +260,42 @@ struct b2WeldJointDef {
     float frequencyHz = 0.0f, dampingRatio = 0.0f;
 };
 
+// b2WheelJointDef, b2RopeJointDef, b2FrictionJointDef, b2MotorJointDef (Box2D/Dynamics/Joints/
+// b2WheelJoint.h:30-68, b2RopeJoint.h:28-45, b2FrictionJoint.h:25-45, b2MotorJoint.h:26-55), with
+// the reference's defaults
+struct b2WheelJointDef {
+    b2Body* bodyA = nullptr;
+    b2Body* bodyB = nullptr;
+    bool collideConnected = false;
+    b2Vec2 localAnchorA, localAnchorB;
+    b2Vec2 localAxisA{1.0f, 0.0f};
+    bool enableMotor = false;
+    float maxMotorTorque = 0.0f, motorSpeed = 0.0f;
+    float frequencyHz = 2.0f, dampingRatio = 0.7f;
+};
+struct b2RopeJointDef {
+    b2Body* bodyA = nullptr;
+    b2Body* bodyB = nullptr;
+    bool collideConnected = false;
+    b2Vec2 localAnchorA{-1.0f, 0.0f}, localAnchorB{1.0f, 0.0f};
+    float maxLength = 0.0f;
+};
+struct b2FrictionJointDef {
+    b2Body* bodyA = nullptr;
+    b2Body* bodyB = nullptr;
+    bool collideConnected = false;
+    b2Vec2 localAnchorA, localAnchorB;
+    float maxForce = 0.0f, maxTorque = 0.0f;
+};
+struct b2MotorJointDef {
+    b2Body* bodyA = nullptr;
+    b2Body* bodyB = nullptr;
+    bool collideConnected = false;
+    b2Vec2 linearOffset;
+    float angularOffset = 0.0f;
+    float maxForce = 1.0f, maxTorque = 1.0f, correctionFactor = 0.3f;
+};
+
 // b2PrismaticJointDef (Box2D/Dynamics/Joints/b2PrismaticJoint.h:30-88)
 struct b2PrismaticJointDef {
     b2Body* bodyA = nullptr;
@@ -397,6 +433,32 @@ public:
                                           def->localAnchorB.y, def->referenceAngle, def->frequencyHz,
                                           def->dampingRatio};
         return AddJoint(GB_JOINT_WELD, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
+    }
+    b2Joint* CreateJoint(const b2WheelJointDef* def)
+    {
+        const float f[GB_JOINT_FLOATS] = {def->localAnchorA.x, def->localAnchorA.y, def->localAnchorB.x,
+                                          def->localAnchorB.y, def->localAxisA.x, def->localAxisA.y,
+                                          def->maxMotorTorque, def->motorSpeed, def->frequencyHz, def->dampingRatio};
+        const int flags = (def->enableMotor ? 2 : 0) | (def->collideConnected ? 4 : 0);
+        return AddJoint(GB_JOINT_WHEEL, def->bodyA, def->bodyB, f, flags);
+    }
+    b2Joint* CreateJoint(const b2RopeJointDef* def)
+    {
+        const float f[GB_JOINT_FLOATS] = {def->localAnchorA.x, def->localAnchorA.y, def->localAnchorB.x,
+                                          def->localAnchorB.y, def->maxLength};
+        return AddJoint(GB_JOINT_ROPE, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
+    }
+    b2Joint* CreateJoint(const b2FrictionJointDef* def)
+    {
+        const float f[GB_JOINT_FLOATS] = {def->localAnchorA.x, def->localAnchorA.y, def->localAnchorB.x,
+                                          def->localAnchorB.y, def->maxForce, def->maxTorque};
+        return AddJoint(GB_JOINT_FRICTION, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
+    }
+    b2Joint* CreateJoint(const b2MotorJointDef* def)
+    {
+        const float f[GB_JOINT_FLOATS] = {def->linearOffset.x, def->linearOffset.y, def->angularOffset, def->maxForce,
+                                          def->maxTorque, def->correctionFactor};
+        return AddJoint(GB_JOINT_MOTOR, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
     }
     b2Joint* CreateJoint(const b2PrismaticJointDef* def)
     {

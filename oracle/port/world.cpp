@@ -146,7 +146,30 @@ int World::CreateJoint(int type, int a, int b, const float* f, int fl)
     j.bodyA = a; j.bodyB = b;
     j.localAnchorA = V(f[0], f[1]);
     j.localAnchorB = V(f[2], f[3]);
-    if (type == kPrismaticJoint) {
+    if (type == kWheelJoint) {
+        // b2WheelJoint::b2WheelJoint (b2WheelJoint.cpp): the axis as given, its normal b2Cross(1, axis)
+        j.localXAxisA = V(f[4], f[5]);
+        j.localYAxisA = Cross(1.0f, j.localXAxisA);
+        j.maxMotorTorque = f[6];
+        j.motorSpeed = f[7];
+        j.frequencyHz = f[8];
+        j.dampingRatio = f[9];
+        j.enableMotor = (fl & 2) != 0;
+    } else if (type == kRopeJoint) {
+        j.maxLength = f[4];
+    } else if (type == kFrictionJoint) {
+        j.maxForce = f[4];
+        j.maxTorque = f[5];
+    } else if (type == kMotorJoint) {
+        // b2MotorJoint::b2MotorJoint (b2MotorJoint.cpp): no anchors, the offsets in f[0..2]
+        j.localAnchorA = V(0.0f, 0.0f);
+        j.localAnchorB = V(0.0f, 0.0f);
+        j.linearOffset = V(f[0], f[1]);
+        j.angularOffset = f[2];
+        j.maxForce = f[3];
+        j.maxTorque = f[4];
+        j.correctionFactor = f[5];
+    } else if (type == kPrismaticJoint) {
         // b2PrismaticJoint::b2PrismaticJoint (b2PrismaticJoint.cpp:102-126)
         j.localXAxisA = V(f[4], f[5]);
         Normalize(j.localXAxisA);
@@ -1002,6 +1025,14 @@ bool WeldSolvePosition(Joint& j, Position* pos);
 void PrisInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel);
 void PrisSolveVelocity(Joint& j, const StepInfo& step, Velocity* vel);
 bool PrisSolvePosition(Joint& j, Position* pos);
+void WheelInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel);
+void WheelSolveVelocity(Joint& j, const StepInfo& step, Velocity* vel);
+bool WheelSolvePosition(Joint& j, Position* pos);
+void RopeInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel);
+void RopeSolveVelocity(Joint& j, const StepInfo& step, Velocity* vel);
+bool RopeSolvePosition(Joint& j, Position* pos);
+void FrictionMotorInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel);
+void FrictionMotorSolveVelocity(Joint& j, const StepInfo& step, Velocity* vel);
 
 // b2Mat33::Solve33 / Solve22 (Common/b2Math.cpp:24-56)
 inline void Solve33(const float* M, const float* b, float* x)
@@ -1634,6 +1665,343 @@ bool PrisSolvePosition(Joint& j, Position* pos)
     return linearError <= kLinearSlop && angularError <= kAngularSlop;
 }
 
+
+// ---------------------------------------------------------------- wheel joint
+// b2WheelJoint::InitVelocityConstraints (Dynamics/Joints/b2WheelJoint.cpp)
+void WheelInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel)
+{
+    const Body& A = w->bodies[j.bodyA];
+    const Body& B = w->bodies[j.bodyB];
+    j.indexA = A.islandIndex; j.indexB = B.islandIndex;
+    j.localCenterA = A.sweep.localCenter; j.localCenterB = B.sweep.localCenter;
+    j.invMassA = A.invMass; j.invMassB = B.invMass;
+    j.invIA = A.invI; j.invIB = B.invI;
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    const Vec2 cA = pos[j.indexA].c, cB = pos[j.indexB].c;
+    const float aA = pos[j.indexA].a, aB = pos[j.indexB].a;
+    Vec2 vA = vel[j.indexA].v, vB = vel[j.indexB].v;
+    float wA = vel[j.indexA].w, wB = vel[j.indexB].w;
+    const Rot qA = RotOf(aA), qB = RotOf(aB);
+    const Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    const Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    const Vec2 d = cB + rB - cA - rA;
+    j.ay = Mul(qA, j.localYAxisA);
+    j.sAy = Cross(d + rA, j.ay);
+    j.sBy = Cross(rB, j.ay);
+    j.mass[0] = mA + mB + iA * j.sAy * j.sAy + iB * j.sBy * j.sBy;
+    if (j.mass[0] > 0.0f) j.mass[0] = 1.0f / j.mass[0];
+    j.springMass = 0.0f;
+    j.bias = 0.0f;
+    j.gamma = 0.0f;
+    if (j.frequencyHz > 0.0f) {
+        j.ax = Mul(qA, j.localXAxisA);
+        j.sAx = Cross(d + rA, j.ax);
+        j.sBx = Cross(rB, j.ax);
+        const float invMass = mA + mB + iA * j.sAx * j.sAx + iB * j.sBx * j.sBx;
+        if (invMass > 0.0f) {
+            j.springMass = 1.0f / invMass;
+            const float C = Dot(d, j.ax);
+            const float omega = 2.0f * kPi * j.frequencyHz;
+            const float damp = 2.0f * j.springMass * j.dampingRatio * omega;
+            const float k = j.springMass * omega * omega;
+            const float h = step.dt;
+            j.gamma = h * (damp + h * k);
+            if (j.gamma > 0.0f) j.gamma = 1.0f / j.gamma;
+            j.bias = C * h * k * j.gamma;
+            j.springMass = invMass + j.gamma;
+            if (j.springMass > 0.0f) j.springMass = 1.0f / j.springMass;
+        }
+    } else {
+        j.springImpulse = 0.0f;
+    }
+    if (j.enableMotor) {
+        j.motorMass = iA + iB;
+        if (j.motorMass > 0.0f) j.motorMass = 1.0f / j.motorMass;
+    } else {
+        j.motorMass = 0.0f;
+        j.motorImpulse = 0.0f;
+    }
+    if (step.warmStarting) {
+        j.impulse[0] *= step.dtRatio;
+        j.springImpulse *= step.dtRatio;
+        j.motorImpulse *= step.dtRatio;
+        const Vec2 P = j.impulse[0] * j.ay + j.springImpulse * j.ax;
+        const float LA = j.impulse[0] * j.sAy + j.springImpulse * j.sAx + j.motorImpulse;
+        const float LB = j.impulse[0] * j.sBy + j.springImpulse * j.sBx + j.motorImpulse;
+        vA = vA - j.invMassA * P;
+        wA -= j.invIA * LA;
+        vB = vB + j.invMassB * P;
+        wB += j.invIB * LB;
+    } else {
+        j.impulse[0] = 0.0f;
+        j.springImpulse = 0.0f;
+        j.motorImpulse = 0.0f;
+    }
+    vel[j.indexA].v = vA; vel[j.indexA].w = wA;
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+}
+
+// b2WheelJoint::SolveVelocityConstraints: spring, rotational motor, point to line
+void WheelSolveVelocity(Joint& j, const StepInfo& step, Velocity* vel)
+{
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    Vec2 vA = vel[j.indexA].v, vB = vel[j.indexB].v;
+    float wA = vel[j.indexA].w, wB = vel[j.indexB].w;
+    {
+        const float Cdot = Dot(j.ax, vB - vA) + j.sBx * wB - j.sAx * wA;
+        const float impulse = -j.springMass * (Cdot + j.bias + j.gamma * j.springImpulse);
+        j.springImpulse += impulse;
+        const Vec2 P = impulse * j.ax;
+        const float LA = impulse * j.sAx, LB = impulse * j.sBx;
+        vA = vA - mA * P;
+        wA -= iA * LA;
+        vB = vB + mB * P;
+        wB += iB * LB;
+    }
+    {
+        const float Cdot = wB - wA - j.motorSpeed;
+        float impulse = -j.motorMass * Cdot;
+        const float oldImpulse = j.motorImpulse;
+        const float maxImpulse = step.dt * j.maxMotorTorque;
+        j.motorImpulse = Clamp(j.motorImpulse + impulse, -maxImpulse, maxImpulse);
+        impulse = j.motorImpulse - oldImpulse;
+        wA -= iA * impulse;
+        wB += iB * impulse;
+    }
+    {
+        const float Cdot = Dot(j.ay, vB - vA) + j.sBy * wB - j.sAy * wA;
+        const float impulse = -j.mass[0] * Cdot;
+        j.impulse[0] += impulse;
+        const Vec2 P = impulse * j.ay;
+        const float LA = impulse * j.sAy, LB = impulse * j.sBy;
+        vA = vA - mA * P;
+        wA -= iA * LA;
+        vB = vB + mB * P;
+        wB += iB * LB;
+    }
+    vel[j.indexA].v = vA; vel[j.indexA].w = wA;
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+}
+
+// b2WheelJoint::SolvePositionConstraints (its mass uses the velocity step's lever arms m_sAy, m_sBy)
+bool WheelSolvePosition(Joint& j, Position* pos)
+{
+    Vec2 cA = pos[j.indexA].c, cB = pos[j.indexB].c;
+    float aA = pos[j.indexA].a, aB = pos[j.indexB].a;
+    const Rot qA = RotOf(aA), qB = RotOf(aB);
+    const Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    const Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    const Vec2 d = (cB - cA) + rB - rA;
+    const Vec2 ay = Mul(qA, j.localYAxisA);
+    const float sAy = Cross(d + rA, ay), sBy = Cross(rB, ay);
+    const float C = Dot(d, ay);
+    const float k = j.invMassA + j.invMassB + j.invIA * j.sAy * j.sAy + j.invIB * j.sBy * j.sBy;
+    float impulse;
+    if (k != 0.0f) impulse = -C / k;
+    else impulse = 0.0f;
+    const Vec2 P = impulse * ay;
+    const float LA = impulse * sAy, LB = impulse * sBy;
+    cA = cA - j.invMassA * P;
+    aA -= j.invIA * LA;
+    cB = cB + j.invMassB * P;
+    aB += j.invIB * LB;
+    pos[j.indexA].c = cA; pos[j.indexA].a = aA;
+    pos[j.indexB].c = cB; pos[j.indexB].a = aB;
+    return Abs(C) <= kLinearSlop;
+}
+
+// ---------------------------------------------------------------- rope joint
+// b2RopeJoint::InitVelocityConstraints (Dynamics/Joints/b2RopeJoint.cpp)
+void RopeInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel)
+{
+    const Body& A = w->bodies[j.bodyA];
+    const Body& B = w->bodies[j.bodyB];
+    j.indexA = A.islandIndex; j.indexB = B.islandIndex;
+    j.localCenterA = A.sweep.localCenter; j.localCenterB = B.sweep.localCenter;
+    j.invMassA = A.invMass; j.invMassB = B.invMass;
+    j.invIA = A.invI; j.invIB = B.invI;
+    const Vec2 cA = pos[j.indexA].c, cB = pos[j.indexB].c;
+    const float aA = pos[j.indexA].a, aB = pos[j.indexB].a;
+    Vec2 vA = vel[j.indexA].v, vB = vel[j.indexB].v;
+    float wA = vel[j.indexA].w, wB = vel[j.indexB].w;
+    const Rot qA = RotOf(aA), qB = RotOf(aB);
+    j.rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    j.rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    j.u = cB + j.rB - cA - j.rA;
+    j.ropeLength = Length(j.u);
+    const float C = j.ropeLength - j.maxLength;
+    j.limitState = C > 0.0f ? 2 : 0;
+    if (j.ropeLength > kLinearSlop) {
+        const float inv = 1.0f / j.ropeLength;
+        j.u.x *= inv;
+        j.u.y *= inv;
+    } else {
+        j.u = V(0.0f, 0.0f);
+        j.motorMass = 0.0f;
+        j.impulse[0] = 0.0f;
+        return;
+    }
+    const float crA = Cross(j.rA, j.u), crB = Cross(j.rB, j.u);
+    const float invMass = j.invMassA + j.invIA * crA * crA + j.invMassB + j.invIB * crB * crB;
+    j.motorMass = invMass != 0.0f ? 1.0f / invMass : 0.0f;
+    if (step.warmStarting) {
+        j.impulse[0] *= step.dtRatio;
+        const Vec2 P = j.impulse[0] * j.u;
+        vA = vA - j.invMassA * P;
+        wA -= j.invIA * Cross(j.rA, P);
+        vB = vB + j.invMassB * P;
+        wB += j.invIB * Cross(j.rB, P);
+    } else {
+        j.impulse[0] = 0.0f;
+    }
+    vel[j.indexA].v = vA; vel[j.indexA].w = wA;
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+}
+
+void RopeSolveVelocity(Joint& j, const StepInfo& step, Velocity* vel)
+{
+    Vec2 vA = vel[j.indexA].v, vB = vel[j.indexB].v;
+    float wA = vel[j.indexA].w, wB = vel[j.indexB].w;
+    const Vec2 vpA = vA + Cross(wA, j.rA);
+    const Vec2 vpB = vB + Cross(wB, j.rB);
+    const float C = j.ropeLength - j.maxLength;
+    float Cdot = Dot(j.u, vpB - vpA);
+    if (C < 0.0f) Cdot += step.inv_dt * C;
+    float impulse = -j.motorMass * Cdot;
+    const float oldImpulse = j.impulse[0];
+    j.impulse[0] = Min(0.0f, j.impulse[0] + impulse);
+    impulse = j.impulse[0] - oldImpulse;
+    const Vec2 P = impulse * j.u;
+    vA = vA - j.invMassA * P;
+    wA -= j.invIA * Cross(j.rA, P);
+    vB = vB + j.invMassB * P;
+    wB += j.invIB * Cross(j.rB, P);
+    vel[j.indexA].v = vA; vel[j.indexA].w = wA;
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+}
+
+bool RopeSolvePosition(Joint& j, Position* pos)
+{
+    Vec2 cA = pos[j.indexA].c, cB = pos[j.indexB].c;
+    float aA = pos[j.indexA].a, aB = pos[j.indexB].a;
+    const Rot qA = RotOf(aA), qB = RotOf(aB);
+    const Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    const Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    Vec2 u = cB + rB - cA - rA;
+    const float length = Normalize(u);
+    float C = length - j.maxLength;
+    C = Clamp(C, 0.0f, kMaxLinearCorrection);
+    const float impulse = -j.motorMass * C;
+    const Vec2 P = impulse * u;
+    cA = cA - j.invMassA * P;
+    aA -= j.invIA * Cross(rA, P);
+    cB = cB + j.invMassB * P;
+    aB += j.invIB * Cross(rB, P);
+    pos[j.indexA].c = cA; pos[j.indexA].a = aA;
+    pos[j.indexB].c = cB; pos[j.indexB].a = aB;
+    return length - j.maxLength < kLinearSlop;
+}
+
+// ---------------------------------------------------------------- friction and motor joints
+// b2FrictionJoint (Dynamics/Joints/b2FrictionJoint.cpp) and b2MotorJoint (b2MotorJoint.cpp):
+// InitVelocityConstraints; both have no position constraint.
+void FrictionMotorInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel)
+{
+    const Body& A = w->bodies[j.bodyA];
+    const Body& B = w->bodies[j.bodyB];
+    j.indexA = A.islandIndex; j.indexB = B.islandIndex;
+    j.localCenterA = A.sweep.localCenter; j.localCenterB = B.sweep.localCenter;
+    j.invMassA = A.invMass; j.invMassB = B.invMass;
+    j.invIA = A.invI; j.invIB = B.invI;
+    const float aA = pos[j.indexA].a, aB = pos[j.indexB].a;
+    Vec2 vA = vel[j.indexA].v, vB = vel[j.indexB].v;
+    float wA = vel[j.indexA].w, wB = vel[j.indexB].w;
+    const Rot qA = RotOf(aA), qB = RotOf(aB);
+    if (j.type == kMotorJoint) {
+        j.rA = Mul(qA, -j.localCenterA);
+        j.rB = Mul(qB, -j.localCenterB);
+    } else {
+        j.rA = Mul(qA, j.localAnchorA - j.localCenterA);
+        j.rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    }
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    // b2Mat22 K and its inverse (b2Mat22::GetInverse, Common/b2Math.h)
+    const float kexx = mA + mB + iA * j.rA.y * j.rA.y + iB * j.rB.y * j.rB.y;
+    const float kexy = -iA * j.rA.x * j.rA.y - iB * j.rB.x * j.rB.y;
+    const float keyx = kexy;
+    const float keyy = mA + mB + iA * j.rA.x * j.rA.x + iB * j.rB.x * j.rB.x;
+    float det = kexx * keyy - keyx * kexy;
+    if (det != 0.0f) det = 1.0f / det;
+    j.mass[0] = det * keyy; j.mass[2] = -det * keyx;
+    j.mass[1] = -det * kexy; j.mass[3] = det * kexx;
+    j.motorMass = iA + iB;
+    if (j.motorMass > 0.0f) j.motorMass = 1.0f / j.motorMass;
+    if (j.type == kMotorJoint) {
+        const Vec2 cA = pos[j.indexA].c, cB = pos[j.indexB].c;
+        j.linearError = cB + j.rB - cA - j.rA - Mul(qA, j.linearOffset);
+        j.angularError = aB - aA - j.angularOffset;
+    }
+    if (step.warmStarting) {
+        j.impulse[0] *= step.dtRatio; j.impulse[1] *= step.dtRatio;
+        j.impulse[2] *= step.dtRatio;
+        const Vec2 P = V(j.impulse[0], j.impulse[1]);
+        vA = vA - mA * P;
+        wA -= iA * (Cross(j.rA, P) + j.impulse[2]);
+        vB = vB + mB * P;
+        wB += iB * (Cross(j.rB, P) + j.impulse[2]);
+    } else {
+        j.impulse[0] = j.impulse[1] = 0.0f;
+        j.impulse[2] = 0.0f;
+    }
+    vel[j.indexA].v = vA; vel[j.indexA].w = wA;
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+}
+
+// SolveVelocityConstraints of both: angular impulse bounded by dt * maxTorque, linear impulse by
+// dt * maxForce in length; the motor joint adds its position errors scaled by inv_dt * correctionFactor
+void FrictionMotorSolveVelocity(Joint& j, const StepInfo& step, Velocity* vel)
+{
+    Vec2 vA = vel[j.indexA].v, vB = vel[j.indexB].v;
+    float wA = vel[j.indexA].w, wB = vel[j.indexB].w;
+    const float mA = j.invMassA, mB = j.invMassB, iA = j.invIA, iB = j.invIB;
+    const float h = step.dt;
+    const float inv_h = step.inv_dt;
+    const bool motor = j.type == kMotorJoint;
+    {
+        const float Cdot = motor ? wB - wA + inv_h * j.correctionFactor * j.angularError : wB - wA;
+        float impulse = -j.motorMass * Cdot;
+        const float oldImpulse = j.impulse[2];
+        const float maxImpulse = h * j.maxTorque;
+        j.impulse[2] = Clamp(j.impulse[2] + impulse, -maxImpulse, maxImpulse);
+        impulse = j.impulse[2] - oldImpulse;
+        wA -= iA * impulse;
+        wB += iB * impulse;
+    }
+    {
+        Vec2 Cdot = vB + Cross(wB, j.rB) - vA - Cross(wA, j.rA);
+        if (motor) Cdot = Cdot + inv_h * j.correctionFactor * j.linearError;
+        const float* M = j.mass;
+        Vec2 impulse = -V(M[0] * Cdot.x + M[2] * Cdot.y, M[1] * Cdot.x + M[3] * Cdot.y);
+        const Vec2 oldImpulse = V(j.impulse[0], j.impulse[1]);
+        Vec2 li = oldImpulse + impulse;
+        const float maxImpulse = h * j.maxForce;
+        if (LengthSq(li) > maxImpulse * maxImpulse) {
+            Normalize(li);
+            li.x *= maxImpulse;
+            li.y *= maxImpulse;
+        }
+        j.impulse[0] = li.x;
+        j.impulse[1] = li.y;
+        impulse = li - oldImpulse;
+        vA = vA - mA * impulse;
+        wA -= iA * Cross(j.rA, impulse);
+        vB = vB + mB * impulse;
+        wB += iB * Cross(j.rB, impulse);
+    }
+    vel[j.indexA].v = vA; vel[j.indexA].w = wA;
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+}
+
 } // namespace
 
 // ---------------------------------------------------------------- island solve
@@ -1669,6 +2037,10 @@ void World::IslandSolve(const StepInfo& step)
         if (j.type == kDistanceJoint) DistInit(this, j, step, positions.data(), velocities.data());
         else if (j.type == kWeldJoint) WeldInit(this, j, step, positions.data(), velocities.data());
         else if (j.type == kPrismaticJoint) PrisInit(this, j, step, positions.data(), velocities.data());
+        else if (j.type == kWheelJoint) WheelInit(this, j, step, positions.data(), velocities.data());
+        else if (j.type == kRopeJoint) RopeInit(this, j, step, positions.data(), velocities.data());
+        else if (j.type == kFrictionJoint || j.type == kMotorJoint)
+            FrictionMotorInit(this, j, step, positions.data(), velocities.data());
         else RevInit(this, j, step, positions.data(), velocities.data());
     }
     for (int i = 0; i < step.velocityIterations; ++i) {
@@ -1677,6 +2049,10 @@ void World::IslandSolve(const StepInfo& step)
             if (j.type == kDistanceJoint) DistSolveVelocity(j, velocities.data());
             else if (j.type == kWeldJoint) WeldSolveVelocity(j, velocities.data());
             else if (j.type == kPrismaticJoint) PrisSolveVelocity(j, step, velocities.data());
+            else if (j.type == kWheelJoint) WheelSolveVelocity(j, step, velocities.data());
+            else if (j.type == kRopeJoint) RopeSolveVelocity(j, step, velocities.data());
+            else if (j.type == kFrictionJoint || j.type == kMotorJoint)
+                FrictionMotorSolveVelocity(j, step, velocities.data());
             else RevSolveVelocity(j, step, velocities.data());
         }
         cs.SolveVelocity();
@@ -1712,6 +2088,9 @@ void World::IslandSolve(const StepInfo& step)
             bool ok = j.type == kDistanceJoint ? DistSolvePosition(j, positions.data())
                       : j.type == kWeldJoint   ? WeldSolvePosition(j, positions.data())
                       : j.type == kPrismaticJoint ? PrisSolvePosition(j, positions.data())
+                      : j.type == kWheelJoint ? WheelSolvePosition(j, positions.data())
+                      : j.type == kRopeJoint ? RopeSolvePosition(j, positions.data())
+                      : (j.type == kFrictionJoint || j.type == kMotorJoint) ? true
                                                : RevSolvePosition(j, positions.data());
             jointsOkay = jointsOkay && ok;
         }

@@ -55,7 +55,8 @@ struct Contact {
 };
 
 // joint types (b2JointType, Dynamics/Joints/b2Joint.h:28-42, those restated here)
-enum JointType { kRevoluteJoint = 0, kDistanceJoint = 1, kWeldJoint = 2, kPrismaticJoint = 3 };
+enum JointType { kRevoluteJoint = 0, kDistanceJoint = 1, kWeldJoint = 2, kPrismaticJoint = 3, kWheelJoint = 4,
+                 kRopeJoint = 5, kFrictionJoint = 6, kMotorJoint = 7 };
 
 struct Joint {
     int type = kRevoluteJoint;
@@ -84,6 +85,17 @@ struct Joint {
     // force in maxMotorTorque, the 3x3 K in mass[]
     Vec2 localXAxisA{0, 0}, localYAxisA{0, 0}, perp{0, 0};
     float s1 = 0, s2 = 0, a1 = 0, a2 = 0;
+    // wheel joint (b2WheelJoint.h): point-on-line mass in mass[0], motor torque and speed in
+    // maxMotorTorque, motorSpeed
+    Vec2 ax{0, 0}, ay{0, 0};
+    float sAx = 0, sBx = 0, sAy = 0, sBy = 0, springMass = 0, springImpulse = 0;
+    // rope joint (b2RopeJoint.h): impulse in impulse[0], mass in motorMass, state in limitState
+    float maxLength = 0, ropeLength = 0;
+    // friction and motor joints: linear impulse impulse[0..1], angular impulse[2], 2x2 linear mass
+    // mass[0..3] (columns ex, ey), angular mass motorMass
+    float maxForce = 0, maxTorque = 0;
+    Vec2 linearOffset{0, 0}, linearError{0, 0};
+    float angularOffset = 0, angularError = 0, correctionFactor = 0;
 };
 
 struct Position { Vec2 c; float a; };

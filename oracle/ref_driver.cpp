@@ -182,6 +182,50 @@ int rw_joint(void* h, int type, int bodyA, int bodyB, const float* f, int flags)
         jd.dampingRatio = f[6];
         jd.collideConnected = (flags & 4) != 0;
         w->joints.push_back(w->world.CreateJoint(&jd));
+    } else if (type == 4) {
+        b2WheelJointDef jd;
+        jd.bodyA = w->bodies[bodyA];
+        jd.bodyB = w->bodies[bodyB];
+        jd.localAnchorA.Set(f[0], f[1]);
+        jd.localAnchorB.Set(f[2], f[3]);
+        jd.localAxisA.Set(f[4], f[5]);
+        jd.maxMotorTorque = f[6];
+        jd.motorSpeed = f[7];
+        jd.frequencyHz = f[8];
+        jd.dampingRatio = f[9];
+        jd.enableMotor = (flags & 2) != 0;
+        jd.collideConnected = (flags & 4) != 0;
+        w->joints.push_back(w->world.CreateJoint(&jd));
+    } else if (type == 5) {
+        b2RopeJointDef jd;
+        jd.bodyA = w->bodies[bodyA];
+        jd.bodyB = w->bodies[bodyB];
+        jd.localAnchorA.Set(f[0], f[1]);
+        jd.localAnchorB.Set(f[2], f[3]);
+        jd.maxLength = f[4];
+        jd.collideConnected = (flags & 4) != 0;
+        w->joints.push_back(w->world.CreateJoint(&jd));
+    } else if (type == 6) {
+        b2FrictionJointDef jd;
+        jd.bodyA = w->bodies[bodyA];
+        jd.bodyB = w->bodies[bodyB];
+        jd.localAnchorA.Set(f[0], f[1]);
+        jd.localAnchorB.Set(f[2], f[3]);
+        jd.maxForce = f[4];
+        jd.maxTorque = f[5];
+        jd.collideConnected = (flags & 4) != 0;
+        w->joints.push_back(w->world.CreateJoint(&jd));
+    } else if (type == 7) {
+        b2MotorJointDef jd;
+        jd.bodyA = w->bodies[bodyA];
+        jd.bodyB = w->bodies[bodyB];
+        jd.linearOffset.Set(f[0], f[1]);
+        jd.angularOffset = f[2];
+        jd.maxForce = f[3];
+        jd.maxTorque = f[4];
+        jd.correctionFactor = f[5];
+        jd.collideConnected = (flags & 4) != 0;
+        w->joints.push_back(w->world.CreateJoint(&jd));
     } else {
         b2PrismaticJointDef jd;
         jd.bodyA = w->bodies[bodyA];

@@ -62,6 +62,7 @@ def cases():
         ("chains6x16", lambda: chains_with_load(), 300, [1, 100, 300]),
         ("joint_mix", lambda: scenes.joint_mix(scenes.SplitMix64(3)), 300, [1, 60, 150, 300]),
         ("prismatic_mix", lambda: scenes.prismatic_mix(scenes.SplitMix64(5)), 300, [1, 60, 150, 300]),
+        ("joint_zoo", lambda: scenes.joint_zoo(scenes.SplitMix64(6)), 300, [1, 60, 150, 300]),
     ] + [(f"batch{i}", (lambda i=i: batch_world(i)), 200, [200]) for i in range(24)]
 
 
