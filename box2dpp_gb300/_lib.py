@@ -37,7 +37,7 @@ EXPORTS = [
 # gb_body_edit ops (GB_EDIT_*) and the record layout: world, body, op, wake (int32), v[4] (float32)
 EDIT_OPS = {"set_transform": 0, "set_linear_velocity": 1, "set_angular_velocity": 2, "set_awake": 3,
             "apply_force": 4, "apply_force_to_center": 5, "apply_torque": 6, "apply_linear_impulse": 7,
-            "apply_angular_impulse": 8}
+            "apply_angular_impulse": 8, "mouse_target": 9}
 EDIT_DTYPE = np.dtype([("world", np.int32), ("body", np.int32), ("op", np.int32), ("wake", np.int32),
                        ("v", np.float32, 4)])
 

@@ -807,6 +807,20 @@ gb_status CreateJoint(HWorld& W, int type, int a, int b, const float* f, int fl,
         j.localYAxisA = Cross(1.0f, j.localXAxisA);
         j.maxMotorTorque = f[6]; j.motorSpeed = f[7]; j.frequencyHz = f[8]; j.dampingRatio = f[9];
         j.enableMotor = (fl & 2) != 0;
+    } else if (type == kJointMouse) {
+        // b2MouseJoint::b2MouseJoint (Dynamics/Joints/b2MouseJoint.cpp:33-52): the target's point on
+        // body B at creation
+        j.target = V(f[0], f[1]);
+        j.localAnchorA = V(0.0f, 0.0f);
+        j.localAnchorB = MulT(W.bodies[b].xf, j.target);
+        j.maxForce = f[2]; j.frequencyHz = f[3]; j.dampingRatio = f[4];
+    } else if (type == kJointPulley) {
+        // b2PulleyJoint::b2PulleyJoint (b2PulleyJoint.cpp:53-69)
+        j.groundAnchorA = V(f[0], f[1]); j.groundAnchorB = V(f[2], f[3]);
+        j.localAnchorA = V(f[4], f[5]); j.localAnchorB = V(f[6], f[7]);
+        j.lengthA = f[8]; j.lengthB = f[9]; j.ratio = f[10];
+        if (!(j.ratio != 0.0f)) return GB_ERR_INVALID;
+        j.pulleyConstant = f[8] + j.ratio * f[9];
     } else if (type == kJointRope) {
         j.maxLength = f[4];  // b2RopeJoint::b2RopeJoint (b2RopeJoint.cpp:35-45)
     } else if (type == kJointFriction) {
@@ -901,8 +915,14 @@ gb_status gb_body_edits(gb_world* g, int n, const gb_body_edit* edits)
     for (int i = 0; i < n; ++i) {
         const gb_body_edit& e = edits[i];
         if (e.world < 0 || e.world >= (int)g->worlds.size()) return GB_ERR_INVALID;
-        if (e.body < 0 || e.body >= (int)g->worlds[e.world].bodies.size()) return GB_ERR_INVALID;
         if (e.op < 0 || e.op >= kEditOps) return GB_ERR_INVALID;
+        const HWorld& W = g->worlds[e.world];
+        if (e.op == kEditMouseTarget) {
+            // body is the joint index; only a mouse joint has a target
+            if (e.body < 0 || e.body >= (int)W.joints.size() || W.joints[e.body].type != kJointMouse) return GB_ERR_INVALID;
+        } else if (e.body < 0 || e.body >= (int)W.bodies.size()) {
+            return GB_ERR_INVALID;
+        }
     }
     gb_status s = Upload(g);
     if (s != GB_OK) return s;

@@ -1351,10 +1351,190 @@ __device__ void FrictionMotorSolveVelocity(Joint& j, float4* vel, float dt)
     vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
 }
 
+// ------------------------------------------------------------------ mouse joint
+// b2MouseJoint (Dynamics/Joints/b2MouseJoint.cpp:33-205): a soft spring pulling a point of body B to
+// a target, force bounded by maxForce; body B's angular velocity is damped by 2% at each solve.
+__device__ void MouseInit(const Wd& W, Joint& j, float4* pos, float4* vel, bool warmStarting, float dtRatio, float dt)
+{
+    const float4 mB4 = W.mas[j.bodyB];
+    j.localCenterB = V(mB4.z, mB4.w);
+    j.invMassB = mB4.x; j.invIB = mB4.y;
+    const float4 pb = pos[j.indexB], vb = vel[j.indexB];
+    const Vec2 cB = V(pb.x, pb.y);
+    Vec2 vB = V(vb.x, vb.y);
+    float wB = vb.z;
+    const Rot qB = RotOf(pb.z);
+    const float mass = W.prop[j.bodyB].w;
+    const float omega = 2.0f * kPi * j.frequencyHz;
+    const float d = 2.0f * mass * j.dampingRatio * omega;
+    const float k = mass * (omega * omega);
+    const float h = dt;
+    j.gamma = h * (d + h * k);
+    if (j.gamma != 0.0f) j.gamma = 1.0f / j.gamma;
+    j.beta = h * k * j.gamma;
+    j.rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    float K[4];
+    K[0] = j.invMassB + j.invIB * j.rB.y * j.rB.y + j.gamma;
+    K[1] = -j.invIB * j.rB.x * j.rB.y;
+    K[2] = K[1];
+    K[3] = j.invMassB + j.invIB * j.rB.x * j.rB.x + j.gamma;
+    Mat22Inverse(K, j.mass);
+    j.mouseC = cB + j.rB - j.target;
+    j.mouseC.x *= j.beta;
+    j.mouseC.y *= j.beta;
+    wB *= 0.98f;
+    if (warmStarting) {
+        j.impulse[0] *= dtRatio;
+        j.impulse[1] *= dtRatio;
+        const Vec2 I = V(j.impulse[0], j.impulse[1]);
+        vB = vB + j.invMassB * I;
+        wB += j.invIB * Cross(j.rB, I);
+    } else {
+        j.impulse[0] = j.impulse[1] = 0.0f;
+    }
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
+__device__ void MouseSolveVelocity(Joint& j, float4* vel, float dt)
+{
+    const float4 vb = vel[j.indexB];
+    Vec2 vB = V(vb.x, vb.y);
+    float wB = vb.z;
+    const Vec2 Cdot = vB + Cross(wB, j.rB);
+    const Vec2 oldImpulse = V(j.impulse[0], j.impulse[1]);
+    const Vec2 rhs = -(Cdot + j.mouseC + j.gamma * oldImpulse);
+    const float* M = j.mass;
+    Vec2 impulse = V(M[0] * rhs.x + M[2] * rhs.y, M[1] * rhs.x + M[3] * rhs.y);
+    Vec2 total = oldImpulse + impulse;
+    const float maxImpulse = dt * j.maxForce;
+    if (LengthSq(total) > maxImpulse * maxImpulse) {
+        const float s = maxImpulse / Length(total);
+        total.x *= s;
+        total.y *= s;
+    }
+    j.impulse[0] = total.x;
+    j.impulse[1] = total.y;
+    impulse = total - oldImpulse;
+    vB = vB + j.invMassB * impulse;
+    wB += j.invIB * Cross(j.rB, impulse);
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
+// ------------------------------------------------------------------ pulley joint
+// b2PulleyJoint (Dynamics/Joints/b2PulleyJoint.cpp:53-275): lengthA + ratio * lengthB stays constant.
+// The anchor-to-ground-anchor unit vectors of bodies A and B (zero when shorter than 10 linear slops).
+__device__ inline void PulleyAxes(const Joint& j, Vec2 cA, Vec2 rA, Vec2 cB, Vec2 rB, Vec2& uA, Vec2& uB,
+                                  float& lengthA, float& lengthB)
+{
+    uA = cA + rA - j.groundAnchorA;
+    uB = cB + rB - j.groundAnchorB;
+    lengthA = Length(uA);
+    lengthB = Length(uB);
+    if (lengthA > 10.0f * kLinearSlop) {
+        const float inv = 1.0f / lengthA;
+        uA.x *= inv;
+        uA.y *= inv;
+    } else {
+        uA = V(0.0f, 0.0f);
+    }
+    if (lengthB > 10.0f * kLinearSlop) {
+        const float inv = 1.0f / lengthB;
+        uB.x *= inv;
+        uB.y *= inv;
+    } else {
+        uB = V(0.0f, 0.0f);
+    }
+}
+
+__device__ void PulleyInit(const Wd& W, Joint& j, float4* pos, float4* vel, bool warmStarting, float dtRatio)
+{
+    const float4 mA4 = W.mas[j.bodyA], mB4 = W.mas[j.bodyB];
+    j.localCenterA = V(mA4.z, mA4.w); j.localCenterB = V(mB4.z, mB4.w);
+    j.invMassA = mA4.x; j.invMassB = mB4.x; j.invIA = mA4.y; j.invIB = mB4.y;
+    const float4 pa = pos[j.indexA], pb = pos[j.indexB], va = vel[j.indexA], vb = vel[j.indexB];
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const Rot qA = RotOf(pa.z), qB = RotOf(pb.z);
+    j.rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    j.rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    float lengthA, lengthB;
+    PulleyAxes(j, V(pa.x, pa.y), j.rA, V(pb.x, pb.y), j.rB, j.uA, j.uB, lengthA, lengthB);
+    const float ruA = Cross(j.rA, j.uA), ruB = Cross(j.rB, j.uB);
+    const float mA = j.invMassA + j.invIA * ruA * ruA;
+    const float mB = j.invMassB + j.invIB * ruB * ruB;
+    j.motorMass = mA + j.ratio * j.ratio * mB;
+    if (j.motorMass > 0.0f) j.motorMass = 1.0f / j.motorMass;
+    if (warmStarting) {
+        j.impulse[0] *= dtRatio;
+        const Vec2 PA = -(j.impulse[0]) * j.uA;
+        const Vec2 PB = (-j.ratio * j.impulse[0]) * j.uB;
+        vA = vA + j.invMassA * PA;
+        wA += j.invIA * Cross(j.rA, PA);
+        vB = vB + j.invMassB * PB;
+        wB += j.invIB * Cross(j.rB, PB);
+    } else {
+        j.impulse[0] = 0.0f;
+    }
+    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
+__device__ void PulleySolveVelocity(Joint& j, float4* vel)
+{
+    const float4 va = vel[j.indexA], vb = vel[j.indexB];
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y);
+    float wA = va.z, wB = vb.z;
+    const Vec2 vpA = vA + Cross(wA, j.rA);
+    const Vec2 vpB = vB + Cross(wB, j.rB);
+    const float Cdot = -Dot(j.uA, vpA) - j.ratio * Dot(j.uB, vpB);
+    const float impulse = -j.motorMass * Cdot;
+    j.impulse[0] += impulse;
+    const Vec2 PA = -impulse * j.uA;
+    const Vec2 PB = -j.ratio * impulse * j.uB;
+    vA = vA + j.invMassA * PA;
+    wA += j.invIA * Cross(j.rA, PA);
+    vB = vB + j.invMassB * PB;
+    wB += j.invIB * Cross(j.rB, PB);
+    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+}
+
+__device__ bool PulleySolvePosition(Joint& j, float4* pos)
+{
+    const float4 pa = pos[j.indexA], pb = pos[j.indexB];
+    Vec2 cA = V(pa.x, pa.y), cB = V(pb.x, pb.y);
+    float aA = pa.z, aB = pb.z;
+    const Rot qA = RotOf(aA), qB = RotOf(aB);
+    const Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
+    const Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    Vec2 uA, uB;
+    float lengthA, lengthB;
+    PulleyAxes(j, cA, rA, cB, rB, uA, uB, lengthA, lengthB);
+    const float ruA = Cross(rA, uA), ruB = Cross(rB, uB);
+    const float mA = j.invMassA + j.invIA * ruA * ruA;
+    const float mB = j.invMassB + j.invIB * ruB * ruB;
+    float mass = mA + j.ratio * j.ratio * mB;
+    if (mass > 0.0f) mass = 1.0f / mass;
+    const float C = j.pulleyConstant - lengthA - j.ratio * lengthB;
+    const float linearError = Absf(C);
+    const float impulse = -mass * C;
+    const Vec2 PA = -impulse * uA;
+    const Vec2 PB = -j.ratio * impulse * uB;
+    cA = cA + j.invMassA * PA;
+    aA += j.invIA * Cross(rA, PA);
+    cB = cB + j.invMassB * PB;
+    aB += j.invIB * Cross(rB, PB);
+    pos[j.indexA] = make_float4(cA.x, cA.y, aA, 0.0f);
+    pos[j.indexB] = make_float4(cB.x, cB.y, aB, 0.0f);
+    return linearError < kLinearSlop;
+}
+
 // ------------------------------------------------------------------ joint dispatch
 __device__ void JointInit(const Wd& W, Joint& j, float4* pos, float4* vel, bool warmStarting, float dtRatio, float dt)
 {
     if (j.type == kJointWheel) WheelInit(W, j, pos, vel, warmStarting, dtRatio, dt);
+    else if (j.type == kJointMouse) MouseInit(W, j, pos, vel, warmStarting, dtRatio, dt);
+    else if (j.type == kJointPulley) PulleyInit(W, j, pos, vel, warmStarting, dtRatio);
     else if (j.type == kJointRope) RopeInit(W, j, pos, vel, warmStarting, dtRatio);
     else if (j.type == kJointFriction || j.type == kJointMotor) FrictionMotorInit(W, j, pos, vel, warmStarting, dtRatio);
     else if (j.type == kJointDistance) DistInit(W, j, pos, vel, warmStarting, dtRatio, dt);
@@ -1365,6 +1545,8 @@ __device__ void JointInit(const Wd& W, Joint& j, float4* pos, float4* vel, bool 
 __device__ void JointSolveVelocity(Joint& j, float4* vel, float dt)
 {
     if (j.type == kJointWheel) WheelSolveVelocity(j, vel, dt);
+    else if (j.type == kJointMouse) MouseSolveVelocity(j, vel, dt);
+    else if (j.type == kJointPulley) PulleySolveVelocity(j, vel);
     else if (j.type == kJointRope) RopeSolveVelocity(j, vel, dt);
     else if (j.type == kJointFriction || j.type == kJointMotor) FrictionMotorSolveVelocity(j, vel, dt);
     else if (j.type == kJointDistance) DistSolveVelocity(j, vel);
@@ -1375,6 +1557,8 @@ __device__ void JointSolveVelocity(Joint& j, float4* vel, float dt)
 __device__ bool JointSolvePosition(Joint& j, float4* pos)
 {
     if (j.type == kJointWheel) return WheelSolvePosition(j, pos);
+    if (j.type == kJointMouse) return true;
+    if (j.type == kJointPulley) return PulleySolvePosition(j, pos);
     if (j.type == kJointRope) return RopeSolvePosition(j, pos);
     if (j.type == kJointFriction || j.type == kJointMotor) return true;
     if (j.type == kJointDistance) return DistSolvePosition(j, pos);

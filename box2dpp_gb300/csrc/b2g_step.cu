@@ -382,6 +382,13 @@ struct Wd {
     // 419-441 and b2Body.h:501-830), with the reference's type checks, wakes and sleep rules.
     __device__ void applyEdit(const BodyEdit& e)
     {
+        if (e.op == kEditMouseTarget) {
+            // b2MouseJoint::SetTarget (Dynamics/Joints/b2MouseJoint.cpp:54-61): wakes body B
+            Joint& J = jt[e.body];
+            if (!awake(J.bodyB)) setAwake(J.bodyB, true);
+            J.target = V(e.v[0], e.v[1]);
+            return;
+        }
         const int b = e.body;
         const int type = bi[b].x;
         auto wakeOnRequest = [&]() {

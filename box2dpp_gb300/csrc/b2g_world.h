@@ -82,7 +82,7 @@ struct WorldState {
 
 // Joint types (b2JointType, Dynamics/Joints/b2Joint.h:28-42, those built here).
 enum : int { kJointRevolute = 0, kJointDistance = 1, kJointWeld = 2, kJointPrismatic = 3, kJointWheel = 4,
-             kJointRope = 5, kJointFriction = 6, kJointMotor = 7, kJointTypes };
+             kJointRope = 5, kJointFriction = 6, kJointMotor = 7, kJointMouse = 8, kJointPulley = 9, kJointTypes };
 
 // A joint (Dynamics/Joints/b2RevoluteJoint.h, b2DistanceJoint.h, b2WeldJoint.h), stored whole: joints
 // are few. Fields a type does not use stay zero; the distance joint keeps its scalar impulse in
@@ -124,6 +124,14 @@ struct Joint {
     float maxForce, maxTorque;
     Vec2 linearOffset, linearError;           // motor
     float angularOffset, angularError, correctionFactor;
+    // mouse (b2MouseJoint.h): target point (world), this step's position error; maxForce, the spring
+    // in frequencyHz / dampingRatio, the 2x2 mass in mass[0..3], the impulse in impulse[0..1]
+    Vec2 target, mouseC;
+    float beta;
+    // pulley (b2PulleyJoint.h): ground anchors, lengths, ratio, constant; this step's unit vectors
+    // uA, uB; the impulse in impulse[0], mass in motorMass
+    Vec2 groundAnchorA, groundAnchorB, uA, uB;
+    float lengthA, lengthB, ratio, pulleyConstant;
 };
 
 // Island solver records: the fields of b2ContactVelocityConstraint and b2ContactPositionConstraint
@@ -240,7 +248,8 @@ struct Batch {
 
 // A b2Body state change between steps (the device copy of the C-ABI's gb_body_edit, same layout).
 enum : int { kEditSetTransform = 0, kEditSetLinearVelocity, kEditSetAngularVelocity, kEditSetAwake, kEditApplyForce,
-             kEditApplyForceToCenter, kEditApplyTorque, kEditApplyLinearImpulse, kEditApplyAngularImpulse, kEditOps };
+             kEditApplyForceToCenter, kEditApplyTorque, kEditApplyLinearImpulse, kEditApplyAngularImpulse,
+             kEditMouseTarget, kEditOps };
 struct BodyEdit {
     int world, body, op, wake;
     float v[4];

@@ -35,7 +35,7 @@ import numpy as np
 STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 # shape encodings of the bulk build call
 CIRCLE, EDGE, POLYGON, BOX = 0, 1, 2, 3
-REVOLUTE, DISTANCE, WELD, PRISMATIC, WHEEL, ROPE, FRICTION, MOTOR = 0, 1, 2, 3, 4, 5, 6, 7
+REVOLUTE, DISTANCE, WELD, PRISMATIC, WHEEL, ROPE, FRICTION, MOTOR, MOUSE, PULLEY = 0, 1, 2, 3, 4, 5, 6, 7, 8, 9
 DEFAULT_FLAGS = 1 | 2 | 16  # allowSleep, awake, active
 
 
@@ -131,6 +131,20 @@ class Scene:
         """b2MotorJointDef: drives body B to linear_offset and angular_offset in body A's frame."""
         self.joints.append((a, b, [linear_offset[0], linear_offset[1], angular_offset, max_force, max_torque,
                                    correction_factor] + [0.0] * 6, flags, MOTOR))
+        return len(self.joints) - 1
+
+    def mouse(self, a, b, target, max_force, frequency_hz=5.0, damping_ratio=0.7, flags=0) -> int:
+        """b2MouseJointDef: body B's point under `target` (world) is pulled to the target, which
+        gb_body_edits' mouse-target op moves between steps; body A is normally a static body."""
+        self.joints.append((a, b, [target[0], target[1], max_force, frequency_hz, damping_ratio] + [0.0] * 7,
+                            flags, MOUSE))
+        return len(self.joints) - 1
+
+    def pulley(self, a, b, ground_a, ground_b, anchor_a, anchor_b, length_a, length_b, ratio=1.0, flags=4) -> int:
+        """b2PulleyJointDef: length_a + ratio * length_b stays constant; anchors local to each body,
+        ground anchors in world coordinates (the def's default collideConnected is true)."""
+        self.joints.append((a, b, [ground_a[0], ground_a[1], ground_b[0], ground_b[1], anchor_a[0], anchor_a[1],
+                                   anchor_b[0], anchor_b[1], length_a, length_b, ratio, 0.0], flags, PULLEY))
         return len(self.joints) - 1
 
     def prismatic(self, a, b, anchor_a, anchor_b, axis, ref_angle=0.0, lower=0.0, upper=0.0, max_motor_force=0.0,
@@ -422,6 +436,43 @@ def joint_zoo(rng: SplitMix64, allow_sleep: bool = True) -> Scene:
         b = s.body(DYNAMIC, _q(-12.0 + 5.0 * i + rng.uniform(-0.5, 0.5)), _q(6.0 + rng.uniform(0.0, 3.0)),
                    angle=_q(rng.uniform(-0.5, 0.5)))
         s.fixture(b, CIRCLE if i % 2 else BOX, [0.0, 0.0, 0.35] if i % 2 else [0.35, 0.35], 1 if i % 2 else 2,
+                  density=1.0, friction=0.5)
+    return _settings(s, allow_sleep)
+
+
+def pulley_mouse(rng: SplitMix64, allow_sleep: bool = True) -> Scene:
+    """Pulley and mouse joints: two pulleys (ratios 1.5 and 1) whose boxes swing, load each other and
+    land, boxes falling onto the pulley boxes, and two bodies hung on mouse joints (a stiff one and one
+    whose force bound the load exceeds). The mouse joints are joints 2 and 3."""
+    s = Scene(name="pulley_mouse")
+    g = s.body(STATIC, 0.0, 0.0)
+    s.fixture(g, EDGE, [-30.0, 0.0, 30.0, 0.0, 0, 0, 0, 0, 0, 0], friction=0.6)
+    # pulley 1: box A (2 kg) below ground anchor (-10, 20), box B (2 kg) below (-4, 20), ratio 1.5;
+    # anchors at the boxes' tops, lengths 7 and 5
+    a = s.body(DYNAMIC, -10.0, 12.0)
+    s.fixture(a, BOX, [1.0, 1.0], 2, density=0.5)
+    b = s.body(DYNAMIC, -4.0, 14.0, vx=0.5)
+    s.fixture(b, BOX, [0.5, 1.0], 2, density=1.0)
+    s.pulley(a, b, (-10.0, 20.0), (-4.0, 20.0), (0.0, 1.0), (0.0, 1.0), 7.0, 5.0, 1.5)
+    # pulley 2: a circle and a box, ratio 1, the box off-centre so it rotates
+    c = s.body(DYNAMIC, 4.0, 10.0)
+    s.fixture(c, CIRCLE, [0.0, 0.0, 0.6], 1, density=1.0)
+    d = s.body(DYNAMIC, 9.0, 8.0, angle=0.25)
+    s.fixture(d, BOX, [0.6, 0.4], 2, density=2.0)
+    s.pulley(c, d, (4.0, 18.0), (9.0, 18.0), (0.0, 0.0), (0.3, 0.4), 8.0, 10.0, 1.0)
+    # mouse joints on a fixture-less static anchor (a joint to the ground body would filter the
+    # ground contacts): a box held at a point of it, and a circle on a weak one that sags
+    anchor = s.body(STATIC, 0.0, 0.0)
+    m = s.body(DYNAMIC, 16.0, 6.0, angle=0.1)
+    s.fixture(m, BOX, [0.5, 0.5], 2, density=1.0)
+    s.mouse(anchor, m, (16.25, 6.25), 1000.0)
+    n = s.body(DYNAMIC, 20.0, 7.0)
+    s.fixture(n, CIRCLE, [0.0, 0.0, 0.5], 1, density=1.0)
+    s.mouse(anchor, n, (20.0, 7.5), 6.0, 2.0, 0.3)
+    for i in range(6):
+        x = _q((-10.0, -4.0, 4.0, 9.0, 16.0, -7.0)[i] + rng.uniform(-0.3, 0.3))
+        e = s.body(DYNAMIC, x, _q(16.0 + 2.0 * i + rng.uniform(0.0, 1.0)), angle=_q(rng.uniform(-0.4, 0.4)))
+        s.fixture(e, CIRCLE if i % 2 else BOX, [0.0, 0.0, 0.3] if i % 2 else [0.3, 0.3], 1 if i % 2 else 2,
                   density=1.0, friction=0.5)
     return _settings(s, allow_sleep)
 

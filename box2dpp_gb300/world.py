@@ -232,7 +232,8 @@ class World:
 
     def body_edits(self, edits) -> None:
         """b2Body state changes before the next step, in order: edits is a sequence of (world, body,
-        op name or code, values, wake) with op names from _lib.EDIT_OPS (see gb_body_edits)."""
+        op name or code, values, wake) with op names from _lib.EDIT_OPS (see gb_body_edits); for
+        "mouse_target" the body field is the mouse joint's index and values the new world target."""
         arr = np.zeros(len(edits), dtype=_lib.EDIT_DTYPE)
         for i, (w, b, op, vals, wake) in enumerate(edits):
             arr[i]["world"], arr[i]["body"] = w, b

@@ -73,7 +73,7 @@ gb_status gb_create_revolute_joints(gb_world* world, int w, int n, const int* bo
 /* b2World::CreateJoint for the joint definitions built here (Box2D/Dynamics/b2World.cpp:185;
  * Box2D/Dynamics/Joints/b2RevoluteJoint.h:36, b2DistanceJoint.h:30, b2WeldJoint.h:28,
  * b2PrismaticJoint.h:30, b2WheelJoint.h:30, b2RopeJoint.h:28, b2FrictionJoint.h:25,
- * b2MotorJoint.h:26). type: GB_JOINT_*. f[GB_JOINT_FLOATS] per joint (the fields of the definition;
+ * b2MotorJoint.h:26, b2MouseJoint.h:24, b2PulleyJoint.h:26). type: GB_JOINT_*. f[GB_JOINT_FLOATS] per joint (the fields of the definition;
  * anchors and axes in body-local coordinates):
  *   revolute   localAnchorA.x, .y, localAnchorB.x, .y, referenceAngle, lowerAngle, upperAngle,
  *              motorSpeed, maxMotorTorque (as gb_create_revolute_joints)
@@ -87,6 +87,10 @@ gb_status gb_create_revolute_joints(gb_world* world, int w, int n, const int* bo
  *   rope       localAnchorA.x, .y, localAnchorB.x, .y, maxLength
  *   friction   localAnchorA.x, .y, localAnchorB.x, .y, maxForce, maxTorque
  *   motor      linearOffset.x, .y, angularOffset, maxForce, maxTorque, correctionFactor
+ *   mouse      target.x, .y (world; body B's local anchor is the target's point on B at creation),
+ *              maxForce, frequencyHz, dampingRatio (body A is normally a static body)
+ *   pulley     groundAnchorA.x, .y, groundAnchorB.x, .y (world), localAnchorA.x, .y, localAnchorB.x,
+ *              .y, lengthA, lengthB, ratio (non-zero)
  * Unused trailing floats are ignored. flags: 1 enableLimit (revolute, prismatic), 2 enableMotor
  * (revolute, prismatic, wheel), 4 collideConnected. */
 #define GB_JOINT_REVOLUTE 0
@@ -97,6 +101,8 @@ gb_status gb_create_revolute_joints(gb_world* world, int w, int n, const int* bo
 #define GB_JOINT_ROPE 5
 #define GB_JOINT_FRICTION 6
 #define GB_JOINT_MOTOR 7
+#define GB_JOINT_MOUSE 8
+#define GB_JOINT_PULLEY 9
 #define GB_JOINT_FLOATS 12
 gb_status gb_create_joints(gb_world* world, int w, int n, const int* type, const int* body_a, const int* body_b,
                            const float* f, const int* flags, int* out_ids);
@@ -263,6 +269,8 @@ gb_status gb_world_stage_times(gb_world* world, float dt, int velocity_iteration
 #define GB_EDIT_APPLY_TORQUE 6         /* v: torque */
 #define GB_EDIT_APPLY_LINEAR_IMPULSE 7 /* v: impulse.x, impulse.y, point.x, point.y (world) */
 #define GB_EDIT_APPLY_ANGULAR_IMPULSE 8 /* v: impulse */
+#define GB_EDIT_MOUSE_TARGET 9         /* b2MouseJoint::SetTarget (b2MouseJoint.cpp:54): body is the
+                                          joint index, v: target.x, target.y (world); wakes body B */
 typedef struct gb_body_edit {
     int world;  /* world index in the batch */
     int body;   /* body index (creation order) */

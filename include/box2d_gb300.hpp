@@ -296,6 +296,29 @@ struct b2MotorJointDef {
     float maxForce = 1.0f, maxTorque = 1.0f, correctionFactor = 0.3f;
 };
 
+// b2MouseJointDef (Box2D/Dynamics/Joints/b2MouseJoint.h:28-56): body B's point under `target` is
+// pulled to the target, which b2MouseJoint::SetTarget moves between steps
+struct b2MouseJointDef {
+    b2Body* bodyA = nullptr;
+    b2Body* bodyB = nullptr;
+    bool collideConnected = false;
+    b2Vec2 target;
+    float maxForce = 0.0f, frequencyHz = 5.0f, dampingRatio = 0.7f;
+};
+
+// b2PulleyJointDef (Box2D/Dynamics/Joints/b2PulleyJoint.h:30-72): lengthA + ratio * lengthB constant
+struct b2PulleyJointDef {
+    b2Body* bodyA = nullptr;
+    b2Body* bodyB = nullptr;
+    bool collideConnected = true;
+    b2Vec2 groundAnchorA{-1.0f, 1.0f}, groundAnchorB{1.0f, 1.0f};
+    b2Vec2 localAnchorA{-1.0f, 0.0f}, localAnchorB{1.0f, 0.0f};
+    float lengthA = 0.0f, lengthB = 0.0f, ratio = 1.0f;
+    // b2PulleyJointDef::Initialize (b2PulleyJoint.cpp:37-51): anchors given in world coordinates
+    void Initialize(b2Body* bA, b2Body* bB, const b2Vec2& groundA, const b2Vec2& groundB, const b2Vec2& anchorA,
+                    const b2Vec2& anchorB, float r);
+};
+
 // b2PrismaticJointDef (Box2D/Dynamics/Joints/b2PrismaticJoint.h:30-88)
 struct b2PrismaticJointDef {
     b2Body* bodyA = nullptr;
@@ -312,14 +335,28 @@ struct b2PrismaticJointDef {
 
 class b2Joint {
 public:
+    virtual ~b2Joint() = default;
     int GetIndex() const { return m_index; }
     b2Body* GetBodyA() const { return m_a; }
     b2Body* GetBodyB() const { return m_b; }
 
-private:
+protected:
     friend class b2World;
     int m_index = -1;
     b2Body *m_a = nullptr, *m_b = nullptr;
+    b2World* m_world = nullptr;
+};
+
+// b2MouseJoint (Box2D/Dynamics/Joints/b2MouseJoint.h:63-124): what CreateJoint returns for a
+// b2MouseJointDef, so the reference's static_cast<b2MouseJoint*> and SetTarget read the same.
+class b2MouseJoint : public b2Joint {
+public:
+    void SetTarget(const b2Vec2& target);  // one gb_body_edits record (GB_EDIT_MOUSE_TARGET)
+    const b2Vec2& GetTarget() const { return m_target; }
+
+private:
+    friend class b2World;
+    b2Vec2 m_target;
 };
 
 struct b2ManifoldPoint {
@@ -414,6 +451,7 @@ public:
         int id = -1;
         if (gb_create_revolute_joints(m_h, 0, 1, &a, &b, f, &flags, &id) != GB_OK) return nullptr;
         std::unique_ptr<b2Joint> j(new b2Joint());
+        j->m_world = this;
         j->m_index = id;
         j->m_a = def->bodyA;
         j->m_b = def->bodyB;
@@ -459,6 +497,22 @@ public:
         const float f[GB_JOINT_FLOATS] = {def->linearOffset.x, def->linearOffset.y, def->angularOffset, def->maxForce,
                                           def->maxTorque, def->correctionFactor};
         return AddJoint(GB_JOINT_MOTOR, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
+    }
+    b2Joint* CreateJoint(const b2MouseJointDef* def)
+    {
+        const float f[GB_JOINT_FLOATS] = {def->target.x, def->target.y, def->maxForce, def->frequencyHz,
+                                          def->dampingRatio};
+        std::unique_ptr<b2MouseJoint> j(new b2MouseJoint());
+        j->m_target = def->target;
+        return AddJoint(GB_JOINT_MOUSE, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(j));
+    }
+    b2Joint* CreateJoint(const b2PulleyJointDef* def)
+    {
+        const float f[GB_JOINT_FLOATS] = {def->groundAnchorA.x, def->groundAnchorA.y, def->groundAnchorB.x,
+                                          def->groundAnchorB.y, def->localAnchorA.x, def->localAnchorA.y,
+                                          def->localAnchorB.x, def->localAnchorB.y, def->lengthA, def->lengthB,
+                                          def->ratio};
+        return AddJoint(GB_JOINT_PULLEY, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
     }
     b2Joint* CreateJoint(const b2PrismaticJointDef* def)
     {
@@ -544,13 +598,15 @@ public:
     }
 
 private:
-    b2Joint* AddJoint(int type, b2Body* a, b2Body* b, const float* f, int flags)
+    b2Joint* AddJoint(int type, b2Body* a, b2Body* b, const float* f, int flags,
+                      std::unique_ptr<b2Joint> j = nullptr)
     {
         if (!Handle() || !a || !b) return nullptr;
         const int ia = a->m_index, ib = b->m_index;
         int id = -1;
         if (gb_create_joints(m_h, 0, 1, &type, &ia, &ib, f, &flags, &id) != GB_OK) return nullptr;
-        std::unique_ptr<b2Joint> j(new b2Joint());
+        if (!j) j.reset(new b2Joint());
+        j->m_world = this;
         j->m_index = id;
         j->m_a = a;
         j->m_b = b;
@@ -657,5 +713,32 @@ inline void b2Body::ApplyForceToCenter(const b2Vec2& f, bool wake) { m_world->Ed
 inline void b2Body::ApplyTorque(float torque, bool wake) { m_world->Edit(m_index, GB_EDIT_APPLY_TORQUE, torque, 0.0f, 0.0f, 0.0f, wake); }
 inline void b2Body::ApplyLinearImpulse(const b2Vec2& i, const b2Vec2& p, bool wake) { m_world->Edit(m_index, GB_EDIT_APPLY_LINEAR_IMPULSE, i.x, i.y, p.x, p.y, wake); }
 inline void b2Body::ApplyAngularImpulse(float impulse, bool wake) { m_world->Edit(m_index, GB_EDIT_APPLY_ANGULAR_IMPULSE, impulse, 0.0f, 0.0f, 0.0f, wake); }
+
+inline void b2MouseJoint::SetTarget(const b2Vec2& target)
+{
+    m_target = target;
+    m_world->Edit(m_index, GB_EDIT_MOUSE_TARGET, target.x, target.y, 0.0f, 0.0f, true);
+}
+
+inline void b2PulleyJointDef::Initialize(b2Body* bA, b2Body* bB, const b2Vec2& groundA, const b2Vec2& groundB,
+                                         const b2Vec2& anchorA, const b2Vec2& anchorB, float r)
+{
+    // the anchors in each body's frame (the transpose of its rotation applied to anchor - position)
+    auto local = [](const b2Transform& t, const b2Vec2& p) {
+        const float dx = p.x - t.p.x, dy = p.y - t.p.y;
+        return b2Vec2(t.q.c * dx + t.q.s * dy, -t.q.s * dx + t.q.c * dy);
+    };
+    bodyA = bA;
+    bodyB = bB;
+    groundAnchorA = groundA;
+    groundAnchorB = groundB;
+    localAnchorA = local(bA->GetTransform(), anchorA);
+    localAnchorB = local(bB->GetTransform(), anchorB);
+    const float ax = anchorA.x - groundA.x, ay = anchorA.y - groundA.y;
+    const float bx = anchorB.x - groundB.x, by = anchorB.y - groundB.y;
+    lengthA = std::sqrt(ax * ax + ay * ay);
+    lengthB = std::sqrt(bx * bx + by * by);
+    ratio = r;
+}
 
 } // namespace box2d

@@ -155,6 +155,24 @@ int World::CreateJoint(int type, int a, int b, const float* f, int fl)
         j.frequencyHz = f[8];
         j.dampingRatio = f[9];
         j.enableMotor = (fl & 2) != 0;
+    } else if (type == kMouseJoint) {
+        // b2MouseJoint::b2MouseJoint (b2MouseJoint.cpp:33-52): body B's point under the target
+        j.target = V(f[0], f[1]);
+        j.localAnchorA = V(0.0f, 0.0f);
+        j.localAnchorB = MulT(bodies[b].xf, j.target);
+        j.maxForce = f[2];
+        j.frequencyHz = f[3];
+        j.dampingRatio = f[4];
+    } else if (type == kPulleyJoint) {
+        // b2PulleyJoint::b2PulleyJoint (b2PulleyJoint.cpp:53-69)
+        j.groundAnchorA = V(f[0], f[1]);
+        j.groundAnchorB = V(f[2], f[3]);
+        j.localAnchorA = V(f[4], f[5]);
+        j.localAnchorB = V(f[6], f[7]);
+        j.lengthA = f[8];
+        j.lengthB = f[9];
+        j.ratio = f[10];
+        j.pulleyConstant = f[8] + j.ratio * f[9];
     } else if (type == kRopeJoint) {
         j.maxLength = f[4];
     } else if (type == kFrictionJoint) {
@@ -305,6 +323,13 @@ void World::SynchronizeFixturesFrom(int bi, const Xf& xf1, const Xf& xf2)
 // ApplyTorque, ApplyLinearImpulse, ApplyAngularImpulse (b2Body.h:739-830). op: the C-ABI's GB_EDIT_*.
 void World::ApplyEdit(int op, int bi, int wake, const float* v)
 {
+    if (op == 9) {
+        // b2MouseJoint::SetTarget (b2MouseJoint.cpp:54-61); bi is the joint
+        Joint& j = joints[bi];
+        if ((bodies[j.bodyB].flags & kBAwake) == 0) SetAwake(j.bodyB, true);
+        j.target = V(v[0], v[1]);
+        return;
+    }
     Body& b = bodies[bi];
     auto wakeOnRequest = [&]() {
         if (wake && (b.flags & kBAwake) == 0) SetAwake(bi, true);
@@ -1032,6 +1057,11 @@ void RopeInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity*
 void RopeSolveVelocity(Joint& j, const StepInfo& step, Velocity* vel);
 bool RopeSolvePosition(Joint& j, Position* pos);
 void FrictionMotorInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel);
+void MouseInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel);
+void MouseSolveVelocity(Joint& j, const StepInfo& step, Velocity* vel);
+void PulleyInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel);
+void PulleySolveVelocity(Joint& j, Velocity* vel);
+bool PulleySolvePosition(Joint& j, Position* pos);
 void FrictionMotorSolveVelocity(Joint& j, const StepInfo& step, Velocity* vel);
 
 // b2Mat33::Solve33 / Solve22 (Common/b2Math.cpp:24-56)
@@ -2002,6 +2032,179 @@ void FrictionMotorSolveVelocity(Joint& j, const StepInfo& step, Velocity* vel)
     vel[j.indexB].v = vB; vel[j.indexB].w = wB;
 }
 
+// ---------------------------------------------------------------- mouse joint
+// b2MouseJoint::InitVelocityConstraints (Dynamics/Joints/b2MouseJoint.cpp:95-166): the spring's gamma
+// and beta from body B's mass, the 2x2 soft mass, the scaled position error, 2% angular damping of
+// body B, warm start.
+void MouseInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel)
+{
+    const Body& B = w->bodies[j.bodyB];
+    j.indexB = B.islandIndex;
+    j.localCenterB = B.sweep.localCenter;
+    j.invMassB = B.invMass;
+    j.invIB = B.invI;
+    const Vec2 cB = pos[j.indexB].c;
+    const Rot qB = RotOf(pos[j.indexB].a);
+    Vec2 vB = vel[j.indexB].v;
+    float wB = vel[j.indexB].w;
+    const float omega = 2.0f * kPi * j.frequencyHz;
+    const float dampC = 2.0f * B.mass * j.dampingRatio * omega;
+    const float stiff = B.mass * (omega * omega);
+    const float h = step.dt;
+    j.gamma = h * (dampC + h * stiff);
+    if (j.gamma != 0.0f) j.gamma = 1.0f / j.gamma;
+    j.beta = h * stiff * j.gamma;
+    j.rB = Mul(qB, j.localAnchorB - j.localCenterB);
+    const float kexx = j.invMassB + j.invIB * j.rB.y * j.rB.y + j.gamma;
+    const float kexy = -j.invIB * j.rB.x * j.rB.y;
+    const float keyx = kexy;
+    const float keyy = j.invMassB + j.invIB * j.rB.x * j.rB.x + j.gamma;
+    float det = kexx * keyy - keyx * kexy;
+    if (det != 0.0f) det = 1.0f / det;
+    j.mass[0] = det * keyy; j.mass[2] = -det * keyx;
+    j.mass[1] = -det * kexy; j.mass[3] = det * kexx;
+    j.mouseC = cB + j.rB - j.target;
+    j.mouseC.x *= j.beta;
+    j.mouseC.y *= j.beta;
+    wB *= 0.98f;
+    if (step.warmStarting) {
+        j.impulse[0] *= step.dtRatio;
+        j.impulse[1] *= step.dtRatio;
+        const Vec2 P = V(j.impulse[0], j.impulse[1]);
+        vB = vB + j.invMassB * P;
+        wB += j.invIB * Cross(j.rB, P);
+    } else {
+        j.impulse[0] = j.impulse[1] = 0.0f;
+    }
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+}
+
+// b2MouseJoint::SolveVelocityConstraints (b2MouseJoint.cpp:168-192): the accumulated impulse is
+// rescaled to length dt * maxForce when longer.
+void MouseSolveVelocity(Joint& j, const StepInfo& step, Velocity* vel)
+{
+    Vec2 vB = vel[j.indexB].v;
+    float wB = vel[j.indexB].w;
+    const Vec2 Cdot = vB + Cross(wB, j.rB);
+    const Vec2 old = V(j.impulse[0], j.impulse[1]);
+    const Vec2 rhs = -(Cdot + j.mouseC + j.gamma * old);
+    const float* M = j.mass;
+    const Vec2 d = V(M[0] * rhs.x + M[2] * rhs.y, M[1] * rhs.x + M[3] * rhs.y);
+    Vec2 acc = old + d;
+    const float maxImpulse = step.dt * j.maxForce;
+    if (LengthSq(acc) > maxImpulse * maxImpulse) {
+        const float scale = maxImpulse / Length(acc);
+        acc.x *= scale;
+        acc.y *= scale;
+    }
+    j.impulse[0] = acc.x;
+    j.impulse[1] = acc.y;
+    const Vec2 applied = acc - old;
+    vB = vB + j.invMassB * applied;
+    wB += j.invIB * Cross(j.rB, applied);
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+}
+
+// ---------------------------------------------------------------- pulley joint
+// The unit vectors from the ground anchors to the body anchors, zero below 10 linear slops
+// (b2PulleyJoint.cpp:99-121 and 218-240).
+static void PulleyUnit(Vec2 c, Vec2 r, Vec2 ground, Vec2& u, float& len)
+{
+    u = c + r - ground;
+    len = Length(u);
+    if (len > 10.0f * kLinearSlop) {
+        const float inv = 1.0f / len;
+        u.x *= inv;
+        u.y *= inv;
+    } else {
+        u = V(0.0f, 0.0f);
+    }
+}
+
+// b2PulleyJoint::InitVelocityConstraints (b2PulleyJoint.cpp:72-154)
+void PulleyInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel)
+{
+    const Body& A = w->bodies[j.bodyA];
+    const Body& B = w->bodies[j.bodyB];
+    j.indexA = A.islandIndex; j.indexB = B.islandIndex;
+    j.localCenterA = A.sweep.localCenter; j.localCenterB = B.sweep.localCenter;
+    j.invMassA = A.invMass; j.invMassB = B.invMass;
+    j.invIA = A.invI; j.invIB = B.invI;
+    Vec2 vA = vel[j.indexA].v, vB = vel[j.indexB].v;
+    float wA = vel[j.indexA].w, wB = vel[j.indexB].w;
+    j.rA = Mul(RotOf(pos[j.indexA].a), j.localAnchorA - j.localCenterA);
+    j.rB = Mul(RotOf(pos[j.indexB].a), j.localAnchorB - j.localCenterB);
+    float lenA, lenB;
+    PulleyUnit(pos[j.indexA].c, j.rA, j.groundAnchorA, j.uA, lenA);
+    PulleyUnit(pos[j.indexB].c, j.rB, j.groundAnchorB, j.uB, lenB);
+    const float ruA = Cross(j.rA, j.uA), ruB = Cross(j.rB, j.uB);
+    const float mA = j.invMassA + j.invIA * ruA * ruA;
+    const float mB = j.invMassB + j.invIB * ruB * ruB;
+    j.motorMass = mA + j.ratio * j.ratio * mB;
+    if (j.motorMass > 0.0f) j.motorMass = 1.0f / j.motorMass;
+    if (step.warmStarting) {
+        j.impulse[0] *= step.dtRatio;
+        const Vec2 PA = (-j.impulse[0]) * j.uA;
+        const Vec2 PB = (-j.ratio * j.impulse[0]) * j.uB;
+        vA = vA + j.invMassA * PA;
+        wA += j.invIA * Cross(j.rA, PA);
+        vB = vB + j.invMassB * PB;
+        wB += j.invIB * Cross(j.rB, PB);
+    } else {
+        j.impulse[0] = 0.0f;
+    }
+    vel[j.indexA].v = vA; vel[j.indexA].w = wA;
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+}
+
+// b2PulleyJoint::SolveVelocityConstraints (b2PulleyJoint.cpp:156-180)
+void PulleySolveVelocity(Joint& j, Velocity* vel)
+{
+    Vec2 vA = vel[j.indexA].v, vB = vel[j.indexB].v;
+    float wA = vel[j.indexA].w, wB = vel[j.indexB].w;
+    const float Cdot = -Dot(j.uA, vA + Cross(wA, j.rA)) - j.ratio * Dot(j.uB, vB + Cross(wB, j.rB));
+    const float impulse = -j.motorMass * Cdot;
+    j.impulse[0] += impulse;
+    const Vec2 PA = (-impulse) * j.uA;
+    const Vec2 PB = (-j.ratio * impulse) * j.uB;
+    vA = vA + j.invMassA * PA;
+    wA += j.invIA * Cross(j.rA, PA);
+    vB = vB + j.invMassB * PB;
+    wB += j.invIB * Cross(j.rB, PB);
+    vel[j.indexA].v = vA; vel[j.indexA].w = wA;
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+}
+
+// b2PulleyJoint::SolvePositionConstraints (b2PulleyJoint.cpp:182-275): one Newton step on
+// constant - lengthA - ratio * lengthB.
+bool PulleySolvePosition(Joint& j, Position* pos)
+{
+    Vec2 cA = pos[j.indexA].c, cB = pos[j.indexB].c;
+    float aA = pos[j.indexA].a, aB = pos[j.indexB].a;
+    const Vec2 rA = Mul(RotOf(aA), j.localAnchorA - j.localCenterA);
+    const Vec2 rB = Mul(RotOf(aB), j.localAnchorB - j.localCenterB);
+    Vec2 uA, uB;
+    float lenA, lenB;
+    PulleyUnit(cA, rA, j.groundAnchorA, uA, lenA);
+    PulleyUnit(cB, rB, j.groundAnchorB, uB, lenB);
+    const float ruA = Cross(rA, uA), ruB = Cross(rB, uB);
+    const float mA = j.invMassA + j.invIA * ruA * ruA;
+    const float mB = j.invMassB + j.invIB * ruB * ruB;
+    float mass = mA + j.ratio * j.ratio * mB;
+    if (mass > 0.0f) mass = 1.0f / mass;
+    const float C = j.pulleyConstant - lenA - j.ratio * lenB;
+    const float impulse = -mass * C;
+    const Vec2 PA = (-impulse) * uA;
+    const Vec2 PB = (-j.ratio * impulse) * uB;
+    cA = cA + j.invMassA * PA;
+    aA += j.invIA * Cross(rA, PA);
+    cB = cB + j.invMassB * PB;
+    aB += j.invIB * Cross(rB, PB);
+    pos[j.indexA].c = cA; pos[j.indexA].a = aA;
+    pos[j.indexB].c = cB; pos[j.indexB].a = aB;
+    return Abs(C) < kLinearSlop;
+}
+
 } // namespace
 
 // ---------------------------------------------------------------- island solve
@@ -2041,6 +2244,8 @@ void World::IslandSolve(const StepInfo& step)
         else if (j.type == kRopeJoint) RopeInit(this, j, step, positions.data(), velocities.data());
         else if (j.type == kFrictionJoint || j.type == kMotorJoint)
             FrictionMotorInit(this, j, step, positions.data(), velocities.data());
+        else if (j.type == kMouseJoint) MouseInit(this, j, step, positions.data(), velocities.data());
+        else if (j.type == kPulleyJoint) PulleyInit(this, j, step, positions.data(), velocities.data());
         else RevInit(this, j, step, positions.data(), velocities.data());
     }
     for (int i = 0; i < step.velocityIterations; ++i) {
@@ -2053,6 +2258,8 @@ void World::IslandSolve(const StepInfo& step)
             else if (j.type == kRopeJoint) RopeSolveVelocity(j, step, velocities.data());
             else if (j.type == kFrictionJoint || j.type == kMotorJoint)
                 FrictionMotorSolveVelocity(j, step, velocities.data());
+            else if (j.type == kMouseJoint) MouseSolveVelocity(j, step, velocities.data());
+            else if (j.type == kPulleyJoint) PulleySolveVelocity(j, velocities.data());
             else RevSolveVelocity(j, step, velocities.data());
         }
         cs.SolveVelocity();
@@ -2090,7 +2297,8 @@ void World::IslandSolve(const StepInfo& step)
                       : j.type == kPrismaticJoint ? PrisSolvePosition(j, positions.data())
                       : j.type == kWheelJoint ? WheelSolvePosition(j, positions.data())
                       : j.type == kRopeJoint ? RopeSolvePosition(j, positions.data())
-                      : (j.type == kFrictionJoint || j.type == kMotorJoint) ? true
+                      : j.type == kPulleyJoint ? PulleySolvePosition(j, positions.data())
+                      : (j.type == kFrictionJoint || j.type == kMotorJoint || j.type == kMouseJoint) ? true
                                                : RevSolvePosition(j, positions.data());
             jointsOkay = jointsOkay && ok;
         }

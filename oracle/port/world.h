@@ -56,7 +56,7 @@ struct Contact {
 
 // joint types (b2JointType, Dynamics/Joints/b2Joint.h:28-42, those restated here)
 enum JointType { kRevoluteJoint = 0, kDistanceJoint = 1, kWeldJoint = 2, kPrismaticJoint = 3, kWheelJoint = 4,
-                 kRopeJoint = 5, kFrictionJoint = 6, kMotorJoint = 7 };
+                 kRopeJoint = 5, kFrictionJoint = 6, kMotorJoint = 7, kMouseJoint = 8, kPulleyJoint = 9 };
 
 struct Joint {
     int type = kRevoluteJoint;
@@ -96,6 +96,13 @@ struct Joint {
     float maxForce = 0, maxTorque = 0;
     Vec2 linearOffset{0, 0}, linearError{0, 0};
     float angularOffset = 0, angularError = 0, correctionFactor = 0;
+    // mouse joint (b2MouseJoint.h): soft point-to-target spring on body B; impulse[0..1], the 2x2 mass
+    // in mass[0..3], gamma as the distance joint's
+    Vec2 target{0, 0}, mouseC{0, 0};
+    float beta = 0;
+    // pulley joint (b2PulleyJoint.h): impulse in impulse[0], effective mass in motorMass
+    Vec2 groundAnchorA{0, 0}, groundAnchorB{0, 0}, uA{0, 0}, uB{0, 0};
+    float lengthA = 0, lengthB = 0, ratio = 1, pulleyConstant = 0;
 };
 
 struct Position { Vec2 c; float a; };

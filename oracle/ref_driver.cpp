@@ -226,6 +226,29 @@ int rw_joint(void* h, int type, int bodyA, int bodyB, const float* f, int flags)
         jd.correctionFactor = f[5];
         jd.collideConnected = (flags & 4) != 0;
         w->joints.push_back(w->world.CreateJoint(&jd));
+    } else if (type == 8) {
+        b2MouseJointDef jd;
+        jd.bodyA = w->bodies[bodyA];
+        jd.bodyB = w->bodies[bodyB];
+        jd.target.Set(f[0], f[1]);
+        jd.maxForce = f[2];
+        jd.frequencyHz = f[3];
+        jd.dampingRatio = f[4];
+        jd.collideConnected = (flags & 4) != 0;
+        w->joints.push_back(w->world.CreateJoint(&jd));
+    } else if (type == 9) {
+        b2PulleyJointDef jd;
+        jd.bodyA = w->bodies[bodyA];
+        jd.bodyB = w->bodies[bodyB];
+        jd.groundAnchorA.Set(f[0], f[1]);
+        jd.groundAnchorB.Set(f[2], f[3]);
+        jd.localAnchorA.Set(f[4], f[5]);
+        jd.localAnchorB.Set(f[6], f[7]);
+        jd.lengthA = f[8];
+        jd.lengthB = f[9];
+        jd.ratio = f[10];
+        jd.collideConnected = (flags & 4) != 0;
+        w->joints.push_back(w->world.CreateJoint(&jd));
     } else {
         b2PrismaticJointDef jd;
         jd.bodyA = w->bodies[bodyA];
@@ -267,6 +290,10 @@ void rw_step(void* h, float dt, int vi, int pi) { static_cast<RefWorld*>(h)->wor
 // A b2Body state change between steps through the reference's own methods. op: the C-ABI's GB_EDIT_*.
 void rw_body_edit(void* h, int op, int body, int wake, const float* v)
 {
+    if (op == 9) { // body is the joint index of a mouse joint
+        static_cast<b2MouseJoint*>(static_cast<RefWorld*>(h)->joints[body])->SetTarget(b2Vec2(v[0], v[1]));
+        return;
+    }
     b2Body* b = static_cast<RefWorld*>(h)->bodies[body];
     const bool w = wake != 0;
     switch (op) {

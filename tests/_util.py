@@ -47,6 +47,28 @@ def first_divergence(world, steps: int, golden_digests: np.ndarray):
 # op codes of gb_body_edit (GB_EDIT_*)
 SET_TRANSFORM, SET_LINEAR_VELOCITY, SET_ANGULAR_VELOCITY, SET_AWAKE = 0, 1, 2, 3
 APPLY_FORCE, APPLY_FORCE_TO_CENTER, APPLY_TORQUE, APPLY_LINEAR_IMPULSE, APPLY_ANGULAR_IMPULSE = 4, 5, 6, 7, 8
+MOUSE_TARGET = 9  # the body field is the mouse joint's index
+
+
+def mouse_script():
+    """{step: [(op, body, values, wake)]} for the pulley_mouse scene (mouse joints 2 and 3): the stiff
+    joint's target dragged along a circle every 3 steps, the weak one lifted and dropped, an impulse
+    in between, and a target set on a body put to sleep (SetTarget wakes it)."""
+    import math
+
+    script = {}
+    for s in range(20, 200, 3):
+        t = (s - 20) * 0.05
+        tx = float(np.float32(16.25 + 2.0 * math.sin(t)))
+        ty = float(np.float32(6.25 + 1.5 - 1.5 * math.cos(t)))
+        script.setdefault(s, []).append((MOUSE_TARGET, 2, (tx, ty), True))
+    script.setdefault(50, []).append((MOUSE_TARGET, 3, (21.0, 4.0), True))
+    script.setdefault(120, []).append((MOUSE_TARGET, 3, (19.0, 0.5), True))
+    script.setdefault(130, []).append((APPLY_LINEAR_IMPULSE, 7, (0.0, 3.0, 20.0, 0.6), True))
+    script.setdefault(320, []).append((SET_AWAKE, 7, (0.0,), True))
+    script.setdefault(330, []).append((MOUSE_TARGET, 2, (14.0, 3.0), True))
+    script.setdefault(331, []).append((MOUSE_TARGET, 3, (20.0, 6.0), True))
+    return script
 
 
 def edit_scene():

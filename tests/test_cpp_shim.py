@@ -118,3 +118,58 @@ def test_cpp_body_edits_match_oracle(gpu, tmp_path):
         want.append([s[0], s[1], s[2]])
     want = np.array(want, dtype=np.float32)
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+MOUSE_PULLEY_SRC = os.path.join(ROOT, "tests", "cpp", "mouse_pulley.cpp")
+
+
+def _compile_mouse_pulley(tmp_path):
+    lib = _lib.library_path()
+    exe = str(tmp_path / "mouse_pulley")
+    libdir = os.path.dirname(lib)
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "include"), MOUSE_PULLEY_SRC,
+           "-o", exe, "-L", libdir, "-lbox2d_gb300", f"-Wl,-rpath,{libdir}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return exe
+
+
+def test_cpp_mouse_pulley_compile(tmp_path):
+    _compile_mouse_pulley(tmp_path)
+
+
+@pytest.mark.gpu
+def test_cpp_mouse_pulley_match_oracle(gpu, tmp_path):
+    """b2PulleyJointDef::Initialize and b2MouseJoint::SetTarget through the C++ mirror, bit for bit
+    like the CPU oracle on the same scene (the pulley's anchors and lengths are exact in float)."""
+    from tests._util import MOUSE_TARGET
+
+    exe = _compile_mouse_pulley(tmp_path)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    got = np.array([[float.fromhex(v) for v in ln.split()[1:]] for ln in r.stdout.strip().splitlines()],
+                   dtype=np.float32)
+    sc = scenes.Scene(name="mouse_pulley")
+    g = sc.body(scenes.STATIC, 0.0, -10.0)
+    sc.fixture(g, 3, [50.0, 10.0], n=2, density=0.0)
+    anchor = sc.body(scenes.STATIC, 0.0, 0.0)
+    a = sc.body(scenes.DYNAMIC, -3.0, 5.0)
+    sc.fixture(a, 3, [0.5, 1.0], n=2, density=1.0)
+    b = sc.body(scenes.DYNAMIC, 3.0, 4.0)
+    sc.fixture(b, 3, [0.5, 1.0], n=2, density=1.0)
+    sc.pulley(a, b, (-3.0, 10.0), (3.0, 10.0), (0.0, 1.0), (0.0, 1.0), 4.0, 5.0, 1.2)
+    d = sc.body(scenes.DYNAMIC, 0.0, 3.0)
+    sc.fixture(d, 3, [0.5, 0.5], n=2, density=1.0)
+    sc.mouse(anchor, d, (0.25, 3.25), 200.0)
+    o = oracle.OracleWorld(sc, "port", "project")
+    want = []
+    for i in range(120):
+        if 10 <= i < 70:
+            o.body_edit(MOUSE_TARGET, 1, (0.25 + 0.125 * (i - 10), 3.25), True)
+        o.step(1.0 / 60.0, 8, 3)
+        s = o.bodies()
+        want.append([s[k, c] for k in (a, b, d) for c in (0, 1, 2)])
+    want = np.array(want, dtype=np.float32)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    # the dragged box followed the target to the right, the pulley moved
+    assert want[-1, 6] > 5.0 and want[-1, 1] != 5.0

@@ -7,7 +7,7 @@ import pytest
 import oracle
 from box2dpp_gb300 import scenes
 from box2dpp_gb300.world import World
-from tests._util import DT, PI, VI, digest, edit_scene, edit_script
+from tests._util import DT, PI, VI, digest, edit_scene, edit_script, mouse_script
 
 pytestmark = pytest.mark.gpu
 
@@ -30,6 +30,33 @@ def test_gpu_edits_match_oracle(gpu):
         gi, gf = w.contacts()
         oi, of = o.contacts()
         assert np.array_equal(digest(gb, gi, gf), digest(ob, oi, of)), f"contacts differ at step {s}"
+    w.sync()
+
+
+def test_gpu_mouse_targets_match_oracle(gpu):
+    """Mouse joint targets moved through gb_body_edits, against the CPU oracle (which matches the
+    reference's b2MouseJoint::SetTarget) bit for bit every step; a target edit for a joint that is
+    not a mouse joint is refused."""
+    sc = scenes.pulley_mouse(scenes.SplitMix64(4))
+    script = mouse_script()
+    w = World(sc)
+    o = oracle.OracleWorld(sc, "port", "project")
+    for s in range(1, 361):
+        edits = script.get(s, [])
+        for (op, body, vals, wake) in edits:
+            o.body_edit(op, body, vals, wake)
+        if edits:
+            w.body_edits([(0, body, op, vals, wake) for (op, body, vals, wake) in edits])
+        w.step(DT, VI, PI)
+        o.step(DT, VI, PI)
+        gb, ob = w.bodies(), o.bodies()
+        assert np.array_equal(gb.view(np.uint32), ob.view(np.uint32)), f"bodies differ at step {s}"
+        gi, gf = w.contacts()
+        oi, of = o.contacts()
+        assert np.array_equal(digest(gb, gi, gf), digest(ob, oi, of)), f"contacts differ at step {s}"
+    for bad in [(0, 0, "mouse_target", (1.0, 1.0), True), (0, 4, "mouse_target", (1.0, 1.0), True)]:
+        with pytest.raises(Exception):
+            w.body_edits([bad])
     w.sync()
 
 
