@@ -781,8 +781,8 @@ gb_status CreateFixture(HWorld& W, int body, int type, const float* s, int n, co
     return GB_OK;
 }
 
-// b2World::CreateJoint (Dynamics/b2World.cpp:185-250) for a revolute, distance, weld or prismatic
-// joint definition; f as gb_create_joints documents (revolute, distance and weld use f[0..8]).
+// b2World::CreateJoint (Dynamics/b2World.cpp:185-250) for any joint definition; f as gb_create_joints
+// documents.
 gb_status CreateJoint(HWorld& W, int type, int a, int b, const float* f, int fl, int* id)
 {
     int nb = (int)W.bodies.size();
@@ -821,6 +821,45 @@ gb_status CreateJoint(HWorld& W, int type, int a, int b, const float* f, int fl,
         j.lengthA = f[8]; j.lengthB = f[9]; j.ratio = f[10];
         if (!(j.ratio != 0.0f)) return GB_ERR_INVALID;
         j.pulleyConstant = f[8] + j.ratio * f[9];
+    } else if (type == kJointGear) {
+        // b2GearJoint::b2GearJoint (Dynamics/Joints/b2GearJoint.cpp:49-136): f[0], f[1] the indices of
+        // two existing revolute or prismatic joints, f[2] the ratio. Bodies A and B become the joints'
+        // bodies B (the joint edges go there), C and D their bodies A; the constant is the coordinates'
+        // combination at creation.
+        const int j1 = (int)f[0], j2 = (int)f[1];
+        const int nj = (int)W.joints.size();
+        if ((float)j1 != f[0] || (float)j2 != f[1] || j1 < 0 || j1 >= nj || j2 < 0 || j2 >= nj) return GB_ERR_INVALID;
+        const Joint& J1 = W.joints[j1];
+        const Joint& J2 = W.joints[j2];
+        if ((J1.type != kJointRevolute && J1.type != kJointPrismatic) ||
+            (J2.type != kJointRevolute && J2.type != kJointPrismatic))
+            return GB_ERR_INVALID;
+        j.gearTypeA = J1.type; j.gearTypeB = J2.type;
+        j.bodyC = J1.bodyA; j.bodyA = J1.bodyB;
+        j.bodyD = J2.bodyA; j.bodyB = J2.bodyB;
+        const HBody &bA = W.bodies[j.bodyA], &bC = W.bodies[j.bodyC];
+        const HBody &bB = W.bodies[j.bodyB], &bD = W.bodies[j.bodyD];
+        j.localAnchorC = J1.localAnchorA; j.localAnchorA = J1.localAnchorB; j.referenceAngle = J1.referenceAngle;
+        j.localAnchorD = J2.localAnchorA; j.localAnchorB = J2.localAnchorB; j.referenceAngleB = J2.referenceAngle;
+        float coordinateA, coordinateB;
+        if (J1.type == kJointRevolute) {
+            j.localAxisC = V(0.0f, 0.0f);
+            coordinateA = bA.sw.a - bC.sw.a - j.referenceAngle;
+        } else {
+            j.localAxisC = J1.localXAxisA;
+            const Vec2 pA = MulT(bC.xf.q, Mul(bA.xf.q, j.localAnchorA) + (bA.xf.p - bC.xf.p));
+            coordinateA = Dot(pA - j.localAnchorC, j.localAxisC);
+        }
+        if (J2.type == kJointRevolute) {
+            j.localAxisD = V(0.0f, 0.0f);
+            coordinateB = bB.sw.a - bD.sw.a - j.referenceAngleB;
+        } else {
+            j.localAxisD = J2.localXAxisA;
+            const Vec2 pB = MulT(bD.xf.q, Mul(bB.xf.q, j.localAnchorB) + (bB.xf.p - bD.xf.p));
+            coordinateB = Dot(pB - j.localAnchorD, j.localAxisD);
+        }
+        j.ratio = f[2];
+        j.gearConstant = coordinateA + j.ratio * coordinateB;
     } else if (type == kJointRope) {
         j.maxLength = f[4];  // b2RopeJoint::b2RopeJoint (b2RopeJoint.cpp:35-45)
     } else if (type == kJointFriction) {
@@ -848,9 +887,10 @@ gb_status CreateJoint(HWorld& W, int type, int a, int b, const float* f, int fl,
     j.next = W.jointList;
     if (W.jointList != kNullIdx) W.joints[W.jointList].prev = idx;
     W.jointList = idx;
-    // edge 2*idx on bodyA's joint list, 2*idx+1 on bodyB's (b2World.cpp:212-236)
+    // edge 2*idx on bodyA's joint list, 2*idx+1 on bodyB's (b2World.cpp:212-236); the joint's bodies,
+    // which for a gear joint are not the definition's
     for (int side = 0; side < 2; ++side) {
-        HBody& body = W.bodies[side == 0 ? a : b];
+        HBody& body = W.bodies[side == 0 ? j.bodyA : j.bodyB];
         int e = 2 * idx + side;
         j.ePrev[side] = kNullIdx;
         j.eNext[side] = body.jointList;
@@ -858,7 +898,7 @@ gb_status CreateJoint(HWorld& W, int type, int a, int b, const float* f, int fl,
         body.jointList = e;
     }
     W.joints.push_back(j);
-    // Contacts between the two bodies are flagged for filtering (b2World.cpp:238-250).
+    // Contacts between the definition's two bodies are flagged for filtering (b2World.cpp:238-250).
     if (!j.collideConnected && W.hasState) {
         HContacts& C = W.contacts;
         for (int e = W.bodies[b].contactList; e != kNullIdx;) {

@@ -1529,12 +1529,165 @@ __device__ bool PulleySolvePosition(Joint& j, float4* pos)
     return linearError < kLinearSlop;
 }
 
+// ------------------------------------------------------------------ gear joint
+// b2GearJoint (Dynamics/Joints/b2GearJoint.cpp:139-352): coordinate1 + ratio * coordinate2 stays
+// constant, a coordinate being a revolute joint's relative angle or a prismatic joint's translation.
+// Four bodies: A and B (the joints' bodies B) and C and D (their bodies A). The warm start does not
+// scale the impulse by dtRatio, and the position solve always reports success.
+__device__ void GearInit(const Wd& W, Joint& j, float4* pos, float4* vel, bool warmStarting)
+{
+    const float4 mA4 = W.mas[j.bodyA], mB4 = W.mas[j.bodyB], mC4 = W.mas[j.bodyC], mD4 = W.mas[j.bodyD];
+    j.localCenterA = V(mA4.z, mA4.w); j.localCenterB = V(mB4.z, mB4.w);
+    j.localCenterC = V(mC4.z, mC4.w); j.localCenterD = V(mD4.z, mD4.w);
+    j.invMassA = mA4.x; j.invMassB = mB4.x; j.invMassC = mC4.x; j.invMassD = mD4.x;
+    j.invIA = mA4.y; j.invIB = mB4.y; j.invIC = mC4.y; j.invID = mD4.y;
+    const float4 va = vel[j.indexA], vb = vel[j.indexB], vc = vel[j.indexC], vd = vel[j.indexD];
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y), vC = V(vc.x, vc.y), vD = V(vd.x, vd.y);
+    float wA = va.z, wB = vb.z, wC = vc.z, wD = vd.z;
+    const Rot qA = RotOf(pos[j.indexA].z), qB = RotOf(pos[j.indexB].z);
+    const Rot qC = RotOf(pos[j.indexC].z), qD = RotOf(pos[j.indexD].z);
+    float mass = 0.0f;
+    if (j.gearTypeA == kJointRevolute) {
+        j.JvAC = V(0.0f, 0.0f);
+        j.JwA = 1.0f;
+        j.JwC = 1.0f;
+        mass += j.invIA + j.invIC;
+    } else {
+        const Vec2 u = Mul(qC, j.localAxisC);
+        const Vec2 rC = Mul(qC, j.localAnchorC - j.localCenterC);
+        const Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
+        j.JvAC = u;
+        j.JwC = Cross(rC, u);
+        j.JwA = Cross(rA, u);
+        mass += j.invMassC + j.invMassA + j.invIC * j.JwC * j.JwC + j.invIA * j.JwA * j.JwA;
+    }
+    if (j.gearTypeB == kJointRevolute) {
+        j.JvBD = V(0.0f, 0.0f);
+        j.JwB = j.ratio;
+        j.JwD = j.ratio;
+        mass += j.ratio * j.ratio * (j.invIB + j.invID);
+    } else {
+        const Vec2 u = Mul(qD, j.localAxisD);
+        const Vec2 rD = Mul(qD, j.localAnchorD - j.localCenterD);
+        const Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
+        j.JvBD = j.ratio * u;
+        j.JwD = j.ratio * Cross(rD, u);
+        j.JwB = j.ratio * Cross(rB, u);
+        mass += j.ratio * j.ratio * (j.invMassD + j.invMassB) + j.invID * j.JwD * j.JwD + j.invIB * j.JwB * j.JwB;
+    }
+    j.motorMass = mass > 0.0f ? 1.0f / mass : 0.0f;
+    if (warmStarting) {
+        const float P = j.impulse[0];
+        vA = vA + (j.invMassA * P) * j.JvAC;
+        wA += j.invIA * P * j.JwA;
+        vB = vB + (j.invMassB * P) * j.JvBD;
+        wB += j.invIB * P * j.JwB;
+        vC = vC - (j.invMassC * P) * j.JvAC;
+        wC -= j.invIC * P * j.JwC;
+        vD = vD - (j.invMassD * P) * j.JvBD;
+        wD -= j.invID * P * j.JwD;
+    } else {
+        j.impulse[0] = 0.0f;
+    }
+    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+    vel[j.indexC] = make_float4(vC.x, vC.y, wC, 0.0f);
+    vel[j.indexD] = make_float4(vD.x, vD.y, wD, 0.0f);
+}
+
+__device__ void GearSolveVelocity(Joint& j, float4* vel)
+{
+    const float4 va = vel[j.indexA], vb = vel[j.indexB], vc = vel[j.indexC], vd = vel[j.indexD];
+    Vec2 vA = V(va.x, va.y), vB = V(vb.x, vb.y), vC = V(vc.x, vc.y), vD = V(vd.x, vd.y);
+    float wA = va.z, wB = vb.z, wC = vc.z, wD = vd.z;
+    float Cdot = Dot(j.JvAC, vA - vC) + Dot(j.JvBD, vB - vD);
+    Cdot += (j.JwA * wA - j.JwC * wC) + (j.JwB * wB - j.JwD * wD);
+    const float impulse = -j.motorMass * Cdot;
+    j.impulse[0] += impulse;
+    vA = vA + (j.invMassA * impulse) * j.JvAC;
+    wA += j.invIA * impulse * j.JwA;
+    vB = vB + (j.invMassB * impulse) * j.JvBD;
+    wB += j.invIB * impulse * j.JwB;
+    vC = vC - (j.invMassC * impulse) * j.JvAC;
+    wC -= j.invIC * impulse * j.JwC;
+    vD = vD - (j.invMassD * impulse) * j.JvBD;
+    wD -= j.invID * impulse * j.JwD;
+    vel[j.indexA] = make_float4(vA.x, vA.y, wA, 0.0f);
+    vel[j.indexB] = make_float4(vB.x, vB.y, wB, 0.0f);
+    vel[j.indexC] = make_float4(vC.x, vC.y, wC, 0.0f);
+    vel[j.indexD] = make_float4(vD.x, vD.y, wD, 0.0f);
+}
+
+__device__ bool GearSolvePosition(Joint& j, float4* pos)
+{
+    const float4 pa = pos[j.indexA], pb = pos[j.indexB], pc = pos[j.indexC], pd = pos[j.indexD];
+    Vec2 cA = V(pa.x, pa.y), cB = V(pb.x, pb.y), cC = V(pc.x, pc.y), cD = V(pd.x, pd.y);
+    float aA = pa.z, aB = pb.z, aC = pc.z, aD = pd.z;
+    const Rot qA = RotOf(aA), qB = RotOf(aB), qC = RotOf(aC), qD = RotOf(aD);
+    Vec2 JvAC, JvBD;
+    float JwA, JwB, JwC, JwD, coordinateA, coordinateB;
+    float mass = 0.0f;
+    if (j.gearTypeA == kJointRevolute) {
+        JvAC = V(0.0f, 0.0f);
+        JwA = 1.0f;
+        JwC = 1.0f;
+        mass += j.invIA + j.invIC;
+        coordinateA = aA - aC - j.referenceAngle;
+    } else {
+        const Vec2 u = Mul(qC, j.localAxisC);
+        const Vec2 rC = Mul(qC, j.localAnchorC - j.localCenterC);
+        const Vec2 rA = Mul(qA, j.localAnchorA - j.localCenterA);
+        JvAC = u;
+        JwC = Cross(rC, u);
+        JwA = Cross(rA, u);
+        mass += j.invMassC + j.invMassA + j.invIC * JwC * JwC + j.invIA * JwA * JwA;
+        const Vec2 pC = j.localAnchorC - j.localCenterC;
+        const Vec2 pA = MulT(qC, rA + (cA - cC));
+        coordinateA = Dot(pA - pC, j.localAxisC);
+    }
+    if (j.gearTypeB == kJointRevolute) {
+        JvBD = V(0.0f, 0.0f);
+        JwB = j.ratio;
+        JwD = j.ratio;
+        mass += j.ratio * j.ratio * (j.invIB + j.invID);
+        coordinateB = aB - aD - j.referenceAngleB;
+    } else {
+        const Vec2 u = Mul(qD, j.localAxisD);
+        const Vec2 rD = Mul(qD, j.localAnchorD - j.localCenterD);
+        const Vec2 rB = Mul(qB, j.localAnchorB - j.localCenterB);
+        JvBD = j.ratio * u;
+        JwD = j.ratio * Cross(rD, u);
+        JwB = j.ratio * Cross(rB, u);
+        mass += j.ratio * j.ratio * (j.invMassD + j.invMassB) + j.invID * JwD * JwD + j.invIB * JwB * JwB;
+        const Vec2 pD = j.localAnchorD - j.localCenterD;
+        const Vec2 pB = MulT(qD, rB + (cB - cD));
+        coordinateB = Dot(pB - pD, j.localAxisD);
+    }
+    const float C = (coordinateA + j.ratio * coordinateB) - j.gearConstant;
+    float impulse = 0.0f;
+    if (mass > 0.0f) impulse = -C / mass;
+    cA = cA + (j.invMassA * impulse) * JvAC;
+    aA += j.invIA * impulse * JwA;
+    cB = cB + (j.invMassB * impulse) * JvBD;
+    aB += j.invIB * impulse * JwB;
+    cC = cC - (j.invMassC * impulse) * JvAC;
+    aC -= j.invIC * impulse * JwC;
+    cD = cD - (j.invMassD * impulse) * JvBD;
+    aD -= j.invID * impulse * JwD;
+    pos[j.indexA] = make_float4(cA.x, cA.y, aA, 0.0f);
+    pos[j.indexB] = make_float4(cB.x, cB.y, aB, 0.0f);
+    pos[j.indexC] = make_float4(cC.x, cC.y, aC, 0.0f);
+    pos[j.indexD] = make_float4(cD.x, cD.y, aD, 0.0f);
+    return true;
+}
+
 // ------------------------------------------------------------------ joint dispatch
 __device__ void JointInit(const Wd& W, Joint& j, float4* pos, float4* vel, bool warmStarting, float dtRatio, float dt)
 {
     if (j.type == kJointWheel) WheelInit(W, j, pos, vel, warmStarting, dtRatio, dt);
     else if (j.type == kJointMouse) MouseInit(W, j, pos, vel, warmStarting, dtRatio, dt);
     else if (j.type == kJointPulley) PulleyInit(W, j, pos, vel, warmStarting, dtRatio);
+    else if (j.type == kJointGear) GearInit(W, j, pos, vel, warmStarting);
     else if (j.type == kJointRope) RopeInit(W, j, pos, vel, warmStarting, dtRatio);
     else if (j.type == kJointFriction || j.type == kJointMotor) FrictionMotorInit(W, j, pos, vel, warmStarting, dtRatio);
     else if (j.type == kJointDistance) DistInit(W, j, pos, vel, warmStarting, dtRatio, dt);
@@ -1547,6 +1700,7 @@ __device__ void JointSolveVelocity(Joint& j, float4* vel, float dt)
     if (j.type == kJointWheel) WheelSolveVelocity(j, vel, dt);
     else if (j.type == kJointMouse) MouseSolveVelocity(j, vel, dt);
     else if (j.type == kJointPulley) PulleySolveVelocity(j, vel);
+    else if (j.type == kJointGear) GearSolveVelocity(j, vel);
     else if (j.type == kJointRope) RopeSolveVelocity(j, vel, dt);
     else if (j.type == kJointFriction || j.type == kJointMotor) FrictionMotorSolveVelocity(j, vel, dt);
     else if (j.type == kJointDistance) DistSolveVelocity(j, vel);
@@ -1559,6 +1713,7 @@ __device__ bool JointSolvePosition(Joint& j, float4* pos)
     if (j.type == kJointWheel) return WheelSolvePosition(j, pos);
     if (j.type == kJointMouse) return true;
     if (j.type == kJointPulley) return PulleySolvePosition(j, pos);
+    if (j.type == kJointGear) return GearSolvePosition(j, pos);
     if (j.type == kJointRope) return RopeSolvePosition(j, pos);
     if (j.type == kJointFriction || j.type == kJointMotor) return true;
     if (j.type == kJointDistance) return DistSolvePosition(j, pos);

@@ -1339,6 +1339,11 @@ __device__ bool Wd::buildIslandsTable(unsigned char* base, int capacity, bool co
                 Joint& J = jt[sJoint[i]];
                 J.indexA = bStart + local[J.bodyA];
                 J.indexB = bStart + local[J.bodyB];
+                if (J.type == kJointGear) {
+                    // the coupled joints, and with them bodies C and D, are in the same island
+                    J.indexC = bStart + local[J.bodyC];
+                    J.indexD = bStart + local[J.bodyD];
+                }
             }
             for (int i = 0; i < nStatics; ++i) bflag[statics[i]] &= (unsigned char)~fIsl;
         }
@@ -1472,6 +1477,10 @@ __device__ void Wd::solve(const StepParams& P, float4* smem, int smemRows, int s
                 Joint& J = jt[sJoint[i]];
                 J.indexA = bStart + bj[J.bodyA].z;
                 J.indexB = bStart + bj[J.bodyB].z;
+                if (J.type == kJointGear) {
+                    J.indexC = bStart + bj[J.bodyC].z;
+                    J.indexD = bStart + bj[J.bodyD].z;
+                }
             }
             for (int i = bStart; i < bCur; ++i)
                 if (bi[sBody[i]].x == kStatic) bi[sBody[i]].y &= ~kBIsland;

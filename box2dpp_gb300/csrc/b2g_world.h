@@ -82,7 +82,7 @@ struct WorldState {
 
 // Joint types (b2JointType, Dynamics/Joints/b2Joint.h:28-42, those built here).
 enum : int { kJointRevolute = 0, kJointDistance = 1, kJointWeld = 2, kJointPrismatic = 3, kJointWheel = 4,
-             kJointRope = 5, kJointFriction = 6, kJointMotor = 7, kJointMouse = 8, kJointPulley = 9, kJointTypes };
+             kJointRope = 5, kJointFriction = 6, kJointMotor = 7, kJointMouse = 8, kJointPulley = 9, kJointGear = 10, kJointTypes };
 
 // A joint (Dynamics/Joints/b2RevoluteJoint.h, b2DistanceJoint.h, b2WeldJoint.h), stored whole: joints
 // are few. Fields a type does not use stay zero; the distance joint keeps its scalar impulse in
@@ -132,6 +132,15 @@ struct Joint {
     // uA, uB; the impulse in impulse[0], mass in motorMass
     Vec2 groundAnchorA, groundAnchorB, uA, uB;
     float lengthA, lengthB, ratio, pulleyConstant;
+    // gear (b2GearJoint.h): couples a revolute or prismatic joint 1 (bodies C, A) with joint 2 (D, B);
+    // bodyA/bodyB are the joints' bodies B, localAnchorA/B and referenceAngle (A's) theirs, the axes
+    // zero for a revolute joint; ratio as the pulley's; this step's Jacobian, the island rows and mass
+    // data of C and D; the impulse in impulse[0], mass in motorMass
+    int bodyC, bodyD, indexC, indexD, gearTypeA, gearTypeB;
+    Vec2 localAnchorC, localAnchorD, localAxisC, localAxisD, localCenterC, localCenterD;
+    float referenceAngleB, gearConstant, invMassC, invMassD, invIC, invID;
+    Vec2 JvAC, JvBD;
+    float JwA, JwB, JwC, JwD;
 };
 
 // Island solver records: the fields of b2ContactVelocityConstraint and b2ContactPositionConstraint

@@ -35,7 +35,7 @@ import numpy as np
 STATIC, KINEMATIC, DYNAMIC = 0, 1, 2
 # shape encodings of the bulk build call
 CIRCLE, EDGE, POLYGON, BOX = 0, 1, 2, 3
-REVOLUTE, DISTANCE, WELD, PRISMATIC, WHEEL, ROPE, FRICTION, MOTOR, MOUSE, PULLEY = 0, 1, 2, 3, 4, 5, 6, 7, 8, 9
+REVOLUTE, DISTANCE, WELD, PRISMATIC, WHEEL, ROPE, FRICTION, MOTOR, MOUSE, PULLEY, GEAR = 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10
 DEFAULT_FLAGS = 1 | 2 | 16  # allowSleep, awake, active
 
 
@@ -145,6 +145,13 @@ class Scene:
         ground anchors in world coordinates (the def's default collideConnected is true)."""
         self.joints.append((a, b, [ground_a[0], ground_a[1], ground_b[0], ground_b[1], anchor_a[0], anchor_a[1],
                                    anchor_b[0], anchor_b[1], length_a, length_b, ratio, 0.0], flags, PULLEY))
+        return len(self.joints) - 1
+
+    def gear(self, a, b, joint1, joint2, ratio=1.0, flags=0) -> int:
+        """b2GearJointDef: couples revolute or prismatic joints joint1 and joint2 (indices of joints
+        created before it) so that coordinate1 + ratio * coordinate2 stays constant; a and b are the
+        definition's bodyA and bodyB (normally joint1's and joint2's body B)."""
+        self.joints.append((a, b, [float(joint1), float(joint2), ratio] + [0.0] * 9, flags, GEAR))
         return len(self.joints) - 1
 
     def prismatic(self, a, b, anchor_a, anchor_b, axis, ref_angle=0.0, lower=0.0, upper=0.0, max_motor_force=0.0,
@@ -472,6 +479,56 @@ def pulley_mouse(rng: SplitMix64, allow_sleep: bool = True) -> Scene:
     for i in range(6):
         x = _q((-10.0, -4.0, 4.0, 9.0, 16.0, -7.0)[i] + rng.uniform(-0.3, 0.3))
         e = s.body(DYNAMIC, x, _q(16.0 + 2.0 * i + rng.uniform(0.0, 1.0)), angle=_q(rng.uniform(-0.4, 0.4)))
+        s.fixture(e, CIRCLE if i % 2 else BOX, [0.0, 0.0, 0.3] if i % 2 else [0.3, 0.3], 1 if i % 2 else 2,
+                  density=1.0, friction=0.5)
+    return _settings(s, allow_sleep)
+
+
+def gears(rng: SplitMix64, allow_sleep: bool = True) -> Scene:
+    """Gear joints: a motor-driven wheel geared to a larger one (revolute-revolute), a spinning
+    pinion geared to a vertical rack on a prismatic joint with limits, two horizontal sliders geared
+    together (prismatic-prismatic), and a car whose two wheels are geared to each other through their
+    revolute joints on the chassis (bodies C and D of that gear are both the moving chassis); boxes and
+    circles fall among them."""
+    s = Scene(name="gears")
+    g = s.body(STATIC, 0.0, 0.0)
+    s.fixture(g, EDGE, [-40.0, 0.0, 40.0, 0.0, 0, 0, 0, 0, 0, 0], friction=0.7)
+    w1 = s.body(DYNAMIC, -12.0, 8.0)
+    s.fixture(w1, CIRCLE, [0.0, 0.0, 1.0], 1, density=1.0)
+    w2 = s.body(DYNAMIC, -8.5, 8.0)
+    s.fixture(w2, CIRCLE, [0.0, 0.0, 2.0], 1, density=1.0)
+    j0 = s.revolute(g, w1, (-12.0, 8.0), (0.0, 0.0), motor_speed=2.0, max_motor_torque=60.0, flags=2)
+    j1 = s.revolute(g, w2, (-8.5, 8.0), (0.0, 0.0))
+    s.gear(w1, w2, j0, j1, 2.0)
+    # rack and pinion
+    p = s.body(DYNAMIC, 2.0, 6.0, w=3.0)
+    s.fixture(p, CIRCLE, [0.0, 0.0, 1.0], 1, density=1.0)
+    rack = s.body(DYNAMIC, 3.5, 6.0)
+    s.fixture(rack, BOX, [0.25, 1.5], 2, density=1.0)
+    j3 = s.revolute(g, p, (2.0, 6.0), (0.0, 0.0))
+    j4 = s.prismatic(g, rack, (3.5, 6.0), (0.0, 0.0), (0.0, 1.0), lower=-3.0, upper=3.0, flags=1)
+    s.gear(p, rack, j3, j4, -1.0)
+    # geared sliders on horizontal rails
+    s1 = s.body(DYNAMIC, 10.0, 3.0, vx=2.0)
+    s.fixture(s1, BOX, [0.5, 0.25], 2, density=1.0)
+    s2 = s.body(DYNAMIC, 10.0, 6.0)
+    s.fixture(s2, BOX, [0.5, 0.25], 2, density=2.0)
+    j6 = s.prismatic(g, s1, (10.0, 3.0), (0.0, 0.0), (1.0, 0.0))
+    j7 = s.prismatic(g, s2, (10.0, 6.0), (0.0, 0.0), (1.0, 0.0))
+    s.gear(s1, s2, j6, j7, 1.5)
+    # a car with geared wheels
+    car = s.body(DYNAMIC, 20.0, 3.0, vx=-3.0)
+    s.fixture(car, BOX, [1.5, 0.3], 2, density=1.0)
+    wa = s.body(DYNAMIC, 19.0, 2.3, vx=-3.0)
+    s.fixture(wa, CIRCLE, [0.0, 0.0, 0.5], 1, density=1.0, friction=0.9)
+    wb = s.body(DYNAMIC, 21.0, 2.3, vx=-3.0)
+    s.fixture(wb, CIRCLE, [0.0, 0.0, 0.5], 1, density=1.0, friction=0.9)
+    j9 = s.revolute(car, wa, (-1.0, -0.7), (0.0, 0.0))
+    j10 = s.revolute(car, wb, (1.0, -0.7), (0.0, 0.0))
+    s.gear(wa, wb, j9, j10, -1.0)
+    for i in range(6):
+        x = _q((-12.0, -8.5, 2.0, 10.0, 20.0, 3.5)[i] + rng.uniform(-0.3, 0.3))
+        e = s.body(DYNAMIC, x, _q(12.0 + 1.5 * i + rng.uniform(0.0, 1.0)), angle=_q(rng.uniform(-0.4, 0.4)))
         s.fixture(e, CIRCLE if i % 2 else BOX, [0.0, 0.0, 0.3] if i % 2 else [0.3, 0.3], 1 if i % 2 else 2,
                   density=1.0, friction=0.5)
     return _settings(s, allow_sleep)

@@ -73,7 +73,7 @@ gb_status gb_create_revolute_joints(gb_world* world, int w, int n, const int* bo
 /* b2World::CreateJoint for the joint definitions built here (Box2D/Dynamics/b2World.cpp:185;
  * Box2D/Dynamics/Joints/b2RevoluteJoint.h:36, b2DistanceJoint.h:30, b2WeldJoint.h:28,
  * b2PrismaticJoint.h:30, b2WheelJoint.h:30, b2RopeJoint.h:28, b2FrictionJoint.h:25,
- * b2MotorJoint.h:26, b2MouseJoint.h:24, b2PulleyJoint.h:26). type: GB_JOINT_*. f[GB_JOINT_FLOATS] per joint (the fields of the definition;
+ * b2MotorJoint.h:26, b2MouseJoint.h:24, b2PulleyJoint.h:26, b2GearJoint.h:24). type: GB_JOINT_*. f[GB_JOINT_FLOATS] per joint (the fields of the definition;
  * anchors and axes in body-local coordinates):
  *   revolute   localAnchorA.x, .y, localAnchorB.x, .y, referenceAngle, lowerAngle, upperAngle,
  *              motorSpeed, maxMotorTorque (as gb_create_revolute_joints)
@@ -91,6 +91,9 @@ gb_status gb_create_revolute_joints(gb_world* world, int w, int n, const int* bo
  *              maxForce, frequencyHz, dampingRatio (body A is normally a static body)
  *   pulley     groundAnchorA.x, .y, groundAnchorB.x, .y (world), localAnchorA.x, .y, localAnchorB.x,
  *              .y, lengthA, lengthB, ratio (non-zero)
+ *   gear       joint1, joint2 (indices of revolute or prismatic joints of the same world, as exact
+ *              floats), ratio; a and b are the definition's bodyA/bodyB (contact filtering only:
+ *              the joint acts on joint1's and joint2's body B, b2GearJoint.cpp:49-136)
  * Unused trailing floats are ignored. flags: 1 enableLimit (revolute, prismatic), 2 enableMotor
  * (revolute, prismatic, wheel), 4 collideConnected. */
 #define GB_JOINT_REVOLUTE 0
@@ -103,6 +106,7 @@ gb_status gb_create_revolute_joints(gb_world* world, int w, int n, const int* bo
 #define GB_JOINT_MOTOR 7
 #define GB_JOINT_MOUSE 8
 #define GB_JOINT_PULLEY 9
+#define GB_JOINT_GEAR 10
 #define GB_JOINT_FLOATS 12
 gb_status gb_create_joints(gb_world* world, int w, int n, const int* type, const int* body_a, const int* body_b,
                            const float* f, const int* flags, int* out_ids);

@@ -319,6 +319,18 @@ struct b2PulleyJointDef {
                     const b2Vec2& anchorB, float r);
 };
 
+// b2GearJointDef (Box2D/Dynamics/Joints/b2GearJoint.h:26-46): joint1 and joint2 are revolute or
+// prismatic joints created before it
+class b2Joint;
+struct b2GearJointDef {
+    b2Body* bodyA = nullptr;
+    b2Body* bodyB = nullptr;
+    bool collideConnected = false;
+    b2Joint* joint1 = nullptr;
+    b2Joint* joint2 = nullptr;
+    float ratio = 1.0f;
+};
+
 // b2PrismaticJointDef (Box2D/Dynamics/Joints/b2PrismaticJoint.h:30-88)
 struct b2PrismaticJointDef {
     b2Body* bodyA = nullptr;
@@ -513,6 +525,17 @@ public:
                                           def->localAnchorB.x, def->localAnchorB.y, def->lengthA, def->lengthB,
                                           def->ratio};
         return AddJoint(GB_JOINT_PULLEY, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
+    }
+    b2Joint* CreateJoint(const b2GearJointDef* def)
+    {
+        if (!def->joint1 || !def->joint2) return nullptr;
+        const float f[GB_JOINT_FLOATS] = {(float)def->joint1->GetIndex(), (float)def->joint2->GetIndex(), def->ratio};
+        b2Joint* j = AddJoint(GB_JOINT_GEAR, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
+        if (j) {  // b2GearJoint::GetBodyA/B: the coupled joints' bodies B
+            j->m_a = def->joint1->GetBodyB();
+            j->m_b = def->joint2->GetBodyB();
+        }
+        return j;
     }
     b2Joint* CreateJoint(const b2PrismaticJointDef* def)
     {

@@ -173,6 +173,37 @@ int World::CreateJoint(int type, int a, int b, const float* f, int fl)
         j.lengthB = f[9];
         j.ratio = f[10];
         j.pulleyConstant = f[8] + j.ratio * f[9];
+    } else if (type == kGearJoint) {
+        // b2GearJoint::b2GearJoint (b2GearJoint.cpp:49-136): f[0], f[1] the coupled joints, f[2] the
+        // ratio; the joint's own bodies become the coupled joints' bodies B
+        const Joint& j1 = joints[(int)f[0]];
+        const Joint& j2 = joints[(int)f[1]];
+        j.typeA = j1.type;
+        j.typeB = j2.type;
+        j.bodyC = j1.bodyA; j.bodyA = j1.bodyB;
+        j.bodyD = j2.bodyA; j.bodyB = j2.bodyB;
+        j.localAnchorC = j1.localAnchorA; j.localAnchorA = j1.localAnchorB;
+        j.localAnchorD = j2.localAnchorA; j.localAnchorB = j2.localAnchorB;
+        j.referenceAngle = j1.referenceAngle;
+        j.referenceAngleB = j2.referenceAngle;
+        const Body &A = bodies[j.bodyA], &B = bodies[j.bodyB], &Cb = bodies[j.bodyC], &Db = bodies[j.bodyD];
+        float coordA, coordB;
+        if (j1.type == kRevoluteJoint) {
+            coordA = A.sweep.a - Cb.sweep.a - j.referenceAngle;
+        } else {
+            j.localAxisC = j1.localXAxisA;
+            const Vec2 rel = MulT(Cb.xf.q, Mul(A.xf.q, j.localAnchorA) + (A.xf.p - Cb.xf.p));
+            coordA = Dot(rel - j.localAnchorC, j.localAxisC);
+        }
+        if (j2.type == kRevoluteJoint) {
+            coordB = B.sweep.a - Db.sweep.a - j.referenceAngleB;
+        } else {
+            j.localAxisD = j2.localXAxisA;
+            const Vec2 rel = MulT(Db.xf.q, Mul(B.xf.q, j.localAnchorB) + (B.xf.p - Db.xf.p));
+            coordB = Dot(rel - j.localAnchorD, j.localAxisD);
+        }
+        j.ratio = f[2];
+        j.gearConstant = coordA + j.ratio * coordB;
     } else if (type == kRopeJoint) {
         j.maxLength = f[4];
     } else if (type == kFrictionJoint) {
@@ -220,9 +251,10 @@ int World::LinkJoint(Joint& j, int a, int b)
     if (jointList != kNull) joints[jointList].prev = id;
     jointList = id;
     ++jointCount;
-    // edge 2*id is on bodyA's list (other = bodyB), 2*id+1 on bodyB's list (other = bodyA)
+    // edge 2*id is on bodyA's list (other = bodyB), 2*id+1 on bodyB's list (other = bodyA); the
+    // joint's bodies (a gear joint's are not the definition's a, b, which the filter flag uses)
     for (int side = 0; side < 2; ++side) {
-        Body& body = bodies[side == 0 ? a : b];
+        Body& body = bodies[side == 0 ? j.bodyA : j.bodyB];
         int e = 2 * id + side;
         joints[id].ePrev[side] = kNull;
         joints[id].eNext[side] = body.jointList;
@@ -1060,6 +1092,9 @@ void FrictionMotorInit(World* w, Joint& j, const StepInfo& step, Position* pos, 
 void MouseInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel);
 void MouseSolveVelocity(Joint& j, const StepInfo& step, Velocity* vel);
 void PulleyInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel);
+void GearInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel);
+void GearSolveVelocity(Joint& j, Velocity* vel);
+bool GearSolvePosition(Joint& j, Position* pos);
 void PulleySolveVelocity(Joint& j, Velocity* vel);
 bool PulleySolvePosition(Joint& j, Position* pos);
 void FrictionMotorSolveVelocity(Joint& j, const StepInfo& step, Velocity* vel);
@@ -2205,6 +2240,138 @@ bool PulleySolvePosition(Joint& j, Position* pos)
     return Abs(C) < kLinearSlop;
 }
 
+// ---------------------------------------------------------------- gear joint
+// The gear Jacobian of one coupled joint (b2GearJoint.cpp:171-201, 309-347): for a revolute joint the
+// angular terms 1 (scaled by s), for a prismatic joint the axis u in the frame of the joint's body A
+// (g) and the lever arms of both bodies; adds the joint's share of the effective mass to *mass, in
+// the reference's order (joint 1: mG + mM + ..., joint 2: s*s*(mG + mM) + ...).
+static void GearTerms(int type, bool second, float s, Rot qG, Rot qM, Vec2 anchorG, Vec2 anchorM, Vec2 lcG, Vec2 lcM,
+                      Vec2 axisG, float mG, float mM, float iG, float iM, Vec2& Jv, float& JwM, float& JwG, Vec2& rM,
+                      float* mass)
+{
+    if (type == kRevoluteJoint) {
+        Jv = V(0.0f, 0.0f);
+        JwM = s;
+        JwG = s;
+        *mass += second ? s * s * (iM + iG) : iM + iG;
+        return;
+    }
+    const Vec2 u = Mul(qG, axisG);
+    const Vec2 rG = Mul(qG, anchorG - lcG);
+    rM = Mul(qM, anchorM - lcM);
+    if (second) {
+        Jv = s * u;
+        JwG = s * Cross(rG, u);
+        JwM = s * Cross(rM, u);
+        *mass += s * s * (mG + mM) + iG * JwG * JwG + iM * JwM * JwM;
+    } else {
+        Jv = u;
+        JwG = Cross(rG, u);
+        JwM = Cross(rM, u);
+        *mass += mG + mM + iG * JwG * JwG + iM * JwM * JwM;
+    }
+}
+
+// b2GearJoint::InitVelocityConstraints (b2GearJoint.cpp:139-240): no dtRatio scaling of the impulse
+void GearInit(World* w, Joint& j, const StepInfo& step, Position* pos, Velocity* vel)
+{
+    const Body &A = w->bodies[j.bodyA], &B = w->bodies[j.bodyB], &Cb = w->bodies[j.bodyC], &Db = w->bodies[j.bodyD];
+    j.indexA = A.islandIndex; j.indexB = B.islandIndex; j.indexC = Cb.islandIndex; j.indexD = Db.islandIndex;
+    j.localCenterA = A.sweep.localCenter; j.localCenterB = B.sweep.localCenter;
+    j.lcC = Cb.sweep.localCenter; j.lcD = Db.sweep.localCenter;
+    j.invMassA = A.invMass; j.invMassB = B.invMass; j.invMassC = Cb.invMass; j.invMassD = Db.invMass;
+    j.invIA = A.invI; j.invIB = B.invI; j.invIC = Cb.invI; j.invID = Db.invI;
+    Vec2 vA = vel[j.indexA].v, vB = vel[j.indexB].v, vC = vel[j.indexC].v, vD = vel[j.indexD].v;
+    float wA = vel[j.indexA].w, wB = vel[j.indexB].w, wC = vel[j.indexC].w, wD = vel[j.indexD].w;
+    const Rot qA = RotOf(pos[j.indexA].a), qB = RotOf(pos[j.indexB].a);
+    const Rot qC = RotOf(pos[j.indexC].a), qD = RotOf(pos[j.indexD].a);
+    float mass = 0.0f;
+    Vec2 rA, rB;
+    GearTerms(j.typeA, false, 1.0f, qC, qA, j.localAnchorC, j.localAnchorA, j.lcC, j.localCenterA, j.localAxisC,
+              j.invMassC, j.invMassA, j.invIC, j.invIA, j.JvAC, j.JwA, j.JwC, rA, &mass);
+    GearTerms(j.typeB, true, j.ratio, qD, qB, j.localAnchorD, j.localAnchorB, j.lcD, j.localCenterB, j.localAxisD,
+              j.invMassD, j.invMassB, j.invID, j.invIB, j.JvBD, j.JwB, j.JwD, rB, &mass);
+    j.motorMass = mass > 0.0f ? 1.0f / mass : 0.0f;
+    if (step.warmStarting) {
+        const float P = j.impulse[0];
+        vA = vA + (j.invMassA * P) * j.JvAC;
+        wA += j.invIA * P * j.JwA;
+        vB = vB + (j.invMassB * P) * j.JvBD;
+        wB += j.invIB * P * j.JwB;
+        vC = vC - (j.invMassC * P) * j.JvAC;
+        wC -= j.invIC * P * j.JwC;
+        vD = vD - (j.invMassD * P) * j.JvBD;
+        wD -= j.invID * P * j.JwD;
+    } else {
+        j.impulse[0] = 0.0f;
+    }
+    vel[j.indexA].v = vA; vel[j.indexA].w = wA;
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+    vel[j.indexC].v = vC; vel[j.indexC].w = wC;
+    vel[j.indexD].v = vD; vel[j.indexD].w = wD;
+}
+
+// b2GearJoint::SolveVelocityConstraints (b2GearJoint.cpp:242-277)
+void GearSolveVelocity(Joint& j, Velocity* vel)
+{
+    Vec2 vA = vel[j.indexA].v, vB = vel[j.indexB].v, vC = vel[j.indexC].v, vD = vel[j.indexD].v;
+    float wA = vel[j.indexA].w, wB = vel[j.indexB].w, wC = vel[j.indexC].w, wD = vel[j.indexD].w;
+    float Cdot = Dot(j.JvAC, vA - vC) + Dot(j.JvBD, vB - vD);
+    Cdot += (j.JwA * wA - j.JwC * wC) + (j.JwB * wB - j.JwD * wD);
+    const float P = -j.motorMass * Cdot;
+    j.impulse[0] += P;
+    vA = vA + (j.invMassA * P) * j.JvAC;
+    wA += j.invIA * P * j.JwA;
+    vB = vB + (j.invMassB * P) * j.JvBD;
+    wB += j.invIB * P * j.JwB;
+    vC = vC - (j.invMassC * P) * j.JvAC;
+    wC -= j.invIC * P * j.JwC;
+    vD = vD - (j.invMassD * P) * j.JvBD;
+    wD -= j.invID * P * j.JwD;
+    vel[j.indexA].v = vA; vel[j.indexA].w = wA;
+    vel[j.indexB].v = vB; vel[j.indexB].w = wB;
+    vel[j.indexC].v = vC; vel[j.indexC].w = wC;
+    vel[j.indexD].v = vD; vel[j.indexD].w = wD;
+}
+
+// b2GearJoint::SolvePositionConstraints (b2GearJoint.cpp:279-352): one correction of
+// (coordinate1 + ratio * coordinate2) - constant; always reports success
+bool GearSolvePosition(Joint& j, Position* pos)
+{
+    Vec2 cA = pos[j.indexA].c, cB = pos[j.indexB].c, cC = pos[j.indexC].c, cD = pos[j.indexD].c;
+    float aA = pos[j.indexA].a, aB = pos[j.indexB].a, aC = pos[j.indexC].a, aD = pos[j.indexD].a;
+    const Rot qA = RotOf(aA), qB = RotOf(aB), qC = RotOf(aC), qD = RotOf(aD);
+    Vec2 JvAC, JvBD, rA, rB;
+    float JwA, JwB, JwC, JwD;
+    float mass = 0.0f;
+    GearTerms(j.typeA, false, 1.0f, qC, qA, j.localAnchorC, j.localAnchorA, j.lcC, j.localCenterA, j.localAxisC,
+              j.invMassC, j.invMassA, j.invIC, j.invIA, JvAC, JwA, JwC, rA, &mass);
+    GearTerms(j.typeB, true, j.ratio, qD, qB, j.localAnchorD, j.localAnchorB, j.lcD, j.localCenterB, j.localAxisD,
+              j.invMassD, j.invMassB, j.invID, j.invIB, JvBD, JwB, JwD, rB, &mass);
+    const float coordA = j.typeA == kRevoluteJoint
+                             ? aA - aC - j.referenceAngle
+                             : Dot(MulT(qC, rA + (cA - cC)) - (j.localAnchorC - j.lcC), j.localAxisC);
+    const float coordB = j.typeB == kRevoluteJoint
+                             ? aB - aD - j.referenceAngleB
+                             : Dot(MulT(qD, rB + (cB - cD)) - (j.localAnchorD - j.lcD), j.localAxisD);
+    const float C = (coordA + j.ratio * coordB) - j.gearConstant;
+    float P = 0.0f;
+    if (mass > 0.0f) P = -C / mass;
+    cA = cA + (j.invMassA * P) * JvAC;
+    aA += j.invIA * P * JwA;
+    cB = cB + (j.invMassB * P) * JvBD;
+    aB += j.invIB * P * JwB;
+    cC = cC - (j.invMassC * P) * JvAC;
+    aC -= j.invIC * P * JwC;
+    cD = cD - (j.invMassD * P) * JvBD;
+    aD -= j.invID * P * JwD;
+    pos[j.indexA].c = cA; pos[j.indexA].a = aA;
+    pos[j.indexB].c = cB; pos[j.indexB].a = aB;
+    pos[j.indexC].c = cC; pos[j.indexC].a = aC;
+    pos[j.indexD].c = cD; pos[j.indexD].a = aD;
+    return true;
+}
+
 } // namespace
 
 // ---------------------------------------------------------------- island solve
@@ -2246,6 +2413,7 @@ void World::IslandSolve(const StepInfo& step)
             FrictionMotorInit(this, j, step, positions.data(), velocities.data());
         else if (j.type == kMouseJoint) MouseInit(this, j, step, positions.data(), velocities.data());
         else if (j.type == kPulleyJoint) PulleyInit(this, j, step, positions.data(), velocities.data());
+        else if (j.type == kGearJoint) GearInit(this, j, step, positions.data(), velocities.data());
         else RevInit(this, j, step, positions.data(), velocities.data());
     }
     for (int i = 0; i < step.velocityIterations; ++i) {
@@ -2260,6 +2428,7 @@ void World::IslandSolve(const StepInfo& step)
                 FrictionMotorSolveVelocity(j, step, velocities.data());
             else if (j.type == kMouseJoint) MouseSolveVelocity(j, step, velocities.data());
             else if (j.type == kPulleyJoint) PulleySolveVelocity(j, velocities.data());
+            else if (j.type == kGearJoint) GearSolveVelocity(j, velocities.data());
             else RevSolveVelocity(j, step, velocities.data());
         }
         cs.SolveVelocity();
@@ -2298,6 +2467,7 @@ void World::IslandSolve(const StepInfo& step)
                       : j.type == kWheelJoint ? WheelSolvePosition(j, positions.data())
                       : j.type == kRopeJoint ? RopeSolvePosition(j, positions.data())
                       : j.type == kPulleyJoint ? PulleySolvePosition(j, positions.data())
+                      : j.type == kGearJoint ? GearSolvePosition(j, positions.data())
                       : (j.type == kFrictionJoint || j.type == kMotorJoint || j.type == kMouseJoint) ? true
                                                : RevSolvePosition(j, positions.data());
             jointsOkay = jointsOkay && ok;

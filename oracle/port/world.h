@@ -56,7 +56,7 @@ struct Contact {
 
 // joint types (b2JointType, Dynamics/Joints/b2Joint.h:28-42, those restated here)
 enum JointType { kRevoluteJoint = 0, kDistanceJoint = 1, kWeldJoint = 2, kPrismaticJoint = 3, kWheelJoint = 4,
-                 kRopeJoint = 5, kFrictionJoint = 6, kMotorJoint = 7, kMouseJoint = 8, kPulleyJoint = 9 };
+                 kRopeJoint = 5, kFrictionJoint = 6, kMotorJoint = 7, kMouseJoint = 8, kPulleyJoint = 9, kGearJoint = 10 };
 
 struct Joint {
     int type = kRevoluteJoint;
@@ -103,6 +103,14 @@ struct Joint {
     // pulley joint (b2PulleyJoint.h): impulse in impulse[0], effective mass in motorMass
     Vec2 groundAnchorA{0, 0}, groundAnchorB{0, 0}, uA{0, 0}, uB{0, 0};
     float lengthA = 0, lengthB = 0, ratio = 1, pulleyConstant = 0;
+    // gear joint (b2GearJoint.h): joint 1 couples bodies C and A, joint 2 D and B (bodyA/bodyB here);
+    // A's reference angle in referenceAngle; impulse in impulse[0], mass in motorMass
+    int bodyC = kNull, bodyD = kNull, typeA = 0, typeB = 0, indexC = 0, indexD = 0;
+    Vec2 localAnchorC{0, 0}, localAnchorD{0, 0}, localAxisC{0, 0}, localAxisD{0, 0};
+    Vec2 lcC{0, 0}, lcD{0, 0};
+    float referenceAngleB = 0, gearConstant = 0, invMassC = 0, invMassD = 0, invIC = 0, invID = 0;
+    Vec2 JvAC{0, 0}, JvBD{0, 0};
+    float JwA = 0, JwB = 0, JwC = 0, JwD = 0;
 };
 
 struct Position { Vec2 c; float a; };

@@ -236,6 +236,15 @@ int rw_joint(void* h, int type, int bodyA, int bodyB, const float* f, int flags)
         jd.dampingRatio = f[4];
         jd.collideConnected = (flags & 4) != 0;
         w->joints.push_back(w->world.CreateJoint(&jd));
+    } else if (type == 10) {
+        b2GearJointDef jd;
+        jd.bodyA = w->bodies[bodyA];
+        jd.bodyB = w->bodies[bodyB];
+        jd.joint1 = w->joints[(int)f[0]];
+        jd.joint2 = w->joints[(int)f[1]];
+        jd.ratio = f[2];
+        jd.collideConnected = (flags & 4) != 0;
+        w->joints.push_back(w->world.CreateJoint(&jd));
     } else if (type == 9) {
         b2PulleyJointDef jd;
         jd.bodyA = w->bodies[bodyA];

@@ -59,3 +59,26 @@ def test_invalid_arguments_rejected():
     bad = lib.gb_create_bodies(w.h, 0, 1, np.array([7], np.int32), np.zeros(9, np.float32),
                                np.zeros(1, np.int32), np.zeros(1, np.int32))
     assert bad == _lib.GB_ERR_INVALID
+
+
+def test_joint_records_validated():
+    """gb_create_joints refuses a gear joint that does not couple two existing revolute or prismatic
+    joints (b2GearJoint.cpp:54-55 asserts the types), a gear index that is not an integer, and a
+    pulley with ratio 0 (b2PulleyJoint.cpp:64); a valid gear is accepted."""
+    lib = _lib.load()
+    w = World(scenes.gears(scenes.SplitMix64(8)))
+    out = np.zeros(1, np.int32)
+
+    def joint(jtype, a, b, vals):
+        f = np.zeros(12, np.float32)
+        f[:len(vals)] = vals
+        return lib.gb_create_joints(w.h, 0, 1, np.array([jtype], np.int32), np.array([a], np.int32),
+                                    np.array([b], np.int32), f, np.zeros(1, np.int32), out)
+
+    assert joint(scenes.GEAR, 1, 2, [0.0, 99.0, 1.0]) == _lib.GB_ERR_INVALID  # no joint 99
+    assert joint(scenes.GEAR, 1, 2, [0.0, 2.0, 1.0]) == _lib.GB_ERR_INVALID   # joint 2 is a gear
+    assert joint(scenes.GEAR, 1, 2, [0.5, 1.0, 1.0]) == _lib.GB_ERR_INVALID   # not an index
+    assert joint(scenes.PULLEY, 1, 2, [0.0] * 10 + [0.0]) == _lib.GB_ERR_INVALID
+    assert joint(11, 1, 2, []) == _lib.GB_ERR_INVALID
+    n = len(scenes.gears(scenes.SplitMix64(8)).joints)
+    assert joint(scenes.GEAR, 1, 2, [0.0, 1.0, 2.0]) == _lib.GB_OK and out[0] == n
