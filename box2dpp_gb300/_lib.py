@@ -20,7 +20,8 @@ STATUS_NAMES = {0: "GB_OK", 1: "GB_ERR_CAPACITY", 2: "GB_ERR_TIMEOUT", 3: "GB_ER
 
 # Every symbol include/box2d_gb300.h declares.
 EXPORTS = [
-    "gb_world_create", "gb_world_destroy", "gb_create_bodies", "gb_create_fixtures", "gb_create_revolute_joints",
+    "gb_world_create", "gb_world_destroy", "gb_create_bodies", "gb_create_fixtures", "gb_create_chain",
+    "gb_create_revolute_joints",
     "gb_build_world", "gb_world_upload", "gb_world_step", "gb_world_sync", "gb_world_set_stream",
     "gb_world_counts", "gb_get_bodies", "gb_get_contacts", "gb_get_proxies", "gb_world_stats", "gb_sincos",
     "gb_collide", "gb_version", "gb_world_totals", "gb_set_forces", "gb_get_transforms", "gb_world_profile",
@@ -92,6 +93,7 @@ def load(build_if_missing: bool = True):
         "gb_world_destroy": [vp],
         "gb_create_bodies": [vp, i, i, _i32, _f32, _i32, _i32],
         "gb_create_fixtures": [vp, i, i, _i32, _i32, _f32, _i32, _f32, _i32, _i32],
+        "gb_create_chain": [vp, i, i, _f32, i, i, vp, i, _f32, _i32, vp],
         "gb_create_revolute_joints": [vp, i, i, _i32, _i32, _f32, _i32, _i32],
         "gb_build_world": [vp, i, i, _i32, _f32, _i32, i, _i32, _i32, _f32, _i32, _f32, _i32, i, _i32, _i32, _i32, _f32,
                            _i32],

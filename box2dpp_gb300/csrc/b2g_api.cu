@@ -229,6 +229,7 @@ Shape MakeShape(int type, const float* s, int n)
         sh.type = kEdge; sh.count = 2; sh.radius = kPolygonRadius;
         sh.v[0] = V(s[0], s[1]); sh.v[1] = V(s[2], s[3]); sh.v[2] = V(s[4], s[5]); sh.v[3] = V(s[6], s[7]);
         sh.hasV0 = s[8] != 0.0f; sh.hasV3 = s[9] != 0.0f;
+        sh.chain = (int)s[10];
         break;
     case 2: {
         Vec2 pts[kMaxPolyVerts];
@@ -761,6 +762,13 @@ gb_status CreateFixture(HWorld& W, int body, int type, const float* s, int n, co
     HFixture fx;
     fx.body = body;
     fx.shape = MakeShape(type, s, n);
+    // a chain's next child follows the previous child of the same body
+    const int prevChild = (int)W.fixtures.size() - 1;
+    if (type == 1 && !(s[10] == 0.0f || s[10] == 1.0f || s[10] == 2.0f)) return GB_ERR_INVALID;
+    if (type == 1 && fx.shape.chain == 2 &&
+        (prevChild < 0 || W.fixtures[prevChild].body != body || W.fixtures[prevChild].shape.type != kEdge ||
+         W.fixtures[prevChild].shape.chain == 0))
+        return GB_ERR_INVALID;
     fx.density = mat[0]; fx.friction = mat[1]; fx.restitution = mat[2];
     fx.category = filt[0] & 0xFFFF; fx.mask = filt[1] & 0xFFFF; fx.group = (int16_t)filt[2]; fx.sensor = filt[3] != 0;
     int idx = (int)W.fixtures.size();
@@ -772,8 +780,15 @@ gb_status CreateFixture(HWorld& W, int body, int type, const float* s, int n, co
                                  fx.aabb.z + kAabbExtension, fx.aabb.w + kAabbExtension);
         fx.proxyId = AllocateProxy(W, fat, idx);
     }
-    fx.next = b.fixtureList;
-    b.fixtureList = idx;
+    if (fx.shape.type == kEdge && fx.shape.chain == 2) {
+        // after the previous child: the body's list visits a chain's children in ascending order, as
+        // b2Fixture::Synchronize moves them (b2Fixture.cpp:154-177)
+        fx.next = W.fixtures[prevChild].next;
+        W.fixtures[prevChild].next = idx;
+    } else {
+        fx.next = b.fixtureList;
+        b.fixtureList = idx;
+    }
     W.fixtures.push_back(fx);
     if (fx.density > 0.0f) ResetMassData(W, body);
     W.newFixture = 1;
@@ -999,6 +1014,40 @@ gb_status gb_create_fixtures(gb_world* g, int w, int n, const int* body, const i
         if ((s = CreateFixture(g->worlds[w], body[i], shape_type[i], shape + 16 * i, shape_n[i], mat + 3 * i, filt + 4 * i,
                                out_ids ? out_ids + i : nullptr)) != GB_OK)
             return s;
+    return GB_OK;
+}
+
+gb_status gb_create_chain(gb_world* g, int w, int body, const float* xy, int count, int loop, const float* prev_next,
+                          int ghost_flags, const float* mat, const int* filt, int* first_id)
+{
+    gb_status s = Mutable(g, w);
+    if (s != GB_OK) return s;
+    if (!xy || !mat || !filt || count < (loop ? 3 : 2) || (!loop && ghost_flags != 0 && !prev_next)) return GB_ERR_INVALID;
+    // b2ChainShape::CreateLoop / CreateChain (Collision/Shapes/b2ChainShape.cpp:36-80): a loop repeats
+    // its first vertex and takes the last and second vertices as its ghosts
+    std::vector<Vec2> v((size_t)count + (loop ? 1 : 0));
+    for (int i = 0; i < count; ++i) v[i] = V(xy[2 * i], xy[2 * i + 1]);
+    Vec2 prevV = V(0.0f, 0.0f), nextV = V(0.0f, 0.0f);
+    bool hasPrev = false, hasNext = false;
+    if (loop) {
+        v[count] = v[0];
+        prevV = v[count - 1]; nextV = v[1];
+        hasPrev = hasNext = true;
+    } else {
+        if (ghost_flags & 1) { prevV = V(prev_next[0], prev_next[1]); hasPrev = true; }
+        if (ghost_flags & 2) { nextV = V(prev_next[2], prev_next[3]); hasNext = true; }
+    }
+    // b2ChainShape::GetChildEdge (b2ChainShape.cpp:112-142) for each child, one fixture each
+    const int m = (int)v.size();
+    for (int i = 0; i < m - 1; ++i) {
+        const Vec2 v0 = i > 0 ? v[i - 1] : prevV, v3 = i < m - 2 ? v[i + 2] : nextV;
+        const bool h0 = i > 0 || hasPrev, h3 = i < m - 2 || hasNext;
+        float rec[16] = {v[i].x, v[i].y, v[i + 1].x, v[i + 1].y, v0.x, v0.y, v3.x, v3.y, h0 ? 1.0f : 0.0f,
+                         h3 ? 1.0f : 0.0f, i == 0 ? 1.0f : 2.0f};
+        int id = -1;
+        if ((s = CreateFixture(g->worlds[w], body, 1, rec, 2, mat, filt, &id)) != GB_OK) return s;
+        if (i == 0 && first_id) *first_id = id;
+    }
     return GB_OK;
 }
 

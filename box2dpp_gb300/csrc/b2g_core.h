@@ -249,7 +249,8 @@ struct Shape {
     int count;
     int hasV0, hasV3;
     float radius;
-    float pad[3];
+    int chain;     // an edge that is a chain's child (b2ChainShape::GetChildEdge): 1 the first, 2 a next one
+    float pad[2];
     Vec2 centroid;
     Vec2 v[kMaxPolyVerts];
     Vec2 n[kMaxPolyVerts];
@@ -387,7 +388,8 @@ B2G_HD void ComputeMass(const Shape& s, float density, MassData* md)
     md->I += md->mass * (Dot(md->center, md->center) - Dot(center, center));
 }
 
-// ComputeAABB: polygon (b2PolygonShape.cpp:342-359), circle (b2CircleShape.cpp:86-93), edge (b2EdgeShape.cpp:118-130)
+// ComputeAABB: polygon (b2PolygonShape.cpp:342-359), circle (b2CircleShape.cpp:86-93), edge (b2EdgeShape.cpp:118-130);
+// a chain's child edge has no radius in its box (b2ChainShape.cpp:171-187)
 B2G_HD float4 ComputeAABB(const Shape& s, const Xf& xf)
 {
     float4 o;
@@ -401,6 +403,10 @@ B2G_HD float4 ComputeAABB(const Shape& s, const Xf& xf)
         Vec2 a = Mul(xf, s.v[0]), b = Mul(xf, s.v[1]);
         lower = Min(a, b);
         upper = Max(a, b);
+        if (s.chain) {
+            o.x = lower.x; o.y = lower.y; o.z = upper.x; o.w = upper.y;
+            return o;
+        }
     } else {
         lower = Mul(xf, s.v[0]);
         upper = lower;

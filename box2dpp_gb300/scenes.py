@@ -91,6 +91,30 @@ class Scene:
                               [category, mask, group, int(sensor)]))
         return len(self.fixtures) - 1
 
+    def chain(self, body, vertices, loop=False, prev=None, next_=None, density=0.0, friction=0.2, restitution=0.0,
+              category=1, mask=0xFFFF, group=0, sensor=False) -> int:
+        """b2ChainShape::CreateChain (or CreateLoop) + b2Body::CreateFixture: one edge fixture per child,
+        as b2ChainShape::GetChildEdge (Collision/Shapes/b2ChainShape.cpp:112-142) lays them out, ghost
+        vertices included, flagged as the chain's children (shape[10]: 1 the first, 2 the next ones).
+        prev/next_ are the open chain's SetPrevVertex/SetNextVertex. Returns the first child's id."""
+        pts = [(float(x), float(y)) for (x, y) in vertices]
+        if loop:
+            verts, prev_v, next_v, has_prev, has_next = pts + [pts[0]], pts[-1], pts[1], True, True
+        else:
+            verts = pts
+            prev_v, has_prev = (prev, True) if prev is not None else ((0.0, 0.0), False)
+            next_v, has_next = (next_, True) if next_ is not None else ((0.0, 0.0), False)
+        m = len(verts)
+        assert m >= 2
+        first = len(self.fixtures)
+        for i in range(m - 1):
+            v0, h0 = (verts[i - 1], True) if i > 0 else (prev_v, has_prev)
+            v3, h3 = (verts[i + 2], True) if i < m - 2 else (next_v, has_next)
+            shape = [verts[i][0], verts[i][1], verts[i + 1][0], verts[i + 1][1], v0[0], v0[1], v3[0], v3[1],
+                     float(h0), float(h3), 1.0 if i == 0 else 2.0]
+            self.fixture(body, EDGE, shape, 2, density, friction, restitution, category, mask, group, sensor)
+        return first
+
     def revolute(self, a, b, anchor_a, anchor_b, ref_angle=0.0, lower=0.0, upper=0.0, motor_speed=0.0,
                  max_motor_torque=0.0, flags=0) -> int:
         self.joints.append((a, b, [anchor_a[0], anchor_a[1], anchor_b[0], anchor_b[1], ref_angle, lower,
@@ -531,6 +555,37 @@ def gears(rng: SplitMix64, allow_sleep: bool = True) -> Scene:
         e = s.body(DYNAMIC, x, _q(12.0 + 1.5 * i + rng.uniform(0.0, 1.0)), angle=_q(rng.uniform(-0.4, 0.4)))
         s.fixture(e, CIRCLE if i % 2 else BOX, [0.0, 0.0, 0.3] if i % 2 else [0.3, 0.3], 1 if i % 2 else 2,
                   density=1.0, friction=0.5)
+    return _settings(s, allow_sleep)
+
+
+def chain_terrain(rng: SplitMix64, allow_sleep: bool = True) -> Scene:
+    """Chain shapes: a static open terrain chain of 40 segments with ghost vertices past both ends, a
+    static closed loop holding a few bodies, a kinematic body carrying a zig-zag chain across the
+    scene, and circles, boxes and fast bullets (continuous collision against chain children) falling
+    onto them."""
+    s = Scene(name="chain_terrain")
+    g = s.body(STATIC, 0.0, 0.0)
+    terrain = [(-40.0 + 2.0 * i, _q(1.2 * math.sin(0.6 * i) + 0.4 * rng.uniform(-1.0, 1.0))) for i in range(41)]
+    s.chain(g, terrain, prev=(-42.0, 0.0), next_=(42.0, 0.0), friction=0.6)
+    box = s.body(STATIC, 28.0, 10.0, angle=0.1)
+    s.chain(box, [(-4.0, -3.0), (4.0, -3.0), (4.0, 3.0), (-4.0, 3.0)], loop=True, friction=0.4)
+    for i in range(4):
+        b = s.body(DYNAMIC, _q(26.0 + 1.3 * i), _q(10.0 + rng.uniform(-1.0, 1.0)), vx=_q(rng.uniform(-4.0, 4.0)),
+                   w=_q(rng.uniform(-2.0, 2.0)))
+        s.fixture(b, CIRCLE if i % 2 else BOX, [0.0, 0.0, 0.5] if i % 2 else [0.5, 0.4], 1 if i % 2 else 2,
+                  density=1.0, friction=0.3, restitution=0.3)
+    k = s.body(KINEMATIC, -12.0, 9.0, vx=1.5, w=0.15)
+    s.chain(k, [(-3.0, 0.0), (-1.0, 1.0), (1.0, 0.0), (3.0, 1.0)], friction=0.5)
+    for i in range(40):
+        x = _q(rng.uniform(-36.0, 22.0))
+        y = _q(rng.uniform(5.0, 22.0))
+        bullet = i % 10 == 9
+        b = s.body(DYNAMIC, x, y, angle=_q(rng.uniform(-1.0, 1.0)), vy=-60.0 if bullet else 0.0,
+                   flags=DEFAULT_FLAGS | (8 if bullet else 0))
+        if i % 3 == 0:
+            s.fixture(b, CIRCLE, [0.0, 0.0, _q(rng.uniform(0.2, 0.6))], 1, density=1.0, friction=0.4)
+        else:
+            s.fixture(b, BOX, [_q(rng.uniform(0.2, 0.6)), _q(rng.uniform(0.2, 0.6))], 2, density=1.0, friction=0.4)
     return _settings(s, allow_sleep)
 
 

@@ -201,7 +201,10 @@ class World:
         return ints[:cnt], flts[:cnt]
 
     def proxies(self, w: int = 0):
-        nf = self.n_fixtures[w]
+        # sized from the library's count: fixtures may have been added by direct C-ABI calls
+        n = C.c_int()
+        _lib.check(self.lib.gb_world_counts(self.h, w, None, C.byref(n), None, None), "gb_world_counts")
+        nf = n.value
         ids = np.zeros(max(nf, 1), dtype=np.int32)
         fat = np.zeros((max(nf, 1), 4), dtype=np.float32)
         _lib.check(self.lib.gb_get_proxies(self.h, w, ids, fat), "gb_get_proxies")

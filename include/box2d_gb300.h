@@ -55,13 +55,25 @@ gb_status gb_create_bodies(gb_world* world, int w, int n, const int* type, const
                            int* out_ids);
 
 /* b2Body::CreateFixture (Box2D/Dynamics/b2Body.cpp:151). Per fixture: body index; shape type
- * 0 circle {p.x, p.y, radius}, 1 edge {v1.x, v1.y, v2.x, v2.y, v0.x, v0.y, v3.x, v3.y, hasV0, hasV3},
+ * 0 circle {p.x, p.y, radius}, 1 edge {v1.x, v1.y, v2.x, v2.y, v0.x, v0.y, v3.x, v3.y, hasV0, hasV3,
+ * chain} (chain 0 for a b2EdgeShape; 1 and 2 for the first and each next child of a chain, as
+ * gb_create_chain writes them: a child's box has no radius, b2ChainShape.cpp:171-187),
  * 2 polygon from n points (b2PolygonShape::Set), 3 box {hx, hy} or, with n == 5, {hx, hy, center.x,
  * center.y, angle} (b2PolygonShape::SetAsBox); shape[16] per fixture; mat[3] = density, friction,
  * restitution; filt[4] = categoryBits, maskBits, groupIndex, isSensor. */
 gb_status gb_create_fixtures(gb_world* world, int w, int n, const int* body, const int* shape_type,
                              const float* shape, const int* shape_n, const float* mat, const int* filt,
                              int* out_ids);
+
+/* b2ChainShape::CreateChain or CreateLoop + b2Body::CreateFixture (Box2D/Collision/Shapes/
+ * b2ChainShape.cpp:36-80, Box2D/Dynamics/b2Fixture.cpp:121-137): count vertices xy[2 * count] make
+ * count - 1 child edges (a loop, loop != 0, closes with a count-th), each with its ghost vertices as
+ * b2ChainShape::GetChildEdge gives them, created as consecutive fixtures from *first_id on; the
+ * fixture ids that contacts, events and queries report for the chain are first_id + child index.
+ * An open chain's SetPrevVertex / SetNextVertex: prev_next = {prev.x, prev.y, next.x, next.y} with
+ * ghost_flags bit 0 / bit 1. mat and filt as gb_create_fixtures, shared by the children. */
+gb_status gb_create_chain(gb_world* world, int w, int body, const float* xy, int count, int loop,
+                          const float* prev_next, int ghost_flags, const float* mat, const int* filt, int* first_id);
 
 /* b2World::CreateJoint with a b2RevoluteJointDef (Box2D/Dynamics/b2World.cpp:185,
  * Box2D/Dynamics/Joints/b2RevoluteJoint.h:36). f[9] = localAnchorA.x, .y, localAnchorB.x, .y,

@@ -66,7 +66,7 @@ struct b2BodyDef {
 // ---------------------------------------------------------------- shapes (Collision/Shapes/*.h)
 class b2Shape {
 public:
-    enum Type { e_circle = 0, e_edge = 1, e_polygon = 2 };
+    enum Type { e_circle = 0, e_edge = 1, e_polygon = 2, e_chain = 3 };
     virtual ~b2Shape() = default;
     Type GetType() const { return m_type; }
     // C-ABI encoding (gb_create_fixtures): type code, 16 floats, count
@@ -99,6 +99,55 @@ public:
     }
     b2Vec2 m_vertex1, m_vertex2, m_vertex0, m_vertex3;
     bool m_hasVertex0 = false, m_hasVertex3 = false;
+};
+
+// b2ChainShape (Box2D/Collision/Shapes/b2ChainShape.h:33-94): a free-form sequence of edges, open
+// (CreateChain, optional ghost vertices before the first and after the last vertex) or closed
+// (CreateLoop). b2Body::CreateFixture makes it through gb_create_chain, one device fixture per child.
+class b2ChainShape : public b2Shape {
+public:
+    b2ChainShape() { m_type = e_chain; m_radius = 0.01f; }
+    void CreateLoop(const b2Vec2* vertices, int count)
+    {
+        m_vertices.assign(vertices, vertices + count);
+        m_loop = true;
+        m_hasPrevVertex = m_hasNextVertex = false;
+    }
+    void CreateChain(const b2Vec2* vertices, int count)
+    {
+        m_vertices.assign(vertices, vertices + count);
+        m_loop = false;
+        m_hasPrevVertex = m_hasNextVertex = false;
+    }
+    void SetPrevVertex(const b2Vec2& v) { m_prevVertex = v; m_hasPrevVertex = true; }
+    void SetNextVertex(const b2Vec2& v) { m_nextVertex = v; m_hasNextVertex = true; }
+    int GetChildCount() const
+    {
+        const int n = (int)m_vertices.size();
+        return m_loop ? n : (n > 0 ? n - 1 : 0);
+    }
+    // b2ChainShape::GetChildEdge (b2ChainShape.cpp:112-142): child index's edge with its ghost vertices
+    void GetChildEdge(b2EdgeShape* edge, int index) const
+    {
+        const int n = (int)m_vertices.size();
+        auto at = [&](int i) { return m_vertices[m_loop ? i % n : i]; };
+        const int last = GetChildCount() - 1;
+        edge->m_radius = m_radius;
+        edge->m_vertex1 = at(index);
+        edge->m_vertex2 = at(index + 1);
+        if (index > 0) { edge->m_vertex0 = at(index - 1); edge->m_hasVertex0 = true; }
+        else if (m_loop) { edge->m_vertex0 = m_vertices[n - 1]; edge->m_hasVertex0 = true; }
+        else { edge->m_vertex0 = m_prevVertex; edge->m_hasVertex0 = m_hasPrevVertex; }
+        if (index < last) { edge->m_vertex3 = at(index + 2); edge->m_hasVertex3 = true; }
+        else if (m_loop) { edge->m_vertex3 = m_vertices[1]; edge->m_hasVertex3 = true; }
+        else { edge->m_vertex3 = m_nextVertex; edge->m_hasVertex3 = m_hasNextVertex; }
+    }
+    // no single record: b2World::AddFixture passes the vertices to gb_create_chain
+    void Encode(int* type, float* shape, int* n) const override { *type = -1; *n = 0; (void)shape; }
+
+    std::vector<b2Vec2> m_vertices;
+    b2Vec2 m_prevVertex, m_nextVertex;
+    bool m_hasPrevVertex = false, m_hasNextVertex = false, m_loop = false;
 };
 
 class b2PolygonShape : public b2Shape {
@@ -388,6 +437,8 @@ class b2Contact {
 public:
     b2Fixture* GetFixtureA() const { return m_a; }
     b2Fixture* GetFixtureB() const { return m_b; }
+    int GetChildIndexA() const { return m_childA; }  // the chain child, 0 for other shapes
+    int GetChildIndexB() const { return m_childB; }
     bool IsTouching() const { return (m_flags & 2) != 0; }
     bool IsEnabled() const { return (m_flags & 4) != 0; }
     const b2Manifold* GetManifold() const { return &m_manifold; }
@@ -395,6 +446,8 @@ public:
 private:
     friend class b2World;
     b2Fixture *m_a = nullptr, *m_b = nullptr;
+    int m_childA = 0, m_childB = 0;
+    int m_idA = -1, m_idB = -1;  // device fixture ids (one per chain child)
     int m_flags = 0;
     b2Manifold m_manifold;
 };
@@ -595,14 +648,28 @@ public:
         const float mat[3] = {def->density, def->friction, def->restitution};
         const int filt[4] = {def->filter.categoryBits, def->filter.maskBits, def->filter.groupIndex, def->isSensor ? 1 : 0};
         const int b = body->GetIndex();
-        int id = -1;
-        if (gb_create_fixtures(m_h, 0, 1, &b, &type, shape, &n, mat, filt, &id) != GB_OK) return nullptr;
+        int id = -1, children = 1;
+        if (def->shape->GetType() == b2Shape::e_chain) {
+            const b2ChainShape* chain = static_cast<const b2ChainShape*>(def->shape);
+            std::vector<float> xy;
+            for (const b2Vec2& v : chain->m_vertices) { xy.push_back(v.x); xy.push_back(v.y); }
+            const float pn[4] = {chain->m_prevVertex.x, chain->m_prevVertex.y, chain->m_nextVertex.x,
+                                 chain->m_nextVertex.y};
+            const int ghosts = (chain->m_hasPrevVertex ? 1 : 0) | (chain->m_hasNextVertex ? 2 : 0);
+            if (gb_create_chain(m_h, 0, b, xy.data(), (int)chain->m_vertices.size(), chain->m_loop ? 1 : 0, pn,
+                                ghosts, mat, filt, &id) != GB_OK)
+                return nullptr;
+            children = chain->GetChildCount();
+        } else if (gb_create_fixtures(m_h, 0, 1, &b, &type, shape, &n, mat, filt, &id) != GB_OK) {
+            return nullptr;
+        }
         std::unique_ptr<b2Fixture> fx(new b2Fixture());
         fx->m_body = body;
         fx->m_index = id;
         fx->m_def = *def;
         fx->m_def.shape = nullptr;
         fx->m_type = def->shape->GetType();
+        for (int k = 0; k < children; ++k) m_fixtureOfId.push_back({fx.get(), k});
         m_fixtures.push_back(std::move(fx));
         m_stale = true;
         return m_fixtures.back().get();
@@ -659,8 +726,12 @@ private:
             std::unique_ptr<b2Contact> c(new b2Contact());
             const int* I = &ints[8 * (size_t)i];
             const float* F = &flts[12 * (size_t)i];
-            c->m_a = m_fixtures[I[0]].get();
-            c->m_b = m_fixtures[I[1]].get();
+            c->m_a = m_fixtureOfId[I[0]].first;
+            c->m_b = m_fixtureOfId[I[1]].first;
+            c->m_childA = m_fixtureOfId[I[0]].second;
+            c->m_childB = m_fixtureOfId[I[1]].second;
+            c->m_idA = I[0];
+            c->m_idB = I[1];
             c->m_flags = I[2];
             b2Manifold& m = c->m_manifold;
             m.pointCount = I[3];
@@ -681,8 +752,8 @@ private:
         std::vector<std::unique_ptr<b2Contact>> old = std::move(m_contacts);
         ReadContacts();
         std::map<std::pair<int, int>, b2Contact*> now, before;
-        for (auto& c : m_contacts) now[{c->m_a->GetIndex(), c->m_b->GetIndex()}] = c.get();
-        for (auto& c : old) before[{c->m_a->GetIndex(), c->m_b->GetIndex()}] = c.get();
+        for (auto& c : m_contacts) now[{c->m_idA, c->m_idB}] = c.get();
+        for (auto& c : old) before[{c->m_idA, c->m_idB}] = c.get();
         int n = 0;
         gb_world_read_events(m_h, 0, nullptr, nullptr, 0, &n);
         std::vector<int> rec(4 * (size_t)(n > 0 ? n : 1));
@@ -717,6 +788,7 @@ private:
     b2ContactListener* m_listener = nullptr;
     std::vector<std::unique_ptr<b2Body>> m_bodies;
     std::vector<std::unique_ptr<b2Fixture>> m_fixtures;
+    std::vector<std::pair<b2Fixture*, int>> m_fixtureOfId;  // device fixture id -> fixture, chain child
     std::vector<std::unique_ptr<b2Joint>> m_joints;
     std::vector<std::unique_ptr<b2Contact>> m_contacts, m_old;
     bool m_eventsOn = false;

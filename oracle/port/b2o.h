@@ -174,6 +174,7 @@ struct Shape {
     Vec2 p{0, 0};                    // circle center
     Vec2 v0{0, 0}, v1{0, 0}, v2{0, 0}, v3{0, 0};
     bool hasV0 = false, hasV3 = false; // edge
+    int chain = 0;                     // edge that is a chain's child: 1 the first, 2 a next one
     int count = 0;
     Vec2 verts[kMaxPolygonVertices], normals[kMaxPolygonVertices];
     Vec2 centroid{0, 0};             // polygon

@@ -20,6 +20,7 @@ Shape MakeShape(int type, const float* s, int n)
         sh.type = kEdge; sh.radius = kPolygonRadius;
         sh.v1 = V(s[0], s[1]); sh.v2 = V(s[2], s[3]); sh.v0 = V(s[4], s[5]); sh.v3 = V(s[6], s[7]);
         sh.hasV0 = s[8] != 0.0f; sh.hasV3 = s[9] != 0.0f;
+        sh.chain = (int)s[10];
         break;
     case 2: {
         Vec2 pts[kMaxPolygonVertices];

@@ -151,7 +151,8 @@ void ComputeMass(const Shape& s, float density, MassData* md)
     md->I += md->mass * (Dot(md->center, md->center) - Dot(center, center));
 }
 
-// ComputeAABB: polygon (b2PolygonShape.cpp:342-359), circle (b2CircleShape.cpp:86-93), edge (b2EdgeShape.cpp:118-130)
+// ComputeAABB: polygon (b2PolygonShape.cpp:342-359), circle (b2CircleShape.cpp:86-93), edge (b2EdgeShape.cpp:118-130);
+// a chain's child edge without the radius (b2ChainShape.cpp:171-187)
 void ComputeAABB(const Shape& s, const Xf& xf, AABB* out)
 {
     if (s.type == kCircle) {
@@ -165,6 +166,11 @@ void ComputeAABB(const Shape& s, const Xf& xf, AABB* out)
         Vec2 a = Mul(xf, s.v1), b = Mul(xf, s.v2);
         lower = Min(a, b);
         upper = Max(a, b);
+        if (s.chain) {
+            out->lo = lower;
+            out->hi = upper;
+            return;
+        }
     } else {
         lower = Mul(xf, s.verts[0]);
         upper = lower;

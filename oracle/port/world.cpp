@@ -109,8 +109,15 @@ int World::CreateFixture(int bi, const Shape& shape, float density, float fricti
         ComputeAABB(f.shape, b.xf, &f.aabb);
         f.proxyId = bp.CreateProxy(f.aabb, id);
     }
-    fixtures[id].next = b.fixtureList;
-    b.fixtureList = id;
+    if (shape.chain == 2) {
+        // a chain's next child: after the previous one, so the body's list visits a chain's children
+        // in ascending order as b2Fixture::Synchronize does (b2Fixture.cpp:154-177)
+        fixtures[id].next = fixtures[id - 1].next;
+        fixtures[id - 1].next = id;
+    } else {
+        fixtures[id].next = b.fixtureList;
+        b.fixtureList = id;
+    }
     if (density > 0.0f) ResetMassData(bi);
     wflags |= 0x1; // e_newFixture
     return id;

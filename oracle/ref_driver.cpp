@@ -98,6 +98,7 @@ int rw_fixture(void* h, int body, int shapeType, const float* s, int n, const fl
         fd.shape = &circle;
         break;
     case 1:
+        if (s[10] != 0.0f) return -1;  // chain children are built by rw_build (rw_chain)
         edge.Set(b2Vec2(s[0], s[1]), b2Vec2(s[2], s[3]));
         edge.m_vertex0.Set(s[4], s[5]);
         edge.m_vertex3.Set(s[6], s[7]);
@@ -278,6 +279,8 @@ int rw_joint(void* h, int type, int bodyA, int bodyB, const float* f, int flags)
     return (int)w->joints.size() - 1;
 }
 
+int rw_chain(void* h, int body, int nchild, const float* s, const float* mat, const int* filt);
+
 // Bulk scene build: body b is created, then its fixtures (fbody is non-decreasing), then all joints.
 void rw_build(void* h, int nb, const int* btype, const float* bf, const int* bflags, int nf, const int* fbody,
               const int* ftype, const float* fshape, const int* fn, const float* fmat, const int* ffilt, int nj,
@@ -287,7 +290,15 @@ void rw_build(void* h, int nb, const int* btype, const float* bf, const int* bfl
     for (int b = 0; b < nb; ++b) {
         rw_body(h, btype[b], bf + 9 * b, bflags[b]);
         while (fi < nf && fbody[fi] == b) {
-            rw_fixture(h, b, ftype[fi], fshape + 16 * fi, fn[fi], fmat + 3 * fi, ffilt + 4 * fi);
+            const float* s = fshape + 16 * fi;
+            if (ftype[fi] == 1 && s[10] == 1.0f) {
+                int n = 1;
+                while (fi + n < nf && fbody[fi + n] == b && ftype[fi + n] == 1 && fshape[16 * (fi + n) + 10] == 2.0f) ++n;
+                rw_chain(h, b, n, s, fmat + 3 * fi, ffilt + 4 * fi);
+                fi += n;
+                continue;
+            }
+            rw_fixture(h, b, ftype[fi], s, fn[fi], fmat + 3 * fi, ffilt + 4 * fi);
             ++fi;
         }
     }
@@ -338,6 +349,39 @@ void rw_get_bodies(void* h, float* out)
     }
 }
 
+// A chain fixture from consecutive edge records flagged as chain children (s[10]: 1 the first
+// child, 2 each next one): b2ChainShape::CreateChain over the children's first vertices and the last
+// child's second, the first child's ghost vertex as prevVertex and the last child's as nextVertex
+// (for a closed chain this equals b2ChainShape::CreateLoop). One b2Fixture stands for the records;
+// their ids are its first id + the child index.
+int rw_chain(void* h, int body, int nchild, const float* s, const float* mat, const int* filt)
+{
+    RefWorld* w = static_cast<RefWorld*>(h);
+    std::vector<b2Vec2> v((size_t)nchild + 1);
+    for (int i = 0; i < nchild; ++i) v[i].Set(s[16 * i], s[16 * i + 1]);
+    const float* first = s;
+    const float* last = s + 16 * (nchild - 1);
+    v[nchild].Set(last[2], last[3]);
+    b2ChainShape chain;
+    chain.CreateChain(v.data(), nchild + 1);
+    if (first[8] != 0.0f) chain.SetPrevVertex(b2Vec2(first[4], first[5]));
+    if (last[9] != 0.0f) chain.SetNextVertex(b2Vec2(last[6], last[7]));
+    b2FixtureDef fd;
+    fd.shape = &chain;
+    fd.density = mat[0];
+    fd.friction = mat[1];
+    fd.restitution = mat[2];
+    fd.filter.categoryBits = (uint16)filt[0];
+    fd.filter.maskBits = (uint16)filt[1];
+    fd.filter.groupIndex = (int16)filt[2];
+    fd.isSensor = filt[3] != 0;
+    const int id = (int)w->fixtures.size();
+    fd.userData = (void*)(intptr_t)(id + 1);
+    b2Fixture* fx = w->bodies[body]->CreateFixture(&fd);
+    for (int i = 0; i < nchild; ++i) w->fixtures.push_back(fx);
+    return id;
+}
+
 // Contacts in world-list order. ints (8 per contact): fixtureA, fixtureB, flags, pointCount,
 // manifold type, id0 key, id1 key, toiCount. floats (12 per contact): localNormal.xy,
 // localPoint.xy, then per point: localPoint.xy, normalImpulse, tangentImpulse.
@@ -350,7 +394,8 @@ int rw_get_contacts(void* h, int* ints, float* flts, int cap)
             int* i = ints + 8 * n;
             float* f = flts + 12 * n;
             const b2Manifold& m = c->m_manifold;
-            i[0] = fixture_index(c->m_fixtureA); i[1] = fixture_index(c->m_fixtureB);
+            i[0] = fixture_index(c->m_fixtureA) + c->GetChildIndexA();
+            i[1] = fixture_index(c->m_fixtureB) + c->GetChildIndexB();
             i[2] = (int)c->m_flags; i[3] = m.pointCount; i[4] = m.pointCount > 0 ? (int)m.type : 0;
             i[5] = m.pointCount > 0 ? (int)m.points[0].id.key : 0;
             i[6] = m.pointCount > 1 ? (int)m.points[1].id.key : 0;

@@ -65,6 +65,7 @@ def cases():
         ("joint_zoo", lambda: scenes.joint_zoo(scenes.SplitMix64(6)), 300, [1, 60, 150, 300]),
         ("pulley_mouse", lambda: scenes.pulley_mouse(scenes.SplitMix64(4)), 300, [1, 60, 150, 300]),
         ("gears", lambda: scenes.gears(scenes.SplitMix64(8)), 300, [1, 60, 150, 300]),
+        ("chain_terrain", lambda: scenes.chain_terrain(scenes.SplitMix64(12)), 300, [1, 60, 150, 300]),
     ] + [(f"batch{i}", (lambda i=i: batch_world(i)), 200, [200]) for i in range(24)]
 
 

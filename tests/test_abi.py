@@ -35,6 +35,7 @@ def test_library_exports_every_declared_symbol():
     lambda: scenes.drop(300, scenes.SplitMix64(2)),
     lambda: scenes.chains(3, 6, scenes.SplitMix64(1)),
     lambda: scenes.stacks(50, scenes.SplitMix64(8)),
+    lambda: scenes.chain_terrain(scenes.SplitMix64(12)),
 ])
 def test_host_setup_equals_oracle(make):
     sc = make()
@@ -82,3 +83,40 @@ def test_joint_records_validated():
     assert joint(11, 1, 2, []) == _lib.GB_ERR_INVALID
     n = len(scenes.gears(scenes.SplitMix64(8)).joints)
     assert joint(scenes.GEAR, 1, 2, [0.0, 1.0, 2.0]) == _lib.GB_OK and out[0] == n
+
+
+def test_create_chain_matches_child_records():
+    """gb_create_chain (b2ChainShape::CreateChain / CreateLoop + CreateFixture) makes the same child
+    fixtures, proxies and fat AABBs as the scene's child-edge records, for an open chain with ghost
+    vertices and a loop; too few vertices are refused."""
+    import ctypes as C
+
+    lib = _lib.load()
+    pts = [(-6.0, 0.0), (-3.0, 1.0), (0.0, 0.5), (3.0, 1.5), (6.0, 0.0)]
+    box = [(-2.0, -1.0), (2.0, -1.0), (2.0, 1.0), (-2.0, 1.0)]
+    ref = scenes.Scene(name="chain_records")
+    g = ref.body(scenes.STATIC, 0.0, 0.0)
+    ref.chain(g, pts, prev=(-8.0, -1.0), next_=(8.0, -1.0), friction=0.5)
+    k = ref.body(scenes.KINEMATIC, 1.0, 5.0, angle=0.3)
+    ref.chain(k, box, loop=True, friction=0.5)
+    want = World(ref)
+
+    bare = scenes.Scene(name="chain_call")
+    bare.body(scenes.STATIC, 0.0, 0.0)
+    bare.body(scenes.KINEMATIC, 1.0, 5.0, angle=0.3)
+    got = World(bare)
+    mat = np.array([0.0, 0.5, 0.0], np.float32)
+    filt = np.array([1, 0xFFFF, 0, 0], np.int32)
+    first = C.c_int(-1)
+    pn = np.array([-8.0, -1.0, 8.0, -1.0], np.float32)
+    assert lib.gb_create_chain(got.h, 0, 0, np.array(pts, np.float32).ravel(), len(pts), 0, pn.ctypes.data, 3, mat,
+                               filt, C.byref(first)) == _lib.GB_OK and first.value == 0
+    assert lib.gb_create_chain(got.h, 0, 1, np.array(box, np.float32).ravel(), len(box), 1, None, 0, mat, filt,
+                               C.byref(first)) == _lib.GB_OK and first.value == len(pts) - 1
+    gi, gf = got.proxies()
+    wi, wf = want.proxies()
+    assert len(gi) == len(pts) - 1 + len(box)
+    assert np.array_equal(gi, wi)
+    assert np.array_equal(gf.view(np.uint32), wf.view(np.uint32))
+    assert lib.gb_create_chain(got.h, 0, 1, np.array(box[:2], np.float32).ravel(), 2, 1, None, 0, mat, filt,
+                               C.byref(first)) == _lib.GB_ERR_INVALID

@@ -173,3 +173,66 @@ def test_cpp_mouse_pulley_match_oracle(gpu, tmp_path):
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
     # the dragged box followed the target to the right, the pulley moved
     assert want[-1, 6] > 5.0 and want[-1, 1] != 5.0
+
+
+CHAIN_SRC = os.path.join(ROOT, "tests", "cpp", "chain.cpp")
+
+
+def _compile_chain(tmp_path):
+    lib = _lib.library_path()
+    exe = str(tmp_path / "chain")
+    libdir = os.path.dirname(lib)
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "include"), CHAIN_SRC, "-o", exe,
+           "-L", libdir, "-lbox2d_gb300", f"-Wl,-rpath,{libdir}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return exe
+
+
+def test_cpp_chain_compile(tmp_path):
+    _compile_chain(tmp_path)
+
+
+def chain_scene():
+    """The scene tests/cpp/chain.cpp builds, as scene records."""
+    sc = scenes.Scene(name="chain_cpp")
+    g = sc.body(scenes.STATIC, 0.0, 0.0)
+    terrain = [(-8.0 + 2.0 * i, 0.5 if i % 2 else 0.0) for i in range(9)]
+    sc.chain(g, terrain, prev=(-10.0, 1.0), next_=(10.0, 1.0), friction=0.6)
+    c = sc.body(scenes.STATIC, 14.0, 4.0, angle=0.2)
+    sc.chain(c, [(-3.0, -2.0), (3.0, -2.0), (3.0, 2.0), (-3.0, 2.0)], loop=True, friction=0.4)
+    for i in range(8):
+        b = sc.body(scenes.DYNAMIC, -7.0 + 2.5 * i if i < 6 else 13.0 + 2.0 * (i - 6), 3.0 if i < 6 else 4.0,
+                    angle=float(np.float32(0.1) * np.float32(i)))
+        if i % 2:
+            sc.fixture(b, scenes.CIRCLE, [0.0, 0.0, 0.4], 1, density=1.0, friction=0.4)
+        else:
+            sc.fixture(b, scenes.BOX, [0.4, 0.3], 2, density=1.0, friction=0.4)
+    return sc
+
+
+@pytest.mark.gpu
+def test_cpp_chain_match_oracle(gpu, tmp_path):
+    """b2ChainShape::CreateChain / CreateLoop through the C++ mirror: positions bit for bit like the
+    CPU oracle (itself bit-exact with the reference's b2ChainShape), and the contacts' chain child
+    indices (b2Contact::GetChildIndexA) as the oracle's fixture ids give them."""
+    exe = _compile_chain(tmp_path)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.strip().splitlines()
+    got = np.array([[float.fromhex(v) for v in ln.split()[1:]] for ln in lines[:120]], dtype=np.float32)
+    got_children = sorted(tuple(int(t) for t in ln.split()[1::2]) for ln in lines[120:])
+    sc = chain_scene()
+    o = oracle.OracleWorld(sc, "port", "project")
+    want = []
+    for _ in range(120):
+        o.step(1.0 / 60.0, 8, 3)
+        s = o.bodies()
+        want.append([s[k, c] for k in range(2, 10) for c in (0, 1)])
+    want = np.array(want, dtype=np.float32)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    ci, _ = o.contacts()
+    fbody = [f[0] for f in sc.fixtures]
+    want_children = sorted((0 if f < 8 else 1, f if f < 8 else f - 8, fbody[fb]) for f, fb in zip(ci[:, 0], ci[:, 1])
+                           if f < 12)
+    assert got_children == want_children and len(want_children) > 0
