@@ -19,10 +19,11 @@
 #include "../../include/box2d_gb300.h"
 #include "b2g_world.h"
 
-cudaError_t b2gLaunchNarrowphase(const b2g::Batch& B, cudaStream_t stream);
+cudaError_t b2gLaunchNarrowphase(const b2g::Batch& B, const int* slotOf, int first, int count, cudaStream_t stream);
 cudaError_t b2gLaunchStep(const b2g::Batch& B, const b2g::StepParams& P, const int* schedule, int first, int count,
                           int threads, int smemRows, int smemContacts, cudaStream_t stream);
-cudaError_t b2gLaunchToi(const b2g::Batch& B, const b2g::StepParams& P, cudaStream_t stream);
+cudaError_t b2gLaunchToi(const b2g::Batch& B, const b2g::StepParams& P, const int* slotOf, int first, int count,
+                         cudaStream_t stream);
 cudaError_t b2gLaunchBodyEdits(const b2g::Batch& B, const b2g::BodyEdit* edits, int n, cudaStream_t stream);
 cudaError_t b2gLaunchStepToi(const b2g::Batch& B, const b2g::StepParams& P, const int* schedule, int first, int count,
                              int threads, int smemRows, int smemContacts, cudaStream_t stream);
@@ -102,6 +103,7 @@ struct gb_world {
     Batch batch{};
     std::vector<void*> allocations;
     int* dSchedule = nullptr;
+    int* dSlotOf = nullptr;  // schedule slot of each world (the inverse of dSchedule)
     cudaStream_t stream = nullptr;
     bool ownStream = false;
     bool onDevice = false;   // device columns hold the current state
@@ -113,6 +115,9 @@ struct gb_world {
     LaunchPlan plan;
     cudaStream_t side[kMaxClasses] = {};
     cudaEvent_t fork = nullptr, join[kMaxClasses] = {};
+    // the step's per-class pipelines: class i on pipe[i], priorities falling with i
+    cudaStream_t pipe[kMaxClasses] = {};
+    cudaEvent_t pipeJoin[kMaxClasses] = {};
     // online autotuning of the plan over real steps (every plan gives identical results)
     std::vector<LaunchPlan> candidates;
     std::vector<float> candidateMs;
@@ -266,6 +271,7 @@ void FreeDevice(gb_world* g)
     g->allocations.clear();
     std::memset(&g->batch, 0, sizeof(g->batch));
     g->dSchedule = nullptr;
+    g->dSlotOf = nullptr;
 }
 
 int NextPow2(int x)
@@ -470,15 +476,45 @@ gb_status LaunchClasses(gb_world* g, const StepParams& P, const LaunchPlan& plan
     return GB_OK;
 }
 
-// One step of every world with the given plan: the flat narrowphase pre-pass, the per-world step up
-// to the continuous phase, the flat time-of-impact pre-pass, the per-world continuous phase.
+gb_status EnsurePipeStreams(gb_world* g, int n)
+{
+    if (!g->fork) GB_CUDA(cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming));
+    int least = 0, greatest = 0;
+    GB_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    for (int i = 0; i < n && i < kMaxClasses; ++i) {
+        // greatest is the numerically lowest value; class 0 (the largest worlds) gets it
+        const int prio = std::min(greatest + i, least);
+        if (!g->pipe[i]) GB_CUDA(cudaStreamCreateWithPriority(&g->pipe[i], cudaStreamNonBlocking, prio));
+        if (!g->pipeJoin[i]) GB_CUDA(cudaEventCreateWithFlags(&g->pipeJoin[i], cudaEventDisableTiming));
+    }
+    return GB_OK;
+}
+
+// One step of every world with the given plan. Each class of the plan is a pipeline of its own on
+// its own stream: the narrowphase pre-pass over its worlds' contact rows, the per-world step up to
+// the continuous phase, the time-of-impact pre-pass over its worlds' rows, the per-world continuous
+// phase. No stage waits for another class, so the continuous-phase tail of one class (a few worlds'
+// event loops) overlaps the step of the others; stream priorities falling with the class keep the
+// largest worlds' CTAs dispatched first. Worlds are independent, so any interleaving gives the
+// same results.
 gb_status LaunchPlanStep(gb_world* g, const StepParams& P, const LaunchPlan& plan)
 {
-    GB_CUDA(b2gLaunchNarrowphase(g->batch, g->stream));
-    gb_status s = LaunchClasses(g, P, plan, b2gLaunchStep);
+    const int n = std::min((int)plan.size(), kMaxClasses);
+    gb_status s = EnsurePipeStreams(g, n);
     if (s != GB_OK) return s;
-    GB_CUDA(b2gLaunchToi(g->batch, P, g->stream));
-    return LaunchClasses(g, P, plan, b2gLaunchStepToi);
+    GB_CUDA(cudaEventRecord(g->fork, g->stream));
+    for (int i = 0; i < n; ++i) {
+        const LaunchClass& c = plan[i];
+        cudaStream_t st = g->pipe[i];
+        GB_CUDA(cudaStreamWaitEvent(st, g->fork, 0));
+        GB_CUDA(b2gLaunchNarrowphase(g->batch, g->dSlotOf, c.first, c.count, st));
+        GB_CUDA(b2gLaunchStep(g->batch, P, g->dSchedule, c.first, c.count, c.threads, c.rows, c.contacts, st));
+        GB_CUDA(b2gLaunchToi(g->batch, P, g->dSlotOf, c.first, c.count, st));
+        GB_CUDA(b2gLaunchStepToi(g->batch, P, g->dSchedule, c.first, c.count, c.threads, c.rows, c.contacts, st));
+        GB_CUDA(cudaEventRecord(g->pipeJoin[i], st));
+    }
+    for (int i = 0; i < n; ++i) GB_CUDA(cudaStreamWaitEvent(g->stream, g->pipeJoin[i], 0));
+    return GB_OK;
 }
 
 // A step of the online autotuner: the candidate under trial, timed with events on the handle's
@@ -540,6 +576,12 @@ void ReleaseLaunchResources(gb_world* g)
         if (g->join[i]) cudaEventDestroy(g->join[i]);
         g->side[i] = nullptr;
         g->join[i] = nullptr;
+    }
+    for (int i = 0; i < kMaxClasses; ++i) {
+        if (g->pipe[i]) cudaStreamDestroy(g->pipe[i]);
+        if (g->pipeJoin[i]) cudaEventDestroy(g->pipeJoin[i]);
+        g->pipe[i] = nullptr;
+        g->pipeJoin[i] = nullptr;
     }
     if (g->fork) cudaEventDestroy(g->fork);
     g->fork = nullptr;
@@ -707,6 +749,10 @@ gb_status Upload(gb_world* g)
     });
     if ((s = DevAlloc(g, &g->dSchedule, nw)) != GB_OK) return s;
     GB_CUDA(cudaMemcpy(g->dSchedule, schedule.data(), nw * sizeof(int), cudaMemcpyHostToDevice));
+    std::vector<int> slotOf(nw);
+    for (int i = 0; i < nw; ++i) slotOf[schedule[i]] = i;
+    if ((s = DevAlloc(g, &g->dSlotOf, nw)) != GB_OK) return s;
+    GB_CUDA(cudaMemcpy(g->dSlotOf, slotOf.data(), nw * sizeof(int), cudaMemcpyHostToDevice));
     g->schedule = schedule;
     g->scheduleSize.resize(nw);
     for (int i = 0; i < nw; ++i) g->scheduleSize[i] = g->desc[schedule[i]].bodyCount;
@@ -1144,7 +1190,8 @@ gb_status gb_world_graph_step(gb_world* g, float dt, int vi, int pi)
         const cudaError_t ec = cudaStreamEndCapture(g->stream, &graph);
         if (s != GB_OK) { if (graph) cudaGraphDestroy(graph); return s; }
         GB_CUDA(ec);
-        const cudaError_t ei = cudaGraphInstantiate(&g->graph, graph, 0);
+        // node priorities from the capture (the class pipelines' stream priorities) are kept
+        const cudaError_t ei = cudaGraphInstantiate(&g->graph, graph, cudaGraphInstantiateFlagUseNodePriority);
         cudaGraphDestroy(graph);
         GB_CUDA(ei);
         g->graphDt = dt; g->graphVi = vi; g->graphPi = pi; g->graphSolver = g->solver;
@@ -1632,11 +1679,11 @@ gb_status gb_world_stage_times(gb_world* g, float dt, int vi, int pi, float* ms)
     for (int i = 0; i < 5 && err == cudaSuccess; ++i) err = cudaEventCreate(&e[i]);
     const StepParams P = MakeParams(g, dt, vi, pi);
     if (err == cudaSuccess) err = cudaEventRecord(e[0], g->stream);
-    if (err == cudaSuccess) err = b2gLaunchNarrowphase(g->batch, g->stream);
+    if (err == cudaSuccess) err = b2gLaunchNarrowphase(g->batch, nullptr, 0, 0, g->stream);
     if (err == cudaSuccess) err = cudaEventRecord(e[1], g->stream);
     if (err == cudaSuccess) s = LaunchClasses(g, P, g->plan, b2gLaunchStep);
     if (err == cudaSuccess && s == GB_OK) err = cudaEventRecord(e[2], g->stream);
-    if (err == cudaSuccess && s == GB_OK) err = b2gLaunchToi(g->batch, P, g->stream);
+    if (err == cudaSuccess && s == GB_OK) err = b2gLaunchToi(g->batch, P, nullptr, 0, 0, g->stream);
     if (err == cudaSuccess && s == GB_OK) err = cudaEventRecord(e[3], g->stream);
     if (err == cudaSuccess && s == GB_OK) s = LaunchClasses(g, P, g->plan, b2gLaunchStepToi);
     if (err == cudaSuccess && s == GB_OK) err = cudaEventRecord(e[4], g->stream);

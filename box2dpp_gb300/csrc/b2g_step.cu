@@ -2090,11 +2090,21 @@ __device__ void ResetStepCounters(WorldState* st)
 // inputs, so the collide phase commits the record when it reaches the contact; contacts left out
 // (tag 0: asleep, sensors, apart) it evaluates itself. Worlds with new fixtures create contacts
 // before their collide phase and are left out whole. Row 0 of each world resets its counters.
-__global__ void __launch_bounds__(256) NarrowphaseKernel(Batch B)
+// Whether world w belongs to the schedule slots [first, first + count) of one class of the launch
+// plan (slotOf: schedule slot of each world); every world when slotOf is null.
+__device__ inline bool InClass(const int* slotOf, int first, int count, int w)
+{
+    if (!slotOf) return true;
+    const int s = slotOf[w];
+    return s >= first && s < first + count;
+}
+
+__global__ void __launch_bounds__(256) NarrowphaseKernel(Batch B, const int* slotOf, int first, int count)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= B.contactRows) return;
     const int w = B.cWorld[r];
+    if (!InClass(slotOf, first, count, w)) return;
     WorldState* st = B.state + w;
     const int k = r - B.desc[w].contactBase;
     const bool newFixture = st->newFixture != 0;
@@ -2170,11 +2180,12 @@ __global__ void __launch_bounds__(128, B2G_STEP_MIN_BLOCKS) StepKernel(Batch B, 
 // reset), so the scan advances no sweep and each time of impact depends on its contact alone.
 // StepToiKernel's event loop then finds them cached. The body-flag bits the classification reads
 // (type, awake, bullet) are not the ones the reset clears.
-__global__ void __launch_bounds__(256, 2) ToiKernel(Batch B, float dt)
+__global__ void __launch_bounds__(256, 2) ToiKernel(Batch B, float dt, const int* slotOf, int first, int count)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r < B.bodyRows) {
         const int w = B.bWorld[r];
+        if (!InClass(slotOf, first, count, w)) return;
         WorldState* st = B.state + w;
         if (!(st->continuous && dt > 0.0f && st->stepComplete)) return;
         const int b = r - B.desc[w].bodyBase;
@@ -2188,6 +2199,7 @@ __global__ void __launch_bounds__(256, 2) ToiKernel(Batch B, float dt)
     const int q = r - B.bodyRows;
     if (q >= B.contactRows) return;
     const int w = B.cWorld[q];
+    if (!InClass(slotOf, first, count, w)) return;
     WorldState* st = B.state + w;
     if (!(st->continuous && dt > 0.0f && st->stepComplete)) return;
     const int k = q - B.desc[w].contactBase;
@@ -2255,10 +2267,10 @@ __global__ void BodyEditKernel(Batch B, const BodyEdit* edits, int n)
 
 // Launch entries used by the host runtime (b2g_api.cu). A step is b2gLaunchNarrowphase, then
 // b2gLaunchStep for every launch class, then b2gLaunchToi, then b2gLaunchStepToi for every class.
-cudaError_t b2gLaunchNarrowphase(const b2g::Batch& B, cudaStream_t stream)
+cudaError_t b2gLaunchNarrowphase(const b2g::Batch& B, const int* slotOf, int first, int count, cudaStream_t stream)
 {
     if (B.contactRows <= 0) return cudaSuccess;
-    b2g::NarrowphaseKernel<<<(B.contactRows + 255) / 256, 256, 0, stream>>>(B);
+    b2g::NarrowphaseKernel<<<(B.contactRows + 255) / 256, 256, 0, stream>>>(B, slotOf, first, count);
     return cudaGetLastError();
 }
 
@@ -2269,11 +2281,12 @@ cudaError_t b2gLaunchBodyEdits(const b2g::Batch& B, const b2g::BodyEdit* edits, 
     return cudaGetLastError();
 }
 
-cudaError_t b2gLaunchToi(const b2g::Batch& B, const b2g::StepParams& P, cudaStream_t stream)
+cudaError_t b2gLaunchToi(const b2g::Batch& B, const b2g::StepParams& P, const int* slotOf, int first, int count,
+                         cudaStream_t stream)
 {
     if (!(P.dt > 0.0f)) return cudaSuccess;
     const long long rows = (long long)B.bodyRows + B.contactRows;
-    b2g::ToiKernel<<<(unsigned)((rows + 255) / 256), 256, 0, stream>>>(B, P.dt);
+    b2g::ToiKernel<<<(unsigned)((rows + 255) / 256), 256, 0, stream>>>(B, P.dt, slotOf, first, count);
     return cudaGetLastError();
 }
 
