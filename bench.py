@@ -144,9 +144,9 @@ STAGE_KERNELS = ["b2g::NarrowphaseKernel", "b2g::StepKernel", "b2g::ToiKernel", 
 
 
 def launches_per_step(n_classes: int) -> int:
-    """Kernel launches of one step: the flat NarrowphaseKernel and ToiKernel, and StepKernel and
-    StepToiKernel once per class of the launch plan."""
-    return 2 + 2 * n_classes
+    """Kernel launches of one step: each class of the launch plan is a pipeline of NarrowphaseKernel
+    and ToiKernel (over that class's worlds' rows), StepKernel and StepToiKernel."""
+    return 4 * n_classes
 
 
 def measured_peaks():
