@@ -161,8 +161,8 @@ def measured_peaks():
 
 # DRAM bytes (read + write) per algorithmic byte of StepKernel (coloured solver), from one full ncu
 # capture of the 1024-world case of this workload (111.0 MB read + 80.6 MB written for 41.4 MB
-# algorithmic, profiles/StepKernel_coloured_1024_worlds.md); traffic grows with the units processed,
-# so the full launch's traffic is this ratio x its algorithmic bytes.
+# algorithmic); traffic grows with the units processed, so the full launch's traffic is this ratio x
+# its algorithmic bytes.
 TRAFFIC_PER_ALGORITHMIC_BYTE = 191.6 / 41.4
 
 

@@ -1750,10 +1750,11 @@ gb_status gb_sincos(const float* x, float* s, float* c, int n)
 {
     if (n <= 0) return GB_OK;
     float *dx = nullptr, *ds = nullptr, *dc = nullptr;
-    GB_CUDA(cudaMalloc(&dx, n * sizeof(float)));
-    GB_CUDA(cudaMalloc(&ds, n * sizeof(float)));
-    GB_CUDA(cudaMalloc(&dc, n * sizeof(float)));
-    cudaError_t e = cudaMemcpy(dx, x, n * sizeof(float), cudaMemcpyHostToDevice);
+    // every allocation is checked into e, so a failure part way frees what was allocated before it
+    cudaError_t e = cudaMalloc(&dx, n * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&ds, n * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&dc, n * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpy(dx, x, n * sizeof(float), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = b2gLaunchSinCos(dx, ds, dc, n, 0);
     if (e == cudaSuccess) e = cudaMemcpy(s, ds, n * sizeof(float), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(c, dc, n * sizeof(float), cudaMemcpyDeviceToHost);
@@ -1781,13 +1782,14 @@ gb_status gb_collide(int n, const int* type_a, const float* shape_a, const int* 
     Shape *dsa = nullptr, *dsb = nullptr;
     float4 *dxa = nullptr, *dxb = nullptr, *dof = nullptr;
     int4* doi = nullptr;
-    GB_CUDA(cudaMalloc(&dsa, n * sizeof(Shape)));
-    GB_CUDA(cudaMalloc(&dsb, n * sizeof(Shape)));
-    GB_CUDA(cudaMalloc(&dxa, n * sizeof(float4)));
-    GB_CUDA(cudaMalloc(&dxb, n * sizeof(float4)));
-    GB_CUDA(cudaMalloc(&doi, n * sizeof(int4)));
-    GB_CUDA(cudaMalloc(&dof, 3 * n * sizeof(float4)));
-    cudaError_t e = cudaMemcpy(dsa, sa.data(), n * sizeof(Shape), cudaMemcpyHostToDevice);
+    // every allocation is checked into e, so a failure part way frees what was allocated before it
+    cudaError_t e = cudaMalloc(&dsa, n * sizeof(Shape));
+    if (e == cudaSuccess) e = cudaMalloc(&dsb, n * sizeof(Shape));
+    if (e == cudaSuccess) e = cudaMalloc(&dxa, n * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc(&dxb, n * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc(&doi, n * sizeof(int4));
+    if (e == cudaSuccess) e = cudaMalloc(&dof, 3 * n * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMemcpy(dsa, sa.data(), n * sizeof(Shape), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(dsb, sb.data(), n * sizeof(Shape), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(dxa, xa.data(), n * sizeof(float4), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(dxb, xb.data(), n * sizeof(float4), cudaMemcpyHostToDevice);
@@ -1805,7 +1807,9 @@ const char* gb_version(void) { return "box2d_gb300 0.1 (Box2D 2.3.2 step semanti
 // ------------------------------------------------------------------ narrowphase without allocation
 // gb_collide_noalloc stages its inputs and outputs in one fixed device buffer defined here (static
 // device storage for GB_COLLIDE_NOALLOC_MAX_PAIRS pairs) instead of allocating per call. The
-// buffer's address is resolved once per device, with that device current, and cached.
+// buffer's address is resolved once per device, with that device current, and cached; each call
+// checks that the cached address is still device memory of the current context (a cudaDeviceReset
+// moves the buffer) and resolves it again when it is not.
 namespace {
 
 constexpr int kNoAllocMaxDevices = 64;
@@ -1831,6 +1835,17 @@ gb_status CollideScratch(unsigned char** out)
     GB_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kNoAllocMaxDevices) return GB_ERR_INVALID;
     std::lock_guard<std::mutex> lock(gCollideScratchMutex);
+    if (gCollideScratchAddr[dev] != nullptr) {
+        // A cudaDeviceReset in this process ends the context the cached address belongs to; the
+        // buffer then lives at a new address in the next context. An address that is no longer
+        // device memory of the current context is dropped and resolved again.
+        cudaPointerAttributes a{};
+        const cudaError_t e = cudaPointerGetAttributes(&a, gCollideScratchAddr[dev]);
+        if (e != cudaSuccess || a.type != cudaMemoryTypeDevice || a.device != dev) {
+            (void)cudaGetLastError();
+            gCollideScratchAddr[dev] = nullptr;
+        }
+    }
     if (gCollideScratchAddr[dev] == nullptr) {
         void* p = nullptr;
         GB_CUDA(cudaGetSymbolAddress(&p, gCollideScratch));

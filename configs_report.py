@@ -1,7 +1,7 @@
 """Throughput of the single-world configurations on the GPU, beside the CPU restatement of the
 reference step on one host core, on the same seeded scenes.
 
-  python -m box2dpp_gb300.configs_report [--configs 1,2,5] [--cpu-seconds 15]
+  python configs_report.py [--configs 1,2,5] [--cpu-seconds 15]
 
 Configurations (the batched one is bench.py's):
   1  the 210-box pyramid on an edge ground, sleep on (the reference default), 600 steps;
@@ -11,23 +11,28 @@ Configurations (the batched one is bench.py's):
 
 GPU: one world per handle, the plain (reference-order, bit-exact) and the graph-coloured solver,
 8/3 iterations, each step timed with CUDA events on the handle's stream; body-steps/s over the timed
-steps. CPU: the oracle's restatement of b2World::Step (plain order, project trig) on one thread,
-stepped from the same initial state for as many of the same steps as fit in --cpu-seconds. Prints
-one JSON line per configuration.
+steps. CPU: the oracle's restatement of b2World::Step (plain order) with glibc's sinf/cosf (the
+reference's own trig) on one thread, stepped from the same initial state for as many of the same
+steps as fit in --cpu-seconds. Prints one JSON line per configuration. A CPU-baseline reporter like
+bench.py's CPU leg: it sits beside bench.py, outside the package, because it runs the oracle.
 """
 from __future__ import annotations
 
 import argparse
 import json
+import os
+import sys
 import time
 
 import numpy as np
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
 
 DT, VI, PI = 1.0 / 60.0, 8, 3
 
 
 def scene(cfg: int):
-    from . import scenes
+    from box2dpp_gb300 import scenes
 
     if cfg == 1:
         return scenes.config1(), 600
@@ -41,7 +46,7 @@ def scene(cfg: int):
 def gpu_rate(sc, steps: int, solver: str) -> dict:
     import torch
 
-    from .world import World
+    from box2dpp_gb300.world import World
 
     w = World(sc)
     w.set_solver(solver)
@@ -66,7 +71,7 @@ def gpu_rate(sc, steps: int, solver: str) -> dict:
 def cpu_rate(sc, steps: int, budget_s: float) -> dict:
     import oracle
 
-    w = oracle.OracleWorld(sc, "port", "project")
+    w = oracle.OracleWorld(sc, "port", "libm")
     n = sum(1 for b in sc.bodies if b[0] == 2)
     done, t0 = 0, time.perf_counter()
     while done < steps and time.perf_counter() - t0 < budget_s:

@@ -324,7 +324,9 @@ gb_status gb_collide(int n, const int* type_a, const float* shape_a, const int* 
  * GB_ERR_CAPACITY before any device work. The buffer is shared by every call on a device: calls
  * whose device work overlaps (for example from several host threads) race on it, so the caller
  * serialises them. The first call on each device resolves the buffer's address
- * (cudaGetSymbolAddress) and should come before any CUDA stream capture. */
+ * (cudaGetSymbolAddress) and should come before any CUDA stream capture. A cudaDeviceReset in the
+ * caller's process moves the buffer to a new address in the next context: later calls notice that
+ * the cached address is no longer device memory of the current context and resolve it again. */
 #define GB_COLLIDE_NOALLOC_MAX_PAIRS 4096
 gb_status gb_collide_noalloc(int n, const int* type_a, const float* shape_a, const int* n_a, const float* xf_a,
                              const int* type_b, const float* shape_b, const int* n_b, const float* xf_b,

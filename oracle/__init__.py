@@ -20,7 +20,20 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_TREE = os.environ.get("B2_REFERENCE_TREE", "/root/reference/Regression/box2d-ref")
+
+
+def _reference_tree() -> str:
+    """The reference's Regression/box2d-ref directory as oracle/reference_tree.sh locates it (the
+    B2_REFERENCE_TREE environment variable, else the recipe's own fallback), or "" when absent."""
+    try:
+        out = subprocess.run(["sh", os.path.join(HERE, "reference_tree.sh")], capture_output=True, text=True,
+                             env=os.environ.copy(), timeout=30)
+    except (OSError, subprocess.SubprocessError):
+        return ""
+    return out.stdout.strip() if out.returncode == 0 else ""
+
+
+REF_TREE = _reference_tree()
 
 _f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
@@ -35,7 +48,7 @@ def build_port(quiet: bool = True) -> str:
 
 
 def reference_available() -> bool:
-    return os.path.isdir(os.path.join(REF_TREE, "Box2DRef"))
+    return bool(REF_TREE) and os.path.isdir(os.path.join(REF_TREE, "Box2DRef"))
 
 
 def build_reference() -> None:
