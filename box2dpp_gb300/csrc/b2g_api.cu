@@ -393,17 +393,17 @@ std::vector<LaunchPlan> CandidatePlans(const gb_world* g)
     c.push_back(DefaultPlan(g));
     if (g->schedule.size() < 2) return c;
     c.push_back(LaunchPlan{MakeClass(g, 0, (int)g->schedule.size(), 64)});
-    c.push_back(LaunchPlan{MakeClass(g, 0, (int)g->schedule.size(), 32)});
     c.push_back(SplitPlan(g, {160}, {64, 32}));
-    c.push_back(SplitPlan(g, {160}, {64, 64}));
     c.push_back(SplitPlan(g, {256, 64}, {64, 64, 32}));
-    c.push_back(SplitPlan(g, {256, 64}, {64, 32, 32}));
-    c.push_back(SplitPlan(g, {96}, {64, 32}));
     c.push_back(SplitPlan(g, {320, 160, 64}, {128, 64, 32, 32}));
     // the largest worlds set the step's critical path: a small first class with wider CTAs
     c.push_back(SplitPlan(g, {400, 96}, {128, 64, 32}));
     c.push_back(SplitPlan(g, {320, 96}, {128, 64, 32}));
     c.push_back(SplitPlan(g, {400, 160}, {128, 64, 32}));
+    c.push_back(SplitPlan(g, {400, 96}, {256, 64, 32}));
+    c.push_back(SplitPlan(g, {320, 96}, {256, 64, 32}));
+    c.push_back(SplitPlan(g, {400, 160, 64}, {256, 128, 64, 32}));
+    c.push_back(SplitPlan(g, {320, 160, 64}, {256, 128, 64, 32}));
     // (classes with shared memory capped at 18-24 KB, for more resident worlds per SM, measured 15-25%
     // slower than the best plan on the bench batch: the solve's staging matters more)
     return c;
@@ -1251,7 +1251,7 @@ gb_status gb_world_set_launch_plan(gb_world* g, const int* classes, int n)
     for (int i = 0; i < n; ++i) {
         LaunchClass c{classes[5 * i], classes[5 * i + 1], classes[5 * i + 2], classes[5 * i + 3], classes[5 * i + 4]};
         const size_t smem = (2 * (size_t)std::max(c.rows, 0) + std::max(c.contacts, 0)) * sizeof(float4);
-        if (c.first != next || c.count < 1 || c.threads < 32 || c.threads > 128 || c.threads % 32 != 0 ||
+        if (c.first != next || c.count < 1 || c.threads < 32 || c.threads > 256 || c.threads % 32 != 0 ||
             c.rows < 0 || c.contacts < 0 || smem > 48 * 1024)
             return GB_ERR_INVALID;
         next += c.count;

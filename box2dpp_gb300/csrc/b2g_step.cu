@@ -479,6 +479,9 @@ struct Wd {
     template <class L>
     __device__ bool buildIslandsTable(unsigned char* base, int capacity, bool coloured, int* colourCount, int& nIsl,
                                       int& nRows, int& nCons, int& movers);
+    template <class L>
+    __device__ bool buildIslandsParallel(unsigned char* base, int capacity, int* radixWork, int* colourCount, int& nIsl,
+                                         int& nRows, int& nCons, int& movers);
     __device__ void solveIslands(const StepParams& P, int nIsl, int nRows, int nContacts, float4* smem, int smemRows,
                                  int smemContacts, const int* colourStart);
     __device__ void solveTOI(const StepParams& P);
@@ -505,31 +508,55 @@ __device__ inline int WarpAppend(bool keep, int* count)
     return keep ? base + __popc(bal & ((1u << lane) - 1u)) : -1;
 }
 
+// Largest CTA of a per-world launch.
+constexpr int kMaxCta = 256;
+// the continuous phase (StepToiKernel) runs with at most this many threads per CTA
+constexpr int kMaxToiCta = 128;
+
+// Exclusive prefix sums over the CTA of up to three per-thread counts (threads in index order), by
+// warp shuffles and one shared slot per warp and count; totals receive the CTA-wide sums. Every
+// thread of the CTA calls it (CTA sizes are multiples of 32).
+__device__ inline void ctaExclusiveScan3(int& a, int& b, int& c, int* totals)
+{
+    __shared__ int sWarp[3][kMaxCta / 32 + 1];
+    const int lane = tid() & 31, warp = tid() >> 5, nWarps = (nthreads() + 31) >> 5;
+    int ia = a, ib = b, ic = c;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int xa = __shfl_up_sync(0xffffffffu, ia, o), xb = __shfl_up_sync(0xffffffffu, ib, o),
+                  xc = __shfl_up_sync(0xffffffffu, ic, o);
+        if (lane >= o) { ia += xa; ib += xb; ic += xc; }
+    }
+    if (lane == 31) { sWarp[0][warp] = ia; sWarp[1][warp] = ib; sWarp[2][warp] = ic; }
+    __syncthreads();
+    int pa = 0, pb = 0, pc = 0, ta = 0, tb = 0, tc = 0;
+    for (int w = 0; w < nWarps; ++w) {
+        if (w < warp) { pa += sWarp[0][w]; pb += sWarp[1][w]; pc += sWarp[2][w]; }
+        ta += sWarp[0][w]; tb += sWarp[1][w]; tc += sWarp[2][w];
+    }
+    a = pa + ia - a;
+    b = pb + ib - b;
+    c = pc + ic - c;
+    totals[0] = ta;
+    totals[1] = tb;
+    totals[2] = tc;
+    __syncthreads();
+}
+
 // Order-preserving compaction over the CTA: out receives in[k] for every k < n with keep(k), in k
 // order; returns the count (same value in every thread). Each thread takes one contiguous chunk.
-constexpr int kMaxCta = 128;
 template <typename Keep>
 __device__ int ctaCompact(const int* in, int n, int* out, Keep keep)
 {
-    __shared__ int sOff[kMaxCta + 1];
     const int T = nthreads(), t = tid();
     const int chunk = (n + T - 1) / T;
     const int lo = min(n, t * chunk), hi = min(n, lo + chunk);
-    int cnt = 0;
-    for (int k = lo; k < hi; ++k) cnt += keep(k) ? 1 : 0;
-    sOff[t + 1] = cnt;
-    __syncthreads();
-    if (t == 0) {
-        sOff[0] = 0;
-        for (int i = 1; i <= T; ++i) sOff[i] += sOff[i - 1];
-    }
-    __syncthreads();
-    int o = sOff[t];
+    int o = 0, u1 = 0, u2 = 0, tot[3];
+    for (int k = lo; k < hi; ++k) o += keep(k) ? 1 : 0;
+    ctaExclusiveScan3(o, u1, u2, tot);
     for (int k = lo; k < hi; ++k)
         if (keep(k)) out[o++] = in[k];
-    const int total = sOff[T];
     __syncthreads();
-    return total;
+    return tot[0];
 }
 
 // Bitonic sort of n 64-bit keys in global memory (n <= capacity, capacity a power of two); the
@@ -563,10 +590,12 @@ __device__ void ctaSortKeys(unsigned long long* keys, int n, int capacity)
 // worlds; both give the same order (equal keys are equal values). work: kRadixWork ints of shared
 // memory (the digit bases and the per-warp tile counts); the caller checks RadixSortFits first.
 constexpr int kRadixWork = 256 + (kMaxCta / 32) * 256;
+// the work a CTA of this launch uses: the digit bases and one row of tile counts per warp
+__device__ inline int RadixWorkInts() { return 256 + ((nthreads() + 31) / 32) * 256; }
 __device__ inline bool RadixSortFits(int n, int workBytes)
 {
     // tile stamps are packed with a 6-bit count into an int: at most 2^24 tiles over all passes
-    return workBytes >= kRadixWork * (int)sizeof(int) && (long long)((n + 31) / 32) * 8 < (1ll << 24);
+    return workBytes >= RadixWorkInts() * (int)sizeof(int) && (long long)((n + 31) / 32) * 8 < (1ll << 24);
 }
 __device__ void ctaRadixSort(unsigned long long* keys, unsigned long long* tmp, int n, int* work)
 {
@@ -576,7 +605,7 @@ __device__ void ctaRadixSort(unsigned long long* keys, unsigned long long* tmp, 
     if (n <= 1) return;
     const int T = nthreads(), t = tid(), lane = t & 31, warp = t >> 5;
     if (t == 0) { sOr = 0ull; sAnd = ~0ull; }
-    for (int i = t; i < (kMaxCta / 32) * 256; i += T) work[256 + i] = -1;
+    for (int i = t; i < ((T + 31) / 32) * 256; i += T) work[256 + i] = -1;
     __syncthreads();
     {
         unsigned long long o = 0ull, a = ~0ull;
@@ -906,18 +935,10 @@ __device__ void Wd::findNewContacts()
         const int T = nthreads(), t = tid();
         const int chunk = (n + T - 1) / T;
         const int lo = min(n, t * chunk), hi = min(n, lo + chunk);
-        __shared__ int sOff2[kMaxCta + 1];
-        int cnt = 0;
-        for (int k = lo; k < hi; ++k) cnt += pairKeep[k] != 0;
-        sOff2[t + 1] = cnt;
-        __syncthreads();
-        if (t == 0) {
-            sOff2[0] = 0;
-            for (int i = 1; i <= T; ++i) sOff2[i] += sOff2[i - 1];
-            sKept = sOff2[T];
-        }
-        __syncthreads();
-        int o = sOff2[t];
+        int o = 0, u1 = 0, u2 = 0, tot[3];
+        for (int k = lo; k < hi; ++k) o += pairKeep[k] != 0;
+        ctaExclusiveScan3(o, u1, u2, tot);
+        if (t == 0) sKept = tot[0];
         for (int k = lo; k < hi; ++k)
             if (pairKeep[k] && o < d.contactCap) keptIdx[o++] = k;
         __syncthreads();
@@ -1100,20 +1121,14 @@ __device__ void Wd::collide()
     // Listener calls of the collide phase in list order (b2ContactManager::Collide visits the list in
     // order; each contact's Update or Destroy makes its calls), appended to the event log.
     if (rec) {
-        __shared__ int sEvOff[kMaxCta + 1];
         const int T = nthreads(), t = tid();
         const int chunk = (n + T - 1) / T;
         const int lo = min(n, t * chunk), hi = min(n, lo + chunk);
-        int cnt = 0;
-        for (int k = lo; k < hi; ++k) cnt += __popc(evType[k] & 7);
-        sEvOff[t + 1] = cnt;
-        __syncthreads();
-        if (t == 0) {
-            sEvOff[0] = st->eventCount;
-            for (int i = 1; i <= T; ++i) sEvOff[i] += sEvOff[i - 1];
-        }
-        __syncthreads();
-        int slot = sEvOff[t];
+        int slot = 0, u1 = 0, u2 = 0, tot[3];
+        for (int k = lo; k < hi; ++k) slot += __popc(evType[k] & 7);
+        const int base = st->eventCount;
+        ctaExclusiveScan3(slot, u1, u2, tot);
+        slot += base;
         for (int k = lo; k < hi; ++k) {
             const int bits = evType[k] & 7;
             if (!bits) continue;
@@ -1122,7 +1137,7 @@ __device__ void Wd::collide()
                 if (bits & (1 << b)) putEvent(slot++, b, info.y, info.z);
         }
         __syncthreads();
-        if (t == 0) st->eventCount = sEvOff[T];
+        if (t == 0) st->eventCount = base + tot[0];
         __syncthreads();
     }
     // Survivors keep their relative order; destroyed contacts are unlinked in list order.
@@ -1168,6 +1183,11 @@ struct IslPacked {
     __device__ static Pair pair(int a, int b) { return (unsigned)a | ((unsigned)b << 16); }
     __device__ static int pairA(Pair p) { return (int)(p & 0xffffu); }
     __device__ static int pairB(Pair p) { return (int)(p >> 16); }
+    // a contact's dynamic bodies for the colouring (kNone: static or kinematic)
+    static constexpr int kNone = 0xffff;
+    __device__ static Entry cinfo(int a, int b) { return (unsigned)a | ((unsigned)b << 16); }
+    __device__ static int cinfoA(Entry u) { return (int)(u & 0xffffu); }
+    __device__ static int cinfoB(Entry u) { return (int)(u >> 16); }
 };
 struct IslWide {
     using Idx = int;
@@ -1181,6 +1201,10 @@ struct IslWide {
     __device__ static Pair pair(int a, int b) { return make_int2(a, b); }
     __device__ static int pairA(Pair p) { return p.x; }
     __device__ static int pairB(Pair p) { return p.y; }
+    static constexpr int kNone = -1;
+    __device__ static Entry cinfo(int a, int b) { return make_int2(a, b); }
+    __device__ static int cinfoA(Entry u) { return u.x; }
+    __device__ static int cinfoB(Entry u) { return u.y; }
 };
 
 template <class L>
@@ -1371,6 +1395,394 @@ __device__ bool Wd::buildIslandsTable(unsigned char* base, int capacity, bool co
     return true;
 }
 
+// Island build of the graph-coloured solver, spread over the CTA. That solver does not depend on the
+// order in which b2World::Solve's depth-first search (Dynamics/b2World.cpp:410-497) visits bodies and
+// contacts, only on which bodies, contacts and joints form each island, so the islands are built as
+// connected components instead of by the search:
+//   * the same eligible edges as the search (touching, enabled, non-sensor contacts, taken flat from
+//     the world's contact list; joints whose bodies are active) join non-static bodies by union-find
+//     (a root is linked under the smaller root, so each component's root is its smallest body index
+//     whatever the schedule);
+//   * a component is an island when it holds an awake, active, non-static body (a search seed); the
+//     islands are numbered by root;
+//   * one 64-bit key per island member, (island, kind, index) with kind 0 non-static body, 1 static
+//     body (one row per island that reaches it, as the search gives it), 2 contact, 3 joint, sorted
+//     once: each island's rows, contacts and joints in index order;
+//   * contacts are coloured by rounds of a parallel maximal-independent-set selection (Luby's): an
+//     uncoloured contact takes the current colour when its hashed key is the smallest among the
+//     candidate contacts at each of its dynamic bodies; contacts next to a winner wait for the next
+//     colour. Every result is a function of the world state alone, not of thread timing or count.
+// Returns false (nothing written outside the scratch) when the scratch does not fit; the caller then
+// takes the search.
+
+// The colouring's key of island contact i in round gr: rounds count down in the top 16 bits (a later
+// round's key is smaller than any earlier one), then a 16-bit hash of i (the priority order), then i
+// (unique keys).
+__device__ inline unsigned long long ColourKey(int i, int gr)
+{
+    unsigned h = (unsigned)i * 0x9E3779B1u;
+    h ^= h >> 15;
+    h *= 0x85EBCA77u;
+    h ^= h >> 13;
+    return ((unsigned long long)(0xffffu - (unsigned)gr) << 48) | ((unsigned long long)(h & 0xffffu) << 32) |
+           (unsigned)i;
+}
+
+template <class L>
+__device__ bool Wd::buildIslandsParallel(unsigned char* base, int capacity, int* radixWork, int* colourCount,
+                                         int& nIslOut, int& nRowsOut, int& nConsOut, int& moversOut)
+{
+    using Entry = typename L::Entry;
+    __shared__ int sN, sMovers, sFlags[4];
+    enum : unsigned char { fStatic = 2, fAwake = 4, fActive = 8, fDynamic = 16 };
+    const int nb = d.bodyCount, C = d.contactCap, NJ = d.jointCount;
+    const int T = nthreads(), t = tid();
+    if (!base || nb == 0 || nb >= L::kMaxBodies || C >= L::kMaxContacts || T > kMaxCta) return false;
+    const unsigned long long tBuild0 = clock64();
+    const int nc = st->contactCount;
+    auto up = [](long long x) { return (x + 15) & ~15ll; };
+    // layout (bytes): flags nb | parent 4nb | island 4nb | row 4nb | static rows 4nb | colour stamp 4nb
+    // | owner 8nb | colour nc | dynamic bodies of each island contact nc x Entry (the stamps and
+    // owners, contiguous, first hold the island extents: 12 bytes per island)
+    const long long oFlag = 0;
+    const long long oParent = up(oFlag + nb);
+    const long long oIsl = up(oParent + 4ll * nb);
+    const long long oRow = up(oIsl + 4ll * nb);
+    const long long oSStart = up(oRow + 4ll * nb);
+    const long long oTaken = up(oSStart + 4ll * nb);
+    const long long oOwner = up(oTaken + 4ll * nb);
+    const long long oCol = up(oOwner + 8ll * nb);
+    const long long oCinf = up(oCol + nc);
+    if (oCinf + (long long)sizeof(Entry) * nc > capacity) return false;
+    unsigned char* bflag = base + oFlag;
+    int* parent = reinterpret_cast<int*>(base + oParent);
+    int* islOf = reinterpret_cast<int*>(base + oIsl);
+    int* rowOf = reinterpret_cast<int*>(base + oRow);
+    int* sStart = reinterpret_cast<int*>(base + oSStart);
+    int* taken = reinterpret_cast<int*>(base + oTaken);
+    unsigned long long* owner = reinterpret_cast<unsigned long long*>(base + oOwner);
+    signed char* ccol = reinterpret_cast<signed char*>(base + oCol);
+    Entry* cinf = reinterpret_cast<Entry*>(base + oCinf);
+    // a live contact joins its bodies when b2World::Solve's search would follow it
+    auto eligible = [&](const int4& info) {
+        return (info.x & kCEnabled) != 0 && (info.x & kCTouching) != 0 && fi[info.y].w == 0 && fi[info.z].w == 0;
+    };
+    for (int b = t; b < nb; b += T) {
+        const int4 B = bi[b];
+        unsigned char f = 0;
+        if (B.x == kStatic) f |= fStatic;
+        if (B.x == kDynamic) f |= fDynamic;
+        if (B.y & kBAwake) f |= fAwake;
+        if (B.y & kBActive) f |= fActive;
+        bflag[b] = f;
+        parent[b] = b;
+    }
+    if (t == 0) sN = 0;
+    __syncthreads();
+    // union-find over the edges between non-static bodies. find halves the path it walks (a node
+    // that is not a root takes its grandparent, still an ancestor; roots change only by the linking
+    // compare-and-swap); every loop is bounded by the body count.
+    volatile int* vp = parent;
+    auto find = [&](int x) {
+        for (int g = 0; g <= nb; ++g) {
+            const int p = vp[x];
+            if (p == x) break;
+            const int gp = vp[p];
+            if (gp != p) vp[x] = gp;
+            x = gp;
+        }
+        return x;
+    };
+    auto unite = [&](int a, int b) {
+        for (int g = 0; g <= 2 * nb; ++g) {
+            a = find(a);
+            b = find(b);
+            if (a == b) return;
+            if (a > b) { const int x = a; a = b; b = x; }
+            if (atomicCAS(&parent[b], b, a) == b) return;
+        }
+        atomicOr(&st->error, kErrInvalid);
+    };
+    for (int k = t; k < nc; k += T) {
+        const int4 info = ci[order[k]];
+        if (!eligible(info)) continue;
+        const int bA = fixBody(info.y), bB = fixBody(info.z);
+        if (!(bflag[bA] & fStatic) && !(bflag[bB] & fStatic)) unite(bA, bB);
+    }
+    for (int j = t; j < NJ; j += T) {
+        const int A = jt[j].bodyA, B = jt[j].bodyB;
+        const unsigned char fa = bflag[A], fb = bflag[B];
+        if (!(fa & fStatic) && !(fb & fStatic) && (fa & fActive) && (fb & fActive)) unite(A, B);
+    }
+    __syncthreads();
+    // roots: the trees no longer change, so a read-only walk (no halving) into a separate array,
+    // then copied once every walk is done
+    for (int b = t; b < nb; b += T) {
+        int x = b;
+        if (!(bflag[b] & fStatic))
+            for (int g = 0; g <= nb && parent[x] != x; ++g) x = parent[x];
+        sStart[b] = x;
+    }
+    __syncthreads();
+    for (int b = t; b < nb; b += T) {
+        parent[b] = sStart[b];
+        islOf[b] = 0;
+    }
+    __syncthreads();
+    // a component is an island when it holds a seed: an awake, active, non-static body
+    for (int b = t; b < nb; b += T) {
+        const unsigned char f = bflag[b];
+        if (!(f & fStatic) && (f & fAwake) && (f & fActive)) islOf[parent[b]] = 1;
+    }
+    __syncthreads();
+    // islands numbered by root, in root order (chunked scan over the bodies)
+    int nIsl = 0;
+    {
+        const int chunk = (nb + T - 1) / T;
+        const int lo = min(nb, t * chunk), hi = min(nb, lo + chunk);
+        int o = 0, u1 = 0, u2 = 0, tot[3];
+        for (int b = lo; b < hi; ++b) o += (!(bflag[b] & fStatic) && parent[b] == b && islOf[b] == 1) ? 1 : 0;
+        ctaExclusiveScan3(o, u1, u2, tot);
+        nIsl = tot[0];
+        for (int b = lo; b < hi; ++b) {
+            if (bflag[b] & fStatic) continue;
+            if (parent[b] == b) islOf[b] = islOf[b] == 1 ? o++ : -1;
+        }
+    }
+    __syncthreads();
+    for (int b = t; b < nb; b += T) {
+        if (bflag[b] & fStatic) { islOf[b] = -1; continue; }
+        if (parent[b] != b) islOf[b] = islOf[parent[b]];
+    }
+    __syncthreads();
+    // keys (island << 34 | kind << 32 | index) in the pair-key scratch, which the solve does not use;
+    // more keys than its capacity returns false
+    unsigned long long* keys = pairs;
+    unsigned long long* tmp = reinterpret_cast<unsigned long long*>(pairInfo);
+    const int keyCap = d.pairCap;
+    auto push = [&](int isl, int kind, int index) {
+        const int p = atomicAdd(&sN, 1);
+        if (p < keyCap) keys[p] = ((unsigned long long)isl << 34) | ((unsigned long long)kind << 32) | (unsigned)index;
+    };
+    const unsigned long long tKeys0 = clock64();
+    for (int b = t; b < nb; b += T)
+        if (islOf[b] >= 0) push(islOf[b], 0, b);
+    for (int k = t; k < nc; k += T) {
+        const int c = order[k];
+        const int4 info = ci[c];
+        if (!eligible(info)) continue;
+        const int bA = fixBody(info.y), bB = fixBody(info.z);
+        const bool sA = (bflag[bA] & fStatic) != 0, sB = (bflag[bB] & fStatic) != 0;
+        const int isl = !sA ? islOf[bA] : islOf[bB];
+        if (isl < 0) continue;
+        push(isl, 2, c);
+        if (sA) push(isl, 1, bA);
+        if (sB) push(isl, 1, bB);
+    }
+    for (int j = t; j < NJ; j += T) {
+        const int A = jt[j].bodyA, B = jt[j].bodyB;
+        const unsigned char fa = bflag[A], fb = bflag[B];
+        if (!(fa & fActive) || !(fb & fActive)) continue;
+        const int isl = !(fa & fStatic) ? islOf[A] : (!(fb & fStatic) ? islOf[B] : -1);
+        if (isl < 0) continue;
+        push(isl, 3, j);
+        if (fa & fStatic) push(isl, 1, A);
+        if (fb & fStatic) push(isl, 1, B);
+    }
+    __syncthreads();
+    const int n = sN;
+    if (n > keyCap) return false;
+    if (radixWork && RadixSortFits(n, RadixWorkInts() * (int)sizeof(int)))
+        ctaRadixSort(keys, tmp, n, radixWork);
+    else
+        ctaSortKeys(keys, n, keyCap);
+    __syncthreads();
+    const unsigned long long tSort1 = clock64();
+    auto kIsl = [&](unsigned long long k) { return (int)(k >> 34); };
+    auto kKind = [&](unsigned long long k) { return (int)((k >> 32) & 3ull); };
+    auto kIdx = [&](unsigned long long k) { return (int)(k & 0xffffffffull); };
+    for (int i = t; i < nIsl; i += T) sStart[i] = -1;
+    __syncthreads();
+    // rows (non-static bodies, then each distinct static body), contacts and joints in key order:
+    // one chunked scan with three counters
+    int nRows = 0, nCons = 0, nJ = 0;
+    {
+        const int chunk = (n + T - 1) / T;
+        const int lo = min(n, t * chunk), hi = min(n, lo + chunk);
+        int cr = 0, cc = 0, cj = 0;
+        for (int k = lo; k < hi; ++k) {
+            const unsigned long long key = keys[k];
+            const int kind = kKind(key);
+            if (kind == 0 || (kind == 1 && (k == 0 || keys[k - 1] != key))) ++cr;
+            else if (kind == 2) ++cc;
+            else if (kind == 3) ++cj;
+        }
+        if (t == 0) sMovers = 0;
+        int tot[3];
+        ctaExclusiveScan3(cr, cc, cj, tot);
+        nRows = tot[0];
+        nCons = tot[1];
+        nJ = tot[2];
+        if (nRows > d.rowCap || nCons > nc) return false;
+        int r = cr, c = cc, jj = cj;
+        int movers = 0;
+        for (int k = lo; k < hi; ++k) {
+            const unsigned long long key = keys[k];
+            const int kind = kKind(key), idx = kIdx(key), isl = kIsl(key);
+            const bool first = k == 0 || kIsl(keys[k - 1]) != isl;
+            if (first) {
+                islands[isl] = make_int4(r, 0, c, 0);
+                islandJ[isl] = make_int2(jj, 0);
+            }
+            if (kind == 0) {
+                rowOf[idx] = r;
+                sBody[r++] = idx;
+                ++movers;
+            } else if (kind == 1) {
+                if (k > 0 && keys[k - 1] == key) continue;
+                if (k == 0 || kKind(keys[k - 1]) != 1 || kIsl(keys[k - 1]) != isl) sStart[isl] = r;
+                sBody[r++] = idx;
+            } else if (kind == 2) {
+                sContact[c++] = idx;
+            } else {
+                sJoint[jj++] = idx;
+            }
+        }
+        atomicAdd(&sMovers, movers);
+    }
+    __syncthreads();
+    // island extents from the next island's starts, read in one pass and written in the next (the
+    // colour stamps and owners, not yet in use, hold three counts per island in between); an island
+    // without static rows has its static range empty at the end of its rows
+    int* extent = taken;
+    for (int i = t; i < nIsl; i += T) {
+        const int4 I = islands[i];
+        const int2 J = islandJ[i];
+        extent[3 * i] = (i + 1 < nIsl ? islands[i + 1].x : nRows) - I.x;
+        extent[3 * i + 1] = (i + 1 < nIsl ? islands[i + 1].z : nCons) - I.z;
+        extent[3 * i + 2] = (i + 1 < nIsl ? islandJ[i + 1].x : nJ) - J.x;
+    }
+    __syncthreads();
+    for (int i = t; i < nIsl; i += T) {
+        const int4 I = islands[i];
+        islands[i] = make_int4(I.x, extent[3 * i], I.z, extent[3 * i + 1]);
+        islandJ[i] = make_int2(islandJ[i].x, extent[3 * i + 2]);
+        if (sStart[i] < 0) sStart[i] = I.x + extent[3 * i];
+    }
+    __syncthreads();
+    // row of body b in island isl: its own row, or a binary search over the island's static rows
+    auto rowIn = [&](int isl, int b) {
+        if (!(bflag[b] & fStatic)) return rowOf[b];
+        const int end = islands[isl].x + islands[isl].y;
+        int lo = sStart[isl], hi = end;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (sBody[mid] < b) lo = mid + 1;
+            else hi = mid;
+        }
+        if (lo >= end || sBody[lo] != b) {
+            // every static body an island reaches has a row in it; report and stay in bounds
+            atomicOr(&st->error, kErrInvalid);
+            return islands[isl].x;
+        }
+        return lo;
+    };
+    for (int i = t; i < nCons; i += T) {
+        const int4 info = ci[sContact[i]];
+        const int bA = fixBody(info.y), bB = fixBody(info.z);
+        const int isl = !(bflag[bA] & fStatic) ? islOf[bA] : islOf[bB];
+        vc[i].idx = make_int4(rowIn(isl, bA), rowIn(isl, bB), 0, 0);
+        ccol[i] = -1;
+        cinf[i] = L::cinfo((bflag[bA] & fDynamic) ? bA : L::kNone, (bflag[bB] & fDynamic) ? bB : L::kNone);
+        ci[sContact[i]].x = info.x | kCIsland;
+    }
+    for (int q = t; q < nJ; q += T) {
+        Joint& J = jt[sJoint[q]];
+        const int isl = !(bflag[J.bodyA] & fStatic) ? islOf[J.bodyA] : islOf[J.bodyB];
+        J.islandFlag = 1;
+        J.indexA = rowIn(isl, J.bodyA);
+        J.indexB = rowIn(isl, J.bodyB);
+        if (J.type == kJointGear) {
+            J.indexC = rowIn(isl, J.bodyC);
+            J.indexD = rowIn(isl, J.bodyD);
+        }
+    }
+    for (int b = t; b < nb; b += T) {
+        const int y = bi[b].y;
+        const bool inIsland = islOf[b] >= 0;
+        bi[b].y = inIsland ? (y | kBIsland) : (y & ~kBIsland);
+        if (inIsland) bj[b].z = rowOf[b] - islands[islOf[b]].x;
+        taken[b] = -1;
+        owner[b] = ~0ull;
+    }
+    if (t == 0) { sFlags[0] = sFlags[1] = sFlags[2] = sFlags[3] = 0; }
+    __syncthreads();
+    for (int r = t; r < nRows; r += T) setAwake(sBody[r], true);
+    // colouring in shared memory: rounds of two passes. Pass A: every uncoloured contact with no
+    // dynamic body already holding the current colour (a candidate) lowers its bodies' owner keys to
+    // its own; pass B: a candidate that owns all its dynamic bodies takes the colour and claims them.
+    // Keys carry the round in their top bits (later rounds smaller), so owners need no reset. A
+    // colour ends when no candidate is left; the colouring when no contact is uncoloured.
+    int col = 0;
+    for (int gr = 0; gr < 4096; ++gr) {
+        const int par = gr & 1;
+        int cand = 0, unc = 0;
+        for (int i = t; i < nCons; i += T) {
+            if (ccol[i] >= 0) continue;
+            unc = 1;
+            const Entry u = cinf[i];
+            const int a = L::cinfoA(u), b = L::cinfoB(u);
+            if ((a != L::kNone && taken[a] == col) || (b != L::kNone && taken[b] == col)) continue;
+            cand = 1;
+            const unsigned long long key = ColourKey(i, gr);
+            if (a != L::kNone) atomicMin(&owner[a], key);
+            if (b != L::kNone) atomicMin(&owner[b], key);
+        }
+        if (unc) sFlags[2 * par] = 1;
+        if (cand) sFlags[2 * par + 1] = 1;
+        __syncthreads();
+        const bool anyUnc = sFlags[2 * par] != 0, anyCand = sFlags[2 * par + 1] != 0;
+        if (!anyUnc) break;
+        // the other parity's flags were last read before the previous barrier
+        if (t == 0) { sFlags[2 * (par ^ 1)] = 0; sFlags[2 * (par ^ 1) + 1] = 0; }
+        if (!anyCand) {
+            if (++col == kSerialColour) break;
+            __syncthreads();
+            continue;
+        }
+        for (int i = t; i < nCons; i += T) {
+            if (ccol[i] >= 0) continue;
+            const Entry u = cinf[i];
+            const int a = L::cinfoA(u), b = L::cinfoB(u);
+            if ((a != L::kNone && taken[a] == col) || (b != L::kNone && taken[b] == col)) continue;
+            const unsigned long long key = ColourKey(i, gr);
+            if ((a == L::kNone || owner[a] == key) && (b == L::kNone || owner[b] == key)) {
+                ccol[i] = (signed char)col;
+                if (a != L::kNone) taken[a] = col;
+                if (b != L::kNone) taken[b] = col;
+            }
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    // contacts left over take the serial colour (solved by one thread in island order)
+    for (int i = t; i < nCons; i += T) {
+        const int c = ccol[i] >= 0 ? ccol[i] : kSerialColour;
+        cColour[i] = c;
+        atomicAdd(&colourCount[c], 1);
+    }
+    __syncthreads();
+    if (t == 0) {
+        st->cyc[22] = tKeys0 - tBuild0;
+        st->cyc[23] = tSort1 - tKeys0;
+    }
+    nIslOut = nIsl;
+    nRowsOut = nRows;
+    nConsOut = nCons;
+    moversOut = sMovers;
+    return true;
+}
+
 __device__ void Wd::solve(const StepParams& P, float4* smem, int smemRows, int smemContacts)
 {
     __shared__ int sIslands, sRows, sCons;
@@ -1389,8 +1801,25 @@ __device__ void Wd::solve(const StepParams& P, float4* smem, int smemRows, int s
     const int smemMaskRows = 2 * smemRows;
     auto mask = [&](int r) -> unsigned long long& { return r < smemMaskRows ? smemMask[r] : rowMask[r]; };
     int fIsl = 0, fRows = 0, fCons = 0, fMovers = 0;
-    bool fast = buildIslandsTable<IslPacked>(reinterpret_cast<unsigned char*>(smemBase), smemBytes, coloured,
-                                             sColourStart + 1, fIsl, fRows, fCons, fMovers);
+    bool fast = false;
+    if (coloured) {
+        // the coloured solver's islands as connected components over the CTA: the table in shared
+        // memory with the radix sort's work area at its end, else in the world's global table region
+        // with the shared-memory area as the sort's work
+        const int workBytes = RadixWorkInts() * (int)sizeof(int);
+        unsigned char* sm = reinterpret_cast<unsigned char*>(smemBase);
+        const int tableBytes = (smemBytes - workBytes) & ~15;
+        if (sm && tableBytes > 0)
+            fast = buildIslandsParallel<IslPacked>(sm, tableBytes, reinterpret_cast<int*>(sm + tableBytes),
+                                                   sColourStart + 1, fIsl, fRows, fCons, fMovers);
+        if (!fast)
+            fast = buildIslandsParallel<IslWide>(islTab, d.islTabBytes,
+                                                 sm && smemBytes >= workBytes ? reinterpret_cast<int*>(sm) : nullptr,
+                                                 sColourStart + 1, fIsl, fRows, fCons, fMovers);
+    }
+    if (!fast)
+        fast = buildIslandsTable<IslPacked>(reinterpret_cast<unsigned char*>(smemBase), smemBytes, coloured,
+                                            sColourStart + 1, fIsl, fRows, fCons, fMovers);
     if (!fast)
         fast = buildIslandsTable<IslWide>(islTab, d.islTabBytes, coloured, sColourStart + 1, fIsl, fRows, fCons,
                                           fMovers);
@@ -1610,8 +2039,8 @@ __device__ void Wd::solveTOI(const StepParams& P)
     __syncthreads();
     if (tid() == 0) st->toiPrepared = 0;
     __shared__ int sAdvance;
-    __shared__ float sBestA[kMaxCta];
-    __shared__ int sBestK[kMaxCta];
+    __shared__ float sBestA[kMaxToiCta];
+    __shared__ int sBestK[kMaxToiCta];
     unsigned long long tMark = clock64();
     auto stamp = [&](int slot) {
         if (tid() == 0) {
@@ -1630,7 +2059,7 @@ __device__ void Wd::solveTOI(const StepParams& P)
     // first pass classifies the whole list. These scratch columns belong to the collide and solve
     // phases, which set them before use.
     __shared__ int sDirty, sNeed;
-    __shared__ int sSortT[kMaxCta * 2], sSortC[kMaxCta * 2];
+    __shared__ int sSortT[kMaxToiCta * 2], sSortC[kMaxToiCta * 2];
     if (tid() == 0) sDirty = 0;
     for (int event = 0;; ++event) {
         const int n = st->contactCount;
@@ -1639,7 +2068,7 @@ __device__ void Wd::solveTOI(const StepParams& P)
         if (tid() == 0) { sAdvance = 0; sNeed = 0; }
         if (event > 0 && nTask > 1) {
             // dirty contacts into list order (descending tail index), for the sweep advances below
-            if (nTask <= 2 * kMaxCta) {
+            if (nTask <= 2 * kMaxToiCta) {
                 for (int i = tid(); i < nTask; i += nthreads()) {
                     const int c = colourList[i];
                     sSortC[i] = c;
@@ -2139,14 +2568,15 @@ __global__ void __launch_bounds__(256) NarrowphaseKernel(Batch B, const int* slo
 // (positions, then velocities) and the accumulated impulses of the island contacts when a world's
 // fit, and the broadphase proxies, pair keys and list heads outside the island solve; every use
 // falls back to global memory when the world is larger, so the shape changes speed, never results.
-// Minimum resident CTAs per SM the register allocation must allow at 128 threads: StepKernel 4
-// (128 registers), StepToiKernel 3 (168; its time-of-impact code spills more when capped lower).
-// Measured on the bench batch: 4/3 3.89 ms per step coloured, 10.20 plain; 3/3 4.05, 10.51; 4/4
-// 4.01, 10.33; 5/4 4.24, 11.37.
+// Register caps: StepKernel 128 registers (at most 256 threads, 2 resident CTAs of 256 = 4 of 128),
+// StepToiKernel 168 (at most 128 threads, 3 resident; its time-of-impact code spills more when
+// capped lower). Measured on the bench batch with 128-thread CTAs at most: StepKernel/StepToiKernel
+// resident CTAs 4/3 3.89 ms per step coloured, 10.20 plain; 3/3 4.05, 10.51; 4/4 4.01, 10.33; 5/4
+// 4.24, 11.37.
 #ifndef B2G_STEP_MIN_BLOCKS
-#define B2G_STEP_MIN_BLOCKS 4
+#define B2G_STEP_MIN_BLOCKS 2
 #endif
-__global__ void __launch_bounds__(128, B2G_STEP_MIN_BLOCKS) StepKernel(Batch B, StepParams P, const int* schedule, LaunchShape L)
+__global__ void __launch_bounds__(256, B2G_STEP_MIN_BLOCKS) StepKernel(Batch B, StepParams P, const int* schedule, LaunchShape L)
 {
     extern __shared__ float4 smem[];
     Wd W;
@@ -2312,6 +2742,8 @@ cudaError_t b2gLaunchStepToi(const b2g::Batch& B, const b2g::StepParams& P, cons
 {
     if (count <= 0) return cudaSuccess;
     const size_t smem = (2 * (size_t)smemRows + smemContacts) * sizeof(float4);
-    b2g::StepToiKernel<<<count, threads, smem, stream>>>(B, P, schedule + first, Shape(smemRows, smemContacts));
+    // the continuous phase is mostly one thread's event loop: its CTA is capped at kMaxToiCta
+    b2g::StepToiKernel<<<count, threads < b2g::kMaxToiCta ? threads : b2g::kMaxToiCta, smem, stream>>>(
+        B, P, schedule + first, Shape(smemRows, smemContacts));
     return cudaGetLastError();
 }

@@ -225,7 +225,7 @@ class World:
     PHASES = ["new_pairs", "collide", "island_build", "island_solve", "fixture_sync", "pairs", "toi", "step",
               "solve_init", "solve_velocity", "solve_store_integrate", "solve_position", "solve_writeback",
               "solve_sleep", "pairs_find_sort", "pairs_create", "toi_classify", "toi_select", "toi_island",
-              "toi_solve", "toi_sync", "toi_pairs", "unused22", "unused23"]
+              "toi_solve", "toi_sync", "toi_pairs", "build_components", "build_sort"]
 
     def profile(self) -> np.ndarray:
         """SM clock cycles per world and phase of the last step, shape (worlds, 24) (see PHASES)."""

@@ -175,7 +175,8 @@ gb_status gb_world_solver_stats(gb_world* world, int* colours, int* vel_iters, f
  * gb_world_launch_plan reports the plan, classes[5 * i] = first schedule slot, count, threads per
  * CTA, shared-memory island rows, shared-memory contacts, and after tuning the best time (ms) each
  * candidate took. gb_world_set_launch_plan sets a plan in the same layout (classes must cover the
- * schedule in order; threads a multiple of 32 in [32, 128]; at most 48 KB of shared memory). */
+ * schedule in order; threads a multiple of 32 in [32, 256], the continuous phase using at most 128
+ * of them; at most 48 KB of shared memory). */
 gb_status gb_world_autotune(gb_world* world, int steps_per_candidate);
 /* gb_world_step as a CUDA graph: the first call (and any call after the step's parameters, solver
  * or plan changed, or device memory was reallocated) captures one step, every launch of the plan,
@@ -254,7 +255,8 @@ gb_status gb_world_totals(gb_world* world, long long* out);
  * 11 position sweeps, 12 write-back, 13 sleep; 14 broadphase pair finding and sorting, 15 contact
  * creation; the continuous split 16 classification + time of impact, 17 earliest-event selection,
  * 18 event mini-island build, 19 mini-island solve, 20 fixture sync + contact invalidation,
- * 21 pair finding after events (22, 23 unused). The narrowphase and time-of-impact pre-passes run
+ * 21 pair finding after events; the coloured solver's island build split 22 components and keys,
+ * 23 key sort (zero for the plain solver). The narrowphase and time-of-impact pre-passes run
  * flat over all worlds' contacts before the collide and continuous phases and are not counted. */
 #define GB_PROFILE_SLOTS 24
 gb_status gb_world_profile(gb_world* world, unsigned long long* out);
