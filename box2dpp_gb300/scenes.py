@@ -325,6 +325,37 @@ def drop(n_bodies: int, rng: SplitMix64, half_size: float | None = None, allow_s
     return _settings(s, allow_sleep)
 
 
+def sensors(rng: SplitMix64, allow_sleep: bool = True, n_bodies: int = 80) -> Scene:
+    """Sensor fixtures of every kind a b2Fixture can carry (isSensor, b2Fixture.h:107): a static body
+    with two sensor zones across the fall (begin and end calls as bodies pass through), dynamic
+    bodies of which every third carries a large proximity-sensor circle beside its solid fixture
+    (sensor contacts with the ground, the zones' body and other bodies), and a kinematic sweeper
+    whose only fixture is a sensor box crossing the pile. Sensor contacts are touching when the
+    shapes overlap (b2TestOverlap), have no manifold, are never solved and do not wake bodies."""
+    s = Scene(name="sensors")
+    g = s.body(STATIC, 0.0, 0.0)
+    s.fixture(g, EDGE, [-20.0, 0.0, 20.0, 0.0, 0, 0, 0, 0, 0, 0], friction=0.5)
+    s.fixture(g, EDGE, [-20.0, 0.0, -20.0, 30.0, 0, 0, 0, 0, 0, 0], friction=0.5)
+    s.fixture(g, EDGE, [20.0, 0.0, 20.0, 30.0, 0, 0, 0, 0, 0, 0], friction=0.5)
+    z = s.body(STATIC, 0.0, 0.0)
+    s.fixture(z, BOX, [8.0, 1.0, -6.0, 6.0, 0.0], 5, sensor=True)
+    s.fixture(z, BOX, [6.0, 1.5, 7.0, 11.0, 0.3], 5, sensor=True)
+    for i in range(n_bodies):
+        x = _q(rng.uniform(-17.0, 17.0))
+        y = _q(4.0 + 0.45 * i + rng.uniform(0.0, 0.3))
+        b = s.body(DYNAMIC, x, y, angle=_q(rng.uniform(-1.0, 1.0)))
+        r = _q(rng.uniform(0.25, 0.6))
+        if i % 2:
+            s.fixture(b, CIRCLE, [0.0, 0.0, r], density=1.0, friction=0.4)
+        else:
+            s.fixture(b, BOX, [r, _q(r * 0.7)], 2, density=1.0, friction=0.4)
+        if i % 3 == 0:
+            s.fixture(b, CIRCLE, [0.0, 0.0, _q(3.0 * r)], sensor=True)
+    k = s.body(KINEMATIC, -18.0, 1.5, vx=3.0)
+    s.fixture(k, BOX, [1.0, 1.5], 2, sensor=True)
+    return _settings(s, allow_sleep)
+
+
 def chains(n_chains: int, links: int, rng: SplitMix64, allow_sleep: bool = True, spacing: float = 3.0,
            limit: float = math.pi / 6.0) -> Scene:
     """Chains of revolute-jointed 0.1 x 0.5 m box links (limits +/-30 degrees) hanging from a static

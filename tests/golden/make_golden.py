@@ -8,7 +8,10 @@ Two builds of the reference are used: ``libm`` (glibc sinf/cosf, the reference a
 
 * ``<case>_<trig>.npz``: for a scene stepped N times, the SHA-256 of every step's full state
   (bodies 12 x float32 + contacts 8 x int32 + 12 x float32 in world-list order, as dumped by the
-  C-ABIs) and the full body/contact arrays at a few checkpoint steps.
+  C-ABIs) and the full body/contact arrays at a few checkpoint steps (none for the 10,000-body
+  drop, whose arrays would be megabytes).
+
+  python tests/golden/make_golden.py --case <name>   writes one trajectory case only.
 * ``collide.npz``: seeded shape pairs of every supported type pair with the reference manifolds.
 * ``toi.npz``: seeded sweeps with the reference b2TimeOfImpact result.
 * ``trig.npz``: glibc sinf/cosf on seeded angles (how far the project trig is from libm).
@@ -66,6 +69,10 @@ def cases():
         ("pulley_mouse", lambda: scenes.pulley_mouse(scenes.SplitMix64(4)), 300, [1, 60, 150, 300]),
         ("gears", lambda: scenes.gears(scenes.SplitMix64(8)), 300, [1, 60, 150, 300]),
         ("chain_terrain", lambda: scenes.chain_terrain(scenes.SplitMix64(12)), 300, [1, 60, 150, 300]),
+        ("sensors", lambda: scenes.sensors(scenes.SplitMix64(13)), 300, [1, 100, 300]),
+        # the 10,000-body drop at full size: per-step digests only (no checkpoint arrays, which would
+        # be megabytes)
+        ("config2_10k", lambda: scenes.config2(10000, seed=1, allow_sleep=True), 200, []),
     ] + [(f"batch{i}", (lambda i=i: batch_world(i)), 200, [200]) for i in range(24)]
 
 

@@ -42,6 +42,13 @@ def test_events_single_worlds(gpu):
     assert _compare([scenes.chains(3, 6, scenes.SplitMix64(2))], 60).sum() == 0
 
 
+def test_events_sensors(gpu):
+    """Sensor fixtures: begin and end calls of sensor contacts (static zones, proximity circles on
+    dynamic bodies, a kinematic sweeper), no pre-solve or post-solve for them."""
+    kinds = _compare([scenes.sensors(scenes.SplitMix64(13))], 200)
+    assert kinds[0] > 0 and kinds[1] > 0, kinds
+
+
 def test_events_batch(gpu):
     kinds = _compare(scenes.config3(12, seed=21), 60)
     assert kinds.min() > 0, kinds  # begin, end, pre-solve and post-solve all occur
