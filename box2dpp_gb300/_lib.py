@@ -31,7 +31,8 @@ EXPORTS = [
     "gb_mlp_forward", "gb_mlp_gradients", "gb_mlp_train", "gb_world_set_warm_start", "gb_world_warm_stats",
     "gb_world_set_contact_log", "gb_world_read_contact_log", "gb_world_contact_stats", "gb_world_set_events",
     "gb_world_read_events", "gb_world_query_aabb", "gb_world_raycast", "gb_create_joints",
-    "gb_world_stage_times", "gb_body_edits",
+    "gb_world_stage_times", "gb_body_edits", "gb_world_set_limits", "gb_destroy_body", "gb_destroy_joint",
+    "gb_destroy_fixture",
 ]
 
 
@@ -111,6 +112,10 @@ def load(build_if_missing: bool = True):
         "gb_collide": [i, _i32, _f32, _i32, _f32, _i32, _f32, _i32, _f32, _i32, _f32],
         "gb_collide_noalloc": [i, _i32, _f32, _i32, _f32, _i32, _f32, _i32, _f32, _i32, _f32],
         "gb_world_set_solver": [vp, i, f, i],
+        "gb_world_set_limits": [vp, i, i],
+        "gb_destroy_body": [vp, i, i, _i32, i, C.POINTER(C.c_int)],
+        "gb_destroy_joint": [vp, i, i, _i32, i, C.POINTER(C.c_int)],
+        "gb_destroy_fixture": [vp, i, i, _i32, i, C.POINTER(C.c_int)],
         "gb_world_solver_stats": [vp, _i32, _i32, _f32],
         "gb_world_autotune": [vp, i],
         "gb_world_graph_step": [vp, f, i, i],

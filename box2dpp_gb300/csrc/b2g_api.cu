@@ -51,6 +51,7 @@ struct HBody {
     float mass = 0, invMass = 0, I = 0, invI = 0;
     float linDamp = 0, angDamp = 0, gravScale = 1, sleepTime = 0;
     int fixtureList = kNullIdx, contactList = kNullIdx, jointList = kNullIdx, next = kNullIdx;
+    bool alive = true; // false once destroyed: its columns are zeros and it is in no list
 };
 
 struct HFixture {
@@ -76,7 +77,13 @@ struct HWorld {
     std::vector<Joint> joints;
     std::vector<float4> fat;
     std::vector<int> pfix, moved;
-    int nodeCount = 0, proxyCount = 0;
+    // The reference tree's node ids (b2DynamicTree): never-used ids are handed out in order from
+    // nodeFresh; freed ids are reused last-in first-out. nodeFree holds the freed ids, -1 standing for
+    // an internal node (a leaf's parent) whose id is never needed: a freed leaf is always on top of
+    // its parent, and a proxy takes a leaf and then a parent, so leaves only ever come back as leaves.
+    int nodeFresh = 0, proxyCount = 0;
+    std::vector<int> nodeFree;
+    bool treeLost = false; // a leaf would have taken an internal node's id (never expected)
     int newFixture = 0;
     WorldState state{};
     bool hasState = false; // state/contacts valid (pulled back from, or never sent to, the device)
@@ -131,6 +138,8 @@ struct gb_world {
     float graphTol = -1.0f;
     LaunchPlan graphPlan;
     int solver = kSolverPlain;
+    int contactCapLimit = 0;    // > 0: contact slots per world at the first upload (gb_world_set_limits)
+    int maxToiEvents = 4096;    // time-of-impact events per world per step
     float tolerance = 0.0f;
     int measureResidual = 0;
     int warmMode = kWarmReference;
@@ -203,14 +212,29 @@ void ResetMassData(HWorld& W, int bi)
     b.v = b.v + Cross(b.w, b.sw.c - oldCenter);
 }
 
-// Proxy ids are node ids of the reference's b2DynamicTree: its free list hands out 0, 1, 2, ... and
-// every insertion after the first also takes one internal node (b2DynamicTree.cpp:56-105, 112-131),
-// so without removals the k-th proxy gets id 0 for k = 0 and 2k - 1 otherwise.
+// Proxy ids are node ids of the reference's b2DynamicTree. b2DynamicTree::CreateProxy takes a node
+// for the leaf, and InsertLeaf one more for its new parent unless the tree was empty
+// (b2DynamicTree.cpp:56-131, 179-194); DestroyProxy's RemoveLeaf frees the leaf's parent unless the
+// leaf was the root, then the leaf itself (:124-130, 319-377); MoveProxy frees one internal node and
+// takes it straight back (LIFO), and Balance moves no ids. The free list is therefore a stack of
+// (parent, leaf) pairs over the never-used ids, and the next leaf id follows without the tree's shape.
+int AllocNode(HWorld& W, bool leaf)
+{
+    if (!W.nodeFree.empty()) {
+        const int id = W.nodeFree.back();
+        W.nodeFree.pop_back();
+        if (leaf && id < 0) W.treeLost = true;
+        return id;
+    }
+    return W.nodeFresh++;
+}
+
 int AllocateProxy(HWorld& W, float4 fatAabb, int fixture)
 {
-    int id = W.nodeCount++;
-    if (W.proxyCount > 0) W.nodeCount++;
+    int id = AllocNode(W, true);
+    if (W.proxyCount > 0) AllocNode(W, false);
     ++W.proxyCount;
+    if (id < 0) id = W.nodeFresh++;  // unreachable by the pairing above; keeps the id valid
     if ((int)W.fat.size() <= id) {
         W.fat.resize(id + 1, make_float4(0, 0, 0, 0));
         W.pfix.resize(id + 1, kNullIdx);
@@ -220,6 +244,18 @@ int AllocateProxy(HWorld& W, float4 fatAabb, int fixture)
     W.pfix[id] = fixture;
     W.moved[id] = 1;
     return id;
+}
+
+// b2BroadPhase::DestroyProxy (Collision/b2BroadPhase.cpp:74-79): out of the move buffer, the leaf's
+// parent (when the tree has more leaves) and then the leaf back to the free list.
+void FreeProxy(HWorld& W, int id)
+{
+    if (W.proxyCount > 1) W.nodeFree.push_back(-1);
+    W.nodeFree.push_back(id);
+    --W.proxyCount;
+    W.fat[id] = make_float4(0, 0, 0, 0);
+    W.pfix[id] = kNullIdx;
+    W.moved[id] = 0;
 }
 
 Shape MakeShape(int type, const float* s, int n)
@@ -416,7 +452,7 @@ StepParams MakeParams(const gb_world* g, float dt, int vi, int pi)
     P.dt = dt;
     P.velocityIterations = vi;
     P.positionIterations = pi;
-    P.maxToiEvents = 4096;
+    P.maxToiEvents = g->maxToiEvents;
     P.solver = g->solver;
     P.tolerance = g->tolerance;
     P.measureResidual = g->measureResidual;
@@ -611,6 +647,7 @@ gb_status Upload(gb_world* g)
         d.proxyBase = (int)tp; d.proxyCap = std::max(1, (int)W.fat.size());
         int oldCap = W.hasState ? (int)W.contacts.ci.size() : 0;
         int cap = std::max(64, 8 * d.fixCount);
+        if (g->contactCapLimit > 0 && !W.hasState) cap = g->contactCapLimit;
         cap = std::max(cap, oldCap);
         d.contactBase = (int)tc; d.contactCap = cap;
         d.jointBase = (int)tj; d.jointCount = (int)W.joints.size();
@@ -975,6 +1012,184 @@ gb_status CreateJoint(HWorld& W, int type, int a, int b, const float* f, int fl,
     return GB_OK;
 }
 
+// ------------------------------------------------------------------ destruction (host mirror)
+// The listener calls a destruction makes, in order: {0, joint, 0} SayGoodbye(joint), {1, fixture, 0}
+// SayGoodbye(fixture), {2, fixtureA, fixtureB} EndContact.
+using Calls = std::vector<int>;
+
+void WakeHost(HBody& b)
+{
+    if ((b.flags & kBAwake) == 0) {
+        b.flags |= kBAwake;
+        b.sleepTime = 0.0f;
+    }
+}
+
+// b2ContactManager::Destroy + b2Contact::Destroy (Dynamics/b2ContactManager.cpp:46-104,
+// Contacts/b2Contact.cpp:102-125) on the pulled-back contact columns: EndContact when touching, out
+// of the world list (order kept) and both bodies' edge lists, both bodies woken when the manifold had
+// points and neither fixture is a sensor, the slot back to the free list.
+void DestroyContactHost(HWorld& W, int c, Calls& calls)
+{
+    HContacts& C = W.contacts;
+    const int4 info = C.ci[c];
+    const int fA = info.y, fB = info.z;
+    const int bA = W.fixtures[fA].body, bB = W.fixtures[fB].body;
+    if (info.x & kCTouching) calls.insert(calls.end(), {2, fA, fB});
+    const int n = W.state.contactCount;
+    int k = 0;
+    while (k < n && C.order[k] != c) ++k;
+    for (; k + 1 < n; ++k) C.order[k] = C.order[k + 1];
+    W.state.contactCount = n - 1;
+    for (int side = 0; side < 2; ++side) {
+        HBody& body = W.bodies[side == 0 ? bA : bB];
+        const int e = 2 * c + side;
+        const int4 v = C.ce[c];
+        const int pe = side == 0 ? v.x : v.z, ne = side == 0 ? v.y : v.w;
+        if (pe != kNullIdx) (pe & 1 ? C.ce[pe >> 1].w : C.ce[pe >> 1].y) = ne;
+        if (ne != kNullIdx) (ne & 1 ? C.ce[ne >> 1].z : C.ce[ne >> 1].x) = pe;
+        if (body.contactList == e) body.contactList = ne;
+    }
+    if (C.mh[c].y > 0 && !W.fixtures[fA].sensor && !W.fixtures[fB].sensor) {
+        WakeHost(W.bodies[bA]);
+        WakeHost(W.bodies[bB]);
+    }
+    C.ci[c] = make_int4(0, 0, 0, 0);
+    C.ce[c] = make_int4(kNullIdx, kNullIdx, kNullIdx, kNullIdx);
+    C.cnext[c] = W.state.freeContact;
+    W.state.freeContact = c;
+}
+
+// b2World::DestroyJoint (Dynamics/b2World.cpp:274-362). The slot stays, with no bodies.
+void DestroyJointHost(HWorld& W, int jn)
+{
+    Joint& j = W.joints[jn];
+    const bool collideConnected = j.collideConnected;
+    if (j.prev != kNullIdx) W.joints[j.prev].next = j.next;
+    if (j.next != kNullIdx) W.joints[j.next].prev = j.prev;
+    if (W.jointList == jn) W.jointList = j.next;
+    const int bA = j.bodyA, bB = j.bodyB;
+    WakeHost(W.bodies[bA]);
+    WakeHost(W.bodies[bB]);
+    for (int side = 0; side < 2; ++side) {
+        HBody& body = W.bodies[side == 0 ? bA : bB];
+        const int e = 2 * jn + side;
+        const int pe = j.ePrev[side], ne = j.eNext[side];
+        if (pe != kNullIdx) W.joints[pe >> 1].eNext[pe & 1] = ne;
+        if (ne != kNullIdx) W.joints[ne >> 1].ePrev[ne & 1] = pe;
+        if (body.jointList == e) body.jointList = ne;
+        j.ePrev[side] = j.eNext[side] = kNullIdx;
+    }
+    j.prev = j.next = kNullIdx;
+    j.bodyA = j.bodyB = kNullIdx;
+    j.islandFlag = 0;
+    if (!collideConnected && W.hasState) {
+        HContacts& C = W.contacts;
+        for (int e = W.bodies[bB].contactList; e != kNullIdx;) {
+            const int c = e >> 1;
+            const int4 info = C.ci[c];
+            const int other = (e & 1) == 0 ? W.fixtures[info.z].body : W.fixtures[info.y].body;
+            if (other == bA) C.ci[c].x |= kCFilter;
+            const int4 v = C.ce[c];
+            e = (e & 1) ? v.w : v.y;
+        }
+    }
+}
+
+int NextContactEdge(const HWorld& W, int e)
+{
+    const int4 v = W.contacts.ce[e >> 1];
+    return (e & 1) ? v.w : v.y;
+}
+
+// b2World::DestroyBody (Dynamics/b2World.cpp:133-212)
+void DestroyBodyHost(HWorld& W, int bi, Calls& calls)
+{
+    for (int e = W.bodies[bi].jointList; e != kNullIdx;) {
+        const int jn = e >> 1;
+        e = W.joints[jn].eNext[e & 1];
+        calls.insert(calls.end(), {0, jn, 0});
+        DestroyJointHost(W, jn);
+        W.bodies[bi].jointList = e;
+    }
+    W.bodies[bi].jointList = kNullIdx;
+    if (W.hasState)
+        for (int e = W.bodies[bi].contactList; e != kNullIdx;) {
+            const int c = e >> 1;
+            e = NextContactEdge(W, e);
+            DestroyContactHost(W, c, calls);
+        }
+    W.bodies[bi].contactList = kNullIdx;
+    for (int f = W.bodies[bi].fixtureList; f != kNullIdx;) {
+        HFixture& fx = W.fixtures[f];
+        const int next = fx.next;
+        if (fx.shape.chain != 2) calls.insert(calls.end(), {1, f, 0});  // a chain is one b2Fixture
+        if (fx.proxyId != kNullIdx) FreeProxy(W, fx.proxyId);
+        fx.proxyId = kNullIdx;
+        fx.body = kNullIdx;
+        fx.next = kNullIdx;
+        W.bodies[bi].fixtureList = next;
+        f = next;
+    }
+    if (W.bodyList == bi) {
+        W.bodyList = W.bodies[bi].next;
+    } else {
+        for (int b = W.bodyList; b != kNullIdx; b = W.bodies[b].next)
+            if (W.bodies[b].next == bi) { W.bodies[b].next = W.bodies[bi].next; break; }
+    }
+    HBody dead;
+    dead.alive = false;
+    dead.xf.p = V(0.0f, 0.0f);
+    dead.xf.q.s = 0.0f;
+    dead.xf.q.c = 0.0f;
+    dead.sw.localCenter = V(0.0f, 0.0f);
+    dead.sw.c0 = dead.sw.c = V(0.0f, 0.0f);
+    dead.sw.a0 = dead.sw.a = dead.sw.alpha0 = 0.0f;
+    dead.gravScale = 0.0f;
+    W.bodies[bi] = dead;
+}
+
+// b2Body::DestroyFixture (Dynamics/b2Body.cpp:216-281); a chain (its first child) goes whole
+void DestroyFixtureHost(HWorld& W, int f, Calls& calls)
+{
+    const int bi = W.fixtures[f].body;
+    int last = f;
+    if (W.fixtures[f].shape.type == kEdge && W.fixtures[f].shape.chain == 1)
+        while (last + 1 < (int)W.fixtures.size() && W.fixtures[last + 1].body == bi &&
+               W.fixtures[last + 1].shape.type == kEdge && W.fixtures[last + 1].shape.chain == 2)
+            ++last;
+    auto mine = [&](int id) { return id >= f && id <= last; };
+    int* node = &W.bodies[bi].fixtureList;
+    while (*node != kNullIdx && !mine(*node)) node = &W.fixtures[*node].next;
+    int after = *node;
+    while (after != kNullIdx && mine(after)) after = W.fixtures[after].next;
+    if (*node != kNullIdx) *node = after;
+    if (W.hasState)
+        for (int e = W.bodies[bi].contactList; e != kNullIdx;) {
+            const int c = e >> 1;
+            e = NextContactEdge(W, e);
+            const int4 info = W.contacts.ci[c];
+            if (mine(info.y) || mine(info.z)) DestroyContactHost(W, c, calls);
+        }
+    for (int id = f; id <= last; ++id) {
+        HFixture& fx = W.fixtures[id];
+        if ((W.bodies[bi].flags & kBActive) && fx.proxyId != kNullIdx) FreeProxy(W, fx.proxyId);
+        fx.proxyId = kNullIdx;
+        fx.body = kNullIdx;
+        fx.next = kNullIdx;
+    }
+    ResetMassData(W, bi);
+}
+
+gb_status Finish(const Calls& calls, int* out, int cap, int* n_calls)
+{
+    const int n = (int)calls.size() / 3;
+    if (out)
+        for (int i = 0; i < 3 * std::min(n, std::max(cap, 0)); ++i) out[i] = calls[i];
+    if (n_calls) *n_calls = n;
+    return GB_OK;
+}
+
 } // namespace
 
 extern "C" {
@@ -1276,6 +1491,16 @@ gb_status gb_world_sync(gb_world* g)
     if (err & kErrCapacity) return GB_ERR_CAPACITY;
     if (err & kErrTimeout) return GB_ERR_TIMEOUT;
     if (err & kErrInvalid) return GB_ERR_INVALID;
+    return GB_OK;
+}
+
+gb_status gb_world_set_limits(gb_world* g, int contact_capacity, int max_toi_events)
+{
+    if (!g || contact_capacity < 0 || max_toi_events < 1) return GB_ERR_INVALID;
+    if (contact_capacity > 0 && g->onDevice) return GB_ERR_INVALID;
+    g->contactCapLimit = contact_capacity;
+    if (g->maxToiEvents != max_toi_events) ReleaseGraph(g);
+    g->maxToiEvents = max_toi_events;
     return GB_OK;
 }
 
@@ -1798,6 +2023,41 @@ gb_status gb_collide(int n, const int* type_a, const float* shape_a, const int* 
     if (e == cudaSuccess) e = cudaMemcpy(out_floats, dof, 3 * n * sizeof(float4), cudaMemcpyDeviceToHost);
     cudaFree(dsa); cudaFree(dsb); cudaFree(dxa); cudaFree(dxb); cudaFree(doi); cudaFree(dof);
     return cudaErr(e);
+}
+
+gb_status gb_destroy_body(gb_world* g, int w, int body, int* calls, int cap, int* n_calls)
+{
+    gb_status s = Mutable(g, w);
+    if (s != GB_OK) return s;
+    HWorld& W = g->worlds[w];
+    if (body < 0 || body >= (int)W.bodies.size() || !W.bodies[body].alive) return GB_ERR_INVALID;
+    Calls c;
+    DestroyBodyHost(W, body, c);
+    return Finish(c, calls, cap, n_calls);
+}
+
+gb_status gb_destroy_joint(gb_world* g, int w, int joint, int* calls, int cap, int* n_calls)
+{
+    gb_status s = Mutable(g, w);
+    if (s != GB_OK) return s;
+    HWorld& W = g->worlds[w];
+    if (joint < 0 || joint >= (int)W.joints.size() || W.joints[joint].bodyA == kNullIdx) return GB_ERR_INVALID;
+    Calls c;
+    DestroyJointHost(W, joint);
+    return Finish(c, calls, cap, n_calls);
+}
+
+gb_status gb_destroy_fixture(gb_world* g, int w, int fixture, int* calls, int cap, int* n_calls)
+{
+    gb_status s = Mutable(g, w);
+    if (s != GB_OK) return s;
+    HWorld& W = g->worlds[w];
+    if (fixture < 0 || fixture >= (int)W.fixtures.size() || W.fixtures[fixture].body == kNullIdx) return GB_ERR_INVALID;
+    const Shape& sh = W.fixtures[fixture].shape;
+    if (sh.type == kEdge && sh.chain == 2) return GB_ERR_INVALID;  // a chain goes by its first child
+    Calls c;
+    DestroyFixtureHost(W, fixture, c);
+    return Finish(c, calls, cap, n_calls);
 }
 
 const char* gb_version(void) { return "box2d_gb300 0.1 (Box2D 2.3.2 step semantics, sm_103a)"; }

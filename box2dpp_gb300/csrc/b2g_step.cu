@@ -1511,6 +1511,7 @@ __device__ bool Wd::buildIslandsParallel(unsigned char* base, int capacity, int*
     }
     for (int j = t; j < NJ; j += T) {
         const int A = jt[j].bodyA, B = jt[j].bodyB;
+        if (A < 0 || B < 0) continue;  // a destroyed joint's slot
         const unsigned char fa = bflag[A], fb = bflag[B];
         if (!(fa & fStatic) && !(fb & fStatic) && (fa & fActive) && (fb & fActive)) unite(A, B);
     }
@@ -1581,6 +1582,7 @@ __device__ bool Wd::buildIslandsParallel(unsigned char* base, int capacity, int*
     }
     for (int j = t; j < NJ; j += T) {
         const int A = jt[j].bodyA, B = jt[j].bodyB;
+        if (A < 0 || B < 0) continue;  // a destroyed joint's slot
         const unsigned char fa = bflag[A], fb = bflag[B];
         if (!(fa & fActive) || !(fb & fActive)) continue;
         const int isl = !(fa & fStatic) ? islOf[A] : (!(fb & fStatic) ? islOf[B] : -1);

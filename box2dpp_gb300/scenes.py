@@ -325,6 +325,39 @@ def drop(n_bodies: int, rng: SplitMix64, half_size: float | None = None, allow_s
     return _settings(s, allow_sleep)
 
 
+def destroy_mix(rng: SplitMix64, allow_sleep: bool = True) -> Scene:
+    """The scene of the destruction cases: an 8-row box pyramid and a small static ledge on an edge
+    ground, a chain of 8 links hanging from a static anchor by revolute joints, a body with two
+    fixtures (a box and a circle), a pair of circles tied by a distance joint that does not let them
+    collide, and a loose drop of circles. Body indices: 0 ground, 1..36 the pyramid, 37 the ledge,
+    38 the anchor, 39..46 the links (joints 0..7), 47 the two-fixture body, 48 and 49 the tied pair
+    (joint 8), 50.. the drop."""
+    s = pyramid(8, allow_sleep=allow_sleep)
+    s.name = "destroy_mix"
+    ledge = s.body(STATIC, 9.0, 3.0)
+    s.fixture(ledge, BOX, [1.5, 0.2], 2, friction=0.5)
+    anchor = s.body(STATIC, -12.0, 12.0)
+    s.fixture(anchor, CIRCLE, [0.0, 0.0, 0.2])
+    prev = anchor
+    for k in range(8):
+        b = s.body(DYNAMIC, _q(-12.0 + 0.5 + 1.0 * k), 12.0)
+        s.fixture(b, BOX, [0.5, 0.1], 2, density=2.0, friction=0.3, group=-1)
+        s.revolute(prev, b, [0.5 if k else 0.0, 0.0], [-0.5, 0.0])
+        prev = b
+    t = s.body(DYNAMIC, 9.0, 6.0, angle=0.3)
+    s.fixture(t, BOX, [0.6, 0.4], 2, density=1.5, friction=0.5)
+    s.fixture(t, CIRCLE, [0.5, 0.3, 0.35], density=3.0, friction=0.5)
+    a = s.body(DYNAMIC, 3.0, 9.0)
+    s.fixture(a, CIRCLE, [0.0, 0.0, 0.4], density=1.0, friction=0.4)
+    b = s.body(DYNAMIC, 3.6, 9.5)
+    s.fixture(b, CIRCLE, [0.0, 0.0, 0.4], density=1.0, friction=0.4)
+    s.distance(a, b, [0.0, 0.0], [0.0, 0.0], 0.8)
+    for i in range(12):
+        c = s.body(DYNAMIC, _q(rng.uniform(-6.0, 6.0)), _q(10.0 + 0.9 * i))
+        s.fixture(c, CIRCLE, [0.0, 0.0, _q(rng.uniform(0.2, 0.45))], density=1.0, friction=0.4)
+    return s
+
+
 def sensors(rng: SplitMix64, allow_sleep: bool = True, n_bodies: int = 80) -> Scene:
     """Sensor fixtures of every kind a b2Fixture can carry (isSensor, b2Fixture.h:107): a static body
     with two sensor zones across the fall (begin and end calls as bodies pass through), dynamic

@@ -75,6 +75,54 @@ class World:
         _lib.check(self.lib.gb_world_set_solver(self.h, code, float(tolerance), int(measure_residual)),
                    "gb_world_set_solver")
 
+    # ------------------------------------------------------------------ changes between steps
+    def add_body(self, type_: int, f, flags: int, w: int = 0) -> int:
+        """b2World::CreateBody between steps (f: the 9 floats of the body encoding); returns its index."""
+        out = np.zeros(1, dtype=np.int32)
+        _lib.check(self.lib.gb_create_bodies(self.h, w, 1, np.array([type_], np.int32),
+                                             np.ascontiguousarray(f, dtype=np.float32), np.array([flags], np.int32),
+                                             out), "gb_create_bodies")
+        self.n_bodies[w] += 1
+        if type_ == 2:
+            self.dynamic_bodies += 1
+        return int(out[0])
+
+    def add_fixture(self, body: int, type_: int, shape, n: int, mat, filt, w: int = 0) -> int:
+        """b2Body::CreateFixture between steps (one fixture record); returns its index."""
+        s = np.zeros(16, dtype=np.float32)
+        s[:len(shape)] = shape
+        out = np.zeros(1, dtype=np.int32)
+        _lib.check(self.lib.gb_create_fixtures(self.h, w, 1, np.array([body], np.int32), np.array([type_], np.int32),
+                                               s, np.array([n], np.int32), np.asarray(mat, dtype=np.float32),
+                                               np.asarray(filt, dtype=np.int32), out), "gb_create_fixtures")
+        self.n_fixtures[w] += 1
+        return int(out[0])
+
+    def _destroy(self, fn: str, index: int, w: int):
+        calls = np.zeros((256, 3), dtype=np.int32)
+        n = C.c_int()
+        _lib.check(getattr(self.lib, fn)(self.h, w, int(index), calls, 256, C.byref(n)), fn)
+        return calls[:min(n.value, 256)]
+
+    def destroy_body(self, body: int, w: int = 0) -> np.ndarray:
+        """b2World::DestroyBody; returns the listener calls as rows {kind, a, b} (see gb_destroy_body):
+        kind 0 SayGoodbye(joint a), 1 SayGoodbye(fixture a), 2 EndContact(a, b)."""
+        return self._destroy("gb_destroy_body", body, w)
+
+    def destroy_joint(self, joint: int, w: int = 0) -> np.ndarray:
+        """b2World::DestroyJoint (no listener calls)."""
+        return self._destroy("gb_destroy_joint", joint, w)
+
+    def destroy_fixture(self, fixture: int, w: int = 0) -> np.ndarray:
+        """b2Body::DestroyFixture; returns its EndContact calls as rows {2, fixtureA, fixtureB}."""
+        return self._destroy("gb_destroy_fixture", fixture, w)
+
+    def set_limits(self, contact_capacity: int = 0, max_toi_events: int = 4096) -> None:
+        """Fixed capacities of the device step (see gb_world_set_limits): contact slots per world at
+        the first upload (0: the default) and time-of-impact events per world per step."""
+        _lib.check(self.lib.gb_world_set_limits(self.h, int(contact_capacity), int(max_toi_events)),
+                   "gb_world_set_limits")
+
     def solver_stats(self):
         """(colours, velocity iterations, velocity residual) per world of the last step."""
         col = np.zeros(self.n_worlds, dtype=np.int32)

@@ -141,7 +141,35 @@ gb_status gb_world_upload(gb_world* world);
 gb_status gb_world_step(gb_world* world, float dt, int velocity_iterations, int position_iterations);
 
 /* Waits for queued steps and returns the first error any world raised since the last sync. */
+/* b2World::DestroyBody (Box2D/Dynamics/b2World.cpp:133), b2World::DestroyJoint (:274) and
+ * b2Body::DestroyFixture (Box2D/Dynamics/b2Body.cpp:216), between steps, with the reference's order of
+ * effects: a body's joints (each announced to the destruction listener, then destroyed: both bodies
+ * woken, contacts between them flagged for filtering unless the joint let them collide), its contacts
+ * (EndContact when touching; both bodies woken when the manifold had points), its fixtures (each
+ * announced) and their broadphase proxies; a fixture's contacts and proxies, then the body's mass data
+ * reset. A chain fixture is destroyed by its first child's id, with all its children. Indices of other
+ * bodies, fixtures and joints do not change; a destroyed body reads back as zeros, and bodies created
+ * later take the next indices. Proxy ids of later fixtures reuse the freed tree nodes exactly as the
+ * reference's b2DynamicTree does. The listener calls go to calls (3 ints each, at most cap):
+ * {0, joint, 0} SayGoodbye(b2Joint*), {1, fixture, 0} SayGoodbye(b2Fixture*), {2, fixtureA, fixtureB}
+ * EndContact; n_calls receives their number. GB_ERR_INVALID for an index that is out of range or
+ * already destroyed. */
+gb_status gb_destroy_body(gb_world* world, int w, int body, int* calls, int cap, int* n_calls);
+gb_status gb_destroy_joint(gb_world* world, int w, int joint, int* calls, int cap, int* n_calls);
+gb_status gb_destroy_fixture(gb_world* world, int w, int fixture, int* calls, int cap, int* n_calls);
+
 gb_status gb_world_sync(gb_world* world);
+
+/* No counterpart in the reference (whose buffers grow on demand). The fixed capacities of the device
+ * step, for callers that size memory themselves and for tests of the error paths: contact_capacity
+ * > 0 sets the contact slots of each world at its first upload (0 keeps the default, max(64, 8 x
+ * fixtures); GB_ERR_INVALID once the world is on the device); max_toi_events bounds the
+ * time-of-impact events of each world in one step (default 4096). A step that needs more contact
+ * slots than it has, or more events, stops that work, completes the step and makes the next
+ * gb_world_sync return GB_ERR_CAPACITY or GB_ERR_TIMEOUT; the world's state after such a step is not
+ * the reference's and the world should be rebuilt (gb_world_destroy, then create it again with larger
+ * limits). Every loop on the device is bounded, so the error never stalls the GPU. */
+gb_status gb_world_set_limits(gb_world* world, int contact_capacity, int max_toi_events);
 
 /* Island solver of the following steps. GB_SOLVER_PLAIN (default) is b2Island::Solve's sequential
  * per-island Gauss-Seidel order (Box2D/Dynamics/b2Island.cpp:185-384), bit-exact with the reference.

@@ -85,6 +85,10 @@ def _declare(lib, p: str) -> None:
         "body_edit": (None, [vp, C.c_int, C.c_int, C.c_int, _f32p]),
     }
     sig["joint"] = (C.c_int, [vp, C.c_int, C.c_int, C.c_int, _f32p, C.c_int])
+    sig["body"] = (C.c_int, [vp, C.c_int, _f32p, C.c_int])
+    sig["fixture"] = (C.c_int, [vp, C.c_int, C.c_int, _f32p, C.c_int, _f32p, _i32p])
+    for kind in ("body", "joint", "fixture"):
+        sig["destroy_" + kind] = (C.c_int, [vp, C.c_int, _i32p, C.c_int])
     if p == "rw_":
         sig["query_aabb"] = (C.c_int, [vp, _f32p, _i32p, C.c_int])
         sig["raycast"] = (C.c_int, [vp, _f32p, _f32p])
@@ -168,6 +172,35 @@ class OracleWorld:
 
     def step(self, dt: float = 1.0 / 60.0, vi: int = 8, pi: int = 3) -> None:
         self._fn("step")(self.h, dt, vi, pi)
+
+    def add_body(self, type_: int, f, flags: int) -> int:
+        """b2World::CreateBody between steps: f = the 9 floats of the body encoding, returns its index."""
+        return self._fn("body")(self.h, int(type_), np.ascontiguousarray(f, dtype=np.float32), int(flags))
+
+    def add_fixture(self, body: int, type_: int, shape, n: int, mat, filt) -> int:
+        """b2Body::CreateFixture between steps (one fixture record; no chains), returns its index."""
+        s = np.zeros(16, dtype=np.float32)
+        s[:len(shape)] = shape
+        self.n_fixtures += 1
+        return self._fn("fixture")(self.h, int(body), int(type_), s, int(n), np.asarray(mat, dtype=np.float32),
+                                   np.asarray(filt, dtype=np.int32))
+
+    def _destroy(self, kind: str, index: int):
+        calls = np.zeros((64, 2), dtype=np.int32)
+        n = self._fn("destroy_" + kind)(self.h, int(index), calls, 64)
+        return calls[:min(n, 64)]
+
+    def destroy_body(self, body: int) -> np.ndarray:
+        """b2World::DestroyBody; returns the destruction listener's calls {0 joint / 1 fixture, index}."""
+        return self._destroy("body", body)
+
+    def destroy_joint(self, joint: int) -> np.ndarray:
+        """b2World::DestroyJoint (no listener calls)."""
+        return self._destroy("joint", joint)
+
+    def destroy_fixture(self, fixture: int) -> np.ndarray:
+        """b2Body::DestroyFixture (no listener calls)."""
+        return self._destroy("fixture", fixture)
 
     def body_edit(self, op: int, body: int, values, wake: bool = True) -> None:
         """A b2Body state change between steps (op: the C-ABI's GB_EDIT_* code)."""

@@ -87,6 +87,33 @@ void po_body_edit(void* h, int op, int body, int wake, const float* v) { static_
 // which the caller orders by estimated cost). Used for the all-cores CPU baseline.
 void po_step_many(void** hs, int n, float dt, int vi, int pi, int steps, int threads);
 int po_body_count(void* h) { return (int)static_cast<World*>(h)->bodies.size(); }
+// b2World::DestroyBody / DestroyJoint, b2Body::DestroyFixture; the destruction listener's calls
+// {0 joint / 1 fixture, index} of the call go to calls (2 ints each, up to cap), their count returned
+static int Goodbyes(World* w, int* calls, int cap)
+{
+    const int n = (int)w->goodbyes.size();
+    for (int i = 0; i < n && i < cap; ++i) { calls[2 * i] = w->goodbyes[i].first; calls[2 * i + 1] = w->goodbyes[i].second; }
+    return n;
+}
+int po_destroy_body(void* h, int b, int* calls, int cap)
+{
+    World* w = static_cast<World*>(h);
+    w->DestroyBody(b);
+    return Goodbyes(w, calls, cap);
+}
+int po_destroy_joint(void* h, int j, int* calls, int cap)
+{
+    World* w = static_cast<World*>(h);
+    w->goodbyes.clear();
+    w->DestroyJoint(j);
+    return Goodbyes(w, calls, cap);
+}
+int po_destroy_fixture(void* h, int f, int* calls, int cap)
+{
+    World* w = static_cast<World*>(h);
+    w->DestroyFixture(f);
+    return Goodbyes(w, calls, cap);
+}
 int po_contact_count(void* h) { return static_cast<World*>(h)->contactCount; }
 
 void po_get_bodies(void* h, float* out)
@@ -95,6 +122,10 @@ void po_get_bodies(void* h, float* out)
     for (size_t i = 0; i < w->bodies.size(); ++i) {
         const Body& b = w->bodies[i];
         float* o = out + 12 * i;
+        if (!b.alive) {
+            std::memset(o, 0, 12 * sizeof(float));
+            continue;
+        }
         o[0] = b.xf.p.x; o[1] = b.xf.p.y; o[2] = b.sweep.a;
         o[3] = b.sweep.c.x; o[4] = b.sweep.c.y;
         o[5] = b.v.x; o[6] = b.v.y; o[7] = b.w;

@@ -2805,3 +2805,114 @@ void World::Step(float dt, int vi, int pi)
 }
 
 } // namespace b2o
+
+// ---------------------------------------------------------------- destruction
+namespace b2o {
+
+// b2World::DestroyJoint (Dynamics/b2World.cpp:274-362)
+void World::DestroyJoint(int jn)
+{
+    Joint& j = joints[jn];
+    const bool collideConnected = j.collideConnected;
+    if (j.prev != kNull) joints[j.prev].next = j.next;
+    if (j.next != kNull) joints[j.next].prev = j.prev;
+    if (jn == jointList) jointList = j.next;
+    const int bA = j.bodyA, bB = j.bodyB;
+    SetAwake(bA, true);
+    SetAwake(bB, true);
+    for (int side = 0; side < 2; ++side) {
+        const int body = side == 0 ? bA : bB;
+        const int e = 2 * jn + side;
+        const int pe = j.ePrev[side], ne = j.eNext[side];
+        if (pe != kNull) joints[pe >> 1].eNext[pe & 1] = ne;
+        if (ne != kNull) joints[ne >> 1].ePrev[ne & 1] = pe;
+        if (bodies[body].jointList == e) bodies[body].jointList = ne;
+        j.ePrev[side] = j.eNext[side] = kNull;
+    }
+    --jointCount;
+    if (!collideConnected)
+        for (int e = bodies[bB].contactList; e != kNull; e = contacts[e >> 1].eNext[e & 1])
+            if (EdgeOther(e) == bA) contacts[e >> 1].flags |= kCFilter;
+}
+
+// b2World::DestroyBody (Dynamics/b2World.cpp:133-212): attached joints (each announced to the
+// destruction listener first), attached contacts, fixtures with their proxies (each announced), then
+// the body leaves the body list.
+void World::DestroyBody(int bi)
+{
+    goodbyes.clear();
+    for (int e = bodies[bi].jointList; e != kNull;) {
+        const int jn = e >> 1;
+        e = joints[jn].eNext[e & 1];
+        goodbyes.push_back({0, jn});
+        DestroyJoint(jn);
+        bodies[bi].jointList = e;
+    }
+    bodies[bi].jointList = kNull;
+    for (int e = bodies[bi].contactList; e != kNull;) {
+        const int c = e >> 1;
+        e = contacts[c].eNext[e & 1];
+        Destroy(c);
+    }
+    bodies[bi].contactList = kNull;
+    for (int f = bodies[bi].fixtureList; f != kNull;) {
+        Fixture& fx = fixtures[f];
+        const int next = fx.next;
+        // a chain is one b2Fixture: announced once, at its first child
+        if (fx.shape.chain != 2) goodbyes.push_back({1, f});
+        if (fx.proxyCount > 0) {
+            bp.DestroyProxy(fx.proxyId);
+            fx.proxyId = kNull;
+            fx.proxyCount = 0;
+        }
+        fx.body = kNull;
+        fx.next = kNull;
+        bodies[bi].fixtureList = next;
+        f = next;
+    }
+    Body& b = bodies[bi];
+    if (b.prev != kNull) bodies[b.prev].next = b.next;
+    if (b.next != kNull) bodies[b.next].prev = b.prev;
+    if (bi == bodyList) bodyList = b.next;
+    --bodyCount;
+    b = Body();
+    b.alive = false;
+}
+
+// b2Body::DestroyFixture (Dynamics/b2Body.cpp:216-281): the fixture leaves the body's list, its
+// contacts are destroyed in the body's contact-list order, its proxies are destroyed and the body's
+// mass data is reset. A chain (its first child's index) goes with all of its children.
+void World::DestroyFixture(int f)
+{
+    goodbyes.clear();
+    const int bi = fixtures[f].body;
+    int last = f;
+    if (fixtures[f].shape.chain == 1)
+        while (last + 1 < (int)fixtures.size() && fixtures[last + 1].body == bi && fixtures[last + 1].shape.chain == 2)
+            ++last;
+    auto mine = [&](int id) { return id >= f && id <= last; };
+    // unlink the children (consecutive in the list) from the body's fixture list
+    int* node = &bodies[bi].fixtureList;
+    while (*node != kNull && !mine(*node)) node = &fixtures[*node].next;
+    int after = *node;
+    while (after != kNull && mine(after)) after = fixtures[after].next;
+    if (*node != kNull) *node = after;
+    for (int e = bodies[bi].contactList; e != kNull;) {
+        const int c = e >> 1;
+        e = contacts[c].eNext[e & 1];
+        if (mine(contacts[c].fA) || mine(contacts[c].fB)) Destroy(c);
+    }
+    for (int id = f; id <= last; ++id) {
+        Fixture& fx = fixtures[id];
+        if ((bodies[bi].flags & kBActive) && fx.proxyCount > 0) {
+            bp.DestroyProxy(fx.proxyId);
+        }
+        fx.proxyId = kNull;
+        fx.proxyCount = 0;
+        fx.body = kNull;
+        fx.next = kNull;
+    }
+    ResetMassData(bi);
+}
+
+} // namespace b2o

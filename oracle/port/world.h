@@ -27,6 +27,7 @@ struct Body {
     int fixtureList = kNull;
     int contactList = kNull; // edge id: contact * 2 + side
     int jointList = kNull;   // edge id: joint * 2 + side
+    bool alive = true;       // false once destroyed (its dump is zeros)
     bool IsAwake() const { return (flags & kBAwake) != 0; }
 };
 
@@ -140,6 +141,11 @@ struct World {
     std::vector<Position> positions;
     std::vector<Velocity> velocities;
 
+    // destruction listener calls of the last Destroy* call: {0 joint / 1 fixture, index}
+    std::vector<std::pair<int, int>> goodbyes;
+    void DestroyBody(int b);
+    void DestroyJoint(int j);
+    void DestroyFixture(int f);
     int CreateBody(int type, const float* f, int flags);
     int CreateFixture(int body, const Shape& shape, float density, float friction, float restitution,
                       int category, int mask, int group, bool sensor);

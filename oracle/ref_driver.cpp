@@ -27,13 +27,39 @@ using namespace box2dref;
 
 namespace {
 
+struct RefWorld;
+
+// b2DestructionListener recording its calls as {0 joint / 1 fixture, creation index}
+struct Goodbye : public b2DestructionListener {
+    RefWorld* owner = nullptr;
+    std::vector<int> calls;
+    void SayGoodbye(b2Joint* joint) override;
+    void SayGoodbye(b2Fixture* fixture) override;
+};
+
 struct RefWorld {
     b2World world;
-    std::vector<b2Body*> bodies;      // creation order
-    std::vector<b2Fixture*> fixtures; // creation order
-    std::vector<b2Joint*> joints;
-    explicit RefWorld(const b2Vec2& g) : world(g) {}
+    std::vector<b2Body*> bodies;      // creation order; null once destroyed
+    std::vector<b2Fixture*> fixtures; // creation order (a chain's children share one); null once destroyed
+    std::vector<b2Joint*> joints;     // creation order; null once destroyed
+    Goodbye goodbye;
+    explicit RefWorld(const b2Vec2& g) : world(g)
+    {
+        goodbye.owner = this;
+        world.SetDestructionListener(&goodbye);
+    }
 };
+
+void Goodbye::SayGoodbye(b2Joint* joint)
+{
+    for (size_t i = 0; i < owner->joints.size(); ++i)
+        if (owner->joints[i] == joint) { calls.push_back(0); calls.push_back((int)i); }
+}
+void Goodbye::SayGoodbye(b2Fixture* fixture)
+{
+    calls.push_back(1);
+    calls.push_back((int)(intptr_t)fixture->GetUserData() - 1);
+}
 
 int fixture_index(const b2Fixture* f) { return (int)(intptr_t)f->GetUserData() - 1; }
 int body_index(const b2Body* b) { return (int)(intptr_t)b->GetUserData() - 1; }
@@ -331,6 +357,56 @@ void rw_body_edit(void* h, int op, int body, int wake, const float* v)
 }
 
 int rw_body_count(void* h) { return (int)static_cast<RefWorld*>(h)->bodies.size(); }
+
+// Forget every pointer a destruction made dangling: joints and fixtures that are no longer attached
+// to a live body, after a DestroyBody / DestroyJoint / DestroyFixture call.
+static void ForgetDestroyed(RefWorld* w, b2Body* gone)
+{
+    for (size_t i = 0; i < w->bodies.size(); ++i)
+        if (w->bodies[i] == gone) w->bodies[i] = nullptr;
+    std::vector<b2Joint*> live;
+    for (b2Joint* j = w->world.GetJointList(); j; j = j->GetNext()) live.push_back(j);
+    for (b2Joint*& j : w->joints)
+        if (j && std::find(live.begin(), live.end(), j) == live.end()) j = nullptr;
+    std::vector<b2Fixture*> liveF;
+    for (b2Body* b = w->world.GetBodyList(); b; b = b->GetNext())
+        for (b2Fixture* f = b->GetFixtureList(); f; f = f->GetNext()) liveF.push_back(f);
+    for (b2Fixture*& f : w->fixtures)
+        if (f && std::find(liveF.begin(), liveF.end(), f) == liveF.end()) f = nullptr;
+}
+static int TakeGoodbyes(RefWorld* w, int* calls, int cap)
+{
+    const int n = (int)w->goodbye.calls.size() / 2;
+    for (int i = 0; i < 2 * n && i < 2 * cap; ++i) calls[i] = w->goodbye.calls[i];
+    w->goodbye.calls.clear();
+    return n;
+}
+int rw_destroy_body(void* h, int b, int* calls, int cap)
+{
+    RefWorld* w = static_cast<RefWorld*>(h);
+    b2Body* body = w->bodies[b];
+    w->goodbye.calls.clear();
+    w->world.DestroyBody(body);
+    ForgetDestroyed(w, body);
+    return TakeGoodbyes(w, calls, cap);
+}
+int rw_destroy_joint(void* h, int j, int* calls, int cap)
+{
+    RefWorld* w = static_cast<RefWorld*>(h);
+    w->goodbye.calls.clear();
+    w->world.DestroyJoint(w->joints[j]);
+    ForgetDestroyed(w, nullptr);
+    return TakeGoodbyes(w, calls, cap);
+}
+int rw_destroy_fixture(void* h, int f, int* calls, int cap)
+{
+    RefWorld* w = static_cast<RefWorld*>(h);
+    w->goodbye.calls.clear();
+    b2Fixture* fx = w->fixtures[f];
+    fx->GetBody()->DestroyFixture(fx);
+    ForgetDestroyed(w, nullptr);
+    return TakeGoodbyes(w, calls, cap);
+}
 int rw_contact_count(void* h) { return static_cast<RefWorld*>(h)->world.GetContactCount(); }
 
 // Per body (creation order), 12 floats: xf.p.x, xf.p.y, sweep.a, sweep.c.x, sweep.c.y, v.x, v.y, w,
@@ -341,6 +417,10 @@ void rw_get_bodies(void* h, float* out)
     for (size_t i = 0; i < w->bodies.size(); ++i) {
         const b2Body* b = w->bodies[i];
         float* o = out + 12 * i;
+        if (!b) {
+            std::memset(o, 0, 12 * sizeof(float));
+            continue;
+        }
         o[0] = b->m_xf.p.x; o[1] = b->m_xf.p.y; o[2] = b->m_sweep.a;
         o[3] = b->m_sweep.c.x; o[4] = b->m_sweep.c.y;
         o[5] = b->m_linearVelocity.x; o[6] = b->m_linearVelocity.y; o[7] = b->m_angularVelocity;
@@ -424,7 +504,7 @@ void rw_get_proxies(void* h, int* proxyIds, float* fat)
     const b2BroadPhase& bp = w->world.m_contactManager.m_broadPhase;
     for (size_t i = 0; i < w->fixtures.size(); ++i) {
         const b2Fixture* f = w->fixtures[i];
-        int id = f->m_proxyCount > 0 ? f->m_proxies[0].proxyId : -1;
+        int id = f && f->m_proxyCount > 0 ? f->m_proxies[0].proxyId : -1;
         proxyIds[i] = id;
         if (id >= 0) {
             const b2AABB& a = bp.GetFatAABB(id);

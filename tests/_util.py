@@ -98,3 +98,48 @@ def edit_script():
               (SET_AWAKE, 27, (1.0,), True), (APPLY_ANGULAR_IMPULSE, 28, (3.0,), True)],
         310: [(SET_TRANSFORM, kin, (15.0, 3.0, 0.2), True), (SET_LINEAR_VELOCITY, 40, (0.0, 0.0), True)],
     }
+
+
+def destroy_script():
+    """{step: [op]} applied before that step to scenes.destroy_mix: every kind of destruction, and new
+    bodies created after destructions (their proxies take the freed tree nodes). Ops: ("body", i),
+    ("joint", i), ("fixture", i) destroy; ("add", type, f9, fixtures) creates a body whose fixtures
+    are (type, shape, n, density) records."""
+    box = (3, [0.4, 0.4], 2, 1.0)
+    circle = (0, [0.0, 0.0, 0.3], 0, 1.0)
+    tri = (2, [-0.4, -0.3, 0.4, -0.3, 0.0, 0.45], 3, 2.0)
+
+    def add(x, y, *fixtures):
+        return ("add", 2, [x, y, 0.1, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0], list(fixtures))
+
+    return {
+        30: [("body", 12)],                      # a pyramid box in the second row, touching four
+        45: [("joint", 3)],                      # the chain splits
+        60: [("fixture", 48)],                   # the two-fixture body loses its circle
+        75: [add(-2.0, 14.0, box), add(0.0, 15.0, circle), add(2.0, 14.0, tri)],
+        90: [("body", 43)],                      # a link with two joints: goodbyes, then its fixture
+        100: [("joint", 8)],                     # the tied pair may now collide
+        110: [("body", 37)],                     # the static ledge
+        130: [("body", 5), ("body", 20), ("body", 51), add(-4.0, 12.0, box, circle), add(4.0, 12.0, tri),
+              add(0.0, 18.0, circle), add(1.0, 20.0, box)],
+        150: [("body", 60), ("fixture", 64)],
+    }
+
+
+def apply_ops(world, ops, w: int = 0):
+    """Applies destroy_script() ops to an oracle world or a device world (same method names); returns
+    the destruction listener's calls of the ops as (kind, index), in order."""
+    calls = []
+    for op in ops:
+        if op[0] == "add":
+            b = world.add_body(op[1], op[2], 1 | 2 | 16) if w == 0 else world.add_body(op[1], op[2], 1 | 2 | 16, w)
+            for (t, shape, n, density) in op[3]:
+                args = (b, t, shape, n, [density, 0.4, 0.0], [1, 0xFFFF, 0, 0])
+                world.add_fixture(*args) if w == 0 else world.add_fixture(*args, w)
+        else:
+            fn = getattr(world, "destroy_" + op[0])
+            got = fn(op[1]) if w == 0 else fn(op[1], w)
+            # the destruction listener's calls {kind 0 joint / 1 fixture, index}; a device world also
+            # reports EndContact calls (kind 2), which the oracles record with their other events
+            calls.extend([(int(c[0]), int(c[1])) for c in got if int(c[0]) in (0, 1)])
+    return calls

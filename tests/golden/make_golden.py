@@ -12,6 +12,9 @@ Two builds of the reference are used: ``libm`` (glibc sinf/cosf, the reference a
   drop, whose arrays would be megabytes).
 
   python tests/golden/make_golden.py --case <name>   writes one trajectory case only.
+* ``destroy_mix_<trig>.npz``: a scene changed between steps (bodies, joints and fixtures destroyed,
+  bodies created) with the per-step digests, the destruction listener's calls and the final proxy
+  ids (freed tree nodes are reused).
 * ``collide.npz``: seeded shape pairs of every supported type pair with the reference manifolds.
 * ``toi.npz``: seeded sweeps with the reference b2TimeOfImpact result.
 * ``trig.npz``: glibc sinf/cosf on seeded angles (how far the project trig is from libm).
@@ -74,6 +77,34 @@ def cases():
         # be megabytes)
         ("config2_10k", lambda: scenes.config2(10000, seed=1, allow_sleep=True), 200, []),
     ] + [(f"batch{i}", (lambda i=i: batch_world(i)), 200, [200]) for i in range(24)]
+
+
+def scripted_cases():
+    """Trajectory cases with b2World changes between steps: (name, scene factory, steps, ops by step).
+    The ops (tests/_util.py destroy_script) destroy bodies, joints and fixtures and create bodies."""
+    sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
+    from tests._util import destroy_script
+
+    return [("destroy_mix", lambda: scenes.destroy_mix(scenes.SplitMix64(5)), 200, destroy_script())]
+
+
+def run_scripted(scene, steps, script, trig):
+    """Per-step state digests, the destruction listener's calls as (step, kind, index) rows and the
+    final proxy ids and fat AABBs of the reference on a scripted case."""
+    from tests._util import apply_ops
+
+    w = oracle.OracleWorld(scene, "reference", trig)
+    digests = np.zeros((steps, 32), dtype=np.uint8)
+    calls = []
+    for s in range(1, steps + 1):
+        if s in script:
+            calls += [(s, k, i) for (k, i) in apply_ops(w, script[s])]
+        w.step(DT, VI, PI)
+        b = w.bodies()
+        ci, cf = w.contacts()
+        digests[s - 1] = np.frombuffer(state_digest(b, ci, cf), dtype=np.uint8)
+    ids, fat = w.proxies()
+    return digests, np.array(calls, np.int32).reshape(-1, 3), ids, fat
 
 
 def chains_with_load():
@@ -244,6 +275,14 @@ def main():
         print("done")
         return
     only = sys.argv[sys.argv.index("--case") + 1] if "--case" in sys.argv else None
+    for name, make, steps, script in scripted_cases():
+        if only and name != only:
+            continue
+        for trig in ("libm", "project"):
+            digests, calls, ids, fat = run_scripted(make(), steps, script, trig)
+            np.savez_compressed(os.path.join(HERE, f"{name}_{trig}.npz"), digests=digests, goodbyes=calls,
+                                proxy_ids=ids, proxy_fat=fat, steps=np.int32(steps))
+        print("wrote", name)
     for name, make, steps, cps in cases():
         if only and name != only:
             continue

@@ -92,3 +92,29 @@ def test_project_trig_nearly_correctly_rounded():
         s, c = oracle.sincosf("port", "project", float(v))
         bad += (np.float32(s) != ref_s[i]) + (np.float32(c) != ref_c[i])
     assert bad <= 2
+
+
+@pytest.mark.parametrize("trig", ["project", "libm"])
+def test_port_destroy_case_matches_reference(trig):
+    """Bodies, joints and fixtures destroyed and bodies created between steps: per-step state, the
+    destruction listener's calls and the final proxy ids (freed tree nodes reused) as the reference."""
+    import platform
+
+    from box2dpp_gb300 import scenes
+    from tests._util import apply_ops, destroy_script, digest
+
+    g = golden(f"destroy_mix_{trig}")
+    w = oracle.OracleWorld(scenes.destroy_mix(scenes.SplitMix64(5)), "port", trig)
+    script = destroy_script()
+    calls = []
+    for s in range(1, int(g["steps"]) + 1):
+        if s in script:
+            calls += [(s, k, i) for (k, i) in apply_ops(w, script[s])]
+        w.step()
+        if not np.array_equal(digest(w.bodies(), *w.contacts()), g["digests"][s - 1]):
+            if trig == "libm" and platform.machine() != "x86_64":
+                pytest.skip("libm trig differs on this machine")
+            raise AssertionError(f"first divergence at step {s}")
+    assert np.array_equal(np.array(calls, np.int32).reshape(-1, 3), g["goodbyes"])
+    ids, fat = w.proxies()
+    assert np.array_equal(ids, g["proxy_ids"])
