@@ -32,7 +32,7 @@ EXPORTS = [
     "gb_world_set_contact_log", "gb_world_read_contact_log", "gb_world_contact_stats", "gb_world_set_events",
     "gb_world_read_events", "gb_world_query_aabb", "gb_world_raycast", "gb_create_joints",
     "gb_world_stage_times", "gb_body_edits", "gb_world_set_limits", "gb_destroy_body", "gb_destroy_joint",
-    "gb_destroy_fixture",
+    "gb_destroy_fixture", "gb_world_raycast_all", "gb_world_get_profile",
 ]
 
 
@@ -113,6 +113,8 @@ def load(build_if_missing: bool = True):
         "gb_collide_noalloc": [i, _i32, _f32, _i32, _f32, _i32, _f32, _i32, _f32, _i32, _f32],
         "gb_world_set_solver": [vp, i, f, i],
         "gb_world_set_limits": [vp, i, i],
+        "gb_world_raycast_all": [vp, i, _f32, _i32, _f32, i, C.POINTER(C.c_int)],
+        "gb_world_get_profile": [vp, i, _f32],
         "gb_destroy_body": [vp, i, i, _i32, i, C.POINTER(C.c_int)],
         "gb_destroy_joint": [vp, i, i, _i32, i, C.POINTER(C.c_int)],
         "gb_destroy_fixture": [vp, i, i, _i32, i, C.POINTER(C.c_int)],

@@ -33,6 +33,8 @@ cudaError_t b2gLaunchQueryAabb(const b2g::Batch& B, int w, const float4* boxes, 
                                int* fill, int cap, cudaStream_t stream);
 cudaError_t b2gLaunchRayCast(const b2g::Batch& B, int w, const float4* rays, int n, int* fixture, float* hit,
                              cudaStream_t stream);
+cudaError_t b2gLaunchRayCastAll(const b2g::Batch& B, int w, int fixCount, float4 ray, float4* hits, int* count, int cap,
+                                cudaStream_t stream);
 cudaError_t b2gLaunchCollide(int n, const b2g::Shape* a, const float4* xa, const b2g::Shape* b, const float4* xb,
                              int4* oi, float4* of, cudaStream_t stream);
 
@@ -154,6 +156,13 @@ struct gb_world {
 };
 
 namespace {
+
+inline int __float_as_int_host(float f)
+{
+    int i;
+    std::memcpy(&i, &f, sizeof(i));
+    return i;
+}
 
 gb_status cudaErr(cudaError_t e)
 {
@@ -1556,6 +1565,71 @@ gb_status gb_world_query_aabb(gb_world* g, int w, int n, const float* aabbs, int
     cudaFree(dBoxes); cudaFree(dCounts); cudaFree(dOffsets); cudaFree(dFill);
     GB_CUDA(e);
     return *total > cap ? GB_ERR_CAPACITY : GB_OK;
+}
+
+gb_status gb_world_raycast_all(gb_world* g, int w, const float* ray, int* fixtures, float* hits, int cap, int* n)
+{
+    if (!g || w < 0 || w >= (int)g->worlds.size() || !ray || !n || cap < 0 || (cap > 0 && (!fixtures || !hits)))
+        return GB_ERR_INVALID;
+    gb_status s = Upload(g);
+    if (s != GB_OK) return s;
+    *n = 0;
+    const int nf = g->desc[w].fixCount;
+    if (nf == 0) return GB_OK;
+    float4* dHits = nullptr;
+    int* dCount = nullptr;
+    cudaError_t e = cudaMalloc(&dHits, nf * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc(&dCount, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(dCount, 0, sizeof(int), g->stream);
+    if (e == cudaSuccess)
+        e = b2gLaunchRayCastAll(g->batch, w, nf, make_float4(ray[0], ray[1], ray[2], ray[3]), dHits, dCount, nf,
+                                g->stream);
+    int count = 0;
+    std::vector<float4> h;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&count, dCount, sizeof(int), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e == cudaSuccess && count > 0) {
+        h.resize(count);
+        e = cudaMemcpy(h.data(), dHits, count * sizeof(float4), cudaMemcpyDeviceToHost);
+    }
+    cudaFree(dHits);
+    cudaFree(dCount);
+    GB_CUDA(e);
+    // fixture order: the order the reference's callbacks would see is its tree's, which is not kept
+    std::sort(h.begin(), h.end(), [](const float4& a, const float4& b) { return __float_as_int_host(a.x) < __float_as_int_host(b.x); });
+    const Vec2 p1 = V(ray[0], ray[1]), p2 = V(ray[2], ray[3]);
+    for (int k = 0; k < count && k < cap; ++k) {
+        const float f = h[k].y;
+        const Vec2 pt = (1.0f - f) * p1 + f * p2;
+        fixtures[k] = __float_as_int_host(h[k].x);
+        hits[5 * k] = f;
+        hits[5 * k + 1] = pt.x;
+        hits[5 * k + 2] = pt.y;
+        hits[5 * k + 3] = h[k].z;
+        hits[5 * k + 4] = h[k].w;
+    }
+    *n = count;
+    return count > cap ? GB_ERR_CAPACITY : GB_OK;
+}
+
+gb_status gb_world_get_profile(gb_world* g, int w, float* ms)
+{
+    if (!g || w < 0 || w >= (int)g->worlds.size() || !ms) return GB_ERR_INVALID;
+    for (int k = 0; k < 8; ++k) ms[k] = 0.0f;
+    if (!g->onDevice) return GB_OK;
+    GB_CUDA(cudaStreamSynchronize(g->stream));
+    WorldState st;
+    GB_CUDA(cudaMemcpy(&st, g->batch.state + w, sizeof(WorldState), cudaMemcpyDeviceToHost));
+    int dev = 0, khz = 0;
+    GB_CUDA(cudaGetDevice(&dev));
+    GB_CUDA(cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, dev));
+    const double perMs = khz > 0 ? (double)khz : 1.0;
+    auto c = [&](int k) { return (double)st.cyc[k]; };
+    // b2Profile (Box2D/Dynamics/b2TimeStep.h:27-37): step, collide, solve, solveInit, solveVelocity,
+    // solvePosition, broadphase (fixture sync and pair finding after the islands), solveTOI
+    const double v[8] = {c(7), c(0) + c(1), c(2) + c(3) + c(4) + c(5), c(8), c(9), c(11), c(4) + c(5), c(6)};
+    for (int k = 0; k < 8; ++k) ms[k] = (float)(v[k] / perMs);
+    return GB_OK;
 }
 
 gb_status gb_world_raycast(gb_world* g, int w, int n, const float* rays, int* fixture, float* hit)

@@ -105,7 +105,10 @@ __global__ void RayCastKernel(Batch B, int w, const float4* rays, int n, int* fi
     float bestF = 0.0f;
     Vec2 bestN = V(0.0f, 0.0f);
     for (int f = 0; f < d.fixCount; ++f) {
-        const int body = B.fi[d.fixBase + f].x;
+        // the tree holds only fixtures with a proxy (not those of inactive or destroyed bodies)
+        const int4 fx = B.fi[d.fixBase + f];
+        if (fx.z < 0 || fx.x < 0) continue;
+        const int body = fx.x;
         const float4 x = B.xf[d.bodyBase + body];
         Xf xf;
         xf.p = V(x.x, x.y);
@@ -125,7 +128,37 @@ __global__ void RayCastKernel(Batch B, int w, const float4* rays, int n, int* fi
     hit[5 * i + 4] = bestN.y;
 }
 
+// Every fixture the segment p1 -> p2 hits (b2Fixture::RayCast with maxFraction 1), one thread per
+// fixture of the world: hits[k] = {fixture, fraction, normal.x, normal.y} appended at an atomic slot
+// (order restored by the caller), *count the number of hits (slots past cap are not written).
+__global__ void RayCastAllKernel(Batch B, int w, float4 ray, float4* hits, int* count, int cap)
+{
+    const WorldDesc d = B.desc[w];
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= d.fixCount) return;
+    const int4 fx = B.fi[d.fixBase + f];
+    if (fx.z < 0 || fx.x < 0) return;
+    const float4 x = B.xf[d.bodyBase + fx.x];
+    Xf xf;
+    xf.p = V(x.x, x.y);
+    xf.q.s = x.z;
+    xf.q.c = x.w;
+    float fr;
+    Vec2 nrm;
+    if (!RayCastShape(B.shape[d.fixBase + f], xf, V(ray.x, ray.y), V(ray.z, ray.w), 1.0f, &fr, &nrm)) return;
+    const int slot = atomicAdd(count, 1);
+    if (slot < cap) hits[slot] = make_float4(__int_as_float(f), fr, nrm.x, nrm.y);
+}
+
 } // namespace b2g
+
+cudaError_t b2gLaunchRayCastAll(const b2g::Batch& B, int w, int fixCount, float4 ray, float4* hits, int* count, int cap,
+                                cudaStream_t stream)
+{
+    if (fixCount <= 0) return cudaSuccess;
+    b2g::RayCastAllKernel<<<(fixCount + 127) / 128, 128, 0, stream>>>(B, w, ray, hits, count, cap);
+    return cudaGetLastError();
+}
 
 cudaError_t b2gLaunchQueryAabb(const b2g::Batch& B, int w, const float4* boxes, int n, const int* offsets, int* counts,
                                int* fill, int cap, cudaStream_t stream)

@@ -224,6 +224,24 @@ class World:
         _lib.check(self.lib.gb_world_raycast(self.h, w, n, rays, fixture, hit), "gb_world_raycast")
         return fixture[:n], hit[:n]
 
+    def raycast_all(self, ray, w: int = 0):
+        """Every fixture the segment hits (gb_world_raycast_all): (fixtures, hits[k] = fraction, point,
+        normal), in fixture order."""
+        nf = self.n_fixtures[w]
+        fix = np.zeros(max(nf, 1), dtype=np.int32)
+        hits = np.zeros((max(nf, 1), 5), dtype=np.float32)
+        n = C.c_int()
+        _lib.check(self.lib.gb_world_raycast_all(self.h, w, np.ascontiguousarray(ray, dtype=np.float32), fix, hits,
+                                                 nf, C.byref(n)), "gb_world_raycast_all")
+        return fix[:n.value], hits[:n.value]
+
+    def profile_ms(self, w: int = 0) -> dict:
+        """b2World::GetProfile of the last step (gb_world_get_profile), milliseconds."""
+        out = np.zeros(8, dtype=np.float32)
+        _lib.check(self.lib.gb_world_get_profile(self.h, w, out), "gb_world_get_profile")
+        keys = ["step", "collide", "solve", "solveInit", "solveVelocity", "solvePosition", "broadphase", "solveTOI"]
+        return dict(zip(keys, map(float, out)))
+
     def set_stream(self, stream_handle: int) -> None:
         _lib.check(self.lib.gb_world_set_stream(self.h, C.c_void_p(stream_handle)), "gb_world_set_stream")
 

@@ -247,6 +247,18 @@ gb_status gb_world_read_events(gb_world* world, int w, int* records, float* impu
 gb_status gb_world_query_aabb(gb_world* world, int w, int n, const float* aabbs, int* offsets, int* fixtures, int cap,
                              int* total);
 gb_status gb_world_raycast(gb_world* world, int w, int n, const float* rays, int* fixture, float* hit);
+/* Every fixture the segment ray[4] = p1.x, p1.y, p2.x, p2.y hits (b2Fixture::RayCast with maxFraction
+ * 1, Box2D/Dynamics/b2Fixture.h:308-311), the material b2World::RayCast's callback loop needs
+ * (Box2D/Dynamics/b2World.cpp:1021-1035): fixtures[k] and hits[5 k] = fraction, point.x, point.y,
+ * normal.x, normal.y, in fixture order (the reference's order is its tree's), at most cap; *n receives
+ * the number of hits, GB_ERR_CAPACITY when it exceeds cap. A caller replays its callback over them,
+ * skipping hits beyond the fraction the callback has clipped the ray to. */
+gb_status gb_world_raycast_all(gb_world* world, int w, const float* ray, int* fixtures, float* hits, int cap, int* n);
+/* b2World::GetProfile (Box2D/Dynamics/b2World.h:196, b2Profile in b2TimeStep.h:27-37) of world w's
+ * last step in milliseconds at the GPU's SM clock: ms[8] = step, collide, solve, solveInit,
+ * solveVelocity, solvePosition, broadphase, solveTOI (the flat narrowphase and time-of-impact
+ * pre-passes over all worlds are not in any world's figure). */
+gb_status gb_world_get_profile(gb_world* world, int w, float* ms);
 
 /* Counts (b2World::GetBodyCount, GetContactCount, GetProxyCount: b2World.h:160-170). */
 gb_status gb_world_counts(gb_world* world, int w, int* bodies, int* fixtures, int* contacts, int* joints);

@@ -10,13 +10,23 @@
 //    once (the getters of that step are then host reads);
 //  - the world settings (SetAllowSleeping, SetWarmStarting, SetContinuousPhysics, SetSubStepping)
 //    take effect when the device world is created, at the first Step;
-//  - bodies, fixtures and joints are created but never destroyed (the reference's Destroy* calls
-//    are not part of this API);
+//  - DestroyBody, DestroyJoint and DestroyFixture run between steps with the reference's order of
+//    effects; the destroyed objects stay allocated (their pointers stay valid, but dead) until the
+//    world is destroyed, and the destruction listener and the contact listener's EndContact are
+//    called during the Destroy call, as in the reference;
+//  - QueryAABB and RayCast call their callbacks in fixture-creation order (the reference's order is
+//    its broadphase tree's, which the device does not keep), with the reference's protocol: a
+//    QueryAABB callback that returns false ends the query; a RayCast callback's return value ignores
+//    the fixture (-1), ends the cast (0) or clips the ray (a fraction); the results of callbacks that
+//    do not depend on the order (closest hit, all hits) are the reference's;
+//  - b2Contact::GetWorldManifold computes on the host: bit-exact with the reference when the caller is
+//    compiled without floating-point contraction (-ffp-contract=off);
 //  - b2ContactListener calls are recorded on the device during the step, in the reference's order,
 //    and made after it: BeginContact, EndContact, PreSolve (a notification: the contact can no longer
 //    be changed for this step) and PostSolve with the solver's impulses.
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <map>
@@ -208,6 +218,12 @@ struct b2FixtureDef {
 
 class b2World;
 class b2Body;
+class b2Joint;
+
+// b2AABB (Box2D/Collision/b2Collision.h:206-247)
+struct b2AABB {
+    b2Vec2 lowerBound, upperBound;
+};
 
 class b2Fixture {
 public:
@@ -219,13 +235,17 @@ public:
     bool IsSensor() const { return m_def.isSensor; }
     void* GetUserData() const { return m_def.userData; }
     b2Shape::Type GetType() const { return m_type; }
+    float GetRadius() const { return m_radius; }  // the shape's m_radius
 
 private:
     friend class b2World;
+    friend class b2Body;
     b2Body* m_body = nullptr;
     int m_index = -1;
     b2FixtureDef m_def;
     b2Shape::Type m_type = b2Shape::e_circle;
+    float m_radius = 0.0f;
+    bool m_alive = true;
 };
 
 class b2Body {
@@ -238,6 +258,10 @@ public:
         d.density = density;
         return CreateFixture(&d);
     }
+    // b2Body::DestroyFixture (Box2D/Dynamics/b2Body.cpp:216-281)
+    void DestroyFixture(b2Fixture* fixture);
+    // the next body of the world's body list (newest first), as b2Body::GetNext
+    b2Body* GetNext() const;
     b2BodyType GetType() const { return m_type; }
     int GetIndex() const { return m_index; }
     b2World* GetWorld() const { return m_world; }
@@ -277,6 +301,7 @@ private:
     int m_index = -1;
     b2BodyType m_type = b2_staticBody;
     void* m_userData = nullptr;
+    bool m_alive = true;
 };
 
 struct b2RevoluteJointDef {
@@ -406,6 +431,7 @@ protected:
     int m_index = -1;
     b2Body *m_a = nullptr, *m_b = nullptr;
     b2World* m_world = nullptr;
+    bool m_alive = true;
 };
 
 // b2MouseJoint (Box2D/Dynamics/Joints/b2MouseJoint.h:63-124): what CreateJoint returns for a
@@ -433,6 +459,73 @@ struct b2Manifold {
     int pointCount = 0;
 };
 
+// b2WorldManifold (Box2D/Collision/b2Collision.h:115-126) and its Initialize (b2Collision.cpp:25-66):
+// the world normal (A to B), contact points (midway between the surfaces) and separations.
+struct b2WorldManifold {
+    b2Vec2 normal;
+    b2Vec2 points[2];
+    float separations[2] = {0.0f, 0.0f};
+    void Initialize(const b2Manifold* manifold, const b2Transform& xfA, float radiusA, const b2Transform& xfB,
+                    float radiusB)
+    {
+        if (manifold->pointCount == 0) return;
+        auto mul = [](const b2Transform& t, const b2Vec2& v) {
+            return b2Vec2((t.q.c * v.x - t.q.s * v.y) + t.p.x, (t.q.s * v.x + t.q.c * v.y) + t.p.y);
+        };
+        auto rot = [](const b2Transform& t, const b2Vec2& v) {
+            return b2Vec2(t.q.c * v.x - t.q.s * v.y, t.q.s * v.x + t.q.c * v.y);
+        };
+        auto dot = [](const b2Vec2& a, const b2Vec2& b) { return a.x * b.x + a.y * b.y; };
+        switch (manifold->type) {
+        case b2Manifold::e_circles: {
+            normal = b2Vec2(1.0f, 0.0f);
+            const b2Vec2 pointA = mul(xfA, manifold->localPoint);
+            const b2Vec2 pointB = mul(xfB, manifold->points[0].localPoint);
+            const b2Vec2 d(pointA.x - pointB.x, pointA.y - pointB.y);
+            const float eps = 1.19209289550781250e-7f;  // FLT_EPSILON
+            if (dot(d, d) > eps * eps) {
+                normal = b2Vec2(pointB.x - pointA.x, pointB.y - pointA.y);
+                const float length = std::sqrt(normal.x * normal.x + normal.y * normal.y);
+                if (length >= eps) {
+                    const float inv = 1.0f / length;
+                    normal.x *= inv;
+                    normal.y *= inv;
+                }
+            }
+            const b2Vec2 cA(pointA.x + radiusA * normal.x, pointA.y + radiusA * normal.y);
+            const b2Vec2 cB(pointB.x - radiusB * normal.x, pointB.y - radiusB * normal.y);
+            points[0] = b2Vec2(0.5f * (cA.x + cB.x), 0.5f * (cA.y + cB.y));
+            separations[0] = dot(b2Vec2(cB.x - cA.x, cB.y - cA.y), normal);
+        } break;
+        case b2Manifold::e_faceA: {
+            normal = rot(xfA, manifold->localNormal);
+            const b2Vec2 planePoint = mul(xfA, manifold->localPoint);
+            for (int i = 0; i < manifold->pointCount; ++i) {
+                const b2Vec2 clip = mul(xfB, manifold->points[i].localPoint);
+                const float s = radiusA - dot(b2Vec2(clip.x - planePoint.x, clip.y - planePoint.y), normal);
+                const b2Vec2 cA(clip.x + s * normal.x, clip.y + s * normal.y);
+                const b2Vec2 cB(clip.x - radiusB * normal.x, clip.y - radiusB * normal.y);
+                points[i] = b2Vec2(0.5f * (cA.x + cB.x), 0.5f * (cA.y + cB.y));
+                separations[i] = dot(b2Vec2(cB.x - cA.x, cB.y - cA.y), normal);
+            }
+        } break;
+        case b2Manifold::e_faceB: {
+            normal = rot(xfB, manifold->localNormal);
+            const b2Vec2 planePoint = mul(xfB, manifold->localPoint);
+            for (int i = 0; i < manifold->pointCount; ++i) {
+                const b2Vec2 clip = mul(xfA, manifold->points[i].localPoint);
+                const float s = radiusB - dot(b2Vec2(clip.x - planePoint.x, clip.y - planePoint.y), normal);
+                const b2Vec2 cB(clip.x + s * normal.x, clip.y + s * normal.y);
+                const b2Vec2 cA(clip.x - radiusA * normal.x, clip.y - radiusA * normal.y);
+                points[i] = b2Vec2(0.5f * (cA.x + cB.x), 0.5f * (cA.y + cB.y));
+                separations[i] = dot(b2Vec2(cA.x - cB.x, cA.y - cB.y), normal);
+            }
+            normal = b2Vec2(-normal.x, -normal.y);
+        } break;
+        }
+    }
+};
+
 class b2Contact {
 public:
     b2Fixture* GetFixtureA() const { return m_a; }
@@ -442,6 +535,8 @@ public:
     bool IsTouching() const { return (m_flags & 2) != 0; }
     bool IsEnabled() const { return (m_flags & 4) != 0; }
     const b2Manifold* GetManifold() const { return &m_manifold; }
+    // b2Contact::GetWorldManifold (Box2D/Dynamics/Contacts/b2Contact.h:223-231)
+    void GetWorldManifold(b2WorldManifold* worldManifold) const;
 
 private:
     friend class b2World;
@@ -467,6 +562,30 @@ public:
     virtual void PostSolve(b2Contact*, const b2ContactImpulse*) {}
 };
 
+// b2DestructionListener, b2QueryCallback, b2RayCastCallback (Box2D/Dynamics/b2WorldCallbacks.h:38-155)
+class b2DestructionListener {
+public:
+    virtual ~b2DestructionListener() = default;
+    virtual void SayGoodbye(b2Joint* joint) = 0;
+    virtual void SayGoodbye(b2Fixture* fixture) = 0;
+};
+class b2QueryCallback {
+public:
+    virtual ~b2QueryCallback() = default;
+    virtual bool ReportFixture(b2Fixture* fixture) = 0;
+};
+class b2RayCastCallback {
+public:
+    virtual ~b2RayCastCallback() = default;
+    virtual float ReportFixture(b2Fixture* fixture, const b2Vec2& point, const b2Vec2& normal, float fraction) = 0;
+};
+
+// b2Profile (Box2D/Dynamics/b2TimeStep.h:27-37), milliseconds of the device step
+struct b2Profile {
+    float step = 0, collide = 0, solve = 0, solveInit = 0, solveVelocity = 0, solvePosition = 0, broadphase = 0,
+          solveTOI = 0;
+};
+
 class b2World {
 public:
     explicit b2World(const b2Vec2& gravity) : m_gravity(gravity) {}
@@ -484,6 +603,99 @@ public:
     bool GetAllowSleeping() const { return m_def.allow_sleep != 0; }
     b2Vec2 GetGravity() const { return m_gravity; }
     void SetContactListener(b2ContactListener* listener) { m_listener = listener; }
+    void SetDestructionListener(b2DestructionListener* listener) { m_destruction = listener; }
+
+    // b2World::DestroyBody (Box2D/Dynamics/b2World.cpp:133-212)
+    void DestroyBody(b2Body* body)
+    {
+        if (!m_h || !body || !body->m_alive || body->m_world != this) return;
+        std::vector<int> calls;
+        if (Destroy(gb_destroy_body, body->m_index, calls) != GB_OK) return;
+        body->m_alive = false;
+        Announce(calls);
+        for (auto& f : m_fixtures)
+            if (f->m_body == body) f->m_alive = false;
+    }
+    // b2World::DestroyJoint (Box2D/Dynamics/b2World.cpp:274-362)
+    void DestroyJoint(b2Joint* joint)
+    {
+        if (!m_h || !joint || !joint->m_alive || joint->m_world != this) return;
+        std::vector<int> calls;
+        if (Destroy(gb_destroy_joint, joint->m_index, calls) != GB_OK) return;
+        joint->m_alive = false;
+    }
+    void DestroyFixture(b2Fixture* fixture)
+    {
+        if (!m_h || !fixture || !fixture->m_alive) return;
+        std::vector<int> calls;
+        if (Destroy(gb_destroy_fixture, fixture->m_index, calls) != GB_OK) return;
+        fixture->m_alive = false;
+        Announce(calls);
+    }
+
+    // b2World::QueryAABB (Box2D/Dynamics/b2World.cpp:988-994): each fixture proxy whose fat AABB
+    // overlaps the box, until the callback returns false
+    void QueryAABB(b2QueryCallback* callback, const b2AABB& aabb)
+    {
+        if (!Handle() || !callback) return;
+        const float box[4] = {aabb.lowerBound.x, aabb.lowerBound.y, aabb.upperBound.x, aabb.upperBound.y};
+        int offsets[2] = {0, 0}, total = 0;
+        gb_world_query_aabb(m_h, 0, 1, box, offsets, nullptr, 0, &total);
+        std::vector<int> ids((size_t)(total > 0 ? total : 1));
+        if (total > 0 && gb_world_query_aabb(m_h, 0, 1, box, offsets, ids.data(), total, &total) != GB_OK) return;
+        for (int k = 0; k < total; ++k)
+            if (!callback->ReportFixture(m_fixtureOfId[ids[k]].first)) return;
+    }
+    // b2World::RayCast (Box2D/Dynamics/b2World.cpp:1021-1035) and b2DynamicTree::RayCast's use of the
+    // callback's value (b2DynamicTree.h:218-280)
+    void RayCast(b2RayCastCallback* callback, const b2Vec2& point1, const b2Vec2& point2)
+    {
+        if (!Handle() || !callback) return;
+        const float ray[4] = {point1.x, point1.y, point2.x, point2.y};
+        const int cap = (int)m_fixtureOfId.size();
+        std::vector<int> ids((size_t)(cap > 0 ? cap : 1));
+        std::vector<float> hits(5 * (size_t)(cap > 0 ? cap : 1));
+        int n = 0;
+        if (gb_world_raycast_all(m_h, 0, ray, ids.data(), hits.data(), cap, &n) != GB_OK) return;
+        float maxFraction = 1.0f;
+        for (int k = 0; k < n; ++k) {
+            const float* h = &hits[5 * (size_t)k];
+            if (h[0] > maxFraction) continue;  // beyond the clipped ray: the fixture reports no hit
+            const float value = callback->ReportFixture(m_fixtureOfId[ids[k]].first, b2Vec2(h[1], h[2]),
+                                                        b2Vec2(h[3], h[4]), h[0]);
+            if (value == 0.0f) return;
+            if (value > 0.0f) maxFraction = value;
+        }
+    }
+
+    // b2World::GetBodyList (newest first, as the reference's list)
+    b2Body* GetBodyList() const { return PreviousAlive(m_bodies.size()); }
+    b2Body* PreviousAlive(size_t index) const
+    {
+        for (size_t i = index; i-- > 0;)
+            if (m_bodies[i]->m_alive) return m_bodies[i].get();
+        return nullptr;
+    }
+    // b2World::GetProxyCount (Box2D/Dynamics/b2World.cpp:1241): broadphase proxies (one per chain child)
+    int GetProxyCount()
+    {
+        if (!Handle() || m_fixtureOfId.empty()) return 0;
+        std::vector<int> ids(m_fixtureOfId.size());
+        if (gb_get_proxies(m_h, 0, ids.data(), nullptr) != GB_OK) return 0;
+        int n = 0;
+        for (int id : ids) n += id >= 0 ? 1 : 0;
+        return n;
+    }
+    // b2World::GetProfile (Box2D/Dynamics/b2World.h:196) of the last step
+    const b2Profile& GetProfile()
+    {
+        float ms[8] = {0};
+        if (m_h) gb_world_get_profile(m_h, 0, ms);
+        m_profile.step = ms[0]; m_profile.collide = ms[1]; m_profile.solve = ms[2]; m_profile.solveInit = ms[3];
+        m_profile.solveVelocity = ms[4]; m_profile.solvePosition = ms[5]; m_profile.broadphase = ms[6];
+        m_profile.solveTOI = ms[7];
+        return m_profile;
+    }
 
     b2Body* CreateBody(const b2BodyDef* def)
     {
@@ -612,8 +824,18 @@ public:
         if (m_listener) Report();
     }
 
-    int GetBodyCount() const { return (int)m_bodies.size(); }
-    int GetJointCount() const { return (int)m_joints.size(); }
+    int GetBodyCount() const
+    {
+        int n = 0;
+        for (const auto& b : m_bodies) n += b->m_alive ? 1 : 0;
+        return n;
+    }
+    int GetJointCount() const
+    {
+        int n = 0;
+        for (const auto& j : m_joints) n += j->m_alive ? 1 : 0;
+        return n;
+    }
     int GetContactCount()
     {
         int b = 0, f = 0, c = 0, j = 0;
@@ -669,6 +891,7 @@ public:
         fx->m_def = *def;
         fx->m_def.shape = nullptr;
         fx->m_type = def->shape->GetType();
+        fx->m_radius = def->shape->m_radius;
         for (int k = 0; k < children; ++k) m_fixtureOfId.push_back({fx.get(), k});
         m_fixtures.push_back(std::move(fx));
         m_stale = true;
@@ -688,6 +911,37 @@ public:
     }
 
 private:
+    // one gb_destroy_* call; its listener calls in calls (3 ints each)
+    gb_status Destroy(gb_status (*fn)(gb_world*, int, int, int*, int, int*), int index, std::vector<int>& calls)
+    {
+        if (m_listener) ReadContacts();  // the contacts an EndContact may name
+        // room for every call the destruction can make: each joint, contact and fixture of the world
+        const int cap = GetContactCount() + (int)m_joints.size() + (int)m_fixtureOfId.size() + 1;
+        int n = 0;
+        calls.assign(3 * (size_t)cap, 0);
+        gb_status s = fn(m_h, 0, index, calls.data(), cap, &n);
+        calls.resize(3 * (size_t)(s == GB_OK ? std::min(n, cap) : 0));
+        m_stale = true;
+        return s;
+    }
+    void Announce(const std::vector<int>& calls)
+    {
+        for (size_t k = 0; k + 2 < calls.size(); k += 3) {
+            const int kind = calls[k], a = calls[k + 1], b = calls[k + 2];
+            if (kind == 0) {
+                for (auto& j : m_joints)
+                    if (j->m_index == a) {
+                        j->m_alive = false;
+                        if (m_destruction) m_destruction->SayGoodbye(j.get());
+                    }
+            } else if (kind == 1) {
+                if (m_destruction) m_destruction->SayGoodbye(m_fixtureOfId[a].first);
+            } else if (m_listener) {
+                for (auto& c : m_contacts)
+                    if (c->m_idA == a && c->m_idB == b) m_listener->EndContact(c.get());
+            }
+        }
+    }
     b2Joint* AddJoint(int type, b2Body* a, b2Body* b, const float* f, int flags,
                       std::unique_ptr<b2Joint> j = nullptr)
     {
@@ -786,6 +1040,8 @@ private:
     gb_world_def m_def{0.0f, 0.0f, 1, 1, 1, 0};
     gb_world* m_h = nullptr;
     b2ContactListener* m_listener = nullptr;
+    b2DestructionListener* m_destruction = nullptr;
+    b2Profile m_profile;
     std::vector<std::unique_ptr<b2Body>> m_bodies;
     std::vector<std::unique_ptr<b2Fixture>> m_fixtures;
     std::vector<std::pair<b2Fixture*, int>> m_fixtureOfId;  // device fixture id -> fixture, chain child
@@ -798,6 +1054,16 @@ private:
 };
 
 inline b2Fixture* b2Body::CreateFixture(const b2FixtureDef* def) { return m_world->AddFixture(this, def); }
+inline void b2Body::DestroyFixture(b2Fixture* fixture)
+{
+    if (fixture && fixture->m_body == this) m_world->DestroyFixture(fixture);
+}
+inline b2Body* b2Body::GetNext() const { return m_world->PreviousAlive((size_t)m_index); }
+inline void b2Contact::GetWorldManifold(b2WorldManifold* worldManifold) const
+{
+    worldManifold->Initialize(&m_manifold, m_a->GetBody()->GetTransform(), m_a->GetRadius(),
+                              m_b->GetBody()->GetTransform(), m_b->GetRadius());
+}
 inline const float* b2Body::State() const { return m_world->BodyState(m_index); }
 inline void b2Body::SetTransform(const b2Vec2& p, float angle) { m_world->Edit(m_index, GB_EDIT_SET_TRANSFORM, p.x, p.y, angle, 0.0f, true); }
 inline void b2Body::SetLinearVelocity(const b2Vec2& v) { m_world->Edit(m_index, GB_EDIT_SET_LINEAR_VELOCITY, v.x, v.y, 0.0f, 0.0f, true); }

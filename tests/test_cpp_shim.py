@@ -236,3 +236,169 @@ def test_cpp_chain_match_oracle(gpu, tmp_path):
     want_children = sorted((0 if f < 8 else 1, f if f < 8 else f - 8, fbody[fb]) for f, fb in zip(ci[:, 0], ci[:, 1])
                            if f < 12)
     assert got_children == want_children and len(want_children) > 0
+
+
+DQ_SRC = os.path.join(ROOT, "tests", "cpp", "destroy_queries.cpp")
+
+
+def _compile_dq(tmp_path):
+    lib = _lib.library_path()
+    exe = str(tmp_path / "destroy_queries")
+    libdir = os.path.dirname(lib)
+    # without contraction: GetWorldManifold runs in the caller's code and is compared bit for bit
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
+           DQ_SRC, "-o", exe, "-L", libdir, "-lbox2d_gb300", f"-Wl,-rpath,{libdir}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return exe
+
+
+def _dq_scene():
+    s = scenes.Scene(name="destroy_queries")
+    g = s.body(scenes.STATIC, 0.0, 0.0)
+    s.fixture(g, scenes.EDGE, [-20.0, 0.0, 20.0, 0.0, 0, 0, 0, 0, 0, 0], friction=0.6)
+    for r in range(3):
+        for j in range(4 - r):
+            b = s.body(scenes.DYNAMIC, float(np.float32(-1.875 + r * 0.625 + j * 1.25)), 0.5 + r * 1.0)
+            s.fixture(b, scenes.BOX, [0.5, 0.5], 2, density=5.0, friction=0.6)
+    a = s.body(scenes.STATIC, 6.0, 6.0)
+    s.fixture(a, scenes.CIRCLE, [0.0, 0.0, 0.25])
+    bob = s.body(scenes.DYNAMIC, 8.0, 6.0)
+    s.fixture(bob, scenes.CIRCLE, [0.0, 0.0, 0.5], density=1.0)
+    s.revolute(a, bob, [0.0, 0.0], [-2.0, 0.0])
+    t = s.body(scenes.DYNAMIC, -6.0, 3.0)
+    s.fixture(t, scenes.BOX, [0.5, 0.25], 2, density=1.0)
+    s.fixture(t, scenes.CIRCLE, [0.5, 0.0, 0.25], density=2.0)
+    return s
+
+
+def _world_manifold(m_ints, m_flts, xa, ra, xb, rb):
+    """b2WorldManifold::Initialize (b2Collision.cpp:25-66) in float32, operation for operation."""
+    f = np.float32
+    mul = lambda x, v: (f(f(x[3] * v[0]) - f(x[2] * v[1])) + x[0], f(f(x[2] * v[0]) + f(x[3] * v[1])) + x[1])
+    rot = lambda x, v: (f(x[3] * v[0]) - f(x[2] * v[1]), f(x[2] * v[0]) + f(x[3] * v[1]))
+    dot = lambda a, b: f(a[0] * b[0]) + f(a[1] * b[1])
+    kind, count = int(m_ints[4]), int(m_ints[3])
+    ln, lp = (m_flts[0], m_flts[1]), (m_flts[2], m_flts[3])
+    pts = [(m_flts[4], m_flts[5]), (m_flts[8], m_flts[9])]
+    pts_out, seps = [(f(0), f(0)), (f(0), f(0))], [f(0), f(0)]
+    if kind == 0:
+        normal = (f(1), f(0))
+        pa, pb = mul(xa, lp), mul(xb, pts[0])
+        d = (pa[0] - pb[0], pa[1] - pb[1])
+        eps = f(np.finfo(np.float32).eps)
+        if dot(d, d) > f(eps * eps):
+            normal = (pb[0] - pa[0], pb[1] - pa[1])
+            length = np.sqrt(f(f(normal[0] * normal[0]) + f(normal[1] * normal[1])), dtype=np.float32)
+            if length >= eps:
+                inv = f(f(1) / length)
+                normal = (f(normal[0] * inv), f(normal[1] * inv))
+        ca = (pa[0] + f(ra * normal[0]), pa[1] + f(ra * normal[1]))
+        cb = (pb[0] - f(rb * normal[0]), pb[1] - f(rb * normal[1]))
+        pts_out[0] = (f(f(0.5) * f(ca[0] + cb[0])), f(f(0.5) * f(ca[1] + cb[1])))
+        seps[0] = dot((cb[0] - ca[0], cb[1] - ca[1]), normal)
+    else:
+        xp, xq = (xa, xb) if kind == 1 else (xb, xa)
+        rp, rq = (ra, rb) if kind == 1 else (rb, ra)
+        normal = rot(xp, ln)
+        plane = mul(xp, lp)
+        for i in range(count):
+            clip = mul(xq, pts[i])
+            s = f(rp - dot((clip[0] - plane[0], clip[1] - plane[1]), normal))
+            cp_ = (clip[0] + f(s * normal[0]), clip[1] + f(s * normal[1]))
+            cq = (clip[0] - f(rq * normal[0]), clip[1] - f(rq * normal[1]))
+            ca, cb = (cp_, cq) if kind == 1 else (cq, cp_)
+            pts_out[i] = (f(f(0.5) * f(ca[0] + cb[0])), f(f(0.5) * f(ca[1] + cb[1])))
+            seps[i] = dot((cb[0] - ca[0], cb[1] - ca[1]), normal) if kind == 1 else \
+                dot((ca[0] - cb[0], ca[1] - cb[1]), normal)
+        if kind == 2:
+            normal = (-normal[0], -normal[1])
+    return np.array([normal[0], normal[1], pts_out[0][0], pts_out[0][1], pts_out[1][0], pts_out[1][1], seps[0],
+                     seps[1]], dtype=np.float32)
+
+
+@pytest.mark.gpu
+def test_cpp_destroy_queries_match_oracle(gpu, tmp_path):
+    """DestroyBody / DestroyFixture / SetDestructionListener, GetBodyList, GetProxyCount, QueryAABB and
+    RayCast callbacks and GetWorldManifold of the C++ mirror against the CPU oracle (state, listener
+    calls, proxies, manifold bits) and against the device queries (callback protocol)."""
+    from box2dpp_gb300.world import World
+
+    exe = _compile_dq(tmp_path)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    out = {}
+    bodies = {}
+    for ln in r.stdout.strip().splitlines():
+        parts = ln.split()
+        if parts[0] == "body":
+            bodies[int(parts[1])] = np.array([float.fromhex(v) for v in parts[2:]], dtype=np.float32)
+        else:
+            out[parts[0]] = parts[1:]
+    sc = _dq_scene()
+    o = oracle.OracleWorld(sc, "port", "project")
+    o.record_events(True)
+    gw = World(sc)
+    ends, goodbyes = 0, []
+
+    def step(n):
+        nonlocal ends
+        for _ in range(n):
+            o.step(1.0 / 60.0, 8, 3)
+            gw.step(1.0 / 60.0, 8, 3)
+            ends += int((o.events()[0][:, 0] == 1).sum())
+
+    def destroy(kind, i):
+        nonlocal ends
+        seen = len(o.events()[0])
+        goodbyes.extend(int(x) for row in getattr(o, "destroy_" + kind)(i) for x in row)
+        getattr(gw, "destroy_" + kind)(i)
+        ends += int((o.events()[0][seen:, 0] == 1).sum())
+
+    step(40)
+    destroy("body", 5)
+    destroy("fixture", 13)
+    assert int(out["ends_after_first"][0]) == ends
+    step(20)
+    destroy("body", 10)
+    for w_ in (o, gw):
+        b = w_.add_body(2, [0.0, 8.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0], 1 | 2 | 16)
+        w_.add_fixture(b, 3, [0.5, 0.5], 2, [1.0, 0.2, 0.0], [1, 0xFFFF, 0, 0])
+    step(40)
+    assert [int(x) for x in out["goodbyes"]] == goodbyes
+    e = out["ends"]
+    assert int(e[0]) == ends
+    ob = o.bodies()
+    alive = [i for i in range(len(ob)) if i not in (5, 10)]
+    assert int(e[2]) == len(alive) and int(e[4]) == 0
+    ids, _ = o.proxies()
+    assert int(e[6]) == int((ids >= 0).sum())
+    assert [int(x) for x in out["list"]] == sorted(alive, reverse=True)
+    for i, got in bodies.items():
+        want = ob[i][[0, 1, 2, 5, 6, 7]]
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), i
+    q = gw.query_aabb(np.array([[-3.0, -1.0, 3.0, 2.0]], np.float32))[0]
+    assert [int(x) for x in out["query"]] == list(q)
+    assert [int(x) for x in out["query_stop"]] == list(q[:2])
+    ray = np.array([-10.0, 0.75, 10.0, 0.25], np.float32)
+    fix, hit = gw.raycast(ray[None, :])
+    allf, _ = gw.raycast_all(ray)
+    rr = out["ray"]
+    assert int(rr[0]) == int(fix[0]) and int(rr[-1]) == len(allf)
+    got = np.array([float.fromhex(v) for v in rr[1:6]], dtype=np.float32)
+    assert np.array_equal(got.view(np.uint32), hit[0].view(np.uint32))
+    ci, cf = o.contacts()
+    m = out["manifold"]
+    assert [int(m[0]), int(m[1]), int(m[2])] == [int(ci[0, 0]), int(ci[0, 1]), int(ci[0, 3])]
+    fx_body = {f: b for f, b in enumerate(sc.arrays()["fix_body"])}
+    fx_body[14] = 13  # the body created after the destructions
+    radius = lambda f: (np.float32(sc.fixtures[f][2][2]) if f < len(sc.fixtures) and sc.fixtures[f][1] == scenes.CIRCLE
+                        else np.float32(0.01))
+    xf = lambda b: np.array([ob[b][0], ob[b][1], ob[b][8], ob[b][9]], dtype=np.float32)
+    want = _world_manifold(ci[0], cf[0], xf(fx_body[int(ci[0, 0])]), radius(int(ci[0, 0])), xf(fx_body[int(ci[0, 1])]),
+                           radius(int(ci[0, 1])))
+    got = np.array([float.fromhex(v) for v in m[3:]], dtype=np.float32)
+    n = int(ci[0, 3])
+    sel = [0, 1] + [2 + 2 * k for k in range(n)] + [3 + 2 * k for k in range(n)] + [6 + k for k in range(n)]
+    assert np.array_equal(got[sel].view(np.uint32), want[sel].view(np.uint32)), (got, want)
+    assert int(out["profile"][0]) == 1
