@@ -32,8 +32,15 @@ EXPORTS = [
     "gb_world_set_contact_log", "gb_world_read_contact_log", "gb_world_contact_stats", "gb_world_set_events",
     "gb_world_read_events", "gb_world_query_aabb", "gb_world_raycast", "gb_create_joints",
     "gb_world_stage_times", "gb_body_edits", "gb_world_set_limits", "gb_destroy_body", "gb_destroy_joint",
-    "gb_destroy_fixture", "gb_world_raycast_all", "gb_world_get_profile",
+    "gb_destroy_fixture", "gb_world_raycast_all", "gb_world_get_profile", "gb_world_step_begin",
+    "gb_contact_edits", "gb_world_step_end",
 ]
+
+# gb_contact_edit records: world, contact (list position), flags (1 enabled, 2 friction, 4 restitution,
+# 8 tangent speed), enabled (int32), friction, restitution, tangent speed, reserved (float32)
+CONTACT_EDIT_DTYPE = np.dtype([("world", np.int32), ("contact", np.int32), ("flags", np.int32),
+                               ("enabled", np.int32), ("friction", np.float32), ("restitution", np.float32),
+                               ("tangent_speed", np.float32), ("reserved", np.float32)])
 
 
 # gb_body_edit ops (GB_EDIT_*) and the record layout: world, body, op, wake (int32), v[4] (float32)
@@ -113,6 +120,9 @@ def load(build_if_missing: bool = True):
         "gb_collide_noalloc": [i, _i32, _f32, _i32, _f32, _i32, _f32, _i32, _f32, _i32, _f32],
         "gb_world_set_solver": [vp, i, f, i],
         "gb_world_set_limits": [vp, i, i],
+        "gb_world_step_begin": [vp, f, i, i],
+        "gb_contact_edits": [vp, i, C.c_void_p],
+        "gb_world_step_end": [vp],
         "gb_world_raycast_all": [vp, i, _f32, _i32, _f32, i, C.POINTER(C.c_int)],
         "gb_world_get_profile": [vp, i, _f32],
         "gb_destroy_body": [vp, i, i, _i32, i, C.POINTER(C.c_int)],

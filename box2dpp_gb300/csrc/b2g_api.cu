@@ -25,6 +25,7 @@ cudaError_t b2gLaunchStep(const b2g::Batch& B, const b2g::StepParams& P, const i
 cudaError_t b2gLaunchToi(const b2g::Batch& B, const b2g::StepParams& P, const int* slotOf, int first, int count,
                          cudaStream_t stream);
 cudaError_t b2gLaunchBodyEdits(const b2g::Batch& B, const b2g::BodyEdit* edits, int n, cudaStream_t stream);
+cudaError_t b2gLaunchContactEdits(const b2g::Batch& B, const b2g::ContactEdit* edits, int n, cudaStream_t stream);
 cudaError_t b2gLaunchStepToi(const b2g::Batch& B, const b2g::StepParams& P, const int* schedule, int first, int count,
                              int threads, int smemRows, int smemContacts, cudaStream_t stream);
 cudaError_t b2gLaunchSinCos(const float* x, float* s, float* c, int n, cudaStream_t stream);
@@ -149,6 +150,11 @@ struct gb_world {
     MlpView mlp{};
     BodyEdit* dEdits = nullptr;  // device copy of the last gb_body_edits call
     int editCap = 0;
+    ContactEdit* dContactEdits = nullptr;  // device copy of the last gb_contact_edits call
+    int contactEditCap = 0;
+    bool splitOpen = false;  // gb_world_step_begin ran, gb_world_step_end not yet
+    float splitDt = 0.0f;
+    int splitVi = 0, splitPi = 0;
     float* logX = nullptr;   // contact-point log (device), see gb_world_set_contact_log
     float* logT = nullptr;
     int* logCount = nullptr;
@@ -552,10 +558,13 @@ gb_status LaunchPlanStep(gb_world* g, const StepParams& P, const LaunchPlan& pla
         const LaunchClass& c = plan[i];
         cudaStream_t st = g->pipe[i];
         GB_CUDA(cudaStreamWaitEvent(st, g->fork, 0));
-        GB_CUDA(b2gLaunchNarrowphase(g->batch, g->dSlotOf, c.first, c.count, st));
+        // a split step (P.phase 1, then 2) runs the narrowphase and collide phase in its first half
+        if (P.phase != 2) GB_CUDA(b2gLaunchNarrowphase(g->batch, g->dSlotOf, c.first, c.count, st));
         GB_CUDA(b2gLaunchStep(g->batch, P, g->dSchedule, c.first, c.count, c.threads, c.rows, c.contacts, st));
-        GB_CUDA(b2gLaunchToi(g->batch, P, g->dSlotOf, c.first, c.count, st));
-        GB_CUDA(b2gLaunchStepToi(g->batch, P, g->dSchedule, c.first, c.count, c.threads, c.rows, c.contacts, st));
+        if (P.phase != 1) {
+            GB_CUDA(b2gLaunchToi(g->batch, P, g->dSlotOf, c.first, c.count, st));
+            GB_CUDA(b2gLaunchStepToi(g->batch, P, g->dSchedule, c.first, c.count, c.threads, c.rows, c.contacts, st));
+        }
         GB_CUDA(cudaEventRecord(g->pipeJoin[i], st));
     }
     for (int i = 0; i < n; ++i) GB_CUDA(cudaStreamWaitEvent(g->stream, g->pipeJoin[i], 0));
@@ -1226,6 +1235,7 @@ gb_status gb_world_destroy(gb_world* g)
     ReleaseLaunchResources(g);
     FreeLog(g);
     if (g->dEdits) cudaFree(g->dEdits);
+    if (g->dContactEdits) cudaFree(g->dContactEdits);
     if (g->ownStream && g->stream) cudaStreamDestroy(g->stream);
     delete g;
     return GB_OK;
@@ -1377,9 +1387,54 @@ gb_status gb_world_upload(gb_world* g)
     return Upload(g);
 }
 
+gb_status gb_world_step_begin(gb_world* g, float dt, int vi, int pi)
+{
+    if (!g || vi < 0 || pi < 0 || g->splitOpen) return GB_ERR_INVALID;
+    gb_status s = Upload(g);
+    if (s != GB_OK) return s;
+    StepParams P = MakeParams(g, dt, vi, pi);
+    P.phase = 1;
+    s = LaunchPlanStep(g, P, g->plan);
+    if (s != GB_OK) return s;
+    g->splitOpen = true;
+    g->locked = true;  // as inside b2World::Step: no creation or destruction until the step ends
+    g->splitDt = dt;
+    g->splitVi = vi;
+    g->splitPi = pi;
+    return GB_OK;
+}
+
+gb_status gb_contact_edits(gb_world* g, int n, const gb_contact_edit* edits)
+{
+    static_assert(sizeof(gb_contact_edit) == sizeof(ContactEdit), "gb_contact_edit mirrors the device record");
+    if (!g || n < 0 || (n > 0 && !edits) || !g->splitOpen) return GB_ERR_INVALID;
+    if (n == 0) return GB_OK;
+    if (n > g->contactEditCap) {
+        if (g->dContactEdits) cudaFree(g->dContactEdits);
+        g->dContactEdits = nullptr;
+        g->contactEditCap = 0;
+        GB_CUDA(cudaMalloc(&g->dContactEdits, n * sizeof(ContactEdit)));
+        g->contactEditCap = n;
+    }
+    GB_CUDA(cudaMemcpyAsync(g->dContactEdits, edits, n * sizeof(ContactEdit), cudaMemcpyHostToDevice, g->stream));
+    GB_CUDA(b2gLaunchContactEdits(g->batch, g->dContactEdits, n, g->stream));
+    GB_CUDA(cudaStreamSynchronize(g->stream));  // the host array may go once the call returns
+    return GB_OK;
+}
+
+gb_status gb_world_step_end(gb_world* g)
+{
+    if (!g || !g->splitOpen) return GB_ERR_INVALID;
+    StepParams P = MakeParams(g, g->splitDt, g->splitVi, g->splitPi);
+    P.phase = 2;
+    g->splitOpen = false;
+    g->locked = false;
+    return LaunchPlanStep(g, P, g->plan);
+}
+
 gb_status gb_world_step(gb_world* g, float dt, int vi, int pi)
 {
-    if (!g || vi < 0 || pi < 0) return GB_ERR_INVALID;
+    if (!g || vi < 0 || pi < 0 || g->splitOpen) return GB_ERR_INVALID;
     gb_status s = Upload(g);
     if (s != GB_OK) return s;
     const StepParams P = MakeParams(g, dt, vi, pi);
@@ -1393,7 +1448,7 @@ gb_status gb_world_step(gb_world* g, float dt, int vi, int pi)
 
 gb_status gb_world_graph_step(gb_world* g, float dt, int vi, int pi)
 {
-    if (!g || vi < 0 || pi < 0) return GB_ERR_INVALID;
+    if (!g || vi < 0 || pi < 0 || g->splitOpen) return GB_ERR_INVALID;
     if (g->tuneIndex >= 0) return gb_world_step(g, dt, vi, pi);  // tuning steps are timed one by one
     gb_status s = Upload(g);
     if (s != GB_OK) return s;

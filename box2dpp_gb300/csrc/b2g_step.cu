@@ -2585,22 +2585,50 @@ __global__ void __launch_bounds__(256, B2G_STEP_MIN_BLOCKS) StepKernel(Batch B, 
     W.init(B, schedule ? schedule[blockIdx.x] : blockIdx.x);
     W.smemBase = smem;
     W.smemBytes = (2 * L.smemRows + L.smemContacts) * (int)sizeof(float4);
-    const bool newFixture = W.st->newFixture != 0;
     const unsigned long long t0 = clock64();
-    __syncthreads();
-    if (tid() == 0) W.st->newFixture = 0;
-    if (newFixture) W.findNewContacts();
-    __syncthreads();
-    const unsigned long long t1 = clock64();
-    W.collide();
-    const unsigned long long t2 = clock64();
-    if (W.st->stepComplete && P.dt > 0.0f) W.solve(P, smem, L.smemRows, L.smemContacts);
+    unsigned long long t1 = t0, t2 = t0;
+    if (P.phase != 2) {
+        const bool newFixture = W.st->newFixture != 0;
+        __syncthreads();
+        if (tid() == 0) W.st->newFixture = 0;
+        if (newFixture) W.findNewContacts();
+        __syncthreads();
+        t1 = clock64();
+        W.collide();
+        t2 = clock64();
+    }
+    if (P.phase != 1 && W.st->stepComplete && P.dt > 0.0f) W.solve(P, smem, L.smemRows, L.smemContacts);
     __syncthreads();
     if (tid() == 0) {
         const unsigned long long t3 = clock64();
-        W.st->cyc[0] = t1 - t0;
-        W.st->cyc[1] = t2 - t1;
-        W.st->cyc[7] = t3 - t0;
+        if (P.phase != 2) {
+            W.st->cyc[0] = t1 - t0;
+            W.st->cyc[1] = t2 - t1;
+            W.st->cyc[7] = t3 - t0;
+        } else {
+            W.st->cyc[7] += t3 - t0;
+        }
+    }
+}
+
+// Contact changes between the halves of a split step (b2Contact::SetEnabled, SetFriction,
+// SetRestitution, SetTangentSpeed made by a PreSolve listener), in order, one thread.
+__global__ void ContactEditKernel(Batch B, const ContactEdit* edits, int n)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    for (int i = 0; i < n; ++i) {
+        const ContactEdit e = edits[i];
+        if (e.world < 0 || e.world >= B.worlds) continue;
+        Wd W;
+        W.init(B, e.world);
+        if (e.contact < 0 || e.contact >= W.st->contactCount) continue;
+        const int c = W.order[e.contact];
+        if (e.flags & 1) W.ci[c].x = e.enabled ? (W.ci[c].x | kCEnabled) : (W.ci[c].x & ~kCEnabled);
+        float4 p = W.cp[c];
+        if (e.flags & 2) p.x = e.friction;
+        if (e.flags & 4) p.y = e.restitution;
+        if (e.flags & 8) p.z = e.tangentSpeed;
+        W.cp[c] = p;
     }
 }
 
@@ -2703,6 +2731,13 @@ cudaError_t b2gLaunchNarrowphase(const b2g::Batch& B, const int* slotOf, int fir
 {
     if (B.contactRows <= 0) return cudaSuccess;
     b2g::NarrowphaseKernel<<<(B.contactRows + 255) / 256, 256, 0, stream>>>(B, slotOf, first, count);
+    return cudaGetLastError();
+}
+
+cudaError_t b2gLaunchContactEdits(const b2g::Batch& B, const b2g::ContactEdit* edits, int n, cudaStream_t stream)
+{
+    if (n <= 0) return cudaSuccess;
+    b2g::ContactEditKernel<<<1, 32, 0, stream>>>(B, edits, n);
     return cudaGetLastError();
 }
 

@@ -255,6 +255,14 @@ struct Batch {
     unsigned char* islTab; // island-DFS tables of the worlds whose table does not fit in shared memory
 };
 
+// A change to a contact between the halves of a split step (the device copy of gb_contact_edit):
+// contact = position in the world's contact list; flags bit 0 enabled, 1 friction, 2 restitution,
+// 3 tangent speed.
+struct ContactEdit {
+    int world, contact, flags, enabled;
+    float friction, restitution, tangentSpeed, pad;
+};
+
 // A b2Body state change between steps (the device copy of the C-ABI's gb_body_edit, same layout).
 enum : int { kEditSetTransform = 0, kEditSetLinearVelocity, kEditSetAngularVelocity, kEditSetAwake, kEditApplyForce,
              kEditApplyForceToCenter, kEditApplyTorque, kEditApplyLinearImpulse, kEditApplyAngularImpulse,
@@ -289,6 +297,8 @@ struct StepParams {
     float tolerance;    // > 0: stop the velocity iterations once the velocity residual is <= tolerance
     int measureResidual;// 1: record the velocity residual after the velocity iterations
     int recordEvents;   // 1: record the listener calls of the step in the event log
+    int phase;          // 0 the whole step; 1 up to the collide phase; 2 the rest (a step split for a
+                        // PreSolve that changes contacts)
     int warmMode;       // kWarmReference, or kWarmLearned (the network below, reference as fallback)
     MlpView mlp;
     // contact-point log (plain solver): features at the start of the velocity solve, then the

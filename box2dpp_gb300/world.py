@@ -61,6 +61,23 @@ class World:
     def step(self, dt: float = 1.0 / 60.0, vi: int = 8, pi: int = 3) -> None:
         _lib.check(self.lib.gb_world_step(self.h, dt, vi, pi), "gb_world_step")
 
+    def step_begin(self, dt: float = 1.0 / 60.0, vi: int = 8, pi: int = 3) -> None:
+        """First half of a split step: up to and including the collide phase (gb_world_step_begin)."""
+        _lib.check(self.lib.gb_world_step_begin(self.h, dt, vi, pi), "gb_world_step_begin")
+
+    def contact_edits(self, edits) -> None:
+        """Contact changes between the halves: (world, list position, flags, enabled, friction,
+        restitution, tangent speed) records (see gb_contact_edits)."""
+        arr = np.zeros(len(edits), dtype=_lib.CONTACT_EDIT_DTYPE)
+        for k, e in enumerate(edits):
+            arr[k] = tuple(e) + (0.0,) * (8 - len(e))
+        _lib.check(self.lib.gb_contact_edits(self.h, len(arr), arr.ctypes.data if len(arr) else None),
+                   "gb_contact_edits")
+
+    def step_end(self) -> None:
+        """Second half of a split step (gb_world_step_end)."""
+        _lib.check(self.lib.gb_world_step_end(self.h), "gb_world_step_end")
+
     def graph_step(self, dt: float = 1.0 / 60.0, vi: int = 8, pi: int = 3) -> None:
         """One step replayed from a captured CUDA graph (see gb_world_graph_step)."""
         _lib.check(self.lib.gb_world_graph_step(self.h, dt, vi, pi), "gb_world_graph_step")

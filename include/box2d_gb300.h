@@ -158,6 +158,27 @@ gb_status gb_destroy_body(gb_world* world, int w, int body, int* calls, int cap,
 gb_status gb_destroy_joint(gb_world* world, int w, int joint, int* calls, int cap, int* n_calls);
 gb_status gb_destroy_fixture(gb_world* world, int w, int fixture, int* calls, int cap, int* n_calls);
 
+/* A step split at its collide phase, for a b2ContactListener::PreSolve that changes contacts
+ * (Box2D/Dynamics/b2WorldCallbacks.h:105-120; b2Contact::SetEnabled, SetFriction, SetRestitution,
+ * SetTangentSpeed, Contacts/b2Contact.h:98-152), with one synchronisation: gb_world_step_begin runs
+ * b2World::Step up to and including b2ContactManager::Collide (new-fixture pairs, narrowphase,
+ * Begin/End/PreSolve calls recorded, gb_world_read_events reads them); gb_contact_edits then applies
+ * the listener's changes, in order: edit.contact is the contact's position in the world's contact
+ * list (gb_get_contacts order at this point), flags bit 0 sets the enabled flag to edit.enabled, bit 1
+ * the friction, bit 2 the restitution, bit 3 the tangent speed; gb_world_step_end runs the rest of the
+ * step (islands, solver, continuous phase). The world is locked between the two (creation and
+ * destruction return GB_ERR_INVALID) and gb_world_step / gb_world_graph_step are refused. The
+ * continuous phase's own PreSolve calls (contacts with a static, kinematic or bullet body updated at
+ * a time of impact) stay notifications: the split is exact for listeners that change only other
+ * contacts. */
+typedef struct gb_contact_edit {
+    int world, contact, flags, enabled;
+    float friction, restitution, tangent_speed, reserved;
+} gb_contact_edit;
+gb_status gb_world_step_begin(gb_world* world, float dt, int velocity_iterations, int position_iterations);
+gb_status gb_contact_edits(gb_world* world, int n, const gb_contact_edit* edits);
+gb_status gb_world_step_end(gb_world* world);
+
 gb_status gb_world_sync(gb_world* world);
 
 /* No counterpart in the reference (whose buffers grow on demand). The fixed capacities of the device

@@ -21,9 +21,13 @@
 //    do not depend on the order (closest hit, all hits) are the reference's;
 //  - b2Contact::GetWorldManifold computes on the host: bit-exact with the reference when the caller is
 //    compiled without floating-point contraction (-ffp-contract=off);
-//  - b2ContactListener calls are recorded on the device during the step, in the reference's order,
-//    and made after it: BeginContact, EndContact, PreSolve (a notification: the contact can no longer
-//    be changed for this step) and PostSolve with the solver's impulses.
+//  - b2ContactListener calls are recorded on the device during the step, in the reference's order.
+//    With a listener set, Step runs in two halves (gb_world_step_begin / gb_world_step_end): the
+//    collide phase's BeginContact, EndContact and PreSolve are made between them, and what PreSolve
+//    changes (SetEnabled, SetFriction, SetRestitution, SetTangentSpeed) acts on the rest of the step;
+//    PostSolve (with the solver's impulses) and the continuous phase's calls follow the step. The
+//    continuous phase's own PreSolve calls (contacts with a static, kinematic or bullet body at a time
+//    of impact) are notifications.
 #pragma once
 
 #include <algorithm>
@@ -98,7 +102,7 @@ public:
 
 class b2EdgeShape : public b2Shape {
 public:
-    b2EdgeShape() { m_type = e_edge; }
+    b2EdgeShape() { m_type = e_edge; m_radius = 0.01f; }  // b2_polygonRadius, as the reference
     void Set(const b2Vec2& v1, const b2Vec2& v2) { m_vertex1 = v1; m_vertex2 = v2; m_hasVertex0 = m_hasVertex3 = false; }
     void Encode(int* type, float* shape, int* n) const override
     {
@@ -162,7 +166,7 @@ public:
 
 class b2PolygonShape : public b2Shape {
 public:
-    b2PolygonShape() { m_type = e_polygon; }
+    b2PolygonShape() { m_type = e_polygon; m_radius = 0.01f; }  // b2_polygonRadius, as the reference
     // b2PolygonShape::Set: the hull is computed by the library exactly as the reference does
     void Set(const b2Vec2* points, int count)
     {
@@ -534,6 +538,16 @@ public:
     int GetChildIndexB() const { return m_childB; }
     bool IsTouching() const { return (m_flags & 2) != 0; }
     bool IsEnabled() const { return (m_flags & 4) != 0; }
+    // b2Contact::SetEnabled, SetFriction, SetRestitution, SetTangentSpeed (Contacts/b2Contact.h:98-152),
+    // in effect for the rest of a step when made in PreSolve
+    void SetEnabled(bool flag)
+    {
+        m_flags = flag ? (m_flags | 4) : (m_flags & ~4);
+        m_edit |= 1;
+    }
+    void SetFriction(float friction) { m_friction = friction; m_edit |= 2; }
+    void SetRestitution(float restitution) { m_restitution = restitution; m_edit |= 4; }
+    void SetTangentSpeed(float speed) { m_tangentSpeed = speed; m_edit |= 8; }
     const b2Manifold* GetManifold() const { return &m_manifold; }
     // b2Contact::GetWorldManifold (Box2D/Dynamics/Contacts/b2Contact.h:223-231)
     void GetWorldManifold(b2WorldManifold* worldManifold) const;
@@ -544,6 +558,8 @@ private:
     int m_childA = 0, m_childB = 0;
     int m_idA = -1, m_idB = -1;  // device fixture ids (one per chain child)
     int m_flags = 0;
+    int m_edit = 0;               // changes made by the listener (gb_contact_edit flags)
+    float m_friction = 0.0f, m_restitution = 0.0f, m_tangentSpeed = 0.0f;
     b2Manifold m_manifold;
 };
 
@@ -815,13 +831,29 @@ public:
     void Step(float timeStep, int velocityIterations, int positionIterations)
     {
         if (!Handle()) return;
-        if (m_listener) {
-            if (!m_eventsOn) m_eventsOn = gb_world_set_events(m_h, 1) == GB_OK;
-            ReadContacts();  // the contacts before the step: destroyed contacts and old manifolds
+        if (!m_listener) {
+            gb_world_step(m_h, timeStep, velocityIterations, positionIterations);
+            m_stale = true;
+            return;
         }
-        gb_world_step(m_h, timeStep, velocityIterations, positionIterations);
+        if (!m_eventsOn) m_eventsOn = gb_world_set_events(m_h, 1) == GB_OK;
+        ReadContacts();  // the contacts before the step: destroyed contacts and old manifolds
+        if (gb_world_step_begin(m_h, timeStep, velocityIterations, positionIterations) != GB_OK) return;
         m_stale = true;
-        if (m_listener) Report();
+        const int collideCalls = Report(0);
+        // what PreSolve changed, by list position
+        std::vector<gb_contact_edit> edits;
+        for (size_t k = 0; k < m_contacts.size(); ++k) {
+            const b2Contact& c = *m_contacts[k];
+            if (!c.m_edit) continue;
+            gb_contact_edit e{0, (int)k, c.m_edit, c.IsEnabled() ? 1 : 0, c.m_friction, c.m_restitution,
+                              c.m_tangentSpeed, 0.0f};
+            edits.push_back(e);
+        }
+        if (!edits.empty()) gb_contact_edits(m_h, (int)edits.size(), edits.data());
+        gb_world_step_end(m_h);
+        m_stale = true;
+        Report(collideCalls);
     }
 
     int GetBodyCount() const
@@ -1001,7 +1033,9 @@ private:
             m_contacts.push_back(std::move(c));
         }
     }
-    void Report()
+    // Makes the recorded listener calls from index `first` on, with the contacts as they are now and
+    // as they were before (m_contacts); returns the number of calls recorded so far.
+    int Report(int first)
     {
         std::vector<std::unique_ptr<b2Contact>> old = std::move(m_contacts);
         ReadContacts();
@@ -1014,7 +1048,7 @@ private:
         std::vector<float> imp(4 * (size_t)(n > 0 ? n : 1));
         if (n > 0) gb_world_read_events(m_h, 0, rec.data(), imp.data(), n, &n);
         const b2Manifold empty;
-        for (int i = 0; i < n; ++i) {
+        for (int i = first; i < n; ++i) {
             const std::pair<int, int> key{rec[4 * i + 1], rec[4 * i + 2]};
             auto itNow = now.find(key);
             auto itOld = before.find(key);
@@ -1033,7 +1067,10 @@ private:
             }
             }
         }
-        m_old = std::move(old);  // kept alive: a listener may hold the pointers until the next Step
+        // kept alive: a listener may hold the pointers until the next Step
+        if (first == 0) m_old.clear();
+        for (auto& c : old) m_old.push_back(std::move(c));
+        return n;
     }
 
     b2Vec2 m_gravity;

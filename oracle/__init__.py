@@ -87,6 +87,7 @@ def _declare(lib, p: str) -> None:
     sig["joint"] = (C.c_int, [vp, C.c_int, C.c_int, C.c_int, _f32p, C.c_int])
     sig["body"] = (C.c_int, [vp, C.c_int, _f32p, C.c_int])
     sig["fixture"] = (C.c_int, [vp, C.c_int, C.c_int, _f32p, C.c_int, _f32p, _i32p])
+    sig["set_presolve_rule"] = (None, [vp, _i32p, C.c_int])
     for kind in ("body", "joint", "fixture"):
         sig["destroy_" + kind] = (C.c_int, [vp, C.c_int, _i32p, C.c_int])
     if p == "rw_":
@@ -184,6 +185,13 @@ class OracleWorld:
         self.n_fixtures += 1
         return self._fn("fixture")(self.h, int(body), int(type_), s, int(n), np.asarray(mat, dtype=np.float32),
                                    np.asarray(filt, dtype=np.int32))
+
+    def set_presolve_rule(self, bits) -> None:
+        """A PreSolve listener applying a rule per fixture pair (bits per fixture: 1 ghost, 2 ice,
+        4 bouncy; a contact between two fixtures sharing a bit is disabled, gets friction 0 or
+        restitution 0.9)."""
+        b = np.ascontiguousarray(bits, dtype=np.int32)
+        self._fn("set_presolve_rule")(self.h, b, len(b))
 
     def _destroy(self, kind: str, index: int):
         calls = np.zeros((64, 2), dtype=np.int32)

@@ -608,6 +608,15 @@ void World::Update(int c)
         if (wasTouching && !touching) events.push_back(Event{1, ct.fA, ct.fB, 0, 0, 0, 0});
         if (!sensor && touching) events.push_back(Event{2, ct.fA, ct.fB, 0, 0, 0, 0});
     }
+    // a PreSolve listener's changes (b2ContactListener::PreSolve, called here in b2Contact::Update)
+    if (!sensor && touching && !preSolveRule.empty()) {
+        const int ra = ct.fA < (int)preSolveRule.size() ? preSolveRule[ct.fA] : 0;
+        const int rb = ct.fB < (int)preSolveRule.size() ? preSolveRule[ct.fB] : 0;
+        const int both = ra & rb;
+        if (both & 1) ct.flags &= ~kCEnabled;
+        if (both & 2) ct.friction = 0.0f;
+        if (both & 4) ct.restitution = 0.9f;
+    }
 }
 
 // b2ContactManager::Collide (Dynamics/b2ContactManager.cpp:107-172)

@@ -141,6 +141,9 @@ struct World {
     std::vector<Position> positions;
     std::vector<Velocity> velocities;
 
+    // A PreSolve listener's rule, per fixture: bit 0 ghost, 1 ice, 2 bouncy; a contact between two
+    // fixtures sharing a bit is disabled (ghost), gets friction 0 (ice) or restitution 0.9 (bouncy).
+    std::vector<int> preSolveRule;
     // destruction listener calls of the last Destroy* call: {0 joint / 1 fixture, index}
     std::vector<std::pair<int, int>> goodbyes;
     void DestroyBody(int b);

@@ -27,6 +27,9 @@ using namespace box2dref;
 
 namespace {
 
+int fixture_index(const b2Fixture* f) { return (int)(intptr_t)f->GetUserData() - 1; }
+int body_index(const b2Body* b) { return (int)(intptr_t)b->GetUserData() - 1; }
+
 struct RefWorld;
 
 // b2DestructionListener recording its calls as {0 joint / 1 fixture, creation index}
@@ -37,8 +40,25 @@ struct Goodbye : public b2DestructionListener {
     void SayGoodbye(b2Fixture* fixture) override;
 };
 
+// A b2ContactListener whose PreSolve applies a rule per fixture pair (bits per fixture: 1 ghost,
+// 2 ice, 4 bouncy; a contact between two fixtures sharing a bit is disabled, gets friction 0 or
+// restitution 0.9).
+struct PreSolveRule : public b2ContactListener {
+    std::vector<int> bits;
+    void PreSolve(b2Contact* contact, const b2Manifold*) override
+    {
+        const int a = fixture_index(contact->GetFixtureA()) + contact->GetChildIndexA();
+        const int b = fixture_index(contact->GetFixtureB()) + contact->GetChildIndexB();
+        const int both = (a < (int)bits.size() ? bits[a] : 0) & (b < (int)bits.size() ? bits[b] : 0);
+        if (both & 1) contact->SetEnabled(false);
+        if (both & 2) contact->SetFriction(0.0f);
+        if (both & 4) contact->SetRestitution(0.9f);
+    }
+};
+
 struct RefWorld {
     b2World world;
+    PreSolveRule rule;
     std::vector<b2Body*> bodies;      // creation order; null once destroyed
     std::vector<b2Fixture*> fixtures; // creation order (a chain's children share one); null once destroyed
     std::vector<b2Joint*> joints;     // creation order; null once destroyed
@@ -61,8 +81,6 @@ void Goodbye::SayGoodbye(b2Fixture* fixture)
     calls.push_back((int)(intptr_t)fixture->GetUserData() - 1);
 }
 
-int fixture_index(const b2Fixture* f) { return (int)(intptr_t)f->GetUserData() - 1; }
-int body_index(const b2Body* b) { return (int)(intptr_t)b->GetUserData() - 1; }
 
 } // namespace
 
@@ -380,6 +398,12 @@ static int TakeGoodbyes(RefWorld* w, int* calls, int cap)
     for (int i = 0; i < 2 * n && i < 2 * cap; ++i) calls[i] = w->goodbye.calls[i];
     w->goodbye.calls.clear();
     return n;
+}
+void rw_set_presolve_rule(void* h, const int* bits, int n)
+{
+    RefWorld* w = static_cast<RefWorld*>(h);
+    w->rule.bits.assign(bits, bits + n);
+    w->world.SetContactListener(&w->rule);
 }
 int rw_destroy_body(void* h, int b, int* calls, int cap)
 {

@@ -143,3 +143,34 @@ def apply_ops(world, ops, w: int = 0):
             # reports EndContact calls (kind 2), which the oracles record with their other events
             calls.extend([(int(c[0]), int(c[1])) for c in got if int(c[0]) in (0, 1)])
     return calls
+
+
+def presolve_case():
+    """The scene and the PreSolve rule bits of the split-step case: 200 circles and polygons dropped
+    into an edge box (sleep on); dynamic fixture i is a ghost when i % 3 == 0, ice when i % 4 == 0 and
+    bouncy when i % 5 == 0 (contacts between two ghosts are disabled, between two ice fixtures get
+    friction 0, between two bouncy ones restitution 0.9). The static walls take no part, so the
+    continuous phase, whose contacts always involve a static body here, never meets the rule."""
+    from box2dpp_gb300 import scenes
+
+    sc = scenes.drop(200, scenes.SplitMix64(23))
+    bits = np.array([0 if i < 4 else ((i % 3 == 0) * 1 | (i % 4 == 0) * 2 | (i % 5 == 0) * 4)
+                     for i in range(len(sc.fixtures))], np.int32)
+    return sc, bits
+
+
+def presolve_edits(world, bits, w: int = 0):
+    """The rule applied to the PreSolve calls recorded by the first half of a split device step: one
+    gb_contact_edit per change, by list position."""
+    rec, _ = world.events(w)
+    ints, _ = world.contacts(w)
+    pos = {(int(a), int(b)): k for k, (a, b) in enumerate(ints[:, :2])}
+    edits = []
+    for kind, fa, fb in rec[:, :3]:
+        if kind != 2:
+            continue
+        both = int(bits[fa]) & int(bits[fb])
+        flags = (1 if both & 1 else 0) | (2 if both & 2 else 0) | (4 if both & 4 else 0)
+        if flags:
+            edits.append((w, pos[(int(fa), int(fb))], flags, 0, 0.0, 0.9, 0.0))
+    return edits

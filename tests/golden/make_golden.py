@@ -15,6 +15,8 @@ Two builds of the reference are used: ``libm`` (glibc sinf/cosf, the reference a
 * ``destroy_mix_<trig>.npz``: a scene changed between steps (bodies, joints and fixtures destroyed,
   bodies created) with the per-step digests, the destruction listener's calls and the final proxy
   ids (freed tree nodes are reused).
+* ``presolve_rule_<trig>.npz``: a drop with a PreSolve listener that disables, de-frictions or
+  bounces contacts by a per-fixture rule (tests/_util.py presolve_case), per-step digests.
 * ``collide.npz``: seeded shape pairs of every supported type pair with the reference manifolds.
 * ``toi.npz``: seeded sweeps with the reference b2TimeOfImpact result.
 * ``trig.npz``: glibc sinf/cosf on seeded angles (how far the project trig is from libm).
@@ -275,6 +277,19 @@ def main():
         print("done")
         return
     only = sys.argv[sys.argv.index("--case") + 1] if "--case" in sys.argv else None
+    if only in (None, "presolve_rule"):
+        from tests._util import presolve_case
+
+        sc, bits = presolve_case()
+        for trig in ("libm", "project"):
+            w = oracle.OracleWorld(sc, "reference", trig)
+            w.set_presolve_rule(bits)
+            digests = np.zeros((300, 32), dtype=np.uint8)
+            for s in range(1, 301):
+                w.step(DT, VI, PI)
+                digests[s - 1] = np.frombuffer(state_digest(w.bodies(), *w.contacts()), dtype=np.uint8)
+            np.savez_compressed(os.path.join(HERE, f"presolve_rule_{trig}.npz"), digests=digests, steps=np.int32(300))
+        print("wrote presolve_rule")
     for name, make, steps, script in scripted_cases():
         if only and name != only:
             continue

@@ -118,3 +118,23 @@ def test_port_destroy_case_matches_reference(trig):
     assert np.array_equal(np.array(calls, np.int32).reshape(-1, 3), g["goodbyes"])
     ids, fat = w.proxies()
     assert np.array_equal(ids, g["proxy_ids"])
+
+
+@pytest.mark.parametrize("trig", ["project", "libm"])
+def test_port_presolve_rule_matches_reference(trig):
+    """A PreSolve listener that disables contacts and changes friction and restitution (the reference
+    with a b2ContactListener doing it, the restatement with the same rule), step by step."""
+    import platform
+
+    from tests._util import digest, presolve_case
+
+    g = golden(f"presolve_rule_{trig}")
+    sc, bits = presolve_case()
+    w = oracle.OracleWorld(sc, "port", trig)
+    w.set_presolve_rule(bits)
+    for s in range(1, int(g["steps"]) + 1):
+        w.step()
+        if not np.array_equal(digest(w.bodies(), *w.contacts()), g["digests"][s - 1]):
+            if trig == "libm" and platform.machine() != "x86_64":
+                pytest.skip("libm trig differs on this machine")
+            raise AssertionError(f"first divergence at step {s}")
