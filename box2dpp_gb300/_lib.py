@@ -33,8 +33,12 @@ EXPORTS = [
     "gb_world_read_events", "gb_world_query_aabb", "gb_world_raycast", "gb_create_joints",
     "gb_world_stage_times", "gb_body_edits", "gb_world_set_limits", "gb_destroy_body", "gb_destroy_joint",
     "gb_destroy_fixture", "gb_world_raycast_all", "gb_world_get_profile", "gb_world_step_begin",
-    "gb_contact_edits", "gb_world_step_end",
+    "gb_contact_edits", "gb_world_step_end", "gb_world_set_contact_filter", "gb_world_refilter",
+    "gb_world_filter_stats",
 ]
+
+# gb_should_collide_fn
+SHOULD_COLLIDE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int)
 
 # gb_contact_edit records: world, contact (list position), flags (1 enabled, 2 friction, 4 restitution,
 # 8 tangent speed), enabled (int32), friction, restitution, tangent speed, reserved (float32)
@@ -123,6 +127,9 @@ def load(build_if_missing: bool = True):
         "gb_world_step_begin": [vp, f, i, i],
         "gb_contact_edits": [vp, i, C.c_void_p],
         "gb_world_step_end": [vp],
+        "gb_world_set_contact_filter": [vp, SHOULD_COLLIDE_FN, vp],
+        "gb_world_refilter": [vp, i, i],
+        "gb_world_filter_stats": [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_int)],
         "gb_world_raycast_all": [vp, i, _f32, _i32, _f32, i, C.POINTER(C.c_int)],
         "gb_world_get_profile": [vp, i, _f32],
         "gb_destroy_body": [vp, i, i, _i32, i, C.POINTER(C.c_int)],

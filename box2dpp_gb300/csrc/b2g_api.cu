@@ -112,6 +112,17 @@ struct gb_world {
     std::vector<WorldDesc> desc;
     Batch batch{};
     std::vector<void*> allocations;
+    std::vector<size_t> allocationBytes;  // sizes of allocations (the filtered step's snapshot)
+    // user contact filter (gb_world_set_contact_filter): the callback, the device verdict table,
+    // and a copy of every device column taken before each step so that a step can be run again
+    gb_should_collide_fn filterFn = nullptr;
+    void* filterUser = nullptr;
+    unsigned long long* dFilterKeys = nullptr;
+    int* dFilterVals = nullptr;
+    int* dFilterMiss = nullptr;
+    int filterCap = 0, filterUsed = 0;
+    std::vector<void*> shadow;
+    long long filterReplays = 0;
     int* dSchedule = nullptr;
     int* dSlotOf = nullptr;  // schedule slot of each world (the inverse of dSchedule)
     cudaStream_t stream = nullptr;
@@ -309,6 +320,7 @@ template <typename T> gb_status DevAlloc(gb_world* g, T** p, size_t n)
     void* ptr = nullptr;
     GB_CUDA(cudaMalloc(&ptr, n * sizeof(T)));
     g->allocations.push_back(ptr);
+    g->allocationBytes.push_back(n * sizeof(T));
     *p = static_cast<T*>(ptr);
     return GB_OK;
 }
@@ -320,6 +332,9 @@ void FreeDevice(gb_world* g)
     g->graph = nullptr;
     for (void* p : g->allocations) cudaFree(p);
     g->allocations.clear();
+    g->allocationBytes.clear();
+    for (void* p : g->shadow) cudaFree(p);
+    g->shadow.clear();
     std::memset(&g->batch, 0, sizeof(g->batch));
     g->dSchedule = nullptr;
     g->dSlotOf = nullptr;
@@ -645,6 +660,61 @@ void ReleaseLaunchResources(gb_world* g)
 }
 
 // (Re)allocate device columns for the current world sizes and copy the host mirror over.
+// The user contact filter's verdict table in the batch (or the default filter when none is set).
+void AttachFilter(gb_world* g)
+{
+    Batch& B = g->batch;
+    B.filterKeys = g->filterFn ? g->dFilterKeys : nullptr;
+    B.filterVals = g->filterFn ? g->dFilterVals : nullptr;
+    B.filterCap = g->filterFn ? g->filterCap : 0;
+    B.filterMiss = g->filterFn ? g->dFilterMiss : nullptr;
+    B.filterMissCap = 0;  // the host reads the pending verdicts from the table itself
+}
+
+void FreeFilter(gb_world* g)
+{
+    if (g->dFilterKeys) cudaFree(g->dFilterKeys);
+    if (g->dFilterVals) cudaFree(g->dFilterVals);
+    if (g->dFilterMiss) cudaFree(g->dFilterMiss);
+    g->dFilterKeys = nullptr;
+    g->dFilterVals = nullptr;
+    g->dFilterMiss = nullptr;
+    g->filterCap = g->filterUsed = 0;
+}
+
+// A verdict table of cap slots holding the given (key, value) entries.
+gb_status BuildFilterTable(gb_world* g, int cap, const std::vector<unsigned long long>& keys, const std::vector<int>& vals)
+{
+    std::vector<unsigned long long> k((size_t)cap, ~0ull);
+    std::vector<int> v((size_t)cap, 2);
+    for (size_t i = 0; i < keys.size(); ++i) {
+        unsigned slot = FilterSlot(keys[i], cap);
+        while (k[slot] != ~0ull) slot = (slot + 1) & (unsigned)(cap - 1);
+        k[slot] = keys[i];
+        v[slot] = vals[i];
+    }
+    if (g->dFilterKeys) cudaFree(g->dFilterKeys);
+    if (g->dFilterVals) cudaFree(g->dFilterVals);
+    g->dFilterKeys = nullptr;
+    g->dFilterVals = nullptr;
+    GB_CUDA(cudaMalloc(&g->dFilterKeys, cap * sizeof(unsigned long long)));
+    GB_CUDA(cudaMalloc(&g->dFilterVals, cap * sizeof(int)));
+    GB_CUDA(cudaMemcpy(g->dFilterKeys, k.data(), cap * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(g->dFilterVals, v.data(), cap * sizeof(int), cudaMemcpyHostToDevice));
+    g->filterCap = cap;
+    g->filterUsed = (int)keys.size();
+    return GB_OK;
+}
+
+// b2ContactFilter::ShouldCollide's default (Dynamics/b2WorldCallbacks.cpp:26-38) on the host mirror
+bool HostDefaultFilter(const HWorld& W, int fA, int fB)
+{
+    const HFixture& a = W.fixtures[fA];
+    const HFixture& b = W.fixtures[fB];
+    if (a.group == b.group && a.group != 0) return a.group > 0;
+    return (a.mask & b.category) != 0 && (a.category & b.mask) != 0;
+}
+
 gb_status Upload(gb_world* g)
 {
     if (!g->hostDirty && g->onDevice) return GB_OK;
@@ -814,7 +884,67 @@ gb_status Upload(gb_world* g)
     g->plan = DefaultPlan(g);
     g->onDevice = true;
     g->hostDirty = false;
+    AttachFilter(g);
     return GB_OK;
+}
+
+// A step with a user contact filter. The device takes the default filter's verdict for pairs the
+// table does not know yet and logs that it met them; afterwards the user's filter decides each such
+// pair (b2ContactFilter::ShouldCollide, called here on the host with the ordered fixture pair). When
+// every decision equals the default's the step stands; otherwise every device column is restored
+// from the copy taken before the step and the step runs again with the decisions known (a bounded
+// number of times: each run leaves more pairs decided). The filter must give the same verdict for
+// the same ordered fixture pair until gb_world_refilter says otherwise.
+gb_status FilteredStep(gb_world* g, const StepParams& P)
+{
+    if (g->shadow.size() != g->allocations.size()) {
+        for (void* p : g->shadow) cudaFree(p);
+        g->shadow.assign(g->allocations.size(), nullptr);
+        for (size_t i = 0; i < g->allocations.size(); ++i)
+            GB_CUDA(cudaMalloc(&g->shadow[i], g->allocationBytes[i]));
+    }
+    for (int attempt = 0; attempt < 16; ++attempt) {
+        for (size_t i = 0; i < g->allocations.size(); ++i)
+            GB_CUDA(cudaMemcpyAsync(g->shadow[i], g->allocations[i], g->allocationBytes[i], cudaMemcpyDeviceToDevice,
+                                    g->stream));
+        GB_CUDA(cudaMemsetAsync(g->dFilterMiss, 0, sizeof(int), g->stream));
+        gb_status s = LaunchPlanStep(g, P, g->plan);
+        if (s != GB_OK) return s;
+        int missed = 0;
+        GB_CUDA(cudaMemcpyAsync(&missed, g->dFilterMiss, sizeof(int), cudaMemcpyDeviceToHost, g->stream));
+        GB_CUDA(cudaStreamSynchronize(g->stream));
+        if (missed == 0) return GB_OK;
+        // every pending verdict of the table, decided by the user's filter
+        std::vector<unsigned long long> keys((size_t)g->filterCap);
+        std::vector<int> vals((size_t)g->filterCap);
+        GB_CUDA(cudaMemcpy(keys.data(), g->dFilterKeys, g->filterCap * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(vals.data(), g->dFilterVals, g->filterCap * sizeof(int), cudaMemcpyDeviceToHost));
+        bool differs = false;
+        std::vector<unsigned long long> allKeys;
+        std::vector<int> allVals;
+        for (int i = 0; i < g->filterCap; ++i) {
+            if (keys[i] == ~0ull) continue;
+            if (vals[i] == 2) {
+                const int w = (int)(keys[i] >> 40), fA = (int)((keys[i] >> 20) & 0xFFFFF), fB = (int)(keys[i] & 0xFFFFF);
+                vals[i] = g->filterFn(g->filterUser, w, fA, fB) ? 1 : 0;
+                if ((vals[i] != 0) != HostDefaultFilter(g->worlds[w], fA, fB)) differs = true;
+            }
+            allKeys.push_back(keys[i]);
+            allVals.push_back(vals[i]);
+        }
+        int cap = g->filterCap;
+        while ((int)allKeys.size() * 2 > cap) cap *= 2;  // keep the table at most half full
+        s = BuildFilterTable(g, cap, allKeys, allVals);
+        if (s != GB_OK) return s;
+        AttachFilter(g);
+        if (!differs) return GB_OK;
+        ++g->filterReplays;
+        ReleaseGraph(g);
+        for (size_t i = 0; i < g->allocations.size(); ++i)
+            GB_CUDA(cudaMemcpyAsync(g->allocations[i], g->shadow[i], g->allocationBytes[i], cudaMemcpyDeviceToDevice,
+                                    g->stream));
+    }
+    return GB_ERR_TIMEOUT;
 }
 
 gb_status Mutable(gb_world* g, int w)
@@ -1236,6 +1366,7 @@ gb_status gb_world_destroy(gb_world* g)
     FreeLog(g);
     if (g->dEdits) cudaFree(g->dEdits);
     if (g->dContactEdits) cudaFree(g->dContactEdits);
+    FreeFilter(g);
     if (g->ownStream && g->stream) cudaStreamDestroy(g->stream);
     delete g;
     return GB_OK;
@@ -1389,7 +1520,7 @@ gb_status gb_world_upload(gb_world* g)
 
 gb_status gb_world_step_begin(gb_world* g, float dt, int vi, int pi)
 {
-    if (!g || vi < 0 || pi < 0 || g->splitOpen) return GB_ERR_INVALID;
+    if (!g || vi < 0 || pi < 0 || g->splitOpen || g->filterFn) return GB_ERR_INVALID;
     gb_status s = Upload(g);
     if (s != GB_OK) return s;
     StepParams P = MakeParams(g, dt, vi, pi);
@@ -1438,6 +1569,7 @@ gb_status gb_world_step(gb_world* g, float dt, int vi, int pi)
     gb_status s = Upload(g);
     if (s != GB_OK) return s;
     const StepParams P = MakeParams(g, dt, vi, pi);
+    if (g->filterFn) return FilteredStep(g, P);
     if (g->tuneIndex >= 0) {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         GB_CUDA(cudaStreamIsCapturing(g->stream, &cs));
@@ -1446,9 +1578,61 @@ gb_status gb_world_step(gb_world* g, float dt, int vi, int pi)
     return LaunchPlanStep(g, P, g->plan);
 }
 
+gb_status gb_world_set_contact_filter(gb_world* g, gb_should_collide_fn fn, void* user)
+{
+    if (!g || g->splitOpen) return GB_ERR_INVALID;
+    ReleaseGraph(g);
+    g->filterFn = fn;
+    g->filterUser = user;
+    if (!fn) {
+        FreeFilter(g);
+        AttachFilter(g);
+        return GB_OK;
+    }
+    for (const HWorld& W : g->worlds)
+        if ((int)W.fixtures.size() >= (1 << 20) || g->worlds.size() >= (1u << 23)) return GB_ERR_CAPACITY;
+    if (!g->dFilterMiss) GB_CUDA(cudaMalloc(&g->dFilterMiss, sizeof(int)));
+    gb_status s = BuildFilterTable(g, 4096, {}, {});
+    if (s != GB_OK) return s;
+    AttachFilter(g);
+    return GB_OK;
+}
+
+gb_status gb_world_refilter(gb_world* g, int w, int fixture)
+{
+    if (!g || w < 0 || w >= (int)g->worlds.size() || !g->filterFn) return GB_ERR_INVALID;
+    std::vector<unsigned long long> keys((size_t)g->filterCap);
+    std::vector<int> vals((size_t)g->filterCap);
+    GB_CUDA(cudaMemcpy(keys.data(), g->dFilterKeys, g->filterCap * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    GB_CUDA(cudaMemcpy(vals.data(), g->dFilterVals, g->filterCap * sizeof(int), cudaMemcpyDeviceToHost));
+    std::vector<unsigned long long> kk;
+    std::vector<int> vv;
+    for (int i = 0; i < g->filterCap; ++i) {
+        if (keys[i] == ~0ull) continue;
+        const int kw = (int)(keys[i] >> 40), fA = (int)((keys[i] >> 20) & 0xFFFFF), fB = (int)(keys[i] & 0xFFFFF);
+        if (kw == w && (fA == fixture || fB == fixture)) continue;  // decided again when next met
+        kk.push_back(keys[i]);
+        vv.push_back(vals[i]);
+    }
+    gb_status s = BuildFilterTable(g, g->filterCap, kk, vv);
+    if (s != GB_OK) return s;
+    AttachFilter(g);
+    ReleaseGraph(g);
+    return GB_OK;
+}
+
+gb_status gb_world_filter_stats(gb_world* g, long long* replays, int* verdicts)
+{
+    if (!g) return GB_ERR_INVALID;
+    if (replays) *replays = g->filterReplays;
+    if (verdicts) *verdicts = g->filterUsed;
+    return GB_OK;
+}
+
 gb_status gb_world_graph_step(gb_world* g, float dt, int vi, int pi)
 {
     if (!g || vi < 0 || pi < 0 || g->splitOpen) return GB_ERR_INVALID;
+    if (g->filterFn) return gb_world_step(g, dt, vi, pi);  // a filtered step may run again: no graph
     if (g->tuneIndex >= 0) return gb_world_step(g, dt, vi, pi);  // tuning steps are timed one by one
     gb_status s = Upload(g);
     if (s != GB_OK) return s;

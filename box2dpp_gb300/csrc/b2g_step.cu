@@ -68,6 +68,12 @@ struct Wd {
     int* liveProxies;
     int4* pairInfo;
     unsigned char* islTab; // the world's global island-table region (d.islTabBytes bytes)
+    int wIndex;            // the world's index in the batch
+    unsigned long long* filterKeys;  // user contact-filter verdicts (Batch::filterKeys), or nullptr
+    int* filterVals;
+    int filterCap;
+    int* filterMiss;
+    int filterMissCap;
     float4* smemBase;   // the CTA's dynamic shared memory, free outside the island solve
     int smemBytes;
 
@@ -94,6 +100,12 @@ struct Wd {
         evCap = 4 * d.contactCap;
         pairs = B.pairs + q; pairKeep = B.pairKeep + q; pairInfo = B.pairInfo + q;
         islTab = B.islTab ? B.islTab + d.islTabBase : nullptr;
+        wIndex = w;
+        filterKeys = B.filterKeys;
+        filterVals = B.filterVals;
+        filterCap = B.filterCap;
+        filterMiss = B.filterMiss;
+        filterMissCap = B.filterMissCap;
         smemBase = nullptr;
         smemBytes = 0;
     }
@@ -214,11 +226,43 @@ struct Wd {
         return true;
     }
     // default b2ContactFilter::ShouldCollide (Dynamics/b2WorldCallbacks.cpp:26-38)
-    __device__ bool filterCollide(int fA, int fB) const
+    __device__ bool defaultFilter(int fA, int fB) const
     {
         int4 a = ff[fA], b = ff[fB];
         if (a.z == b.z && a.z != 0) return a.z > 0;
         return (a.y & b.x) != 0 && (a.x & b.y) != 0;
+    }
+    // b2ContactFilter::ShouldCollide as the world's filter decides it: the default filter, or the
+    // user filter's verdict for this ordered fixture pair. A pair without a verdict yet is logged for
+    // the host (which asks the user's filter after the step) and takes the default filter's verdict
+    // for now; the host re-runs the step from its start when a logged verdict differs. The probe is
+    // bounded by the table size; a full table is a capacity error.
+    __device__ bool filterCollide(int fA, int fB) const
+    {
+        if (!filterKeys) return defaultFilter(fA, fB);
+        const unsigned long long key = FilterKey(wIndex, fA, fB);
+        unsigned slot = FilterSlot(key, filterCap);
+        for (int probe = 0; probe < filterCap; ++probe, slot = (slot + 1) & (unsigned)(filterCap - 1)) {
+            unsigned long long k = filterKeys[slot];
+            if (k == ~0ull) {
+                k = atomicCAS(&filterKeys[slot], ~0ull, key);
+                if (k == ~0ull) {
+                    const int m = atomicAdd(&filterMiss[0], 1);
+                    if (m < filterMissCap) {
+                        filterMiss[1 + 3 * m] = wIndex;
+                        filterMiss[2 + 3 * m] = fA;
+                        filterMiss[3 + 3 * m] = fB;
+                    }
+                    return defaultFilter(fA, fB);
+                }
+            }
+            if (k == key) {
+                const int v = filterVals[slot];
+                return v == 2 ? defaultFilter(fA, fB) : v != 0;
+            }
+        }
+        atomicOr(&st->error, kErrCapacity);
+        return defaultFilter(fA, fB);
     }
 
     // ---------------------------------------------------------------- manifold IO
@@ -2611,6 +2655,20 @@ __global__ void __launch_bounds__(256, B2G_STEP_MIN_BLOCKS) StepKernel(Batch B, 
     }
 }
 
+// Verdicts of the user contact filter written into the table: keys[i] -> vals[i], one thread per
+// verdict (the keys were inserted by the step that met them).
+__global__ void FilterVerdictKernel(Batch B, const unsigned long long* keys, const int* vals, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long key = keys[i];
+    unsigned slot = FilterSlot(key, B.filterCap);
+    for (int probe = 0; probe < B.filterCap; ++probe, slot = (slot + 1) & (unsigned)(B.filterCap - 1)) {
+        if (B.filterKeys[slot] == key) { B.filterVals[slot] = vals[i]; return; }
+        if (B.filterKeys[slot] == ~0ull) return;
+    }
+}
+
 // Contact changes between the halves of a split step (b2Contact::SetEnabled, SetFriction,
 // SetRestitution, SetTangentSpeed made by a PreSolve listener), in order, one thread.
 __global__ void ContactEditKernel(Batch B, const ContactEdit* edits, int n)
@@ -2731,6 +2789,14 @@ cudaError_t b2gLaunchNarrowphase(const b2g::Batch& B, const int* slotOf, int fir
 {
     if (B.contactRows <= 0) return cudaSuccess;
     b2g::NarrowphaseKernel<<<(B.contactRows + 255) / 256, 256, 0, stream>>>(B, slotOf, first, count);
+    return cudaGetLastError();
+}
+
+cudaError_t b2gLaunchFilterVerdicts(const b2g::Batch& B, const unsigned long long* keys, const int* vals, int n,
+                                    cudaStream_t stream)
+{
+    if (n <= 0) return cudaSuccess;
+    b2g::FilterVerdictKernel<<<(n + 127) / 128, 128, 0, stream>>>(B, keys, vals, n);
     return cudaGetLastError();
 }
 

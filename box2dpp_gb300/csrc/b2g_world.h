@@ -253,7 +253,28 @@ struct Batch {
     int* movedList;  // proxy-sized
     int* liveProxies; // proxy-sized: pair finding's list of live proxies when it is not in shared memory
     unsigned char* islTab; // island-DFS tables of the worlds whose table does not fit in shared memory
+    // A user contact filter (b2World::SetContactFilter): verdicts of b2ContactFilter::ShouldCollide per
+    // (world, fixtureA, fixtureB) in an open-addressing table (filterCap slots, a power of two; key
+    // ~0 empty; value 1 collide, 0 not, 2 not known yet), and the pairs met without a verdict:
+    // filterMiss[0] their count, then (world, fixtureA, fixtureB) triples, at most filterMissCap.
+    // filterKeys == nullptr: the default filter (category, mask, group) runs on the device.
+    unsigned long long* filterKeys;
+    int* filterVals;
+    int filterCap;
+    int* filterMiss;
+    int filterMissCap;
 };
+
+// Key and first probe of a verdict in the contact-filter table (fixtures below 2^20 per world).
+B2G_HD unsigned long long FilterKey(int w, int fA, int fB)
+{
+    return ((unsigned long long)(unsigned)w << 40) | ((unsigned long long)(unsigned)fA << 20) | (unsigned)fB;
+}
+B2G_HD unsigned FilterSlot(unsigned long long key, int cap)
+{
+    unsigned long long h = key * 0x9E3779B97F4A7C15ull;
+    return (unsigned)(h >> 32) & (unsigned)(cap - 1);
+}
 
 // A change to a contact between the halves of a split step (the device copy of gb_contact_edit):
 // contact = position in the world's contact list; flags bit 0 enabled, 1 friction, 2 restitution,

@@ -61,6 +61,23 @@ class World:
     def step(self, dt: float = 1.0 / 60.0, vi: int = 8, pi: int = 3) -> None:
         _lib.check(self.lib.gb_world_step(self.h, dt, vi, pi), "gb_world_step")
 
+    def set_contact_filter(self, should_collide=None) -> None:
+        """b2World::SetContactFilter: should_collide(world, fixtureA, fixtureB) -> bool, or None for
+        the default filter (see gb_world_set_contact_filter)."""
+        if should_collide is None:
+            self._filter_cb = None
+            _lib.check(self.lib.gb_world_set_contact_filter(self.h, _lib.SHOULD_COLLIDE_FN(), None),
+                       "gb_world_set_contact_filter")
+            return
+        self._filter_cb = _lib.SHOULD_COLLIDE_FN(lambda _u, w, a, b: 1 if should_collide(w, a, b) else 0)
+        _lib.check(self.lib.gb_world_set_contact_filter(self.h, self._filter_cb, None), "gb_world_set_contact_filter")
+
+    def filter_stats(self):
+        """(steps run again, verdicts kept) of the user contact filter."""
+        r, v = C.c_longlong(), C.c_int()
+        _lib.check(self.lib.gb_world_filter_stats(self.h, C.byref(r), C.byref(v)), "gb_world_filter_stats")
+        return r.value, v.value
+
     def step_begin(self, dt: float = 1.0 / 60.0, vi: int = 8, pi: int = 3) -> None:
         """First half of a split step: up to and including the collide phase (gb_world_step_begin)."""
         _lib.check(self.lib.gb_world_step_begin(self.h, dt, vi, pi), "gb_world_step_begin")

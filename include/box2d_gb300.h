@@ -179,6 +179,24 @@ gb_status gb_world_step_begin(gb_world* world, float dt, int velocity_iterations
 gb_status gb_contact_edits(gb_world* world, int n, const gb_contact_edit* edits);
 gb_status gb_world_step_end(gb_world* world);
 
+/* b2World::SetContactFilter (Box2D/Dynamics/b2World.cpp:94, b2ContactFilter in b2WorldCallbacks.h:
+ * 52-63): should_collide(user, world, fixtureA, fixtureB) decides, in place of the default
+ * category/mask/group filter, whether the fixtures of a new pair get a contact (b2ContactManager::
+ * AddPair) and whether a contact flagged for filtering survives (b2ContactManager::Collide), with the
+ * reference's ordered fixture pair; nonzero means collide. The verdicts are kept per ordered pair and
+ * asked once: the device uses the default filter's verdict for a pair it meets first, the library asks
+ * the callback after the step, and when an answer differs it restores the state from before the step
+ * (a copy of every device column, kept while a filter is set) and runs the step again, so every step
+ * equals the reference's. Steps with a filter are therefore synchronous (the callback runs on the
+ * calling thread inside gb_world_step), gb_world_graph_step runs plain steps, and the split step is
+ * refused. gb_world_refilter forgets a fixture's verdicts (b2Fixture::Refilter; flag its contacts with
+ * a filter change too). gb_world_filter_stats: steps run again so far and verdicts kept. fn == NULL
+ * restores the default filter. At most 2^20 fixtures per world. */
+typedef int (*gb_should_collide_fn)(void* user, int world, int fixture_a, int fixture_b);
+gb_status gb_world_set_contact_filter(gb_world* world, gb_should_collide_fn fn, void* user);
+gb_status gb_world_refilter(gb_world* world, int w, int fixture);
+gb_status gb_world_filter_stats(gb_world* world, long long* replays, int* verdicts);
+
 gb_status gb_world_sync(gb_world* world);
 
 /* No counterpart in the reference (whose buffers grow on demand). The fixed capacities of the device

@@ -240,6 +240,7 @@ public:
     void* GetUserData() const { return m_def.userData; }
     b2Shape::Type GetType() const { return m_type; }
     float GetRadius() const { return m_radius; }  // the shape's m_radius
+    const b2Filter& GetFilterData() const { return m_def.filter; }
 
 private:
     friend class b2World;
@@ -585,6 +586,19 @@ public:
     virtual void SayGoodbye(b2Joint* joint) = 0;
     virtual void SayGoodbye(b2Fixture* fixture) = 0;
 };
+// b2ContactFilter (Box2D/Dynamics/b2WorldCallbacks.h:52-63); the default is category/mask/group
+// (b2WorldCallbacks.cpp:26-38)
+class b2ContactFilter {
+public:
+    virtual ~b2ContactFilter() = default;
+    virtual bool ShouldCollide(b2Fixture* fixtureA, b2Fixture* fixtureB)
+    {
+        const b2Filter& a = fixtureA->GetFilterData();
+        const b2Filter& b = fixtureB->GetFilterData();
+        if (a.groupIndex == b.groupIndex && a.groupIndex != 0) return a.groupIndex > 0;
+        return (a.maskBits & b.categoryBits) != 0 && (a.categoryBits & b.maskBits) != 0;
+    }
+};
 class b2QueryCallback {
 public:
     virtual ~b2QueryCallback() = default;
@@ -620,6 +634,15 @@ public:
     b2Vec2 GetGravity() const { return m_gravity; }
     void SetContactListener(b2ContactListener* listener) { m_listener = listener; }
     void SetDestructionListener(b2DestructionListener* listener) { m_destruction = listener; }
+    // b2World::SetContactFilter (Box2D/Dynamics/b2World.cpp:94): the filter decides each ordered
+    // fixture pair once (see gb_world_set_contact_filter); with a filter set, Step runs whole (a
+    // PreSolve listener is then notified only)
+    void SetContactFilter(b2ContactFilter* filter)
+    {
+        m_filter = filter;
+        if (!Handle()) return;
+        gb_world_set_contact_filter(m_h, filter ? &b2World::FilterTrampoline : nullptr, this);
+    }
 
     // b2World::DestroyBody (Box2D/Dynamics/b2World.cpp:133-212)
     void DestroyBody(b2Body* body)
@@ -836,6 +859,14 @@ public:
             m_stale = true;
             return;
         }
+        if (m_filter) {
+            if (!m_eventsOn) m_eventsOn = gb_world_set_events(m_h, 1) == GB_OK;
+            ReadContacts();
+            gb_world_step(m_h, timeStep, velocityIterations, positionIterations);
+            m_stale = true;
+            Report(0);
+            return;
+        }
         if (!m_eventsOn) m_eventsOn = gb_world_set_events(m_h, 1) == GB_OK;
         ReadContacts();  // the contacts before the step: destroyed contacts and old manifolds
         if (gb_world_step_begin(m_h, timeStep, velocityIterations, positionIterations) != GB_OK) return;
@@ -943,6 +974,13 @@ public:
     }
 
 private:
+    static int FilterTrampoline(void* user, int, int fixtureA, int fixtureB)
+    {
+        b2World* self = static_cast<b2World*>(user);
+        return self->m_filter->ShouldCollide(self->m_fixtureOfId[fixtureA].first, self->m_fixtureOfId[fixtureB].first)
+                   ? 1
+                   : 0;
+    }
     // one gb_destroy_* call; its listener calls in calls (3 ints each)
     gb_status Destroy(gb_status (*fn)(gb_world*, int, int, int*, int, int*), int index, std::vector<int>& calls)
     {
@@ -1078,6 +1116,7 @@ private:
     gb_world* m_h = nullptr;
     b2ContactListener* m_listener = nullptr;
     b2DestructionListener* m_destruction = nullptr;
+    b2ContactFilter* m_filter = nullptr;
     b2Profile m_profile;
     std::vector<std::unique_ptr<b2Body>> m_bodies;
     std::vector<std::unique_ptr<b2Fixture>> m_fixtures;

@@ -88,6 +88,7 @@ def _declare(lib, p: str) -> None:
     sig["body"] = (C.c_int, [vp, C.c_int, _f32p, C.c_int])
     sig["fixture"] = (C.c_int, [vp, C.c_int, C.c_int, _f32p, C.c_int, _f32p, _i32p])
     sig["set_presolve_rule"] = (None, [vp, _i32p, C.c_int])
+    sig["set_filter_rule"] = (None, [vp, C.c_int, C.c_int])
     for kind in ("body", "joint", "fixture"):
         sig["destroy_" + kind] = (C.c_int, [vp, C.c_int, _i32p, C.c_int])
     if p == "rw_":
@@ -185,6 +186,11 @@ class OracleWorld:
         self.n_fixtures += 1
         return self._fn("fixture")(self.h, int(body), int(type_), s, int(n), np.asarray(mat, dtype=np.float32),
                                    np.asarray(filt, dtype=np.int32))
+
+    def set_filter_rule(self, modulus: int, first_other: int) -> None:
+        """A b2ContactFilter: fixtures below first_other keep the default filter; any other pair
+        collides unless (fixtureA + fixtureB) % modulus == 0."""
+        self._fn("set_filter_rule")(self.h, int(modulus), int(first_other))
 
     def set_presolve_rule(self, bits) -> None:
         """A PreSolve listener applying a rule per fixture pair (bits per fixture: 1 ghost, 2 ice,

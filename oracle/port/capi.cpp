@@ -95,6 +95,12 @@ static int Goodbyes(World* w, int* calls, int cap)
     for (int i = 0; i < n && i < cap; ++i) { calls[2 * i] = w->goodbyes[i].first; calls[2 * i + 1] = w->goodbyes[i].second; }
     return n;
 }
+void po_set_filter_rule(void* h, int modulus, int firstOther)
+{
+    World* w = static_cast<World*>(h);
+    w->filterModulus = modulus;
+    w->filterStatic = firstOther;
+}
 void po_set_presolve_rule(void* h, const int* bits, int n)
 {
     World* w = static_cast<World*>(h);

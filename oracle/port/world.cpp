@@ -462,14 +462,9 @@ void World::AddPair(int proxyA, int proxyB)
         }
     }
     if (!ShouldCollide(bodyB, bodyA)) return;
-    // default b2ContactFilter::ShouldCollide (Dynamics/b2WorldCallbacks.cpp:26-38)
     const Fixture& fa = fixtures[fixtureA];
     const Fixture& fb = fixtures[fixtureB];
-    if (fa.group == fb.group && fa.group != 0) {
-        if (!(fa.group > 0)) return;
-    } else if (!((fa.mask & fb.category) != 0 && (fa.category & fb.mask) != 0)) {
-        return;
-    }
+    if (!FilterShouldCollide(fixtureA, fixtureB)) return;
     bool exists;
     bool primary = PrimaryOrder(fa.shape.type, fb.shape.type, &exists);
     if (!exists) return;
@@ -628,12 +623,7 @@ void World::Collide()
         int bA = fixtures[ct.fA].body, bB = fixtures[ct.fB].body;
         if (ct.flags & kCFilter) {
             bool keep = ShouldCollide(bB, bA);
-            if (keep) {
-                const Fixture& fa = fixtures[ct.fA];
-                const Fixture& fb = fixtures[ct.fB];
-                if (fa.group == fb.group && fa.group != 0) keep = fa.group > 0;
-                else keep = (fa.mask & fb.category) != 0 && (fa.category & fb.mask) != 0;
-            }
+            if (keep) keep = FilterShouldCollide(ct.fA, ct.fB);
             if (!keep) { int nuke = c; c = ct.next; Destroy(nuke); continue; }
             ct.flags &= ~kCFilter;
         }
@@ -2922,6 +2912,27 @@ void World::DestroyFixture(int f)
         fx.next = kNull;
     }
     ResetMassData(bi);
+}
+
+} // namespace b2o
+
+namespace b2o {
+
+// default b2ContactFilter::ShouldCollide (Dynamics/b2WorldCallbacks.cpp:26-38)
+bool World::DefaultFilter(int fA, int fB) const
+{
+    const Fixture& fa = fixtures[fA];
+    const Fixture& fb = fixtures[fB];
+    if (fa.group == fb.group && fa.group != 0) return fa.group > 0;
+    return (fa.mask & fb.category) != 0 && (fa.category & fb.mask) != 0;
+}
+
+// The world's b2ContactFilter: the default, or the test filter (the first filterStatic fixtures keep
+// the default; any other pair collides unless (fixtureA + fixtureB) % filterModulus == 0)
+bool World::FilterShouldCollide(int fA, int fB) const
+{
+    if (filterModulus <= 0 || fA < filterStatic || fB < filterStatic) return DefaultFilter(fA, fB);
+    return (fA + fB) % filterModulus != 0;
 }
 
 } // namespace b2o

@@ -144,6 +144,11 @@ struct World {
     // A PreSolve listener's rule, per fixture: bit 0 ghost, 1 ice, 2 bouncy; a contact between two
     // fixtures sharing a bit is disabled (ghost), gets friction 0 (ice) or restitution 0.9 (bouncy).
     std::vector<int> preSolveRule;
+    // A test b2ContactFilter (filterModulus > 0): fixtures below filterStatic use the default filter;
+    // any other pair collides unless (fixtureA + fixtureB) % filterModulus == 0.
+    int filterModulus = 0, filterStatic = 0;
+    bool DefaultFilter(int fA, int fB) const;
+    bool FilterShouldCollide(int fA, int fB) const;
     // destruction listener calls of the last Destroy* call: {0 joint / 1 fixture, index}
     std::vector<std::pair<int, int>> goodbyes;
     void DestroyBody(int b);

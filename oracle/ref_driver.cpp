@@ -56,9 +56,22 @@ struct PreSolveRule : public b2ContactListener {
     }
 };
 
+// A b2ContactFilter for tests: fixtures below firstOther keep the default filter; any other pair
+// collides unless (fixtureA + fixtureB) % modulus == 0.
+struct FilterRule : public b2ContactFilter {
+    int modulus = 0, firstOther = 0;
+    bool ShouldCollide(b2Fixture* a, b2Fixture* b) override
+    {
+        const int fa = fixture_index(a), fb = fixture_index(b);
+        if (fa < firstOther || fb < firstOther) return b2ContactFilter::ShouldCollide(a, b);
+        return (fa + fb) % modulus != 0;
+    }
+};
+
 struct RefWorld {
     b2World world;
     PreSolveRule rule;
+    FilterRule filter;
     std::vector<b2Body*> bodies;      // creation order; null once destroyed
     std::vector<b2Fixture*> fixtures; // creation order (a chain's children share one); null once destroyed
     std::vector<b2Joint*> joints;     // creation order; null once destroyed
@@ -398,6 +411,13 @@ static int TakeGoodbyes(RefWorld* w, int* calls, int cap)
     for (int i = 0; i < 2 * n && i < 2 * cap; ++i) calls[i] = w->goodbye.calls[i];
     w->goodbye.calls.clear();
     return n;
+}
+void rw_set_filter_rule(void* h, int modulus, int firstOther)
+{
+    RefWorld* w = static_cast<RefWorld*>(h);
+    w->filter.modulus = modulus;
+    w->filter.firstOther = firstOther;
+    w->world.SetContactFilter(&w->filter);
 }
 void rw_set_presolve_rule(void* h, const int* bits, int n)
 {

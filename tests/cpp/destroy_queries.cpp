@@ -169,14 +169,18 @@ int main()
     world.RayCast(&every, b2Vec2(-10.0f, 0.75f), b2Vec2(10.0f, 0.25f));
     std::printf("ray %d %a %a %a %a %a hits %d\n", closest.id, closest.fraction, closest.point.x, closest.point.y,
                 closest.normal.x, closest.normal.y, every.hits);
+    // the world manifold of the first contact in the list that has points (a new contact has none)
     const std::vector<b2Contact*>& contacts = world.GetContactList();
-    if (!contacts.empty()) {
+    for (size_t k = 0; k < contacts.size(); ++k) {
+        const b2Contact* c = contacts[k];
+        if (c->GetManifold()->pointCount == 0) continue;
         b2WorldManifold wm;
-        contacts[0]->GetWorldManifold(&wm);
-        std::printf("manifold %d %d %d %a %a %a %a %a %a %a %a\n", contacts[0]->GetFixtureA()->GetIndex(),
-                    contacts[0]->GetFixtureB()->GetIndex(), contacts[0]->GetManifold()->pointCount, wm.normal.x,
-                    wm.normal.y, wm.points[0].x, wm.points[0].y, wm.points[1].x, wm.points[1].y, wm.separations[0],
+        c->GetWorldManifold(&wm);
+        std::printf("manifold %d %d %d %d %a %a %a %a %a %a %a %a\n", (int)k, c->GetFixtureA()->GetIndex(),
+                    c->GetFixtureB()->GetIndex(), c->GetManifold()->pointCount, wm.normal.x, wm.normal.y,
+                    wm.points[0].x, wm.points[0].y, wm.points[1].x, wm.points[1].y, wm.separations[0],
                     wm.separations[1]);
+        break;
     }
     const b2Profile& prof = world.GetProfile();
     std::printf("profile %d\n", prof.step > 0.0f && prof.solve > 0.0f ? 1 : 0);

@@ -17,6 +17,8 @@ Two builds of the reference are used: ``libm`` (glibc sinf/cosf, the reference a
   ids (freed tree nodes are reused).
 * ``presolve_rule_<trig>.npz``: a drop with a PreSolve listener that disables, de-frictions or
   bounces contacts by a per-fixture rule (tests/_util.py presolve_case), per-step digests.
+* ``filter_rule_<trig>.npz``: a drop with a user b2ContactFilter (walls default; other pairs collide
+  unless (fixtureA + fixtureB) % 5 == 0), per-step digests.
 * ``collide.npz``: seeded shape pairs of every supported type pair with the reference manifolds.
 * ``toi.npz``: seeded sweeps with the reference b2TimeOfImpact result.
 * ``trig.npz``: glibc sinf/cosf on seeded angles (how far the project trig is from libm).
@@ -290,6 +292,17 @@ def main():
                 digests[s - 1] = np.frombuffer(state_digest(w.bodies(), *w.contacts()), dtype=np.uint8)
             np.savez_compressed(os.path.join(HERE, f"presolve_rule_{trig}.npz"), digests=digests, steps=np.int32(300))
         print("wrote presolve_rule")
+    if only in (None, "filter_rule"):
+        sc = scenes.drop(200, scenes.SplitMix64(29))
+        for trig in ("libm", "project"):
+            w = oracle.OracleWorld(sc, "reference", trig)
+            w.set_filter_rule(5, 4)
+            digests = np.zeros((300, 32), dtype=np.uint8)
+            for s in range(1, 301):
+                w.step(DT, VI, PI)
+                digests[s - 1] = np.frombuffer(state_digest(w.bodies(), *w.contacts()), dtype=np.uint8)
+            np.savez_compressed(os.path.join(HERE, f"filter_rule_{trig}.npz"), digests=digests, steps=np.int32(300))
+        print("wrote filter_rule")
     for name, make, steps, script in scripted_cases():
         if only and name != only:
             continue

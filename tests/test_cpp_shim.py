@@ -279,6 +279,7 @@ def _world_manifold(m_ints, m_flts, xa, ra, xb, rb):
     rot = lambda x, v: (f(x[3] * v[0]) - f(x[2] * v[1]), f(x[2] * v[0]) + f(x[3] * v[1]))
     dot = lambda a, b: f(a[0] * b[0]) + f(a[1] * b[1])
     kind, count = int(m_ints[4]), int(m_ints[3])
+    assert count > 0  # Initialize returns at once for an empty manifold
     ln, lp = (m_flts[0], m_flts[1]), (m_flts[2], m_flts[3])
     pts = [(m_flts[4], m_flts[5]), (m_flts[8], m_flts[9])]
     pts_out, seps = [(f(0), f(0)), (f(0), f(0))], [f(0), f(0)]
@@ -389,6 +390,9 @@ def test_cpp_destroy_queries_match_oracle(gpu, tmp_path):
     assert np.array_equal(got.view(np.uint32), hit[0].view(np.uint32))
     ci, cf = o.contacts()
     m = out["manifold"]
+    k = int(m[0])
+    assert k == int(np.argmax(ci[:, 3] > 0))
+    ci, cf, m = ci[k:], cf[k:], m[1:]
     assert [int(m[0]), int(m[1]), int(m[2])] == [int(ci[0, 0]), int(ci[0, 1]), int(ci[0, 3])]
     fx_body = {f: b for f, b in enumerate(sc.arrays()["fix_body"])}
     fx_body[14] = 13  # the body created after the destructions

@@ -138,3 +138,22 @@ def test_port_presolve_rule_matches_reference(trig):
             if trig == "libm" and platform.machine() != "x86_64":
                 pytest.skip("libm trig differs on this machine")
             raise AssertionError(f"first divergence at step {s}")
+
+
+@pytest.mark.parametrize("trig", ["project", "libm"])
+def test_port_contact_filter_matches_reference(trig):
+    """A user b2ContactFilter (walls default; other pairs collide unless (fA + fB) % 5 == 0)."""
+    import platform
+
+    from box2dpp_gb300 import scenes
+    from tests._util import digest
+
+    g = golden(f"filter_rule_{trig}")
+    w = oracle.OracleWorld(scenes.drop(200, scenes.SplitMix64(29)), "port", trig)
+    w.set_filter_rule(5, 4)
+    for s in range(1, int(g["steps"]) + 1):
+        w.step()
+        if not np.array_equal(digest(w.bodies(), *w.contacts()), g["digests"][s - 1]):
+            if trig == "libm" and platform.machine() != "x86_64":
+                pytest.skip("libm trig differs on this machine")
+            raise AssertionError(f"first divergence at step {s}")
