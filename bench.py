@@ -172,11 +172,12 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-# DRAM bytes (read + write) per algorithmic byte of StepKernel, from one full ncu capture per solver
-# of the 1024-world case of this workload (coloured: 111.0 MB read + 80.6 MB written; plain: 114.6 MB
-# + 82.2 MB; 41.4 MB algorithmic); traffic grows with the units processed, so the full launch's
-# traffic is this ratio x its algorithmic bytes.
-TRAFFIC_PER_ALGORITHMIC_BYTE = {"coloured": 191.6 / 41.4, "plain": 196.7 / 41.4}
+# DRAM bytes (read + write) per algorithmic byte of StepKernel, from a full ncu capture per solver of
+# one step of the 1024-world case of this workload (coloured, all four classes of the tuned plan:
+# 84.6 MB read + 17.4 MB written for 42.0 MB algorithmic; plain, default plan: 114.6 MB + 82.2 MB for
+# 41.4 MB); traffic grows with the units processed, so the full launch's traffic is this ratio x its
+# algorithmic bytes.
+TRAFFIC_PER_ALGORITHMIC_BYTE = {"coloured": 102.0 / 42.0, "plain": 196.7 / 41.4}
 
 
 def algorithmic_bytes(t: dict) -> int:
