@@ -71,10 +71,12 @@ def dist_env():
 
 
 def workload(args, rank: int, allow_sleep: bool = False):
-    """This rank's shard: its own args.worlds worlds (weak scaling, no data-path collective)."""
+    """This rank's shard: its part, by estimated cost, of the job's args.worlds worlds per rank (weak
+    scaling, no data-path collective)."""
     from box2dpp_gb300 import shard
 
-    return shard.shard_workload(args.worlds, args.seed, rank, allow_sleep=allow_sleep)
+    _, world_size, _ = dist_env()
+    return shard.shard_workload(args.worlds, args.seed, rank, allow_sleep=allow_sleep, world_size=world_size)
 
 
 def config_dict(args, worlds):

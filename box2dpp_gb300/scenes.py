@@ -672,25 +672,35 @@ def config4(n_worlds: int, first_seed: int, n_bodies: int = 256, allow_sleep: bo
     return [drop(n_bodies, SplitMix64(first_seed + k), allow_sleep=allow_sleep) for k in range(n_worlds)]
 
 
+def config3_specs(n_worlds: int = 4096, seed: int = 1, min_bodies: int = 16, max_bodies: int = 512) -> list:
+    """The batched workload's worlds as (body count, kind, sub-seed) triples, cheap to draw: the body
+    count log-uniform in [min, max], the kind among pyramid (0) / stacks (1) / drop (2)."""
+    rng = SplitMix64(seed)
+    specs = []
+    for _ in range(n_worlds):
+        n = int(round(math.exp(rng.uniform(math.log(min_bodies), math.log(max_bodies)))))
+        kind = rng.randint(0, 2)
+        specs.append((n, kind, rng.next_u64()))
+    return specs
+
+
+def config3_world(spec, allow_sleep: bool = True) -> Scene:
+    """One world of the batched workload from its (body count, kind, sub-seed) spec."""
+    n, kind, sub_seed = spec
+    sub = SplitMix64(sub_seed)
+    if kind == 0:
+        rows = max(1, int((math.sqrt(8 * n + 1) - 1) // 2))
+        return pyramid(rows, allow_sleep=allow_sleep)
+    if kind == 1:
+        return stacks(n, sub, allow_sleep=allow_sleep)
+    return drop(n, sub, allow_sleep=allow_sleep)
+
+
 def config3(n_worlds: int = 4096, seed: int = 1, allow_sleep: bool = True, min_bodies: int = 16,
             max_bodies: int = 512) -> list:
     """Independent worlds with log-uniform body counts in [min, max] and a seeded kind among
     pyramid / stacks / drop (dt 1/60, 8/3 iterations, 600 steps)."""
-    rng = SplitMix64(seed)
-    worlds = []
-    for w in range(n_worlds):
-        n = int(round(math.exp(rng.uniform(math.log(min_bodies), math.log(max_bodies)))))
-        kind = rng.randint(0, 2)
-        sub = SplitMix64(rng.next_u64())
-        if kind == 0:
-            rows = max(1, int((math.sqrt(8 * n + 1) - 1) // 2))
-            sc = pyramid(rows, allow_sleep=allow_sleep)
-        elif kind == 1:
-            sc = stacks(n, sub, allow_sleep=allow_sleep)
-        else:
-            sc = drop(n, sub, allow_sleep=allow_sleep)
-        worlds.append(sc)
-    return worlds
+    return [config3_world(sp, allow_sleep) for sp in config3_specs(n_worlds, seed, min_bodies, max_bodies)]
 
 
 def config5(n_bodies: int = 65536, n_chains: int = 512, links: int = 16, half: float = 150.0, seed: int = 1,

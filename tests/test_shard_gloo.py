@@ -1,5 +1,6 @@
-"""The N > 1 path of the batched workload on CPU: two gloo ranks, each stepping its own shard with
-the CPU oracle (no GPU), aggregated the way bench.py aggregates its ranks."""
+"""The N > 1 path of the batched workload on CPU: two gloo ranks, each stepping its part of one world
+set with the CPU oracle (no GPU), aggregated the way bench.py aggregates its ranks; the cost
+partition covers every world once and balances the ranks' body counts."""
 from __future__ import annotations
 
 import os
@@ -31,8 +32,10 @@ def _rank_main(rank, world_size, port, out):
 
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world_size)
-    worlds = shard.shard_workload(6, seed=1, rank=rank)
-    names = [w.name for w in worlds]
+    from box2dpp_gb300 import scenes
+
+    worlds = shard.shard_workload(3, seed=1, rank=rank, world_size=world_size)
+    names = shard.shard_indices(scenes.config3_specs(3 * world_size, seed=1), rank, world_size)
     bodies = sum(w.dynamic_count for w in worlds)
     ws = [oracle.OracleWorld(w, "port", "project") for w in worlds]
     dist.barrier()
@@ -62,20 +65,52 @@ def test_two_rank_shards_are_disjoint_and_aggregate():
         p.join(timeout=600)
         assert p.exitcode == 0
     r0, r1 = out[0], out[1]
-    assert r0[0] != r1[0]                                      # disjoint shards (different worlds)
+    assert sorted(r0[0] + r1[0]) == list(range(6))             # every world on exactly one rank
     assert r0[5] == r1[5] == r0[1] + r1[1]                     # bodies summed over ranks
     assert r0[4] == r1[4] == max(r0[2], r1[2])                 # slowest rank's time
     assert abs(r0[3] - (r0[1] + r1[1]) * 3 / max(r0[2], r1[2])) < 1e-6 * r0[3]
     assert r0[3] == r1[3]
 
 
-def test_shard_seeds_are_reproducible():
+def _shard():
     import sys
 
     sys.path.insert(0, ROOT)
     from box2dpp_gb300 import shard
 
-    a = [w.name for w in shard.shard_workload(5, 3, 1)]
-    b = [w.name for w in shard.shard_workload(5, 3, 1)]
-    c = [w.name for w in shard.shard_workload(5, 3, 0)]
+    return shard
+
+
+def test_partition_covers_each_world_once_and_balances():
+    from box2dpp_gb300 import scenes
+
+    shard = _shard()
+    specs = scenes.config3_specs(4 * 512, seed=1)
+    costs = [sp[0] for sp in specs]
+    for n in (1, 2, 4, 8):
+        parts = shard.partition_by_cost(costs, n)
+        flat = sorted(i for p in parts for i in p)
+        assert flat == list(range(len(costs)))
+        assert all(p == sorted(p) for p in parts)
+        loads = [sum(costs[i] for i in p) for p in parts]
+        # greedy largest-first: the spread is at most the largest single cost
+        assert max(loads) - min(loads) <= max(costs)
+        assert max(loads) <= sum(costs) / n * 1.01
+
+
+def test_partition_is_deterministic_with_ties_to_the_lowest_rank():
+    shard = _shard()
+    assert shard.partition_by_cost([5, 5, 5, 5], 2) == [[0, 2], [1, 3]]
+    assert shard.partition_by_cost([1, 9, 4, 4], 2) == [[1], [0, 2, 3]]
+    assert shard.partition_by_cost([], 3) == [[], [], []]
+
+
+def test_one_rank_is_the_whole_world_set_in_order():
+    from box2dpp_gb300 import scenes
+
+    shard = _shard()
+    assert [w.name for w in shard.shard_workload(40, 3, 0)] == [w.name for w in scenes.config3(40, seed=3, allow_sleep=False)]
+    a = [w.name for w in shard.shard_workload(20, 3, 1, world_size=2)]
+    b = [w.name for w in shard.shard_workload(20, 3, 1, world_size=2)]
+    c = [w.name for w in shard.shard_workload(20, 3, 0, world_size=2)]
     assert a == b and a != c
