@@ -13,6 +13,10 @@ arms.plain: the reference-order solver (bit-exact with the reference), 8/3 itera
 velocity residual at the last timed step is the accuracy every other arm must reach.
 arms.coloured: the graph-coloured island solver at the fewest velocity iterations (of COLOURED_VI)
 whose median residual is no larger than plain's (coloured_search lists each try).
+arms.learned: the reference-order solver with the learned warm start (a network trained first by the
+library's kernels on the plain solver's converged impulses, logged from held-out worlds of the same
+workload), at the fewest velocity iterations (of LEARNED_VI) whose median residual is no larger than
+plain's (learned_search lists each try; no arm when none qualifies).
 value: the faster of those arms (headline names it): device time of the K timed steps, each step
 replayed from a captured CUDA graph, CUDA events on the stream the step runs on, state resident in
 HBM (several hundred MB, larger than L2, so no flush between steps).
@@ -46,6 +50,10 @@ PRE_STEPS = 24
 # velocity iterations tried for the graph-coloured solver, fewest first, until its median residual
 # matches the reference-order solver's
 COLOURED_VI = (8, 10, 12, 16, 20, 24, 32)
+# velocity iterations tried for the reference-order solver with the learned warm start
+LEARNED_VI = (4, 5, 6, 7, 8)
+# the learned warm start's training: held-out worlds (seed offset), logged steps, Adam steps
+LEARN_SEED_OFFSET, LEARN_WORLDS, LEARN_LOG_STEPS, LEARN_LOG_VI, LEARN_TRAIN_STEPS = 1000, 512, 8, 40, 3000
 METRIC = "body-steps/sec at fixed residual (batched worlds)"
 UNIT = "body-steps/s"
 
@@ -61,6 +69,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-coloured", action="store_true", help="measure the reference-order solver only")
     p.add_argument("--no-sleep-on", action="store_true", help="skip the sleep-on line")
+    p.add_argument("--no-learned", action="store_true", help="skip the learned warm-start arm")
     return p.parse_args()
 
 
@@ -93,7 +102,7 @@ def config_dict(args, worlds):
         "accuracy": "matched: median velocity residual no larger than the reference-order solver's at 8/3 "
                     "iterations",
         "l2": "state resident in HBM is larger than the 129 MB L2; no flush between steps",
-        "parallelism": "independent worlds sharded across GPUs, no collective",
+        "parallelism": "one world set partitioned across GPUs by body count, no collective",
     }
 
 
@@ -255,16 +264,18 @@ def _timed_steps(w, stream, steps: int, vi: int):
     return start.elapsed_time(end)
 
 
-def _prepare(worlds, stream, solver: str, vi: int, warmup: int, plan=None):
-    """World batch on the GPU with the given solver, advanced to the timed window: PRE_STEPS steps
-    (the online autotuner picks the launch plan during them unless a plan is given) and `warmup`
-    graph-replayed steps."""
+def _prepare(worlds, stream, solver: str, vi: int, warmup: int, plan=None, mlp=None):
+    """World batch on the GPU with the given solver (and learned warm start, with a network),
+    advanced to the timed window: PRE_STEPS steps (the online autotuner picks the launch plan during
+    them unless a plan is given) and `warmup` graph-replayed steps."""
     from box2dpp_gb300.world import World
 
     w = World(worlds)
     w.set_stream(stream.cuda_stream)
     w.set_solver(solver, measure_residual=True)
     w.upload()
+    if mlp is not None:
+        w.set_warm_start(mlp)
     if plan is None:
         w.autotune(2)
     else:
@@ -279,14 +290,46 @@ def _prepare(worlds, stream, solver: str, vi: int, warmup: int, plan=None):
     return w
 
 
-def _e2e(worlds, stream, solver: str, vi: int, plan, args, clk, max_over_ranks, barrier):
+def train_learned(args):
+    """The learned warm start's network, trained by the library's kernels: the plain solver's final
+    impulses at LEARN_LOG_VI velocity iterations, logged for LEARN_LOG_STEPS steps after PRE_STEPS
+    steps on LEARN_WORLDS held-out worlds of the workload (another seed), at the points the reference
+    warm start leaves cold. Returns (network, points trained on, seconds)."""
+    import numpy as np
+
+    from box2dpp_gb300 import shard
+    from box2dpp_gb300.learn import Mlp
+    from box2dpp_gb300.train_warmstart import cold_points, correction_targets
+    from box2dpp_gb300.world import World
+
+    t0 = time.perf_counter()
+    w = World(shard.shard_workload(LEARN_WORLDS, args.seed + LEARN_SEED_OFFSET, 0))
+    w.set_solver("plain")
+    for _ in range(PRE_STEPS):
+        w.step(DT, VI, PI)
+    w.set_contact_log(1_000_000)
+    xs, ts = [], []
+    for _ in range(LEARN_LOG_STEPS):
+        w.step(DT, LEARN_LOG_VI, PI)
+        x, t = w.read_contact_log()
+        xs.append(x.copy())
+        ts.append(t.copy())
+    w.close()
+    x, t = cold_points(np.concatenate(xs), np.concatenate(ts))
+    m = Mlp(1)
+    m.fit_normaliser(x)
+    m.train(x, correction_targets(x, t), steps=LEARN_TRAIN_STEPS, batch=min(65536, len(x)), lr=1e-3, seed=1)
+    return m, len(x), time.perf_counter() - t0
+
+
+def _e2e(worlds, stream, solver: str, vi: int, plan, args, clk, max_over_ranks, barrier, mlp=None):
     """The same K steps end to end through the C-ABI with pinned host buffers: a handle on the same
     worlds with the given plan, advanced through the same steps, then per step gb_set_forces (every
     body's force and torque from pinned host memory), gb_world_graph_step and gb_get_transforms
     (every body's transform into pinned host memory), wall-clock timed."""
     import torch
 
-    we = _prepare(worlds, stream, solver, vi, args.warmup, plan)
+    we = _prepare(worlds, stream, solver, vi, args.warmup, plan, mlp)
     nb = we.total_bodies
     forces = torch.zeros((nb, 4), dtype=torch.float32).pin_memory()
     xforms = torch.zeros((nb, 4), dtype=torch.float32).pin_memory()
@@ -333,9 +376,9 @@ def run_gpu(args):
     total_bodies = n_dyn * world_size
     clk = ClockSampler(local)
 
-    def device_arm(solver: str, vi: int, plan=None):
+    def device_arm(solver: str, vi: int, plan=None, mlp=None):
         """K timed steps of one solver; (record, handle) with the handle kept for the stage times."""
-        w = _prepare(worlds, stream, solver, vi, args.warmup, plan)
+        w = _prepare(worlds, stream, solver, vi, args.warmup, plan, mlp)
         t_before = w.totals()
         barrier()
         with clk:
@@ -345,7 +388,8 @@ def run_gpu(args):
         t_after = w.totals()
         _, _, res = w.solver_stats()
         chosen, cand_ms = w.launch_plan()
-        rec = {"solver": solver, "velocity_iterations": vi, "value": total_bodies * args.steps / (ms / 1e3),
+        rec = {"solver": solver, "warm_start": "reference" if mlp is None else "learned", "velocity_iterations": vi,
+               "value": total_bodies * args.steps / (ms / 1e3),
                "unit": UNIT, "ms_per_step": ms / args.steps, "residual_median": float(np.median(res)),
                "launch_plan": chosen.tolist(), "autotune_candidate_ms": [round(float(x), 3) for x in cand_ms],
                "counts_per_step": {k: (t_before[k] + t_after[k]) / 2.0 for k in
@@ -371,6 +415,27 @@ def run_gpu(args):
                 arms["coloured"] = (rec, wc)
                 break
             wc.close()
+    # 3. the reference-order solver with the learned warm start at the fewest velocity iterations whose
+    #    median residual is no larger than the plain solver's
+    learned_search = []
+    learned_info = None
+    mlps = {}
+    if not args.no_learned:
+        mlp, n_points, train_s = train_learned(args)
+        learned_info = {"points_trained": n_points, "seconds": round(train_s, 1), "train_steps": LEARN_TRAIN_STEPS,
+                        "worlds": LEARN_WORLDS, "seed": args.seed + LEARN_SEED_OFFSET}
+        plain_plan = np.asarray(plain["launch_plan"], dtype=np.int32)
+        for vi in LEARNED_VI:
+            rec, wl = device_arm("plain", vi, plain_plan, mlp)
+            used, _ = wl.warm_stats()
+            searched_rec = {"velocity_iterations": vi, "residual_median": rec["residual_median"],
+                            "ms_per_step": rec["ms_per_step"], "islands_keeping_prediction": int(used.sum())}
+            learned_search.append(searched_rec)
+            if rec["residual_median"] <= plain["residual_median"]:
+                arms["learned"] = (rec, wl)
+                mlps["learned"] = mlp
+                break
+            wl.close()
     # the headline: the fastest arm at matched accuracy (plain always qualifies)
     head_name = max(arms, key=lambda k: arms[k][0]["value"])
     head, wh = arms[head_name]
@@ -388,7 +453,8 @@ def run_gpu(args):
     # end to end through the C-ABI, for every arm
     for name, (rec, _) in arms.items():
         e2e_s, nb = _e2e(worlds, stream, rec["solver"], rec["velocity_iterations"],
-                         np.asarray(rec["launch_plan"], dtype=np.int32), args, clk, max_over_ranks, barrier)
+                         np.asarray(rec["launch_plan"], dtype=np.int32), args, clk, max_over_ranks, barrier,
+                         mlps.get(name))
         rec["e2e"] = {"value": total_bodies * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nb * 16,
                       "d2h_bytes_per_step": nb * 16,
                       "calls": "gb_set_forces + gb_world_graph_step + gb_get_transforms per step, pinned host "
@@ -398,7 +464,7 @@ def run_gpu(args):
     if not args.no_sleep_on:
         worlds_sleep = workload(args, rank, allow_sleep=True)
         ws = _prepare(worlds_sleep, stream, head["solver"], head["velocity_iterations"], args.warmup,
-                      np.asarray(head["launch_plan"], dtype=np.int32))
+                      np.asarray(head["launch_plan"], dtype=np.int32), mlps.get(head_name))
         barrier()
         with clk:
             ms_s = max_over_ranks(_timed_steps(ws, stream, args.steps, head["velocity_iterations"]))
@@ -433,12 +499,15 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": config_dict(args, worlds),
-            "headline": {"solver": head["solver"], "velocity_iterations": head["velocity_iterations"],
+            "headline": {"solver": head["solver"], "warm_start": head["warm_start"],
+                         "velocity_iterations": head["velocity_iterations"],
                          "residual_median": head["residual_median"],
                          "rule": "the fastest arm whose median velocity residual is no larger than the reference-"
                                  "order solver's at 8 iterations (that solver is bit-exact with the reference)"},
             "arms": {k: r for k, (r, _) in arms.items()},
             "coloured_search": searched,
+            "learned_search": learned_search,
+            "learned_training": learned_info,
             "residual_definition": "max over contact points of the natural-map residual in m/s: |vn - bias| on "
                                    "active normal points, |vt| on friction inside its cone, 0 at a solution; after "
                                    "the velocity iterations; median over worlds at the last timed step",

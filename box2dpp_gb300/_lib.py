@@ -15,7 +15,7 @@ from . import build as _build
 GB_OK, GB_ERR_CAPACITY, GB_ERR_TIMEOUT, GB_ERR_INVALID, GB_ERR_CUDA = 0, 1, 2, 3, 4
 COLLIDE_NOALLOC_MAX_PAIRS = 4096  # GB_COLLIDE_NOALLOC_MAX_PAIRS
 SOLVER_PLAIN, SOLVER_COLOURED = 0, 1
-WARM_REFERENCE, WARM_LEARNED = 0, 1
+WARM_REFERENCE, WARM_LEARNED, WARM_LEARNED_ALL = 0, 1, 2
 STATUS_NAMES = {0: "GB_OK", 1: "GB_ERR_CAPACITY", 2: "GB_ERR_TIMEOUT", 3: "GB_ERR_INVALID", 4: "GB_ERR_CUDA"}
 
 # Every symbol include/box2d_gb300.h declares.

@@ -1763,9 +1763,10 @@ gb_status gb_world_set_solver(gb_world* g, int solver, float tolerance, int meas
 
 gb_status gb_world_set_warm_start(gb_world* g, gb_mlp* mlp, int mode)
 {
-    if (!g || (mode != kWarmReference && mode != kWarmLearned) || (mode == kWarmLearned && !mlp)) return GB_ERR_INVALID;
+    if (!g || mode < kWarmReference || mode > kWarmLearnedAll || (mode != kWarmReference && !mlp)) return GB_ERR_INVALID;
     g->warmMode = mode;
-    g->mlp = mode == kWarmLearned ? b2gMlpView(mlp) : MlpView{};
+    g->mlp = mode != kWarmReference ? b2gMlpView(mlp) : MlpView{};
+    ReleaseGraph(g);  // a captured step holds the previous network's view
     return GB_OK;
 }
 

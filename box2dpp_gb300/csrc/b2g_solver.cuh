@@ -1819,9 +1819,10 @@ __device__ void PointFeatures(const VelConstraint& v, const float4 imp, const fl
 // contacts, 2 points each) per warp at a time; rows of absent points are zero and ignored. The
 // outputs are corrections to the reference warm start in velocity units: normal impulse
 // max(0, ref + y0 * normalMass), tangent impulse ref + y1 * tangentMass clamped to the friction
-// cone (an output of zero reproduces the reference warm start). Points the reference starts warm
-// (a positive normal impulse carried over) keep it: the network is used where the reference has
-// nothing to offer, new or previously inactive points.
+// cone (an output of zero reproduces the reference warm start). With kWarmLearned, points the
+// reference starts warm (a positive normal impulse carried over) keep it: the network is used where
+// the reference has nothing to offer, new or previously inactive points; kWarmLearnedAll corrects
+// every point.
 __device__ __noinline__ void Wd::learnedImpulses(const StepParams& P, int nContacts, const float4* imp, const float4* vel)
 {
     __shared__ __align__(16) __nv_bfloat16 xTile[kMaxCta / 32][16 * kMlpInPad];
@@ -1859,7 +1860,7 @@ __device__ __noinline__ void Wd::learnedImpulses(const StepParams& P, int nConta
                 const float4 ref = imp[i];
                 const float niRef = j == 0 ? ref.x : ref.z, tiRef = j == 0 ? ref.y : ref.w;
                 float ni = niRef, ti = tiRef;
-                if (!(niRef > 0.0f)) {
+                if (P.warmMode == kWarmLearnedAll || !(niRef > 0.0f)) {
                     ni = fmaxf(0.0f, niRef + out[2 * h] * c.x);
                     const float bound = v.nf.z * ni;
                     ti = fminf(fmaxf(tiRef + out[2 * h + 1] * c.y, -bound), bound);
@@ -1916,7 +1917,7 @@ __device__ void Wd::solveIslands(const StepParams& P, int nIsl, int nRows, int n
     const float gx = st->gx, gy = st->gy;
     const bool rowsInSmem = nRows <= smemRows;
     const bool coloured = colourStart != nullptr;
-    const bool learned = P.warmMode == kWarmLearned && warm;
+    const bool learned = (P.warmMode == kWarmLearned || P.warmMode == kWarmLearnedAll) && warm;
     const bool logging = P.logX != nullptr && !coloured;
     const bool needSep = learned || logging;
     // island of each island contact during the learned warm-start choice (contact-sized scratch that

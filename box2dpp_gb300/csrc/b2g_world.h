@@ -297,7 +297,7 @@ struct BodyEdit {
 // (bit-exact with the reference). kSolverColoured solves the same constraints colour by colour: the
 // constraints of one colour share no dynamic body and are solved in parallel across the CTA.
 enum : int { kSolverPlain = 0, kSolverColoured = 1 };
-enum : int { kWarmReference = 0, kWarmLearned = 1 };
+enum : int { kWarmReference = 0, kWarmLearned = 1, kWarmLearnedAll = 2 };
 // b2ContactListener calls (Dynamics/b2WorldCallbacks.h:84-130) as event log kinds
 enum : int { kEvBegin = 0, kEvEnd = 1, kEvPreSolve = 2, kEvPostSolve = 3 };
 // Colours 0..62 are solved in parallel; colour 63 collects the constraints for which no colour was
@@ -320,7 +320,7 @@ struct StepParams {
     int recordEvents;   // 1: record the listener calls of the step in the event log
     int phase;          // 0 the whole step; 1 up to the collide phase; 2 the rest (a step split for a
                         // PreSolve that changes contacts)
-    int warmMode;       // kWarmReference, or kWarmLearned (the network below, reference as fallback)
+    int warmMode;       // kWarmReference, kWarmLearned or kWarmLearnedAll (the network below, reference as fallback)
     MlpView mlp;
     // contact-point log (plain solver): features at the start of the velocity solve, then the
     // scaled impulses the velocity iterations end with; logX == nullptr disables it

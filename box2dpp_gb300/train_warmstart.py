@@ -9,7 +9,9 @@
    features at the start of the velocity solve and the impulses the iterations end with (in velocity
    units); the network learns the difference between those and the reference warm start.
 2. Training: the library's tensor-core kernels, Adam for ``--steps`` steps on batches of ``--batch``
-   points drawn from the log.
+   points drawn from the log: the points the reference warm start leaves cold (``--points cold``, the
+   network then predicts only those), or every point (``--points all``, the network corrects every
+   point's reference warm start).
 3. Evaluation on other seeds: first the plain solver with the reference warm start at 8 velocity
    iterations gives the residual the reference reaches (the median over the evaluation worlds and
    steps: the benchmark's matched accuracy); then the plain solver with that residual as its
@@ -70,7 +72,7 @@ def cold_points(x: np.ndarray, t: np.ndarray):
 
 
 def iterations_to_tolerance(mlp, first_seed: int, n_seeds: int, bodies: int, settle: int, steps: int, tol: float,
-                            max_vi: int):
+                            max_vi: int, all_points: bool = False):
     """Mean velocity iterations per island contact the plain solver runs to reach tol (at most
     max_vi), the share of islands that kept the learned prediction (None without a network) and the
     median residual the iterations end with."""
@@ -81,7 +83,7 @@ def iterations_to_tolerance(mlp, first_seed: int, n_seeds: int, bodies: int, set
     w.set_solver("plain", tolerance=tol, measure_residual=True)
     for _ in range(settle):
         w.step(DT, 8, PI)
-    w.set_warm_start(mlp)
+    w.set_warm_start(mlp, all_points)
     its = contacts = isl = kept = 0
     res = []
     for _ in range(steps):
@@ -130,6 +132,8 @@ def main():
     ap.add_argument("--eval-steps", type=int, default=30)
     ap.add_argument("--tol", type=float, default=0.0, help="> 0: this target instead of the measured one")
     ap.add_argument("--max-vi", type=int, default=64)
+    ap.add_argument("--points", default="cold", choices=["cold", "all"],
+                    help="train on (and predict) the cold points only, or every point")
     ap.add_argument("--out", default=DEFAULT_OUT)
     args = ap.parse_args()
 
@@ -139,7 +143,9 @@ def main():
     x, t = log_points(args.first_seed, args.seeds, args.bodies, args.settle, args.log_steps, args.log_vi)
     t_log = time.time() - t0
     n_logged = len(x)
-    x, t = cold_points(x, t)
+    all_points = args.points == "all"
+    if not all_points:
+        x, t = cold_points(x, t)
     m = Mlp(1)
     m.fit_normaliser(x)
     t0 = time.time()
@@ -150,9 +156,9 @@ def main():
     ref_its, _, ref_res = iterations_to_tolerance(None, args.eval_first_seed, args.eval_seeds, args.bodies,
                                                   args.settle, args.eval_steps, target, args.max_vi)
     lrn_its, used, lrn_res = iterations_to_tolerance(m, args.eval_first_seed, args.eval_seeds, args.bodies,
-                                                     args.settle, args.eval_steps, target, args.max_vi)
+                                                     args.settle, args.eval_steps, target, args.max_vi, all_points)
     report = {
-        "points_logged": int(n_logged), "points_cold": int(len(x)), "log_seconds": round(t_log, 1), "train_steps": args.steps, "batch": args.batch,
+        "points_logged": int(n_logged), "points_trained": int(len(x)), "points": args.points, "log_seconds": round(t_log, 1), "train_steps": args.steps, "batch": args.batch,
         "train_seconds": round(t_train, 1), "loss_first": float(losses[:10].mean()),
         "loss_last": float(losses[-100:].mean()), "tolerance": target,
         "tolerance_rule": "given" if args.tol > 0 else "median residual of the reference warm start after 8 iterations",

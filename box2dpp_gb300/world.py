@@ -182,13 +182,15 @@ class World:
         arr = np.ascontiguousarray(np.asarray(classes, dtype=np.int32).reshape(-1, 5))
         _lib.check(self.lib.gb_world_set_launch_plan(self.h, arr.reshape(-1), len(arr)), "gb_world_set_launch_plan")
 
-    def set_warm_start(self, mlp=None) -> None:
+    def set_warm_start(self, mlp=None, all_points: bool = False) -> None:
         """Learned warm start with the given network (reference warm start as fallback); None: the
-        reference warm start only. The network must outlive its use by this world."""
+        reference warm start only. all_points: the network corrects every contact point, not only
+        the ones the reference starts cold. The network must outlive its use by this world."""
         if mlp is None:
             _lib.check(self.lib.gb_world_set_warm_start(self.h, None, _lib.WARM_REFERENCE), "gb_world_set_warm_start")
         else:
-            _lib.check(self.lib.gb_world_set_warm_start(self.h, mlp.h, _lib.WARM_LEARNED), "gb_world_set_warm_start")
+            mode = _lib.WARM_LEARNED_ALL if all_points else _lib.WARM_LEARNED
+            _lib.check(self.lib.gb_world_set_warm_start(self.h, mlp.h, mode), "gb_world_set_warm_start")
         self._mlp = mlp
 
     def warm_stats(self):

@@ -446,12 +446,14 @@ gb_status gb_mlp_train(gb_mlp* mlp, const float* x, const float* t, int n, int s
  * effective mass, are corrections added to the reference warm-start impulses (the normal result
  * clamped at 0, the tangent one to the friction cone), applied at the points the reference starts
  * cold (no normal impulse carried over); the network is trained on such logged points, on the final
- * impulses minus the reference warm start (t - x[9..10] in the log's units).
+ * impulses minus the reference warm start (t - x[9..10] in the log's units). GB_WARM_LEARNED_ALL
+ * applies the corrections at every point (a network trained on all logged points).
  * Each world then warm-starts its velocities both ways and keeps the one whose velocity residual is
  * smaller, island by island (islands share no dynamic body), so an island falls back to the reference
  * warm start whenever the prediction is worse. The network must outlive its use by the world. */
 #define GB_WARM_REFERENCE 0
 #define GB_WARM_LEARNED 1
+#define GB_WARM_LEARNED_ALL 2
 gb_status gb_world_set_warm_start(gb_world* world, gb_mlp* mlp, int mode);
 /* Per world of the last step (arrays of n_worlds, each may be NULL): islands that kept the learned
  * warm start, and the contact-iterations of the velocity solve (each island's iterations times its

@@ -35,7 +35,7 @@ def _log(seed, n_worlds, steps):
 _TARGET = {}
 
 
-def _iterations(mlp, seed):
+def _iterations(mlp, seed, all_points=False):
     """Iterations per island contact to reach the residual the reference warm start reaches in 8
     iterations on the same worlds (the matched accuracy), and the share of islands keeping the
     learned start."""
@@ -43,7 +43,7 @@ def _iterations(mlp, seed):
 
     if seed not in _TARGET:
         _TARGET[seed] = reference_residual(seed, 32, 120, 40, 30)
-    its, kept, _ = iterations_to_tolerance(mlp, seed, 32, 120, 40, 30, _TARGET[seed], MAX_VI)
+    its, kept, _ = iterations_to_tolerance(mlp, seed, 32, 120, 40, 30, _TARGET[seed], MAX_VI, all_points)
     return its, kept
 
 
@@ -58,6 +58,18 @@ def trained():
     m.fit_normaliser(xc)
     losses = m.train(xc, correction_targets(xc, tc), steps=1500, batch=4096, lr=2e-3, seed=3)
     return m, losses, x, t
+
+
+@pytest.fixture(scope="module")
+def trained_all(trained):
+    """The network trained on every logged point (it then corrects every point's warm start)."""
+    from box2dpp_gb300.train_warmstart import correction_targets
+
+    _, _, x, t = trained
+    m = Mlp(7)
+    m.fit_normaliser(x)
+    m.train(x, correction_targets(x, t), steps=1500, batch=4096, lr=2e-3, seed=3)
+    return m
 
 
 def test_contact_log_is_consistent(gpu):
@@ -93,3 +105,13 @@ def test_untrained_network_falls_back(gpu):
     ref, _ = _iterations(None, 6000)
     assert kept < 0.5
     assert lrn <= ref * 1.1 + 0.5
+
+
+def test_learned_all_points_is_not_worse_than_reference(gpu, trained_all):
+    """Corrections at every point (not only the cold ones) keep the per-island fallback: never more
+    iterations than the reference warm start."""
+    ref, _ = _iterations(None, 5000)
+    lrn, kept = _iterations(trained_all, 5000, all_points=True)
+    print(f"every point corrected: reference warm start {ref:.2f}, learned {lrn:.2f} (ratio {lrn / ref:.2f}); "
+          f"prediction kept by {kept * 100:.0f}% of islands")
+    assert lrn <= ref * 1.02 + 0.25
