@@ -53,7 +53,7 @@ COLOURED_VI = (8, 10, 12, 16, 20, 24, 32)
 # velocity iterations tried for the reference-order solver with the learned warm start
 LEARNED_VI = (4, 5, 6, 7, 8)
 # the learned warm start's training: held-out worlds (seed offset), logged steps, Adam steps
-LEARN_SEED_OFFSET, LEARN_WORLDS, LEARN_LOG_STEPS, LEARN_LOG_VI, LEARN_TRAIN_STEPS = 1000, 512, 8, 40, 3000
+LEARN_SEED_OFFSET, LEARN_WORLDS, LEARN_LOG_STEPS, LEARN_LOG_VI, LEARN_TRAIN_STEPS, LEARN_BATCH = 1000, 512, 8, 40, 3000, 16384
 METRIC = "body-steps/sec at fixed residual (batched worlds)"
 UNIT = "body-steps/s"
 
@@ -275,7 +275,7 @@ def _prepare(worlds, stream, solver: str, vi: int, warmup: int, plan=None, mlp=N
     w.set_solver(solver, measure_residual=True)
     w.upload()
     if mlp is not None:
-        w.set_warm_start(mlp)
+        w.set_warm_start(mlp, all_points=True)
     if plan is None:
         w.autotune(2)
     else:
@@ -293,13 +293,13 @@ def _prepare(worlds, stream, solver: str, vi: int, warmup: int, plan=None, mlp=N
 def train_learned(args):
     """The learned warm start's network, trained by the library's kernels: the plain solver's final
     impulses at LEARN_LOG_VI velocity iterations, logged for LEARN_LOG_STEPS steps after PRE_STEPS
-    steps on LEARN_WORLDS held-out worlds of the workload (another seed), at the points the reference
-    warm start leaves cold. Returns (network, points trained on, seconds)."""
+    steps on LEARN_WORLDS held-out worlds of the workload (another seed), every logged point (the
+    network corrects every point's warm start). Returns (network, points trained on, seconds)."""
     import numpy as np
 
     from box2dpp_gb300 import shard
     from box2dpp_gb300.learn import Mlp
-    from box2dpp_gb300.train_warmstart import cold_points, correction_targets
+    from box2dpp_gb300.train_warmstart import correction_targets
     from box2dpp_gb300.world import World
 
     t0 = time.perf_counter()
@@ -315,10 +315,10 @@ def train_learned(args):
         xs.append(x.copy())
         ts.append(t.copy())
     w.close()
-    x, t = cold_points(np.concatenate(xs), np.concatenate(ts))
+    x, t = np.concatenate(xs), np.concatenate(ts)
     m = Mlp(1)
     m.fit_normaliser(x)
-    m.train(x, correction_targets(x, t), steps=LEARN_TRAIN_STEPS, batch=min(65536, len(x)), lr=1e-3, seed=1)
+    m.train(x, correction_targets(x, t), steps=LEARN_TRAIN_STEPS, batch=LEARN_BATCH, lr=1e-3, seed=1)
     return m, len(x), time.perf_counter() - t0
 
 
