@@ -188,27 +188,16 @@ struct Wd {
     // b2Body::Advance (Dynamics/b2Body.h:856-864)
     __device__ void advance(int b, float alpha)
     {
-        const Sweep s = advancedSweep(b, alpha);
-        setSweep(b, s);
-        setXform(b, XfOfSweep(s));
-    }
-    // the sweep and transform b2Body::Advance would give body b, without changing the body
-    __device__ Sweep advancedSweep(int b, float alpha) const
-    {
         Sweep s = sweep(b);
         SweepAdvance(s, alpha);
         s.c = s.c0;
         s.a = s.a0;
-        return s;
-    }
-    __device__ static Xf XfOfSweep(const Sweep& s)
-    {
+        setSweep(b, s);
         Xf x;
         x.q = RotOf(s.a);
         x.p = s.c - Mul(x.q, s.localCenter);
-        return x;
+        setXform(b, x);
     }
-    __device__ Xf advancedXform(int b, float alpha) const { return XfOfSweep(advancedSweep(b, alpha)); }
 
     // ---------------------------------------------------------------- contact edge helpers
     // Edge e = 2*slot + side: side 0 is on bodyA's list (other = bodyB), side 1 on bodyB's list.
@@ -312,13 +301,8 @@ struct Wd {
     __device__ void evaluateManifold(int c, Manifold& m, Shape* stage) const
     {
         const int4 info = ci[c];
-        evaluateManifoldAt(c, m, stage, xform(fixBody(info.y)), xform(fixBody(info.z)));
-    }
-    // the same at given transforms of the bodies of fixture A and fixture B
-    __device__ void evaluateManifoldAt(int c, Manifold& m, Shape* stage, const Xf& xfA, const Xf& xfB) const
-    {
-        const int4 info = ci[c];
         const int fA = info.y, fB = info.z;
+        const Xf xfA = xform(fixBody(fA)), xfB = xform(fixBody(fB));
         Manifold old;
         loadManifold(c, old);
         m.count = 0;
@@ -572,9 +556,6 @@ __device__ inline int WarpAppend(bool keep, int* count)
 constexpr int kMaxCta = 256;
 // the continuous phase (StepToiKernel) runs with at most this many threads per CTA
 constexpr int kMaxToiCta = 128;
-// contact edges of a time-of-impact event's mini-island walk evaluated ahead in parallel (more: the
-// walk evaluates them itself)
-constexpr int kMaxToiCand = 256;
 
 // Exclusive prefix sums over the CTA of up to three per-thread counts (threads in index order), by
 // warp shuffles and one shared slot per warp and count; totals receive the CTA-wide sums. Every
@@ -2121,11 +2102,6 @@ __device__ void Wd::solveTOI(const StepParams& P)
     // phases, which set them before use.
     __shared__ int sDirty, sNeed;
     __shared__ int sSortT[kMaxToiCta * 2], sSortC[kMaxToiCta * 2];
-    // the event's state between its single-thread and CTA-wide parts: skipped, event bodies,
-    // mini-island sizes and woken bodies, and the contact edges of the mini-island walk
-    __shared__ int sSkip, sEvA, sEvB, sNB, sNC, sNCand, sCandSplit;
-    __shared__ unsigned long long sWoke;
-    __shared__ int sCand[kMaxToiCand];
     if (tid() == 0) sDirty = 0;
     for (int event = 0;; ++event) {
         const int n = st->contactCount;
@@ -2340,10 +2316,6 @@ __device__ void Wd::solveTOI(const StepParams& P)
         __syncthreads();
         stamp(17);
         if (sDone) break;
-        // The event (b2World.cpp:682-896). Order-defining steps run on thread 0; the work between
-        // them that is independent per contact or per body is spread over the CTA: the manifolds the
-        // mini-island walk will compute, the constraint setup, the integration and the fixture
-        // synchronisation of the island bodies.
         if (tid() == 0) {
             st->toiEvents = event + 1;
             sDirty = 0;
@@ -2373,11 +2345,6 @@ __device__ void Wd::solveTOI(const StepParams& P)
                 syncTransform(bB);
                 skip = true;
             }
-            sSkip = skip ? 1 : 0;
-            sEvA = bA;
-            sEvB = bB;
-            sNCand = 0;
-            sCandSplit = 0;
             if (!skip) {
                 // island bodies (bit = island position) this event woke: a woken kinematic body's
                 // contacts join the dirty list below (an awake one's cannot change their outcome)
@@ -2387,232 +2354,143 @@ __device__ void Wd::solveTOI(const StepParams& P)
                 if ((bi[bB].y & kBAwake) == 0) woke |= 2ull;
                 setAwake(bA, true);
                 setAwake(bB, true);
-                sWoke = woke;
-                // The contact edges the mini-island walk below visits, in its order, with the checks
-                // that no step of the walk changes (body types, bullet flags, sensors). A contact of
-                // both event bodies is met twice; its second entry is stored complemented.
-                int nCand = 0, split = 0;
-                const int pairB[2] = {bA, bB};
-                for (int kk = 0; kk < 2 && nCand >= 0; ++kk) {
-                    const int body = pairB[kk];
-                    if (kk == 1) split = nCand;
-                    if (bi[body].x != kDynamic) continue;
-                    B2G_WALK(e, bi[body].w, eNext(e), 2 * d.contactCap + 2) {
-                        const int c = e >> 1;
-                        const int4 ic = ci[c];
-                        const int other = (e & 1) == 0 ? fixBody(ic.z) : fixBody(ic.y);
-                        if (bi[other].x == kDynamic && (bi[body].y & kBBullet) == 0 && (bi[other].y & kBBullet) == 0)
-                            continue;
-                        if (fi[ic.y].w != 0 || fi[ic.z].w != 0) continue;
-                        if (nCand == kMaxToiCand) { nCand = -1; break; }
-                        bool again = false;
-                        for (int j = 0; j < split && kk == 1; ++j) again = again || (sCand[j] >> 1) == c;
-                        sCand[nCand++] = again ? ~e : e;
-                    }
-                }
-                sNCand = nCand;
-                sCandSplit = split;
-            }
-        }
-        __syncthreads();
-        // The manifolds of the walk's candidates, in parallel: each is b2Contact::Update's evaluation
-        // with the event bodies at the event time and the other body advanced to it (the walk
-        // advances a body not yet in the island before updating, restores it when the contact is
-        // not kept, and never re-advances one in the island), so it is the value the walk computes.
-        if (!sSkip && sNCand > 0) {
-            const float minAlpha = sMinAlpha;
-            const int bA = sEvA, bB = sEvB, split = sCandSplit;
-            for (int k = tid(); k < sNCand; k += nthreads()) {
-                const int e = sCand[k];
-                if (e < 0) continue;
-                const int c = e >> 1;
-                const int4 ic = ci[c];
-                const int body = k < split ? bA : bB;
-                const int other = (e & 1) == 0 ? fixBody(ic.z) : fixBody(ic.y);
-                const Xf xo = (other == bA || other == bB) ? xform(other) : advancedXform(other, minAlpha);
-                const Xf xb = xform(body);
-                Manifold m;
-                if ((e & 1) == 0) evaluateManifoldAt(c, m, nullptr, xb, xo);
-                else evaluateManifoldAt(c, m, nullptr, xo, xb);
-                writeStage(c, m);
-                stageOf(c)->tag = 1;
-            }
-        }
-        __syncthreads();
-        if (tid() == 0 && !sSkip) {
-            const int mc = sMin;
-            const float minAlpha = sMinAlpha;
-            const int bA = sEvA, bB = sEvB;
-            unsigned long long woke = sWoke;
-            // mini island in the scratch rows (b2World.cpp:700-780)
-            int nBodies = 0, nContacts = 0;
-            const int bodyCap = 2 * kMaxTOIContacts, contactCap = kMaxTOIContacts;
-            bj[bA].z = nBodies; sBody[nBodies++] = bA;
-            bj[bB].z = nBodies; sBody[nBodies++] = bB;
-            sContact[nContacts++] = mc;
-            bi[bA].y |= kBIsland;
-            bi[bB].y |= kBIsland;
-            ci[mc].x |= kCIsland;
-            // one edge of the walk; false ends the walk of this body. staged: the edge is a
-            // candidate whose manifold was evaluated above.
-            auto visit = [&](int body, int e, bool staged) -> bool {
-                if (nBodies == bodyCap) return false;
-                if (nContacts == contactCap) return false;
-                int c = e >> 1;
-                int4 ic = ci[c];
-                if (ic.x & kCIsland) return true;
-                int other = (e & 1) == 0 ? fixBody(ic.z) : fixBody(ic.y);
-                if (!staged) {
-                    if (bi[other].x == kDynamic && (bi[body].y & kBBullet) == 0 && (bi[other].y & kBBullet) == 0)
-                        return true;
-                    if (fi[ic.y].w != 0 || fi[ic.z].w != 0) return true;
-                }
-                Sweep backup = sweep(other);
-                if ((bi[other].y & kBIsland) == 0) advance(other, minAlpha);
-                update(c, nullptr, staged);
-                if (evLog)
-                    appendUpdateEvents(c, updateEventBits((ic.x & kCTouching) != 0, (ci[c].x & kCTouching) != 0,
-                                                          fi[ic.y].w != 0 || fi[ic.z].w != 0));
-                int fc = ci[c].x;
-                if ((fc & kCEnabled) == 0 || (fc & kCTouching) == 0) {
-                    setSweep(other, backup);
-                    syncTransform(other);
-                    return true;
-                }
-                ci[c].x = fc | kCIsland;
-                sContact[nContacts++] = c;
-                if (bi[other].y & kBIsland) return true;
-                bi[other].y |= kBIsland;
-                if (bi[other].x != kStatic) {
-                    if ((bi[other].y & kBAwake) == 0) woke |= 1ull << nBodies;
-                    setAwake(other, true);
-                }
-                bj[other].z = nBodies;
-                sBody[nBodies++] = other;
-                return true;
-            };
-            const int pairB[2] = {bA, bB};
-            if (sNCand >= 0) {
-                const int n = sNCand, split = sCandSplit;
-                for (int kk = 0; kk < 2; ++kk)
-                    for (int k = kk == 0 ? 0 : split; k < (kk == 0 ? split : n); ++k) {
-                        const int v = sCand[k];
-                        if (!visit(pairB[kk], v < 0 ? ~v : v, true)) break;
-                    }
-            } else {
+                // mini island in the scratch rows (b2World.cpp:700-780)
+                int nBodies = 0, nContacts = 0;
+                const int bodyCap = 2 * kMaxTOIContacts, contactCap = kMaxTOIContacts;
+                bj[bA].z = nBodies; sBody[nBodies++] = bA;
+                bj[bB].z = nBodies; sBody[nBodies++] = bB;
+                sContact[nContacts++] = mc;
+                bi[bA].y |= kBIsland;
+                bi[bB].y |= kBIsland;
+                ci[mc].x |= kCIsland;
+                int pairB[2] = {bA, bB};
                 for (int kk = 0; kk < 2; ++kk) {
                     int body = pairB[kk];
                     if (bi[body].x != kDynamic) continue;
                     B2G_WALK(e, bi[body].w, eNext(e), 2 * d.contactCap + 2) {
-                        if (!visit(body, e, false)) break;
+                        if (nBodies == bodyCap) break;
+                        if (nContacts == contactCap) break;
+                        int c = e >> 1;
+                        int4 ic = ci[c];
+                        if (ic.x & kCIsland) continue;
+                        int other = (e & 1) == 0 ? fixBody(ic.z) : fixBody(ic.y);
+                        if (bi[other].x == kDynamic && (bi[body].y & kBBullet) == 0 && (bi[other].y & kBBullet) == 0)
+                            continue;
+                        if (fi[ic.y].w != 0 || fi[ic.z].w != 0) continue;
+                        Sweep backup = sweep(other);
+                        if ((bi[other].y & kBIsland) == 0) advance(other, minAlpha);
+                        update(c);
+                        if (evLog)
+                            appendUpdateEvents(c, updateEventBits((ic.x & kCTouching) != 0, (ci[c].x & kCTouching) != 0,
+                                                                  fi[ic.y].w != 0 || fi[ic.z].w != 0));
+                        int fc = ci[c].x;
+                        if ((fc & kCEnabled) == 0 || (fc & kCTouching) == 0) {
+                            setSweep(other, backup);
+                            syncTransform(other);
+                            continue;
+                        }
+                        ci[c].x = fc | kCIsland;
+                        sContact[nContacts++] = c;
+                        if (bi[other].y & kBIsland) continue;
+                        bi[other].y |= kBIsland;
+                        if (bi[other].x != kStatic) {
+                            if ((bi[other].y & kBAwake) == 0) woke |= 1ull << nBodies;
+                            setAwake(other, true);
+                        }
+                        bj[other].z = nBodies;
+                        sBody[nBodies++] = other;
                     }
                 }
-            }
-            sWoke = woke;
-            sNB = nBodies;
-            sNC = nContacts;
-            stamp(18);
-        }
-        __syncthreads();
-        // b2Island::SolveTOI (Dynamics/b2Island.cpp:386-485). The mini island's rows and constraint
-        // records live in shared memory when they fit (the CTA's dynamic shared memory is free during
-        // the continuous phase), else in the global scratch.
-        const int bodyCapT = 2 * kMaxTOIContacts;
-        const int miniBytes = (2 * bodyCapT) * (int)sizeof(float4) +
-                              kMaxTOIContacts * (int)(sizeof(VelConstraint) + sizeof(PosConstraint) + sizeof(float4));
-        const bool miniShared = miniBytes <= smemBytes;
-        float4* mPos = miniShared ? smemBase : sPos;
-        float4* mVel = miniShared ? smemBase + bodyCapT : sVel;
-        VelConstraint* mVc = miniShared ? reinterpret_cast<VelConstraint*>(smemBase + 2 * bodyCapT) : vc;
-        PosConstraint* mPc = miniShared ? reinterpret_cast<PosConstraint*>(mVc + kMaxTOIContacts) : pc;
-        float4* mImp = miniShared ? reinterpret_cast<float4*>(mPc + kMaxTOIContacts) : vimp;
-        if (!sSkip) {
-            // rows 0..nBodies-1 of the scratch hold the mini island (island index == row)
-            const int nBodies = sNB, nContacts = sNC;
-            for (int i = tid(); i < nBodies; i += nthreads()) {
-                int b = sBody[i];
-                float4 s = sw[b], v = vel[b];
-                mPos[i] = make_float4(s.x, s.y, s.z, 0.0f);
-                mVel[i] = make_float4(v.x, v.y, v.z, 0.0f);
-            }
-            for (int i = tid(); i < nContacts; i += nthreads()) {
-                int4 ic = ci[sContact[i]];
-                VelConstraint v;
-                v.idx = make_int4(bj[fixBody(ic.y)].z, bj[fixBody(ic.z)].z, 0, 0);
-                PosConstraint p;
-                float4 im;
-                ContactSetup(*this, v, p, im, sContact[i], false, 1.0f);
-                mVc[i] = v;
-                mPc[i] = p;
-                mImp[i] = im;
-            }
-            __syncthreads();
-            if (tid() == 0) {
-                const int bA = sEvA, bB = sEvB;
+                stamp(18);
+                // b2Island::SolveTOI (Dynamics/b2Island.cpp:386-485). The mini island's rows and
+                // constraint records live in shared memory when they fit (the CTA's dynamic shared
+                // memory is free during the continuous phase), else in the global scratch.
+                const int miniBytes = (2 * bodyCap) * (int)sizeof(float4) +
+                                      kMaxTOIContacts * (int)(sizeof(VelConstraint) + sizeof(PosConstraint) + sizeof(float4));
+                const bool miniShared = miniBytes <= smemBytes;
+                float4* mPos = miniShared ? smemBase : sPos;
+                float4* mVel = miniShared ? smemBase + bodyCap : sVel;
+                VelConstraint* mVc = miniShared ? reinterpret_cast<VelConstraint*>(smemBase + 2 * bodyCap) : vc;
+                PosConstraint* mPc = miniShared ? reinterpret_cast<PosConstraint*>(mVc + kMaxTOIContacts) : pc;
+                float4* mImp = miniShared ? reinterpret_cast<float4*>(mPc + kMaxTOIContacts) : vimp;
+                float subDt = (1.0f - minAlpha) * P.dt;
+                for (int i = 0; i < nBodies; ++i) {
+                    int b = sBody[i];
+                    float4 s = sw[b], v = vel[b];
+                    mPos[i] = make_float4(s.x, s.y, s.z, 0.0f);
+                    mVel[i] = make_float4(v.x, v.y, v.z, 0.0f);
+                }
+                // rows 0..nBodies-1 of the scratch hold the mini island (island index == row)
+                for (int i = 0; i < nContacts; ++i) {
+                    int4 ic = ci[sContact[i]];
+                    VelConstraint v;
+                    v.idx = make_int4(bj[fixBody(ic.y)].z, bj[fixBody(ic.z)].z, 0, 0);
+                    PosConstraint p;
+                    float4 im;
+                    ContactSetup(*this, v, p, im, sContact[i], false, 1.0f);
+                    mVc[i] = v;
+                    mPc[i] = p;
+                    mImp[i] = im;
+                }
                 const int toiA = bj[bA].z, toiB = bj[bB].z;
                 for (int it = 0; it < 20; ++it)
                     if (SweepPosition(mPc, 0, nContacts, mPos, true, toiA, toiB)) break;
-                float4 pA = mPos[toiA], pB = mPos[toiB];
-                float4 a0 = sw0[bA];
-                sw0[bA] = make_float4(pA.x, pA.y, pA.z, a0.w);
-                float4 b0 = sw0[bB];
-                sw0[bB] = make_float4(pB.x, pB.y, pB.z, b0.w);
-            }
-            __syncthreads();
-            for (int i = tid(); i < nContacts; i += nthreads()) ContactInitVelocity(*this, mVc[i], mPc[i], mPos, mVel);
-            __syncthreads();
-            if (tid() == 0)
+                {
+                    float4 pA = mPos[toiA], pB = mPos[toiB];
+                    float4 a0 = sw0[bA];
+                    sw0[bA] = make_float4(pA.x, pA.y, pA.z, a0.w);
+                    float4 b0 = sw0[bB];
+                    sw0[bB] = make_float4(pB.x, pB.y, pB.z, b0.w);
+                }
+                for (int i = 0; i < nContacts; ++i) ContactInitVelocity(*this, mVc[i], mPc[i], mPos, mVel);
                 for (int it = 0; it < P.velocityIterations; ++it) SweepVelocity(mVc, mImp, 0, nContacts, mVel);
-            __syncthreads();
-            const float h = (1.0f - sMinAlpha) * P.dt;
-            for (int i = tid(); i < nBodies; i += nthreads()) {
-                float4 p4 = mPos[i], v4 = mVel[i];
-                IntegratePosition(p4, v4, h);
-                mPos[i] = p4;
-                mVel[i] = v4;
-                int b = sBody[i];
-                sw[b] = make_float4(p4.x, p4.y, p4.z, sw[b].w);
-                vel[b] = make_float4(v4.x, v4.y, v4.z, 0.0f);
-                syncTransform(b);
-            }
-            __syncthreads();
-            // b2Island::Report of the sub-step island (b2Island.cpp:515): PostSolve with the TOI
-            // velocity impulses, which are not stored in the manifolds
-            if (tid() == 0 && evLog)
-                for (int i = 0; i < nContacts; ++i) {
-                    const int4 ic = ci[sContact[i]];
-                    const float4 im = mImp[i];
-                    const int pcn = mVc[i].idx.z;
-                    putEvent(st->eventCount++, kEvPostSolve, ic.y, ic.z, pcn, pcn > 0 ? im.x : 0.0f,
-                             pcn > 1 ? im.z : 0.0f, pcn > 0 ? im.y : 0.0f, pcn > 1 ? im.w : 0.0f);
+                const float h = subDt;
+                for (int i = 0; i < nBodies; ++i) {
+                    float4 p4 = mPos[i], v4 = mVel[i];
+                    IntegratePosition(p4, v4, h);
+                    mPos[i] = p4;
+                    mVel[i] = v4;
+                    int b = sBody[i];
+                    sw[b] = make_float4(p4.x, p4.y, p4.z, sw[b].w);
+                    vel[b] = make_float4(v4.x, v4.y, v4.z, 0.0f);
+                    syncTransform(b);
                 }
-            stamp(19);
-            // dynamic bodies: fixtures synchronised, contacts' TOIs invalidated; the contacts of every
-            // dynamic island body and of every kinematic one this event woke join the dirty list (in
-            // any order here: it is put in list order before it is classified)
-            const unsigned long long woke = sWoke;
-            for (int i = tid(); i < nBodies; i += nthreads()) {
-                int b = sBody[i];
-                bi[b].y &= ~kBIsland;
-                if (bi[b].x == kStatic) continue;
-                const bool dynamic = bi[b].x == kDynamic;
-                if (dynamic) syncFixtures(b);
-                else if (((woke >> i) & 1ull) == 0ull) continue;
-                B2G_WALK(e, bi[b].w, eNext(e), 2 * d.contactCap + 2) {
-                    const int c = e >> 1;
-                    if (dynamic) atomicAnd(&ci[c].x, ~(kCToi | kCIsland));
-                    if (atomicExch(&evType[c], event + 1) != event + 1) colourList[atomicAdd(&sDirty, 1)] = c;
+                // b2Island::Report of the sub-step island (b2Island.cpp:515): PostSolve with the TOI
+                // velocity impulses, which are not stored in the manifolds
+                if (evLog)
+                    for (int i = 0; i < nContacts; ++i) {
+                        const int4 ic = ci[sContact[i]];
+                        const float4 im = mImp[i];
+                        const int pcn = mVc[i].idx.z;
+                        putEvent(st->eventCount++, kEvPostSolve, ic.y, ic.z, pcn, pcn > 0 ? im.x : 0.0f,
+                                 pcn > 1 ? im.z : 0.0f, pcn > 0 ? im.y : 0.0f, pcn > 1 ? im.w : 0.0f);
+                    }
+                stamp(19);
+                // dynamic bodies: fixtures synchronised, contacts' TOIs invalidated; the contacts of
+                // every dynamic island body and of every kinematic one this event woke join the dirty
+                // list
+                for (int i = 0; i < nBodies; ++i) {
+                    int b = sBody[i];
+                    bi[b].y &= ~kBIsland;
+                    if (bi[b].x == kStatic) continue;
+                    const bool dynamic = bi[b].x == kDynamic;
+                    if (dynamic) syncFixtures(b);
+                    else if (((woke >> i) & 1ull) == 0ull) continue;
+                    B2G_WALK(e, bi[b].w, eNext(e), 2 * d.contactCap + 2) {
+                        const int c = e >> 1;
+                        if (dynamic) ci[c].x &= ~(kCToi | kCIsland);
+                        if (evType[c] != event + 1) {
+                            evType[c] = event + 1;
+                            colourList[sDirty++] = c;
+                        }
+                    }
                 }
             }
-            __syncthreads();
-        }
-        if (tid() == 0) {
-            const int mc = sMin;
             if (evType[mc] != event + 1) {
                 evType[mc] = event + 1;
                 colourList[sDirty++] = mc;
             }
-            sDone = sSkip ? 2 : 0;
+            sDone = skip ? 2 : 0;
         }
         __syncthreads();
         stamp(20);
