@@ -21,9 +21,11 @@ value: the faster of those arms (headline names it): device time of the K timed 
 replayed from a captured CUDA graph, CUDA events on the stream the step runs on, state resident in
 HBM (several hundred MB, larger than L2, so no flush between steps).
 e2e: the headline arm's same K steps through the C-ABI with host buffers: every step uploads the
-force and torque of every body from pinned host memory (gb_set_forces), steps
+force and torque of every body from pinned host memory (gb_set_forces_async), steps
 (gb_world_graph_step) and reads every body transform back into pinned host memory
-(gb_get_transforms), wall-clock timed; each arm carries its own e2e figure.
+(gb_get_transforms_async); the copies run on their own streams and overlap the neighbouring steps,
+and gb_world_sync after the last step waits for every copy; wall-clock timed; each arm carries its
+own e2e figure.
 sleep_on: the headline arm with sleeping allowed (the reference's default), beside the CPU figure.
 --impl reference: the reference CPU step (the compiled reference where its build exists, else the
 project's CPU restatement of it, bit-exact with it) with glibc trig on all host cores over the same
@@ -324,9 +326,10 @@ def train_learned(args):
 
 def _e2e(worlds, stream, solver: str, vi: int, plan, args, clk, max_over_ranks, barrier, mlp=None):
     """The same K steps end to end through the C-ABI with pinned host buffers: a handle on the same
-    worlds with the given plan, advanced through the same steps, then per step gb_set_forces (every
-    body's force and torque from pinned host memory), gb_world_graph_step and gb_get_transforms
-    (every body's transform into pinned host memory), wall-clock timed."""
+    worlds with the given plan, advanced through the same steps, then per step gb_set_forces_async
+    (every body's force and torque from pinned host memory), gb_world_graph_step and
+    gb_get_transforms_async (every body's transform into pinned host memory; the copies of one step
+    overlap the next step), and gb_world_sync after the last, wall-clock timed."""
     import torch
 
     we = _prepare(worlds, stream, solver, vi, args.warmup, plan, mlp)
@@ -337,9 +340,9 @@ def _e2e(worlds, stream, solver: str, vi: int, plan, args, clk, max_over_ranks, 
     with clk:
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            we.set_forces_ptr(forces.data_ptr())
+            we.set_forces_async_ptr(forces.data_ptr())
             we.graph_step(DT, vi, PI)
-            we.get_transforms_ptr(xforms.data_ptr())
+            we.get_transforms_async_ptr(xforms.data_ptr())
         we.sync()
         e2e_s = max_over_ranks(time.perf_counter() - t0)
     we.close()
@@ -457,8 +460,9 @@ def run_gpu(args):
                          mlps.get(name))
         rec["e2e"] = {"value": total_bodies * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nb * 16,
                       "d2h_bytes_per_step": nb * 16,
-                      "calls": "gb_set_forces + gb_world_graph_step + gb_get_transforms per step, pinned host "
-                               "buffers"}
+                      "calls": "gb_set_forces_async + gb_world_graph_step + gb_get_transforms_async per step "
+                               "(pinned host buffers, copies overlapping the next step), gb_world_sync after "
+                               "the last"}
     # sleep on (the reference's default): the headline arm on the same worlds with sleeping allowed
     sleep_on = None
     if not args.no_sleep_on:

@@ -24,7 +24,8 @@ EXPORTS = [
     "gb_create_revolute_joints",
     "gb_build_world", "gb_world_upload", "gb_world_step", "gb_world_sync", "gb_world_set_stream",
     "gb_world_counts", "gb_get_bodies", "gb_get_contacts", "gb_get_proxies", "gb_world_stats", "gb_sincos",
-    "gb_collide", "gb_version", "gb_world_totals", "gb_set_forces", "gb_get_transforms", "gb_world_profile",
+    "gb_collide", "gb_version", "gb_world_totals", "gb_set_forces", "gb_get_transforms", "gb_set_forces_async",
+    "gb_get_transforms_async", "gb_world_profile",
     "gb_collide_noalloc", "gb_world_set_solver", "gb_world_solver_stats", "gb_world_autotune",
     "gb_world_launch_plan", "gb_world_set_launch_plan", "gb_world_graph_step",
     "gb_mlp_create", "gb_mlp_destroy", "gb_mlp_param_count", "gb_mlp_set_params", "gb_mlp_get_params",
@@ -159,6 +160,8 @@ def load(build_if_missing: bool = True):
         "gb_world_totals": [vp, C.POINTER(C.c_longlong)],
         "gb_set_forces": [vp, vp],
         "gb_get_transforms": [vp, vp],
+        "gb_set_forces_async": [vp, vp],
+        "gb_get_transforms_async": [vp, vp],
         "gb_world_profile": [vp, np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")],
         "gb_world_stage_times": [vp, f, i, i, _f32],
         "gb_body_edits": [vp, i, vp],

@@ -170,6 +170,15 @@ struct gb_world {
     float* logT = nullptr;
     int* logCount = nullptr;
     int logCap = 0;
+    // pipelined transfers (gb_set_forces_async, gb_get_transforms_async): an upload and a download
+    // stream, two device staging buffers per direction used in turn, and the events that order them
+    // against the handle's stream
+    cudaStream_t upStream = nullptr, downStream = nullptr;
+    float4* forceStage[2] = {};
+    float4* xfStage[2] = {};
+    size_t stageBodies = 0;
+    cudaEvent_t upDone[2] = {}, forceTaken[2] = {}, xfReady[2] = {}, downDone[2] = {};
+    unsigned upCount = 0, downCount = 0;
 };
 
 namespace {
@@ -635,6 +644,24 @@ bool SamePlan(const LaunchPlan& a, const LaunchPlan& b)
             a[i].rows != b[i].rows || a[i].contacts != b[i].contacts)
             return false;
     return true;
+}
+
+// Streams, staging buffers and events of the pipelined transfers (after their work is done).
+void ReleaseTransferResources(gb_world* g)
+{
+    if (g->upStream) { cudaStreamSynchronize(g->upStream); cudaStreamDestroy(g->upStream); }
+    if (g->downStream) { cudaStreamSynchronize(g->downStream); cudaStreamDestroy(g->downStream); }
+    g->upStream = g->downStream = nullptr;
+    for (int i = 0; i < 2; ++i) {
+        if (g->forceStage[i]) cudaFree(g->forceStage[i]);
+        if (g->xfStage[i]) cudaFree(g->xfStage[i]);
+        g->forceStage[i] = g->xfStage[i] = nullptr;
+        for (cudaEvent_t* e : {&g->upDone[i], &g->forceTaken[i], &g->xfReady[i], &g->downDone[i]}) {
+            if (*e) cudaEventDestroy(*e);
+            *e = nullptr;
+        }
+    }
+    g->stageBodies = 0;
 }
 
 void ReleaseLaunchResources(gb_world* g)
@@ -1361,6 +1388,7 @@ gb_status gb_world_destroy(gb_world* g)
     if (g->stream) cudaStreamSynchronize(g->stream);
     for (int i = 0; i < kMaxClasses; ++i)
         if (g->side[i]) cudaStreamSynchronize(g->side[i]);
+    ReleaseTransferResources(g);
     FreeDevice(g);
     ReleaseLaunchResources(g);
     FreeLog(g);
@@ -1731,6 +1759,8 @@ gb_status gb_world_sync(gb_world* g)
     if (!g) return GB_ERR_INVALID;
     if (!g->onDevice) return GB_OK;
     GB_CUDA(cudaStreamSynchronize(g->stream));
+    if (g->upStream) GB_CUDA(cudaStreamSynchronize(g->upStream));
+    if (g->downStream) GB_CUDA(cudaStreamSynchronize(g->downStream));
     const int nw = (int)g->worlds.size();
     std::vector<WorldState> st(nw);
     GB_CUDA(cudaMemcpy(st.data(), g->batch.state, nw * sizeof(WorldState), cudaMemcpyDeviceToHost));
@@ -2025,6 +2055,7 @@ gb_status gb_world_set_stream(gb_world* g, void* stream)
 {
     if (!g) return GB_ERR_INVALID;
     if (g->stream) GB_CUDA(cudaStreamSynchronize(g->stream));
+    ReleaseTransferResources(g);
     if (g->ownStream && g->stream) cudaStreamDestroy(g->stream);
     if (stream) { g->stream = static_cast<cudaStream_t>(stream); g->ownStream = false; }
     else {
@@ -2261,6 +2292,65 @@ gb_status gb_set_forces(gb_world* g, const float* forces)
                                     cudaMemcpyHostToDevice, g->stream));
         off += d.bodyCount;
     }
+    return GB_OK;
+}
+
+// The streams, staging buffers (one body column of float4 each) and events of the pipelined
+// transfers, created on first use and again when the body count changed.
+gb_status EnsureTransfers(gb_world* g, size_t n)
+{
+    if (g->upStream && g->stageBodies == n) return GB_OK;
+    ReleaseTransferResources(g);
+    GB_CUDA(cudaStreamCreateWithFlags(&g->upStream, cudaStreamNonBlocking));
+    GB_CUDA(cudaStreamCreateWithFlags(&g->downStream, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; ++i) {
+        GB_CUDA(cudaMalloc(&g->forceStage[i], std::max<size_t>(n, 1) * sizeof(float4)));
+        GB_CUDA(cudaMalloc(&g->xfStage[i], std::max<size_t>(n, 1) * sizeof(float4)));
+        for (cudaEvent_t* e : {&g->upDone[i], &g->forceTaken[i], &g->xfReady[i], &g->downDone[i]})
+            GB_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    }
+    g->stageBodies = n;
+    g->upCount = g->downCount = 0;
+    return GB_OK;
+}
+
+gb_status gb_set_forces_async(gb_world* g, const float* forces)
+{
+    if (!g || !forces) return GB_ERR_INVALID;
+    gb_status s = Upload(g);
+    if (s != GB_OK) return s;
+    if (!BodyRowsContiguous(g)) return gb_set_forces(g, forces);
+    size_t n = 0;
+    for (const WorldDesc& d : g->desc) n += d.bodyCount;
+    if ((s = EnsureTransfers(g, n)) != GB_OK) return s;
+    const int i = (int)(g->upCount++ & 1u);
+    // the upload stream refills buffer i once the handle's stream has taken its previous contents
+    if (g->upCount > 2) GB_CUDA(cudaStreamWaitEvent(g->upStream, g->forceTaken[i], 0));
+    GB_CUDA(cudaMemcpyAsync(g->forceStage[i], forces, n * sizeof(float4), cudaMemcpyHostToDevice, g->upStream));
+    GB_CUDA(cudaEventRecord(g->upDone[i], g->upStream));
+    GB_CUDA(cudaStreamWaitEvent(g->stream, g->upDone[i], 0));
+    GB_CUDA(cudaMemcpyAsync(g->batch.frc, g->forceStage[i], n * sizeof(float4), cudaMemcpyDeviceToDevice, g->stream));
+    GB_CUDA(cudaEventRecord(g->forceTaken[i], g->stream));
+    return GB_OK;
+}
+
+gb_status gb_get_transforms_async(gb_world* g, float* xf)
+{
+    if (!g || !xf) return GB_ERR_INVALID;
+    gb_status s = Upload(g);
+    if (s != GB_OK) return s;
+    if (!BodyRowsContiguous(g)) return gb_get_transforms(g, xf);
+    size_t n = 0;
+    for (const WorldDesc& d : g->desc) n += d.bodyCount;
+    if ((s = EnsureTransfers(g, n)) != GB_OK) return s;
+    const int i = (int)(g->downCount++ & 1u);
+    // the handle's stream refills buffer i once the download stream has sent its previous contents
+    if (g->downCount > 2) GB_CUDA(cudaStreamWaitEvent(g->stream, g->downDone[i], 0));
+    GB_CUDA(cudaMemcpyAsync(g->xfStage[i], g->batch.xf, n * sizeof(float4), cudaMemcpyDeviceToDevice, g->stream));
+    GB_CUDA(cudaEventRecord(g->xfReady[i], g->stream));
+    GB_CUDA(cudaStreamWaitEvent(g->downStream, g->xfReady[i], 0));
+    GB_CUDA(cudaMemcpyAsync(xf, g->xfStage[i], n * sizeof(float4), cudaMemcpyDeviceToHost, g->downStream));
+    GB_CUDA(cudaEventRecord(g->downDone[i], g->downStream));
     return GB_OK;
 }
 

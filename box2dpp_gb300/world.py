@@ -369,6 +369,16 @@ class World:
         """Copy every body transform (float4 per body, all worlds) into a host pointer."""
         _lib.check(self.lib.gb_get_transforms(self.h, C.c_void_p(host_ptr)), "gb_get_transforms")
 
+    def set_forces_async_ptr(self, host_ptr: int) -> None:
+        """Pipelined upload of force/torque (see gb_set_forces_async); the host memory must stay
+        untouched until sync()."""
+        _lib.check(self.lib.gb_set_forces_async(self.h, C.c_void_p(host_ptr)), "gb_set_forces_async")
+
+    def get_transforms_async_ptr(self, host_ptr: int) -> None:
+        """Pipelined read-back of every body transform after the queued steps (see
+        gb_get_transforms_async); the host memory holds them once sync() returns."""
+        _lib.check(self.lib.gb_get_transforms_async(self.h, C.c_void_p(host_ptr)), "gb_get_transforms_async")
+
     def get_transforms(self) -> np.ndarray:
         out = np.zeros((self.total_bodies, 4), dtype=np.float32)
         self.get_transforms_ptr(out.ctypes.data)

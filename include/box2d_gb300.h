@@ -387,6 +387,17 @@ gb_status gb_set_forces(gb_world* world, const float* forces);
  * world order then creation order = p.x, p.y, q.s, q.c. Waits for queued steps. */
 gb_status gb_get_transforms(gb_world* world, float* xf);
 
+/* Pipelined forms of gb_set_forces and gb_get_transforms for a loop of steps (no reference
+ * counterpart; same layouts). gb_set_forces_async copies the host forces into a device staging
+ * buffer on an upload stream of the handle, and the handle's stream takes them from there before the
+ * next step, so the copy of step k+1's forces overlaps step k. gb_get_transforms_async copies the
+ * transforms after the steps queued so far into a staging buffer on the handle's stream and from
+ * there to the host on a download stream, overlapping the next step; it does not wait. Two staging
+ * buffers per direction are used in turn. The host arrays (pinned memory for true overlap) must stay
+ * untouched until gb_world_sync returns, which waits for both transfer streams. */
+gb_status gb_set_forces_async(gb_world* world, const float* forces);
+gb_status gb_get_transforms_async(gb_world* world, float* xf);
+
 /* The project sin/cos used for every b2Rot (b2Rot::Set, Box2D/Common/b2Math.h:305-312) evaluated on
  * the device for n inputs (host arrays). */
 gb_status gb_sincos(const float* x, float* s, float* c, int n);

@@ -90,3 +90,34 @@ def test_graph_step_matches_step(gpu, solver):
         b.graph_step(DT, VI, PI)
     b.sync()
     assert _same(_state(a), _state(b))
+
+
+def test_pipelined_transfers_match_synchronous_ones(gpu):
+    """gb_set_forces_async / gb_get_transforms_async in a graph-replayed loop give the bits of
+    gb_set_forces / gb_get_transforms with a step between them (per-step forces differ, so a late or
+    early upload would show)."""
+    import torch
+
+    ws = scenes.config3(24, seed=17, allow_sleep=False)
+    a, b = World(ws), World(ws)
+    for w in (a, b):
+        w.set_solver("coloured")
+        w.upload()
+    n = a.total_bodies
+    rng = np.random.default_rng(5)
+    forces = [rng.normal(0.0, 20.0, (n, 4)).astype(np.float32) for _ in range(12)]
+    host_f = [torch.from_numpy(f).pin_memory() for f in forces]
+    host_x = [torch.zeros((n, 4), dtype=torch.float32).pin_memory() for _ in forces]
+    sync_x = []
+    for k in range(len(forces)):
+        a.set_forces_ptr(host_f[k].data_ptr())
+        a.graph_step(DT, VI, PI)
+        sync_x.append(a.get_transforms())
+    for k in range(len(forces)):
+        b.set_forces_async_ptr(host_f[k].data_ptr())
+        b.graph_step(DT, VI, PI)
+        b.get_transforms_async_ptr(host_x[k].data_ptr())
+    b.sync()
+    for k in range(len(forces)):
+        assert np.array_equal(sync_x[k].view(np.uint32), host_x[k].numpy().view(np.uint32)), k
+    assert not np.array_equal(sync_x[0], sync_x[-1])
