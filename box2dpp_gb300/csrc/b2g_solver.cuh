@@ -1825,11 +1825,14 @@ __device__ void PointFeatures(const VelConstraint& v, const float4 imp, const fl
 // every point.
 __device__ __noinline__ void Wd::learnedImpulses(const StepParams& P, int nContacts, const float4* imp, const float4* vel)
 {
-    __shared__ __align__(16) __nv_bfloat16 xTile[kMaxCta / 32][16 * kMlpInPad];
+    // at most kLearnWarps warps evaluate tiles (their input tiles are static shared memory that every
+    // launch of the kernel holds, so it is not sized for the widest CTA)
+    constexpr int kLearnWarps = 8;
+    __shared__ __align__(16) __nv_bfloat16 xTile[kLearnWarps][16 * kMlpInPad];
     const int warp = tid() >> 5, lane = tid() & 31, g = lane >> 2, t = lane & 3;
-    const int warps = nthreads() >> 5;
-    const int tiles = (nContacts + 7) / 8;
-    __nv_bfloat16* x = xTile[warp];
+    const int warps = min(nthreads() >> 5, kLearnWarps);
+    const int tiles = warp < warps ? (nContacts + 7) / 8 : 0;
+    __nv_bfloat16* x = xTile[warp < warps ? warp : 0];
     for (int tile = warp; tile < tiles; tile += warps) {
         if (lane < 16) {
             const int i = 8 * tile + (lane >> 1), j = lane & 1;

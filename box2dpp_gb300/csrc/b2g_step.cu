@@ -553,7 +553,7 @@ __device__ inline int WarpAppend(bool keep, int* count)
 }
 
 // Largest CTA of a per-world launch.
-constexpr int kMaxCta = 256;
+constexpr int kMaxCta = 512;
 // the continuous phase (StepToiKernel) runs with at most this many threads per CTA
 constexpr int kMaxToiCta = 128;
 
@@ -2610,15 +2610,12 @@ __global__ void __launch_bounds__(256) NarrowphaseKernel(Batch B, const int* slo
 // (positions, then velocities) and the accumulated impulses of the island contacts when a world's
 // fit, and the broadphase proxies, pair keys and list heads outside the island solve; every use
 // falls back to global memory when the world is larger, so the shape changes speed, never results.
-// Register caps: StepKernel 128 registers (at most 256 threads, 2 resident CTAs of 256 = 4 of 128),
-// StepToiKernel 168 (at most 128 threads, 3 resident; its time-of-impact code spills more when
-// capped lower). Measured on the bench batch with 128-thread CTAs at most: StepKernel/StepToiKernel
-// resident CTAs 4/3 3.89 ms per step coloured, 10.20 plain; 3/3 4.05, 10.51; 4/4 4.01, 10.33; 5/4
-// 4.24, 11.37.
-#ifndef B2G_STEP_MIN_BLOCKS
-#define B2G_STEP_MIN_BLOCKS 2
-#endif
-__global__ void __launch_bounds__(256, B2G_STEP_MIN_BLOCKS) StepKernel(Batch B, StepParams P, const int* schedule, LaunchShape L)
+// Register caps: StepKernel 128 registers (CTAs of up to 512 threads, the width single large worlds
+// use; 2 resident CTAs of 256 = 4 of 128), StepToiKernel 168 (at most 128 threads, 3 resident; its
+// time-of-impact code spills more when capped lower). Measured on the bench batch with 128-thread
+// CTAs at most: StepKernel/StepToiKernel resident CTAs 4/3 3.89 ms per step coloured, 10.20 plain;
+// 3/3 4.05, 10.51; 4/4 4.01, 10.33; 5/4 4.24, 11.37 (fewer registers spill).
+__global__ void __launch_bounds__(kMaxCta, 1) StepKernel(Batch B, StepParams P, const int* schedule, LaunchShape L)
 {
     extern __shared__ float4 smem[];
     Wd W;

@@ -1,7 +1,7 @@
 """Throughput of the single-world configurations on the GPU, beside the CPU restatement of the
 reference step on one host core, on the same seeded scenes.
 
-  python configs_report.py [--configs 1,2,5] [--cpu-seconds 15]
+  python configs_report.py [--configs 1,2,5] [--cpu-seconds 15] [--threads 128,256,512]
 
 Configurations (the batched one is bench.py's):
   1  the 210-box pyramid on an edge ground, sleep on (the reference default), 600 steps;
@@ -10,8 +10,8 @@ Configurations (the batched one is bench.py's):
      sleep off, steps 1..60.
 
 GPU: one world per handle, the plain (reference-order, bit-exact) and the graph-coloured solver,
-8/3 iterations, each step timed with CUDA events on the handle's stream; body-steps/s over the timed
-steps. CPU: the oracle's restatement of b2World::Step (plain order) with glibc's sinf/cosf (the
+8/3 iterations, one CTA of each --threads width (every width computes the same bits), each step timed
+with CUDA events on the handle's stream; body-steps/s over the timed steps. CPU: the oracle's restatement of b2World::Step (plain order) with glibc's sinf/cosf (the
 reference's own trig) on one thread, stepped from the same initial state for as many of the same
 steps as fit in --cpu-seconds. Prints one JSON line per configuration. A CPU-baseline reporter like
 bench.py's CPU leg: it sits beside bench.py, outside the package, because it runs the oracle.
@@ -43,7 +43,7 @@ def scene(cfg: int):
     raise ValueError(cfg)
 
 
-def gpu_rate(sc, steps: int, solver: str) -> dict:
+def gpu_rate(sc, steps: int, solver: str, threads: int) -> dict:
     import torch
 
     from box2dpp_gb300.world import World
@@ -53,6 +53,7 @@ def gpu_rate(sc, steps: int, solver: str) -> dict:
     stream = torch.cuda.Stream()
     w.set_stream(stream.cuda_stream)
     w.upload()
+    w.set_launch_plan([[0, 1, threads, 640, 1024]])
     ms = []
     for _ in range(steps):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -64,7 +65,7 @@ def gpu_rate(sc, steps: int, solver: str) -> dict:
     w.sync()
     n = w.dynamic_bodies
     w.close()
-    return {"solver": solver, "steps": steps, "ms_per_step_mean": float(np.mean(ms)),
+    return {"solver": solver, "threads": threads, "steps": steps, "ms_per_step_mean": float(np.mean(ms)),
             "ms_per_step_median": float(np.median(ms)), "body_steps_per_s": n * steps / (sum(ms) / 1e3)}
 
 
@@ -86,12 +87,14 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--configs", default="1,2,5")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--threads", default="128,256,512", help="CTA widths to time")
     a = ap.parse_args()
+    widths = [int(t) for t in a.threads.split(",")]
     for cfg in [int(c) for c in a.configs.split(",")]:
         sc, steps = scene(cfg)
         n = sum(1 for b in sc.bodies if b[0] == 2)
         line = {"config": cfg, "dynamic_bodies": n, "joints": len(sc.joints), "sleep": bool(sc.allow_sleep),
-                "gpu": [gpu_rate(sc, steps, s) for s in ("plain", "coloured")],
+                "gpu": [gpu_rate(sc, steps, s, t) for s in ("plain", "coloured") for t in widths],
                 "cpu": cpu_rate(sc, steps, a.cpu_seconds)}
         print(json.dumps(line), flush=True)
 

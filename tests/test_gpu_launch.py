@@ -121,3 +121,21 @@ def test_pipelined_transfers_match_synchronous_ones(gpu):
     for k in range(len(forces)):
         assert np.array_equal(sync_x[k].view(np.uint32), host_x[k].numpy().view(np.uint32)), k
     assert not np.array_equal(sync_x[0], sync_x[-1])
+
+
+@pytest.mark.parametrize("solver", ["plain", "coloured"])
+def test_wide_ctas_compute_identical_bits(gpu, solver):
+    """One world on CTAs of 128, 256 and 512 threads (the widths a single world's plans use)."""
+    sc = scenes.config2(1500, seed=3, allow_sleep=False)
+    runs = []
+    for threads in (128, 256, 512):
+        w = World([sc])
+        w.set_solver(solver)
+        w.upload()
+        w.set_launch_plan([[0, 1, threads, 640, 1024]])
+        for _ in range(60):
+            w.step(DT, VI, PI)
+        w.sync()
+        runs.append(_state(w))
+        w.close()
+    assert _same(runs[0], runs[1]) and _same(runs[0], runs[2])
