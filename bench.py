@@ -187,10 +187,10 @@ def measured_peaks():
 
 # DRAM bytes (read + write) per algorithmic byte of StepKernel, from a full ncu capture per solver of
 # one step of the 1024-world case of this workload (coloured, all four classes of the tuned plan:
-# 84.6 MB read + 17.4 MB written for 42.0 MB algorithmic; plain, default plan: 114.6 MB + 82.2 MB for
+# 84.5 MB read + 17.1 MB written for 42.0 MB algorithmic; plain, default plan: 114.6 MB + 82.2 MB for
 # 41.4 MB); traffic grows with the units processed, so the full launch's traffic is this ratio x its
 # algorithmic bytes.
-TRAFFIC_PER_ALGORITHMIC_BYTE = {"coloured": 102.0 / 42.0, "plain": 196.7 / 41.4}
+TRAFFIC_PER_ALGORITHMIC_BYTE = {"coloured": 101.6 / 42.0, "plain": 196.7 / 41.4}
 
 
 def algorithmic_bytes(t: dict) -> int:
