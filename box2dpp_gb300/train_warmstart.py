@@ -132,7 +132,7 @@ def main():
     ap.add_argument("--eval-steps", type=int, default=30)
     ap.add_argument("--tol", type=float, default=0.0, help="> 0: this target instead of the measured one")
     ap.add_argument("--max-vi", type=int, default=64)
-    ap.add_argument("--points", default="cold", choices=["cold", "all"],
+    ap.add_argument("--points", default="all", choices=["cold", "all"],
                     help="train on (and predict) the cold points only, or every point")
     ap.add_argument("--out", default=DEFAULT_OUT)
     args = ap.parse_args()
