@@ -19,11 +19,10 @@
 #include "../../include/box2d_gb300.h"
 #include "b2g_world.h"
 
-cudaError_t b2gLaunchNarrowphase(const b2g::Batch& B, const int* slotOf, int first, int count, cudaStream_t stream);
+cudaError_t b2gLaunchNarrowphase(const b2g::Batch& B, const int4* chunks, int n, cudaStream_t stream);
 cudaError_t b2gLaunchStep(const b2g::Batch& B, const b2g::StepParams& P, const int* schedule, int first, int count,
                           int threads, int smemRows, int smemContacts, cudaStream_t stream);
-cudaError_t b2gLaunchToi(const b2g::Batch& B, const b2g::StepParams& P, const int* slotOf, int first, int count,
-                         cudaStream_t stream);
+cudaError_t b2gLaunchToi(const b2g::Batch& B, const b2g::StepParams& P, const int4* chunks, int n, cudaStream_t stream);
 cudaError_t b2gLaunchBodyEdits(const b2g::Batch& B, const b2g::BodyEdit* edits, int n, cudaStream_t stream);
 cudaError_t b2gLaunchContactEdits(const b2g::Batch& B, const b2g::ContactEdit* edits, int n, cudaStream_t stream);
 cudaError_t b2gLaunchStepToi(const b2g::Batch& B, const b2g::StepParams& P, const int* schedule, int first, int count,
@@ -124,7 +123,11 @@ struct gb_world {
     std::vector<void*> shadow;
     long long filterReplays = 0;
     int* dSchedule = nullptr;
-    int* dSlotOf = nullptr;  // schedule slot of each world (the inverse of dSchedule)
+    // row chunks of the flat pre-passes in schedule order (see kRowChunk), and the first chunk of
+    // each schedule slot (one entry more: the total)
+    int4* dNpChunks = nullptr;
+    int4* dToiChunks = nullptr;
+    std::vector<int> npChunkStart, toiChunkStart;
     cudaStream_t stream = nullptr;
     bool ownStream = false;
     bool onDevice = false;   // device columns hold the current state
@@ -346,7 +349,9 @@ void FreeDevice(gb_world* g)
     g->shadow.clear();
     std::memset(&g->batch, 0, sizeof(g->batch));
     g->dSchedule = nullptr;
-    g->dSlotOf = nullptr;
+    g->dNpChunks = g->dToiChunks = nullptr;
+    g->npChunkStart.clear();
+    g->toiChunkStart.clear();
 }
 
 int NextPow2(int x)
@@ -590,10 +595,12 @@ gb_status LaunchPlanStep(gb_world* g, const StepParams& P, const LaunchPlan& pla
         cudaStream_t st = g->pipe[i];
         GB_CUDA(cudaStreamWaitEvent(st, g->fork, 0));
         // a split step (P.phase 1, then 2) runs the narrowphase and collide phase in its first half
-        if (P.phase != 2) GB_CUDA(b2gLaunchNarrowphase(g->batch, g->dSlotOf, c.first, c.count, st));
+        const int np0 = g->npChunkStart[c.first], toi0 = g->toiChunkStart[c.first];
+        if (P.phase != 2)
+            GB_CUDA(b2gLaunchNarrowphase(g->batch, g->dNpChunks + np0, g->npChunkStart[c.first + c.count] - np0, st));
         GB_CUDA(b2gLaunchStep(g->batch, P, g->dSchedule, c.first, c.count, c.threads, c.rows, c.contacts, st));
         if (P.phase != 1) {
-            GB_CUDA(b2gLaunchToi(g->batch, P, g->dSlotOf, c.first, c.count, st));
+            GB_CUDA(b2gLaunchToi(g->batch, P, g->dToiChunks + toi0, g->toiChunkStart[c.first + c.count] - toi0, st));
             GB_CUDA(b2gLaunchStepToi(g->batch, P, g->dSchedule, c.first, c.count, c.threads, c.rows, c.contacts, st));
         }
         GB_CUDA(cudaEventRecord(g->pipeJoin[i], st));
@@ -908,10 +915,34 @@ gb_status Upload(gb_world* g)
     });
     if ((s = DevAlloc(g, &g->dSchedule, nw)) != GB_OK) return s;
     GB_CUDA(cudaMemcpy(g->dSchedule, schedule.data(), nw * sizeof(int), cudaMemcpyHostToDevice));
-    std::vector<int> slotOf(nw);
-    for (int i = 0; i < nw; ++i) slotOf[schedule[i]] = i;
-    if ((s = DevAlloc(g, &g->dSlotOf, nw)) != GB_OK) return s;
-    GB_CUDA(cudaMemcpy(g->dSlotOf, slotOf.data(), nw * sizeof(int), cudaMemcpyHostToDevice));
+    {
+        // row chunks of the flat pre-passes, world by world in schedule order: the narrowphase's over
+        // contact rows, the time-of-impact pass's over body rows (at least one) then contact rows
+        std::vector<int4> np, toi;
+        g->npChunkStart.assign(nw + 1, 0);
+        g->toiChunkStart.assign(nw + 1, 0);
+        for (int slot = 0; slot < nw; ++slot) {
+            const int w = schedule[slot];
+            const WorldDesc& d = g->desc[w];
+            g->npChunkStart[slot] = (int)np.size();
+            g->toiChunkStart[slot] = (int)toi.size();
+            const int bodyRows = std::max(1, d.bodyCount);
+            for (int k = 0; k < d.contactCap; k += kRowChunk)
+                np.push_back(make_int4(w, k, std::min(kRowChunk, d.contactCap - k), 0));
+            for (int k = 0; k < bodyRows; k += kRowChunk)
+                toi.push_back(make_int4(w, k, std::min(kRowChunk, bodyRows - k), 0));
+            for (int k = 0; k < d.contactCap; k += kRowChunk)
+                toi.push_back(make_int4(w, k, std::min(kRowChunk, d.contactCap - k), 1));
+        }
+        g->npChunkStart[nw] = (int)np.size();
+        g->toiChunkStart[nw] = (int)toi.size();
+        if ((s = DevAlloc(g, &g->dNpChunks, np.size())) != GB_OK) return s;
+        if ((s = DevAlloc(g, &g->dToiChunks, toi.size())) != GB_OK) return s;
+        if (!np.empty())
+            GB_CUDA(cudaMemcpy(g->dNpChunks, np.data(), np.size() * sizeof(int4), cudaMemcpyHostToDevice));
+        if (!toi.empty())
+            GB_CUDA(cudaMemcpy(g->dToiChunks, toi.data(), toi.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    }
     g->schedule = schedule;
     g->scheduleSize.resize(nw);
     for (int i = 0; i < nw; ++i) g->scheduleSize[i] = g->desc[schedule[i]].bodyCount;
@@ -2256,11 +2287,12 @@ gb_status gb_world_stage_times(gb_world* g, float dt, int vi, int pi, float* ms)
     for (int i = 0; i < 5 && err == cudaSuccess; ++i) err = cudaEventCreate(&e[i]);
     const StepParams P = MakeParams(g, dt, vi, pi);
     if (err == cudaSuccess) err = cudaEventRecord(e[0], g->stream);
-    if (err == cudaSuccess) err = b2gLaunchNarrowphase(g->batch, nullptr, 0, 0, g->stream);
+    const int nw = (int)g->schedule.size();
+    if (err == cudaSuccess) err = b2gLaunchNarrowphase(g->batch, g->dNpChunks, g->npChunkStart[nw], g->stream);
     if (err == cudaSuccess) err = cudaEventRecord(e[1], g->stream);
     if (err == cudaSuccess) s = LaunchClasses(g, P, g->plan, b2gLaunchStep);
     if (err == cudaSuccess && s == GB_OK) err = cudaEventRecord(e[2], g->stream);
-    if (err == cudaSuccess && s == GB_OK) err = b2gLaunchToi(g->batch, P, nullptr, 0, 0, g->stream);
+    if (err == cudaSuccess && s == GB_OK) err = b2gLaunchToi(g->batch, P, g->dToiChunks, g->toiChunkStart[nw], g->stream);
     if (err == cudaSuccess && s == GB_OK) err = cudaEventRecord(e[3], g->stream);
     if (err == cudaSuccess && s == GB_OK) s = LaunchClasses(g, P, g->plan, b2gLaunchStepToi);
     if (err == cudaSuccess && s == GB_OK) err = cudaEventRecord(e[4], g->stream);

@@ -555,7 +555,12 @@ __device__ inline int WarpAppend(bool keep, int* count)
 // Largest CTA of a per-world launch.
 constexpr int kMaxCta = 512;
 // the continuous phase (StepToiKernel) runs with at most this many threads per CTA
+// the continuous phase's CTA width: its event loop is one thread's work, so in a batch narrower CTAs
+// let more worlds' loops run side by side (bench batch, one call: 3.49 ms per step at 128 threads,
+// 3.40 at 64, 3.55 at 32); a class of one world keeps the wider CTA (kMaxToiCta, which also sizes the
+// loop's shared arrays)
 constexpr int kMaxToiCta = 128;
+constexpr int kBatchToiCta = 64;
 
 // Exclusive prefix sums over the CTA of up to three per-thread counts (threads in index order), by
 // warp shuffles and one shared slot per warp and count; totals receive the CTA-wide sums. Every
@@ -2521,18 +2526,20 @@ __device__ void Wd::solveTOI(const StepParams& P)
 
 // ------------------------------------------------------------------ kernels
 // One step of a batch is, in stream order:
-//   NarrowphaseKernel  (flat, every contact row of the batch) per-step counters reset; manifolds of
-//                      the collide phase evaluated ahead
+//   NarrowphaseKernel  (flat, every contact row of the class's worlds) per-step counters reset;
+//                      manifolds of the collide phase evaluated ahead
 //   StepKernel         (per world, per launch class) new-fixture pairs, collide (commits the staged
 //                      manifolds), island solve, fixture sync and pair finding
-//   ToiKernel          (flat, every body and contact row) the continuous phase's reset and the first
-//                      pass of times of impact
+//   ToiKernel          (flat, every body and contact row of the class's worlds) the continuous
+//                      phase's reset and the first pass of times of impact
 //   StepToiKernel      (per world, per launch class) the continuous phase's event loop, force clearing
 // The flat pre-passes compute, per contact and in any order, values the reference computes while it
 // walks the contact list; the per-world kernels consume them in list order, so the results are the
 // reference's bit for bit. One thread per contact row keeps every SM busy with short independent
 // work (most rows are spare capacity and return at once), where the per-world kernels hold a
-// world's sequential phases.
+// world's sequential phases. Each class launches only its own worlds' rows: chunks of kRowChunk rows
+// of one world, listed in schedule order (bench batch, one call: the two pre-pass stages 0.19 + 0.27
+// ms with full-batch grids gated by class, 0.16 + 0.22 ms with the chunks).
 
 // Per-step counters of the world, zeroed before the step (profile slots included).
 __device__ void ResetStepCounters(WorldState* st)
@@ -2554,30 +2561,21 @@ __device__ void ResetStepCounters(WorldState* st)
 }
 
 // The evaluations of b2ContactManager::Collide (Dynamics/b2ContactManager.cpp:107-172), ahead of the
-// step, one thread per contact row of the batch: the k-th live contact of a world's list, if it is a
-// non-sensor contact with an awake non-static body whose fat AABBs overlap, gets the manifold
+// step, one thread per contact row of the class's worlds: the k-th live contact of a world's list, if
+// it is a non-sensor contact with an awake non-static body whose fat AABBs overlap, gets the manifold
 // b2Contact::Update would compute (evaluation at the current transforms, impulses matched by id) in
 // its stage record. Nothing the collide phase does before it updates a contact changes those
 // inputs, so the collide phase commits the record when it reaches the contact; contacts left out
 // (tag 0: asleep, sensors, apart) it evaluates itself. Worlds with new fixtures create contacts
 // before their collide phase and are left out whole. Row 0 of each world resets its counters.
-// Whether world w belongs to the schedule slots [first, first + count) of one class of the launch
-// plan (slotOf: schedule slot of each world); every world when slotOf is null.
-__device__ inline bool InClass(const int* slotOf, int first, int count, int w)
+// chunks: one per CTA, {world, first contact index, contacts, 0} (kRowChunk rows at most).
+__global__ void __launch_bounds__(kRowChunk) NarrowphaseKernel(Batch B, const int4* chunks)
 {
-    if (!slotOf) return true;
-    const int s = slotOf[w];
-    return s >= first && s < first + count;
-}
-
-__global__ void __launch_bounds__(256) NarrowphaseKernel(Batch B, const int* slotOf, int first, int count)
-{
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= B.contactRows) return;
-    const int w = B.cWorld[r];
-    if (!InClass(slotOf, first, count, w)) return;
+    const int4 ch = chunks[blockIdx.x];
+    if ((int)threadIdx.x >= ch.z) return;
+    const int w = ch.x;
     WorldState* st = B.state + w;
-    const int k = r - B.desc[w].contactBase;
+    const int k = ch.y + (int)threadIdx.x;
     const bool newFixture = st->newFixture != 0;
     if (k == 0) {
         ResetStepCounters(st);
@@ -2611,7 +2609,7 @@ __global__ void __launch_bounds__(256) NarrowphaseKernel(Batch B, const int* slo
 // fit, and the broadphase proxies, pair keys and list heads outside the island solve; every use
 // falls back to global memory when the world is larger, so the shape changes speed, never results.
 // Register caps: StepKernel 128 registers (CTAs of up to 512 threads, the width single large worlds
-// use; 2 resident CTAs of 256 = 4 of 128), StepToiKernel 168 (at most 128 threads, 3 resident; its
+// use; 2 resident CTAs of 256 = 4 of 128), StepToiKernel 168 (at most 64 threads, 6 resident; its
 // time-of-impact code spills more when capped lower). Measured on the bench batch with 128-thread
 // CTAs at most: StepKernel/StepToiKernel resident CTAs 4/3 3.89 ms per step coloured, 10.20 plain;
 // 3/3 4.05, 10.51; 4/4 4.01, 10.33; 5/4 4.24, 11.37 (fewer registers spill).
@@ -2684,36 +2682,32 @@ __global__ void ContactEditKernel(Batch B, const ContactEdit* edits, int n)
 }
 
 // The first pass of b2World::SolveTOI (Dynamics/b2World.cpp:579-680) after a completed step, one
-// thread per body row and per contact row of the batch: the reset (body island flags and sweep
+// thread per body row and per contact row of the class's worlds: the reset (body island flags and sweep
 // times, contact TOI flags, counts and cached times), then for every contact the scan would compute
 // a time of impact for, that time, cached on the contact as the scan caches it. After the reset every
 // sweep starts at alpha0 = 0 (a contact thread takes that value instead of waiting for its bodies'
 // reset), so the scan advances no sweep and each time of impact depends on its contact alone.
 // StepToiKernel's event loop then finds them cached. The body-flag bits the classification reads
 // (type, awake, bullet) are not the ones the reset clears.
-__global__ void __launch_bounds__(256, 2) ToiKernel(Batch B, float dt, const int* slotOf, int first, int count)
+// chunks: one per CTA, {world, first row, rows, 0 for body rows / 1 for contact rows}.
+__global__ void __launch_bounds__(kRowChunk, 4) ToiKernel(Batch B, float dt, const int4* chunks)
 {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r < B.bodyRows) {
-        const int w = B.bWorld[r];
-        if (!InClass(slotOf, first, count, w)) return;
-        WorldState* st = B.state + w;
-        if (!(st->continuous && dt > 0.0f && st->stepComplete)) return;
-        const int b = r - B.desc[w].bodyBase;
+    const int4 ch = chunks[blockIdx.x];
+    if ((int)threadIdx.x >= ch.z) return;
+    const int w = ch.x;
+    WorldState* st = B.state + w;
+    if (!(st->continuous && dt > 0.0f && st->stepComplete)) return;
+    if (ch.w == 0) {
+        const int b = ch.y + (int)threadIdx.x;
         if (b == 0) st->toiPrepared = 1;
         if (b < B.desc[w].bodyCount) {
+            const int r = B.desc[w].bodyBase + b;
             B.bi[r].y &= ~kBIsland;
             B.sw[r].w = 0.0f;
         }
         return;
     }
-    const int q = r - B.bodyRows;
-    if (q >= B.contactRows) return;
-    const int w = B.cWorld[q];
-    if (!InClass(slotOf, first, count, w)) return;
-    WorldState* st = B.state + w;
-    if (!(st->continuous && dt > 0.0f && st->stepComplete)) return;
-    const int k = q - B.desc[w].contactBase;
+    const int k = ch.y + (int)threadIdx.x;
     if (k >= st->contactCount) return;
     Wd W;
     W.init(B, w);
@@ -2739,10 +2733,10 @@ __global__ void __launch_bounds__(256, 2) ToiKernel(Batch B, float dt, const int
 
 // The continuous phase of b2World::Step (b2World.cpp:948-958) and the end of the step: the TOI
 // event loop, force clearing, inv_dt0.
-#ifndef B2G_TOI_MIN_BLOCKS
-#define B2G_TOI_MIN_BLOCKS 3
-#endif
-__global__ void __launch_bounds__(128, B2G_TOI_MIN_BLOCKS) StepToiKernel(Batch B, StepParams P, const int* schedule, LaunchShape L)
+// 168 registers: 6 resident CTAs of 64 threads, or 3 of 128 (the single-world form)
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads, 384 / kThreads) StepToiKernel(Batch B, StepParams P, const int* schedule,
+                                                                      LaunchShape L)
 {
     extern __shared__ float4 smem[];
     Wd W;
@@ -2778,10 +2772,10 @@ __global__ void BodyEditKernel(Batch B, const BodyEdit* edits, int n)
 
 // Launch entries used by the host runtime (b2g_api.cu). A step is b2gLaunchNarrowphase, then
 // b2gLaunchStep for every launch class, then b2gLaunchToi, then b2gLaunchStepToi for every class.
-cudaError_t b2gLaunchNarrowphase(const b2g::Batch& B, const int* slotOf, int first, int count, cudaStream_t stream)
+cudaError_t b2gLaunchNarrowphase(const b2g::Batch& B, const int4* chunks, int n, cudaStream_t stream)
 {
-    if (B.contactRows <= 0) return cudaSuccess;
-    b2g::NarrowphaseKernel<<<(B.contactRows + 255) / 256, 256, 0, stream>>>(B, slotOf, first, count);
+    if (n <= 0) return cudaSuccess;
+    b2g::NarrowphaseKernel<<<n, b2g::kRowChunk, 0, stream>>>(B, chunks);
     return cudaGetLastError();
 }
 
@@ -2807,12 +2801,10 @@ cudaError_t b2gLaunchBodyEdits(const b2g::Batch& B, const b2g::BodyEdit* edits, 
     return cudaGetLastError();
 }
 
-cudaError_t b2gLaunchToi(const b2g::Batch& B, const b2g::StepParams& P, const int* slotOf, int first, int count,
-                         cudaStream_t stream)
+cudaError_t b2gLaunchToi(const b2g::Batch& B, const b2g::StepParams& P, const int4* chunks, int n, cudaStream_t stream)
 {
-    if (!(P.dt > 0.0f)) return cudaSuccess;
-    const long long rows = (long long)B.bodyRows + B.contactRows;
-    b2g::ToiKernel<<<(unsigned)((rows + 255) / 256), 256, 0, stream>>>(B, P.dt, slotOf, first, count);
+    if (!(P.dt > 0.0f) || n <= 0) return cudaSuccess;
+    b2g::ToiKernel<<<n, b2g::kRowChunk, 0, stream>>>(B, P.dt, chunks);
     return cudaGetLastError();
 }
 
@@ -2838,8 +2830,13 @@ cudaError_t b2gLaunchStepToi(const b2g::Batch& B, const b2g::StepParams& P, cons
 {
     if (count <= 0) return cudaSuccess;
     const size_t smem = (2 * (size_t)smemRows + smemContacts) * sizeof(float4);
-    // the continuous phase is mostly one thread's event loop: its CTA is capped at kMaxToiCta
-    b2g::StepToiKernel<<<count, threads < b2g::kMaxToiCta ? threads : b2g::kMaxToiCta, smem, stream>>>(
-        B, P, schedule + first, Shape(smemRows, smemContacts));
+    // the continuous phase is mostly one thread's event loop: CTAs of at most kBatchToiCta threads,
+    // or kMaxToiCta for a class of one world
+    if (count == 1 && threads >= b2g::kMaxToiCta)
+        b2g::StepToiKernel<b2g::kMaxToiCta><<<1, b2g::kMaxToiCta, smem, stream>>>(B, P, schedule + first,
+                                                                                Shape(smemRows, smemContacts));
+    else
+        b2g::StepToiKernel<b2g::kBatchToiCta><<<count, threads < b2g::kBatchToiCta ? threads : b2g::kBatchToiCta, smem,
+                                                 stream>>>(B, P, schedule + first, Shape(smemRows, smemContacts));
     return cudaGetLastError();
 }

@@ -41,6 +41,10 @@ struct WorldDesc {
 };
 
 constexpr int kProfileSlots = 24;
+// Rows per chunk of the flat pre-passes (NarrowphaseKernel, ToiKernel): one CTA of kRowChunk threads
+// per chunk of one world's contact (or body) rows; the chunks are listed in schedule order, so a
+// class of the launch plan launches exactly its own worlds' chunks.
+constexpr int kRowChunk = 128;
 
 // Per-world mutable scalars.
 struct WorldState {

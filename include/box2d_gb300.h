@@ -242,7 +242,7 @@ gb_status gb_world_solver_stats(gb_world* world, int* colours, int* vel_iters, f
  * gb_world_launch_plan reports the plan, classes[5 * i] = first schedule slot, count, threads per
  * CTA, shared-memory island rows, shared-memory contacts, and after tuning the best time (ms) each
  * candidate took. gb_world_set_launch_plan sets a plan in the same layout (classes must cover the
- * schedule in order; threads a multiple of 32 in [32, 512], the continuous phase using at most 128
+ * schedule in order; threads a multiple of 32 in [32, 512], the continuous phase using at most 64
  * of them; at most 48 KB of shared memory). */
 gb_status gb_world_autotune(gb_world* world, int steps_per_candidate);
 /* gb_world_step as a CUDA graph: the first call (and any call after the step's parameters, solver
