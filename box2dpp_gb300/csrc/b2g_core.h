@@ -61,7 +61,7 @@ constexpr float kAngularSleepTolerance = 2.0f / 180.0f * kPi;
 // about one input in 10^5. The only fused operations are the explicit fmaf calls (the build disables
 // contraction everywhere else), so host and device round identically.
 #ifdef __CUDACC__
-static __device__ const float kTrigTableDev[512 * 4] = {B2G_TRIG_TABLE_ROWS};
+static __device__ const __align__(16) float kTrigTableDev[512 * 4] = {B2G_TRIG_TABLE_ROWS};
 #endif
 static const float kTrigTableHost[512 * 4] = {B2G_TRIG_TABLE_ROWS};
 
@@ -108,9 +108,14 @@ B2G_HD void SinCos(float x, float* s_out, float* c_out)
     const float b3 = ch - 1.0f;
     const float che = (1.0f - (ch - b3)) + (-uh - b3);
     const float cl = che + (w - ul);
-    // table
+    // table (one 16-byte row: S high, S low, C high, C low)
+#ifdef __CUDA_ARCH__
+    const float4 T = reinterpret_cast<const float4*>(kTrigTableDev)[idx];
+    const float Sh = T.x, Sl = T.y, Ch = T.z, Cl = T.w;
+#else
     const float* T = TrigTable() + 4 * idx;
     const float Sh = T[0], Sl = T[1], Ch = T[2], Cl = T[3];
+#endif
     // sin x = S cos r + C sin r
     const float a1 = Sh * ch;
     const float a1l = fmaf(Sh, ch, -a1) + (Sh * cl + Sl * ch);
