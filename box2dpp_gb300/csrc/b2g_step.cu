@@ -742,6 +742,11 @@ __device__ inline float FromOrderedBits(unsigned o)
 // until contact creation), the cell ranges after them.
 __device__ void Wd::gridPairs(int m, int* pairCount)
 {
+    // moved proxies larger than the cell size (container walls, ground) are tested against every
+    // live proxy with the scan spread over the CTA, one such proxy at a time, after the others
+    constexpr int kLargeCap = 64;
+    __shared__ int sLargeMoved[kLargeCap];
+    __shared__ int sNLarge;
     __shared__ float sSizeSum;
     __shared__ int sLive, sSmall, sCursor;
     __shared__ unsigned sMaxW, sMinX, sMinY, sMaxX, sMaxY;
@@ -749,6 +754,7 @@ __device__ void Wd::gridPairs(int m, int* pairCount)
     if (tid() == 0) {
         sSizeSum = 0.0f; sLive = 0; sSmall = 0; sCursor = 0; sMaxW = 0u;
         sMinX = sMinY = 0xffffffffu; sMaxX = sMaxY = 0u;
+        sNLarge = 0;
     }
     __syncthreads();
     auto size = [](const float4& f) { return fmaxf(f.z - f.x, f.w - f.y); };
@@ -838,19 +844,24 @@ __device__ void Wd::gridPairs(int m, int* pairCount)
         if (i == nSmall - 1 || (unsigned)(keys[i + 1] >> 32) != c) cellEnd[c] = i + 1;
     }
     __syncthreads();
+    auto test = [&](int p, int q, const float4& Fq) {
+        if (p == q) return;
+        if (moved[p] && p < q) return;
+        if (!Overlap(fat[p], Fq)) return;
+        const int k = atomicAdd(pairCount, 1);
+        const unsigned long long lo = (unsigned long long)(p < q ? p : q), hi = (unsigned long long)(p < q ? q : p);
+        if (k < d.pairCap) pairs[k] = (lo << 32) | hi;
+    };
     for (int t = tid(); t < m; t += nthreads()) {
         const int q = movedList[t];
         const float4 Fq = fat[q];
-        auto test = [&](int p) {
-            if (p == q) return;
-            if (moved[p] && p < q) return;
-            if (!Overlap(fat[p], Fq)) return;
-            const int k = atomicAdd(pairCount, 1);
-            const unsigned long long lo = (unsigned long long)(p < q ? p : q), hi = (unsigned long long)(p < q ? q : p);
-            if (k < d.pairCap) pairs[k] = (lo << 32) | hi;
-        };
         if (size(Fq) > wLarge) {
-            for (int j = 0; j < nLive; ++j) test((int)(keys[j] & 0xffffffffu));
+            const int slot = atomicAdd(&sNLarge, 1);
+            if (slot < kLargeCap) {
+                sLargeMoved[slot] = q;
+            } else {
+                for (int j = 0; j < nLive; ++j) test((int)(keys[j] & 0xffffffffu), q, Fq);
+            }
             continue;
         }
         const float lowX = Fq.x - W - 1e-4f * fabsf(Fq.x), lowY = Fq.y - W - 1e-4f * fabsf(Fq.y);
@@ -859,9 +870,16 @@ __device__ void Wd::gridPairs(int m, int* pairCount)
         for (int cy = cy0; cy <= cy1; ++cy)
             for (int cx = cx0; cx <= cx1; ++cx) {
                 const int c = cy * nx + cx;
-                for (int i = cellStart[c], e = cellEnd[c]; i < e; ++i) test((int)(keys[i] & 0xffffffffu));
+                for (int i = cellStart[c], e = cellEnd[c]; i < e; ++i) test((int)(keys[i] & 0xffffffffu), q, Fq);
             }
-        for (int j = nSmall; j < nLive; ++j) test((int)(keys[j] & 0xffffffffu));
+        for (int j = nSmall; j < nLive; ++j) test((int)(keys[j] & 0xffffffffu), q, Fq);
+    }
+    __syncthreads();
+    const int nLarge = min(sNLarge, kLargeCap);
+    for (int l = 0; l < nLarge; ++l) {
+        const int q = sLargeMoved[l];
+        const float4 Fq = fat[q];
+        for (int j = tid(); j < nLive; j += nthreads()) test((int)(keys[j] & 0xffffffffu), q, Fq);
     }
     __syncthreads();
 }
