@@ -51,7 +51,7 @@ DT, VI, PI = 1.0 / 60.0, 8, 3
 PRE_STEPS = 24
 # velocity iterations tried for the graph-coloured solver, fewest first, until its median residual
 # matches the reference-order solver's
-COLOURED_VI = (8, 10, 12, 16, 20, 24, 32)
+COLOURED_VI = (8, 9, 10, 11, 12, 14, 16, 20, 24, 32)
 # velocity iterations tried for the reference-order solver with the learned warm start
 LEARNED_VI = (4, 5, 6, 7, 8)
 # the learned warm start's training: held-out worlds (seed offset), logged steps, Adam steps
