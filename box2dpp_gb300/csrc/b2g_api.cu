@@ -395,6 +395,7 @@ gb_status Download(gb_world* g)
         W.fat.resize(np); W.moved.resize(np);
         GB_CUDA(cudaMemcpy(W.fat.data(), B.fat + d.proxyBase, np * sizeof(float4), cudaMemcpyDeviceToHost));
         GB_CUDA(cudaMemcpy(W.moved.data(), B.moved + d.proxyBase, np * sizeof(int), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(&W.state, B.state + wi, sizeof(WorldState), cudaMemcpyDeviceToHost));
         HContacts& C = W.contacts;
         C.ci.resize(nc); C.ce.resize(nc); C.mh.resize(nc); C.cp.resize(nc); C.mv.resize(nc); C.mp0.resize(nc);
         C.mp1.resize(nc); C.order.resize(nc); C.cnext.resize(nc);
@@ -405,7 +406,14 @@ gb_status Download(gb_world* g)
         GB_CUDA(cudaMemcpy(C.mv.data(), B.mv + d.contactBase, nc * sizeof(float4), cudaMemcpyDeviceToHost));
         GB_CUDA(cudaMemcpy(C.mp0.data(), B.mp0 + d.contactBase, nc * sizeof(float4), cudaMemcpyDeviceToHost));
         GB_CUDA(cudaMemcpy(C.mp1.data(), B.mp1 + d.contactBase, nc * sizeof(float4), cudaMemcpyDeviceToHost));
-        GB_CUDA(cudaMemcpy(C.order.data(), B.order + d.contactBase, nc * sizeof(int), cudaMemcpyDeviceToHost));
+        {
+            // the contact list (orderStart of the state read above)
+            std::fill(C.order.begin(), C.order.end(), 0);
+            const int live = std::min(W.state.contactCount, nc);
+            if (live > 0)
+                GB_CUDA(cudaMemcpy(C.order.data(), B.order + 2 * (size_t)d.contactBase + W.state.orderStart,
+                                   live * sizeof(int), cudaMemcpyDeviceToHost));
+        }
         GB_CUDA(cudaMemcpy(C.cnext.data(), B.cnext + d.contactBase, nc * sizeof(int), cudaMemcpyDeviceToHost));
         if (d.jointCount > 0)
             GB_CUDA(cudaMemcpy(W.joints.data(), B.joint + d.jointBase, d.jointCount * sizeof(Joint), cudaMemcpyDeviceToHost));
@@ -803,8 +811,9 @@ gb_status Upload(gb_world* g)
     ALLOC(bi, tb); ALLOC(bj, tb);
     ALLOC(fi, tf); ALLOC(fm, tf); ALLOC(ff, tf); ALLOC(faabb, tf); ALLOC(shape, tf);
     ALLOC(fat, tp); ALLOC(pfix, tp); ALLOC(moved, tp); ALLOC(movedList, tp); ALLOC(liveProxies, tp);
+    ALLOC(gridIds, tp); ALLOC(gridNext, tp); ALLOC(gridPrev, tp); ALLOC(gridCellOf, tp); ALLOC(gridHead, tq + nw);
     ALLOC(ci, tc); ALLOC(ce, tc); ALLOC(cp, tc); ALLOC(mh, tc); ALLOC(mv, tc); ALLOC(mp0, tc); ALLOC(mp1, tc);
-    ALLOC(order, tc); ALLOC(cnext, tc);
+    ALLOC(order, 2 * tc); ALLOC(cnext, tc);
     ALLOC(joint, tj); ALLOC(sJoint, tj);
     ALLOC(sBody, tr); ALLOC(sStack, tb); ALLOC(sWake, tb); ALLOC(sPos, tr); ALLOC(sVel, tr); ALLOC(islands, tb);
     ALLOC(islandJ, tb); ALLOC(sleepOut, tb); ALLOC(rowMask, tr); ALLOC(sVelL, tr);
@@ -825,7 +834,7 @@ gb_status Upload(gb_world* g)
     std::vector<int> pfix(tp, kNullIdx), moved(tp, 0);
     std::vector<int4> ci(tc, make_int4(0, 0, 0, 0)), ce(tc, make_int4(-1, -1, -1, -1)), mh(tc, make_int4(0, 0, 0, 0));
     std::vector<float4> cp(tc, make_float4(0, 0, 0, 1)), mv(tc), mp0(tc), mp1(tc);
-    std::vector<int> order(tc, 0), cnext(tc, kNullIdx);
+    std::vector<int> order(2 * tc, 0), cnext(tc, kNullIdx);
     std::vector<Joint> joints(tj);
     for (int wi = 0; wi < nw; ++wi) {
         HWorld& W = g->worlds[wi];
@@ -864,9 +873,15 @@ gb_status Upload(gb_world* g)
         for (int i = 0; i < old; ++i) {
             const int r = d.contactBase + i;
             ci[r] = C.ci[i]; ce[r] = C.ce[i]; mh[r] = C.mh[i]; cp[r] = C.cp[i]; mv[r] = C.mv[i];
-            mp0[r] = C.mp0[i]; mp1[r] = C.mp1[i]; order[r] = C.order[i]; cnext[r] = C.cnext[i];
+            mp0[r] = C.mp0[i]; mp1[r] = C.mp1[i]; cnext[r] = C.cnext[i];
         }
         WorldState st = W.hasState ? W.state : WorldState{};
+        {
+            // the contact list at the end of the world's 2 x cap order rows (room to prepend in front)
+            const int live = W.hasState ? st.contactCount : 0;
+            st.orderStart = 2 * cap - live;
+            for (int i = 0; i < live; ++i) order[2 * (size_t)d.contactBase + st.orderStart + i] = C.order[i];
+        }
         int freeHead = W.hasState ? W.state.freeContact : kNullIdx;
         for (int i = cap - 1; i >= old; --i) { cnext[d.contactBase + i] = freeHead; freeHead = i; }
         if (!W.hasState) st.contactCount = 0;
@@ -879,6 +894,7 @@ gb_status Upload(gb_world* g)
         st.allowSleep = W.def.allow_sleep; st.warmStarting = W.def.warm_starting;
         st.continuous = W.def.continuous_physics; st.subStepping = W.def.sub_stepping;
         st.error = 0;
+        st.gridValid = 0;
         states[wi] = st;
         for (int j = 0; j < d.jointCount; ++j) joints[d.jointBase + j] = W.joints[j];
         W.hasState = true;
@@ -893,7 +909,7 @@ gb_status Upload(gb_world* g)
         (s = Put(B.fat, fat, tp)) != GB_OK || (s = Put(B.pfix, pfix, tp)) != GB_OK || (s = Put(B.moved, moved, tp)) != GB_OK ||
         (s = Put(B.ci, ci, tc)) != GB_OK || (s = Put(B.ce, ce, tc)) != GB_OK || (s = Put(B.mh, mh, tc)) != GB_OK ||
         (s = Put(B.cp, cp, tc)) != GB_OK || (s = Put(B.mv, mv, tc)) != GB_OK || (s = Put(B.mp0, mp0, tc)) != GB_OK ||
-        (s = Put(B.mp1, mp1, tc)) != GB_OK || (s = Put(B.order, order, tc)) != GB_OK ||
+        (s = Put(B.mp1, mp1, tc)) != GB_OK || (s = Put(B.order, order, 2 * tc)) != GB_OK ||
         (s = Put(B.cnext, cnext, tc)) != GB_OK || (s = Put(B.joint, joints, tj)) != GB_OK)
         return s;
     GB_CUDA(cudaMemcpy(B.state, states.data(), nw * sizeof(WorldState), cudaMemcpyHostToDevice));
@@ -2178,7 +2194,8 @@ gb_status gb_get_contacts(gb_world* g, int w, int* ints, float* floats, int cap,
         GB_CUDA(cudaMemcpy(local.mp0.data(), g->batch.mp0 + d.contactBase, nc * sizeof(float4), cudaMemcpyDeviceToHost));
         GB_CUDA(cudaMemcpy(local.mp1.data(), g->batch.mp1 + d.contactBase, nc * sizeof(float4), cudaMemcpyDeviceToHost));
         if (n > 0)
-            GB_CUDA(cudaMemcpy(local.order.data(), g->batch.order + d.contactBase, n * sizeof(int), cudaMemcpyDeviceToHost));
+            GB_CUDA(cudaMemcpy(local.order.data(), g->batch.order + 2 * (size_t)d.contactBase + st.orderStart,
+                               n * sizeof(int), cudaMemcpyDeviceToHost));
         C = &local;
     }
     if (count) *count = n;

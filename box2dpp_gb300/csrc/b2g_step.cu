@@ -39,7 +39,8 @@ struct Wd {
     float4* cp;
     int4* mh;
     float4 *mv, *mp0, *mp1;
-    int* order;
+    int* order;      // the contact list: orderBase + st->orderStart
+    int* orderBase;
     int* cnext;
     Joint* jt;
     int *sBody, *sStack, *sWake;
@@ -66,6 +67,11 @@ struct Wd {
     int* pairKeep;
     int* movedList;
     int* liveProxies;
+    int* gridIds;
+    int* gridNext;
+    int* gridPrev;
+    int* gridCellOf;
+    int* gridHead;
     int4* pairInfo;
     unsigned char* islTab; // the world's global island-table region (d.islTabBytes bytes)
     int wIndex;            // the world's index in the batch
@@ -86,8 +92,12 @@ struct Wd {
         prop = B.prop + b; bi = B.bi + b; bj = B.bj + b;
         fi = B.fi + f; fm = B.fm + f; ff = B.ff + f; faabb = B.faabb + f; shape = B.shape + f;
         fat = B.fat + p; pfix = B.pfix + p; moved = B.moved + p; movedList = B.movedList + p; liveProxies = B.liveProxies + p;
+        gridIds = B.gridIds + p; gridNext = B.gridNext + p; gridPrev = B.gridPrev + p; gridCellOf = B.gridCellOf + p;
+        gridHead = B.gridHead + q + w;
         ci = B.ci + c; ce = B.ce + c; cp = B.cp + c; mh = B.mh + c; mv = B.mv + c; mp0 = B.mp0 + c; mp1 = B.mp1 + c;
-        order = B.order + c; cnext = B.cnext + c;
+        orderBase = B.order + 2 * (size_t)c;
+        order = orderBase + st->orderStart;
+        cnext = B.cnext + c;
         jt = B.joint + j; sJoint = B.sJoint + j;
         sBody = B.sBody + d.rowBase; sPos = B.sPos + d.rowBase; sVel = B.sVel + d.rowBase;
         rowMask = B.rowMask + d.rowBase; sVelL = B.sVelL + d.rowBase;
@@ -389,19 +399,20 @@ struct Wd {
 
     // ---------------------------------------------------------------- broadphase
     // b2Fixture::Synchronize + b2DynamicTree::MoveProxy (b2Fixture.cpp:154-177, b2DynamicTree.cpp:133-177)
-    __device__ void syncFixtures(int b)
+    // movedOut (optional, one thread): the proxies this call marks moved are appended to movedList
+    __device__ void syncFixtures(int b, int* movedOut = nullptr)
     {
         float4 s0 = sw0[b], m = mas[b];
         Xf xf1;
         xf1.q = RotOf(s0.z);
         xf1.p = V(s0.x, s0.y) - Mul(xf1.q, V(m.z, m.w));
-        syncFixturesFrom(b, xf1, xform(b));
+        syncFixturesFrom(b, xf1, xform(b), movedOut);
     }
 
     // b2Fixture::Synchronize (Dynamics/b2Fixture.cpp:154-177) of every fixture of body b between two
     // transforms, with b2BroadPhase::MoveProxy (b2DynamicTree.cpp:133-177): the swept AABB, and a
     // new fat AABB (grown by the extension and the predicted displacement) when it left the old one.
-    __device__ void syncFixturesFrom(int b, const Xf& xf1, const Xf& xf2)
+    __device__ void syncFixturesFrom(int b, const Xf& xf1, const Xf& xf2, int* movedOut = nullptr)
     {
         B2G_WALK(f, bi[b].z, fi[f].y, d.fixCount + 1) {
             int pid = fi[f].z;
@@ -418,6 +429,7 @@ struct Wd {
             if (dd.x < 0.0f) nb.x += dd.x; else nb.z += dd.x;
             if (dd.y < 0.0f) nb.y += dd.y; else nb.w += dd.y;
             fat[pid] = nb;
+            if (movedOut && moved[pid] == 0) movedList[(*movedOut)++] = pid;
             moved[pid] = 1;
         }
     }
@@ -516,8 +528,9 @@ struct Wd {
     __device__ static bool primaryOrder(int t1, int t2) { return t1 == t2 || (t1 == kPolygon && t2 == kCircle) || t1 == kEdge; }
 
     // b2ContactManager::FindNewContacts -> b2BroadPhase::UpdatePairs -> AddPair, CTA-wide.
-    __device__ void findNewContacts();
+    __device__ void findNewContacts(bool inToi = false, int knownMoved = -1);
     __device__ void gridPairs(int m, int* pairCount);
+    __device__ void gridEventPairs(int m, int* pairCount);
     __device__ void collide();
     __device__ void solve(const StepParams& P, float4* smem, int smemRows, int smemContacts);
     template <class L>
@@ -844,6 +857,34 @@ __device__ void Wd::gridPairs(int m, int* pairCount)
         if (i == nSmall - 1 || (unsigned)(keys[i + 1] >> 32) != c) cellEnd[c] = i + 1;
     }
     __syncthreads();
+    // the grid kept for the continuous phase's events: each cell (and the large proxies, list nCells)
+    // as a doubly linked list in the sorted order
+    for (int i = tid(); i < nLive; i += nthreads()) {
+        const unsigned long long k = keys[i];
+        const int p = (int)(k & 0xffffffffu);
+        const bool small = i < nSmall;
+        const int c = small ? (int)(k >> 32) : nCells;
+        const int lo = small ? cellStart[c] : nSmall, hi = small ? cellEnd[c] : nLive;
+        gridIds[i] = p;
+        gridPrev[p] = i > lo ? (int)(keys[i - 1] & 0xffffffffu) : -1;
+        gridNext[p] = i + 1 < hi ? (int)(keys[i + 1] & 0xffffffffu) : -1;
+        gridCellOf[p] = c;
+    }
+    for (int c = tid(); c <= nCells; c += nthreads()) {
+        if (c < nCells) gridHead[c] = cellEnd[c] > cellStart[c] ? (int)(keys[cellStart[c]] & 0xffffffffu) : -1;
+        else gridHead[c] = nLive > nSmall ? (int)(keys[nSmall] & 0xffffffffu) : -1;
+    }
+    if (tid() == 0) {
+        st->gridValid = 1;
+        st->gridNx = nx;
+        st->gridNy = ny;
+        st->gridLive = nLive;
+        st->gridOx = ox;
+        st->gridOy = oy;
+        st->gridInvH = invH;
+        st->gridW = W;
+        st->gridWLarge = wLarge;
+    }
     auto test = [&](int p, int q, const float4& Fq) {
         if (p == q) return;
         if (moved[p] && p < q) return;
@@ -884,20 +925,116 @@ __device__ void Wd::gridPairs(int m, int* pairCount)
     __syncthreads();
 }
 
-__device__ void Wd::findNewContacts()
+// The pairs of a continuous-phase event's moved proxies from the grid the step's pair finding kept:
+// thread 0 moves each moved proxy to the cell list of its current box (so every live proxy sits in
+// the list of its current low corner, or in the large proxies' list), then each moved proxy walks
+// the lists of the cells its box can reach. Every live proxy is in exactly one list, so a pair is
+// met once (both moved: from the lower id, as in the other paths).
+__device__ void Wd::gridEventPairs(int m, int* pairCount)
 {
-    __shared__ int sMoved, sPairs, sNew, sKept, sLive;
-    if (tid() == 0) { sMoved = 0; sPairs = 0; sNew = 0; }
+    constexpr int kLargeCap = 64;
+    __shared__ int sLargeQ[kLargeCap];
+    __shared__ int sNLargeQ;
+    const int nx = st->gridNx, ny = st->gridNy, nCells = nx * ny, nLive = st->gridLive;
+    const float ox = st->gridOx, oy = st->gridOy, invH = st->gridInvH, wLarge = st->gridWLarge;
+    auto size = [](const float4& f) { return fmaxf(f.z - f.x, f.w - f.y); };
+    auto cellOf = [&](float x, float o, int n) {
+        const float c = fminf(fmaxf(floorf((x - o) * invH), -1.0f), (float)n);
+        return (int)c;
+    };
+    if (tid() == 0) {
+        float W = st->gridW;
+        for (int t = 0; t < m; ++t) {
+            const int q = movedList[t];
+            const float4 f = fat[q];
+            int c = nCells;
+            if (!(size(f) > wLarge)) {
+                c = min(max(cellOf(f.y, oy, ny), 0), ny - 1) * nx + min(max(cellOf(f.x, ox, nx), 0), nx - 1);
+                W = fmaxf(W, fmaxf(size(f), 0.0f) * 1.0001f + 1e-4f);
+            }
+            const int old = gridCellOf[q];
+            if (old == c) continue;
+            const int pv = gridPrev[q], nt = gridNext[q];
+            if (pv >= 0) gridNext[pv] = nt;
+            else gridHead[old] = nt;
+            if (nt >= 0) gridPrev[nt] = pv;
+            const int h = gridHead[c];
+            gridPrev[q] = -1;
+            gridNext[q] = h;
+            if (h >= 0) gridPrev[h] = q;
+            gridHead[c] = q;
+            gridCellOf[q] = c;
+        }
+        st->gridW = W;
+        sNLargeQ = 0;
+    }
+    __syncthreads();
+    const float W = st->gridW;
+    auto test = [&](int p, int q, const float4& Fq) {
+        if (p == q) return;
+        if (moved[p] && p < q) return;
+        if (!Overlap(fat[p], Fq)) return;
+        const int k = atomicAdd(pairCount, 1);
+        const unsigned long long lo = (unsigned long long)(p < q ? p : q), hi = (unsigned long long)(p < q ? q : p);
+        if (k < d.pairCap) pairs[k] = (lo << 32) | hi;
+    };
+    // a list walk visits at most every live proxy once; a longer one would mean broken links
+    auto walk = [&](int c, int q, const float4& Fq) {
+        int guard = 0;
+        for (int p = gridHead[c]; p >= 0; p = gridNext[p]) {
+            if (++guard > nLive) { atomicOr(&st->error, kErrInvalid); break; }
+            test(p, q, Fq);
+        }
+    };
+    for (int t = tid(); t < m; t += nthreads()) {
+        const int q = movedList[t];
+        const float4 Fq = fat[q];
+        if (size(Fq) > wLarge) {
+            const int slot = atomicAdd(&sNLargeQ, 1);
+            if (slot < kLargeCap) sLargeQ[slot] = q;
+            else for (int j = 0; j < nLive; ++j) test(gridIds[j], q, Fq);
+            continue;
+        }
+        const float lowX = Fq.x - W - 1e-4f * fabsf(Fq.x), lowY = Fq.y - W - 1e-4f * fabsf(Fq.y);
+        const int cx0 = max(cellOf(lowX, ox, nx), 0), cx1 = min(cellOf(Fq.z, ox, nx), nx - 1);
+        const int cy0 = max(cellOf(lowY, oy, ny), 0), cy1 = min(cellOf(Fq.w, oy, ny), ny - 1);
+        for (int cy = cy0; cy <= cy1; ++cy)
+            for (int cx = cx0; cx <= cx1; ++cx) walk(cy * nx + cx, q, Fq);
+        walk(nCells, q, Fq);
+    }
+    __syncthreads();
+    const int nLarge = min(sNLargeQ, kLargeCap);
+    for (int l = 0; l < nLarge; ++l) {
+        const int q = sLargeQ[l];
+        const float4 Fq = fat[q];
+        for (int j = tid(); j < nLive; j += nthreads()) test(gridIds[j], q, Fq);
+    }
+    __syncthreads();
+}
+
+// knownMoved >= 0: movedList already holds that many moved proxies (a continuous-phase event lists
+// the proxies its synchronisation moves), so the proxy range is not scanned for them.
+__device__ void Wd::findNewContacts(bool inToi, int knownMoved)
+{
+    __shared__ int sMoved, sPairs, sNew, sKept, sLive, sEventGrid;
+    if (tid() == 0) {
+        sMoved = 0; sPairs = 0; sNew = 0;
+        // a continuous-phase event queries the grid the step kept; any other call builds it anew
+        sEventGrid = inToi && st->gridValid ? 1 : 0;
+        if (!inToi) st->gridValid = 0;
+    }
     __syncthreads();
     const unsigned long long tPairs0 = clock64();
     const int np = d.proxyCap;
-    for (int p0 = 0; p0 < np; p0 += nthreads()) {
-        const int p = p0 + tid();
-        const int i = WarpAppend(p < np && moved[p] != 0, &sMoved);
-        if (i >= 0) movedList[i] = p;
+    if (knownMoved < 0) {
+        for (int p0 = 0; p0 < np; p0 += nthreads()) {
+            const int p = p0 + tid();
+            const int i = WarpAppend(p < np && moved[p] != 0, &sMoved);
+            if (i >= 0) movedList[i] = p;
+        }
     }
     __syncthreads();
-    const int m = sMoved;
+    const int m = knownMoved < 0 ? sMoved : knownMoved;
     // Query every moved proxy's fat AABB against all proxies (b2BroadPhase.h:188-217); a pair whose
     // both proxies moved is emitted once, from the lower proxy id. Proxy ids are tree node ids, so
     // about half the id range is internal nodes: the live proxies (those with a fixture) are listed
@@ -911,7 +1048,7 @@ __device__ void Wd::findNewContacts()
     int* liveList = staged ? sId : liveProxies;
     if (tid() == 0) sLive = 0;
     __syncthreads();
-    if (m > 0) {
+    if (m > 0 && !sEventGrid) {
         for (int p0 = 0; p0 < np; p0 += nthreads()) {
             const int p = p0 + tid();
             const int i = WarpAppend(p < np && pfix[p] >= 0, &sLive);
@@ -926,7 +1063,9 @@ __device__ void Wd::findNewContacts()
     __syncthreads();
     const int nLive = sLive;
     const long long total = (long long)m * nLive;
-    if (total > kSweepThreshold) {
+    if (sEventGrid) {
+        if (m > 0) gridEventPairs(m, &sPairs);
+    } else if (total > kSweepThreshold) {
         __syncthreads();
         gridPairs(m, &sPairs);
     } else
@@ -1076,16 +1215,27 @@ __device__ void Wd::findNewContacts()
         }
     }
     __syncthreads();
-    // order = reverse(new) ++ order (the pair-keep flags are dead now: reuse them as the copy buffer)
+    // order = reverse(new) ++ order: the new contacts go in front of the list's first row; when the
+    // rows in front have run out, the list first moves to the end of the world's 2 x contactCap rows
+    // (the pair-keep flags are dead now: the copy buffer)
     if (created > 0) {
         const int live = st->contactCount;
-        int* tmp = pairKeep;
-        for (int i = tid(); i < live; i += nthreads()) tmp[i] = order[i];
+        int start = st->orderStart;
+        if (start < created) {
+            int* tmp = pairKeep;
+            for (int i = tid(); i < live; i += nthreads()) tmp[i] = order[i];
+            __syncthreads();
+            start = 2 * d.contactCap - live;
+            for (int i = tid(); i < live; i += nthreads()) orderBase[start + i] = tmp[i];
+        }
+        start -= created;
+        for (int i = tid(); i < created; i += nthreads()) orderBase[start + created - 1 - i] = sContact[i];
         __syncthreads();
-        for (int i = tid(); i < live; i += nthreads()) order[i + created] = tmp[i];
-        for (int i = tid(); i < created; i += nthreads()) order[created - 1 - i] = sContact[i];
-        __syncthreads();
-        if (tid() == 0) st->contactCount = live + created;
+        order = orderBase + start;
+        if (tid() == 0) {
+            st->orderStart = start;
+            st->contactCount = live + created;
+        }
     }
     for (int i = tid(); i < m; i += nthreads()) moved[movedList[i]] = 0;
     __syncthreads();
@@ -2123,7 +2273,7 @@ __device__ void Wd::solveTOI(const StepParams& P)
     // colourList, deduplicated by the event stamp in evType) are the only ones classified again; the
     // first pass classifies the whole list. These scratch columns belong to the collide and solve
     // phases, which set them before use.
-    __shared__ int sDirty, sNeed;
+    __shared__ int sDirty, sNeed, sEvMoved;
     __shared__ int sSortT[kMaxToiCta * 2], sSortC[kMaxToiCta * 2];
     if (tid() == 0) sDirty = 0;
     for (int event = 0;; ++event) {
@@ -2342,6 +2492,7 @@ __device__ void Wd::solveTOI(const StepParams& P)
         if (tid() == 0) {
             st->toiEvents = event + 1;
             sDirty = 0;
+            int nMovedEv = 0;  // proxies the event's fixture synchronisation moves (listed in movedList)
             const int mc = sMin;
             const float minAlpha = sMinAlpha;
             int4 info = ci[mc];
@@ -2497,7 +2648,7 @@ __device__ void Wd::solveTOI(const StepParams& P)
                     bi[b].y &= ~kBIsland;
                     if (bi[b].x == kStatic) continue;
                     const bool dynamic = bi[b].x == kDynamic;
-                    if (dynamic) syncFixtures(b);
+                    if (dynamic) syncFixtures(b, &nMovedEv);
                     else if (((woke >> i) & 1ull) == 0ull) continue;
                     B2G_WALK(e, bi[b].w, eNext(e), 2 * d.contactCap + 2) {
                         const int c = e >> 1;
@@ -2514,11 +2665,12 @@ __device__ void Wd::solveTOI(const StepParams& P)
                 colourList[sDirty++] = mc;
             }
             sDone = skip ? 2 : 0;
+            sEvMoved = nMovedEv;
         }
         __syncthreads();
         stamp(20);
         if (sDone == 2) continue;
-        findNewContacts();
+        findNewContacts(true, sEvMoved);
         __syncthreads();
         {
             // the contacts the event created sit at the head of the list

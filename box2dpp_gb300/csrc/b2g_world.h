@@ -73,6 +73,13 @@ struct WorldState {
     int eventsDropped;  // 1 when the log ran out of room
     int staged;         // 1 while this step's manifolds wait in the stage (NarrowphaseKernel -> collide)
     int toiPrepared;    // 1 while this step's first time-of-impact pass is done (ToiKernel -> solveTOI)
+    // the uniform grid of the step's pair finding, kept for the continuous phase's events (cells as
+    // linked lists that an event's moved proxies relink): valid while gridValid is 1
+    int gridValid, gridNx, gridNy, gridLive;
+    // the contact list (newest first) is order[orderStart, orderStart + contactCount) of the world's
+    // 2 x contactCap order rows: new contacts are prepended in front of it without moving the rest
+    int orderStart;
+    float gridOx, gridOy, gridInvH, gridW, gridWLarge;
     // SM clock cycles of the last step per phase: 0 new-fixture pairs, 1 collide, 2 island DFS,
     // 3 island solve, 4 fixture sync, 5 pairs after solve, 6 TOI, 7 whole step; then the island solve
     // split: 8 integrate + constraint init, 9 warm start + velocity sweeps, 10 impulses + position
@@ -256,6 +263,11 @@ struct Batch {
     int4* pairInfo;  // pair-sized: a new contact's fixtures and bodies, worked out before creation
     int* movedList;  // proxy-sized
     int* liveProxies; // proxy-sized: pair finding's list of live proxies when it is not in shared memory
+    int* gridIds;     // proxy-sized: the live proxies of the kept grid
+    int* gridNext;    // proxy-sized: next proxy in the same cell list (-1 at the end)
+    int* gridPrev;    // proxy-sized: previous proxy in the same cell list (-1 at the head)
+    int* gridCellOf;  // proxy-sized: the cell list holding the proxy (nx * ny: the large proxies' list)
+    int* gridHead;    // pair-sized: first proxy of each cell list (nx * ny + 1 lists)
     unsigned char* islTab; // island-DFS tables of the worlds whose table does not fit in shared memory
     // A user contact filter (b2World::SetContactFilter): verdicts of b2ContactFilter::ShouldCollide per
     // (world, fixtureA, fixtureB) in an open-addressing table (filterCap slots, a power of two; key
