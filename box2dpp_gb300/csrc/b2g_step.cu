@@ -782,15 +782,32 @@ __device__ void Wd::gridPairs(int m, int* pairCount)
     __syncthreads();
     const int nLive = sLive;
     const float wLarge = 4.0f * (sSizeSum / (float)max(nLive, 1));
-    for (int p = tid(); p < np; p += nthreads()) {
-        if (pfix[p] < 0) continue;
-        const float4 f = fat[p];
-        if (size(f) > wLarge) continue;
-        atomicMax(&sMaxW, __float_as_uint(fmaxf(size(f), 0.0f)));
-        atomicMin(&sMinX, OrderedBits(f.x));
-        atomicMin(&sMinY, OrderedBits(f.y));
-        atomicMax(&sMaxX, OrderedBits(f.x));
-        atomicMax(&sMaxY, OrderedBits(f.y));
+    {
+        // extents of the small proxies: per thread, then per warp, then one atomic per warp
+        unsigned maxW = 0u, minX = 0xffffffffu, minY = 0xffffffffu, maxX = 0u, maxY = 0u;
+        for (int p0 = 0; p0 < np; p0 += nthreads()) {
+            const int p = p0 + tid();
+            if (p >= np || pfix[p] < 0) continue;
+            const float4 f = fat[p];
+            if (size(f) > wLarge) continue;
+            maxW = max(maxW, __float_as_uint(fmaxf(size(f), 0.0f)));
+            minX = min(minX, OrderedBits(f.x));
+            minY = min(minY, OrderedBits(f.y));
+            maxX = max(maxX, OrderedBits(f.x));
+            maxY = max(maxY, OrderedBits(f.y));
+        }
+        maxW = __reduce_max_sync(0xffffffffu, maxW);
+        minX = __reduce_min_sync(0xffffffffu, minX);
+        minY = __reduce_min_sync(0xffffffffu, minY);
+        maxX = __reduce_max_sync(0xffffffffu, maxX);
+        maxY = __reduce_max_sync(0xffffffffu, maxY);
+        if ((tid() & 31) == 0) {
+            atomicMax(&sMaxW, maxW);
+            atomicMin(&sMinX, minX);
+            atomicMin(&sMinY, minY);
+            atomicMax(&sMaxX, maxX);
+            atomicMax(&sMaxY, maxY);
+        }
     }
     __syncthreads();
     // the grid: cell size h >= the largest small proxy, at most cellCap cells (h grows to fit)
@@ -817,17 +834,24 @@ __device__ void Wd::gridPairs(int m, int* pairCount)
     unsigned long long* keys = reinterpret_cast<unsigned long long*>(pairInfo);
     // keys: cell << 32 | proxy for the small proxies, all-ones << 32 | proxy for the large ones, so
     // they sort last
-    for (int p = tid(); p < np; p += nthreads()) {
-        if (pfix[p] < 0) continue;
-        const float4 f = fat[p];
-        const bool large = size(f) > wLarge;
-        unsigned hi = 0xffffffffu;
-        if (!large) {
-            const int cx = min(max(cellOf(f.x, ox, nx), 0), nx - 1), cy = min(max(cellOf(f.y, oy, ny), 0), ny - 1);
-            hi = (unsigned)(cy * nx + cx);
-            atomicAdd(&sSmall, 1);
+    {
+        int small = 0;
+        for (int p0 = 0; p0 < np; p0 += nthreads()) {
+            const int p = p0 + tid();
+            const bool live = p < np && pfix[p] >= 0;
+            unsigned hi = 0xffffffffu;
+            if (live) {
+                const float4 f = fat[p];
+                if (!(size(f) > wLarge)) {
+                    const int cx = min(max(cellOf(f.x, ox, nx), 0), nx - 1), cy = min(max(cellOf(f.y, oy, ny), 0), ny - 1);
+                    hi = (unsigned)(cy * nx + cx);
+                    ++small;
+                }
+            }
+            const int slot = WarpAppend(live, &sCursor);
+            if (slot >= 0) keys[slot] = ((unsigned long long)hi << 32) | (unsigned)p;
         }
-        keys[atomicAdd(&sCursor, 1)] = ((unsigned long long)hi << 32) | (unsigned)p;
+        atomicAdd(&sSmall, small);
     }
     __syncthreads();
     int P2 = 1;
