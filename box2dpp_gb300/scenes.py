@@ -666,7 +666,7 @@ def config2(n_bodies: int = 10000, seed: int = 1, allow_sleep: bool = True) -> S
 
 def config4(n_worlds: int, first_seed: int, n_bodies: int = 256, allow_sleep: bool = False) -> list:
     """Worlds of the config-2 mix (circles / convex polygons dropped into an edge container), one per
-    seed first_seed, first_seed + 1, ...: the scenes the learned warm start is trained and judged on.
+    seed first_seed, first_seed + 1, ...: the scenes the learned warm start is trained and evaluated on.
     n_bodies per world (the full-size mix has 10,000 in a 200 m box; the container here scales with
     the body count as in drop())."""
     return [drop(n_bodies, SplitMix64(first_seed + k), allow_sleep=allow_sleep) for k in range(n_worlds)]

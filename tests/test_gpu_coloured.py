@@ -1,7 +1,7 @@
 """The graph-coloured island solver against the plain (reference-order) solver on the GPU.
 
 The coloured solver is not bit-exact with the reference (its Gauss-Seidel order differs), so it is
-judged the way the solver variants are compared: the velocity residual it reaches, the physical
+checked the way the solver variants are compared: the velocity residual it reaches, the physical
 state it settles into, run-to-run determinism, and the iterations a residual tolerance saves.
 """
 from __future__ import annotations
