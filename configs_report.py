@@ -10,8 +10,9 @@ Configurations (the batched one is bench.py's):
      sleep off, steps 1..60.
 
 GPU: one world per handle, the plain (reference-order, bit-exact) and the graph-coloured solver,
-8/3 iterations, one CTA of each --threads width (every width computes the same bits), each step timed
-with CUDA events on the handle's stream; body-steps/s over the timed steps. CPU: the oracle's restatement of b2World::Step (plain order) with glibc's sinf/cosf (the
+8/3 iterations, one CTA of each --threads width (every width computes the same bits), every step
+replayed from the captured graph and timed in blocks of 50 steps with CUDA events on the handle's
+stream; body-steps/s over the timed steps. CPU: the oracle's restatement of b2World::Step (plain order) with glibc's sinf/cosf (the
 reference's own trig) on one thread, stepped from the same initial state for as many of the same
 steps as fit in --cpu-seconds. Prints one JSON line per configuration. A CPU-baseline reporter like
 bench.py's CPU leg: it sits beside bench.py, outside the package, because it runs the oracle.
@@ -54,14 +55,20 @@ def gpu_rate(sc, steps: int, solver: str, threads: int) -> dict:
     w.set_stream(stream.cuda_stream)
     w.upload()
     w.set_launch_plan([[0, 1, threads, 640, 1024]])
+    # every step replayed from the captured graph (as the benchmark steps), timed in blocks of 50
+    # steps between CUDA events on the handle's stream
     ms = []
-    for _ in range(steps):
+    done = 0
+    while done < steps:
+        k = min(50, steps - done)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        w.step(DT, VI, PI)
+        for _ in range(k):
+            w.graph_step(DT, VI, PI)
         b.record(stream)
         b.synchronize()
-        ms.append(a.elapsed_time(b))
+        ms.extend([a.elapsed_time(b) / k] * k)
+        done += k
     w.sync()
     n = w.dynamic_bodies
     w.close()
