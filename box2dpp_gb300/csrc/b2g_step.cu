@@ -2298,6 +2298,13 @@ __device__ void Wd::solveTOI(const StepParams& P)
     // first pass classifies the whole list. These scratch columns belong to the collide and solve
     // phases, which set them before use.
     __shared__ int sDirty, sNeed, sEvMoved;
+    // blocks of the earliest-event selection whose minimum an event made stale (listed as they are
+    // marked; more than kStaleCap: every block's flag is read instead), and the block count the
+    // previous selection covered (blocks beyond it are new and always computed)
+    constexpr int kStaleCap = 256;
+    __shared__ int sStale[kStaleCap];
+    __shared__ int sNStale, sNBlkPrev;
+    if (tid() == 0) { sNStale = 0; sNBlkPrev = 0; }
     __shared__ int sSortT[kMaxToiCta * 2], sSortC[kMaxToiCta * 2];
     if (tid() == 0) sDirty = 0;
     for (int event = 0;; ++event) {
@@ -2446,7 +2453,12 @@ __device__ void Wd::solveTOI(const StepParams& P)
                 evType[c] = 0;
             } else {
                 t = cColour[c];
-                vimpL[t / kSelBlock].z = 1.0f;  // its block's minimum is stale
+                // its block's minimum is stale: flag it, and list it the first time
+                const int bk = t / kSelBlock;
+                if (atomicExch(reinterpret_cast<int*>(&vimpL[bk]) + 2, __float_as_int(1.0f)) == 0) {
+                    const int slot = atomicAdd(&sNStale, 1);
+                    if (slot < kStaleCap) sStale[slot] = bk;
+                }
             }
             vsep[t] = make_float2(T.kind != 0 ? cp[c].w : 2.0f, __int_as_float(c));
         }
@@ -2460,8 +2472,13 @@ __device__ void Wd::solveTOI(const StepParams& P)
         {
             const int nBlk = (n + kSelBlock - 1) / kSelBlock;
             const int lane = tid() & 31, nWarps = nthreads() >> 5;
-            for (int bk = tid() >> 5; bk < nBlk; bk += nWarps) {
-                if (event > 0 && vimpL[bk].z == 0.0f) continue;
+            const int nStale = sNStale, nPrev = sNBlkPrev;
+            const bool full = event == 0 || nStale > kStaleCap;
+            const int nWork = full ? nBlk : nStale + max(nBlk - nPrev, 0);
+            for (int i = tid() >> 5; i < nWork; i += nWarps) {
+                const int bk = full ? i : (i < nStale ? sStale[i] : nPrev + (i - nStale));
+                if (full && event > 0 && vimpL[bk].z == 0.0f) continue;
+                if (!full && i < nStale && bk >= nPrev) continue;  // a new block: computed below
                 float ba = 1.0f;
                 int bt = -1;
                 for (int t = bk * kSelBlock + lane; t < min(n, (bk + 1) * kSelBlock); t += 32) {
@@ -2498,6 +2515,8 @@ __device__ void Wd::solveTOI(const StepParams& P)
                 }
             }
             int minC = minT < 0 ? kNullIdx : __float_as_int(vsep[minT].y);
+            sNStale = 0;
+            sNBlkPrev = (n + kSelBlock - 1) / kSelBlock;
             sMin = minC;
             sMinAlpha = minAlpha;
             sDone = 0;
