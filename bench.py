@@ -10,7 +10,8 @@ second (dynamic bodies x steps / time) over the whole job, at a matched velocity
 Every arm runs the same simulation steps: PRE_STEPS steps (the launch-plan autotuner's trials on
 the GPU), W warm-up steps, then the K timed steps.
 arms.plain: the reference-order solver (bit-exact with the reference), 8/3 iterations; its median
-velocity residual at the last timed step is the accuracy every other arm must reach.
+velocity residual (measured on the step after the timed window, which the timed steps do not spend
+time on) is the accuracy every other arm must reach.
 arms.coloured: the graph-coloured island solver at the fewest velocity iterations (of COLOURED_VI)
 whose median residual is no larger than plain's (coloured_search lists each try).
 arms.learned: the reference-order solver with the learned warm start (a network trained first by the
@@ -274,7 +275,7 @@ def _prepare(worlds, stream, solver: str, vi: int, warmup: int, plan=None, mlp=N
 
     w = World(worlds)
     w.set_stream(stream.cuda_stream)
-    w.set_solver(solver, measure_residual=True)
+    w.set_solver(solver)
     w.upload()
     if mlp is not None:
         w.set_warm_start(mlp, all_points=True)
@@ -389,7 +390,13 @@ def run_gpu(args):
         barrier()
         w.sync()
         t_after = w.totals()
+        # the accuracy of the arm: the velocity residual measured on the step after the timed window
+        # (measuring it is a diagnostic, not part of b2World::Step, so the timed steps do not)
+        w.set_solver(solver, measure_residual=True)
+        w.graph_step(DT, vi, PI)
+        w.sync()
         _, _, res = w.solver_stats()
+        w.set_solver(solver)
         chosen, cand_ms = w.launch_plan()
         rec = {"solver": solver, "warm_start": "reference" if mlp is None else "learned", "velocity_iterations": vi,
                "value": total_bodies * args.steps / (ms / 1e3),
@@ -514,7 +521,8 @@ def run_gpu(args):
             "learned_training": learned_info,
             "residual_definition": "max over contact points of the natural-map residual in m/s: |vn - bias| on "
                                    "active normal points, |vt| on friction inside its cone, 0 at a solution; after "
-                                   "the velocity iterations; median over worlds at the last timed step",
+                                   "the velocity iterations; median over worlds at the step after the timed window "
+                                   "(the timed steps do not measure it)",
             "sleep_on": sleep_on,
             "roofline": roof,
             "e2e": head["e2e"],
