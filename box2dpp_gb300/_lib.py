@@ -32,7 +32,7 @@ EXPORTS = [
     "gb_mlp_forward", "gb_mlp_gradients", "gb_mlp_train", "gb_world_set_warm_start", "gb_world_warm_stats",
     "gb_world_set_contact_log", "gb_world_read_contact_log", "gb_world_contact_stats", "gb_world_set_events",
     "gb_world_read_events", "gb_world_query_aabb", "gb_world_raycast", "gb_create_joints",
-    "gb_world_stage_times", "gb_body_edits", "gb_world_set_limits", "gb_destroy_body", "gb_destroy_joint",
+    "gb_world_stage_times", "gb_body_edits", "gb_world_set_limits", "gb_world_set_settings", "gb_world_clear_forces", "gb_destroy_body", "gb_destroy_joint",
     "gb_destroy_fixture", "gb_world_raycast_all", "gb_world_get_profile", "gb_world_step_begin",
     "gb_contact_edits", "gb_world_step_end", "gb_world_set_contact_filter", "gb_world_refilter",
     "gb_world_filter_stats",
@@ -125,6 +125,8 @@ def load(build_if_missing: bool = True):
         "gb_collide_noalloc": [i, _i32, _f32, _i32, _f32, _i32, _f32, _i32, _f32, _i32, _f32],
         "gb_world_set_solver": [vp, i, f, i],
         "gb_world_set_limits": [vp, i, i],
+        "gb_world_set_settings": [vp, i, C.POINTER(WorldDef), i],
+        "gb_world_clear_forces": [vp, i],
         "gb_world_step_begin": [vp, f, i, i],
         "gb_contact_edits": [vp, i, C.c_void_p],
         "gb_world_step_end": [vp],

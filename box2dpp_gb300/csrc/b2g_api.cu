@@ -73,6 +73,7 @@ struct HContacts { // device contact columns of one world, pulled back before a 
 
 struct HWorld {
     gb_world_def def{};
+    bool autoClear = true;  // b2World::SetAutoClearForces
     int bodyList = kNullIdx, jointList = kNullIdx;
     std::vector<HBody> bodies;
     std::vector<HFixture> fixtures;
@@ -893,6 +894,7 @@ gb_status Upload(gb_world* g)
         if (!W.hasState) { st.stepComplete = 1; st.inv_dt0 = 0.0f; }
         st.allowSleep = W.def.allow_sleep; st.warmStarting = W.def.warm_starting;
         st.continuous = W.def.continuous_physics; st.subStepping = W.def.sub_stepping;
+        st.clearForces = W.autoClear ? 1 : 0;
         st.error = 0;
         st.gridValid = 0;
         states[wi] = st;
@@ -1823,6 +1825,43 @@ gb_status gb_world_sync(gb_world* g)
     if (err & kErrCapacity) return GB_ERR_CAPACITY;
     if (err & kErrTimeout) return GB_ERR_TIMEOUT;
     if (err & kErrInvalid) return GB_ERR_INVALID;
+    return GB_OK;
+}
+
+// b2World::SetGravity, SetAllowSleeping, SetWarmStarting, SetContinuousPhysics, SetSubStepping and
+// SetAutoClearForces (Dynamics/b2World.h:145-217, b2World.cpp:370-385) between steps: turning sleep
+// off wakes every body of the world's body list (b2Body::SetAwake(true): awake, sleep time 0).
+gb_status gb_world_set_settings(gb_world* g, int w, const gb_world_def* def, int auto_clear_forces)
+{
+    if (!g || !def || w < 0 || w >= (int)g->worlds.size() || g->locked) return GB_ERR_INVALID;
+    gb_status s = Mutable(g, w);
+    if (s != GB_OK) return s;
+    HWorld& W = g->worlds[w];
+    if (W.def.allow_sleep && !def->allow_sleep) {
+        int guard = 0;
+        for (int b = W.bodyList; b != kNullIdx && guard <= (int)W.bodies.size(); b = W.bodies[b].next, ++guard) {
+            HBody& B = W.bodies[b];
+            if ((B.flags & kBAwake) == 0) {
+                B.flags |= kBAwake;
+                B.sleepTime = 0.0f;
+            }
+        }
+    }
+    W.def = *def;
+    W.autoClear = auto_clear_forces != 0;
+    return GB_OK;
+}
+
+// b2World::ClearForces (Dynamics/b2World.cpp:967-974): every body's force and torque zeroed.
+gb_status gb_world_clear_forces(gb_world* g, int w)
+{
+    if (!g || w < 0 || w >= (int)g->worlds.size() || g->locked) return GB_ERR_INVALID;
+    gb_status s = Mutable(g, w);
+    if (s != GB_OK) return s;
+    for (HBody& B : g->worlds[w].bodies) {
+        B.force = V(0.0f, 0.0f);
+        B.torque = 0.0f;
+    }
     return GB_OK;
 }
 

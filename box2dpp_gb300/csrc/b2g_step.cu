@@ -2959,7 +2959,8 @@ __global__ void __launch_bounds__(kThreads, 384 / kThreads) StepToiKernel(Batch 
     const unsigned long long t0 = clock64();
     if (W.st->continuous && P.dt > 0.0f) W.solveTOI(P);
     __syncthreads();
-    for (int b = tid(); b < W.d.bodyCount; b += nthreads()) W.frc[b] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (W.st->clearForces)
+        for (int b = tid(); b < W.d.bodyCount; b += nthreads()) W.frc[b] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (tid() == 0) {
         if (P.dt > 0.0f) W.st->inv_dt0 = 1.0f / P.dt;
         const unsigned long long t1 = clock64();

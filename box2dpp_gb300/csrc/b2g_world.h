@@ -57,6 +57,7 @@ struct WorldState {
     int newFixture;     // b2World::e_newFixture
     int stepComplete;
     int allowSleep, warmStarting, continuous, subStepping;
+    int clearForces;    // b2World's e_clearForces: forces and torques cleared at the end of each step
     int error;          // kErr* bits
     int toiEvents;      // TOI sub-steps taken in the last step (diagnostic)
     int islands;        // islands solved in the last step (diagnostic)

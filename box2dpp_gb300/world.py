@@ -151,6 +151,21 @@ class World:
         """b2Body::DestroyFixture; returns its EndContact calls as rows {2, fixtureA, fixtureB}."""
         return self._destroy("gb_destroy_fixture", fixture, w)
 
+    def set_settings(self, gravity, allow_sleep: bool, warm_starting: bool, continuous: bool, sub_stepping: bool,
+                     auto_clear_forces: bool = True, w: int = 0) -> None:
+        """b2World::SetGravity, SetAllowSleeping (turning it off wakes every body), SetWarmStarting,
+        SetContinuousPhysics, SetSubStepping and SetAutoClearForces of world w between steps."""
+        d = _lib.WorldDef()
+        d.gravity_x, d.gravity_y = float(gravity[0]), float(gravity[1])
+        d.allow_sleep, d.warm_starting = int(allow_sleep), int(warm_starting)
+        d.continuous_physics, d.sub_stepping = int(continuous), int(sub_stepping)
+        _lib.check(self.lib.gb_world_set_settings(self.h, int(w), C.byref(d), int(auto_clear_forces)),
+                   "gb_world_set_settings")
+
+    def clear_forces(self, w: int = 0) -> None:
+        """b2World::ClearForces of world w."""
+        _lib.check(self.lib.gb_world_clear_forces(self.h, int(w)), "gb_world_clear_forces")
+
     def set_limits(self, contact_capacity: int = 0, max_toi_events: int = 4096) -> None:
         """Fixed capacities of the device step (see gb_world_set_limits): contact slots per world at
         the first upload (0: the default) and time-of-impact events per world per step."""

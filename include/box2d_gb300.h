@@ -42,6 +42,14 @@ typedef struct gb_world_def {
     int sub_stepping;
 } gb_world_def;
 
+/* b2World::SetGravity, SetAllowSleeping, SetWarmStarting, SetContinuousPhysics, SetSubStepping and
+ * SetAutoClearForces (Box2D/Dynamics/b2World.h:145-217, b2World.cpp:370-385) of world w between
+ * steps: def holds the new settings; turning allow_sleep off wakes every body (b2Body::SetAwake(true));
+ * auto_clear_forces 0 keeps each body's force and torque after a step (cleared by
+ * gb_world_clear_forces, b2World::ClearForces, Box2D/Dynamics/b2World.cpp:967-974). */
+gb_status gb_world_set_settings(gb_world* world, int w, const gb_world_def* def, int auto_clear_forces);
+gb_status gb_world_clear_forces(gb_world* world, int w);
+
 /* b2World::b2World (Box2D/Dynamics/b2World.cpp:34) for n_worlds independent worlds. */
 gb_status gb_world_create(int n_worlds, const gb_world_def* defs, gb_world** out);
 /* b2World::~b2World (Box2D/Dynamics/b2World.cpp:58) */

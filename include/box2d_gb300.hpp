@@ -8,8 +8,8 @@
 // b2Body getters. Differences, all of them consequences of the state living on the GPU:
 //  - a Step is queued on the device; the first getter after it waits for it and reads every body
 //    once (the getters of that step are then host reads);
-//  - the world settings (SetAllowSleeping, SetWarmStarting, SetContinuousPhysics, SetSubStepping)
-//    take effect when the device world is created, at the first Step;
+//  - the world settings (SetGravity, SetAllowSleeping, SetWarmStarting, SetContinuousPhysics,
+//    SetSubStepping, SetAutoClearForces) and ClearForces act between steps, as in the reference;
 //  - DestroyBody, DestroyJoint and DestroyFixture run between steps with the reference's order of
 //    effects; the destroyed objects stay allocated (their pointers stay valid, but dead) until the
 //    world is destroyed, and the destruction listener and the contact listener's EndContact are
@@ -626,12 +626,25 @@ public:
     b2World(const b2World&) = delete;
     b2World& operator=(const b2World&) = delete;
 
-    void SetAllowSleeping(bool flag) { m_def.allow_sleep = flag; }
-    void SetWarmStarting(bool flag) { m_def.warm_starting = flag; }
-    void SetContinuousPhysics(bool flag) { m_def.continuous_physics = flag; }
-    void SetSubStepping(bool flag) { m_def.sub_stepping = flag; }
+    // the world settings (Box2D/Dynamics/b2World.h:145-217): kept here and, once the device world
+    // exists, applied to it between steps (gb_world_set_settings)
+    void SetAllowSleeping(bool flag) { m_def.allow_sleep = flag; ApplySettings(); }
+    void SetWarmStarting(bool flag) { m_def.warm_starting = flag; ApplySettings(); }
+    void SetContinuousPhysics(bool flag) { m_def.continuous_physics = flag; ApplySettings(); }
+    void SetSubStepping(bool flag) { m_def.sub_stepping = flag; ApplySettings(); }
+    void SetGravity(const b2Vec2& gravity) { m_gravity = gravity; ApplySettings(); }
+    void SetAutoClearForces(bool flag) { m_autoClear = flag; ApplySettings(); }
     bool GetAllowSleeping() const { return m_def.allow_sleep != 0; }
+    bool GetWarmStarting() const { return m_def.warm_starting != 0; }
+    bool GetContinuousPhysics() const { return m_def.continuous_physics != 0; }
+    bool GetSubStepping() const { return m_def.sub_stepping != 0; }
+    bool GetAutoClearForces() const { return m_autoClear; }
     b2Vec2 GetGravity() const { return m_gravity; }
+    // b2World::ClearForces (Box2D/Dynamics/b2World.cpp:967-974)
+    void ClearForces()
+    {
+        if (m_h) gb_world_clear_forces(m_h, 0);
+    }
     void SetContactListener(b2ContactListener* listener) { m_listener = listener; }
     void SetDestructionListener(b2DestructionListener* listener) { m_destruction = listener; }
     // b2World::SetContactFilter (Box2D/Dynamics/b2World.cpp:94): the filter decides each ordered
@@ -1033,8 +1046,15 @@ private:
             m_def.gravity_x = m_gravity.x;
             m_def.gravity_y = m_gravity.y;
             if (gb_world_create(1, &m_def, &m_h) != GB_OK) m_h = nullptr;
+            if (m_h && !m_autoClear) gb_world_set_settings(m_h, 0, &m_def, 0);
         }
         return m_h;
+    }
+    void ApplySettings()
+    {
+        m_def.gravity_x = m_gravity.x;
+        m_def.gravity_y = m_gravity.y;
+        if (m_h) gb_world_set_settings(m_h, 0, &m_def, m_autoClear ? 1 : 0);
     }
     void ReadContacts()
     {
@@ -1113,6 +1133,7 @@ private:
 
     b2Vec2 m_gravity;
     gb_world_def m_def{0.0f, 0.0f, 1, 1, 1, 0};
+    bool m_autoClear = true;
     gb_world* m_h = nullptr;
     b2ContactListener* m_listener = nullptr;
     b2DestructionListener* m_destruction = nullptr;

@@ -89,6 +89,8 @@ def _declare(lib, p: str) -> None:
     sig["fixture"] = (C.c_int, [vp, C.c_int, C.c_int, _f32p, C.c_int, _f32p, _i32p])
     sig["set_presolve_rule"] = (None, [vp, _i32p, C.c_int])
     sig["set_filter_rule"] = (None, [vp, C.c_int, C.c_int])
+    sig["set_settings"] = (None, [vp, C.c_float, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int])
+    sig["clear_forces"] = (None, [vp])
     for kind in ("body", "joint", "fixture"):
         sig["destroy_" + kind] = (C.c_int, [vp, C.c_int, _i32p, C.c_int])
     if p == "rw_":
@@ -191,6 +193,17 @@ class OracleWorld:
         """A b2ContactFilter: fixtures below first_other keep the default filter; any other pair
         collides unless (fixtureA + fixtureB) % modulus == 0."""
         self._fn("set_filter_rule")(self.h, int(modulus), int(first_other))
+
+    def set_settings(self, gravity, allow_sleep: bool, warm_starting: bool, continuous: bool, sub_stepping: bool,
+                     auto_clear_forces: bool) -> None:
+        """b2World::SetGravity, SetAllowSleeping, SetWarmStarting, SetContinuousPhysics, SetSubStepping
+        and SetAutoClearForces between steps."""
+        self._fn("set_settings")(self.h, float(gravity[0]), float(gravity[1]), int(allow_sleep), int(warm_starting),
+                                 int(continuous), int(sub_stepping), int(auto_clear_forces))
+
+    def clear_forces(self) -> None:
+        """b2World::ClearForces."""
+        self._fn("clear_forces")(self.h)
 
     def set_presolve_rule(self, bits) -> None:
         """A PreSolve listener applying a rule per fixture pair (bits per fixture: 1 ghost, 2 ice,

@@ -101,6 +101,31 @@ void po_set_filter_rule(void* h, int modulus, int firstOther)
     w->filterModulus = modulus;
     w->filterStatic = firstOther;
 }
+// b2World::SetGravity, SetAllowSleeping (b2World.cpp:370-385: turning sleep off wakes every body of
+// the list), SetWarmStarting, SetContinuousPhysics, SetSubStepping, SetAutoClearForces
+void po_set_settings(void* h, float gx, float gy, int allowSleep, int warm, int continuous, int subStepping,
+                     int autoClear)
+{
+    World* w = static_cast<World*>(h);
+    w->gravity = V(gx, gy);
+    if (w->allowSleep && !allowSleep)
+        for (int b = w->bodyList; b != kNull; b = w->bodies[b].next) w->SetAwake(b, true);
+    w->allowSleep = allowSleep != 0;
+    w->warmStarting = warm != 0;
+    w->continuous = continuous != 0;
+    w->subStepping = subStepping != 0;
+    if (autoClear) w->wflags |= 0x4u;
+    else w->wflags &= ~0x4u;
+}
+// b2World::ClearForces (b2World.cpp:967-974)
+void po_clear_forces(void* h)
+{
+    World* w = static_cast<World*>(h);
+    for (int b = w->bodyList; b != kNull; b = w->bodies[b].next) {
+        w->bodies[b].force = V(0.0f, 0.0f);
+        w->bodies[b].torque = 0.0f;
+    }
+}
 void po_set_presolve_rule(void* h, const int* bits, int n)
 {
     World* w = static_cast<World*>(h);

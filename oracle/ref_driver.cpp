@@ -419,6 +419,21 @@ void rw_set_filter_rule(void* h, int modulus, int firstOther)
     w->filter.firstOther = firstOther;
     w->world.SetContactFilter(&w->filter);
 }
+void rw_set_settings(void* h, float gx, float gy, int allowSleep, int warm, int continuous, int subStepping,
+                     int autoClear)
+{
+    RefWorld* w = static_cast<RefWorld*>(h);
+    w->world.SetGravity(b2Vec2(gx, gy));
+    w->world.SetAllowSleeping(allowSleep != 0);
+    w->world.SetWarmStarting(warm != 0);
+    w->world.SetContinuousPhysics(continuous != 0);
+    w->world.SetSubStepping(subStepping != 0);
+    w->world.SetAutoClearForces(autoClear != 0);
+}
+void rw_clear_forces(void* h)
+{
+    static_cast<RefWorld*>(h)->world.ClearForces();
+}
 void rw_set_presolve_rule(void* h, const int* bits, int n)
 {
     RefWorld* w = static_cast<RefWorld*>(h);

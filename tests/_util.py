@@ -126,12 +126,45 @@ def destroy_script():
     }
 
 
+def settings_script():
+    """{step: [op]} applied before that step to scenes.destroy_mix: the b2World settings changed
+    between steps. Ops: ("settings", gx, gy, allow_sleep, warm_starting, continuous, sub_stepping,
+    auto_clear_forces), ("force", body, fx, fy, torque) (b2Body::ApplyForceToCenter + ApplyTorque,
+    waking the body), ("clear_forces",) (b2World::ClearForces)."""
+    def st(gx, gy, sleep=1, warm=1, cont=1, sub=0, clear=1):
+        return ("settings", gx, gy, sleep, warm, cont, sub, clear)
+
+    return {
+        40: [st(3.0, -6.0)],                                    # gravity changes
+        60: [st(0.0, -10.0)],
+        100: [st(0.0, -10.0, clear=0), ("force", 50, 0.0, 12.0, 1.0)],   # forces kept between steps
+        120: [("clear_forces",), st(0.0, -10.0, warm=0)],       # cleared; no warm start
+        140: [st(0.0, -10.0, cont=0)],                          # no continuous collision
+        160: [st(0.0, -10.0, sub=1)],                           # single-event sub-stepping
+        180: [st(0.0, -10.0)],                                  # all back on
+        300: [st(0.0, -10.0, sleep=0)],                         # sleep off: the sleeping bodies wake
+        320: [st(-2.0, -9.0)],                                  # sleep on again, another gravity
+    }
+
+
 def apply_ops(world, ops, w: int = 0):
-    """Applies destroy_script() ops to an oracle world or a device world (same method names); returns
-    the destruction listener's calls of the ops as (kind, index), in order."""
+    """Applies destroy_script() and settings_script() ops to an oracle world or a device world (same
+    method names); returns the destruction listener's calls of the ops as (kind, index), in order."""
     calls = []
     for op in ops:
-        if op[0] == "add":
+        if op[0] == "settings":
+            args = ((op[1], op[2]), bool(op[3]), bool(op[4]), bool(op[5]), bool(op[6]), bool(op[7]))
+            world.set_settings(*args) if w == 0 else world.set_settings(*args, w=w)
+        elif op[0] == "clear_forces":
+            world.clear_forces() if w == 0 else world.clear_forces(w)
+        elif op[0] == "force":
+            _, b, fx, fy, t = op
+            if hasattr(world, "body_edits"):
+                world.body_edits([(w, b, "apply_force_to_center", [fx, fy], True), (w, b, "apply_torque", [t], True)])
+            else:
+                world.body_edit(5, b, [fx, fy], True)
+                world.body_edit(6, b, [t], True)
+        elif op[0] == "add":
             b = world.add_body(op[1], op[2], 1 | 2 | 16) if w == 0 else world.add_body(op[1], op[2], 1 | 2 | 16, w)
             for (t, shape, n, density) in op[3]:
                 args = (b, t, shape, n, [density, 0.4, 0.0], [1, 0xFFFF, 0, 0])

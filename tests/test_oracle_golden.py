@@ -157,3 +157,25 @@ def test_port_contact_filter_matches_reference(trig):
             if trig == "libm" and platform.machine() != "x86_64":
                 pytest.skip("libm trig differs on this machine")
             raise AssertionError(f"first divergence at step {s}")
+
+
+@pytest.mark.parametrize("trig", ["project", "libm"])
+def test_port_settings_case_matches_reference(trig):
+    """b2World settings changed between steps (gravity, sleep off and on, warm starting, continuous
+    collision, sub-stepping, forces kept across steps and cleared): per-step state as the reference."""
+    import platform
+
+    from box2dpp_gb300 import scenes
+    from tests._util import apply_ops, digest, settings_script
+
+    g = golden(f"settings_mix_{trig}")
+    w = oracle.OracleWorld(scenes.destroy_mix(scenes.SplitMix64(7)), "port", trig)
+    script = settings_script()
+    for s in range(1, int(g["steps"]) + 1):
+        if s in script:
+            apply_ops(w, script[s])
+        w.step()
+        if not np.array_equal(digest(w.bodies(), *w.contacts()), g["digests"][s - 1]):
+            if trig == "libm" and platform.machine() != "x86_64":
+                pytest.skip("libm trig differs on this machine")
+            raise AssertionError(f"first divergence at step {s}")
