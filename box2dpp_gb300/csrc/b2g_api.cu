@@ -2524,6 +2524,135 @@ gb_status gb_collide(int n, const int* type_a, const float* shape_a, const int* 
     return cudaErr(e);
 }
 
+// b2Body::SynchronizeFixtures (Dynamics/b2Body.cpp:443-455) on the host copy: each proxy's swept box
+// and, when it left the fat box, a new fat box (b2DynamicTree::MoveProxy, b2DynamicTree.cpp:133-177)
+// with the proxy marked moved.
+void SyncFixturesHost(HWorld& W, int bi)
+{
+    const HBody& b = W.bodies[bi];
+    Xf xf1;
+    xf1.q = RotOf(b.sw.a0);
+    xf1.p = b.sw.c0 - Mul(xf1.q, b.sw.localCenter);
+    for (int f = b.fixtureList; f != kNullIdx; f = W.fixtures[f].next) {
+        HFixture& fx = W.fixtures[f];
+        if (fx.proxyId == kNullIdx) continue;
+        const float4 a = Combine(ComputeAABB(fx.shape, xf1), ComputeAABB(fx.shape, b.xf));
+        fx.aabb = a;
+        if (Contains(W.fat[fx.proxyId], a)) continue;
+        const Vec2 disp = b.xf.p - xf1.p;
+        float4 nb = make_float4(a.x - kAabbExtension, a.y - kAabbExtension, a.z + kAabbExtension, a.w + kAabbExtension);
+        const Vec2 dd = kAabbMultiplier * disp;
+        if (dd.x < 0.0f) nb.x += dd.x; else nb.z += dd.x;
+        if (dd.y < 0.0f) nb.y += dd.y; else nb.w += dd.y;
+        W.fat[fx.proxyId] = nb;
+        W.moved[fx.proxyId] = 1;
+    }
+}
+
+// b2Body property changes between steps on the host copy (prop: GB_BODY_*): SetType
+// (Dynamics/b2Body.cpp:115-166), SetActive (:456-499), SetFixedRotation (:501-520), SetBullet,
+// SetSleepingAllowed, SetLinearDamping, SetAngularDamping, SetGravityScale (b2Body.h:593-682), with
+// the reference's order of effects; destroyed contacts report EndContact calls.
+gb_status SetBodyPropertyHost(HWorld& W, int bi, int prop, const float* v, Calls& calls)
+{
+    HBody& b = W.bodies[bi];
+    const bool flag = v[0] != 0.0f;
+    auto destroyContacts = [&]() {
+        if (W.hasState)
+            for (int e = W.bodies[bi].contactList; e != kNullIdx;) {
+                const int c = e >> 1;
+                e = NextContactEdge(W, e);
+                DestroyContactHost(W, c, calls);
+            }
+        W.bodies[bi].contactList = kNullIdx;
+    };
+    switch (prop) {
+    case GB_BODY_TYPE: {
+        const int type = (int)v[0];
+        if (type < 0 || type > 2) return GB_ERR_INVALID;
+        if (b.type == type) return GB_OK;
+        b.type = type;
+        ResetMassData(W, bi);
+        if (type == kStatic) {
+            W.bodies[bi].v = V(0.0f, 0.0f);
+            W.bodies[bi].w = 0.0f;
+            W.bodies[bi].sw.a0 = W.bodies[bi].sw.a;
+            W.bodies[bi].sw.c0 = W.bodies[bi].sw.c;
+            SyncFixturesHost(W, bi);
+        }
+        WakeHost(W.bodies[bi]);
+        W.bodies[bi].force = V(0.0f, 0.0f);
+        W.bodies[bi].torque = 0.0f;
+        destroyContacts();
+        // b2BroadPhase::TouchProxy: the proxies are queried again at the next pair finding
+        for (int f = W.bodies[bi].fixtureList; f != kNullIdx; f = W.fixtures[f].next)
+            if (W.fixtures[f].proxyId != kNullIdx) W.moved[W.fixtures[f].proxyId] = 1;
+        return GB_OK;
+    }
+    case GB_BODY_ACTIVE: {
+        const bool active = (b.flags & kBActive) != 0;
+        if (flag == active) return GB_OK;
+        if (flag) {
+            b.flags |= kBActive;
+            // b2Fixture::CreateProxies (Dynamics/b2Fixture.cpp:121-137) in the fixture list's order
+            for (int f = b.fixtureList; f != kNullIdx; f = W.fixtures[f].next) {
+                HFixture& fx = W.fixtures[f];
+                fx.aabb = ComputeAABB(fx.shape, b.xf);
+                const float4 fat = make_float4(fx.aabb.x - kAabbExtension, fx.aabb.y - kAabbExtension,
+                                               fx.aabb.z + kAabbExtension, fx.aabb.w + kAabbExtension);
+                fx.proxyId = AllocateProxy(W, fat, f);
+            }
+        } else {
+            b.flags &= ~kBActive;
+            for (int f = b.fixtureList; f != kNullIdx; f = W.fixtures[f].next) {
+                HFixture& fx = W.fixtures[f];
+                if (fx.proxyId != kNullIdx) FreeProxy(W, fx.proxyId);
+                fx.proxyId = kNullIdx;
+            }
+            destroyContacts();
+        }
+        return GB_OK;
+    }
+    case GB_BODY_FIXED_ROTATION: {
+        const bool fixed = (b.flags & kBFixedRot) != 0;
+        if (fixed == flag) return GB_OK;
+        if (flag) b.flags |= kBFixedRot;
+        else b.flags &= ~kBFixedRot;
+        b.w = 0.0f;
+        ResetMassData(W, bi);
+        return GB_OK;
+    }
+    case GB_BODY_BULLET:
+        if (flag) b.flags |= kBBullet;
+        else b.flags &= ~kBBullet;
+        return GB_OK;
+    case GB_BODY_SLEEPING_ALLOWED:
+        if (flag) {
+            b.flags |= kBAutoSleep;
+        } else {
+            b.flags &= ~kBAutoSleep;
+            WakeHost(b);
+        }
+        return GB_OK;
+    case GB_BODY_LINEAR_DAMPING: b.linDamp = v[0]; return GB_OK;
+    case GB_BODY_ANGULAR_DAMPING: b.angDamp = v[0]; return GB_OK;
+    case GB_BODY_GRAVITY_SCALE: b.gravScale = v[0]; return GB_OK;
+    default: return GB_ERR_INVALID;
+    }
+}
+
+gb_status gb_body_set(gb_world* g, int w, int body, int prop, const float* v, int* calls, int cap, int* n_calls)
+{
+    if (!v) return GB_ERR_INVALID;
+    gb_status s = Mutable(g, w);
+    if (s != GB_OK) return s;
+    HWorld& W = g->worlds[w];
+    if (body < 0 || body >= (int)W.bodies.size() || !W.bodies[body].alive) return GB_ERR_INVALID;
+    Calls c;
+    if ((s = SetBodyPropertyHost(W, body, prop, v, c)) != GB_OK) return s;
+    return Finish(c, calls, cap, n_calls);
+}
+
 gb_status gb_destroy_body(gb_world* g, int w, int body, int* calls, int cap, int* n_calls)
 {
     gb_status s = Mutable(g, w);

@@ -143,6 +143,18 @@ class World:
         kind 0 SayGoodbye(joint a), 1 SayGoodbye(fixture a), 2 EndContact(a, b)."""
         return self._destroy("gb_destroy_body", body, w)
 
+    def body_set(self, body: int, prop: int, value: float, w: int = 0) -> np.ndarray:
+        """b2Body::SetType (prop BODY_TYPE, value 0 static / 1 kinematic / 2 dynamic), SetActive,
+        SetFixedRotation, SetBullet, SetSleepingAllowed (flags: value != 0), SetLinearDamping,
+        SetAngularDamping or SetGravityScale between steps; returns the EndContact calls of the
+        contacts it destroys as rows {2, fixtureA, fixtureB}."""
+        calls = np.zeros((256, 3), dtype=np.int32)
+        n = C.c_int()
+        v = np.array([value], dtype=np.float32)
+        _lib.check(self.lib.gb_body_set(self.h, int(w), int(body), int(prop), v, calls, 256, C.byref(n)),
+                   "gb_body_set")
+        return calls[:min(n.value, 256)]
+
     def destroy_joint(self, joint: int, w: int = 0) -> np.ndarray:
         """b2World::DestroyJoint (no listener calls)."""
         return self._destroy("gb_destroy_joint", joint, w)

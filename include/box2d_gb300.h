@@ -149,6 +149,25 @@ gb_status gb_world_upload(gb_world* world);
 gb_status gb_world_step(gb_world* world, float dt, int velocity_iterations, int position_iterations);
 
 /* Waits for queued steps and returns the first error any world raised since the last sync. */
+/* b2Body property changes between steps (no step in progress): prop GB_BODY_TYPE (v[0] 0 static,
+ * 1 kinematic, 2 dynamic; b2Body::SetType, Box2D/Dynamics/b2Body.cpp:115-166: mass reset, a static
+ * body's velocities zeroed and fixtures synchronised, the body woken, its force cleared, its contacts
+ * destroyed and its proxies queried again at the next step), GB_BODY_ACTIVE (v[0] != 0; SetActive,
+ * :456-499: proxies created in the fixture list's order, or destroyed with the contacts),
+ * GB_BODY_FIXED_ROTATION (SetFixedRotation, :501-520), GB_BODY_BULLET, GB_BODY_SLEEPING_ALLOWED
+ * (turning it off wakes the body), GB_BODY_LINEAR_DAMPING, GB_BODY_ANGULAR_DAMPING,
+ * GB_BODY_GRAVITY_SCALE (v[0]; b2Body.h:593-682). calls (optional, cap records of 3 ints, *n_calls
+ * the count) receives the EndContact calls {2, fixtureA, fixtureB} of the contacts it destroys. */
+#define GB_BODY_TYPE 0
+#define GB_BODY_ACTIVE 1
+#define GB_BODY_FIXED_ROTATION 2
+#define GB_BODY_BULLET 3
+#define GB_BODY_SLEEPING_ALLOWED 4
+#define GB_BODY_LINEAR_DAMPING 5
+#define GB_BODY_ANGULAR_DAMPING 6
+#define GB_BODY_GRAVITY_SCALE 7
+gb_status gb_body_set(gb_world* world, int w, int body, int prop, const float* v, int* calls, int cap, int* n_calls);
+
 /* b2World::DestroyBody (Box2D/Dynamics/b2World.cpp:133), b2World::DestroyJoint (:274) and
  * b2Body::DestroyFixture (Box2D/Dynamics/b2Body.cpp:216), between steps, with the reference's order of
  * effects: a body's joints (each announced to the destruction listener, then destroyed: both bodies

@@ -9,7 +9,10 @@
 //  - a Step is queued on the device; the first getter after it waits for it and reads every body
 //    once (the getters of that step are then host reads);
 //  - the world settings (SetGravity, SetAllowSleeping, SetWarmStarting, SetContinuousPhysics,
-//    SetSubStepping, SetAutoClearForces) and ClearForces act between steps, as in the reference;
+//    SetSubStepping, SetAutoClearForces) and ClearForces act between steps, as in the reference, and
+//    so do the body properties (SetType, SetActive, SetFixedRotation, SetBullet, SetSleepingAllowed,
+//    SetLinearDamping, SetAngularDamping, SetGravityScale), with EndContact for the contacts SetType
+//    and SetActive(false) destroy;
 //  - DestroyBody, DestroyJoint and DestroyFixture run between steps with the reference's order of
 //    effects; the destroyed objects stay allocated (their pointers stay valid, but dead) until the
 //    world is destroyed, and the destruction listener and the contact listener's EndContact are
@@ -298,6 +301,17 @@ public:
     void ApplyTorque(float torque, bool wake);
     void ApplyLinearImpulse(const b2Vec2& impulse, const b2Vec2& point, bool wake);
     void ApplyAngularImpulse(float impulse, bool wake);
+    // Property changes between steps (Box2D/Dynamics/b2Body.cpp:115-166 SetType, :456-499
+    // SetActive, :501-520 SetFixedRotation; b2Body.h:593-682), each one gb_body_set call; the
+    // contacts SetType and SetActive(false) destroy make their EndContact calls.
+    void SetType(b2BodyType type);
+    void SetActive(bool flag);
+    void SetFixedRotation(bool flag);
+    void SetBullet(bool flag);
+    void SetSleepingAllowed(bool flag);
+    void SetLinearDamping(float linearDamping);
+    void SetAngularDamping(float angularDamping);
+    void SetGravityScale(float scale);
 
 private:
     friend class b2World;
@@ -675,6 +689,21 @@ public:
         std::vector<int> calls;
         if (Destroy(gb_destroy_joint, joint->m_index, calls) != GB_OK) return;
         joint->m_alive = false;
+    }
+    // one gb_body_set call (b2Body::SetType, SetActive, ...); EndContact for the contacts it destroys
+    bool SetBodyProperty(b2Body* body, int prop, float value)
+    {
+        if (!Handle() || !body || !body->m_alive || body->m_world != this) return false;
+        if (m_listener) ReadContacts();  // the contacts an EndContact may name
+        const int cap = GetContactCount() + 1;
+        std::vector<int> calls(3 * (size_t)cap, 0);
+        int n = 0;
+        const gb_status s = gb_body_set(m_h, 0, body->m_index, prop, &value, calls.data(), cap, &n);
+        m_stale = true;
+        if (s != GB_OK) return false;
+        calls.resize(3 * (size_t)std::min(n, cap));
+        Announce(calls);
+        return true;
     }
     void DestroyFixture(b2Fixture* fixture)
     {
@@ -1171,6 +1200,17 @@ inline void b2Body::ApplyForceToCenter(const b2Vec2& f, bool wake) { m_world->Ed
 inline void b2Body::ApplyTorque(float torque, bool wake) { m_world->Edit(m_index, GB_EDIT_APPLY_TORQUE, torque, 0.0f, 0.0f, 0.0f, wake); }
 inline void b2Body::ApplyLinearImpulse(const b2Vec2& i, const b2Vec2& p, bool wake) { m_world->Edit(m_index, GB_EDIT_APPLY_LINEAR_IMPULSE, i.x, i.y, p.x, p.y, wake); }
 inline void b2Body::ApplyAngularImpulse(float impulse, bool wake) { m_world->Edit(m_index, GB_EDIT_APPLY_ANGULAR_IMPULSE, impulse, 0.0f, 0.0f, 0.0f, wake); }
+inline void b2Body::SetType(b2BodyType type)
+{
+    if (m_world->SetBodyProperty(this, GB_BODY_TYPE, (float)type)) m_type = type;
+}
+inline void b2Body::SetActive(bool flag) { m_world->SetBodyProperty(this, GB_BODY_ACTIVE, flag ? 1.0f : 0.0f); }
+inline void b2Body::SetFixedRotation(bool flag) { m_world->SetBodyProperty(this, GB_BODY_FIXED_ROTATION, flag ? 1.0f : 0.0f); }
+inline void b2Body::SetBullet(bool flag) { m_world->SetBodyProperty(this, GB_BODY_BULLET, flag ? 1.0f : 0.0f); }
+inline void b2Body::SetSleepingAllowed(bool flag) { m_world->SetBodyProperty(this, GB_BODY_SLEEPING_ALLOWED, flag ? 1.0f : 0.0f); }
+inline void b2Body::SetLinearDamping(float d) { m_world->SetBodyProperty(this, GB_BODY_LINEAR_DAMPING, d); }
+inline void b2Body::SetAngularDamping(float d) { m_world->SetBodyProperty(this, GB_BODY_ANGULAR_DAMPING, d); }
+inline void b2Body::SetGravityScale(float scale) { m_world->SetBodyProperty(this, GB_BODY_GRAVITY_SCALE, scale); }
 
 inline void b2MouseJoint::SetTarget(const b2Vec2& target)
 {

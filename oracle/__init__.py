@@ -91,6 +91,7 @@ def _declare(lib, p: str) -> None:
     sig["set_filter_rule"] = (None, [vp, C.c_int, C.c_int])
     sig["set_settings"] = (None, [vp, C.c_float, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int])
     sig["clear_forces"] = (None, [vp])
+    sig["body_set"] = (None, [vp, C.c_int, C.c_int, _f32p])
     for kind in ("body", "joint", "fixture"):
         sig["destroy_" + kind] = (C.c_int, [vp, C.c_int, _i32p, C.c_int])
     if p == "rw_":
@@ -204,6 +205,16 @@ class OracleWorld:
     def clear_forces(self) -> None:
         """b2World::ClearForces."""
         self._fn("clear_forces")(self.h)
+
+    def body_set(self, body: int, prop: int, value: float):
+        """A b2Body property change between steps (prop: the C-ABI's GB_BODY_* code: 0 SetType,
+        1 SetActive, 2 SetFixedRotation, 3 SetBullet, 4 SetSleepingAllowed, 5 SetLinearDamping,
+        6 SetAngularDamping, 7 SetGravityScale). Returns no listener calls (the reference driver's
+        EndContact calls go to its recorded events, when recording)."""
+        v = np.zeros(4, dtype=np.float32)
+        v[0] = value
+        self._fn("body_set")(self.h, int(body), int(prop), v)
+        return np.zeros((0, 3), dtype=np.int32)
 
     def set_presolve_rule(self, bits) -> None:
         """A PreSolve listener applying a rule per fixture pair (bits per fixture: 1 ghost, 2 ice,

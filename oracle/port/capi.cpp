@@ -117,6 +117,10 @@ void po_set_settings(void* h, float gx, float gy, int allowSleep, int warm, int 
     if (autoClear) w->wflags |= 0x4u;
     else w->wflags &= ~0x4u;
 }
+void po_body_set(void* h, int b, int prop, const float* v)
+{
+    static_cast<World*>(h)->SetBodyProperty(b, prop, v);
+}
 // b2World::ClearForces (b2World.cpp:967-974)
 void po_clear_forces(void* h)
 {

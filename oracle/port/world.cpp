@@ -357,6 +357,93 @@ void World::SynchronizeFixturesFrom(int bi, const Xf& xf1, const Xf& xf2)
     }
 }
 
+// b2Body property changes between steps (prop: the C-ABI's GB_BODY_* code): SetType
+// (Dynamics/b2Body.cpp:115-166), SetActive (:456-499), SetFixedRotation (:501-520), SetBullet,
+// SetSleepingAllowed, SetLinearDamping, SetAngularDamping, SetGravityScale (b2Body.h:593-682).
+void World::SetBodyProperty(int bi, int prop, const float* v)
+{
+    Body& b = bodies[bi];
+    const bool flag = v[0] != 0.0f;
+    auto destroyContacts = [&]() {
+        for (int e = bodies[bi].contactList; e != kNull;) {
+            const int c = e >> 1;
+            e = contacts[c].eNext[e & 1];
+            Destroy(c);
+        }
+        bodies[bi].contactList = kNull;
+    };
+    switch (prop) {
+    case 0: {  // type
+        const int type = (int)v[0];
+        if (b.type == type) return;
+        b.type = type;
+        ResetMassData(bi);
+        if (type == kStatic) {
+            bodies[bi].v = V(0.0f, 0.0f);
+            bodies[bi].w = 0.0f;
+            bodies[bi].sweep.a0 = bodies[bi].sweep.a;
+            bodies[bi].sweep.c0 = bodies[bi].sweep.c;
+            SynchronizeFixtures(bi);
+        }
+        SetAwake(bi, true);
+        bodies[bi].force = V(0.0f, 0.0f);
+        bodies[bi].torque = 0.0f;
+        destroyContacts();
+        for (int f = bodies[bi].fixtureList; f != kNull; f = fixtures[f].next)
+            if (fixtures[f].proxyCount > 0) bp.TouchProxy(fixtures[f].proxyId);
+        return;
+    }
+    case 1: {  // active
+        const bool active = (b.flags & kBActive) != 0;
+        if (flag == active) return;
+        if (flag) {
+            b.flags |= kBActive;
+            for (int f = b.fixtureList; f != kNull; f = fixtures[f].next) {
+                Fixture& fx = fixtures[f];
+                fx.proxyCount = 1;
+                ComputeAABB(fx.shape, b.xf, &fx.aabb);
+                fx.proxyId = bp.CreateProxy(fx.aabb, f);
+            }
+        } else {
+            b.flags &= ~kBActive;
+            for (int f = b.fixtureList; f != kNull; f = fixtures[f].next) {
+                Fixture& fx = fixtures[f];
+                if (fx.proxyCount > 0) bp.DestroyProxy(fx.proxyId);
+                fx.proxyId = kNull;
+                fx.proxyCount = 0;
+            }
+            destroyContacts();
+        }
+        return;
+    }
+    case 2: {  // fixed rotation
+        const bool fixed = (b.flags & kBFixedRot) != 0;
+        if (fixed == flag) return;
+        if (flag) b.flags |= kBFixedRot;
+        else b.flags &= ~kBFixedRot;
+        b.w = 0.0f;
+        ResetMassData(bi);
+        return;
+    }
+    case 3:  // bullet
+        if (flag) b.flags |= kBBullet;
+        else b.flags &= ~kBBullet;
+        return;
+    case 4:  // sleeping allowed
+        if (flag) {
+            b.flags |= kBAutoSleep;
+        } else {
+            b.flags &= ~kBAutoSleep;
+            SetAwake(bi, true);
+        }
+        return;
+    case 5: b.linearDamping = v[0]; return;
+    case 6: b.angularDamping = v[0]; return;
+    case 7: b.gravityScale = v[0]; return;
+    default: return;
+    }
+}
+
 // b2Body state changes between steps: SetTransform (Dynamics/b2Body.cpp:419-441), SetLinearVelocity,
 // SetAngularVelocity (b2Body.h:501-530), SetAwake (b2Body.h:635-655), ApplyForce, ApplyForceToCenter,
 // ApplyTorque, ApplyLinearImpulse, ApplyAngularImpulse (b2Body.h:739-830). op: the C-ABI's GB_EDIT_*.

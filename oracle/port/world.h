@@ -166,6 +166,8 @@ struct World {
     void SynchronizeFixtures(int b);
     void SynchronizeFixturesFrom(int b, const Xf& xf1, const Xf& xf2);
     void ApplyEdit(int op, int b, int wake, const float* v);
+    // b2Body property changes between steps (the C-ABI's GB_BODY_* prop codes)
+    void SetBodyProperty(int b, int prop, const float* v);
     void SynchronizeTransform(int b);
     void Advance(int b, float alpha);
 

@@ -430,6 +430,24 @@ void rw_set_settings(void* h, float gx, float gy, int allowSleep, int warm, int 
     w->world.SetSubStepping(subStepping != 0);
     w->world.SetAutoClearForces(autoClear != 0);
 }
+// b2Body property changes between steps (prop: the C-ABI's GB_BODY_* code)
+void rw_body_set(void* h, int b, int prop, const float* v)
+{
+    RefWorld* w = static_cast<RefWorld*>(h);
+    b2Body* body = w->bodies[b];
+    const bool flag = v[0] != 0.0f;
+    switch (prop) {
+    case 0: body->SetType((b2BodyType)(int)v[0]); break;
+    case 1: body->SetActive(flag); break;
+    case 2: body->SetFixedRotation(flag); break;
+    case 3: body->SetBullet(flag); break;
+    case 4: body->SetSleepingAllowed(flag); break;
+    case 5: body->SetLinearDamping(v[0]); break;
+    case 6: body->SetAngularDamping(v[0]); break;
+    case 7: body->SetGravityScale(v[0]); break;
+    default: break;
+    }
+}
 void rw_clear_forces(void* h)
 {
     static_cast<RefWorld*>(h)->world.ClearForces();

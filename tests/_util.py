@@ -147,8 +147,30 @@ def settings_script():
     }
 
 
+def body_props_script():
+    """{step: [op]} applied before that step to scenes.destroy_mix: b2Body properties changed between
+    steps. Op ("prop", body, prop, value): prop 0 SetType (0 static, 1 kinematic, 2 dynamic),
+    1 SetActive, 2 SetFixedRotation, 3 SetBullet, 4 SetSleepingAllowed, 5 SetLinearDamping,
+    6 SetAngularDamping, 7 SetGravityScale."""
+    return {
+        30: [("prop", 12, 0, 0.0)],                              # a pyramid box turns static
+        45: [("prop", 43, 1, 0.0)],                              # a chain link leaves the world
+        60: [("prop", 47, 2, 1.0), ("prop", 50, 7, -0.5)],       # fixed rotation; a circle rises
+        75: [("prop", 43, 1, 1.0)],                              # the link comes back
+        90: [("prop", 12, 0, 2.0)],                              # the box is dynamic again
+        100: [("prop", 37, 0, 2.0)],                             # the static ledge falls
+        110: [("prop", 48, 0, 1.0)],                             # a tied circle turns kinematic
+        120: [("prop", 51, 3, 1.0), ("prop", 52, 5, 3.0), ("prop", 53, 6, 2.0)],
+        140: [("prop", 47, 2, 0.0), ("prop", 50, 7, 1.0)],
+        160: [("prop", 30, 1, 0.0)],                             # a loaded pyramid box leaves
+        200: [("prop", 48, 0, 2.0), ("prop", 30, 1, 1.0)],
+        250: [("prop", 5, 4, 0.0)],                              # one body may not sleep
+        300: [("prop", 5, 4, 1.0)],
+    }
+
+
 def apply_ops(world, ops, w: int = 0):
-    """Applies destroy_script() and settings_script() ops to an oracle world or a device world (same
+    """Applies destroy_script(), settings_script() and body_props_script() ops to an oracle world or a device world (same
     method names); returns the destruction listener's calls of the ops as (kind, index), in order."""
     calls = []
     for op in ops:
@@ -157,6 +179,10 @@ def apply_ops(world, ops, w: int = 0):
             world.set_settings(*args) if w == 0 else world.set_settings(*args, w=w)
         elif op[0] == "clear_forces":
             world.clear_forces() if w == 0 else world.clear_forces(w)
+        elif op[0] == "prop":
+            # a device world also returns the EndContact calls, which the oracles record with their
+            # other events
+            world.body_set(op[1], op[2], op[3]) if w == 0 else world.body_set(op[1], op[2], op[3], w)
         elif op[0] == "force":
             _, b, fx, fy, t = op
             if hasattr(world, "body_edits"):

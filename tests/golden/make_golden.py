@@ -87,10 +87,11 @@ def scripted_cases():
     """Trajectory cases with b2World changes between steps: (name, scene factory, steps, ops by step).
     The ops (tests/_util.py destroy_script) destroy bodies, joints and fixtures and create bodies."""
     sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
-    from tests._util import destroy_script, settings_script
+    from tests._util import body_props_script, destroy_script, settings_script
 
     return [("destroy_mix", lambda: scenes.destroy_mix(scenes.SplitMix64(5)), 200, destroy_script()),
-            ("settings_mix", lambda: scenes.destroy_mix(scenes.SplitMix64(7)), 340, settings_script())]
+            ("settings_mix", lambda: scenes.destroy_mix(scenes.SplitMix64(7)), 340, settings_script()),
+            ("body_props", lambda: scenes.destroy_mix(scenes.SplitMix64(11)), 320, body_props_script())]
 
 
 def run_scripted(scene, steps, script, trig):

@@ -406,3 +406,74 @@ def test_cpp_destroy_queries_match_oracle(gpu, tmp_path):
     sel = [0, 1] + [2 + 2 * k for k in range(n)] + [3 + 2 * k for k in range(n)] + [6 + k for k in range(n)]
     assert np.array_equal(got[sel].view(np.uint32), want[sel].view(np.uint32)), (got, want)
     assert int(out["profile"][0]) == 1
+
+
+BP_SRC = os.path.join(ROOT, "tests", "cpp", "body_props.cpp")
+
+
+def _compile_bp(tmp_path):
+    lib = _lib.library_path()
+    exe = str(tmp_path / "body_props")
+    libdir = os.path.dirname(lib)
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "include"), BP_SRC, "-o", exe,
+           "-L", libdir, "-lbox2d_gb300", f"-Wl,-rpath,{libdir}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return exe
+
+
+def test_cpp_body_props_compile(tmp_path):
+    _compile_bp(tmp_path)
+
+
+@pytest.mark.gpu
+def test_cpp_body_props_match_oracle(gpu, tmp_path):
+    """b2Body::SetType, SetActive, SetFixedRotation, SetBullet, SetSleepingAllowed, SetLinearDamping,
+    SetAngularDamping and SetGravityScale of the C++ mirror against the CPU oracle: body states bit
+    for bit and the contact listener's EndContact count (the ones the changes make included)."""
+    exe = _compile_bp(tmp_path)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    out, bodies = {}, {}
+    for ln in r.stdout.strip().splitlines():
+        parts = ln.split()
+        if parts[0] == "body":
+            bodies[int(parts[1])] = np.array([float.fromhex(v) for v in parts[2:]], dtype=np.float32)
+        else:
+            out[parts[0]] = parts[1:]
+    o = oracle.OracleWorld(_dq_scene(), "port", "project")
+    o.record_events(True)
+    ends = 0
+
+    def step(n):
+        nonlocal ends
+        for _ in range(n):
+            o.step(1.0 / 60.0, 8, 3)
+            ends += int((o.events()[0][:, 0] == 1).sum())
+
+    def prop(body, p, v):
+        nonlocal ends
+        seen = len(o.events()[0])
+        o.body_set(body, p, v)
+        ends += int((o.events()[0][seen:, 0] == 1).sum())
+
+    step(40)
+    prop(2, _lib.BODY_TYPE, 0.0)
+    prop(8, _lib.BODY_ACTIVE, 0.0)
+    prop(11, _lib.BODY_GRAVITY_SCALE, 0.5)
+    prop(11, _lib.BODY_LINEAR_DAMPING, 0.5)
+    assert [int(x) for x in out["ends_after_first"]] == [ends, 0]
+    step(20)
+    prop(8, _lib.BODY_ACTIVE, 1.0)
+    prop(2, _lib.BODY_TYPE, 2.0)
+    prop(12, _lib.BODY_FIXED_ROTATION, 1.0)
+    prop(9, _lib.BODY_BULLET, 1.0)
+    prop(1, _lib.BODY_SLEEPING_ALLOWED, 0.0)
+    prop(11, _lib.BODY_ANGULAR_DAMPING, 0.3)
+    step(40)
+    assert int(out["ends"][0]) == ends and ends > 0
+    ob = o.bodies()
+    assert len(bodies) == len(ob)
+    for i, got in bodies.items():
+        want = ob[i][[0, 1, 2, 5, 6, 7]]
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), i

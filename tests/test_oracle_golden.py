@@ -160,6 +160,31 @@ def test_port_contact_filter_matches_reference(trig):
 
 
 @pytest.mark.parametrize("trig", ["project", "libm"])
+def test_port_body_props_case_matches_reference(trig):
+    """b2Body properties changed between steps (SetType to static, kinematic and dynamic, SetActive
+    off and on, SetFixedRotation, SetBullet, SetSleepingAllowed, damping, gravity scale): per-step
+    state and the final proxy ids (SetActive frees and creates proxies) as the reference."""
+    import platform
+
+    from box2dpp_gb300 import scenes
+    from tests._util import apply_ops, body_props_script, digest
+
+    g = golden(f"body_props_{trig}")
+    w = oracle.OracleWorld(scenes.destroy_mix(scenes.SplitMix64(11)), "port", trig)
+    script = body_props_script()
+    for s in range(1, int(g["steps"]) + 1):
+        if s in script:
+            apply_ops(w, script[s])
+        w.step()
+        if not np.array_equal(digest(w.bodies(), *w.contacts()), g["digests"][s - 1]):
+            if trig == "libm" and platform.machine() != "x86_64":
+                pytest.skip("libm trig differs on this machine")
+            raise AssertionError(f"first divergence at step {s}")
+    ids, _ = w.proxies()
+    assert np.array_equal(ids, g["proxy_ids"])
+
+
+@pytest.mark.parametrize("trig", ["project", "libm"])
 def test_port_settings_case_matches_reference(trig):
     """b2World settings changed between steps (gravity, sleep off and on, warm starting, continuous
     collision, sub-stepping, forces kept across steps and cleared): per-step state as the reference."""
