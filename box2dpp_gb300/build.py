@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbox2d_gb300.so")
 SOURCES = ["b2g_step.cu", "b2g_api.cu", "b2g_tools.cu", "b2g_learn.cu"]
-HEADERS = ["b2g_core.h", "b2g_world.h", "b2g_solver.cuh", "b2g_trig_table.h", "b2g_mlp.cuh"]
+HEADERS = ["b2g_core.h", "b2g_world.h", "b2g_solver.cuh", "b2g_trig_table.h", "b2g_mlp.cuh", "b2g_tree.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
                      "-ftz=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-diag-suppress", "177"]

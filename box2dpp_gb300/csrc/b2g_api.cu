@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/box2d_gb300.h"
+#include "b2g_tree.h"
 #include "b2g_world.h"
 
 cudaError_t b2gLaunchNarrowphase(const b2g::Batch& B, const int4* chunks, int n, cudaStream_t stream);
@@ -87,6 +88,10 @@ struct HWorld {
     int nodeFresh = 0, proxyCount = 0;
     std::vector<int> nodeFree;
     bool treeLost = false; // a leaf would have taken an internal node's id (never expected)
+    // the reference tree's shape, kept only when the handle tracks trees (gb_world_track_tree):
+    // treeIncomplete when the device's tree log ran out of room or an id disagreed with nodeFresh
+    bool trackTree = false, treeIncomplete = false;
+    ProxyTree tree;
     int newFixture = 0;
     WorldState state{};
     bool hasState = false; // state/contacts valid (pulled back from, or never sent to, the device)
@@ -162,6 +167,7 @@ struct gb_world {
     int measureResidual = 0;
     int warmMode = kWarmReference;
     bool eventsEnabled = false;
+    bool treeTrack = false;  // every world keeps its tree (gb_world_track_tree); the device logs moves
     MlpView mlp{};
     BodyEdit* dEdits = nullptr;  // device copy of the last gb_body_edits call
     int editCap = 0;
@@ -282,6 +288,7 @@ int AllocateProxy(HWorld& W, float4 fatAabb, int fixture)
     W.fat[id] = fatAabb;
     W.pfix[id] = fixture;
     W.moved[id] = 1;
+    if (W.trackTree && W.tree.Insert(fatAabb) != id) W.treeIncomplete = true;
     return id;
 }
 
@@ -292,6 +299,7 @@ void FreeProxy(HWorld& W, int id)
     if (W.proxyCount > 1) W.nodeFree.push_back(-1);
     W.nodeFree.push_back(id);
     --W.proxyCount;
+    if (W.trackTree) W.tree.Remove(id);
     W.fat[id] = make_float4(0, 0, 0, 0);
     W.pfix[id] = kNullIdx;
     W.moved[id] = 0;
@@ -363,10 +371,80 @@ int NextPow2(int x)
 }
 
 // Pull the device state of every world back into the host mirror.
+// The device's tree log replayed into each world's host tree (gb_world_track_tree), its count cleared
+// on the device. Records go in log order, except that each step's discrete-phase records, written by
+// many threads at once, are first put in the reference's order: the world's body list (newest body
+// first), then each body's fixture list (b2World::Solve, Dynamics/b2World.cpp:494-514). The caller has
+// synchronised the world's streams.
+gb_status DrainTreeLog(gb_world* g)
+{
+    if (!g->treeTrack || !g->onDevice || !g->batch.treeLogId) return GB_OK;
+    const int nw = (int)g->worlds.size();
+    std::vector<WorldState> st(nw);
+    GB_CUDA(cudaMemcpy(st.data(), g->batch.state, nw * sizeof(WorldState), cudaMemcpyDeviceToHost));
+    std::vector<int> ids, rank, run;
+    std::vector<float4> fats;
+    for (int wi = 0; wi < nw; ++wi) {
+        const int n = st[wi].treeLogCount;
+        if (n == 0) continue;
+        HWorld& W = g->worlds[wi];
+        const WorldDesc& d = g->desc[wi];
+        const int cap = kTreeLogPerProxy * d.proxyCap + kTreeLogExtra;
+        const size_t at = (size_t)kTreeLogPerProxy * d.proxyBase + (size_t)kTreeLogExtra * wi;
+        const int zero = 0;
+        GB_CUDA(cudaMemcpy(&g->batch.state[wi].treeLogCount, &zero, sizeof(int), cudaMemcpyHostToDevice));
+        if (n > cap) {
+            W.treeIncomplete = true;
+            continue;
+        }
+        ids.resize(n);
+        fats.resize(n);
+        GB_CUDA(cudaMemcpy(ids.data(), g->batch.treeLogId + at, n * sizeof(int), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(fats.data(), g->batch.treeLogFat + at, n * sizeof(float4), cudaMemcpyDeviceToHost));
+        rank.assign(d.proxyCap, d.proxyCap);
+        int r = 0;
+        for (int b = W.bodyList; b != kNullIdx; b = W.bodies[b].next)
+            for (int f = W.bodies[b].fixtureList; f != kNullIdx; f = W.fixtures[f].next)
+                if (W.fixtures[f].proxyId != kNullIdx) rank[W.fixtures[f].proxyId] = r++;
+        for (int k = 0; k < n;) {
+            const int kind = ids[k] & 3, pid = ids[k] >> 2;
+            if (pid < 0 || pid >= d.proxyCap) {
+                W.treeIncomplete = true;
+                break;
+            }
+            if (kind != kTreeDiscrete) {
+                if (kind == kTreeOrdered) W.tree.Move(pid, fats[k]);
+                ++k;
+                continue;
+            }
+            int e = k;
+            while (e < n && (ids[e] & 3) == kTreeDiscrete) ++e;
+            run.resize(e - k);
+            std::iota(run.begin(), run.end(), k);
+            std::sort(run.begin(), run.end(), [&](int a, int b) { return rank[ids[a] >> 2] < rank[ids[b] >> 2]; });
+            for (int i : run) W.tree.Move(ids[i] >> 2, fats[i]);
+            k = e;
+        }
+    }
+    return GB_OK;
+}
+
+// Before a step of a handle that tracks trees: the previous step's tree log is replayed first.
+gb_status TreeSync(gb_world* g)
+{
+    if (!g->treeTrack || !g->onDevice) return GB_OK;
+    GB_CUDA(cudaStreamSynchronize(g->stream));
+    return DrainTreeLog(g);
+}
+
 gb_status Download(gb_world* g)
 {
     if (!g->onDevice) return GB_OK;
     GB_CUDA(cudaStreamSynchronize(g->stream));
+    {
+        gb_status s = DrainTreeLog(g);
+        if (s != GB_OK) return s;
+    }
     const Batch& B = g->batch;
     for (size_t wi = 0; wi < g->worlds.size(); ++wi) {
         HWorld& W = g->worlds[wi];
@@ -821,6 +899,13 @@ gb_status Upload(gb_world* g)
     ALLOC(sContact, tc); ALLOC(sStatus, tc); ALLOC(vc, tc); ALLOC(pc, tc); ALLOC(vimp, tc); ALLOC(vimpL, tc); ALLOC(vsep, tc); ALLOC(toi, tc); ALLOC(cColour, tc); ALLOC(colourList, tc);
     ALLOC(evType, tc);
     if (g->eventsEnabled) { ALLOC(evLog, 8 * tc); } else { B.evLog = nullptr; }
+    if (g->treeTrack) {
+        ALLOC(treeLogId, kTreeLogPerProxy * tp + (long long)kTreeLogExtra * nw);
+        ALLOC(treeLogFat, kTreeLogPerProxy * tp + (long long)kTreeLogExtra * nw);
+    } else {
+        B.treeLogId = nullptr;
+        B.treeLogFat = nullptr;
+    }
     ALLOC(pairs, tq); ALLOC(pairKeep, tq); ALLOC(pairInfo, tq); ALLOC(islTab, tt);
 #undef ALLOC
     GB_CUDA(cudaMemcpy(B.desc, g->desc.data(), nw * sizeof(WorldDesc), cudaMemcpyHostToDevice));
@@ -897,6 +982,7 @@ gb_status Upload(gb_world* g)
         st.clearForces = W.autoClear ? 1 : 0;
         st.error = 0;
         st.gridValid = 0;
+        st.treeLogCount = 0;
         states[wi] = st;
         for (int j = 0; j < d.jointCount; ++j) joints[d.jointBase + j] = W.joints[j];
         W.hasState = true;
@@ -1605,7 +1691,8 @@ gb_status gb_world_upload(gb_world* g)
 gb_status gb_world_step_begin(gb_world* g, float dt, int vi, int pi)
 {
     if (!g || vi < 0 || pi < 0 || g->splitOpen || g->filterFn) return GB_ERR_INVALID;
-    gb_status s = Upload(g);
+    gb_status s = TreeSync(g);
+    if (s == GB_OK) s = Upload(g);
     if (s != GB_OK) return s;
     StepParams P = MakeParams(g, dt, vi, pi);
     P.phase = 1;
@@ -1650,7 +1737,8 @@ gb_status gb_world_step_end(gb_world* g)
 gb_status gb_world_step(gb_world* g, float dt, int vi, int pi)
 {
     if (!g || vi < 0 || pi < 0 || g->splitOpen) return GB_ERR_INVALID;
-    gb_status s = Upload(g);
+    gb_status s = TreeSync(g);
+    if (s == GB_OK) s = Upload(g);
     if (s != GB_OK) return s;
     const StepParams P = MakeParams(g, dt, vi, pi);
     if (g->filterFn) return FilteredStep(g, P);
@@ -1718,7 +1806,8 @@ gb_status gb_world_graph_step(gb_world* g, float dt, int vi, int pi)
     if (!g || vi < 0 || pi < 0 || g->splitOpen) return GB_ERR_INVALID;
     if (g->filterFn) return gb_world_step(g, dt, vi, pi);  // a filtered step may run again: no graph
     if (g->tuneIndex >= 0) return gb_world_step(g, dt, vi, pi);  // tuning steps are timed one by one
-    gb_status s = Upload(g);
+    gb_status s = TreeSync(g);
+    if (s == GB_OK) s = Upload(g);
     if (s != GB_OK) return s;
     const bool reuse = g->graph && g->graphDt == dt && g->graphVi == vi && g->graphPi == pi &&
                        g->graphSolver == g->solver && g->graphTol == g->tolerance &&
@@ -2524,6 +2613,10 @@ gb_status gb_collide(int n, const int* type_a, const float* shape_a, const int* 
     return cudaErr(e);
 }
 
+} // extern "C"
+
+namespace {
+
 // b2Body::SynchronizeFixtures (Dynamics/b2Body.cpp:443-455) on the host copy: each proxy's swept box
 // and, when it left the fat box, a new fat box (b2DynamicTree::MoveProxy, b2DynamicTree.cpp:133-177)
 // with the proxy marked moved.
@@ -2546,6 +2639,7 @@ void SyncFixturesHost(HWorld& W, int bi)
         if (dd.y < 0.0f) nb.y += dd.y; else nb.w += dd.y;
         W.fat[fx.proxyId] = nb;
         W.moved[fx.proxyId] = 1;
+        if (W.trackTree) W.tree.Move(fx.proxyId, nb);
     }
 }
 
@@ -2639,6 +2733,44 @@ gb_status SetBodyPropertyHost(HWorld& W, int bi, int prop, const float* v, Calls
     case GB_BODY_GRAVITY_SCALE: b.gravScale = v[0]; return GB_OK;
     default: return GB_ERR_INVALID;
     }
+}
+
+} // namespace
+
+extern "C" {
+
+gb_status gb_world_track_tree(gb_world* g, int on)
+{
+    if (!g || g->splitOpen) return GB_ERR_INVALID;
+    for (const HWorld& W : g->worlds)
+        if (W.nodeFresh != 0) return GB_ERR_INVALID;  // a proxy exists or existed: its history is gone
+    g->treeTrack = on != 0;
+    for (HWorld& W : g->worlds) {
+        W.trackTree = g->treeTrack;
+        W.treeIncomplete = false;
+        W.tree = ProxyTree();
+    }
+    ReleaseGraph(g);
+    g->hostDirty = true;  // the next upload allocates (or drops) the device's tree log
+    return GB_OK;
+}
+
+gb_status gb_world_tree_stats(gb_world* g, int w, int* height, int* balance, float* quality)
+{
+    if (!g || w < 0 || w >= (int)g->worlds.size() || !g->treeTrack || g->splitOpen) return GB_ERR_INVALID;
+    if (g->onDevice) {
+        GB_CUDA(cudaStreamSynchronize(g->stream));
+        if (g->upStream) GB_CUDA(cudaStreamSynchronize(g->upStream));
+        if (g->downStream) GB_CUDA(cudaStreamSynchronize(g->downStream));
+        gb_status s = DrainTreeLog(g);
+        if (s != GB_OK) return s;
+    }
+    const HWorld& W = g->worlds[w];
+    if (W.treeIncomplete) return GB_ERR_CAPACITY;
+    if (height) *height = W.tree.Height();
+    if (balance) *balance = W.tree.MaxBalance();
+    if (quality) *quality = W.tree.AreaRatio();
+    return GB_OK;
 }
 
 gb_status gb_body_set(gb_world* g, int w, int body, int prop, const float* v, int* calls, int cap, int* n_calls)

@@ -82,6 +82,9 @@ struct Wd {
     int filterMissCap;
     float4* smemBase;   // the CTA's dynamic shared memory, free outside the island solve
     int smemBytes;
+    int* treeLogId;     // the world's tree-log records (Batch::treeLogId), or nullptr
+    float4* treeLogFat;
+    int treeLogCap;
 
     __device__ void init(const Batch& B, int w)
     {
@@ -118,6 +121,26 @@ struct Wd {
         filterMissCap = B.filterMissCap;
         smemBase = nullptr;
         smemBytes = 0;
+        if (B.treeLogId) {
+            const size_t at = (size_t)kTreeLogPerProxy * d.proxyBase + (size_t)kTreeLogExtra * w;
+            treeLogId = B.treeLogId + at;
+            treeLogFat = B.treeLogFat + at;
+            treeLogCap = kTreeLogPerProxy * d.proxyCap + kTreeLogExtra;
+        } else {
+            treeLogId = nullptr;
+            treeLogFat = nullptr;
+            treeLogCap = 0;
+        }
+    }
+
+    // One tree-log record (a proxy's new fat box, or a step mark). Past the log's room the count still
+    // grows, which tells the host that the tree's history is incomplete.
+    __device__ void treeLog(int pid, float4 fat, int kind)
+    {
+        const int k = atomicAdd(&st->treeLogCount, 1);
+        if (k >= treeLogCap) return;
+        treeLogId[k] = pid << 2 | kind;
+        treeLogFat[k] = fat;
     }
 
     // ---------------------------------------------------------------- listener event log
@@ -400,19 +423,21 @@ struct Wd {
     // ---------------------------------------------------------------- broadphase
     // b2Fixture::Synchronize + b2DynamicTree::MoveProxy (b2Fixture.cpp:154-177, b2DynamicTree.cpp:133-177)
     // movedOut (optional, one thread): the proxies this call marks moved are appended to movedList
-    __device__ void syncFixtures(int b, int* movedOut = nullptr)
+    __device__ void syncFixtures(int b, int* movedOut = nullptr, int logKind = kTreeOrdered)
     {
         float4 s0 = sw0[b], m = mas[b];
         Xf xf1;
         xf1.q = RotOf(s0.z);
         xf1.p = V(s0.x, s0.y) - Mul(xf1.q, V(m.z, m.w));
-        syncFixturesFrom(b, xf1, xform(b), movedOut);
+        syncFixturesFrom(b, xf1, xform(b), movedOut, logKind);
     }
 
     // b2Fixture::Synchronize (Dynamics/b2Fixture.cpp:154-177) of every fixture of body b between two
     // transforms, with b2BroadPhase::MoveProxy (b2DynamicTree.cpp:133-177): the swept AABB, and a
     // new fat AABB (grown by the extension and the predicted displacement) when it left the old one.
-    __device__ void syncFixturesFrom(int b, const Xf& xf1, const Xf& xf2, int* movedOut = nullptr)
+    // logKind: the tree-log kind of the re-insertions (when the world keeps a tree log).
+    __device__ void syncFixturesFrom(int b, const Xf& xf1, const Xf& xf2, int* movedOut = nullptr,
+                                     int logKind = kTreeOrdered)
     {
         B2G_WALK(f, bi[b].z, fi[f].y, d.fixCount + 1) {
             int pid = fi[f].z;
@@ -429,6 +454,7 @@ struct Wd {
             if (dd.x < 0.0f) nb.x += dd.x; else nb.z += dd.x;
             if (dd.y < 0.0f) nb.y += dd.y; else nb.w += dd.y;
             fat[pid] = nb;
+            if (treeLogId) treeLog(pid, nb, logKind);
             if (movedOut && moved[pid] == 0) movedList[(*movedOut)++] = pid;
             moved[pid] = 1;
         }
@@ -2212,10 +2238,11 @@ __device__ void Wd::solve(const StepParams& P, float4* smem, int smemRows, int s
         if (sleepOut[i]) bi[b].y &= ~kBAwake;
         else bi[b].y |= kBAwake;
     }
+    if (treeLogId && tid() == 0) treeLog(0, make_float4(0.0f, 0.0f, 0.0f, 0.0f), kTreeStepMark);
     __syncthreads();
     for (int b = tid(); b < nb; b += nthreads()) {
         if ((bi[b].y & kBIsland) == 0 || bi[b].x == kStatic) continue;
-        syncFixtures(b);
+        syncFixtures(b, nullptr, kTreeDiscrete);
     }
     __syncthreads();
     unsigned long long t3 = clock64();

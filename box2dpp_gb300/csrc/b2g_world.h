@@ -81,6 +81,7 @@ struct WorldState {
     // 2 x contactCap order rows: new contacts are prepended in front of it without moving the rest
     int orderStart;
     float gridOx, gridOy, gridInvH, gridW, gridWLarge;
+    int treeLogCount;   // records written to the world's tree log since the host last read it
     // SM clock cycles of the last step per phase: 0 new-fixture pairs, 1 collide, 2 island DFS,
     // 3 island solve, 4 fixture sync, 5 pairs after solve, 6 TOI, 7 whole step; then the island solve
     // split: 8 integrate + constraint init, 9 warm start + velocity sweeps, 10 impulses + position
@@ -280,7 +281,23 @@ struct Batch {
     int filterCap;
     int* filterMiss;
     int filterMissCap;
+    // The tree log (b2World::GetTreeHeight and the other tree diagnostics), or nullptr when no world
+    // of the batch keeps its tree: every fat box the device gives a proxy (b2DynamicTree::MoveProxy
+    // re-inserting the leaf), world w's records at kTreeLogPerProxy * proxyBase + kTreeLogExtra * w,
+    // kTreeLogPerProxy * proxyCap + kTreeLogExtra of them. treeLogId = proxy << 2 | kind (TreeLogKind).
+    int* treeLogId;
+    float4* treeLogFat;
 };
+
+// Records of the tree log per proxy slot and per world.
+constexpr int kTreeLogPerProxy = 8;
+constexpr int kTreeLogExtra = 256;
+// Kinds of tree-log records: kTreeOrdered re-insertions happen in log order (body edits between steps,
+// the continuous phase's events); the kTreeDiscrete ones are the discrete phase's fixture
+// synchronisation, written by many threads at once, whose order is the world's body list, then each
+// body's fixture list (b2World::Solve, Dynamics/b2World.cpp:494-514); kTreeStepMark opens a step's
+// discrete records.
+enum TreeLogKind : int { kTreeOrdered = 0, kTreeDiscrete = 1, kTreeStepMark = 2 };
 
 // Key and first probe of a verdict in the contact-filter table (fixtures below 2^20 per world).
 B2G_HD unsigned long long FilterKey(int w, int fA, int fB)

@@ -16,7 +16,9 @@ from .scenes import Scene
 class World:
     """A batch of Box2D worlds resident on the GPU (a single world is a batch of one)."""
 
-    def __init__(self, scenes):
+    def __init__(self, scenes, track_tree: bool = False):
+        """track_tree: keep every world's broadphase tree on the host for tree_stats (see
+        gb_world_track_tree; each step then waits for the previous one)."""
         if isinstance(scenes, Scene):
             scenes = [scenes]
         self.lib = _lib.load()
@@ -29,6 +31,8 @@ class World:
         h = C.c_void_p()
         _lib.check(self.lib.gb_world_create(self.n_worlds, defs, C.byref(h)), "gb_world_create")
         self.h = h
+        if track_tree:
+            _lib.check(self.lib.gb_world_track_tree(self.h, 1), "gb_world_track_tree")
         self.n_fixtures = []
         self.n_bodies = []
         self.dynamic_bodies = 0
@@ -142,6 +146,14 @@ class World:
         """b2World::DestroyBody; returns the listener calls as rows {kind, a, b} (see gb_destroy_body):
         kind 0 SayGoodbye(joint a), 1 SayGoodbye(fixture a), 2 EndContact(a, b)."""
         return self._destroy("gb_destroy_body", body, w)
+
+    def tree_stats(self, w: int = 0):
+        """b2World::GetTreeHeight, GetTreeBalance and GetTreeQuality of world w: (height, balance,
+        quality); the handle must have been made with track_tree=True."""
+        h, b, q = C.c_int(), C.c_int(), C.c_float()
+        _lib.check(self.lib.gb_world_tree_stats(self.h, int(w), C.byref(h), C.byref(b), C.byref(q)),
+                   "gb_world_tree_stats")
+        return h.value, b.value, np.float32(q.value)
 
     def body_set(self, body: int, prop: int, value: float, w: int = 0) -> np.ndarray:
         """b2Body::SetType (prop BODY_TYPE, value 0 static / 1 kinematic / 2 dynamic), SetActive,

@@ -149,6 +149,19 @@ gb_status gb_world_upload(gb_world* world);
 gb_status gb_world_step(gb_world* world, float dt, int velocity_iterations, int position_iterations);
 
 /* Waits for queued steps and returns the first error any world raised since the last sync. */
+/* b2World::GetTreeHeight, GetTreeBalance and GetTreeQuality (Box2D/Dynamics/b2World.cpp:1246-1259):
+ * the height, the largest child height difference and the node-perimeter ratio of the reference
+ * broadphase's dynamic tree. The device step keeps no tree (its pair finding works on the fat boxes),
+ * so a handle that answers these keeps one on the host: gb_world_track_tree(world, 1), before any
+ * fixture with a proxy exists in any of its worlds (GB_ERR_INVALID after), has every world replay
+ * the tree's history: the proxies created and destroyed between steps, and every fat box the device
+ * gives a proxy, which the step logs. A tracking handle replays the previous step's log before each
+ * step, which waits for that step. gb_world_tree_stats reads world w's three values (any pointer may be
+ * NULL); GB_ERR_INVALID when the handle does not track, GB_ERR_CAPACITY when a world's log ran out of
+ * room (more than 8 re-insertions per proxy plus 256 between two replays). */
+gb_status gb_world_track_tree(gb_world* world, int on);
+gb_status gb_world_tree_stats(gb_world* world, int w, int* height, int* balance, float* quality);
+
 /* b2Body property changes between steps (no step in progress): prop GB_BODY_TYPE (v[0] 0 static,
  * 1 kinematic, 2 dynamic; b2Body::SetType, Box2D/Dynamics/b2Body.cpp:115-166: mass reset, a static
  * body's velocities zeroed and fixtures synchronised, the body woken, its force cleared, its contacts

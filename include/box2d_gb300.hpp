@@ -767,6 +767,26 @@ public:
         for (int id : ids) n += id >= 0 ? 1 : 0;
         return n;
     }
+    // b2World::GetTreeHeight, GetTreeBalance, GetTreeQuality (Box2D/Dynamics/b2World.cpp:1246-1259): the
+    // broadphase tree the world replays on the host (0 when it cannot)
+    int GetTreeHeight()
+    {
+        int h = 0;
+        if (!Handle() || gb_world_tree_stats(m_h, 0, &h, nullptr, nullptr) != GB_OK) return 0;
+        return h;
+    }
+    int GetTreeBalance()
+    {
+        int b = 0;
+        if (!Handle() || gb_world_tree_stats(m_h, 0, nullptr, &b, nullptr) != GB_OK) return 0;
+        return b;
+    }
+    float GetTreeQuality()
+    {
+        float q = 0.0f;
+        if (!Handle() || gb_world_tree_stats(m_h, 0, nullptr, nullptr, &q) != GB_OK) return 0.0f;
+        return q;
+    }
     // b2World::GetProfile (Box2D/Dynamics/b2World.h:196) of the last step
     const b2Profile& GetProfile()
     {
@@ -1075,6 +1095,8 @@ private:
             m_def.gravity_x = m_gravity.x;
             m_def.gravity_y = m_gravity.y;
             if (gb_world_create(1, &m_def, &m_h) != GB_OK) m_h = nullptr;
+            // the broadphase tree's history, for GetTreeHeight, GetTreeBalance and GetTreeQuality
+            if (m_h) gb_world_track_tree(m_h, 1);
             if (m_h && !m_autoClear) gb_world_set_settings(m_h, 0, &m_def, 0);
         }
         return m_h;

@@ -92,6 +92,7 @@ def _declare(lib, p: str) -> None:
     sig["set_settings"] = (None, [vp, C.c_float, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int])
     sig["clear_forces"] = (None, [vp])
     sig["body_set"] = (None, [vp, C.c_int, C.c_int, _f32p])
+    sig["tree_stats"] = (None, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_float)])
     for kind in ("body", "joint", "fixture"):
         sig["destroy_" + kind] = (C.c_int, [vp, C.c_int, _i32p, C.c_int])
     if p == "rw_":
@@ -201,6 +202,12 @@ class OracleWorld:
         and SetAutoClearForces between steps."""
         self._fn("set_settings")(self.h, float(gravity[0]), float(gravity[1]), int(allow_sleep), int(warm_starting),
                                  int(continuous), int(sub_stepping), int(auto_clear_forces))
+
+    def tree_stats(self):
+        """b2World::GetTreeHeight, GetTreeBalance and GetTreeQuality: (height, balance, quality)."""
+        h, b, q = C.c_int(), C.c_int(), C.c_float()
+        self._fn("tree_stats")(self.h, C.byref(h), C.byref(b), C.byref(q))
+        return h.value, b.value, np.float32(q.value)
 
     def clear_forces(self) -> None:
         """b2World::ClearForces."""

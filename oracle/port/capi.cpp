@@ -121,6 +121,14 @@ void po_body_set(void* h, int b, int prop, const float* v)
 {
     static_cast<World*>(h)->SetBodyProperty(b, prop, v);
 }
+// b2World::GetTreeHeight, GetTreeBalance, GetTreeQuality (b2World.cpp:1246-1259)
+void po_tree_stats(void* h, int* height, int* balance, float* quality)
+{
+    const Tree& t = static_cast<World*>(h)->bp.tree;
+    *height = t.Height();
+    *balance = t.MaxBalance();
+    *quality = t.AreaRatio();
+}
 // b2World::ClearForces (b2World.cpp:967-974)
 void po_clear_forces(void* h)
 {

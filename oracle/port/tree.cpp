@@ -235,6 +235,32 @@ int Tree::Balance(int iA)
 
 int Tree::Height() const { return root == kNull ? 0 : nodes[root].height; }
 
+// b2DynamicTree::GetMaxBalance (b2DynamicTree.cpp:675-697): the largest child height difference of
+// the internal nodes, over the whole node pool.
+int Tree::MaxBalance() const
+{
+    int best = 0;
+    for (int i = 0; i < capacity; ++i) {
+        const TreeNode& n = nodes[i];
+        if (n.height <= 1) continue;
+        const int d = nodes[n.child2].height - nodes[n.child1].height;
+        best = Max(best, d < 0 ? -d : d);
+    }
+    return best;
+}
+
+// b2DynamicTree::GetAreaRatio (b2DynamicTree.cpp:534-559): the perimeters of every allocated node,
+// summed in pool order, over the root's.
+float Tree::AreaRatio() const
+{
+    if (root == kNull) return 0.0f;
+    const float rootArea = Perimeter(nodes[root].aabb);
+    float total = 0.0f;
+    for (int i = 0; i < capacity; ++i)
+        if (nodes[i].height >= 0) total += Perimeter(nodes[i].aabb);
+    return total / rootArea;
+}
+
 // ---------------------------------------------------------------- broadphase
 int BroadPhase::CreateProxy(const AABB& aabb, int user)
 {

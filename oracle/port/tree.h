@@ -29,6 +29,8 @@ struct Tree {
     void RemoveLeaf(int leaf);
     int Balance(int iA);
     int Height() const;
+    int MaxBalance() const;
+    float AreaRatio() const;
 };
 
 struct Pair { int a, b; };

@@ -448,6 +448,13 @@ void rw_body_set(void* h, int b, int prop, const float* v)
     default: break;
     }
 }
+void rw_tree_stats(void* h, int* height, int* balance, float* quality)
+{
+    const b2World& w = static_cast<RefWorld*>(h)->world;
+    *height = w.GetTreeHeight();
+    *balance = w.GetTreeBalance();
+    *quality = w.GetTreeQuality();
+}
 void rw_clear_forces(void* h)
 {
     static_cast<RefWorld*>(h)->world.ClearForces();

@@ -33,6 +33,30 @@ def trajectory_cases():
     return [(n, f, s) for (n, f, s, _c) in mod.cases()]
 
 
+def tree_cases():
+    """(name, scene factory, steps, ops by step) of the tree_stats.npz golden cases."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.tree_cases()
+
+
+def tree_stats_mismatch(world, steps: int, script: dict, g, name: str):
+    """Steps `world` (oracle or device) with the case's ops and compares its tree height, balance and
+    quality (bits) with the golden ones after every step; returns the first differing step or None."""
+    hb, q = g[f"{name}_hb"], g[f"{name}_quality"]
+    for s in range(1, steps + 1):
+        if s in script:
+            apply_ops(world, script[s])
+        world.step(DT, VI, PI)
+        h, b, qq = world.tree_stats()
+        if (h, b) != tuple(int(x) for x in hb[s - 1]) or np.float32(qq).view(np.uint32) != q[s - 1].view(np.uint32):
+            return s, (h, b, qq), (hb[s - 1], q[s - 1])
+    return None
+
+
 def first_divergence(world, steps: int, golden_digests: np.ndarray):
     """Step index (1-based) where `world`'s state digest first differs from the golden one, or None."""
     for s in range(1, steps + 1):

@@ -2,7 +2,8 @@
 // a box pyramid, a pendulum on a revolute joint and a two-fixture body; bodies, a fixture and (with its
 // anchor body) the joint are destroyed between steps and a body is created after them. Prints the
 // listener calls, the body states as hex floats, the body list, the proxy count, query and ray-cast
-// callback results, the first contact's world manifold and whether the profile was filled.
+// callback results, the first contact's world manifold, the broadphase tree's height, balance and
+// quality, and whether the profile was filled.
 #include <cstdio>
 #include <vector>
 
@@ -182,6 +183,7 @@ int main()
                     wm.separations[1]);
         break;
     }
+    std::printf("tree %d %d %a\n", world.GetTreeHeight(), world.GetTreeBalance(), world.GetTreeQuality());
     const b2Profile& prof = world.GetProfile();
     std::printf("profile %d\n", prof.step > 0.0f && prof.solve > 0.0f ? 1 : 0);
     return 0;

@@ -22,6 +22,8 @@ Two builds of the reference are used: ``libm`` (glibc sinf/cosf, the reference a
 * ``collide.npz``: seeded shape pairs of every supported type pair with the reference manifolds.
 * ``toi.npz``: seeded sweeps with the reference b2TimeOfImpact result.
 * ``trig.npz``: glibc sinf/cosf on seeded angles (how far the project trig is from libm).
+* ``tree_stats.npz``: b2World::GetTreeHeight, GetTreeBalance and GetTreeQuality after every step of
+  trajectory and scripted cases (project trig; ``--tree`` writes only this file).
 * ``query_<scene>.npz``: b2World::QueryAABB and closest-hit b2World::RayCast results on a stepped
   scene (project trig) for seeded boxes and segments (``--queries`` writes only these).
 """
@@ -274,10 +276,51 @@ def make_trig(n: int = 200000):
     np.savez_compressed(os.path.join(HERE, "trig.npz"), x=x, sin=s, cos=c)
 
 
+def tree_cases():
+    """Cases of tree_stats.npz: (name, scene factory, steps, ops by step)."""
+    from tests._util import body_props_script, destroy_script
+
+    return [("pyramid20", lambda: scenes.config1(), 200, {}),
+            ("drop300", lambda: scenes.drop(300, scenes.SplitMix64(7)), 300, {}),
+            ("chains6x16", lambda: chains_with_load(), 200, {}),
+            ("chain_terrain", lambda: scenes.chain_terrain(scenes.SplitMix64(12)), 200, {}),
+            ("sensors", lambda: scenes.sensors(scenes.SplitMix64(13)), 200, {}),
+            ("batch3", lambda: batch_world(3), 200, {}),
+            ("config2_10k", lambda: scenes.config2(10000, seed=1, allow_sleep=True), 100, {}),
+            ("destroy_mix", lambda: scenes.destroy_mix(scenes.SplitMix64(5)), 200, destroy_script()),
+            ("body_props", lambda: scenes.destroy_mix(scenes.SplitMix64(11)), 320, body_props_script())]
+
+
+def make_tree():
+    """b2World::GetTreeHeight, GetTreeBalance and GetTreeQuality of the reference (project trig) after
+    every step: ``<case>_hb`` (steps x 2 int32, height and balance), ``<case>_quality`` (float32)."""
+    from tests._util import apply_ops
+
+    out = {}
+    for name, make, steps, script in tree_cases():
+        w = oracle.OracleWorld(make(), "reference", "project")
+        hb = np.zeros((steps, 2), dtype=np.int32)
+        q = np.zeros(steps, dtype=np.float32)
+        for s in range(1, steps + 1):
+            if s in script:
+                apply_ops(w, script[s])
+            w.step(DT, VI, PI)
+            h, b, qq = w.tree_stats()
+            hb[s - 1] = (h, b)
+            q[s - 1] = qq
+        out[f"{name}_hb"] = hb
+        out[f"{name}_quality"] = q
+    np.savez_compressed(os.path.join(HERE, "tree_stats.npz"), **out)
+
+
 def main():
     oracle.build_reference()
     if "--queries" in sys.argv:
         make_queries()
+        print("done")
+        return
+    if "--tree" in sys.argv:
+        make_tree()
         print("done")
         return
     only = sys.argv[sys.argv.index("--case") + 1] if "--case" in sys.argv else None
@@ -327,6 +370,7 @@ def main():
     make_toi()
     make_trig()
     make_queries()
+    make_tree()
     print("done")
 
 

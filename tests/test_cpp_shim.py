@@ -388,6 +388,10 @@ def test_cpp_destroy_queries_match_oracle(gpu, tmp_path):
     assert int(rr[0]) == int(fix[0]) and int(rr[-1]) == len(allf)
     got = np.array([float.fromhex(v) for v in rr[1:6]], dtype=np.float32)
     assert np.array_equal(got.view(np.uint32), hit[0].view(np.uint32))
+    th, tb, tq = o.tree_stats()
+    t = out["tree"]
+    assert [int(t[0]), int(t[1])] == [th, tb]
+    assert np.float32(float.fromhex(t[2])).view(np.uint32) == tq.view(np.uint32)
     ci, cf = o.contacts()
     m = out["manifold"]
     k = int(m[0])

@@ -204,3 +204,16 @@ def test_port_settings_case_matches_reference(trig):
             if trig == "libm" and platform.machine() != "x86_64":
                 pytest.skip("libm trig differs on this machine")
             raise AssertionError(f"first divergence at step {s}")
+
+
+@pytest.mark.parametrize("case", [c[0] for c in __import__("tests._util", fromlist=["tree_cases"]).tree_cases()])
+def test_port_tree_stats_match_reference(case):
+    """b2World::GetTreeHeight, GetTreeBalance and GetTreeQuality of the restatement's dynamic tree after
+    every step (trajectories with time of impact, joints, chains and sensors, a 10,000-body drop, and
+    the destruction and body-property scripts) as the reference's."""
+    from tests._util import tree_cases, tree_stats_mismatch
+
+    name, make, steps, script = next(c for c in tree_cases() if c[0] == case)
+    g = golden("tree_stats")
+    w = oracle.OracleWorld(make(), "port", "project")
+    assert tree_stats_mismatch(w, steps, script, g, name) is None
