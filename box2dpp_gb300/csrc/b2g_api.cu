@@ -14,6 +14,8 @@
 #include <mutex>
 #include <new>
 #include <numeric>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "../../include/box2d_gb300.h"
@@ -2735,9 +2737,196 @@ gb_status SetBodyPropertyHost(HWorld& W, int bi, int prop, const float* v, Calls
     }
 }
 
+// ---- world checkpoints: a versioned record of everything a later step reads (the host copy after the
+// device state was pulled back), each column a count and its raw records. Records are copied whole,
+// so a checkpoint restores only into a build with the same record layouts, which the header's sizes
+// check.
+constexpr unsigned kCheckpointMagic = 0x57473242u;  // "B2GW"
+constexpr unsigned kCheckpointVersion = 1;
+
+template <typename T> void PutColumn(std::vector<unsigned char>& out, const std::vector<T>& v)
+{
+    static_assert(std::is_trivially_copyable<T>::value, "checkpoint columns are raw records");
+    const long long n = (long long)v.size();
+    const unsigned char* b = reinterpret_cast<const unsigned char*>(&n);
+    out.insert(out.end(), b, b + sizeof(n));
+    if (n > 0) {
+        const unsigned char* d = reinterpret_cast<const unsigned char*>(v.data());
+        out.insert(out.end(), d, d + n * sizeof(T));
+    }
+}
+template <typename T> void PutValue(std::vector<unsigned char>& out, const T& x)
+{
+    static_assert(std::is_trivially_copyable<T>::value, "checkpoint values are raw records");
+    const unsigned char* b = reinterpret_cast<const unsigned char*>(&x);
+    out.insert(out.end(), b, b + sizeof(T));
+}
+template <typename T> bool GetColumn(const unsigned char*& p, const unsigned char* end, std::vector<T>& v)
+{
+    long long n = 0;
+    if ((size_t)(end - p) < sizeof(n)) return false;
+    std::memcpy(&n, p, sizeof(n));
+    p += sizeof(n);
+    if (n < 0 || (unsigned long long)n > (unsigned long long)(end - p) / sizeof(T)) return false;
+    v.resize((size_t)n);
+    if (n > 0) std::memcpy(v.data(), p, (size_t)n * sizeof(T));
+    p += (size_t)n * sizeof(T);
+    return true;
+}
+template <typename T> bool GetValue(const unsigned char*& p, const unsigned char* end, T& x)
+{
+    if ((size_t)(end - p) < sizeof(T)) return false;
+    std::memcpy(&x, p, sizeof(T));
+    p += sizeof(T);
+    return true;
+}
+
+// the record sizes a checkpoint was written with (a build with other layouts refuses it)
+std::vector<int> CheckpointLayout()
+{
+    return {(int)sizeof(gb_world_def), (int)sizeof(HBody), (int)sizeof(HFixture), (int)sizeof(Joint),
+            (int)sizeof(WorldState), (int)sizeof(int4), (int)sizeof(float4)};
+}
+
+void SaveWorld(const HWorld& W, std::vector<unsigned char>& out)
+{
+    PutValue(out, kCheckpointMagic);
+    PutValue(out, kCheckpointVersion);
+    PutColumn(out, CheckpointLayout());
+    PutValue(out, W.def);
+    const int flags[10] = {W.autoClear ? 1 : 0, W.bodyList, W.jointList, W.nodeFresh, W.proxyCount,
+                           W.treeLost ? 1 : 0, W.newFixture, W.hasState ? 1 : 0,
+                           W.trackTree && !W.treeIncomplete ? 1 : 0, 0};
+    PutValue(out, flags);
+    PutColumn(out, W.bodies);
+    PutColumn(out, W.fixtures);
+    PutColumn(out, W.joints);
+    PutColumn(out, W.fat);
+    PutColumn(out, W.pfix);
+    PutColumn(out, W.moved);
+    PutColumn(out, W.nodeFree);
+    PutValue(out, W.state);
+    const HContacts& C = W.contacts;
+    PutColumn(out, C.ci); PutColumn(out, C.ce); PutColumn(out, C.mh);
+    PutColumn(out, C.cp); PutColumn(out, C.mv); PutColumn(out, C.mp0); PutColumn(out, C.mp1);
+    PutColumn(out, C.order); PutColumn(out, C.cnext);
+    if (flags[8]) W.tree.Save(out);
+}
+
+// A checkpoint into W (whole or not at all). The indices inside are checked against the columns'
+// sizes so that no later step reads outside them.
+bool LoadWorld(HWorld& W, const unsigned char* p, const unsigned char* end)
+{
+    unsigned magic = 0, version = 0;
+    if (!GetValue(p, end, magic) || !GetValue(p, end, version)) return false;
+    if (magic != kCheckpointMagic || version != kCheckpointVersion) return false;
+    std::vector<int> layout;
+    if (!GetColumn(p, end, layout) || layout != CheckpointLayout()) return false;
+    HWorld N;
+    int flags[10];
+    if (!GetValue(p, end, N.def) || !GetValue(p, end, flags)) return false;
+    HContacts& C = N.contacts;
+    if (!GetColumn(p, end, N.bodies) || !GetColumn(p, end, N.fixtures) || !GetColumn(p, end, N.joints) ||
+        !GetColumn(p, end, N.fat) || !GetColumn(p, end, N.pfix) || !GetColumn(p, end, N.moved) ||
+        !GetColumn(p, end, N.nodeFree) || !GetValue(p, end, N.state) || !GetColumn(p, end, C.ci) ||
+        !GetColumn(p, end, C.ce) || !GetColumn(p, end, C.mh) || !GetColumn(p, end, C.cp) ||
+        !GetColumn(p, end, C.mv) || !GetColumn(p, end, C.mp0) || !GetColumn(p, end, C.mp1) ||
+        !GetColumn(p, end, C.order) || !GetColumn(p, end, C.cnext))
+        return false;
+    const bool hasTree = flags[8] != 0;
+    if (hasTree && !N.tree.Load(p, end)) return false;
+    if (p != end) return false;
+    N.autoClear = flags[0] != 0;
+    N.bodyList = flags[1];
+    N.jointList = flags[2];
+    N.nodeFresh = flags[3];
+    N.proxyCount = flags[4];
+    N.treeLost = flags[5] != 0;
+    N.newFixture = flags[6];
+    N.hasState = flags[7] != 0;
+    // index ranges: bodies, fixtures and joints refer to each other, proxies to fixtures
+    const int nb = (int)N.bodies.size(), nf = (int)N.fixtures.size(), nj = (int)N.joints.size();
+    const int np = (int)N.fat.size();
+    auto inRange = [](int i, int n) { return i == kNullIdx || (i >= 0 && i < n); };
+    if (!inRange(N.bodyList, nb) || !inRange(N.jointList, nj) || (int)N.pfix.size() != np ||
+        (int)N.moved.size() != np || N.nodeFresh < 0)
+        return false;
+    for (const HBody& b : N.bodies)
+        if (!inRange(b.fixtureList, nf) || !inRange(b.next, nb) || b.type < 0 || b.type > 2) return false;
+    for (const HFixture& f : N.fixtures)
+        if (!inRange(f.body, nb) || !inRange(f.next, nf) || !inRange(f.proxyId, np) || f.shape.count < 0 ||
+            f.shape.count > kMaxPolyVerts)
+            return false;
+    for (const Joint& j : N.joints)
+        if (j.bodyA != kNullIdx && (!inRange(j.bodyA, nb) || !inRange(j.bodyB, nb) || j.type < 0 ||
+                                    j.type >= kJointTypes))
+            return false;
+    for (int x : N.pfix)
+        if (!inRange(x, nf)) return false;
+    if (N.hasState) {
+        const size_t nc = C.ci.size();
+        if (C.ce.size() != nc || C.mh.size() != nc || C.cp.size() != nc || C.mv.size() != nc ||
+            C.mp0.size() != nc || C.mp1.size() != nc || C.order.size() != nc || C.cnext.size() != nc ||
+            N.state.contactCount < 0 || (size_t)N.state.contactCount > nc)
+            return false;
+    }
+    N.trackTree = W.trackTree;
+    N.treeIncomplete = W.trackTree && !hasTree;
+    if (!N.trackTree) N.tree = ProxyTree();
+    W = std::move(N);
+    return true;
+}
+
 } // namespace
 
 extern "C" {
+
+gb_status gb_world_checkpoint(gb_world* g, int w, void* buf, size_t cap, size_t* size)
+{
+    if (!g || w < 0 || w >= (int)g->worlds.size() || g->splitOpen || !size) return GB_ERR_INVALID;
+    if (g->onDevice) {
+        GB_CUDA(cudaStreamSynchronize(g->stream));
+        if (g->upStream) GB_CUDA(cudaStreamSynchronize(g->upStream));
+        if (g->downStream) GB_CUDA(cudaStreamSynchronize(g->downStream));
+        // the world's device state as the host copy (the device keeps it: nothing is marked changed)
+        gb_status s = Download(g);
+        if (s != GB_OK) return s;
+    }
+    std::vector<unsigned char> out;
+    SaveWorld(g->worlds[w], out);
+    *size = out.size();
+    if (!buf || cap < out.size()) return buf ? GB_ERR_CAPACITY : GB_OK;
+    std::memcpy(buf, out.data(), out.size());
+    return GB_OK;
+}
+
+gb_status gb_world_restore(gb_world* g, int w, const void* buf, size_t size)
+{
+    if (!g || w < 0 || w >= (int)g->worlds.size() || !buf || g->splitOpen || g->locked) return GB_ERR_INVALID;
+    gb_status s = Mutable(g, w);
+    if (s != GB_OK) return s;
+    const unsigned char* p = static_cast<const unsigned char*>(buf);
+    if (!LoadWorld(g->worlds[w], p, p + size)) return GB_ERR_INVALID;
+    ReleaseGraph(g);
+    if (g->filterFn) {
+        // verdicts of the world's old fixture pairs are decided again when met
+        std::vector<unsigned long long> keys((size_t)g->filterCap);
+        std::vector<int> vals((size_t)g->filterCap);
+        GB_CUDA(cudaMemcpy(keys.data(), g->dFilterKeys, g->filterCap * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(vals.data(), g->dFilterVals, g->filterCap * sizeof(int), cudaMemcpyDeviceToHost));
+        std::vector<unsigned long long> kk;
+        std::vector<int> vv;
+        for (int i = 0; i < g->filterCap; ++i)
+            if (keys[i] != ~0ull && (int)(keys[i] >> 40) != w) {
+                kk.push_back(keys[i]);
+                vv.push_back(vals[i]);
+            }
+        s = BuildFilterTable(g, g->filterCap, kk, vv);
+        if (s != GB_OK) return s;
+        AttachFilter(g);
+    }
+    return GB_OK;
+}
 
 gb_status gb_world_track_tree(gb_world* g, int on)
 {

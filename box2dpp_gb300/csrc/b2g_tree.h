@@ -7,6 +7,7 @@
 // swept box leaves its fat box), which the step logs in the reference's order.
 #pragma once
 
+#include <cstring>
 #include <vector>
 
 #include "b2g_core.h"
@@ -67,7 +68,42 @@ public:
         return sum / rootP;
     }
 
+    // the whole tree as bytes (world checkpoints) and back; Load returns false on malformed input
+    void Save(std::vector<unsigned char>& out) const
+    {
+        const int head[3] = {(int)nodes_.size(), root_, free_};
+        Append(out, head, sizeof(head));
+        if (!nodes_.empty()) Append(out, nodes_.data(), nodes_.size() * sizeof(Node));
+    }
+    bool Load(const unsigned char*& p, const unsigned char* end)
+    {
+        int head[3];
+        if (end - p < (long)sizeof(head)) return false;
+        std::memcpy(head, p, sizeof(head));
+        p += sizeof(head);
+        const int n = head[0];
+        if (n < 0 || (size_t)(end - p) < (size_t)n * sizeof(Node) || head[1] < kNone || head[1] >= n ||
+            head[2] < kNone || head[2] >= n)
+            return false;
+        nodes_.resize(n);
+        if (n > 0) std::memcpy(nodes_.data(), p, n * sizeof(Node));
+        p += n * sizeof(Node);
+        for (const Node& x : nodes_)
+            if (x.parent < kNone || x.parent >= n || x.child1 < kNone || x.child1 >= n || x.child2 < kNone ||
+                x.child2 >= n || (x.height > 0 && (x.child1 < 0 || x.child2 < 0)))
+                return false;
+        root_ = head[1];
+        free_ = head[2];
+        return true;
+    }
+
 private:
+    static void Append(std::vector<unsigned char>& out, const void* src, size_t bytes)
+    {
+        const unsigned char* b = static_cast<const unsigned char*>(src);
+        out.insert(out.end(), b, b + bytes);
+    }
+
     struct Node {
         float4 box = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         int parent = kNone;  // the next free node while the node is in the free list

@@ -147,6 +147,23 @@ class World:
         kind 0 SayGoodbye(joint a), 1 SayGoodbye(fixture a), 2 EndContact(a, b)."""
         return self._destroy("gb_destroy_body", body, w)
 
+    def checkpoint(self, w: int = 0) -> bytes:
+        """World w's whole state between steps (gb_world_checkpoint), as bytes."""
+        n = C.c_size_t()
+        _lib.check(self.lib.gb_world_checkpoint(self.h, int(w), None, 0, C.byref(n)), "gb_world_checkpoint")
+        buf = C.create_string_buffer(n.value)
+        _lib.check(self.lib.gb_world_checkpoint(self.h, int(w), buf, n.value, C.byref(n)), "gb_world_checkpoint")
+        return buf.raw[:n.value]
+
+    def restore(self, data: bytes, w: int = 0) -> None:
+        """Replaces world w with a checkpoint (gb_world_restore); the following steps are those of the
+        world it was taken from, bit for bit."""
+        _lib.check(self.lib.gb_world_restore(self.h, int(w), data, len(data)), "gb_world_restore")
+        b, f, c, j = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        _lib.check(self.lib.gb_world_counts(self.h, int(w), C.byref(b), C.byref(f), C.byref(c), C.byref(j)),
+                   "gb_world_counts")
+        self.n_bodies[w], self.n_fixtures[w] = b.value, f.value
+
     def tree_stats(self, w: int = 0):
         """b2World::GetTreeHeight, GetTreeBalance and GetTreeQuality of world w: (height, balance,
         quality); the handle must have been made with track_tree=True."""

@@ -149,6 +149,18 @@ gb_status gb_world_upload(gb_world* world);
 gb_status gb_world_step(gb_world* world, float dt, int velocity_iterations, int position_iterations);
 
 /* Waits for queued steps and returns the first error any world raised since the last sync. */
+/* World checkpoints (the reference has only b2World::Dump, Box2D/Dynamics/b2World.cpp:1271-1328,
+ * which prints code that rebuilds the scene without its contacts): gb_world_checkpoint writes world
+ * w's whole state between steps (bodies with their sweeps, sleep times and forces; fixtures, proxies
+ * and the tree's free list; joints with their impulses; the contact list in order with manifolds and
+ * impulses; the world's settings; the broadphase tree when the handle tracks it) to buf and puts the
+ * byte count in *size (buf NULL: only the count; cap too small: GB_ERR_CAPACITY). gb_world_restore
+ * replaces world w of any handle with such a checkpoint; the steps that follow are bit for bit those
+ * of the world it was taken from (under the same solver settings). A checkpoint restores only into
+ * a library of the same build layout (GB_ERR_INVALID otherwise, and for malformed data). */
+gb_status gb_world_checkpoint(gb_world* world, int w, void* buf, size_t cap, size_t* size);
+gb_status gb_world_restore(gb_world* world, int w, const void* buf, size_t size);
+
 /* b2World::GetTreeHeight, GetTreeBalance and GetTreeQuality (Box2D/Dynamics/b2World.cpp:1246-1259):
  * the height, the largest child height difference and the node-perimeter ratio of the reference
  * broadphase's dynamic tree. The device step keeps no tree (its pair finding works on the fat boxes),
