@@ -18,7 +18,7 @@ def _digests(w, steps, k=0):
     out = []
     for _ in range(steps):
         w.step(DT, VI, PI)
-        out.append(digest(w.bodies(k), *w.contacts(k)))
+        out.append(bytes(digest(w.bodies(k), *w.contacts(k))))
     return out
 
 
