@@ -95,6 +95,7 @@ struct HWorld {
     bool trackTree = false, treeIncomplete = false;
     ProxyTree tree;
     int newFixture = 0;
+    int capHint = 0;  // contact slots the next upload gives at least (grown after an overflow)
     WorldState state{};
     bool hasState = false; // state/contacts valid (pulled back from, or never sent to, the device)
     HContacts contacts;
@@ -129,6 +130,11 @@ struct gb_world {
     int* dFilterMiss = nullptr;
     int filterCap = 0, filterUsed = 0;
     std::vector<void*> shadow;
+    // grow-and-retry (gb_world_set_recovery): attempts per step, a copy of every device column taken
+    // before each step, and the steps that were run again
+    int recoverAttempts = 0;
+    std::vector<void*> recoverShadow;
+    long long recoveries = 0;
     long long filterReplays = 0;
     int* dSchedule = nullptr;
     // row chunks of the flat pre-passes in schedule order (see kRowChunk), and the first chunk of
@@ -358,6 +364,8 @@ void FreeDevice(gb_world* g)
     g->allocationBytes.clear();
     for (void* p : g->shadow) cudaFree(p);
     g->shadow.clear();
+    for (void* p : g->recoverShadow) cudaFree(p);
+    g->recoverShadow.clear();
     std::memset(&g->batch, 0, sizeof(g->batch));
     g->dSchedule = nullptr;
     g->dNpChunks = g->dToiChunks = nullptr;
@@ -866,7 +874,7 @@ gb_status Upload(gb_world* g)
         int oldCap = W.hasState ? (int)W.contacts.ci.size() : 0;
         int cap = std::max(64, 8 * d.fixCount);
         if (g->contactCapLimit > 0 && !W.hasState) cap = g->contactCapLimit;
-        cap = std::max(cap, oldCap);
+        cap = std::max(std::max(cap, oldCap), W.capHint);
         d.contactBase = (int)tc; d.contactCap = cap;
         d.jointBase = (int)tj; d.jointCount = (int)W.joints.size();
         d.pairBase = (int)tq; d.pairCap = NextPow2(std::max(256, cap));
@@ -1116,6 +1124,65 @@ gb_status FilteredStep(gb_world* g, const StepParams& P)
                                     g->stream));
     }
     return GB_ERR_TIMEOUT;
+}
+
+// One step with grow-and-retry: every device column is copied aside, the step runs and is waited for,
+// and when a world overflowed a fixed buffer (GB_ERR_CAPACITY: contact slots, pairs, island rows) or
+// hit the time-of-impact event limit (GB_ERR_TIMEOUT), the columns are put back, the world's contact
+// capacity (which sizes the pair and row buffers too) or the event limit is doubled, the state goes
+// through the host to the larger buffers, and the step runs again; the overflowing attempt leaves no
+// trace, so the result is the step the reference takes. After recoverAttempts retries the last
+// error stands, as without recovery.
+gb_status StepOnce(gb_world* g, const StepParams& P)
+{
+    if (g->filterFn) return FilteredStep(g, P);
+    if (g->tuneIndex >= 0) return TunedStep(g, P);
+    return LaunchPlanStep(g, P, g->plan);
+}
+
+gb_status RecoveringStep(gb_world* g, float dt, int vi, int pi)
+{
+    for (int attempt = 0;; ++attempt) {
+        if (g->recoverShadow.size() != g->allocations.size()) {
+            for (void* p : g->recoverShadow) cudaFree(p);
+            g->recoverShadow.assign(g->allocations.size(), nullptr);
+            for (size_t i = 0; i < g->allocations.size(); ++i)
+                GB_CUDA(cudaMalloc(&g->recoverShadow[i], g->allocationBytes[i]));
+        }
+        for (size_t i = 0; i < g->allocations.size(); ++i)
+            GB_CUDA(cudaMemcpyAsync(g->recoverShadow[i], g->allocations[i], g->allocationBytes[i],
+                                    cudaMemcpyDeviceToDevice, g->stream));
+        gb_status s = StepOnce(g, MakeParams(g, dt, vi, pi));
+        if (s != GB_OK) return s;
+        GB_CUDA(cudaStreamSynchronize(g->stream));
+        const int nw = (int)g->worlds.size();
+        std::vector<WorldState> st(nw);
+        GB_CUDA(cudaMemcpy(st.data(), g->batch.state, nw * sizeof(WorldState), cudaMemcpyDeviceToHost));
+        bool capacity = false, timeout = false;
+        for (const WorldState& x : st) {
+            capacity |= (x.error & kErrCapacity) != 0;
+            timeout |= (x.error & kErrTimeout) != 0;
+        }
+        if (!capacity && !timeout) return GB_OK;
+        if (attempt >= g->recoverAttempts) return GB_OK;  // the error stays in the state for gb_world_sync
+        for (size_t i = 0; i < g->allocations.size(); ++i)
+            GB_CUDA(cudaMemcpyAsync(g->allocations[i], g->recoverShadow[i], g->allocationBytes[i],
+                                    cudaMemcpyDeviceToDevice, g->stream));
+        GB_CUDA(cudaStreamSynchronize(g->stream));
+        for (int wi = 0; wi < nw; ++wi)
+            if (st[wi].error & kErrCapacity)
+                g->worlds[wi].capHint = 2 * g->desc[wi].contactCap;
+        if (timeout) {
+            g->maxToiEvents *= 2;
+            ReleaseGraph(g);
+        }
+        ++g->recoveries;
+        s = Download(g);
+        if (s != GB_OK) return s;
+        g->hostDirty = true;
+        s = Upload(g);
+        if (s != GB_OK) return s;
+    }
 }
 
 gb_status Mutable(gb_world* g, int w)
@@ -1742,6 +1809,7 @@ gb_status gb_world_step(gb_world* g, float dt, int vi, int pi)
     gb_status s = TreeSync(g);
     if (s == GB_OK) s = Upload(g);
     if (s != GB_OK) return s;
+    if (g->recoverAttempts > 0) return RecoveringStep(g, dt, vi, pi);
     const StepParams P = MakeParams(g, dt, vi, pi);
     if (g->filterFn) return FilteredStep(g, P);
     if (g->tuneIndex >= 0) {
@@ -1807,6 +1875,7 @@ gb_status gb_world_graph_step(gb_world* g, float dt, int vi, int pi)
 {
     if (!g || vi < 0 || pi < 0 || g->splitOpen) return GB_ERR_INVALID;
     if (g->filterFn) return gb_world_step(g, dt, vi, pi);  // a filtered step may run again: no graph
+    if (g->recoverAttempts > 0) return gb_world_step(g, dt, vi, pi);  // so may a recovering one
     if (g->tuneIndex >= 0) return gb_world_step(g, dt, vi, pi);  // tuning steps are timed one by one
     gb_status s = TreeSync(g);
     if (s == GB_OK) s = Upload(g);
@@ -1953,6 +2022,24 @@ gb_status gb_world_clear_forces(gb_world* g, int w)
         B.force = V(0.0f, 0.0f);
         B.torque = 0.0f;
     }
+    return GB_OK;
+}
+
+gb_status gb_world_set_recovery(gb_world* g, int attempts)
+{
+    if (!g || attempts < 0 || attempts > 30 || g->splitOpen) return GB_ERR_INVALID;
+    g->recoverAttempts = attempts;
+    if (attempts == 0) {
+        for (void* p : g->recoverShadow) cudaFree(p);
+        g->recoverShadow.clear();
+    }
+    return GB_OK;
+}
+
+gb_status gb_world_recoveries(gb_world* g, long long* retries)
+{
+    if (!g || !retries) return GB_ERR_INVALID;
+    *retries = g->recoveries;
     return GB_OK;
 }
 

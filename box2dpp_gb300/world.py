@@ -207,6 +207,16 @@ class World:
         """b2World::ClearForces of world w."""
         _lib.check(self.lib.gb_world_clear_forces(self.h, int(w)), "gb_world_clear_forces")
 
+    def set_recovery(self, attempts: int) -> None:
+        """Grow-and-retry of overflowing steps (gb_world_set_recovery); 0 turns it off."""
+        _lib.check(self.lib.gb_world_set_recovery(self.h, int(attempts)), "gb_world_set_recovery")
+
+    def recoveries(self) -> int:
+        """Steps run again after an overflow so far."""
+        n = C.c_longlong()
+        _lib.check(self.lib.gb_world_recoveries(self.h, C.byref(n)), "gb_world_recoveries")
+        return n.value
+
     def set_limits(self, contact_capacity: int = 0, max_toi_events: int = 4096) -> None:
         """Fixed capacities of the device step (see gb_world_set_limits): contact slots per world at
         the first upload (0: the default) and time-of-impact events per world per step."""

@@ -251,6 +251,16 @@ gb_status gb_world_filter_stats(gb_world* world, long long* replays, int* verdic
 
 gb_status gb_world_sync(gb_world* world);
 
+/* Grow-and-retry: with attempts > 0 every gb_world_step (and gb_world_graph_step, which then does not
+ * replay a graph) keeps a copy of the device state, waits for the step, and when a world overflowed a
+ * fixed buffer (contact slots, pairs, island rows: GB_ERR_CAPACITY) or reached the time-of-impact
+ * event limit (GB_ERR_TIMEOUT) puts the state back, doubles that world's contact capacity (or the
+ * event limit) and runs the step again, up to `attempts` times; the step's result is then the one the
+ * reference takes. Each step waits for the device; not for steps captured into a caller's graph.
+ * gb_world_recoveries: the steps run again so far. */
+gb_status gb_world_set_recovery(gb_world* world, int attempts);
+gb_status gb_world_recoveries(gb_world* world, long long* retries);
+
 /* No counterpart in the reference (whose buffers grow on demand). The fixed capacities of the device
  * step, for callers that size memory themselves and for tests of the error paths: contact_capacity
  * > 0 sets the contact slots of each world at its first upload (0 keeps the default, max(64, 8 x

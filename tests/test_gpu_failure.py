@@ -1,7 +1,8 @@
 """Failure paths of the device step, made on the host and ended by bounded device loops (no fault,
 trap or hang): a world whose contact slots run out returns GB_ERR_CAPACITY from gb_world_sync, a
 world whose time-of-impact events in a step exceed the limit returns GB_ERR_TIMEOUT, and in both cases
-the CUDA context stays usable: a new world steps bit-exactly afterwards."""
+the CUDA context stays usable: a new world steps bit-exactly afterwards. With grow-and-retry on, the
+same worlds complete every step bit-exactly, the overflowing steps run again with larger buffers."""
 from __future__ import annotations
 
 import numpy as np
@@ -68,3 +69,33 @@ def test_limits_are_checked(gpu):
     w.set_limits(max_toi_events=8)
     w.step(DT, VI, PI)
     w.sync()
+
+
+def test_recovery_grows_the_contact_slots(gpu):
+    sc = scenes.pyramid(8)
+    w = World(sc)
+    w.set_limits(contact_capacity=16)
+    w.set_recovery(6)
+    o = oracle.OracleWorld(sc, "port", "project")
+    for _ in range(30):
+        w.step(DT, VI, PI)
+        o.step(DT, VI, PI)
+    w.sync()  # no error left
+    assert w.recoveries() >= 1
+    assert np.array_equal(w.bodies().view(np.uint32), o.bodies().view(np.uint32))
+    ints, _ = w.contacts()
+    assert len(ints) == len(o.contacts()[0]) > 16
+
+
+def test_recovery_raises_the_event_limit(gpu):
+    sc = scenes.drop(400, scenes.SplitMix64(11), allow_sleep=False)
+    w = World(sc)
+    w.set_limits(max_toi_events=1)
+    w.set_recovery(8)
+    o = oracle.OracleWorld(sc, "port", "project")
+    for _ in range(60):
+        w.step(DT, VI, PI)
+        o.step(DT, VI, PI)
+    w.sync()
+    assert w.recoveries() >= 1
+    assert np.array_equal(w.bodies().view(np.uint32), o.bodies().view(np.uint32))
