@@ -1199,8 +1199,10 @@ __device__ void Wd::findNewContacts(bool inToi, int knownMoved)
             if (pairKeep[k] && o < d.contactCap) keptIdx[o++] = k;
         __syncthreads();
     }
-    // more new contacts than contact slots cannot be created: the free list runs dry below
+    // more new contacts than contact slots cannot be created: those beyond the capacity are an overflow
+    // here, and the free list runs dry below when fewer slots are free
     const int nKept = min(sKept, d.contactCap);
+    if (sKept > d.contactCap && tid() == 0) atomicOr(&st->error, kErrCapacity);
     int4* info = pairInfo;
     for (int r = tid(); r < nKept; r += nthreads()) {
         const int k = keptIdx[r];
