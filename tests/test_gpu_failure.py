@@ -43,6 +43,16 @@ def test_contact_slots_running_out_reports_capacity(gpu):
     _context_still_usable()
 
 
+def test_more_new_pairs_than_slots_reports_capacity_at_once(gpu):
+    # the first step finds about 90 pairs for 16 free slots
+    w = World(scenes.pyramid(8))
+    w.set_limits(contact_capacity=16)
+    w.step(DT, VI, PI)
+    with pytest.raises(_lib.GbError) as e:
+        w.sync()
+    assert e.value.status == _lib.GB_ERR_CAPACITY
+
+
 def test_time_of_impact_event_limit_reports_timeout(gpu):
     sc = scenes.drop(400, scenes.SplitMix64(11), allow_sleep=False)  # several events per step
     w = World(sc)
