@@ -2820,6 +2820,28 @@ gb_status SetBodyPropertyHost(HWorld& W, int bi, int prop, const float* v, Calls
     case GB_BODY_LINEAR_DAMPING: b.linDamp = v[0]; return GB_OK;
     case GB_BODY_ANGULAR_DAMPING: b.angDamp = v[0]; return GB_OK;
     case GB_BODY_GRAVITY_SCALE: b.gravScale = v[0]; return GB_OK;
+    case GB_BODY_MASS_DATA: {
+        // b2Body::SetMassData (Dynamics/b2Body.cpp:355-394): v = mass, center x, center y, inertia about
+        // the body origin; dynamic bodies only; the center of mass moves and its velocity follows
+        if (b.type != kDynamic) return GB_OK;
+        b.invMass = 0.0f;
+        b.I = 0.0f;
+        b.invI = 0.0f;
+        b.mass = v[0] <= 0.0f ? 1.0f : v[0];
+        b.invMass = 1.0f / b.mass;
+        const Vec2 center = V(v[1], v[2]);
+        if (v[3] > 0.0f && (b.flags & kBFixedRot) == 0) {
+            b.I = v[3] - b.mass * Dot(center, center);
+            b.invI = 1.0f / b.I;
+        }
+        const Vec2 oldCenter = b.sw.c;
+        b.sw.localCenter = center;
+        b.sw.c = Mul(b.xf, center);
+        b.sw.c0 = b.sw.c;
+        b.v = b.v + Cross(b.w, b.sw.c - oldCenter);
+        return GB_OK;
+    }
+    case GB_BODY_RESET_MASS_DATA: ResetMassData(W, bi); return GB_OK;
     default: return GB_ERR_INVALID;
     }
 }
@@ -3046,6 +3068,26 @@ gb_status gb_world_tree_stats(gb_world* g, int w, int* height, int* balance, flo
     if (height) *height = W.tree.Height();
     if (balance) *balance = W.tree.MaxBalance();
     if (quality) *quality = W.tree.AreaRatio();
+    return GB_OK;
+}
+
+gb_status gb_get_body_info(gb_world* g, int w, int body, float* out, int* flags)
+{
+    if (!g || w < 0 || w >= (int)g->worlds.size() || !out) return GB_ERR_INVALID;
+    const HWorld& W = g->worlds[w];
+    if (body < 0 || body >= (int)W.bodies.size() || !W.bodies[body].alive) return GB_ERR_INVALID;
+    // mass data, damping and flags other than awake change only on the host, so its copy is current
+    const HBody& b = W.bodies[body];
+    out[0] = b.mass;
+    out[1] = b.I + b.mass * Dot(b.sw.localCenter, b.sw.localCenter);  // b2Body::GetInertia (b2Body.h:546)
+    out[2] = b.sw.localCenter.x;
+    out[3] = b.sw.localCenter.y;
+    out[4] = b.linDamp;
+    out[5] = b.angDamp;
+    out[6] = b.gravScale;
+    if (flags)
+        *flags = b.type | ((b.flags & kBBullet) ? 4 : 0) | ((b.flags & kBFixedRot) ? 8 : 0) |
+                 ((b.flags & kBAutoSleep) ? 16 : 0) | ((b.flags & kBActive) ? 32 : 0);
     return GB_OK;
 }
 

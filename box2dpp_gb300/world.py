@@ -172,17 +172,29 @@ class World:
                    "gb_world_tree_stats")
         return h.value, b.value, np.float32(q.value)
 
-    def body_set(self, body: int, prop: int, value: float, w: int = 0) -> np.ndarray:
+    def body_set(self, body: int, prop: int, value=0.0, w: int = 0) -> np.ndarray:
         """b2Body::SetType (prop BODY_TYPE, value 0 static / 1 kinematic / 2 dynamic), SetActive,
         SetFixedRotation, SetBullet, SetSleepingAllowed (flags: value != 0), SetLinearDamping,
-        SetAngularDamping or SetGravityScale between steps; returns the EndContact calls of the
-        contacts it destroys as rows {2, fixtureA, fixtureB}."""
+        SetAngularDamping, SetGravityScale, SetMassData (value = mass, center x, center y, inertia)
+        or ResetMassData between steps; returns the EndContact calls of the contacts it destroys as
+        rows {2, fixtureA, fixtureB}."""
         calls = np.zeros((256, 3), dtype=np.int32)
         n = C.c_int()
-        v = np.array([value], dtype=np.float32)
+        v = np.zeros(4, dtype=np.float32)
+        vals = np.atleast_1d(np.asarray(value, dtype=np.float32))
+        v[:len(vals)] = vals
         _lib.check(self.lib.gb_body_set(self.h, int(w), int(body), int(prop), v, calls, 256, C.byref(n)),
                    "gb_body_set")
         return calls[:min(n.value, 256)]
+
+    def body_info(self, body: int, w: int = 0):
+        """(mass, inertia, local center x, y, linear damping, angular damping, gravity scale) as float32
+        and the flags (type | 4 bullet | 8 fixed rotation | 16 sleeping allowed | 32 active) of a body
+        (gb_get_body_info)."""
+        out = np.zeros(7, dtype=np.float32)
+        fl = C.c_int()
+        _lib.check(self.lib.gb_get_body_info(self.h, int(w), int(body), out, C.byref(fl)), "gb_get_body_info")
+        return out, fl.value
 
     def destroy_joint(self, joint: int, w: int = 0) -> np.ndarray:
         """b2World::DestroyJoint (no listener calls)."""

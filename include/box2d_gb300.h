@@ -181,7 +181,9 @@ gb_status gb_world_tree_stats(gb_world* world, int w, int* height, int* balance,
  * :456-499: proxies created in the fixture list's order, or destroyed with the contacts),
  * GB_BODY_FIXED_ROTATION (SetFixedRotation, :501-520), GB_BODY_BULLET, GB_BODY_SLEEPING_ALLOWED
  * (turning it off wakes the body), GB_BODY_LINEAR_DAMPING, GB_BODY_ANGULAR_DAMPING,
- * GB_BODY_GRAVITY_SCALE (v[0]; b2Body.h:593-682). calls (optional, cap records of 3 ints, *n_calls
+ * GB_BODY_GRAVITY_SCALE (v[0]; b2Body.h:593-682), GB_BODY_MASS_DATA (SetMassData, :355-394: v[0] mass,
+ * v[1..2] center, v[3] inertia about the body origin; dynamic bodies only), GB_BODY_RESET_MASS_DATA
+ * (ResetMassData, :283-353; v unused). calls (optional, cap records of 3 ints, *n_calls
  * the count) receives the EndContact calls {2, fixtureA, fixtureB} of the contacts it destroys. */
 #define GB_BODY_TYPE 0
 #define GB_BODY_ACTIVE 1
@@ -191,7 +193,15 @@ gb_status gb_world_tree_stats(gb_world* world, int w, int* height, int* balance,
 #define GB_BODY_LINEAR_DAMPING 5
 #define GB_BODY_ANGULAR_DAMPING 6
 #define GB_BODY_GRAVITY_SCALE 7
+#define GB_BODY_MASS_DATA 8
+#define GB_BODY_RESET_MASS_DATA 9
 gb_status gb_body_set(gb_world* world, int w, int body, int prop, const float* v, int* calls, int cap, int* n_calls);
+
+/* b2Body::GetMass, GetInertia (about the body origin), GetLocalCenter, GetLinearDamping,
+ * GetAngularDamping, GetGravityScale (Box2D/Dynamics/b2Body.h:227-260, 546-556, 593-682) into
+ * out[0..6]; *flags (optional) = GetType() | 4 IsBullet | 8 IsFixedRotation | 16 IsSleepingAllowed
+ * | 32 IsActive. None of these change during a step, so no device read is made. */
+gb_status gb_get_body_info(gb_world* world, int w, int body, float* out, int* flags);
 
 /* b2World::DestroyBody (Box2D/Dynamics/b2World.cpp:133), b2World::DestroyJoint (:274) and
  * b2Body::DestroyFixture (Box2D/Dynamics/b2Body.cpp:216), between steps, with the reference's order of

@@ -22,8 +22,9 @@
 //    QueryAABB callback that returns false ends the query; a RayCast callback's return value ignores
 //    the fixture (-1), ends the cast (0) or clips the ray (a fraction); the results of callbacks that
 //    do not depend on the order (closest hit, all hits) are the reference's;
-//  - b2Contact::GetWorldManifold computes on the host: bit-exact with the reference when the caller is
-//    compiled without floating-point contraction (-ffp-contract=off);
+//  - b2Contact::GetWorldManifold and the b2Body frame getters (GetWorldPoint, GetLocalPoint, ...)
+//    compute on the host: bit-exact with the reference when the caller is compiled without
+//    floating-point contraction (-ffp-contract=off);
 //  - b2ContactListener calls are recorded on the device during the step, in the reference's order.
 //    With a listener set, Step runs in two halves (gb_world_step_begin / gb_world_step_end): the
 //    collide phase's BeginContact, EndContact and PreSolve are made between them, and what PreSolve
@@ -62,6 +63,14 @@ struct b2Transform {
 };
 
 enum b2BodyType { b2_staticBody = 0, b2_kinematicBody = 1, b2_dynamicBody = 2 };
+
+// b2MassData (Box2D/Collision/Shapes/b2Shape.h:28-38): mass, centroid relative to the body origin,
+// rotational inertia about the body origin
+struct b2MassData {
+    float mass = 0.0f;
+    b2Vec2 center;
+    float I = 0.0f;
+};
 
 struct b2BodyDef {
     b2BodyType type = b2_staticBody;
@@ -289,6 +298,57 @@ public:
         return t;
     }
     bool IsAwake() const { return State()[11] != 0.0f; }
+    // frames (Box2D/Dynamics/b2Body.h:558-600), with the reference's operation order: b2Mul, b2MulT,
+    // b2Cross of the body's transform, center and velocities
+    b2Vec2 GetWorldPoint(const b2Vec2& local) const
+    {
+        const b2Transform t = GetTransform();
+        return b2Vec2((t.q.c * local.x - t.q.s * local.y) + t.p.x, (t.q.s * local.x + t.q.c * local.y) + t.p.y);
+    }
+    b2Vec2 GetWorldVector(const b2Vec2& local) const
+    {
+        const b2Transform t = GetTransform();
+        return b2Vec2(t.q.c * local.x - t.q.s * local.y, t.q.s * local.x + t.q.c * local.y);
+    }
+    b2Vec2 GetLocalPoint(const b2Vec2& world) const
+    {
+        const b2Transform t = GetTransform();
+        const float px = world.x - t.p.x, py = world.y - t.p.y;
+        return b2Vec2(t.q.c * px + t.q.s * py, -t.q.s * px + t.q.c * py);
+    }
+    b2Vec2 GetLocalVector(const b2Vec2& world) const
+    {
+        const b2Transform t = GetTransform();
+        return b2Vec2(t.q.c * world.x + t.q.s * world.y, -t.q.s * world.x + t.q.c * world.y);
+    }
+    b2Vec2 GetLinearVelocityFromWorldPoint(const b2Vec2& world) const
+    {
+        const b2Vec2 v = GetLinearVelocity(), c = GetWorldCenter();
+        const float w = GetAngularVelocity();
+        return b2Vec2(v.x + -w * (world.y - c.y), v.y + w * (world.x - c.x));
+    }
+    b2Vec2 GetLinearVelocityFromLocalPoint(const b2Vec2& local) const
+    {
+        return GetLinearVelocityFromWorldPoint(GetWorldPoint(local));
+    }
+    // mass data, damping and flags (Box2D/Dynamics/b2Body.h:227-260, 546-556, 593-682), read from the
+    // library's host copy (gb_get_body_info)
+    float GetMass() const { return Info(0); }
+    float GetInertia() const { return Info(1); }
+    const b2Vec2 GetLocalCenter() const { return b2Vec2(Info(2), Info(3)); }
+    void GetMassData(b2MassData* data) const
+    {
+        data->mass = Info(0);
+        data->I = Info(1);
+        data->center = b2Vec2(Info(2), Info(3));
+    }
+    float GetLinearDamping() const { return Info(4); }
+    float GetAngularDamping() const { return Info(5); }
+    float GetGravityScale() const { return Info(6); }
+    bool IsBullet() const { return (InfoFlags() & 4) != 0; }
+    bool IsFixedRotation() const { return (InfoFlags() & 8) != 0; }
+    bool IsSleepingAllowed() const { return (InfoFlags() & 16) != 0; }
+    bool IsActive() const { return (InfoFlags() & 32) != 0; }
     // State changes between steps (Box2D/Dynamics/b2Body.cpp:419, b2Body.h:501-830), each one
     // gb_body_edits record applied on the device in call order before the next Step, with the
     // reference's semantics (type checks, wakes, no accumulation on sleeping bodies).
@@ -312,10 +372,15 @@ public:
     void SetLinearDamping(float linearDamping);
     void SetAngularDamping(float angularDamping);
     void SetGravityScale(float scale);
+    // b2Body::SetMassData (Box2D/Dynamics/b2Body.cpp:355-394), ResetMassData (:283-353)
+    void SetMassData(const b2MassData* data);
+    void ResetMassData();
 
 private:
     friend class b2World;
     const float* State() const;
+    float Info(int k) const;
+    int InfoFlags() const;
     b2World* m_world = nullptr;
     int m_index = -1;
     b2BodyType m_type = b2_staticBody;
@@ -691,14 +756,15 @@ public:
         joint->m_alive = false;
     }
     // one gb_body_set call (b2Body::SetType, SetActive, ...); EndContact for the contacts it destroys
-    bool SetBodyProperty(b2Body* body, int prop, float value)
+    bool SetBodyProperty(b2Body* body, int prop, float value, float v1 = 0.0f, float v2 = 0.0f, float v3 = 0.0f)
     {
         if (!Handle() || !body || !body->m_alive || body->m_world != this) return false;
         if (m_listener) ReadContacts();  // the contacts an EndContact may name
         const int cap = GetContactCount() + 1;
         std::vector<int> calls(3 * (size_t)cap, 0);
         int n = 0;
-        const gb_status s = gb_body_set(m_h, 0, body->m_index, prop, &value, calls.data(), cap, &n);
+        const float v[4] = {value, v1, v2, v3};
+        const gb_status s = gb_body_set(m_h, 0, body->m_index, prop, v, calls.data(), cap, &n);
         m_stale = true;
         if (s != GB_OK) return false;
         calls.resize(3 * (size_t)std::min(n, cap));
@@ -977,6 +1043,13 @@ public:
     }
 
     // raw access used by b2Body
+    // a body's mass data, damping and flags (gb_get_body_info), for the b2Body getters
+    int BodyInfo(int index, float* out)
+    {
+        int flags = 0;
+        if (!Handle() || gb_get_body_info(m_h, 0, index, out, &flags) != GB_OK) return 0;
+        return flags;
+    }
     const float* BodyState(int index)
     {
         if (m_stale) {
@@ -1233,6 +1306,22 @@ inline void b2Body::SetSleepingAllowed(bool flag) { m_world->SetBodyProperty(thi
 inline void b2Body::SetLinearDamping(float d) { m_world->SetBodyProperty(this, GB_BODY_LINEAR_DAMPING, d); }
 inline void b2Body::SetAngularDamping(float d) { m_world->SetBodyProperty(this, GB_BODY_ANGULAR_DAMPING, d); }
 inline void b2Body::SetGravityScale(float scale) { m_world->SetBodyProperty(this, GB_BODY_GRAVITY_SCALE, scale); }
+inline void b2Body::SetMassData(const b2MassData* d)
+{
+    if (d) m_world->SetBodyProperty(this, GB_BODY_MASS_DATA, d->mass, d->center.x, d->center.y, d->I);
+}
+inline void b2Body::ResetMassData() { m_world->SetBodyProperty(this, GB_BODY_RESET_MASS_DATA, 0.0f); }
+inline float b2Body::Info(int k) const
+{
+    float out[7] = {0};
+    m_world->BodyInfo(m_index, out);
+    return out[k];
+}
+inline int b2Body::InfoFlags() const
+{
+    float out[7] = {0};
+    return m_world->BodyInfo(m_index, out);
+}
 
 inline void b2MouseJoint::SetTarget(const b2Vec2& target)
 {

@@ -93,6 +93,7 @@ def _declare(lib, p: str) -> None:
     sig["clear_forces"] = (None, [vp])
     sig["body_set"] = (None, [vp, C.c_int, C.c_int, _f32p])
     sig["tree_stats"] = (None, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_float)])
+    sig["body_info"] = (None, [vp, C.c_int, _f32p, C.POINTER(C.c_int)])
     for kind in ("body", "joint", "fixture"):
         sig["destroy_" + kind] = (C.c_int, [vp, C.c_int, _i32p, C.c_int])
     if p == "rw_":
@@ -203,6 +204,14 @@ class OracleWorld:
         self._fn("set_settings")(self.h, float(gravity[0]), float(gravity[1]), int(allow_sleep), int(warm_starting),
                                  int(continuous), int(sub_stepping), int(auto_clear_forces))
 
+    def body_info(self, body: int):
+        """(mass, inertia, local center x, y, linear damping, angular damping, gravity scale) and the
+        flags (type | 4 bullet | 8 fixed rotation | 16 sleeping allowed | 32 active) of a body."""
+        out = np.zeros(7, dtype=np.float32)
+        fl = C.c_int()
+        self._fn("body_info")(self.h, int(body), out, C.byref(fl))
+        return out, fl.value
+
     def tree_stats(self):
         """b2World::GetTreeHeight, GetTreeBalance and GetTreeQuality: (height, balance, quality)."""
         h, b, q = C.c_int(), C.c_int(), C.c_float()
@@ -213,13 +222,15 @@ class OracleWorld:
         """b2World::ClearForces."""
         self._fn("clear_forces")(self.h)
 
-    def body_set(self, body: int, prop: int, value: float):
+    def body_set(self, body: int, prop: int, value=0.0):
         """A b2Body property change between steps (prop: the C-ABI's GB_BODY_* code: 0 SetType,
         1 SetActive, 2 SetFixedRotation, 3 SetBullet, 4 SetSleepingAllowed, 5 SetLinearDamping,
-        6 SetAngularDamping, 7 SetGravityScale). Returns no listener calls (the reference driver's
-        EndContact calls go to its recorded events, when recording)."""
+        6 SetAngularDamping, 7 SetGravityScale, 8 SetMassData with value = (mass, center x, center y,
+        inertia), 9 ResetMassData). Returns no listener calls (the reference driver's EndContact calls
+        go to its recorded events, when recording)."""
         v = np.zeros(4, dtype=np.float32)
-        v[0] = value
+        vals = np.atleast_1d(np.asarray(value, dtype=np.float32))
+        v[:len(vals)] = vals
         self._fn("body_set")(self.h, int(body), int(prop), v)
         return np.zeros((0, 3), dtype=np.int32)
 

@@ -121,6 +121,20 @@ void po_body_set(void* h, int b, int prop, const float* v)
 {
     static_cast<World*>(h)->SetBodyProperty(b, prop, v);
 }
+// b2Body::GetMass, GetInertia, GetLocalCenter, damping, gravity scale and flags (b2Body.h:227-682)
+void po_body_info(void* h, int bi, float* out, int* flags)
+{
+    const Body& b = static_cast<World*>(h)->bodies[bi];
+    out[0] = b.mass;
+    out[1] = b.I + b.mass * Dot(b.sweep.localCenter, b.sweep.localCenter);
+    out[2] = b.sweep.localCenter.x;
+    out[3] = b.sweep.localCenter.y;
+    out[4] = b.linearDamping;
+    out[5] = b.angularDamping;
+    out[6] = b.gravityScale;
+    *flags = b.type | ((b.flags & kBBullet) ? 4 : 0) | ((b.flags & kBFixedRot) ? 8 : 0) |
+             ((b.flags & kBAutoSleep) ? 16 : 0) | ((b.flags & kBActive) ? 32 : 0);
+}
 // b2World::GetTreeHeight, GetTreeBalance, GetTreeQuality (b2World.cpp:1246-1259)
 void po_tree_stats(void* h, int* height, int* balance, float* quality)
 {

@@ -440,6 +440,26 @@ void World::SetBodyProperty(int bi, int prop, const float* v)
     case 5: b.linearDamping = v[0]; return;
     case 6: b.angularDamping = v[0]; return;
     case 7: b.gravityScale = v[0]; return;
+    case 8: {  // SetMassData (b2Body.cpp:355-394): v = mass, center x, center y, rotational inertia
+        if (b.type != kDynamic) return;
+        b.invMass = 0.0f;
+        b.I = 0.0f;
+        b.invI = 0.0f;
+        b.mass = v[0] <= 0.0f ? 1.0f : v[0];
+        b.invMass = 1.0f / b.mass;
+        const Vec2 center = V(v[1], v[2]);
+        if (v[3] > 0.0f && (b.flags & kBFixedRot) == 0) {
+            b.I = v[3] - b.mass * Dot(center, center);
+            b.invI = 1.0f / b.I;
+        }
+        const Vec2 oldCenter = b.sweep.c;
+        b.sweep.localCenter = center;
+        b.sweep.c = Mul(b.xf, center);
+        b.sweep.c0 = b.sweep.c;
+        b.v = b.v + Cross(b.w, b.sweep.c - oldCenter);
+        return;
+    }
+    case 9: ResetMassData(bi); return;  // b2Body::ResetMassData (b2Body.cpp:283-353)
     default: return;
     }
 }

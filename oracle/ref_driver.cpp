@@ -445,8 +445,30 @@ void rw_body_set(void* h, int b, int prop, const float* v)
     case 5: body->SetLinearDamping(v[0]); break;
     case 6: body->SetAngularDamping(v[0]); break;
     case 7: body->SetGravityScale(v[0]); break;
+    case 8: {
+        b2MassData md;
+        md.mass = v[0];
+        md.center.Set(v[1], v[2]);
+        md.I = v[3];
+        body->SetMassData(&md);
+        break;
+    }
+    case 9: body->ResetMassData(); break;
     default: break;
     }
+}
+void rw_body_info(void* h, int bi, float* out, int* flags)
+{
+    const b2Body* b = static_cast<RefWorld*>(h)->bodies[bi];
+    out[0] = b->GetMass();
+    out[1] = b->GetInertia();
+    out[2] = b->GetLocalCenter().x;
+    out[3] = b->GetLocalCenter().y;
+    out[4] = b->GetLinearDamping();
+    out[5] = b->GetAngularDamping();
+    out[6] = b->GetGravityScale();
+    *flags = (int)b->GetType() | (b->IsBullet() ? 4 : 0) | (b->IsFixedRotation() ? 8 : 0) |
+             (b->IsSleepingAllowed() ? 16 : 0) | (b->IsActive() ? 32 : 0);
 }
 void rw_tree_stats(void* h, int* height, int* balance, float* quality)
 {

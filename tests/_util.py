@@ -175,7 +175,8 @@ def body_props_script():
     """{step: [op]} applied before that step to scenes.destroy_mix: b2Body properties changed between
     steps. Op ("prop", body, prop, value): prop 0 SetType (0 static, 1 kinematic, 2 dynamic),
     1 SetActive, 2 SetFixedRotation, 3 SetBullet, 4 SetSleepingAllowed, 5 SetLinearDamping,
-    6 SetAngularDamping, 7 SetGravityScale."""
+    6 SetAngularDamping, 7 SetGravityScale, 8 SetMassData (value: mass, center x, center y, inertia
+    about the body origin), 9 ResetMassData."""
     return {
         30: [("prop", 12, 0, 0.0)],                              # a pyramid box turns static
         45: [("prop", 43, 1, 0.0)],                              # a chain link leaves the world
@@ -185,9 +186,12 @@ def body_props_script():
         100: [("prop", 37, 0, 2.0)],                             # the static ledge falls
         110: [("prop", 48, 0, 1.0)],                             # a tied circle turns kinematic
         120: [("prop", 51, 3, 1.0), ("prop", 52, 5, 3.0), ("prop", 53, 6, 2.0)],
+        130: [("prop", 47, 8, (3.0, 0.2, -0.1, 2.5))],            # user mass data, shifted center
         140: [("prop", 47, 2, 0.0), ("prop", 50, 7, 1.0)],
         160: [("prop", 30, 1, 0.0)],                             # a loaded pyramid box leaves
+        170: [("prop", 47, 9, 0.0), ("prop", 13, 8, (0.5, 0.0, 0.0, 0.0))],  # mass from fixtures; no inertia
         200: [("prop", 48, 0, 2.0), ("prop", 30, 1, 1.0)],
+        220: [("prop", 13, 9, 0.0)],
         250: [("prop", 5, 4, 0.0)],                              # one body may not sleep
         300: [("prop", 5, 4, 1.0)],
     }

@@ -1,8 +1,10 @@
 // b2Body property changes between steps through the C++ mirror of b2World (include/box2d_gb300.hpp):
 // a box pyramid, a pendulum on a revolute joint and a two-fixture body; a loaded box turns static and
 // back, an upper box is deactivated and activated again, and the pendulum, the two-fixture body and
-// other boxes get gravity scale, damping, fixed rotation, bullet and sleeping changes. Prints the
-// EndContact count after the first changes and at the end, and the body states as hex floats.
+// other boxes get gravity scale, damping, fixed rotation, bullet and sleeping changes, user mass data
+// and a mass reset. Prints the EndContact count after the first changes and at the end, the body
+// states as hex floats, the mass data, damping and flags of some bodies, and the pendulum bob's
+// frame conversions.
 #include <cstdio>
 #include <vector>
 
@@ -98,9 +100,31 @@ int main()
     bodies[9]->SetBullet(true);
     bodies[1]->SetSleepingAllowed(false);
     bob->SetAngularDamping(0.3f);
-    Step(world, 40);
+    b2MassData md;
+    md.mass = 3.0f;
+    md.center.Set(0.2f, -0.1f);
+    md.I = 2.5f;
+    bodies[5]->SetMassData(&md);
+    Step(world, 20);
+    bodies[6]->SetMassData(&md);
+    bodies[6]->ResetMassData();
+    Step(world, 20);
 
     std::printf("ends %d\n", listener.ends);
+    for (int i : {1, 2, 5, 6, 9, 11, 12}) {
+        b2Body* b = bodies[i];
+        const b2Vec2 lc = b->GetLocalCenter();
+        std::printf("info %d %a %a %a %a %a %a %a %d %d %d %d %d\n", i, b->GetMass(), b->GetInertia(), lc.x, lc.y,
+                    b->GetLinearDamping(), b->GetAngularDamping(), b->GetGravityScale(), (int)b->GetType(),
+                    b->IsBullet() ? 1 : 0, b->IsFixedRotation() ? 1 : 0, b->IsSleepingAllowed() ? 1 : 0,
+                    b->IsActive() ? 1 : 0);
+    }
+    const b2Vec2 wp = bob->GetWorldPoint(b2Vec2(0.5f, 0.25f)), wv = bob->GetWorldVector(b2Vec2(0.5f, 0.25f));
+    const b2Vec2 lp = bob->GetLocalPoint(b2Vec2(7.0f, 3.0f)), lv = bob->GetLocalVector(b2Vec2(7.0f, 3.0f));
+    const b2Vec2 vw = bob->GetLinearVelocityFromWorldPoint(b2Vec2(7.0f, 3.0f));
+    const b2Vec2 vl = bob->GetLinearVelocityFromLocalPoint(b2Vec2(0.5f, 0.25f));
+    std::printf("frames %a %a %a %a %a %a %a %a %a %a %a %a\n", wp.x, wp.y, wv.x, wv.y, lp.x, lp.y, lv.x, lv.y, vw.x,
+                vw.y, vl.x, vl.y);
     for (b2Body* b : bodies) {
         const b2Vec2 p = b->GetPosition(), v = b->GetLinearVelocity();
         std::printf("body %d %a %a %a %a %a %a\n", b->GetIndex(), p.x, p.y, b->GetAngle(), v.x, v.y,

@@ -419,7 +419,9 @@ def _compile_bp(tmp_path):
     lib = _lib.library_path()
     exe = str(tmp_path / "body_props")
     libdir = os.path.dirname(lib)
-    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "include"), BP_SRC, "-o", exe,
+    # without contraction: the frame getters run in the caller's code and are compared bit for bit
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
+           BP_SRC, "-o", exe,
            "-L", libdir, "-lbox2d_gb300", f"-Wl,-rpath,{libdir}"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
@@ -475,8 +477,37 @@ def test_cpp_body_props_match_oracle(gpu, tmp_path):
     prop(9, _lib.BODY_BULLET, 1.0)
     prop(1, _lib.BODY_SLEEPING_ALLOWED, 0.0)
     prop(11, _lib.BODY_ANGULAR_DAMPING, 0.3)
-    step(40)
+    prop(5, _lib.BODY_MASS_DATA, (3.0, 0.2, -0.1, 2.5))
+    step(20)
+    prop(6, _lib.BODY_MASS_DATA, (3.0, 0.2, -0.1, 2.5))
+    prop(6, _lib.BODY_RESET_MASS_DATA, 0.0)
+    step(20)
     assert int(out["ends"][0]) == ends and ends > 0
+    f32 = np.float32
+    for ln in r.stdout.strip().splitlines():
+        parts = ln.split()
+        if parts[0] != "info":
+            continue
+        i = int(parts[1])
+        got = np.array([float.fromhex(v) for v in parts[2:9]], dtype=np.float32)
+        want, fl = o.body_info(i)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (i, got, want)
+        flags = [int(x) for x in parts[9:14]]
+        assert flags == [fl & 3, (fl >> 2) & 1, (fl >> 3) & 1, (fl >> 4) & 1, (fl >> 5) & 1], (i, flags, fl)
+    # frame conversions of the bob (body 11) from its state, in the reference's operation order
+    s = o.bodies()[11]
+    px, py, cx, cy, vx, vy, w, sn, cs = s[0], s[1], s[3], s[4], s[5], s[6], s[7], s[8], s[9]
+    lx, ly, gx, gy = f32(0.5), f32(0.25), f32(7.0), f32(3.0)
+    wp = (f32(cs * lx - sn * ly) + px, f32(sn * lx + cs * ly) + py)
+    wv = (f32(cs * lx - sn * ly), f32(sn * lx + cs * ly))
+    qx, qy = f32(gx - px), f32(gy - py)
+    lp = (f32(cs * qx + sn * qy), f32(-sn * qx + cs * qy))
+    lv = (f32(cs * gx + sn * gy), f32(-sn * gx + cs * gy))
+    vw = (vx + f32(-w * f32(gy - cy)), vy + f32(w * f32(gx - cx)))
+    vl = (vx + f32(-w * f32(wp[1] - cy)), vy + f32(w * f32(wp[0] - cx)))
+    want = np.array([*wp, *wv, *lp, *lv, *vw, *vl], dtype=np.float32)
+    got = np.array([float.fromhex(v) for v in out["frames"]], dtype=np.float32)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (got, want)
     ob = o.bodies()
     assert len(bodies) == len(ob)
     for i, got in bodies.items():

@@ -1,6 +1,6 @@
 """b2Body properties changed between device steps (SetType to static, kinematic and dynamic, SetActive
 off and on, SetFixedRotation, SetBullet, SetSleepingAllowed, SetLinearDamping, SetAngularDamping,
-SetGravityScale): bit-exact against the reference's golden digests step by step with the reference's
+SetGravityScale, SetMassData, ResetMassData): bit-exact against the reference's golden digests step by step with the reference's
 final proxy ids; the EndContact calls of the contacts SetType and SetActive destroy as the CPU oracle
 makes them; and one world of a batch changed while the others step on."""
 from __future__ import annotations
@@ -29,6 +29,15 @@ def test_body_props_case_bit_exact_vs_reference(gpu):
     w.sync()
     ids, _ = w.proxies()
     assert np.array_equal(ids, g["proxy_ids"])
+    # mass data, damping and flags as the CPU restatement has them after the same script
+    o = oracle.OracleWorld(scenes.destroy_mix(scenes.SplitMix64(11)), "port", "project")
+    for s in range(1, int(g["steps"]) + 1):
+        if s in script:
+            apply_ops(o, script[s])
+        o.step(DT, VI, PI)
+    for b in range(w.n_bodies[0]):
+        (a, fa), (c, fc) = w.body_info(b), o.body_info(b)
+        assert fa == fc and np.array_equal(a.view(np.uint32), c.view(np.uint32)), (b, a, c)
 
 
 def test_body_props_end_contact_calls_match_oracle(gpu):

@@ -217,3 +217,28 @@ def test_port_tree_stats_match_reference(case):
     g = golden("tree_stats")
     w = oracle.OracleWorld(make(), "port", "project")
     assert tree_stats_mismatch(w, steps, script, g, name) is None
+
+
+def test_port_body_info_matches_reference():
+    """b2Body::GetMass, GetInertia, GetLocalCenter, the dampings, gravity scale and flags of every body
+    after the body-property script (SetMassData and ResetMassData included), restatement against the
+    reference."""
+    if not oracle.reference_available():
+        pytest.skip("reference tree not present")
+    from box2dpp_gb300 import scenes
+    from tests._util import apply_ops, body_props_script
+
+    sc = scenes.destroy_mix(scenes.SplitMix64(11))
+    p = oracle.OracleWorld(sc, "port", "project")
+    r = oracle.OracleWorld(sc, "reference", "project")
+    script = body_props_script()
+    for s in range(1, 241):
+        if s in script:
+            apply_ops(p, script[s])
+            apply_ops(r, script[s])
+        p.step()
+        r.step()
+        if s in (131, 171, 240):
+            for b in range(len(sc.bodies)):
+                (a, fa), (c, fc) = p.body_info(b), r.body_info(b)
+                assert fa == fc and np.array_equal(a.view(np.uint32), c.view(np.uint32)), (s, b, a, c)
