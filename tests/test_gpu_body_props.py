@@ -83,7 +83,7 @@ def test_body_props_in_one_world_of_a_batch(gpu):
 def test_body_set_rejects_bad_arguments(gpu):
     w = World(scenes.pyramid(3))
     with pytest.raises(GbError):
-        w.body_set(0, 9, 1.0)
+        w.body_set(0, 10, 1.0)
     with pytest.raises(GbError):
         w.body_set(0, 0, 5.0)
     with pytest.raises(GbError):
