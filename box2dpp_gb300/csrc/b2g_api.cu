@@ -2986,9 +2986,73 @@ bool LoadWorld(HWorld& W, const unsigned char* p, const unsigned char* end)
     return true;
 }
 
+// b2Fixture changes between steps on the host copy (prop: GB_FIXTURE_*): SetFriction, SetRestitution,
+// SetDensity (Dynamics/b2Fixture.h:300-340), SetSensor (b2Fixture.cpp:418-425: the body wakes on a
+// change), SetFilterData with Refilter (b2Fixture.cpp:181-214: the fixture's contacts are flagged for
+// filtering at the next collide phase and its proxies are queried again). A chain (its first child's
+// index) is one b2Fixture and changes with all of its children.
+gb_status SetFixturePropertyHost(HWorld& W, int f, int prop, const float* v)
+{
+    const int body = W.fixtures[f].body;
+    int last = f;
+    if (W.fixtures[f].shape.type == kEdge && W.fixtures[f].shape.chain == 1)
+        while (last + 1 < (int)W.fixtures.size() && W.fixtures[last + 1].body == body &&
+               W.fixtures[last + 1].shape.chain == 2)
+            ++last;
+    switch (prop) {
+    case GB_FIXTURE_FRICTION:
+        for (int k = f; k <= last; ++k) W.fixtures[k].friction = v[0];
+        return GB_OK;
+    case GB_FIXTURE_RESTITUTION:
+        for (int k = f; k <= last; ++k) W.fixtures[k].restitution = v[0];
+        return GB_OK;
+    case GB_FIXTURE_DENSITY:
+        if (!(v[0] >= 0.0f)) return GB_ERR_INVALID;  // b2Fixture::SetDensity asserts a valid density >= 0
+        for (int k = f; k <= last; ++k) W.fixtures[k].density = v[0];
+        return GB_OK;
+    case GB_FIXTURE_SENSOR: {
+        const int sensor = v[0] != 0.0f ? 1 : 0;
+        if (sensor == W.fixtures[f].sensor) return GB_OK;
+        WakeHost(W.bodies[body]);
+        for (int k = f; k <= last; ++k) W.fixtures[k].sensor = sensor;
+        return GB_OK;
+    }
+    case GB_FIXTURE_FILTER: {
+        for (int k = f; k <= last; ++k) {
+            W.fixtures[k].category = (int)v[0] & 0xFFFF;
+            W.fixtures[k].mask = (int)v[1] & 0xFFFF;
+            W.fixtures[k].group = (int16_t)(int)v[2];
+        }
+        if (W.hasState) {
+            HContacts& C = W.contacts;
+            for (int e = W.bodies[body].contactList; e != kNullIdx; e = NextContactEdge(W, e)) {
+                int4& ci = C.ci[e >> 1];
+                if ((ci.y >= f && ci.y <= last) || (ci.z >= f && ci.z <= last)) ci.x |= kCFilter;
+            }
+        }
+        for (int k = f; k <= last; ++k)
+            if (W.fixtures[k].proxyId != kNullIdx) W.moved[W.fixtures[k].proxyId] = 1;
+        return GB_OK;
+    }
+    default: return GB_ERR_INVALID;
+    }
+}
+
 } // namespace
 
 extern "C" {
+
+gb_status gb_fixture_set(gb_world* g, int w, int fixture, int prop, const float* v)
+{
+    if (!v) return GB_ERR_INVALID;
+    gb_status s = Mutable(g, w);
+    if (s != GB_OK) return s;
+    HWorld& W = g->worlds[w];
+    if (fixture < 0 || fixture >= (int)W.fixtures.size() || W.fixtures[fixture].body == kNullIdx) return GB_ERR_INVALID;
+    const Shape& sh = W.fixtures[fixture].shape;
+    if (sh.type == kEdge && sh.chain == 2) return GB_ERR_INVALID;  // a chain goes by its first child
+    return SetFixturePropertyHost(W, fixture, prop, v);
+}
 
 gb_status gb_world_checkpoint(gb_world* g, int w, void* buf, size_t cap, size_t* size)
 {

@@ -187,6 +187,15 @@ class World:
                    "gb_body_set")
         return calls[:min(n.value, 256)]
 
+    def fixture_set(self, fixture: int, prop: int, value=0.0, w: int = 0) -> np.ndarray:
+        """b2Fixture::SetFriction, SetRestitution, SetDensity, SetSensor or SetFilterData (value =
+        category, mask, group) between steps (gb_fixture_set); makes no listener calls."""
+        v = np.zeros(4, dtype=np.float32)
+        vals = np.atleast_1d(np.asarray(value, dtype=np.float32))
+        v[:len(vals)] = vals
+        _lib.check(self.lib.gb_fixture_set(self.h, int(w), int(fixture), int(prop), v), "gb_fixture_set")
+        return np.zeros((0, 3), dtype=np.int32)
+
     def body_info(self, body: int, w: int = 0):
         """(mass, inertia, local center x, y, linear damping, angular damping, gravity scale) as float32
         and the flags (type | 4 bullet | 8 fixed rotation | 16 sleeping allowed | 32 active) of a body

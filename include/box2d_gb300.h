@@ -197,6 +197,21 @@ gb_status gb_world_tree_stats(gb_world* world, int w, int* height, int* balance,
 #define GB_BODY_RESET_MASS_DATA 9
 gb_status gb_body_set(gb_world* world, int w, int body, int prop, const float* v, int* calls, int cap, int* n_calls);
 
+/* b2Fixture changes between steps (no step in progress): prop GB_FIXTURE_FRICTION, GB_FIXTURE_RESTITUTION
+ * (v[0]; b2Fixture::SetFriction, SetRestitution, Box2D/Dynamics/b2Fixture.h:300-340: new contacts mix
+ * the new value, existing ones keep theirs, as in the reference), GB_FIXTURE_DENSITY (v[0] >= 0;
+ * SetDensity: the body's mass follows at its next mass reset), GB_FIXTURE_SENSOR (v[0] != 0;
+ * SetSensor, b2Fixture.cpp:418-425: a change wakes the body), GB_FIXTURE_FILTER (v[0] category,
+ * v[1] mask, v[2] group; SetFilterData, b2Fixture.cpp:181-214: the fixture's contacts are filtered
+ * again at the next step and its proxies look for new pairs). A chain is addressed by its first
+ * child's index and changes as a whole. */
+#define GB_FIXTURE_FRICTION 0
+#define GB_FIXTURE_RESTITUTION 1
+#define GB_FIXTURE_DENSITY 2
+#define GB_FIXTURE_SENSOR 3
+#define GB_FIXTURE_FILTER 4
+gb_status gb_fixture_set(gb_world* world, int w, int fixture, int prop, const float* v);
+
 /* b2Body::GetMass, GetInertia (about the body origin), GetLocalCenter, GetLinearDamping,
  * GetAngularDamping, GetGravityScale (Box2D/Dynamics/b2Body.h:227-260, 546-556, 593-682) into
  * out[0..6]; *flags (optional) = GetType() | 4 IsBullet | 8 IsFixedRotation | 16 IsSleepingAllowed

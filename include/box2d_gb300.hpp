@@ -253,6 +253,15 @@ public:
     b2Shape::Type GetType() const { return m_type; }
     float GetRadius() const { return m_radius; }  // the shape's m_radius
     const b2Filter& GetFilterData() const { return m_def.filter; }
+    // changes between steps (Box2D/Dynamics/b2Fixture.h:300-340, b2Fixture.cpp:181-214, 418-425), each a
+    // gb_fixture_set call: friction and restitution reach new contacts, density the next mass reset,
+    // a sensor change wakes the body, new filter data filters the fixture's contacts again
+    void SetFriction(float friction);
+    void SetRestitution(float restitution);
+    void SetDensity(float density);
+    void SetSensor(bool sensor);
+    void SetFilterData(const b2Filter& filter);
+    void Refilter() { SetFilterData(m_def.filter); }
 
 private:
     friend class b2World;
@@ -754,6 +763,14 @@ public:
         std::vector<int> calls;
         if (Destroy(gb_destroy_joint, joint->m_index, calls) != GB_OK) return;
         joint->m_alive = false;
+    }
+    // one gb_fixture_set call (b2Fixture::SetFriction, ...)
+    bool SetFixtureProperty(b2Fixture* f, int prop, float v0, float v1 = 0.0f, float v2 = 0.0f)
+    {
+        if (!Handle() || !f || !f->m_alive) return false;
+        const float v[4] = {v0, v1, v2, 0.0f};
+        m_stale = true;
+        return gb_fixture_set(m_h, 0, f->m_index, prop, v) == GB_OK;
     }
     // one gb_body_set call (b2Body::SetType, SetActive, ...); EndContact for the contacts it destroys
     bool SetBodyProperty(b2Body* body, int prop, float value, float v1 = 0.0f, float v2 = 0.0f, float v3 = 0.0f)
@@ -1306,6 +1323,28 @@ inline void b2Body::SetSleepingAllowed(bool flag) { m_world->SetBodyProperty(thi
 inline void b2Body::SetLinearDamping(float d) { m_world->SetBodyProperty(this, GB_BODY_LINEAR_DAMPING, d); }
 inline void b2Body::SetAngularDamping(float d) { m_world->SetBodyProperty(this, GB_BODY_ANGULAR_DAMPING, d); }
 inline void b2Body::SetGravityScale(float scale) { m_world->SetBodyProperty(this, GB_BODY_GRAVITY_SCALE, scale); }
+inline void b2Fixture::SetFriction(float friction)
+{
+    if (m_body->GetWorld()->SetFixtureProperty(this, GB_FIXTURE_FRICTION, friction)) m_def.friction = friction;
+}
+inline void b2Fixture::SetRestitution(float restitution)
+{
+    if (m_body->GetWorld()->SetFixtureProperty(this, GB_FIXTURE_RESTITUTION, restitution)) m_def.restitution = restitution;
+}
+inline void b2Fixture::SetDensity(float density)
+{
+    if (m_body->GetWorld()->SetFixtureProperty(this, GB_FIXTURE_DENSITY, density)) m_def.density = density;
+}
+inline void b2Fixture::SetSensor(bool sensor)
+{
+    if (m_body->GetWorld()->SetFixtureProperty(this, GB_FIXTURE_SENSOR, sensor ? 1.0f : 0.0f)) m_def.isSensor = sensor;
+}
+inline void b2Fixture::SetFilterData(const b2Filter& filter)
+{
+    if (m_body->GetWorld()->SetFixtureProperty(this, GB_FIXTURE_FILTER, (float)filter.categoryBits,
+                                               (float)filter.maskBits, (float)filter.groupIndex))
+        m_def.filter = filter;
+}
 inline void b2Body::SetMassData(const b2MassData* d)
 {
     if (d) m_world->SetBodyProperty(this, GB_BODY_MASS_DATA, d->mass, d->center.x, d->center.y, d->I);

@@ -94,6 +94,7 @@ def _declare(lib, p: str) -> None:
     sig["body_set"] = (None, [vp, C.c_int, C.c_int, _f32p])
     sig["tree_stats"] = (None, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_float)])
     sig["body_info"] = (None, [vp, C.c_int, _f32p, C.POINTER(C.c_int)])
+    sig["fixture_set"] = (None, [vp, C.c_int, C.c_int, _f32p])
     for kind in ("body", "joint", "fixture"):
         sig["destroy_" + kind] = (C.c_int, [vp, C.c_int, _i32p, C.c_int])
     if p == "rw_":
@@ -203,6 +204,15 @@ class OracleWorld:
         and SetAutoClearForces between steps."""
         self._fn("set_settings")(self.h, float(gravity[0]), float(gravity[1]), int(allow_sleep), int(warm_starting),
                                  int(continuous), int(sub_stepping), int(auto_clear_forces))
+
+    def fixture_set(self, fixture: int, prop: int, value=0.0):
+        """A b2Fixture change between steps (prop: 0 SetFriction, 1 SetRestitution, 2 SetDensity,
+        3 SetSensor, 4 SetFilterData with value = (category, mask, group))."""
+        v = np.zeros(4, dtype=np.float32)
+        vals = np.atleast_1d(np.asarray(value, dtype=np.float32))
+        v[:len(vals)] = vals
+        self._fn("fixture_set")(self.h, int(fixture), int(prop), v)
+        return np.zeros((0, 3), dtype=np.int32)
 
     def body_info(self, body: int):
         """(mass, inertia, local center x, y, linear damping, angular damping, gravity scale) and the

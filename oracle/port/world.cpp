@@ -464,6 +464,46 @@ void World::SetBodyProperty(int bi, int prop, const float* v)
     }
 }
 
+// b2Fixture changes between steps (prop: the C-ABI's GB_FIXTURE_*): SetFriction, SetRestitution,
+// SetDensity (b2Fixture.h:300-340), SetSensor (b2Fixture.cpp:418-425, wakes the body on a change),
+// SetFilterData with Refilter (b2Fixture.cpp:181-214: the fixture's contacts flagged for filtering,
+// its proxies touched). A chain (its first child's index) changes with all of its children.
+void World::SetFixtureProperty(int f, int prop, const float* v)
+{
+    int last = f;
+    const int body = fixtures[f].body;
+    if (fixtures[f].shape.chain == 1)
+        while (last + 1 < (int)fixtures.size() && fixtures[last + 1].body == body && fixtures[last + 1].shape.chain == 2)
+            ++last;
+    switch (prop) {
+    case 0: for (int k = f; k <= last; ++k) fixtures[k].friction = v[0]; return;
+    case 1: for (int k = f; k <= last; ++k) fixtures[k].restitution = v[0]; return;
+    case 2: for (int k = f; k <= last; ++k) fixtures[k].density = v[0]; return;
+    case 3: {
+        const bool sensor = v[0] != 0.0f;
+        if (sensor == fixtures[f].sensor) return;
+        SetAwake(body, true);
+        for (int k = f; k <= last; ++k) fixtures[k].sensor = sensor;
+        return;
+    }
+    case 4: {
+        for (int k = f; k <= last; ++k) {
+            fixtures[k].category = (uint16_t)(int)v[0];
+            fixtures[k].mask = (uint16_t)(int)v[1];
+            fixtures[k].group = (int16_t)(int)v[2];
+        }
+        for (int e = bodies[body].contactList; e != kNull; e = contacts[e >> 1].eNext[e & 1]) {
+            Contact& c = contacts[e >> 1];
+            if ((c.fA >= f && c.fA <= last) || (c.fB >= f && c.fB <= last)) c.flags |= kCFilter;
+        }
+        for (int k = f; k <= last; ++k)
+            if (fixtures[k].proxyCount > 0) bp.TouchProxy(fixtures[k].proxyId);
+        return;
+    }
+    default: return;
+    }
+}
+
 // b2Body state changes between steps: SetTransform (Dynamics/b2Body.cpp:419-441), SetLinearVelocity,
 // SetAngularVelocity (b2Body.h:501-530), SetAwake (b2Body.h:635-655), ApplyForce, ApplyForceToCenter,
 // ApplyTorque, ApplyLinearImpulse, ApplyAngularImpulse (b2Body.h:739-830). op: the C-ABI's GB_EDIT_*.

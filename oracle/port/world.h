@@ -168,6 +168,7 @@ struct World {
     void ApplyEdit(int op, int b, int wake, const float* v);
     // b2Body property changes between steps (the C-ABI's GB_BODY_* prop codes)
     void SetBodyProperty(int b, int prop, const float* v);
+    void SetFixtureProperty(int f, int prop, const float* v);
     void SynchronizeTransform(int b);
     void Advance(int b, float alpha);
 

@@ -457,6 +457,25 @@ void rw_body_set(void* h, int b, int prop, const float* v)
     default: break;
     }
 }
+void rw_fixture_set(void* h, int f, int prop, const float* v)
+{
+    b2Fixture* fx = static_cast<RefWorld*>(h)->fixtures[f];
+    switch (prop) {
+    case 0: fx->SetFriction(v[0]); break;
+    case 1: fx->SetRestitution(v[0]); break;
+    case 2: fx->SetDensity(v[0]); break;
+    case 3: fx->SetSensor(v[0] != 0.0f); break;
+    case 4: {
+        b2Filter filter;
+        filter.categoryBits = (uint16)(int)v[0];
+        filter.maskBits = (uint16)(int)v[1];
+        filter.groupIndex = (int16)(int)v[2];
+        fx->SetFilterData(filter);
+        break;
+    }
+    default: break;
+    }
+}
 void rw_body_info(void* h, int bi, float* out, int* flags)
 {
     const b2Body* b = static_cast<RefWorld*>(h)->bodies[bi];

@@ -197,8 +197,26 @@ def body_props_script():
     }
 
 
+def fixture_props_script():
+    """{step: [op]} applied before that step to scenes.destroy_mix: b2Fixture properties changed between
+    steps. Op ("fix", fixture, prop, value): prop 0 SetFriction, 1 SetRestitution, 2 SetDensity,
+    3 SetSensor, 4 SetFilterData (value: category, mask, group). Fixtures: 1..36 the pyramid's boxes,
+    47 and 48 the two-fixture body's box and circle, 49 and 50 the tied pair, 51.. the drop."""
+    return {
+        30: [("fix", 9, 3, 1.0)],                                   # a loaded box becomes a sensor
+        34: [("fix", 9, 3, 0.0)],                                   # solid again, sunk into the pile
+        50: [("fix", 20, 0, 0.0), ("fix", 51, 1, 0.8)],              # no friction; a bouncy circle
+        60: [("fix", 52, 4, (1.0, 0xFFFF, -5.0)), ("fix", 53, 4, (1.0, 0xFFFF, -5.0))],  # a group
+        80: [("fix", 47, 2, 5.0), ("prop", 47, 9, 0.0)],             # density, then the mass reset
+        90: [("fix", 30, 4, (2.0, 0xFFFE, 0.0))],                    # a box no longer meets category 1
+        94: [("fix", 30, 4, (1.0, 0xFFFF, 0.0))],                    # and meets it again, overlapping
+        150: [("fix", 52, 4, (1.0, 0xFFFF, 0.0))],
+        200: [("fix", 48, 3, 1.0), ("fix", 49, 0, 0.9)],
+    }
+
+
 def apply_ops(world, ops, w: int = 0):
-    """Applies destroy_script(), settings_script() and body_props_script() ops to an oracle world or a device world (same
+    """Applies destroy_script(), settings_script(), body_props_script() and fixture_props_script() ops to an oracle world or a device world (same
     method names); returns the destruction listener's calls of the ops as (kind, index), in order."""
     calls = []
     for op in ops:
@@ -207,6 +225,8 @@ def apply_ops(world, ops, w: int = 0):
             world.set_settings(*args) if w == 0 else world.set_settings(*args, w=w)
         elif op[0] == "clear_forces":
             world.clear_forces() if w == 0 else world.clear_forces(w)
+        elif op[0] == "fix":
+            world.fixture_set(op[1], op[2], op[3]) if w == 0 else world.fixture_set(op[1], op[2], op[3], w)
         elif op[0] == "prop":
             # a device world also returns the EndContact calls, which the oracles record with their
             # other events

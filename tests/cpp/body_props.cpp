@@ -2,7 +2,7 @@
 // a box pyramid, a pendulum on a revolute joint and a two-fixture body; a loaded box turns static and
 // back, an upper box is deactivated and activated again, and the pendulum, the two-fixture body and
 // other boxes get gravity scale, damping, fixed rotation, bullet and sleeping changes, user mass data
-// and a mass reset. Prints the EndContact count after the first changes and at the end, the body
+// and a mass reset; box fixtures get friction, restitution, sensor and filter-group changes. Prints the EndContact count after the first changes and at the end, the body
 // states as hex floats, the mass data, damping and flags of some bodies, and the pendulum bob's
 // frame conversions.
 #include <cstdio>
@@ -28,6 +28,7 @@ int main()
     Listener listener;
     world.SetContactListener(&listener);
     std::vector<b2Body*> bodies;
+    std::vector<b2Fixture*> boxFixtures(1, nullptr);  // the boxes' fixtures, by body index
 
     b2BodyDef gd;
     b2Body* ground = world.CreateBody(&gd);
@@ -50,7 +51,7 @@ int main()
             fd.shape = &box;
             fd.density = 5.0f;
             fd.friction = 0.6f;
-            b->CreateFixture(&fd);
+            boxFixtures.push_back(b->CreateFixture(&fd));
             bodies.push_back(b);
         }
     b2BodyDef ad;
@@ -92,10 +93,19 @@ int main()
     bodies[8]->SetActive(false);
     bob->SetGravityScale(0.5f);
     bob->SetLinearDamping(0.5f);
+    boxFixtures[4]->SetFriction(0.0f);
+    boxFixtures[3]->SetRestitution(0.5f);
+    boxFixtures[7]->SetSensor(true);
+    b2Filter group;
+    group.groupIndex = -3;
+    boxFixtures[8]->SetFilterData(group);
+    boxFixtures[9]->SetFilterData(group);
     std::printf("ends_after_first %d type %d\n", listener.ends, (int)bodies[2]->GetType());
     Step(world, 20);
     bodies[8]->SetActive(true);
     bodies[2]->SetType(b2_dynamicBody);
+    boxFixtures[7]->SetSensor(false);
+    boxFixtures[9]->Refilter();
     two->SetFixedRotation(true);
     bodies[9]->SetBullet(true);
     bodies[1]->SetSleepingAllowed(false);

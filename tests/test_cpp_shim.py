@@ -468,11 +468,18 @@ def test_cpp_body_props_match_oracle(gpu, tmp_path):
     prop(8, _lib.BODY_ACTIVE, 0.0)
     prop(11, _lib.BODY_GRAVITY_SCALE, 0.5)
     prop(11, _lib.BODY_LINEAR_DAMPING, 0.5)
+    o.fixture_set(4, _lib.FIXTURE_FRICTION, 0.0)
+    o.fixture_set(3, _lib.FIXTURE_RESTITUTION, 0.5)
+    o.fixture_set(7, _lib.FIXTURE_SENSOR, 1.0)
+    o.fixture_set(8, _lib.FIXTURE_FILTER, (1.0, 0xFFFF, -3.0))
+    o.fixture_set(9, _lib.FIXTURE_FILTER, (1.0, 0xFFFF, -3.0))
     first = out["ends_after_first"]  # "<count> type <type of the box>"
     assert [int(first[0]), int(first[2])] == [ends, 0]
     step(20)
     prop(8, _lib.BODY_ACTIVE, 1.0)
     prop(2, _lib.BODY_TYPE, 2.0)
+    o.fixture_set(7, _lib.FIXTURE_SENSOR, 0.0)
+    o.fixture_set(9, _lib.FIXTURE_FILTER, (1.0, 0xFFFF, -3.0))
     prop(12, _lib.BODY_FIXED_ROTATION, 1.0)
     prop(9, _lib.BODY_BULLET, 1.0)
     prop(1, _lib.BODY_SLEEPING_ALLOWED, 0.0)

@@ -1,6 +1,7 @@
 """b2Body properties changed between device steps (SetType to static, kinematic and dynamic, SetActive
 off and on, SetFixedRotation, SetBullet, SetSleepingAllowed, SetLinearDamping, SetAngularDamping,
-SetGravityScale, SetMassData, ResetMassData): bit-exact against the reference's golden digests step by step with the reference's
+SetGravityScale, SetMassData, ResetMassData) and fixture properties (SetSensor, SetFriction,
+SetRestitution, SetFilterData, SetDensity): bit-exact against the reference's golden digests step by step with the reference's
 final proxy ids; the EndContact calls of the contacts SetType and SetActive destroy as the CPU oracle
 makes them; and one world of a batch changed while the others step on."""
 from __future__ import annotations
@@ -12,7 +13,7 @@ import oracle
 from box2dpp_gb300 import scenes
 from box2dpp_gb300._lib import GbError
 from box2dpp_gb300.world import World
-from tests._util import DT, PI, VI, apply_ops, body_props_script, digest, golden
+from tests._util import DT, PI, VI, apply_ops, body_props_script, digest, fixture_props_script, golden
 
 pytestmark = pytest.mark.gpu
 
@@ -38,6 +39,20 @@ def test_body_props_case_bit_exact_vs_reference(gpu):
     for b in range(w.n_bodies[0]):
         (a, fa), (c, fc) = w.body_info(b), o.body_info(b)
         assert fa == fc and np.array_equal(a.view(np.uint32), c.view(np.uint32)), (b, a, c)
+
+
+def test_fixture_props_case_bit_exact_vs_reference(gpu):
+    g = golden("fixture_props_project")
+    w = World(scenes.destroy_mix(scenes.SplitMix64(13)))
+    script = fixture_props_script()
+    for s in range(1, int(g["steps"]) + 1):
+        if s in script:
+            apply_ops(w, script[s])
+        w.step(DT, VI, PI)
+        assert np.array_equal(digest(w.bodies(), *w.contacts()), g["digests"][s - 1]), f"first divergence at step {s}"
+    w.sync()
+    ids, _ = w.proxies()
+    assert np.array_equal(ids, g["proxy_ids"])
 
 
 def test_body_props_end_contact_calls_match_oracle(gpu):
@@ -88,3 +103,7 @@ def test_body_set_rejects_bad_arguments(gpu):
         w.body_set(0, 0, 5.0)
     with pytest.raises(GbError):
         w.body_set(10_000, 3, 1.0)
+    with pytest.raises(GbError):
+        w.fixture_set(1, 5, 0.0)
+    with pytest.raises(GbError):
+        w.fixture_set(1, 2, -1.0)  # negative density

@@ -185,6 +185,31 @@ def test_port_body_props_case_matches_reference(trig):
 
 
 @pytest.mark.parametrize("trig", ["project", "libm"])
+def test_port_fixture_props_case_matches_reference(trig):
+    """b2Fixture changes between steps (SetSensor on and off inside a pile, SetFriction,
+    SetRestitution, SetFilterData groups and categories with the refiltering of existing contacts,
+    SetDensity with a mass reset): per-step state and final proxy ids as the reference."""
+    import platform
+
+    from box2dpp_gb300 import scenes
+    from tests._util import apply_ops, digest, fixture_props_script
+
+    g = golden(f"fixture_props_{trig}")
+    w = oracle.OracleWorld(scenes.destroy_mix(scenes.SplitMix64(13)), "port", trig)
+    script = fixture_props_script()
+    for s in range(1, int(g["steps"]) + 1):
+        if s in script:
+            apply_ops(w, script[s])
+        w.step()
+        if not np.array_equal(digest(w.bodies(), *w.contacts()), g["digests"][s - 1]):
+            if trig == "libm" and platform.machine() != "x86_64":
+                pytest.skip("libm trig differs on this machine")
+            raise AssertionError(f"first divergence at step {s}")
+    ids, _ = w.proxies()
+    assert np.array_equal(ids, g["proxy_ids"])
+
+
+@pytest.mark.parametrize("trig", ["project", "libm"])
 def test_port_settings_case_matches_reference(trig):
     """b2World settings changed between steps (gravity, sleep off and on, warm starting, continuous
     collision, sub-stepping, forces kept across steps and cleared): per-step state as the reference."""
