@@ -3042,6 +3042,33 @@ gb_status SetFixturePropertyHost(HWorld& W, int f, int prop, const float* v)
 
 extern "C" {
 
+gb_status gb_world_shift_origin(gb_world* g, int w, float x, float y)
+{
+    gb_status s = Mutable(g, w);
+    if (s != GB_OK) return s;
+    HWorld& W = g->worlds[w];
+    // b2World::ShiftOrigin (Dynamics/b2World.cpp:1261-1282)
+    const Vec2 o = V(x, y);
+    for (int b = W.bodyList; b != kNullIdx; b = W.bodies[b].next) {
+        HBody& hb = W.bodies[b];
+        hb.xf.p = hb.xf.p - o;
+        hb.sw.c0 = hb.sw.c0 - o;
+        hb.sw.c = hb.sw.c - o;
+    }
+    for (Joint& j : W.joints) {
+        if (j.type == kJointMouse) j.target = j.target - o;  // b2MouseJoint::ShiftOrigin (b2MouseJoint.cpp:222)
+        if (j.type == kJointPulley) {                        // b2PulleyJoint::ShiftOrigin (b2PulleyJoint.cpp:347)
+            j.groundAnchorA = j.groundAnchorA - o;
+            j.groundAnchorB = j.groundAnchorB - o;
+        }
+    }
+    // b2BroadPhase::ShiftOrigin: the tree's boxes (the proxies' fat boxes; the fixtures' own boxes are
+    // left as the reference leaves them)
+    for (float4& f : W.fat) f = make_float4(f.x - x, f.y - y, f.z - x, f.w - y);
+    if (W.trackTree) W.tree.ShiftOrigin(x, y);
+    return GB_OK;
+}
+
 gb_status gb_fixture_set(gb_world* g, int w, int fixture, int prop, const float* v)
 {
     if (!v) return GB_ERR_INVALID;

@@ -68,6 +68,17 @@ public:
         return sum / rootP;
     }
 
+    // b2DynamicTree::ShiftOrigin (:773-781): every node box of the pool moves by -origin
+    void ShiftOrigin(float x, float y)
+    {
+        for (Node& n : nodes_) {
+            n.box.x = n.box.x - x;
+            n.box.y = n.box.y - y;
+            n.box.z = n.box.z - x;
+            n.box.w = n.box.w - y;
+        }
+    }
+
     // the whole tree as bytes (world checkpoints) and back; Load returns false on malformed input
     void Save(std::vector<unsigned char>& out) const
     {

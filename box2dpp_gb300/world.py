@@ -187,6 +187,10 @@ class World:
                    "gb_body_set")
         return calls[:min(n.value, 256)]
 
+    def shift_origin(self, x: float, y: float, w: int = 0) -> None:
+        """b2World::ShiftOrigin(b2Vec2(x, y)) of world w between steps."""
+        _lib.check(self.lib.gb_world_shift_origin(self.h, int(w), float(x), float(y)), "gb_world_shift_origin")
+
     def fixture_set(self, fixture: int, prop: int, value=0.0, w: int = 0) -> np.ndarray:
         """b2Fixture::SetFriction, SetRestitution, SetDensity, SetSensor or SetFilterData (value =
         category, mask, group) between steps (gb_fixture_set); makes no listener calls."""

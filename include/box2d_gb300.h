@@ -197,6 +197,10 @@ gb_status gb_world_tree_stats(gb_world* world, int w, int* height, int* balance,
 #define GB_BODY_RESET_MASS_DATA 9
 gb_status gb_body_set(gb_world* world, int w, int body, int prop, const float* v, int* calls, int cap, int* n_calls);
 
+/* b2World::ShiftOrigin (Box2D/Dynamics/b2World.cpp:1261-1282) of world w between steps: bodies, the
+ * mouse joints' targets, the pulleys' ground anchors and the broadphase's boxes move by -(x, y). */
+gb_status gb_world_shift_origin(gb_world* world, int w, float x, float y);
+
 /* b2Fixture changes between steps (no step in progress): prop GB_FIXTURE_FRICTION, GB_FIXTURE_RESTITUTION
  * (v[0]; b2Fixture::SetFriction, SetRestitution, Box2D/Dynamics/b2Fixture.h:300-340: new contacts mix
  * the new value, existing ones keep theirs, as in the reference), GB_FIXTURE_DENSITY (v[0] >= 0;

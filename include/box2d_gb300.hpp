@@ -764,6 +764,13 @@ public:
         if (Destroy(gb_destroy_joint, joint->m_index, calls) != GB_OK) return;
         joint->m_alive = false;
     }
+    // b2World::ShiftOrigin (Box2D/Dynamics/b2World.cpp:1261-1282)
+    void ShiftOrigin(const b2Vec2& newOrigin)
+    {
+        if (!Handle()) return;
+        gb_world_shift_origin(m_h, 0, newOrigin.x, newOrigin.y);
+        m_stale = true;
+    }
     // one gb_fixture_set call (b2Fixture::SetFriction, ...)
     bool SetFixtureProperty(b2Fixture* f, int prop, float v0, float v1 = 0.0f, float v2 = 0.0f)
     {

@@ -95,6 +95,7 @@ def _declare(lib, p: str) -> None:
     sig["tree_stats"] = (None, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_float)])
     sig["body_info"] = (None, [vp, C.c_int, _f32p, C.POINTER(C.c_int)])
     sig["fixture_set"] = (None, [vp, C.c_int, C.c_int, _f32p])
+    sig["shift_origin"] = (None, [vp, C.c_float, C.c_float])
     for kind in ("body", "joint", "fixture"):
         sig["destroy_" + kind] = (C.c_int, [vp, C.c_int, _i32p, C.c_int])
     if p == "rw_":
@@ -204,6 +205,10 @@ class OracleWorld:
         and SetAutoClearForces between steps."""
         self._fn("set_settings")(self.h, float(gravity[0]), float(gravity[1]), int(allow_sleep), int(warm_starting),
                                  int(continuous), int(sub_stepping), int(auto_clear_forces))
+
+    def shift_origin(self, x: float, y: float) -> None:
+        """b2World::ShiftOrigin(b2Vec2(x, y))."""
+        self._fn("shift_origin")(self.h, float(x), float(y))
 
     def fixture_set(self, fixture: int, prop: int, value=0.0):
         """A b2Fixture change between steps (prop: 0 SetFriction, 1 SetRestitution, 2 SetDensity,

@@ -117,6 +117,10 @@ void po_set_settings(void* h, float gx, float gy, int allowSleep, int warm, int 
     if (autoClear) w->wflags |= 0x4u;
     else w->wflags &= ~0x4u;
 }
+void po_shift_origin(void* h, float x, float y)
+{
+    static_cast<World*>(h)->ShiftOrigin(V(x, y));
+}
 void po_fixture_set(void* h, int f, int prop, const float* v)
 {
     static_cast<World*>(h)->SetFixtureProperty(f, prop, v);

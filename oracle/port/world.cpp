@@ -464,6 +464,30 @@ void World::SetBodyProperty(int bi, int prop, const float* v)
     }
 }
 
+// b2World::ShiftOrigin (b2World.cpp:1261-1282): body transforms and sweep centres, the mouse joint's
+// target and the pulley's ground anchors (b2MouseJoint.cpp:222, b2PulleyJoint.cpp:347), and every
+// node box of the broadphase tree (b2DynamicTree.cpp:773-781) move by -origin.
+void World::ShiftOrigin(Vec2 o)
+{
+    for (int b = bodyList; b != kNull; b = bodies[b].next) {
+        Body& x = bodies[b];
+        x.xf.p = x.xf.p - o;
+        x.sweep.c0 = x.sweep.c0 - o;
+        x.sweep.c = x.sweep.c - o;
+    }
+    for (Joint& j : joints) {
+        if (j.type == kMouseJoint) j.target = j.target - o;
+        if (j.type == kPulleyJoint) {
+            j.groundAnchorA = j.groundAnchorA - o;
+            j.groundAnchorB = j.groundAnchorB - o;
+        }
+    }
+    for (TreeNode& n : bp.tree.nodes) {
+        n.aabb.lo = n.aabb.lo - o;
+        n.aabb.hi = n.aabb.hi - o;
+    }
+}
+
 // b2Fixture changes between steps (prop: the C-ABI's GB_FIXTURE_*): SetFriction, SetRestitution,
 // SetDensity (b2Fixture.h:300-340), SetSensor (b2Fixture.cpp:418-425, wakes the body on a change),
 // SetFilterData with Refilter (b2Fixture.cpp:181-214: the fixture's contacts flagged for filtering,

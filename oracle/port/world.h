@@ -169,6 +169,7 @@ struct World {
     // b2Body property changes between steps (the C-ABI's GB_BODY_* prop codes)
     void SetBodyProperty(int b, int prop, const float* v);
     void SetFixtureProperty(int f, int prop, const float* v);
+    void ShiftOrigin(Vec2 origin);
     void SynchronizeTransform(int b);
     void Advance(int b, float alpha);
 

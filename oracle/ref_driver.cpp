@@ -457,6 +457,10 @@ void rw_body_set(void* h, int b, int prop, const float* v)
     default: break;
     }
 }
+void rw_shift_origin(void* h, float x, float y)
+{
+    static_cast<RefWorld*>(h)->world.ShiftOrigin(b2Vec2(x, y));
+}
 void rw_fixture_set(void* h, int f, int prop, const float* v)
 {
     b2Fixture* fx = static_cast<RefWorld*>(h)->fixtures[f];

@@ -215,8 +215,15 @@ def fixture_props_script():
     }
 
 
+def shift_script():
+    """{step: [op]} applied before that step to scenes.pulley_mouse: b2World::ShiftOrigin, op ("shift", x,
+    y) (bodies, the mouse joint's target, the pulley's ground anchors and the broadphase move)."""
+    return {40: [("shift", 10.0, -3.0)], 120: [("shift", -25.5, 7.25)], 200: [("shift", 0.1, 0.0)]}
+
+
 def apply_ops(world, ops, w: int = 0):
-    """Applies destroy_script(), settings_script(), body_props_script() and fixture_props_script() ops to an oracle world or a device world (same
+    """Applies destroy_script(), settings_script(), body_props_script(), fixture_props_script() and
+    shift_script() ops to an oracle world or a device world (same
     method names); returns the destruction listener's calls of the ops as (kind, index), in order."""
     calls = []
     for op in ops:
@@ -225,6 +232,8 @@ def apply_ops(world, ops, w: int = 0):
             world.set_settings(*args) if w == 0 else world.set_settings(*args, w=w)
         elif op[0] == "clear_forces":
             world.clear_forces() if w == 0 else world.clear_forces(w)
+        elif op[0] == "shift":
+            world.shift_origin(op[1], op[2]) if w == 0 else world.shift_origin(op[1], op[2], w)
         elif op[0] == "fix":
             world.fixture_set(op[1], op[2], op[3]) if w == 0 else world.fixture_set(op[1], op[2], op[3], w)
         elif op[0] == "prop":

@@ -89,12 +89,13 @@ def scripted_cases():
     """Trajectory cases with b2World changes between steps: (name, scene factory, steps, ops by step).
     The ops (tests/_util.py destroy_script) destroy bodies, joints and fixtures and create bodies."""
     sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
-    from tests._util import body_props_script, destroy_script, fixture_props_script, settings_script
+    from tests._util import body_props_script, destroy_script, fixture_props_script, settings_script, shift_script
 
     return [("destroy_mix", lambda: scenes.destroy_mix(scenes.SplitMix64(5)), 200, destroy_script()),
             ("settings_mix", lambda: scenes.destroy_mix(scenes.SplitMix64(7)), 340, settings_script()),
             ("body_props", lambda: scenes.destroy_mix(scenes.SplitMix64(11)), 320, body_props_script()),
-            ("fixture_props", lambda: scenes.destroy_mix(scenes.SplitMix64(13)), 300, fixture_props_script())]
+            ("fixture_props", lambda: scenes.destroy_mix(scenes.SplitMix64(13)), 300, fixture_props_script()),
+            ("shift_origin", lambda: scenes.pulley_mouse(scenes.SplitMix64(4)), 260, shift_script())]
 
 
 def run_scripted(scene, steps, script, trig):
@@ -279,7 +280,7 @@ def make_trig(n: int = 200000):
 
 def tree_cases():
     """Cases of tree_stats.npz: (name, scene factory, steps, ops by step)."""
-    from tests._util import body_props_script, destroy_script, fixture_props_script
+    from tests._util import body_props_script, destroy_script, fixture_props_script, shift_script
 
     return [("pyramid20", lambda: scenes.config1(), 200, {}),
             ("drop300", lambda: scenes.drop(300, scenes.SplitMix64(7)), 300, {}),
@@ -290,7 +291,8 @@ def tree_cases():
             ("config2_10k", lambda: scenes.config2(10000, seed=1, allow_sleep=True), 100, {}),
             ("destroy_mix", lambda: scenes.destroy_mix(scenes.SplitMix64(5)), 200, destroy_script()),
             ("body_props", lambda: scenes.destroy_mix(scenes.SplitMix64(11)), 320, body_props_script()),
-            ("fixture_props", lambda: scenes.destroy_mix(scenes.SplitMix64(13)), 300, fixture_props_script())]
+            ("fixture_props", lambda: scenes.destroy_mix(scenes.SplitMix64(13)), 300, fixture_props_script()),
+            ("shift_origin", lambda: scenes.pulley_mouse(scenes.SplitMix64(4)), 260, shift_script())]
 
 
 def make_tree():

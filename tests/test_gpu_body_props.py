@@ -1,7 +1,7 @@
 """b2Body properties changed between device steps (SetType to static, kinematic and dynamic, SetActive
 off and on, SetFixedRotation, SetBullet, SetSleepingAllowed, SetLinearDamping, SetAngularDamping,
 SetGravityScale, SetMassData, ResetMassData) and fixture properties (SetSensor, SetFriction,
-SetRestitution, SetFilterData, SetDensity): bit-exact against the reference's golden digests step by step with the reference's
+SetRestitution, SetFilterData, SetDensity) and b2World::ShiftOrigin: bit-exact against the reference's golden digests step by step with the reference's
 final proxy ids; the EndContact calls of the contacts SetType and SetActive destroy as the CPU oracle
 makes them; and one world of a batch changed while the others step on."""
 from __future__ import annotations
@@ -13,7 +13,8 @@ import oracle
 from box2dpp_gb300 import scenes
 from box2dpp_gb300._lib import GbError
 from box2dpp_gb300.world import World
-from tests._util import DT, PI, VI, apply_ops, body_props_script, digest, fixture_props_script, golden
+from tests._util import (DT, PI, VI, apply_ops, body_props_script, digest, fixture_props_script, golden,
+                         shift_script)
 
 pytestmark = pytest.mark.gpu
 
@@ -53,6 +54,21 @@ def test_fixture_props_case_bit_exact_vs_reference(gpu):
     w.sync()
     ids, _ = w.proxies()
     assert np.array_equal(ids, g["proxy_ids"])
+
+
+def test_shift_origin_case_bit_exact_vs_reference(gpu):
+    g = golden("shift_origin_project")
+    w = World(scenes.pulley_mouse(scenes.SplitMix64(4)))
+    script = shift_script()
+    for s in range(1, int(g["steps"]) + 1):
+        if s in script:
+            apply_ops(w, script[s])
+        w.step(DT, VI, PI)
+        assert np.array_equal(digest(w.bodies(), *w.contacts()), g["digests"][s - 1]), f"first divergence at step {s}"
+    w.sync()
+    ids, fat = w.proxies()
+    assert np.array_equal(ids, g["proxy_ids"])
+    assert np.array_equal(fat.view(np.uint32), g["proxy_fat"].view(np.uint32))
 
 
 def test_body_props_end_contact_calls_match_oracle(gpu):

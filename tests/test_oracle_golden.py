@@ -210,6 +210,31 @@ def test_port_fixture_props_case_matches_reference(trig):
 
 
 @pytest.mark.parametrize("trig", ["project", "libm"])
+def test_port_shift_origin_case_matches_reference(trig):
+    """b2World::ShiftOrigin between steps of a scene with a mouse and a pulley joint: per-step state and
+    the final proxies (ids and fat boxes) as the reference."""
+    import platform
+
+    from box2dpp_gb300 import scenes
+    from tests._util import apply_ops, digest, shift_script
+
+    g = golden(f"shift_origin_{trig}")
+    w = oracle.OracleWorld(scenes.pulley_mouse(scenes.SplitMix64(4)), "port", trig)
+    script = shift_script()
+    for s in range(1, int(g["steps"]) + 1):
+        if s in script:
+            apply_ops(w, script[s])
+        w.step()
+        if not np.array_equal(digest(w.bodies(), *w.contacts()), g["digests"][s - 1]):
+            if trig == "libm" and platform.machine() != "x86_64":
+                pytest.skip("libm trig differs on this machine")
+            raise AssertionError(f"first divergence at step {s}")
+    ids, fat = w.proxies()
+    assert np.array_equal(ids, g["proxy_ids"])
+    assert np.array_equal(fat.view(np.uint32), g["proxy_fat"].view(np.uint32))
+
+
+@pytest.mark.parametrize("trig", ["project", "libm"])
 def test_port_settings_case_matches_reference(trig):
     """b2World settings changed between steps (gravity, sleep off and on, warm starting, continuous
     collision, sub-stepping, forces kept across steps and cleared): per-step state as the reference."""

@@ -57,3 +57,18 @@ def test_tree_calls_argument_rules():
     assert w.lib.gb_world_track_tree(w.h, 1) == GB_ERR_INVALID
     empty = World(scenes.Scene(name="empty"), track_tree=True)
     assert empty.tree_stats() == (0, 0, np.float32(0.0))
+
+
+def test_shift_origin_before_stepping_matches():
+    """b2World::ShiftOrigin on the host: bodies, proxies (ids and fat boxes) and the tree as the
+    reference's."""
+    sc = scenes.pulley_mouse(scenes.SplitMix64(4))
+    w = World(sc, track_tree=True)
+    o = oracle.OracleWorld(sc, _kind(), "project")
+    for x, y in ((10.0, -3.0), (-25.5, 7.25)):
+        w.shift_origin(x, y)
+        o.shift_origin(x, y)
+    assert np.array_equal(w.bodies().view(np.uint32), o.bodies().view(np.uint32))
+    (i1, f1), (i2, f2) = w.proxies(), o.proxies()
+    assert np.array_equal(i1, i2) and np.array_equal(f1.view(np.uint32), f2.view(np.uint32))
+    assert _same(w.tree_stats(), o.tree_stats())
