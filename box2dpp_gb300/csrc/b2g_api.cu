@@ -3038,9 +3038,122 @@ gb_status SetFixturePropertyHost(HWorld& W, int f, int prop, const float* v)
     }
 }
 
+// Joint changes between steps on the host copy (prop: GB_JOINT_*), with the reference's wakes and limit
+// impulse resets: b2RevoluteJoint::EnableMotor, SetMotorSpeed, SetMaxMotorTorque, EnableLimit,
+// SetLimits (Dynamics/Joints/b2RevoluteJoint.cpp:419-483), the prismatic joint's
+// (b2PrismaticJoint.cpp:546-604; translations in lowerAngle/upperAngle, the motor force in
+// maxMotorTorque) and the wheel joint's (b2WheelJoint.cpp:377-396) counterparts; the length, spring,
+// force and offset setters of the distance, weld, wheel, rope, friction, motor, gear and mouse joints
+// (their headers; b2MotorJoint.cpp:228-284). A property the joint's type does not have is invalid.
+gb_status SetJointPropertyHost(HWorld& W, int ji, int prop, const float* v)
+{
+    Joint& j = W.joints[ji];
+    const int t = j.type;
+    const bool motorised = t == kJointRevolute || t == kJointPrismatic || t == kJointWheel;
+    const bool limited = t == kJointRevolute || t == kJointPrismatic;
+    const bool spring = t == kJointDistance || t == kJointWeld || t == kJointWheel || t == kJointMouse;
+    auto wake = [&]() {
+        WakeHost(W.bodies[j.bodyA]);
+        WakeHost(W.bodies[j.bodyB]);
+    };
+    switch (prop) {
+    case GB_JOINT_MOTOR_SPEED:
+        if (!motorised) return GB_ERR_INVALID;
+        wake();
+        j.motorSpeed = v[0];
+        return GB_OK;
+    case GB_JOINT_MAX_MOTOR:
+        if (!motorised) return GB_ERR_INVALID;
+        wake();
+        j.maxMotorTorque = v[0];
+        return GB_OK;
+    case GB_JOINT_ENABLE_MOTOR:
+        if (!motorised) return GB_ERR_INVALID;
+        wake();
+        j.enableMotor = v[0] != 0.0f ? 1 : 0;
+        return GB_OK;
+    case GB_JOINT_ENABLE_LIMIT: {
+        if (!limited) return GB_ERR_INVALID;
+        const int flag = v[0] != 0.0f ? 1 : 0;
+        if (flag != j.enableLimit) {
+            wake();
+            j.enableLimit = flag;
+            j.impulse[2] = 0.0f;
+        }
+        return GB_OK;
+    }
+    case GB_JOINT_LIMITS:
+        if (!limited || !(v[0] <= v[1])) return GB_ERR_INVALID;
+        if (v[0] != j.lowerAngle || v[1] != j.upperAngle) {
+            wake();
+            j.impulse[2] = 0.0f;
+            j.lowerAngle = v[0];
+            j.upperAngle = v[1];
+        }
+        return GB_OK;
+    case GB_JOINT_LENGTH:
+        if (t != kJointDistance) return GB_ERR_INVALID;
+        j.length = v[0];
+        return GB_OK;
+    case GB_JOINT_FREQUENCY:
+        if (!spring) return GB_ERR_INVALID;
+        j.frequencyHz = v[0];
+        return GB_OK;
+    case GB_JOINT_DAMPING_RATIO:
+        if (!spring) return GB_ERR_INVALID;
+        j.dampingRatio = v[0];
+        return GB_OK;
+    case GB_JOINT_MAX_LENGTH:
+        if (t != kJointRope) return GB_ERR_INVALID;
+        j.maxLength = v[0];
+        return GB_OK;
+    case GB_JOINT_MAX_FORCE:
+        if (t != kJointFriction && t != kJointMotor && t != kJointMouse) return GB_ERR_INVALID;
+        j.maxForce = v[0];
+        return GB_OK;
+    case GB_JOINT_MAX_TORQUE:
+        if (t != kJointFriction && t != kJointMotor) return GB_ERR_INVALID;
+        j.maxTorque = v[0];
+        return GB_OK;
+    case GB_JOINT_LINEAR_OFFSET:
+        if (t != kJointMotor) return GB_ERR_INVALID;
+        if (v[0] != j.linearOffset.x || v[1] != j.linearOffset.y) {
+            wake();
+            j.linearOffset = V(v[0], v[1]);
+        }
+        return GB_OK;
+    case GB_JOINT_ANGULAR_OFFSET:
+        if (t != kJointMotor) return GB_ERR_INVALID;
+        if (v[0] != j.angularOffset) {
+            wake();
+            j.angularOffset = v[0];
+        }
+        return GB_OK;
+    case GB_JOINT_CORRECTION_FACTOR:
+        if (t != kJointMotor) return GB_ERR_INVALID;
+        j.correctionFactor = v[0];
+        return GB_OK;
+    case GB_JOINT_RATIO:
+        if (t != kJointGear) return GB_ERR_INVALID;
+        j.ratio = v[0];
+        return GB_OK;
+    default: return GB_ERR_INVALID;
+    }
+}
+
 } // namespace
 
 extern "C" {
+
+gb_status gb_joint_set(gb_world* g, int w, int joint, int prop, const float* v)
+{
+    if (!v) return GB_ERR_INVALID;
+    gb_status s = Mutable(g, w);
+    if (s != GB_OK) return s;
+    HWorld& W = g->worlds[w];
+    if (joint < 0 || joint >= (int)W.joints.size() || W.joints[joint].bodyA == kNullIdx) return GB_ERR_INVALID;
+    return SetJointPropertyHost(W, joint, prop, v);
+}
 
 gb_status gb_world_shift_origin(gb_world* g, int w, float x, float y)
 {

@@ -187,6 +187,13 @@ class World:
                    "gb_body_set")
         return calls[:min(n.value, 256)]
 
+    def joint_set(self, joint: int, prop: int, value=0.0, w: int = 0) -> None:
+        """A joint setter between steps (gb_joint_set; prop GB_JOINT_*, value a number or a pair)."""
+        v = np.zeros(4, dtype=np.float32)
+        vals = np.atleast_1d(np.asarray(value, dtype=np.float32))
+        v[:len(vals)] = vals
+        _lib.check(self.lib.gb_joint_set(self.h, int(w), int(joint), int(prop), v), "gb_joint_set")
+
     def shift_origin(self, x: float, y: float, w: int = 0) -> None:
         """b2World::ShiftOrigin(b2Vec2(x, y)) of world w between steps."""
         _lib.check(self.lib.gb_world_shift_origin(self.h, int(w), float(x), float(y)), "gb_world_shift_origin")

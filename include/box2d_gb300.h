@@ -197,6 +197,34 @@ gb_status gb_world_tree_stats(gb_world* world, int w, int* height, int* balance,
 #define GB_BODY_RESET_MASS_DATA 9
 gb_status gb_body_set(gb_world* world, int w, int body, int prop, const float* v, int* calls, int cap, int* n_calls);
 
+/* Joint changes between steps (no step in progress), with the reference's wakes of both bodies and
+ * resets of the limit impulse: GB_JOINT_MOTOR_SPEED, GB_JOINT_MAX_MOTOR (torque; a prismatic joint's
+ * force), GB_JOINT_ENABLE_MOTOR (revolute, prismatic, wheel: b2RevoluteJoint.cpp:419-443,
+ * b2PrismaticJoint.cpp:585-604, b2WheelJoint.cpp:377-396); GB_JOINT_ENABLE_LIMIT, GB_JOINT_LIMITS
+ * (v[0] lower <= v[1] upper; revolute, prismatic: b2RevoluteJoint.cpp:450-483,
+ * b2PrismaticJoint.cpp:546-577); GB_JOINT_LENGTH (distance); GB_JOINT_FREQUENCY,
+ * GB_JOINT_DAMPING_RATIO (distance, weld, the wheel's spring, mouse); GB_JOINT_MAX_LENGTH (rope);
+ * GB_JOINT_MAX_FORCE (friction, motor, mouse); GB_JOINT_MAX_TORQUE (friction, motor);
+ * GB_JOINT_LINEAR_OFFSET (v[0..1]), GB_JOINT_ANGULAR_OFFSET, GB_JOINT_CORRECTION_FACTOR (motor,
+ * b2MotorJoint.cpp:228-284); GB_JOINT_RATIO (gear). A property the joint's type does not have
+ * returns GB_ERR_INVALID. */
+#define GB_JOINT_MOTOR_SPEED 0
+#define GB_JOINT_MAX_MOTOR 1
+#define GB_JOINT_ENABLE_MOTOR 2
+#define GB_JOINT_ENABLE_LIMIT 3
+#define GB_JOINT_LIMITS 4
+#define GB_JOINT_LENGTH 5
+#define GB_JOINT_FREQUENCY 6
+#define GB_JOINT_DAMPING_RATIO 7
+#define GB_JOINT_MAX_LENGTH 8
+#define GB_JOINT_MAX_FORCE 9
+#define GB_JOINT_MAX_TORQUE 10
+#define GB_JOINT_LINEAR_OFFSET 11
+#define GB_JOINT_ANGULAR_OFFSET 12
+#define GB_JOINT_CORRECTION_FACTOR 13
+#define GB_JOINT_RATIO 14
+gb_status gb_joint_set(gb_world* world, int w, int joint, int prop, const float* v);
+
 /* b2World::ShiftOrigin (Box2D/Dynamics/b2World.cpp:1261-1282) of world w between steps: bodies, the
  * mouse joints' targets, the pulleys' ground anchors and the broadphase's boxes move by -(x, y). */
 gb_status gb_world_shift_origin(gb_world* world, int w, float x, float y);

@@ -521,10 +521,152 @@ public:
 
 protected:
     friend class b2World;
+    // one gb_joint_set call (GB_JOINT_*); false when it did not apply
+    bool Set(int prop, float v0, float v1 = 0.0f);
     int m_index = -1;
     b2Body *m_a = nullptr, *m_b = nullptr;
     b2World* m_world = nullptr;
     bool m_alive = true;
+};
+
+// The typed joints CreateJoint returns, so that the reference's static_cast<b2RevoluteJoint*> and its
+// setters read the same (Box2D/Dynamics/Joints/*.h). Each setter is a gb_joint_set call with the
+// reference's wakes and limit-impulse resets; the getters return what was defined or set.
+class b2RevoluteJoint : public b2Joint {
+public:
+    void EnableMotor(bool flag) { if (Set(GB_JOINT_ENABLE_MOTOR, flag ? 1.0f : 0.0f)) m_enableMotor = flag; }
+    void SetMotorSpeed(float speed) { if (Set(GB_JOINT_MOTOR_SPEED, speed)) m_motorSpeed = speed; }
+    void SetMaxMotorTorque(float torque) { if (Set(GB_JOINT_MAX_MOTOR, torque)) m_maxMotorTorque = torque; }
+    void EnableLimit(bool flag) { if (Set(GB_JOINT_ENABLE_LIMIT, flag ? 1.0f : 0.0f)) m_enableLimit = flag; }
+    void SetLimits(float lower, float upper)
+    {
+        if (Set(GB_JOINT_LIMITS, lower, upper)) { m_lower = lower; m_upper = upper; }
+    }
+    bool IsMotorEnabled() const { return m_enableMotor; }
+    float GetMotorSpeed() const { return m_motorSpeed; }
+    float GetMaxMotorTorque() const { return m_maxMotorTorque; }
+    bool IsLimitEnabled() const { return m_enableLimit; }
+    float GetLowerLimit() const { return m_lower; }
+    float GetUpperLimit() const { return m_upper; }
+
+private:
+    friend class b2World;
+    bool m_enableMotor = false, m_enableLimit = false;
+    float m_motorSpeed = 0.0f, m_maxMotorTorque = 0.0f, m_lower = 0.0f, m_upper = 0.0f;
+};
+class b2PrismaticJoint : public b2Joint {
+public:
+    void EnableMotor(bool flag) { if (Set(GB_JOINT_ENABLE_MOTOR, flag ? 1.0f : 0.0f)) m_enableMotor = flag; }
+    void SetMotorSpeed(float speed) { if (Set(GB_JOINT_MOTOR_SPEED, speed)) m_motorSpeed = speed; }
+    void SetMaxMotorForce(float force) { if (Set(GB_JOINT_MAX_MOTOR, force)) m_maxMotorForce = force; }
+    void EnableLimit(bool flag) { if (Set(GB_JOINT_ENABLE_LIMIT, flag ? 1.0f : 0.0f)) m_enableLimit = flag; }
+    void SetLimits(float lower, float upper)
+    {
+        if (Set(GB_JOINT_LIMITS, lower, upper)) { m_lower = lower; m_upper = upper; }
+    }
+    bool IsMotorEnabled() const { return m_enableMotor; }
+    float GetMotorSpeed() const { return m_motorSpeed; }
+    float GetMaxMotorForce() const { return m_maxMotorForce; }
+    bool IsLimitEnabled() const { return m_enableLimit; }
+    float GetLowerLimit() const { return m_lower; }
+    float GetUpperLimit() const { return m_upper; }
+
+private:
+    friend class b2World;
+    bool m_enableMotor = false, m_enableLimit = false;
+    float m_motorSpeed = 0.0f, m_maxMotorForce = 0.0f, m_lower = 0.0f, m_upper = 0.0f;
+};
+class b2WheelJoint : public b2Joint {
+public:
+    void EnableMotor(bool flag) { if (Set(GB_JOINT_ENABLE_MOTOR, flag ? 1.0f : 0.0f)) m_enableMotor = flag; }
+    void SetMotorSpeed(float speed) { if (Set(GB_JOINT_MOTOR_SPEED, speed)) m_motorSpeed = speed; }
+    void SetMaxMotorTorque(float torque) { if (Set(GB_JOINT_MAX_MOTOR, torque)) m_maxMotorTorque = torque; }
+    void SetSpringFrequencyHz(float hz) { if (Set(GB_JOINT_FREQUENCY, hz)) m_frequencyHz = hz; }
+    void SetSpringDampingRatio(float ratio) { if (Set(GB_JOINT_DAMPING_RATIO, ratio)) m_dampingRatio = ratio; }
+    bool IsMotorEnabled() const { return m_enableMotor; }
+    float GetMotorSpeed() const { return m_motorSpeed; }
+    float GetMaxMotorTorque() const { return m_maxMotorTorque; }
+    float GetSpringFrequencyHz() const { return m_frequencyHz; }
+    float GetSpringDampingRatio() const { return m_dampingRatio; }
+
+private:
+    friend class b2World;
+    bool m_enableMotor = false;
+    float m_motorSpeed = 0.0f, m_maxMotorTorque = 0.0f, m_frequencyHz = 0.0f, m_dampingRatio = 0.0f;
+};
+class b2DistanceJoint : public b2Joint {
+public:
+    void SetLength(float length) { if (Set(GB_JOINT_LENGTH, length)) m_length = length; }
+    void SetFrequency(float hz) { if (Set(GB_JOINT_FREQUENCY, hz)) m_frequencyHz = hz; }
+    void SetDampingRatio(float ratio) { if (Set(GB_JOINT_DAMPING_RATIO, ratio)) m_dampingRatio = ratio; }
+    float GetLength() const { return m_length; }
+    float GetFrequency() const { return m_frequencyHz; }
+    float GetDampingRatio() const { return m_dampingRatio; }
+
+private:
+    friend class b2World;
+    float m_length = 1.0f, m_frequencyHz = 0.0f, m_dampingRatio = 0.0f;
+};
+class b2WeldJoint : public b2Joint {
+public:
+    void SetFrequency(float hz) { if (Set(GB_JOINT_FREQUENCY, hz)) m_frequencyHz = hz; }
+    void SetDampingRatio(float ratio) { if (Set(GB_JOINT_DAMPING_RATIO, ratio)) m_dampingRatio = ratio; }
+    float GetFrequency() const { return m_frequencyHz; }
+    float GetDampingRatio() const { return m_dampingRatio; }
+
+private:
+    friend class b2World;
+    float m_frequencyHz = 0.0f, m_dampingRatio = 0.0f;
+};
+class b2RopeJoint : public b2Joint {
+public:
+    void SetMaxLength(float length) { if (Set(GB_JOINT_MAX_LENGTH, length)) m_maxLength = length; }
+    float GetMaxLength() const { return m_maxLength; }
+
+private:
+    friend class b2World;
+    float m_maxLength = 0.0f;
+};
+class b2FrictionJoint : public b2Joint {
+public:
+    void SetMaxForce(float force) { if (Set(GB_JOINT_MAX_FORCE, force)) m_maxForce = force; }
+    void SetMaxTorque(float torque) { if (Set(GB_JOINT_MAX_TORQUE, torque)) m_maxTorque = torque; }
+    float GetMaxForce() const { return m_maxForce; }
+    float GetMaxTorque() const { return m_maxTorque; }
+
+private:
+    friend class b2World;
+    float m_maxForce = 0.0f, m_maxTorque = 0.0f;
+};
+class b2MotorJoint : public b2Joint {
+public:
+    void SetLinearOffset(const b2Vec2& offset)
+    {
+        if (Set(GB_JOINT_LINEAR_OFFSET, offset.x, offset.y)) m_linearOffset = offset;
+    }
+    void SetAngularOffset(float offset) { if (Set(GB_JOINT_ANGULAR_OFFSET, offset)) m_angularOffset = offset; }
+    void SetMaxForce(float force) { if (Set(GB_JOINT_MAX_FORCE, force)) m_maxForce = force; }
+    void SetMaxTorque(float torque) { if (Set(GB_JOINT_MAX_TORQUE, torque)) m_maxTorque = torque; }
+    void SetCorrectionFactor(float factor) { if (Set(GB_JOINT_CORRECTION_FACTOR, factor)) m_correctionFactor = factor; }
+    const b2Vec2& GetLinearOffset() const { return m_linearOffset; }
+    float GetAngularOffset() const { return m_angularOffset; }
+    float GetMaxForce() const { return m_maxForce; }
+    float GetMaxTorque() const { return m_maxTorque; }
+    float GetCorrectionFactor() const { return m_correctionFactor; }
+
+private:
+    friend class b2World;
+    b2Vec2 m_linearOffset;
+    float m_angularOffset = 0.0f, m_maxForce = 0.0f, m_maxTorque = 0.0f, m_correctionFactor = 0.0f;
+};
+class b2GearJoint : public b2Joint {
+public:
+    void SetRatio(float ratio) { if (Set(GB_JOINT_RATIO, ratio)) m_ratio = ratio; }
+    float GetRatio() const { return m_ratio; }
+
+private:
+    friend class b2World;
+    float m_ratio = 1.0f;
 };
 
 // b2MouseJoint (Box2D/Dynamics/Joints/b2MouseJoint.h:63-124): what CreateJoint returns for a
@@ -533,10 +675,17 @@ class b2MouseJoint : public b2Joint {
 public:
     void SetTarget(const b2Vec2& target);  // one gb_body_edits record (GB_EDIT_MOUSE_TARGET)
     const b2Vec2& GetTarget() const { return m_target; }
+    void SetMaxForce(float force) { if (Set(GB_JOINT_MAX_FORCE, force)) m_maxForce = force; }
+    void SetFrequency(float hz) { if (Set(GB_JOINT_FREQUENCY, hz)) m_frequencyHz = hz; }
+    void SetDampingRatio(float ratio) { if (Set(GB_JOINT_DAMPING_RATIO, ratio)) m_dampingRatio = ratio; }
+    float GetMaxForce() const { return m_maxForce; }
+    float GetFrequency() const { return m_frequencyHz; }
+    float GetDampingRatio() const { return m_dampingRatio; }
 
 private:
     friend class b2World;
     b2Vec2 m_target;
+    float m_maxForce = 0.0f, m_frequencyHz = 5.0f, m_dampingRatio = 0.7f;
 };
 
 struct b2ManifoldPoint {
@@ -764,6 +913,14 @@ public:
         if (Destroy(gb_destroy_joint, joint->m_index, calls) != GB_OK) return;
         joint->m_alive = false;
     }
+    // one gb_joint_set call (the typed joints' setters)
+    bool SetJointProperty(b2Joint* j, int prop, float v0, float v1)
+    {
+        if (!Handle() || !j || !j->m_alive || j->m_world != this) return false;
+        const float v[4] = {v0, v1, 0.0f, 0.0f};
+        m_stale = true;
+        return gb_joint_set(m_h, 0, j->m_index, prop, v) == GB_OK;
+    }
     // b2World::ShiftOrigin (Box2D/Dynamics/b2World.cpp:1261-1282)
     void ShiftOrigin(const b2Vec2& newOrigin)
     {
@@ -918,7 +1075,13 @@ public:
         const int a = def->bodyA->m_index, b = def->bodyB->m_index;
         int id = -1;
         if (gb_create_revolute_joints(m_h, 0, 1, &a, &b, f, &flags, &id) != GB_OK) return nullptr;
-        std::unique_ptr<b2Joint> j(new b2Joint());
+        std::unique_ptr<b2RevoluteJoint> j(new b2RevoluteJoint());
+        j->m_enableMotor = def->enableMotor;
+        j->m_enableLimit = def->enableLimit;
+        j->m_motorSpeed = def->motorSpeed;
+        j->m_maxMotorTorque = def->maxMotorTorque;
+        j->m_lower = def->lowerAngle;
+        j->m_upper = def->upperAngle;
         j->m_world = this;
         j->m_index = id;
         j->m_a = def->bodyA;
@@ -931,14 +1094,21 @@ public:
     {
         const float f[GB_JOINT_FLOATS] = {def->localAnchorA.x, def->localAnchorA.y, def->localAnchorB.x,
                                           def->localAnchorB.y, def->length, def->frequencyHz, def->dampingRatio};
-        return AddJoint(GB_JOINT_DISTANCE, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
+        std::unique_ptr<b2DistanceJoint> j(new b2DistanceJoint());
+        j->m_length = def->length;
+        j->m_frequencyHz = def->frequencyHz;
+        j->m_dampingRatio = def->dampingRatio;
+        return AddJoint(GB_JOINT_DISTANCE, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(j));
     }
     b2Joint* CreateJoint(const b2WeldJointDef* def)
     {
         const float f[GB_JOINT_FLOATS] = {def->localAnchorA.x, def->localAnchorA.y, def->localAnchorB.x,
                                           def->localAnchorB.y, def->referenceAngle, def->frequencyHz,
                                           def->dampingRatio};
-        return AddJoint(GB_JOINT_WELD, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
+        std::unique_ptr<b2WeldJoint> j(new b2WeldJoint());
+        j->m_frequencyHz = def->frequencyHz;
+        j->m_dampingRatio = def->dampingRatio;
+        return AddJoint(GB_JOINT_WELD, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(j));
     }
     b2Joint* CreateJoint(const b2WheelJointDef* def)
     {
@@ -946,25 +1116,42 @@ public:
                                           def->localAnchorB.y, def->localAxisA.x, def->localAxisA.y,
                                           def->maxMotorTorque, def->motorSpeed, def->frequencyHz, def->dampingRatio};
         const int flags = (def->enableMotor ? 2 : 0) | (def->collideConnected ? 4 : 0);
-        return AddJoint(GB_JOINT_WHEEL, def->bodyA, def->bodyB, f, flags);
+        std::unique_ptr<b2WheelJoint> j(new b2WheelJoint());
+        j->m_enableMotor = def->enableMotor;
+        j->m_motorSpeed = def->motorSpeed;
+        j->m_maxMotorTorque = def->maxMotorTorque;
+        j->m_frequencyHz = def->frequencyHz;
+        j->m_dampingRatio = def->dampingRatio;
+        return AddJoint(GB_JOINT_WHEEL, def->bodyA, def->bodyB, f, flags, std::move(j));
     }
     b2Joint* CreateJoint(const b2RopeJointDef* def)
     {
         const float f[GB_JOINT_FLOATS] = {def->localAnchorA.x, def->localAnchorA.y, def->localAnchorB.x,
                                           def->localAnchorB.y, def->maxLength};
-        return AddJoint(GB_JOINT_ROPE, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
+        std::unique_ptr<b2RopeJoint> j(new b2RopeJoint());
+        j->m_maxLength = def->maxLength;
+        return AddJoint(GB_JOINT_ROPE, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(j));
     }
     b2Joint* CreateJoint(const b2FrictionJointDef* def)
     {
         const float f[GB_JOINT_FLOATS] = {def->localAnchorA.x, def->localAnchorA.y, def->localAnchorB.x,
                                           def->localAnchorB.y, def->maxForce, def->maxTorque};
-        return AddJoint(GB_JOINT_FRICTION, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
+        std::unique_ptr<b2FrictionJoint> j(new b2FrictionJoint());
+        j->m_maxForce = def->maxForce;
+        j->m_maxTorque = def->maxTorque;
+        return AddJoint(GB_JOINT_FRICTION, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(j));
     }
     b2Joint* CreateJoint(const b2MotorJointDef* def)
     {
         const float f[GB_JOINT_FLOATS] = {def->linearOffset.x, def->linearOffset.y, def->angularOffset, def->maxForce,
                                           def->maxTorque, def->correctionFactor};
-        return AddJoint(GB_JOINT_MOTOR, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
+        std::unique_ptr<b2MotorJoint> j(new b2MotorJoint());
+        j->m_linearOffset = def->linearOffset;
+        j->m_angularOffset = def->angularOffset;
+        j->m_maxForce = def->maxForce;
+        j->m_maxTorque = def->maxTorque;
+        j->m_correctionFactor = def->correctionFactor;
+        return AddJoint(GB_JOINT_MOTOR, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(j));
     }
     b2Joint* CreateJoint(const b2MouseJointDef* def)
     {
@@ -972,6 +1159,9 @@ public:
                                           def->dampingRatio};
         std::unique_ptr<b2MouseJoint> j(new b2MouseJoint());
         j->m_target = def->target;
+        j->m_maxForce = def->maxForce;
+        j->m_frequencyHz = def->frequencyHz;
+        j->m_dampingRatio = def->dampingRatio;
         return AddJoint(GB_JOINT_MOUSE, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(j));
     }
     b2Joint* CreateJoint(const b2PulleyJointDef* def)
@@ -986,7 +1176,9 @@ public:
     {
         if (!def->joint1 || !def->joint2) return nullptr;
         const float f[GB_JOINT_FLOATS] = {(float)def->joint1->GetIndex(), (float)def->joint2->GetIndex(), def->ratio};
-        b2Joint* j = AddJoint(GB_JOINT_GEAR, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
+        std::unique_ptr<b2GearJoint> g(new b2GearJoint());
+        g->m_ratio = def->ratio;
+        b2Joint* j = AddJoint(GB_JOINT_GEAR, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(g));
         if (j) {  // b2GearJoint::GetBodyA/B: the coupled joints' bodies B
             j->m_a = def->joint1->GetBodyB();
             j->m_b = def->joint2->GetBodyB();
@@ -1000,7 +1192,14 @@ public:
                                           def->referenceAngle, def->lowerTranslation, def->upperTranslation,
                                           def->maxMotorForce, def->motorSpeed};
         const int flags = (def->enableLimit ? 1 : 0) | (def->enableMotor ? 2 : 0) | (def->collideConnected ? 4 : 0);
-        return AddJoint(GB_JOINT_PRISMATIC, def->bodyA, def->bodyB, f, flags);
+        std::unique_ptr<b2PrismaticJoint> j(new b2PrismaticJoint());
+        j->m_enableMotor = def->enableMotor;
+        j->m_enableLimit = def->enableLimit;
+        j->m_motorSpeed = def->motorSpeed;
+        j->m_maxMotorForce = def->maxMotorForce;
+        j->m_lower = def->lowerTranslation;
+        j->m_upper = def->upperTranslation;
+        return AddJoint(GB_JOINT_PRISMATIC, def->bodyA, def->bodyB, f, flags, std::move(j));
     }
 
     void Step(float timeStep, int velocityIterations, int positionIterations)
@@ -1330,6 +1529,7 @@ inline void b2Body::SetSleepingAllowed(bool flag) { m_world->SetBodyProperty(thi
 inline void b2Body::SetLinearDamping(float d) { m_world->SetBodyProperty(this, GB_BODY_LINEAR_DAMPING, d); }
 inline void b2Body::SetAngularDamping(float d) { m_world->SetBodyProperty(this, GB_BODY_ANGULAR_DAMPING, d); }
 inline void b2Body::SetGravityScale(float scale) { m_world->SetBodyProperty(this, GB_BODY_GRAVITY_SCALE, scale); }
+inline bool b2Joint::Set(int prop, float v0, float v1) { return m_world->SetJointProperty(this, prop, v0, v1); }
 inline void b2Fixture::SetFriction(float friction)
 {
     if (m_body->GetWorld()->SetFixtureProperty(this, GB_FIXTURE_FRICTION, friction)) m_def.friction = friction;

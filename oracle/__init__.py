@@ -96,6 +96,7 @@ def _declare(lib, p: str) -> None:
     sig["body_info"] = (None, [vp, C.c_int, _f32p, C.POINTER(C.c_int)])
     sig["fixture_set"] = (None, [vp, C.c_int, C.c_int, _f32p])
     sig["shift_origin"] = (None, [vp, C.c_float, C.c_float])
+    sig["joint_set"] = (C.c_int, [vp, C.c_int, C.c_int, _f32p])
     for kind in ("body", "joint", "fixture"):
         sig["destroy_" + kind] = (C.c_int, [vp, C.c_int, _i32p, C.c_int])
     if p == "rw_":
@@ -205,6 +206,14 @@ class OracleWorld:
         and SetAutoClearForces between steps."""
         self._fn("set_settings")(self.h, float(gravity[0]), float(gravity[1]), int(allow_sleep), int(warm_starting),
                                  int(continuous), int(sub_stepping), int(auto_clear_forces))
+
+    def joint_set(self, joint: int, prop: int, value=0.0) -> None:
+        """A joint setter between steps (prop: the C-ABI's GB_JOINT_*; value a number or a pair)."""
+        v = np.zeros(4, dtype=np.float32)
+        vals = np.atleast_1d(np.asarray(value, dtype=np.float32))
+        v[:len(vals)] = vals
+        if self._fn("joint_set")(self.h, int(joint), int(prop), v) != 0:
+            raise ValueError(f"joint {joint} has no property {prop}")
 
     def shift_origin(self, x: float, y: float) -> None:
         """b2World::ShiftOrigin(b2Vec2(x, y))."""

@@ -117,6 +117,10 @@ void po_set_settings(void* h, float gx, float gy, int allowSleep, int warm, int 
     if (autoClear) w->wflags |= 0x4u;
     else w->wflags &= ~0x4u;
 }
+int po_joint_set(void* h, int j, int prop, const float* v)
+{
+    return static_cast<World*>(h)->SetJointProperty(j, prop, v);
+}
 void po_shift_origin(void* h, float x, float y)
 {
     static_cast<World*>(h)->ShiftOrigin(V(x, y));

@@ -464,6 +464,72 @@ void World::SetBodyProperty(int bi, int prop, const float* v)
     }
 }
 
+// Joint changes between steps (prop: the C-ABI's GB_JOINT_*), with the reference's wakes and limit
+// impulse resets: b2RevoluteJoint::EnableMotor, SetMotorSpeed, SetMaxMotorTorque, EnableLimit,
+// SetLimits (b2RevoluteJoint.cpp:419-483), the prismatic's (b2PrismaticJoint.cpp:546-604) and the
+// wheel's (b2WheelJoint.cpp:377-396) counterparts, the spring, length, force and offset setters of the
+// distance, weld, wheel, rope, friction, motor, gear and mouse joints (their headers; b2MotorJoint.cpp:
+// 228-284). Returns 0, or 1 when the joint has no such property.
+int World::SetJointProperty(int ji, int prop, const float* v)
+{
+    Joint& j = joints[ji];
+    const int t = j.type;
+    const bool motorised = t == kRevoluteJoint || t == kPrismaticJoint || t == kWheelJoint;
+    const bool limited = t == kRevoluteJoint || t == kPrismaticJoint;
+    const bool spring = t == kDistanceJoint || t == kWeldJoint || t == kWheelJoint || t == kMouseJoint;
+    auto wake = [&]() {
+        SetAwake(j.bodyA, true);
+        SetAwake(j.bodyB, true);
+    };
+    switch (prop) {
+    case 0: if (!motorised) return 1; wake(); j.motorSpeed = v[0]; return 0;
+    case 1: if (!motorised) return 1; wake(); j.maxMotorTorque = v[0]; return 0;
+    case 2: if (!motorised) return 1; wake(); j.enableMotor = v[0] != 0.0f; return 0;
+    case 3: {
+        if (!limited) return 1;
+        const bool flag = v[0] != 0.0f;
+        if (flag != j.enableLimit) {
+            wake();
+            j.enableLimit = flag;
+            j.impulse[2] = 0.0f;
+        }
+        return 0;
+    }
+    case 4:
+        if (!limited || !(v[0] <= v[1])) return 1;
+        if (v[0] != j.lowerAngle || v[1] != j.upperAngle) {
+            wake();
+            j.impulse[2] = 0.0f;
+            j.lowerAngle = v[0];
+            j.upperAngle = v[1];
+        }
+        return 0;
+    case 5: if (t != kDistanceJoint) return 1; j.length = v[0]; return 0;
+    case 6: if (!spring) return 1; j.frequencyHz = v[0]; return 0;
+    case 7: if (!spring) return 1; j.dampingRatio = v[0]; return 0;
+    case 8: if (t != kRopeJoint) return 1; j.maxLength = v[0]; return 0;
+    case 9: if (t != kFrictionJoint && t != kMotorJoint && t != kMouseJoint) return 1; j.maxForce = v[0]; return 0;
+    case 10: if (t != kFrictionJoint && t != kMotorJoint) return 1; j.maxTorque = v[0]; return 0;
+    case 11:
+        if (t != kMotorJoint) return 1;
+        if (v[0] != j.linearOffset.x || v[1] != j.linearOffset.y) {
+            wake();
+            j.linearOffset = V(v[0], v[1]);
+        }
+        return 0;
+    case 12:
+        if (t != kMotorJoint) return 1;
+        if (v[0] != j.angularOffset) {
+            wake();
+            j.angularOffset = v[0];
+        }
+        return 0;
+    case 13: if (t != kMotorJoint) return 1; j.correctionFactor = v[0]; return 0;
+    case 14: if (t != kGearJoint) return 1; j.ratio = v[0]; return 0;
+    default: return 1;
+    }
+}
+
 // b2World::ShiftOrigin (b2World.cpp:1261-1282): body transforms and sweep centres, the mouse joint's
 // target and the pulley's ground anchors (b2MouseJoint.cpp:222, b2PulleyJoint.cpp:347), and every
 // node box of the broadphase tree (b2DynamicTree.cpp:773-781) move by -origin.

@@ -170,6 +170,7 @@ struct World {
     void SetBodyProperty(int b, int prop, const float* v);
     void SetFixtureProperty(int f, int prop, const float* v);
     void ShiftOrigin(Vec2 origin);
+    int SetJointProperty(int j, int prop, const float* v);
     void SynchronizeTransform(int b);
     void Advance(int b, float alpha);
 

@@ -457,6 +457,88 @@ void rw_body_set(void* h, int b, int prop, const float* v)
     default: break;
     }
 }
+// joint setters through the reference's own classes; 1 when the joint type has no such setter
+int rw_joint_set(void* h, int ji, int prop, const float* v)
+{
+    b2Joint* j = static_cast<RefWorld*>(h)->joints[ji];
+    const b2JointType t = j->GetType();
+    const bool flag = v[0] != 0.0f;
+    if (t == e_revoluteJoint) {
+        b2RevoluteJoint* r = static_cast<b2RevoluteJoint*>(j);
+        switch (prop) {
+        case 0: r->SetMotorSpeed(v[0]); return 0;
+        case 1: r->SetMaxMotorTorque(v[0]); return 0;
+        case 2: r->EnableMotor(flag); return 0;
+        case 3: r->EnableLimit(flag); return 0;
+        case 4: r->SetLimits(v[0], v[1]); return 0;
+        default: return 1;
+        }
+    }
+    if (t == e_prismaticJoint) {
+        b2PrismaticJoint* p = static_cast<b2PrismaticJoint*>(j);
+        switch (prop) {
+        case 0: p->SetMotorSpeed(v[0]); return 0;
+        case 1: p->SetMaxMotorForce(v[0]); return 0;
+        case 2: p->EnableMotor(flag); return 0;
+        case 3: p->EnableLimit(flag); return 0;
+        case 4: p->SetLimits(v[0], v[1]); return 0;
+        default: return 1;
+        }
+    }
+    if (t == e_wheelJoint) {
+        b2WheelJoint* w = static_cast<b2WheelJoint*>(j);
+        switch (prop) {
+        case 0: w->SetMotorSpeed(v[0]); return 0;
+        case 1: w->SetMaxMotorTorque(v[0]); return 0;
+        case 2: w->EnableMotor(flag); return 0;
+        case 6: w->SetSpringFrequencyHz(v[0]); return 0;
+        case 7: w->SetSpringDampingRatio(v[0]); return 0;
+        default: return 1;
+        }
+    }
+    if (t == e_distanceJoint) {
+        b2DistanceJoint* d = static_cast<b2DistanceJoint*>(j);
+        switch (prop) {
+        case 5: d->SetLength(v[0]); return 0;
+        case 6: d->SetFrequency(v[0]); return 0;
+        case 7: d->SetDampingRatio(v[0]); return 0;
+        default: return 1;
+        }
+    }
+    if (t == e_weldJoint) {
+        b2WeldJoint* d = static_cast<b2WeldJoint*>(j);
+        if (prop == 6) { d->SetFrequency(v[0]); return 0; }
+        if (prop == 7) { d->SetDampingRatio(v[0]); return 0; }
+        return 1;
+    }
+    if (t == e_mouseJoint) {
+        b2MouseJoint* m = static_cast<b2MouseJoint*>(j);
+        if (prop == 6) { m->SetFrequency(v[0]); return 0; }
+        if (prop == 7) { m->SetDampingRatio(v[0]); return 0; }
+        if (prop == 9) { m->SetMaxForce(v[0]); return 0; }
+        return 1;
+    }
+    if (t == e_ropeJoint && prop == 8) { static_cast<b2RopeJoint*>(j)->SetMaxLength(v[0]); return 0; }
+    if (t == e_frictionJoint) {
+        b2FrictionJoint* f = static_cast<b2FrictionJoint*>(j);
+        if (prop == 9) { f->SetMaxForce(v[0]); return 0; }
+        if (prop == 10) { f->SetMaxTorque(v[0]); return 0; }
+        return 1;
+    }
+    if (t == e_motorJoint) {
+        b2MotorJoint* m = static_cast<b2MotorJoint*>(j);
+        switch (prop) {
+        case 9: m->SetMaxForce(v[0]); return 0;
+        case 10: m->SetMaxTorque(v[0]); return 0;
+        case 11: m->SetLinearOffset(b2Vec2(v[0], v[1])); return 0;
+        case 12: m->SetAngularOffset(v[0]); return 0;
+        case 13: m->SetCorrectionFactor(v[0]); return 0;
+        default: return 1;
+        }
+    }
+    if (t == e_gearJoint && prop == 14) { static_cast<b2GearJoint*>(j)->SetRatio(v[0]); return 0; }
+    return 1;
+}
 void rw_shift_origin(void* h, float x, float y)
 {
     static_cast<RefWorld*>(h)->world.ShiftOrigin(b2Vec2(x, y));

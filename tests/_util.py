@@ -221,9 +221,42 @@ def shift_script():
     return {40: [("shift", 10.0, -3.0)], 120: [("shift", -25.5, 7.25)], 200: [("shift", 0.1, 0.0)]}
 
 
+def joint_scripts():
+    """Joint setters between steps, {case: (scene factory, steps, {step: [op]})}. Op ("joint", j, prop,
+    value): prop 0 motor speed, 1 maximum motor torque (force for a prismatic joint), 2 enable motor,
+    3 enable limit, 4 limits (lower, upper), 5 length, 6 spring frequency, 7 damping ratio, 8 maximum
+    length, 9 maximum force, 10 maximum torque, 11 linear offset (x, y), 12 angular offset,
+    13 correction factor, 14 ratio."""
+    from box2dpp_gb300 import scenes
+
+    zoo = {  # joints 0, 1 wheels, 2..6 ropes, 7..9 friction, 10 motor
+        40: [("joint", 0, 0, -20.0), ("joint", 0, 1, 50.0), ("joint", 1, 2, 1.0), ("joint", 1, 0, -10.0)],
+        60: [("joint", 0, 6, 2.0), ("joint", 0, 7, 0.3)],
+        80: [("joint", 3, 8, 0.5)],
+        100: [("joint", 8, 9, 0.0), ("joint", 8, 10, 0.0)],
+        120: [("joint", 10, 11, (3.0, 2.0)), ("joint", 10, 12, 0.7), ("joint", 10, 13, 0.1),
+              ("joint", 10, 9, 200.0), ("joint", 10, 10, 100.0)],
+        160: [("joint", 0, 2, 0.0)],
+    }
+    prismatic = {  # joints 0..5 and 7 prismatic, 6 revolute
+        40: [("joint", 0, 0, 2.0), ("joint", 0, 1, 100.0), ("joint", 2, 2, 1.0)],
+        60: [("joint", 1, 4, (-0.5, 0.5)), ("joint", 3, 3, 0.0)],
+        90: [("joint", 6, 2, 1.0), ("joint", 6, 0, 3.0), ("joint", 6, 1, 200.0), ("joint", 6, 4, (-0.3, 0.3)),
+             ("joint", 6, 3, 1.0)],
+        120: [("joint", 1, 3, 0.0), ("joint", 6, 4, (-0.3, 0.3))],  # the same limits again: no change
+    }
+    mix = {  # joints 0..3 distance, 4..13 weld, 14 revolute
+        40: [("joint", 0, 5, 2.5), ("joint", 0, 6, 4.0), ("joint", 0, 7, 0.5), ("joint", 4, 6, 3.0)],
+        90: [("joint", 1, 5, 0.5), ("joint", 5, 7, 0.9)],
+    }
+    return {"joint_props_zoo": (lambda: scenes.joint_zoo(scenes.SplitMix64(6)), 220, zoo),
+            "joint_props_prismatic": (lambda: scenes.prismatic_mix(scenes.SplitMix64(5)), 200, prismatic),
+            "joint_props_mix": (lambda: scenes.joint_mix(scenes.SplitMix64(3)), 160, mix)}
+
+
 def apply_ops(world, ops, w: int = 0):
-    """Applies destroy_script(), settings_script(), body_props_script(), fixture_props_script() and
-    shift_script() ops to an oracle world or a device world (same
+    """Applies destroy_script(), settings_script(), body_props_script(), fixture_props_script(),
+    shift_script() and joint_scripts() ops to an oracle world or a device world (same
     method names); returns the destruction listener's calls of the ops as (kind, index), in order."""
     calls = []
     for op in ops:
@@ -232,6 +265,8 @@ def apply_ops(world, ops, w: int = 0):
             world.set_settings(*args) if w == 0 else world.set_settings(*args, w=w)
         elif op[0] == "clear_forces":
             world.clear_forces() if w == 0 else world.clear_forces(w)
+        elif op[0] == "joint":
+            world.joint_set(op[1], op[2], op[3]) if w == 0 else world.joint_set(op[1], op[2], op[3], w)
         elif op[0] == "shift":
             world.shift_origin(op[1], op[2]) if w == 0 else world.shift_origin(op[1], op[2], w)
         elif op[0] == "fix":

@@ -89,13 +89,15 @@ def scripted_cases():
     """Trajectory cases with b2World changes between steps: (name, scene factory, steps, ops by step).
     The ops (tests/_util.py destroy_script) destroy bodies, joints and fixtures and create bodies."""
     sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
-    from tests._util import body_props_script, destroy_script, fixture_props_script, settings_script, shift_script
+    from tests._util import (body_props_script, destroy_script, fixture_props_script, joint_scripts, settings_script,
+                             shift_script)
 
     return [("destroy_mix", lambda: scenes.destroy_mix(scenes.SplitMix64(5)), 200, destroy_script()),
             ("settings_mix", lambda: scenes.destroy_mix(scenes.SplitMix64(7)), 340, settings_script()),
             ("body_props", lambda: scenes.destroy_mix(scenes.SplitMix64(11)), 320, body_props_script()),
             ("fixture_props", lambda: scenes.destroy_mix(scenes.SplitMix64(13)), 300, fixture_props_script()),
-            ("shift_origin", lambda: scenes.pulley_mouse(scenes.SplitMix64(4)), 260, shift_script())]
+            ("shift_origin", lambda: scenes.pulley_mouse(scenes.SplitMix64(4)), 260, shift_script())] + \
+        [(name, make, steps, script) for name, (make, steps, script) in joint_scripts().items()]
 
 
 def run_scripted(scene, steps, script, trig):

@@ -520,3 +520,77 @@ def test_cpp_body_props_match_oracle(gpu, tmp_path):
     for i, got in bodies.items():
         want = ob[i][[0, 1, 2, 5, 6, 7]]
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), i
+
+
+JS_SRC = os.path.join(ROOT, "tests", "cpp", "joint_setters.cpp")
+
+
+def _compile_js(tmp_path):
+    lib = _lib.library_path()
+    exe = str(tmp_path / "joint_setters")
+    libdir = os.path.dirname(lib)
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "include"), JS_SRC, "-o", exe,
+           "-L", libdir, "-lbox2d_gb300", f"-Wl,-rpath,{libdir}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return exe
+
+
+def test_cpp_joint_setters_compile(tmp_path):
+    _compile_js(tmp_path)
+
+
+def _js_scene():
+    s = scenes.Scene(name="joint_setters")
+    g = s.body(scenes.STATIC, 0.0, 0.0)
+    s.fixture(g, scenes.EDGE, [-20.0, 0.0, 20.0, 0.0, 0, 0, 0, 0, 0, 0])
+    p = s.body(scenes.DYNAMIC, 0.0, 5.0)
+    s.fixture(p, scenes.BOX, [0.25, 1.0], 2, density=1.0)
+    s.revolute(g, p, [0.0, 6.0], [0.0, 1.0])
+    sl = s.body(scenes.DYNAMIC, 5.0, 2.0)
+    s.fixture(sl, scenes.BOX, [0.5, 0.25], 2, density=1.0)
+    s.prismatic(g, sl, [5.0, 2.0], [0.0, 0.0], [1.0, 0.0], lower=-1.0, upper=1.0, flags=1)
+    ch = s.body(scenes.DYNAMIC, -8.0, 1.5)
+    s.fixture(ch, scenes.BOX, [1.0, 0.25], 2, density=1.0)
+    wh = s.body(scenes.DYNAMIC, -8.5, 0.6)
+    s.fixture(wh, scenes.CIRCLE, [0.0, 0.0, 0.4], density=1.0)
+    s.wheel(ch, wh, [-0.5, -0.9], [0.0, 0.0], [0.0, 1.0], max_motor_torque=20.0, motor_speed=0.0, frequency_hz=4.0,
+            damping_ratio=0.7, flags=2)
+    c1 = s.body(scenes.DYNAMIC, 10.0, 6.0)
+    s.fixture(c1, scenes.CIRCLE, [0.0, 0.0, 0.3], density=1.0)
+    c2 = s.body(scenes.DYNAMIC, 11.0, 6.0)
+    s.fixture(c2, scenes.CIRCLE, [0.0, 0.0, 0.3], density=1.0)
+    s.distance(c1, c2, [0.0, 0.0], [0.0, 0.0], 1.0)
+    h = s.body(scenes.DYNAMIC, -3.0, 3.0)
+    s.fixture(h, scenes.BOX, [0.3, 0.3], 2, density=1.0)
+    s.motor(g, h, [-3.0, 3.0], 0.0, 100.0, 10.0, 0.3)
+    return s
+
+
+@pytest.mark.gpu
+def test_cpp_joint_setters_match_oracle(gpu, tmp_path):
+    """The typed joints of the C++ mirror (revolute, prismatic, wheel, distance, motor) and their
+    setters against the CPU oracle with the same changes: every body bit for bit."""
+    exe = _compile_js(tmp_path)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.strip().splitlines()
+    rev = lines[0].split()
+    assert rev[1:3] == ["1", "1"] and [float.fromhex(v) for v in rev[3:]] == [2.0, 100.0, -0.5, 0.5]
+    o = oracle.OracleWorld(_js_scene(), "port", "project")
+    for _ in range(30):
+        o.step(1.0 / 60.0, 8, 3)
+    for j, prop, v in [(0, 2, 1.0), (0, 0, 2.0), (0, 1, 100.0), (0, 4, (-0.5, 0.5)), (0, 3, 1.0),
+                       (1, 2, 1.0), (1, 0, -1.5), (1, 1, 50.0), (1, 4, (-2.0, 0.5)),
+                       (2, 0, -15.0), (2, 1, 60.0), (2, 6, 2.5), (2, 7, 0.4),
+                       (3, 5, 1.6), (3, 6, 3.0), (3, 7, 0.2),
+                       (4, 11, (-2.0, 4.0)), (4, 12, 0.5), (4, 9, 300.0), (4, 10, 200.0), (4, 13, 0.5)]:
+        o.joint_set(j, prop, v)
+    for _ in range(60):
+        o.step(1.0 / 60.0, 8, 3)
+    ob = o.bodies()
+    for ln in lines[1:]:
+        parts = ln.split()
+        i = int(parts[1])
+        got = np.array([float.fromhex(v) for v in parts[2:]], dtype=np.float32)
+        assert np.array_equal(got.view(np.uint32), ob[i][[0, 1, 2, 5, 6, 7]].view(np.uint32)), i

@@ -234,6 +234,29 @@ def test_port_shift_origin_case_matches_reference(trig):
     assert np.array_equal(fat.view(np.uint32), g["proxy_fat"].view(np.uint32))
 
 
+@pytest.mark.parametrize("case", ["joint_props_zoo", "joint_props_prismatic", "joint_props_mix"])
+@pytest.mark.parametrize("trig", ["project", "libm"])
+def test_port_joint_props_cases_match_reference(case, trig):
+    """Joint setters between steps (motor speed, torque and force, motor and limit switches, limits,
+    distance length, springs, rope length, friction and motor-joint forces, offsets and correction):
+    per-step state as the reference."""
+    import platform
+
+    from tests._util import apply_ops, digest, joint_scripts
+
+    make, _, script = joint_scripts()[case]
+    g = golden(f"{case}_{trig}")
+    w = oracle.OracleWorld(make(), "port", trig)
+    for s in range(1, int(g["steps"]) + 1):
+        if s in script:
+            apply_ops(w, script[s])
+        w.step()
+        if not np.array_equal(digest(w.bodies(), *w.contacts()), g["digests"][s - 1]):
+            if trig == "libm" and platform.machine() != "x86_64":
+                pytest.skip("libm trig differs on this machine")
+            raise AssertionError(f"first divergence at step {s}")
+
+
 @pytest.mark.parametrize("trig", ["project", "libm"])
 def test_port_settings_case_matches_reference(trig):
     """b2World settings changed between steps (gravity, sleep off and on, warm starting, continuous
