@@ -222,7 +222,7 @@ def shift_script():
 
 
 def joint_scripts():
-    """Joint setters between steps, {case: (scene factory, steps, {step: [op]})}. Op ("joint", j, prop,
+    """Joint setters between steps, {case: (scene factory, steps, {step: [op]})}. Op ("jset", j, prop,
     value): prop 0 motor speed, 1 maximum motor torque (force for a prismatic joint), 2 enable motor,
     3 enable limit, 4 limits (lower, upper), 5 length, 6 spring frequency, 7 damping ratio, 8 maximum
     length, 9 maximum force, 10 maximum torque, 11 linear offset (x, y), 12 angular offset,
@@ -230,24 +230,24 @@ def joint_scripts():
     from box2dpp_gb300 import scenes
 
     zoo = {  # joints 0, 1 wheels, 2..6 ropes, 7..9 friction, 10 motor
-        40: [("joint", 0, 0, -20.0), ("joint", 0, 1, 50.0), ("joint", 1, 2, 1.0), ("joint", 1, 0, -10.0)],
-        60: [("joint", 0, 6, 2.0), ("joint", 0, 7, 0.3)],
-        80: [("joint", 3, 8, 0.5)],
-        100: [("joint", 8, 9, 0.0), ("joint", 8, 10, 0.0)],
-        120: [("joint", 10, 11, (3.0, 2.0)), ("joint", 10, 12, 0.7), ("joint", 10, 13, 0.1),
-              ("joint", 10, 9, 200.0), ("joint", 10, 10, 100.0)],
-        160: [("joint", 0, 2, 0.0)],
+        40: [("jset", 0, 0, -20.0), ("jset", 0, 1, 50.0), ("jset", 1, 2, 1.0), ("jset", 1, 0, -10.0)],
+        60: [("jset", 0, 6, 2.0), ("jset", 0, 7, 0.3)],
+        80: [("jset", 3, 8, 0.5)],
+        100: [("jset", 8, 9, 0.0), ("jset", 8, 10, 0.0)],
+        120: [("jset", 10, 11, (3.0, 2.0)), ("jset", 10, 12, 0.7), ("jset", 10, 13, 0.1),
+              ("jset", 10, 9, 200.0), ("jset", 10, 10, 100.0)],
+        160: [("jset", 0, 2, 0.0)],
     }
     prismatic = {  # joints 0..5 and 7 prismatic, 6 revolute
-        40: [("joint", 0, 0, 2.0), ("joint", 0, 1, 100.0), ("joint", 2, 2, 1.0)],
-        60: [("joint", 1, 4, (-0.5, 0.5)), ("joint", 3, 3, 0.0)],
-        90: [("joint", 6, 2, 1.0), ("joint", 6, 0, 3.0), ("joint", 6, 1, 200.0), ("joint", 6, 4, (-0.3, 0.3)),
-             ("joint", 6, 3, 1.0)],
-        120: [("joint", 1, 3, 0.0), ("joint", 6, 4, (-0.3, 0.3))],  # the same limits again: no change
+        40: [("jset", 0, 0, 2.0), ("jset", 0, 1, 100.0), ("jset", 2, 2, 1.0)],
+        60: [("jset", 1, 4, (-0.5, 0.5)), ("jset", 3, 3, 0.0)],
+        90: [("jset", 6, 2, 1.0), ("jset", 6, 0, 3.0), ("jset", 6, 1, 200.0), ("jset", 6, 4, (-0.3, 0.3)),
+             ("jset", 6, 3, 1.0)],
+        120: [("jset", 1, 3, 0.0), ("jset", 6, 4, (-0.3, 0.3))],  # the same limits again: no change
     }
     mix = {  # joints 0..3 distance, 4..13 weld, 14 revolute
-        40: [("joint", 0, 5, 2.5), ("joint", 0, 6, 4.0), ("joint", 0, 7, 0.5), ("joint", 4, 6, 3.0)],
-        90: [("joint", 1, 5, 0.5), ("joint", 5, 7, 0.9)],
+        40: [("jset", 0, 5, 2.5), ("jset", 0, 6, 4.0), ("jset", 0, 7, 0.5), ("jset", 4, 6, 3.0)],
+        90: [("jset", 1, 5, 0.5), ("jset", 5, 7, 0.9)],
     }
     return {"joint_props_zoo": (lambda: scenes.joint_zoo(scenes.SplitMix64(6)), 220, zoo),
             "joint_props_prismatic": (lambda: scenes.prismatic_mix(scenes.SplitMix64(5)), 200, prismatic),
@@ -265,7 +265,7 @@ def apply_ops(world, ops, w: int = 0):
             world.set_settings(*args) if w == 0 else world.set_settings(*args, w=w)
         elif op[0] == "clear_forces":
             world.clear_forces() if w == 0 else world.clear_forces(w)
-        elif op[0] == "joint":
+        elif op[0] == "jset":
             world.joint_set(op[1], op[2], op[3]) if w == 0 else world.joint_set(op[1], op[2], op[3], w)
         elif op[0] == "shift":
             world.shift_origin(op[1], op[2]) if w == 0 else world.shift_origin(op[1], op[2], w)
