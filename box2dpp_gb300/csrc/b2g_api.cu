@@ -3145,6 +3145,65 @@ gb_status SetJointPropertyHost(HWorld& W, int ji, int prop, const float* v)
 
 extern "C" {
 
+gb_status gb_get_joint_reaction(gb_world* g, int w, int joint, float inv_dt, float* out)
+{
+    if (!g || w < 0 || w >= (int)g->worlds.size() || !out) return GB_ERR_INVALID;
+    const HWorld& W = g->worlds[w];
+    if (joint < 0 || joint >= (int)W.joints.size() || W.joints[joint].bodyA == kNullIdx) return GB_ERR_INVALID;
+    Joint j = W.joints[joint];
+    if (g->onDevice) {
+        // the impulses and axes of the last step live on the device
+        GB_CUDA(cudaStreamSynchronize(g->stream));
+        GB_CUDA(cudaMemcpy(&j, g->batch.joint + g->desc[w].jointBase + joint, sizeof(Joint), cudaMemcpyDeviceToHost));
+    }
+    // b2Joint::GetReactionForce, GetReactionTorque of each type (Dynamics/Joints/*.cpp), in the
+    // reference's operation order
+    Vec2 F = V(0.0f, 0.0f);
+    float T = 0.0f;
+    switch (j.type) {
+    case kJointRevolute:
+    case kJointWeld:
+    case kJointFriction:
+    case kJointMotor:
+        F = V(inv_dt * j.impulse[0], inv_dt * j.impulse[1]);
+        T = inv_dt * j.impulse[2];
+        break;
+    case kJointPrismatic: {
+        const float k = j.motorImpulse + j.impulse[2];
+        F = V(inv_dt * (j.impulse[0] * j.perp.x + k * j.u.x), inv_dt * (j.impulse[0] * j.perp.y + k * j.u.y));
+        T = inv_dt * j.impulse[1];
+        break;
+    }
+    case kJointDistance:
+    case kJointRope: {
+        const float s = inv_dt * j.impulse[0];
+        F = V(s * j.u.x, s * j.u.y);
+        break;
+    }
+    case kJointWheel:
+        F = V(inv_dt * (j.impulse[0] * j.ay.x + j.springImpulse * j.ax.x),
+              inv_dt * (j.impulse[0] * j.ay.y + j.springImpulse * j.ax.y));
+        T = inv_dt * j.motorImpulse;
+        break;
+    case kJointMouse:
+        F = V(inv_dt * j.impulse[0], inv_dt * j.impulse[1]);
+        T = inv_dt * 0.0f;
+        break;
+    case kJointPulley:
+        F = V(inv_dt * (j.impulse[0] * j.uB.x), inv_dt * (j.impulse[0] * j.uB.y));
+        break;
+    case kJointGear:
+        F = V(inv_dt * (j.impulse[0] * j.JvAC.x), inv_dt * (j.impulse[0] * j.JvAC.y));
+        T = inv_dt * (j.impulse[0] * j.JwA);
+        break;
+    default: break;
+    }
+    out[0] = F.x;
+    out[1] = F.y;
+    out[2] = T;
+    return GB_OK;
+}
+
 gb_status gb_joint_set(gb_world* g, int w, int joint, int prop, const float* v)
 {
     if (!v) return GB_ERR_INVALID;

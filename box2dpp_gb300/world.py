@@ -187,6 +187,14 @@ class World:
                    "gb_body_set")
         return calls[:min(n.value, 256)]
 
+    def joint_reaction(self, joint: int, inv_dt: float, w: int = 0) -> np.ndarray:
+        """b2Joint::GetReactionForce and GetReactionTorque after the last step: (force x, force y,
+        torque) as float32 (gb_get_joint_reaction)."""
+        out = np.zeros(3, dtype=np.float32)
+        _lib.check(self.lib.gb_get_joint_reaction(self.h, int(w), int(joint), float(inv_dt), out),
+                   "gb_get_joint_reaction")
+        return out
+
     def joint_set(self, joint: int, prop: int, value=0.0, w: int = 0) -> None:
         """A joint setter between steps (gb_joint_set; prop GB_JOINT_*, value a number or a pair)."""
         v = np.zeros(4, dtype=np.float32)

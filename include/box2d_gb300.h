@@ -225,6 +225,11 @@ gb_status gb_body_set(gb_world* world, int w, int body, int prop, const float* v
 #define GB_JOINT_RATIO 14
 gb_status gb_joint_set(gb_world* world, int w, int joint, int prop, const float* v);
 
+/* b2Joint::GetReactionForce(inv_dt) and GetReactionTorque(inv_dt) of any joint type
+ * (Box2D/Dynamics/Joints/*.cpp) after the last step: out[0..1] the force on body B at the anchor,
+ * out[2] the torque. Waits for the step in flight. */
+gb_status gb_get_joint_reaction(gb_world* world, int w, int joint, float inv_dt, float* out);
+
 /* b2World::ShiftOrigin (Box2D/Dynamics/b2World.cpp:1261-1282) of world w between steps: bodies, the
  * mouse joints' targets, the pulleys' ground anchors and the broadphase's boxes move by -(x, y). */
 gb_status gb_world_shift_origin(gb_world* world, int w, float x, float y);

@@ -518,6 +518,9 @@ public:
     int GetIndex() const { return m_index; }
     b2Body* GetBodyA() const { return m_a; }
     b2Body* GetBodyB() const { return m_b; }
+    // b2Joint::GetReactionForce / GetReactionTorque (Box2D/Dynamics/Joints/*.cpp) after the last step
+    b2Vec2 GetReactionForce(float inv_dt) const;
+    float GetReactionTorque(float inv_dt) const;
 
 protected:
     friend class b2World;
@@ -912,6 +915,12 @@ public:
         std::vector<int> calls;
         if (Destroy(gb_destroy_joint, joint->m_index, calls) != GB_OK) return;
         joint->m_alive = false;
+    }
+    // a joint's reaction force and torque (gb_get_joint_reaction)
+    void JointReaction(int index, float inv_dt, float* out)
+    {
+        out[0] = out[1] = out[2] = 0.0f;
+        if (Handle()) gb_get_joint_reaction(m_h, 0, index, inv_dt, out);
     }
     // one gb_joint_set call (the typed joints' setters)
     bool SetJointProperty(b2Joint* j, int prop, float v0, float v1)
@@ -1530,6 +1539,18 @@ inline void b2Body::SetLinearDamping(float d) { m_world->SetBodyProperty(this, G
 inline void b2Body::SetAngularDamping(float d) { m_world->SetBodyProperty(this, GB_BODY_ANGULAR_DAMPING, d); }
 inline void b2Body::SetGravityScale(float scale) { m_world->SetBodyProperty(this, GB_BODY_GRAVITY_SCALE, scale); }
 inline bool b2Joint::Set(int prop, float v0, float v1) { return m_world->SetJointProperty(this, prop, v0, v1); }
+inline b2Vec2 b2Joint::GetReactionForce(float inv_dt) const
+{
+    float out[3];
+    m_world->JointReaction(m_index, inv_dt, out);
+    return b2Vec2(out[0], out[1]);
+}
+inline float b2Joint::GetReactionTorque(float inv_dt) const
+{
+    float out[3];
+    m_world->JointReaction(m_index, inv_dt, out);
+    return out[2];
+}
 inline void b2Fixture::SetFriction(float friction)
 {
     if (m_body->GetWorld()->SetFixtureProperty(this, GB_FIXTURE_FRICTION, friction)) m_def.friction = friction;

@@ -97,6 +97,7 @@ def _declare(lib, p: str) -> None:
     sig["fixture_set"] = (None, [vp, C.c_int, C.c_int, _f32p])
     sig["shift_origin"] = (None, [vp, C.c_float, C.c_float])
     sig["joint_set"] = (C.c_int, [vp, C.c_int, C.c_int, _f32p])
+    sig["joint_reaction"] = (None, [vp, C.c_int, C.c_float, _f32p])
     for kind in ("body", "joint", "fixture"):
         sig["destroy_" + kind] = (C.c_int, [vp, C.c_int, _i32p, C.c_int])
     if p == "rw_":
@@ -206,6 +207,12 @@ class OracleWorld:
         and SetAutoClearForces between steps."""
         self._fn("set_settings")(self.h, float(gravity[0]), float(gravity[1]), int(allow_sleep), int(warm_starting),
                                  int(continuous), int(sub_stepping), int(auto_clear_forces))
+
+    def joint_reaction(self, joint: int, inv_dt: float) -> np.ndarray:
+        """b2Joint::GetReactionForce and GetReactionTorque: (force x, force y, torque) as float32."""
+        out = np.zeros(3, dtype=np.float32)
+        self._fn("joint_reaction")(self.h, int(joint), float(inv_dt), out)
+        return out
 
     def joint_set(self, joint: int, prop: int, value=0.0) -> None:
         """A joint setter between steps (prop: the C-ABI's GB_JOINT_*; value a number or a pair)."""

@@ -117,6 +117,55 @@ void po_set_settings(void* h, float gx, float gy, int allowSleep, int warm, int 
     if (autoClear) w->wflags |= 0x4u;
     else w->wflags &= ~0x4u;
 }
+// b2Joint::GetReactionForce and GetReactionTorque of every joint type (Dynamics/Joints/*.cpp), with
+// the reference's operation order: out = force x, force y, torque
+void po_joint_reaction(void* h, int ji, float inv_dt, float* out)
+{
+    const Joint& j = static_cast<World*>(h)->joints[ji];
+    Vec2 F = V(0.0f, 0.0f);
+    float T = 0.0f;
+    switch (j.type) {
+    case kRevoluteJoint:
+    case kWeldJoint:
+    case kFrictionJoint:
+    case kMotorJoint:
+        F = V(inv_dt * j.impulse[0], inv_dt * j.impulse[1]);
+        T = inv_dt * j.impulse[2];
+        break;
+    case kPrismaticJoint: {
+        const float k = j.motorImpulse + j.impulse[2];
+        F = V(inv_dt * (j.impulse[0] * j.perp.x + k * j.u.x), inv_dt * (j.impulse[0] * j.perp.y + k * j.u.y));
+        T = inv_dt * j.impulse[1];
+        break;
+    }
+    case kDistanceJoint:
+    case kRopeJoint: {
+        const float s = inv_dt * j.impulse[0];
+        F = V(s * j.u.x, s * j.u.y);
+        break;
+    }
+    case kWheelJoint:
+        F = V(inv_dt * (j.impulse[0] * j.ay.x + j.springImpulse * j.ax.x),
+              inv_dt * (j.impulse[0] * j.ay.y + j.springImpulse * j.ax.y));
+        T = inv_dt * j.motorImpulse;
+        break;
+    case kMouseJoint:
+        F = V(inv_dt * j.impulse[0], inv_dt * j.impulse[1]);
+        T = inv_dt * 0.0f;
+        break;
+    case kPulleyJoint:
+        F = V(inv_dt * (j.impulse[0] * j.uB.x), inv_dt * (j.impulse[0] * j.uB.y));
+        break;
+    case kGearJoint:
+        F = V(inv_dt * (j.impulse[0] * j.JvAC.x), inv_dt * (j.impulse[0] * j.JvAC.y));
+        T = inv_dt * (j.impulse[0] * j.JwA);
+        break;
+    default: break;
+    }
+    out[0] = F.x;
+    out[1] = F.y;
+    out[2] = T;
+}
 int po_joint_set(void* h, int j, int prop, const float* v)
 {
     return static_cast<World*>(h)->SetJointProperty(j, prop, v);

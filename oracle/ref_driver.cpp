@@ -457,6 +457,14 @@ void rw_body_set(void* h, int b, int prop, const float* v)
     default: break;
     }
 }
+void rw_joint_reaction(void* h, int ji, float inv_dt, float* out)
+{
+    const b2Joint* j = static_cast<RefWorld*>(h)->joints[ji];
+    const b2Vec2 F = j->GetReactionForce(inv_dt);
+    out[0] = F.x;
+    out[1] = F.y;
+    out[2] = j->GetReactionTorque(inv_dt);
+}
 // joint setters through the reference's own classes; 1 when the joint type has no such setter
 int rw_joint_set(void* h, int ji, int prop, const float* v)
 {

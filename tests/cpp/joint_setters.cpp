@@ -2,8 +2,9 @@
 // so on, as user code of the reference writes it): a box pendulum on a revolute joint, a box slider on
 // a prismatic joint with limits, a car wheel on a wheel joint, two circles on a distance joint and a
 // box held by a motor joint, all over an edge ground. 30 steps, then motors switched on and driven,
-// limits set, springs, length and offsets changed; 60 more steps. Prints the revolute joint's getters
-// and every body's position, angle and velocities as hex floats.
+// limits set, springs, length and offsets changed; 60 more steps. Prints the revolute joint's getters,
+// every joint's reaction force and torque, and every body's position, angle and velocities as hex
+// floats.
 #include <cstdio>
 
 #include "box2d_gb300.hpp"
@@ -132,6 +133,11 @@ int main()
 
     std::printf("revolute %d %d %a %a %a %a\n", rj->IsMotorEnabled() ? 1 : 0, rj->IsLimitEnabled() ? 1 : 0,
                 rj->GetMotorSpeed(), rj->GetMaxMotorTorque(), rj->GetLowerLimit(), rj->GetUpperLimit());
+    const b2Joint* joints[5] = {rj, pj, wj, dj, mj};
+    for (int k = 0; k < 5; ++k) {
+        const b2Vec2 f = joints[k]->GetReactionForce(60.0f);
+        std::printf("reaction %d %a %a %a\n", k, f.x, f.y, joints[k]->GetReactionTorque(60.0f));
+    }
     for (size_t i = 0; i < bodies.size(); ++i) {
         const b2Vec2 p = bodies[i]->GetPosition(), v = bodies[i]->GetLinearVelocity();
         std::printf("body %d %a %a %a %a %a %a\n", (int)i, p.x, p.y, bodies[i]->GetAngle(), v.x, v.y,

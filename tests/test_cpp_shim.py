@@ -589,8 +589,14 @@ def test_cpp_joint_setters_match_oracle(gpu, tmp_path):
     for _ in range(60):
         o.step(1.0 / 60.0, 8, 3)
     ob = o.bodies()
+    reactions = 0
     for ln in lines[1:]:
         parts = ln.split()
         i = int(parts[1])
         got = np.array([float.fromhex(v) for v in parts[2:]], dtype=np.float32)
+        if parts[0] == "reaction":
+            assert np.array_equal(got.view(np.uint32), o.joint_reaction(i, 60.0).view(np.uint32)), ("joint", i)
+            reactions += 1
+            continue
         assert np.array_equal(got.view(np.uint32), ob[i][[0, 1, 2, 5, 6, 7]].view(np.uint32)), i
+    assert reactions == 5

@@ -38,3 +38,21 @@ def test_joint_set_rejects_what_a_type_does_not_have(gpu):
     w2 = World(scenes.prismatic_mix(scenes.SplitMix64(5)))
     with pytest.raises(GbError):
         w2.joint_set(0, 4, (1.0, -1.0))  # lower above upper
+
+
+@pytest.mark.parametrize("name,seed", [("joint_zoo", 6), ("prismatic_mix", 5), ("joint_mix", 3), ("pulley_mouse", 4),
+                                       ("gears", 8)])
+def test_joint_reactions_match_oracle(gpu, name, seed):
+    """b2Joint::GetReactionForce / GetReactionTorque of every joint after 50 device steps, against the
+    CPU restatement (itself bit-exact with the reference)."""
+    import oracle
+
+    sc = getattr(scenes, name)(scenes.SplitMix64(seed))
+    w = World(sc)
+    o = oracle.OracleWorld(sc, "port", "project")
+    for _ in range(50):
+        w.step(DT, VI, PI)
+        o.step(DT, VI, PI)
+    for j in range(len(sc.joints)):
+        a, b = w.joint_reaction(j, 60.0), o.joint_reaction(j, 60.0)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (j, a, b)

@@ -315,3 +315,30 @@ def test_port_body_info_matches_reference():
             for b in range(len(sc.bodies)):
                 (a, fa), (c, fc) = p.body_info(b), r.body_info(b)
                 assert fa == fc and np.array_equal(a.view(np.uint32), c.view(np.uint32)), (s, b, a, c)
+
+
+JOINT_SCENES = ["joint_zoo", "prismatic_mix", "joint_mix", "pulley_mouse", "gears"]
+
+
+def _joint_scene(name):
+    from box2dpp_gb300 import scenes
+
+    seeds = {"joint_zoo": 6, "prismatic_mix": 5, "joint_mix": 3, "pulley_mouse": 4, "gears": 8}
+    return getattr(scenes, name)(scenes.SplitMix64(seeds[name]))
+
+
+@pytest.mark.parametrize("name", JOINT_SCENES)
+def test_port_joint_reactions_match_reference(name):
+    """b2Joint::GetReactionForce and GetReactionTorque of every joint type after 50 steps, restatement
+    against the reference, bit for bit."""
+    if not oracle.reference_available():
+        pytest.skip("reference tree not present")
+    sc = _joint_scene(name)
+    p = oracle.OracleWorld(sc, "port", "project")
+    r = oracle.OracleWorld(sc, "reference", "project")
+    for _ in range(50):
+        p.step()
+        r.step()
+    for j in range(len(sc.joints)):
+        a, b = p.joint_reaction(j, 60.0), r.joint_reaction(j, 60.0)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (j, a, b)
