@@ -2972,12 +2972,46 @@ bool LoadWorld(HWorld& W, const unsigned char* p, const unsigned char* end)
             return false;
     for (int x : N.pfix)
         if (!inRange(x, nf)) return false;
+    // the free list of tree node ids (a corrupt id would size the proxy columns)
+    if (N.nodeFresh > 2 * np + 2) return false;
+    for (int x : N.nodeFree)
+        if (x < -1 || x >= N.nodeFresh) return false;
+    for (const HFixture& f : N.fixtures)
+        if (f.shape.type < 0 || f.shape.type > 3) return false;
+    // joint list links and edges (edge id = 2 x joint + side)
+    for (const Joint& j : N.joints) {
+        if (j.bodyA == kNullIdx) continue;
+        if (!inRange(j.prev, nj) || !inRange(j.next, nj)) return false;
+        for (int side = 0; side < 2; ++side)
+            if (!inRange(j.ePrev[side], 2 * nj) || !inRange(j.eNext[side], 2 * nj)) return false;
+        if (j.type == kJointGear && (!inRange(j.bodyC, nb) || !inRange(j.bodyD, nb))) return false;
+    }
+    for (const HBody& b : N.bodies)
+        if (!inRange(b.jointList, 2 * nj)) return false;
     if (N.hasState) {
         const size_t nc = C.ci.size();
         if (C.ce.size() != nc || C.mh.size() != nc || C.cp.size() != nc || C.mv.size() != nc ||
             C.mp0.size() != nc || C.mp1.size() != nc || C.order.size() != nc || C.cnext.size() != nc ||
-            N.state.contactCount < 0 || (size_t)N.state.contactCount > nc)
+            N.state.contactCount < 0 || (size_t)N.state.contactCount > nc || nc > (1u << 28))
             return false;
+        const int ncap = (int)nc;
+        // contact slots, edges (2 x slot + side) and list: every index the step follows stays in range
+        if (!inRange(N.state.freeContact, ncap)) return false;
+        for (int c = 0; c < ncap; ++c) {
+            if (!inRange(C.cnext[c], ncap)) return false;
+            const int4 e = C.ce[c];
+            if (!inRange(e.x, 2 * ncap) || !inRange(e.y, 2 * ncap) || !inRange(e.z, 2 * ncap) || !inRange(e.w, 2 * ncap))
+                return false;
+        }
+        for (int k = 0; k < N.state.contactCount; ++k) {
+            const int c = C.order[k];
+            if (c < 0 || c >= ncap) return false;
+            if (C.ci[c].y < 0 || C.ci[c].y >= nf || C.ci[c].z < 0 || C.ci[c].z >= nf) return false;
+            // manifold type and point count
+            if (C.mh[c].x < 0 || C.mh[c].x > 2 || C.mh[c].y < 0 || C.mh[c].y > 2) return false;
+        }
+        for (const HBody& b : N.bodies)
+            if (!inRange(b.contactList, 2 * ncap)) return false;
     }
     N.trackTree = W.trackTree;
     N.treeIncomplete = W.trackTree && !hasTree;

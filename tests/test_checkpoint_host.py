@@ -73,3 +73,27 @@ def test_foreign_and_corrupt_checkpoints_are_refused():
         v.restore(bytes(bad_head), 0)
     with pytest.raises(GbError):
         v.restore(bytes(data) + b"\0", 0)  # trailing bytes
+
+
+def test_corrupt_bytes_never_break_the_host():
+    """Random byte corruption anywhere in a checkpoint: the restore is refused, or it is accepted only
+    with every index the step follows in range, and the world can be checkpointed again."""
+    import random
+
+    w = World(scenes.destroy_mix(scenes.SplitMix64(5)))
+    data = w.checkpoint()
+    rng = random.Random(7)
+    refused = accepted = 0
+    for _ in range(300):
+        blob = bytearray(data)
+        for _ in range(rng.randint(1, 4)):
+            blob[rng.randrange(len(blob))] = rng.randrange(256)
+        v = World([scenes.pyramid(2)])
+        try:
+            v.restore(bytes(blob), 0)
+        except GbError:
+            refused += 1
+            continue
+        accepted += 1
+        assert len(v.checkpoint(0)) == len(blob)
+    assert refused > 0 and accepted > 0
