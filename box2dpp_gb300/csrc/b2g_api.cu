@@ -3179,6 +3179,63 @@ gb_status SetJointPropertyHost(HWorld& W, int ji, int prop, const float* v)
 
 extern "C" {
 
+gb_status gb_fixture_query(gb_world* g, int w, int fixture, int op, const float* in, float* out)
+{
+    if (!g || w < 0 || w >= (int)g->worlds.size() || !out || (op != 2 && !in) || op < 0 || op > 2) return GB_ERR_INVALID;
+    const HWorld& W = g->worlds[w];
+    if (fixture < 0 || fixture >= (int)W.fixtures.size() || W.fixtures[fixture].body == kNullIdx) return GB_ERR_INVALID;
+    const HFixture& fx = W.fixtures[fixture];
+    const Shape& sh = fx.shape;
+    Xf xf = W.bodies[fx.body].xf;
+    float4 aabb = fx.aabb;
+    if (g->onDevice) {
+        // the body's transform and the proxy box of the last step live on the device
+        const WorldDesc& d = g->desc[w];
+        float4 x;
+        GB_CUDA(cudaStreamSynchronize(g->stream));
+        GB_CUDA(cudaMemcpy(&x, g->batch.xf + d.bodyBase + fx.body, sizeof(float4), cudaMemcpyDeviceToHost));
+        GB_CUDA(cudaMemcpy(&aabb, g->batch.faabb + d.fixBase + fixture, sizeof(float4), cudaMemcpyDeviceToHost));
+        xf.p = V(x.x, x.y);
+        xf.q.s = x.z;
+        xf.q.c = x.w;
+    }
+    out[0] = out[1] = out[2] = out[3] = 0.0f;
+    if (op == 0) {
+        // b2Shape::TestPoint (Collision/Shapes/b2CircleShape.cpp:37-42, b2PolygonShape.cpp:255-268;
+        // edges contain no point)
+        const Vec2 p = V(in[0], in[1]);
+        bool inside = false;
+        if (sh.type == kCircle) {
+            const Vec2 center = xf.p + Mul(xf.q, sh.v[0]);
+            const Vec2 dd = p - center;
+            inside = Dot(dd, dd) <= sh.radius * sh.radius;
+        } else if (sh.type == kPolygon) {
+            const Vec2 local = MulT(xf.q, p - xf.p);
+            inside = true;
+            for (int i = 0; i < sh.count && inside; ++i)
+                if (Dot(sh.n[i], local - sh.v[i]) > 0.0f) inside = false;
+        }
+        out[0] = inside ? 1.0f : 0.0f;
+    } else if (op == 1) {
+        // b2Fixture::RayCast of the first child (b2Fixture.h:333-336)
+        float fraction = 0.0f;
+        Vec2 normal = V(0.0f, 0.0f);
+        if (RayCastShape(sh, xf, V(in[0], in[1]), V(in[2], in[3]), in[4], &fraction, &normal)) {
+            out[0] = 1.0f;
+            out[1] = normal.x;
+            out[2] = normal.y;
+            out[3] = fraction;
+        }
+    } else {
+        // b2Fixture::GetAABB (b2Fixture.h:338-342): the proxy's swept box of the last synchronisation
+        out[0] = aabb.x;
+        out[1] = aabb.y;
+        out[2] = aabb.z;
+        out[3] = aabb.w;
+    }
+    return GB_OK;
+}
+
 gb_status gb_get_joint_reaction(gb_world* g, int w, int joint, float inv_dt, float* out)
 {
     if (!g || w < 0 || w >= (int)g->worlds.size() || !out) return GB_ERR_INVALID;

@@ -187,6 +187,15 @@ class World:
                    "gb_body_set")
         return calls[:min(n.value, 256)]
 
+    def fixture_query(self, fixture: int, op: int, inp=(), w: int = 0) -> np.ndarray:
+        """b2Fixture::TestPoint (op 0), RayCast (op 1: p1, p2, maxFraction -> hit, normal, fraction) or
+        GetAABB (op 2) at the body's current transform (gb_fixture_query), as float32."""
+        v = np.zeros(8, dtype=np.float32)
+        v[:len(inp)] = inp
+        out = np.zeros(4, dtype=np.float32)
+        _lib.check(self.lib.gb_fixture_query(self.h, int(w), int(fixture), int(op), v, out), "gb_fixture_query")
+        return out
+
     def joint_reaction(self, joint: int, inv_dt: float, w: int = 0) -> np.ndarray:
         """b2Joint::GetReactionForce and GetReactionTorque after the last step: (force x, force y,
         torque) as float32 (gb_get_joint_reaction)."""

@@ -230,6 +230,12 @@ gb_status gb_joint_set(gb_world* world, int w, int joint, int prop, const float*
  * out[2] the torque. Waits for the step in flight. */
 gb_status gb_get_joint_reaction(gb_world* world, int w, int joint, float inv_dt, float* out);
 
+/* b2Fixture::TestPoint (op 0: in[0..1] the point; out[0] 1 when inside), RayCast (op 1: in[0..1] p1,
+ * in[2..3] p2, in[4] maxFraction; out = hit, normal x, y, fraction) and GetAABB (op 2: out = lower x,
+ * y, upper x, y) of a fixture (a chain child by its own index) at the body's current transform
+ * (Box2D/Dynamics/b2Fixture.h:313-342). Waits for the step in flight. */
+gb_status gb_fixture_query(gb_world* world, int w, int fixture, int op, const float* in, float* out);
+
 /* b2World::ShiftOrigin (Box2D/Dynamics/b2World.cpp:1261-1282) of world w between steps: bodies, the
  * mouse joints' targets, the pulleys' ground anchors and the broadphase's boxes move by -(x, y). */
 gb_status gb_world_shift_origin(gb_world* world, int w, float x, float y);

@@ -240,6 +240,15 @@ class b2Joint;
 struct b2AABB {
     b2Vec2 lowerBound, upperBound;
 };
+// b2RayCastInput, b2RayCastOutput (Box2D/Collision/b2Collision.h:153-166)
+struct b2RayCastInput {
+    b2Vec2 p1, p2;
+    float maxFraction = 1.0f;
+};
+struct b2RayCastOutput {
+    b2Vec2 normal;
+    float fraction = 0.0f;
+};
 
 class b2Fixture {
 public:
@@ -262,6 +271,11 @@ public:
     void SetSensor(bool sensor);
     void SetFilterData(const b2Filter& filter);
     void Refilter() { SetFilterData(m_def.filter); }
+    // b2Fixture::TestPoint, RayCast, GetAABB (Box2D/Dynamics/b2Fixture.h:313-342) at the body's
+    // current transform (gb_fixture_query); a chain's child by childIndex
+    bool TestPoint(const b2Vec2& p) const;
+    bool RayCast(b2RayCastOutput* output, const b2RayCastInput& input, int childIndex) const;
+    const b2AABB GetAABB(int childIndex) const;
 
 private:
     friend class b2World;
@@ -916,6 +930,12 @@ public:
         if (Destroy(gb_destroy_joint, joint->m_index, calls) != GB_OK) return;
         joint->m_alive = false;
     }
+    // one gb_fixture_query call (b2Fixture::TestPoint, RayCast, GetAABB)
+    bool FixtureQuery(int index, int op, const float* in, float* out)
+    {
+        out[0] = out[1] = out[2] = out[3] = 0.0f;
+        return Handle() && gb_fixture_query(m_h, 0, index, op, in, out) == GB_OK;
+    }
     // a joint's reaction force and torque (gb_get_joint_reaction)
     void JointReaction(int index, float inv_dt, float* out)
     {
@@ -1550,6 +1570,31 @@ inline float b2Joint::GetReactionTorque(float inv_dt) const
     float out[3];
     m_world->JointReaction(m_index, inv_dt, out);
     return out[2];
+}
+inline bool b2Fixture::TestPoint(const b2Vec2& p) const
+{
+    const float in[8] = {p.x, p.y, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    float out[4];
+    return m_body->GetWorld()->FixtureQuery(m_index, 0, in, out) && out[0] != 0.0f;
+}
+inline bool b2Fixture::RayCast(b2RayCastOutput* output, const b2RayCastInput& input, int childIndex) const
+{
+    const float in[8] = {input.p1.x, input.p1.y, input.p2.x, input.p2.y, input.maxFraction, 0.0f, 0.0f, 0.0f};
+    float out[4];
+    if (!m_body->GetWorld()->FixtureQuery(m_index + childIndex, 1, in, out) || out[0] == 0.0f) return false;
+    output->normal = b2Vec2(out[1], out[2]);
+    output->fraction = out[3];
+    return true;
+}
+inline const b2AABB b2Fixture::GetAABB(int childIndex) const
+{
+    const float in[8] = {0};
+    float out[4];
+    m_body->GetWorld()->FixtureQuery(m_index + childIndex, 2, in, out);
+    b2AABB a;
+    a.lowerBound = b2Vec2(out[0], out[1]);
+    a.upperBound = b2Vec2(out[2], out[3]);
+    return a;
 }
 inline void b2Fixture::SetFriction(float friction)
 {

@@ -63,6 +63,10 @@ def build_reference() -> None:
 _LIBS: dict = {}
 
 
+# entry points only the reference driver has (queries of the reference's own classes)
+REFERENCE_ONLY = {"fixture_query"}
+
+
 def _declare(lib, p: str) -> None:
     vp = C.c_void_p
     sig = {
@@ -98,6 +102,7 @@ def _declare(lib, p: str) -> None:
     sig["shift_origin"] = (None, [vp, C.c_float, C.c_float])
     sig["joint_set"] = (C.c_int, [vp, C.c_int, C.c_int, _f32p])
     sig["joint_reaction"] = (None, [vp, C.c_int, C.c_float, _f32p])
+    sig["fixture_query"] = (None, [vp, C.c_int, C.c_int, _f32p, _f32p])
     for kind in ("body", "joint", "fixture"):
         sig["destroy_" + kind] = (C.c_int, [vp, C.c_int, _i32p, C.c_int])
     if p == "rw_":
@@ -109,6 +114,8 @@ def _declare(lib, p: str) -> None:
         sig["get_pairs"] = (C.c_int, [vp, _i32p, C.c_int])
         sig["get_events"] = (C.c_int, [vp, _i32p, _f32p, C.c_int])
     for name, (res, args) in sig.items():
+        if name in REFERENCE_ONLY and not hasattr(lib, p + name):
+            continue
         fn = getattr(lib, p + name)
         fn.restype = res
         fn.argtypes = args
@@ -207,6 +214,15 @@ class OracleWorld:
         and SetAutoClearForces between steps."""
         self._fn("set_settings")(self.h, float(gravity[0]), float(gravity[1]), int(allow_sleep), int(warm_starting),
                                  int(continuous), int(sub_stepping), int(auto_clear_forces))
+
+    def fixture_query(self, fixture: int, op: int, inp=()) -> np.ndarray:
+        """b2Fixture::TestPoint (op 0), RayCast (op 1: p1, p2, maxFraction -> hit, normal, fraction) or
+        GetAABB (op 2) of a fixture's first child; the reference driver only."""
+        v = np.zeros(8, dtype=np.float32)
+        v[:len(inp)] = inp
+        out = np.zeros(4, dtype=np.float32)
+        self._fn("fixture_query")(self.h, int(fixture), int(op), v, out)
+        return out
 
     def joint_reaction(self, joint: int, inv_dt: float) -> np.ndarray:
         """b2Joint::GetReactionForce and GetReactionTorque: (force x, force y, torque) as float32."""

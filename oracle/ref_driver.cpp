@@ -457,6 +457,34 @@ void rw_body_set(void* h, int b, int prop, const float* v)
     default: break;
     }
 }
+// b2Fixture::TestPoint (op 0: in = point; out[0] 1 inside), RayCast (op 1: in = p1, p2, maxFraction;
+// out = hit, normal, fraction) and GetAABB (op 2: out = lower, upper) of a fixture's first child
+void rw_fixture_query(void* h, int f, int op, const float* in, float* out)
+{
+    const b2Fixture* fx = static_cast<RefWorld*>(h)->fixtures[f];
+    if (op == 0) {
+        out[0] = fx->TestPoint(b2Vec2(in[0], in[1])) ? 1.0f : 0.0f;
+    } else if (op == 1) {
+        b2RayCastInput input;
+        input.p1.Set(in[0], in[1]);
+        input.p2.Set(in[2], in[3]);
+        input.maxFraction = in[4];
+        b2RayCastOutput output;
+        output.normal.SetZero();
+        output.fraction = 0.0f;
+        const bool hit = fx->RayCast(&output, input, 0);
+        out[0] = hit ? 1.0f : 0.0f;
+        out[1] = hit ? output.normal.x : 0.0f;
+        out[2] = hit ? output.normal.y : 0.0f;
+        out[3] = hit ? output.fraction : 0.0f;
+    } else {
+        const b2AABB& a = fx->GetAABB(0);
+        out[0] = a.lowerBound.x;
+        out[1] = a.lowerBound.y;
+        out[2] = a.upperBound.x;
+        out[3] = a.upperBound.y;
+    }
+}
 void rw_joint_reaction(void* h, int ji, float inv_dt, float* out)
 {
     const b2Joint* j = static_cast<RefWorld*>(h)->joints[ji];

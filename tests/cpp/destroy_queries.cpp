@@ -102,7 +102,7 @@ int main()
     b2Body* bob = world.CreateBody(&pd);
     b2CircleShape ball;
     ball.m_radius = 0.5f;
-    bob->CreateFixture(&ball, 1.0f);
+    b2Fixture* bobFixture = bob->CreateFixture(&ball, 1.0f);
     bodies.push_back(bob);
     b2RevoluteJointDef jd;
     jd.bodyA = anchor;
@@ -184,6 +184,18 @@ int main()
         break;
     }
     std::printf("tree %d %d %a\n", world.GetTreeHeight(), world.GetTreeBalance(), world.GetTreeQuality());
+    {
+        const b2Vec2 c = bob->GetPosition();
+        b2RayCastInput in;
+        in.p1.Set(c.x - 2.0f, c.y + 0.1f);
+        in.p2.Set(c.x + 2.0f, c.y - 0.1f);
+        in.maxFraction = 1.0f;
+        b2RayCastOutput out;
+        const bool hit = bobFixture->RayCast(&out, in, 0);
+        const b2AABB box = bobFixture->GetAABB(0);
+        std::printf("fixq %d %d %a %a %a %a %a %a %a\n", bobFixture->TestPoint(c) ? 1 : 0, hit ? 1 : 0, out.normal.x,
+                    out.normal.y, out.fraction, box.lowerBound.x, box.lowerBound.y, box.upperBound.x, box.upperBound.y);
+    }
     const b2Profile& prof = world.GetProfile();
     std::printf("profile %d\n", prof.step > 0.0f && prof.solve > 0.0f ? 1 : 0);
     return 0;

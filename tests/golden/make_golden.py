@@ -22,6 +22,8 @@ Two builds of the reference are used: ``libm`` (glibc sinf/cosf, the reference a
 * ``collide.npz``: seeded shape pairs of every supported type pair with the reference manifolds.
 * ``toi.npz``: seeded sweeps with the reference b2TimeOfImpact result.
 * ``trig.npz``: glibc sinf/cosf on seeded angles (how far the project trig is from libm).
+* ``fixture_queries.npz``: b2Fixture::TestPoint, RayCast and GetAABB of every fixture of a stepped
+  scene for seeded points and rays (``--fixture-queries`` writes only this file).
 * ``tree_stats.npz``: b2World::GetTreeHeight, GetTreeBalance and GetTreeQuality after every step of
   trajectory and scripted cases (project trig; ``--tree`` writes only this file).
 * ``query_<scene>.npz``: b2World::QueryAABB and closest-hit b2World::RayCast results on a stepped
@@ -319,8 +321,39 @@ def make_tree():
     np.savez_compressed(os.path.join(HERE, "tree_stats.npz"), **out)
 
 
+def fixture_query_inputs(bodies: np.ndarray, fix_body: np.ndarray, seed: int = 3):
+    """Seeded b2Fixture queries around each fixture's body: rows (fixture, op, 5 inputs); op 0 a point
+    within 1 m of the body origin, op 1 a 6 m horizontal-ish ray through it (maxFraction 1), op 2 the
+    box."""
+    rng = np.random.default_rng(seed)
+    rows = []
+    for f, b in enumerate(fix_body):
+        px, py = float(bodies[b, 0]), float(bodies[b, 1])
+        for _ in range(4):
+            rows.append([f, 0, px + rng.uniform(-1, 1), py + rng.uniform(-1, 1), 0.0, 0.0, 0.0])
+            rows.append([f, 1, px - 3.0, py + rng.uniform(-0.5, 0.5), px + 3.0, py + rng.uniform(-0.5, 0.5), 1.0])
+        rows.append([f, 2, 0.0, 0.0, 0.0, 0.0, 0.0])
+    return np.array(rows, dtype=np.float32)
+
+
+def make_fixture_queries(steps: int = 60):
+    """b2Fixture::TestPoint, RayCast and GetAABB of every fixture of destroy_mix (seed 5) after `steps`
+    steps of the reference (project trig): inputs (fixture, op, 5 floats) and outputs (4 floats)."""
+    sc = scenes.destroy_mix(scenes.SplitMix64(5))
+    w = oracle.OracleWorld(sc, "reference", "project")
+    for _ in range(steps):
+        w.step(DT, VI, PI)
+    q = fixture_query_inputs(w.bodies(), sc.arrays()["fix_body"])
+    out = np.array([w.fixture_query(int(r[0]), int(r[1]), r[2:]) for r in q], dtype=np.float32)
+    np.savez_compressed(os.path.join(HERE, "fixture_queries.npz"), queries=q, outputs=out, steps=np.int32(steps))
+
+
 def main():
     oracle.build_reference()
+    if "--fixture-queries" in sys.argv:
+        make_fixture_queries()
+        print("done")
+        return
     if "--queries" in sys.argv:
         make_queries()
         print("done")
@@ -377,6 +410,7 @@ def main():
     make_trig()
     make_queries()
     make_tree()
+    make_fixture_queries()
     print("done")
 
 

@@ -40,3 +40,23 @@ def test_body_info_rejects_bad_bodies():
         w.body_info(1000)
     with pytest.raises(GbError):
         w.body_set(0, 10, 0.0)
+
+
+def test_fixture_queries_before_stepping_match_reference():
+    """b2Fixture::TestPoint, RayCast and GetAABB on the host copy (no step yet) against the reference's
+    for seeded points and rays around every fixture."""
+    if not oracle.reference_available():
+        pytest.skip("reference tree not present")
+    import importlib.util
+    import os
+
+    here = os.path.dirname(os.path.abspath(__file__))
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(here, "golden", "make_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    sc = scenes.destroy_mix(scenes.SplitMix64(5))
+    w = World(sc)
+    r = oracle.OracleWorld(sc, "reference", "project")
+    for q in mod.fixture_query_inputs(r.bodies(), sc.arrays()["fix_body"], seed=11):
+        a, b = w.fixture_query(int(q[0]), int(q[1]), q[2:]), r.fixture_query(int(q[0]), int(q[1]), q[2:])
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (q, a, b)

@@ -388,6 +388,15 @@ def test_cpp_destroy_queries_match_oracle(gpu, tmp_path):
     assert int(rr[0]) == int(fix[0]) and int(rr[-1]) == len(allf)
     got = np.array([float.fromhex(v) for v in rr[1:6]], dtype=np.float32)
     assert np.array_equal(got.view(np.uint32), hit[0].view(np.uint32))
+    fq = out["fixq"]
+    bob = gw.bodies()[11]
+    cx, cy = np.float32(bob[0]), np.float32(bob[1])
+    ray = gw.fixture_query(11, 1, (cx - np.float32(2.0), cy + np.float32(0.1), cx + np.float32(2.0), cy - np.float32(0.1), 1.0))
+    box = gw.fixture_query(11, 2)
+    assert int(fq[0]) == int(gw.fixture_query(11, 0, (cx, cy))[0]) == 1
+    assert int(fq[1]) == int(ray[0]) == 1
+    got = np.array([float.fromhex(v) for v in fq[2:]], dtype=np.float32)
+    assert np.array_equal(got.view(np.uint32), np.concatenate([ray[1:], box]).view(np.uint32))
     th, tb, tq = o.tree_stats()
     t = out["tree"]
     assert [int(t[0]), int(t[1])] == [th, tb]

@@ -36,3 +36,21 @@ def test_queries_match_reference(gpu, name, make, steps):
     hits = fix >= 0
     assert np.array_equal(hit[hits].view(np.uint32), g["ray_hit"][hits].view(np.uint32)), name
     w.sync()
+
+
+def test_fixture_queries_match_reference_golden(gpu):
+    """b2Fixture::TestPoint, RayCast and GetAABB of every fixture after 60 device steps, bit for bit
+    with the reference's results (golden fixture_queries.npz)."""
+    import numpy as np
+
+    from box2dpp_gb300 import scenes
+    from box2dpp_gb300.world import World
+    from tests._util import DT, PI, VI, golden
+
+    g = golden("fixture_queries")
+    w = World(scenes.destroy_mix(scenes.SplitMix64(5)))
+    for _ in range(int(g["steps"])):
+        w.step(DT, VI, PI)
+    for q, want in zip(g["queries"], g["outputs"]):
+        got = w.fixture_query(int(q[0]), int(q[1]), q[2:])
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (q, got, want)
