@@ -259,6 +259,9 @@ public:
     float GetDensity() const { return m_def.density; }
     bool IsSensor() const { return m_def.isSensor; }
     void* GetUserData() const { return m_def.userData; }
+    void SetUserData(void* data) { m_def.userData = data; }
+    // the next fixture of the body's list (newest first), as b2Fixture::GetNext
+    b2Fixture* GetNext() const;
     b2Shape::Type GetType() const { return m_type; }
     float GetRadius() const { return m_radius; }  // the shape's m_radius
     const b2Filter& GetFilterData() const { return m_def.filter; }
@@ -282,6 +285,7 @@ private:
     friend class b2Body;
     b2Body* m_body = nullptr;
     int m_index = -1;
+    size_t m_slot = 0;  // position in the world's fixtures (creation order)
     b2FixtureDef m_def;
     b2Shape::Type m_type = b2Shape::e_circle;
     float m_radius = 0.0f;
@@ -306,6 +310,9 @@ public:
     int GetIndex() const { return m_index; }
     b2World* GetWorld() const { return m_world; }
     void* GetUserData() const { return m_userData; }
+    void SetUserData(void* data) { m_userData = data; }
+    // the body's fixture list (newest first), as b2Body::GetFixtureList
+    b2Fixture* GetFixtureList() const;
     const b2Vec2 GetPosition() const { const float* s = State(); return b2Vec2(s[0], s[1]); }
     float GetAngle() const { return State()[2]; }
     const b2Vec2 GetWorldCenter() const { const float* s = State(); return b2Vec2(s[3], s[4]); }
@@ -532,6 +539,10 @@ public:
     int GetIndex() const { return m_index; }
     b2Body* GetBodyA() const { return m_a; }
     b2Body* GetBodyB() const { return m_b; }
+    void* GetUserData() const { return m_userData; }
+    void SetUserData(void* data) { m_userData = data; }
+    // the next joint of the world's joint list (newest first), as b2Joint::GetNext
+    b2Joint* GetNext() const;
     // b2Joint::GetReactionForce / GetReactionTorque (Box2D/Dynamics/Joints/*.cpp) after the last step
     b2Vec2 GetReactionForce(float inv_dt) const;
     float GetReactionTorque(float inv_dt) const;
@@ -541,8 +552,10 @@ protected:
     // one gb_joint_set call (GB_JOINT_*); false when it did not apply
     bool Set(int prop, float v0, float v1 = 0.0f);
     int m_index = -1;
+    size_t m_slot = 0;  // position in the world's joints (creation order)
     b2Body *m_a = nullptr, *m_b = nullptr;
     b2World* m_world = nullptr;
+    void* m_userData = nullptr;
     bool m_alive = true;
 };
 
@@ -1027,6 +1040,22 @@ public:
 
     // b2World::GetBodyList (newest first, as the reference's list)
     b2Body* GetBodyList() const { return PreviousAlive(m_bodies.size()); }
+    // b2World::GetJointList (newest first)
+    b2Joint* GetJointList() const { return PreviousJoint(m_joints.size()); }
+    b2Joint* PreviousJoint(size_t slot) const
+    {
+        for (size_t i = slot; i-- > 0;)
+            if (m_joints[i]->m_alive) return m_joints[i].get();
+        return nullptr;
+    }
+    b2Fixture* FixtureListOf(const b2Body* body) const { return PreviousFixture(m_fixtures.size(), body); }
+    // a body's fixtures before `slot` in creation order, newest first (b2Body::GetFixtureList order)
+    b2Fixture* PreviousFixture(size_t slot, const b2Body* body) const
+    {
+        for (size_t i = slot; i-- > 0;)
+            if (m_fixtures[i]->m_alive && m_fixtures[i]->m_body == body) return m_fixtures[i].get();
+        return nullptr;
+    }
     b2Body* PreviousAlive(size_t index) const
     {
         for (size_t i = index; i-- > 0;)
@@ -1115,6 +1144,7 @@ public:
         j->m_index = id;
         j->m_a = def->bodyA;
         j->m_b = def->bodyB;
+        j->m_slot = m_joints.size();
         m_joints.push_back(std::move(j));
         return m_joints.back().get();
     }
@@ -1343,6 +1373,7 @@ public:
         fx->m_type = def->shape->GetType();
         fx->m_radius = def->shape->m_radius;
         for (int k = 0; k < children; ++k) m_fixtureOfId.push_back({fx.get(), k});
+        fx->m_slot = m_fixtures.size();
         m_fixtures.push_back(std::move(fx));
         m_stale = true;
         return m_fixtures.back().get();
@@ -1411,6 +1442,7 @@ private:
         j->m_index = id;
         j->m_a = a;
         j->m_b = b;
+        j->m_slot = m_joints.size();
         m_joints.push_back(std::move(j));
         return m_joints.back().get();
     }
@@ -1532,6 +1564,9 @@ inline void b2Body::DestroyFixture(b2Fixture* fixture)
     if (fixture && fixture->m_body == this) m_world->DestroyFixture(fixture);
 }
 inline b2Body* b2Body::GetNext() const { return m_world->PreviousAlive((size_t)m_index); }
+inline b2Fixture* b2Body::GetFixtureList() const { return m_world->FixtureListOf(this); }
+inline b2Fixture* b2Fixture::GetNext() const { return m_body->GetWorld()->PreviousFixture(m_slot, m_body); }
+inline b2Joint* b2Joint::GetNext() const { return m_world->PreviousJoint(m_slot); }
 inline void b2Contact::GetWorldManifold(b2WorldManifold* worldManifold) const
 {
     worldManifold->Initialize(&m_manifold, m_a->GetBody()->GetTransform(), m_a->GetRadius(),

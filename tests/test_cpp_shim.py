@@ -609,3 +609,28 @@ def test_cpp_joint_setters_match_oracle(gpu, tmp_path):
             continue
         assert np.array_equal(got.view(np.uint32), ob[i][[0, 1, 2, 5, 6, 7]].view(np.uint32)), i
     assert reactions == 5
+
+
+LISTS_SRC = os.path.join(ROOT, "tests", "cpp", "lists.cpp")
+
+
+def test_cpp_lists_and_user_data(tmp_path):
+    """b2Body::GetFixtureList / b2Fixture::GetNext and b2World::GetJointList / b2Joint::GetNext run
+    newest first and skip destroyed entries, as the reference's lists; user data round-trips. No step
+    is taken, so this runs without a GPU."""
+    lib = _lib.library_path()
+    exe = str(tmp_path / "lists")
+    libdir = os.path.dirname(lib)
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "include"), LISTS_SRC, "-o", exe,
+           "-L", libdir, "-lbox2d_gb300", f"-Wl,-rpath,{libdir}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    out = {ln.split()[0]: ln.split()[1:] for ln in r.stdout.strip().splitlines()}
+    assert out["fixtures"] == ["2", "1", "0"]
+    assert out["joints"] == ["2", "1", "0"]
+    assert out["fixtures_after"] == ["2", "0"]
+    assert out["joints_after"] == ["2", "0"]
+    assert out["user"] == ["7", "8", "9"]
+    assert out["ground_fixtures"] == ["3"]
