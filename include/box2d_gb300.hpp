@@ -292,6 +292,21 @@ private:
     bool m_alive = true;
 };
 
+class b2Contact;
+// b2ContactEdge, b2JointEdge (Box2D/Dynamics/Contacts/b2Contact.h:70-76, Joints/b2Joint.h:63-69)
+struct b2ContactEdge {
+    b2Body* other = nullptr;
+    b2Contact* contact = nullptr;
+    b2ContactEdge* prev = nullptr;
+    b2ContactEdge* next = nullptr;
+};
+struct b2JointEdge {
+    b2Body* other = nullptr;
+    b2Joint* joint = nullptr;
+    b2JointEdge* prev = nullptr;
+    b2JointEdge* next = nullptr;
+};
+
 class b2Body {
 public:
     b2Fixture* CreateFixture(const b2FixtureDef* def);
@@ -313,6 +328,10 @@ public:
     void SetUserData(void* data) { m_userData = data; }
     // the body's fixture list (newest first), as b2Body::GetFixtureList
     b2Fixture* GetFixtureList() const;
+    // the body's contact and joint edges (newest first, as the reference's lists), rebuilt at each
+    // call from the world's contact list and joints: valid until the next call or step
+    b2ContactEdge* GetContactList();
+    b2JointEdge* GetJointList();
     const b2Vec2 GetPosition() const { const float* s = State(); return b2Vec2(s[0], s[1]); }
     float GetAngle() const { return State()[2]; }
     const b2Vec2 GetWorldCenter() const { const float* s = State(); return b2Vec2(s[3], s[4]); }
@@ -416,6 +435,8 @@ private:
     b2BodyType m_type = b2_staticBody;
     void* m_userData = nullptr;
     bool m_alive = true;
+    std::vector<b2ContactEdge> m_contactEdges;
+    std::vector<b2JointEdge> m_jointEdges;
 };
 
 struct b2RevoluteJointDef {
@@ -1565,6 +1586,40 @@ inline void b2Body::DestroyFixture(b2Fixture* fixture)
 }
 inline b2Body* b2Body::GetNext() const { return m_world->PreviousAlive((size_t)m_index); }
 inline b2Fixture* b2Body::GetFixtureList() const { return m_world->FixtureListOf(this); }
+inline b2ContactEdge* b2Body::GetContactList()
+{
+    m_contactEdges.clear();
+    for (b2Contact* c : m_world->GetContactList()) {
+        b2Body* a = c->GetFixtureA()->GetBody();
+        b2Body* b = c->GetFixtureB()->GetBody();
+        if (a != this && b != this) continue;
+        b2ContactEdge e;
+        e.other = a == this ? b : a;
+        e.contact = c;
+        m_contactEdges.push_back(e);
+    }
+    for (size_t i = 0; i < m_contactEdges.size(); ++i) {
+        m_contactEdges[i].prev = i > 0 ? &m_contactEdges[i - 1] : nullptr;
+        m_contactEdges[i].next = i + 1 < m_contactEdges.size() ? &m_contactEdges[i + 1] : nullptr;
+    }
+    return m_contactEdges.empty() ? nullptr : &m_contactEdges[0];
+}
+inline b2JointEdge* b2Body::GetJointList()
+{
+    m_jointEdges.clear();
+    for (b2Joint* j = m_world->GetJointList(); j; j = j->GetNext()) {
+        if (j->GetBodyA() != this && j->GetBodyB() != this) continue;
+        b2JointEdge e;
+        e.other = j->GetBodyA() == this ? j->GetBodyB() : j->GetBodyA();
+        e.joint = j;
+        m_jointEdges.push_back(e);
+    }
+    for (size_t i = 0; i < m_jointEdges.size(); ++i) {
+        m_jointEdges[i].prev = i > 0 ? &m_jointEdges[i - 1] : nullptr;
+        m_jointEdges[i].next = i + 1 < m_jointEdges.size() ? &m_jointEdges[i + 1] : nullptr;
+    }
+    return m_jointEdges.empty() ? nullptr : &m_jointEdges[0];
+}
 inline b2Fixture* b2Fixture::GetNext() const { return m_body->GetWorld()->PreviousFixture(m_slot, m_body); }
 inline b2Joint* b2Joint::GetNext() const { return m_world->PreviousJoint(m_slot); }
 inline void b2Contact::GetWorldManifold(b2WorldManifold* worldManifold) const

@@ -184,6 +184,14 @@ int main()
         break;
     }
     std::printf("tree %d %d %a\n", world.GetTreeHeight(), world.GetTreeBalance(), world.GetTreeQuality());
+    // each body's contact edges (b2Body::GetContactList): how many, and the other bodies in order
+    std::printf("edges");
+    for (b2Body* b : bodies) {
+        int n = 0;
+        for (b2ContactEdge* e = b->GetContactList(); e; e = e->next) ++n;
+        std::printf(" %d:%d", b->GetIndex(), n);
+    }
+    std::printf("\n");
     {
         const b2Vec2 c = bob->GetPosition();
         b2RayCastInput in;

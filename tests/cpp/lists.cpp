@@ -52,6 +52,10 @@ int main()
     for (b2Joint* j = world.GetJointList(); j; j = j->GetNext()) std::printf(" %d", j->GetIndex());
     std::printf("\nuser %d %d %d\n", *static_cast<int*>(body->GetUserData()), *static_cast<int*>(f1->GetUserData()),
                 *static_cast<int*>(j2->GetUserData()));
+    std::printf("body_joints");
+    for (b2JointEdge* e = body->GetJointList(); e; e = e->next)
+        std::printf(" %d:%d", e->joint->GetIndex(), e->other == ground ? 0 : 1);
+    std::printf("\nground_contacts %d\n", ground->GetContactList() ? 1 : 0);
     std::printf("ground_fixtures");
     for (b2Fixture* f = ground->GetFixtureList(); f; f = f->GetNext()) std::printf(" %d", f->GetIndex());
     std::printf("\n");

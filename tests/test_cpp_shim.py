@@ -388,6 +388,14 @@ def test_cpp_destroy_queries_match_oracle(gpu, tmp_path):
     assert int(rr[0]) == int(fix[0]) and int(rr[-1]) == len(allf)
     got = np.array([float.fromhex(v) for v in rr[1:6]], dtype=np.float32)
     assert np.array_equal(got.view(np.uint32), hit[0].view(np.uint32))
+    # contact edges per body: the device's contacts that involve the body
+    fb = {f: b for f, b in enumerate(sc.arrays()["fix_body"])}
+    fb[14] = 13  # the body created after the destructions
+    gci, _ = gw.contacts()
+    for item in out["edges"]:
+        b, n = (int(x) for x in item.split(":"))
+        want = sum(1 for row in gci if fb[int(row[0])] == b or fb[int(row[1])] == b)
+        assert n == want, (b, n, want)
     fq = out["fixq"]
     bob = gw.bodies()[11]
     cx, cy = np.float32(bob[0]), np.float32(bob[1])
@@ -634,3 +642,5 @@ def test_cpp_lists_and_user_data(tmp_path):
     assert out["joints_after"] == ["2", "0"]
     assert out["user"] == ["7", "8", "9"]
     assert out["ground_fixtures"] == ["3"]
+    assert out["body_joints"] == ["2:0", "0:0"]  # newest first, the destroyed joint left out
+    assert out["ground_contacts"] == ["0"]  # no step yet: no contacts
