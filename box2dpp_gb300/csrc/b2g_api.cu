@@ -3181,7 +3181,7 @@ extern "C" {
 
 gb_status gb_fixture_query(gb_world* g, int w, int fixture, int op, const float* in, float* out)
 {
-    if (!g || w < 0 || w >= (int)g->worlds.size() || !out || (op != 2 && !in) || op < 0 || op > 2) return GB_ERR_INVALID;
+    if (!g || w < 0 || w >= (int)g->worlds.size() || !out || (op < 2 && !in) || op < 0 || op > 3) return GB_ERR_INVALID;
     const HWorld& W = g->worlds[w];
     if (fixture < 0 || fixture >= (int)W.fixtures.size() || W.fixtures[fixture].body == kNullIdx) return GB_ERR_INVALID;
     const HFixture& fx = W.fixtures[fixture];
@@ -3226,6 +3226,14 @@ gb_status gb_fixture_query(gb_world* g, int w, int fixture, int op, const float*
             out[2] = normal.y;
             out[3] = fraction;
         }
+    } else if (op == 3) {
+        // b2Fixture::GetMassData (b2Fixture.h:344-347): b2Shape::ComputeMass with the fixture's density
+        MassData md;
+        ComputeMass(sh, fx.density, &md);
+        out[0] = md.mass;
+        out[1] = md.center.x;
+        out[2] = md.center.y;
+        out[3] = md.I;
     } else {
         // b2Fixture::GetAABB (b2Fixture.h:338-342): the proxy's swept box of the last synchronisation
         out[0] = aabb.x;

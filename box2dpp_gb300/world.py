@@ -188,8 +188,9 @@ class World:
         return calls[:min(n.value, 256)]
 
     def fixture_query(self, fixture: int, op: int, inp=(), w: int = 0) -> np.ndarray:
-        """b2Fixture::TestPoint (op 0), RayCast (op 1: p1, p2, maxFraction -> hit, normal, fraction) or
-        GetAABB (op 2) at the body's current transform (gb_fixture_query), as float32."""
+        """b2Fixture::TestPoint (op 0), RayCast (op 1: p1, p2, maxFraction -> hit, normal, fraction),
+        GetAABB (op 2) or GetMassData (op 3: mass, center, inertia) at the body's current transform
+        (gb_fixture_query), as float32."""
         v = np.zeros(8, dtype=np.float32)
         v[:len(inp)] = inp
         out = np.zeros(4, dtype=np.float32)

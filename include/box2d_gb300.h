@@ -231,8 +231,9 @@ gb_status gb_joint_set(gb_world* world, int w, int joint, int prop, const float*
 gb_status gb_get_joint_reaction(gb_world* world, int w, int joint, float inv_dt, float* out);
 
 /* b2Fixture::TestPoint (op 0: in[0..1] the point; out[0] 1 when inside), RayCast (op 1: in[0..1] p1,
- * in[2..3] p2, in[4] maxFraction; out = hit, normal x, y, fraction) and GetAABB (op 2: out = lower x,
- * y, upper x, y) of a fixture (a chain child by its own index) at the body's current transform
+ * in[2..3] p2, in[4] maxFraction; out = hit, normal x, y, fraction), GetAABB (op 2: out = lower x,
+ * y, upper x, y) and GetMassData (op 3: out = mass, center x, y, inertia about the body origin) of a
+ * fixture (a chain child by its own index) at the body's current transform
  * (Box2D/Dynamics/b2Fixture.h:313-342). Waits for the step in flight. */
 gb_status gb_fixture_query(gb_world* world, int w, int fixture, int op, const float* in, float* out);
 

@@ -279,6 +279,7 @@ public:
     bool TestPoint(const b2Vec2& p) const;
     bool RayCast(b2RayCastOutput* output, const b2RayCastInput& input, int childIndex) const;
     const b2AABB GetAABB(int childIndex) const;
+    void GetMassData(b2MassData* massData) const;
 
 private:
     friend class b2World;
@@ -1675,6 +1676,15 @@ inline bool b2Fixture::RayCast(b2RayCastOutput* output, const b2RayCastInput& in
     output->normal = b2Vec2(out[1], out[2]);
     output->fraction = out[3];
     return true;
+}
+inline void b2Fixture::GetMassData(b2MassData* md) const
+{
+    const float in[8] = {0};
+    float out[4];
+    m_body->GetWorld()->FixtureQuery(m_index, 3, in, out);
+    md->mass = out[0];
+    md->center = b2Vec2(out[1], out[2]);
+    md->I = out[3];
 }
 inline const b2AABB b2Fixture::GetAABB(int childIndex) const
 {

@@ -477,6 +477,13 @@ void rw_fixture_query(void* h, int f, int op, const float* in, float* out)
         out[1] = hit ? output.normal.x : 0.0f;
         out[2] = hit ? output.normal.y : 0.0f;
         out[3] = hit ? output.fraction : 0.0f;
+    } else if (op == 3) {
+        b2MassData md;
+        fx->GetMassData(&md);
+        out[0] = md.mass;
+        out[1] = md.center.x;
+        out[2] = md.center.y;
+        out[3] = md.I;
     } else {
         const b2AABB& a = fx->GetAABB(0);
         out[0] = a.lowerBound.x;

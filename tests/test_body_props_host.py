@@ -43,8 +43,8 @@ def test_body_info_rejects_bad_bodies():
 
 
 def test_fixture_queries_before_stepping_match_reference():
-    """b2Fixture::TestPoint, RayCast and GetAABB on the host copy (no step yet) against the reference's
-    for seeded points and rays around every fixture."""
+    """b2Fixture::TestPoint, RayCast, GetAABB and GetMassData on the host copy (no step yet) against the
+    reference's for seeded points and rays around every fixture."""
     if not oracle.reference_available():
         pytest.skip("reference tree not present")
     import importlib.util
@@ -60,3 +60,7 @@ def test_fixture_queries_before_stepping_match_reference():
     for q in mod.fixture_query_inputs(r.bodies(), sc.arrays()["fix_body"], seed=11):
         a, b = w.fixture_query(int(q[0]), int(q[1]), q[2:]), r.fixture_query(int(q[0]), int(q[1]), q[2:])
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (q, a, b)
+    # b2Fixture::GetMassData of every fixture (op 3)
+    for f in range(len(sc.fixtures)):
+        a, b = w.fixture_query(f, 3), r.fixture_query(f, 3)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (f, a, b)
