@@ -924,6 +924,8 @@ public:
     void SetGravity(const b2Vec2& gravity) { m_gravity = gravity; ApplySettings(); }
     void SetAutoClearForces(bool flag) { m_autoClear = flag; ApplySettings(); }
     bool GetAllowSleeping() const { return m_def.allow_sleep != 0; }
+    // b2World::IsLocked (Box2D/Dynamics/b2World.h:169): true while the contact listener is being called
+    bool IsLocked() const { return m_locked; }
     bool GetWarmStarting() const { return m_def.warm_starting != 0; }
     bool GetContinuousPhysics() const { return m_def.continuous_physics != 0; }
     bool GetSubStepping() const { return m_def.sub_stepping != 0; }
@@ -1525,6 +1527,12 @@ private:
     // as they were before (m_contacts); returns the number of calls recorded so far.
     int Report(int first)
     {
+        // b2World::IsLocked inside the listener's calls, as during the reference's Step
+        struct Lock {
+            bool& flag;
+            explicit Lock(bool& f) : flag(f) { flag = true; }
+            ~Lock() { flag = false; }
+        } lock(m_locked);
         std::vector<std::unique_ptr<b2Contact>> old = std::move(m_contacts);
         ReadContacts();
         std::map<std::pair<int, int>, b2Contact*> now, before;
@@ -1575,6 +1583,7 @@ private:
     std::vector<std::unique_ptr<b2Joint>> m_joints;
     std::vector<std::unique_ptr<b2Contact>> m_contacts, m_old;
     bool m_eventsOn = false;
+    bool m_locked = false;
     std::vector<b2Contact*> m_contactView;
     std::vector<float> m_state;
     bool m_stale = true;
