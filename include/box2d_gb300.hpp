@@ -441,6 +441,7 @@ private:
 };
 
 struct b2RevoluteJointDef {
+    void* userData = nullptr;
     b2Body* bodyA = nullptr;
     b2Body* bodyB = nullptr;
     bool collideConnected = false;
@@ -450,30 +451,39 @@ struct b2RevoluteJointDef {
     float lowerAngle = 0.0f, upperAngle = 0.0f;
     bool enableMotor = false;
     float motorSpeed = 0.0f, maxMotorTorque = 0.0f;
+    // b2RevoluteJointDef::Initialize (b2RevoluteJoint.cpp:40-47): anchor in world coordinates
+    void Initialize(b2Body* bA, b2Body* bB, const b2Vec2& anchor);
 };
 
 struct b2DistanceJointDef {
+    void* userData = nullptr;
     b2Body* bodyA = nullptr;
     b2Body* bodyB = nullptr;
     bool collideConnected = false;
     b2Vec2 localAnchorA, localAnchorB;
     float length = 1.0f;
     float frequencyHz = 0.0f, dampingRatio = 0.0f;
+    // b2DistanceJointDef::Initialize (b2DistanceJoint.cpp:41-50): anchors in world coordinates
+    void Initialize(b2Body* bA, b2Body* bB, const b2Vec2& anchorA, const b2Vec2& anchorB);
 };
 
 struct b2WeldJointDef {
+    void* userData = nullptr;
     b2Body* bodyA = nullptr;
     b2Body* bodyB = nullptr;
     bool collideConnected = false;
     b2Vec2 localAnchorA, localAnchorB;
     float referenceAngle = 0.0f;
     float frequencyHz = 0.0f, dampingRatio = 0.0f;
+    // b2WeldJointDef::Initialize (b2WeldJoint.cpp:36-43)
+    void Initialize(b2Body* bA, b2Body* bB, const b2Vec2& anchor);
 };
 
 // b2WheelJointDef, b2RopeJointDef, b2FrictionJointDef, b2MotorJointDef (Box2D/Dynamics/Joints/
 // b2WheelJoint.h:30-68, b2RopeJoint.h:28-45, b2FrictionJoint.h:25-45, b2MotorJoint.h:26-55), with
 // the reference's defaults
 struct b2WheelJointDef {
+    void* userData = nullptr;
     b2Body* bodyA = nullptr;
     b2Body* bodyB = nullptr;
     bool collideConnected = false;
@@ -482,8 +492,11 @@ struct b2WheelJointDef {
     bool enableMotor = false;
     float maxMotorTorque = 0.0f, motorSpeed = 0.0f;
     float frequencyHz = 2.0f, dampingRatio = 0.7f;
+    // b2WheelJointDef::Initialize (b2WheelJoint.cpp:39-46)
+    void Initialize(b2Body* bA, b2Body* bB, const b2Vec2& anchor, const b2Vec2& axis);
 };
 struct b2RopeJointDef {
+    void* userData = nullptr;
     b2Body* bodyA = nullptr;
     b2Body* bodyB = nullptr;
     bool collideConnected = false;
@@ -491,24 +504,31 @@ struct b2RopeJointDef {
     float maxLength = 0.0f;
 };
 struct b2FrictionJointDef {
+    void* userData = nullptr;
     b2Body* bodyA = nullptr;
     b2Body* bodyB = nullptr;
     bool collideConnected = false;
     b2Vec2 localAnchorA, localAnchorB;
     float maxForce = 0.0f, maxTorque = 0.0f;
+    // b2FrictionJointDef::Initialize (b2FrictionJoint.cpp:35-41)
+    void Initialize(b2Body* bA, b2Body* bB, const b2Vec2& anchor);
 };
 struct b2MotorJointDef {
+    void* userData = nullptr;
     b2Body* bodyA = nullptr;
     b2Body* bodyB = nullptr;
     bool collideConnected = false;
     b2Vec2 linearOffset;
     float angularOffset = 0.0f;
     float maxForce = 1.0f, maxTorque = 1.0f, correctionFactor = 0.3f;
+    // b2MotorJointDef::Initialize (b2MotorJoint.cpp:35-44)
+    void Initialize(b2Body* bA, b2Body* bB);
 };
 
 // b2MouseJointDef (Box2D/Dynamics/Joints/b2MouseJoint.h:28-56): body B's point under `target` is
 // pulled to the target, which b2MouseJoint::SetTarget moves between steps
 struct b2MouseJointDef {
+    void* userData = nullptr;
     b2Body* bodyA = nullptr;
     b2Body* bodyB = nullptr;
     bool collideConnected = false;
@@ -518,6 +538,7 @@ struct b2MouseJointDef {
 
 // b2PulleyJointDef (Box2D/Dynamics/Joints/b2PulleyJoint.h:30-72): lengthA + ratio * lengthB constant
 struct b2PulleyJointDef {
+    void* userData = nullptr;
     b2Body* bodyA = nullptr;
     b2Body* bodyB = nullptr;
     bool collideConnected = true;
@@ -533,6 +554,7 @@ struct b2PulleyJointDef {
 // prismatic joints created before it
 class b2Joint;
 struct b2GearJointDef {
+    void* userData = nullptr;
     b2Body* bodyA = nullptr;
     b2Body* bodyB = nullptr;
     bool collideConnected = false;
@@ -543,6 +565,7 @@ struct b2GearJointDef {
 
 // b2PrismaticJointDef (Box2D/Dynamics/Joints/b2PrismaticJoint.h:30-88)
 struct b2PrismaticJointDef {
+    void* userData = nullptr;
     b2Body* bodyA = nullptr;
     b2Body* bodyB = nullptr;
     bool collideConnected = false;
@@ -553,6 +576,8 @@ struct b2PrismaticJointDef {
     float lowerTranslation = 0.0f, upperTranslation = 0.0f;
     bool enableMotor = false;
     float maxMotorForce = 0.0f, motorSpeed = 0.0f;
+    // b2PrismaticJointDef::Initialize (b2PrismaticJoint.cpp:92-100)
+    void Initialize(b2Body* bA, b2Body* bB, const b2Vec2& anchor, const b2Vec2& axis);
 };
 
 class b2Joint {
@@ -1168,6 +1193,7 @@ public:
         j->m_index = id;
         j->m_a = def->bodyA;
         j->m_b = def->bodyB;
+        j->m_userData = def->userData;
         j->m_slot = m_joints.size();
         m_joints.push_back(std::move(j));
         return m_joints.back().get();
@@ -1181,7 +1207,9 @@ public:
         j->m_length = def->length;
         j->m_frequencyHz = def->frequencyHz;
         j->m_dampingRatio = def->dampingRatio;
-        return AddJoint(GB_JOINT_DISTANCE, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(j));
+        b2Joint* r = AddJoint(GB_JOINT_DISTANCE, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(j));
+        if (r) r->m_userData = def->userData;
+        return r;
     }
     b2Joint* CreateJoint(const b2WeldJointDef* def)
     {
@@ -1191,7 +1219,9 @@ public:
         std::unique_ptr<b2WeldJoint> j(new b2WeldJoint());
         j->m_frequencyHz = def->frequencyHz;
         j->m_dampingRatio = def->dampingRatio;
-        return AddJoint(GB_JOINT_WELD, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(j));
+        b2Joint* r = AddJoint(GB_JOINT_WELD, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(j));
+        if (r) r->m_userData = def->userData;
+        return r;
     }
     b2Joint* CreateJoint(const b2WheelJointDef* def)
     {
@@ -1205,7 +1235,9 @@ public:
         j->m_maxMotorTorque = def->maxMotorTorque;
         j->m_frequencyHz = def->frequencyHz;
         j->m_dampingRatio = def->dampingRatio;
-        return AddJoint(GB_JOINT_WHEEL, def->bodyA, def->bodyB, f, flags, std::move(j));
+        b2Joint* r = AddJoint(GB_JOINT_WHEEL, def->bodyA, def->bodyB, f, flags, std::move(j));
+        if (r) r->m_userData = def->userData;
+        return r;
     }
     b2Joint* CreateJoint(const b2RopeJointDef* def)
     {
@@ -1213,7 +1245,9 @@ public:
                                           def->localAnchorB.y, def->maxLength};
         std::unique_ptr<b2RopeJoint> j(new b2RopeJoint());
         j->m_maxLength = def->maxLength;
-        return AddJoint(GB_JOINT_ROPE, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(j));
+        b2Joint* r = AddJoint(GB_JOINT_ROPE, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(j));
+        if (r) r->m_userData = def->userData;
+        return r;
     }
     b2Joint* CreateJoint(const b2FrictionJointDef* def)
     {
@@ -1222,7 +1256,9 @@ public:
         std::unique_ptr<b2FrictionJoint> j(new b2FrictionJoint());
         j->m_maxForce = def->maxForce;
         j->m_maxTorque = def->maxTorque;
-        return AddJoint(GB_JOINT_FRICTION, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(j));
+        b2Joint* r = AddJoint(GB_JOINT_FRICTION, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(j));
+        if (r) r->m_userData = def->userData;
+        return r;
     }
     b2Joint* CreateJoint(const b2MotorJointDef* def)
     {
@@ -1234,7 +1270,9 @@ public:
         j->m_maxForce = def->maxForce;
         j->m_maxTorque = def->maxTorque;
         j->m_correctionFactor = def->correctionFactor;
-        return AddJoint(GB_JOINT_MOTOR, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(j));
+        b2Joint* r = AddJoint(GB_JOINT_MOTOR, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(j));
+        if (r) r->m_userData = def->userData;
+        return r;
     }
     b2Joint* CreateJoint(const b2MouseJointDef* def)
     {
@@ -1245,7 +1283,9 @@ public:
         j->m_maxForce = def->maxForce;
         j->m_frequencyHz = def->frequencyHz;
         j->m_dampingRatio = def->dampingRatio;
-        return AddJoint(GB_JOINT_MOUSE, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(j));
+        b2Joint* r = AddJoint(GB_JOINT_MOUSE, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(j));
+        if (r) r->m_userData = def->userData;
+        return r;
     }
     b2Joint* CreateJoint(const b2PulleyJointDef* def)
     {
@@ -1253,7 +1293,9 @@ public:
                                           def->groundAnchorB.y, def->localAnchorA.x, def->localAnchorA.y,
                                           def->localAnchorB.x, def->localAnchorB.y, def->lengthA, def->lengthB,
                                           def->ratio};
-        return AddJoint(GB_JOINT_PULLEY, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
+        b2Joint* r = AddJoint(GB_JOINT_PULLEY, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0);
+        if (r) r->m_userData = def->userData;
+        return r;
     }
     b2Joint* CreateJoint(const b2GearJointDef* def)
     {
@@ -1262,6 +1304,7 @@ public:
         std::unique_ptr<b2GearJoint> g(new b2GearJoint());
         g->m_ratio = def->ratio;
         b2Joint* j = AddJoint(GB_JOINT_GEAR, def->bodyA, def->bodyB, f, def->collideConnected ? 4 : 0, std::move(g));
+        if (j) j->m_userData = def->userData;
         if (j) {  // b2GearJoint::GetBodyA/B: the coupled joints' bodies B
             j->m_a = def->joint1->GetBodyB();
             j->m_b = def->joint2->GetBodyB();
@@ -1282,7 +1325,9 @@ public:
         j->m_maxMotorForce = def->maxMotorForce;
         j->m_lower = def->lowerTranslation;
         j->m_upper = def->upperTranslation;
-        return AddJoint(GB_JOINT_PRISMATIC, def->bodyA, def->bodyB, f, flags, std::move(j));
+        b2Joint* r = AddJoint(GB_JOINT_PRISMATIC, def->bodyA, def->bodyB, f, flags, std::move(j));
+        if (r) r->m_userData = def->userData;
+        return r;
     }
 
     void Step(float timeStep, int velocityIterations, int positionIterations)
@@ -1750,6 +1795,62 @@ inline void b2MouseJoint::SetTarget(const b2Vec2& target)
     m_world->Edit(m_index, GB_EDIT_MOUSE_TARGET, target.x, target.y, 0.0f, 0.0f, true);
 }
 
+inline void b2RevoluteJointDef::Initialize(b2Body* bA, b2Body* bB, const b2Vec2& anchor)
+{
+    bodyA = bA;
+    bodyB = bB;
+    localAnchorA = bA->GetLocalPoint(anchor);
+    localAnchorB = bB->GetLocalPoint(anchor);
+    referenceAngle = bB->GetAngle() - bA->GetAngle();
+}
+inline void b2DistanceJointDef::Initialize(b2Body* bA, b2Body* bB, const b2Vec2& anchorA, const b2Vec2& anchorB)
+{
+    bodyA = bA;
+    bodyB = bB;
+    localAnchorA = bA->GetLocalPoint(anchorA);
+    localAnchorB = bB->GetLocalPoint(anchorB);
+    const float dx = anchorB.x - anchorA.x, dy = anchorB.y - anchorA.y;
+    length = std::sqrt(dx * dx + dy * dy);
+}
+inline void b2WeldJointDef::Initialize(b2Body* bA, b2Body* bB, const b2Vec2& anchor)
+{
+    bodyA = bA;
+    bodyB = bB;
+    localAnchorA = bA->GetLocalPoint(anchor);
+    localAnchorB = bB->GetLocalPoint(anchor);
+    referenceAngle = bB->GetAngle() - bA->GetAngle();
+}
+inline void b2WheelJointDef::Initialize(b2Body* bA, b2Body* bB, const b2Vec2& anchor, const b2Vec2& axis)
+{
+    bodyA = bA;
+    bodyB = bB;
+    localAnchorA = bA->GetLocalPoint(anchor);
+    localAnchorB = bB->GetLocalPoint(anchor);
+    localAxisA = bA->GetLocalVector(axis);
+}
+inline void b2FrictionJointDef::Initialize(b2Body* bA, b2Body* bB, const b2Vec2& anchor)
+{
+    bodyA = bA;
+    bodyB = bB;
+    localAnchorA = bA->GetLocalPoint(anchor);
+    localAnchorB = bB->GetLocalPoint(anchor);
+}
+inline void b2MotorJointDef::Initialize(b2Body* bA, b2Body* bB)
+{
+    bodyA = bA;
+    bodyB = bB;
+    linearOffset = bA->GetLocalPoint(bB->GetPosition());
+    angularOffset = bB->GetAngle() - bA->GetAngle();
+}
+inline void b2PrismaticJointDef::Initialize(b2Body* bA, b2Body* bB, const b2Vec2& anchor, const b2Vec2& axis)
+{
+    bodyA = bA;
+    bodyB = bB;
+    localAnchorA = bA->GetLocalPoint(anchor);
+    localAnchorB = bB->GetLocalPoint(anchor);
+    localAxisA = bA->GetLocalVector(axis);
+    referenceAngle = bB->GetAngle() - bA->GetAngle();
+}
 inline void b2PulleyJointDef::Initialize(b2Body* bA, b2Body* bB, const b2Vec2& groundA, const b2Vec2& groundB,
                                          const b2Vec2& anchorA, const b2Vec2& anchorB, float r)
 {

@@ -59,6 +59,46 @@ int main()
     std::printf("ground_fixtures");
     for (b2Fixture* f = ground->GetFixtureList(); f; f = f->GetNext()) std::printf(" %d", f->GetIndex());
     std::printf("\n");
+    // joint definitions from world anchors (the defs' Initialize), between a turned body and another
+    b2BodyDef ad;
+    ad.type = b2_dynamicBody;
+    ad.position.Set(1.25f, -0.5f);
+    ad.angle = 0.7f;
+    b2Body* a = world.CreateBody(&ad);
+    b2BodyDef cd;
+    cd.type = b2_dynamicBody;
+    cd.position.Set(-2.0f, 3.5f);
+    cd.angle = -1.3f;
+    b2Body* c = world.CreateBody(&cd);
+    const b2Vec2 anchor(0.3f, 1.1f), anchor2(-1.7f, 2.9f), axis(0.6f, 0.8f);
+    for (b2Body* b : {a, c}) {
+        const b2Transform t = b->GetTransform();
+        std::printf("xf %a %a %a %a %a\n", t.p.x, t.p.y, t.q.s, t.q.c, b->GetAngle());
+    }
+    b2RevoluteJointDef rj;
+    rj.Initialize(a, c, anchor);
+    std::printf("rev %a %a %a %a %a\n", rj.localAnchorA.x, rj.localAnchorA.y, rj.localAnchorB.x, rj.localAnchorB.y,
+                rj.referenceAngle);
+    b2PrismaticJointDef pj;
+    pj.Initialize(a, c, anchor, axis);
+    std::printf("pri %a %a %a %a %a %a %a\n", pj.localAnchorA.x, pj.localAnchorA.y, pj.localAnchorB.x,
+                pj.localAnchorB.y, pj.localAxisA.x, pj.localAxisA.y, pj.referenceAngle);
+    b2WheelJointDef wj;
+    wj.Initialize(a, c, anchor, axis);
+    std::printf("whe %a %a %a %a %a %a\n", wj.localAnchorA.x, wj.localAnchorA.y, wj.localAnchorB.x, wj.localAnchorB.y,
+                wj.localAxisA.x, wj.localAxisA.y);
+    b2DistanceJointDef dj;
+    dj.Initialize(a, c, anchor, anchor2);
+    std::printf("dis %a %a %a %a %a\n", dj.localAnchorA.x, dj.localAnchorA.y, dj.localAnchorB.x, dj.localAnchorB.y,
+                dj.length);
+    b2MotorJointDef mj;
+    mj.Initialize(a, c);
+    std::printf("mot %a %a %a\n", mj.linearOffset.x, mj.linearOffset.y, mj.angularOffset);
+    b2WeldJointDef weld;
+    weld.Initialize(a, c, anchor);
+    weld.userData = &tags[2];
+    b2Joint* wjoint = world.CreateJoint(&weld);
+    std::printf("weld_user %d\n", *static_cast<int*>(wjoint->GetUserData()));
     (void)f0;
     (void)f2;
     (void)j0;

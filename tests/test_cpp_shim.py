@@ -624,12 +624,15 @@ LISTS_SRC = os.path.join(ROOT, "tests", "cpp", "lists.cpp")
 
 def test_cpp_lists_and_user_data(tmp_path):
     """b2Body::GetFixtureList / b2Fixture::GetNext and b2World::GetJointList / b2Joint::GetNext run
-    newest first and skip destroyed entries, as the reference's lists; user data round-trips. No step
+    newest first and skip destroyed entries, as the reference's lists; user data round-trips; the joint
+    definitions' Initialize computes the reference's local anchors, axes, lengths and angles. No step
     is taken, so this runs without a GPU."""
     lib = _lib.library_path()
     exe = str(tmp_path / "lists")
     libdir = os.path.dirname(lib)
-    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "include"), LISTS_SRC, "-o", exe,
+    # without contraction: the definitions' Initialize runs in the caller's code, compared bit for bit
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
+           LISTS_SRC, "-o", exe,
            "-L", libdir, "-lbox2d_gb300", f"-Wl,-rpath,{libdir}"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
@@ -644,3 +647,29 @@ def test_cpp_lists_and_user_data(tmp_path):
     assert out["ground_fixtures"] == ["3"]
     assert out["body_joints"] == ["2:0", "0:0"]  # newest first, the destroyed joint left out
     assert out["ground_contacts"] == ["0"]  # no step yet: no contacts
+    # the joint definitions' Initialize, restated in float32 from the printed transforms
+    f32 = np.float32
+    xfs = [[f32(float.fromhex(v)) for v in ln.split()[1:]] for ln in r.stdout.splitlines() if ln.startswith("xf ")]
+
+    def local_point(t, p):
+        dx, dy = f32(p[0] - t[0]), f32(p[1] - t[1])
+        return [f32(t[3] * dx + t[2] * dy), f32(-t[2] * dx + t[3] * dy)]
+
+    def local_vector(t, v):
+        return [f32(t[3] * v[0] + t[2] * v[1]), f32(-t[2] * v[0] + t[3] * v[1])]
+
+    a, c = xfs
+    anchor, anchor2, axis = (f32(0.3), f32(1.1)), (f32(-1.7), f32(2.9)), (f32(0.6), f32(0.8))
+    ref = f32(c[4] - a[4])
+    dx, dy = f32(anchor2[0] - anchor[0]), f32(anchor2[1] - anchor[1])
+    want = {
+        "rev": local_point(a, anchor) + local_point(c, anchor) + [ref],
+        "pri": local_point(a, anchor) + local_point(c, anchor) + local_vector(a, axis) + [ref],
+        "whe": local_point(a, anchor) + local_point(c, anchor) + local_vector(a, axis),
+        "dis": local_point(a, anchor) + local_point(c, anchor2) + [np.sqrt(f32(f32(dx * dx) + f32(dy * dy)), dtype=np.float32)],
+        "mot": local_point(a, (c[0], c[1])) + [ref],
+    }
+    for key, vals in want.items():
+        got = np.array([float.fromhex(v) for v in out[key]], dtype=np.float32)
+        assert np.array_equal(got.view(np.uint32), np.array(vals, dtype=np.float32).view(np.uint32)), key
+    assert out["weld_user"] == ["9"]
