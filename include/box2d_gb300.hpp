@@ -852,6 +852,9 @@ public:
     int GetChildIndexA() const { return m_childA; }  // the chain child, 0 for other shapes
     int GetChildIndexB() const { return m_childB; }
     bool IsTouching() const { return (m_flags & 2) != 0; }
+    // the next contact of the world's list (b2Contact::GetNext), valid until the next step
+    b2Contact* GetNext() { return m_next; }
+    const b2Contact* GetNext() const { return m_next; }
     bool IsEnabled() const { return (m_flags & 4) != 0; }
     // b2Contact::SetEnabled, SetFriction, SetRestitution, SetTangentSpeed (Contacts/b2Contact.h:98-152),
     // in effect for the rest of a step when made in PreSolve
@@ -874,6 +877,7 @@ private:
     int m_idA = -1, m_idB = -1;  // device fixture ids (one per chain child)
     int m_flags = 0;
     int m_edit = 0;               // changes made by the listener (gb_contact_edit flags)
+    b2Contact* m_next = nullptr;  // the next contact of the world's list
     float m_friction = 0.0f, m_restitution = 0.0f, m_tangentSpeed = 0.0f;
     b2Manifold m_manifold;
 };
@@ -1009,7 +1013,7 @@ public:
     {
         if (!Handle() || !j || !j->m_alive || j->m_world != this) return false;
         const float v[4] = {v0, v1, 0.0f, 0.0f};
-        m_stale = true;
+        MarkStale();
         return gb_joint_set(m_h, 0, j->m_index, prop, v) == GB_OK;
     }
     // b2World::ShiftOrigin (Box2D/Dynamics/b2World.cpp:1261-1282)
@@ -1017,14 +1021,14 @@ public:
     {
         if (!Handle()) return;
         gb_world_shift_origin(m_h, 0, newOrigin.x, newOrigin.y);
-        m_stale = true;
+        MarkStale();
     }
     // one gb_fixture_set call (b2Fixture::SetFriction, ...)
     bool SetFixtureProperty(b2Fixture* f, int prop, float v0, float v1 = 0.0f, float v2 = 0.0f)
     {
         if (!Handle() || !f || !f->m_alive) return false;
         const float v[4] = {v0, v1, v2, 0.0f};
-        m_stale = true;
+        MarkStale();
         return gb_fixture_set(m_h, 0, f->m_index, prop, v) == GB_OK;
     }
     // one gb_body_set call (b2Body::SetType, SetActive, ...); EndContact for the contacts it destroys
@@ -1037,7 +1041,7 @@ public:
         int n = 0;
         const float v[4] = {value, v1, v2, v3};
         const gb_status s = gb_body_set(m_h, 0, body->m_index, prop, v, calls.data(), cap, &n);
-        m_stale = true;
+        MarkStale();
         if (s != GB_OK) return false;
         calls.resize(3 * (size_t)std::min(n, cap));
         Announce(calls);
@@ -1168,7 +1172,7 @@ public:
         b->m_type = def->type;
         b->m_userData = def->userData;
         m_bodies.push_back(std::move(b));
-        m_stale = true;
+        MarkStale();
         return m_bodies.back().get();
     }
 
@@ -1335,21 +1339,21 @@ public:
         if (!Handle()) return;
         if (!m_listener) {
             gb_world_step(m_h, timeStep, velocityIterations, positionIterations);
-            m_stale = true;
+            MarkStale();
             return;
         }
         if (m_filter) {
             if (!m_eventsOn) m_eventsOn = gb_world_set_events(m_h, 1) == GB_OK;
             ReadContacts();
             gb_world_step(m_h, timeStep, velocityIterations, positionIterations);
-            m_stale = true;
+            MarkStale();
             Report(0);
             return;
         }
         if (!m_eventsOn) m_eventsOn = gb_world_set_events(m_h, 1) == GB_OK;
         ReadContacts();  // the contacts before the step: destroyed contacts and old manifolds
         if (gb_world_step_begin(m_h, timeStep, velocityIterations, positionIterations) != GB_OK) return;
-        m_stale = true;
+        MarkStale();
         const int collideCalls = Report(0);
         // what PreSolve changed, by list position
         std::vector<gb_contact_edit> edits;
@@ -1362,7 +1366,7 @@ public:
         }
         if (!edits.empty()) gb_contact_edits(m_h, (int)edits.size(), edits.data());
         gb_world_step_end(m_h);
-        m_stale = true;
+        MarkStale();
         Report(collideCalls);
     }
 
@@ -1384,15 +1388,33 @@ public:
         if (m_h) gb_world_counts(m_h, 0, &b, &f, &c, &j);
         return c;
     }
-    // b2World::GetContactList as a vector in list order (newest first)
-    const std::vector<b2Contact*>& GetContactList()
+    // b2World::GetContactList (Box2D/Dynamics/b2World.h:127): the head of the world's contact list
+    // (newest first; b2Contact::GetNext walks it), read once after each step or change
+    b2Contact* GetContactList()
     {
-        ReadContacts();
+        const std::vector<b2Contact*>& v = Contacts();
+        return v.empty() ? nullptr : v[0];
+    }
+    // the same list as a vector; the contacts stay the same objects until the next step or change
+    const std::vector<b2Contact*>& Contacts()
+    {
+        if (!m_contactsStale && !m_contactView.empty()) return m_contactView;
+        // inside the listener's calls the list is the one being reported (read at this half's end)
+        if (!m_locked) {
+            ReadContacts();
+            m_contactsStale = false;
+        }
         m_contactView.clear();
         for (auto& c : m_contacts) m_contactView.push_back(c.get());
         return m_contactView;
     }
 
+    // the body states and the contact list are read again at their next use
+    void MarkStale()
+    {
+        m_stale = true;
+        m_contactsStale = true;
+    }
     // raw access used by b2Body
     // a body's mass data, damping and flags (gb_get_body_info), for the b2Body getters
     int BodyInfo(int index, float* out)
@@ -1444,7 +1466,7 @@ public:
         for (int k = 0; k < children; ++k) m_fixtureOfId.push_back({fx.get(), k});
         fx->m_slot = m_fixtures.size();
         m_fixtures.push_back(std::move(fx));
-        m_stale = true;
+        MarkStale();
         return m_fixtures.back().get();
     }
     void Edit(int index, int op, float v0, float v1, float v2, float v3, bool wake)
@@ -1457,7 +1479,7 @@ public:
         e.wake = wake ? 1 : 0;
         e.v[0] = v0; e.v[1] = v1; e.v[2] = v2; e.v[3] = v3;
         gb_body_edits(m_h, 1, &e);
-        m_stale = true;
+        MarkStale();
     }
 
 private:
@@ -1478,7 +1500,7 @@ private:
         calls.assign(3 * (size_t)cap, 0);
         gb_status s = fn(m_h, 0, index, calls.data(), cap, &n);
         calls.resize(3 * (size_t)(s == GB_OK ? std::min(n, cap) : 0));
-        m_stale = true;
+        MarkStale();
         return s;
     }
     void Announce(const std::vector<int>& calls)
@@ -1567,6 +1589,9 @@ private:
             }
             m_contacts.push_back(std::move(c));
         }
+        // b2Contact::GetNext: the world's list order (newest first)
+        for (size_t k = 0; k < m_contacts.size(); ++k)
+            m_contacts[k]->m_next = k + 1 < m_contacts.size() ? m_contacts[k + 1].get() : nullptr;
     }
     // Makes the recorded listener calls from index `first` on, with the contacts as they are now and
     // as they were before (m_contacts); returns the number of calls recorded so far.
@@ -1629,6 +1654,7 @@ private:
     std::vector<std::unique_ptr<b2Contact>> m_contacts, m_old;
     bool m_eventsOn = false;
     bool m_locked = false;
+    bool m_contactsStale = true;  // the contact list must be read again (a step or a change since)
     std::vector<b2Contact*> m_contactView;
     std::vector<float> m_state;
     bool m_stale = true;
@@ -1644,7 +1670,7 @@ inline b2Fixture* b2Body::GetFixtureList() const { return m_world->FixtureListOf
 inline b2ContactEdge* b2Body::GetContactList()
 {
     m_contactEdges.clear();
-    for (b2Contact* c : m_world->GetContactList()) {
+    for (b2Contact* c : m_world->Contacts()) {
         b2Body* a = c->GetFixtureA()->GetBody();
         b2Body* b = c->GetFixtureB()->GetBody();
         if (a != this && b != this) continue;

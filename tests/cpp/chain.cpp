@@ -69,7 +69,7 @@ int main()
         }
         std::printf("\n");
     }
-    for (b2Contact* c : world.GetContactList()) {
+    for (b2Contact* c = world.GetContactList(); c; c = c->GetNext()) {
         const b2Fixture* a = c->GetFixtureA();
         const int which = a == terrainFixture ? 0 : (a == loopFixture ? 1 : -1);
         if (which < 0) continue;

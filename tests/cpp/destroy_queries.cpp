@@ -171,7 +171,8 @@ int main()
     std::printf("ray %d %a %a %a %a %a hits %d\n", closest.id, closest.fraction, closest.point.x, closest.point.y,
                 closest.normal.x, closest.normal.y, every.hits);
     // the world manifold of the first contact in the list that has points (a new contact has none)
-    const std::vector<b2Contact*>& contacts = world.GetContactList();
+    std::vector<b2Contact*> contacts;  // the world's list, walked as the reference's
+    for (b2Contact* c = world.GetContactList(); c; c = c->GetNext()) contacts.push_back(c);
     for (size_t k = 0; k < contacts.size(); ++k) {
         const b2Contact* c = contacts[k];
         if (c->GetManifold()->pointCount == 0) continue;

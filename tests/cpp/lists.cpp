@@ -55,7 +55,7 @@ int main()
     std::printf("body_joints");
     for (b2JointEdge* e = body->GetJointList(); e; e = e->next)
         std::printf(" %d:%d", e->joint->GetIndex(), e->other == ground ? 0 : 1);
-    std::printf("\nground_contacts %d\n", ground->GetContactList() ? 1 : 0);
+    std::printf("\nground_contacts %d %d\n", ground->GetContactList() ? 1 : 0, world.GetContactList() ? 1 : 0);
     std::printf("ground_fixtures");
     for (b2Fixture* f = ground->GetFixtureList(); f; f = f->GetNext()) std::printf(" %d", f->GetIndex());
     std::printf("\n");

@@ -646,7 +646,7 @@ def test_cpp_lists_and_user_data(tmp_path):
     assert out["user"] == ["7", "8", "9"]
     assert out["ground_fixtures"] == ["3"]
     assert out["body_joints"] == ["2:0", "0:0"]  # newest first, the destroyed joint left out
-    assert out["ground_contacts"] == ["0"]  # no step yet: no contacts
+    assert out["ground_contacts"] == ["0", "0"]  # no step yet: no contacts
     # the joint definitions' Initialize, restated in float32 from the printed transforms
     f32 = np.float32
     xfs = [[f32(float.fromhex(v)) for v in ln.split()[1:]] for ln in r.stdout.splitlines() if ln.startswith("xf ")]
