@@ -38,7 +38,7 @@ EXPORTS = [
     "gb_mlp_forward", "gb_mlp_gradients", "gb_mlp_train", "gb_world_set_warm_start", "gb_world_warm_stats",
     "gb_world_set_contact_log", "gb_world_read_contact_log", "gb_world_contact_stats", "gb_world_set_events",
     "gb_world_read_events", "gb_world_query_aabb", "gb_world_raycast", "gb_create_joints",
-    "gb_world_stage_times", "gb_body_edits", "gb_world_set_limits", "gb_world_set_settings", "gb_world_clear_forces", "gb_destroy_body", "gb_body_set", "gb_get_body_info", "gb_fixture_set", "gb_world_shift_origin", "gb_joint_set", "gb_get_joint_reaction", "gb_fixture_query", "gb_world_track_tree", "gb_world_tree_stats", "gb_world_checkpoint", "gb_world_restore", "gb_world_set_recovery", "gb_world_recoveries", "gb_destroy_joint",
+    "gb_world_stage_times", "gb_body_edits", "gb_world_set_limits", "gb_world_set_settings", "gb_world_clear_forces", "gb_destroy_body", "gb_body_set", "gb_get_body_info", "gb_fixture_set", "gb_world_shift_origin", "gb_joint_set", "gb_get_joint_reaction", "gb_fixture_query", "gb_polygon_shape", "gb_world_track_tree", "gb_world_tree_stats", "gb_world_checkpoint", "gb_world_restore", "gb_world_set_recovery", "gb_world_recoveries", "gb_destroy_joint",
     "gb_destroy_fixture", "gb_world_raycast_all", "gb_world_get_profile", "gb_world_step_begin",
     "gb_contact_edits", "gb_world_step_end", "gb_world_set_contact_filter", "gb_world_refilter",
     "gb_world_filter_stats",
@@ -150,6 +150,7 @@ def load(build_if_missing: bool = True):
         "gb_joint_set": [vp, i, i, i, _f32],
         "gb_get_joint_reaction": [vp, i, i, f, _f32],
         "gb_fixture_query": [vp, i, i, i, _f32, _f32],
+        "gb_polygon_shape": [i, _f32, i, _f32, C.POINTER(C.c_int)],
         "gb_world_track_tree": [vp, i],
         "gb_world_set_recovery": [vp, i],
         "gb_world_recoveries": [vp, C.POINTER(C.c_longlong)],

@@ -3179,6 +3179,32 @@ gb_status SetJointPropertyHost(HWorld& W, int ji, int prop, const float* v)
 
 extern "C" {
 
+gb_status gb_polygon_shape(int mode, const float* in, int n, float* out, int* count)
+{
+    if (!in || !out || !count || mode < 0 || mode > 2 || (mode == 0 && (n < 0 || n > kMaxPolyVerts))) return GB_ERR_INVALID;
+    Shape s;
+    std::memset(&s, 0, sizeof(s));
+    if (mode == 0) {
+        Vec2 pts[kMaxPolyVerts];
+        for (int i = 0; i < n; ++i) pts[i] = V(in[2 * i], in[2 * i + 1]);
+        PolygonSet(s, pts, n);
+    } else if (mode == 1) {
+        PolygonSetAsBox(s, in[0], in[1]);
+    } else {
+        PolygonSetAsBox(s, in[0], in[1], V(in[2], in[3]), in[4]);
+    }
+    out[0] = s.centroid.x;
+    out[1] = s.centroid.y;
+    for (int i = 0; i < kMaxPolyVerts; ++i) {
+        out[2 + 2 * i] = i < s.count ? s.v[i].x : 0.0f;
+        out[3 + 2 * i] = i < s.count ? s.v[i].y : 0.0f;
+        out[18 + 2 * i] = i < s.count ? s.n[i].x : 0.0f;
+        out[19 + 2 * i] = i < s.count ? s.n[i].y : 0.0f;
+    }
+    *count = s.count;
+    return GB_OK;
+}
+
 gb_status gb_fixture_query(gb_world* g, int w, int fixture, int op, const float* in, float* out)
 {
     if (!g || w < 0 || w >= (int)g->worlds.size() || !out || (op < 2 && !in) || op < 0 || op > 3) return GB_ERR_INVALID;

@@ -237,6 +237,12 @@ gb_status gb_get_joint_reaction(gb_world* world, int w, int joint, float inv_dt,
  * (Box2D/Dynamics/b2Fixture.h:313-342). Waits for the step in flight. */
 gb_status gb_fixture_query(gb_world* world, int w, int fixture, int op, const float* in, float* out);
 
+/* b2PolygonShape::Set (mode 0: in = n points x, y; Box2D/Collision/Shapes/b2PolygonShape.cpp:119-252,
+ * the hull of welded points), SetAsBox(hx, hy) (mode 1: in = hx, hy) and SetAsBox(hx, hy, center,
+ * angle) (mode 2: in = hx, hy, cx, cy, angle; :47-70): out = centroid (2), vertices (8 x 2), normals
+ * (8 x 2), *count the vertices, as the library stores the shape. No device work. */
+gb_status gb_polygon_shape(int mode, const float* in, int n, float* out, int* count);
+
 /* b2World::ShiftOrigin (Box2D/Dynamics/b2World.cpp:1261-1282) of world w between steps: bodies, the
  * mouse joints' targets, the pulleys' ground anchors and the broadphase's boxes move by -(x, y). */
 gb_status gb_world_shift_origin(gb_world* world, int w, float x, float y);

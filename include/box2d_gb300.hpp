@@ -183,17 +183,35 @@ public:
     void Set(const b2Vec2* points, int count)
     {
         m_mode = kPoints;
-        m_count = count < 8 ? count : 8;
-        for (int i = 0; i < m_count; ++i) m_points[i] = points[i];
+        m_inputCount = count < 8 ? count : 8;
+        float in[16];
+        for (int i = 0; i < m_inputCount; ++i) {
+            m_points[i] = points[i];
+            in[2 * i] = points[i].x;
+            in[2 * i + 1] = points[i].y;
+        }
+        Fill(0, in, m_inputCount);
     }
     void SetAsBox(float hx, float hy)
     {
         m_mode = kBox; m_hx = hx; m_hy = hy; m_oriented = false;
+        const float in[2] = {hx, hy};
+        Fill(1, in, 0);
     }
     void SetAsBox(float hx, float hy, const b2Vec2& center, float angle)
     {
         m_mode = kBox; m_hx = hx; m_hy = hy; m_center = center; m_angle = angle; m_oriented = true;
+        const float in[5] = {hx, hy, center.x, center.y, angle};
+        Fill(2, in, 0);
     }
+    int GetVertexCount() const { return m_count; }
+    const b2Vec2& GetVertex(int index) const { return m_vertices[index]; }
+    // the shape as the reference's b2PolygonShape holds it (b2PolygonShape.h:86-89), filled by Set and
+    // SetAsBox through gb_polygon_shape
+    b2Vec2 m_centroid;
+    b2Vec2 m_vertices[8];
+    b2Vec2 m_normals[8];
+    int m_count = 0;
     void Encode(int* type, float* shape, int* n) const override
     {
         if (m_mode == kBox) {
@@ -202,15 +220,27 @@ public:
             if (m_oriented) { shape[2] = m_center.x; shape[3] = m_center.y; shape[4] = m_angle; *n = 5; }
             else *n = 2;
         } else {
-            *type = 2; *n = m_count;
-            for (int i = 0; i < m_count; ++i) { shape[2 * i] = m_points[i].x; shape[2 * i + 1] = m_points[i].y; }
+            *type = 2; *n = m_inputCount;
+            for (int i = 0; i < m_inputCount; ++i) { shape[2 * i] = m_points[i].x; shape[2 * i + 1] = m_points[i].y; }
         }
     }
 
 private:
+    void Fill(int mode, const float* in, int n)
+    {
+        float out[34] = {0};
+        int count = 0;
+        if (gb_polygon_shape(mode, in, n, out, &count) != GB_OK) return;
+        m_centroid = b2Vec2(out[0], out[1]);
+        m_count = count;
+        for (int i = 0; i < 8; ++i) {
+            m_vertices[i] = b2Vec2(out[2 + 2 * i], out[3 + 2 * i]);
+            m_normals[i] = b2Vec2(out[18 + 2 * i], out[19 + 2 * i]);
+        }
+    }
     enum Mode { kPoints, kBox } m_mode = kBox;
     b2Vec2 m_points[8];
-    int m_count = 0;
+    int m_inputCount = 0;
     float m_hx = 0.0f, m_hy = 0.0f, m_angle = 0.0f;
     b2Vec2 m_center;
     bool m_oriented = false;

@@ -457,6 +457,30 @@ void rw_body_set(void* h, int b, int prop, const float* v)
     default: break;
     }
 }
+// b2PolygonShape::Set (mode 0), SetAsBox(hx, hy) (mode 1), SetAsBox(hx, hy, center, angle) (mode 2):
+// out = centroid, 8 vertices, 8 normals; returns the vertex count
+int rw_polygon_shape(int mode, const float* in, int n, float* out)
+{
+    b2PolygonShape s;
+    if (mode == 0) {
+        b2Vec2 pts[b2_maxPolygonVertices];
+        for (int i = 0; i < n; ++i) pts[i].Set(in[2 * i], in[2 * i + 1]);
+        s.Set(pts, n);
+    } else if (mode == 1) {
+        s.SetAsBox(in[0], in[1]);
+    } else {
+        s.SetAsBox(in[0], in[1], b2Vec2(in[2], in[3]), in[4]);
+    }
+    out[0] = s.m_centroid.x;
+    out[1] = s.m_centroid.y;
+    for (int i = 0; i < b2_maxPolygonVertices; ++i) {
+        out[2 + 2 * i] = i < s.m_count ? s.m_vertices[i].x : 0.0f;
+        out[3 + 2 * i] = i < s.m_count ? s.m_vertices[i].y : 0.0f;
+        out[18 + 2 * i] = i < s.m_count ? s.m_normals[i].x : 0.0f;
+        out[19 + 2 * i] = i < s.m_count ? s.m_normals[i].y : 0.0f;
+    }
+    return s.m_count;
+}
 // b2Fixture::TestPoint (op 0: in = point; out[0] 1 inside), RayCast (op 1: in = p1, p2, maxFraction;
 // out = hit, normal, fraction) and GetAABB (op 2: out = lower, upper) of a fixture's first child
 void rw_fixture_query(void* h, int f, int op, const float* in, float* out)

@@ -99,6 +99,19 @@ int main()
     weld.userData = &tags[2];
     b2Joint* wjoint = world.CreateJoint(&weld);
     std::printf("weld_user %d\n", *static_cast<int*>(wjoint->GetUserData()));
+    // b2PolygonShape as the reference holds it after Set and SetAsBox
+    b2PolygonShape hull;
+    const b2Vec2 pts[5] = {b2Vec2(0.0f, 0.0f), b2Vec2(1.5f, 0.2f), b2Vec2(0.7f, 1.1f), b2Vec2(0.6f, 0.5f),
+                           b2Vec2(-0.4f, 0.9f)};
+    hull.Set(pts, 5);
+    b2PolygonShape turned;
+    turned.SetAsBox(0.5f, 0.25f, b2Vec2(1.0f, -2.0f), 0.7f);
+    for (const b2PolygonShape* s : {&hull, &turned}) {
+        std::printf("poly %d %a %a", s->GetVertexCount(), s->m_centroid.x, s->m_centroid.y);
+        for (int i = 0; i < s->m_count; ++i)
+            std::printf(" %a %a %a %a", s->GetVertex(i).x, s->GetVertex(i).y, s->m_normals[i].x, s->m_normals[i].y);
+        std::printf("\n");
+    }
     (void)f0;
     (void)f2;
     (void)j0;

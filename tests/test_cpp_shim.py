@@ -2,6 +2,7 @@
 runs the Box2D manual's HelloWorld bit for bit like the CPU oracle."""
 from __future__ import annotations
 
+import ctypes as C
 import os
 import subprocess
 
@@ -673,3 +674,17 @@ def test_cpp_lists_and_user_data(tmp_path):
         got = np.array([float.fromhex(v) for v in out[key]], dtype=np.float32)
         assert np.array_equal(got.view(np.uint32), np.array(vals, dtype=np.float32).view(np.uint32)), key
     assert out["weld_user"] == ["9"]
+    # polygons after Set and SetAsBox(hx, hy, center, angle), as the library builds them
+    polys = [ln.split()[1:] for ln in r.stdout.splitlines() if ln.startswith("poly ")]
+    lib = _lib.load()
+    for mode, inp, n, got in [(0, [0.0, 0.0, 1.5, 0.2, 0.7, 1.1, 0.6, 0.5, -0.4, 0.9], 5, polys[0]),
+                              (2, [0.5, 0.25, 1.0, -2.0, 0.7], 0, polys[1])]:
+        v = np.zeros(16, dtype=np.float32)
+        v[:len(inp)] = inp
+        o = np.zeros(34, dtype=np.float32)
+        cnt = C.c_int()
+        lib.gb_polygon_shape(mode, v, n, o, C.byref(cnt))
+        assert int(got[0]) == cnt.value
+        want = [o[0], o[1]] + [x for i in range(cnt.value) for x in (o[2 + 2 * i], o[3 + 2 * i], o[18 + 2 * i], o[19 + 2 * i])]
+        vals = np.array([float.fromhex(x) for x in got[1:]], dtype=np.float32)
+        assert np.array_equal(vals.view(np.uint32), np.array(want, dtype=np.float32).view(np.uint32))
